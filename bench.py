@@ -1,0 +1,337 @@
+"""Benchmark of the b200 render path on one or more GB300s.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME] [--impl ours|reference]
+
+A step is one rendered frame of the workload (one ospRenderFrame into an
+accumulating framebuffer).  Prints one JSON line (rank 0).
+
+value      Mrays/s of all ranks: rays traced (counted by the kernels' stats
+           pass over the same frames) / device time of the timed frames
+           (CUDA events on the render stream; L2 flushed before every frame).
+e2e        the same metric through the C ABI with host buffers: per step the
+           camera/renderer parameters go host->device and the RGBA32F colour
+           buffer comes back device->host (ospRenderFrame + ospMapFrameBuffer).
+roofline   algorithmic bytes of the traversal (48 B ray record + 80 B per BVH
+           node visit + 48 B per triangle and 20 B per sphere fetched) per
+           frame / frame time, against the measured HBM copy bandwidth.
+cpu_baseline  the CPU oracle (a restatement of the reference's ISPC path) on
+           this machine's host cores, on a bounded sample of the same frames.
+--impl reference  times that CPU implementation alone, as the reference arm
+           (the reference's ISPC+Embree device cannot be built here).
+
+Multi-GPU: the render path does not exchange data between GPUs; N ranks
+render N independent replicas ("replicas only"), scaling is weak.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+L2_FLUSH_BYTES = 512 << 20
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return p["hbm_gbs"], "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """Samples SM clocks and throttle reasons with nvidia-smi during a region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        try:
+            for line in open(self.path):
+                f = [x.strip() for x in line.split(",")]
+                if len(f) < 8:
+                    continue
+                try:
+                    sm.append(float(f[0]))
+                    mx.append(float(f[1]))
+                except ValueError:
+                    continue
+                for n, v in zip(names, f[4:8]):
+                    if v.lower() == "active":
+                        reasons.add(n)
+        except Exception:
+            pass
+        finally:
+            try:
+                os.unlink(self.path)
+            except Exception:
+                pass
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# --------------------------------------------------------------------------- workloads
+
+
+class AOWorkload:
+    """AO renderer, aoSamples 1, aoDistance 1e20, 512x512 RGBA32F, 1 spp, on
+    the 256x256 height field (130,050 triangles) + 1,000 spheres (seed 0)."""
+    name = "ao_heightfield_512"
+    metric = "Mrays/s"
+
+    def __init__(self, w=512, h=512):
+        from ospray_gb300 import scenes
+        self.w, self.h = w, h
+        self.data = scenes.ao_heightfield_scene()
+        self.config = {"workload": self.name, "renderer": "ao", "width": w, "height": h, "spp": 1,
+                       "aoSamples": 1, "triangles": int(len(self.data["index"])),
+                       "spheres": int(len(self.data["spheres"])), "pixelFilter": "gauss"}
+
+    def setup(self, og, dev):
+        from ospray_gb300 import scenes
+        self.og = og
+        t0 = time.perf_counter()
+        self.scene = og.Scene(dev)
+        scenes.build_ao_scene(self.scene, self.data)
+        self.build_ms = (time.perf_counter() - t0) * 1e3
+        c = self.data["camera"]
+        self.cam = og.camera_desc(c["position"], c["direction"], c["up"], aspect=self.w / self.h)
+        self.params = og.ao_params(spp=1, ao_samples=1, pixel_filter=og.PF_GAUSS)
+        self.sparams = og.ao_params(spp=1, ao_samples=1, pixel_filter=og.PF_GAUSS, stats=True)
+        self.fb = og.Frame(dev, self.w, self.h, og.FB_COLOR | og.FB_DEPTH | og.FB_ACCUM)
+        self.color = np.empty((self.h, self.w, 4), np.float32)
+
+    def step(self, stats=False):
+        self.og.render_ao(self.scene, self.cam, self.sparams if stats else self.params, self.fb)
+
+    def e2e_step(self):
+        # parameters travel host->device with the launch; colour comes back
+        self.og.render_ao(self.scene, self.cam, self.params, self.fb)
+        self.og.lib().b200_frame_read(self.fb._h, self.og.FB_COLOR, self.color.ctypes.data, self.color.nbytes)
+        return 40 + 52, self.color.nbytes
+
+    def reset(self):
+        self.fb.reset()
+
+    def counters(self, reset=False):
+        return self.scene.counters(reset)
+
+    def cpu_frames(self, budget_s, nthreads):
+        """Oracle frames on the host cores until budget_s: (rays, seconds, frames)."""
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        import oracle
+        from ospray_gb300 import scenes
+        o = oracle.Scene()
+        scenes.build_ao_scene(o, self.data)
+        c = self.data["camera"]
+        cam = oracle.camera(c["position"], c["direction"], c["up"], aspect=self.w / self.h)
+        oracle.lib().or_ray_count.restype = __import__("ctypes").c_uint64
+        oracle.lib().or_ray_count(1)
+        t0 = time.perf_counter()
+        frames = 0
+        while True:
+            oracle.render_ao(o, cam, 2, self.w, self.h, frames=1, nthreads=nthreads)
+            frames += 1
+            if time.perf_counter() - t0 >= budget_s or frames >= 2000:
+                break
+        dt = time.perf_counter() - t0
+        return int(oracle.lib().or_ray_count(1)), dt, frames
+
+
+WORKLOADS = {"ao": AOWorkload}
+
+
+# --------------------------------------------------------------------------- arms
+
+
+def dist_setup(args):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def run_reference(args):
+    ws, rank, local = dist_setup(args)
+    if rank != 0:
+        return
+    wl = WORKLOADS[args.workload]()
+    nthreads = os.cpu_count() or 1
+    per_step = []
+    rays_total = 0
+    for i in range(args.warmup + args.steps):
+        rays, dt, frames = wl.cpu_frames(args.cpu_budget / max(1, args.steps), nthreads)
+        if i >= args.warmup:
+            per_step.append((rays, dt))
+            rays_total += rays
+    secs = sum(dt for _, dt in per_step)
+    value = rays_total / secs / 1e6
+    line = {"metric": wl.metric, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(secs / args.steps * 1e3, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded generators)", "config": wl.config, "impl": "reference",
+            "cpu_baseline": {"value": round(value, 3), "unit": "Mrays/s", "cores": nthreads, "kind": "port",
+                             "sample": "whole frames of the same workload, about %.1f s of CPU work per step"
+                                       % (args.cpu_budget / max(1, args.steps))},
+            "e2e": {"value": round(value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    import ospray_gb300 as og
+    ws, rank, local = dist_setup(args)
+    if ws > 1:
+        import torch.distributed as tdist
+        torch.cuda.set_device(local)
+        tdist.init_process_group("nccl")
+    wl = WORKLOADS[args.workload]()
+    dev = og.Device(local)
+    wl.setup(og, dev)
+    stream = torch.cuda.ExternalStream(dev.stream, device=torch.device("cuda", local))
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=torch.device("cuda", local))
+
+    for _ in range(args.warmup):
+        wl.step()
+    dev.sync()
+    first_timed = wl.fb.frame_id
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize(local)
+    dev.sync()
+    with Clocks(local) as clk:
+        for i in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(float(i))
+                evs[i][0].record(stream)
+            wl.step()
+            with torch.cuda.stream(stream):
+                evs[i][1].record(stream)
+        dev.sync()
+        torch.cuda.synchronize(local)
+    if ws > 1:
+        torch.distributed.barrier()
+    times = [a.elapsed_time(b) for a, b in evs]
+    dev_ms = float(sum(times))
+    # rays of exactly the timed frames: replay the same frame sequence in stats mode
+    wl.reset()
+    for _ in range(first_timed):
+        wl.step()
+    wl.counters(reset=True)
+    for _ in range(args.steps):
+        wl.step(stats=True)
+    c = wl.counters(reset=True)
+    rays, nodes, tris, sph = (int(x) for x in c)
+    # end-to-end through the C ABI with host buffers
+    wl.reset()
+    for _ in range(2):
+        wl.e2e_step()
+    dev.sync()
+    t0 = time.perf_counter()
+    h2d = d2h = 0
+    for _ in range(args.steps):
+        hb, db = wl.e2e_step()
+        h2d, d2h = hb, db
+    dev.sync()
+    e2e_s = time.perf_counter() - t0
+
+    local_vals = torch.tensor([dev_ms, e2e_s, float(rays)], dtype=torch.float64, device=torch.device("cuda", local))
+    if ws > 1:
+        mx = local_vals.clone()
+        torch.distributed.all_reduce(mx, op=torch.distributed.ReduceOp.MAX)
+        sm = local_vals.clone()
+        torch.distributed.all_reduce(sm, op=torch.distributed.ReduceOp.SUM)
+        dev_ms_max, e2e_max, rays_all = float(mx[0]), float(mx[1]), float(sm[2])
+    else:
+        dev_ms_max, e2e_max, rays_all = dev_ms, e2e_s, float(rays)
+    if rank != 0:
+        if ws > 1:
+            torch.distributed.destroy_process_group()
+        return
+    value = rays_all / (dev_ms_max * 1e-3) / 1e6
+    e2e_val = rays_all / e2e_max / 1e6
+    bytes_per_frame = (48.0 * rays + 80.0 * nodes + 48.0 * tris + 20.0 * sph) / args.steps
+    frame_s = dev_ms / args.steps * 1e-3
+    peak, kind = peaks()
+    achieved = bytes_per_frame / frame_s / 1e9
+    line = {"metric": wl.metric, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(dev_ms_max / args.steps, 4), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generators)",
+            "config": dict(wl.config, l2="flushed before every frame (512 MiB write)",
+                           parallelism="replicas" if ws > 1 else "single", build_ms=round(wl.build_ms, 2),
+                           rays_per_frame=rays / args.steps, node_visits_per_ray=round(nodes / max(rays, 1), 3),
+                           tri_tests_per_ray=round(tris / max(rays, 1), 3)),
+            "e2e": {"value": round(e2e_val, 3), "unit": "Mrays/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "gpu_launches": args.steps,
+            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                         "frac": round(achieved / peak, 4), "traffic": None,
+                         "note": "algorithmic traversal bytes per frame / frame time; peak %s" % kind},
+            "clocks": clk.summary()}
+    if not args.no_cpu_baseline:
+        nthreads = os.cpu_count() or 1
+        crays, cdt, cframes = wl.cpu_frames(args.cpu_budget, nthreads)
+        line["cpu_baseline"] = {"value": round(crays / cdt / 1e6, 3), "unit": "Mrays/s", "cores": nthreads,
+                                "kind": "port", "sample": "%d whole frames of the same workload (%.1f s)"
+                                                          % (cframes, cdt)}
+    print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--workload", default="ao", choices=sorted(WORKLOADS))
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU-baseline work")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

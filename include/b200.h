@@ -1,0 +1,144 @@
+/* b200: the GB300 device module's C ABI for the OSPRay render hot path.
+ *
+ * Plain C: opaque handles, host or device pointers with explicit sizes, and
+ * an int status on every call (0 = success, otherwise an OSPError value;
+ * ospray/include/ospray/OSPEnums.h OSPError).  No call throws.  The message
+ * of the last failure on a device is returned by b200_device_last_error
+ * (ospDeviceGetLastErrorMsg, ospray/api/API.cpp:28-66).
+ *
+ * Each group of entry points names the reference interface it replaces.
+ * Coordinates, ray layouts, identifier conventions and framebuffer formats
+ * are those of the reference: triangle u/v with P = (1-u-v) v0 + u v1 + v v2,
+ * RGBA32F colour, images with row 0 at the bottom, invalid IDs = 0xffffffff.
+ */
+#ifndef B200_H
+#define B200_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define B200_VERSION_MAJOR 3
+#define B200_VERSION_MINOR 3
+#define B200_VERSION_PATCH 0
+
+/* status codes = OSPError (ospray/include/ospray/OSPEnums.h) */
+enum {
+  B200_NO_ERROR = 0,
+  B200_UNKNOWN_ERROR = 1,
+  B200_INVALID_ARGUMENT = 2,
+  B200_INVALID_OPERATION = 3,
+  B200_OUT_OF_MEMORY = 4,
+  B200_UNSUPPORTED_CPU = 5,
+  B200_VERSION_MISMATCH = 6
+};
+
+typedef struct b200_device_t *b200_device;
+typedef struct b200_scene_t *b200_scene;
+typedef struct b200_frame_t *b200_frame;
+
+/* ---- device (replaces ISPCDevice construction/commit,
+ *      modules/cpu/ISPCDevice.cpp:207-326, and ospDeviceGetLastErrorMsg) */
+int b200_device_create(int cuda_device, b200_device *out);
+int b200_device_release(b200_device dev);
+const char *b200_device_last_error(b200_device dev);
+/* the CUDA stream (cudaStream_t) all work of this device is ordered on */
+void *b200_device_stream(b200_device dev);
+int b200_device_sync(b200_device dev);
+
+/* ---- world: geometry upload and acceleration-structure build
+ *      (Mesh::commit modules/cpu/geometry/Mesh.cpp:37-204,
+ *       Spheres::commit geometry/Spheres.cpp:46-106,
+ *       Group::commit common/Group.cpp:69-143,
+ *       World::commit common/World.cpp:70-188).
+ * Host arrays are copied to the device at the call; the caller keeps
+ * ownership of its memory. */
+int b200_scene_create(b200_device dev, b200_scene *out);
+int b200_scene_release(b200_scene scene);
+/* vertex: nverts x 3 float; index: ntris x 3 uint32 (vec3ui) */
+int b200_scene_add_mesh(b200_scene scene, const float *vertex, int64_t nverts, const uint32_t *index,
+                        int64_t ntris, int *geom_out);
+/* spheres: n x 4 float (center xyz, radius), OSP_SPHERE */
+int b200_scene_add_spheres(b200_scene scene, const float *spheres, int64_t n, int *geom_out);
+/* one (instance, geometric model) pair: geometry `geom` placed by the
+ * row-major 3x4 affine `xfm` (null = identity), reported as instID/geomID;
+ * material_id indexes the renderer's material list (or -1 for none) */
+int b200_scene_add_instance(b200_scene scene, int geom, uint32_t inst_id, uint32_t geom_id, const float *xfm,
+                            int material_id);
+/* builds every BLAS not yet built and the TLAS */
+int b200_scene_commit(b200_scene scene);
+/* world bounds after commit: lo xyz, hi xyz */
+int b200_scene_bounds(b200_scene scene, float *box6);
+/* BVH statistics after commit: [nodes, primitives] summed over BLASes, TLAS nodes */
+int b200_scene_stats(b200_scene scene, int64_t *stats3);
+
+/* ---- ray queries (rtcIntersectV / rtcOccludedV behind traceGeometryRay and
+ *      isOccluded, modules/cpu/common/World.ih:29-52,311-380).
+ * Device pointers.  rays: n x 8 float (org xyz, tnear, dir xyz, tfar).
+ * occlusion == 0: hit_f n x 6 float (t, u, v, Ng xyz object space; t = inf
+ *   on a miss), hit_id n x 3 uint32 (primID, geomID, instID).
+ * occlusion != 0: hit_f[6 i] = 1 if any hit in [tnear, tfar] else 0.
+ * stream: cudaStream_t or null for the device stream. */
+int b200_trace(b200_scene scene, const float *rays, int64_t n, int occlusion, float *hit_f, uint32_t *hit_id,
+               void *stream);
+
+/* ---- camera (PerspectiveCamera::commit, modules/cpu/camera/PerspectiveCamera.cpp:30-117) */
+typedef struct {
+  float position[3], direction[3], up[3];
+  float fovy, aspect, nearClip;
+} b200_camera_desc;
+
+/* ---- framebuffer (LocalFrameBuffer, modules/cpu/fb/LocalFB.cpp; channels as
+ *      OSPFrameBufferChannel bits: COLOR 1, DEPTH 2, ACCUM 4, VARIANCE 8,
+ *      NORMAL 16, ALBEDO 32, PRIMID 128, GEOMID 256, INSTID 512) */
+enum {
+  B200_FB_COLOR = 1,
+  B200_FB_DEPTH = 2,
+  B200_FB_ACCUM = 4,
+  B200_FB_VARIANCE = 8,
+  B200_FB_NORMAL = 16,
+  B200_FB_ALBEDO = 32,
+  B200_FB_ID_PRIMITIVE = 128,
+  B200_FB_ID_OBJECT = 256,
+  B200_FB_ID_INSTANCE = 512
+};
+int b200_frame_create(b200_device dev, int width, int height, uint32_t channels, b200_frame *out);
+int b200_frame_release(b200_frame fb);
+/* ospResetAccumulation: frameID back to 0 */
+int b200_frame_reset(b200_frame fb);
+int b200_frame_id(b200_frame fb);
+/* device pointer of one channel (COLOR: RGBA32F W*H*4; DEPTH float; IDs uint32) */
+void *b200_frame_channel(b200_frame fb, uint32_t channel);
+/* ospMapFrameBuffer: copies a channel to host memory (waits for the device) */
+int b200_frame_read(b200_frame fb, uint32_t channel, void *host_dst, size_t bytes);
+
+/* ---- AO renderer (AORenderer::commit modules/cpu/render/ao/AORenderer.cpp:26-35,
+ *      AORenderer_renderSample render/ao/AORenderer.ispc:23-149).
+ * One call renders one frame and accumulates it into fb (ospRenderFrame). */
+enum { B200_PF_POINT = 0, B200_PF_BOX = 1, B200_PF_GAUSS = 2, B200_PF_MITCHELL = 3, B200_PF_BLACKMAN_HARRIS = 4 };
+typedef struct {
+  int pixelSamples;  /* spp, >= 1 */
+  int aoSamples;
+  float aoDistance;  /* aoRadius */
+  float aoIntensity;
+  float backgroundColor[4];
+  int pixelFilter;   /* B200_PF_* */
+  int collectStats;  /* nonzero: count rays / node visits / primitive tests */
+} b200_ao_params;
+
+/* Traversal counters accumulated by renders with collectStats set:
+ * [rays traced, BVH node visits, triangle tests, sphere tests]; reset != 0
+ * zeroes them after reading.  (Frame statistics; the reference reports only
+ * task durations, ospGetTaskDuration.) */
+int b200_scene_counters(b200_scene scene, int64_t *out4, int reset);
+int b200_render_ao(b200_scene scene, const b200_camera_desc *camera, const b200_ao_params *params, b200_frame fb,
+                   void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* B200_H */

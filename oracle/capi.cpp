@@ -1,0 +1,193 @@
+// Oracle (test infrastructure only): flat C interface used by the tests and
+// by bench.py's CPU-baseline leg through ctypes.  Nothing in the product
+// links or loads this library.
+#include <cstring>
+
+#include "render.h"
+
+using namespace orc;
+
+namespace {
+// rkcommon rcp(AffineSpace3f): adjoint / det in float, p' = -(l' p)
+A3 rcpAffine(const A3 &a) {
+  const L3 &l = a.l;
+  const float det = dot(l.vx, cross(l.vy, l.vz));
+  const L3 adjT = {cross(l.vy, l.vz), cross(l.vz, l.vx), cross(l.vx, l.vy)};
+  const L3 adj = transposed(adjT);
+  L3 il = {adj.vx / det, adj.vy / det, adj.vz / det};
+  A3 r;
+  r.l = il;
+  r.p = -xfmVector(il, a.p);
+  return r;
+}
+A3 fromRowMajor(const float *X) {
+  A3 a;
+  a.l.vx = {X[0], X[4], X[8]};
+  a.l.vy = {X[1], X[5], X[9]};
+  a.l.vz = {X[2], X[6], X[10]};
+  a.p = {X[3], X[7], X[11]};
+  return a;
+}
+}  // namespace
+
+struct OrCamera {
+  float pos[3], dir[3], up[3];
+  float fovy, aspect, nearClip;
+};
+
+extern "C" {
+
+void *or_scene_new() { return new Scene(); }
+void or_scene_free(void *s) { delete static_cast<Scene *>(s); }
+
+int or_scene_add_mesh(void *sp, const float *verts, int nverts, const uint32_t *index, int ntris) {
+  Scene &s = *static_cast<Scene *>(sp);
+  Geometry g;
+  g.type = 0;
+  g.verts.resize(nverts);
+  std::memcpy(g.verts.data(), verts, sizeof(float) * 3 * nverts);
+  g.index.assign(index, index + 3 * size_t(ntris));
+  s.geoms.push_back(std::move(g));
+  return int(s.geoms.size() - 1);
+}
+
+int or_scene_add_spheres(void *sp, const float *xyzr, int n) {
+  Scene &s = *static_cast<Scene *>(sp);
+  Geometry g;
+  g.type = 1;
+  g.spheres.resize(n);
+  std::memcpy(g.spheres.data(), xyzr, sizeof(float) * 4 * n);
+  s.geoms.push_back(std::move(g));
+  return int(s.geoms.size() - 1);
+}
+
+// xfm: row-major 3x4 affine or null for identity
+void or_scene_add_instance(void *sp, int geom, uint32_t instID, uint32_t geomID, const float *xfm) {
+  Scene &s = *static_cast<Scene *>(sp);
+  InstanceEntry e;
+  e.geom = geom;
+  e.instID = instID;
+  e.geomID = geomID;
+  static const float I[12] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0};
+  e.identity = xfm == nullptr;
+  e.xfm = fromRowMajor(xfm ? xfm : I);
+  e.rcp = rcpAffine(e.xfm);
+  s.entries.push_back(e);
+}
+
+void or_scene_commit(void *sp) { static_cast<Scene *>(sp)->commit(); }
+
+// rays: n x 8 floats (org xyz, tnear, dir xyz, tfar).
+// out_f: n x 6 floats (t, u, v, Ng xyz); out_id: n x 3 uint32 (prim, geom, inst).
+// occlusion != 0: out_f[6i] = 1 when occluded else 0, ids untouched.
+void or_trace(void *sp, const float *rays, int n, int occlusion, float *out_f, uint32_t *out_id, int nthreads) {
+  const Scene &s = *static_cast<Scene *>(sp);
+  const int rowsz = 1024;
+  const int nrows = (n + rowsz - 1) / rowsz;
+  parallelRows(nrows, nthreads, [&](int r) {
+    for (int i = r * rowsz; i < std::min(n, (r + 1) * rowsz); i++) {
+      const float *R = rays + 8 * size_t(i);
+      const Ray ray = {{R[0], R[1], R[2]}, R[3], {R[4], R[5], R[6]}, R[7]};
+      if (occlusion) {
+        out_f[6 * size_t(i)] = s.occluded(ray) ? 1.f : 0.f;
+        continue;
+      }
+      Hit h;
+      const bool hit = s.intersect(ray, h);
+      float *F = out_f + 6 * size_t(i);
+      uint32_t *I = out_id + 3 * size_t(i);
+      if (!hit) {
+        F[0] = INFINITY;
+        F[1] = F[2] = F[3] = F[4] = F[5] = 0.f;
+        I[0] = I[1] = I[2] = INVALID_ID;
+        continue;
+      }
+      F[0] = h.t;
+      F[1] = h.u;
+      F[2] = h.v;
+      F[3] = h.Ng.x;
+      F[4] = h.Ng.y;
+      F[5] = h.Ng.z;
+      I[0] = h.primID;
+      I[1] = h.geomID;
+      I[2] = h.instID;
+    }
+  });
+}
+
+// Primary camera rays for a W x H image at frame `frameID` with `spp`
+// samples per pixel (sample s of pixel (x,y) at index ((y*W)+x)*spp+s),
+// exactly as the renderers generate them.  out: 8 floats per ray.
+void or_camera_rays(const OrCamera *c, int pixelFilter, int W, int H, int spp, int frameID, float *out) {
+  const Camera cam = makeCamera({c->pos[0], c->pos[1], c->pos[2]}, {c->dir[0], c->dir[1], c->dir[2]},
+                                {c->up[0], c->up[1], c->up[2]}, c->fovy, c->aspect, c->nearClip);
+  PixelFilter pf;
+  pf.init(pixelFilter);
+  const V2 rcpSize = {1.f / float(W), 1.f / float(H)};
+  const uint32_t start = uint32_t(frameID * spp + 1);
+  for (int y = 0; y < H; y++)
+    for (int x = 0; x < W; x++)
+      for (int sp = 0; sp < spp; sp++) {
+        const uint32_t sid = start + sp;
+        const V2 ps = {Halton_sample2(sid), CranleyPattersonRotation(Halton_sample3(sid), 1.f / 6.f)};
+        const V2 pfs = pf.sample(ps);
+        const V2 center = {(float(x) + 0.5f) * rcpSize.x, (float(y) + 0.5f) * rcpSize.y};
+        const V2 screen = {center.x + pfs.x * rcpSize.x, center.y + pfs.y * rcpSize.y};
+        const Ray r = cameraRay(cam, screen);
+        float *o = out + 8 * ((size_t(y) * W + x) * spp + sp);
+        o[0] = r.org.x;
+        o[1] = r.org.y;
+        o[2] = r.org.z;
+        o[3] = r.tnear;
+        o[4] = r.dir.x;
+        o[5] = r.dir.y;
+        o[6] = r.dir.z;
+        o[7] = r.tfar;
+      }
+}
+
+struct OrFrame {
+  float *color;      // W*H*4
+  float *depth;      // W*H
+  uint32_t *primID;  // W*H
+  uint32_t *geomID;
+  uint32_t *instID;
+};
+
+// Renders `frames` accumulated frames of the AO renderer; outputs the final
+// accumulation buffers.
+void or_render_ao(void *sp, const OrCamera *c, int pixelFilter, int W, int H, int spp, int aoSamples,
+                  float aoRadius, float aoIntensity, const float *bg, int frames, OrFrame *out, int nthreads) {
+  const Scene &s = *static_cast<Scene *>(sp);
+  const Camera cam = makeCamera({c->pos[0], c->pos[1], c->pos[2]}, {c->dir[0], c->dir[1], c->dir[2]},
+                                {c->up[0], c->up[1], c->up[2]}, c->fovy, c->aspect, c->nearClip);
+  PixelFilter pf;
+  pf.init(pixelFilter);
+  FrameBuffer fb;
+  fb.resize(W, H);
+  AOParams p = {spp, aoSamples, aoRadius, aoIntensity, {bg[0], bg[1], bg[2], bg[3]}};
+  for (int f = 0; f < frames; f++) renderAO(s, cam, pf, p, fb, nthreads);
+  const size_t N = size_t(W) * H;
+  std::memcpy(out->color, fb.color.data(), N * 4 * sizeof(float));
+  std::memcpy(out->depth, fb.depth.data(), N * sizeof(float));
+  std::memcpy(out->primID, fb.primID.data(), N * 4);
+  std::memcpy(out->geomID, fb.geomID.data(), N * 4);
+  std::memcpy(out->instID, fb.instID.data(), N * 4);
+}
+
+uint64_t or_ray_count(int reset) {
+  const uint64_t n = g_rayCount.load();
+  if (reset) g_rayCount.store(0);
+  return n;
+}
+
+// Sampler tables for the pinning test against the reference's tables.
+void or_tables(uint32_t *perm3, uint32_t *perm5, uint32_t *perm7, uint32_t *sobolRev) {
+  const Tables &t = tables();
+  std::memcpy(perm3, t.perm3, sizeof(t.perm3));
+  std::memcpy(perm5, t.perm5, sizeof(t.perm5));
+  std::memcpy(perm7, t.perm7, sizeof(t.perm7));
+  std::memcpy(sobolRev, t.sobolRev, sizeof(t.sobolRev));
+}
+
+}  // extern "C"

@@ -1,0 +1,280 @@
+// Oracle (test infrastructure only): camera, pixel filter, postIntersect,
+// framebuffer accumulation and the AO renderer; see render.h for citations.
+#include "render.h"
+
+#include <algorithm>
+
+namespace orc {
+
+const Tables &tables() {
+  static const Tables t;
+  return t;
+}
+
+std::atomic<uint64_t> g_rayCount{0};
+thread_local uint64_t tl_rays = 0;  // flushed into g_rayCount once per image row
+
+Camera makeCamera(V3 pos, V3 dir, V3 up, float fovy, float aspect, float nearClip) {
+  Camera c;
+  const float deg2rad = float(1.745329251994329576923690768489e-2);
+  const float ipy = 2.f * std::tan(deg2rad * (0.5f * fovy));
+  const float ipx = ipy * aspect;
+  V3 d00 = normalize(dir);
+  V3 du = normalize(cross(d00, up));
+  V3 dv = cross(du, d00);
+  du = du * ipx;
+  dv = dv * ipy;
+  d00 = d00 - 0.5f * du - 0.5f * dv;
+  c.org = pos;
+  c.dir_00 = d00;
+  c.du_size = du;
+  c.dv_up = dv;
+  c.nearClip = nearClip;
+  return c;
+}
+
+namespace {
+float create1D(int n, float *cdf) {
+  float sum = cdf[0];
+  for (int i = 1; i < n; i++) cdf[i] = sum += cdf[i];
+  const float rcpSum = 1.f / sum;
+  const float nextAfter1 = 0x1.000002p+0f;
+  for (int i = 0; i < n; i++) cdf[i] = cdf[i] >= sum ? nextAfter1 : cdf[i] * rcpSum;
+  return sum;
+}
+struct S1 {
+  int idx;
+  float frac;
+};
+S1 sample1D(int size, const float *cdf, float s) {
+  int first = 0, len = size;
+  while (len > 0) {
+    const int half = len >> 1, mid = first + half;
+    if (s < cdf[mid]) {
+      len = half;
+    } else {
+      first = mid + 1;
+      len -= half + 1;
+    }
+  }
+  const float bef = first == 0 ? 0.f : cdf[first - 1];
+  const float dpdf = cdf[first] - bef;
+  return {first, (s - bef) / dpdf};
+}
+}  // namespace
+
+void PixelFilter::init(int t) {
+  type = t;
+  if (t == PF_POINT) {
+    width = 0.f;
+    return;
+  }
+  if (t == PF_BOX) {
+    width = 1.f;
+    return;
+  }
+  width = t == PF_MITCHELL ? 4.f : 3.f;
+  lutW = int(std::ceil(width)) * 5;
+  cdf_x.assign(size_t(lutW) * lutW, 0.f);
+  cdf_y.assign(lutW, 0.f);
+  for (int y = 0; y < lutW; y++) {
+    const float fy = (y + 0.5f) * (1.f / float(lutW));
+    for (int x = 0; x < lutW; x++) {
+      const float fx = (x + 0.5f) * (1.f / float(lutW));
+      const V2 c = {(fx - 0.5f) * width, (fy - 0.5f) * width};
+      float e = 0.f;
+      if (t == PF_GAUSS) {
+        const float sigma = (0.5f * width) / 3.f;
+        e = std::exp(-0.5f * ((c.x * c.x + c.y * c.y) / (sigma * sigma)));
+      } else if (t == PF_MITCHELL) {
+        const float B = 1.f / 3.f, C = 1.f / 3.f;
+        const float tx = c.x / width * 4.f, ty = c.y / width * 4.f;
+        const float f = std::sqrt(tx * tx + ty * ty), f2 = f * f, f3 = f2 * f;
+        if (f < 1.f)
+          e = (1.f / 6.f) * ((12.f - 9.f * B - 6.f * C) * f3 + (-18.f + 12.f * B + 6.f * C) * f2 +
+                             (6.f - 2.f * B));
+        else if (f < 2.f)
+          e = (1.f / 6.f) * ((-B - 6.f * C) * f3 + (6.f * B + 30.f * C) * f2 +
+                             (-12.f * B - 48.f * C) * f + (8.f * B + 24.f * C));
+      } else {
+        const float f = std::sqrt(c.x * c.x + c.y * c.y) + width / 2.f;
+        const float w = 1.f / width;
+        const float pi2 = float(2.0 * M_PI);
+        e = 0.35875f - 0.48829f * std::cos(pi2 * f * w) + 0.14128f * std::cos(2.f * pi2 * f * w) -
+            0.01168f * std::cos(3.f * pi2 * f * w);
+      }
+      cdf_x[size_t(y) * lutW + x] = std::max(0.f, e);
+    }
+    cdf_y[y] = create1D(lutW, &cdf_x[size_t(y) * lutW]);
+  }
+  create1D(lutW, cdf_y.data());
+}
+
+V2 PixelFilter::sample(V2 s) const {
+  if (type == PF_POINT) return {0.f, 0.f};
+  if (type == PF_BOX) return {(s.x - 0.5f) * width, (s.y - 0.5f) * width};
+  const S1 sy = sample1D(lutW, cdf_y.data(), s.y);
+  const S1 sx = sample1D(lutW, &cdf_x[size_t(sy.idx) * lutW], s.x);
+  const float r = 1.f / float(lutW);
+  const V2 uv = {(sx.idx + sx.frac) * r, (sy.idx + sy.frac) * r};
+  return {(uv.x - 0.5f) * width, (uv.y - 0.5f) * width};
+}
+
+DG postIntersect(const Scene &s, const Ray &ray, const Hit &hit) {
+  DG dg;
+  dg.primID = hit.primID;
+  dg.geomID = hit.geomID;
+  dg.instID = hit.instID;
+  dg.P = ray.org + hit.t * ray.dir;
+  // find the entry of this (instance, model)
+  const InstanceEntry *e = nullptr;
+  for (const auto &en : s.entries)
+    if (en.instID == hit.instID && en.geomID == hit.geomID) {
+      e = &en;
+      break;
+    }
+  const Geometry &g = s.geoms[e->geom];
+  V3 Ng = hit.Ng, Ns = hit.Ng;
+  float eps;
+  if (g.type == 0) {
+    const V3 a = g.verts[g.index[3 * hit.primID]], b = g.verts[g.index[3 * hit.primID + 1]],
+             c = g.verts[g.index[3 * hit.primID + 2]];
+    eps = reduce_max(vmax(vmax(vabs(a), vabs(b)), vabs(c))) * ulpEpsilon;
+  } else {
+    eps = g.spheres[hit.primID].w * ulpEpsilon;
+  }
+  // Instance_postIntersect: normals by the inverse transpose, epsilon by the
+  // largest diagonal scale
+  const L3 it = transposed(e->rcp.l);
+  Ns = xfmVector(it, Ns);
+  Ng = xfmVector(it, Ng);
+  eps *= std::fmax(std::fabs(e->xfm.l.vx.x), std::fmax(std::fabs(e->xfm.l.vy.y), std::fabs(e->xfm.l.vz.z)));
+  // calcEpsilon(P, dir, t)
+  const float e2 = std::fmax(reduce_max(vabs(dg.P)), reduce_max(vabs(ray.dir)) * hit.t) * ulpEpsilon;
+  dg.epsilon = std::fmax(eps, e2);
+  V3 ffnng = normalize(Ng);
+  Ng = ffnng;
+  Ns = normalize(Ns);
+  if (dot(ray.dir, Ng) >= 0.f) {
+    ffnng = -ffnng;
+    Ng = -Ng;
+  }
+  if (dot(Ng, Ns) < 0.f) Ns = -Ns;
+  dg.Ng = Ng;
+  dg.Ns = Ns;
+  dg.P = dg.P + dg.epsilon * ffnng;
+  return dg;
+}
+
+void fbAccumulate(FrameBuffer &fb, int x, int y, const ScreenSample &s) {
+  const size_t i = size_t(y) * fb.W + x;
+  const float accScale = 1.f / float(fb.frameID + 1);
+  const float c[4] = {s.rgb.x, s.rgb.y, s.rgb.z, s.alpha};
+  for (int k = 0; k < 4; k++)
+    fb.color[4 * i + k] = accScale > 0.8f ? c[k] : lerpf(accScale, fb.color[4 * i + k], c[k]);
+  bool upd = fb.frameID == 0;
+  if (fb.frameID > 0 && std::fabs(s.z) < std::fabs(fb.depth[i])) upd = true;
+  if (upd) {
+    fb.depth[i] = s.z;
+    fb.primID[i] = s.primID;
+    fb.geomID[i] = s.geomID;
+    fb.instID[i] = s.instID;
+  }
+}
+
+// ---------------------------------------------------------------- AO renderer
+// AORenderer_renderSample (render/ao/AORenderer.ispc:23-149),
+// AORenderer_computeShading (render/ao/surfaces.ispc:44-74),
+// computeAO (render/util.ispc:12-54).
+static float computeAO(const Scene &s, const DG &dg, int sampleCnt, float aoRadius, int px, int py,
+                       uint32_t sampleZ) {
+  const uint32_t accumID = sampleZ * uint32_t(sampleCnt);
+  uint32_t t0 = uint32_t(px), t1 = uint32_t(py);
+  tea8(t0, t1);
+  const V2 rot = {to_float_unorm(t0), to_float_unorm(t1)};
+  int hits = 0;
+  const L3 l2w = frame(dg.Ns);
+  for (int i = 0; i < sampleCnt; i++) {
+    const float hx = PermHalton_sample5(accumID + i), hy = PermHalton_sample7(accumID + i);
+    const float rx = CranleyPattersonRotation(hx, rot.x), ry = CranleyPattersonRotation(hy, rot.y);
+    // cosineSampleHemisphere (math/sampling.ih:49-56)
+    const float phi = float(2.0 * M_PI) * rx;
+    const float cosT = std::sqrt(ry), sinT = std::sqrt(1.f - ry);
+    const V3 local = {std::cos(phi) * sinT, std::sin(phi) * sinT, cosT};
+    const V3 dir = xfmVector(l2w, local);
+    if (dot(dir, dg.Ns) < 0.01f) {
+      hits++;
+      continue;
+    }
+    tl_rays++;
+    if (s.occluded({dg.P, dg.epsilon, dir, aoRadius})) hits++;
+  }
+  return 1.f - float(hits) / float(sampleCnt);
+}
+
+void renderAO(const Scene &s, const Camera &cam, const PixelFilter &pf, const AOParams &p, FrameBuffer &fb,
+              int nthreads) {
+  const int W = fb.W, H = fb.H;
+  const V2 rcpSize = {1.f / float(W), 1.f / float(H)};
+  const uint32_t startSampleID = uint32_t(fb.frameID * p.spp + 1);
+  parallelRows(H, nthreads, [&](int y) {
+    for (int x = 0; x < W; x++) {
+      ScreenSample acc;
+      for (int sp = 0; sp < p.spp; sp++) {
+        const uint32_t sid = startSampleID + sp;
+        const V2 ps = {Halton_sample2(sid), CranleyPattersonRotation(Halton_sample3(sid), 1.f / 6.f)};
+        const V2 pfs = pf.sample(ps);
+        const V2 center = {(float(x) + 0.5f) * rcpSize.x, (float(y) + 0.5f) * rcpSize.y};
+        const V2 screen = {center.x + pfs.x * rcpSize.x, center.y + pfs.y * rcpSize.y};
+        Ray ray = cameraRay(cam, screen);
+        ScreenSample smp;
+        V4 out = {0, 0, 0, 0};
+        bool first = true;
+        const float tfar0 = ray.tfar;
+        while (out.w < 0.99f) {
+          Hit hit;
+          tl_rays++;
+          const bool h = s.intersect(ray, hit);
+          V4 blended;
+          if (h) {
+            const DG dg = postIntersect(s, ray, hit);
+            const float eye = std::fabs(dot(dg.Ns, ray.dir));
+            float intensity = eye;
+            if (p.aoSamples > 0 && p.aoIntensity > 0.01f) {
+              const float ao = computeAO(s, dg, p.aoSamples, p.aoRadius, x, y, sid);
+              intensity *= (1.f - p.aoIntensity) + ao * p.aoIntensity;
+            }
+            blended = {intensity, intensity, intensity, 1.f};
+            if (first) {
+              smp.z = hit.t;
+              smp.primID = dg.primID;
+              smp.geomID = dg.geomID;
+              smp.instID = dg.instID;
+            }
+            ray.tnear = hit.t + dg.epsilon;
+            ray.tfar = tfar0;
+          } else {
+            blended = p.bgColor;
+            if (first) smp.z = ray.tfar;
+          }
+          const float f = 1.f - out.w;
+          out = {out.x + f * blended.x, out.y + f * blended.y, out.z + f * blended.z, out.w + f * blended.w};
+          first = false;
+          if (!h) break;
+        }
+        smp.rgb = {out.x, out.y, out.z};
+        smp.alpha = out.w;
+        accumulateScreen(acc, smp);
+      }
+      const float rspp = 1.f / float(p.spp);
+      acc.rgb = acc.rgb * rspp;
+      acc.alpha *= rspp;
+      fbAccumulate(fb, x, y, acc);
+    }
+    g_rayCount.fetch_add(tl_rays);
+    tl_rays = 0;
+  });
+  fb.frameID++;
+}
+
+}  // namespace orc

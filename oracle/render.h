@@ -1,0 +1,123 @@
+// Oracle (test infrastructure only): camera, pixel filter, screen samples,
+// differential geometry and framebuffer accumulation shared by the CPU
+// renderers.
+//   camera:  modules/cpu/camera/PerspectiveCamera.cpp:30-117, .ispc:16-64,
+//            modules/cpu/camera/Camera.cpp:38-52
+//   filter:  modules/cpu/pf/PixelFilter.cpp:28-55, LUTPixelFilter.ispc:60-144,
+//            PixelFilter.ih:20-30, math/Distribution1D.ispc, Distribution2D.ispc
+//   pixel:   modules/cpu/render/RendererRenderTaskFn.inl:5-88, ScreenSample.ih
+//   dg:      modules/cpu/common/World.ih:389-465, Instance.ih:44-107,
+//            geometry/GeometricModel.ih:47-76, Mesh.ispc:30-33,178+,
+//            Spheres.ispc:24-42, common/DifferentialGeometry.ih:46-58
+//   fb:      modules/cpu/fb/LocalFB.ispc:14-78, FrameBuffer.ih:21-22
+#pragma once
+#include <atomic>
+#include <cmath>
+#include <cstdint>
+#include <thread>
+#include <vector>
+
+#include "samplers.h"
+#include "scene.h"
+
+namespace orc {
+
+struct Camera {
+  V3 org, dir_00, du_size, dv_up;
+  float nearClip;
+};
+
+// PerspectiveCamera::commit without stereo/aperture/motion blur
+Camera makeCamera(V3 pos, V3 dir, V3 up, float fovy, float aspect, float nearClip);
+
+inline Ray cameraRay(const Camera &c, V2 screen) {
+  const V3 d = c.dir_00 + screen.x * c.du_size + screen.y * c.dv_up;
+  return {c.org, c.nearClip, normalize(d), INFINITY};
+}
+
+enum PixelFilterType { PF_POINT = 0, PF_BOX = 1, PF_GAUSS = 2, PF_MITCHELL = 3, PF_BLACKMAN_HARRIS = 4 };
+
+struct PixelFilter {
+  int type = PF_GAUSS;
+  float width = 3.f;
+  int lutW = 15;
+  std::vector<float> cdf_x, cdf_y;
+  void init(int t);
+  V2 sample(V2 s) const;
+};
+
+struct DG {
+  V3 P, Ng, Ns;
+  float epsilon;
+  uint32_t primID, geomID, instID;
+};
+
+// postIntersect with DG_NG | DG_NS | DG_NORMALIZE | DG_FACEFORWARD (meshes
+// carry no per-vertex normals or colours in these scenes)
+DG postIntersect(const Scene &s, const Ray &ray, const Hit &hit);
+
+struct FrameBuffer {
+  int W = 0, H = 0;
+  int frameID = 0;
+  std::vector<float> color;  // RGBA
+  std::vector<float> depth;
+  std::vector<uint32_t> primID, geomID, instID;
+  void resize(int w, int h) {
+    W = w;
+    H = h;
+    color.assign(size_t(W) * H * 4, 0.f);
+    depth.assign(size_t(W) * H, INFINITY);
+    primID.assign(size_t(W) * H, INVALID_ID);
+    geomID.assign(size_t(W) * H, INVALID_ID);
+    instID.assign(size_t(W) * H, INVALID_ID);
+    frameID = 0;
+  }
+};
+
+struct ScreenSample {
+  V3 rgb = v3(0.f);
+  float alpha = 0.f;
+  float z = INFINITY;
+  uint32_t primID = INVALID_ID, geomID = INVALID_ID, instID = INVALID_ID;
+};
+
+inline void accumulateScreen(ScreenSample &acc, const ScreenSample &s) {
+  acc.rgb = acc.rgb + s.rgb;
+  acc.alpha += s.alpha;
+  if (std::fabs(s.z) < std::fabs(acc.z)) {
+    acc.z = s.z;
+    acc.primID = s.primID;
+    acc.geomID = s.geomID;
+    acc.instID = s.instID;
+  }
+}
+
+// LocalFB_accumulateSample: lerp accumulation, ID buffers from the closest |z|
+void fbAccumulate(FrameBuffer &fb, int x, int y, const ScreenSample &s);
+
+template <class F>
+void parallelRows(int H, int nthreads, F f) {
+  if (nthreads <= 0) nthreads = int(std::thread::hardware_concurrency());
+  if (nthreads <= 0) nthreads = 1;
+  std::vector<std::thread> th;
+  for (int t = 0; t < nthreads; t++)
+    th.emplace_back([=]() {
+      for (int y = t; y < H; y += nthreads) f(y);
+    });
+  for (auto &x : th) x.join();
+}
+
+constexpr float ulpEpsilon = 0x1.0fp-21f;
+
+// rays traced by the renderers since the last reset (CPU-baseline Mrays/s)
+extern std::atomic<uint64_t> g_rayCount;
+
+struct AOParams {
+  int spp, aoSamples;
+  float aoRadius, aoIntensity;
+  V4 bgColor;
+};
+void renderAO(const Scene &s, const Camera &cam, const PixelFilter &pf, const AOParams &p, FrameBuffer &fb,
+              int nthreads);
+
+}  // namespace orc

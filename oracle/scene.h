@@ -1,0 +1,75 @@
+// Oracle (test infrastructure only): two-level scene, CPU binned-SAH BVH and
+// ray queries standing in for the reference's Embree calls.
+//   modules/cpu/common/World.ih:29-52   traceGeometryRay -> rtcIntersectV
+//   modules/cpu/common/World.ih:311-380 isOccluded -> rtcOccludedV
+//   modules/cpu/common/Group.cpp:17-31,69-143, World.cpp:16-35,70-188  (BLAS/TLAS)
+// Embree 4.3.3 (not vendored) is the reference's intersector.  The oracle
+// uses the published watertight ray/triangle test (Woop, Benthin, Wald 2013)
+// and the geometric ray/sphere test of Haines et al. (Ray Tracing Gems, 2019,
+// ch. 7), which is also the form of Embree's sphere intersector.  Closest-hit
+// ties at equal t are broken by the smallest (instID, geomID, primID), so the
+// result does not depend on traversal order.
+#pragma once
+#include <cstdint>
+#include <vector>
+
+#include "vecmath.h"
+
+namespace orc {
+
+constexpr uint32_t INVALID_ID = 0xffffffffu;
+
+struct Ray {
+  V3 org;
+  float tnear;
+  V3 dir;
+  float tfar;
+};
+
+struct Hit {
+  float t, u, v;
+  V3 Ng;  // unnormalised geometric normal in object space
+  uint32_t primID, geomID, instID;
+};
+
+struct Box {
+  V3 lo, hi;
+};
+
+struct Geometry {
+  int type;  // 0 triangles, 1 spheres
+  std::vector<V3> verts;
+  std::vector<uint32_t> index;  // 3 per triangle
+  std::vector<V4> spheres;      // center, radius
+  // BVH2 (binned SAH)
+  struct Node {
+    Box box;
+    int32_t left;   // >=0 internal: left child index (right = left+1); <0 leaf
+    uint32_t first, count;
+  };
+  std::vector<Node> nodes;
+  std::vector<uint32_t> prims;
+  uint32_t nprims() const { return type == 0 ? uint32_t(index.size() / 3) : uint32_t(spheres.size()); }
+  Box primBox(uint32_t p) const;
+  void build();
+};
+
+struct InstanceEntry {
+  int geom;          // index into Scene::geoms
+  uint32_t instID;   // world instance index
+  uint32_t geomID;   // model index within the instance's group
+  bool identity;
+  A3 xfm, rcp;
+  Box worldBox;
+};
+
+struct Scene {
+  std::vector<Geometry> geoms;
+  std::vector<InstanceEntry> entries;
+  void commit();
+  // closest hit; returns false on miss
+  bool intersect(const Ray &ray, Hit &hit) const;
+  bool occluded(const Ray &ray) const;
+};
+
+}  // namespace orc

@@ -1,0 +1,268 @@
+"""ospray_gb300: GB300-native device module for the OSPRay render path.
+
+The compute path is the CUDA library ``_build/libb200.so`` (C ABI in
+``include/b200.h``); this package is a thin ctypes layer over it, used by the
+tests, the benchmark and Python callers.  There is no CPU fallback: every
+call goes to the CUDA library, and importing a renderer without the built
+library raises.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+
+_lib = None
+_scenes = None
+
+# OSPFrameBufferChannel bits
+FB_COLOR, FB_DEPTH, FB_ACCUM, FB_VARIANCE = 1, 2, 4, 8
+FB_NORMAL, FB_ALBEDO = 16, 32
+FB_ID_PRIMITIVE, FB_ID_OBJECT, FB_ID_INSTANCE = 128, 256, 512
+# OSPPixelFilterType
+PF_POINT, PF_BOX, PF_GAUSS, PF_MITCHELL, PF_BLACKMAN_HARRIS = range(5)
+
+ERRORS = {0: "OSP_NO_ERROR", 1: "OSP_UNKNOWN_ERROR", 2: "OSP_INVALID_ARGUMENT",
+          3: "OSP_INVALID_OPERATION", 4: "OSP_OUT_OF_MEMORY", 5: "OSP_UNSUPPORTED_CPU",
+          6: "OSP_VERSION_MISMATCH"}
+
+
+class B200Error(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s: %s" % (ERRORS.get(code, code), msg))
+        self.code = code
+
+
+class CameraDesc(ctypes.Structure):
+    _fields_ = [("position", ctypes.c_float * 3), ("direction", ctypes.c_float * 3),
+                ("up", ctypes.c_float * 3), ("fovy", ctypes.c_float), ("aspect", ctypes.c_float),
+                ("nearClip", ctypes.c_float)]
+
+
+class AOParams(ctypes.Structure):
+    _fields_ = [("pixelSamples", ctypes.c_int), ("aoSamples", ctypes.c_int),
+                ("aoDistance", ctypes.c_float), ("aoIntensity", ctypes.c_float),
+                ("backgroundColor", ctypes.c_float * 4), ("pixelFilter", ctypes.c_int),
+                ("collectStats", ctypes.c_int)]
+
+
+def lib_path():
+    return os.path.join(BUILD, "libb200.so")
+
+
+def lib():
+    """The loaded CUDA library; raises if it was not built."""
+    global _lib
+    if _lib is None:
+        path = lib_path()
+        if not os.path.exists(path):
+            raise RuntimeError("b200 CUDA library missing (%s): run __graft_entry__.build()" % path)
+        L = ctypes.CDLL(path)
+        P, I, I64, U32, F = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctypes.c_uint32, ctypes.c_float
+        sig = {
+            "b200_device_create": (I, [I, ctypes.POINTER(P)]),
+            "b200_device_release": (I, [P]),
+            "b200_device_last_error": (ctypes.c_char_p, [P]),
+            "b200_device_stream": (P, [P]),
+            "b200_device_sync": (I, [P]),
+            "b200_scene_create": (I, [P, ctypes.POINTER(P)]),
+            "b200_scene_release": (I, [P]),
+            "b200_scene_add_mesh": (I, [P, P, I64, P, I64, ctypes.POINTER(I)]),
+            "b200_scene_add_spheres": (I, [P, P, I64, ctypes.POINTER(I)]),
+            "b200_scene_add_instance": (I, [P, I, U32, U32, P, I]),
+            "b200_scene_commit": (I, [P]),
+            "b200_scene_bounds": (I, [P, P]),
+            "b200_scene_stats": (I, [P, P]),
+            "b200_scene_counters": (I, [P, P, I]),
+            "b200_trace": (I, [P, P, I64, I, P, P, P]),
+            "b200_frame_create": (I, [P, I, I, U32, ctypes.POINTER(P)]),
+            "b200_frame_release": (I, [P]),
+            "b200_frame_reset": (I, [P]),
+            "b200_frame_id": (I, [P]),
+            "b200_frame_channel": (P, [P, U32]),
+            "b200_frame_read": (I, [P, U32, P, ctypes.c_size_t]),
+            "b200_render_ao": (I, [P, ctypes.POINTER(CameraDesc), ctypes.POINTER(AOParams), P, P]),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def scenes_lib():
+    global _scenes
+    if _scenes is None:
+        path = os.path.join(BUILD, "libb200_scenes.so")
+        if not os.path.exists(path):
+            raise RuntimeError("scene generator library missing (%s): run __graft_entry__.build()" % path)
+        _scenes = ctypes.CDLL(path)
+    return _scenes
+
+
+def _ptr(a):
+    return ctypes.c_void_p(a.ctypes.data) if a is not None else None
+
+
+class Device:
+    def __init__(self, cuda_device=0):
+        self._h = ctypes.c_void_p()
+        self._check(lib().b200_device_create(cuda_device, ctypes.byref(self._h)), None)
+
+    def _check(self, code, h="self"):
+        if code != 0:
+            msg = lib().b200_device_last_error(self._h if h == "self" else None)
+            raise B200Error(code, (msg or b"").decode())
+
+    @property
+    def stream(self):
+        return lib().b200_device_stream(self._h)
+
+    def sync(self):
+        self._check(lib().b200_device_sync(self._h))
+
+    def release(self):
+        if self._h:
+            lib().b200_device_release(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.release()
+        except Exception:
+            pass
+
+
+class Scene:
+    """A committed world: geometries (BLAS each) and instance entries (TLAS)."""
+
+    def __init__(self, device):
+        self.device = device
+        self._h = ctypes.c_void_p()
+        device._check(lib().b200_scene_create(device._h, ctypes.byref(self._h)))
+        self._keep = []
+
+    def add_mesh(self, vertex, index):
+        v = np.ascontiguousarray(vertex, dtype=np.float32).reshape(-1, 3)
+        i = np.ascontiguousarray(index, dtype=np.uint32).reshape(-1, 3)
+        g = ctypes.c_int()
+        self.device._check(lib().b200_scene_add_mesh(self._h, _ptr(v), len(v), _ptr(i), len(i), ctypes.byref(g)))
+        return g.value
+
+    def add_spheres(self, xyzr):
+        s = np.ascontiguousarray(xyzr, dtype=np.float32).reshape(-1, 4)
+        g = ctypes.c_int()
+        self.device._check(lib().b200_scene_add_spheres(self._h, _ptr(s), len(s), ctypes.byref(g)))
+        return g.value
+
+    def add_instance(self, geom, inst_id, geom_id, xfm=None, material=-1):
+        x = None if xfm is None else np.ascontiguousarray(xfm, dtype=np.float32).reshape(12)
+        self.device._check(lib().b200_scene_add_instance(self._h, geom, inst_id, geom_id, _ptr(x), material))
+
+    def commit(self):
+        self.device._check(lib().b200_scene_commit(self._h))
+
+    def bounds(self):
+        b = np.zeros(6, np.float32)
+        self.device._check(lib().b200_scene_bounds(self._h, _ptr(b)))
+        return b
+
+    def stats(self):
+        s = np.zeros(3, np.int64)
+        self.device._check(lib().b200_scene_stats(self._h, _ptr(s)))
+        return s
+
+    def counters(self, reset=False):
+        """[rays, node visits, triangle tests, sphere tests] from stats renders."""
+        c = np.zeros(4, np.int64)
+        self.device._check(lib().b200_scene_counters(self._h, _ptr(c), int(bool(reset))))
+        return c
+
+    def trace(self, rays_ptr, n, hit_f_ptr, hit_id_ptr, occlusion=False, stream=None):
+        """Device pointers (e.g. torch tensor data_ptr())."""
+        self.device._check(lib().b200_trace(self._h, ctypes.c_void_p(rays_ptr), n, int(bool(occlusion)),
+                                            ctypes.c_void_p(hit_f_ptr),
+                                            ctypes.c_void_p(hit_id_ptr) if hit_id_ptr else None,
+                                            ctypes.c_void_p(stream) if stream else None))
+
+    def release(self):
+        if self._h:
+            lib().b200_scene_release(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.release()
+        except Exception:
+            pass
+
+
+class Frame:
+    def __init__(self, device, width, height, channels=FB_COLOR | FB_DEPTH | FB_ACCUM):
+        self.device = device
+        self.width, self.height, self.channels = width, height, channels
+        self._h = ctypes.c_void_p()
+        device._check(lib().b200_frame_create(device._h, width, height, channels, ctypes.byref(self._h)))
+
+    def reset(self):
+        self.device._check(lib().b200_frame_reset(self._h))
+
+    @property
+    def frame_id(self):
+        return lib().b200_frame_id(self._h)
+
+    def channel_ptr(self, ch):
+        return lib().b200_frame_channel(self._h, ch)
+
+    def read(self, ch=FB_COLOR):
+        n = self.width * self.height
+        if ch in (FB_COLOR, FB_VARIANCE):
+            out = np.empty((self.height, self.width, 4), np.float32)
+        elif ch in (FB_NORMAL, FB_ALBEDO):
+            out = np.empty((self.height, self.width, 3), np.float32)
+        elif ch == FB_DEPTH:
+            out = np.empty((self.height, self.width), np.float32)
+        else:
+            out = np.empty((self.height, self.width), np.uint32)
+        self.device._check(lib().b200_frame_read(self._h, ch, _ptr(out), out.nbytes))
+        assert out.size in (n, 3 * n, 4 * n)
+        return out
+
+    def release(self):
+        if self._h:
+            lib().b200_frame_release(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.release()
+        except Exception:
+            pass
+
+
+def camera_desc(position, direction, up=(0, 1, 0), fovy=60.0, aspect=1.0, near_clip=1e-6):
+    c = CameraDesc()
+    c.position[:] = list(map(float, position))
+    c.direction[:] = list(map(float, direction))
+    c.up[:] = list(map(float, up))
+    c.fovy, c.aspect, c.nearClip = float(fovy), float(aspect), float(near_clip)
+    return c
+
+
+def ao_params(spp=1, ao_samples=1, ao_distance=1e20, ao_intensity=1.0, bg=(0, 0, 0, 0), pixel_filter=PF_GAUSS,
+              stats=False):
+    p = AOParams()
+    p.collectStats = int(bool(stats))
+    p.pixelSamples, p.aoSamples = int(spp), int(ao_samples)
+    p.aoDistance, p.aoIntensity = float(ao_distance), float(ao_intensity)
+    p.backgroundColor[:] = list(map(float, bg))
+    p.pixelFilter = int(pixel_filter)
+    return p
+
+
+def render_ao(scene, camera, params, frame, stream=None):
+    scene.device._check(lib().b200_render_ao(scene._h, ctypes.byref(camera), ctypes.byref(params), frame._h,
+                                             ctypes.c_void_p(stream) if stream else None))

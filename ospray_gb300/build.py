@@ -1,0 +1,79 @@
+"""Builds the b200 device library (CUDA, sm_103a) and the scene generator.
+
+    python -m ospray_gb300.build          # or __graft_entry__.build()
+
+Outputs go to ospray_gb300/_build/ (git-ignored): libb200.so (the C ABI of
+include/b200.h) and libb200_scenes.so (seeded synthetic scene generators).
+Translation units are compiled in parallel; a unit is rebuilt only when it or
+a header it may include is newer than its object file.
+"""
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+OUT = os.path.join(HERE, "_build")
+ROOT = os.path.dirname(HERE)
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ARCH + [
+    "-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr",
+    "-Xcompiler", "-fPIC,-ffp-contract=off", "-I" + os.path.join(ROOT, "include"),
+]
+CUDA_UNITS = ["bvh.cu", "render_ao.cu", "api.cu"]
+
+
+def nvcc():
+    for cand in (shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found")
+
+
+def _newest_header():
+    t = 0.0
+    for d in (CSRC, os.path.join(ROOT, "include")):
+        for f in os.listdir(d):
+            if f.endswith((".h", ".cuh")):
+                t = max(t, os.path.getmtime(os.path.join(d, f)))
+    return t
+
+
+def _run(cmd):
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("build failed: %s\n%s%s" % (" ".join(cmd), r.stdout, r.stderr))
+    return r
+
+
+def build(verbose=False):
+    os.makedirs(OUT, exist_ok=True)
+    hdr = _newest_header()
+    nv = nvcc()
+    jobs = []
+    objs = []
+    for u in CUDA_UNITS:
+        src = os.path.join(CSRC, u)
+        obj = os.path.join(OUT, u + ".o")
+        objs.append(obj)
+        if not os.path.exists(obj) or os.path.getmtime(obj) < max(os.path.getmtime(src), hdr):
+            jobs.append([nv] + NVCC_FLAGS + ["-c", src, "-o", obj])
+    with ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
+        for r in ex.map(_run, jobs):
+            if verbose and r.stderr:
+                print(r.stderr, file=sys.stderr)
+    lib = os.path.join(OUT, "libb200.so")
+    if jobs or not os.path.exists(lib):
+        _run([nv] + ARCH + ["-shared", "-o", lib] + objs)
+    scenes = os.path.join(OUT, "libb200_scenes.so")
+    src = os.path.join(CSRC, "scenegen.cpp")
+    if not os.path.exists(scenes) or os.path.getmtime(scenes) < os.path.getmtime(src):
+        _run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-o", scenes, src, "-lpthread"])
+    return lib
+
+
+if __name__ == "__main__":
+    print(build(verbose=True))

@@ -1,0 +1,626 @@
+// Host side of the b200 C ABI (include/b200.h): device, world, framebuffer
+// and renderer objects that own device memory and launch the kernels.
+// Every entry point catches its own failures and returns an OSPError code,
+// like the reference's API wrappers (ospray/api/API.cpp:28-66).
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/b200.h"
+#include "api_internal.h"
+
+namespace b200 {
+
+void check(cudaError_t e, const char *what) {
+  if (e != cudaSuccess) throw Error(e == cudaErrorMemoryAllocation ? B200_OUT_OF_MEMORY : B200_UNKNOWN_ERROR,
+                                    std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+namespace {
+
+// Halton digit permutations (Faure) and bit-reversed Joe-Kuo Sobol matrices;
+// the constructions behind modules/cpu/math/halton.inl and sobol.inl.
+void buildTables(SamplerTables &t) {
+  auto perm = [](uint32_t base, int nd, const uint32_t *sigma, uint32_t *out) {
+    uint32_t n = 1;
+    for (int k = 0; k < nd; k++) n *= base;
+    for (uint32_t i = 0; i < n; i++) {
+      uint32_t v = 0, x = i;
+      for (int k = 0; k < nd; k++, x /= base) v = v * base + sigma[x % base];
+      out[i] = v;
+    }
+  };
+  static const uint32_t f3[3] = {0, 1, 2}, f5[5] = {0, 3, 2, 1, 4}, f7[7] = {0, 2, 5, 3, 1, 4, 6};
+  perm(3, 5, f3, t.perm3);
+  perm(5, 3, f5, t.perm5);
+  perm(7, 3, f7, t.perm7);
+  struct Dim {
+    int s;
+    uint32_t a, m[3];
+  };
+  static const Dim dims[4] = {{1, 0, {1, 0, 0}}, {2, 1, {1, 3, 0}}, {3, 1, {1, 3, 1}}, {3, 2, {1, 1, 1}}};
+  for (int d = 0; d < 4; d++) {
+    uint64_t m[33];
+    const int s = dims[d].s;
+    for (int k = 1; k <= s; k++) m[k] = dims[d].m[k - 1];
+    for (int k = s + 1; k <= 32; k++) {
+      uint64_t v = m[k - s] ^ (m[k - s] << s);
+      for (int j = 1; j < s; j++)
+        if ((dims[d].a >> (s - 1 - j)) & 1u) v ^= m[k - j] << j;
+      m[k] = v;
+    }
+    for (int i = 0; i < 32; i++) {
+      uint32_t x = uint32_t(m[i + 1] << (31 - i)), r = 0;
+      for (int b = 0; b < 32; b++) r |= ((x >> b) & 1u) << (31 - b);
+      t.sobolRev[4 * i + d] = r;
+    }
+  }
+}
+
+// LUT importance table of a pixel filter (pf/LUTPixelFilter.ispc:60-144 with
+// Distribution1D_create / Distribution2D_init)
+void buildFilterLUT(int type, float &width, int &lutW, std::vector<float> &cx, std::vector<float> &cy) {
+  width = type == B200_PF_MITCHELL ? 4.f : 3.f;
+  lutW = int(std::ceil(width)) * 5;
+  cx.assign(size_t(lutW) * lutW, 0.f);
+  cy.assign(lutW, 0.f);
+  auto create1D = [](int n, float *cdf) {
+    float sum = cdf[0];
+    for (int i = 1; i < n; i++) cdf[i] = sum += cdf[i];
+    const float rcpSum = 1.f / sum;
+    for (int i = 0; i < n; i++) cdf[i] = cdf[i] >= sum ? 0x1.000002p+0f : cdf[i] * rcpSum;
+    return sum;
+  };
+  for (int y = 0; y < lutW; y++) {
+    const float fy = (y + 0.5f) * (1.f / float(lutW));
+    for (int x = 0; x < lutW; x++) {
+      const float fx = (x + 0.5f) * (1.f / float(lutW));
+      const float px = (fx - 0.5f) * width, py = (fy - 0.5f) * width;
+      float e = 0.f;
+      if (type == B200_PF_GAUSS) {
+        const float sigma = (0.5f * width) / 3.f;
+        e = std::exp(-0.5f * ((px * px + py * py) / (sigma * sigma)));
+      } else if (type == B200_PF_MITCHELL) {
+        const float B = 1.f / 3.f, C = 1.f / 3.f;
+        const float tx = px / width * 4.f, ty = py / width * 4.f;
+        const float f = std::sqrt(tx * tx + ty * ty), f2 = f * f, f3 = f2 * f;
+        if (f < 1.f)
+          e = (1.f / 6.f) * ((12.f - 9.f * B - 6.f * C) * f3 + (-18.f + 12.f * B + 6.f * C) * f2 + (6.f - 2.f * B));
+        else if (f < 2.f)
+          e = (1.f / 6.f) *
+              ((-B - 6.f * C) * f3 + (6.f * B + 30.f * C) * f2 + (-12.f * B - 48.f * C) * f + (8.f * B + 24.f * C));
+      } else {
+        const float f = std::sqrt(px * px + py * py) + width / 2.f;
+        const float w = 1.f / width;
+        const float pi2 = float(2.0 * M_PI);
+        e = 0.35875f - 0.48829f * std::cos(pi2 * f * w) + 0.14128f * std::cos(2.f * pi2 * f * w) -
+            0.01168f * std::cos(3.f * pi2 * f * w);
+      }
+      cx[size_t(y) * lutW + x] = e > 0.f ? e : 0.f;
+    }
+    cy[y] = create1D(lutW, &cx[size_t(y) * lutW]);
+  }
+  create1D(lutW, cy.data());
+}
+
+}  // namespace
+
+DeviceObj::DeviceObj(int cudaDev) : dev(cudaDev) {
+  check(cudaSetDevice(dev), "cudaSetDevice");
+  check(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
+  SamplerTables t;
+  buildTables(t);
+  check(cudaMalloc(&tables, sizeof(SamplerTables)), "cudaMalloc tables");
+  check(cudaMemcpy(tables, &t, sizeof(t), cudaMemcpyHostToDevice), "upload tables");
+  for (int type = B200_PF_GAUSS; type <= B200_PF_BLACKMAN_HARRIS; type++) {
+    std::vector<float> cx, cy;
+    float w;
+    int lw;
+    buildFilterLUT(type, w, lw, cx, cy);
+    FilterLUT &L = luts[type];
+    L.width = w;
+    L.lutW = lw;
+    check(cudaMalloc(&L.cdf_x, cx.size() * 4), "cudaMalloc lut");
+    check(cudaMalloc(&L.cdf_y, cy.size() * 4), "cudaMalloc lut");
+    check(cudaMemcpy(L.cdf_x, cx.data(), cx.size() * 4, cudaMemcpyHostToDevice), "upload lut");
+    check(cudaMemcpy(L.cdf_y, cy.data(), cy.size() * 4, cudaMemcpyHostToDevice), "upload lut");
+  }
+}
+
+DeviceObj::~DeviceObj() {
+  cudaSetDevice(dev);
+  cudaStreamSynchronize(stream);
+  cudaFree(tables);
+  for (auto &L : luts) {
+    cudaFree(L.cdf_x);
+    cudaFree(L.cdf_y);
+  }
+  cudaStreamDestroy(stream);
+}
+
+PixelFilterD DeviceObj::filter(int type) const {
+  PixelFilterD pf = {};
+  pf.type = type <= B200_PF_BOX ? type : 2;
+  if (type == B200_PF_POINT) pf.width = 0.f;
+  if (type == B200_PF_BOX) pf.width = 1.f;
+  if (type >= B200_PF_GAUSS && type <= B200_PF_BLACKMAN_HARRIS) {
+    pf.width = luts[type].width;
+    pf.lutW = luts[type].lutW;
+    pf.cdf_x = luts[type].cdf_x;
+    pf.cdf_y = luts[type].cdf_y;
+  }
+  return pf;
+}
+
+// PerspectiveCamera::commit without stereo, aperture or motion blur
+CameraD makeCamera(const b200_camera_desc &c) {
+  const V3 pos = mk(c.position[0], c.position[1], c.position[2]);
+  const V3 dir = mk(c.direction[0], c.direction[1], c.direction[2]);
+  const V3 up = mk(c.up[0], c.up[1], c.up[2]);
+  const float deg2rad = float(1.745329251994329576923690768489e-2);
+  const float ipy = 2.f * std::tan(deg2rad * (0.5f * c.fovy));
+  const float ipx = ipy * c.aspect;
+  V3 d00 = normalize(dir);
+  V3 du = normalize(cross(d00, up));
+  V3 dv = cross(du, d00);
+  du = mul(du, ipx);
+  dv = mul(dv, ipy);
+  d00 = sub(sub(d00, mul(0.5f, du)), mul(0.5f, dv));
+  CameraD cam;
+  cam.org = pos;
+  cam.dir_00 = d00;
+  cam.du_size = du;
+  cam.dv_up = dv;
+  cam.nearClip = c.nearClip > 0.f ? c.nearClip : 0.f;
+  return cam;
+}
+
+// rkcommon rcp(AffineSpace3f): adjoint / det in float, p' = -(l' p)
+static void rcpAffine(const float *X, float *R) {
+  const V3 vx = mk(X[0], X[4], X[8]), vy = mk(X[1], X[5], X[9]), vz = mk(X[2], X[6], X[10]);
+  const float det = dot(vx, cross(vy, vz));
+  const V3 a = cross(vy, vz), b = cross(vz, vx), c = cross(vx, vy);
+  // adjoint = transpose of (a, b, c) as columns -> rows a, b, c; inverse
+  // columns are the rows of (a b c) divided by det
+  const V3 ix = vdiv(mk(a.x, b.x, c.x), det), iy = vdiv(mk(a.y, b.y, c.y), det), iz = vdiv(mk(a.z, b.z, c.z), det);
+  const V3 p = mk(X[3], X[7], X[11]);
+  const V3 ip = add(add(mul(ix, p.x), mul(iy, p.y)), mul(iz, p.z));
+  const float r[12] = {ix.x, iy.x, iz.x, -ip.x, ix.y, iy.y, iz.y, -ip.y, ix.z, iy.z, iz.z, -ip.z};
+  std::memcpy(R, r, sizeof(r));
+}
+
+SceneObj::SceneObj(DeviceObj *d) : dev(d) {
+  check(cudaMalloc(&status, 16), "cudaMalloc status");
+  check(cudaMalloc(&counters, 64), "cudaMalloc counters");
+  check(cudaMemset(counters, 0, 64), "memset counters");
+  check(cudaMemset(status, 0, 16), "memset status");
+}
+
+SceneObj::~SceneObj() {
+  cudaStream_t st = dev->stream;
+  for (auto &g : geoms) {
+    freeBLAS(g.blas, st);
+    if (g.dverts) cudaFreeAsync(g.dverts, st);
+    if (g.dindex) cudaFreeAsync(g.dindex, st);
+    if (g.dsph) cudaFreeAsync(g.dsph, st);
+  }
+  if (tlas.nodes) cudaFreeAsync(tlas.nodes, st);
+  if (tlas.leafPrim) cudaFreeAsync(tlas.leafPrim, st);
+  if (dEntries) cudaFreeAsync(dEntries, st);
+  cudaStreamSynchronize(st);
+  cudaFree(status);
+  cudaFree(counters);
+}
+
+void SceneObj::commit() {
+  cudaStream_t st = dev->stream;
+  for (auto &g : geoms) {
+    if (g.built) continue;
+    if (g.type == GEOM_TRIANGLES)
+      check(buildTriangleBLAS(g.dverts, g.dindex, int(g.nprims), st, g.blas), "BLAS build");
+    else
+      check(buildSphereBLAS(g.dsph, int(g.nprims), st, g.blas), "BLAS build");
+    g.built = true;
+  }
+  // entries and their world boxes
+  std::vector<Entry> he(entries.size());
+  std::vector<float4> lo(entries.size()), hi(entries.size());
+  float wlo[3] = {INFINITY, INFINITY, INFINITY}, whi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  for (size_t i = 0; i < entries.size(); i++) {
+    const EntryH &e = entries[i];
+    const GeomObj &g = geoms[e.geom];
+    Entry &d = he[i];
+    std::memset(&d, 0, sizeof(d));
+    d.nodes = g.blas.bvh.nodes;
+    d.prims = g.blas.prims;
+    d.primIDs = g.blas.primIDs;
+    d.verts = g.dverts;
+    d.index = g.dindex;
+    d.spheres = g.dsph;
+    d.type = uint32_t(g.type);
+    d.instID = e.instID;
+    d.geomID = e.geomID;
+    d.identity = e.identity ? 1u : 0u;
+    std::memcpy(d.xfm.m, e.xfm, sizeof(e.xfm));
+    rcpAffine(e.xfm, d.rcp.m);
+    d.epsScale = std::fmax(std::fabs(e.xfm[0]), std::fmax(std::fabs(e.xfm[5]), std::fabs(e.xfm[10])));
+    d.materialID = uint32_t(e.material);
+    const float *blo = g.blas.bvh.lo, *bhi = g.blas.bvh.hi;
+    float l[3] = {INFINITY, INFINITY, INFINITY}, h[3] = {-INFINITY, -INFINITY, -INFINITY};
+    if (g.nprims == 0) {
+      l[0] = l[1] = l[2] = h[0] = h[1] = h[2] = 0.f;
+    } else if (e.identity) {
+      for (int k = 0; k < 3; k++) {
+        l[k] = blo[k];
+        h[k] = bhi[k];
+      }
+    } else {
+      for (int c = 0; c < 8; c++) {
+        const float p[3] = {c & 1 ? bhi[0] : blo[0], c & 2 ? bhi[1] : blo[1], c & 4 ? bhi[2] : blo[2]};
+        for (int r = 0; r < 3; r++) {
+          const float v = ((e.xfm[4 * r] * p[0] + e.xfm[4 * r + 1] * p[1]) + e.xfm[4 * r + 2] * p[2]) + e.xfm[4 * r + 3];
+          l[r] = std::fmin(l[r], v);
+          h[r] = std::fmax(h[r], v);
+        }
+      }
+      for (int k = 0; k < 3; k++) {
+        const float pad = 1e-6f * (std::fabs(l[k]) + std::fabs(h[k])) + 1e-30f;
+        l[k] -= pad;
+        h[k] += pad;
+      }
+    }
+    lo[i] = make_float4(l[0], l[1], l[2], 0.f);
+    hi[i] = make_float4(h[0], h[1], h[2], 0.f);
+    for (int k = 0; k < 3; k++) {
+      wlo[k] = std::fmin(wlo[k], l[k]);
+      whi[k] = std::fmax(whi[k], h[k]);
+    }
+  }
+  for (int k = 0; k < 3; k++) {
+    bounds[k] = wlo[k];
+    bounds[3 + k] = whi[k];
+  }
+  if (tlas.nodes) cudaFreeAsync(tlas.nodes, st);
+  if (tlas.leafPrim) cudaFreeAsync(tlas.leafPrim, st);
+  if (dEntries) cudaFreeAsync(dEntries, st);
+  tlas = WideBVH{};
+  dEntries = nullptr;
+  if (!entries.empty()) {
+    float4 *dlo, *dhi;
+    const size_t n = entries.size();
+    check(cudaMallocAsync(&dEntries, sizeof(Entry) * n, st), "alloc entries");
+    check(cudaMemcpyAsync(dEntries, he.data(), sizeof(Entry) * n, cudaMemcpyHostToDevice, st), "upload entries");
+    check(cudaMallocAsync(&dlo, sizeof(float4) * n, st), "alloc");
+    check(cudaMallocAsync(&dhi, sizeof(float4) * n, st), "alloc");
+    check(cudaMemcpyAsync(dlo, lo.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, st), "upload");
+    check(cudaMemcpyAsync(dhi, hi.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, st), "upload");
+    check(buildWide(dlo, dhi, int(n), st, tlas), "TLAS build");
+    cudaFreeAsync(dlo, st);
+    cudaFreeAsync(dhi, st);
+  }
+  check(cudaStreamSynchronize(st), "commit");
+  committed = true;
+}
+
+Scene SceneObj::view() const {
+  Scene s;
+  s.tlas = tlas.nodes;
+  s.tlasLeaf = tlas.leafPrim;
+  s.entries = dEntries;
+  s.nentries = int(entries.size());
+  s.ntlas = entries.empty() ? 0 : tlas.nnodes;
+  s.status = status;
+  s.counters = counters;
+  return s;
+}
+
+FrameObj::FrameObj(DeviceObj *d, int w, int h, uint32_t ch) : dev(d), W(w), H(h), channels(ch) {
+  const size_t n = size_t(w) * h;
+  auto alloc = [&](void **p, size_t bytes) {
+    check(cudaMalloc(p, bytes), "cudaMalloc framebuffer");
+    check(cudaMemset(*p, 0, bytes), "cudaMemset framebuffer");
+  };
+  alloc((void **)&color, n * sizeof(float4));
+  if (ch & B200_FB_DEPTH) alloc((void **)&depth, n * 4);
+  if (ch & B200_FB_VARIANCE) alloc((void **)&variance, n * sizeof(float4));
+  if (ch & B200_FB_NORMAL) alloc((void **)&normal, n * sizeof(float3));
+  if (ch & B200_FB_ALBEDO) alloc((void **)&albedo, n * sizeof(float3));
+  if (ch & B200_FB_ID_PRIMITIVE) alloc((void **)&primID, n * 4);
+  if (ch & B200_FB_ID_OBJECT) alloc((void **)&geomID, n * 4);
+  if (ch & B200_FB_ID_INSTANCE) alloc((void **)&instID, n * 4);
+}
+
+FrameObj::~FrameObj() {
+  cudaStreamSynchronize(dev->stream);
+  for (void *p : {(void *)color, (void *)depth, (void *)variance, (void *)normal, (void *)albedo, (void *)primID,
+                  (void *)geomID, (void *)instID})
+    if (p) cudaFree(p);
+}
+
+FrameD FrameObj::view() const {
+  FrameD f = {};
+  f.color = color;
+  f.depth = depth;
+  f.primID = primID;
+  f.geomID = geomID;
+  f.instID = instID;
+  f.variance = variance;
+  f.normal = normal;
+  f.albedo = albedo;
+  f.W = W;
+  f.H = H;
+  f.frameID = frameID;
+  return f;
+}
+
+void *FrameObj::channel(uint32_t c) const {
+  switch (c) {
+    case B200_FB_COLOR: return color;
+    case B200_FB_DEPTH: return depth;
+    case B200_FB_VARIANCE: return variance;
+    case B200_FB_NORMAL: return normal;
+    case B200_FB_ALBEDO: return albedo;
+    case B200_FB_ID_PRIMITIVE: return primID;
+    case B200_FB_ID_OBJECT: return geomID;
+    case B200_FB_ID_INSTANCE: return instID;
+    default: return nullptr;
+  }
+}
+
+size_t FrameObj::channelBytes(uint32_t c) const {
+  const size_t n = size_t(W) * H;
+  switch (c) {
+    case B200_FB_COLOR:
+    case B200_FB_VARIANCE: return n * 16;
+    case B200_FB_NORMAL:
+    case B200_FB_ALBEDO: return n * 12;
+    default: return n * 4;
+  }
+}
+
+}  // namespace b200
+
+using namespace b200;
+
+namespace {
+thread_local std::string g_noDeviceError;
+
+template <class F>
+int guarded(DeviceObj *dev, F f) {
+  try {
+    if (dev) check(cudaSetDevice(dev->dev), "cudaSetDevice");
+    f();
+    return B200_NO_ERROR;
+  } catch (const Error &e) {
+    (dev ? dev->lastError : g_noDeviceError) = e.what();
+    return e.code;
+  } catch (const std::bad_alloc &) {
+    (dev ? dev->lastError : g_noDeviceError) = "host out of memory";
+    return B200_OUT_OF_MEMORY;
+  } catch (const std::exception &e) {
+    (dev ? dev->lastError : g_noDeviceError) = e.what();
+    return B200_UNKNOWN_ERROR;
+  }
+}
+
+inline void require(bool c, const char *msg) {
+  if (!c) throw Error(B200_INVALID_ARGUMENT, msg);
+}
+}  // namespace
+
+extern "C" {
+
+int b200_device_create(int cuda_device, b200_device *out) {
+  if (!out) return B200_INVALID_ARGUMENT;
+  return guarded(nullptr, [&]() {
+    int n = 0;
+    check(cudaGetDeviceCount(&n), "cudaGetDeviceCount");
+    require(cuda_device >= 0 && cuda_device < n, "no such CUDA device");
+    *out = reinterpret_cast<b200_device>(new DeviceObj(cuda_device));
+  });
+}
+
+int b200_device_release(b200_device d) {
+  if (!d) return B200_INVALID_ARGUMENT;
+  delete reinterpret_cast<DeviceObj *>(d);
+  return B200_NO_ERROR;
+}
+
+const char *b200_device_last_error(b200_device d) {
+  return d ? reinterpret_cast<DeviceObj *>(d)->lastError.c_str() : g_noDeviceError.c_str();
+}
+
+void *b200_device_stream(b200_device d) { return d ? (void *)reinterpret_cast<DeviceObj *>(d)->stream : nullptr; }
+
+int b200_device_sync(b200_device d) {
+  if (!d) return B200_INVALID_ARGUMENT;
+  DeviceObj *dev = reinterpret_cast<DeviceObj *>(d);
+  return guarded(dev, [&]() { check(cudaStreamSynchronize(dev->stream), "sync"); });
+}
+
+int b200_scene_create(b200_device d, b200_scene *out) {
+  if (!d || !out) return B200_INVALID_ARGUMENT;
+  DeviceObj *dev = reinterpret_cast<DeviceObj *>(d);
+  return guarded(dev, [&]() { *out = reinterpret_cast<b200_scene>(new SceneObj(dev)); });
+}
+
+int b200_scene_release(b200_scene s) {
+  if (!s) return B200_INVALID_ARGUMENT;
+  SceneObj *sc = reinterpret_cast<SceneObj *>(s);
+  return guarded(sc->dev, [&]() { delete sc; });
+}
+
+int b200_scene_add_mesh(b200_scene s, const float *vertex, int64_t nverts, const uint32_t *index, int64_t ntris,
+                        int *geom_out) {
+  if (!s) return B200_INVALID_ARGUMENT;
+  SceneObj *sc = reinterpret_cast<SceneObj *>(s);
+  return guarded(sc->dev, [&]() {
+    require(nverts >= 0 && ntris >= 0 && (nverts == 0 || vertex) && (ntris == 0 || index), "bad mesh arrays");
+    require(ntris < (int64_t(1) << 31) && nverts < (int64_t(1) << 31), "mesh too large");
+    for (int64_t i = 0; i < 3 * ntris; i++) require(index[i] < uint64_t(nverts), "mesh index out of range");
+    GeomObj g;
+    g.type = GEOM_TRIANGLES;
+    g.nprims = ntris;
+    cudaStream_t st = sc->dev->stream;
+    check(cudaMallocAsync(&g.dverts, sizeof(float) * 3 * size_t(nverts > 0 ? nverts : 1), st), "alloc vertices");
+    check(cudaMallocAsync(&g.dindex, sizeof(uint32_t) * 3 * size_t(ntris > 0 ? ntris : 1), st), "alloc index");
+    if (nverts) check(cudaMemcpyAsync(g.dverts, vertex, 12 * size_t(nverts), cudaMemcpyHostToDevice, st), "upload");
+    if (ntris) check(cudaMemcpyAsync(g.dindex, index, 12 * size_t(ntris), cudaMemcpyHostToDevice, st), "upload");
+    check(cudaStreamSynchronize(st), "upload mesh");
+    sc->geoms.push_back(g);
+    if (geom_out) *geom_out = int(sc->geoms.size() - 1);
+  });
+}
+
+int b200_scene_add_spheres(b200_scene s, const float *spheres, int64_t n, int *geom_out) {
+  if (!s) return B200_INVALID_ARGUMENT;
+  SceneObj *sc = reinterpret_cast<SceneObj *>(s);
+  return guarded(sc->dev, [&]() {
+    require(n >= 0 && (n == 0 || spheres) && n < (int64_t(1) << 31), "bad sphere array");
+    GeomObj g;
+    g.type = GEOM_SPHERES;
+    g.nprims = n;
+    cudaStream_t st = sc->dev->stream;
+    check(cudaMallocAsync(&g.dsph, sizeof(float4) * size_t(n > 0 ? n : 1), st), "alloc spheres");
+    if (n) check(cudaMemcpyAsync(g.dsph, spheres, 16 * size_t(n), cudaMemcpyHostToDevice, st), "upload");
+    check(cudaStreamSynchronize(st), "upload spheres");
+    sc->geoms.push_back(g);
+    if (geom_out) *geom_out = int(sc->geoms.size() - 1);
+  });
+}
+
+int b200_scene_add_instance(b200_scene s, int geom, uint32_t inst_id, uint32_t geom_id, const float *xfm,
+                            int material_id) {
+  if (!s) return B200_INVALID_ARGUMENT;
+  SceneObj *sc = reinterpret_cast<SceneObj *>(s);
+  return guarded(sc->dev, [&]() {
+    require(geom >= 0 && size_t(geom) < sc->geoms.size(), "no such geometry");
+    EntryH e;
+    e.geom = geom;
+    e.instID = inst_id;
+    e.geomID = geom_id;
+    e.identity = xfm == nullptr;
+    static const float I[12] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0};
+    std::memcpy(e.xfm, xfm ? xfm : I, sizeof(e.xfm));
+    e.material = material_id;
+    sc->entries.push_back(e);
+    sc->committed = false;
+  });
+}
+
+int b200_scene_commit(b200_scene s) {
+  if (!s) return B200_INVALID_ARGUMENT;
+  SceneObj *sc = reinterpret_cast<SceneObj *>(s);
+  return guarded(sc->dev, [&]() { sc->commit(); });
+}
+
+int b200_scene_bounds(b200_scene s, float *box6) {
+  if (!s || !box6) return B200_INVALID_ARGUMENT;
+  SceneObj *sc = reinterpret_cast<SceneObj *>(s);
+  if (!sc->committed) return B200_INVALID_OPERATION;
+  std::memcpy(box6, sc->bounds, sizeof(sc->bounds));
+  return B200_NO_ERROR;
+}
+
+int b200_scene_stats(b200_scene s, int64_t *st) {
+  if (!s || !st) return B200_INVALID_ARGUMENT;
+  SceneObj *sc = reinterpret_cast<SceneObj *>(s);
+  st[0] = st[1] = 0;
+  for (auto &g : sc->geoms) {
+    st[0] += g.blas.bvh.nnodes;
+    st[1] += g.nprims;
+  }
+  st[2] = sc->tlas.nnodes;
+  return B200_NO_ERROR;
+}
+
+int b200_trace(b200_scene s, const float *rays, int64_t n, int occlusion, float *hit_f, uint32_t *hit_id,
+               void *stream) {
+  if (!s) return B200_INVALID_ARGUMENT;
+  SceneObj *sc = reinterpret_cast<SceneObj *>(s);
+  return guarded(sc->dev, [&]() {
+    if (!sc->committed) throw Error(B200_INVALID_OPERATION, "scene not committed");
+    require(n >= 0 && (n == 0 || (rays && hit_f && (occlusion || hit_id))), "bad ray arrays");
+    require((reinterpret_cast<uintptr_t>(rays) & 15) == 0, "rays must be 16-byte aligned");
+    cudaStream_t st = stream ? (cudaStream_t)stream : sc->dev->stream;
+    check(launchTrace(sc->view(), reinterpret_cast<const float4 *>(rays), n, occlusion, hit_f, hit_id, st),
+          "trace launch");
+  });
+}
+
+int b200_frame_create(b200_device d, int w, int h, uint32_t channels, b200_frame *out) {
+  if (!d || !out) return B200_INVALID_ARGUMENT;
+  DeviceObj *dev = reinterpret_cast<DeviceObj *>(d);
+  return guarded(dev, [&]() {
+    require(w > 0 && h > 0 && int64_t(w) * h < (int64_t(1) << 31), "bad framebuffer size");
+    *out = reinterpret_cast<b200_frame>(new FrameObj(dev, w, h, channels));
+  });
+}
+
+int b200_frame_release(b200_frame f) {
+  if (!f) return B200_INVALID_ARGUMENT;
+  FrameObj *fb = reinterpret_cast<FrameObj *>(f);
+  return guarded(fb->dev, [&]() { delete fb; });
+}
+
+int b200_frame_reset(b200_frame f) {
+  if (!f) return B200_INVALID_ARGUMENT;
+  reinterpret_cast<FrameObj *>(f)->frameID = 0;
+  return B200_NO_ERROR;
+}
+
+int b200_frame_id(b200_frame f) { return f ? reinterpret_cast<FrameObj *>(f)->frameID : -1; }
+
+void *b200_frame_channel(b200_frame f, uint32_t c) { return f ? reinterpret_cast<FrameObj *>(f)->channel(c) : nullptr; }
+
+int b200_frame_read(b200_frame f, uint32_t c, void *dst, size_t bytes) {
+  if (!f || !dst) return B200_INVALID_ARGUMENT;
+  FrameObj *fb = reinterpret_cast<FrameObj *>(f);
+  return guarded(fb->dev, [&]() {
+    void *src = fb->channel(c);
+    require(src != nullptr, "channel not present");
+    require(bytes >= fb->channelBytes(c), "destination too small");
+    check(cudaMemcpyAsync(dst, src, fb->channelBytes(c), cudaMemcpyDeviceToHost, fb->dev->stream), "read");
+    check(cudaStreamSynchronize(fb->dev->stream), "read");
+  });
+}
+
+int b200_render_ao(b200_scene s, const b200_camera_desc *camera, const b200_ao_params *p, b200_frame f, void *stream) {
+  if (!s || !camera || !p || !f) return B200_INVALID_ARGUMENT;
+  SceneObj *sc = reinterpret_cast<SceneObj *>(s);
+  FrameObj *fb = reinterpret_cast<FrameObj *>(f);
+  return guarded(sc->dev, [&]() {
+    if (!sc->committed) throw Error(B200_INVALID_OPERATION, "scene not committed");
+    require(p->pixelSamples >= 1 && p->aoSamples >= 0, "bad AO parameters");
+    require(p->pixelFilter >= B200_PF_POINT && p->pixelFilter <= B200_PF_BLACKMAN_HARRIS, "bad pixel filter");
+    AOParamsD d;
+    d.spp = p->pixelSamples;
+    d.aoSamples = p->aoSamples;
+    d.aoRadius = p->aoDistance;
+    d.aoIntensity = p->aoIntensity;
+    for (int k = 0; k < 4; k++) d.bg[k] = p->backgroundColor[k];
+    cudaStream_t st = stream ? (cudaStream_t)stream : sc->dev->stream;
+    check(launchRenderAO(sc->dev->tables, sc->view(), makeCamera(*camera), sc->dev->filter(p->pixelFilter), d,
+                         fb->view(), p->collectStats != 0, st),
+          "AO launch");
+    fb->frameID++;
+  });
+}
+
+int b200_scene_counters(b200_scene s, int64_t *out4, int reset) {
+  if (!s || !out4) return B200_INVALID_ARGUMENT;
+  SceneObj *sc = reinterpret_cast<SceneObj *>(s);
+  return guarded(sc->dev, [&]() {
+    unsigned long long c[4];
+    check(cudaStreamSynchronize(sc->dev->stream), "sync");
+    check(cudaMemcpy(c, sc->counters, sizeof(c), cudaMemcpyDeviceToHost), "read counters");
+    for (int k = 0; k < 4; k++) out4[k] = int64_t(c[k]);
+    if (reset) check(cudaMemset(sc->counters, 0, sizeof(c)), "reset counters");
+  });
+}
+
+}  // extern "C"

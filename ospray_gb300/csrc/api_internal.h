@@ -1,0 +1,89 @@
+// Host objects behind the b200 C ABI handles.
+#pragma once
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/b200.h"
+#include "bvh.h"
+#include "kernels.h"
+
+namespace b200 {
+
+struct Error : std::runtime_error {
+  int code;
+  Error(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+
+void check(cudaError_t e, const char *what);
+
+struct FilterLUT {
+  float width = 0.f;
+  int lutW = 0;
+  float *cdf_x = nullptr, *cdf_y = nullptr;
+};
+
+struct DeviceObj {
+  int dev;
+  cudaStream_t stream = nullptr;
+  std::string lastError;
+  SamplerTables *tables = nullptr;
+  FilterLUT luts[5];
+  explicit DeviceObj(int cudaDev);
+  ~DeviceObj();
+  PixelFilterD filter(int type) const;
+};
+
+struct GeomObj {
+  int type = GEOM_TRIANGLES;
+  int64_t nprims = 0;
+  float *dverts = nullptr;
+  uint32_t *dindex = nullptr;
+  float4 *dsph = nullptr;
+  BLAS blas;
+  bool built = false;
+};
+
+struct EntryH {
+  int geom;
+  uint32_t instID, geomID;
+  bool identity;
+  float xfm[12];
+  int material;
+};
+
+struct SceneObj {
+  DeviceObj *dev;
+  std::vector<GeomObj> geoms;
+  std::vector<EntryH> entries;
+  Entry *dEntries = nullptr;
+  WideBVH tlas;
+  uint32_t *status = nullptr;
+  unsigned long long *counters = nullptr;  // traversal statistics (render stats mode)
+  bool committed = false;
+  float bounds[6] = {0, 0, 0, 0, 0, 0};
+  explicit SceneObj(DeviceObj *d);
+  ~SceneObj();
+  void commit();
+  Scene view() const;
+};
+
+struct FrameObj {
+  DeviceObj *dev;
+  int W, H;
+  uint32_t channels;
+  int frameID = 0;
+  float4 *color = nullptr, *variance = nullptr;
+  float *depth = nullptr;
+  float3 *normal = nullptr, *albedo = nullptr;
+  uint32_t *primID = nullptr, *geomID = nullptr, *instID = nullptr;
+  FrameObj(DeviceObj *d, int w, int h, uint32_t ch);
+  ~FrameObj();
+  FrameD view() const;
+  void *channel(uint32_t c) const;
+  size_t channelBytes(uint32_t c) const;
+};
+
+CameraD makeCamera(const b200_camera_desc &c);
+
+}  // namespace b200

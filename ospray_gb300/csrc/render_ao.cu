@@ -1,0 +1,175 @@
+// Ray-query entry kernel (rtcIntersect/rtcOccluded over a ray array) and the
+// AO renderer.
+//   AORenderer_renderSample    modules/cpu/render/ao/AORenderer.ispc:23-149
+//   AORenderer_computeShading  modules/cpu/render/ao/surfaces.ispc:44-74
+//   computeAO                  modules/cpu/render/util.ispc:12-54
+#include "kernels.h"
+#include "render_common.cuh"
+
+namespace b200 {
+
+
+namespace {
+
+__global__ void k_trace(Scene sc, const float4 *rays, long long n, int occlusion, float *outF, uint32_t *outI) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4 a = rays[2 * i], b = rays[2 * i + 1];
+  Ray r;
+  r.org = mk(a.x, a.y, a.z);
+  r.tnear = a.w;
+  r.dir = mk(b.x, b.y, b.z);
+  r.tfar = b.w;
+  HitRec h;
+  if (occlusion) {
+    outF[6 * i] = traceScene<true>(sc, r, h) ? 1.f : 0.f;
+    return;
+  }
+  const bool hit = traceScene<false>(sc, r, h);
+  float *F = outF + 6 * i;
+  uint32_t *I = outI + 3 * i;
+  if (!hit) {
+    F[0] = INFINITY;
+    F[1] = F[2] = F[3] = F[4] = F[5] = 0.f;
+    I[0] = I[1] = I[2] = INVALID_ID;
+    return;
+  }
+  F[0] = h.t;
+  F[1] = h.u;
+  F[2] = h.v;
+  F[3] = h.Ng.x;
+  F[4] = h.Ng.y;
+  F[5] = h.Ng.z;
+  I[0] = h.primID;
+  I[1] = h.geomID;
+  I[2] = h.instID;
+}
+
+template <bool STATS>
+B200_D float computeAO(const SamplerTables *T, const Scene &sc, const DG &dg, int sampleCnt, float aoRadius, int px, int py,
+                       uint32_t sid, TraceStats *ts) {
+  const uint32_t accumID = sid * uint32_t(sampleCnt);
+  uint32_t t0 = uint32_t(px), t1 = uint32_t(py);
+  tea8(t0, t1);
+  const float rx0 = to_float_unorm(t0), ry0 = to_float_unorm(t1);
+  V3 dx, dy;
+  frame(dg.Ns, dx, dy);
+  int hits = 0;
+  for (int i = 0; i < sampleCnt; i++) {
+    const float rx = cpRotate(PermHalton_sample5(T, accumID + i), rx0);
+    const float ry = cpRotate(PermHalton_sample7(T, accumID + i), ry0);
+    const float phi = fmul(6.283185307179586f, rx);
+    const float cosT = fsqrt(ry), sinT = fsqrt(fsub(1.f, ry));
+    float sp, cp;
+    sincosf(phi, &sp, &cp);
+    const V3 dir = toWorld(dx, dy, dg.Ns, mk(fmul(cp, sinT), fmul(sp, sinT), cosT));
+    if (dot(dir, dg.Ns) < 0.01f) {
+      hits++;
+      continue;
+    }
+    Ray r;
+    r.org = dg.P;
+    r.tnear = dg.epsilon;
+    r.dir = dir;
+    r.tfar = aoRadius;
+    HitRec h;
+    if (traceScene<true, STATS>(sc, r, h, ts)) hits++;
+  }
+  return 1.f - float(hits) / float(sampleCnt);
+}
+
+template <bool STATS>
+__global__ void __launch_bounds__(128) k_render_ao(const SamplerTables *T, Scene sc, CameraD cam, PixelFilterD pf, AOParamsD p, FrameD fb) {
+  const int x = blockIdx.x * 16 + (threadIdx.x & 15);
+  const int y = blockIdx.y * 8 + (threadIdx.x >> 4);
+  TraceStats ts = {0, 0, 0, 0};
+  if (x >= fb.W || y >= fb.H) {
+    if (STATS) flushStats(sc, ts);
+    return;
+  }
+  const float rcpW = fdiv(1.f, float(fb.W)), rcpH = fdiv(1.f, float(fb.H));
+  const uint32_t start = uint32_t(fb.frameID * p.spp + 1);
+  float ar = 0.f, ag = 0.f, ab = 0.f, aa = 0.f;
+  PixelOut acc = {0, 0, 0, 0, INFINITY, INVALID_ID, INVALID_ID, INVALID_ID};
+  for (int s = 0; s < p.spp; s++) {
+    const uint32_t sid = start + s;
+    Ray ray = primaryRay(T, cam, pf, x, y, rcpW, rcpH, sid);
+    const float tfar0 = ray.tfar;
+    float o[4] = {0.f, 0.f, 0.f, 0.f};
+    bool first = true;
+    float z = INFINITY;
+    uint32_t prim = INVALID_ID, geom = INVALID_ID, inst = INVALID_ID;
+    for (int layer = 0; layer < 64 && o[3] < 0.99f; layer++) {
+      HitRec h;
+      const bool hit = traceScene<false, STATS>(sc, ray, h, &ts);
+      float bl[4];
+      if (hit) {
+        const DG dg = postIntersect(sc, ray, h);
+        float intensity = fabsf(dot(dg.Ns, ray.dir));
+        if (p.aoSamples > 0 && p.aoIntensity > 0.01f) {
+          const float ao = computeAO<STATS>(T, sc, dg, p.aoSamples, p.aoRadius, x, y, sid, &ts);
+          intensity = fmul(intensity, fadd(fsub(1.f, p.aoIntensity), fmul(ao, p.aoIntensity)));
+        }
+        bl[0] = bl[1] = bl[2] = intensity;
+        bl[3] = 1.f;
+        if (first) {
+          z = h.t;
+          prim = h.primID;
+          geom = h.geomID;
+          inst = h.instID;
+        }
+        ray.tnear = fadd(h.t, dg.epsilon);
+        ray.tfar = tfar0;
+      } else {
+        bl[0] = p.bg[0];
+        bl[1] = p.bg[1];
+        bl[2] = p.bg[2];
+        bl[3] = p.bg[3];
+        if (first) z = ray.tfar;
+      }
+      const float f = fsub(1.f, o[3]);
+      for (int k = 0; k < 4; k++) o[k] = fadd(o[k], fmul(f, bl[k]));
+      first = false;
+      if (!hit) break;
+    }
+    ar = fadd(ar, o[0]);
+    ag = fadd(ag, o[1]);
+    ab = fadd(ab, o[2]);
+    aa = fadd(aa, o[3]);
+    if (fabsf(z) < fabsf(acc.z)) {
+      acc.z = z;
+      acc.primID = prim;
+      acc.geomID = geom;
+      acc.instID = inst;
+    }
+  }
+  const float rspp = fdiv(1.f, float(p.spp));
+  acc.r = fmul(ar, rspp);
+  acc.g = fmul(ag, rspp);
+  acc.b = fmul(ab, rspp);
+  acc.a = fmul(aa, rspp);
+  fbAccumulate(fb, x, y, acc);
+  if (STATS) flushStats(sc, ts);
+}
+
+}  // namespace
+
+cudaError_t launchTrace(const Scene &sc, const float4 *rays, long long n, int occlusion, float *outF, uint32_t *outI,
+                        cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  const int bs = 128;
+  k_trace<<<unsigned((n + bs - 1) / bs), bs, 0, st>>>(sc, rays, n, occlusion, outF, outI);
+  return cudaGetLastError();
+}
+
+cudaError_t launchRenderAO(const SamplerTables *T, const Scene &sc, const CameraD &cam, const PixelFilterD &pf, const AOParamsD &p,
+                           const FrameD &fb, bool stats, cudaStream_t st) {
+  dim3 grid((fb.W + 15) / 16, (fb.H + 7) / 8);
+  if (stats)
+    k_render_ao<true><<<grid, 128, 0, st>>>(T, sc, cam, pf, p, fb);
+  else
+    k_render_ao<false><<<grid, 128, 0, st>>>(T, sc, cam, pf, p, fb);
+  return cudaGetLastError();
+}
+
+}  // namespace b200

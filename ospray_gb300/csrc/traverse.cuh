@@ -1,0 +1,339 @@
+// Two-level ray traversal of the quantised 8-wide BVH with watertight
+// triangle and geometric sphere tests.  Replaces rtcIntersectV / rtcOccludedV
+// as called from traceGeometryRay / isOccluded
+// (modules/cpu/common/World.ih:29-52,311-380).
+//
+// Triangle test: Woop, Benthin, Wald, "Watertight Ray/Triangle
+// Intersection", JCGT 2013.  Sphere test: Haines et al., "Precision
+// Improvements for Ray/Sphere Intersection", Ray Tracing Gems 2019, ch. 7.
+// Both run on non-contracted IEEE operations so a scalar CPU evaluation of
+// the same formulas gives the same t bit for bit.  Equal-t ties resolve to
+// the smallest (instID, geomID, primID), independent of traversal order.
+#pragma once
+#include "common.cuh"
+
+namespace b200 {
+
+constexpr int TRAVERSAL_STACK = 96;
+
+struct HitRec {
+  float t, u, v;
+  V3 Ng;
+  uint32_t primID, geomID, instID, entry;
+};
+
+// Per-thread traversal counters, filled only by the STATS instantiations.
+struct TraceStats {
+  uint32_t rays, nodes, tris, spheres;
+};
+
+struct Scene {
+  const Node8 *tlas;         // root at 0 (empty when ntlas == 0)
+  const uint32_t *tlasLeaf;   // entry index per TLAS leaf slot
+  const Entry *entries;
+  int nentries;
+  int ntlas;
+  uint32_t *status;           // bit 0: traversal stack overflow seen
+  unsigned long long *counters;  // [rays, node visits, triangle tests, sphere tests]
+};
+
+// Adds a warp's per-thread counters to the scene counters (one atomic per
+// field per warp).
+B200_D void flushStats(const Scene &sc, const TraceStats &t) {
+  uint32_t v[4] = {t.rays, t.nodes, t.tris, t.spheres};
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    uint32_t x = v[k];
+    for (int o = 16; o; o >>= 1) x += __shfl_xor_sync(__activemask(), x, o);
+    v[k] = x;
+  }
+  if ((threadIdx.x & 31) == __ffs(__activemask()) - 1)
+    for (int k = 0; k < 4; k++)
+      if (v[k]) atomicAdd(sc.counters + k, (unsigned long long)v[k]);
+}
+
+struct TriPre {
+  int kx, ky, kz;
+  float Sx, Sy, Sz;
+};
+
+B200_D TriPre triPre(V3 d) {
+  TriPre p;
+  const V3 a = vabs(d);
+  p.kz = 0;
+  if (a.y > comp(a, p.kz)) p.kz = 1;
+  if (a.z > comp(a, p.kz)) p.kz = 2;
+  p.kx = p.kz == 2 ? 0 : p.kz + 1;
+  p.ky = p.kx == 2 ? 0 : p.kx + 1;
+  if (comp(d, p.kz) < 0.f) {
+    const int t = p.kx;
+    p.kx = p.ky;
+    p.ky = t;
+  }
+  p.Sx = fdiv(comp(d, p.kx), comp(d, p.kz));
+  p.Sy = fdiv(comp(d, p.ky), comp(d, p.kz));
+  p.Sz = fdiv(1.f, comp(d, p.kz));
+  return p;
+}
+
+B200_D bool triTest(const TriPre &p, V3 org, float tnear, float tfar, V3 v0, V3 v1, V3 v2, float &t, float &u,
+                    float &v) {
+  const V3 A = sub(v0, org), B = sub(v1, org), C = sub(v2, org);
+  const float Akz = comp(A, p.kz), Bkz = comp(B, p.kz), Ckz = comp(C, p.kz);
+  const float Ax = fsub(comp(A, p.kx), fmul(p.Sx, Akz));
+  const float Ay = fsub(comp(A, p.ky), fmul(p.Sy, Akz));
+  const float Bx = fsub(comp(B, p.kx), fmul(p.Sx, Bkz));
+  const float By = fsub(comp(B, p.ky), fmul(p.Sy, Bkz));
+  const float Cx = fsub(comp(C, p.kx), fmul(p.Sx, Ckz));
+  const float Cy = fsub(comp(C, p.ky), fmul(p.Sy, Ckz));
+  float U = fsub(fmul(Cx, By), fmul(Cy, Bx));
+  float V = fsub(fmul(Ax, Cy), fmul(Ay, Cx));
+  float W = fsub(fmul(Bx, Ay), fmul(By, Ax));
+  if (U == 0.f || V == 0.f || W == 0.f) {
+    U = float(__dsub_rn(__dmul_rn(double(Cx), double(By)), __dmul_rn(double(Cy), double(Bx))));
+    V = float(__dsub_rn(__dmul_rn(double(Ax), double(Cy)), __dmul_rn(double(Ay), double(Cx))));
+    W = float(__dsub_rn(__dmul_rn(double(Bx), double(Ay)), __dmul_rn(double(By), double(Ax))));
+  }
+  if ((U < 0.f || V < 0.f || W < 0.f) && (U > 0.f || V > 0.f || W > 0.f)) return false;
+  const float det = fadd(fadd(U, V), W);
+  if (det == 0.f) return false;
+  const float Az = fmul(p.Sz, Akz), Bz = fmul(p.Sz, Bkz), Cz = fmul(p.Sz, Ckz);
+  const float T = fadd(fadd(fmul(U, Az), fmul(V, Bz)), fmul(W, Cz));
+  t = fdiv(T, det);
+  if (!(t >= tnear && t <= tfar)) return false;
+  u = fdiv(V, det);
+  v = fdiv(W, det);
+  return true;
+}
+
+B200_D bool sphTest(V3 org, V3 d, float tnear, float tfar, float4 s, float &t, V3 &Ng) {
+  const float rd2 = fdiv(1.f, dot(d, d));
+  const V3 c0 = sub(mk(s.x, s.y, s.z), org);
+  const float projC0 = fmul(dot(c0, d), rd2);
+  const V3 perp = sub(c0, mul(projC0, d));
+  const float l2 = dot(perp, perp);
+  const float r2 = fmul(s.w, s.w);
+  if (!(l2 <= r2)) return false;
+  const float td = fsqrt(fmul(fsub(r2, l2), rd2));
+  const float tf = fsub(projC0, td), tb = fadd(projC0, td);
+  if (tf >= tnear && tf <= tfar)
+    t = tf;
+  else if (tb >= tnear && tb <= tfar)
+    t = tb;
+  else
+    return false;
+  Ng = sub(mul(t, d), c0);
+  return true;
+}
+
+B200_D bool better(float t, uint32_t inst, uint32_t geom, uint32_t prim, const HitRec &h) {
+  if (t != h.t) return t < h.t;
+  if (inst != h.instID) return inst < h.instID;
+  if (geom != h.geomID) return geom < h.geomID;
+  return prim < h.primID;
+}
+
+// Loads a node and intersects its 8 child boxes.  Returns a bit mask of hit
+// children; dist[i] holds the entry distance of hit child i.
+struct NodeView {
+  uint4 q[5];
+  B200_D float px() const { return __uint_as_float(q[0].x); }
+  B200_D float py() const { return __uint_as_float(q[0].y); }
+  B200_D float pz() const { return __uint_as_float(q[0].z); }
+  B200_D uint32_t exw() const { return q[0].w; }  // ex | ey<<8 | ez<<16 | imask<<24
+  B200_D uint32_t childBase() const { return q[1].x; }
+  B200_D uint32_t primBase() const { return q[1].y; }
+  B200_D uint32_t meta(int i) const { return ((i < 4 ? q[1].z : q[1].w) >> (8 * (i & 3))) & 0xffu; }
+  // quantised byte b of the 48-byte box block (qlo[3][8] then qhi[3][8])
+  B200_D uint32_t qbyte(int b) const {
+    const int w = b >> 2;  // word in q[2..4]
+    const uint4 v = q[2 + (w >> 2)];
+    const uint32_t word = (w & 3) == 0 ? v.x : ((w & 3) == 1 ? v.y : ((w & 3) == 2 ? v.z : v.w));
+    return (word >> (8 * (b & 3))) & 0xffu;
+  }
+};
+
+B200_D NodeView loadNode(const Node8 *nodes, uint32_t i) {
+  const uint4 *p = reinterpret_cast<const uint4 *>(nodes + i);
+  NodeView n;
+#pragma unroll
+  for (int k = 0; k < 5; k++) n.q[k] = __ldg(p + k);
+  return n;
+}
+
+B200_D uint32_t intersectChildren(const NodeView &n, V3 org, V3 rdir, float tnear, float tfar, float dist[8]) {
+  const uint32_t e = n.exw();
+  const float sx = __uint_as_float((e & 0xffu) << 23);
+  const float sy = __uint_as_float(((e >> 8) & 0xffu) << 23);
+  const float sz = __uint_as_float(((e >> 16) & 0xffu) << 23);
+  // per-axis near/far byte offsets from the ray octant
+  const int nx = rdir.x >= 0.f ? 0 : 24, ny = rdir.y >= 0.f ? 0 : 24, nz = rdir.z >= 0.f ? 0 : 24;
+  const float ox = n.px() - org.x, oy = n.py() - org.y, oz = n.pz() - org.z;
+  uint32_t mask = 0;
+#pragma unroll
+  for (int i = 0; i < 8; i++) {
+    if (n.meta(i) == 0) continue;
+    const float qnx = float(n.qbyte(nx + 0 + i)), qfx = float(n.qbyte(24 - nx + 0 + i));
+    const float qny = float(n.qbyte(ny + 8 + i)), qfy = float(n.qbyte(24 - ny + 8 + i));
+    const float qnz = float(n.qbyte(nz + 16 + i)), qfz = float(n.qbyte(24 - nz + 16 + i));
+    const float t0x = fmaf(qnx, sx, ox) * rdir.x, t1x = fmaf(qfx, sx, ox) * rdir.x;
+    const float t0y = fmaf(qny, sy, oy) * rdir.y, t1y = fmaf(qfy, sy, oy) * rdir.y;
+    const float t0z = fmaf(qnz, sz, oz) * rdir.z, t1z = fmaf(qfz, sz, oz) * rdir.z;
+    const float t0 = fmaxf(fmaxf(t0x, t0y), fmaxf(t0z, tnear));
+    const float t1 = fminf(fminf(t1x, t1y), t1z) * 1.0000004f;
+    if (t0 <= fminf(t1, tfar)) {
+      mask |= 1u << i;
+      dist[i] = t0;
+    }
+  }
+  return mask;
+}
+
+struct StackEntry {
+  uint32_t node;
+  float dist;
+};
+
+template <bool ANY, bool STATS = false>
+B200_D bool traverseBLAS(const Entry &e, V3 org, V3 dir, float tnear, HitRec &hit, StackEntry *stack, int cap,
+                         uint32_t entryIdx, uint32_t *status, TraceStats *ts = nullptr) {
+  const V3 rdir = mk(1.f / dir.x, 1.f / dir.y, 1.f / dir.z);
+  const TriPre pre = triPre(dir);
+  int sp = 0;
+  uint32_t node = 0;
+  bool found = false;
+  bool haveNode = true;
+  for (int guard = 0; guard < (1 << 24); guard++) {
+    if (!haveNode) {
+      if (sp == 0) break;
+      const StackEntry s = stack[--sp];
+      if (s.dist > hit.t) continue;
+      node = s.node;
+    }
+    haveNode = false;
+    const NodeView n = loadNode(e.nodes, node);
+    if (STATS) ts->nodes++;
+    float dist[8];
+    const uint32_t mask = intersectChildren(n, org, rdir, tnear, hit.t, dist);
+    if (!mask) continue;
+    // leaves first: they tighten hit.t before children are ordered
+    uint32_t nearest = 0xffffffffu;
+    float nearestD = INFINITY;
+    for (uint32_t m = mask; m; m &= m - 1) {
+      const int i = __ffs(m) - 1;
+      const uint32_t meta = n.meta(i);
+      if (meta & 0x80u) continue;
+      const uint32_t cnt = meta >> 5, first = n.primBase() + (meta & 31u);
+      for (uint32_t k = 0; k < cnt; k++) {
+        const uint32_t slot = first + k;
+        float t, u = 0.f, v = 0.f;
+        V3 Ng;
+        uint32_t prim;
+        bool h;
+        if (STATS) (e.type == GEOM_TRIANGLES ? ts->tris : ts->spheres)++;
+        if (e.type == GEOM_TRIANGLES) {
+          const float4 a = __ldg(e.prims + 3 * slot), b = __ldg(e.prims + 3 * slot + 1),
+                       c = __ldg(e.prims + 3 * slot + 2);
+          const V3 v0 = mk(a.x, a.y, a.z), v1 = mk(b.x, b.y, b.z), v2 = mk(c.x, c.y, c.z);
+          h = triTest(pre, org, tnear, hit.t, v0, v1, v2, t, u, v);
+          if (h) Ng = cross(sub(v1, v0), sub(v2, v0));
+          prim = __float_as_uint(a.w);
+        } else {
+          h = sphTest(org, dir, tnear, hit.t, __ldg(e.prims + slot), t, Ng);
+          prim = __ldg(e.primIDs + slot);
+        }
+        if (!h) continue;
+        if (ANY) return true;
+        if (better(t, e.instID, e.geomID, prim, hit)) {
+          hit.t = t;
+          hit.u = u;
+          hit.v = v;
+          hit.Ng = Ng;
+          hit.primID = prim;
+          hit.geomID = e.geomID;
+          hit.instID = e.instID;
+          hit.entry = entryIdx;
+          found = true;
+        }
+      }
+    }
+    for (uint32_t m = mask; m; m &= m - 1) {
+      const int i = __ffs(m) - 1;
+      const uint32_t meta = n.meta(i);
+      if (!(meta & 0x80u)) continue;
+      if (dist[i] > hit.t) continue;
+      const uint32_t child = n.childBase() + (meta & 7u);
+      if (dist[i] < nearestD) {
+        if (nearest != 0xffffffffu) {
+          if (sp < cap)
+            stack[sp++] = {nearest, nearestD};
+          else
+            atomicOr(status, 1u);
+        }
+        nearest = child;
+        nearestD = dist[i];
+      } else {
+        if (sp < cap)
+          stack[sp++] = {child, dist[i]};
+        else
+          atomicOr(status, 1u);
+      }
+    }
+    if (nearest != 0xffffffffu) {
+      node = nearest;
+      haveNode = true;
+    }
+  }
+  return found;
+}
+
+// Closest hit (ANY = false) or any hit (ANY = true) over the whole scene.
+template <bool ANY, bool STATS = false>
+B200_D bool traceScene(const Scene &sc, const Ray &ray, HitRec &hit, TraceStats *ts = nullptr) {
+  hit.t = ray.tfar;
+  hit.u = hit.v = 0.f;
+  hit.primID = hit.geomID = hit.instID = hit.entry = INVALID_ID;
+  if (STATS) ts->rays++;
+  if (sc.ntlas == 0) return false;
+  StackEntry stack[TRAVERSAL_STACK];
+  const V3 rdir = mk(1.f / ray.dir.x, 1.f / ray.dir.y, 1.f / ray.dir.z);
+  int sp = 0;
+  stack[sp++] = {0u, -INFINITY};
+  bool found = false;
+  for (int guard = 0; guard < (1 << 20) && sp > 0; guard++) {
+    const StackEntry s = stack[--sp];
+    if (s.dist > hit.t) continue;
+    const NodeView n = loadNode(sc.tlas, s.node);
+    if (STATS) ts->nodes++;
+    float dist[8];
+    const uint32_t mask = intersectChildren(n, ray.org, rdir, ray.tnear, hit.t, dist);
+    for (uint32_t m = mask; m; m &= m - 1) {
+      const int i = __ffs(m) - 1;
+      const uint32_t meta = n.meta(i);
+      if (meta & 0x80u) {
+        if (sp < TRAVERSAL_STACK)
+          stack[sp++] = {n.childBase() + (meta & 7u), dist[i]};
+        else
+          atomicOr(sc.status, 1u);
+        continue;
+      }
+      const uint32_t cnt = meta >> 5, first = n.primBase() + (meta & 31u);
+      for (uint32_t k = 0; k < cnt; k++) {
+        const uint32_t ei = __ldg(sc.tlasLeaf + first + k);
+        const Entry &e = sc.entries[ei];
+        V3 o = ray.org, d = ray.dir;
+        if (!e.identity) {
+          o = xfmPoint(e.rcp, ray.org);
+          d = xfmVector(e.rcp, ray.dir);
+        }
+        if (traverseBLAS<ANY, STATS>(e, o, d, ray.tnear, hit, stack + sp, TRAVERSAL_STACK - sp, ei, sc.status, ts)) {
+          if (ANY) return true;
+          found = true;
+        }
+      }
+    }
+  }
+  return found;
+}
+
+}  // namespace b200

@@ -1,0 +1,90 @@
+"""Seeded synthetic workloads (the render configurations the module is
+measured on), built by the C generators in csrc/scenegen.cpp.
+
+Each function returns plain numpy arrays plus camera/renderer settings, so
+the CUDA renderer and the CPU oracle consume identical inputs.
+"""
+import ctypes
+
+import numpy as np
+
+from . import scenes_lib
+
+_U64, _I, _F, _P, _U32 = ctypes.c_uint64, ctypes.c_int, ctypes.c_float, ctypes.c_void_p, ctypes.c_uint32
+
+
+def _p(a):
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+def heightfield(seed, n):
+    """n x n vertices over [0,1]^2, 2 (n-1)^2 triangles (see scenegen.cpp)."""
+    v = np.empty((n * n, 3), np.float32)
+    i = np.empty((2 * (n - 1) * (n - 1), 3), np.uint32)
+    f = scenes_lib().b200sg_heightfield
+    f.argtypes = [_U64, _I, _P, _P]
+    f(seed, n, _p(v), _p(i))
+    return v, i
+
+
+def spheres(seed, count, r0=0.005, r1=0.02):
+    s = np.empty((count, 4), np.float32)
+    f = scenes_lib().b200sg_spheres
+    f.argtypes = [_U64, _I, _F, _F, _P]
+    f(seed, count, r0, r1, _p(s))
+    return s
+
+
+def displaced_sphere(levels=6, amp=0.05, freq=8.0, seed=7):
+    f = scenes_lib().b200sg_displaced_sphere
+    f.argtypes = [_I, _F, _F, _U32, _P, _P, _P]
+    nv = ctypes.c_int()
+    f(levels, amp, freq, seed, None, None, ctypes.byref(nv))
+    v = np.empty((nv.value, 3), np.float32)
+    i = np.empty((8 * 4 ** levels, 3), np.uint32)
+    f(levels, amp, freq, seed, _p(v), _p(i), ctypes.byref(nv))
+    return v, i
+
+
+def instances(seed, count, s0=0.5, s1=2.0, box=10.0, pmetal=0.2):
+    x = np.empty((count, 12), np.float32)
+    m = np.empty((count, 5), np.float32)
+    f = scenes_lib().b200sg_instances
+    f.argtypes = [_U64, _I, _F, _F, _F, _F, _P, _P]
+    f(seed, count, s0, s1, box, pmetal, _p(x), _p(m))
+    return x, m
+
+
+def fractal_volume(n, octaves=5, base_freq=4.0, seed=11):
+    out = np.empty((n, n, n), np.float32)
+    f = scenes_lib().b200sg_fractal_volume
+    f.argtypes = [_I, _I, _F, _U32, _P]
+    f(n, octaves, base_freq, seed, _p(out))
+    return out
+
+
+def color_ramp(seed, count=256):
+    out = np.empty((count, 3), np.float32)
+    f = scenes_lib().b200sg_color_ramp
+    f.argtypes = [_U64, _I, _P]
+    f(seed, count, _p(out))
+    return out
+
+
+def ao_heightfield_scene(seed=0, n=256, nspheres=1000):
+    """AO workload: 256x256-vertex height field (130,050 triangles) and 1,000
+    spheres from seed 0, one instance holding both models (geomID 0 mesh,
+    1 spheres), camera at (0.5, 2, -1.5) looking at (0.5, 0, 0.5), fovy 60."""
+    v, i = heightfield(seed, n)
+    s = spheres(seed + 1, nspheres)
+    cam = dict(position=(0.5, 2.0, -1.5), direction=(0.0, -2.0, 2.0), up=(0.0, 1.0, 0.0), fovy=60.0, aspect=1.0)
+    return dict(vertex=v, index=i, spheres=s, camera=cam)
+
+
+def build_ao_scene(scene, data):
+    """Adds the AO workload's geometry to a b200 Scene (or the oracle)."""
+    gm = scene.add_mesh(data["vertex"], data["index"])
+    gs = scene.add_spheres(data["spheres"])
+    scene.add_instance(gm, 0, 0)
+    scene.add_instance(gs, 0, 1)
+    scene.commit()

@@ -1,0 +1,121 @@
+"""ctypes wrapper of the CPU oracle (oracle/_build/liboracle.so).
+
+Test infrastructure only: the tests and bench.py's CPU-baseline leg use it
+as the checker/baseline; nothing in the product imports it.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+ORACLE_DIR = os.path.join(ROOT, "oracle")
+LIB = os.path.join(ORACLE_DIR, "_build", "liboracle.so")
+_lib = None
+
+P, I, U32, F = ctypes.c_void_p, ctypes.c_int, ctypes.c_uint32, ctypes.c_float
+
+
+class OrCamera(ctypes.Structure):
+    _fields_ = [("pos", F * 3), ("dir", F * 3), ("up", F * 3), ("fovy", F), ("aspect", F), ("nearClip", F)]
+
+
+class OrFrame(ctypes.Structure):
+    _fields_ = [("color", P), ("depth", P), ("primID", P), ("geomID", P), ("instID", P)]
+
+
+def build():
+    subprocess.run(["make", "-s", "-C", ORACLE_DIR], check=True)
+    return LIB
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(LIB)
+        L.or_scene_new.restype = P
+        L.or_scene_free.argtypes = [P]
+        L.or_scene_add_mesh.argtypes = [P, P, I, P, I]
+        L.or_scene_add_spheres.argtypes = [P, P, I]
+        L.or_scene_add_instance.argtypes = [P, I, U32, U32, P]
+        L.or_scene_commit.argtypes = [P]
+        L.or_trace.argtypes = [P, P, I, I, P, P, I]
+        L.or_camera_rays.argtypes = [ctypes.POINTER(OrCamera), I, I, I, I, I, P]
+        L.or_render_ao.argtypes = [P, ctypes.POINTER(OrCamera), I, I, I, I, I, F, F, P, I,
+                                   ctypes.POINTER(OrFrame), I]
+        L.or_tables.argtypes = [P, P, P, P]
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return ctypes.c_void_p(a.ctypes.data) if a is not None else None
+
+
+def camera(position, direction, up=(0, 1, 0), fovy=60.0, aspect=1.0, near_clip=1e-6):
+    c = OrCamera()
+    c.pos[:], c.dir[:], c.up[:] = list(position), list(direction), list(up)
+    c.fovy, c.aspect, c.nearClip = fovy, aspect, near_clip
+    return c
+
+
+class Scene:
+    def __init__(self):
+        self.h = lib().or_scene_new()
+        self._keep = []
+
+    def add_mesh(self, vertex, index):
+        v = np.ascontiguousarray(vertex, np.float32)
+        i = np.ascontiguousarray(index, np.uint32)
+        return lib().or_scene_add_mesh(self.h, _p(v), len(v), _p(i), len(i))
+
+    def add_spheres(self, xyzr):
+        s = np.ascontiguousarray(xyzr, np.float32)
+        return lib().or_scene_add_spheres(self.h, _p(s), len(s))
+
+    def add_instance(self, geom, inst_id, geom_id, xfm=None, material=-1):
+        x = None if xfm is None else np.ascontiguousarray(xfm, np.float32).reshape(12)
+        lib().or_scene_add_instance(self.h, geom, inst_id, geom_id, _p(x))
+
+    def commit(self):
+        lib().or_scene_commit(self.h)
+
+    def trace(self, rays, occlusion=False, nthreads=0):
+        rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)
+        f = np.zeros((len(rays), 6), np.float32)
+        ids = np.zeros((len(rays), 3), np.uint32)
+        lib().or_trace(self.h, _p(rays), len(rays), int(occlusion), _p(f), _p(ids), nthreads)
+        return f, ids
+
+    def __del__(self):
+        try:
+            lib().or_scene_free(self.h)
+        except Exception:
+            pass
+
+
+def camera_rays(cam, pixel_filter, w, h, spp=1, frame_id=0):
+    out = np.empty((h, w, spp, 8), np.float32)
+    lib().or_camera_rays(ctypes.byref(cam), pixel_filter, w, h, spp, frame_id, _p(out))
+    return out
+
+
+def render_ao(scene, cam, pixel_filter, w, h, spp=1, ao_samples=1, ao_radius=1e20, ao_intensity=1.0,
+              bg=(0, 0, 0, 0), frames=1, nthreads=0):
+    color = np.zeros((h, w, 4), np.float32)
+    depth = np.zeros((h, w), np.float32)
+    ids = [np.zeros((h, w), np.uint32) for _ in range(3)]
+    fr = OrFrame(color.ctypes.data, depth.ctypes.data, ids[0].ctypes.data, ids[1].ctypes.data, ids[2].ctypes.data)
+    bgv = np.asarray(bg, np.float32)
+    lib().or_render_ao(scene.h, ctypes.byref(cam), pixel_filter, w, h, spp, ao_samples, ao_radius, ao_intensity,
+                       _p(bgv), frames, ctypes.byref(fr), nthreads)
+    return dict(color=color, depth=depth, primID=ids[0], geomID=ids[1], instID=ids[2])
+
+
+def tables():
+    p3, p5, p7 = np.zeros(243, np.uint32), np.zeros(125, np.uint32), np.zeros(343, np.uint32)
+    s = np.zeros(128, np.uint32)
+    lib().or_tables(_p(p3), _p(p5), _p(p7), _p(s))
+    return {"halton_perm3": p3, "halton_perm5": p5, "halton_perm7": p7, "Sobol_revMatrices": s}

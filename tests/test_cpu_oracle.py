@@ -1,0 +1,152 @@
+"""CPU-only checks: the oracle against the reference's own tables, the oracle's
+BVH and intersection against brute force, scene generation, and the C ABI
+library's exported symbols (loaded, never called, so no GPU is needed)."""
+import ctypes
+import hashlib
+import json
+import os
+import re
+
+import numpy as np
+import pytest
+
+import oracle
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+INF = np.float32(np.inf)
+
+
+def test_sampler_tables_match_reference_golden():
+    """Halton permutations and Sobol matrices regenerated from Faure /
+    Joe-Kuo constructions equal the reference's math/halton.inl and
+    math/sobol.inl tables (digests in tests/golden/sampler_tables.json)."""
+    golden = json.load(open(os.path.join(ROOT, "tests", "golden", "sampler_tables.json")))
+    t = oracle.tables()
+    for name, g in golden.items():
+        a = t[name]
+        assert a.size == g["count"]
+        assert [int(x) for x in a[:16]] == g["head"], name
+        assert hashlib.sha256(a.astype("<u4").tobytes()).hexdigest() == g["sha256"], name
+
+
+def _rand_tris(rng, n):
+    c = rng.uniform(0, 1, (n, 1, 3))
+    v = (c + rng.uniform(-0.08, 0.08, (n, 3, 3))).astype(np.float32)
+    return v.reshape(-1, 3), np.arange(3 * n, dtype=np.uint32).reshape(-1, 3)
+
+
+def _brute(rays, tris, spheres):
+    """float64 closest hit: (t, kind, index); kind 0 triangle, 1 sphere."""
+    o, d = rays[:, None, 0:3].astype(np.float64), rays[:, None, 4:7].astype(np.float64)
+    tn, tf = rays[:, 3:4].astype(np.float64), rays[:, 7:8].astype(np.float64)
+    v0, v1, v2 = (tris[None, :, k].astype(np.float64) for k in range(3))
+    e1, e2 = v1 - v0, v2 - v0
+    p = np.cross(d, e2)
+    det = np.sum(e1 * p, -1)
+    s = o - v0
+    with np.errstate(divide="ignore", invalid="ignore"):
+        u = np.sum(s * p, -1) / det
+        q = np.cross(s, e1)
+        v = np.sum(d * q, -1) / det
+        t = np.sum(e2 * q, -1) / det
+    ok = (u >= 0) & (v >= 0) & (u + v <= 1) & (t >= tn) & (t <= tf) & np.isfinite(t)
+    tt = np.where(ok, t, np.inf)
+    c, r = spheres[None, :, :3].astype(np.float64), spheres[None, :, 3].astype(np.float64)
+    oc = c - o
+    a = np.sum(d * d, -1)
+    b = np.sum(oc * d, -1) / a
+    perp = oc - b[..., None] * d
+    l2 = np.sum(perp * perp, -1)
+    with np.errstate(invalid="ignore"):
+        td = np.sqrt((r * r - l2) / a)
+    t0, t1 = b - td, b + td
+    ts = np.where((t0 >= tn) & (t0 <= tf), t0, np.where((t1 >= tn) & (t1 <= tf), t1, np.inf))
+    ts = np.where(l2 <= r * r, ts, np.inf)
+    allt = np.concatenate([tt, ts], 1)
+    idx = np.argmin(allt, 1)
+    best = allt[np.arange(len(rays)), idx]
+    kind = (idx >= tris.shape[1]).astype(int)
+    return best, kind, np.where(kind == 0, idx, idx - tris.shape[1])
+
+
+def test_oracle_bvh_matches_brute_force():
+    rng = np.random.default_rng(1)
+    v, i = _rand_tris(rng, 300)
+    sph = np.concatenate([rng.uniform(0, 1, (60, 3)), rng.uniform(0.01, 0.05, (60, 1))], 1).astype(np.float32)
+    sc = oracle.Scene()
+    gm, gs = sc.add_mesh(v, i), sc.add_spheres(sph)
+    sc.add_instance(gm, 0, 0)
+    sc.add_instance(gs, 0, 1)
+    sc.commit()
+    n = 4000
+    org = rng.uniform(-0.5, 1.5, (n, 3))
+    tgt = rng.uniform(0, 1, (n, 3))
+    d = tgt - org
+    rays = np.concatenate([org, np.zeros((n, 1)), d, np.full((n, 1), np.inf)], 1).astype(np.float32)
+    f, ids = sc.trace(rays)
+    bt, kind, idx = _brute(rays, v.reshape(-1, 3, 3), sph)
+    hit = np.isfinite(bt)
+    assert np.array_equal(hit, np.isfinite(f[:, 0]) | False) or np.mean(hit != np.isfinite(f[:, 0])) < 1e-3
+    both = hit & np.isfinite(f[:, 0])
+    rel = np.abs(f[both, 0] - bt[both]) / np.maximum(bt[both], 1e-6)
+    assert rel.max() < 1e-4
+    agree = (ids[both, 1] == kind[both]) & (ids[both, 0] == idx[both])
+    # disagreements only at near-ties
+    assert np.all(agree | (rel < 1e-5)), np.flatnonzero(~agree)[:10]
+    # occlusion agrees with closest-hit existence
+    occ, _ = sc.trace(rays, occlusion=True)
+    assert np.array_equal(occ[:, 0] > 0, np.isfinite(f[:, 0]))
+
+
+def test_oracle_watertight_on_shared_edges_and_vertices():
+    """Rays aimed exactly at the vertices and edge midpoints of a flat grid
+    all hit: the watertight test leaves no cracks between triangles."""
+    n = 17
+    xs = np.linspace(0, 1, n, dtype=np.float32)
+    X, Z = np.meshgrid(xs, xs)
+    v = np.stack([X.ravel(), np.zeros(n * n, np.float32), Z.ravel()], 1)
+    idx = []
+    for j in range(n - 1):
+        for i in range(n - 1):
+            a = j * n + i
+            idx += [[a, a + n, a + 1], [a + 1, a + n, a + n + 1]]
+    sc = oracle.Scene()
+    g = sc.add_mesh(v, np.array(idx, np.uint32))
+    sc.add_instance(g, 0, 0)
+    sc.commit()
+    inner = v[(v[:, 0] > 0) & (v[:, 0] < 1) & (v[:, 2] > 0) & (v[:, 2] < 1)]
+    mids = 0.5 * (inner[:-1] + inner[1:])
+    pts = np.concatenate([inner, mids], 0)
+    rays = np.zeros((len(pts), 8), np.float32)
+    rays[:, 0], rays[:, 1], rays[:, 2] = pts[:, 0], 1.0, pts[:, 2]
+    rays[:, 5], rays[:, 7] = -1.0, np.inf
+    f, ids = sc.trace(rays)
+    assert np.all(np.isfinite(f[:, 0])) and np.allclose(f[:, 0], 1.0)
+
+
+def test_scene_generators_deterministic():
+    from ospray_gb300 import scenes
+    a = scenes.ao_heightfield_scene()
+    b = scenes.ao_heightfield_scene()
+    assert a["index"].shape == (130050, 3) and a["vertex"].shape == (65536, 3)
+    assert a["spheres"].shape == (1000, 4)
+    assert np.array_equal(a["vertex"], b["vertex"]) and np.array_equal(a["spheres"], b["spheres"])
+    s = a["spheres"]
+    assert s[:, 1].max() <= 0.3 and s[:, 3].min() >= 0.005 and s[:, 3].max() <= 0.02
+    v, i = scenes.displaced_sphere(6)
+    assert i.shape == (32768, 3) and v.shape[0] == 16386
+
+
+def _header_symbols(path):
+    text = open(path).read()
+    return sorted(set(re.findall(r"^\s*(?:[\w\s\*]+?)\b(b200_\w+)\s*\(", text, re.M)))
+
+
+def test_c_abi_library_exports_header_symbols():
+    """Every function include/b200.h declares is exported by libb200.so."""
+    import ospray_gb300 as og
+    syms = _header_symbols(os.path.join(ROOT, "include", "b200.h"))
+    assert "b200_trace" in syms and "b200_render_ao" in syms
+    lib = ctypes.CDLL(og.lib_path())
+    missing = [s for s in syms if not hasattr(lib, s)]
+    assert not missing, missing

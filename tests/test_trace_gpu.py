@@ -1,0 +1,146 @@
+"""Ray-query parity: b200_trace (CUDA, quantised 8-wide BVH) against the CPU
+oracle on identical rays.  Closest hits must agree on (primID, geomID,
+instID) and on t bit for bit; any-hit queries must agree exactly."""
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+def gpu_trace(scene, rays, occlusion=False):
+    r = torch.from_numpy(np.ascontiguousarray(rays, np.float32)).cuda()
+    n = r.shape[0]
+    f = torch.zeros((max(n, 1), 6), dtype=torch.float32, device="cuda")
+    ids = torch.zeros((max(n, 1), 3), dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    scene.trace(r.data_ptr(), n, f.data_ptr(), ids.data_ptr(), occlusion=occlusion)
+    scene.device.sync()
+    return f[:n].cpu().numpy(), ids[:n].cpu().numpy().view(np.uint32)
+
+
+def both(b200_device, build):
+    import ospray_gb300 as og
+    g = og.Scene(b200_device)
+    o = oracle.Scene()
+    build(g)
+    build(o)
+    return g, o
+
+
+def assert_closest_parity(gf, gi, of, oi, min_agree=1.0):
+    same_id = np.all(gi == oi, axis=1)
+    same_t = (gf[:, 0].view(np.uint32) == of[:, 0].view(np.uint32))
+    agree = np.mean(same_id & same_t)
+    assert agree >= min_agree, (agree, np.flatnonzero(~(same_id & same_t))[:10])
+
+
+@pytest.fixture(scope="module")
+def ao_scene(b200_device):
+    from ospray_gb300 import scenes
+    d = scenes.ao_heightfield_scene()
+    g, o = both(b200_device, lambda s: scenes.build_ao_scene(s, d))
+    return d, g, o
+
+
+def test_primary_rays_match_oracle(ao_scene):
+    import ospray_gb300 as og
+    d, g, o = ao_scene
+    cam = oracle.camera(d["camera"]["position"], d["camera"]["direction"], d["camera"]["up"])
+    rays = oracle.camera_rays(cam, og.PF_POINT, 512, 512).reshape(-1, 8)
+    gf, gi = gpu_trace(g, rays)
+    of, oi = o.trace(rays)
+    assert np.isfinite(of[:, 0]).sum() > 10000
+    assert_closest_parity(gf, gi, of, oi, min_agree=0.9999)
+    np.testing.assert_array_equal(gf[:, 3:6], of[:, 3:6])
+
+
+def test_random_rays_and_occlusion_match_oracle(ao_scene):
+    d, g, o = ao_scene
+    rng = np.random.default_rng(5)
+    n = 200000
+    org = rng.uniform([-0.2, -0.1, -0.2], [1.2, 0.4, 1.2], (n, 3))
+    dirs = rng.normal(size=(n, 3))
+    tfar = rng.choice([np.inf, 0.3], n)
+    rays = np.concatenate([org, np.full((n, 1), 1e-4), dirs, tfar[:, None]], 1).astype(np.float32)
+    gf, gi = gpu_trace(g, rays)
+    of, oi = o.trace(rays)
+    assert_closest_parity(gf, gi, of, oi, min_agree=0.9999)
+    go, _ = gpu_trace(g, rays, occlusion=True)
+    oo, _ = o.trace(rays, occlusion=True)
+    assert np.mean(go[:, 0] == oo[:, 0]) >= 0.9999
+
+
+def test_instanced_scene_matches_oracle(b200_device):
+    from ospray_gb300 import scenes
+    v, i = scenes.displaced_sphere(3)
+    x, _ = scenes.instances(3, 12, box=4.0)
+
+    def build(s):
+        gm = s.add_mesh(v, i)
+        gs = s.add_spheres(np.array([[1, 1, 1, 0.5], [3, 2, 1, 0.25]], np.float32))
+        for k in range(12):
+            s.add_instance(gm, k, 0, x[k])
+        s.add_instance(gs, 12, 0, x[0])
+        s.add_instance(gs, 13, 0)
+        s.commit()
+
+    g, o = both(b200_device, build)
+    rng = np.random.default_rng(9)
+    n = 100000
+    org = rng.uniform(-3, 7, (n, 3))
+    dirs = rng.uniform(0, 4, (n, 3)) - org
+    rays = np.concatenate([org, np.zeros((n, 1)), dirs, np.full((n, 1), np.inf)], 1).astype(np.float32)
+    gf, gi = gpu_trace(g, rays)
+    of, oi = o.trace(rays)
+    assert np.isfinite(of[:, 0]).mean() > 0.2
+    assert_closest_parity(gf, gi, of, oi, min_agree=0.9999)
+    go, _ = gpu_trace(g, rays, occlusion=True)
+    oo, _ = o.trace(rays, occlusion=True)
+    assert np.mean(go[:, 0] == oo[:, 0]) >= 0.9999
+
+
+def test_edge_cases(b200_device):
+    import ospray_gb300 as og
+    # empty world: everything misses
+    e = og.Scene(b200_device)
+    e.commit()
+    rays = np.array([[0, 0, 0, 0, 0, 0, 1, np.inf]], np.float32)
+    f, ids = gpu_trace(e, rays)
+    assert np.isinf(f[0, 0]) and ids[0, 0] == 0xffffffff
+    # zero rays
+    f, ids = gpu_trace(e, np.zeros((0, 8), np.float32))
+    assert f.shape == (0, 6)
+    # single triangle, axis-aligned rays through its vertices and edges
+    tri_v = np.array([[0, 0, 0], [1, 0, 0], [0, 0, 1]], np.float32)
+
+    def build(s):
+        gm = s.add_mesh(tri_v, np.array([[0, 1, 2]], np.uint32))
+        s.add_instance(gm, 0, 0)
+        s.commit()
+
+    g, o = both(b200_device, build)
+    pts = np.array([[0, 0], [1, 0], [0, 1], [0.5, 0], [0, 0.5], [0.5, 0.5], [0.25, 0.25], [0.7, 0.7]], np.float32)
+    rays = np.zeros((len(pts), 8), np.float32)
+    rays[:, 0], rays[:, 1], rays[:, 2], rays[:, 5], rays[:, 7] = pts[:, 0], 2.0, pts[:, 1], -1.0, np.inf
+    gf, gi = gpu_trace(g, rays)
+    of, oi = o.trace(rays)
+    assert_closest_parity(gf, gi, of, oi)
+    assert np.isinf(gf[-1, 0]) and np.all(np.isfinite(gf[:-1, 0]))
+
+
+def test_invalid_arguments_raise(b200_device):
+    import ospray_gb300 as og
+    s = og.Scene(b200_device)
+    with pytest.raises(og.B200Error) as e:
+        s.add_mesh(np.zeros((3, 3), np.float32), np.array([[0, 1, 5]], np.uint32))
+    assert e.value.code == 2
+    with pytest.raises(og.B200Error) as e:
+        s.add_instance(7, 0, 0)
+    assert e.value.code == 2
+    with pytest.raises(og.B200Error) as e:
+        s.trace(0, 0, 0, 0)  # not committed
+    assert e.value.code == 3
