@@ -174,7 +174,7 @@ __global__ void k_bottom_up(int n, const uint32_t *left, const uint32_t *right, 
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   uint32_t p = parentLeaf[i];
-  while (p != 0xffffffffu) {
+  for (int guard = 0; p != 0xffffffffu && guard < n; guard++) {
     __threadfence();
     if (atomicAdd(&flags[p], 1u) == 0) return;
     __threadfence();
@@ -430,7 +430,12 @@ cudaError_t buildWide(const float4 *lo, const float4 *hi, int n, cudaStream_t st
   uint32_t *hcnt = nullptr;
   cudaMallocHost(&hcnt, 16);
   cudaMemcpyAsync(counters, cinit, sizeof(cinit), cudaMemcpyHostToDevice, st);
-  while (ntasks > 0) {
+  // every level consumes at least one binary level, so 2n+64 levels bound it
+  for (int level = 0; ntasks > 0; level++) {
+    if (level > 2 * n + 64) {
+      err = cudaErrorUnknown;
+      break;
+    }
     cudaMemsetAsync(counters + 2, 0, 4, st);
     k_collapse<<<blocks(ntasks, 128), 128, 0, st>>>(qa, ntasks, qb, counters, left, right, first, sorted, lo, hi, blo,
                                                     bhi, out.nodes, out.leafPrim);
@@ -455,6 +460,7 @@ cudaError_t buildWide(const float4 *lo, const float4 *hi, int n, cudaStream_t st
     out.hi[k] = unflip(accHost[9 + k]);
   }
   cudaFreeAsync(base, st);
+  if (err != cudaSuccess) return err;
   return cudaGetLastError();
 }
 

@@ -203,7 +203,8 @@ B200_D bool traverseBLAS(const Entry &e, V3 org, V3 dir, float tnear, HitRec &hi
   uint32_t node = 0;
   bool found = false;
   bool haveNode = true;
-  for (int guard = 0; guard < (1 << 24); guard++) {
+  // bounded: no ray visits more nodes than this, a stuck traversal gives up
+  for (int guard = 0; guard < (1 << 18); guard++) {
     if (!haveNode) {
       if (sp == 0) break;
       const StackEntry s = stack[--sp];
@@ -300,7 +301,7 @@ B200_D bool traceScene(const Scene &sc, const Ray &ray, HitRec &hit, TraceStats 
   int sp = 0;
   stack[sp++] = {0u, -INFINITY};
   bool found = false;
-  for (int guard = 0; guard < (1 << 20) && sp > 0; guard++) {
+  for (int guard = 0; guard < (1 << 14) && sp > 0; guard++) {
     const StackEntry s = stack[--sp];
     if (s.dist > hit.t) continue;
     const NodeView n = loadNode(sc.tlas, s.node);
