@@ -194,6 +194,7 @@ static void rcpAffine(const float *X, float *R) {
 }
 
 SceneObj::SceneObj(DeviceObj *d) : dev(d) {
+  dev->retain();
   check(cudaMalloc(&status, 16), "cudaMalloc status");
   check(cudaMalloc(&counters, 64), "cudaMalloc counters");
   check(cudaMemset(counters, 0, 64), "memset counters");
@@ -214,6 +215,7 @@ SceneObj::~SceneObj() {
   cudaStreamSynchronize(st);
   cudaFree(status);
   cudaFree(counters);
+  dev->release();
 }
 
 void SceneObj::commit() {
@@ -319,6 +321,7 @@ Scene SceneObj::view() const {
 }
 
 FrameObj::FrameObj(DeviceObj *d, int w, int h, uint32_t ch) : dev(d), W(w), H(h), channels(ch) {
+  dev->retain();
   const size_t n = size_t(w) * h;
   auto alloc = [&](void **p, size_t bytes) {
     check(cudaMalloc(p, bytes), "cudaMalloc framebuffer");
@@ -339,6 +342,7 @@ FrameObj::~FrameObj() {
   for (void *p : {(void *)color, (void *)depth, (void *)variance, (void *)normal, (void *)albedo, (void *)primID,
                   (void *)geomID, (void *)instID})
     if (p) cudaFree(p);
+  dev->release();
 }
 
 FrameD FrameObj::view() const {
@@ -426,7 +430,7 @@ int b200_device_create(int cuda_device, b200_device *out) {
 
 int b200_device_release(b200_device d) {
   if (!d) return B200_INVALID_ARGUMENT;
-  delete reinterpret_cast<DeviceObj *>(d);
+  reinterpret_cast<DeviceObj *>(d)->release();
   return B200_NO_ERROR;
 }
 
@@ -451,7 +455,9 @@ int b200_scene_create(b200_device d, b200_scene *out) {
 int b200_scene_release(b200_scene s) {
   if (!s) return B200_INVALID_ARGUMENT;
   SceneObj *sc = reinterpret_cast<SceneObj *>(s);
-  return guarded(sc->dev, [&]() { delete sc; });
+  cudaSetDevice(sc->dev->dev);
+  delete sc;  // may drop the last reference to its device
+  return B200_NO_ERROR;
 }
 
 int b200_scene_add_mesh(b200_scene s, const float *vertex, int64_t nverts, const uint32_t *index, int64_t ntris,
@@ -564,7 +570,9 @@ int b200_frame_create(b200_device d, int w, int h, uint32_t channels, b200_frame
 int b200_frame_release(b200_frame f) {
   if (!f) return B200_INVALID_ARGUMENT;
   FrameObj *fb = reinterpret_cast<FrameObj *>(f);
-  return guarded(fb->dev, [&]() { delete fb; });
+  cudaSetDevice(fb->dev->dev);
+  delete fb;  // may drop the last reference to its device
+  return B200_NO_ERROR;
 }
 
 int b200_frame_reset(b200_frame f) {

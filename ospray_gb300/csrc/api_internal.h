@@ -23,7 +23,15 @@ struct FilterLUT {
   float *cdf_x = nullptr, *cdf_y = nullptr;
 };
 
+// Handles are reference counted like OSPRay objects (ospRetain/ospRelease):
+// b200_device_release drops the creator's reference, and every scene and
+// framebuffer holds one on its device, so a device outlives its objects.
 struct DeviceObj {
+  int refs = 1;
+  void retain() { __atomic_add_fetch(&refs, 1, __ATOMIC_ACQ_REL); }
+  void release() {
+    if (__atomic_sub_fetch(&refs, 1, __ATOMIC_ACQ_REL) == 0) delete this;
+  }
   int dev;
   cudaStream_t stream = nullptr;
   std::string lastError;

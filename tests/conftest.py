@@ -21,4 +21,4 @@ def b200_device():
     og.lib()  # raises when the CUDA library is missing: no fallback
     dev = og.Device(0)
     yield dev
-    dev.release()
+    dev.release()  # scenes/frames still alive keep the C-side device until they go
