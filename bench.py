@@ -173,7 +173,91 @@ class AOWorkload:
         return int(oracle.lib().or_ray_count(1)), dt, frames
 
 
-WORKLOADS = {"ao": AOWorkload}
+class PTWorkload:
+    """Path tracer, 1920x1080, 16 spp, maxPathLength 5, Russian roulette from
+    depth 3, on 64 instances of a 32,768-triangle displaced sphere (2.1 M
+    triangles instanced) over a ground quad; principled materials; one 2x2
+    quad light (intensity 20) and an ambient light (0.1)."""
+    name = "pt_instanced_spheres_1080p"
+    metric = "Mrays/s"
+
+    def __init__(self, w=1920, h=1080, spp=16):
+        from ospray_gb300 import scenes
+        self.w, self.h, self.spp = w, h, spp
+        self.data = scenes.pt_instanced_scene(width=w, height=h)
+        self.config = {"workload": self.name, "renderer": "pathtracer", "width": w, "height": h, "spp": spp,
+                       "maxPathLength": 5, "roulettePathLength": 3, "instances": len(self.data["xfm"]),
+                       "triangles_per_instance": int(len(self.data["index"])),
+                       "triangles_instanced": int(len(self.data["index"]) * len(self.data["xfm"]) + 2),
+                       "lights": "quad 2x2 intensity 20 + ambient 0.1", "pixelFilter": "gauss"}
+
+    def setup(self, og, dev):
+        from ospray_gb300 import scenes
+        self.og = og
+        t0 = time.perf_counter()
+        self.scene = og.Scene(dev)
+        scenes.build_pt_scene(self.scene, self.data)
+        lights = []
+        for L in self.data["lights"]:
+            if L["type"] == "quad":
+                lights.append(og.quad_light(L["position"], L["edge1"], L["edge2"], L["intensity"]))
+            else:
+                lights.append(og.ambient_light(L["intensity"]))
+        self.scene.set_lights(lights)
+        self.build_ms = (time.perf_counter() - t0) * 1e3
+        c = self.data["camera"]
+        self.cam = og.camera_desc(c["position"], c["direction"], c["up"], fovy=c["fovy"], aspect=c["aspect"])
+        self.params = og.pt_params(spp=self.spp, max_path_length=5, roulette_path_length=3)
+        self.sparams = og.pt_params(spp=self.spp, max_path_length=5, roulette_path_length=3, stats=True)
+        self.mats = og.materials_array(self.data["materials"])
+        self.fb = og.Frame(dev, self.w, self.h, og.FB_COLOR | og.FB_DEPTH | og.FB_ACCUM)
+        self.color = np.empty((self.h, self.w, 4), np.float32)
+
+    def step(self, stats=False):
+        self.og.render_pt(self.scene, self.cam, self.sparams if stats else self.params, self.mats, self.fb)
+
+    def e2e_step(self):
+        self.og.render_pt(self.scene, self.cam, self.params, self.mats, self.fb)
+        self.og.lib().b200_frame_read(self.fb._h, self.og.FB_COLOR, self.color.ctypes.data, self.color.nbytes)
+        return 40 + 76, self.color.nbytes
+
+    def reset(self):
+        self.fb.reset()
+
+    def counters(self, reset=False):
+        return self.scene.counters(reset)
+
+    def cpu_frames(self, budget_s, nthreads):
+        """Oracle on a band of whole rows of the frame, sized to budget_s."""
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        import oracle
+        from ospray_gb300 import scenes
+        if not hasattr(self, "_orc"):
+            o = oracle.Scene()
+            scenes.build_pt_scene(o, self.data)
+            self._orc = (o, oracle.PtWorld(self.data["materials"], self.data["lights"]))
+            c = self.data["camera"]
+            self._ocam = oracle.camera(c["position"], c["direction"], c["up"], fovy=c["fovy"], aspect=c["aspect"])
+            self._op = oracle.pt_params(spp=self.spp, max_path_length=5, roulette_path_length=3)
+            oracle.render_pt(o, self._orc[1], self._ocam, oracle.pt_params(spp=1), 4, 4)  # albedo tables
+            self._rows = 2
+        o, ow = self._orc
+        y0 = self.h // 2 - self._rows // 2
+        oracle.lib().or_ray_count(1)
+        t0 = time.perf_counter()
+        oracle.render_pt(o, ow, self._ocam, self._op, self.w, self.h, rows=(y0, y0 + self._rows), nthreads=nthreads)
+        dt = time.perf_counter() - t0
+        rays = int(oracle.lib().or_ray_count(1))
+        rows = self._rows
+        # grow the band toward the budget for the next call
+        self._rows = int(max(2, min(self.h, rows * min(8.0, budget_s / max(dt, 1e-3)))))
+        if dt < 0.25 * budget_s and self._rows > rows:
+            return self.cpu_frames(budget_s, nthreads)
+        self.cpu_sample = "%d centre rows x %d px x %d spp" % (rows, self.w, self.spp)
+        return rays, dt, rows / self.h
+
+
+WORKLOADS = {"ao": AOWorkload, "pt": PTWorkload}
 
 
 # --------------------------------------------------------------------------- arms
@@ -206,8 +290,8 @@ def run_reference(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded generators)", "config": wl.config, "impl": "reference",
             "cpu_baseline": {"value": round(value, 3), "unit": "Mrays/s", "cores": nthreads, "kind": "port",
-                             "sample": "whole frames of the same workload, about %.1f s of CPU work per step"
-                                       % (args.cpu_budget / max(1, args.steps))},
+                             "sample": "%s, about %.1f s of CPU work per step"
+                                       % (getattr(wl, "cpu_sample", "whole frames"), args.cpu_budget / max(1, args.steps))},
             "e2e": {"value": round(value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -307,9 +391,9 @@ def run_ours(args):
     if not args.no_cpu_baseline:
         nthreads = os.cpu_count() or 1
         crays, cdt, cframes = wl.cpu_frames(args.cpu_budget, nthreads)
+        sample = getattr(wl, "cpu_sample", "%s frames of the same workload" % cframes)
         line["cpu_baseline"] = {"value": round(crays / cdt / 1e6, 3), "unit": "Mrays/s", "cores": nthreads,
-                                "kind": "port", "sample": "%d whole frames of the same workload (%.1f s)"
-                                                          % (cframes, cdt)}
+                                "kind": "port", "sample": "%s (%.1f s)" % (sample, cdt)}
     print(json.dumps(line), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()
@@ -320,7 +404,7 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
-    ap.add_argument("--workload", default="ao", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="pt", choices=sorted(WORKLOADS))
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU-baseline work")
     ap.add_argument("--no-cpu-baseline", action="store_true")

@@ -129,6 +129,48 @@ typedef struct {
   int collectStats;  /* nonzero: count rays / node visits / primitive tests */
 } b200_ao_params;
 
+/* ---- lights of the world (QuadLight::commit lights/QuadLight.cpp:68-108,
+ *      AmbientLight::commit lights/AmbientLight.cpp:40-60, Light::commit
+ *      lights/Light.cpp:22-35).  radiance = color * intensity (the default
+ *      intensityQuantity of both).  The list order is the light index order of
+ *      the path tracer's light CDF (render/pathtracer/PathTracerData.cpp:32-82). */
+enum { B200_LIGHT_QUAD = 0, B200_LIGHT_AMBIENT = 1 };
+typedef struct {
+  int type;
+  int visible;
+  float position[3], edge1[3], edge2[3];
+  float color[3];
+  float intensity;
+} b200_light;
+int b200_scene_set_lights(b200_scene scene, const b200_light *lights, int n);
+
+/* ---- path tracer (PathTracer::commit render/pathtracer/PathTracer.cpp:29-51,
+ *      PathTracer_renderPixel render/pathtracer/PathTracer.ispc:75-216).
+ * Materials are "principled" (render/materials/Principled.cpp:37-79) with the
+ * parameters below; every other principled parameter has its default
+ * (specular 1, ior 1, edgeColor 1, opacity 1, no coat/sheen/transmission).
+ * material_id of an instance (b200_scene_add_instance) indexes `materials`. */
+typedef struct {
+  float baseColor[3];
+  float roughness;
+  float metallic;
+} b200_material;
+typedef struct {
+  int pixelSamples;        /* spp */
+  int maxPathLength;       /* default 20 */
+  int roulettePathLength;  /* default 5 */
+  int maxScatteringEvents; /* default 20 */
+  int lightSamples;        /* default -1: all lights at the first bounce */
+  int limitIndirectLightSamples; /* default 1 */
+  float minContribution;   /* default 0.001 */
+  float maxContribution;   /* default inf */
+  float backgroundColor[4];
+  int pixelFilter;
+  int collectStats;
+} b200_pt_params;
+int b200_render_pt(b200_scene scene, const b200_camera_desc *camera, const b200_pt_params *params,
+                   const b200_material *materials, int nmaterials, b200_frame fb, void *stream);
+
 /* Traversal counters accumulated by renders with collectStats set:
  * [rays traced, BVH node visits, triangle tests, sphere tests]; reset != 0
  * zeroes them after reading.  (Frame statistics; the reference reports only

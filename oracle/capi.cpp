@@ -62,9 +62,10 @@ int or_scene_add_spheres(void *sp, const float *xyzr, int n) {
 }
 
 // xfm: row-major 3x4 affine or null for identity
-void or_scene_add_instance(void *sp, int geom, uint32_t instID, uint32_t geomID, const float *xfm) {
+void or_scene_add_instance(void *sp, int geom, uint32_t instID, uint32_t geomID, const float *xfm, int material) {
   Scene &s = *static_cast<Scene *>(sp);
   InstanceEntry e;
+  e.material = material;
   e.geom = geom;
   e.instID = instID;
   e.geomID = geomID;

@@ -1,0 +1,346 @@
+// Oracle (test infrastructure only): CPU restatement of the path tracer.
+//   PathTracer_renderPixel  render/pathtracer/PathTracer.ispc:75-216
+//   samplePath              render/pathtracer/PathSampler.ispc:109-415
+//   nextEventEstimation     render/pathtracer/NextEventEstimation.ispc:25-160
+//   evaluateVirtualLights   render/pathtracer/VirtualLight.ispc:38-107
+//   transparentShadow       render/pathtracer/TransparentShadow.ispc:18-85
+//                           (opaque materials: the first hit blocks the light)
+//   misHeuristic            render/pathtracer/PathTracerUtil.ih:30-46
+//   light list + CDF        render/pathtracer/PathTracerData.cpp:32-82
+//   parameters              render/pathtracer/PathTracer.cpp:29-51
+#include <cstring>
+
+#include "pt_bsdf.h"
+
+namespace orc {
+
+extern thread_local uint64_t tl_rays;
+
+struct PtParams {
+  int spp, maxPathLength, roulettePathLength, maxScatteringEvents, lightSamples, limitIndirectLightSamples;
+  float minContribution, maxContribution;
+  V4 bg;
+};
+
+struct PtLights {
+  std::vector<int> kind;  // 0 quad, 1 ambient
+  std::vector<QuadLight> quads;
+  std::vector<AmbientLight> ambients;
+  std::vector<int> index;
+  std::vector<float> cdf;
+  void finalize() {
+    cdf.assign(kind.size(), 1.f);
+    if (cdf.empty()) return;
+    float sum = cdf[0];
+    for (size_t i = 1; i < cdf.size(); i++) cdf[i] = sum += cdf[i];
+    const float r = 1.f / sum;
+    for (auto &c : cdf) c = c >= sum ? 0x1.000002p+0f : c * r;
+  }
+  LightSample sample(int i, const DG &dg, V2 s) const {
+    return kind[i] == 0 ? quads[index[i]].sample(dg, s) : ambients[index[i]].sample(dg, s);
+  }
+  LightEval eval(int i, const DG &dg, V3 dir, float lo, float hi) const {
+    return kind[i] == 0 ? quads[index[i]].eval(dg, dir, lo, hi) : ambients[index[i]].eval(dg, dir, lo, hi);
+  }
+  bool visible(int i) const { return kind[i] == 0 ? quads[index[i]].visible : ambients[index[i]].visible; }
+};
+
+namespace {
+
+inline float luminance(V3 c) { return 0.212671f * c.x + 0.715160f * c.y + 0.072169f * c.z; }
+inline float mis(float p1, float p2) {
+  const float p = sqr(p1) / (sqr(p1) + sqr(p2));
+  return p1 > 1e17f ? 1.f : p;
+}
+
+struct Vertex {
+  DG dg;
+  float pdf_w;
+  int numLightSamples;
+  bool env;
+};
+
+struct Ctx {
+  const Scene &sc;
+  const PtLights &L;
+  const std::vector<PrincipledParams> &mats;
+  const PtParams &p;
+  int nFirst, nIndirect;
+};
+
+// shading frame: makeShadingFrame(dg) with dPds = instance xfm * (1,0,0)
+L3 shadingFrame(const DG &dg, V3 dPds) {
+  const V3 N = dg.Ns;
+  V3 U = normalize(dPds);
+  V3 V = cross(N, U);
+  if (dot(V, V) > 0.f) {
+    V = normalize(V);
+    U = cross(V, N);
+    return {U, V, N};
+  }
+  return frame(N);
+}
+
+V3 virtualLights(const Ctx &c, bool straightPath, const Vertex &last, bool env, const Ray &ray, float t,
+                 V3 throughput) {
+  V3 L = v3(0.f);
+  const float lo = length(last.dg.P - ray.org);
+  const float hi = env ? INFINITY : length(last.dg.P - (ray.org + t * ray.dir));
+  const float selPdf = float(last.numLightSamples) / float(c.L.kind.size());
+  for (size_t i = 0; i < c.L.kind.size(); i++) {
+    if (straightPath && !c.L.visible(int(i))) continue;
+    const LightEval le = c.L.eval(int(i), last.dg, ray.dir, lo, hi);
+    if (reduce_max(le.radiance) > 0.f) {
+      const float w = selPdf != 0.f ? mis(last.pdf_w, selPdf * le.pdf) : 1.f;
+      L = L + throughput * le.radiance * w;
+    }
+  }
+  return L;
+}
+
+V3 nee(const Ctx &c, LDSampler &ld, const DG &dg, const Principled &bsdf, V3 wo, V3 throughput, int numLS) {
+  V3 L = v3(0.f);
+  const int nl = int(c.L.kind.size());
+  for (int i = 0; i < numLS; i++) {
+    float ss;
+    const V2 s = ld.get3LightSamples(uint32_t(i), numLS > 1, ss);
+    // Distribution1D_sample over the light CDF
+    int first = 0, len = nl;
+    while (len > 0) {
+      const int half = len >> 1, mid = first + half;
+      if (ss < c.L.cdf[mid]) {
+        len = half;
+      } else {
+        first = mid + 1;
+        len -= half + 1;
+      }
+    }
+    const float prob = c.L.cdf[first] - (first == 0 ? 0.f : c.L.cdf[first - 1]);
+    const float selProb = prob * float(numLS);
+    LightSample ls = c.L.sample(first, dg, s);
+    ls.weight = ls.weight / selProb;
+    ls.pdf *= selProb;
+    if (reduce_max(ls.weight) <= 0.f || ls.pdf <= 0.f) continue;
+    const BSDFEval fe = bsdf.eval(wo, ls.dir);
+    if (reduce_max(fe.value) <= 0.f) continue;
+    V3 org = dg.P;
+    if (dot(dg.Ng, ls.dir) < 0.f) org = org - (2.f * dg.epsilon) * dg.Ng;
+    tl_rays++;
+    if (c.sc.occluded({org, 0.f, ls.dir, ls.dist})) continue;
+    const V3 contrib = throughput * fe.value * ls.weight;
+    L = L + contrib * mis(ls.pdf, fe.pdf);
+  }
+  return L;
+}
+
+struct PathOut {
+  V3 rgb;
+  float alpha, z;
+  uint32_t primID, geomID, instID;
+};
+
+PathOut samplePath(const Ctx &c, LDSampler &ld, Ray ray) {
+  PathOut out = {v3(0.f), 1.f, INFINITY, INVALID_ID, INVALID_ID, INVALID_ID};
+  V3 throughput = v3(1.f), contribution = v3(0.f);
+  int depth = 0, scatteringEvents = 0;
+  bool straightPath = true, firstBounceLight = true;
+  Vertex last;
+  last.env = false;
+  last.pdf_w = INFINITY;
+  last.dg.P = ray.org;
+  last.dg.epsilon = reduce_max(vabs(ray.org)) * ulpEpsilon;
+  last.dg.Ns = last.dg.Ng = ray.dir;
+  last.numLightSamples = 0;
+  do {
+    Hit hit;
+    tl_rays++;
+    const bool h = c.sc.intersect(ray, hit);
+    const float t = h ? hit.t : ray.tfar;
+    const V3 wo = -ray.dir;
+    if (depth == 0) out.z = t;
+    if (!h && straightPath) {
+      out.alpha -= luminance(throughput) * (1.f - c.p.bg.w);
+      contribution = contribution + throughput * v3(c.p.bg.x, c.p.bg.y, c.p.bg.z);
+    }
+    contribution = contribution + virtualLights(c, straightPath, last, !h, ray, t, throughput);
+    if (!h) break;
+    if (depth >= c.p.maxPathLength) break;  // no geometry lights
+    const DG dg = postIntersect(c.sc, ray, hit);
+    if (depth == 0) {
+      out.primID = dg.primID;
+      out.geomID = dg.geomID;
+      out.instID = dg.instID;
+    }
+    if (depth >= c.p.maxPathLength || scatteringEvents >= c.p.maxScatteringEvents) break;
+    const InstanceEntry *e = nullptr;
+    for (const auto &en : c.sc.entries)
+      if (en.instID == hit.instID && en.geomID == hit.geomID) e = &en;
+    if (!e || e->material < 0 || size_t(e->material) >= c.mats.size()) break;  // no material: no BSDF
+    Principled bsdf;
+    bsdf.init(c.mats[e->material], shadingFrame(dg, e->identity ? v3(1, 0, 0) : e->xfm.l.vx));
+    if (bsdf.impSum == 0.f) break;
+    ld.nextGroup();
+    int numLS = 0;
+    {  // isSmooth: diffuse or glossy lobes present
+      numLS = firstBounceLight ? c.nFirst : c.nIndirect;
+      contribution = contribution + nee(c, ld, dg, bsdf, wo, throughput, numLS);
+      firstBounceLight = false;
+    }
+    float ss;
+    uint32_t uu3;
+    const V2 s = ld.getNext4Samples(ss, uu3);
+    BSDFSample fs = bsdf.sample(wo, s, ss);
+    const bool sameSide = dot(fs.wi, dg.Ng) >= 0.f;
+    if (!sameSide) fs.weight = v3(0.f);  // every lobe here is a reflection
+    if (reduce_max(fs.weight) <= 0.f || fs.pdf <= 0.f) break;
+    throughput = throughput * fs.weight;
+    if (depth >= c.p.roulettePathLength) {
+      const float rr = ld.finalizeDim3(uu3);
+      const float contProb = std::fmin(reduce_max(throughput), 0.95f);
+      if (rr > contProb) break;
+      throughput = throughput * (1.f / contProb);
+    }
+    last.dg = dg;
+    last.pdf_w = fs.pdf;
+    last.numLightSamples = numLS;
+    if (!(ray.dir.x == fs.wi.x && ray.dir.y == fs.wi.y && ray.dir.z == fs.wi.z)) straightPath = false;
+    ray = {dg.P, 0.f, fs.wi, INFINITY};
+    depth++;
+    scatteringEvents++;
+  } while (reduce_max(throughput) > c.p.minContribution);
+  out.rgb = contribution;
+  if (std::isnan(contribution.x) || std::isnan(contribution.y) || std::isnan(contribution.z)) {
+    out.rgb = v3(0.f);
+    out.alpha = 1.f;
+  }
+  return out;
+}
+
+}  // namespace
+
+void renderPT(const Scene &sc, const PtLights &lights, const std::vector<PrincipledParams> &mats, const Camera &cam,
+              const PixelFilter &pf, const PtParams &p, FrameBuffer &fb, int nthreads, int y0, int y1) {
+  const int W = fb.W;
+  const int nl = int(lights.kind.size());
+  const int nFirst = p.lightSamples >= 0 && nl > 0 ? p.lightSamples : std::min(1024, nl);
+  const int nIndirect = p.limitIndirectLightSamples && nFirst >= 1 ? 1 : nFirst;
+  const Ctx c = {sc, lights, mats, p, nFirst, nIndirect};
+  const V2 rcpSize = {1.f / float(fb.W), 1.f / float(fb.H)};
+  const uint32_t accumID = uint32_t(fb.frameID);
+  parallelRows(y1 - y0, nthreads, [&](int yy) {
+    const int y = y0 + yy;
+    for (int x = 0; x < W; x++) {
+      ScreenSample acc;
+      const uint32_t seed = 0x49c5f37eu ^ uint32_t(W * y + x);
+      for (int s = 0; s < p.spp; s++) {
+        const uint32_t sampleID = accumID * uint32_t(p.spp) + uint32_t(s);
+        LDSampler ld;
+        ld.init(seed, sampleID, sampleID * uint32_t(nFirst), 16, 16);
+        uint32_t ss234[3];
+        const V2 ps = ld.getNext5Samples(ss234);
+        const V2 pfs = pf.sample(ps);
+        const V2 center = {(float(x) + 0.5f) * rcpSize.x, (float(y) + 0.5f) * rcpSize.y};
+        const V2 screen = {center.x + pfs.x * rcpSize.x, center.y + pfs.y * rcpSize.y};
+        const Ray ray = cameraRay(cam, screen);
+        const PathOut o = samplePath(c, ld, ray);
+        ScreenSample smp;
+        smp.rgb = vmin(o.rgb, v3(p.maxContribution));
+        smp.alpha = o.alpha;
+        smp.z = o.z;
+        smp.primID = o.primID;
+        smp.geomID = o.geomID;
+        smp.instID = o.instID;
+        accumulateScreen(acc, smp);
+      }
+      const float rspp = 1.f / float(p.spp);
+      acc.rgb = acc.rgb * rspp;
+      acc.alpha *= rspp;
+      fbAccumulate(fb, x, y, acc);
+    }
+    g_rayCount.fetch_add(tl_rays);
+    tl_rays = 0;
+  });
+}
+
+}  // namespace orc
+
+using namespace orc;
+
+struct OrCameraPT {
+  float pos[3], dir[3], up[3];
+  float fovy, aspect, nearClip;
+};
+
+struct OrPtScene {
+  PtLights lights;
+  std::vector<PrincipledParams> mats;
+};
+
+extern "C" {
+
+void *or_pt_new() { return new OrPtScene(); }
+void or_pt_free(void *p) { delete static_cast<OrPtScene *>(p); }
+int or_pt_add_material(void *p, const float *baseColor, float roughness, float metallic) {
+  OrPtScene &s = *static_cast<OrPtScene *>(p);
+  s.mats.push_back({{baseColor[0], baseColor[1], baseColor[2]}, roughness, metallic});
+  return int(s.mats.size() - 1);
+}
+// position, edge1, edge2 (3 floats each), radiance rgb
+void or_pt_add_quad_light(void *p, const float *pos, const float *e1, const float *e2, const float *radiance) {
+  OrPtScene &s = *static_cast<OrPtScene *>(p);
+  QuadLight q;
+  q.init({pos[0], pos[1], pos[2]}, {e1[0], e1[1], e1[2]}, {e2[0], e2[1], e2[2]},
+         {radiance[0], radiance[1], radiance[2]});
+  s.lights.kind.push_back(0);
+  s.lights.index.push_back(int(s.lights.quads.size()));
+  s.lights.quads.push_back(q);
+  s.lights.finalize();
+}
+void or_pt_add_ambient_light(void *p, const float *radiance) {
+  OrPtScene &s = *static_cast<OrPtScene *>(p);
+  s.lights.kind.push_back(1);
+  s.lights.index.push_back(int(s.lights.ambients.size()));
+  s.lights.ambients.push_back({{radiance[0], radiance[1], radiance[2]}, true});
+  s.lights.finalize();
+}
+
+struct OrPtParams {
+  int spp, maxPathLength, roulettePathLength, maxScatteringEvents, lightSamples, limitIndirectLightSamples;
+  float minContribution, maxContribution;
+  float bg[4];
+  int pixelFilter;
+};
+
+// Renders `frames` accumulated frames of rows [y0, y1) (y1 <= 0: all rows).
+void or_render_pt(void *scp, void *ptp, const OrCameraPT *cam, const OrPtParams *pp, int W, int H, int frames,
+                  int y0, int y1, float *color, float *depth, uint32_t *ids, int nthreads) {
+  const Scene &sc = *static_cast<Scene *>(scp);
+  const OrPtScene &pt = *static_cast<OrPtScene *>(ptp);
+  const Camera c = makeCamera({cam->pos[0], cam->pos[1], cam->pos[2]}, {cam->dir[0], cam->dir[1], cam->dir[2]},
+                              {cam->up[0], cam->up[1], cam->up[2]}, cam->fovy, cam->aspect, cam->nearClip);
+  PixelFilter pf;
+  pf.init(pp->pixelFilter);
+  PtParams p = {pp->spp, pp->maxPathLength, pp->roulettePathLength, pp->maxScatteringEvents, pp->lightSamples,
+                pp->limitIndirectLightSamples, pp->minContribution, pp->maxContribution,
+                {pp->bg[0], pp->bg[1], pp->bg[2], pp->bg[3]}};
+  if (y1 <= 0) {
+    y0 = 0;
+    y1 = H;
+  }
+  FrameBuffer fb;
+  fb.resize(W, H);
+  for (int f = 0; f < frames; f++) {
+    renderPT(sc, pt.lights, pt.mats, c, pf, p, fb, nthreads, y0, y1);
+    fb.frameID++;
+  }
+  const size_t N = size_t(W) * H;
+  if (color) std::memcpy(color, fb.color.data(), N * 16);
+  if (depth) std::memcpy(depth, fb.depth.data(), N * 4);
+  if (ids) {
+    std::memcpy(ids, fb.primID.data(), N * 4);
+    std::memcpy(ids + N, fb.geomID.data(), N * 4);
+    std::memcpy(ids + 2 * N, fb.instID.data(), N * 4);
+  }
+}
+
+}  // extern "C"

@@ -59,6 +59,7 @@ struct InstanceEntry {
   uint32_t instID;   // world instance index
   uint32_t geomID;   // model index within the instance's group
   bool identity;
+  int material = -1;  // renderer material slot of the geometric model
   A3 xfm, rcp;
   Box worldBox;
 };

@@ -48,6 +48,65 @@ class AOParams(ctypes.Structure):
                 ("collectStats", ctypes.c_int)]
 
 
+LIGHT_QUAD, LIGHT_AMBIENT = 0, 1
+
+
+class Light(ctypes.Structure):
+    _fields_ = [("type", ctypes.c_int), ("visible", ctypes.c_int), ("position", ctypes.c_float * 3),
+                ("edge1", ctypes.c_float * 3), ("edge2", ctypes.c_float * 3), ("color", ctypes.c_float * 3),
+                ("intensity", ctypes.c_float)]
+
+
+class Material(ctypes.Structure):
+    _fields_ = [("baseColor", ctypes.c_float * 3), ("roughness", ctypes.c_float), ("metallic", ctypes.c_float)]
+
+
+class PTParams(ctypes.Structure):
+    _fields_ = [("pixelSamples", ctypes.c_int), ("maxPathLength", ctypes.c_int),
+                ("roulettePathLength", ctypes.c_int), ("maxScatteringEvents", ctypes.c_int),
+                ("lightSamples", ctypes.c_int), ("limitIndirectLightSamples", ctypes.c_int),
+                ("minContribution", ctypes.c_float), ("maxContribution", ctypes.c_float),
+                ("backgroundColor", ctypes.c_float * 4), ("pixelFilter", ctypes.c_int),
+                ("collectStats", ctypes.c_int)]
+
+
+def quad_light(position, edge1, edge2, intensity=1.0, color=(1, 1, 1), visible=True):
+    L = Light()
+    L.type, L.visible = LIGHT_QUAD, int(visible)
+    L.position[:], L.edge1[:], L.edge2[:] = list(position), list(edge1), list(edge2)
+    L.color[:], L.intensity = list(color), float(intensity)
+    return L
+
+
+def ambient_light(intensity=1.0, color=(1, 1, 1), visible=True):
+    L = Light()
+    L.type, L.visible = LIGHT_AMBIENT, int(visible)
+    L.color[:], L.intensity = list(color), float(intensity)
+    return L
+
+
+def materials_array(mats):
+    """mats: iterable of (r, g, b, roughness, metallic)."""
+    arr = (Material * max(1, len(mats)))()
+    for i, m in enumerate(mats):
+        arr[i].baseColor[:] = [float(m[0]), float(m[1]), float(m[2])]
+        arr[i].roughness, arr[i].metallic = float(m[3]), float(m[4])
+    return arr, len(mats)
+
+
+def pt_params(spp=1, max_path_length=20, roulette_path_length=5, max_scattering_events=20, light_samples=-1,
+              limit_indirect_light_samples=True, min_contribution=0.001, max_contribution=float("inf"),
+              bg=(0, 0, 0, 0), pixel_filter=PF_GAUSS, stats=False):
+    p = PTParams()
+    p.pixelSamples, p.maxPathLength, p.roulettePathLength = int(spp), int(max_path_length), int(roulette_path_length)
+    p.maxScatteringEvents, p.lightSamples = int(max_scattering_events), int(light_samples)
+    p.limitIndirectLightSamples = int(bool(limit_indirect_light_samples))
+    p.minContribution, p.maxContribution = float(min_contribution), float(max_contribution)
+    p.backgroundColor[:] = list(map(float, bg))
+    p.pixelFilter, p.collectStats = int(pixel_filter), int(bool(stats))
+    return p
+
+
 def lib_path():
     return os.path.join(BUILD, "libb200.so")
 
@@ -84,6 +143,8 @@ def lib():
             "b200_frame_channel": (P, [P, U32]),
             "b200_frame_read": (I, [P, U32, P, ctypes.c_size_t]),
             "b200_render_ao": (I, [P, ctypes.POINTER(CameraDesc), ctypes.POINTER(AOParams), P, P]),
+            "b200_scene_set_lights": (I, [P, P, I]),
+            "b200_render_pt": (I, [P, ctypes.POINTER(CameraDesc), ctypes.POINTER(PTParams), P, I, P, P]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -164,6 +225,10 @@ class Scene:
 
     def commit(self):
         self.device._check(lib().b200_scene_commit(self._h))
+
+    def set_lights(self, lights):
+        arr = (Light * max(1, len(lights)))(*lights)
+        self.device._check(lib().b200_scene_set_lights(self._h, ctypes.cast(arr, ctypes.c_void_p), len(lights)))
 
     def bounds(self):
         b = np.zeros(6, np.float32)
@@ -265,4 +330,12 @@ def ao_params(spp=1, ao_samples=1, ao_distance=1e20, ao_intensity=1.0, bg=(0, 0,
 
 def render_ao(scene, camera, params, frame, stream=None):
     scene.device._check(lib().b200_render_ao(scene._h, ctypes.byref(camera), ctypes.byref(params), frame._h,
+                                             ctypes.c_void_p(stream) if stream else None))
+
+
+def render_pt(scene, camera, params, materials, frame, stream=None):
+    """materials: (ctypes array, count) from materials_array()."""
+    arr, n = materials
+    scene.device._check(lib().b200_render_pt(scene._h, ctypes.byref(camera), ctypes.byref(params),
+                                             ctypes.cast(arr, ctypes.c_void_p), n, frame._h,
                                              ctypes.c_void_p(stream) if stream else None))

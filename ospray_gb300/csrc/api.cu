@@ -131,10 +131,19 @@ DeviceObj::DeviceObj(int cudaDev) : dev(cudaDev) {
   }
 }
 
+const AlbedoTablesD *DeviceObj::albedoTables() {
+  if (!albedo) {
+    check(cudaMalloc(&albedo, sizeof(AlbedoTablesD)), "cudaMalloc albedo tables");
+    check(computeAlbedoTables(albedo, stream), "albedo tables");
+  }
+  return albedo;
+}
+
 DeviceObj::~DeviceObj() {
   cudaSetDevice(dev);
   cudaStreamSynchronize(stream);
   cudaFree(tables);
+  if (albedo) cudaFree(albedo);
   for (auto &L : luts) {
     cudaFree(L.cdf_x);
     cudaFree(L.cdf_y);
@@ -213,6 +222,9 @@ SceneObj::~SceneObj() {
   if (tlas.leafPrim) cudaFreeAsync(tlas.leafPrim, st);
   if (dEntries) cudaFreeAsync(dEntries, st);
   cudaStreamSynchronize(st);
+  if (dLights) cudaFree(dLights);
+  if (dLightCdf) cudaFree(dLightCdf);
+  if (dMaterials) cudaFree(dMaterials);
   cudaFree(status);
   cudaFree(counters);
   dev->release();
@@ -615,6 +627,105 @@ int b200_render_ao(b200_scene s, const b200_camera_desc *camera, const b200_ao_p
     check(launchRenderAO(sc->dev->tables, sc->view(), makeCamera(*camera), sc->dev->filter(p->pixelFilter), d,
                          fb->view(), p->collectStats != 0, st),
           "AO launch");
+    fb->frameID++;
+  });
+}
+
+int b200_scene_set_lights(b200_scene s, const b200_light *lights, int n) {
+  if (!s) return B200_INVALID_ARGUMENT;
+  SceneObj *sc = reinterpret_cast<SceneObj *>(s);
+  return guarded(sc->dev, [&]() {
+    require(n >= 0 && (n == 0 || lights), "bad light array");
+    std::vector<LightD> h(n);
+    for (int i = 0; i < n; i++) {
+      const b200_light &L = lights[i];
+      require(L.type == B200_LIGHT_QUAD || L.type == B200_LIGHT_AMBIENT, "unsupported light type");
+      LightD &d = h[i];
+      std::memset(&d, 0, sizeof(d));
+      d.type = L.type;
+      d.visible = L.visible;
+      d.radiance = mk(L.color[0] * L.intensity, L.color[1] * L.intensity, L.color[2] * L.intensity);
+      if (L.type == B200_LIGHT_QUAD) {
+        d.position = mk(L.position[0], L.position[1], L.position[2]);
+        d.edge1 = mk(L.edge1[0], L.edge1[1], L.edge1[2]);
+        d.edge2 = mk(L.edge2[0], L.edge2[1], L.edge2[2]);
+        const V3 nd = cross(d.edge2, d.edge1);
+        d.ppdf = 1.f / std::sqrt(dot(nd, nd));
+        require(std::isfinite(d.ppdf), "degenerate quad light");
+        d.nnormal = mul(nd, d.ppdf);
+      }
+    }
+    // uniform light-selection CDF (Distribution1D_create over all-ones)
+    std::vector<float> cdf(n, 1.f);
+    if (n) {
+      float sum = cdf[0];
+      for (int i = 1; i < n; i++) cdf[i] = sum += cdf[i];
+      const float r = 1.f / sum;
+      for (auto &c : cdf) c = c >= sum ? 0x1.000002p+0f : c * r;
+    }
+    if (sc->dLights) cudaFree(sc->dLights);
+    if (sc->dLightCdf) cudaFree(sc->dLightCdf);
+    sc->dLights = nullptr;
+    sc->dLightCdf = nullptr;
+    sc->nLights = n;
+    if (n) {
+      check(cudaMalloc(&sc->dLights, sizeof(LightD) * n), "alloc lights");
+      check(cudaMalloc(&sc->dLightCdf, sizeof(float) * n), "alloc lights");
+      check(cudaMemcpy(sc->dLights, h.data(), sizeof(LightD) * n, cudaMemcpyHostToDevice), "upload lights");
+      check(cudaMemcpy(sc->dLightCdf, cdf.data(), sizeof(float) * n, cudaMemcpyHostToDevice), "upload lights");
+    }
+  });
+}
+
+int b200_render_pt(b200_scene s, const b200_camera_desc *camera, const b200_pt_params *p,
+                   const b200_material *materials, int nmaterials, b200_frame f, void *stream) {
+  if (!s || !camera || !p || !f) return B200_INVALID_ARGUMENT;
+  SceneObj *sc = reinterpret_cast<SceneObj *>(s);
+  FrameObj *fb = reinterpret_cast<FrameObj *>(f);
+  return guarded(sc->dev, [&]() {
+    if (!sc->committed) throw Error(B200_INVALID_OPERATION, "scene not committed");
+    require(p->pixelSamples >= 1 && p->maxPathLength >= 0, "bad path tracer parameters");
+    require(p->pixelFilter >= B200_PF_POINT && p->pixelFilter <= B200_PF_BLACKMAN_HARRIS, "bad pixel filter");
+    require(nmaterials >= 0 && (nmaterials == 0 || materials), "bad material array");
+    cudaStream_t st = stream ? (cudaStream_t)stream : sc->dev->stream;
+    // upload the material list when it changed since the last frame
+    const bool same = int(sc->lastMaterials.size()) == nmaterials &&
+                      (nmaterials == 0 ||
+                       std::memcmp(sc->lastMaterials.data(), materials, sizeof(b200_material) * nmaterials) == 0);
+    if (!same) {
+      std::vector<MaterialD> h(nmaterials);
+      for (int i = 0; i < nmaterials; i++)
+        h[i] = {materials[i].baseColor[0], materials[i].baseColor[1], materials[i].baseColor[2],
+                materials[i].roughness, materials[i].metallic};
+      if (nmaterials > sc->capMaterials) {
+        if (sc->dMaterials) cudaFree(sc->dMaterials);
+        check(cudaMalloc(&sc->dMaterials, sizeof(MaterialD) * nmaterials), "alloc materials");
+        sc->capMaterials = nmaterials;
+      }
+      if (nmaterials)
+        check(cudaMemcpy(sc->dMaterials, h.data(), sizeof(MaterialD) * nmaterials, cudaMemcpyHostToDevice),
+              "upload materials");
+      sc->lastMaterials.assign(materials, materials + nmaterials);
+    }
+    sc->nMaterials = nmaterials;
+    PtParamsD d;
+    d.spp = p->pixelSamples;
+    d.maxPathLength = p->maxPathLength;
+    d.roulettePathLength = p->roulettePathLength;
+    d.maxScatteringEvents = p->maxScatteringEvents;
+    const int nl = sc->nLights;
+    d.nFirst = p->lightSamples >= 0 && nl > 0 ? p->lightSamples : std::min(1024, nl);
+    d.nIndirect = p->limitIndirectLightSamples && d.nFirst >= 1 ? 1 : d.nFirst;
+    if (nl == 0) d.nFirst = d.nIndirect = 0;
+    d.numLights = nl;
+    d.numMaterials = nmaterials;
+    d.minContribution = p->minContribution;
+    d.maxContribution = p->maxContribution;
+    for (int k = 0; k < 4; k++) d.bg[k] = p->backgroundColor[k];
+    check(launchRenderPT(sc->dev->tables, sc->view(), makeCamera(*camera), sc->dev->filter(p->pixelFilter), d,
+                         sc->dMaterials, sc->dLights, sc->dLightCdf, sc->dev->albedoTables(), fb->view(),
+                         p->collectStats != 0, st),
+          "path tracer launch");
     fb->frameID++;
   });
 }

@@ -37,7 +37,9 @@ struct DeviceObj {
   std::string lastError;
   SamplerTables *tables = nullptr;
   FilterLUT luts[5];
+  AlbedoTablesD *albedo = nullptr;  // computed at the first path-traced frame
   explicit DeviceObj(int cudaDev);
+  const AlbedoTablesD *albedoTables();
   ~DeviceObj();
   PixelFilterD filter(int type) const;
 };
@@ -70,6 +72,13 @@ struct SceneObj {
   unsigned long long *counters = nullptr;  // traversal statistics (render stats mode)
   bool committed = false;
   float bounds[6] = {0, 0, 0, 0, 0, 0};
+  // path-tracer state: world lights and the renderer's material list
+  LightD *dLights = nullptr;
+  float *dLightCdf = nullptr;
+  int nLights = 0;
+  MaterialD *dMaterials = nullptr;
+  int nMaterials = 0, capMaterials = 0;
+  std::vector<b200_material> lastMaterials;
   explicit SceneObj(DeviceObj *d);
   ~SceneObj();
   void commit();

@@ -1,0 +1,453 @@
+// Path tracer: one thread per pixel runs the reference's samplePath for each
+// of the pixel's samples and accumulates into the framebuffer.
+//   PathTracer_renderPixel  render/pathtracer/PathTracer.ispc:75-216
+//   samplePath              render/pathtracer/PathSampler.ispc:109-415
+//   nextEventEstimation     render/pathtracer/NextEventEstimation.ispc:25-160
+//   evaluateVirtualLights   render/pathtracer/VirtualLight.ispc:38-107
+//   transparentShadow       render/pathtracer/TransparentShadow.ispc:18-85
+//     (all materials here are opaque, so a shadow ray is an any-hit query)
+//   misHeuristic            render/pathtracer/PathTracerUtil.ih:30-46
+#include "kernels.h"
+#include "pt_bsdf.cuh"
+
+namespace b200 {
+
+namespace {
+
+// ---------------------------------------------------------------- lights
+struct SphQuad {
+  V3 e0, e1, z;
+  float S, k, n0z, n2z, x0, x1, y0, y1, z0;
+};
+
+B200_D SphQuad sphQuad(V3 q0, V3 e0, V3 e1, V3 n, V3 P) {
+  const float e0l = sqrtf(fdot(e0, e0)), e1l = sqrtf(fdot(e1, e1));
+  SphQuad q;
+  q.e0 = e0 * (1.f / e0l);
+  q.e1 = e1 * (1.f / e1l);
+  const V3 d = q0 - P;
+  q.z0 = fdot(d, n);
+  q.z = q.z0 > 0.f ? -n : n;
+  q.z0 = -fabsf(q.z0);
+  q.x0 = fdot(d, q.e0);
+  q.y0 = fdot(d, q.e1);
+  q.x1 = q.x0 + e0l;
+  q.y1 = q.y0 + e1l;
+  const V3 v00 = mk(q.x0, q.y0, q.z0), v01 = mk(q.x0, q.y1, q.z0), v10 = mk(q.x1, q.y0, q.z0),
+           v11 = mk(q.x1, q.y1, q.z0);
+  const V3 n0 = fnormalize(fcross(v00, v10)), n1 = fnormalize(fcross(v10, v11));
+  const V3 n2 = fnormalize(fcross(v11, v01)), n3 = fnormalize(fcross(v01, v00));
+  q.n0z = n0.z;
+  q.n2z = n2.z;
+  const float g0 = acosf(fminf(fmaxf(-fdot(n0, n1), -1.f), 1.f));
+  const float g1 = acosf(fminf(fmaxf(-fdot(n1, n2), -1.f), 1.f));
+  const float g2 = acosf(fminf(fmaxf(-fdot(n2, n3), -1.f), 1.f));
+  const float g3 = acosf(fminf(fmaxf(-fdot(n3, n0), -1.f), 1.f));
+  q.k = 2.f * PI_F - g2 - g3;
+  q.S = fmaxf(0.f, g0 + g1 - q.k);
+  return q;
+}
+
+B200_D V3 sampleSphQuad(const SphQuad &q, float sx, float sy) {
+  const float au = sx * q.S + q.k;
+  float sinau, cosau;
+  sincosf(au, &sinau, &cosau);
+  const float fu = (cosau * q.n0z - q.n2z) / sinau;
+  const float sg = float(0.f < fu) - float(fu < 0.f);
+  const float cu = fminf(fmaxf(1.f / sqrtf(fu * fu + sqrf(q.n0z)) * sg, -1.f), 1.f);
+  const float x0 = -(cu * q.z0) / sqrtf(1.f - cu * cu);
+  const float xu = fminf(fmaxf(x0, q.x0), q.x1);
+  const float ds2 = sqrf(xu) + sqrf(q.z0);
+  const float ds = sqrtf(ds2);
+  const float h0 = q.y0 / sqrtf(ds2 + sqrf(q.y0));
+  const float h1 = q.y1 / sqrtf(ds2 + sqrf(q.y1));
+  const float hv = sy * (h1 - h0) + h0;
+  const float hv2 = sqrf(hv);
+  const float yv = hv2 < 1.f - 1e-4f ? (hv * ds) / sqrtf(1.f - hv2) : q.y1;
+  return xu * q.e0 + yv * q.e1 + q.z0 * q.z;
+}
+
+B200_D float solveQuadratic(float A, float B, float C) {
+  if (A == 0.f) return -C / B;
+  float rad = B * B - 4.f * A * C;
+  if (rad < 0.f) return 0.f;
+  rad = sqrtf(rad);
+  float root;
+  if (B >= 0.f) {
+    root = (-B - rad) / (2.f * A);
+    if (root < 0.f || root > 1.f) root = 2.f * C / (-B - rad);
+  } else {
+    root = 2.f * C / (-B + rad);
+    if (root < 0.f || root > 1.f) root = (-B + rad) / (2.f * A);
+  }
+  return root;
+}
+
+// Hart et al. 2020 bilinear warp toward the cosine-weighted corners
+B200_D V3 cosineWeightedRNG(V3 q0, V3 e0, V3 e1, V3 P, V3 Ng, float sx, float sy) {
+  const V3 wp0 = q0, wp1 = q0 + e0, wp2 = q0 + e1, wp3 = wp1 + e1;
+  const float p0 = fmaxf(0.f, fdot(fnormalize(wp0 - P), Ng)), p1 = fmaxf(0.f, fdot(fnormalize(wp1 - P), Ng));
+  const float p2 = fmaxf(0.f, fdot(fnormalize(wp2 - P), Ng)), p3 = fmaxf(0.f, fdot(fnormalize(wp3 - P), Ng));
+  if (p0 + p2 == 0.f) return mk(sx, sy, 1.f);
+  const float tot = p0 + p2 + p1 + p3;
+  const float W00 = p0, W01 = p2, W10 = p1, W11 = p3;
+  float u, v;
+  {
+    const float A = W10 + W11 - W01 - W00, B = 2.f * (W01 + W00);
+    u = (A + B == 0.f) ? sx : solveQuadratic(A, B, -(W00 + W01 + W10 + W11) * sx);
+  }
+  {
+    const float A = (1.f - u) * W01 + u * W11 - (1.f - u) * W00 - u * W10;
+    const float B = 2.f * (1.f - u) * W00 + 2.f * u * W10;
+    v = (A + B == 0.f) ? sy : solveQuadratic(A, B, -((1.f - u) * W01 + u * W11 + (1.f - u) * W00 + u * W10) * sy);
+  }
+  const float pdf = 4.f * ((1.f - u) * (1.f - v) * p0 + u * (1.f - v) * p1 + u * v * p3 + (1.f - u) * v * p2) / tot;
+  return mk(u, v, pdf);
+}
+
+struct LightSampleD {
+  V3 weight, dir;
+  float dist, pdf;
+};
+
+B200_D LightSampleD sampleLight(const LightD &L, V3 P, V3 Ng, V3 Ns, float sx, float sy) {
+  LightSampleD r;
+  if (L.type == LIGHT_QUAD) {
+    if (sx == 0.f && sy == 0.f) {
+      const V3 p = L.position + L.edge1 * 0.5f + L.edge2 * 0.5f;
+      const V3 d = p - P;
+      const float dist = sqrtf(fdot(d, d));
+      r.dir = d * (1.f / dist);
+      r.dist = dist;
+      const float cosd = fdot(L.nnormal, r.dir);
+      r.pdf = L.ppdf * sqrf(dist) / fabsf(cosd);
+      r.weight = L.radiance * (cosd > 0.f ? 1.f / r.pdf : 0.f);
+      return r;
+    }
+    const SphQuad q = sphQuad(L.position, L.edge1, L.edge2, -L.nnormal, P);
+    const V3 cw = cosineWeightedRNG(L.position, L.edge1, L.edge2, P, Ng, sx, sy);
+    const V3 d = sampleSphQuad(q, cw.x, cw.y);
+    const float dist = sqrtf(fdot(d, d));
+    r.dir = d * (1.f / dist);
+    r.dist = dist;
+    const float cosd = fdot(L.nnormal, r.dir);
+    r.pdf = q.S == 0.f ? 0.f : cw.z / q.S;
+    r.weight = (cosd > 0.f && r.pdf != 0.f) ? L.radiance * (1.f / r.pdf) : splat(0.f);
+    return r;
+  }
+  // ambient: cosine hemisphere about Ns
+  V3 dx, dy;
+  frame(Ns, dx, dy);
+  float sp, cp;
+  sincosf(2.f * PI_F * sx, &sp, &cp);
+  const float cosT = sqrtf(sy), sinT = sqrtf(1.f - sy);
+  r.dir = dx * (cp * sinT) + dy * (sp * sinT) + Ns * cosT;
+  r.pdf = cosT / PI_F;
+  r.dist = INFINITY;
+  r.weight = L.radiance * (1.f / r.pdf);
+  return r;
+}
+
+B200_D V3 evalLight(const LightD &L, V3 P, V3 Ns, V3 dir, float minDist, float maxDist, float &pdf) {
+  pdf = 0.f;
+  if (L.type == LIGHT_QUAD) {
+    const float cosd = fdot(L.nnormal, dir);
+    if (cosd <= 0.f) return splat(0.f);
+    const V3 c = L.position - P;
+    const V3 r = fcross(c, dir);
+    const float rcosd = 1.f / cosd;
+    const float u = fdot(r, L.edge1) * rcosd, v = -fdot(r, L.edge2) * rcosd;
+    if (fminf(u, v) < 0.f || fmaxf(u, v) * L.ppdf > 1.f) return splat(0.f);
+    const float dist = fdot(L.nnormal, c) * rcosd;
+    if (dist <= minDist || dist > maxDist) return splat(0.f);
+    const SphQuad q = sphQuad(L.position, L.edge1, L.edge2, -L.nnormal, P);
+    if (q.S > 0.f) {
+      pdf = 1.f / q.S;
+      return L.radiance;
+    }
+    return splat(0.f);
+  }
+  pdf = fmaxf(fdot(Ns, dir), 0.f) / PI_F;
+  return INFINITY <= maxDist ? L.radiance : splat(0.f);
+}
+
+B200_D float misH(float p1, float p2) {
+  const float p = sqrf(p1) / (sqrf(p1) + sqrf(p2));
+  return p1 > 1e17f ? 1.f : p;
+}
+B200_D float maxc(V3 v) { return fmaxf(fmaxf(v.x, v.y), v.z); }
+B200_D float luminance(V3 c) { return 0.212671f * c.x + 0.715160f * c.y + 0.072169f * c.z; }
+
+struct PtCtx {
+  const SamplerTables *T;
+  Scene sc;
+  PtParamsD p;
+  const MaterialD *mats;
+  const LightD *lights;
+  const float *lightCdf;
+  const AlbedoTablesD *AT;
+};
+
+struct PathResult {
+  V3 rgb;
+  float alpha, z;
+  uint32_t primID, geomID, instID;
+};
+
+template <bool STATS>
+B200_D PathResult samplePath(const PtCtx &c, LDSampler &ld, Ray ray, TraceStats *ts) {
+  PathResult out = {splat(0.f), 1.f, INFINITY, INVALID_ID, INVALID_ID, INVALID_ID};
+  V3 throughput = splat(1.f), contribution = splat(0.f);
+  int depth = 0;
+  bool straightPath = true, firstBounceLight = true;
+  // previous vertex (camera at first)
+  V3 lastP = ray.org, lastNs = ray.dir;
+  float lastPdf = INFINITY;
+  int lastNLS = 0;
+  const int nl = c.p.numLights;
+  for (int guard = 0; guard < 4096; guard++) {
+    HitRec h;
+    const bool hit = traceScene<false, STATS>(c.sc, ray, h, ts);
+    const float t = hit ? h.t : ray.tfar;
+    const V3 wo = -ray.dir;
+    if (depth == 0) out.z = t;
+    if (!hit && straightPath) {
+      out.alpha -= luminance(throughput) * (1.f - c.p.bg[3]);
+      contribution = contribution + throughput * mk(c.p.bg[0], c.p.bg[1], c.p.bg[2]);
+    }
+    // evaluateVirtualLights
+    if (nl > 0) {
+      const V3 d0 = lastP - ray.org;
+      const float lo = sqrtf(fdot(d0, d0));
+      float hi = INFINITY;
+      if (hit) {
+        const V3 d1 = lastP - (ray.org + t * ray.dir);
+        hi = sqrtf(fdot(d1, d1));
+      }
+      const float selPdf = float(lastNLS) / float(nl);
+      for (int i = 0; i < nl; i++) {
+        const LightD &L = c.lights[i];
+        if (straightPath && !L.visible) continue;
+        float lpdf;
+        const V3 rad = evalLight(L, lastP, lastNs, ray.dir, lo, hi, lpdf);
+        if (maxc(rad) > 0.f) {
+          const float w = selPdf != 0.f ? misH(lastPdf, selPdf * lpdf) : 1.f;
+          contribution = contribution + throughput * rad * w;
+        }
+      }
+    }
+    if (!hit) break;
+    if (depth >= c.p.maxPathLength) break;
+    const DG dg = postIntersect(c.sc, ray, h);
+    if (depth == 0) {
+      out.primID = h.primID;
+      out.geomID = h.geomID;
+      out.instID = h.instID;
+    }
+    if (depth >= c.p.maxScatteringEvents) break;
+    const Entry &e = c.sc.entries[h.entry];
+    if (e.materialID >= uint32_t(c.p.numMaterials)) break;  // no material: no BSDF
+    // shading frame from the instance's tangent (makeShadingFrame)
+    V3 U = e.identity ? mk(1.f, 0.f, 0.f) : mk(e.xfm.m[0], e.xfm.m[4], e.xfm.m[8]);
+    U = fnormalize(U);
+    V3 Vv = fcross(dg.Ns, U);
+    V3 fxv, fyv;
+    if (fdot(Vv, Vv) > 0.f) {
+      fyv = fnormalize(Vv);
+      fxv = fcross(fyv, dg.Ns);
+    } else {
+      frame(dg.Ns, fxv, fyv);
+    }
+    Principled bsdf;
+    bsdf.init(c.mats[e.materialID], fxv, fyv, dg.Ns, c.AT);
+    if (bsdf.impSum == 0.f) break;
+    ld.nextGroup();
+    // next event estimation (all lobes are smooth)
+    const int numLS = firstBounceLight ? c.p.nFirst : c.p.nIndirect;
+    for (int i = 0; i < numLS; i++) {
+      float ss;
+      const float2 s = ld.get3LightSamples(uint32_t(i), numLS > 1, ss);
+      int first = 0, len = nl;
+      while (len > 0) {
+        const int half = len >> 1, mid = first + half;
+        if (ss < __ldg(c.lightCdf + mid)) {
+          len = half;
+        } else {
+          first = mid + 1;
+          len -= half + 1;
+        }
+      }
+      first = min(first, nl - 1);
+      const float prob = __ldg(c.lightCdf + first) - (first == 0 ? 0.f : __ldg(c.lightCdf + first - 1));
+      const float selProb = prob * float(numLS);
+      LightSampleD ls = sampleLight(c.lights[first], dg.P, dg.Ng, dg.Ns, s.x, s.y);
+      ls.weight = ls.weight * (1.f / selProb);
+      ls.pdf *= selProb;
+      if (maxc(ls.weight) <= 0.f || ls.pdf <= 0.f) continue;
+      const BsdfEval fe = bsdf.eval(wo, ls.dir, c.AT);
+      if (maxc(fe.value) <= 0.f) continue;
+      V3 org = dg.P;
+      if (fdot(dg.Ng, ls.dir) < 0.f) org = org - (2.f * dg.epsilon) * dg.Ng;
+      Ray sr;
+      sr.org = org;
+      sr.tnear = 0.f;
+      sr.dir = ls.dir;
+      sr.tfar = ls.dist;
+      HitRec sh;
+      if (traceScene<true, STATS>(c.sc, sr, sh, ts)) continue;
+      contribution = contribution + throughput * fe.value * ls.weight * misH(ls.pdf, fe.pdf);
+    }
+    firstBounceLight = false;
+    float ss;
+    uint32_t uu3;
+    const float2 s = ld.getNext4Samples(ss, uu3);
+    BsdfSample fs = bsdf.sample(wo, s.x, s.y, ss, c.AT);
+    if (fdot(fs.wi, dg.Ng) < 0.f) fs.weight = splat(0.f);  // reflection lobes only
+    if (maxc(fs.weight) <= 0.f || fs.pdf <= 0.f) break;
+    throughput = throughput * fs.weight;
+    if (depth >= c.p.roulettePathLength) {
+      const float rr = ld.finalizeDim3(uu3);
+      const float contProb = fminf(maxc(throughput), 0.95f);
+      if (rr > contProb) break;
+      throughput = throughput * (1.f / contProb);
+    }
+    lastP = dg.P;
+    lastNs = dg.Ns;
+    lastPdf = fs.pdf;
+    lastNLS = numLS;
+    if (!(ray.dir.x == fs.wi.x && ray.dir.y == fs.wi.y && ray.dir.z == fs.wi.z)) straightPath = false;
+    ray.org = dg.P;
+    ray.tnear = 0.f;
+    ray.dir = fs.wi;
+    ray.tfar = INFINITY;
+    depth++;
+    if (!(maxc(throughput) > c.p.minContribution)) break;
+  }
+  out.rgb = contribution;
+  if (isnan(contribution.x) || isnan(contribution.y) || isnan(contribution.z)) {
+    out.rgb = splat(0.f);
+    out.alpha = 1.f;
+  }
+  return out;
+}
+
+template <bool STATS>
+__global__ void __launch_bounds__(128) k_render_pt(PtCtx c, CameraD cam, PixelFilterD pf, FrameD fb) {
+  const int x = blockIdx.x * 16 + (threadIdx.x & 15);
+  const int y = blockIdx.y * 8 + (threadIdx.x >> 4);
+  TraceStats ts = {0, 0, 0, 0};
+  if (x < fb.W && y < fb.H) {
+    const float rcpW = fdiv(1.f, float(fb.W)), rcpH = fdiv(1.f, float(fb.H));
+    const uint32_t seed = 0x49c5f37eu ^ uint32_t(fb.W * y + x);
+    PixelOut acc = {0.f, 0.f, 0.f, 0.f, INFINITY, INVALID_ID, INVALID_ID, INVALID_ID};
+    for (int s = 0; s < c.p.spp; s++) {
+      const uint32_t sampleID = uint32_t(fb.frameID) * uint32_t(c.p.spp) + uint32_t(s);
+      LDSampler ld;
+      ld.init(c.T, seed, sampleID, sampleID * uint32_t(c.p.nFirst), 16, 16);
+      uint32_t ss234[3];
+      const float2 ps = ld.getNext5Samples(ss234);
+      const float2 pfs = filterSample(pf, ps.x, ps.y);
+      const float cx = fmul(fadd(float(x), 0.5f), rcpW), cy = fmul(fadd(float(y), 0.5f), rcpH);
+      const Ray ray = cameraRay(cam, fadd(cx, fmul(pfs.x, rcpW)), fadd(cy, fmul(pfs.y, rcpH)));
+      const PathResult r = samplePath<STATS>(c, ld, ray, &ts);
+      acc.r += fminf(r.rgb.x, c.p.maxContribution);
+      acc.g += fminf(r.rgb.y, c.p.maxContribution);
+      acc.b += fminf(r.rgb.z, c.p.maxContribution);
+      acc.a += r.alpha;
+      if (fabsf(r.z) < fabsf(acc.z)) {
+        acc.z = r.z;
+        acc.primID = r.primID;
+        acc.geomID = r.geomID;
+        acc.instID = r.instID;
+      }
+    }
+    const float rspp = 1.f / float(c.p.spp);
+    acc.r *= rspp;
+    acc.g *= rspp;
+    acc.b *= rspp;
+    acc.a *= rspp;
+    fbAccumulate(fb, x, y, acc);
+  }
+  if (STATS) flushStats(c.sc, ts);
+}
+
+// ---------------------------------------------------------------- albedo tables
+// MicrofacetAlbedo_integrate / MicrofacetDielectricReflectionAlbedo_integrate:
+// 32x32 stratified visible-normal samples per entry.
+B200_D float albedoIntegrate(float cosO, float roughness, bool dielectric, float eta) {
+  const float a = fmaxf(sqrf(roughness), 0.001f);
+  cosO = fmaxf(cosO, 1e-6f);
+  const V3 wo = mk(sqrtf(fmaxf(0.f, 1.f - cosO * cosO)), 0.f, cosO);
+  float sum = 0.f;
+  for (int i = 0; i < 32; i++)
+    for (int j = 0; j < 32; j++) {
+      const float sx = fminf((i + 0.5f) / 32.f, 1.f - 1e-6f), sy = fminf((j + 0.5f) / 32.f, 1.f - 1e-6f);
+      float whPdf;
+      const V3 wh = ggxSampleVisible(a, wo, whPdf, sx, sy);
+      const float cosOH = fdot(wo, wh);
+      const V3 wi = reflectV(wo, wh, cosOH);
+      if (wi.z <= 0.f) continue;
+      const float w = ggxG2(a, wo, wi, cosOH, fdot(wi, wh)) * rcpSafe(ggxG1(a, wo, cosOH));
+      sum += dielectric ? fresnelDiel(cosOH, eta) * w : w;
+    }
+  return fminf(sum / 1024.f, 1.f);
+}
+
+__global__ void k_albedo_dir(AlbedoTablesD *T) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < 32 * 32) {
+    T->dir[i] = albedoIntegrate(float(i % 32) / 31.f, float(i / 32) / 31.f, false, 1.f);
+  } else if (i < 32 * 32 + 16 * 16 * 16) {
+    const int k = i - 32 * 32;
+    const float t = float((k / 16) % 16) / 15.f;
+    const float eta = (1.f - t) * (1.f / 3.f) + t * 1.f;
+    T->reflDir[k] = albedoIntegrate(float(k % 16) / 15.f, float(k / 256) / 15.f, true, eta);
+  }
+}
+
+// MicrofacetAlbedoTable_integrateAvg over each table row
+__global__ void k_albedo_avg(AlbedoTablesD *T) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  const float *row;
+  int n;
+  float *out;
+  if (r < 32) {
+    row = T->dir + r * 32;
+    n = 32;
+    out = T->avg + r;
+  } else if (r < 32 + 256) {
+    row = T->reflDir + (r - 32) * 16;
+    n = 16;
+    out = T->reflAvg + (r - 32);
+  } else {
+    return;
+  }
+  float sum = 0.f;
+  for (int i = 0; i < 1025; i++) {
+    const float c = float(i) / 1024.f;
+    sum += interp1(c * (n - 1), row, n) * c * ((i == 0 || i == 1024) ? 0.5f : 1.f);
+  }
+  *out = fminf(2.f * (sum / 1024.f), 1.f);
+}
+
+}  // namespace
+
+cudaError_t computeAlbedoTables(AlbedoTablesD *T, cudaStream_t st) {
+  k_albedo_dir<<<(32 * 32 + 4096 + 127) / 128, 128, 0, st>>>(T);
+  k_albedo_avg<<<(32 + 256 + 127) / 128, 128, 0, st>>>(T);
+  return cudaGetLastError();
+}
+
+cudaError_t launchRenderPT(const SamplerTables *T, const Scene &sc, const CameraD &cam, const PixelFilterD &pf,
+                           const PtParamsD &p, const MaterialD *mats, const LightD *lights, const float *lightCdf,
+                           const AlbedoTablesD *AT, const FrameD &fb, bool stats, cudaStream_t st) {
+  PtCtx c = {T, sc, p, mats, lights, lightCdf, AT};
+  dim3 grid((fb.W + 15) / 16, (fb.H + 7) / 8);
+  if (stats)
+    k_render_pt<true><<<grid, 128, 0, st>>>(c, cam, pf, fb);
+  else
+    k_render_pt<false><<<grid, 128, 0, st>>>(c, cam, pf, fb);
+  return cudaGetLastError();
+}
+
+}  // namespace b200

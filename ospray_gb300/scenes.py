@@ -81,6 +81,43 @@ def ao_heightfield_scene(seed=0, n=256, nspheres=1000):
     return dict(vertex=v, index=i, spheres=s, camera=cam)
 
 
+def pt_instanced_scene(seed=1, count=64, levels=6, width=1920, height=1080):
+    """Path-tracer workload: `count` instances of one displaced sphere
+    (subdivided octahedron, 8*4^levels = 32,768 triangles at levels 6,
+    displaced by 0.05 * value noise of frequency 8) with seeded rotation,
+    scale U(0.5, 2) and position U([0,10]^3), each with its own principled
+    material (baseColor U(0,1)^3, roughness U(0.05,1), metallic 1 with
+    p = 0.2), over a 20x20 two-triangle ground at y = -2.2 (grey 0.8,
+    roughness 1).  Lights: a 2x2 quad of intensity 20 at y = 14 facing down
+    and an ambient light of intensity 0.1 (in that order).  Camera at
+    (5, 9, -13) looking at (5, 3, 5), fovy 50."""
+    v, i = displaced_sphere(levels)
+    xfm, mat = instances(seed, count)
+    ground_v = np.array([[-5, -2.2, -5], [15, -2.2, -5], [-5, -2.2, 15], [15, -2.2, 15]], np.float32)
+    ground_i = np.array([[0, 2, 1], [1, 2, 3]], np.uint32)
+    mats = [tuple(float(x) for x in m) for m in mat] + [(0.8, 0.8, 0.8, 1.0, 0.0)]
+    lights = [dict(type="quad", position=(4.0, 14.0, 4.0), edge1=(2.0, 0.0, 0.0), edge2=(0.0, 0.0, 2.0),
+                   intensity=20.0),
+              dict(type="ambient", intensity=0.1)]
+    cam = dict(position=(5.0, 9.0, -13.0), direction=(0.0, -6.0, 18.0), up=(0.0, 1.0, 0.0), fovy=50.0,
+               aspect=width / height)
+    return dict(vertex=v, index=i, xfm=xfm, materials=mats, ground_vertex=ground_v, ground_index=ground_i,
+                lights=lights, camera=cam, width=width, height=height)
+
+
+def build_pt_scene(scene, data):
+    """Adds the path-tracer workload's geometry to a b200 Scene (or the
+    oracle): instance k < count holds the sphere mesh with material k; the
+    ground is instance `count` with the last material."""
+    gm = scene.add_mesh(data["vertex"], data["index"])
+    for k, x in enumerate(data["xfm"]):
+        scene.add_instance(gm, k, 0, x, k)
+    gg = scene.add_mesh(data["ground_vertex"], data["ground_index"])
+    n = len(data["xfm"])
+    scene.add_instance(gg, n, 0, None, n)
+    scene.commit()
+
+
 def build_ao_scene(scene, data):
     """Adds the AO workload's geometry to a b200 Scene (or the oracle)."""
     gm = scene.add_mesh(data["vertex"], data["index"])

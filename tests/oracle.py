@@ -25,6 +25,60 @@ class OrFrame(ctypes.Structure):
     _fields_ = [("color", P), ("depth", P), ("primID", P), ("geomID", P), ("instID", P)]
 
 
+class OrPtParams(ctypes.Structure):
+    _fields_ = [("spp", I), ("maxPathLength", I), ("roulettePathLength", I), ("maxScatteringEvents", I),
+                ("lightSamples", I), ("limitIndirectLightSamples", I), ("minContribution", F),
+                ("maxContribution", F), ("bg", F * 4), ("pixelFilter", I)]
+
+
+def pt_params(spp=1, max_path_length=20, roulette_path_length=5, max_scattering_events=20, light_samples=-1,
+              limit_indirect=True, min_contribution=0.001, max_contribution=float("inf"), bg=(0, 0, 0, 0),
+              pixel_filter=2):
+    p = OrPtParams()
+    p.spp, p.maxPathLength, p.roulettePathLength = spp, max_path_length, roulette_path_length
+    p.maxScatteringEvents, p.lightSamples, p.limitIndirectLightSamples = max_scattering_events, light_samples, \
+        int(limit_indirect)
+    p.minContribution, p.maxContribution = min_contribution, max_contribution
+    p.bg[:] = list(bg)
+    p.pixelFilter = pixel_filter
+    return p
+
+
+class PtWorld:
+    """Materials and lights of the oracle path tracer."""
+
+    def __init__(self, materials, lights):
+        self.h = lib().or_pt_new()
+        for m in materials:
+            bc = np.asarray(m[:3], np.float32)
+            lib().or_pt_add_material(self.h, _p(bc), float(m[3]), float(m[4]))
+        for L in lights:
+            rad = np.asarray(L.get("color", (1, 1, 1)), np.float32) * np.float32(L["intensity"])
+            if L["type"] == "quad":
+                a = [np.asarray(L[k], np.float32) for k in ("position", "edge1", "edge2")]
+                lib().or_pt_add_quad_light(self.h, _p(a[0]), _p(a[1]), _p(a[2]), _p(rad))
+            else:
+                lib().or_pt_add_ambient_light(self.h, _p(rad))
+
+    def __del__(self):
+        try:
+            lib().or_pt_free(self.h)
+        except Exception:
+            pass
+
+
+def render_pt(scene, world, cam, params, w, h, frames=1, rows=None, nthreads=0):
+    """Returns color (h,w,4), depth (h,w), ids (3,h,w); rows=(y0,y1) renders
+    only those rows (the others stay zero)."""
+    color = np.zeros((h, w, 4), np.float32)
+    depth = np.zeros((h, w), np.float32)
+    ids = np.zeros((3, h, w), np.uint32)
+    y0, y1 = rows if rows else (0, 0)
+    lib().or_render_pt(scene.h, world.h, ctypes.byref(cam), ctypes.byref(params), w, h, frames, y0, y1,
+                       _p(color), _p(depth), _p(ids), nthreads)
+    return dict(color=color, depth=depth, primID=ids[0], geomID=ids[1], instID=ids[2])
+
+
 def build():
     subprocess.run(["make", "-s", "-C", ORACLE_DIR], check=True)
     return LIB
@@ -39,7 +93,16 @@ def lib():
         L.or_scene_free.argtypes = [P]
         L.or_scene_add_mesh.argtypes = [P, P, I, P, I]
         L.or_scene_add_spheres.argtypes = [P, P, I]
-        L.or_scene_add_instance.argtypes = [P, I, U32, U32, P]
+        L.or_scene_add_instance.argtypes = [P, I, U32, U32, P, I]
+        L.or_pt_new.restype = P
+        L.or_pt_free.argtypes = [P]
+        L.or_pt_add_material.argtypes = [P, P, F, F]
+        L.or_pt_add_quad_light.argtypes = [P, P, P, P, P]
+        L.or_pt_add_ambient_light.argtypes = [P, P]
+        L.or_render_pt.argtypes = [P, P, ctypes.POINTER(OrCamera), ctypes.POINTER(OrPtParams), I, I, I, I, I,
+                                   P, P, P, I]
+        L.or_ray_count.restype = ctypes.c_uint64
+        L.or_ray_count.argtypes = [I]
         L.or_scene_commit.argtypes = [P]
         L.or_trace.argtypes = [P, P, I, I, P, P, I]
         L.or_camera_rays.argtypes = [ctypes.POINTER(OrCamera), I, I, I, I, I, P]
@@ -77,7 +140,7 @@ class Scene:
 
     def add_instance(self, geom, inst_id, geom_id, xfm=None, material=-1):
         x = None if xfm is None else np.ascontiguousarray(xfm, np.float32).reshape(12)
-        lib().or_scene_add_instance(self.h, geom, inst_id, geom_id, _p(x))
+        lib().or_scene_add_instance(self.h, geom, inst_id, geom_id, _p(x), material)
 
     def commit(self):
         lib().or_scene_commit(self.h)
