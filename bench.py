@@ -408,7 +408,21 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU-baseline work")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--size", default=None, help="WxH override (profiling small cases; not the bench config)")
+    ap.add_argument("--spp", type=int, default=None, help="spp override (path tracer; profiling only)")
     args = ap.parse_args()
+    if args.size or args.spp:
+        base = WORKLOADS[args.workload]
+        w, h = (int(x) for x in args.size.split("x")) if args.size else (None, None)
+
+        def make(base=base, w=w, h=h, spp=args.spp):
+            kw = {}
+            if w:
+                kw.update(w=w, h=h)
+            if spp and base is PTWorkload:
+                kw.update(spp=spp)
+            return base(**kw)
+        WORKLOADS[args.workload] = make
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

@@ -158,7 +158,7 @@ cudaError_t launchTrace(const Scene &sc, const float4 *rays, long long n, int oc
                         cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
   const int bs = 128;
-  k_trace<<<unsigned((n + bs - 1) / bs), bs, 0, st>>>(sc, rays, n, occlusion, outF, outI);
+  k_trace<<<unsigned((n + bs - 1) / bs), TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(sc, rays, n, occlusion, outF, outI);
   return cudaGetLastError();
 }
 
@@ -166,9 +166,9 @@ cudaError_t launchRenderAO(const SamplerTables *T, const Scene &sc, const Camera
                            const FrameD &fb, bool stats, cudaStream_t st) {
   dim3 grid((fb.W + 15) / 16, (fb.H + 7) / 8);
   if (stats)
-    k_render_ao<true><<<grid, 128, 0, st>>>(T, sc, cam, pf, p, fb);
+    k_render_ao<true><<<grid, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(T, sc, cam, pf, p, fb);
   else
-    k_render_ao<false><<<grid, 128, 0, st>>>(T, sc, cam, pf, p, fb);
+    k_render_ao<false><<<grid, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(T, sc, cam, pf, p, fb);
   return cudaGetLastError();
 }
 

@@ -444,9 +444,9 @@ cudaError_t launchRenderPT(const SamplerTables *T, const Scene &sc, const Camera
   PtCtx c = {T, sc, p, mats, lights, lightCdf, AT};
   dim3 grid((fb.W + 15) / 16, (fb.H + 7) / 8);
   if (stats)
-    k_render_pt<true><<<grid, 128, 0, st>>>(c, cam, pf, fb);
+    k_render_pt<true><<<grid, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(c, cam, pf, fb);
   else
-    k_render_pt<false><<<grid, 128, 0, st>>>(c, cam, pf, fb);
+    k_render_pt<false><<<grid, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(c, cam, pf, fb);
   return cudaGetLastError();
 }
 

@@ -14,7 +14,6 @@
 
 namespace b200 {
 
-constexpr int TRAVERSAL_STACK = 96;
 
 struct HitRec {
   float t, u, v;
@@ -166,19 +165,21 @@ B200_D uint32_t intersectChildren(const NodeView &n, V3 org, V3 rdir, float tnea
   const float sx = __uint_as_float((e & 0xffu) << 23);
   const float sy = __uint_as_float(((e >> 8) & 0xffu) << 23);
   const float sz = __uint_as_float(((e >> 16) & 0xffu) << 23);
-  // per-axis near/far byte offsets from the ray octant
-  const int nx = rdir.x >= 0.f ? 0 : 24, ny = rdir.y >= 0.f ? 0 : 24, nz = rdir.z >= 0.f ? 0 : 24;
+  // near/far planes chosen per axis from the ray octant; every byte index is
+  // a compile-time constant so the node stays in registers
+  const bool xn = rdir.x < 0.f, yn = rdir.y < 0.f, zn = rdir.z < 0.f;
   const float ox = n.px() - org.x, oy = n.py() - org.y, oz = n.pz() - org.z;
   uint32_t mask = 0;
 #pragma unroll
   for (int i = 0; i < 8; i++) {
+    dist[i] = INFINITY;
     if (n.meta(i) == 0) continue;
-    const float qnx = float(n.qbyte(nx + 0 + i)), qfx = float(n.qbyte(24 - nx + 0 + i));
-    const float qny = float(n.qbyte(ny + 8 + i)), qfy = float(n.qbyte(24 - ny + 8 + i));
-    const float qnz = float(n.qbyte(nz + 16 + i)), qfz = float(n.qbyte(24 - nz + 16 + i));
-    const float t0x = fmaf(qnx, sx, ox) * rdir.x, t1x = fmaf(qfx, sx, ox) * rdir.x;
-    const float t0y = fmaf(qny, sy, oy) * rdir.y, t1y = fmaf(qfy, sy, oy) * rdir.y;
-    const float t0z = fmaf(qnz, sz, oz) * rdir.z, t1z = fmaf(qfz, sz, oz) * rdir.z;
+    const float lx = fmaf(float(n.qbyte(0 + i)), sx, ox), hx = fmaf(float(n.qbyte(24 + i)), sx, ox);
+    const float ly = fmaf(float(n.qbyte(8 + i)), sy, oy), hy = fmaf(float(n.qbyte(32 + i)), sy, oy);
+    const float lz = fmaf(float(n.qbyte(16 + i)), sz, oz), hz = fmaf(float(n.qbyte(40 + i)), sz, oz);
+    const float t0x = (xn ? hx : lx) * rdir.x, t1x = (xn ? lx : hx) * rdir.x;
+    const float t0y = (yn ? hy : ly) * rdir.y, t1y = (yn ? ly : hy) * rdir.y;
+    const float t0z = (zn ? hz : lz) * rdir.z, t1z = (zn ? lz : hz) * rdir.z;
     const float t0 = fmaxf(fmaxf(t0x, t0y), fmaxf(t0z, tnear));
     const float t1 = fminf(fminf(t1x, t1y), t1z) * 1.0000004f;
     if (t0 <= fminf(t1, tfar)) {
@@ -189,37 +190,143 @@ B200_D uint32_t intersectChildren(const NodeView &n, V3 org, V3 rdir, float tnea
   return mask;
 }
 
-struct StackEntry {
-  uint32_t node;
-  float dist;
+// a[i] for a runtime i without dynamic indexing (keeps `a` in registers)
+B200_D float pick8(const float (&a)[8], int i) {
+  float r = a[0];
+#pragma unroll
+  for (int k = 1; k < 8; k++) r = (i == k) ? a[k] : r;
+  return r;
+}
+
+// ---------------------------------------------------------------- traversal
+// One stack serves both levels.  Items carry a 2-bit tag in the top bits of
+// the word: TLAS node, BLAS node of the instance being traversed, or an
+// instance (entry index) still to enter.  BLAS items always sit above the
+// TLAS/instance items pushed before their instance was entered, so popping a
+// non-BLAS item means the current instance is finished.
+//
+// The first STACK_SMEM items of each thread live in shared memory, one
+// column per thread (item k of thread t at word k * TRACE_BLOCK + t, so a
+// warp's accesses are conflict-free); deeper items spill to a short local
+// array.  Kernels that trace declare TRACE_SMEM_BYTES of dynamic shared
+// memory and launch TRACE_BLOCK threads per block.
+constexpr int TRACE_BLOCK = 128;
+constexpr int STACK_SMEM = 24;
+constexpr int STACK_LOCAL = 40;
+constexpr size_t TRACE_SMEM_BYTES = size_t(STACK_SMEM) * TRACE_BLOCK * sizeof(uint2);
+
+constexpr uint32_t TAG_TLAS = 0u, TAG_BLAS = 1u << 30, TAG_INST = 2u << 30, TAG_MASK = 3u << 30;
+
+struct TraceStack {
+  uint2 *smem;  // this thread's column
+  uint2 local[STACK_LOCAL];
+  int sp;
+  B200_D bool push(uint32_t item, float dist, uint32_t *status) {
+    if (sp < STACK_SMEM) {
+      smem[sp * TRACE_BLOCK] = make_uint2(item, __float_as_uint(dist));
+    } else if (sp < STACK_SMEM + STACK_LOCAL) {
+      local[sp - STACK_SMEM] = make_uint2(item, __float_as_uint(dist));
+    } else {
+      atomicOr(status, 1u);  // overflow: the item is dropped and reported
+      return false;
+    }
+    sp++;
+    return true;
+  }
+  B200_D uint2 pop() {
+    --sp;
+    return sp < STACK_SMEM ? smem[sp * TRACE_BLOCK] : local[sp - STACK_SMEM];
+  }
 };
 
+// this thread's stack column in the kernel's dynamic shared memory
+B200_D uint2 *traceStackBase() {
+  extern __shared__ uint2 s_traceStack[];
+  return s_traceStack + threadIdx.x;
+}
+
+// Closest hit (ANY = false) or any hit (ANY = true) over the whole scene.
 template <bool ANY, bool STATS = false>
-B200_D bool traverseBLAS(const Entry &e, V3 org, V3 dir, float tnear, HitRec &hit, StackEntry *stack, int cap,
-                         uint32_t entryIdx, uint32_t *status, TraceStats *ts = nullptr) {
-  const V3 rdir = mk(1.f / dir.x, 1.f / dir.y, 1.f / dir.z);
-  const TriPre pre = triPre(dir);
-  int sp = 0;
-  uint32_t node = 0;
+B200_D bool traceScene(const Scene &sc, const Ray &ray, HitRec &hit, TraceStats *ts = nullptr) {
+  hit.t = ray.tfar;
+  hit.u = hit.v = 0.f;
+  hit.primID = hit.geomID = hit.instID = hit.entry = INVALID_ID;
+  if (STATS) ts->rays++;
+  if (sc.ntlas == 0) return false;
+  TraceStack st;
+  st.smem = traceStackBase();
+  st.sp = 0;
+  const V3 wrdir = mk(1.f / ray.dir.x, 1.f / ray.dir.y, 1.f / ray.dir.z);
+  // current traversal frame (world for the TLAS, object space in a BLAS)
+  V3 org = ray.org, dir = ray.dir, rdir = wrdir;
+  TriPre pre;
+  const Node8 *nodes = sc.tlas;
+  bool inBlas = false;
+  const float4 *prims = nullptr;
+  const uint32_t *primIDs = nullptr;
+  uint32_t etype = 0, einst = 0, egeom = 0, eidx = 0;
   bool found = false;
-  bool haveNode = true;
-  // bounded: no ray visits more nodes than this, a stuck traversal gives up
+  uint32_t node = 0;
+  bool have = true;
   for (int guard = 0; guard < (1 << 18); guard++) {
-    if (!haveNode) {
-      if (sp == 0) break;
-      const StackEntry s = stack[--sp];
-      if (s.dist > hit.t) continue;
-      node = s.node;
+    if (!have) {
+      if (st.sp == 0) break;
+      const uint2 s = st.pop();
+      if (__uint_as_float(s.y) > hit.t) continue;
+      const uint32_t tag = s.x & TAG_MASK;
+      if (tag != TAG_BLAS && inBlas) {
+        inBlas = false;
+        nodes = sc.tlas;
+        org = ray.org;
+        dir = ray.dir;
+        rdir = wrdir;
+      }
+      if (tag == TAG_INST) {
+        eidx = s.x & ~TAG_MASK;
+        const Entry &e = sc.entries[eidx];
+        nodes = e.nodes;
+        prims = e.prims;
+        primIDs = e.primIDs;
+        etype = e.type;
+        einst = e.instID;
+        egeom = e.geomID;
+        if (!e.identity) {
+          const Xfm r = e.rcp;
+          org = xfmPoint(r, ray.org);
+          dir = xfmVector(r, ray.dir);
+          rdir = mk(1.f / dir.x, 1.f / dir.y, 1.f / dir.z);
+        }
+        pre = triPre(dir);
+        inBlas = true;
+        node = 0;
+      } else {
+        node = s.x & ~TAG_MASK;
+      }
     }
-    haveNode = false;
-    const NodeView n = loadNode(e.nodes, node);
+    have = false;
+    const NodeView n = loadNode(nodes, node);
     if (STATS) ts->nodes++;
     float dist[8];
-    const uint32_t mask = intersectChildren(n, org, rdir, tnear, hit.t, dist);
+    const uint32_t mask = intersectChildren(n, org, rdir, ray.tnear, hit.t, dist);
     if (!mask) continue;
-    // leaves first: they tighten hit.t before children are ordered
     uint32_t nearest = 0xffffffffu;
     float nearestD = INFINITY;
+    if (!inBlas) {
+      // TLAS node: internal children and instances go on the stack
+      for (uint32_t m = mask; m; m &= m - 1) {
+        const int i = __ffs(m) - 1;
+        const uint32_t meta = n.meta(i);
+        const float di = pick8(dist, i);
+        if (meta & 0x80u) {
+          st.push(TAG_TLAS | (n.childBase() + (meta & 7u)), di, sc.status);
+        } else {
+          const uint32_t cnt = meta >> 5, first = n.primBase() + (meta & 31u);
+          for (uint32_t k = 0; k < cnt; k++) st.push(TAG_INST | __ldg(sc.tlasLeaf + first + k), di, sc.status);
+        }
+      }
+      continue;
+    }
+    // BLAS node: leaves first (they tighten hit.t), then internal children
     for (uint32_t m = mask; m; m &= m - 1) {
       const int i = __ffs(m) - 1;
       const uint32_t meta = n.meta(i);
@@ -231,29 +338,28 @@ B200_D bool traverseBLAS(const Entry &e, V3 org, V3 dir, float tnear, HitRec &hi
         V3 Ng;
         uint32_t prim;
         bool h;
-        if (STATS) (e.type == GEOM_TRIANGLES ? ts->tris : ts->spheres)++;
-        if (e.type == GEOM_TRIANGLES) {
-          const float4 a = __ldg(e.prims + 3 * slot), b = __ldg(e.prims + 3 * slot + 1),
-                       c = __ldg(e.prims + 3 * slot + 2);
+        if (STATS) (etype == GEOM_TRIANGLES ? ts->tris : ts->spheres)++;
+        if (etype == GEOM_TRIANGLES) {
+          const float4 a = __ldg(prims + 3 * slot), b = __ldg(prims + 3 * slot + 1), c = __ldg(prims + 3 * slot + 2);
           const V3 v0 = mk(a.x, a.y, a.z), v1 = mk(b.x, b.y, b.z), v2 = mk(c.x, c.y, c.z);
-          h = triTest(pre, org, tnear, hit.t, v0, v1, v2, t, u, v);
+          h = triTest(pre, org, ray.tnear, hit.t, v0, v1, v2, t, u, v);
           if (h) Ng = cross(sub(v1, v0), sub(v2, v0));
           prim = __float_as_uint(a.w);
         } else {
-          h = sphTest(org, dir, tnear, hit.t, __ldg(e.prims + slot), t, Ng);
-          prim = __ldg(e.primIDs + slot);
+          h = sphTest(org, dir, ray.tnear, hit.t, __ldg(prims + slot), t, Ng);
+          prim = __ldg(primIDs + slot);
         }
         if (!h) continue;
         if (ANY) return true;
-        if (better(t, e.instID, e.geomID, prim, hit)) {
+        if (better(t, einst, egeom, prim, hit)) {
           hit.t = t;
           hit.u = u;
           hit.v = v;
           hit.Ng = Ng;
           hit.primID = prim;
-          hit.geomID = e.geomID;
-          hit.instID = e.instID;
-          hit.entry = entryIdx;
+          hit.geomID = egeom;
+          hit.instID = einst;
+          hit.entry = eidx;
           found = true;
         }
       }
@@ -261,77 +367,20 @@ B200_D bool traverseBLAS(const Entry &e, V3 org, V3 dir, float tnear, HitRec &hi
     for (uint32_t m = mask; m; m &= m - 1) {
       const int i = __ffs(m) - 1;
       const uint32_t meta = n.meta(i);
-      if (!(meta & 0x80u)) continue;
-      if (dist[i] > hit.t) continue;
+      const float di = pick8(dist, i);
+      if (!(meta & 0x80u) || di > hit.t) continue;
       const uint32_t child = n.childBase() + (meta & 7u);
-      if (dist[i] < nearestD) {
-        if (nearest != 0xffffffffu) {
-          if (sp < cap)
-            stack[sp++] = {nearest, nearestD};
-          else
-            atomicOr(status, 1u);
-        }
+      if (di < nearestD) {
+        if (nearest != 0xffffffffu) st.push(TAG_BLAS | nearest, nearestD, sc.status);
         nearest = child;
-        nearestD = dist[i];
+        nearestD = di;
       } else {
-        if (sp < cap)
-          stack[sp++] = {child, dist[i]};
-        else
-          atomicOr(status, 1u);
+        st.push(TAG_BLAS | child, di, sc.status);
       }
     }
     if (nearest != 0xffffffffu) {
       node = nearest;
-      haveNode = true;
-    }
-  }
-  return found;
-}
-
-// Closest hit (ANY = false) or any hit (ANY = true) over the whole scene.
-template <bool ANY, bool STATS = false>
-B200_D bool traceScene(const Scene &sc, const Ray &ray, HitRec &hit, TraceStats *ts = nullptr) {
-  hit.t = ray.tfar;
-  hit.u = hit.v = 0.f;
-  hit.primID = hit.geomID = hit.instID = hit.entry = INVALID_ID;
-  if (STATS) ts->rays++;
-  if (sc.ntlas == 0) return false;
-  StackEntry stack[TRAVERSAL_STACK];
-  const V3 rdir = mk(1.f / ray.dir.x, 1.f / ray.dir.y, 1.f / ray.dir.z);
-  int sp = 0;
-  stack[sp++] = {0u, -INFINITY};
-  bool found = false;
-  for (int guard = 0; guard < (1 << 14) && sp > 0; guard++) {
-    const StackEntry s = stack[--sp];
-    if (s.dist > hit.t) continue;
-    const NodeView n = loadNode(sc.tlas, s.node);
-    if (STATS) ts->nodes++;
-    float dist[8];
-    const uint32_t mask = intersectChildren(n, ray.org, rdir, ray.tnear, hit.t, dist);
-    for (uint32_t m = mask; m; m &= m - 1) {
-      const int i = __ffs(m) - 1;
-      const uint32_t meta = n.meta(i);
-      if (meta & 0x80u) {
-        if (sp < TRAVERSAL_STACK)
-          stack[sp++] = {n.childBase() + (meta & 7u), dist[i]};
-        else
-          atomicOr(sc.status, 1u);
-        continue;
-      }
-      const uint32_t cnt = meta >> 5, first = n.primBase() + (meta & 31u);
-      for (uint32_t k = 0; k < cnt; k++) {
-        const uint32_t ei = __ldg(sc.tlasLeaf + first + k);
-        const Entry &e = sc.entries[ei];
-        V3 o = ray.org, d = ray.dir;
-        if (!e.identity) {
-          o = xfmPoint(e.rcp, ray.org);
-          d = xfmVector(e.rcp, ray.dir);
-        }
-        if (traverseBLAS<ANY, STATS>(e, o, d, ray.tnear, hit, stack + sp, TRAVERSAL_STACK - sp, ei, sc.status, ts)) {
-          if (ANY) return true;
-          found = true;
-        }
-      }
+      have = true;
     }
   }
   return found;
