@@ -172,10 +172,8 @@ PathOut samplePath(const Ctx &c, LDSampler &ld, Ray ray) {
       out.instID = dg.instID;
     }
     if (depth >= c.p.maxPathLength || scatteringEvents >= c.p.maxScatteringEvents) break;
-    const InstanceEntry *e = nullptr;
-    for (const auto &en : c.sc.entries)
-      if (en.instID == hit.instID && en.geomID == hit.geomID) e = &en;
-    if (!e || e->material < 0 || size_t(e->material) >= c.mats.size()) break;  // no material: no BSDF
+    const InstanceEntry *e = &c.sc.entries[hit.entry];
+    if (e->material < 0 || size_t(e->material) >= c.mats.size()) break;  // no material: no BSDF
     Principled bsdf;
     bsdf.init(c.mats[e->material], shadingFrame(dg, e->identity ? v3(1, 0, 0) : e->xfm.l.vx));
     if (bsdf.impSum == 0.f) break;

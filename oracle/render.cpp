@@ -127,12 +127,7 @@ DG postIntersect(const Scene &s, const Ray &ray, const Hit &hit) {
   dg.instID = hit.instID;
   dg.P = ray.org + hit.t * ray.dir;
   // find the entry of this (instance, model)
-  const InstanceEntry *e = nullptr;
-  for (const auto &en : s.entries)
-    if (en.instID == hit.instID && en.geomID == hit.geomID) {
-      e = &en;
-      break;
-    }
+  const InstanceEntry *e = &s.entries[hit.entry];
   const Geometry &g = s.geoms[e->geom];
   V3 Ng = hit.Ng, Ns = hit.Ng;
   float eps;

@@ -120,6 +120,7 @@ inline bool better(float t, uint32_t inst, uint32_t geom, uint32_t prim, const H
 }  // namespace
 
 Box Geometry::primBox(uint32_t p) const {
+  if (type == 2) return boxes[p];
   if (type == 0) {
     const V3 a = verts[index[3 * p]], b = verts[index[3 * p + 1]], c = verts[index[3 * p + 2]];
     return {vmin(a, vmin(b, c)), vmax(a, vmax(b, c))};
@@ -243,6 +244,10 @@ void Scene::commit() {
     wb.hi = wb.hi + pad;
     e.worldBox = wb;
   }
+  tlas = Geometry();
+  tlas.type = 2;
+  for (const auto &e : entries) tlas.boxes.push_back(e.worldBox);
+  tlas.build();
 }
 
 namespace {
@@ -299,18 +304,35 @@ template <bool ANY>
 bool traverse(const Scene &s, const Ray &ray, Hit &hit) {
   hit.t = ray.tfar;
   hit.primID = hit.geomID = hit.instID = INVALID_ID;
+  hit.entry = INVALID_ID;
   const V3 rdir = {1.f / ray.dir.x, 1.f / ray.dir.y, 1.f / ray.dir.z};
   bool found = false;
-  for (const auto &e : s.entries) {
-    if (!hitBox(e.worldBox, ray.org, rdir, ray.tnear, hit.t)) continue;
-    V3 o = ray.org, d = ray.dir;
-    if (!e.identity) {
-      o = xfmPoint(e.rcp, ray.org);
-      d = xfmVector(e.rcp.l, ray.dir);
+  if (s.tlas.nodes.empty()) return false;
+  uint32_t stack[128];
+  int sp = 0;
+  stack[sp++] = 0;
+  while (sp) {
+    const Geometry::Node &n = s.tlas.nodes[stack[--sp]];
+    if (!hitBox(n.box, ray.org, rdir, ray.tnear, hit.t)) continue;
+    if (n.left >= 0) {
+      stack[sp++] = uint32_t(n.left);
+      stack[sp++] = uint32_t(n.left + 1);
+      continue;
     }
-    if (traverseBLAS<ANY>(s.geoms[e.geom], o, d, ray.tnear, hit, e.instID, e.geomID)) {
-      if (ANY) return true;
-      found = true;
+    for (uint32_t k = n.first; k < n.first + n.count; k++) {
+      const uint32_t ei = s.tlas.prims[k];
+      const InstanceEntry &e = s.entries[ei];
+      if (!hitBox(e.worldBox, ray.org, rdir, ray.tnear, hit.t)) continue;
+      V3 o = ray.org, d = ray.dir;
+      if (!e.identity) {
+        o = xfmPoint(e.rcp, ray.org);
+        d = xfmVector(e.rcp.l, ray.dir);
+      }
+      if (traverseBLAS<ANY>(s.geoms[e.geom], o, d, ray.tnear, hit, e.instID, e.geomID)) {
+        if (ANY) return true;
+        hit.entry = ei;
+        found = true;
+      }
     }
   }
   return found;

@@ -30,6 +30,7 @@ struct Hit {
   float t, u, v;
   V3 Ng;  // unnormalised geometric normal in object space
   uint32_t primID, geomID, instID;
+  uint32_t entry;  // index of the (instance, model) entry hit
 };
 
 struct Box {
@@ -37,7 +38,8 @@ struct Box {
 };
 
 struct Geometry {
-  int type;  // 0 triangles, 1 spheres
+  int type;  // 0 triangles, 1 spheres, 2 boxes (instance level)
+  std::vector<Box> boxes;
   std::vector<V3> verts;
   std::vector<uint32_t> index;  // 3 per triangle
   std::vector<V4> spheres;      // center, radius
@@ -49,7 +51,9 @@ struct Geometry {
   };
   std::vector<Node> nodes;
   std::vector<uint32_t> prims;
-  uint32_t nprims() const { return type == 0 ? uint32_t(index.size() / 3) : uint32_t(spheres.size()); }
+  uint32_t nprims() const {
+    return type == 0 ? uint32_t(index.size() / 3) : (type == 1 ? uint32_t(spheres.size()) : uint32_t(boxes.size()));
+  }
   Box primBox(uint32_t p) const;
   void build();
 };
@@ -67,6 +71,7 @@ struct InstanceEntry {
 struct Scene {
   std::vector<Geometry> geoms;
   std::vector<InstanceEntry> entries;
+  Geometry tlas;  // type 2: BVH over the entries' world boxes
   void commit();
   // closest hit; returns false on miss
   bool intersect(const Ray &ray, Hit &hit) const;

@@ -115,6 +115,7 @@ DeviceObj::DeviceObj(int cudaDev) : dev(cudaDev) {
   SamplerTables t;
   buildTables(t);
   check(cudaMalloc(&tables, sizeof(SamplerTables)), "cudaMalloc tables");
+  check(cudaMalloc(&work, 64), "cudaMalloc work counter");
   check(cudaMemcpy(tables, &t, sizeof(t), cudaMemcpyHostToDevice), "upload tables");
   for (int type = B200_PF_GAUSS; type <= B200_PF_BLACKMAN_HARRIS; type++) {
     std::vector<float> cx, cy;
@@ -143,6 +144,7 @@ DeviceObj::~DeviceObj() {
   cudaSetDevice(dev);
   cudaStreamSynchronize(stream);
   cudaFree(tables);
+  cudaFree(work);
   if (albedo) cudaFree(albedo);
   for (auto &L : luts) {
     cudaFree(L.cdf_x);
@@ -724,7 +726,7 @@ int b200_render_pt(b200_scene s, const b200_camera_desc *camera, const b200_pt_p
     for (int k = 0; k < 4; k++) d.bg[k] = p->backgroundColor[k];
     check(launchRenderPT(sc->dev->tables, sc->view(), makeCamera(*camera), sc->dev->filter(p->pixelFilter), d,
                          sc->dMaterials, sc->dLights, sc->dLightCdf, sc->dev->albedoTables(), fb->view(),
-                         p->collectStats != 0, st),
+                         p->collectStats != 0, sc->dev->work, st),
           "path tracer launch");
     fb->frameID++;
   });

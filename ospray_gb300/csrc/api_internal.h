@@ -38,6 +38,7 @@ struct DeviceObj {
   SamplerTables *tables = nullptr;
   FilterLUT luts[5];
   AlbedoTablesD *albedo = nullptr;  // computed at the first path-traced frame
+  unsigned int *work = nullptr;     // pixel work counter of the persistent renderers
   explicit DeviceObj(int cudaDev);
   const AlbedoTablesD *albedoTables();
   ~DeviceObj();

@@ -24,7 +24,8 @@ struct PtParamsD {
 cudaError_t computeAlbedoTables(AlbedoTablesD *T, cudaStream_t st);
 cudaError_t launchRenderPT(const SamplerTables *T, const Scene &sc, const CameraD &cam, const PixelFilterD &pf,
                            const PtParamsD &p, const MaterialD *mats, const LightD *lights, const float *lightCdf,
-                           const AlbedoTablesD *AT, const FrameD &fb, bool stats, cudaStream_t st);
+                           const AlbedoTablesD *AT, const FrameD &fb, bool stats, unsigned int *work,
+                           cudaStream_t st);
 
 struct AOParamsD {
   int spp, aoSamples;

@@ -194,179 +194,305 @@ struct PathResult {
   uint32_t primID, geomID, instID;
 };
 
-template <bool STATS>
-B200_D PathResult samplePath(const PtCtx &c, LDSampler &ld, Ray ray, TraceStats *ts) {
-  PathResult out = {splat(0.f), 1.f, INFINITY, INVALID_ID, INVALID_ID, INVALID_ID};
-  V3 throughput = splat(1.f), contribution = splat(0.f);
-  int depth = 0;
-  bool straightPath = true, firstBounceLight = true;
-  // previous vertex (camera at first)
-  V3 lastP = ray.org, lastNs = ray.dir;
-  float lastPdf = INFINITY;
-  int lastNLS = 0;
-  const int nl = c.p.numLights;
-  for (int guard = 0; guard < 4096; guard++) {
-    HitRec h;
-    const bool hit = traceScene<false, STATS>(c.sc, ray, h, ts);
-    const float t = hit ? h.t : ray.tfar;
-    const V3 wo = -ray.dir;
-    if (depth == 0) out.z = t;
-    if (!hit && straightPath) {
-      out.alpha -= luminance(throughput) * (1.f - c.p.bg[3]);
-      contribution = contribution + throughput * mk(c.p.bg[0], c.p.bg[1], c.p.bg[2]);
-    }
-    // evaluateVirtualLights
-    if (nl > 0) {
-      const V3 d0 = lastP - ray.org;
-      const float lo = sqrtf(fdot(d0, d0));
-      float hi = INFINITY;
-      if (hit) {
-        const V3 d1 = lastP - (ray.org + t * ray.dir);
-        hi = sqrtf(fdot(d1, d1));
-      }
-      const float selPdf = float(lastNLS) / float(nl);
-      for (int i = 0; i < nl; i++) {
-        const LightD &L = c.lights[i];
-        if (straightPath && !L.visible) continue;
-        float lpdf;
-        const V3 rad = evalLight(L, lastP, lastNs, ray.dir, lo, hi, lpdf);
-        if (maxc(rad) > 0.f) {
-          const float w = selPdf != 0.f ? misH(lastPdf, selPdf * lpdf) : 1.f;
-          contribution = contribution + throughput * rad * w;
-        }
-      }
-    }
-    if (!hit) break;
-    if (depth >= c.p.maxPathLength) break;
-    const DG dg = postIntersect(c.sc, ray, h);
-    if (depth == 0) {
-      out.primID = h.primID;
-      out.geomID = h.geomID;
-      out.instID = h.instID;
-    }
-    if (depth >= c.p.maxScatteringEvents) break;
-    const Entry &e = c.sc.entries[h.entry];
-    if (e.materialID >= uint32_t(c.p.numMaterials)) break;  // no material: no BSDF
-    // shading frame from the instance's tangent (makeShadingFrame)
-    V3 U = e.identity ? mk(1.f, 0.f, 0.f) : mk(e.xfm.m[0], e.xfm.m[4], e.xfm.m[8]);
-    U = fnormalize(U);
-    V3 Vv = fcross(dg.Ns, U);
-    V3 fxv, fyv;
-    if (fdot(Vv, Vv) > 0.f) {
-      fyv = fnormalize(Vv);
-      fxv = fcross(fyv, dg.Ns);
-    } else {
-      frame(dg.Ns, fxv, fyv);
-    }
-    Principled bsdf;
-    bsdf.init(c.mats[e.materialID], fxv, fyv, dg.Ns, c.AT);
-    if (bsdf.impSum == 0.f) break;
-    ld.nextGroup();
-    // next event estimation (all lobes are smooth)
-    const int numLS = firstBounceLight ? c.p.nFirst : c.p.nIndirect;
-    for (int i = 0; i < numLS; i++) {
-      float ss;
-      const float2 s = ld.get3LightSamples(uint32_t(i), numLS > 1, ss);
-      int first = 0, len = nl;
-      while (len > 0) {
-        const int half = len >> 1, mid = first + half;
-        if (ss < __ldg(c.lightCdf + mid)) {
-          len = half;
-        } else {
-          first = mid + 1;
-          len -= half + 1;
-        }
-      }
-      first = min(first, nl - 1);
-      const float prob = __ldg(c.lightCdf + first) - (first == 0 ? 0.f : __ldg(c.lightCdf + first - 1));
-      const float selProb = prob * float(numLS);
-      LightSampleD ls = sampleLight(c.lights[first], dg.P, dg.Ng, dg.Ns, s.x, s.y);
-      ls.weight = ls.weight * (1.f / selProb);
-      ls.pdf *= selProb;
-      if (maxc(ls.weight) <= 0.f || ls.pdf <= 0.f) continue;
-      const BsdfEval fe = bsdf.eval(wo, ls.dir, c.AT);
-      if (maxc(fe.value) <= 0.f) continue;
-      V3 org = dg.P;
-      if (fdot(dg.Ng, ls.dir) < 0.f) org = org - (2.f * dg.epsilon) * dg.Ng;
-      Ray sr;
-      sr.org = org;
-      sr.tnear = 0.f;
-      sr.dir = ls.dir;
-      sr.tfar = ls.dist;
-      HitRec sh;
-      if (traceScene<true, STATS>(c.sc, sr, sh, ts)) continue;
-      contribution = contribution + throughput * fe.value * ls.weight * misH(ls.pdf, fe.pdf);
-    }
-    firstBounceLight = false;
-    float ss;
-    uint32_t uu3;
-    const float2 s = ld.getNext4Samples(ss, uu3);
-    BsdfSample fs = bsdf.sample(wo, s.x, s.y, ss, c.AT);
-    if (fdot(fs.wi, dg.Ng) < 0.f) fs.weight = splat(0.f);  // reflection lobes only
-    if (maxc(fs.weight) <= 0.f || fs.pdf <= 0.f) break;
-    throughput = throughput * fs.weight;
-    if (depth >= c.p.roulettePathLength) {
-      const float rr = ld.finalizeDim3(uu3);
-      const float contProb = fminf(maxc(throughput), 0.95f);
-      if (rr > contProb) break;
-      throughput = throughput * (1.f / contProb);
-    }
-    lastP = dg.P;
-    lastNs = dg.Ns;
-    lastPdf = fs.pdf;
-    lastNLS = numLS;
-    if (!(ray.dir.x == fs.wi.x && ray.dir.y == fs.wi.y && ray.dir.z == fs.wi.z)) straightPath = false;
-    ray.org = dg.P;
-    ray.tnear = 0.f;
-    ray.dir = fs.wi;
-    ray.tfar = INFINITY;
-    depth++;
-    if (!(maxc(throughput) > c.p.minContribution)) break;
-  }
-  out.rgb = contribution;
-  if (isnan(contribution.x) || isnan(contribution.y) || isnan(contribution.z)) {
-    out.rgb = splat(0.f);
-    out.alpha = 1.f;
-  }
-  return out;
-}
+// Per-thread shadow-ray requests of one NEE step, parked in shared memory
+// (slot k of thread t at [k][t]) so they do not occupy registers while the
+// thread traces them one by one through the common trace call.
+constexpr int MAX_SHADOW = 4;
+struct ShadowSlots {
+  float4 a[MAX_SHADOW][TRACE_BLOCK];  // org.xyz, dist
+  float4 b[MAX_SHADOW][TRACE_BLOCK];  // dir.xyz, contribution.x
+  float2 c[MAX_SHADOW][TRACE_BLOCK];  // contribution.yz
+};
 
+enum Phase : int { PH_NEW_SAMPLE = 0, PH_EXTEND = 1, PH_SHADOW = 2, PH_DONE = 3 };
+
+// Persistent threads: each thread takes a pixel from the work counter, runs
+// its spp samples and accumulates it, then takes the next pixel.  Every loop
+// iteration traces exactly one ray per thread -- an extension ray (closest
+// hit) or a pending shadow ray (any hit) -- through the same call, so the
+// threads of a warp traverse together; shading runs between traces.
 template <bool STATS>
-__global__ void __launch_bounds__(128) k_render_pt(PtCtx c, CameraD cam, PixelFilterD pf, FrameD fb) {
-  const int x = blockIdx.x * 16 + (threadIdx.x & 15);
-  const int y = blockIdx.y * 8 + (threadIdx.x >> 4);
+__global__ void __launch_bounds__(TRACE_BLOCK) k_render_pt(PtCtx c, CameraD cam, PixelFilterD pf, FrameD fb,
+                                                           unsigned int *work) {
+  __shared__ ShadowSlots slots;
   TraceStats ts = {0, 0, 0, 0};
-  if (x < fb.W && y < fb.H) {
-    const float rcpW = fdiv(1.f, float(fb.W)), rcpH = fdiv(1.f, float(fb.H));
-    const uint32_t seed = 0x49c5f37eu ^ uint32_t(fb.W * y + x);
-    PixelOut acc = {0.f, 0.f, 0.f, 0.f, INFINITY, INVALID_ID, INVALID_ID, INVALID_ID};
-    for (int s = 0; s < c.p.spp; s++) {
+  const int npix = fb.W * fb.H;
+  const float rcpW = fdiv(1.f, float(fb.W)), rcpH = fdiv(1.f, float(fb.H));
+  const int nl = c.p.numLights;
+  // pixel state
+  int pix = int(atomicAdd(work, 1u));
+  int x = 0, y = 0, s = 0;
+  uint32_t seed = 0;
+  PixelOut acc;
+  // sample state
+  LDSampler ld;
+  V3 throughput = splat(1.f), contribution = splat(0.f), lastP = splat(0.f), lastNs = splat(0.f);
+  float alpha = 1.f, z = INFINITY, lastPdf = INFINITY;
+  uint32_t prim = INVALID_ID, geom = INVALID_ID, inst = INVALID_ID;
+  int depth = 0, lastNLS = 0;
+  bool straightPath = true, firstBounceLight = true;
+  Ray ray;
+  // pending NEE step and continuation
+  int nShadow = 0, shadowIdx = 0;
+  V3 neeL = splat(0.f);
+  bool hasNext = false;
+  V3 nextDir = splat(0.f);
+  float nextPdf = 0.f;
+  int phase = pix < npix ? PH_NEW_SAMPLE : PH_DONE;
+  if (phase == PH_NEW_SAMPLE) {
+    x = pix % fb.W;
+    y = pix / fb.W;
+    seed = 0x49c5f37eu ^ uint32_t(fb.W * y + x);
+    acc = {0.f, 0.f, 0.f, 0.f, INFINITY, INVALID_ID, INVALID_ID, INVALID_ID};
+  }
+  for (int guard = 0; guard < (1 << 30) && phase != PH_DONE; guard++) {
+    if (phase == PH_NEW_SAMPLE) {
+      if (s == c.p.spp) {
+        const float rspp = 1.f / float(c.p.spp);
+        acc.r *= rspp;
+        acc.g *= rspp;
+        acc.b *= rspp;
+        acc.a *= rspp;
+        fbAccumulate(fb, x, y, acc);
+        pix = int(atomicAdd(work, 1u));
+        if (pix >= npix) {
+          phase = PH_DONE;
+          break;
+        }
+        x = pix % fb.W;
+        y = pix / fb.W;
+        seed = 0x49c5f37eu ^ uint32_t(fb.W * y + x);
+        acc = {0.f, 0.f, 0.f, 0.f, INFINITY, INVALID_ID, INVALID_ID, INVALID_ID};
+        s = 0;
+      }
       const uint32_t sampleID = uint32_t(fb.frameID) * uint32_t(c.p.spp) + uint32_t(s);
-      LDSampler ld;
       ld.init(c.T, seed, sampleID, sampleID * uint32_t(c.p.nFirst), 16, 16);
       uint32_t ss234[3];
       const float2 ps = ld.getNext5Samples(ss234);
       const float2 pfs = filterSample(pf, ps.x, ps.y);
       const float cx = fmul(fadd(float(x), 0.5f), rcpW), cy = fmul(fadd(float(y), 0.5f), rcpH);
-      const Ray ray = cameraRay(cam, fadd(cx, fmul(pfs.x, rcpW)), fadd(cy, fmul(pfs.y, rcpH)));
-      const PathResult r = samplePath<STATS>(c, ld, ray, &ts);
-      acc.r += fminf(r.rgb.x, c.p.maxContribution);
-      acc.g += fminf(r.rgb.y, c.p.maxContribution);
-      acc.b += fminf(r.rgb.z, c.p.maxContribution);
-      acc.a += r.alpha;
-      if (fabsf(r.z) < fabsf(acc.z)) {
-        acc.z = r.z;
-        acc.primID = r.primID;
-        acc.geomID = r.geomID;
-        acc.instID = r.instID;
+      ray = cameraRay(cam, fadd(cx, fmul(pfs.x, rcpW)), fadd(cy, fmul(pfs.y, rcpH)));
+      throughput = splat(1.f);
+      contribution = splat(0.f);
+      alpha = 1.f;
+      z = INFINITY;
+      prim = geom = inst = INVALID_ID;
+      depth = 0;
+      straightPath = firstBounceLight = true;
+      lastP = ray.org;
+      lastNs = ray.dir;
+      lastPdf = INFINITY;
+      lastNLS = 0;
+      phase = PH_EXTEND;
+    }
+    // ---- the one trace of this iteration
+    Ray tr = ray;
+    const bool shadow = phase == PH_SHADOW;
+    if (shadow) {
+      const float4 a = slots.a[shadowIdx][threadIdx.x], b = slots.b[shadowIdx][threadIdx.x];
+      tr.org = mk(a.x, a.y, a.z);
+      tr.tnear = 0.f;
+      tr.dir = mk(b.x, b.y, b.z);
+      tr.tfar = a.w;
+    }
+    HitRec h;
+    const bool hit = traceRay<STATS>(c.sc, tr, h, shadow, &ts);
+    bool endSample = false;
+    if (shadow) {
+      if (!hit) {
+        const float4 b = slots.b[shadowIdx][threadIdx.x];
+        const float2 cc = slots.c[shadowIdx][threadIdx.x];
+        neeL = neeL + mk(b.w, cc.x, cc.y);
+      }
+      if (++shadowIdx < nShadow) continue;
+      contribution = contribution + neeL;
+      // continue the path (or end it) now that the NEE step is complete
+      if (!hasNext) {
+        endSample = true;
+      } else {
+        ray.org = lastP;
+        ray.tnear = 0.f;
+        ray.dir = nextDir;
+        ray.tfar = INFINITY;
+        lastPdf = nextPdf;
+        depth++;
+        if (maxc(throughput) > c.p.minContribution)
+          phase = PH_EXTEND;
+        else
+          endSample = true;
+      }
+    } else {
+      // ---- extension ray result: the body of samplePath's loop
+      const float t = hit ? h.t : ray.tfar;
+      const V3 wo = -ray.dir;
+      if (depth == 0) z = t;
+      if (!hit && straightPath) {
+        alpha -= luminance(throughput) * (1.f - c.p.bg[3]);
+        contribution = contribution + throughput * mk(c.p.bg[0], c.p.bg[1], c.p.bg[2]);
+      }
+      if (nl > 0) {  // evaluateVirtualLights
+        const V3 d0 = lastP - ray.org;
+        const float lo = sqrtf(fdot(d0, d0));
+        float hiD = INFINITY;
+        if (hit) {
+          const V3 d1 = lastP - (ray.org + t * ray.dir);
+          hiD = sqrtf(fdot(d1, d1));
+        }
+        const float selPdf = float(lastNLS) / float(nl);
+        for (int i = 0; i < nl; i++) {
+          const LightD &L = c.lights[i];
+          if (straightPath && !L.visible) continue;
+          float lpdf;
+          const V3 rad = evalLight(L, lastP, lastNs, ray.dir, lo, hiD, lpdf);
+          if (maxc(rad) > 0.f) {
+            const float w = selPdf != 0.f ? misH(lastPdf, selPdf * lpdf) : 1.f;
+            contribution = contribution + throughput * rad * w;
+          }
+        }
+      }
+      if (!hit || depth >= c.p.maxPathLength) {
+        endSample = true;
+      } else {
+        const DG dg = postIntersect(c.sc, ray, h);
+        if (depth == 0) {
+          prim = h.primID;
+          geom = h.geomID;
+          inst = h.instID;
+        }
+        const Entry &e = c.sc.entries[h.entry];
+        if (depth >= c.p.maxScatteringEvents || e.materialID >= uint32_t(c.p.numMaterials)) {
+          endSample = true;
+        } else {
+          // shading frame from the instance tangent (makeShadingFrame)
+          V3 U = e.identity ? mk(1.f, 0.f, 0.f) : mk(e.xfm.m[0], e.xfm.m[4], e.xfm.m[8]);
+          U = fnormalize(U);
+          const V3 Vv = fcross(dg.Ns, U);
+          V3 fxv, fyv;
+          if (fdot(Vv, Vv) > 0.f) {
+            fyv = fnormalize(Vv);
+            fxv = fcross(fyv, dg.Ns);
+          } else {
+            frame(dg.Ns, fxv, fyv);
+          }
+          Principled bsdf;
+          bsdf.init(c.mats[e.materialID], fxv, fyv, dg.Ns, c.AT);
+          if (bsdf.impSum == 0.f) {
+            endSample = true;
+          } else {
+            ld.nextGroup();
+            // next event estimation: light samples now, shadow rays next
+            const int numLS = firstBounceLight ? c.p.nFirst : c.p.nIndirect;
+            nShadow = 0;
+            neeL = splat(0.f);
+            for (int i = 0; i < numLS; i++) {
+              float ss;
+              const float2 sl = ld.get3LightSamples(uint32_t(i), numLS > 1, ss);
+              int first = 0, len = nl;
+              while (len > 0) {
+                const int half = len >> 1, mid = first + half;
+                if (ss < __ldg(c.lightCdf + mid)) {
+                  len = half;
+                } else {
+                  first = mid + 1;
+                  len -= half + 1;
+                }
+              }
+              first = min(first, nl - 1);
+              const float prob = __ldg(c.lightCdf + first) - (first == 0 ? 0.f : __ldg(c.lightCdf + first - 1));
+              const float selProb = prob * float(numLS);
+              LightSampleD ls = sampleLight(c.lights[first], dg.P, dg.Ng, dg.Ns, sl.x, sl.y);
+              ls.weight = ls.weight * (1.f / selProb);
+              ls.pdf *= selProb;
+              if (maxc(ls.weight) <= 0.f || ls.pdf <= 0.f) continue;
+              const BsdfEval fe = bsdf.eval(wo, ls.dir, c.AT);
+              if (maxc(fe.value) <= 0.f) continue;
+              V3 org = dg.P;
+              if (fdot(dg.Ng, ls.dir) < 0.f) org = org - (2.f * dg.epsilon) * dg.Ng;
+              const V3 cval = throughput * fe.value * ls.weight * misH(ls.pdf, fe.pdf);
+              if (nShadow < MAX_SHADOW) {
+                slots.a[nShadow][threadIdx.x] = make_float4(org.x, org.y, org.z, ls.dist);
+                slots.b[nShadow][threadIdx.x] = make_float4(ls.dir.x, ls.dir.y, ls.dir.z, cval.x);
+                slots.c[nShadow][threadIdx.x] = make_float2(cval.y, cval.z);
+                nShadow++;
+              } else {
+                // more light samples than slots: trace this one in place
+                Ray sr;
+                sr.org = org;
+                sr.tnear = 0.f;
+                sr.dir = ls.dir;
+                sr.tfar = ls.dist;
+                HitRec sh;
+                if (!traceRay<STATS>(c.sc, sr, sh, true, &ts)) neeL = neeL + cval;
+              }
+            }
+            firstBounceLight = false;
+            lastNLS = numLS;
+            // continuation: BSDF sample and Russian roulette
+            float ss;
+            uint32_t uu3;
+            const float2 sb = ld.getNext4Samples(ss, uu3);
+            BsdfSample fs = bsdf.sample(wo, sb.x, sb.y, ss, c.AT);
+            if (fdot(fs.wi, dg.Ng) < 0.f) fs.weight = splat(0.f);  // reflection lobes only
+            hasNext = !(maxc(fs.weight) <= 0.f || fs.pdf <= 0.f);
+            if (hasNext) {
+              throughput = throughput * fs.weight;
+              if (depth >= c.p.roulettePathLength) {
+                const float rr = ld.finalizeDim3(uu3);
+                const float contProb = fminf(maxc(throughput), 0.95f);
+                if (rr > contProb)
+                  hasNext = false;
+                else
+                  throughput = throughput * (1.f / contProb);
+              }
+            }
+            if (hasNext) {
+              if (!(ray.dir.x == fs.wi.x && ray.dir.y == fs.wi.y && ray.dir.z == fs.wi.z)) straightPath = false;
+              nextDir = fs.wi;
+              nextPdf = fs.pdf;
+              lastP = dg.P;
+              lastNs = dg.Ns;
+            }
+            if (nShadow > 0) {
+              shadowIdx = 0;
+              phase = PH_SHADOW;
+            } else {
+              contribution = contribution + neeL;
+              if (!hasNext) {
+                endSample = true;
+              } else {
+                ray.org = lastP;
+                ray.tnear = 0.f;
+                ray.dir = nextDir;
+                ray.tfar = INFINITY;
+                lastPdf = nextPdf;
+                depth++;
+                if (!(maxc(throughput) > c.p.minContribution)) endSample = true;
+              }
+            }
+          }
+        }
       }
     }
-    const float rspp = 1.f / float(c.p.spp);
-    acc.r *= rspp;
-    acc.g *= rspp;
-    acc.b *= rspp;
-    acc.a *= rspp;
-    fbAccumulate(fb, x, y, acc);
+    if (endSample) {
+      V3 rgb = contribution;
+      float a = alpha;
+      if (isnan(rgb.x) || isnan(rgb.y) || isnan(rgb.z)) {
+        rgb = splat(0.f);
+        a = 1.f;
+      }
+      acc.r += fminf(rgb.x, c.p.maxContribution);
+      acc.g += fminf(rgb.y, c.p.maxContribution);
+      acc.b += fminf(rgb.z, c.p.maxContribution);
+      acc.a += a;
+      if (fabsf(z) < fabsf(acc.z)) {
+        acc.z = z;
+        acc.primID = prim;
+        acc.geomID = geom;
+        acc.instID = inst;
+      }
+      s++;
+      phase = PH_NEW_SAMPLE;
+    }
   }
   if (STATS) flushStats(c.sc, ts);
 }
@@ -440,13 +566,28 @@ cudaError_t computeAlbedoTables(AlbedoTablesD *T, cudaStream_t st) {
 
 cudaError_t launchRenderPT(const SamplerTables *T, const Scene &sc, const CameraD &cam, const PixelFilterD &pf,
                            const PtParamsD &p, const MaterialD *mats, const LightD *lights, const float *lightCdf,
-                           const AlbedoTablesD *AT, const FrameD &fb, bool stats, cudaStream_t st) {
+                           const AlbedoTablesD *AT, const FrameD &fb, bool stats, unsigned int *work,
+                           cudaStream_t st) {
   PtCtx c = {T, sc, p, mats, lights, lightCdf, AT};
-  dim3 grid((fb.W + 15) / 16, (fb.H + 7) / 8);
+  // persistent grid: as many blocks as fit on the device at once
+  static int blocksPerSM[2] = {0, 0}, numSMs = 0;
+  if (!numSMs) {
+    int dev;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&numSMs, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocksPerSM[0], k_render_pt<false>, TRACE_BLOCK,
+                                                  TRACE_SMEM_BYTES);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocksPerSM[1], k_render_pt<true>, TRACE_BLOCK, TRACE_SMEM_BYTES);
+  }
+  const int npix = fb.W * fb.H;
+  const int maxBlocks = (npix + TRACE_BLOCK - 1) / TRACE_BLOCK;
+  const int blocks = std::max(1, std::min(maxBlocks, numSMs * std::max(1, blocksPerSM[stats ? 1 : 0])));
+  cudaError_t err = cudaMemsetAsync(work, 0, sizeof(unsigned int), st);
+  if (err != cudaSuccess) return err;
   if (stats)
-    k_render_pt<true><<<grid, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(c, cam, pf, fb);
+    k_render_pt<true><<<blocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(c, cam, pf, fb, work);
   else
-    k_render_pt<false><<<grid, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(c, cam, pf, fb);
+    k_render_pt<false><<<blocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(c, cam, pf, fb, work);
   return cudaGetLastError();
 }
 

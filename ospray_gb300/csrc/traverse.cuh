@@ -246,8 +246,10 @@ B200_D uint2 *traceStackBase() {
 }
 
 // Closest hit (ANY = false) or any hit (ANY = true) over the whole scene.
-template <bool ANY, bool STATS = false>
-B200_D bool traceScene(const Scene &sc, const Ray &ray, HitRec &hit, TraceStats *ts = nullptr) {
+// anyHit selects occlusion (stop at the first hit) at run time, so a kernel
+// that traces both kinds of rays needs a single copy of the traversal code.
+template <bool STATS = false>
+B200_D bool traceRay(const Scene &sc, const Ray &ray, HitRec &hit, bool anyHit, TraceStats *ts = nullptr) {
   hit.t = ray.tfar;
   hit.u = hit.v = 0.f;
   hit.primID = hit.geomID = hit.instID = hit.entry = INVALID_ID;
@@ -350,7 +352,7 @@ B200_D bool traceScene(const Scene &sc, const Ray &ray, HitRec &hit, TraceStats 
           prim = __ldg(primIDs + slot);
         }
         if (!h) continue;
-        if (ANY) return true;
+        if (anyHit) return true;
         if (better(t, einst, egeom, prim, hit)) {
           hit.t = t;
           hit.u = u;
@@ -384,6 +386,12 @@ B200_D bool traceScene(const Scene &sc, const Ray &ray, HitRec &hit, TraceStats 
     }
   }
   return found;
+}
+
+// Closest hit (ANY = false) or any hit (ANY = true).
+template <bool ANY, bool STATS = false>
+B200_D bool traceScene(const Scene &sc, const Ray &ray, HitRec &hit, TraceStats *ts = nullptr) {
+  return traceRay<STATS>(sc, ray, hit, ANY, ts);
 }
 
 }  // namespace b200
