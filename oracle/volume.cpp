@@ -1,0 +1,340 @@
+// Oracle (test infrastructure only): SciVis volume rendering of one
+// structured-regular volume through a piecewise-linear transfer function.
+//   SciVis_renderSample              render/scivis/SciVis.ispc:24-222
+//   integrateVolumeIntervalsGradient render/scivis/volumes.ispc:302-439
+//     (the single-volume variant; gradient shading off, its default)
+//   LinearTransferFunction_get       volume/transferFunction/LinearTransferFunction.ispc:11-43
+//   value ranges / max opacity       volume/transferFunction/LinearTransferFunction.cpp:40-155
+// Volume sampling and interval iteration are Open VKL 2.0.1 (not vendored).
+// They are restated with this project's definitions, shared with the CUDA
+// renderer: vertex-centred trilinear sampling of the grid, NaN outside it;
+// intervals are the maximal runs of non-empty 16^3-voxel macrocells along
+// the ray (empty: the transfer function's maximum opacity over the cell's
+// value range is 0); nominalDeltaT = the smallest grid spacing.
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "render.h"
+
+namespace orc {
+
+extern thread_local uint64_t tl_rays;
+
+struct Volume {
+  int nx, ny, nz;
+  V3 origin, spacing;
+  std::vector<float> data;
+  static constexpr int CELL = 16;
+  int cx, cy, cz;
+  std::vector<float> cmin, cmax;
+  std::vector<uint8_t> cellEmpty;
+  float at(int i, int j, int k) const { return data[(size_t(k) * ny + j) * nx + i]; }
+  void buildCells() {
+    cx = (nx - 1 + CELL - 1) / CELL;
+    cy = (ny - 1 + CELL - 1) / CELL;
+    cz = (nz - 1 + CELL - 1) / CELL;
+    cx = cx < 1 ? 1 : cx;
+    cy = cy < 1 ? 1 : cy;
+    cz = cz < 1 ? 1 : cz;
+    cmin.assign(size_t(cx) * cy * cz, INFINITY);
+    cmax.assign(size_t(cx) * cy * cz, -INFINITY);
+    for (int c = 0; c < cz; c++)
+      for (int b = 0; b < cy; b++)
+        for (int a = 0; a < cx; a++) {
+          float lo = INFINITY, hi = -INFINITY;
+          for (int k = c * CELL; k <= std::min(nz - 1, (c + 1) * CELL); k++)
+            for (int j = b * CELL; j <= std::min(ny - 1, (b + 1) * CELL); j++)
+              for (int i = a * CELL; i <= std::min(nx - 1, (a + 1) * CELL); i++) {
+                const float v = at(i, j, k);
+                lo = std::fmin(lo, v);
+                hi = std::fmax(hi, v);
+              }
+          const size_t ci = (size_t(c) * cy + b) * cx + a;
+          cmin[ci] = lo;
+          cmax[ci] = hi;
+        }
+  }
+  // vertex-centred trilinear sample at world point p (identity transform)
+  float sample(V3 p) const {
+    const float u = (p.x - origin.x) / spacing.x, v = (p.y - origin.y) / spacing.y, w = (p.z - origin.z) / spacing.z;
+    if (!(u >= 0.f && v >= 0.f && w >= 0.f && u <= float(nx - 1) && v <= float(ny - 1) && w <= float(nz - 1)))
+      return NAN;
+    const int i = std::min(int(u), nx - 2), j = std::min(int(v), ny - 2), k = std::min(int(w), nz - 2);
+    const float fx = u - float(i), fy = v - float(j), fz = w - float(k);
+    const float c00 = lerpf(fx, at(i, j, k), at(i + 1, j, k));
+    const float c10 = lerpf(fx, at(i, j + 1, k), at(i + 1, j + 1, k));
+    const float c01 = lerpf(fx, at(i, j, k + 1), at(i + 1, j, k + 1));
+    const float c11 = lerpf(fx, at(i, j + 1, k + 1), at(i + 1, j + 1, k + 1));
+    return lerpf(fz, lerpf(fy, c00, c10), lerpf(fy, c01, c11));
+  }
+};
+
+struct TransferFunction {
+  std::vector<V3> color;
+  std::vector<float> opacity;
+  float lo, hi;
+  V4 get(float value) const {
+    value = (value - lo) * (1.f / (hi - lo));
+    value = clampf(value, 0.f, 0x1.fffffep-1f);
+    const int maxC = int(color.size()) - 1;
+    const float fc = value * float(maxC);
+    const int ic = int(fc);
+    const V3 col = lerp3(fc - std::floor(fc), color[ic], color[std::min(maxC, ic + 1)]);
+    const int maxO = int(opacity.size()) - 1;
+    const float fo = value * float(maxO);
+    const int io = int(fo);
+    const float op = lerpf(fo - std::floor(fo), opacity[io], opacity[std::min(maxO, io + 1)]);
+    return {col.x, col.y, col.z, op};
+  }
+  // maximum opacity of the piecewise-linear ramp over [a, b]
+  float maxOpacity(float a, float b) const {
+    const int maxO = int(opacity.size()) - 1;
+    float ta = clampf((a - lo) / (hi - lo), 0.f, 1.f) * maxO, tb = clampf((b - lo) / (hi - lo), 0.f, 1.f) * maxO;
+    float m = 0.f;
+    const int ia = int(std::floor(ta)), ib = std::min(maxO, int(std::ceil(tb)));
+    for (int i = ia; i <= ib; i++) m = std::fmax(m, opacity[i]);
+    return m;
+  }
+};
+
+struct VolumeModel {
+  Volume vol;
+  TransferFunction tf;
+  float densityScale = 1.f;
+  void finalize() {
+    vol.buildCells();
+    vol.cellEmpty.resize(vol.cmin.size());
+    for (size_t i = 0; i < vol.cmin.size(); i++)
+      vol.cellEmpty[i] = tf.maxOpacity(vol.cmin[i], vol.cmax[i]) <= 0.f ? 1 : 0;
+  }
+};
+
+// Iterates maximal runs of non-empty macrocells along a ray (3D DDA).
+struct IntervalIter {
+  const Volume *v;
+  V3 uo, ud;       // ray in voxel units
+  float tEnd;      // exit of the grid box
+  float t;         // current position
+  int c[3], step[3];
+  float tMax[3], tDelta[3];
+  bool done;
+  void init(const Volume &vol, V3 org, V3 dir, float t0, float t1) {
+    v = &vol;
+    done = false;
+    uo = {(org.x - vol.origin.x) / vol.spacing.x, (org.y - vol.origin.y) / vol.spacing.y,
+          (org.z - vol.origin.z) / vol.spacing.z};
+    ud = {dir.x / vol.spacing.x, dir.y / vol.spacing.y, dir.z / vol.spacing.z};
+    const float hi[3] = {float(vol.nx - 1), float(vol.ny - 1), float(vol.nz - 1)};
+    const float o[3] = {uo.x, uo.y, uo.z}, d[3] = {ud.x, ud.y, ud.z};
+    float ta = t0, tb = t1;
+    for (int k = 0; k < 3; k++) {
+      const float r = 1.f / d[k];
+      float n = (0.f - o[k]) * r, f = (hi[k] - o[k]) * r;
+      if (n > f) std::swap(n, f);
+      ta = n > ta ? n : ta;
+      tb = f < tb ? f : tb;
+    }
+    if (!(ta < tb)) {
+      done = true;
+      return;
+    }
+    t = ta;
+    tEnd = tb;
+    const int ncell[3] = {vol.cx, vol.cy, vol.cz};
+    for (int k = 0; k < 3; k++) {
+      const float p = o[k] + t * d[k];
+      int ci = int(std::floor(p / Volume::CELL));
+      ci = std::min(std::max(ci, 0), ncell[k] - 1);
+      c[k] = ci;
+      if (d[k] > 0.f) {
+        step[k] = 1;
+        tMax[k] = (float((ci + 1) * Volume::CELL) - o[k]) / d[k];
+        tDelta[k] = float(Volume::CELL) / d[k];
+      } else if (d[k] < 0.f) {
+        step[k] = -1;
+        tMax[k] = (float(ci * Volume::CELL) - o[k]) / d[k];
+        tDelta[k] = -float(Volume::CELL) / d[k];
+      } else {
+        step[k] = 0;
+        tMax[k] = INFINITY;
+        tDelta[k] = INFINITY;
+      }
+    }
+  }
+  bool cellEmpty() const { return v->cellEmpty[(size_t(c[2]) * v->cy + c[1]) * v->cx + c[0]] != 0; }
+  // advance to the next cell; false when leaving the grid
+  bool advance() {
+    int k = 0;
+    if (tMax[1] < tMax[k]) k = 1;
+    if (tMax[2] < tMax[k]) k = 2;
+    t = tMax[k];
+    if (!(t < tEnd)) return false;
+    c[k] += step[k];
+    const int ncell[3] = {v->cx, v->cy, v->cz};
+    if (c[k] < 0 || c[k] >= ncell[k]) return false;
+    tMax[k] += tDelta[k];
+    return true;
+  }
+  bool next(float &lo, float &hi) {
+    if (done) return false;
+    for (int g = 0; g < 1 << 20; g++) {  // skip empty cells
+      if (!cellEmpty()) break;
+      if (!advance()) {
+        done = true;
+        return false;
+      }
+    }
+    lo = t;
+    for (int g = 0; g < 1 << 20; g++) {  // extend through non-empty cells
+      if (!advance()) {
+        done = true;
+        break;
+      }
+      if (cellEmpty()) break;
+    }
+    hi = std::fmin(t, tEnd);
+    if (done) hi = tEnd;
+    return true;
+  }
+};
+
+V4 integrateVolume(const VolumeModel &m, const Ray &ray, float jitter, float samplingRate, float minContribution,
+                   uint64_t &samples) {
+  IntervalIter it;
+  it.init(m.vol, ray.org, ray.dir, ray.tnear, ray.tfar);
+  const float nominalDeltaT = std::fmin(m.vol.spacing.x, std::fmin(m.vol.spacing.y, m.vol.spacing.z));
+  V3 color = v3(0.f);
+  float T = 1.f;
+  float distance = INFINITY, iuDistance = jitter, iuLength = 0.f, step = 0.f;
+  float ilo = 0.f, ihi = INFINITY;
+  for (int g = 0; g < (1 << 24) && T > minContribution; g++) {
+    float emptySpace = 0.f;
+    while (iuDistance > iuLength) {
+      const float prevUpper = ihi;
+      if (it.next(ilo, ihi)) {
+        emptySpace += std::fmax(ilo - prevUpper, 0.f);
+        iuDistance -= iuLength;
+        step = nominalDeltaT / samplingRate;
+        iuLength = (ihi - ilo) / step;
+        distance = distance == INFINITY ? ilo : distance;
+      } else {
+        return {color.x, color.y, color.z, T};
+      }
+    }
+    const float newDistance = ilo + iuDistance * step;
+    const V3 p = ray.org + newDistance * ray.dir;
+    const float v = m.vol.sample(p);
+    samples++;
+    if (!std::isnan(v)) {
+      V4 c = m.tf.get(v);
+      const float dt = newDistance - distance - emptySpace;
+      c.w = std::exp(-c.w * dt * m.densityScale);
+      color = color + (T * (1.f - c.w)) * v3(c.x, c.y, c.z);
+      T *= c.w;
+    }
+    iuDistance += 1.f;
+    distance = newDistance;
+  }
+  return {color.x, color.y, color.z, T};
+}
+
+}  // namespace orc
+
+using namespace orc;
+
+std::atomic<uint64_t> g_volSamples{0};
+
+extern "C" {
+
+void *or_volume_new(const float *data, int nx, int ny, int nz, const float *origin, const float *spacing,
+                    const float *colors, int ncolors, const float *opacity, int nopacity, float vlo, float vhi,
+                    float densityScale) {
+  VolumeModel *m = new VolumeModel();
+  m->vol.nx = nx;
+  m->vol.ny = ny;
+  m->vol.nz = nz;
+  m->vol.origin = {origin[0], origin[1], origin[2]};
+  m->vol.spacing = {spacing[0], spacing[1], spacing[2]};
+  m->vol.data.assign(data, data + size_t(nx) * ny * nz);
+  for (int i = 0; i < ncolors; i++) m->tf.color.push_back({colors[3 * i], colors[3 * i + 1], colors[3 * i + 2]});
+  m->tf.opacity.assign(opacity, opacity + nopacity);
+  m->tf.lo = vlo;
+  m->tf.hi = vhi;
+  m->densityScale = densityScale;
+  m->finalize();
+  return m;
+}
+
+void or_volume_free(void *m) { delete static_cast<VolumeModel *>(m); }
+
+uint64_t or_volume_sample_count(int reset) {
+  const uint64_t n = g_volSamples.load();
+  if (reset) g_volSamples.store(0);
+  return n;
+}
+
+struct OrCameraV {
+  float pos[3], dir[3], up[3];
+  float fovy, aspect, nearClip;
+};
+
+// SciVis frames of a volume-only world; rows [y0, y1) (y1 <= 0: all)
+void or_render_scivis_volume(void *mp, const OrCameraV *c, int pixelFilter, int W, int H, int spp, float samplingRate,
+                             const float *bg, int frames, int y0, int y1, float *color, int nthreads) {
+  const VolumeModel &m = *static_cast<VolumeModel *>(mp);
+  const Camera cam = makeCamera({c->pos[0], c->pos[1], c->pos[2]}, {c->dir[0], c->dir[1], c->dir[2]},
+                                {c->up[0], c->up[1], c->up[2]}, c->fovy, c->aspect, c->nearClip);
+  PixelFilter pf;
+  pf.init(pixelFilter);
+  FrameBuffer fb;
+  fb.resize(W, H);
+  if (y1 <= 0) {
+    y0 = 0;
+    y1 = H;
+  }
+  const V2 rcpSize = {1.f / float(W), 1.f / float(H)};
+  const float minContribution = 0.001f;
+  for (int f = 0; f < frames; f++) {
+    const uint32_t start = uint32_t(fb.frameID * spp + 1);
+    parallelRows(y1 - y0, nthreads, [&](int yy) {
+      const int y = y0 + yy;
+      uint64_t samples = 0;
+      for (int x = 0; x < W; x++) {
+        ScreenSample acc;
+        for (int s = 0; s < spp; s++) {
+          const uint32_t sid = start + s;
+          const V2 ps = {Halton_sample2(sid), CranleyPattersonRotation(Halton_sample3(sid), 1.f / 6.f)};
+          const V2 pfs = pf.sample(ps);
+          const V2 center = {(float(x) + 0.5f) * rcpSize.x, (float(y) + 0.5f) * rcpSize.y};
+          const Ray ray = cameraRay(cam, {center.x + pfs.x * rcpSize.x, center.y + pfs.y * rcpSize.y});
+          RandomSampler rs;
+          rs.init(uint32_t(x + W * y), sid);
+          const float jitter = rs.getFloat();
+          tl_rays++;
+          const V4 vc = integrateVolume(m, ray, jitter, samplingRate, minContribution, samples);
+          V3 out = {vc.x, vc.y, vc.z};
+          float T = vc.w;
+          out = out + T * v3(bg[0], bg[1], bg[2]);
+          T = T * (1.f - bg[3]);
+          ScreenSample smp;
+          smp.rgb = out;
+          smp.alpha = 1.f - (0.212671f * T + 0.715160f * T + 0.072169f * T);
+          smp.z = INFINITY;
+          accumulateScreen(acc, smp);
+        }
+        const float rspp = 1.f / float(spp);
+        acc.rgb = acc.rgb * rspp;
+        acc.alpha *= rspp;
+        fbAccumulate(fb, x, y, acc);
+      }
+      g_volSamples.fetch_add(samples);
+      g_rayCount.fetch_add(tl_rays);
+      tl_rays = 0;
+    });
+    fb.frameID++;
+  }
+  std::memcpy(color, fb.color.data(), size_t(W) * H * 16);
+}
+
+}  // extern "C"

@@ -245,7 +245,11 @@ __global__ void __launch_bounds__(TRACE_BLOCK) k_render_pt(PtCtx c, CameraD cam,
     seed = 0x49c5f37eu ^ uint32_t(fb.W * y + x);
     acc = {0.f, 0.f, 0.f, 0.f, INFINITY, INVALID_ID, INVALID_ID, INVALID_ID};
   }
-  for (int guard = 0; guard < (1 << 30) && phase != PH_DONE; guard++) {
+  // warp-uniform loop: the vote is the reconvergence point of every
+  // iteration; lanes without work left idle (and trace nothing) until the
+  // whole warp is done
+  for (int guard = 0; guard < (1 << 30); guard++) {
+    if (!__any_sync(0xffffffffu, phase != PH_DONE)) break;
     if (phase == PH_NEW_SAMPLE) {
       if (s == c.p.spp) {
         const float rspp = 1.f / float(c.p.spp);
@@ -255,16 +259,15 @@ __global__ void __launch_bounds__(TRACE_BLOCK) k_render_pt(PtCtx c, CameraD cam,
         acc.a *= rspp;
         fbAccumulate(fb, x, y, acc);
         pix = int(atomicAdd(work, 1u));
-        if (pix >= npix) {
-          phase = PH_DONE;
-          break;
-        }
+        if (pix >= npix) phase = PH_DONE;
         x = pix % fb.W;
         y = pix / fb.W;
         seed = 0x49c5f37eu ^ uint32_t(fb.W * y + x);
         acc = {0.f, 0.f, 0.f, 0.f, INFINITY, INVALID_ID, INVALID_ID, INVALID_ID};
         s = 0;
       }
+    }
+    if (phase == PH_NEW_SAMPLE) {
       const uint32_t sampleID = uint32_t(fb.frameID) * uint32_t(c.p.spp) + uint32_t(s);
       ld.init(c.T, seed, sampleID, sampleID * uint32_t(c.p.nFirst), 16, 16);
       uint32_t ss234[3];
@@ -296,7 +299,9 @@ __global__ void __launch_bounds__(TRACE_BLOCK) k_render_pt(PtCtx c, CameraD cam,
       tr.tfar = a.w;
     }
     HitRec h;
-    const bool hit = traceRay<STATS>(c.sc, tr, h, shadow, &ts);
+    const bool active = phase != PH_DONE;
+    const bool hit = traceRay<STATS>(c.sc, tr, h, shadow, active, &ts);
+    if (!active) continue;
     bool endSample = false;
     if (shadow) {
       if (!hit) {
@@ -422,7 +427,7 @@ __global__ void __launch_bounds__(TRACE_BLOCK) k_render_pt(PtCtx c, CameraD cam,
                 sr.dir = ls.dir;
                 sr.tfar = ls.dist;
                 HitRec sh;
-                if (!traceRay<STATS>(c.sc, sr, sh, true, &ts)) neeL = neeL + cval;
+                if (!traceRay<STATS>(c.sc, sr, sh, true, true, &ts)) neeL = neeL + cval;
               }
             }
             firstBounceLight = false;

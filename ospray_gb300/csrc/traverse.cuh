@@ -245,16 +245,23 @@ B200_D uint2 *traceStackBase() {
   return s_traceStack + threadIdx.x;
 }
 
-// Closest hit (ANY = false) or any hit (ANY = true) over the whole scene.
-// anyHit selects occlusion (stop at the first hit) at run time, so a kernel
+// Closest hit or any hit over the whole scene.  anyHit selects occlusion (stop at the first hit) at run time, so a kernel
 // that traces both kinds of rays needs a single copy of the traversal code.
+//
+// The lanes that call together trace together: every step of the loop
+// starts with a vote over those lanes, which is also where they reconverge;
+// a lane whose ray is finished idles until the last lane of its group is
+// done.  Without this the lanes of a warp drift to different points of the
+// data-dependent loop and execute one at a time.  `active == false` makes a
+// lane take part without tracing anything.
 template <bool STATS = false>
-B200_D bool traceRay(const Scene &sc, const Ray &ray, HitRec &hit, bool anyHit, TraceStats *ts = nullptr) {
+B200_D bool traceRay(const Scene &sc, const Ray &ray, HitRec &hit, bool anyHit, bool active = true,
+                     TraceStats *ts = nullptr) {
   hit.t = ray.tfar;
   hit.u = hit.v = 0.f;
   hit.primID = hit.geomID = hit.instID = hit.entry = INVALID_ID;
-  if (STATS) ts->rays++;
-  if (sc.ntlas == 0) return false;
+  if (STATS && active) ts->rays++;
+  const unsigned group = __activemask();
   TraceStack st;
   st.smem = traceStackBase();
   st.sp = 0;
@@ -269,10 +276,16 @@ B200_D bool traceRay(const Scene &sc, const Ray &ray, HitRec &hit, bool anyHit, 
   uint32_t etype = 0, einst = 0, egeom = 0, eidx = 0;
   bool found = false;
   uint32_t node = 0;
-  bool have = true;
+  bool have = active && sc.ntlas > 0;
+  bool done = !have;
   for (int guard = 0; guard < (1 << 18); guard++) {
+    if (!__any_sync(group, !done)) break;
+    if (done) continue;
     if (!have) {
-      if (st.sp == 0) break;
+      if (st.sp == 0) {
+        done = true;
+        continue;
+      }
       const uint2 s = st.pop();
       if (__uint_as_float(s.y) > hit.t) continue;
       const uint32_t tag = s.x & TAG_MASK;
@@ -311,8 +324,6 @@ B200_D bool traceRay(const Scene &sc, const Ray &ray, HitRec &hit, bool anyHit, 
     float dist[8];
     const uint32_t mask = intersectChildren(n, org, rdir, ray.tnear, hit.t, dist);
     if (!mask) continue;
-    uint32_t nearest = 0xffffffffu;
-    float nearestD = INFINITY;
     if (!inBlas) {
       // TLAS node: internal children and instances go on the stack
       for (uint32_t m = mask; m; m &= m - 1) {
@@ -351,9 +362,7 @@ B200_D bool traceRay(const Scene &sc, const Ray &ray, HitRec &hit, bool anyHit, 
           h = sphTest(org, dir, ray.tnear, hit.t, __ldg(prims + slot), t, Ng);
           prim = __ldg(primIDs + slot);
         }
-        if (!h) continue;
-        if (anyHit) return true;
-        if (better(t, einst, egeom, prim, hit)) {
+        if (h && better(t, einst, egeom, prim, hit)) {
           hit.t = t;
           hit.u = u;
           hit.v = v;
@@ -366,6 +375,12 @@ B200_D bool traceRay(const Scene &sc, const Ray &ray, HitRec &hit, bool anyHit, 
         }
       }
     }
+    if (anyHit && found) {
+      done = true;
+      continue;
+    }
+    uint32_t nearest = 0xffffffffu;
+    float nearestD = INFINITY;
     for (uint32_t m = mask; m; m &= m - 1) {
       const int i = __ffs(m) - 1;
       const uint32_t meta = n.meta(i);
@@ -391,7 +406,7 @@ B200_D bool traceRay(const Scene &sc, const Ray &ray, HitRec &hit, bool anyHit, 
 // Closest hit (ANY = false) or any hit (ANY = true).
 template <bool ANY, bool STATS = false>
 B200_D bool traceScene(const Scene &sc, const Ray &ray, HitRec &hit, TraceStats *ts = nullptr) {
-  return traceRay<STATS>(sc, ray, hit, ANY, ts);
+  return traceRay<STATS>(sc, ray, hit, ANY, true, ts);
 }
 
 }  // namespace b200
