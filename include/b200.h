@@ -171,6 +171,32 @@ typedef struct {
 int b200_render_pt(b200_scene scene, const b200_camera_desc *camera, const b200_pt_params *params,
                    const b200_material *materials, int nmaterials, b200_frame fb, void *stream);
 
+/* ---- structured-regular volume + piecewise-linear transfer function
+ *      (StructuredRegular volume, volume/Volume.cpp:60-222;
+ *       VolumetricModel::commit volume/VolumetricModel.cpp:30-82;
+ *       LinearTransferFunction::commit volume/transferFunction/LinearTransferFunction.cpp:22-155).
+ * data: nx*ny*nz float, x fastest; vertex-centred grid at origin + i*spacing.
+ * color: ncolor x 3 float, opacity: nopacity float over valueRange.
+ * One volumetric model per world; a second call replaces it. */
+int b200_scene_set_volume(b200_scene scene, const float *data, int nx, int ny, int nz, const float *origin,
+                          const float *spacing, const float *color, int ncolor, const float *opacity, int nopacity,
+                          const float *valueRange, float densityScale);
+
+/* ---- SciVis renderer over a volume-only world (SciVis::commit
+ *      render/scivis/SciVis.cpp:27-84, SciVis_renderSample
+ *      render/scivis/SciVis.ispc:24-222).  Gradient shading is off (the
+ *      volumetric model's default gradientShadingScale 0); with no lights in
+ *      the world, shadows and AO have nothing to act on. */
+typedef struct {
+  int pixelSamples;
+  float volumeSamplingRate; /* default 1 */
+  float backgroundColor[4];
+  int pixelFilter;
+  int collectStats;         /* counters: [rays, volume samples, 0, 0] */
+} b200_scivis_params;
+int b200_render_scivis(b200_scene scene, const b200_camera_desc *camera, const b200_scivis_params *params,
+                       b200_frame fb, void *stream);
+
 /* Traversal counters accumulated by renders with collectStats set:
  * [rays traced, BVH node visits, triangle tests, sphere tests]; reset != 0
  * zeroes them after reading.  (Frame statistics; the reference reports only

@@ -107,6 +107,20 @@ def pt_params(spp=1, max_path_length=20, roulette_path_length=5, max_scattering_
     return p
 
 
+class ScivisParams(ctypes.Structure):
+    _fields_ = [("pixelSamples", ctypes.c_int), ("volumeSamplingRate", ctypes.c_float),
+                ("backgroundColor", ctypes.c_float * 4), ("pixelFilter", ctypes.c_int),
+                ("collectStats", ctypes.c_int)]
+
+
+def scivis_params(spp=1, sampling_rate=1.0, bg=(0, 0, 0, 0), pixel_filter=PF_GAUSS, stats=False):
+    p = ScivisParams()
+    p.pixelSamples, p.volumeSamplingRate = int(spp), float(sampling_rate)
+    p.backgroundColor[:] = list(map(float, bg))
+    p.pixelFilter, p.collectStats = int(pixel_filter), int(bool(stats))
+    return p
+
+
 def lib_path():
     return os.path.join(BUILD, "libb200.so")
 
@@ -144,6 +158,8 @@ def lib():
             "b200_frame_read": (I, [P, U32, P, ctypes.c_size_t]),
             "b200_render_ao": (I, [P, ctypes.POINTER(CameraDesc), ctypes.POINTER(AOParams), P, P]),
             "b200_scene_set_lights": (I, [P, P, I]),
+            "b200_scene_set_volume": (I, [P, P, I, I, I, P, P, P, I, P, I, P, F]),
+            "b200_render_scivis": (I, [P, ctypes.POINTER(CameraDesc), ctypes.POINTER(ScivisParams), P, P]),
             "b200_render_pt": (I, [P, ctypes.POINTER(CameraDesc), ctypes.POINTER(PTParams), P, I, P, P]),
         }
         for name, (res, args) in sig.items():
@@ -225,6 +241,17 @@ class Scene:
 
     def commit(self):
         self.device._check(lib().b200_scene_commit(self._h))
+
+    def set_volume(self, data, origin, spacing, color, opacity, value_range=(0.0, 1.0), density_scale=1.0):
+        """data: (nz, ny, nx) float32 (x fastest); color (n,3); opacity (m,)."""
+        d = np.ascontiguousarray(data, np.float32)
+        nz, ny, nx = d.shape
+        o, sp = np.asarray(origin, np.float32), np.asarray(spacing, np.float32)
+        c = np.ascontiguousarray(color, np.float32).reshape(-1, 3)
+        op = np.ascontiguousarray(opacity, np.float32).reshape(-1)
+        vr = np.asarray(value_range, np.float32)
+        self.device._check(lib().b200_scene_set_volume(self._h, _ptr(d), nx, ny, nz, _ptr(o), _ptr(sp), _ptr(c),
+                                                       len(c), _ptr(op), len(op), _ptr(vr), float(density_scale)))
 
     def set_lights(self, lights):
         arr = (Light * max(1, len(lights)))(*lights)
@@ -331,6 +358,11 @@ def ao_params(spp=1, ao_samples=1, ao_distance=1e20, ao_intensity=1.0, bg=(0, 0,
 def render_ao(scene, camera, params, frame, stream=None):
     scene.device._check(lib().b200_render_ao(scene._h, ctypes.byref(camera), ctypes.byref(params), frame._h,
                                              ctypes.c_void_p(stream) if stream else None))
+
+
+def render_scivis(scene, camera, params, frame, stream=None):
+    scene.device._check(lib().b200_render_scivis(scene._h, ctypes.byref(camera), ctypes.byref(params), frame._h,
+                                                 ctypes.c_void_p(stream) if stream else None))
 
 
 def render_pt(scene, camera, params, materials, frame, stream=None):

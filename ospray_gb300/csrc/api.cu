@@ -146,6 +146,7 @@ DeviceObj::~DeviceObj() {
   cudaFree(tables);
   cudaFree(work);
   if (albedo) cudaFree(albedo);
+  if (ptWs) cudaFree(ptWs);
   for (auto &L : luts) {
     cudaFree(L.cdf_x);
     cudaFree(L.cdf_y);
@@ -227,6 +228,8 @@ SceneObj::~SceneObj() {
   if (dLights) cudaFree(dLights);
   if (dLightCdf) cudaFree(dLightCdf);
   if (dMaterials) cudaFree(dMaterials);
+  for (void *p : {(void *)dVolData, (void *)dTfOpacity, (void *)dTfColor, (void *)dCellEmpty})
+    if (p) cudaFree(p);
   cudaFree(status);
   cudaFree(counters);
   dev->release();
@@ -724,10 +727,95 @@ int b200_render_pt(b200_scene s, const b200_camera_desc *camera, const b200_pt_p
     d.minContribution = p->minContribution;
     d.maxContribution = p->maxContribution;
     for (int k = 0; k < 4; k++) d.bg[k] = p->backgroundColor[k];
-    check(launchRenderPT(sc->dev->tables, sc->view(), makeCamera(*camera), sc->dev->filter(p->pixelFilter), d,
-                         sc->dMaterials, sc->dLights, sc->dLightCdf, sc->dev->albedoTables(), fb->view(),
-                         p->collectStats != 0, sc->dev->work, st),
+    // path workspace: grown on demand, kept for later frames
+    const size_t need = ptWorkspaceBytes((long long)fb->W * fb->H * p->pixelSamples);
+    DeviceObj *dev = sc->dev;
+    if (need > dev->ptWsBytes) {
+      if (dev->ptWs) {
+        check(cudaStreamSynchronize(dev->stream), "sync");
+        cudaFree(dev->ptWs);
+        dev->ptWs = nullptr;
+        dev->ptWsBytes = 0;
+      }
+      check(cudaMalloc(&dev->ptWs, need), "path tracer workspace");
+      dev->ptWsBytes = need;
+    }
+    check(launchRenderPT(dev->tables, sc->view(), makeCamera(*camera), dev->filter(p->pixelFilter), d,
+                         sc->dMaterials, sc->dLights, sc->dLightCdf, dev->albedoTables(), fb->view(),
+                         p->collectStats != 0, dev->ptWs, dev->ptWsBytes, st),
           "path tracer launch");
+    fb->frameID++;
+  });
+}
+
+int b200_scene_set_volume(b200_scene s, const float *data, int nx, int ny, int nz, const float *origin,
+                          const float *spacing, const float *color, int ncolor, const float *opacity, int nopacity,
+                          const float *valueRange, float densityScale) {
+  if (!s) return B200_INVALID_ARGUMENT;
+  SceneObj *sc = reinterpret_cast<SceneObj *>(s);
+  return guarded(sc->dev, [&]() {
+    require(data && origin && spacing && color && opacity && valueRange, "null volume argument");
+    require(nx >= 2 && ny >= 2 && nz >= 2, "volume needs at least 2 vertices per axis");
+    require(ncolor >= 1 && nopacity >= 1, "empty transfer function");
+    require(spacing[0] > 0.f && spacing[1] > 0.f && spacing[2] > 0.f, "bad grid spacing");
+    require(valueRange[1] > valueRange[0], "bad value range");
+    for (void *p : {(void *)sc->dVolData, (void *)sc->dTfOpacity, (void *)sc->dTfColor, (void *)sc->dCellEmpty})
+      if (p) cudaFree(p);
+    sc->dVolData = sc->dTfOpacity = nullptr;
+    sc->dTfColor = nullptr;
+    sc->dCellEmpty = nullptr;
+    sc->hasVolume = false;
+    const size_t nvox = size_t(nx) * ny * nz;
+    cudaStream_t st = sc->dev->stream;
+    check(cudaMalloc(&sc->dVolData, nvox * sizeof(float)), "alloc volume");
+    check(cudaMalloc(&sc->dTfColor, ncolor * sizeof(float3)), "alloc transfer function");
+    check(cudaMalloc(&sc->dTfOpacity, nopacity * sizeof(float)), "alloc transfer function");
+    check(cudaMemcpyAsync(sc->dVolData, data, nvox * sizeof(float), cudaMemcpyHostToDevice, st), "upload volume");
+    check(cudaMemcpyAsync(sc->dTfColor, color, ncolor * sizeof(float3), cudaMemcpyHostToDevice, st), "upload tf");
+    check(cudaMemcpyAsync(sc->dTfOpacity, opacity, nopacity * sizeof(float), cudaMemcpyHostToDevice, st),
+          "upload tf");
+    VolumeD &v = sc->vol;
+    v.data = sc->dVolData;
+    v.nx = nx;
+    v.ny = ny;
+    v.nz = nz;
+    v.origin = mk(origin[0], origin[1], origin[2]);
+    v.spacing = mk(spacing[0], spacing[1], spacing[2]);
+    v.cx = std::max(1, (nx - 1 + 15) / 16);
+    v.cy = std::max(1, (ny - 1 + 15) / 16);
+    v.cz = std::max(1, (nz - 1 + 15) / 16);
+    v.tfColor = sc->dTfColor;
+    v.tfOpacity = sc->dTfOpacity;
+    v.ncolor = ncolor;
+    v.nopacity = nopacity;
+    v.vlo = valueRange[0];
+    v.vhi = valueRange[1];
+    v.densityScale = densityScale;
+    check(cudaMalloc(&sc->dCellEmpty, size_t(v.cx) * v.cy * v.cz), "alloc macrocells");
+    check(buildMacrocells(v, sc->dCellEmpty, st), "macrocells");
+    v.cellEmpty = sc->dCellEmpty;
+    check(cudaStreamSynchronize(st), "volume commit");
+    sc->hasVolume = true;
+  });
+}
+
+int b200_render_scivis(b200_scene s, const b200_camera_desc *camera, const b200_scivis_params *p, b200_frame f,
+                       void *stream) {
+  if (!s || !camera || !p || !f) return B200_INVALID_ARGUMENT;
+  SceneObj *sc = reinterpret_cast<SceneObj *>(s);
+  FrameObj *fb = reinterpret_cast<FrameObj *>(f);
+  return guarded(sc->dev, [&]() {
+    if (!sc->hasVolume) throw Error(B200_INVALID_OPERATION, "world has no volume");
+    require(p->pixelSamples >= 1 && p->volumeSamplingRate > 0.f, "bad scivis parameters");
+    require(p->pixelFilter >= B200_PF_POINT && p->pixelFilter <= B200_PF_BLACKMAN_HARRIS, "bad pixel filter");
+    ScivisParamsD d;
+    d.spp = p->pixelSamples;
+    d.samplingRate = p->volumeSamplingRate;
+    for (int k = 0; k < 4; k++) d.bg[k] = p->backgroundColor[k];
+    cudaStream_t st = stream ? (cudaStream_t)stream : sc->dev->stream;
+    check(launchRenderScivisVolume(sc->dev->tables, sc->view(), sc->vol, makeCamera(*camera),
+                                   sc->dev->filter(p->pixelFilter), d, fb->view(), p->collectStats != 0, st),
+          "scivis launch");
     fb->frameID++;
   });
 }

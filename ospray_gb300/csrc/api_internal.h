@@ -39,6 +39,8 @@ struct DeviceObj {
   FilterLUT luts[5];
   AlbedoTablesD *albedo = nullptr;  // computed at the first path-traced frame
   unsigned int *work = nullptr;     // pixel work counter of the persistent renderers
+  void *ptWs = nullptr;             // path-tracer path/queue workspace
+  size_t ptWsBytes = 0;
   explicit DeviceObj(int cudaDev);
   const AlbedoTablesD *albedoTables();
   ~DeviceObj();
@@ -79,6 +81,12 @@ struct SceneObj {
   int nLights = 0;
   MaterialD *dMaterials = nullptr;
   int nMaterials = 0, capMaterials = 0;
+  // one structured-regular volumetric model (device copies)
+  bool hasVolume = false;
+  VolumeD vol = {};
+  float *dVolData = nullptr, *dTfOpacity = nullptr;
+  float3 *dTfColor = nullptr;
+  uint8_t *dCellEmpty = nullptr;
   std::vector<b200_material> lastMaterials;
   explicit SceneObj(DeviceObj *d);
   ~SceneObj();

@@ -21,11 +21,38 @@ struct PtParamsD {
   float bg[4];
 };
 
+// structured-regular volume (x fastest) with its transfer function and
+// macrocell emptiness grid (16^3-voxel cells)
+struct VolumeD {
+  const float *data;
+  int nx, ny, nz;
+  V3 origin, spacing;
+  int cx, cy, cz;
+  const uint8_t *cellEmpty;
+  const float3 *tfColor;
+  const float *tfOpacity;
+  int ncolor, nopacity;
+  float vlo, vhi, densityScale;
+};
+
+struct ScivisParamsD {
+  int spp;
+  float samplingRate;
+  float bg[4];
+};
+
+cudaError_t buildMacrocells(VolumeD &v, uint8_t *empty, cudaStream_t st);
+cudaError_t launchRenderScivisVolume(const SamplerTables *T, const Scene &sc, const VolumeD &vol, const CameraD &cam,
+                                     const PixelFilterD &pf, const ScivisParamsD &p, const FrameD &fb, bool stats,
+                                     cudaStream_t st);
+
 cudaError_t computeAlbedoTables(AlbedoTablesD *T, cudaStream_t st);
 cudaError_t launchRenderPT(const SamplerTables *T, const Scene &sc, const CameraD &cam, const PixelFilterD &pf,
                            const PtParamsD &p, const MaterialD *mats, const LightD *lights, const float *lightCdf,
-                           const AlbedoTablesD *AT, const FrameD &fb, bool stats, unsigned int *work,
-                           cudaStream_t st);
+                           const AlbedoTablesD *AT, const FrameD &fb, bool stats, void *workspace,
+                           size_t wsBytes, cudaStream_t st);
+// bytes of path-tracer workspace for a frame of npaths = W * H * spp paths
+size_t ptWorkspaceBytes(long long npaths);
 
 struct AOParamsD {
   int spp, aoSamples;

@@ -186,6 +186,7 @@ struct PtCtx {
   const LightD *lights;
   const float *lightCdf;
   const AlbedoTablesD *AT;
+  int frameID;
 };
 
 struct PathResult {
@@ -194,143 +195,206 @@ struct PathResult {
   uint32_t primID, geomID, instID;
 };
 
-// Per-thread shadow-ray requests of one NEE step, parked in shared memory
-// (slot k of thread t at [k][t]) so they do not occupy registers while the
-// thread traces them one by one through the common trace call.
-constexpr int MAX_SHADOW = 4;
-struct ShadowSlots {
-  float4 a[MAX_SHADOW][TRACE_BLOCK];  // org.xyz, dist
-  float4 b[MAX_SHADOW][TRACE_BLOCK];  // dir.xyz, contribution.x
-  float2 c[MAX_SHADOW][TRACE_BLOCK];  // contribution.yz
+// ---------------------------------------------------------------- wavefront path tracer
+// A frame's paths (pixel x sample) live in a workspace of 128-byte records.
+// Each bounce runs three kernels over queues of path indices: a persistent
+// closest-hit trace of the extension rays, a shading kernel (the body of
+// samplePath's loop) that appends shadow rays and continuing paths to new
+// queues, and a persistent any-hit trace of the shadow rays, whose unblocked
+// contributions are added to their paths.  A final kernel averages each
+// pixel's samples into the framebuffer.  Queue lengths stay on the device,
+// so a frame is a fixed sequence of launches (graph-capturable).
+
+struct __align__(16) PathRec {
+  float4 org;   // ray origin, first-hit depth z
+  float4 dir;   // ray direction, last vertex BSDF pdf
+  float4 thr;   // throughput, alpha
+  float4 con;   // contribution, (unused)
+  float4 lastP; // previous vertex position, (unused)
+  float4 lastN; // previous vertex shading normal, (unused)
+  uint4 meta;   // LDSampler scramble, flags, first-hit primID, geomID
+  uint4 meta2;  // first-hit instID, (unused)
+};
+static_assert(sizeof(PathRec) == 128, "PathRec must be 128 bytes");
+
+struct __align__(16) HitBuf {
+  float4 a;  // t, primID bits, entry bits, hit flag
+  float4 b;  // unnormalised object-space Ng
 };
 
-enum Phase : int { PH_NEW_SAMPLE = 0, PH_EXTEND = 1, PH_SHADOW = 2, PH_DONE = 3 };
+struct __align__(16) ShadowRec {
+  float4 a;  // origin, tfar
+  float4 b;  // direction, path index bits
+  float4 c;  // contribution if unblocked, (unused)
+};
 
-// Persistent threads: each thread takes a pixel from the work counter, runs
-// its spp samples and accumulates it, then takes the next pixel.  Every loop
-// iteration traces exactly one ray per thread -- an extension ray (closest
-// hit) or a pending shadow ray (any hit) -- through the same call, so the
-// threads of a warp traverse together; shading runs between traces.
-template <bool STATS>
-__global__ void __launch_bounds__(TRACE_BLOCK) k_render_pt(PtCtx c, CameraD cam, PixelFilterD pf, FrameD fb,
-                                                           unsigned int *work) {
-  __shared__ ShadowSlots slots;
-  TraceStats ts = {0, 0, 0, 0};
-  const int npix = fb.W * fb.H;
-  const float rcpW = fdiv(1.f, float(fb.W)), rcpH = fdiv(1.f, float(fb.H));
-  const int nl = c.p.numLights;
-  // pixel state
-  int pix = int(atomicAdd(work, 1u));
-  int x = 0, y = 0, s = 0;
-  uint32_t seed = 0;
-  PixelOut acc;
-  // sample state
-  LDSampler ld;
-  V3 throughput = splat(1.f), contribution = splat(0.f), lastP = splat(0.f), lastNs = splat(0.f);
-  float alpha = 1.f, z = INFINITY, lastPdf = INFINITY;
-  uint32_t prim = INVALID_ID, geom = INVALID_ID, inst = INVALID_ID;
-  int depth = 0, lastNLS = 0;
-  bool straightPath = true, firstBounceLight = true;
-  Ray ray;
-  // pending NEE step and continuation
-  int nShadow = 0, shadowIdx = 0;
-  V3 neeL = splat(0.f);
-  bool hasNext = false;
-  V3 nextDir = splat(0.f);
-  float nextPdf = 0.f;
-  int phase = pix < npix ? PH_NEW_SAMPLE : PH_DONE;
-  if (phase == PH_NEW_SAMPLE) {
-    x = pix % fb.W;
-    y = pix / fb.W;
-    seed = 0x49c5f37eu ^ uint32_t(fb.W * y + x);
-    acc = {0.f, 0.f, 0.f, 0.f, INFINITY, INVALID_ID, INVALID_ID, INVALID_ID};
+// flags: depth 0..7, straightPath bit 8, firstBounceLight bit 9, ended bit 10,
+// lastNLS 16..31
+constexpr uint32_t F_STRAIGHT = 1u << 8, F_FIRST = 1u << 9, F_ENDED = 1u << 10;
+
+struct Workspace {
+  PathRec *paths;
+  HitBuf *hits;
+  uint32_t *qa, *qb;  // path queues
+  ShadowRec *shadows;
+  uint32_t *counters;  // [0] qa count, [1] qb count, [2] shadow count, [3..5] fetch counters
+};
+
+struct FrameInfo {
+  int W, H, spp, frameID;
+  float rcpW, rcpH;
+  long long npaths;
+};
+
+__global__ void k_pt_generate(PtCtx c, CameraD cam, PixelFilterD pf, FrameInfo fi, Workspace ws) {
+  const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (p == 0) {
+    ws.counters[0] = uint32_t(fi.npaths);
+    for (int k = 1; k < 8; k++) ws.counters[k] = 0;
   }
-  // warp-uniform loop: the vote is the reconvergence point of every
-  // iteration; lanes without work left idle (and trace nothing) until the
-  // whole warp is done
+  if (p >= fi.npaths) return;
+  const int pix = int(p / fi.spp), s = int(p % fi.spp);
+  const int x = pix % fi.W, y = pix / fi.W;
+  const uint32_t seed = 0x49c5f37eu ^ uint32_t(fi.W * y + x);
+  const uint32_t sampleID = uint32_t(fi.frameID) * uint32_t(fi.spp) + uint32_t(s);
+  LDSampler ld;
+  ld.init(c.T, seed, sampleID, sampleID * uint32_t(c.p.nFirst), 16, 16);
+  uint32_t ss234[3];
+  const float2 ps = ld.getNext5Samples(ss234);
+  const float2 pfs = filterSample(pf, ps.x, ps.y);
+  const float cx = fmul(fadd(float(x), 0.5f), fi.rcpW), cy = fmul(fadd(float(y), 0.5f), fi.rcpH);
+  const Ray ray = cameraRay(cam, fadd(cx, fmul(pfs.x, fi.rcpW)), fadd(cy, fmul(pfs.y, fi.rcpH)));
+  PathRec r;
+  r.org = make_float4(ray.org.x, ray.org.y, ray.org.z, INFINITY);
+  r.dir = make_float4(ray.dir.x, ray.dir.y, ray.dir.z, INFINITY);
+  r.thr = make_float4(1.f, 1.f, 1.f, 1.f);
+  r.con = make_float4(0.f, 0.f, 0.f, 0.f);
+  r.lastP = make_float4(ray.org.x, ray.org.y, ray.org.z, 0.f);
+  r.lastN = make_float4(ray.dir.x, ray.dir.y, ray.dir.z, 0.f);
+  r.meta = make_uint4(ld.scramble, F_STRAIGHT | F_FIRST, INVALID_ID, INVALID_ID);
+  r.meta2 = make_uint4(INVALID_ID, 0u, 0u, 0u);
+  ws.paths[p] = r;
+}
+
+// Persistent any/closest-hit tracing over a queue with per-lane dynamic
+// fetch: whenever lanes of a warp finish their rays, the warp takes that many
+// new ones with one atomic, so no lane idles while work remains.
+template <bool SHADOW, bool STATS>
+__global__ void __launch_bounds__(TRACE_BLOCK) k_trace_queue(Scene sc, Workspace ws, const uint32_t *queue,
+                                                            const uint32_t *count, uint32_t *fetch) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t n = *(volatile const uint32_t *)count;
+  TraceStats ts = {0, 0, 0, 0};
+  Traverser tv;
+  bool has = false, exhausted = false;
+  uint32_t item = 0;
   for (int guard = 0; guard < (1 << 30); guard++) {
-    if (!__any_sync(0xffffffffu, phase != PH_DONE)) break;
-    if (phase == PH_NEW_SAMPLE) {
-      if (s == c.p.spp) {
-        const float rspp = 1.f / float(c.p.spp);
-        acc.r *= rspp;
-        acc.g *= rspp;
-        acc.b *= rspp;
-        acc.a *= rspp;
-        fbAccumulate(fb, x, y, acc);
-        pix = int(atomicAdd(work, 1u));
-        if (pix >= npix) phase = PH_DONE;
-        x = pix % fb.W;
-        y = pix / fb.W;
-        seed = 0x49c5f37eu ^ uint32_t(fb.W * y + x);
-        acc = {0.f, 0.f, 0.f, 0.f, INFINITY, INVALID_ID, INVALID_ID, INVALID_ID};
-        s = 0;
+    const unsigned need = __ballot_sync(0xffffffffu, !has && !exhausted);
+    if (need) {
+      const int leader = __ffs(need) - 1;
+      uint32_t base = 0;
+      if (lane == leader) base = atomicAdd(fetch, uint32_t(__popc(need)));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (!has && !exhausted) {
+        const uint32_t idx = base + uint32_t(__popc(need & ((1u << lane) - 1u)));
+        if (idx < n) {
+          Ray r;
+          if (SHADOW) {
+            const ShadowRec s = ws.shadows[idx];
+            r.org = mk(s.a.x, s.a.y, s.a.z);
+            r.tnear = 0.f;
+            r.dir = mk(s.b.x, s.b.y, s.b.z);
+            r.tfar = s.a.w;
+            item = idx;
+          } else {
+            item = queue ? __ldg(queue + idx) : idx;
+            const float4 o = ws.paths[item].org, d = ws.paths[item].dir;
+            r.org = mk(o.x, o.y, o.z);
+            r.tnear = 0.f;
+            r.dir = mk(d.x, d.y, d.z);
+            r.tfar = INFINITY;
+          }
+          tv.init(sc, r, SHADOW);
+          if (STATS) ts.rays++;
+          has = true;
+        } else {
+          exhausted = true;
+        }
       }
     }
-    if (phase == PH_NEW_SAMPLE) {
-      const uint32_t sampleID = uint32_t(fb.frameID) * uint32_t(c.p.spp) + uint32_t(s);
-      ld.init(c.T, seed, sampleID, sampleID * uint32_t(c.p.nFirst), 16, 16);
-      uint32_t ss234[3];
-      const float2 ps = ld.getNext5Samples(ss234);
-      const float2 pfs = filterSample(pf, ps.x, ps.y);
-      const float cx = fmul(fadd(float(x), 0.5f), rcpW), cy = fmul(fadd(float(y), 0.5f), rcpH);
-      ray = cameraRay(cam, fadd(cx, fmul(pfs.x, rcpW)), fadd(cy, fmul(pfs.y, rcpH)));
-      throughput = splat(1.f);
-      contribution = splat(0.f);
-      alpha = 1.f;
-      z = INFINITY;
-      prim = geom = inst = INVALID_ID;
-      depth = 0;
-      straightPath = firstBounceLight = true;
-      lastP = ray.org;
-      lastNs = ray.dir;
-      lastPdf = INFINITY;
-      lastNLS = 0;
-      phase = PH_EXTEND;
-    }
-    // ---- the one trace of this iteration
-    Ray tr = ray;
-    const bool shadow = phase == PH_SHADOW;
-    if (shadow) {
-      const float4 a = slots.a[shadowIdx][threadIdx.x], b = slots.b[shadowIdx][threadIdx.x];
-      tr.org = mk(a.x, a.y, a.z);
-      tr.tnear = 0.f;
-      tr.dir = mk(b.x, b.y, b.z);
-      tr.tfar = a.w;
-    }
-    HitRec h;
-    const bool active = phase != PH_DONE;
-    const bool hit = traceRay<STATS>(c.sc, tr, h, shadow, active, &ts);
-    if (!active) continue;
-    bool endSample = false;
-    if (shadow) {
-      if (!hit) {
-        const float4 b = slots.b[shadowIdx][threadIdx.x];
-        const float2 cc = slots.c[shadowIdx][threadIdx.x];
-        neeL = neeL + mk(b.w, cc.x, cc.y);
-      }
-      if (++shadowIdx < nShadow) continue;
-      contribution = contribution + neeL;
-      // continue the path (or end it) now that the NEE step is complete
-      if (!hasNext) {
-        endSample = true;
+    if (!__any_sync(0xffffffffu, has)) break;
+    if (has && tv.step<STATS>(sc, &ts)) {
+      if (SHADOW) {
+        if (!tv.found) {
+          const ShadowRec s = ws.shadows[item];
+          float *con = &ws.paths[__float_as_uint(s.b.w)].con.x;
+          atomicAdd(con + 0, s.c.x);
+          atomicAdd(con + 1, s.c.y);
+          atomicAdd(con + 2, s.c.z);
+        }
       } else {
-        ray.org = lastP;
-        ray.tnear = 0.f;
-        ray.dir = nextDir;
-        ray.tfar = INFINITY;
-        lastPdf = nextPdf;
-        depth++;
-        if (maxc(throughput) > c.p.minContribution)
-          phase = PH_EXTEND;
-        else
-          endSample = true;
+        HitBuf hb;
+        hb.a = make_float4(tv.hit.t, __uint_as_float(tv.hit.primID), __uint_as_float(tv.hit.entry),
+                           tv.found ? 1.f : 0.f);
+        hb.b = make_float4(tv.hit.Ng.x, tv.hit.Ng.y, tv.hit.Ng.z, 0.f);
+        ws.hits[item] = hb;
       }
-    } else {
-      // ---- extension ray result: the body of samplePath's loop
-      const float t = hit ? h.t : ray.tfar;
+      has = false;
+    }
+  }
+  if (STATS) flushStats(sc, ts);
+}
+
+// appends one entry per lane that wants to, with one atomic per warp
+B200_D uint32_t warpAppend(bool want, uint32_t *counter) {
+  const unsigned m = __ballot_sync(__activemask(), want);
+  if (!m) return 0;
+  const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+  uint32_t base = 0;
+  if (lane == leader) base = atomicAdd(counter, uint32_t(__popc(m)));
+  base = __shfl_sync(__activemask(), base, leader);
+  return base + uint32_t(__popc(m & ((1u << lane) - 1u)));
+}
+
+// One bounce of samplePath for every queued path (render/pathtracer/
+// PathSampler.ispc:109-415): environment and virtual lights, postIntersect,
+// principled BSDF, NEE light samples (to the shadow queue), BSDF sample and
+// Russian roulette (to the next queue).
+__global__ void __launch_bounds__(128) k_pt_shade(PtCtx c, Workspace ws, const uint32_t *qin, const uint32_t *cin,
+                                                  uint32_t *qout, uint32_t *cout, uint32_t *cshadow) {
+  const uint32_t n = *(volatile const uint32_t *)cin;
+  const int nl = c.p.numLights;
+  const uint32_t stride = gridDim.x * blockDim.x;
+  // warp-uniform loop so the appends can use warp votes
+  const uint32_t nround = (n + stride - 1) / stride;
+  for (uint32_t r = 0; r < nround; r++) {
+    const uint32_t qi = r * stride + blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = qi < n;
+    const uint32_t p = valid ? (qin ? __ldg(qin + qi) : qi) : 0u;
+    bool cont = false;
+    // shadow requests of this lane (numLS <= MAX_NEE per bounce in the queue)
+    int nsh = 0;
+    ShadowRec sh[2];
+    if (valid) {
+      PathRec pr = ws.paths[p];
+      const HitBuf hb = ws.hits[p];
+      uint32_t flags = pr.meta.y;
+      int depth = int(flags & 0xffu);
+      bool straightPath = (flags & F_STRAIGHT) != 0, firstBounceLight = (flags & F_FIRST) != 0;
+      int lastNLS = int(flags >> 16);
+      V3 throughput = mk(pr.thr.x, pr.thr.y, pr.thr.z), contribution = mk(pr.con.x, pr.con.y, pr.con.z);
+      float alpha = pr.thr.w;
+      Ray ray;
+      ray.org = mk(pr.org.x, pr.org.y, pr.org.z);
+      ray.tnear = 0.f;
+      ray.dir = mk(pr.dir.x, pr.dir.y, pr.dir.z);
+      ray.tfar = INFINITY;
+      const V3 lastP = mk(pr.lastP.x, pr.lastP.y, pr.lastP.z), lastNs = mk(pr.lastN.x, pr.lastN.y, pr.lastN.z);
+      const float lastPdf = pr.dir.w;
+      const bool hit = hb.a.w != 0.f;
+      const float t = hit ? hb.a.x : INFINITY;
       const V3 wo = -ray.dir;
-      if (depth == 0) z = t;
+      if (depth == 0) pr.org.w = t;
       if (!hit && straightPath) {
         alpha -= luminance(throughput) * (1.f - c.p.bg[3]);
         contribution = contribution + throughput * mk(c.p.bg[0], c.p.bg[1], c.p.bg[2]);
@@ -355,20 +419,22 @@ __global__ void __launch_bounds__(TRACE_BLOCK) k_render_pt(PtCtx c, CameraD cam,
           }
         }
       }
-      if (!hit || depth >= c.p.maxPathLength) {
-        endSample = true;
-      } else {
+      if (hit && depth < c.p.maxPathLength) {
+        HitRec h;
+        h.t = t;
+        h.primID = __float_as_uint(hb.a.y);
+        h.entry = __float_as_uint(hb.a.z);
+        h.Ng = mk(hb.b.x, hb.b.y, hb.b.z);
+        const Entry &e = c.sc.entries[h.entry];
+        h.geomID = e.geomID;
+        h.instID = e.instID;
         const DG dg = postIntersect(c.sc, ray, h);
         if (depth == 0) {
-          prim = h.primID;
-          geom = h.geomID;
-          inst = h.instID;
+          pr.meta.z = h.primID;
+          pr.meta.w = h.geomID;
+          pr.meta2.x = h.instID;
         }
-        const Entry &e = c.sc.entries[h.entry];
-        if (depth >= c.p.maxScatteringEvents || e.materialID >= uint32_t(c.p.numMaterials)) {
-          endSample = true;
-        } else {
-          // shading frame from the instance tangent (makeShadingFrame)
+        if (depth < c.p.maxScatteringEvents && e.materialID < uint32_t(c.p.numMaterials)) {
           V3 U = e.identity ? mk(1.f, 0.f, 0.f) : mk(e.xfm.m[0], e.xfm.m[4], e.xfm.m[8]);
           U = fnormalize(U);
           const V3 Vv = fcross(dg.Ns, U);
@@ -381,14 +447,15 @@ __global__ void __launch_bounds__(TRACE_BLOCK) k_render_pt(PtCtx c, CameraD cam,
           }
           Principled bsdf;
           bsdf.init(c.mats[e.materialID], fxv, fyv, dg.Ns, c.AT);
-          if (bsdf.impSum == 0.f) {
-            endSample = true;
-          } else {
+          if (bsdf.impSum != 0.f) {
+            // LDSampler of this path at its current group
+            const int pix = int(p / uint32_t(c.p.spp)), s = int(p % uint32_t(c.p.spp));
+            const uint32_t sampleID = uint32_t(c.frameID) * uint32_t(c.p.spp) + uint32_t(s);
+            (void)pix;
+            LDSampler ld;
+            ld.init(c.T, pr.meta.x, sampleID, sampleID * uint32_t(c.p.nFirst), 16, 16);
             ld.nextGroup();
-            // next event estimation: light samples now, shadow rays next
             const int numLS = firstBounceLight ? c.p.nFirst : c.p.nIndirect;
-            nShadow = 0;
-            neeL = splat(0.f);
             for (int i = 0; i < numLS; i++) {
               float ss;
               const float2 sl = ld.get3LightSamples(uint32_t(i), numLS > 1, ss);
@@ -414,92 +481,102 @@ __global__ void __launch_bounds__(TRACE_BLOCK) k_render_pt(PtCtx c, CameraD cam,
               V3 org = dg.P;
               if (fdot(dg.Ng, ls.dir) < 0.f) org = org - (2.f * dg.epsilon) * dg.Ng;
               const V3 cval = throughput * fe.value * ls.weight * misH(ls.pdf, fe.pdf);
-              if (nShadow < MAX_SHADOW) {
-                slots.a[nShadow][threadIdx.x] = make_float4(org.x, org.y, org.z, ls.dist);
-                slots.b[nShadow][threadIdx.x] = make_float4(ls.dir.x, ls.dir.y, ls.dir.z, cval.x);
-                slots.c[nShadow][threadIdx.x] = make_float2(cval.y, cval.z);
-                nShadow++;
+              if (nsh < 2) {
+                sh[nsh].a = make_float4(org.x, org.y, org.z, ls.dist);
+                sh[nsh].b = make_float4(ls.dir.x, ls.dir.y, ls.dir.z, __uint_as_float(p));
+                sh[nsh].c = make_float4(cval.x, cval.y, cval.z, 0.f);
+                nsh++;
               } else {
-                // more light samples than slots: trace this one in place
+                // beyond two light samples per vertex: trace in place
                 Ray sr;
                 sr.org = org;
                 sr.tnear = 0.f;
                 sr.dir = ls.dir;
                 sr.tfar = ls.dist;
-                HitRec sh;
-                if (!traceRay<STATS>(c.sc, sr, sh, true, true, &ts)) neeL = neeL + cval;
+                HitRec shh;
+                if (!traceRay<false>(c.sc, sr, shh, true, true, nullptr)) contribution = contribution + cval;
               }
             }
-            firstBounceLight = false;
             lastNLS = numLS;
-            // continuation: BSDF sample and Russian roulette
+            firstBounceLight = false;
             float ss;
             uint32_t uu3;
             const float2 sb = ld.getNext4Samples(ss, uu3);
             BsdfSample fs = bsdf.sample(wo, sb.x, sb.y, ss, c.AT);
             if (fdot(fs.wi, dg.Ng) < 0.f) fs.weight = splat(0.f);  // reflection lobes only
-            hasNext = !(maxc(fs.weight) <= 0.f || fs.pdf <= 0.f);
-            if (hasNext) {
+            cont = !(maxc(fs.weight) <= 0.f || fs.pdf <= 0.f);
+            if (cont) {
               throughput = throughput * fs.weight;
               if (depth >= c.p.roulettePathLength) {
                 const float rr = ld.finalizeDim3(uu3);
                 const float contProb = fminf(maxc(throughput), 0.95f);
                 if (rr > contProb)
-                  hasNext = false;
+                  cont = false;
                 else
                   throughput = throughput * (1.f / contProb);
               }
             }
-            if (hasNext) {
+            if (cont) {
               if (!(ray.dir.x == fs.wi.x && ray.dir.y == fs.wi.y && ray.dir.z == fs.wi.z)) straightPath = false;
-              nextDir = fs.wi;
-              nextPdf = fs.pdf;
-              lastP = dg.P;
-              lastNs = dg.Ns;
+              pr.lastP = make_float4(dg.P.x, dg.P.y, dg.P.z, 0.f);
+              pr.lastN = make_float4(dg.Ns.x, dg.Ns.y, dg.Ns.z, 0.f);
+              pr.org = make_float4(dg.P.x, dg.P.y, dg.P.z, pr.org.w);
+              pr.dir = make_float4(fs.wi.x, fs.wi.y, fs.wi.z, fs.pdf);
+              depth++;
+              if (!(maxc(throughput) > c.p.minContribution)) cont = false;
             }
-            if (nShadow > 0) {
-              shadowIdx = 0;
-              phase = PH_SHADOW;
-            } else {
-              contribution = contribution + neeL;
-              if (!hasNext) {
-                endSample = true;
-              } else {
-                ray.org = lastP;
-                ray.tnear = 0.f;
-                ray.dir = nextDir;
-                ray.tfar = INFINITY;
-                lastPdf = nextPdf;
-                depth++;
-                if (!(maxc(throughput) > c.p.minContribution)) endSample = true;
-              }
-            }
+            pr.meta.x = ld.scramble;
           }
         }
       }
+      pr.thr = make_float4(throughput.x, throughput.y, throughput.z, alpha);
+      pr.con = make_float4(contribution.x, contribution.y, contribution.z, 0.f);
+      pr.meta.y = uint32_t(depth) | (straightPath ? F_STRAIGHT : 0u) | (firstBounceLight ? F_FIRST : 0u) |
+                  (cont ? 0u : F_ENDED) | (uint32_t(lastNLS) << 16);
+      ws.paths[p] = pr;
     }
-    if (endSample) {
-      V3 rgb = contribution;
-      float a = alpha;
-      if (isnan(rgb.x) || isnan(rgb.y) || isnan(rgb.z)) {
-        rgb = splat(0.f);
-        a = 1.f;
-      }
-      acc.r += fminf(rgb.x, c.p.maxContribution);
-      acc.g += fminf(rgb.y, c.p.maxContribution);
-      acc.b += fminf(rgb.z, c.p.maxContribution);
-      acc.a += a;
-      if (fabsf(z) < fabsf(acc.z)) {
-        acc.z = z;
-        acc.primID = prim;
-        acc.geomID = geom;
-        acc.instID = inst;
-      }
-      s++;
-      phase = PH_NEW_SAMPLE;
+    // queue appends (warp-uniform region)
+    const uint32_t oi = warpAppend(cont, cout);
+    if (cont) qout[oi] = p;
+    for (int k = 0; k < 2; k++) {
+      const bool want = k < nsh;
+      const uint32_t si = warpAppend(want, cshadow);
+      if (want) ws.shadows[si] = sh[k];
     }
   }
-  if (STATS) flushStats(c.sc, ts);
+}
+
+// averages each pixel's samples into the framebuffer (ScreenSample_accumulate
+// / normalize, maxContribution clamp, NaN -> 0 with alpha 1)
+__global__ void k_pt_finalize(PtCtx c, Workspace ws, FrameInfo fi, FrameD fb) {
+  const int pix = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pix >= fi.W * fi.H) return;
+  PixelOut acc = {0.f, 0.f, 0.f, 0.f, INFINITY, INVALID_ID, INVALID_ID, INVALID_ID};
+  for (int s = 0; s < fi.spp; s++) {
+    const PathRec &pr = ws.paths[size_t(pix) * fi.spp + s];
+    float r = pr.con.x, g = pr.con.y, b = pr.con.z, a = pr.thr.w;
+    if (isnan(r) || isnan(g) || isnan(b)) {
+      r = g = b = 0.f;
+      a = 1.f;
+    }
+    acc.r += fminf(r, c.p.maxContribution);
+    acc.g += fminf(g, c.p.maxContribution);
+    acc.b += fminf(b, c.p.maxContribution);
+    acc.a += a;
+    const float z = pr.org.w;
+    if (fabsf(z) < fabsf(acc.z)) {
+      acc.z = z;
+      acc.primID = pr.meta.z;
+      acc.geomID = pr.meta.w;
+      acc.instID = pr.meta2.x;
+    }
+  }
+  const float rspp = 1.f / float(fi.spp);
+  acc.r *= rspp;
+  acc.g *= rspp;
+  acc.b *= rspp;
+  acc.a *= rspp;
+  fbAccumulate(fb, pix % fi.W, pix / fi.W, acc);
 }
 
 // ---------------------------------------------------------------- albedo tables
@@ -561,6 +638,21 @@ __global__ void k_albedo_avg(AlbedoTablesD *T) {
   *out = fminf(2.f * (sum / 1024.f), 1.f);
 }
 
+__global__ void k_bounce_reset(uint32_t *counters, int cout) {
+  counters[cout] = 0;
+  counters[2] = 0;
+  counters[3] = 0;
+  counters[4] = 0;
+}
+
+int persistentBlocks(const void *kernel, size_t smem) {
+  int dev, sms, per = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, TRACE_BLOCK, smem);
+  return sms * (per > 0 ? per : 1);
+}
+
 }  // namespace
 
 cudaError_t computeAlbedoTables(AlbedoTablesD *T, cudaStream_t st) {
@@ -569,30 +661,68 @@ cudaError_t computeAlbedoTables(AlbedoTablesD *T, cudaStream_t st) {
   return cudaGetLastError();
 }
 
+size_t ptWorkspaceBytes(long long npaths) {
+  auto up = [](size_t x) { return (x + 255) & ~size_t(255); };
+  return up(sizeof(PathRec) * npaths) + up(sizeof(HitBuf) * npaths) + 2 * up(4 * npaths) +
+         up(sizeof(ShadowRec) * 2 * npaths) + up(64);
+}
+
 cudaError_t launchRenderPT(const SamplerTables *T, const Scene &sc, const CameraD &cam, const PixelFilterD &pf,
                            const PtParamsD &p, const MaterialD *mats, const LightD *lights, const float *lightCdf,
-                           const AlbedoTablesD *AT, const FrameD &fb, bool stats, unsigned int *work,
+                           const AlbedoTablesD *AT, const FrameD &fb, bool stats, void *workspace, size_t wsBytes,
                            cudaStream_t st) {
-  PtCtx c = {T, sc, p, mats, lights, lightCdf, AT};
-  // persistent grid: as many blocks as fit on the device at once
-  static int blocksPerSM[2] = {0, 0}, numSMs = 0;
-  if (!numSMs) {
-    int dev;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&numSMs, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocksPerSM[0], k_render_pt<false>, TRACE_BLOCK,
-                                                  TRACE_SMEM_BYTES);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocksPerSM[1], k_render_pt<true>, TRACE_BLOCK, TRACE_SMEM_BYTES);
+  FrameInfo fi;
+  fi.W = fb.W;
+  fi.H = fb.H;
+  fi.spp = p.spp;
+  fi.frameID = fb.frameID;
+  fi.rcpW = fdiv(1.f, float(fb.W));
+  fi.rcpH = fdiv(1.f, float(fb.H));
+  fi.npaths = (long long)fb.W * fb.H * p.spp;
+  if (ptWorkspaceBytes(fi.npaths) > wsBytes) return cudaErrorInvalidValue;
+  Workspace ws;
+  char *base = static_cast<char *>(workspace);
+  auto carve = [&](size_t bytes) {
+    char *q = base;
+    base += (bytes + 255) & ~size_t(255);
+    return q;
+  };
+  ws.paths = (PathRec *)carve(sizeof(PathRec) * fi.npaths);
+  ws.hits = (HitBuf *)carve(sizeof(HitBuf) * fi.npaths);
+  ws.qa = (uint32_t *)carve(4 * fi.npaths);
+  ws.qb = (uint32_t *)carve(4 * fi.npaths);
+  ws.shadows = (ShadowRec *)carve(sizeof(ShadowRec) * 2 * fi.npaths);
+  ws.counters = (uint32_t *)carve(64);
+  PtCtx c = {T, sc, p, mats, lights, lightCdf, AT, fb.frameID};
+  static int traceBlocks = 0, shadowBlocks = 0, shadeBlocks = 0;
+  if (!traceBlocks) {
+    traceBlocks = persistentBlocks((const void *)k_trace_queue<false, false>, TRACE_SMEM_BYTES);
+    shadowBlocks = persistentBlocks((const void *)k_trace_queue<true, false>, TRACE_SMEM_BYTES);
+    shadeBlocks = persistentBlocks((const void *)k_pt_shade, TRACE_SMEM_BYTES);
   }
-  const int npix = fb.W * fb.H;
-  const int maxBlocks = (npix + TRACE_BLOCK - 1) / TRACE_BLOCK;
-  const int blocks = std::max(1, std::min(maxBlocks, numSMs * std::max(1, blocksPerSM[stats ? 1 : 0])));
-  cudaError_t err = cudaMemsetAsync(work, 0, sizeof(unsigned int), st);
-  if (err != cudaSuccess) return err;
-  if (stats)
-    k_render_pt<true><<<blocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(c, cam, pf, fb, work);
-  else
-    k_render_pt<false><<<blocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(c, cam, pf, fb, work);
+  const int gen = int((fi.npaths + 255) / 256);
+  k_pt_generate<<<gen, 256, 0, st>>>(c, cam, pf, fi, ws);
+  uint32_t *qs[2] = {ws.qa, ws.qb};
+  for (int b = 0; b <= p.maxPathLength; b++) {
+    const int cin = b & 1, cout = cin ^ 1;
+    k_bounce_reset<<<1, 1, 0, st>>>(ws.counters, cout);
+    const uint32_t *qin = b == 0 ? nullptr : qs[cin];
+    if (stats)
+      k_trace_queue<false, true><<<traceBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(sc, ws, qin, ws.counters + cin,
+                                                                                   ws.counters + 3);
+    else
+      k_trace_queue<false, false><<<traceBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(sc, ws, qin, ws.counters + cin,
+                                                                                    ws.counters + 3);
+    k_pt_shade<<<shadeBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(c, ws, qin, ws.counters + cin, qs[cout],
+                                                                   ws.counters + cout, ws.counters + 2);
+    if (stats)
+      k_trace_queue<true, true><<<shadowBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(sc, ws, nullptr, ws.counters + 2,
+                                                                                   ws.counters + 4);
+    else
+      k_trace_queue<true, false><<<shadowBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(sc, ws, nullptr,
+                                                                                    ws.counters + 2, ws.counters + 4);
+  }
+  k_pt_finalize<<<(fb.W * fb.H + 127) / 128, 128, 0, st>>>(c, ws, fi, fb);
   return cudaGetLastError();
 }
 

@@ -245,49 +245,51 @@ B200_D uint2 *traceStackBase() {
   return s_traceStack + threadIdx.x;
 }
 
-// Closest hit or any hit over the whole scene.  anyHit selects occlusion (stop at the first hit) at run time, so a kernel
-// that traces both kinds of rays needs a single copy of the traversal code.
-//
-// The lanes that call together trace together: every step of the loop
-// starts with a vote over those lanes, which is also where they reconverge;
-// a lane whose ray is finished idles until the last lane of its group is
-// done.  Without this the lanes of a warp drift to different points of the
-// data-dependent loop and execute one at a time.  `active == false` makes a
-// lane take part without tracing anything.
-template <bool STATS = false>
-B200_D bool traceRay(const Scene &sc, const Ray &ray, HitRec &hit, bool anyHit, bool active = true,
-                     TraceStats *ts = nullptr) {
-  hit.t = ray.tfar;
-  hit.u = hit.v = 0.f;
-  hit.primID = hit.geomID = hit.instID = hit.entry = INVALID_ID;
-  if (STATS && active) ts->rays++;
-  const unsigned group = __activemask();
+// Resumable traversal of one ray: init() sets it up, each step() pops or
+// visits one node (testing the node's leaf primitives), until it reports the
+// ray finished.  Kernels drive the steps so that the lanes of a warp stay in
+// lockstep and can replace finished rays with new ones.
+struct Traverser {
   TraceStack st;
-  st.smem = traceStackBase();
-  st.sp = 0;
-  const V3 wrdir = mk(1.f / ray.dir.x, 1.f / ray.dir.y, 1.f / ray.dir.z);
-  // current traversal frame (world for the TLAS, object space in a BLAS)
-  V3 org = ray.org, dir = ray.dir, rdir = wrdir;
+  Ray ray;
+  V3 wrdir, org, dir, rdir;  // world reciprocal direction; current frame
   TriPre pre;
-  const Node8 *nodes = sc.tlas;
-  bool inBlas = false;
-  const float4 *prims = nullptr;
-  const uint32_t *primIDs = nullptr;
-  uint32_t etype = 0, einst = 0, egeom = 0, eidx = 0;
-  bool found = false;
-  uint32_t node = 0;
-  bool have = active && sc.ntlas > 0;
-  bool done = !have;
-  for (int guard = 0; guard < (1 << 18); guard++) {
-    if (!__any_sync(group, !done)) break;
-    if (done) continue;
+  const Node8 *nodes;
+  const float4 *prims;
+  const uint32_t *primIDs;
+  uint32_t etype, einst, egeom, eidx, node;
+  bool inBlas, have, anyHit, found;
+  HitRec hit;
+
+  B200_D void init(const Scene &sc, const Ray &r, bool any) {
+    ray = r;
+    anyHit = any;
+    st.smem = traceStackBase();
+    st.sp = 0;
+    hit.t = r.tfar;
+    hit.u = hit.v = 0.f;
+    hit.primID = hit.geomID = hit.instID = hit.entry = INVALID_ID;
+    wrdir = mk(1.f / r.dir.x, 1.f / r.dir.y, 1.f / r.dir.z);
+    org = r.org;
+    dir = r.dir;
+    rdir = wrdir;
+    nodes = sc.tlas;
+    prims = nullptr;
+    primIDs = nullptr;
+    etype = einst = egeom = eidx = 0;
+    node = 0;
+    inBlas = false;
+    found = false;
+    have = sc.ntlas > 0;
+  }
+
+  // one traversal step; true when the ray is finished
+  template <bool STATS>
+  B200_D bool step(const Scene &sc, TraceStats *ts) {
     if (!have) {
-      if (st.sp == 0) {
-        done = true;
-        continue;
-      }
+      if (st.sp == 0) return true;
       const uint2 s = st.pop();
-      if (__uint_as_float(s.y) > hit.t) continue;
+      if (__uint_as_float(s.y) > hit.t) return false;
       const uint32_t tag = s.x & TAG_MASK;
       if (tag != TAG_BLAS && inBlas) {
         inBlas = false;
@@ -323,7 +325,7 @@ B200_D bool traceRay(const Scene &sc, const Ray &ray, HitRec &hit, bool anyHit, 
     if (STATS) ts->nodes++;
     float dist[8];
     const uint32_t mask = intersectChildren(n, org, rdir, ray.tnear, hit.t, dist);
-    if (!mask) continue;
+    if (!mask) return false;
     if (!inBlas) {
       // TLAS node: internal children and instances go on the stack
       for (uint32_t m = mask; m; m &= m - 1) {
@@ -337,7 +339,7 @@ B200_D bool traceRay(const Scene &sc, const Ray &ray, HitRec &hit, bool anyHit, 
           for (uint32_t k = 0; k < cnt; k++) st.push(TAG_INST | __ldg(sc.tlasLeaf + first + k), di, sc.status);
         }
       }
-      continue;
+      return false;
     }
     // BLAS node: leaves first (they tighten hit.t), then internal children
     for (uint32_t m = mask; m; m &= m - 1) {
@@ -375,10 +377,7 @@ B200_D bool traceRay(const Scene &sc, const Ray &ray, HitRec &hit, bool anyHit, 
         }
       }
     }
-    if (anyHit && found) {
-      done = true;
-      continue;
-    }
+    if (anyHit && found) return true;
     uint32_t nearest = 0xffffffffu;
     float nearestD = INFINITY;
     for (uint32_t m = mask; m; m &= m - 1) {
@@ -399,8 +398,34 @@ B200_D bool traceRay(const Scene &sc, const Ray &ray, HitRec &hit, bool anyHit, 
       node = nearest;
       have = true;
     }
+    return false;
   }
-  return found;
+};
+
+// Closest hit or any hit over the whole scene, for one ray per lane.  anyHit
+// selects occlusion (stop at the first hit) at run time, so a kernel that
+// traces both kinds of rays needs one copy of the traversal code.
+//
+// The lanes that call together trace together: every step starts with a
+// vote over those lanes, which is also where they reconverge; a lane whose
+// ray is finished idles until the last lane of its group is done.  Without
+// this the lanes of a warp drift to different points of the data-dependent
+// loop and execute one at a time.  `active == false` makes a lane take part
+// without tracing anything.
+template <bool STATS = false>
+B200_D bool traceRay(const Scene &sc, const Ray &ray, HitRec &hit, bool anyHit, bool active = true,
+                     TraceStats *ts = nullptr) {
+  if (STATS && active) ts->rays++;
+  const unsigned group = __activemask();
+  Traverser tv;
+  tv.init(sc, ray, anyHit);
+  bool done = !active || !tv.have;
+  for (int guard = 0; guard < (1 << 18); guard++) {
+    if (!__any_sync(group, !done)) break;
+    if (!done) done = tv.step<STATS>(sc, ts);
+  }
+  hit = tv.hit;
+  return tv.found;
 }
 
 // Closest hit (ANY = false) or any hit (ANY = true).

@@ -118,6 +118,27 @@ def build_pt_scene(scene, data):
     scene.commit()
 
 
+def volume_scene(n=512, seed=11, width=1024, height=1024, orbit_deg=30.0):
+    """SciVis volume workload: n^3 float32 of 5-octave fractal value noise
+    (base frequency 4, lacunarity 2, gain 0.5) normalised to [0,1] over the
+    unit cube (spacing 1/(n-1)); transfer function of 256 seeded ramp
+    colours and 256 opacities (0 below 0.3, then linear to 0.8 at 1.0);
+    camera on an orbit at 2.5 x the cube diagonal, azimuth `orbit_deg`,
+    elevation 20 degrees, looking at the centre, fovy 30."""
+    vol = fractal_volume(n, 5, 4.0, seed)
+    color = color_ramp(seed, 256)
+    v = np.linspace(0.0, 1.0, 256, dtype=np.float32)
+    opacity = np.where(v < 0.3, 0.0, 0.8 * (v - 0.3) / 0.7).astype(np.float32)
+    d = 2.5 * np.sqrt(3.0)
+    az, el = np.radians(orbit_deg), np.radians(20.0)
+    eye = np.array([0.5 + d * np.cos(el) * np.sin(az), 0.5 + d * np.sin(el), 0.5 - d * np.cos(el) * np.cos(az)])
+    cam = dict(position=tuple(eye), direction=tuple(np.array([0.5, 0.5, 0.5]) - eye), up=(0.0, 1.0, 0.0),
+               fovy=30.0, aspect=width / height)
+    sp = 1.0 / (n - 1)
+    return dict(volume=vol, origin=(0.0, 0.0, 0.0), spacing=(sp, sp, sp), color=color, opacity=opacity,
+                value_range=(0.0, 1.0), camera=cam, width=width, height=height)
+
+
 def build_ao_scene(scene, data):
     """Adds the AO workload's geometry to a b200 Scene (or the oracle)."""
     gm = scene.add_mesh(data["vertex"], data["index"])

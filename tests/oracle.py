@@ -103,6 +103,12 @@ def lib():
                                    P, P, P, I]
         L.or_ray_count.restype = ctypes.c_uint64
         L.or_ray_count.argtypes = [I]
+        L.or_volume_new.restype = P
+        L.or_volume_new.argtypes = [P, I, I, I, P, P, P, I, P, I, F, F, F]
+        L.or_volume_free.argtypes = [P]
+        L.or_volume_sample_count.restype = ctypes.c_uint64
+        L.or_volume_sample_count.argtypes = [I]
+        L.or_render_scivis_volume.argtypes = [P, ctypes.POINTER(OrCamera), I, I, I, I, F, P, I, I, I, P, I]
         L.or_scene_commit.argtypes = [P]
         L.or_trace.argtypes = [P, P, I, I, P, P, I]
         L.or_camera_rays.argtypes = [ctypes.POINTER(OrCamera), I, I, I, I, I, P]
@@ -182,3 +188,32 @@ def tables():
     s = np.zeros(128, np.uint32)
     lib().or_tables(_p(p3), _p(p5), _p(p7), _p(s))
     return {"halton_perm3": p3, "halton_perm5": p5, "halton_perm7": p7, "Sobol_revMatrices": s}
+
+
+class VolumeModel:
+    """Oracle structured-regular volume + transfer function."""
+
+    def __init__(self, data, origin, spacing, color, opacity, value_range=(0.0, 1.0), density_scale=1.0):
+        d = np.ascontiguousarray(data, np.float32)
+        nz, ny, nx = d.shape
+        o, sp = np.asarray(origin, np.float32), np.asarray(spacing, np.float32)
+        c = np.ascontiguousarray(color, np.float32).reshape(-1, 3)
+        op = np.ascontiguousarray(opacity, np.float32).reshape(-1)
+        self.h = lib().or_volume_new(_p(d), nx, ny, nz, _p(o), _p(sp), _p(c), len(c), _p(op), len(op),
+                                     float(value_range[0]), float(value_range[1]), float(density_scale))
+
+    def __del__(self):
+        try:
+            lib().or_volume_free(self.h)
+        except Exception:
+            pass
+
+
+def render_scivis_volume(model, cam, pixel_filter, w, h, spp=1, sampling_rate=1.0, bg=(0, 0, 0, 0), frames=1,
+                         rows=None, nthreads=0):
+    color = np.zeros((h, w, 4), np.float32)
+    bgv = np.asarray(bg, np.float32)
+    y0, y1 = rows if rows else (0, 0)
+    lib().or_render_scivis_volume(model.h, ctypes.byref(cam), pixel_filter, w, h, spp, sampling_rate, _p(bgv),
+                                  frames, y0, y1, _p(color), nthreads)
+    return color
