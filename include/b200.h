@@ -171,6 +171,22 @@ typedef struct {
 int b200_render_pt(b200_scene scene, const b200_camera_desc *camera, const b200_pt_params *params,
                    const b200_material *materials, int nmaterials, b200_frame fb, void *stream);
 
+/* ---- path tracer for callers that cannot allocate device memory.
+ * No counterpart in the reference: OSPRay's CPU device allocates freely.
+ * For applications that reserve all device memory up front, must not stall
+ * on the allocator inside a real-time loop, or run under an external memory
+ * cap, this renders exactly like b200_render_pt but takes its scratch (path
+ * workspace, material list, microfacet albedo tables) from a fixed 48 MiB
+ * static device array inside the library instead of cudaMalloc; the call
+ * itself allocates nothing.  Limits: width * height * pixelSamples <=
+ * 190,000 paths and nmaterials <= 4096, else B200_INVALID_ARGUMENT with a
+ * message.  The first call on a device sets the scratch up (looks up its
+ * device address and fills the albedo tables) and waits for that; make it
+ * before capturing any stream.  Calls share the one array: two calls that
+ * overlap on the GPU race and must not be issued. */
+int b200_render_pt_noalloc(b200_scene scene, const b200_camera_desc *camera, const b200_pt_params *params,
+                           const b200_material *materials, int nmaterials, b200_frame fb, void *stream);
+
 /* ---- structured-regular volume + piecewise-linear transfer function
  *      (StructuredRegular volume, volume/Volume.cpp:60-222;
  *       VolumetricModel::commit volume/VolumetricModel.cpp:30-82;
