@@ -257,7 +257,85 @@ class PTWorkload:
         return rays, dt, rows / self.h
 
 
-WORKLOADS = {"ao": AOWorkload, "pt": PTWorkload}
+class ScivisWorkload:
+    """SciVis volume rendering: 512^3 float32 fractal-noise volume through a
+    256-entry transfer function, volumeSamplingRate 1, 1024x1024, 4 spp,
+    orbit camera.  Unit: volume samples (Msamples/s)."""
+    name = "scivis_volume_512cube_1024"
+    metric = "Msamples/s"
+    launches_per_frame = 1
+
+    def __init__(self, w=1024, h=1024, n=512, spp=4):
+        from ospray_gb300 import scenes
+        self.w, self.h, self.spp = w, h, spp
+        self.data = scenes.volume_scene(n=n, width=w, height=h)
+        self.config = {"workload": self.name, "renderer": "scivis", "width": w, "height": h, "spp": spp,
+                       "volume": "%d^3 float32" % n, "volumeSamplingRate": 1.0, "transfer_function": 256,
+                       "pixelFilter": "gauss"}
+
+    def setup(self, og, dev):
+        self.og = og
+        d = self.data
+        t0 = time.perf_counter()
+        self.scene = og.Scene(dev)
+        self.scene.set_volume(d["volume"], d["origin"], d["spacing"], d["color"], d["opacity"], d["value_range"])
+        self.build_ms = (time.perf_counter() - t0) * 1e3
+        c = d["camera"]
+        self.cam = og.camera_desc(c["position"], c["direction"], c["up"], fovy=c["fovy"], aspect=c["aspect"])
+        self.params = og.scivis_params(spp=self.spp)
+        self.sparams = og.scivis_params(spp=self.spp, stats=True)
+        self.fb = og.Frame(dev, self.w, self.h, og.FB_COLOR | og.FB_ACCUM)
+        self.color = np.empty((self.h, self.w, 4), np.float32)
+
+    def step(self, stats=False):
+        self.og.render_scivis(self.scene, self.cam, self.sparams if stats else self.params, self.fb)
+
+    def e2e_step(self):
+        self.og.render_scivis(self.scene, self.cam, self.params, self.fb)
+        self.og.lib().b200_frame_read(self.fb._h, self.og.FB_COLOR, self.color.ctypes.data, self.color.nbytes)
+        return 40 + 32, self.color.nbytes
+
+    def reset(self):
+        self.fb.reset()
+
+    def counters(self, reset=False):
+        c = self.scene.counters(reset)
+        return c
+
+    def units(self, c):
+        return int(c[1])  # volume samples
+
+    def bytes_per_unit(self):
+        return 32.0
+
+    def cpu_frames(self, budget_s, nthreads):
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        import oracle
+        d = self.data
+        if not hasattr(self, "_orc"):
+            self._orc = oracle.VolumeModel(d["volume"], d["origin"], d["spacing"], d["color"], d["opacity"],
+                                           d["value_range"])
+            c = d["camera"]
+            self._ocam = oracle.camera(c["position"], c["direction"], c["up"], fovy=c["fovy"], aspect=c["aspect"])
+            self._rows = 4
+        y0 = self.h // 2 - self._rows // 2
+        oracle.lib().or_volume_sample_count(1)
+        t0 = time.perf_counter()
+        oracle.render_scivis_volume(self._orc, self._ocam, 2, self.w, self.h, spp=self.spp,
+                                    rows=(y0, y0 + self._rows), nthreads=nthreads)
+        dt = time.perf_counter() - t0
+        samples = int(oracle.lib().or_volume_sample_count(1))
+        rows = self._rows
+        self._rows = int(max(2, min(self.h, rows * min(8.0, budget_s / max(dt, 1e-3)))))
+        if dt < 0.25 * budget_s and self._rows > rows:
+            return self.cpu_frames(budget_s, nthreads)
+        self.cpu_sample = "%d centre rows x %d px x %d spp" % (rows, self.w, self.spp)
+        return samples, dt, rows / self.h
+
+
+AOWorkload.launches_per_frame = 1
+PTWorkload.launches_per_frame = 2 + 6 * 4  # generate, finalize, 6 bounces x (reset, trace, shade, shadow)
+WORKLOADS = {"ao": AOWorkload, "pt": PTWorkload, "scivis": ScivisWorkload}
 
 
 # --------------------------------------------------------------------------- arms
@@ -285,14 +363,14 @@ def run_reference(args):
             rays_total += rays
     secs = sum(dt for _, dt in per_step)
     value = rays_total / secs / 1e6
-    line = {"metric": wl.metric, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": args.gpus,
+    line = {"metric": wl.metric, "value": round(value, 3), "unit": wl.metric, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(secs / args.steps * 1e3, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded generators)", "config": wl.config, "impl": "reference",
-            "cpu_baseline": {"value": round(value, 3), "unit": "Mrays/s", "cores": nthreads, "kind": "port",
+            "cpu_baseline": {"value": round(value, 3), "unit": wl.metric, "cores": nthreads, "kind": "port",
                              "sample": "%s, about %.1f s of CPU work per step"
                                        % (getattr(wl, "cpu_sample", "whole frames"), args.cpu_budget / max(1, args.steps))},
-            "e2e": {"value": round(value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "e2e": {"value": round(value, 3), "unit": wl.metric, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
@@ -342,6 +420,7 @@ def run_ours(args):
         wl.step(stats=True)
     c = wl.counters(reset=True)
     rays, nodes, tris, sph = (int(x) for x in c)
+    units = wl.units(c) if hasattr(wl, "units") else rays
     # end-to-end through the C ABI with host buffers
     wl.reset()
     for _ in range(2):
@@ -355,7 +434,7 @@ def run_ours(args):
     dev.sync()
     e2e_s = time.perf_counter() - t0
 
-    local_vals = torch.tensor([dev_ms, e2e_s, float(rays)], dtype=torch.float64, device=torch.device("cuda", local))
+    local_vals = torch.tensor([dev_ms, e2e_s, float(units)], dtype=torch.float64, device=torch.device("cuda", local))
     if ws > 1:
         mx = local_vals.clone()
         torch.distributed.all_reduce(mx, op=torch.distributed.ReduceOp.MAX)
@@ -363,36 +442,41 @@ def run_ours(args):
         torch.distributed.all_reduce(sm, op=torch.distributed.ReduceOp.SUM)
         dev_ms_max, e2e_max, rays_all = float(mx[0]), float(mx[1]), float(sm[2])
     else:
-        dev_ms_max, e2e_max, rays_all = dev_ms, e2e_s, float(rays)
+        dev_ms_max, e2e_max, rays_all = dev_ms, e2e_s, float(units)
     if rank != 0:
         if ws > 1:
             torch.distributed.destroy_process_group()
         return
     value = rays_all / (dev_ms_max * 1e-3) / 1e6
     e2e_val = rays_all / e2e_max / 1e6
-    bytes_per_frame = (48.0 * rays + 80.0 * nodes + 48.0 * tris + 20.0 * sph) / args.steps
+    if hasattr(wl, "bytes_per_unit"):
+        bytes_per_frame = wl.bytes_per_unit() * units / args.steps
+        note = "algorithmic volume bytes (32 B per trilinear sample) per frame / frame time"
+    else:
+        bytes_per_frame = (48.0 * rays + 80.0 * nodes + 48.0 * tris + 20.0 * sph) / args.steps
+        note = "algorithmic traversal bytes per frame / frame time"
     frame_s = dev_ms / args.steps * 1e-3
     peak, kind = peaks()
     achieved = bytes_per_frame / frame_s / 1e9
-    line = {"metric": wl.metric, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": ws, "steps": args.steps,
+    line = {"metric": wl.metric, "value": round(value, 3), "unit": wl.metric, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(dev_ms_max / args.steps, 4), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generators)",
             "config": dict(wl.config, l2="flushed before every frame (512 MiB write)",
                            parallelism="replicas" if ws > 1 else "single", build_ms=round(wl.build_ms, 2),
                            rays_per_frame=rays / args.steps, node_visits_per_ray=round(nodes / max(rays, 1), 3),
                            tri_tests_per_ray=round(tris / max(rays, 1), 3)),
-            "e2e": {"value": round(e2e_val, 3), "unit": "Mrays/s", "h2d_bytes_per_step": h2d,
+            "e2e": {"value": round(e2e_val, 3), "unit": wl.metric, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
-            "gpu_launches": args.steps,
+            "gpu_launches": args.steps * wl.launches_per_frame,
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4), "traffic": None,
-                         "note": "algorithmic traversal bytes per frame / frame time; peak %s" % kind},
+                         "note": "%s; peak %s" % (note, kind)},
             "clocks": clk.summary()}
     if not args.no_cpu_baseline:
         nthreads = os.cpu_count() or 1
         crays, cdt, cframes = wl.cpu_frames(args.cpu_budget, nthreads)
         sample = getattr(wl, "cpu_sample", "%s frames of the same workload" % cframes)
-        line["cpu_baseline"] = {"value": round(crays / cdt / 1e6, 3), "unit": "Mrays/s", "cores": nthreads,
+        line["cpu_baseline"] = {"value": round(crays / cdt / 1e6, 3), "unit": wl.metric, "cores": nthreads,
                                 "kind": "port", "sample": "%s (%.1f s)" % (sample, cdt)}
     print(json.dumps(line), flush=True)
     if ws > 1:
