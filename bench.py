@@ -263,7 +263,7 @@ class ScivisWorkload:
     orbit camera.  Unit: volume samples (Msamples/s)."""
     name = "scivis_volume_512cube_1024"
     metric = "Msamples/s"
-    launches_per_frame = 1
+    launches_per_frame = 2  # march + post-process (colour conversion)
 
     def __init__(self, w=1024, h=1024, n=512, spp=4):
         from ospray_gb300 import scenes
@@ -333,8 +333,8 @@ class ScivisWorkload:
         return samples, dt, rows / self.h
 
 
-AOWorkload.launches_per_frame = 1
-PTWorkload.launches_per_frame = 2 + 6 * 4  # generate, finalize, 6 bounces x (reset, trace, shade, shadow)
+AOWorkload.launches_per_frame = 2  # render + post-process (colour conversion)
+PTWorkload.launches_per_frame = 3 + 6 * 4  # generate, finalize, post-process, 6 bounces x (reset, trace, shade, shadow)
 WORKLOADS = {"ao": AOWorkload, "pt": PTWorkload, "scivis": ScivisWorkload}
 
 

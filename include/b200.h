@@ -91,29 +91,57 @@ typedef struct {
   float fovy, aspect, nearClip;
 } b200_camera_desc;
 
-/* ---- framebuffer (LocalFrameBuffer, modules/cpu/fb/LocalFB.cpp; channels as
- *      OSPFrameBufferChannel bits: COLOR 1, DEPTH 2, ACCUM 4, VARIANCE 8,
- *      NORMAL 16, ALBEDO 32, PRIMID 128, GEOMID 256, INSTID 512) */
+/* ---- framebuffer (LocalFrameBuffer, modules/cpu/fb/LocalFB.cpp:23-226;
+ *      formats OSPFrameBufferFormat and channels OSPFrameBufferChannel,
+ *      ospray/include/ospray/OSPEnums.h:240-266) */
+enum { B200_FB_NONE = 0, B200_FB_RGBA8 = 1, B200_FB_SRGBA = 2, B200_FB_RGBA32F = 3 };
 enum {
-  B200_FB_COLOR = 1,
-  B200_FB_DEPTH = 2,
-  B200_FB_ACCUM = 4,
-  B200_FB_VARIANCE = 8,
-  B200_FB_NORMAL = 16,
-  B200_FB_ALBEDO = 32,
-  B200_FB_ID_PRIMITIVE = 128,
-  B200_FB_ID_OBJECT = 256,
-  B200_FB_ID_INSTANCE = 512
+  B200_FB_COLOR = 1 << 0,
+  B200_FB_DEPTH = 1 << 1,
+  B200_FB_ACCUM = 1 << 2,
+  B200_FB_VARIANCE = 1 << 3,
+  B200_FB_NORMAL = 1 << 4,
+  B200_FB_ALBEDO = 1 << 5,
+  B200_FB_ID_PRIMITIVE = 1 << 6,
+  B200_FB_ID_OBJECT = 1 << 7,
+  B200_FB_ID_INSTANCE = 1 << 8
 };
-int b200_frame_create(b200_device dev, int width, int height, uint32_t channels, b200_frame *out);
+/* ospNewFrameBuffer(width, height, format, channels).  The colour channel
+ * always accumulates in RGBA32F on the device; after every render the
+ * frame's post-processing step (tonemapper, if set, then conversion to
+ * `format`) writes the mapped colour, as LocalFrameBuffer::postProcess does
+ * (fb/LocalFB.cpp:459-477). */
+int b200_frame_create(b200_device dev, int width, int height, int format, uint32_t channels, b200_frame *out);
 int b200_frame_release(b200_frame fb);
 /* ospResetAccumulation: frameID back to 0 */
 int b200_frame_reset(b200_frame fb);
 int b200_frame_id(b200_frame fb);
-/* device pointer of one channel (COLOR: RGBA32F W*H*4; DEPTH float; IDs uint32) */
+/* device pointer of one channel as ospMapFrameBuffer would return it:
+ * COLOR = the converted colour (RGBA8/SRGBA: W*H uint32, RGBA32F: W*H*4
+ * float; FB_NONE: the raw accumulation buffer), DEPTH float, NORMAL/ALBEDO
+ * float3, IDs uint32, VARIANCE float4.  ACCUM gives the accumulated RGBA32F
+ * colour before post-processing (an addition: the reference cannot map it).
+ * Rows bottom-up. */
 void *b200_frame_channel(b200_frame fb, uint32_t channel);
+/* bytes of one mapped channel */
+size_t b200_frame_channel_bytes(b200_frame fb, uint32_t channel);
 /* ospMapFrameBuffer: copies a channel to host memory (waits for the device) */
 int b200_frame_read(b200_frame fb, uint32_t channel, void *host_dst, size_t bytes);
+
+/* ---- tonemapper frame operation (ToneMapper::commit
+ *      fb/frame_ops/ToneMapper.cpp:16-51, ToneMapper_kernel
+ *      fb/frame_ops/ToneMapper.ispc:12-41; parameter defaults are the ACES
+ *      filmic fit: exposure 1, contrast 1.6773, shoulder 0.9714, midIn 0.18,
+ *      midOut 0.18, hdrMax 11.0785, acesColor 1).  Setting it is
+ *      ospSetObjectAsData(fb, "imageOperation", ...) + ospCommit(fb); a null
+ *      `tm` removes it.  It applies from the next render on. */
+typedef struct {
+  float exposure, contrast, shoulder, midIn, midOut, hdrMax;
+  int acesColor;
+} b200_tonemapper;
+/* fills `tm` with the defaults above */
+void b200_tonemapper_defaults(b200_tonemapper *tm);
+int b200_frame_set_tonemapper(b200_frame fb, const b200_tonemapper *tm);
 
 /* ---- AO renderer (AORenderer::commit modules/cpu/render/ao/AORenderer.cpp:26-35,
  *      AORenderer_renderSample render/ao/AORenderer.ispc:23-149).
@@ -220,6 +248,21 @@ int b200_render_scivis(b200_scene scene, const b200_camera_desc *camera, const b
 int b200_scene_counters(b200_scene scene, int64_t *out4, int reset);
 int b200_render_ao(b200_scene scene, const b200_camera_desc *camera, const b200_ao_params *params, b200_frame fb,
                    void *stream);
+
+/* ---- pick (ospPick, ospray/include/ospray/ospray.h:338-352; Renderer::pick
+ *      render/Renderer.cpp:94-140, Renderer_pick render/Renderer.ispc:43-95).
+ * One camera ray through normalised screen position (x, y) in [0,1]^2
+ * (origin bottom-left, lens centre, time 0.5), traced closest-hit.  On a hit
+ * the world position org + t*dir and the instance / geometric-model /
+ * primitive IDs of the instance that was hit; otherwise hasHit 0 and IDs
+ * 0xffffffff.  Synchronous. */
+typedef struct {
+  int hasHit;
+  float worldPosition[3];
+  uint32_t instID, geomID, primID;
+} b200_pick_result;
+int b200_pick(b200_scene scene, const b200_camera_desc *camera, float screen_x, float screen_y,
+              b200_pick_result *result);
 
 #ifdef __cplusplus
 }

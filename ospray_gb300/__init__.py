@@ -17,10 +17,12 @@ BUILD = os.path.join(HERE, "_build")
 _lib = None
 _scenes = None
 
+# OSPFrameBufferFormat
+FB_NONE, FB_RGBA8, FB_SRGBA, FB_RGBA32F = 0, 1, 2, 3
 # OSPFrameBufferChannel bits
 FB_COLOR, FB_DEPTH, FB_ACCUM, FB_VARIANCE = 1, 2, 4, 8
 FB_NORMAL, FB_ALBEDO = 16, 32
-FB_ID_PRIMITIVE, FB_ID_OBJECT, FB_ID_INSTANCE = 128, 256, 512
+FB_ID_PRIMITIVE, FB_ID_OBJECT, FB_ID_INSTANCE = 64, 128, 256
 # OSPPixelFilterType
 PF_POINT, PF_BOX, PF_GAUSS, PF_MITCHELL, PF_BLACKMAN_HARRIS = range(5)
 
@@ -55,6 +57,18 @@ class Light(ctypes.Structure):
     _fields_ = [("type", ctypes.c_int), ("visible", ctypes.c_int), ("position", ctypes.c_float * 3),
                 ("edge1", ctypes.c_float * 3), ("edge2", ctypes.c_float * 3), ("color", ctypes.c_float * 3),
                 ("intensity", ctypes.c_float)]
+
+
+class ToneMapper(ctypes.Structure):
+    """b200_tonemapper: the ACES-fit tonemapper frame operation."""
+    _fields_ = [("exposure", ctypes.c_float), ("contrast", ctypes.c_float), ("shoulder", ctypes.c_float),
+                ("midIn", ctypes.c_float), ("midOut", ctypes.c_float), ("hdrMax", ctypes.c_float),
+                ("acesColor", ctypes.c_int)]
+
+
+class PickResult(ctypes.Structure):
+    _fields_ = [("hasHit", ctypes.c_int), ("worldPosition", ctypes.c_float * 3), ("instID", ctypes.c_uint32),
+                ("geomID", ctypes.c_uint32), ("primID", ctypes.c_uint32)]
 
 
 class Material(ctypes.Structure):
@@ -150,7 +164,11 @@ def lib():
             "b200_scene_stats": (I, [P, P]),
             "b200_scene_counters": (I, [P, P, I]),
             "b200_trace": (I, [P, P, I64, I, P, P, P]),
-            "b200_frame_create": (I, [P, I, I, U32, ctypes.POINTER(P)]),
+            "b200_frame_create": (I, [P, I, I, I, U32, ctypes.POINTER(P)]),
+            "b200_frame_channel_bytes": (ctypes.c_size_t, [P, U32]),
+            "b200_tonemapper_defaults": (None, [ctypes.POINTER(ToneMapper)]),
+            "b200_frame_set_tonemapper": (I, [P, ctypes.POINTER(ToneMapper)]),
+            "b200_pick": (I, [P, ctypes.POINTER(CameraDesc), F, F, ctypes.POINTER(PickResult)]),
             "b200_frame_release": (I, [P]),
             "b200_frame_reset": (I, [P]),
             "b200_frame_id": (I, [P]),
@@ -292,12 +310,25 @@ class Scene:
             pass
 
 
+def tonemapper(**kw):
+    """A b200_tonemapper with the reference's defaults, fields overridden by keyword."""
+    t = ToneMapper()
+    lib().b200_tonemapper_defaults(ctypes.byref(t))
+    for k, v in kw.items():
+        setattr(t, k, v)
+    return t
+
+
 class Frame:
-    def __init__(self, device, width, height, channels=FB_COLOR | FB_DEPTH | FB_ACCUM):
+    def __init__(self, device, width, height, channels=FB_COLOR | FB_DEPTH | FB_ACCUM, format=FB_RGBA32F):
         self.device = device
-        self.width, self.height, self.channels = width, height, channels
+        self.width, self.height, self.channels, self.format = width, height, channels, format
         self._h = ctypes.c_void_p()
-        device._check(lib().b200_frame_create(device._h, width, height, channels, ctypes.byref(self._h)))
+        device._check(lib().b200_frame_create(device._h, width, height, format, channels, ctypes.byref(self._h)))
+
+    def set_tonemapper(self, tm):
+        """tm: ToneMapper (see tonemapper()) or None to remove it; applies from the next render."""
+        self.device._check(lib().b200_frame_set_tonemapper(self._h, ctypes.byref(tm) if tm is not None else None))
 
     def reset(self):
         self.device._check(lib().b200_frame_reset(self._h))
@@ -311,7 +342,9 @@ class Frame:
 
     def read(self, ch=FB_COLOR):
         n = self.width * self.height
-        if ch in (FB_COLOR, FB_VARIANCE):
+        if ch == FB_COLOR and self.format in (FB_RGBA8, FB_SRGBA):
+            out = np.empty((self.height, self.width, 4), np.uint8)
+        elif ch in (FB_COLOR, FB_VARIANCE, FB_ACCUM):
             out = np.empty((self.height, self.width, 4), np.float32)
         elif ch in (FB_NORMAL, FB_ALBEDO):
             out = np.empty((self.height, self.width, 3), np.float32)
@@ -320,7 +353,7 @@ class Frame:
         else:
             out = np.empty((self.height, self.width), np.uint32)
         self.device._check(lib().b200_frame_read(self._h, ch, _ptr(out), out.nbytes))
-        assert out.size in (n, 3 * n, 4 * n)
+        assert out.nbytes == lib().b200_frame_channel_bytes(self._h, ch)
         return out
 
     def release(self):
@@ -353,6 +386,13 @@ def ao_params(spp=1, ao_samples=1, ao_distance=1e20, ao_intensity=1.0, bg=(0, 0,
     p.backgroundColor[:] = list(map(float, bg))
     p.pixelFilter = int(pixel_filter)
     return p
+
+
+def pick(scene, camera, x, y):
+    """ospPick: (hit, world position, instID, geomID, primID) at normalised screen (x, y)."""
+    r = PickResult()
+    scene.device._check(lib().b200_pick(scene._h, ctypes.byref(camera), float(x), float(y), ctypes.byref(r)))
+    return bool(r.hasHit), tuple(r.worldPosition), r.instID, r.geomID, r.primID
 
 
 def render_ao(scene, camera, params, frame, stream=None):

@@ -116,6 +116,7 @@ DeviceObj::DeviceObj(int cudaDev) : dev(cudaDev) {
   buildTables(t);
   check(cudaMalloc(&tables, sizeof(SamplerTables)), "cudaMalloc tables");
   check(cudaMalloc(&work, 64), "cudaMalloc work counter");
+  check(cudaMalloc(&pickBuf, 32), "cudaMalloc pick result");
   check(cudaMemcpy(tables, &t, sizeof(t), cudaMemcpyHostToDevice), "upload tables");
   for (int type = B200_PF_GAUSS; type <= B200_PF_BLACKMAN_HARRIS; type++) {
     std::vector<float> cx, cy;
@@ -145,6 +146,7 @@ DeviceObj::~DeviceObj() {
   cudaStreamSynchronize(stream);
   cudaFree(tables);
   cudaFree(work);
+  cudaFree(pickBuf);
   if (albedo) cudaFree(albedo);
   if (ptWs) cudaFree(ptWs);
   for (auto &L : luts) {
@@ -337,7 +339,7 @@ Scene SceneObj::view() const {
   return s;
 }
 
-FrameObj::FrameObj(DeviceObj *d, int w, int h, uint32_t ch) : dev(d), W(w), H(h), channels(ch) {
+FrameObj::FrameObj(DeviceObj *d, int w, int h, int fmt, uint32_t ch) : dev(d), W(w), H(h), format(fmt), channels(ch) {
   dev->retain();
   const size_t n = size_t(w) * h;
   auto alloc = [&](void **p, size_t bytes) {
@@ -352,12 +354,13 @@ FrameObj::FrameObj(DeviceObj *d, int w, int h, uint32_t ch) : dev(d), W(w), H(h)
   if (ch & B200_FB_ID_PRIMITIVE) alloc((void **)&primID, n * 4);
   if (ch & B200_FB_ID_OBJECT) alloc((void **)&geomID, n * 4);
   if (ch & B200_FB_ID_INSTANCE) alloc((void **)&instID, n * 4);
+  if (fmt != B200_FB_NONE) alloc(&mapped, n * (fmt == B200_FB_RGBA32F ? 16 : 4));
 }
 
 FrameObj::~FrameObj() {
   cudaStreamSynchronize(dev->stream);
   for (void *p : {(void *)color, (void *)depth, (void *)variance, (void *)normal, (void *)albedo, (void *)primID,
-                  (void *)geomID, (void *)instID})
+                  (void *)geomID, (void *)instID, mapped})
     if (p) cudaFree(p);
   dev->release();
 }
@@ -380,7 +383,8 @@ FrameD FrameObj::view() const {
 
 void *FrameObj::channel(uint32_t c) const {
   switch (c) {
-    case B200_FB_COLOR: return color;
+    case B200_FB_COLOR: return mapped ? mapped : (void *)color;
+    case B200_FB_ACCUM: return color;
     case B200_FB_DEPTH: return depth;
     case B200_FB_VARIANCE: return variance;
     case B200_FB_NORMAL: return normal;
@@ -395,7 +399,8 @@ void *FrameObj::channel(uint32_t c) const {
 size_t FrameObj::channelBytes(uint32_t c) const {
   const size_t n = size_t(W) * H;
   switch (c) {
-    case B200_FB_COLOR:
+    case B200_FB_COLOR: return n * (format == B200_FB_RGBA8 || format == B200_FB_SRGBA ? 4 : 16);
+    case B200_FB_ACCUM:
     case B200_FB_VARIANCE: return n * 16;
     case B200_FB_NORMAL:
     case B200_FB_ALBEDO: return n * 12;
@@ -575,12 +580,39 @@ int b200_trace(b200_scene s, const float *rays, int64_t n, int occlusion, float 
   });
 }
 
-int b200_frame_create(b200_device d, int w, int h, uint32_t channels, b200_frame *out) {
+int b200_frame_create(b200_device d, int w, int h, int format, uint32_t channels, b200_frame *out) {
   if (!d || !out) return B200_INVALID_ARGUMENT;
   DeviceObj *dev = reinterpret_cast<DeviceObj *>(d);
   return guarded(dev, [&]() {
     require(w > 0 && h > 0 && int64_t(w) * h < (int64_t(1) << 31), "bad framebuffer size");
-    *out = reinterpret_cast<b200_frame>(new FrameObj(dev, w, h, channels));
+    require(format >= B200_FB_NONE && format <= B200_FB_RGBA32F, "unknown framebuffer format");
+    *out = reinterpret_cast<b200_frame>(new FrameObj(dev, w, h, format, channels));
+  });
+}
+
+size_t b200_frame_channel_bytes(b200_frame f, uint32_t c) {
+  if (!f) return 0;
+  FrameObj *fb = reinterpret_cast<FrameObj *>(f);
+  return fb->channel(c) ? fb->channelBytes(c) : 0;
+}
+
+void b200_tonemapper_defaults(b200_tonemapper *tm) {
+  if (!tm) return;
+  tm->exposure = 1.f;
+  tm->contrast = 1.6773f;
+  tm->shoulder = 0.9714f;
+  tm->midIn = 0.18f;
+  tm->midOut = 0.18f;
+  tm->hdrMax = 11.0785f;
+  tm->acesColor = 1;
+}
+
+int b200_frame_set_tonemapper(b200_frame f, const b200_tonemapper *tm) {
+  if (!f) return B200_INVALID_ARGUMENT;
+  FrameObj *fb = reinterpret_cast<FrameObj *>(f);
+  return guarded(fb->dev, [&]() {
+    fb->toneMapOn = tm != nullptr;
+    if (tm) fb->toneMap = makeToneMap(*tm);
   });
 }
 
@@ -633,6 +665,7 @@ int b200_render_ao(b200_scene s, const b200_camera_desc *camera, const b200_ao_p
                          fb->view(), p->collectStats != 0, st),
           "AO launch");
     fb->frameID++;
+    framePostProcess(fb, st);
   });
 }
 
@@ -745,6 +778,7 @@ int b200_render_pt(b200_scene s, const b200_camera_desc *camera, const b200_pt_p
                          p->collectStats != 0, dev->ptWs, dev->ptWsBytes, st),
           "path tracer launch");
     fb->frameID++;
+    framePostProcess(fb, st);
   });
 }
 
@@ -817,6 +851,25 @@ int b200_render_scivis(b200_scene s, const b200_camera_desc *camera, const b200_
                                    sc->dev->filter(p->pixelFilter), d, fb->view(), p->collectStats != 0, st),
           "scivis launch");
     fb->frameID++;
+    framePostProcess(fb, st);
+  });
+}
+
+int b200_pick(b200_scene s, const b200_camera_desc *camera, float sx, float sy, b200_pick_result *res) {
+  if (!s || !camera || !res) return B200_INVALID_ARGUMENT;
+  SceneObj *sc = reinterpret_cast<SceneObj *>(s);
+  return guarded(sc->dev, [&]() {
+    require(sc->committed, "scene not committed");
+    DeviceObj *dev = sc->dev;
+    check(launchPick(sc->view(), makeCamera(*camera), sx, sy, dev->pickBuf, dev->stream), "pick launch");
+    uint32_t w[8];
+    check(cudaMemcpyAsync(w, dev->pickBuf, sizeof(w), cudaMemcpyDeviceToHost, dev->stream), "pick read");
+    check(cudaStreamSynchronize(dev->stream), "pick sync");
+    res->hasHit = int(w[0]);
+    memcpy(res->worldPosition, w + 1, 12);
+    res->instID = w[4];
+    res->geomID = w[5];
+    res->primID = w[6];
   });
 }
 

@@ -39,6 +39,7 @@ struct DeviceObj {
   FilterLUT luts[5];
   AlbedoTablesD *albedo = nullptr;  // computed at the first path-traced frame
   unsigned int *work = nullptr;     // pixel work counter of the persistent renderers
+  uint32_t *pickBuf = nullptr;      // one pick result (8 words)
   void *ptWs = nullptr;             // path-tracer path/queue workspace
   size_t ptWsBytes = 0;
   explicit DeviceObj(int cudaDev);
@@ -94,16 +95,26 @@ struct SceneObj {
   Scene view() const;
 };
 
+// Tonemapper coefficients after ToneMapper::commit's clamping and solve.
+struct ToneMapD {
+  float exposure, a, b, c, d;
+  int aces;
+};
+
 struct FrameObj {
   DeviceObj *dev;
   int W, H;
+  int format;  // B200_FB_NONE / RGBA8 / SRGBA / RGBA32F
   uint32_t channels;
   int frameID = 0;
+  void *mapped = nullptr;  // converted colour (what ospMapFrameBuffer returns)
+  bool toneMapOn = false;
+  ToneMapD toneMap = {};
   float4 *color = nullptr, *variance = nullptr;
   float *depth = nullptr;
   float3 *normal = nullptr, *albedo = nullptr;
   uint32_t *primID = nullptr, *geomID = nullptr, *instID = nullptr;
-  FrameObj(DeviceObj *d, int w, int h, uint32_t ch);
+  FrameObj(DeviceObj *d, int w, int h, int format, uint32_t ch);
   ~FrameObj();
   FrameD view() const;
   void *channel(uint32_t c) const;
@@ -111,5 +122,9 @@ struct FrameObj {
 };
 
 CameraD makeCamera(const b200_camera_desc &c);
+ToneMapD makeToneMap(const b200_tonemapper &u);
+// tonemap (if set) + conversion of the accumulated colour into fb->mapped,
+// enqueued after every render (LocalFrameBuffer::postProcess)
+void framePostProcess(FrameObj *fb, cudaStream_t st);
 
 }  // namespace b200

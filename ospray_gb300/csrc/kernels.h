@@ -60,6 +60,9 @@ struct AOParamsD {
   float bg[4];
 };
 
+// Renderer_pick: one camera ray at screen (sx, sy), closest hit; out[0] hit,
+// out[1..3] world position bits, out[4..6] instID, geomID, primID.
+cudaError_t launchPick(const Scene &sc, const CameraD &cam, float sx, float sy, uint32_t *out, cudaStream_t st);
 cudaError_t launchTrace(const Scene &sc, const float4 *rays, long long n, int occlusion, float *outF, uint32_t *outI,
                         cudaStream_t st);
 cudaError_t launchRenderAO(const SamplerTables *T, const Scene &sc, const CameraD &cam, const PixelFilterD &pf, const AOParamsD &p,

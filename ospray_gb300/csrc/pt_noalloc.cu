@@ -161,6 +161,11 @@ int b200_render_pt_noalloc(b200_scene s, const b200_camera_desc *camera, const b
                      base + OFF_WORKSPACE, WORKSPACE_BYTES, st);
   if (e != cudaSuccess) return fail(B200_UNKNOWN_ERROR, std::string("path tracer launch: ") + cudaGetErrorString(e));
   fb->frameID++;
+  try {
+    framePostProcess(fb, st);
+  } catch (const Error &er) {
+    return fail(er.code, er.what());
+  }
   return B200_NO_ERROR;
 }
 

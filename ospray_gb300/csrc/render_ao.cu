@@ -162,6 +162,37 @@ cudaError_t launchTrace(const Scene &sc, const float4 *rays, long long n, int oc
   return cudaGetLastError();
 }
 
+// Renderer_pick (render/Renderer.ispc:43-95): the camera ray at the screen
+// position with the lens centre, no depth limit, closest hit; the position is
+// org + dir * t.  One warp is launched so the warp-cooperative traversal has
+// its usual shape; lane 0 carries the ray.
+__global__ void k_pick(Scene sc, CameraD cam, float sx, float sy, uint32_t *out) {
+  const bool active = threadIdx.x == 0;
+  Ray r = cameraRay(cam, sx, sy);
+  HitRec h;
+  bool hit = false;
+  if (active) hit = traceScene<false>(sc, r, h);
+  if (!active) return;
+  out[0] = hit ? 1u : 0u;
+  if (hit) {
+    const V3 p = add(r.org, mul(r.dir, h.t));
+    out[1] = __float_as_uint(p.x);
+    out[2] = __float_as_uint(p.y);
+    out[3] = __float_as_uint(p.z);
+    out[4] = h.instID;
+    out[5] = h.geomID;
+    out[6] = h.primID;
+  } else {
+    out[1] = out[2] = out[3] = 0u;
+    out[4] = out[5] = out[6] = INVALID_ID;
+  }
+}
+
+cudaError_t launchPick(const Scene &sc, const CameraD &cam, float sx, float sy, uint32_t *out, cudaStream_t st) {
+  k_pick<<<1, 32, TRACE_SMEM_BYTES, st>>>(sc, cam, sx, sy, out);
+  return cudaGetLastError();
+}
+
 cudaError_t launchRenderAO(const SamplerTables *T, const Scene &sc, const CameraD &cam, const PixelFilterD &pf, const AOParamsD &p,
                            const FrameD &fb, bool stats, cudaStream_t st) {
   dim3 grid((fb.W + 15) / 16, (fb.H + 7) / 8);

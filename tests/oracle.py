@@ -25,6 +25,40 @@ class OrFrame(ctypes.Structure):
     _fields_ = [("color", P), ("depth", P), ("primID", P), ("geomID", P), ("instID", P)]
 
 
+class OrToneMapper(ctypes.Structure):
+    _fields_ = [("exposure", F), ("contrast", F), ("shoulder", F), ("midIn", F), ("midOut", F), ("hdrMax", F),
+                ("acesColor", I)]
+
+
+def tonemapper(exposure=1.0, contrast=1.6773, shoulder=0.9714, mid_in=0.18, mid_out=0.18, hdr_max=11.0785,
+               aces_color=True):
+    """ToneMapper parameters with the reference's defaults (fb/frame_ops/ToneMapper.cpp:18-36)."""
+    return OrToneMapper(exposure, contrast, shoulder, mid_in, mid_out, hdr_max, int(aces_color))
+
+
+def frame_post(color, fmt, tm=None):
+    """Tonemap (tm or None) + colour conversion of an (h,w,4) float32 image.
+    fmt 1 RGBA8 / 2 SRGBA -> (h,w,4) uint8; 3 RGBA32F -> (h,w,4) float32."""
+    c = np.ascontiguousarray(color, np.float32)
+    n = c.shape[0] * c.shape[1]
+    out = np.zeros(c.shape, np.float32 if fmt == 3 else np.uint8)
+    lib().or_frame_post(_p(c), n, fmt, ctypes.byref(tm) if tm is not None else None, _p(out))
+    return out
+
+
+def tonemap_coefficients(tm):
+    out = np.zeros(5, np.float32)
+    lib().or_tonemap_coefficients(ctypes.byref(tm), _p(out))
+    return dict(zip(("exposure", "a", "b", "c", "d"), out.tolist()))
+
+
+def pick(scene, cam, x, y):
+    pos = np.zeros(3, np.float32)
+    ids = np.zeros(3, np.uint32)
+    hit = lib().or_pick(scene.h, ctypes.byref(cam), float(x), float(y), _p(pos), _p(ids))
+    return bool(hit), pos, ids
+
+
 class OrPtParams(ctypes.Structure):
     _fields_ = [("spp", I), ("maxPathLength", I), ("roulettePathLength", I), ("maxScatteringEvents", I),
                 ("lightSamples", I), ("limitIndirectLightSamples", I), ("minContribution", F),
@@ -115,6 +149,10 @@ def lib():
         L.or_render_ao.argtypes = [P, ctypes.POINTER(OrCamera), I, I, I, I, I, F, F, P, I,
                                    ctypes.POINTER(OrFrame), I]
         L.or_tables.argtypes = [P, P, P, P]
+        L.or_frame_post.argtypes = [P, ctypes.c_longlong, I, ctypes.POINTER(OrToneMapper), P]
+        L.or_tonemap_coefficients.argtypes = [ctypes.POINTER(OrToneMapper), P]
+        L.or_pick.restype = I
+        L.or_pick.argtypes = [P, ctypes.POINTER(OrCamera), F, F, P, P]
         _lib = L
     return _lib
 

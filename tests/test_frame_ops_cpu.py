@@ -1,0 +1,60 @@
+"""Oracle checks for the framebuffer post-processing (no GPU).
+
+The tonemapper's commit solves b and c so that the curve maps midIn to midOut
+and hdrMax to 1 (fb/frame_ops/ToneMapper.cpp:38-50); the colour conversions
+have closed-form known answers (unorm rounding, the sRGB curve)."""
+import numpy as np
+
+import oracle
+
+
+def _curve(co, x):
+    a, b, c, d = (np.float64(co[k]) for k in "abcd")
+    return x ** a / (x ** (a * d) * b + c)
+
+
+def test_tonemap_coefficients_hit_the_anchor_points():
+    for kw in ({}, dict(contrast=1.2, shoulder=0.8, mid_in=0.25, mid_out=0.2, hdr_max=6.0),
+               dict(contrast=2.5, shoulder=1.0, mid_in=0.1, mid_out=0.3, hdr_max=30.0)):
+        tm = oracle.tonemapper(**kw)
+        co = oracle.tonemap_coefficients(tm)
+        assert abs(_curve(co, np.float64(tm.midIn)) - tm.midOut) < 2e-5 * max(1.0, tm.midOut), kw
+        assert abs(_curve(co, np.float64(tm.hdrMax)) - 1.0) < 2e-5, kw
+        assert co["c"] >= 0.0
+
+
+def test_tonemap_parameter_clamping():
+    co = oracle.tonemap_coefficients(oracle.tonemapper(contrast=-3.0, shoulder=5.0))
+    assert np.float32(co["a"]) == np.float32(0.0001)
+    assert co["d"] == 1.0
+
+
+def test_color_conversion_known_answers():
+    img = np.array([[[0.0, 0.5, 1.0, 1.0], [2.0, -1.0, 0.25, 0.5], [0.0031308, 0.04, 0.2, 3.0]]], np.float32)
+    rgba8 = oracle.frame_post(img, 1)
+    # 255 * 0.5 = 127.5 rounds to even (128), 255 * 0.25 = 63.75 -> 64
+    np.testing.assert_array_equal(rgba8[0, 0], [0, 128, 255, 255])
+    np.testing.assert_array_equal(rgba8[0, 1], [255, 0, 64, 128])
+    srgb = oracle.frame_post(img, 2)
+    # sRGB(0.5) = 1.055 * 0.5^(1/2.4) - 0.055 = 0.7354 -> 255 * 0.7354 = 187.5, truncated
+    assert srgb[0, 0, 1] == 187
+    # the linear segment: 12.92 * 0.0031308 = 0.04045 -> 10.3
+    assert srgb[0, 2, 0] == 10
+    # alpha stays linear: 0.5 -> 127 (truncated), 3.0 -> 255
+    assert srgb[0, 1, 3] == 127 and srgb[0, 2, 3] == 255
+    f32 = oracle.frame_post(img, 3)
+    np.testing.assert_array_equal(f32[0, 1], np.float32([2.0, 0.0, 0.25, 0.5]))
+    assert f32[0, 2, 3] == 1.0  # alpha clamped to 1, colour left HDR
+
+
+def test_tonemapper_is_monotone_and_bounded():
+    x = np.linspace(0.0, 40.0, 4001, dtype=np.float32)
+    img = np.zeros((1, x.size, 4), np.float32)
+    img[0, :, 0] = img[0, :, 1] = img[0, :, 2] = x
+    img[0, :, 3] = 1.0
+    for aces in (False, True):
+        out = oracle.frame_post(img, 3, oracle.tonemapper(aces_color=aces))
+        g = out[0, :, 1]
+        assert np.all(np.diff(g) >= -1e-6)
+        assert g.min() >= 0.0 and g.max() <= 1.0
+        assert np.all(out[0, :, 3] == 1.0)

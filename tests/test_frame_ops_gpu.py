@@ -1,0 +1,112 @@
+"""Framebuffer post-processing and pick on the GPU against the oracle.
+
+Post-processing: a small path-traced frame (HDR colours: the quad light is
+visible) is rendered into framebuffers of each format, with and without the
+tonemapper.  The accumulated colour (ACCUM) is read back and run through the
+oracle's restatement of ToneMapper_kernel + ColorConversion_kernel; the
+mapped COLOR must equal it.  Without the tonemapper and for RGBA8/RGBA32F
+the arithmetic has no transcendental, so the bytes/floats are exact; pow()
+differs between CUDA and the host libm in the last ulp, so tonemapped floats
+agree to 1e-5 relative and converted bytes to 1 unit, on all but a few.
+
+Pick: camera rays at a grid of screen positions over the AO workload; hit
+flag, IDs and the float world position must equal the oracle's bit for
+bit (same camera ray, same intersection arithmetic, same org + t*dir)."""
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+W, H = 96, 64
+
+
+@pytest.fixture(scope="module")
+def pt_world(b200_device):
+    import ospray_gb300 as og
+    from ospray_gb300 import scenes
+    d = scenes.pt_instanced_scene(levels=3, width=W, height=H)
+    g = og.Scene(b200_device)
+    scenes.build_pt_scene(g, d)
+    g.set_lights([og.quad_light(L["position"], L["edge1"], L["edge2"], L["intensity"]) if L["type"] == "quad"
+                  else og.ambient_light(L["intensity"]) for L in d["lights"]])
+    return d, g
+
+
+def _render(b200_device, pt_world, fmt, tm):
+    import ospray_gb300 as og
+    d, g = pt_world
+    c = d["camera"]
+    cam = og.camera_desc(c["position"], c["direction"], c["up"], fovy=c["fovy"], aspect=c["aspect"])
+    fb = og.Frame(b200_device, W, H, og.FB_COLOR | og.FB_ACCUM, format=fmt)
+    if tm is not None:
+        fb.set_tonemapper(og.tonemapper(**tm))
+    og.render_pt(g, cam, og.pt_params(spp=2, max_path_length=4), og.materials_array(d["materials"]), fb)
+    return fb.read(og.FB_ACCUM), fb.read(og.FB_COLOR)
+
+
+TM = dict(exposure=2.0)
+TM_ORACLE = dict(exposure=2.0)
+
+
+@pytest.mark.parametrize("fmt", [1, 2, 3])
+@pytest.mark.parametrize("tonemap", [False, True])
+def test_post_process_matches_oracle(b200_device, pt_world, fmt, tonemap):
+    accum, color = _render(b200_device, pt_world, fmt, TM if tonemap else None)
+    assert accum.max() > 1.0  # HDR input: the light is in view
+    ref = oracle.frame_post(accum, fmt, oracle.tonemapper(**TM_ORACLE) if tonemap else None)
+    assert color.shape == ref.shape and color.dtype == ref.dtype
+    if fmt == 3:
+        if tonemap:
+            np.testing.assert_allclose(color, ref, rtol=1e-5, atol=1e-6)
+            assert color[..., :3].max() <= 1.0
+        else:
+            np.testing.assert_array_equal(color, ref)
+    else:
+        diff = np.abs(color.astype(np.int32) - ref.astype(np.int32))
+        if fmt == 1 and not tonemap:
+            assert diff.max() == 0
+        else:
+            assert diff.max() <= 1
+            assert np.mean(diff > 0) < 0.01
+
+
+def test_tonemapper_removed_restores_plain_conversion(b200_device, pt_world):
+    import ospray_gb300 as og
+    d, g = pt_world
+    c = d["camera"]
+    cam = og.camera_desc(c["position"], c["direction"], c["up"], fovy=c["fovy"], aspect=c["aspect"])
+    fb = og.Frame(b200_device, W, H, og.FB_COLOR | og.FB_ACCUM, format=og.FB_RGBA8)
+    fb.set_tonemapper(og.tonemapper())
+    p = og.pt_params(spp=1, max_path_length=3)
+    og.render_pt(g, cam, p, og.materials_array(d["materials"]), fb)
+    fb.set_tonemapper(None)
+    og.render_pt(g, cam, p, og.materials_array(d["materials"]), fb)
+    np.testing.assert_array_equal(fb.read(og.FB_COLOR), oracle.frame_post(fb.read(og.FB_ACCUM), 1))
+
+
+def test_pick_matches_oracle(b200_device):
+    import ospray_gb300 as og
+    from ospray_gb300 import scenes
+    d = scenes.ao_heightfield_scene()
+    g = og.Scene(b200_device)
+    scenes.build_ao_scene(g, d)
+    o = oracle.Scene()
+    scenes.build_ao_scene(o, d)
+    c = d["camera"]
+    cam = og.camera_desc(c["position"], c["direction"], c["up"])
+    ocam = oracle.camera(c["position"], c["direction"], c["up"])
+    hits = 0
+    for y in np.linspace(0.0, 1.0, 13):
+        for x in np.linspace(0.0, 1.0, 13):
+            hit, pos, inst, geom, prim = og.pick(g, cam, x, y)
+            rhit, rpos, rids = oracle.pick(o, ocam, x, y)
+            assert hit == rhit, (x, y)
+            assert (inst, geom, prim) == tuple(int(v) for v in rids), (x, y)
+            if hit:
+                hits += 1
+                np.testing.assert_array_equal(np.float32(pos), rpos)
+            else:
+                assert (inst, geom, prim) == (0xffffffff,) * 3
+    assert 20 < hits < 169  # both hits and misses (sky) were picked
