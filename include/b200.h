@@ -49,6 +49,20 @@ const char *b200_device_last_error(b200_device dev);
 void *b200_device_stream(b200_device dev);
 int b200_device_sync(b200_device dev);
 
+/* ---- completion events on the device stream: what an OSPFuture waits on
+ *      (ospRenderFrame / ospIsReady / ospWait / ospGetTaskDuration,
+ *      ospray/include/ospray/ospray.h:315-336; the reference's future is a
+ *      task-system future, render/RenderingFuture.h:55-87).  An event marks
+ *      the point of the stream where it was recorded. */
+typedef struct b200_event_t *b200_event;
+int b200_event_record(b200_device dev, b200_event *out);
+/* 1 when all work before the event has finished, 0 if not, < 0 on error */
+int b200_event_query(b200_event ev);
+int b200_event_wait(b200_event ev);
+/* milliseconds between two completed events of one device */
+float b200_event_elapsed_ms(b200_event start, b200_event end);
+int b200_event_release(b200_event ev);
+
 /* ---- world: geometry upload and acceleration-structure build
  *      (Mesh::commit modules/cpu/geometry/Mesh.cpp:37-204,
  *       Spheres::commit geometry/Spheres.cpp:46-106,

@@ -3,7 +3,9 @@
     python -m ospray_gb300.build          # or __graft_entry__.build()
 
 Outputs go to ospray_gb300/_build/ (git-ignored): libb200.so (the C ABI of
-include/b200.h) and libb200_scenes.so (seeded synthetic scene generators).
+include/b200.h), libospray.so + libospray_module_b200.so (the OSPRay C API of
+include/ospray/ospray.h over it, with the "b200" device module) and
+libb200_scenes.so (seeded synthetic scene generators).
 Translation units are compiled in parallel; a unit is rebuilt only when it or
 a header it may include is newer than its object file.
 """
@@ -33,9 +35,14 @@ def nvcc():
     raise RuntimeError("nvcc not found")
 
 
+OSP = os.path.join(CSRC, "osp")
+OSP_MODULE_UNITS = ["objects.cpp", "scene_objects.cpp", "b200_device.cpp"]
+CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall", "-Wno-unused-function"]
+
+
 def _newest_header():
     t = 0.0
-    for d in (CSRC, os.path.join(ROOT, "include")):
+    for d in (CSRC, OSP, os.path.join(ROOT, "include"), os.path.join(ROOT, "include", "ospray")):
         for f in os.listdir(d):
             if f.endswith((".h", ".cuh")):
                 t = max(t, os.path.getmtime(os.path.join(d, f)))
@@ -68,11 +75,31 @@ def build(verbose=False):
     lib = os.path.join(OUT, "libb200.so")
     if jobs or not os.path.exists(lib):
         _run([nv] + ARCH + ["-shared", "-o", lib] + objs)
+    _build_ospray(hdr)
     scenes = os.path.join(OUT, "libb200_scenes.so")
     src = os.path.join(CSRC, "scenegen.cpp")
     if not os.path.exists(scenes) or os.path.getmtime(scenes) < os.path.getmtime(src):
         _run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-o", scenes, src, "-lpthread"])
     return lib
+
+
+def _stale(out, srcs, hdr):
+    if not os.path.exists(out):
+        return True
+    return os.path.getmtime(out) < max([hdr] + [os.path.getmtime(s) for s in srcs])
+
+
+def _build_ospray(hdr):
+    """libospray.so (API entry points) and libospray_module_b200.so (the device)."""
+    api = os.path.join(OUT, "libospray.so")
+    mod = os.path.join(OUT, "libospray_module_b200.so")
+    api_src = [os.path.join(OSP, "api.cpp")]
+    if _stale(api, api_src, hdr):
+        _run(["g++"] + CXX_FLAGS + ["-shared", "-Wl,-soname,libospray.so", "-o", api] + api_src + ["-ldl"])
+    mod_src = [os.path.join(OSP, u) for u in OSP_MODULE_UNITS]
+    if _stale(mod, mod_src + [os.path.join(OUT, "libb200.so"), api], hdr):
+        _run(["g++"] + CXX_FLAGS + ["-shared", "-o", mod] + mod_src +
+             ["-L" + OUT, "-lb200", "-lospray", "-Wl,-rpath,$ORIGIN"])
 
 
 if __name__ == "__main__":

@@ -855,6 +855,65 @@ int b200_render_scivis(b200_scene s, const b200_camera_desc *camera, const b200_
   });
 }
 
+namespace {
+struct EventObj {
+  DeviceObj *dev;
+  cudaEvent_t ev = nullptr;
+};
+}  // namespace
+
+int b200_event_record(b200_device d, b200_event *out) {
+  if (!d || !out) return B200_INVALID_ARGUMENT;
+  DeviceObj *dev = reinterpret_cast<DeviceObj *>(d);
+  return guarded(dev, [&]() {
+    EventObj *e = new EventObj{dev};
+    if (cudaEventCreate(&e->ev) != cudaSuccess || cudaEventRecord(e->ev, dev->stream) != cudaSuccess) {
+      if (e->ev) cudaEventDestroy(e->ev);
+      delete e;
+      throw Error(B200_UNKNOWN_ERROR, "cannot record a CUDA event");
+    }
+    dev->retain();
+    *out = reinterpret_cast<b200_event>(e);
+  });
+}
+
+int b200_event_query(b200_event h) {
+  if (!h) return -B200_INVALID_ARGUMENT;
+  EventObj *e = reinterpret_cast<EventObj *>(h);
+  cudaSetDevice(e->dev->dev);
+  const cudaError_t r = cudaEventQuery(e->ev);
+  if (r == cudaSuccess) return 1;
+  if (r == cudaErrorNotReady) return 0;
+  e->dev->lastError = std::string("event query: ") + cudaGetErrorString(r);
+  return -B200_UNKNOWN_ERROR;
+}
+
+int b200_event_wait(b200_event h) {
+  if (!h) return B200_INVALID_ARGUMENT;
+  EventObj *e = reinterpret_cast<EventObj *>(h);
+  return guarded(e->dev, [&]() { check(cudaEventSynchronize(e->ev), "event wait"); });
+}
+
+float b200_event_elapsed_ms(b200_event a, b200_event b) {
+  if (!a || !b) return 0.f;
+  EventObj *ea = reinterpret_cast<EventObj *>(a), *eb = reinterpret_cast<EventObj *>(b);
+  float ms = 0.f;
+  cudaSetDevice(ea->dev->dev);
+  if (cudaEventElapsedTime(&ms, ea->ev, eb->ev) != cudaSuccess) return 0.f;
+  return ms;
+}
+
+int b200_event_release(b200_event h) {
+  if (!h) return B200_INVALID_ARGUMENT;
+  EventObj *e = reinterpret_cast<EventObj *>(h);
+  cudaSetDevice(e->dev->dev);
+  cudaEventDestroy(e->ev);
+  DeviceObj *dev = e->dev;
+  delete e;
+  dev->release();
+  return B200_NO_ERROR;
+}
+
 int b200_pick(b200_scene s, const b200_camera_desc *camera, float sx, float sy, b200_pick_result *res) {
   if (!s || !camera || !res) return B200_INVALID_ARGUMENT;
   SceneObj *sc = reinterpret_cast<SceneObj *>(s);

@@ -1,0 +1,430 @@
+// commit() of the b200 OSPRay device's scene objects.
+#include "scene_objects.h"
+
+#include <cmath>
+#include <map>
+
+#include "b200_device.h"
+
+namespace b200osp {
+
+namespace {
+const float kZero3[3] = {0.f, 0.f, 0.f};
+const float kOne3[3] = {1.f, 1.f, 1.f};
+
+template <class T>
+std::vector<Ref<T>> objectList(DataObj *d, OSPDataType kind, const char *what) {
+  std::vector<Ref<T>> out;
+  if (!d) return out;
+  if (d->elem != kind) throw Error(OSP_INVALID_ARGUMENT, std::string(what) + ": data array of the wrong object type");
+  for (uint64_t i = 0; i < d->count(); i++) {
+    Obj *o = d->object(i);
+    if (!o) throw Error(OSP_INVALID_ARGUMENT, std::string(what) + ": null element");
+    out.push_back(Ref<T>(static_cast<T *>(o)));
+  }
+  return out;
+}
+
+float length3(const float v[3]) { return std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]); }
+}  // namespace
+
+// ---------------------------------------------------------------- geometry
+
+void GeometryObj::commit(B200Device &) {
+  verts.clear();
+  index.clear();
+  spheres.clear();
+  if (type == "mesh") {
+    DataObj *v = getData("vertex.position");
+    DataObj *ix = getData("index");
+    if (!v || v->elem != OSP_VEC3F) throw Error(OSP_INVALID_ARGUMENT, "mesh: 'vertex.position' must be vec3f data");
+    const auto vb = v->compact();
+    verts.resize(v->count() * 3);
+    std::memcpy(verts.data(), vb.data(), vb.size());
+    if (!ix) throw Error(OSP_INVALID_ARGUMENT, "mesh: 'index' data is required");
+    if (ix->elem == OSP_VEC4UI || ix->elem == OSP_VEC4I)
+      throw Error(OSP_INVALID_ARGUMENT, "mesh: quad indices (vec4ui) are not supported by the b200 device");
+    if (ix->elem != OSP_VEC3UI && ix->elem != OSP_VEC3I)
+      throw Error(OSP_INVALID_ARGUMENT, "mesh: 'index' must be vec3ui data");
+    const auto ib = ix->compact();
+    index.resize(ix->count() * 3);
+    std::memcpy(index.data(), ib.data(), ib.size());
+    for (uint32_t i : index)
+      if (i >= v->count()) throw Error(OSP_INVALID_ARGUMENT, "mesh: index out of range of 'vertex.position'");
+  } else {  // sphere
+    DataObj *p = getData("sphere.position");
+    if (!p || p->elem != OSP_VEC3F) throw Error(OSP_INVALID_ARGUMENT, "sphere: 'sphere.position' must be vec3f data");
+    DataObj *r = getData("sphere.radius");
+    const float radius = getFloat("radius", 0.01f);
+    std::vector<float> radii;
+    if (r) {
+      radii = r->toFloats();
+      if (radii.size() != p->count()) throw Error(OSP_INVALID_ARGUMENT, "sphere: 'sphere.radius' size differs");
+    }
+    const auto pb = p->compact();
+    spheres.resize(p->count() * 4);
+    for (uint64_t i = 0; i < p->count(); i++) {
+      std::memcpy(&spheres[4 * i], pb.data() + 12 * i, 12);
+      spheres[4 * i + 3] = r ? radii[i] : radius;
+    }
+  }
+}
+
+void GeometryObj::bounds(float lo[3], float hi[3]) const {
+  for (int k = 0; k < 3; k++) {
+    lo[k] = INFINITY;
+    hi[k] = -INFINITY;
+  }
+  if (type == "mesh") {
+    for (uint32_t i : index)
+      for (int k = 0; k < 3; k++) {
+        lo[k] = std::fmin(lo[k], verts[3 * i + k]);
+        hi[k] = std::fmax(hi[k], verts[3 * i + k]);
+      }
+  } else {
+    for (size_t i = 0; 4 * i < spheres.size(); i++)
+      for (int k = 0; k < 3; k++) {
+        lo[k] = std::fmin(lo[k], spheres[4 * i + k] - spheres[4 * i + 3]);
+        hi[k] = std::fmax(hi[k], spheres[4 * i + k] + spheres[4 * i + 3]);
+      }
+  }
+}
+
+// ---------------------------------------------------------------- materials
+
+void MaterialObj::commit(B200Device &dev) {
+  if (type == "principled") {
+    const float def[3] = {0.8f, 0.8f, 0.8f};
+    getVec3("baseColor", mat.baseColor, def);
+    mat.roughness = getFloat("roughness", 0.f);
+    mat.metallic = getFloat("metallic", 0.f);
+    // parameters of the principled model the GB300 path tracer does not
+    // evaluate: accepted at their defaults, reported otherwise
+    struct Def {
+      const char *name;
+      float value;
+    };
+    static const Def fixed[] = {{"specular", 1.f}, {"ior", 1.f},      {"transmission", 0.f}, {"diffuse", 1.f},
+                                {"anisotropy", 0.f}, {"coat", 0.f},   {"sheen", 0.f},        {"backlight", 0.f},
+                                {"opacity", 1.f},    {"thin", 0.f}};
+    for (const Def &d : fixed)
+      if (has(d.name) && getFloat(d.name, d.value) != d.value)
+        dev.warn(std::string("principled material: '") + d.name + "' other than " + std::to_string(d.value) +
+                 " is not supported by the b200 device; using the default");
+  } else {  // obj: Lambertian kd (the OBJ model with its default ks = 0, d = 1)
+    const float def[3] = {0.8f, 0.8f, 0.8f};
+    getVec3("kd", mat.baseColor, def);
+    mat.roughness = 0.f;
+    mat.metallic = 0.f;
+    float ks[3];
+    getVec3("ks", ks, kZero3);
+    if (ks[0] != 0.f || ks[1] != 0.f || ks[2] != 0.f)
+      dev.warn("obj material: specular 'ks' is not supported by the b200 device; rendered diffuse only");
+    if (getFloat("d", 1.f) != 1.f) dev.warn("obj material: 'd' < 1 (transparency) is not supported by the b200 device");
+  }
+}
+
+void GeometricModelObj::commit(B200Device &) {
+  geometry = Ref<GeometryObj>(static_cast<GeometryObj *>(getObject("geometry", OSP_GEOMETRY)));
+  if (!geometry) throw Error(OSP_INVALID_ARGUMENT, "geometric model without geometry");
+  material = Ref<MaterialObj>();
+  materialIndex = -1;
+  const Param *p = find("material");
+  if (p) {
+    if (p->obj && p->obj->kind == OSP_MATERIAL) {
+      material = Ref<MaterialObj>(static_cast<MaterialObj *>(p->obj));
+    } else if (p->obj && p->obj->kind == OSP_DATA) {
+      DataObj *d = static_cast<DataObj *>(p->obj);
+      if (d->count() != 1)
+        throw Error(OSP_INVALID_ARGUMENT, "geometric model: per-primitive materials are not supported by the b200 device");
+      if (d->elem == OSP_MATERIAL)
+        material = Ref<MaterialObj>(static_cast<MaterialObj *>(d->object(0)));
+      else if (d->elem == OSP_UINT || d->elem == OSP_INT)
+        std::memcpy(&materialIndex, d->at(0), 4);
+      else
+        throw Error(OSP_INVALID_ARGUMENT, "geometric model: 'material' data of an unsupported type");
+    } else {
+      materialIndex = getInt("material", -1);
+    }
+  }
+}
+
+// ---------------------------------------------------------------- volumes
+
+void VolumeObj::commit(B200Device &dev) {
+  DataObj *d = getData("data");
+  if (!d) throw Error(OSP_INVALID_ARGUMENT, "structuredRegular volume: 'data' is required");
+  for (int k = 0; k < 3; k++) dims[k] = int(d->n[k]);
+  voxels = d->toFloats();
+  getVec3("gridOrigin", origin, kZero3);
+  getVec3("gridSpacing", spacing, kOne3);
+  if (getBool("cellCentered", false))
+    dev.warn("structuredRegular volume: cell-centred grids are sampled vertex-centred by the b200 device");
+}
+
+void TransferFunctionObj::commit(B200Device &) {
+  DataObj *c = getData("color");
+  DataObj *o = getData("opacity");
+  if (!c || c->elem != OSP_VEC3F) throw Error(OSP_INVALID_ARGUMENT, "piecewiseLinear: 'color' must be vec3f data");
+  if (!o) throw Error(OSP_INVALID_ARGUMENT, "piecewiseLinear: 'opacity' data is required");
+  const auto cb = c->compact();
+  color.resize(c->count() * 3);
+  std::memcpy(color.data(), cb.data(), cb.size());
+  opacity = o->toFloats();
+  if (!getBox1("value", range) && !getBox1("valueRange", range)) {
+    range[0] = 0.f;
+    range[1] = 1.f;
+  }
+}
+
+void VolumetricModelObj::commit(B200Device &dev) {
+  volume = Ref<VolumeObj>(static_cast<VolumeObj *>(getObject("volume", OSP_VOLUME)));
+  tf = Ref<TransferFunctionObj>(static_cast<TransferFunctionObj *>(getObject("transferFunction", OSP_TRANSFER_FUNCTION)));
+  if (!volume || !tf) throw Error(OSP_INVALID_ARGUMENT, "volumetric model needs 'volume' and 'transferFunction'");
+  densityScale = getFloat("densityScale", 1.f);
+  if (getFloat("gradientShadingScale", 0.f) != 0.f)
+    dev.warn("volumetric model: gradient shading is not supported by the b200 device");
+}
+
+// ---------------------------------------------------------------- hierarchy
+
+void GroupObj::commit(B200Device &dev) {
+  models = objectList<GeometricModelObj>(getData("geometry"), OSP_GEOMETRIC_MODEL, "group 'geometry'");
+  volumes = objectList<VolumetricModelObj>(getData("volume"), OSP_VOLUMETRIC_MODEL, "group 'volume'");
+  if (getData("light")) dev.warn("group lights are not supported by the b200 device; put lights on the world");
+}
+
+void InstanceObj::commit(B200Device &) {
+  group = Ref<GroupObj>(static_cast<GroupObj *>(getObject("group", OSP_GROUP)));
+  if (!group) throw Error(OSP_INVALID_ARGUMENT, "instance without a group");
+  float a[12];  // OSP_AFFINE3F: l.vx, l.vy, l.vz, p
+  identity = true;
+  if (getAffine("transform", a) || getAffine("xfm", a)) {
+    for (int r = 0; r < 3; r++) {
+      xfm[4 * r + 0] = a[0 + r];
+      xfm[4 * r + 1] = a[3 + r];
+      xfm[4 * r + 2] = a[6 + r];
+      xfm[4 * r + 3] = a[9 + r];
+    }
+    static const float id[12] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0};
+    identity = std::memcmp(xfm, id, sizeof(id)) == 0;
+  }
+}
+
+void LightObj::commit(B200Device &dev) {
+  light.visible = getBool("visible", true) ? 1 : 0;
+  getVec3("color", light.color, kOne3);
+  light.intensity = getFloat("intensity", 1.f);
+  if (type == "quad") {
+    light.type = B200_LIGHT_QUAD;
+    const float e1[3] = {1.f, 0.f, 0.f}, e2[3] = {0.f, 1.f, 0.f};
+    getVec3("position", light.position, kZero3);
+    getVec3("edge1", light.edge1, e1);
+    getVec3("edge2", light.edge2, e2);
+    const int q = getInt("intensityQuantity", OSP_INTENSITY_QUANTITY_RADIANCE);
+    const float c[3] = {light.edge1[1] * light.edge2[2] - light.edge1[2] * light.edge2[1],
+                        light.edge1[2] * light.edge2[0] - light.edge1[0] * light.edge2[2],
+                        light.edge1[0] * light.edge2[1] - light.edge1[1] * light.edge2[0]};
+    const float area = length3(c);
+    if (q == OSP_INTENSITY_QUANTITY_INTENSITY) {
+      light.intensity /= area;
+    } else if (q == OSP_INTENSITY_QUANTITY_POWER) {
+      light.intensity /= float(M_PI) * area;
+    } else if (q != OSP_INTENSITY_QUANTITY_RADIANCE) {
+      dev.warn("quad light: unsupported 'intensityQuantity' value");
+      light.intensity = 0.f;
+    }
+  } else {  // ambient
+    light.type = B200_LIGHT_AMBIENT;
+    const int q = getInt("intensityQuantity", OSP_INTENSITY_QUANTITY_RADIANCE);
+    if (q == OSP_INTENSITY_QUANTITY_IRRADIANCE) {
+      light.intensity /= float(M_PI);
+    } else if (q != OSP_INTENSITY_QUANTITY_RADIANCE) {
+      dev.warn("ambient light: unsupported 'intensityQuantity' value");
+      light.intensity = 0.f;
+    }
+  }
+}
+
+// ---------------------------------------------------------------- world
+
+WorldObj::~WorldObj() {
+  if (scene) b200_scene_release(scene);
+}
+
+void WorldObj::commit(B200Device &dev) {
+  instances = objectList<InstanceObj>(getData("instance"), OSP_INSTANCE, "world 'instance'");
+  const std::vector<Ref<LightObj>> lights = objectList<LightObj>(getData("light"), OSP_LIGHT, "world 'light'");
+
+  b200_scene s = nullptr;
+  dev.check(b200_scene_create(dev.handle(), &s));
+  try {
+    std::map<GeometryObj *, int> geomIndex;
+    std::map<MaterialObj *, int> matIndex;
+    objectMaterials.clear();
+    for (const auto &inst : instances)
+      for (const auto &m : inst->group->models)
+        if (m->material && !matIndex.count(m->material.get())) {
+          matIndex[m->material.get()] = int(objectMaterials.size());
+          objectMaterials.push_back(m->material);
+        }
+    const int K = int(objectMaterials.size());
+    hasGeometry = hasVolume = false;
+    for (size_t i = 0; i < instances.size(); i++) {
+      InstanceObj *inst = instances[i].get();
+      for (size_t j = 0; j < inst->group->models.size(); j++) {
+        GeometricModelObj *m = inst->group->models[j].get();
+        GeometryObj *g = m->geometry.get();
+        auto it = geomIndex.find(g);
+        int gi;
+        if (it == geomIndex.end()) {
+          if (g->type == "mesh")
+            dev.check(b200_scene_add_mesh(s, g->verts.data(), int64_t(g->verts.size() / 3), g->index.data(),
+                                          int64_t(g->index.size() / 3), &gi));
+          else
+            dev.check(b200_scene_add_spheres(s, g->spheres.data(), int64_t(g->spheres.size() / 4), &gi));
+          geomIndex[g] = gi;
+        } else {
+          gi = it->second;
+        }
+        const int mat =
+            m->material ? matIndex[m->material.get()] : (m->materialIndex >= 0 ? K + m->materialIndex : -1);
+        dev.check(b200_scene_add_instance(s, gi, uint32_t(i), uint32_t(j), inst->identity ? nullptr : inst->xfm, mat));
+        hasGeometry = true;
+      }
+      for (const auto &vmr : inst->group->volumes) {
+        VolumetricModelObj *vm = vmr.get();
+        if (hasVolume) {
+          dev.warn("world: the b200 device renders one volumetric model per world; further ones are ignored");
+          continue;
+        }
+        if (!inst->identity) dev.warn("world: instance transforms of volumes are not supported by the b200 device");
+        VolumeObj *v = vm->volume.get();
+        TransferFunctionObj *tf = vm->tf.get();
+        dev.check(b200_scene_set_volume(s, v->voxels.data(), v->dims[0], v->dims[1], v->dims[2], v->origin,
+                                        v->spacing, tf->color.data(), int(tf->color.size() / 3), tf->opacity.data(),
+                                        int(tf->opacity.size()), tf->range, vm->densityScale));
+        hasVolume = true;
+      }
+    }
+    std::vector<b200_light> L;
+    for (const auto &l : lights) L.push_back(l->light);
+    dev.check(b200_scene_set_lights(s, L.data(), int(L.size())));
+    dev.check(b200_scene_commit(s));
+  } catch (...) {
+    b200_scene_release(s);
+    throw;
+  }
+  if (scene) b200_scene_release(scene);
+  scene = s;
+}
+
+// ---------------------------------------------------------------- camera, renderer, image ops
+
+void CameraObj::commit(B200Device &dev) {
+  const float dir[3] = {0.f, 0.f, 1.f}, up[3] = {0.f, 1.f, 0.f};
+  getVec3("position", desc.position, kZero3);
+  getVec3("direction", desc.direction, dir);
+  getVec3("up", desc.up, up);
+  desc.fovy = getFloat("fovy", 60.f);
+  desc.aspect = getFloat("aspect", 1.f);
+  desc.nearClip = getFloat("nearClip", 1e-6f);
+  if (getFloat("apertureRadius", 0.f) != 0.f) dev.warn("perspective camera: depth of field is not supported by the b200 device");
+  if (getInt("stereoMode", OSP_STEREO_NONE) != OSP_STEREO_NONE)
+    dev.warn("perspective camera: stereo is not supported by the b200 device");
+}
+
+void RendererObj::commit(B200Device &) {
+  const int spp = std::max(1, getInt("pixelSamples", 1));
+  const float bg0[4] = {0.f, 0.f, 0.f, 0.f};
+  float bg[4];
+  getColor4("backgroundColor", bg, bg0);
+  const int pf = getInt("pixelFilter", OSP_PIXELFILTER_GAUSS);
+  const int maxDepth = std::max(0, getInt("maxPathLength", 20));
+  const float minContribution = getFloat("minContribution", 0.001f);
+  materials = objectList<MaterialObj>(getData("material"), OSP_MATERIAL, "renderer 'material'");
+  if (type == "ao") {
+    ao.pixelSamples = spp;
+    ao.aoSamples = getInt("aoSamples", 1);
+    ao.aoDistance = getFloat("aoDistance", getFloat("aoRadius", 1e20f));
+    ao.aoIntensity = getFloat("aoIntensity", 1.f);
+    std::memcpy(ao.backgroundColor, bg, 16);
+    ao.pixelFilter = pf;
+    ao.collectStats = 0;
+  } else if (type == "pathtracer") {
+    pt.pixelSamples = spp;
+    pt.maxPathLength = maxDepth;
+    pt.roulettePathLength = getInt("roulettePathLength", 5);
+    pt.maxScatteringEvents = getInt("maxScatteringEvents", 20);
+    pt.lightSamples = getInt("lightSamples", -1);
+    pt.limitIndirectLightSamples = getBool("limitIndirectLightSamples", true) ? 1 : 0;
+    pt.minContribution = minContribution;
+    pt.maxContribution = getFloat("maxContribution", INFINITY);
+    std::memcpy(pt.backgroundColor, bg, 16);
+    pt.pixelFilter = pf;
+    pt.collectStats = 0;
+  } else {  // scivis
+    scivis.pixelSamples = spp;
+    scivis.volumeSamplingRate = getFloat("volumeSamplingRate", 1.f);
+    std::memcpy(scivis.backgroundColor, bg, 16);
+    scivis.pixelFilter = pf;
+    scivis.collectStats = 0;
+    getBool("shadows", false);  // inert on volume-only worlds without lights
+    getInt("aoSamples", 0);
+  }
+}
+
+void ImageOpObj::commit(B200Device &) {
+  b200_tonemapper d;
+  b200_tonemapper_defaults(&d);
+  tm.exposure = getFloat("exposure", d.exposure);
+  tm.contrast = getFloat("contrast", d.contrast);
+  tm.shoulder = getFloat("shoulder", d.shoulder);
+  tm.midIn = getFloat("midIn", d.midIn);
+  tm.midOut = getFloat("midOut", d.midOut);
+  tm.hdrMax = getFloat("hdrMax", d.hdrMax);
+  tm.acesColor = getBool("acesColor", d.acesColor != 0) ? 1 : 0;
+}
+
+// ---------------------------------------------------------------- framebuffer
+
+FrameBufferObj::FrameBufferObj(B200Device &dev, int w, int h, OSPFrameBufferFormat fmt, uint32_t ch)
+    : SceneObj(OSP_FRAMEBUFFER, "local"), width(w), height(h), format(fmt), channels(ch) {
+  uint32_t b200ch = B200_FB_COLOR;  // the colour buffer always exists on the device
+  if (ch & OSP_FB_DEPTH) b200ch |= B200_FB_DEPTH;
+  if (ch & OSP_FB_ACCUM) b200ch |= B200_FB_ACCUM;
+  if (ch & OSP_FB_VARIANCE) b200ch |= B200_FB_VARIANCE;
+  if (ch & OSP_FB_NORMAL) b200ch |= B200_FB_NORMAL;
+  if (ch & OSP_FB_ALBEDO) b200ch |= B200_FB_ALBEDO;
+  if (ch & OSP_FB_ID_PRIMITIVE) b200ch |= B200_FB_ID_PRIMITIVE;
+  if (ch & OSP_FB_ID_OBJECT) b200ch |= B200_FB_ID_OBJECT;
+  if (ch & OSP_FB_ID_INSTANCE) b200ch |= B200_FB_ID_INSTANCE;
+  dev.check(b200_frame_create(dev.handle(), w, h, int(fmt), b200ch, &fb));
+}
+
+FrameBufferObj::~FrameBufferObj() {
+  if (fb) b200_frame_release(fb);
+}
+
+void FrameBufferObj::commit(B200Device &dev) {
+  DataObj *ops = getData("imageOperation");
+  const b200_tonemapper *tm = nullptr;
+  if (ops) {
+    if (ops->elem != OSP_IMAGE_OPERATION)
+      throw Error(OSP_INVALID_ARGUMENT, "framebuffer 'imageOperation' must be image-operation data");
+    if (ops->count() > 1) dev.warn("framebuffer: the b200 device applies one tonemapper; further operations ignored");
+    tm = &static_cast<ImageOpObj *>(ops->object(0))->tm;
+  }
+  dev.check(b200_frame_set_tonemapper(fb, tm));
+}
+
+FutureObj::~FutureObj() {
+  if (end) {
+    b200_event_wait(end);
+    b200_event_release(end);
+  }
+  if (start) b200_event_release(start);
+  for (Obj *o : held) o->release();
+}
+
+}  // namespace b200osp

@@ -97,9 +97,9 @@ def test_pick_matches_oracle(b200_device):
     c = d["camera"]
     cam = og.camera_desc(c["position"], c["direction"], c["up"])
     ocam = oracle.camera(c["position"], c["direction"], c["up"])
-    hits = 0
-    for y in np.linspace(0.0, 1.0, 13):
-        for x in np.linspace(0.0, 1.0, 13):
+    hits = misses = 0
+    for y in np.linspace(0.0, 1.0, 21):
+        for x in np.linspace(0.0, 1.0, 21):
             hit, pos, inst, geom, prim = og.pick(g, cam, x, y)
             rhit, rpos, rids = oracle.pick(o, ocam, x, y)
             assert hit == rhit, (x, y)
@@ -108,5 +108,6 @@ def test_pick_matches_oracle(b200_device):
                 hits += 1
                 np.testing.assert_array_equal(np.float32(pos), rpos)
             else:
+                misses += 1
                 assert (inst, geom, prim) == (0xffffffff,) * 3
-    assert 20 < hits < 169  # both hits and misses (sky) were picked
+    assert hits >= 10 and misses >= 10  # both surfaces and the sky were picked

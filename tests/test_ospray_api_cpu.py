@@ -1,0 +1,94 @@
+"""The OSPRay C API layer (libospray.so + libospray_module_b200.so) without a GPU.
+
+* every function include/ospray/ospray.h and ospray_util.h declare is
+  exported, and the module exports ospray_module_init_b200;
+* the module's version check (moduleVersionCheck semantics);
+* an application written against include/ospray compiles and links, and so
+  does the reference's own ospTutorial.c against the reference's headers
+  (when the reference tree is present): the library is a link-compatible
+  drop-in;
+* errors before a device exists come back as codes and messages, not crashes.
+"""
+import ctypes
+import os
+import re
+import shutil
+import subprocess
+
+import pytest
+
+import osp_api
+
+ROOT = osp_api.ROOT
+BUILD = osp_api.BUILD
+INCLUDE = os.path.join(ROOT, "include")
+REF = "/root/reference"
+
+
+def _declared(header):
+    text = open(os.path.join(INCLUDE, "ospray", header)).read()
+    return re.findall(r"OSPRAY_INTERFACE\s+[\w\s\*]*?\b(osp\w+)\s*\(", text)
+
+
+def test_every_declared_function_is_exported():
+    names = _declared("ospray.h") + _declared("ospray_util.h")
+    assert len(names) >= 75
+    lib = ctypes.CDLL(os.path.join(BUILD, "libospray.so"))
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+    mod = ctypes.CDLL(os.path.join(BUILD, "libospray_module_b200.so"))
+    assert hasattr(mod, "ospray_module_init_b200")
+
+
+def test_module_version_check():
+    osp_api.lib()  # the module registers into the loaded libospray.so
+    mod = ctypes.CDLL(os.path.join(BUILD, "libospray_module_b200.so"))
+    init = mod.ospray_module_init_b200
+    init.argtypes = [ctypes.c_int16] * 3
+    init.restype = ctypes.c_int
+    assert init(2, 0, 0) == 6  # OSP_VERSION_MISMATCH
+    assert init(3, 99, 0) == 6
+    assert init(3, 3, 0) == 0
+
+
+def _cc(src, out, incdir):
+    cc = shutil.which("gcc") or shutil.which("cc")
+    r = subprocess.run([cc, "-std=c99", "-Wall", src, "-I", incdir, "-L", BUILD, "-lospray",
+                        "-Wl,-rpath," + BUILD, "-o", out], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    return out
+
+
+def test_application_builds_against_own_headers(tmp_path):
+    exe = _cc(os.path.join(ROOT, "tests", "c", "osp_app.c"), str(tmp_path / "osp_app"), INCLUDE)
+    assert os.path.exists(exe)
+
+
+@pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "apps", "ospTutorial")), reason="reference tree absent")
+def test_reference_tutorial_links_against_this_library(tmp_path):
+    """The reference's unmodified ospTutorial.c, compiled with the reference's
+    own ospray.h, links against this libospray.so (every API symbol it uses
+    resolves)."""
+    exe = _cc(os.path.join(REF, "apps", "ospTutorial", "ospTutorial.c"), str(tmp_path / "ospTutorial"),
+              os.path.join(REF, "ospray", "include"))
+    r = subprocess.run(["ldd", exe], capture_output=True, text=True)
+    assert "libospray.so => " + os.path.join(BUILD, "libospray.so") in r.stdout.replace("\t", "")
+
+
+def test_errors_before_a_device_exists():
+    L = osp_api.lib()
+    assert L.ospGetCurrentDevice() is None
+    assert L.ospNewGeometry(b"mesh") is None
+    assert L.ospDeviceGetLastErrorCode(None) == 3  # OSP_INVALID_OPERATION
+    assert b"not yet initialized" in L.ospDeviceGetLastErrorMsg(None)
+    assert L.ospNewDevice(b"no_such_device_type") is None
+    assert b"no_such_device_type" in L.ospDeviceGetLastErrorMsg(None)
+    assert L.ospLoadModule(b"no_such_module") != 0
+    # creating the b200 device object needs no GPU (the GPU is opened at commit)
+    d = L.ospNewDevice(b"b200")
+    assert d is not None
+    L.ospDeviceRelease(d)
+    # the API's default device type resolves to b200
+    d = L.ospNewDevice(b"cpu")
+    assert d is not None
+    L.ospDeviceRelease(d)

@@ -1,0 +1,146 @@
+"""OSPRay applications on the b200 device, through libospray.so.
+
+* tests/c/osp_app.c (a C99 client of include/ospray, the flow of OSPRay's
+  tutorial: mesh + obj material + ambient light, path tracer, sRGB
+  framebuffer, accumulation, futures, pick) is built and run;
+* the AO workload (height field + spheres) is built with OSPRay API calls
+  from Python (shared data, geometric models, group, instance, world, "ao"
+  renderer, RGBA32F framebuffer with depth and ID channels) and must match
+  the oracle exactly on depth and IDs, like the b200 ABI path does;
+* unsupported object types fail with an error code and message.
+"""
+import ctypes
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+import oracle
+import osp_api
+from osp_api import lib
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def osp_device():
+    L = lib()
+    assert L.ospInit(None, None) == 0, L.ospDeviceGetLastErrorMsg(None)
+    yield L
+    L.ospShutdown()
+
+
+def test_c_application_renders(tmp_path):
+    exe = str(tmp_path / "osp_app")
+    cc = shutil.which("gcc") or shutil.which("cc")
+    r = subprocess.run([cc, "-std=c99", os.path.join(osp_api.ROOT, "tests", "c", "osp_app.c"), "-I",
+                        os.path.join(osp_api.ROOT, "include"), "-L", osp_api.BUILD, "-lospray",
+                        "-Wl,-rpath," + osp_api.BUILD, "-o", exe], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([exe, str(tmp_path)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    tok = r.stdout.split()
+    vals = dict(bounds=[float(v) for v in tok[1:7]], hit=int(tok[8]), prim=int(tok[9]), mean0=float(tok[11]),
+                mean10=float(tok[13]), duration=float(tok[15]))
+    np.testing.assert_allclose(vals["bounds"], [-1, -1, 0.3, 1, 1, 3], rtol=1e-6)
+    assert vals["hit"] == 1 and vals["prim"] in (0, 1)
+    assert 20.0 < vals["mean10"] < 255.0 and vals["duration"] > 0.0
+    assert os.path.getsize(tmp_path / "accumulatedFrame.ppm") > 320 * 240 * 3
+
+
+def test_ao_through_ospray_api_matches_oracle(osp_device):
+    from ospray_gb300 import scenes
+    L = osp_device
+    d = scenes.ao_heightfield_scene()
+    keep = []
+    W = H = 256
+    mesh = L.ospNewGeometry(b"mesh")
+    osp_api.set_data(mesh, "vertex.position", d["vertex"].astype(np.float32), osp_api.OSP_VEC3F,
+                     len(d["vertex"]), keep)
+    osp_api.set_data(mesh, "index", d["index"].astype(np.uint32), osp_api.OSP_VEC3UI, len(d["index"]), keep)
+    L.ospCommit(mesh)
+    sph = L.ospNewGeometry(b"sphere")
+    s = np.asarray(d["spheres"], np.float32)
+    osp_api.set_data(sph, "sphere.position", s[:, :3].copy(), osp_api.OSP_VEC3F, len(s), keep)
+    osp_api.set_data(sph, "sphere.radius", s[:, 3].copy(), osp_api.OSP_FLOAT, len(s), keep)
+    L.ospCommit(sph)
+    models = []
+    for g in (mesh, sph):
+        m = L.ospNewGeometricModel(g)
+        L.ospCommit(m)
+        models.append(m)
+        L.ospRelease(g)
+    arr = (ctypes.c_void_p * 2)(*models)
+    md = L.ospNewSharedData(ctypes.addressof(arr), osp_api.OSP_GEOMETRIC_MODEL, 2, 0, 1, 0, 1, 0, None, None)
+    group = L.ospNewGroup()
+    osp_api.set_param(group, "geometry", osp_api.OSP_DATA, md)
+    L.ospRelease(md)
+    for m in models:
+        L.ospRelease(m)
+    L.ospCommit(group)
+    inst = L.ospNewInstance(group)
+    L.ospCommit(inst)
+    L.ospRelease(group)
+    world = L.ospNewWorld()
+    L.ospSetObjectAsData(world, b"instance", osp_api.OSP_INSTANCE, inst)
+    L.ospRelease(inst)
+    L.ospCommit(world)
+    b = L.ospGetBounds(world)
+    assert b.lower[1] < 0.3 and b.upper[0] > 0.9
+
+    c = d["camera"]
+    cam = L.ospNewCamera(b"perspective")
+    osp_api.set_param(cam, "position", osp_api.OSP_VEC3F, np.float32(c["position"]))
+    osp_api.set_param(cam, "direction", osp_api.OSP_VEC3F, np.float32(c["direction"]))
+    osp_api.set_param(cam, "up", osp_api.OSP_VEC3F, np.float32(c["up"]))
+    osp_api.set_param(cam, "fovy", osp_api.OSP_FLOAT, np.float32(c["fovy"]))
+    osp_api.set_param(cam, "aspect", osp_api.OSP_FLOAT, np.float32(1.0))
+    L.ospCommit(cam)
+    ren = L.ospNewRenderer(b"ao")
+    osp_api.set_param(ren, "pixelFilter", osp_api.OSP_UINT, np.uint32(0))
+    osp_api.set_param(ren, "aoSamples", osp_api.OSP_INT, np.int32(1))
+    L.ospCommit(ren)
+    ch = osp_api.OSP_FB_COLOR | osp_api.OSP_FB_DEPTH | osp_api.OSP_FB_ACCUM | osp_api.OSP_FB_ID_PRIMITIVE | \
+        osp_api.OSP_FB_ID_OBJECT | osp_api.OSP_FB_ID_INSTANCE
+    fb = L.ospNewFrameBuffer(W, H, osp_api.OSP_FB_RGBA32F, ch)
+    fut = L.ospRenderFrame(fb, ren, cam, world)
+    L.ospWait(fut, osp_api.OSP_TASK_FINISHED)
+    assert L.ospIsReady(fut, osp_api.OSP_TASK_FINISHED) == 1
+    L.ospRelease(fut)
+    color = osp_api.map_channel(fb, osp_api.OSP_FB_COLOR, (H, W, 4), np.float32)
+    depth = osp_api.map_channel(fb, osp_api.OSP_FB_DEPTH, (H, W), np.float32)
+    ids = [osp_api.map_channel(fb, ch, (H, W), np.uint32) for ch in
+           (osp_api.OSP_FB_ID_PRIMITIVE, osp_api.OSP_FB_ID_OBJECT, osp_api.OSP_FB_ID_INSTANCE)]
+
+    o = oracle.Scene()
+    scenes.build_ao_scene(o, d)
+    ref = oracle.render_ao(o, oracle.camera(c["position"], c["direction"], c["up"]), 0, W, H)
+    assert np.mean(depth.view(np.uint32) == ref["depth"].view(np.uint32)) >= 0.9999
+    for got, key in zip(ids, ("primID", "geomID", "instID")):
+        assert np.mean(got == ref[key]) >= 0.9999, key
+    assert np.mean(np.all(color == ref["color"], axis=2)) >= 0.999
+    assert {0, 1} <= set(np.unique(ids[1]).tolist())  # both geometric models seen
+
+    res = osp_api.OSPPickResult()
+    L.ospPick(ctypes.byref(res), fb, ren, cam, world, 0.5, 0.5)
+    rhit, rpos, rids = oracle.pick(o, oracle.camera(c["position"], c["direction"], c["up"]), 0.5, 0.5)
+    assert bool(res.hasHit) == rhit
+    if rhit:
+        assert res.primID == rids[2] and res.model and res.instance
+        np.testing.assert_array_equal(np.float32(list(res.worldPosition)), rpos)
+        L.ospRelease(res.model)
+        L.ospRelease(res.instance)
+    for h in (fb, ren, cam, world):
+        L.ospRelease(h)
+
+
+def test_unsupported_types_report_errors(osp_device):
+    L = osp_device
+    dev = L.ospGetCurrentDevice()
+    assert L.ospNewLight(b"spot") is None
+    assert L.ospDeviceGetLastErrorCode(dev) == 2
+    assert b"spot" in L.ospDeviceGetLastErrorMsg(dev)
+    assert L.ospNewCamera(b"orthographic") is None
+    L.ospDeviceRelease(dev)
