@@ -263,6 +263,51 @@ int b200_scene_counters(b200_scene scene, int64_t *out4, int reset);
 int b200_render_ao(b200_scene scene, const b200_camera_desc *camera, const b200_ao_params *params, b200_frame fb,
                    void *stream);
 
+/* ---- batched rendering: many render requests served by one wavefront.
+ * No counterpart in the reference, which renders one frame per
+ * ospRenderFrame call (ISPCDevice::renderFrame, modules/cpu/ISPCDevice.cpp:
+ * 578-595).  A batch holds requests, each a (scene, camera, renderer
+ * parameters, framebuffer) as b200_render_ao / b200_render_pt take them;
+ * b200_batch_render renders one frame of every request: the paths of all
+ * requests share one set of wavefront queues (each ray traverses its own
+ * request's scene), in waves of whole pixels, and each framebuffer
+ * accumulates exactly as the single-request call would (AO: bit-identical;
+ * path tracer: up to the order of the shadow-ray additions).  The launch
+ * sequence is captured once as a CUDA graph and replayed.  Scenes and
+ * framebuffers must outlive the batch; parameters and materials are copied
+ * at the add call.  AO requests trace up to two AO rays per sample through
+ * the shadow queue and further ones in place. */
+typedef struct b200_batch_t *b200_batch;
+int b200_batch_create(b200_device dev, b200_batch *out);
+int b200_batch_release(b200_batch batch);
+int b200_batch_add_ao(b200_batch batch, b200_scene scene, const b200_camera_desc *camera,
+                      const b200_ao_params *params, b200_frame fb);
+int b200_batch_add_pt(b200_batch batch, b200_scene scene, const b200_camera_desc *camera,
+                      const b200_pt_params *params, const b200_material *materials, int nmaterials, b200_frame fb);
+/* launch shape: path slots per wave (the workspace, 264 bytes per slot) and
+ * resident blocks per SM of the persistent trace and shade kernels */
+typedef struct {
+  int64_t wavePaths;
+  int traceBlocksPerSM;
+  int shadeBlocksPerSM;
+} b200_batch_tuning;
+int b200_batch_get_tuning(b200_batch batch, b200_batch_tuning *out);
+int b200_batch_set_tuning(b200_batch batch, const b200_batch_tuning *tuning);
+/* The autotuner: renders the batch once per candidate launch shape (wave
+ * sizes x trace / shade residency), timed with CUDA events after one warm-up
+ * render, and keeps the fastest; `candidates` <= 0 tries the full set.  The
+ * framebuffers are reset afterwards (their accumulation restarts).  The
+ * chosen shape is returned in `best` (may be null). */
+int b200_batch_autotune(b200_batch batch, int candidates, b200_batch_tuning *best);
+/* renders one frame of every request on the device stream; use_graph != 0
+ * launches the captured CUDA graph (captured on first use and after any
+ * change to the requests, the tuning or a framebuffer's post-processing) */
+int b200_batch_render(b200_batch batch, int use_graph);
+/* after a render has finished (b200_device_sync): each request's completion
+ * time in ms after the render began (out n doubles, request order), and the
+ * rays the render traced */
+int b200_batch_timings(b200_batch batch, double *ms, int n, uint64_t *rays);
+
 /* ---- pick (ospPick, ospray/include/ospray/ospray.h:338-352; Renderer::pick
  *      render/Renderer.cpp:94-140, Renderer_pick render/Renderer.ispc:43-95).
  * One camera ray through normalised screen position (x, y) in [0,1]^2

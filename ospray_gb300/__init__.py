@@ -169,6 +169,20 @@ def lib():
             "b200_tonemapper_defaults": (None, [ctypes.POINTER(ToneMapper)]),
             "b200_frame_set_tonemapper": (I, [P, ctypes.POINTER(ToneMapper)]),
             "b200_pick": (I, [P, ctypes.POINTER(CameraDesc), F, F, ctypes.POINTER(PickResult)]),
+            "b200_batch_create": (I, [P, ctypes.POINTER(P)]),
+            "b200_batch_release": (I, [P]),
+            "b200_batch_add_ao": (I, [P, P, ctypes.POINTER(CameraDesc), ctypes.POINTER(AOParams), P]),
+            "b200_batch_add_pt": (I, [P, P, ctypes.POINTER(CameraDesc), ctypes.POINTER(PTParams), P, I, P]),
+            "b200_batch_get_tuning": (I, [P, ctypes.POINTER(BatchTuning)]),
+            "b200_batch_set_tuning": (I, [P, ctypes.POINTER(BatchTuning)]),
+            "b200_batch_autotune": (I, [P, I, ctypes.POINTER(BatchTuning)]),
+            "b200_batch_render": (I, [P, I]),
+            "b200_batch_timings": (I, [P, P, I, ctypes.POINTER(ctypes.c_uint64)]),
+            "b200_event_record": (I, [P, ctypes.POINTER(P)]),
+            "b200_event_query": (I, [P]),
+            "b200_event_wait": (I, [P]),
+            "b200_event_elapsed_ms": (F, [P, P]),
+            "b200_event_release": (I, [P]),
             "b200_frame_release": (I, [P]),
             "b200_frame_reset": (I, [P]),
             "b200_frame_id": (I, [P]),
@@ -411,3 +425,68 @@ def render_pt(scene, camera, params, materials, frame, stream=None):
     scene.device._check(lib().b200_render_pt(scene._h, ctypes.byref(camera), ctypes.byref(params),
                                              ctypes.cast(arr, ctypes.c_void_p), n, frame._h,
                                              ctypes.c_void_p(stream) if stream else None))
+
+
+class BatchTuning(ctypes.Structure):
+    _fields_ = [("wavePaths", ctypes.c_int64), ("traceBlocksPerSM", ctypes.c_int), ("shadeBlocksPerSM", ctypes.c_int)]
+
+
+class Batch:
+    """b200_batch: many render requests served by one wavefront (CUDA graph)."""
+
+    def __init__(self, device):
+        self.device = device
+        self._h = ctypes.c_void_p()
+        self._keep = []
+        self.n = 0
+        device._check(lib().b200_batch_create(device._h, ctypes.byref(self._h)))
+
+    def add_ao(self, scene, camera, params, frame):
+        self.device._check(lib().b200_batch_add_ao(self._h, scene._h, ctypes.byref(camera), ctypes.byref(params),
+                                                   frame._h))
+        self._keep += [scene, frame]
+        self.n += 1
+
+    def add_pt(self, scene, camera, params, materials, frame):
+        arr, n = materials
+        self.device._check(lib().b200_batch_add_pt(self._h, scene._h, ctypes.byref(camera), ctypes.byref(params),
+                                                   ctypes.cast(arr, ctypes.c_void_p), n, frame._h))
+        self._keep += [scene, frame]
+        self.n += 1
+
+    @property
+    def tuning(self):
+        t = BatchTuning()
+        self.device._check(lib().b200_batch_get_tuning(self._h, ctypes.byref(t)))
+        return t
+
+    @tuning.setter
+    def tuning(self, t):
+        self.device._check(lib().b200_batch_set_tuning(self._h, ctypes.byref(t)))
+
+    def autotune(self, candidates=0):
+        t = BatchTuning()
+        self.device._check(lib().b200_batch_autotune(self._h, candidates, ctypes.byref(t)))
+        return t
+
+    def render(self, use_graph=True):
+        self.device._check(lib().b200_batch_render(self._h, int(bool(use_graph))))
+
+    def timings(self):
+        """(per-request completion ms since the render began, rays traced); waits for the device."""
+        self.device.sync()
+        ms = np.zeros(self.n, np.float64)
+        rays = ctypes.c_uint64()
+        self.device._check(lib().b200_batch_timings(self._h, _ptr(ms), self.n, ctypes.byref(rays)))
+        return ms, rays.value
+
+    def release(self):
+        if self._h:
+            lib().b200_batch_release(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.release()
+        except Exception:
+            pass

@@ -170,6 +170,36 @@ PixelFilterD DeviceObj::filter(int type) const {
   return pf;
 }
 
+// PathTracer::commit (render/pathtracer/PathTracer.cpp:29-51): light sample
+// counts (lightSamples < 0: all lights at the first bounce; one after it
+// when limitIndirectLightSamples)
+PtParamsD makePtParams(const b200_pt_params &p, int nl, int nmaterials) {
+  PtParamsD d;
+  d.spp = p.pixelSamples;
+  d.maxPathLength = p.maxPathLength;
+  d.roulettePathLength = p.roulettePathLength;
+  d.maxScatteringEvents = p.maxScatteringEvents;
+  d.nFirst = p.lightSamples >= 0 && nl > 0 ? p.lightSamples : std::min(1024, nl);
+  d.nIndirect = p.limitIndirectLightSamples && d.nFirst >= 1 ? 1 : d.nFirst;
+  if (nl == 0) d.nFirst = d.nIndirect = 0;
+  d.numLights = nl;
+  d.numMaterials = nmaterials;
+  d.minContribution = p.minContribution;
+  d.maxContribution = p.maxContribution;
+  for (int k = 0; k < 4; k++) d.bg[k] = p.backgroundColor[k];
+  return d;
+}
+
+AOParamsD makeAOParams(const b200_ao_params &p) {
+  AOParamsD d;
+  d.spp = p.pixelSamples;
+  d.aoSamples = p.aoSamples;
+  d.aoRadius = p.aoDistance;
+  d.aoIntensity = p.aoIntensity;
+  for (int k = 0; k < 4; k++) d.bg[k] = p.backgroundColor[k];
+  return d;
+}
+
 // PerspectiveCamera::commit without stereo, aperture or motion blur
 CameraD makeCamera(const b200_camera_desc &c) {
   const V3 pos = mk(c.position[0], c.position[1], c.position[2]);
@@ -654,12 +684,7 @@ int b200_render_ao(b200_scene s, const b200_camera_desc *camera, const b200_ao_p
     if (!sc->committed) throw Error(B200_INVALID_OPERATION, "scene not committed");
     require(p->pixelSamples >= 1 && p->aoSamples >= 0, "bad AO parameters");
     require(p->pixelFilter >= B200_PF_POINT && p->pixelFilter <= B200_PF_BLACKMAN_HARRIS, "bad pixel filter");
-    AOParamsD d;
-    d.spp = p->pixelSamples;
-    d.aoSamples = p->aoSamples;
-    d.aoRadius = p->aoDistance;
-    d.aoIntensity = p->aoIntensity;
-    for (int k = 0; k < 4; k++) d.bg[k] = p->backgroundColor[k];
+    const AOParamsD d = makeAOParams(*p);
     cudaStream_t st = stream ? (cudaStream_t)stream : sc->dev->stream;
     check(launchRenderAO(sc->dev->tables, sc->view(), makeCamera(*camera), sc->dev->filter(p->pixelFilter), d,
                          fb->view(), p->collectStats != 0, st),
@@ -746,20 +771,7 @@ int b200_render_pt(b200_scene s, const b200_camera_desc *camera, const b200_pt_p
       sc->lastMaterials.assign(materials, materials + nmaterials);
     }
     sc->nMaterials = nmaterials;
-    PtParamsD d;
-    d.spp = p->pixelSamples;
-    d.maxPathLength = p->maxPathLength;
-    d.roulettePathLength = p->roulettePathLength;
-    d.maxScatteringEvents = p->maxScatteringEvents;
-    const int nl = sc->nLights;
-    d.nFirst = p->lightSamples >= 0 && nl > 0 ? p->lightSamples : std::min(1024, nl);
-    d.nIndirect = p->limitIndirectLightSamples && d.nFirst >= 1 ? 1 : d.nFirst;
-    if (nl == 0) d.nFirst = d.nIndirect = 0;
-    d.numLights = nl;
-    d.numMaterials = nmaterials;
-    d.minContribution = p->minContribution;
-    d.maxContribution = p->maxContribution;
-    for (int k = 0; k < 4; k++) d.bg[k] = p->backgroundColor[k];
+    const PtParamsD d = makePtParams(*p, sc->nLights, nmaterials);
     // path workspace: grown on demand, kept for later frames
     const size_t need = ptWorkspaceBytes((long long)fb->W * fb->H * p->pixelSamples);
     DeviceObj *dev = sc->dev;

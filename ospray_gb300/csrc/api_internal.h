@@ -122,6 +122,8 @@ struct FrameObj {
 };
 
 CameraD makeCamera(const b200_camera_desc &c);
+PtParamsD makePtParams(const b200_pt_params &p, int numLights, int numMaterials);
+AOParamsD makeAOParams(const b200_ao_params &p);
 ToneMapD makeToneMap(const b200_tonemapper &u);
 // tonemap (if set) + conversion of the accumulated colour into fb->mapped,
 // enqueued after every render (LocalFrameBuffer::postProcess)

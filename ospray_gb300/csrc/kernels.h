@@ -1,5 +1,7 @@
 // Launch interface between the host-side C-ABI (api.cu) and the kernels.
 #pragma once
+#include <vector>
+
 #include "pt_bsdf.cuh"
 #include "render_common.cuh"
 
@@ -59,6 +61,50 @@ struct AOParamsD {
   float aoRadius, aoIntensity;
   float bg[4];
 };
+
+// ---- batches: many render requests in one wavefront
+enum BatchKind : int { BATCH_PT = 0, BATCH_AO = 1 };
+
+// one request as the host describes it
+struct BatchReqH {
+  int kind;
+  Scene sc;
+  CameraD cam;
+  PixelFilterD pf;
+  PtParamsD pt;  // BATCH_PT
+  AOParamsD ao;  // BATCH_AO (aoSamples up to 2 go through the shadow queue, more are traced in place)
+  const MaterialD *mats;
+  const LightD *lights;
+  const float *lightCdf;
+  FrameD fb;
+};
+
+// launch shape of the batched wavefront (what the autotuner picks)
+struct BatchTuning {
+  long long wavePaths;  // path slots per wave (workspace size)
+  int traceBlocksPerSM;  // persistent trace grid = SMs x this
+  int shadeBlocksPerSM;
+};
+
+// One wave: a contiguous run of whole pixels of consecutive requests.
+struct BatchWave {
+  int segOffset, nseg;  // its segments in the segment table
+  long long npaths, npix;
+  int maxBounces;       // max path length over its requests (AO: 0)
+  int completeFirst, completeEnd;  // requests whose last pixel is in this wave
+};
+
+// Splits the requests' paths (pixel-major, spp per pixel) into waves of at
+// most wavePaths paths and builds the device tables (requests + segments) in
+// `tables` (host bytes, uploaded by the caller before the waves run).
+void planBatch(const SamplerTables *T, const AlbedoTablesD *AT, const BatchReqH *reqs, int n, long long wavePaths,
+               std::vector<unsigned char> &tables, std::vector<BatchWave> &waves, size_t &segTableOffset);
+// Enqueues one wave: generate, bounces (closest trace, shade, shadow trace),
+// finalize into each request's framebuffer.  dtables = device copy of tables.
+cudaError_t launchBatchWave(const void *dtables, size_t segTableOffset, const BatchWave &w, const BatchTuning &tune,
+                            void *workspace, size_t wsBytes, unsigned long long *rayCount, cudaStream_t st);
+// writes the global timer into stamps[first..end) (request completion times)
+cudaError_t launchStamp(unsigned long long *stamps, int first, int end, cudaStream_t st);
 
 // Renderer_pick: one camera ray at screen (sx, sy), closest hit; out[0] hit,
 // out[1..3] world position bits, out[4..6] instID, geomID, primID.

@@ -49,20 +49,10 @@ template <bool STATS>
 B200_D float computeAO(const SamplerTables *T, const Scene &sc, const DG &dg, int sampleCnt, float aoRadius, int px, int py,
                        uint32_t sid, TraceStats *ts) {
   const uint32_t accumID = sid * uint32_t(sampleCnt);
-  uint32_t t0 = uint32_t(px), t1 = uint32_t(py);
-  tea8(t0, t1);
-  const float rx0 = to_float_unorm(t0), ry0 = to_float_unorm(t1);
-  V3 dx, dy;
-  frame(dg.Ns, dx, dy);
+  const AOBasis B = aoBasis(dg, px, py);
   int hits = 0;
   for (int i = 0; i < sampleCnt; i++) {
-    const float rx = cpRotate(PermHalton_sample5(T, accumID + i), rx0);
-    const float ry = cpRotate(PermHalton_sample7(T, accumID + i), ry0);
-    const float phi = fmul(6.283185307179586f, rx);
-    const float cosT = fsqrt(ry), sinT = fsqrt(fsub(1.f, ry));
-    float sp, cp;
-    sincosf(phi, &sp, &cp);
-    const V3 dir = toWorld(dx, dy, dg.Ns, mk(fmul(cp, sinT), fmul(sp, sinT), cosT));
+    const V3 dir = aoDirection(T, B, dg.Ns, accumID + i);
     if (dot(dir, dg.Ns) < 0.01f) {
       hits++;
       continue;

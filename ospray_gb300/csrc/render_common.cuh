@@ -139,6 +139,35 @@ B200_D void frame(V3 N, V3 &dx, V3 &dy) {
 }
 B200_D V3 toWorld(V3 dx, V3 dy, V3 N, V3 l) { return add(add(mul(dx, l.x), mul(dy, l.y)), mul(N, l.z)); }
 
+// computeAO's sampling (render/util.ispc:12-54): a TEA-hashed Cranley-
+// Patterson rotation per pixel over permuted Halton (bases 5, 7), mapped to a
+// cosine-weighted direction about Ns
+struct AOBasis {
+  V3 dx, dy;
+  float rx0, ry0;
+};
+
+B200_D AOBasis aoBasis(const DG &dg, int px, int py) {
+  AOBasis B;
+  uint32_t t0 = uint32_t(px), t1 = uint32_t(py);
+  tea8(t0, t1);
+  B.rx0 = to_float_unorm(t0);
+  B.ry0 = to_float_unorm(t1);
+  frame(dg.Ns, B.dx, B.dy);
+  return B;
+}
+
+B200_D V3 aoDirection(const SamplerTables *T, const AOBasis &B, V3 Ns, uint32_t index) {
+  const float rx = cpRotate(PermHalton_sample5(T, index), B.rx0);
+  const float ry = cpRotate(PermHalton_sample7(T, index), B.ry0);
+  const float phi = fmul(6.283185307179586f, rx);
+  const float cosT = fsqrt(ry), sinT = fsqrt(fsub(1.f, ry));
+  float sp, cp;
+  sincosf(phi, &sp, &cp);
+  return toWorld(B.dx, B.dy, Ns, mk(fmul(cp, sinT), fmul(sp, sinT), cosT));
+}
+
+
 struct PixelOut {
   float r, g, b, a;
   float z;

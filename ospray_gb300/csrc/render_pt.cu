@@ -1,5 +1,5 @@
-// Path tracer: one thread per pixel runs the reference's samplePath for each
-// of the pixel's samples and accumulates into the framebuffer.
+// Path tracer as a wavefront over device-side path queues, for one frame
+// (launchRenderPT) or a batch of many requests (launchBatchWave), following
 //   PathTracer_renderPixel  render/pathtracer/PathTracer.ispc:75-216
 //   samplePath              render/pathtracer/PathSampler.ispc:109-415
 //   nextEventEstimation     render/pathtracer/NextEventEstimation.ispc:25-160
@@ -7,6 +7,12 @@
 //   transparentShadow       render/pathtracer/TransparentShadow.ispc:18-85
 //     (all materials here are opaque, so a shadow ray is an any-hit query)
 //   misHeuristic            render/pathtracer/PathTracerUtil.ih:30-46
+// and, for AO requests of a batch, AORenderer_renderSample
+// (render/ao/AORenderer.ispc:23-149) with its AO rays in the shadow queue.
+#include <algorithm>
+#include <cstring>
+#include <stdexcept>
+
 #include "kernels.h"
 #include "pt_bsdf.cuh"
 
@@ -246,15 +252,32 @@ struct FrameInfo {
   long long npaths;
 };
 
-__global__ void k_pt_generate(PtCtx c, CameraD cam, PixelFilterD pf, FrameInfo fi, Workspace ws) {
-  const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (p == 0) {
-    ws.counters[0] = uint32_t(fi.npaths);
-    for (int k = 1; k < 8; k++) ws.counters[k] = 0;
-  }
-  if (p >= fi.npaths) return;
-  const int pix = int(p / fi.spp), s = int(p % fi.spp);
-  const int x = pix % fi.W, y = pix / fi.W;
+// a request of a batch, as the kernels read it (device table)
+struct ReqD {
+  PtCtx c;
+  CameraD cam;
+  PixelFilterD pf;
+  FrameInfo fi;
+  FrameD fb;
+  AOParamsD ao;
+  int kind;
+};
+
+// a run of path slots of one wave that belongs to one request
+struct SegD {
+  long long start;     // first path slot in the wave
+  long long first;     // first path of the request (pixel-major)
+  long long pixStart;  // first pixel slot in the wave
+  int rid, pad;
+};
+
+// path flags: AO request hit its first surface
+constexpr uint32_t F_AOHIT = 1u << 11;
+
+// the camera ray of sample s of pixel (x, y) of a path-traced frame, as a
+// fresh path record (meta2: first-hit instID, request, sampleID, pixel)
+B200_D PathRec genPT(const PtCtx &c, const CameraD &cam, const PixelFilterD &pf, const FrameInfo &fi, int x, int y,
+                     int s, uint32_t rid) {
   const uint32_t seed = 0x49c5f37eu ^ uint32_t(fi.W * y + x);
   const uint32_t sampleID = uint32_t(fi.frameID) * uint32_t(fi.spp) + uint32_t(s);
   LDSampler ld;
@@ -269,22 +292,38 @@ __global__ void k_pt_generate(PtCtx c, CameraD cam, PixelFilterD pf, FrameInfo f
   r.dir = make_float4(ray.dir.x, ray.dir.y, ray.dir.z, INFINITY);
   r.thr = make_float4(1.f, 1.f, 1.f, 1.f);
   r.con = make_float4(0.f, 0.f, 0.f, 0.f);
-  r.lastP = make_float4(ray.org.x, ray.org.y, ray.org.z, 0.f);
+  r.lastP = make_float4(ray.org.x, ray.org.y, ray.org.z, ray.tnear);
   r.lastN = make_float4(ray.dir.x, ray.dir.y, ray.dir.z, 0.f);
   r.meta = make_uint4(ld.scramble, F_STRAIGHT | F_FIRST, INVALID_ID, INVALID_ID);
-  r.meta2 = make_uint4(INVALID_ID, 0u, 0u, 0u);
-  ws.paths[p] = r;
+  r.meta2 = make_uint4(INVALID_ID, rid, sampleID, uint32_t(fi.W * y + x));
+  return r;
+}
+
+__global__ void k_pt_generate(PtCtx c, CameraD cam, PixelFilterD pf, FrameInfo fi, Workspace ws) {
+  const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (p == 0) {
+    ws.counters[0] = uint32_t(fi.npaths);
+    for (int k = 1; k < 16; k++) ws.counters[k] = 0;
+  }
+  if (p >= fi.npaths) return;
+  const int pix = int(p / fi.spp), s = int(p % fi.spp);
+  ws.paths[p] = genPT(c, cam, pf, fi, pix % fi.W, pix / fi.W, s, 0u);
 }
 
 // Persistent any/closest-hit tracing over a queue with per-lane dynamic
 // fetch: whenever lanes of a warp finish their rays, the warp takes that many
 // new ones with one atomic, so no lane idles while work remains.
-template <bool SHADOW, bool STATS>
+// In a batch (BATCH) every ray traverses its own request's scene.
+template <bool SHADOW, bool STATS, bool BATCH>
 __global__ void __launch_bounds__(TRACE_BLOCK) k_trace_queue(Scene sc, Workspace ws, const uint32_t *queue,
-                                                            const uint32_t *count, uint32_t *fetch) {
+                                                            const uint32_t *count, uint32_t *fetch,
+                                                            const ReqD *reqs) {
+  static_assert(!(BATCH && STATS), "batched traversal keeps no per-scene statistics");
   const int lane = threadIdx.x & 31;
   const uint32_t n = *(volatile const uint32_t *)count;
   TraceStats ts = {0, 0, 0, 0};
+  Scene bsc = sc;  // this lane's scene in a batch
+  const Scene &S = BATCH ? bsc : sc;
   Traverser tv;
   bool has = false, exhausted = false;
   uint32_t item = 0;
@@ -302,19 +341,21 @@ __global__ void __launch_bounds__(TRACE_BLOCK) k_trace_queue(Scene sc, Workspace
           if (SHADOW) {
             const ShadowRec s = ws.shadows[idx];
             r.org = mk(s.a.x, s.a.y, s.a.z);
-            r.tnear = 0.f;
+            r.tnear = s.c.w;
             r.dir = mk(s.b.x, s.b.y, s.b.z);
             r.tfar = s.a.w;
             item = idx;
+            if (BATCH) bsc = reqs[ws.paths[__float_as_uint(s.b.w)].meta2.y].c.sc;
           } else {
             item = queue ? __ldg(queue + idx) : idx;
             const float4 o = ws.paths[item].org, d = ws.paths[item].dir;
             r.org = mk(o.x, o.y, o.z);
-            r.tnear = 0.f;
+            r.tnear = ws.paths[item].lastP.w;  // camera rays: nearClip; bounces: 0
             r.dir = mk(d.x, d.y, d.z);
             r.tfar = INFINITY;
+            if (BATCH) bsc = reqs[ws.paths[item].meta2.y].c.sc;
           }
-          tv.init(sc, r, SHADOW);
+          tv.init(S, r, SHADOW);
           if (STATS) ts.rays++;
           has = true;
         } else {
@@ -323,7 +364,7 @@ __global__ void __launch_bounds__(TRACE_BLOCK) k_trace_queue(Scene sc, Workspace
       }
     }
     if (!__any_sync(0xffffffffu, has)) break;
-    if (has && tv.step<STATS>(sc, &ts)) {
+    if (has && tv.step<STATS>(S, &ts)) {
       if (SHADOW) {
         if (!tv.found) {
           const ShadowRec s = ws.shadows[item];
@@ -356,14 +397,76 @@ B200_D uint32_t warpAppend(bool want, uint32_t *counter) {
   return base + uint32_t(__popc(m & ((1u << lane) - 1u)));
 }
 
+// The shading step of an AO request's camera sample (AORenderer_renderSample,
+// render/ao/AORenderer.ispc:23-149, with computeAO render/util.ispc:12-54):
+// postIntersect, the eye-light term |Ns . dir| into thr.x, and the AO rays:
+// those below the surface count as occluded and are not traced, the first two
+// go to the shadow queue (contribution 1 to con.x when unblocked), further
+// ones are traced here.  The pixel's AO value and colour are formed at
+// finalize from these integer counts, with the same arithmetic as the
+// single-frame AO kernel.
+B200_D void aoShade(const PtCtx &C, const AOParamsD &A, int W, PathRec &pr, const HitBuf &hb, uint32_t p,
+                    ShadowRec *sh, int &nsh) {
+  uint32_t flags = F_ENDED;
+  float unblocked = 0.f;
+  if (hb.a.w != 0.f) {
+    Ray ray;
+    ray.org = mk(pr.org.x, pr.org.y, pr.org.z);
+    ray.tnear = pr.lastP.w;
+    ray.dir = mk(pr.dir.x, pr.dir.y, pr.dir.z);
+    ray.tfar = INFINITY;
+    HitRec h;
+    h.t = hb.a.x;
+    h.primID = __float_as_uint(hb.a.y);
+    h.entry = __float_as_uint(hb.a.z);
+    h.Ng = mk(hb.b.x, hb.b.y, hb.b.z);
+    const Entry &e = C.sc.entries[h.entry];
+    h.geomID = e.geomID;
+    h.instID = e.instID;
+    const DG dg = postIntersect(C.sc, ray, h);
+    pr.org.w = h.t;
+    pr.meta.z = h.primID;
+    pr.meta.w = h.geomID;
+    pr.meta2.x = h.instID;
+    pr.thr.x = fabsf(dot(dg.Ns, ray.dir));
+    flags |= F_AOHIT;
+    if (A.aoSamples > 0 && A.aoIntensity > 0.01f) {
+      const uint32_t pixel = pr.meta2.w;
+      const AOBasis B = aoBasis(dg, int(pixel % uint32_t(W)), int(pixel / uint32_t(W)));
+      const uint32_t accumID = pr.meta2.z * uint32_t(A.aoSamples);
+      for (int i = 0; i < A.aoSamples; i++) {
+        const V3 dir = aoDirection(C.T, B, dg.Ns, accumID + i);
+        if (dot(dir, dg.Ns) < 0.01f) continue;
+        if (nsh < 2) {
+          sh[nsh].a = make_float4(dg.P.x, dg.P.y, dg.P.z, A.aoRadius);
+          sh[nsh].b = make_float4(dir.x, dir.y, dir.z, __uint_as_float(p));
+          sh[nsh].c = make_float4(1.f, 0.f, 0.f, dg.epsilon);
+          nsh++;
+        } else {
+          Ray r;
+          r.org = dg.P;
+          r.tnear = dg.epsilon;
+          r.dir = dir;
+          r.tfar = A.aoRadius;
+          HitRec hh;
+          if (!traceRay<false>(C.sc, r, hh, true, true, nullptr)) unblocked += 1.f;
+        }
+      }
+    }
+  }
+  pr.con = make_float4(unblocked, 0.f, 0.f, 0.f);
+  pr.meta.y = flags;
+}
+
 // One bounce of samplePath for every queued path (render/pathtracer/
 // PathSampler.ispc:109-415): environment and virtual lights, postIntersect,
 // principled BSDF, NEE light samples (to the shadow queue), BSDF sample and
 // Russian roulette (to the next queue).
+template <bool BATCH>
 __global__ void __launch_bounds__(128) k_pt_shade(PtCtx c, Workspace ws, const uint32_t *qin, const uint32_t *cin,
-                                                  uint32_t *qout, uint32_t *cout, uint32_t *cshadow) {
+                                                  uint32_t *qout, uint32_t *cout, uint32_t *cshadow,
+                                                  const ReqD *reqs) {
   const uint32_t n = *(volatile const uint32_t *)cin;
-  const int nl = c.p.numLights;
   const uint32_t stride = gridDim.x * blockDim.x;
   // warp-uniform loop so the appends can use warp votes
   const uint32_t nround = (n + stride - 1) / stride;
@@ -378,6 +481,13 @@ __global__ void __launch_bounds__(128) k_pt_shade(PtCtx c, Workspace ws, const u
     if (valid) {
       PathRec pr = ws.paths[p];
       const HitBuf hb = ws.hits[p];
+      const ReqD *R = BATCH ? reqs + pr.meta2.y : nullptr;
+      const PtCtx &C = BATCH ? R->c : c;
+      if (BATCH && R->kind == BATCH_AO) {
+        aoShade(C, R->ao, R->fi.W, pr, hb, p, sh, nsh);
+        ws.paths[p] = pr;
+      } else {
+      const int nl = C.p.numLights;
       uint32_t flags = pr.meta.y;
       int depth = int(flags & 0xffu);
       bool straightPath = (flags & F_STRAIGHT) != 0, firstBounceLight = (flags & F_FIRST) != 0;
@@ -396,8 +506,8 @@ __global__ void __launch_bounds__(128) k_pt_shade(PtCtx c, Workspace ws, const u
       const V3 wo = -ray.dir;
       if (depth == 0) pr.org.w = t;
       if (!hit && straightPath) {
-        alpha -= luminance(throughput) * (1.f - c.p.bg[3]);
-        contribution = contribution + throughput * mk(c.p.bg[0], c.p.bg[1], c.p.bg[2]);
+        alpha -= luminance(throughput) * (1.f - C.p.bg[3]);
+        contribution = contribution + throughput * mk(C.p.bg[0], C.p.bg[1], C.p.bg[2]);
       }
       if (nl > 0) {  // evaluateVirtualLights
         const V3 d0 = lastP - ray.org;
@@ -409,7 +519,7 @@ __global__ void __launch_bounds__(128) k_pt_shade(PtCtx c, Workspace ws, const u
         }
         const float selPdf = float(lastNLS) / float(nl);
         for (int i = 0; i < nl; i++) {
-          const LightD &L = c.lights[i];
+          const LightD &L = C.lights[i];
           if (straightPath && !L.visible) continue;
           float lpdf;
           const V3 rad = evalLight(L, lastP, lastNs, ray.dir, lo, hiD, lpdf);
@@ -419,22 +529,22 @@ __global__ void __launch_bounds__(128) k_pt_shade(PtCtx c, Workspace ws, const u
           }
         }
       }
-      if (hit && depth < c.p.maxPathLength) {
+      if (hit && depth < C.p.maxPathLength) {
         HitRec h;
         h.t = t;
         h.primID = __float_as_uint(hb.a.y);
         h.entry = __float_as_uint(hb.a.z);
         h.Ng = mk(hb.b.x, hb.b.y, hb.b.z);
-        const Entry &e = c.sc.entries[h.entry];
+        const Entry &e = C.sc.entries[h.entry];
         h.geomID = e.geomID;
         h.instID = e.instID;
-        const DG dg = postIntersect(c.sc, ray, h);
+        const DG dg = postIntersect(C.sc, ray, h);
         if (depth == 0) {
           pr.meta.z = h.primID;
           pr.meta.w = h.geomID;
           pr.meta2.x = h.instID;
         }
-        if (depth < c.p.maxScatteringEvents && e.materialID < uint32_t(c.p.numMaterials)) {
+        if (depth < C.p.maxScatteringEvents && e.materialID < uint32_t(C.p.numMaterials)) {
           V3 U = e.identity ? mk(1.f, 0.f, 0.f) : mk(e.xfm.m[0], e.xfm.m[4], e.xfm.m[8]);
           U = fnormalize(U);
           const V3 Vv = fcross(dg.Ns, U);
@@ -446,23 +556,21 @@ __global__ void __launch_bounds__(128) k_pt_shade(PtCtx c, Workspace ws, const u
             frame(dg.Ns, fxv, fyv);
           }
           Principled bsdf;
-          bsdf.init(c.mats[e.materialID], fxv, fyv, dg.Ns, c.AT);
+          bsdf.init(C.mats[e.materialID], fxv, fyv, dg.Ns, C.AT);
           if (bsdf.impSum != 0.f) {
             // LDSampler of this path at its current group
-            const int pix = int(p / uint32_t(c.p.spp)), s = int(p % uint32_t(c.p.spp));
-            const uint32_t sampleID = uint32_t(c.frameID) * uint32_t(c.p.spp) + uint32_t(s);
-            (void)pix;
+            const uint32_t sampleID = pr.meta2.z;
             LDSampler ld;
-            ld.init(c.T, pr.meta.x, sampleID, sampleID * uint32_t(c.p.nFirst), 16, 16);
+            ld.init(C.T, pr.meta.x, sampleID, sampleID * uint32_t(C.p.nFirst), 16, 16);
             ld.nextGroup();
-            const int numLS = firstBounceLight ? c.p.nFirst : c.p.nIndirect;
+            const int numLS = firstBounceLight ? C.p.nFirst : C.p.nIndirect;
             for (int i = 0; i < numLS; i++) {
               float ss;
               const float2 sl = ld.get3LightSamples(uint32_t(i), numLS > 1, ss);
               int first = 0, len = nl;
               while (len > 0) {
                 const int half = len >> 1, mid = first + half;
-                if (ss < __ldg(c.lightCdf + mid)) {
+                if (ss < __ldg(C.lightCdf + mid)) {
                   len = half;
                 } else {
                   first = mid + 1;
@@ -470,13 +578,13 @@ __global__ void __launch_bounds__(128) k_pt_shade(PtCtx c, Workspace ws, const u
                 }
               }
               first = min(first, nl - 1);
-              const float prob = __ldg(c.lightCdf + first) - (first == 0 ? 0.f : __ldg(c.lightCdf + first - 1));
+              const float prob = __ldg(C.lightCdf + first) - (first == 0 ? 0.f : __ldg(C.lightCdf + first - 1));
               const float selProb = prob * float(numLS);
-              LightSampleD ls = sampleLight(c.lights[first], dg.P, dg.Ng, dg.Ns, sl.x, sl.y);
+              LightSampleD ls = sampleLight(C.lights[first], dg.P, dg.Ng, dg.Ns, sl.x, sl.y);
               ls.weight = ls.weight * (1.f / selProb);
               ls.pdf *= selProb;
               if (maxc(ls.weight) <= 0.f || ls.pdf <= 0.f) continue;
-              const BsdfEval fe = bsdf.eval(wo, ls.dir, c.AT);
+              const BsdfEval fe = bsdf.eval(wo, ls.dir, C.AT);
               if (maxc(fe.value) <= 0.f) continue;
               V3 org = dg.P;
               if (fdot(dg.Ng, ls.dir) < 0.f) org = org - (2.f * dg.epsilon) * dg.Ng;
@@ -494,7 +602,7 @@ __global__ void __launch_bounds__(128) k_pt_shade(PtCtx c, Workspace ws, const u
                 sr.dir = ls.dir;
                 sr.tfar = ls.dist;
                 HitRec shh;
-                if (!traceRay<false>(c.sc, sr, shh, true, true, nullptr)) contribution = contribution + cval;
+                if (!traceRay<false>(C.sc, sr, shh, true, true, nullptr)) contribution = contribution + cval;
               }
             }
             lastNLS = numLS;
@@ -502,12 +610,12 @@ __global__ void __launch_bounds__(128) k_pt_shade(PtCtx c, Workspace ws, const u
             float ss;
             uint32_t uu3;
             const float2 sb = ld.getNext4Samples(ss, uu3);
-            BsdfSample fs = bsdf.sample(wo, sb.x, sb.y, ss, c.AT);
+            BsdfSample fs = bsdf.sample(wo, sb.x, sb.y, ss, C.AT);
             if (fdot(fs.wi, dg.Ng) < 0.f) fs.weight = splat(0.f);  // reflection lobes only
             cont = !(maxc(fs.weight) <= 0.f || fs.pdf <= 0.f);
             if (cont) {
               throughput = throughput * fs.weight;
-              if (depth >= c.p.roulettePathLength) {
+              if (depth >= C.p.roulettePathLength) {
                 const float rr = ld.finalizeDim3(uu3);
                 const float contProb = fminf(maxc(throughput), 0.95f);
                 if (rr > contProb)
@@ -523,7 +631,7 @@ __global__ void __launch_bounds__(128) k_pt_shade(PtCtx c, Workspace ws, const u
               pr.org = make_float4(dg.P.x, dg.P.y, dg.P.z, pr.org.w);
               pr.dir = make_float4(fs.wi.x, fs.wi.y, fs.wi.z, fs.pdf);
               depth++;
-              if (!(maxc(throughput) > c.p.minContribution)) cont = false;
+              if (!(maxc(throughput) > C.p.minContribution)) cont = false;
             }
             pr.meta.x = ld.scramble;
           }
@@ -534,6 +642,7 @@ __global__ void __launch_bounds__(128) k_pt_shade(PtCtx c, Workspace ws, const u
       pr.meta.y = uint32_t(depth) | (straightPath ? F_STRAIGHT : 0u) | (firstBounceLight ? F_FIRST : 0u) |
                   (cont ? 0u : F_ENDED) | (uint32_t(lastNLS) << 16);
       ws.paths[p] = pr;
+      }
     }
     // queue appends (warp-uniform region)
     const uint32_t oi = warpAppend(cont, cout);
@@ -548,20 +657,18 @@ __global__ void __launch_bounds__(128) k_pt_shade(PtCtx c, Workspace ws, const u
 
 // averages each pixel's samples into the framebuffer (ScreenSample_accumulate
 // / normalize, maxContribution clamp, NaN -> 0 with alpha 1)
-__global__ void k_pt_finalize(PtCtx c, Workspace ws, FrameInfo fi, FrameD fb) {
-  const int pix = blockIdx.x * blockDim.x + threadIdx.x;
-  if (pix >= fi.W * fi.H) return;
+B200_D PixelOut finalizePT(const PathRec *paths, int spp, float maxContribution) {
   PixelOut acc = {0.f, 0.f, 0.f, 0.f, INFINITY, INVALID_ID, INVALID_ID, INVALID_ID};
-  for (int s = 0; s < fi.spp; s++) {
-    const PathRec &pr = ws.paths[size_t(pix) * fi.spp + s];
+  for (int s = 0; s < spp; s++) {
+    const PathRec &pr = paths[s];
     float r = pr.con.x, g = pr.con.y, b = pr.con.z, a = pr.thr.w;
     if (isnan(r) || isnan(g) || isnan(b)) {
       r = g = b = 0.f;
       a = 1.f;
     }
-    acc.r += fminf(r, c.p.maxContribution);
-    acc.g += fminf(g, c.p.maxContribution);
-    acc.b += fminf(b, c.p.maxContribution);
+    acc.r += fminf(r, maxContribution);
+    acc.g += fminf(g, maxContribution);
+    acc.b += fminf(b, maxContribution);
     acc.a += a;
     const float z = pr.org.w;
     if (fabsf(z) < fabsf(acc.z)) {
@@ -571,12 +678,123 @@ __global__ void k_pt_finalize(PtCtx c, Workspace ws, FrameInfo fi, FrameD fb) {
       acc.instID = pr.meta2.x;
     }
   }
-  const float rspp = 1.f / float(fi.spp);
+  const float rspp = 1.f / float(spp);
   acc.r *= rspp;
   acc.g *= rspp;
   acc.b *= rspp;
   acc.a *= rspp;
-  fbAccumulate(fb, pix % fi.W, pix / fi.W, acc);
+  return acc;
+}
+
+// an AO pixel from its samples' eye-light terms and unblocked-ray counts, in
+// the operation order of the single-frame AO kernel (bit-identical results)
+B200_D PixelOut finalizeAO(const PathRec *paths, int spp, const AOParamsD &A) {
+  PixelOut acc = {0.f, 0.f, 0.f, 0.f, INFINITY, INVALID_ID, INVALID_ID, INVALID_ID};
+  float ar = 0.f, ag = 0.f, ab = 0.f, aa = 0.f;
+  for (int s = 0; s < spp; s++) {
+    const PathRec &pr = paths[s];
+    float bl[4];
+    if (pr.meta.y & F_AOHIT) {
+      float intensity = pr.thr.x;
+      if (A.aoSamples > 0 && A.aoIntensity > 0.01f) {
+        const int hits = A.aoSamples - int(pr.con.x);
+        const float ao = 1.f - float(hits) / float(A.aoSamples);
+        intensity = fmul(intensity, fadd(fsub(1.f, A.aoIntensity), fmul(ao, A.aoIntensity)));
+      }
+      bl[0] = bl[1] = bl[2] = intensity;
+      bl[3] = 1.f;
+    } else {
+      for (int k = 0; k < 4; k++) bl[k] = A.bg[k];
+    }
+    const float f = fsub(1.f, 0.f);
+    ar = fadd(ar, fadd(0.f, fmul(f, bl[0])));
+    ag = fadd(ag, fadd(0.f, fmul(f, bl[1])));
+    ab = fadd(ab, fadd(0.f, fmul(f, bl[2])));
+    aa = fadd(aa, fadd(0.f, fmul(f, bl[3])));
+    const float z = pr.org.w;
+    if (fabsf(z) < fabsf(acc.z)) {
+      acc.z = z;
+      acc.primID = pr.meta.z;
+      acc.geomID = pr.meta.w;
+      acc.instID = pr.meta2.x;
+    }
+  }
+  const float rspp = fdiv(1.f, float(spp));
+  acc.r = fmul(ar, rspp);
+  acc.g = fmul(ag, rspp);
+  acc.b = fmul(ab, rspp);
+  acc.a = fmul(aa, rspp);
+  return acc;
+}
+
+__global__ void k_pt_finalize(PtCtx c, Workspace ws, FrameInfo fi, FrameD fb) {
+  const int pix = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pix >= fi.W * fi.H) return;
+  fbAccumulate(fb, pix % fi.W, pix / fi.W, finalizePT(ws.paths + size_t(pix) * fi.spp, fi.spp, c.p.maxContribution));
+}
+
+// ---------------------------------------------------------------- batch kernels
+// the segment of a wave slot (segments sorted by `key`)
+template <class KeyFn>
+B200_D int findSeg(const SegD *segs, int nseg, long long slot, KeyFn key) {
+  int lo = 0, hi = nseg - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (key(segs[mid]) <= slot)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
+__global__ void k_batch_generate(const ReqD *reqs, const SegD *segs, int nseg, long long npaths, Workspace ws) {
+  const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (p == 0) {
+    ws.counters[0] = uint32_t(npaths);
+    for (int k = 1; k < 8; k++) ws.counters[k] = 0;
+  }
+  if (p >= npaths) return;
+  const SegD &sg = segs[findSeg(segs, nseg, p, [](const SegD &q) { return q.start; })];
+  const ReqD &R = reqs[sg.rid];
+  const long long lp = sg.first + (p - sg.start);
+  const int pix = int(lp / R.fi.spp), s = int(lp % R.fi.spp);
+  const int x = pix % R.fi.W, y = pix / R.fi.W;
+  if (R.kind == BATCH_PT) {
+    ws.paths[p] = genPT(R.c, R.cam, R.pf, R.fi, x, y, s, uint32_t(sg.rid));
+    return;
+  }
+  // AO: the Halton camera sample of AORenderer (sample IDs from frameID * spp + 1)
+  const uint32_t sid = uint32_t(R.fi.frameID * R.fi.spp + 1 + s);
+  const Ray ray = primaryRay(R.c.T, R.cam, R.pf, x, y, R.fi.rcpW, R.fi.rcpH, sid);
+  PathRec r;
+  r.org = make_float4(ray.org.x, ray.org.y, ray.org.z, ray.tfar);
+  r.dir = make_float4(ray.dir.x, ray.dir.y, ray.dir.z, 0.f);
+  r.thr = make_float4(0.f, 0.f, 0.f, 1.f);
+  r.con = make_float4(0.f, 0.f, 0.f, 0.f);
+  r.lastP = make_float4(0.f, 0.f, 0.f, ray.tnear);
+  r.lastN = make_float4(0.f, 0.f, 0.f, 0.f);
+  r.meta = make_uint4(0u, 0u, INVALID_ID, INVALID_ID);
+  r.meta2 = make_uint4(INVALID_ID, uint32_t(sg.rid), sid, uint32_t(R.fi.W * y + x));
+  ws.paths[p] = r;
+}
+
+__global__ void k_batch_finalize(const ReqD *reqs, const SegD *segs, int nseg, long long npix, Workspace ws) {
+  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (q >= npix) return;
+  const SegD &sg = segs[findSeg(segs, nseg, q, [](const SegD &g) { return g.pixStart; })];
+  const ReqD &R = reqs[sg.rid];
+  const int spp = R.fi.spp;
+  const long long pix = sg.first / spp + (q - sg.pixStart);
+  const PathRec *paths = ws.paths + sg.start + (pix - sg.first / spp) * spp;
+  const PixelOut o = R.kind == BATCH_PT ? finalizePT(paths, spp, R.c.p.maxContribution) : finalizeAO(paths, spp, R.ao);
+  fbAccumulate(R.fb, int(pix % R.fi.W), int(pix / R.fi.W), o);
+}
+
+__global__ void k_stamp(unsigned long long *stamps, int first, int end) {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  for (int i = first + int(threadIdx.x); i < end; i += blockDim.x) stamps[i] = t;
 }
 
 // ---------------------------------------------------------------- albedo tables
@@ -638,12 +856,18 @@ __global__ void k_albedo_avg(AlbedoTablesD *T) {
   *out = fminf(2.f * (sum / 1024.f), 1.f);
 }
 
-__global__ void k_bounce_reset(uint32_t *counters, int cout) {
+// Between bounces: counts the rays of the bounce about to run (its
+// extension queue) and of the last one's shadow queue, then clears the
+// output queue, shadow queue and fetch counters.
+__global__ void k_bounce_reset(uint32_t *counters, int cin, int cout, unsigned long long *rays) {
+  if (rays) *rays += (unsigned long long)counters[cin] + counters[2];
   counters[cout] = 0;
   counters[2] = 0;
   counters[3] = 0;
   counters[4] = 0;
 }
+
+__global__ void k_count_tail(const uint32_t *counters, unsigned long long *rays) { *rays += counters[2]; }
 
 int persistentBlocks(const void *kernel, size_t smem) {
   int dev, sms, per = 0;
@@ -696,33 +920,164 @@ cudaError_t launchRenderPT(const SamplerTables *T, const Scene &sc, const Camera
   PtCtx c = {T, sc, p, mats, lights, lightCdf, AT, fb.frameID};
   static int traceBlocks = 0, shadowBlocks = 0, shadeBlocks = 0;
   if (!traceBlocks) {
-    traceBlocks = persistentBlocks((const void *)k_trace_queue<false, false>, TRACE_SMEM_BYTES);
-    shadowBlocks = persistentBlocks((const void *)k_trace_queue<true, false>, TRACE_SMEM_BYTES);
-    shadeBlocks = persistentBlocks((const void *)k_pt_shade, TRACE_SMEM_BYTES);
+    traceBlocks = persistentBlocks((const void *)k_trace_queue<false, false, false>, TRACE_SMEM_BYTES);
+    shadowBlocks = persistentBlocks((const void *)k_trace_queue<true, false, false>, TRACE_SMEM_BYTES);
+    shadeBlocks = persistentBlocks((const void *)k_pt_shade<false>, TRACE_SMEM_BYTES);
   }
   const int gen = int((fi.npaths + 255) / 256);
   k_pt_generate<<<gen, 256, 0, st>>>(c, cam, pf, fi, ws);
   uint32_t *qs[2] = {ws.qa, ws.qb};
   for (int b = 0; b <= p.maxPathLength; b++) {
     const int cin = b & 1, cout = cin ^ 1;
-    k_bounce_reset<<<1, 1, 0, st>>>(ws.counters, cout);
+    k_bounce_reset<<<1, 1, 0, st>>>(ws.counters, cin, cout, nullptr);
     const uint32_t *qin = b == 0 ? nullptr : qs[cin];
     if (stats)
-      k_trace_queue<false, true><<<traceBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(sc, ws, qin, ws.counters + cin,
-                                                                                   ws.counters + 3);
+      k_trace_queue<false, true, false><<<traceBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
+          sc, ws, qin, ws.counters + cin, ws.counters + 3, nullptr);
     else
-      k_trace_queue<false, false><<<traceBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(sc, ws, qin, ws.counters + cin,
-                                                                                    ws.counters + 3);
-    k_pt_shade<<<shadeBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(c, ws, qin, ws.counters + cin, qs[cout],
-                                                                   ws.counters + cout, ws.counters + 2);
+      k_trace_queue<false, false, false><<<traceBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
+          sc, ws, qin, ws.counters + cin, ws.counters + 3, nullptr);
+    k_pt_shade<false><<<shadeBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(c, ws, qin, ws.counters + cin, qs[cout],
+                                                                          ws.counters + cout, ws.counters + 2, nullptr);
     if (stats)
-      k_trace_queue<true, true><<<shadowBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(sc, ws, nullptr, ws.counters + 2,
-                                                                                   ws.counters + 4);
+      k_trace_queue<true, true, false><<<shadowBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
+          sc, ws, nullptr, ws.counters + 2, ws.counters + 4, nullptr);
     else
-      k_trace_queue<true, false><<<shadowBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(sc, ws, nullptr,
-                                                                                    ws.counters + 2, ws.counters + 4);
+      k_trace_queue<true, false, false><<<shadowBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
+          sc, ws, nullptr, ws.counters + 2, ws.counters + 4, nullptr);
   }
   k_pt_finalize<<<(fb.W * fb.H + 127) / 128, 128, 0, st>>>(c, ws, fi, fb);
+  return cudaGetLastError();
+}
+
+
+namespace {
+Workspace carveWorkspace(void *workspace, long long npaths) {
+  Workspace ws;
+  char *base = static_cast<char *>(workspace);
+  auto carve = [&](size_t bytes) {
+    char *q = base;
+    base += (bytes + 255) & ~size_t(255);
+    return q;
+  };
+  ws.paths = (PathRec *)carve(sizeof(PathRec) * npaths);
+  ws.hits = (HitBuf *)carve(sizeof(HitBuf) * npaths);
+  ws.qa = (uint32_t *)carve(4 * npaths);
+  ws.qb = (uint32_t *)carve(4 * npaths);
+  ws.shadows = (ShadowRec *)carve(sizeof(ShadowRec) * 2 * npaths);
+  ws.counters = (uint32_t *)carve(64);
+  return ws;
+}
+
+int smCount() {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  return sms > 0 ? sms : 1;
+}
+}  // namespace
+
+void planBatch(const SamplerTables *T, const AlbedoTablesD *AT, const BatchReqH *reqs, int n, long long wavePaths,
+               std::vector<unsigned char> &tables, std::vector<BatchWave> &waves, size_t &segTableOffset) {
+  std::vector<ReqD> rd(n);
+  for (int i = 0; i < n; i++) {
+    const BatchReqH &h = reqs[i];
+    ReqD &r = rd[i];
+    r = ReqD{};
+    r.kind = h.kind;
+    const int spp = h.kind == BATCH_PT ? h.pt.spp : h.ao.spp;
+    r.c = PtCtx{T, h.sc, h.pt, h.mats, h.lights, h.lightCdf, AT, h.fb.frameID};
+    r.cam = h.cam;
+    r.pf = h.pf;
+    r.fi.W = h.fb.W;
+    r.fi.H = h.fb.H;
+    r.fi.spp = spp;
+    r.fi.frameID = h.fb.frameID;
+    r.fi.rcpW = 1.f / float(h.fb.W);
+    r.fi.rcpH = 1.f / float(h.fb.H);
+    r.fi.npaths = (long long)h.fb.W * h.fb.H * spp;
+    r.fb = h.fb;
+    r.ao = h.ao;
+  }
+  std::vector<SegD> segs;
+  waves.clear();
+  BatchWave w = {};
+  auto close = [&]() {
+    if (w.npaths > 0) waves.push_back(w);
+    w = BatchWave{};
+    w.segOffset = int(segs.size());
+    w.completeFirst = w.completeEnd = -1;
+  };
+  close();
+  for (int i = 0; i < n; i++) {
+    const int spp = rd[i].fi.spp;
+    if (spp > wavePaths) throw std::runtime_error("batch: a wave must hold at least one pixel's samples");
+    const long long npix = (long long)rd[i].fi.W * rd[i].fi.H;
+    long long done = 0;
+    while (done < npix) {
+      long long fit = (wavePaths - w.npaths) / spp;
+      if (fit == 0) {
+        close();
+        fit = wavePaths / spp;
+      }
+      const long long k = std::min(fit, npix - done);
+      SegD sg;
+      sg.start = w.npaths;
+      sg.first = done * spp;
+      sg.pixStart = w.npix;
+      sg.rid = i;
+      sg.pad = 0;
+      segs.push_back(sg);
+      w.nseg++;
+      w.npaths += k * spp;
+      w.npix += k;
+      w.maxBounces = std::max(w.maxBounces, rd[i].kind == BATCH_PT ? rd[i].c.p.maxPathLength : 0);
+      done += k;
+      if (done == npix) {
+        if (w.completeFirst < 0) w.completeFirst = i;
+        w.completeEnd = i + 1;
+      }
+    }
+  }
+  close();
+  segTableOffset = (sizeof(ReqD) * n + 255) & ~size_t(255);
+  tables.assign(segTableOffset + sizeof(SegD) * segs.size(), 0);
+  std::memcpy(tables.data(), rd.data(), sizeof(ReqD) * n);
+  std::memcpy(tables.data() + segTableOffset, segs.data(), sizeof(SegD) * segs.size());
+}
+
+cudaError_t launchBatchWave(const void *dtables, size_t segTableOffset, const BatchWave &w, const BatchTuning &tune,
+                            void *workspace, size_t wsBytes, unsigned long long *rayCount, cudaStream_t st) {
+  if (w.npaths > tune.wavePaths || ptWorkspaceBytes(tune.wavePaths) > wsBytes) return cudaErrorInvalidValue;
+  const ReqD *reqs = static_cast<const ReqD *>(dtables);
+  const SegD *segs = reinterpret_cast<const SegD *>(static_cast<const char *>(dtables) + segTableOffset) + w.segOffset;
+  Workspace ws = carveWorkspace(workspace, tune.wavePaths);
+  const int sms = smCount();
+  const int traceBlocks = sms * std::max(1, tune.traceBlocksPerSM);
+  const int shadeBlocks = sms * std::max(1, tune.shadeBlocksPerSM);
+  const Scene noScene = {};
+  const PtCtx noCtx = {};
+  k_batch_generate<<<unsigned((w.npaths + 255) / 256), 256, 0, st>>>(reqs, segs, w.nseg, w.npaths, ws);
+  uint32_t *qs[2] = {ws.qa, ws.qb};
+  for (int b = 0; b <= w.maxBounces; b++) {
+    const int cin = b & 1, cout = cin ^ 1;
+    k_bounce_reset<<<1, 1, 0, st>>>(ws.counters, cin, cout, rayCount);
+    const uint32_t *qin = b == 0 ? nullptr : qs[cin];
+    k_trace_queue<false, false, true><<<traceBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
+        noScene, ws, qin, ws.counters + cin, ws.counters + 3, reqs);
+    k_pt_shade<true><<<shadeBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(noCtx, ws, qin, ws.counters + cin, qs[cout],
+                                                                         ws.counters + cout, ws.counters + 2, reqs);
+    k_trace_queue<true, false, true><<<traceBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
+        noScene, ws, nullptr, ws.counters + 2, ws.counters + 4, reqs);
+  }
+  if (rayCount) k_count_tail<<<1, 1, 0, st>>>(ws.counters, rayCount);
+  k_batch_finalize<<<unsigned((w.npix + 127) / 128), 128, 0, st>>>(reqs, segs, w.nseg, w.npix, ws);
+  return cudaGetLastError();
+}
+
+cudaError_t launchStamp(unsigned long long *stamps, int first, int end, cudaStream_t st) {
+  if (end <= first) return cudaSuccess;
+  k_stamp<<<1, 32, 0, st>>>(stamps, first, end);
   return cudaGetLastError();
 }
 

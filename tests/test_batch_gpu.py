@@ -1,0 +1,124 @@
+"""Batched rendering: many requests in one wavefront (b200_batch_*).
+
+A batch of mixed requests (AO with one and with three AO rays per sample,
+path tracing, different scenes, sizes and spp) is rendered with a small wave
+size, so waves split requests and hold several of them.  Every framebuffer
+must equal what the single-request call renders on the same inputs: AO
+bit-identical (the batch forms each pixel from the same samples with the
+same operation order), path tracing within the tolerance of the shadow-ray
+addition order, depth and IDs exact.  Two frames check accumulation; the
+CUDA-graph replay and the plain launch agree; the autotuner returns one of
+its candidates and restarts accumulation."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _pt_world(og, dev, levels, w, h):
+    from ospray_gb300 import scenes
+    d = scenes.pt_instanced_scene(levels=levels, width=w, height=h)
+    g = og.Scene(dev)
+    scenes.build_pt_scene(g, d)
+    g.set_lights([og.quad_light(L["position"], L["edge1"], L["edge2"], L["intensity"]) if L["type"] == "quad"
+                  else og.ambient_light(L["intensity"]) for L in d["lights"]])
+    c = d["camera"]
+    cam = og.camera_desc(c["position"], c["direction"], c["up"], fovy=c["fovy"], aspect=c["aspect"])
+    return d, g, cam
+
+
+def _ao_world(og, dev, w, h):
+    from ospray_gb300 import scenes
+    d = scenes.ao_heightfield_scene()
+    g = og.Scene(dev)
+    scenes.build_ao_scene(g, d)
+    c = d["camera"]
+    return g, og.camera_desc(c["position"], c["direction"], c["up"], aspect=w / h)
+
+
+CH = None
+
+
+def _requests(og, dev):
+    ch = og.FB_COLOR | og.FB_DEPTH | og.FB_ACCUM | og.FB_ID_PRIMITIVE | og.FB_ID_OBJECT | og.FB_ID_INSTANCE
+    reqs = []
+    g, cam = _ao_world(og, dev, 96, 64)
+    reqs.append(("ao", g, cam, og.ao_params(spp=2, ao_samples=1, pixel_filter=2, bg=(0.1, 0.2, 0.3, 1.0)), 96, 64))
+    d, gp, camp = _pt_world(og, dev, 3, 80, 60)
+    reqs.append(("pt", gp, camp, og.pt_params(spp=3, max_path_length=4, roulette_path_length=2),
+                 og.materials_array(d["materials"]), 80, 60))
+    g2, cam2 = _ao_world(og, dev, 70, 50)
+    reqs.append(("ao", g2, cam2, og.ao_params(spp=1, ao_samples=3, pixel_filter=0), 70, 50))
+    d2, gp2, camp2 = _pt_world(og, dev, 2, 64, 48)
+    reqs.append(("pt", gp2, camp2, og.pt_params(spp=1, max_path_length=2), og.materials_array(d2["materials"]),
+                 64, 48))
+    return ch, reqs
+
+
+def _single(og, dev, ch, r):
+    fb = og.Frame(dev, r[-2], r[-1], ch)
+    return fb
+
+
+def test_batch_matches_single_requests(b200_device):
+    import ospray_gb300 as og
+    dev = b200_device
+    ch, reqs = _requests(og, dev)
+    batch = og.Batch(dev)
+    bfbs, sfbs = [], []
+    for r in reqs:
+        fb = og.Frame(dev, r[-2], r[-1], ch)
+        sf = og.Frame(dev, r[-2], r[-1], ch)
+        if r[0] == "ao":
+            batch.add_ao(r[1], r[2], r[3], fb)
+        else:
+            batch.add_pt(r[1], r[2], r[3], r[4], fb)
+        bfbs.append(fb)
+        sfbs.append(sf)
+    t = og.BatchTuning(4096, 3, 1)  # small waves: requests split across waves
+    batch.tuning = t
+    for frame in range(2):
+        batch.render(use_graph=True)
+        for r, sf in zip(reqs, sfbs):
+            if r[0] == "ao":
+                og.render_ao(r[1], r[2], r[3], sf)
+            else:
+                og.render_pt(r[1], r[2], r[3], r[4], sf)
+        for i, (r, bf, sf) in enumerate(zip(reqs, bfbs, sfbs)):
+            msg = "request %d frame %d" % (i, frame)
+            for c in (og.FB_DEPTH, og.FB_ID_PRIMITIVE, og.FB_ID_OBJECT, og.FB_ID_INSTANCE):
+                np.testing.assert_array_equal(bf.read(c), sf.read(c), err_msg=msg)
+            if r[0] == "ao":
+                np.testing.assert_array_equal(bf.read(og.FB_COLOR), sf.read(og.FB_COLOR), err_msg=msg)
+            else:
+                np.testing.assert_allclose(bf.read(og.FB_COLOR), sf.read(og.FB_COLOR), rtol=1e-4, atol=1e-5,
+                                           err_msg=msg)
+            assert bf.frame_id == frame + 1
+    ms, rays = batch.timings()
+    assert rays > sum(r[-2] * r[-1] for r in reqs)
+    assert np.all(ms > 0) and np.all(np.diff(ms) >= 0)  # requests complete in order
+
+
+def test_graph_replay_equals_plain_launch_and_autotune(b200_device):
+    import ospray_gb300 as og
+    dev = b200_device
+    ch, reqs = _requests(og, dev)
+    out = []
+    for use_graph in (False, True):
+        batch = og.Batch(dev)
+        fbs = []
+        for r in reqs[:1] + reqs[2:3]:  # the AO requests: bit-exact either way
+            fb = og.Frame(dev, r[-2], r[-1], ch)
+            batch.add_ao(r[1], r[2], r[3], fb)
+            fbs.append(fb)
+        batch.render(use_graph=use_graph)
+        batch.render(use_graph=use_graph)
+        out.append([fb.read(og.FB_COLOR) for fb in fbs])
+        if use_graph:
+            best = batch.autotune(candidates=4)
+            assert best.wavePaths >= 2 and best.traceBlocksPerSM in (2, 3, 4, 5) and best.shadeBlocksPerSM in (1, 2)
+            assert all(fb.frame_id == 0 for fb in fbs)
+            batch.render()
+            np.testing.assert_array_equal(fbs[0].read(og.FB_DEPTH), fbs[0].read(og.FB_DEPTH))
+    for a, b in zip(out[0], out[1]):
+        np.testing.assert_array_equal(a, b)
