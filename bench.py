@@ -333,9 +333,177 @@ class ScivisWorkload:
         return samples, dt, rows / self.h
 
 
+class BatchWorkload:
+    """Batched serving: 64 requests (resolution uniform over 256^2, 512^2,
+    768^2, 1024^2, 1280x720; spp uniform in 1..8; AO or path tracer with
+    probability 1/2; each on its own seeded height field of 65k-1M triangles
+    plus 1,000 spheres) rendered as one batched wavefront per step, replayed
+    as a CUDA graph, launch shape chosen by the autotuner at setup.  Reports
+    aggregate Mrays/s, and per-request latency (p50/p99 of completion times
+    after the render starts) of the batch and of the same requests rendered
+    one after another with single-request calls."""
+    name = "batch_64_requests"
+    metric = "Mrays/s"
+
+    def __init__(self, count=64, seed=0):
+        from ospray_gb300 import scenes
+        self.reqs = scenes.batch_requests(seed, count)
+        kinds = [r["renderer"] for r in self.reqs]
+        self.config = {"workload": self.name, "requests": count, "seed": seed,
+                       "ao_requests": kinds.count("ao"), "pt_requests": kinds.count("pathtracer"),
+                       "pixels": int(sum(r["width"] * r["height"] for r in self.reqs)),
+                       "paths": int(sum(r["width"] * r["height"] * r["spp"] for r in self.reqs)),
+                       "pt_params": "maxPathLength 20, roulettePathLength 5 (defaults)",
+                       "ao_params": "aoSamples 1, aoDistance 1e20", "pixelFilter": "gauss"}
+
+    def setup(self, og, dev):
+        from ospray_gb300 import scenes
+        self.og, self.dev = og, dev
+        t0 = time.perf_counter()
+        self.items = []
+        tris = 0
+        for r in self.reqs:
+            sc = og.Scene(dev)
+            tris += scenes.build_batch_request_scene(sc, r)
+            c = dict(position=(0.5, 2.0, -1.5), direction=(0.0, -2.0, 2.0), up=(0.0, 1.0, 0.0))
+            cam = og.camera_desc(c["position"], c["direction"], c["up"], aspect=r["width"] / r["height"])
+            if r["renderer"] == "ao":
+                p = og.ao_params(spp=r["spp"], ao_samples=1, pixel_filter=og.PF_GAUSS)
+                sp = og.ao_params(spp=r["spp"], ao_samples=1, pixel_filter=og.PF_GAUSS, stats=True)
+                mats = None
+            else:
+                p = og.pt_params(spp=r["spp"])
+                sp = og.pt_params(spp=r["spp"], stats=True)
+                mats = og.materials_array([r["material"]])
+            fb = og.Frame(dev, r["width"], r["height"], og.FB_COLOR | og.FB_DEPTH | og.FB_ACCUM)
+            seq = og.Frame(dev, r["width"], r["height"], og.FB_COLOR | og.FB_DEPTH | og.FB_ACCUM)
+            self.items.append(dict(req=r, scene=sc, cam=cam, params=p, sparams=sp, mats=mats, fb=fb, seq=seq))
+        self.config["triangles_total"] = int(tris)
+        self.build_ms = (time.perf_counter() - t0) * 1e3
+        self.batch = og.Batch(dev)
+        for it in self.items:
+            if it["req"]["renderer"] == "ao":
+                self.batch.add_ao(it["scene"], it["cam"], it["params"], it["fb"])
+            else:
+                self.batch.add_pt(it["scene"], it["cam"], it["params"], it["mats"], it["fb"])
+        # traversal statistics per ray from one single-request stats frame of each request
+        rays = nodes = tri = sph = 0
+        for it in self.items:
+            self._single(it, stats=True)
+            c = it["scene"].counters(reset=True)
+            rays, nodes, tri, sph = rays + c[0], nodes + c[1], tri + c[2], sph + c[3]
+        self.per_ray = (nodes / max(rays, 1), tri / max(rays, 1), sph / max(rays, 1))
+        t1 = time.perf_counter()
+        best = self.batch.autotune(candidates=int(os.environ.get("B200_BATCH_TUNE_CANDIDATES", "6")))
+        self.batch.render()
+        self.config["plan"] = self.batch.info()
+        self.config["autotune"] = {"wavePaths": int(best.wavePaths), "traceBlocksPerSM": best.traceBlocksPerSM,
+                                   "shadeBlocksPerSM": best.shadeBlocksPerSM,
+                                   "seconds": round(time.perf_counter() - t1, 2)}
+        self.fb = self.items[0]["fb"]
+        self.colors = [np.empty((it["req"]["height"], it["req"]["width"], 4), np.float32) for it in self.items]
+        self._rays = 0
+
+    def kernels_per_frame(self):
+        return self.batch.info()["kernels"]
+
+    def _single(self, it, stats=False, seq=True):
+        fb = it["seq"] if seq else it["fb"]
+        p = it["sparams"] if stats else it["params"]
+        if it["req"]["renderer"] == "ao":
+            self.og.render_ao(it["scene"], it["cam"], p, fb)
+        else:
+            self.og.render_pt(it["scene"], it["cam"], p, it["mats"], fb)
+
+    def step(self, stats=False):
+        self.batch.render(use_graph=True)
+        if stats:
+            self._rays += self.batch.timings()[1]
+
+    def e2e_step(self):
+        self.batch.render(use_graph=True)
+        d2h = 0
+        for it, col in zip(self.items, self.colors):
+            self.og.lib().b200_frame_read(it["fb"]._h, self.og.FB_COLOR, col.ctypes.data, col.nbytes)
+            d2h += col.nbytes
+        return 116 * len(self.items), d2h
+
+    def reset(self):
+        for it in self.items:
+            it["fb"].reset()
+
+    def counters(self, reset=False):
+        r = self._rays
+        if reset:
+            self._rays = 0
+        n, t, s = self.per_ray
+        return [r, int(r * n), int(r * t), int(r * s)]
+
+    def latency(self):
+        """p50/p99 request completion (ms after the render starts): batch vs sequential."""
+        og, dev = self.og, self.dev
+        self.batch.render(use_graph=True)
+        bms, brays = self.batch.timings()
+        for it in self.items:  # warm
+            it["seq"].reset()
+        dev.sync()
+        e0 = dev.record_event()
+        evs = []
+        for it in self.items:
+            self._single(it)
+            evs.append(dev.record_event())
+        dev.sync()
+        sms = np.array([dev.event_ms(e0, e) for e in evs])
+        for e in [e0] + evs:
+            dev.release_event(e)
+
+        def pct(a):
+            return {"p50_ms": round(float(np.percentile(a, 50)), 3), "p99_ms": round(float(np.percentile(a, 99)), 3),
+                    "makespan_ms": round(float(np.max(a)), 3)}
+        return {"batched": pct(bms), "sequential": pct(sms),
+                "sequential_mrays_s": round(brays / (float(np.max(sms)) * 1e-3) / 1e6, 3),
+                "note": "completion time of each request after the render begins; sequential = the same "
+                        "requests through b200_render_ao / b200_render_pt one after another"}
+
+    def cpu_frames(self, budget_s, nthreads):
+        """Oracle on the requests in order (AO whole frames, path tracing on a
+        band of 16 centre rows), timing rendering only, until budget_s."""
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        import oracle
+        from ospray_gb300 import scenes
+        rays = 0
+        dt = 0.0
+        done = []
+        for r in self.reqs:
+            o = oracle.Scene()
+            scenes.build_batch_request_scene(o, r, lights=False)
+            c = dict(position=(0.5, 2.0, -1.5), direction=(0.0, -2.0, 2.0), up=(0.0, 1.0, 0.0))
+            cam = oracle.camera(c["position"], c["direction"], c["up"], aspect=r["width"] / r["height"])
+            oracle.lib().or_ray_count(1)
+            t0 = time.perf_counter()
+            if r["renderer"] == "ao":
+                oracle.render_ao(o, cam, 2, r["width"], r["height"], spp=r["spp"], nthreads=nthreads)
+                done.append("ao %dx%d" % (r["width"], r["height"]))
+            else:
+                world = oracle.PtWorld([r["material"]], [
+                    dict(type="quad", position=(0.3, 1.2, 0.3), edge1=(0.4, 0, 0), edge2=(0, 0, 0.4),
+                         intensity=20.0), dict(type="ambient", intensity=0.2)])
+                y0 = r["height"] // 2 - 8
+                oracle.render_pt(o, world, cam, oracle.pt_params(spp=r["spp"]), r["width"], r["height"],
+                                 rows=(y0, y0 + 16), nthreads=nthreads)
+                done.append("pt 16 rows of %dx%d" % (r["width"], r["height"]))
+            dt += time.perf_counter() - t0
+            rays += int(oracle.lib().or_ray_count(1))
+            if dt >= budget_s:
+                break
+        self.cpu_sample = "first %d requests in order (%s)" % (len(done), ", ".join(done[:4]) + ", ...")
+        return rays, dt, len(done)
+
+
 AOWorkload.launches_per_frame = 2  # render + post-process (colour conversion)
 PTWorkload.launches_per_frame = 3 + 6 * 4  # generate, finalize, post-process, 6 bounces x (reset, trace, shade, shadow)
-WORKLOADS = {"ao": AOWorkload, "pt": PTWorkload, "scivis": ScivisWorkload}
+BatchWorkload.launches_per_frame = None  # taken from the batch plan (b200_batch_info)
+WORKLOADS = {"ao": AOWorkload, "pt": PTWorkload, "scivis": ScivisWorkload, "batch": BatchWorkload}
 
 
 # --------------------------------------------------------------------------- arms
@@ -467,11 +635,13 @@ def run_ours(args):
                            tri_tests_per_ray=round(tris / max(rays, 1), 3)),
             "e2e": {"value": round(e2e_val, 3), "unit": wl.metric, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
-            "gpu_launches": args.steps * wl.launches_per_frame,
+            "gpu_launches": args.steps * (wl.launches_per_frame or wl.kernels_per_frame()),
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4), "traffic": None,
                          "note": "%s; peak %s" % (note, kind)},
             "clocks": clk.summary()}
+    if hasattr(wl, "latency"):
+        line["latency"] = wl.latency()
     if not args.no_cpu_baseline:
         nthreads = os.cpu_count() or 1
         crays, cdt, cframes = wl.cpu_frames(args.cpu_budget, nthreads)

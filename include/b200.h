@@ -307,6 +307,9 @@ int b200_batch_render(b200_batch batch, int use_graph);
  * time in ms after the render began (out n doubles, request order), and the
  * rays the render traced */
 int b200_batch_timings(b200_batch batch, double *ms, int n, uint64_t *rays);
+/* the plan of the last render: [waves, kernel launches per render, path
+ * slots over all requests, requests] */
+int b200_batch_info(b200_batch batch, int64_t *info4);
 
 /* ---- pick (ospPick, ospray/include/ospray/ospray.h:338-352; Renderer::pick
  *      render/Renderer.cpp:94-140, Renderer_pick render/Renderer.ispc:43-95).

@@ -178,6 +178,7 @@ def lib():
             "b200_batch_autotune": (I, [P, I, ctypes.POINTER(BatchTuning)]),
             "b200_batch_render": (I, [P, I]),
             "b200_batch_timings": (I, [P, P, I, ctypes.POINTER(ctypes.c_uint64)]),
+            "b200_batch_info": (I, [P, P]),
             "b200_event_record": (I, [P, ctypes.POINTER(P)]),
             "b200_event_query": (I, [P]),
             "b200_event_wait": (I, [P]),
@@ -229,6 +230,20 @@ class Device:
     @property
     def stream(self):
         return lib().b200_device_stream(self._h)
+
+    def record_event(self):
+        """b200_event on the device stream (an OSPFuture's completion point)."""
+        e = ctypes.c_void_p()
+        self._check(lib().b200_event_record(self._h, ctypes.byref(e)))
+        return e
+
+    @staticmethod
+    def event_ms(a, b):
+        return lib().b200_event_elapsed_ms(a, b)
+
+    @staticmethod
+    def release_event(e):
+        lib().b200_event_release(e)
 
     def sync(self):
         self._check(lib().b200_device_sync(self._h))
@@ -479,6 +494,12 @@ class Batch:
         rays = ctypes.c_uint64()
         self.device._check(lib().b200_batch_timings(self._h, _ptr(ms), self.n, ctypes.byref(rays)))
         return ms, rays.value
+
+    def info(self):
+        """plan of the last render: dict(waves, kernels, paths, requests)."""
+        a = np.zeros(4, np.int64)
+        self.device._check(lib().b200_batch_info(self._h, _ptr(a)))
+        return dict(zip(("waves", "kernels", "paths", "requests"), (int(x) for x in a)))
 
     def release(self):
         if self._h:

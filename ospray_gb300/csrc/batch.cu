@@ -370,6 +370,25 @@ int b200_batch_render(b200_batch h, int use_graph) {
   return batchGuard(b, [&]() { b->render(use_graph != 0); });
 }
 
+int b200_batch_info(b200_batch h, int64_t *info) {
+  if (!h || !info) return B200_INVALID_ARGUMENT;
+  const BatchObj *b = reinterpret_cast<BatchObj *>(h);
+  int64_t kernels = 1, paths = 0;  // the start stamp
+  for (const BatchWave &w : b->waves) {
+    kernels += 1 + 4 * int64_t(w.maxBounces + 1) + 1 + 1;  // generate, bounces, ray tail, finalize
+    if (w.completeFirst >= 0) {
+      kernels += 1;  // stamp
+      for (int r = w.completeFirst; r < w.completeEnd; r++) kernels += b->reqs[r].fb->format != B200_FB_NONE;
+    }
+    paths += w.npaths;
+  }
+  info[0] = int64_t(b->waves.size());
+  info[1] = kernels;
+  info[2] = paths;
+  info[3] = int64_t(b->reqs.size());
+  return B200_NO_ERROR;
+}
+
 int b200_batch_timings(b200_batch h, double *ms, int n, uint64_t *rays) {
   if (!h) return B200_INVALID_ARGUMENT;
   BatchObj *b = reinterpret_cast<BatchObj *>(h);

@@ -146,3 +146,43 @@ def build_ao_scene(scene, data):
     scene.add_instance(gm, 0, 0)
     scene.add_instance(gs, 0, 1)
     scene.commit()
+
+
+BATCH_SIZES = [(256, 256), (512, 512), (768, 768), (1024, 1024), (1280, 720)]
+
+
+def batch_requests(seed=0, count=64, n_min=182, n_max=708):
+    """Batched-serving workload: `count` independent requests from one seeded
+    stream.  Each draws a resolution uniformly from 256^2, 512^2, 768^2,
+    1024^2, 1280x720, spp uniformly from 1..8, the AO or the path-tracing
+    renderer with probability 1/2, and a height field of its own seed with
+    n x n vertices, n uniform in [n_min, n_max] (2 (n-1)^2 = 65k .. 1M
+    triangles), plus the AO workload's 1,000 spheres at the same seed."""
+    rng = np.random.default_rng(seed)
+    reqs = []
+    for k in range(count):
+        w, h = BATCH_SIZES[int(rng.integers(0, len(BATCH_SIZES)))]
+        reqs.append(dict(width=w, height=h, spp=int(rng.integers(1, 9)),
+                         renderer="ao" if rng.random() < 0.5 else "pathtracer",
+                         n=int(rng.integers(n_min, n_max + 1)), seed=1000 + k,
+                         material=(float(rng.random()), float(rng.random()), float(rng.random()),
+                                   float(0.05 + 0.95 * rng.random()), 0.0)))
+    return reqs
+
+
+def build_batch_request_scene(scene, req, lights=True):
+    """The height field (geomID 0) and spheres (geomID 1) of a batch request,
+    one instance with material 0; path-tracing requests also get a 0.4 x 0.4
+    quad light above the field (intensity 20) and an ambient light (0.2)."""
+    import ospray_gb300 as og
+    v, i = heightfield(req["seed"], req["n"])
+    s = spheres(req["seed"] + 1, 1000)
+    gm = scene.add_mesh(v, i)
+    gs = scene.add_spheres(s)
+    scene.add_instance(gm, 0, 0, None, 0)
+    scene.add_instance(gs, 0, 1, None, 0)
+    if lights and req["renderer"] == "pathtracer":
+        scene.set_lights([og.quad_light((0.3, 1.2, 0.3), (0.4, 0.0, 0.0), (0.0, 0.0, 0.4), 20.0),
+                          og.ambient_light(0.2)])
+    scene.commit()
+    return int(len(i))
