@@ -311,6 +311,41 @@ int b200_batch_timings(b200_batch batch, double *ms, int n, uint64_t *rays);
  * slots over all requests, requests] */
 int b200_batch_info(b200_batch batch, int64_t *info4);
 
+/* ---- neural radiance cache (no counterpart in the reference).
+ * A multiresolution hash-grid encoding (16 levels x 2 FP16 features, 2^19
+ * entries per level, resolutions 16..2048 over the cube around the bounds)
+ * of the position, real spherical harmonics (degree 3, 16 terms) of the
+ * direction, the normal, roughness and albedo, into a 64-wide MLP with 4
+ * hidden ReLU layers and a 3-wide output, BF16 weights on the tensor cores
+ * with FP32 accumulation; trained with Adam on the relative L2 loss.
+ * Records are 16 floats: position[3], direction[3] (unit, pointing away from
+ * the surface), normal[3], roughness, albedo[3], target rgb[3] (training) or
+ * unused.  Device pointers. */
+typedef struct b200_nrc_t *b200_nrc;
+typedef struct {
+  float boundsLo[3], boundsHi[3];
+  float learningRate; /* Adam, default 1e-2 */
+  uint32_t seed;      /* parameter initialisation */
+} b200_nrc_desc;
+int b200_nrc_create(b200_device dev, const b200_nrc_desc *desc, b200_nrc *out);
+int b200_nrc_release(b200_nrc nrc);
+/* out: n x 3 float radiance */
+int b200_nrc_infer(b200_nrc nrc, const float *queries, int64_t n, float *out, void *stream);
+/* one Adam step on the mean loss of n samples; loss (device float, may be null) */
+int b200_nrc_train(b200_nrc nrc, const float *samples, int64_t n, float *loss, void *stream);
+/* the gradients of the mean loss of n samples without a step: weights
+ * (17,408 floats: 4 hidden layers 64x64 then the output layer 64x16, each
+ * row-major [in][out]) and table (16 x 2^19 x 2 floats), device pointers,
+ * each may be null */
+int b200_nrc_gradients(b200_nrc nrc, const float *samples, int64_t n, float *wgrad, float *tgrad, float *loss,
+                       void *stream);
+/* FP32 master parameters in the layouts above (host pointers, may be null) */
+int b200_nrc_get_params(b200_nrc nrc, float *weights, float *table);
+int b200_nrc_set_params(b200_nrc nrc, const float *weights, const float *table);
+/* the grid: lo xyz and 1/extent; per level the scale (N_l - 1) and the dense
+ * side length (0 = hashed) */
+int b200_nrc_grid(b200_nrc nrc, float *lo_invext4, float *scales16, uint32_t *dense16);
+
 /* ---- pick (ospPick, ospray/include/ospray/ospray.h:338-352; Renderer::pick
  *      render/Renderer.cpp:94-140, Renderer_pick render/Renderer.ispc:43-95).
  * One camera ray through normalised screen position (x, y) in [0,1]^2

@@ -179,6 +179,14 @@ def lib():
             "b200_batch_render": (I, [P, I]),
             "b200_batch_timings": (I, [P, P, I, ctypes.POINTER(ctypes.c_uint64)]),
             "b200_batch_info": (I, [P, P]),
+            "b200_nrc_create": (I, [P, ctypes.POINTER(NrcDesc), ctypes.POINTER(P)]),
+            "b200_nrc_release": (I, [P]),
+            "b200_nrc_infer": (I, [P, P, I64, P, P]),
+            "b200_nrc_train": (I, [P, P, I64, P, P]),
+            "b200_nrc_gradients": (I, [P, P, I64, P, P, P, P]),
+            "b200_nrc_get_params": (I, [P, P, P]),
+            "b200_nrc_set_params": (I, [P, P, P]),
+            "b200_nrc_grid": (I, [P, P, P, P]),
             "b200_event_record": (I, [P, ctypes.POINTER(P)]),
             "b200_event_query": (I, [P]),
             "b200_event_wait": (I, [P]),
@@ -504,6 +512,71 @@ class Batch:
     def release(self):
         if self._h:
             lib().b200_batch_release(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.release()
+        except Exception:
+            pass
+
+
+class NrcDesc(ctypes.Structure):
+    _fields_ = [("boundsLo", ctypes.c_float * 3), ("boundsHi", ctypes.c_float * 3), ("learningRate", ctypes.c_float),
+                ("seed", ctypes.c_uint32)]
+
+
+NRC_NUM_W = 4 * 64 * 64 + 64 * 16
+NRC_NUM_T = 16 * (1 << 19) * 2
+
+
+class RadianceCache:
+    """b200_nrc: the neural radiance cache (hash grid + fused BF16 MLP).
+    Query / sample arrays are device pointers to n x 16 float records."""
+
+    def __init__(self, device, lo, hi, learning_rate=1e-2, seed=1):
+        self.device = device
+        d = NrcDesc()
+        d.boundsLo[:], d.boundsHi[:] = list(map(float, lo)), list(map(float, hi))
+        d.learningRate, d.seed = float(learning_rate), int(seed)
+        self._h = ctypes.c_void_p()
+        device._check(lib().b200_nrc_create(device._h, ctypes.byref(d), ctypes.byref(self._h)))
+
+    def infer(self, queries_ptr, n, out_ptr, stream=None):
+        self.device._check(lib().b200_nrc_infer(self._h, ctypes.c_void_p(queries_ptr), n, ctypes.c_void_p(out_ptr),
+                                                ctypes.c_void_p(stream) if stream else None))
+
+    def train(self, samples_ptr, n, loss_ptr=None, stream=None):
+        self.device._check(lib().b200_nrc_train(self._h, ctypes.c_void_p(samples_ptr), n,
+                                                ctypes.c_void_p(loss_ptr) if loss_ptr else None,
+                                                ctypes.c_void_p(stream) if stream else None))
+
+    def gradients(self, samples_ptr, n, wgrad_ptr, tgrad_ptr, loss_ptr=None):
+        self.device._check(lib().b200_nrc_gradients(self._h, ctypes.c_void_p(samples_ptr), n,
+                                                     ctypes.c_void_p(wgrad_ptr), ctypes.c_void_p(tgrad_ptr),
+                                                     ctypes.c_void_p(loss_ptr) if loss_ptr else None, None))
+
+    def get_params(self):
+        w = np.empty(NRC_NUM_W, np.float32)
+        t = np.empty(NRC_NUM_T, np.float32)
+        self.device._check(lib().b200_nrc_get_params(self._h, _ptr(w), _ptr(t)))
+        return w, t
+
+    def set_params(self, weights=None, table=None):
+        w = None if weights is None else np.ascontiguousarray(weights, np.float32)
+        t = None if table is None else np.ascontiguousarray(table, np.float32)
+        self.device._check(lib().b200_nrc_set_params(self._h, _ptr(w), _ptr(t)))
+
+    def grid(self):
+        a = np.empty(4, np.float32)
+        s = np.empty(16, np.float32)
+        dn = np.empty(16, np.uint32)
+        self.device._check(lib().b200_nrc_grid(self._h, _ptr(a), _ptr(s), _ptr(dn)))
+        return dict(lo=a[:3].copy(), inv_extent=float(a[3]), scales=s, dense=dn)
+
+    def release(self):
+        if self._h:
+            lib().b200_nrc_release(self._h)
             self._h = ctypes.c_void_p()
 
     def __del__(self):
