@@ -155,6 +155,11 @@ typedef struct {
 } b200_tonemapper;
 /* fills `tm` with the defaults above */
 void b200_tonemapper_defaults(b200_tonemapper *tm);
+
+/* image error of a framebuffer's accumulated colour against a reference
+ * framebuffer of the same size: relMSE = mean over pixels and rgb of
+ * (x - r)^2 / (r^2 + 0.01).  Synchronous. */
+int b200_frame_relmse(b200_frame fb, b200_frame reference, double *out);
 int b200_frame_set_tonemapper(b200_frame fb, const b200_tonemapper *tm);
 
 /* ---- AO renderer (AORenderer::commit modules/cpu/render/ao/AORenderer.cpp:26-35,
@@ -345,6 +350,26 @@ int b200_nrc_set_params(b200_nrc nrc, const float *weights, const float *table);
 /* the grid: lo xyz and 1/extent; per level the scale (N_l - 1) and the dense
  * side length (0 = hashed) */
 int b200_nrc_grid(b200_nrc nrc, float *lo_invext4, float *scales16, uint32_t *dense16);
+
+/* ---- path tracing with the radiance cache.  Renders one frame like
+ * b200_render_pt, except: every other path, at its first vertex after a
+ * diffuse bounce (a bounce off a non-metallic or rough surface), takes the
+ * cache's radiance there instead of continuing; `trainPaths` evenly spaced
+ * paths per frame (a different subset each frame) are traced in full and
+ * their vertices' path-suffix radiance becomes training data; then the
+ * cache takes `trainSteps` Adam steps of `trainBatch` samples (when
+ * `train`).  The plain path tracer (b200_render_pt) is the same method
+ * without the cache. */
+typedef struct {
+  int trainPaths; /* default 16384 */
+  int trainSteps; /* default 4 */
+  int trainBatch; /* default 16384 (4 x 16384 = 65,536 samples per frame) */
+  int train;      /* default 1 */
+} b200_nrc_frame;
+void b200_nrc_frame_defaults(b200_nrc_frame *f);
+int b200_render_pt_nrc(b200_scene scene, const b200_camera_desc *camera, const b200_pt_params *params,
+                       const b200_material *materials, int nmaterials, b200_frame fb, b200_nrc nrc,
+                       const b200_nrc_frame *frame_params, void *stream);
 
 /* ---- pick (ospPick, ospray/include/ospray/ospray.h:338-352; Renderer::pick
  *      render/Renderer.cpp:94-140, Renderer_pick render/Renderer.ispc:43-95).

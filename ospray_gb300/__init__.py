@@ -187,6 +187,9 @@ def lib():
             "b200_nrc_get_params": (I, [P, P, P]),
             "b200_nrc_set_params": (I, [P, P, P]),
             "b200_nrc_grid": (I, [P, P, P, P]),
+            "b200_nrc_frame_defaults": (None, [P]),
+            "b200_render_pt_nrc": (I, [P, ctypes.POINTER(CameraDesc), ctypes.POINTER(PTParams), P, I, P, P, P, P]),
+            "b200_frame_relmse": (I, [P, P, ctypes.POINTER(ctypes.c_double)]),
             "b200_event_record": (I, [P, ctypes.POINTER(P)]),
             "b200_event_query": (I, [P]),
             "b200_event_wait": (I, [P]),
@@ -584,3 +587,25 @@ class RadianceCache:
             self.release()
         except Exception:
             pass
+
+
+class NrcFrame(ctypes.Structure):
+    _fields_ = [("trainPaths", ctypes.c_int), ("trainSteps", ctypes.c_int), ("trainBatch", ctypes.c_int),
+                ("train", ctypes.c_int)]
+
+
+def render_pt_nrc(scene, camera, params, materials, frame, cache, train=True, train_paths=16384, train_steps=4,
+                  train_batch=16384, stream=None):
+    """One path-traced frame ending paths in the radiance cache (and training it)."""
+    f = NrcFrame(int(train_paths), int(train_steps), int(train_batch), int(bool(train)))
+    arr, n = materials
+    scene.device._check(lib().b200_render_pt_nrc(scene._h, ctypes.byref(camera), ctypes.byref(params),
+                                                 ctypes.cast(arr, ctypes.c_void_p), n, frame._h, cache._h,
+                                                 ctypes.byref(f), ctypes.c_void_p(stream) if stream else None))
+
+
+def relmse(frame, reference):
+    """mean over pixels and rgb of (x - r)^2 / (r^2 + 0.01) of the accumulated colours."""
+    v = ctypes.c_double()
+    frame.device._check(lib().b200_frame_relmse(frame._h, reference._h, ctypes.byref(v)))
+    return v.value

@@ -170,6 +170,42 @@ PixelFilterD DeviceObj::filter(int type) const {
   return pf;
 }
 
+// the renderer's material list on the device, uploaded when it changed
+void uploadMaterials(SceneObj *sc, const b200_material *materials, int nmaterials) {
+  const bool same = int(sc->lastMaterials.size()) == nmaterials &&
+                    (nmaterials == 0 ||
+                     std::memcmp(sc->lastMaterials.data(), materials, sizeof(b200_material) * nmaterials) == 0);
+  if (!same) {
+    std::vector<MaterialD> h(nmaterials);
+    for (int i = 0; i < nmaterials; i++)
+      h[i] = {materials[i].baseColor[0], materials[i].baseColor[1], materials[i].baseColor[2], materials[i].roughness,
+              materials[i].metallic};
+    if (nmaterials > sc->capMaterials) {
+      if (sc->dMaterials) cudaFree(sc->dMaterials);
+      check(cudaMalloc(&sc->dMaterials, sizeof(MaterialD) * nmaterials), "alloc materials");
+      sc->capMaterials = nmaterials;
+    }
+    if (nmaterials)
+      check(cudaMemcpy(sc->dMaterials, h.data(), sizeof(MaterialD) * nmaterials, cudaMemcpyHostToDevice),
+            "upload materials");
+    sc->lastMaterials.assign(materials, materials + nmaterials);
+  }
+  sc->nMaterials = nmaterials;
+}
+
+// the path workspace: grown on demand, kept for later frames
+void ensurePtWorkspace(DeviceObj *dev, size_t need) {
+  if (need <= dev->ptWsBytes) return;
+  if (dev->ptWs) {
+    check(cudaStreamSynchronize(dev->stream), "sync");
+    cudaFree(dev->ptWs);
+    dev->ptWs = nullptr;
+    dev->ptWsBytes = 0;
+  }
+  check(cudaMalloc(&dev->ptWs, need), "path tracer workspace");
+  dev->ptWsBytes = need;
+}
+
 // PathTracer::commit (render/pathtracer/PathTracer.cpp:29-51): light sample
 // counts (lightSamples < 0: all lights at the first bounce; one after it
 // when limitIndirectLightSamples)
@@ -751,40 +787,10 @@ int b200_render_pt(b200_scene s, const b200_camera_desc *camera, const b200_pt_p
     require(p->pixelFilter >= B200_PF_POINT && p->pixelFilter <= B200_PF_BLACKMAN_HARRIS, "bad pixel filter");
     require(nmaterials >= 0 && (nmaterials == 0 || materials), "bad material array");
     cudaStream_t st = stream ? (cudaStream_t)stream : sc->dev->stream;
-    // upload the material list when it changed since the last frame
-    const bool same = int(sc->lastMaterials.size()) == nmaterials &&
-                      (nmaterials == 0 ||
-                       std::memcmp(sc->lastMaterials.data(), materials, sizeof(b200_material) * nmaterials) == 0);
-    if (!same) {
-      std::vector<MaterialD> h(nmaterials);
-      for (int i = 0; i < nmaterials; i++)
-        h[i] = {materials[i].baseColor[0], materials[i].baseColor[1], materials[i].baseColor[2],
-                materials[i].roughness, materials[i].metallic};
-      if (nmaterials > sc->capMaterials) {
-        if (sc->dMaterials) cudaFree(sc->dMaterials);
-        check(cudaMalloc(&sc->dMaterials, sizeof(MaterialD) * nmaterials), "alloc materials");
-        sc->capMaterials = nmaterials;
-      }
-      if (nmaterials)
-        check(cudaMemcpy(sc->dMaterials, h.data(), sizeof(MaterialD) * nmaterials, cudaMemcpyHostToDevice),
-              "upload materials");
-      sc->lastMaterials.assign(materials, materials + nmaterials);
-    }
-    sc->nMaterials = nmaterials;
+    uploadMaterials(sc, materials, nmaterials);
     const PtParamsD d = makePtParams(*p, sc->nLights, nmaterials);
-    // path workspace: grown on demand, kept for later frames
-    const size_t need = ptWorkspaceBytes((long long)fb->W * fb->H * p->pixelSamples);
     DeviceObj *dev = sc->dev;
-    if (need > dev->ptWsBytes) {
-      if (dev->ptWs) {
-        check(cudaStreamSynchronize(dev->stream), "sync");
-        cudaFree(dev->ptWs);
-        dev->ptWs = nullptr;
-        dev->ptWsBytes = 0;
-      }
-      check(cudaMalloc(&dev->ptWs, need), "path tracer workspace");
-      dev->ptWsBytes = need;
-    }
+    ensurePtWorkspace(dev, ptWorkspaceBytes((long long)fb->W * fb->H * p->pixelSamples));
     check(launchRenderPT(dev->tables, sc->view(), makeCamera(*camera), dev->filter(p->pixelFilter), d,
                          sc->dMaterials, sc->dLights, sc->dLightCdf, dev->albedoTables(), fb->view(),
                          p->collectStats != 0, dev->ptWs, dev->ptWsBytes, st),

@@ -123,6 +123,8 @@ struct FrameObj {
 
 CameraD makeCamera(const b200_camera_desc &c);
 PtParamsD makePtParams(const b200_pt_params &p, int numLights, int numMaterials);
+void uploadMaterials(SceneObj *sc, const b200_material *materials, int nmaterials);
+void ensurePtWorkspace(DeviceObj *dev, size_t need);
 AOParamsD makeAOParams(const b200_ao_params &p);
 ToneMapD makeToneMap(const b200_tonemapper &u);
 // tonemap (if set) + conversion of the accumulated colour into fb->mapped,

@@ -48,11 +48,32 @@ cudaError_t launchRenderScivisVolume(const SamplerTables *T, const Scene &sc, co
                                      const PixelFilterD &pf, const ScivisParamsD &p, const FrameD &fb, bool stats,
                                      cudaStream_t st);
 
+// Path tracing with the neural radiance cache: per frame, paths whose index
+// p satisfies (p + trainOffset) % trainStride == 0 are training paths (slot
+// (p + trainOffset) / trainStride < trainSlots); they are traced in full and
+// record every vertex (20 floats: the 13 cache inputs, throughput, the
+// contribution so far, the path index).  Every other path, at its first
+// vertex after a diffuse bounce, appends a cache query (16 floats: inputs and
+// throughput; qpath = its index) and ends; after each bounce the queries are
+// answered (qout, by the caller's inference callback) and throughput x
+// radiance is added to the paths.  After the frame the training vertices
+// become training samples (inputs + suffix radiance (C_end - C_i) / T_i).
+struct NrcFrameD {
+  float *queries;
+  uint32_t *qpath;
+  float *qout;
+  uint32_t *counters;  // [0] queries of the current bounce, [1] training samples
+  float *trainVerts;   // trainSlots x maxLen1 x 20
+  float *samples;      // sampleCap x 16
+  uint32_t maxLen1, trainStride, trainOffset, trainSlots, sampleCap;
+};
+
 cudaError_t computeAlbedoTables(AlbedoTablesD *T, cudaStream_t st);
 cudaError_t launchRenderPT(const SamplerTables *T, const Scene &sc, const CameraD &cam, const PixelFilterD &pf,
                            const PtParamsD &p, const MaterialD *mats, const LightD *lights, const float *lightCdf,
                            const AlbedoTablesD *AT, const FrameD &fb, bool stats, void *workspace,
-                           size_t wsBytes, cudaStream_t st);
+                           size_t wsBytes, cudaStream_t st, const NrcFrameD *nrc = nullptr,
+                           void (*nrcInfer)(void *ctx, cudaStream_t st) = nullptr, void *nrcCtx = nullptr);
 // bytes of path-tracer workspace for a frame of npaths = W * H * spp paths
 size_t ptWorkspaceBytes(long long npaths);
 

@@ -4,6 +4,8 @@
 #include <cstring>
 #include <vector>
 
+#include <algorithm>
+
 #include "api_internal.h"
 #include "nrc.cuh"
 
@@ -109,8 +111,16 @@ B200_D void outputLayer(const __nv_bfloat16 *wt, const uint32_t a[4][4], float o
   }
 }
 
-__global__ void __launch_bounds__(WARPS * 32) k_nrc_infer(Params P, const float *__restrict__ q, long long n,
-                                                          float *__restrict__ out) {
+// n = min(*dn, nmax) when dn is given (a count produced on the device)
+B200_D long long deviceCount(long long nmax, const uint32_t *dn, long long offset) {
+  if (!dn) return nmax;
+  const long long c = (long long)*(volatile const uint32_t *)dn - offset;
+  return c < 0 ? 0 : (c < nmax ? c : nmax);
+}
+
+__global__ void __launch_bounds__(WARPS * 32) k_nrc_infer(Params P, const float *__restrict__ q, long long nmax,
+                                                          const uint32_t *dn, float *__restrict__ out) {
+  const long long n = deviceCount(nmax, dn, 0);
   extern __shared__ __align__(16) unsigned char smem[];
   __nv_bfloat16 *wt = reinterpret_cast<__nv_bfloat16 *>(smem);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -195,8 +205,11 @@ B200_D void scatterGrid(const Params &P, const float *r, int level, float d0, fl
 //   L = 1/(3N) sum_s sum_c (o - y)^2 / (sg(o)^2 + 0.01)
 // Gradients are summed into wgrad (17,408) and tgrad (table, FP32); the loss
 // sum into *loss.
-__global__ void __launch_bounds__(WARPS * 32) k_nrc_train(Params P, const float *__restrict__ samples, long long n,
-                                                          float invN3, float *wgrad, float *tgrad, float *loss) {
+__global__ void __launch_bounds__(WARPS * 32) k_nrc_train(Params P, const float *__restrict__ samples, long long nmax,
+                                                          const uint32_t *dn, long long offset, float *wgrad,
+                                                          float *tgrad, float *loss) {
+  const long long n = deviceCount(nmax, dn, offset);
+  const float invN3 = n > 0 ? 1.f / (3.f * float(n)) : 0.f;
   extern __shared__ __align__(16) unsigned char smem[];
   __nv_bfloat16 *w = reinterpret_cast<__nv_bfloat16 *>(smem);
   __nv_bfloat16 *wt = w + NUM_W;
@@ -318,9 +331,11 @@ constexpr size_t kTrainSmem = size_t(NUM_W) * 2 * 2 + size_t(NUM_W) * 4 +
 static_assert(kTrainSmem <= 227 * 1024, "training kernel shared memory");
 
 // ---------------------------------------------------------------- Adam and parameter copies
+// skipped when the step's device-side sample count (dn - offset) is zero
 __global__ void k_adam(float *__restrict__ p, float *__restrict__ m, float *__restrict__ v,
                        const float *__restrict__ g, long long n, float lr, float b1, float b2, float eps, float bc1,
-                       float bc2) {
+                       float bc2, const uint32_t *dn, long long offset) {
+  if (dn && deviceCount(1, dn, offset) == 0) return;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     const float gi = g[i];
     const float mi = b1 * m[i] + (1.f - b1) * gi;
@@ -425,7 +440,8 @@ struct NrcObj {
     cudaSetDevice(dev->dev);
     cudaStreamSynchronize(dev->stream);
     for (void *p : {(void *)table, (void *)tMaster, (void *)tGrad, (void *)tM, (void *)tV, (void *)w, (void *)wt,
-                    (void *)wMaster, (void *)wGrad, (void *)wM, (void *)wV, (void *)dLoss})
+                    (void *)wMaster, (void *)wGrad, (void *)wM, (void *)wV, (void *)dLoss, (void *)queries,
+                    (void *)qout, (void *)trainVerts, (void *)samples, (void *)qpath, (void *)fcounters})
       if (p) cudaFree(p);
     dev->release();
   }
@@ -434,24 +450,54 @@ struct NrcObj {
     k_table_to_half<<<1024, 256, 0, st>>>(tMaster, table, NUM_T / 2);
   }
   Params params() const { return Params{grid, table, w, wt}; }
+
+  // ---- per-frame buffers of the cache-terminated path tracer
+  float *queries = nullptr, *qout = nullptr, *trainVerts = nullptr, *samples = nullptr;
+  uint32_t *qpath = nullptr, *fcounters = nullptr;
+  long long qcap = 0, vcap = 0;
+  void frameBuffers(long long npaths, long long nverts) {
+    auto grow = [&](void **p, size_t bytes) {
+      if (*p) cudaFree(*p);
+      *p = nullptr;
+      check(cudaMalloc(p, bytes), "radiance cache frame buffers");
+    };
+    if (npaths > qcap || nverts > vcap) check(cudaStreamSynchronize(dev->stream), "sync");
+    if (npaths > qcap) {
+      grow((void **)&queries, size_t(npaths) * REC * 4);
+      grow((void **)&qout, size_t(npaths) * 3 * 4);
+      grow((void **)&qpath, size_t(npaths) * 4);
+      qcap = npaths;
+    }
+    if (nverts > vcap) {
+      grow((void **)&trainVerts, size_t(nverts) * 20 * 4);
+      grow((void **)&samples, size_t(nverts) * REC * 4);
+      vcap = nverts;
+    }
+    if (!fcounters) check(cudaMalloc(&fcounters, 16), "radiance cache counters");
+  }
+  static void inferHook(void *self, cudaStream_t st) {
+    NrcObj *o = static_cast<NrcObj *>(self);
+    o->infer(o->queries, o->qcap, o->qout, st, o->fcounters);
+  }
   void setAttrs() {
     if (attrsSet) return;
     check(cudaFuncSetAttribute(k_nrc_train, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kTrainSmem)), "smem");
     check(cudaFuncSetAttribute(k_nrc_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kInferSmem)), "smem");
     attrsSet = true;
   }
-  void infer(const float *q, long long n, float *out, cudaStream_t st) {
+  // n queries, or min(*dn, n) when dn (a device count) is given
+  void infer(const float *q, long long n, float *out, cudaStream_t st, const uint32_t *dn = nullptr) {
     if (n <= 0) return;
     setAttrs();
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev->dev);
     const long long tiles = (n + 15) / 16;
     const long long blocks = std::min<long long>((tiles + WARPS - 1) / WARPS, (long long)sms * 4);
-    k_nrc_infer<<<unsigned(blocks), WARPS * 32, kInferSmem, st>>>(params(), q, n, out);
+    k_nrc_infer<<<unsigned(blocks), WARPS * 32, kInferSmem, st>>>(params(), q, n, dn, out);
     check(cudaGetLastError(), "radiance cache inference");
   }
   // gradients of the loss over n samples into wGrad / tGrad (cleared first)
-  void gradients(const float *s, long long n, cudaStream_t st) {
+  void gradients(const float *s, long long n, cudaStream_t st, const uint32_t *dn = nullptr, long long offset = 0) {
     setAttrs();
     check(cudaMemsetAsync(tGrad, 0, NUM_T * 4, st), "clear");
     check(cudaMemsetAsync(wGrad, 0, NUM_W * 4, st), "clear");
@@ -461,17 +507,20 @@ struct NrcObj {
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev->dev);
     const long long tiles = (n + 15) / 16;
     const long long blocks = std::min<long long>((tiles + WARPS - 1) / WARPS, (long long)sms);
-    k_nrc_train<<<unsigned(blocks), WARPS * 32, kTrainSmem, st>>>(params(), s, n, 1.f / (3.f * float(n)), wGrad,
+    k_nrc_train<<<unsigned(blocks), WARPS * 32, kTrainSmem, st>>>(params(), s + offset * REC, n, dn, offset, wGrad,
                                                                    tGrad, dLoss);
     check(cudaGetLastError(), "radiance cache training");
   }
-  void train(const float *s, long long n, cudaStream_t st) {
-    gradients(s, n, st);
+  // one Adam step on n samples (with dn: on min(*dn - offset, n) samples
+  // from s + offset records, skipped when that is zero)
+  void train(const float *s, long long n, cudaStream_t st, const uint32_t *dn = nullptr, long long offset = 0) {
+    gradients(s, n, st, dn, offset);
     if (n <= 0) return;
     step++;
     const float bc1 = 1.f - std::pow(beta1, float(step)), bc2 = 1.f - std::pow(beta2, float(step));
-    k_adam<<<2048, 256, 0, st>>>(tMaster, tM, tV, tGrad, NUM_T, lr, beta1, beta2, eps, bc1, bc2);
-    k_adam<<<(NUM_W + 255) / 256, 256, 0, st>>>(wMaster, wM, wV, wGrad, NUM_W, lr, beta1, beta2, eps, bc1, bc2);
+    k_adam<<<2048, 256, 0, st>>>(tMaster, tM, tV, tGrad, NUM_T, lr, beta1, beta2, eps, bc1, bc2, dn, offset);
+    k_adam<<<(NUM_W + 255) / 256, 256, 0, st>>>(wMaster, wM, wV, wGrad, NUM_W, lr, beta1, beta2, eps, bc1, bc2, dn,
+                                                offset);
     refresh(st);
     check(cudaGetLastError(), "radiance cache Adam step");
   }
@@ -564,6 +613,68 @@ int b200_nrc_set_params(b200_nrc h, const float *weights, const float *table) {
     if (table) check(cudaMemcpy(o->tMaster, table, nrc::NUM_T * 4, cudaMemcpyHostToDevice), "write table");
     o->refresh(o->dev->stream);
     check(cudaStreamSynchronize(o->dev->stream), "sync");
+  });
+}
+
+void b200_nrc_frame_defaults(b200_nrc_frame *f) {
+  if (!f) return;
+  f->trainPaths = 16384;
+  f->trainSteps = 4;
+  f->trainBatch = 16384;
+  f->train = 1;
+}
+
+int b200_render_pt_nrc(b200_scene s, const b200_camera_desc *camera, const b200_pt_params *p,
+                       const b200_material *materials, int nmaterials, b200_frame f, b200_nrc h,
+                       const b200_nrc_frame *nfp, void *stream) {
+  if (!s || !camera || !p || !f || !h) return B200_INVALID_ARGUMENT;
+  SceneObj *sc = reinterpret_cast<SceneObj *>(s);
+  FrameObj *fb = reinterpret_cast<FrameObj *>(f);
+  NrcObj *o = reinterpret_cast<NrcObj *>(h);
+  b200_nrc_frame np;
+  b200_nrc_frame_defaults(&np);
+  if (nfp) np = *nfp;
+  return nrcGuard(sc->dev, [&]() {
+    if (!sc->committed) throw Error(B200_INVALID_OPERATION, "scene not committed");
+    if (o->dev != sc->dev) throw Error(B200_INVALID_ARGUMENT, "the cache belongs to another device");
+    if (!(p->pixelSamples >= 1 && p->maxPathLength >= 0 && p->pixelFilter >= B200_PF_POINT &&
+          p->pixelFilter <= B200_PF_BLACKMAN_HARRIS && nmaterials >= 0 && (nmaterials == 0 || materials)))
+      throw Error(B200_INVALID_ARGUMENT, "bad path tracer parameters");
+    if (np.trainPaths < 0 || np.trainSteps < 0 || np.trainBatch < 1)
+      throw Error(B200_INVALID_ARGUMENT, "bad radiance cache frame parameters");
+    cudaStream_t st = stream ? (cudaStream_t)stream : sc->dev->stream;
+    uploadMaterials(sc, materials, nmaterials);
+    const PtParamsD d = makePtParams(*p, sc->nLights, nmaterials);
+    DeviceObj *dev = sc->dev;
+    const long long npaths = (long long)fb->W * fb->H * p->pixelSamples;
+    ensurePtWorkspace(dev, ptWorkspaceBytes(npaths));
+    const uint32_t slots = uint32_t(std::min<long long>(np.trainPaths, npaths));
+    const uint32_t maxLen1 = uint32_t(p->maxPathLength + 1);
+    o->frameBuffers(npaths, std::max<long long>(1, (long long)slots * maxLen1));
+    NrcFrameD nf;
+    nf.queries = o->queries;
+    nf.qpath = o->qpath;
+    nf.qout = o->qout;
+    nf.counters = o->fcounters;
+    nf.trainVerts = o->trainVerts;
+    nf.samples = o->samples;
+    nf.maxLen1 = maxLen1;
+    nf.trainSlots = slots;
+    nf.trainStride = slots ? uint32_t(std::max<long long>(1, npaths / slots)) : 1u;
+    // a different subset of paths trains every frame
+    uint32_t hsh = uint32_t(fb->frameID) * 2654435761u + 0x9e3779b9u;
+    hsh ^= hsh >> 15;
+    nf.trainOffset = hsh % nf.trainStride;
+    nf.sampleCap = uint32_t(o->vcap);
+    check(launchRenderPT(dev->tables, sc->view(), makeCamera(*camera), dev->filter(p->pixelFilter), d,
+                         sc->dMaterials, sc->dLights, sc->dLightCdf, dev->albedoTables(), fb->view(), false, dev->ptWs,
+                         dev->ptWsBytes, st, &nf, &NrcObj::inferHook, o),
+          "path tracer launch");
+    fb->frameID++;
+    framePostProcess(fb, st);
+    if (np.train)
+      for (int k = 0; k < np.trainSteps; k++)
+        o->train(o->samples, np.trainBatch, st, o->fcounters + 1, (long long)k * np.trainBatch);
   });
 }
 

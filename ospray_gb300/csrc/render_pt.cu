@@ -271,8 +271,9 @@ struct SegD {
   int rid, pad;
 };
 
-// path flags: AO request hit its first surface
-constexpr uint32_t F_AOHIT = 1u << 11;
+// path flags: AO request hit its first surface; the path bounced off a
+// diffuse surface (radiance-cache mode)
+constexpr uint32_t F_AOHIT = 1u << 11, F_DIFFUSE = 1u << 12;
 
 // the camera ray of sample s of pixel (x, y) of a path-traced frame, as a
 // fresh path record (meta2: first-hit instID, request, sampleID, pixel)
@@ -299,7 +300,10 @@ B200_D PathRec genPT(const PtCtx &c, const CameraD &cam, const PixelFilterD &pf,
   return r;
 }
 
-__global__ void k_pt_generate(PtCtx c, CameraD cam, PixelFilterD pf, FrameInfo fi, Workspace ws) {
+// nrcStride > 0: the radiance-cache training paths of this frame get their
+// slot in meta2.w (INVALID_ID for the others)
+__global__ void k_pt_generate(PtCtx c, CameraD cam, PixelFilterD pf, FrameInfo fi, Workspace ws, uint32_t nrcStride,
+                              uint32_t nrcOffset, uint32_t nrcSlots) {
   const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (p == 0) {
     ws.counters[0] = uint32_t(fi.npaths);
@@ -307,7 +311,12 @@ __global__ void k_pt_generate(PtCtx c, CameraD cam, PixelFilterD pf, FrameInfo f
   }
   if (p >= fi.npaths) return;
   const int pix = int(p / fi.spp), s = int(p % fi.spp);
-  ws.paths[p] = genPT(c, cam, pf, fi, pix % fi.W, pix / fi.W, s, 0u);
+  PathRec r = genPT(c, cam, pf, fi, pix % fi.W, pix / fi.W, s, 0u);
+  if (nrcStride) {
+    const uint32_t k = uint32_t(p) + nrcOffset;
+    r.meta2.w = (k % nrcStride == 0 && k / nrcStride < nrcSlots) ? k / nrcStride : INVALID_ID;
+  }
+  ws.paths[p] = r;
 }
 
 // Persistent any/closest-hit tracing over a queue with per-lane dynamic
@@ -462,10 +471,13 @@ B200_D void aoShade(const PtCtx &C, const AOParamsD &A, int W, PathRec &pr, cons
 // PathSampler.ispc:109-415): environment and virtual lights, postIntersect,
 // principled BSDF, NEE light samples (to the shadow queue), BSDF sample and
 // Russian roulette (to the next queue).
-template <bool BATCH>
+// NRC: the radiance-cache mode (training paths record their vertices; the
+// others end in a cache query at their first vertex after a diffuse bounce).
+template <bool BATCH, bool NRC>
 __global__ void __launch_bounds__(128) k_pt_shade(PtCtx c, Workspace ws, const uint32_t *qin, const uint32_t *cin,
                                                   uint32_t *qout, uint32_t *cout, uint32_t *cshadow,
-                                                  const ReqD *reqs) {
+                                                  const ReqD *reqs, NrcFrameD nf) {
+  static_assert(!(BATCH && NRC), "the radiance cache runs on single-request frames");
   const uint32_t n = *(volatile const uint32_t *)cin;
   const uint32_t stride = gridDim.x * blockDim.x;
   // warp-uniform loop so the appends can use warp votes
@@ -489,6 +501,7 @@ __global__ void __launch_bounds__(128) k_pt_shade(PtCtx c, Workspace ws, const u
       } else {
       const int nl = C.p.numLights;
       uint32_t flags = pr.meta.y;
+      bool diffuseSeen = (flags & F_DIFFUSE) != 0;
       int depth = int(flags & 0xffu);
       bool straightPath = (flags & F_STRAIGHT) != 0, firstBounceLight = (flags & F_FIRST) != 0;
       int lastNLS = int(flags >> 16);
@@ -556,8 +569,27 @@ __global__ void __launch_bounds__(128) k_pt_shade(PtCtx c, Workspace ws, const u
             frame(dg.Ns, fxv, fyv);
           }
           Principled bsdf;
-          bsdf.init(C.mats[e.materialID], fxv, fyv, dg.Ns, C.AT);
-          if (bsdf.impSum != 0.f) {
+          const MaterialD &mat = C.mats[e.materialID];
+          bsdf.init(mat, fxv, fyv, dg.Ns, C.AT);
+          bool cached = false;
+          if (NRC) {
+            if (pr.meta2.w != INVALID_ID) {  // training path: record the vertex
+              float *v = nf.trainVerts + (size_t(pr.meta2.w) * nf.maxLen1 + depth) * 20;
+              const float rv[20] = {dg.P.x, dg.P.y, dg.P.z, wo.x, wo.y, wo.z, dg.Ns.x, dg.Ns.y, dg.Ns.z,
+                                    mat.roughness, mat.r, mat.g, mat.b, throughput.x, throughput.y, throughput.z,
+                                    contribution.x, contribution.y, contribution.z, __uint_as_float(p)};
+              for (int k = 0; k < 20; k++) v[k] = rv[k];
+            } else if (depth >= 1 && diffuseSeen) {  // end in the cache
+              const uint32_t qn = atomicAdd(nf.counters, 1u);
+              float *q = nf.queries + size_t(qn) * 16;
+              const float qv[16] = {dg.P.x, dg.P.y, dg.P.z, wo.x, wo.y, wo.z, dg.Ns.x, dg.Ns.y, dg.Ns.z,
+                                    mat.roughness, mat.r, mat.g, mat.b, throughput.x, throughput.y, throughput.z};
+              for (int k = 0; k < 16; k++) q[k] = qv[k];
+              nf.qpath[qn] = p;
+              cached = true;
+            }
+          }
+          if (!cached && bsdf.impSum != 0.f) {
             // LDSampler of this path at its current group
             const uint32_t sampleID = pr.meta2.z;
             LDSampler ld;
@@ -625,6 +657,8 @@ __global__ void __launch_bounds__(128) k_pt_shade(PtCtx c, Workspace ws, const u
               }
             }
             if (cont) {
+              // a rough or non-metallic vertex counts as the path's diffuse bounce
+              if (mat.metallic < 0.5f || mat.roughness > 0.3f) diffuseSeen = true;
               if (!(ray.dir.x == fs.wi.x && ray.dir.y == fs.wi.y && ray.dir.z == fs.wi.z)) straightPath = false;
               pr.lastP = make_float4(dg.P.x, dg.P.y, dg.P.z, 0.f);
               pr.lastN = make_float4(dg.Ns.x, dg.Ns.y, dg.Ns.z, 0.f);
@@ -640,7 +674,7 @@ __global__ void __launch_bounds__(128) k_pt_shade(PtCtx c, Workspace ws, const u
       pr.thr = make_float4(throughput.x, throughput.y, throughput.z, alpha);
       pr.con = make_float4(contribution.x, contribution.y, contribution.z, 0.f);
       pr.meta.y = uint32_t(depth) | (straightPath ? F_STRAIGHT : 0u) | (firstBounceLight ? F_FIRST : 0u) |
-                  (cont ? 0u : F_ENDED) | (uint32_t(lastNLS) << 16);
+                  (cont ? 0u : F_ENDED) | (diffuseSeen ? F_DIFFUSE : 0u) | (uint32_t(lastNLS) << 16);
       ws.paths[p] = pr;
       }
     }
@@ -797,6 +831,58 @@ __global__ void k_stamp(unsigned long long *stamps, int first, int end) {
   for (int i = first + int(threadIdx.x); i < end; i += blockDim.x) stamps[i] = t;
 }
 
+// ---------------------------------------------------------------- radiance cache hooks
+// adds throughput x cached radiance to the paths that ended in a query, then
+// clears the query count for the next bounce (one thread per possible query;
+// the count is read before any thread clears it: the last block to finish
+// does the clearing)
+__global__ void k_nrc_apply(NrcFrameD nf, PathRec *paths, uint32_t cap) {
+  const uint32_t n = min(*(volatile const uint32_t *)nf.counters, cap);
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    const float *q = nf.queries + size_t(i) * 16;
+    const float *L = nf.qout + size_t(i) * 3;
+    float *con = &paths[nf.qpath[i]].con.x;
+    for (int k = 0; k < 3; k++) atomicAdd(con + k, q[13 + k] * fmaxf(L[k], 0.f));
+  }
+  __shared__ bool last;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    last = atomicAdd(nf.counters + 2, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (last && threadIdx.x == 0) {
+    nf.counters[0] = 0;
+    nf.counters[2] = 0;
+  }
+}
+
+// training samples from the recorded vertices: inputs and the radiance the
+// rest of the path brought back, (C_end - C_i) / T_i per channel
+__global__ void k_nrc_targets(NrcFrameD nf, const PathRec *paths, long long nv) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= nv) return;
+  const float *v = nf.trainVerts + size_t(i) * 20;
+  const uint32_t p = __float_as_uint(v[19]);
+  if (p == 0xffffffffu) return;
+  const float4 cend = paths[p].con;
+  const float ce[3] = {cend.x, cend.y, cend.z};
+  float tgt[3];
+  bool ok = true;
+  for (int k = 0; k < 3; k++) {
+    const float T = v[13 + k];
+    tgt[k] = T > 0.f ? fmaxf(ce[k] - v[16 + k], 0.f) / T : 0.f;
+    ok = ok && isfinite(tgt[k]);
+  }
+  if (!ok) return;
+  const uint32_t si = atomicAdd(nf.counters + 1, 1u);
+  if (si >= nf.sampleCap) return;
+  float *o = nf.samples + size_t(si) * 16;
+  for (int k = 0; k < 13; k++) o[k] = v[k];
+  for (int k = 0; k < 3; k++) o[13 + k] = tgt[k];
+}
+
 // ---------------------------------------------------------------- albedo tables
 // MicrofacetAlbedo_integrate / MicrofacetDielectricReflectionAlbedo_integrate:
 // 32x32 stratified visible-normal samples per entry.
@@ -879,78 +965,6 @@ int persistentBlocks(const void *kernel, size_t smem) {
 
 }  // namespace
 
-cudaError_t computeAlbedoTables(AlbedoTablesD *T, cudaStream_t st) {
-  k_albedo_dir<<<(32 * 32 + 4096 + 127) / 128, 128, 0, st>>>(T);
-  k_albedo_avg<<<(32 + 256 + 127) / 128, 128, 0, st>>>(T);
-  return cudaGetLastError();
-}
-
-size_t ptWorkspaceBytes(long long npaths) {
-  auto up = [](size_t x) { return (x + 255) & ~size_t(255); };
-  return up(sizeof(PathRec) * npaths) + up(sizeof(HitBuf) * npaths) + 2 * up(4 * npaths) +
-         up(sizeof(ShadowRec) * 2 * npaths) + up(64);
-}
-
-cudaError_t launchRenderPT(const SamplerTables *T, const Scene &sc, const CameraD &cam, const PixelFilterD &pf,
-                           const PtParamsD &p, const MaterialD *mats, const LightD *lights, const float *lightCdf,
-                           const AlbedoTablesD *AT, const FrameD &fb, bool stats, void *workspace, size_t wsBytes,
-                           cudaStream_t st) {
-  FrameInfo fi;
-  fi.W = fb.W;
-  fi.H = fb.H;
-  fi.spp = p.spp;
-  fi.frameID = fb.frameID;
-  fi.rcpW = fdiv(1.f, float(fb.W));
-  fi.rcpH = fdiv(1.f, float(fb.H));
-  fi.npaths = (long long)fb.W * fb.H * p.spp;
-  if (ptWorkspaceBytes(fi.npaths) > wsBytes) return cudaErrorInvalidValue;
-  Workspace ws;
-  char *base = static_cast<char *>(workspace);
-  auto carve = [&](size_t bytes) {
-    char *q = base;
-    base += (bytes + 255) & ~size_t(255);
-    return q;
-  };
-  ws.paths = (PathRec *)carve(sizeof(PathRec) * fi.npaths);
-  ws.hits = (HitBuf *)carve(sizeof(HitBuf) * fi.npaths);
-  ws.qa = (uint32_t *)carve(4 * fi.npaths);
-  ws.qb = (uint32_t *)carve(4 * fi.npaths);
-  ws.shadows = (ShadowRec *)carve(sizeof(ShadowRec) * 2 * fi.npaths);
-  ws.counters = (uint32_t *)carve(64);
-  PtCtx c = {T, sc, p, mats, lights, lightCdf, AT, fb.frameID};
-  static int traceBlocks = 0, shadowBlocks = 0, shadeBlocks = 0;
-  if (!traceBlocks) {
-    traceBlocks = persistentBlocks((const void *)k_trace_queue<false, false, false>, TRACE_SMEM_BYTES);
-    shadowBlocks = persistentBlocks((const void *)k_trace_queue<true, false, false>, TRACE_SMEM_BYTES);
-    shadeBlocks = persistentBlocks((const void *)k_pt_shade<false>, TRACE_SMEM_BYTES);
-  }
-  const int gen = int((fi.npaths + 255) / 256);
-  k_pt_generate<<<gen, 256, 0, st>>>(c, cam, pf, fi, ws);
-  uint32_t *qs[2] = {ws.qa, ws.qb};
-  for (int b = 0; b <= p.maxPathLength; b++) {
-    const int cin = b & 1, cout = cin ^ 1;
-    k_bounce_reset<<<1, 1, 0, st>>>(ws.counters, cin, cout, nullptr);
-    const uint32_t *qin = b == 0 ? nullptr : qs[cin];
-    if (stats)
-      k_trace_queue<false, true, false><<<traceBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
-          sc, ws, qin, ws.counters + cin, ws.counters + 3, nullptr);
-    else
-      k_trace_queue<false, false, false><<<traceBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
-          sc, ws, qin, ws.counters + cin, ws.counters + 3, nullptr);
-    k_pt_shade<false><<<shadeBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(c, ws, qin, ws.counters + cin, qs[cout],
-                                                                          ws.counters + cout, ws.counters + 2, nullptr);
-    if (stats)
-      k_trace_queue<true, true, false><<<shadowBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
-          sc, ws, nullptr, ws.counters + 2, ws.counters + 4, nullptr);
-    else
-      k_trace_queue<true, false, false><<<shadowBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
-          sc, ws, nullptr, ws.counters + 2, ws.counters + 4, nullptr);
-  }
-  k_pt_finalize<<<(fb.W * fb.H + 127) / 128, 128, 0, st>>>(c, ws, fi, fb);
-  return cudaGetLastError();
-}
-
-
 namespace {
 Workspace carveWorkspace(void *workspace, long long npaths) {
   Workspace ws;
@@ -976,6 +990,85 @@ int smCount() {
   return sms > 0 ? sms : 1;
 }
 }  // namespace
+
+cudaError_t computeAlbedoTables(AlbedoTablesD *T, cudaStream_t st) {
+  k_albedo_dir<<<(32 * 32 + 4096 + 127) / 128, 128, 0, st>>>(T);
+  k_albedo_avg<<<(32 + 256 + 127) / 128, 128, 0, st>>>(T);
+  return cudaGetLastError();
+}
+
+size_t ptWorkspaceBytes(long long npaths) {
+  auto up = [](size_t x) { return (x + 255) & ~size_t(255); };
+  return up(sizeof(PathRec) * npaths) + up(sizeof(HitBuf) * npaths) + 2 * up(4 * npaths) +
+         up(sizeof(ShadowRec) * 2 * npaths) + up(64);
+}
+
+cudaError_t launchRenderPT(const SamplerTables *T, const Scene &sc, const CameraD &cam, const PixelFilterD &pf,
+                           const PtParamsD &p, const MaterialD *mats, const LightD *lights, const float *lightCdf,
+                           const AlbedoTablesD *AT, const FrameD &fb, bool stats, void *workspace, size_t wsBytes,
+                           cudaStream_t st, const NrcFrameD *nrc, void (*nrcInfer)(void *, cudaStream_t),
+                           void *nrcCtx) {
+  FrameInfo fi;
+  fi.W = fb.W;
+  fi.H = fb.H;
+  fi.spp = p.spp;
+  fi.frameID = fb.frameID;
+  fi.rcpW = fdiv(1.f, float(fb.W));
+  fi.rcpH = fdiv(1.f, float(fb.H));
+  fi.npaths = (long long)fb.W * fb.H * p.spp;
+  if (ptWorkspaceBytes(fi.npaths) > wsBytes) return cudaErrorInvalidValue;
+  if (nrc && (stats || !nrcInfer)) return cudaErrorInvalidValue;
+  Workspace ws = carveWorkspace(workspace, fi.npaths);
+  PtCtx c = {T, sc, p, mats, lights, lightCdf, AT, fb.frameID};
+  static int traceBlocks = 0, shadowBlocks = 0, shadeBlocks = 0, shadeNrcBlocks = 0;
+  if (!traceBlocks) {
+    traceBlocks = persistentBlocks((const void *)k_trace_queue<false, false, false>, TRACE_SMEM_BYTES);
+    shadowBlocks = persistentBlocks((const void *)k_trace_queue<true, false, false>, TRACE_SMEM_BYTES);
+    shadeBlocks = persistentBlocks((const void *)k_pt_shade<false, false>, TRACE_SMEM_BYTES);
+    shadeNrcBlocks = persistentBlocks((const void *)k_pt_shade<false, true>, TRACE_SMEM_BYTES);
+  }
+  const NrcFrameD nf = nrc ? *nrc : NrcFrameD{};
+  if (nrc) {
+    cudaMemsetAsync(nf.counters, 0, 16, st);
+    cudaMemsetAsync(nf.trainVerts, 0xff, size_t(nf.trainSlots) * nf.maxLen1 * 20 * 4, st);
+  }
+  const int gen = int((fi.npaths + 255) / 256);
+  k_pt_generate<<<gen, 256, 0, st>>>(c, cam, pf, fi, ws, nf.trainStride, nf.trainOffset, nf.trainSlots);
+  uint32_t *qs[2] = {ws.qa, ws.qb};
+  for (int b = 0; b <= p.maxPathLength; b++) {
+    const int cin = b & 1, cout = cin ^ 1;
+    k_bounce_reset<<<1, 1, 0, st>>>(ws.counters, cin, cout, nullptr);
+    const uint32_t *qin = b == 0 ? nullptr : qs[cin];
+    if (stats)
+      k_trace_queue<false, true, false><<<traceBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
+          sc, ws, qin, ws.counters + cin, ws.counters + 3, nullptr);
+    else
+      k_trace_queue<false, false, false><<<traceBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
+          sc, ws, qin, ws.counters + cin, ws.counters + 3, nullptr);
+    if (nrc)
+      k_pt_shade<false, true><<<shadeNrcBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
+          c, ws, qin, ws.counters + cin, qs[cout], ws.counters + cout, ws.counters + 2, nullptr, nf);
+    else
+      k_pt_shade<false, false><<<shadeBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
+          c, ws, qin, ws.counters + cin, qs[cout], ws.counters + cout, ws.counters + 2, nullptr, nf);
+    if (stats)
+      k_trace_queue<true, true, false><<<shadowBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
+          sc, ws, nullptr, ws.counters + 2, ws.counters + 4, nullptr);
+    else
+      k_trace_queue<true, false, false><<<shadowBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
+          sc, ws, nullptr, ws.counters + 2, ws.counters + 4, nullptr);
+    if (nrc) {  // answer this bounce's cache queries
+      nrcInfer(nrcCtx, st);
+      k_nrc_apply<<<unsigned((fi.npaths + 255) / 256), 256, 0, st>>>(nf, ws.paths, uint32_t(fi.npaths));
+    }
+  }
+  k_pt_finalize<<<(fb.W * fb.H + 127) / 128, 128, 0, st>>>(c, ws, fi, fb);
+  if (nrc) {
+    const long long nv = (long long)nf.trainSlots * nf.maxLen1;
+    k_nrc_targets<<<unsigned((nv + 255) / 256), 256, 0, st>>>(nf, ws.paths, nv);
+  }
+  return cudaGetLastError();
+}
 
 void planBatch(const SamplerTables *T, const AlbedoTablesD *AT, const BatchReqH *reqs, int n, long long wavePaths,
                std::vector<unsigned char> &tables, std::vector<BatchWave> &waves, size_t &segTableOffset) {
@@ -1065,8 +1158,8 @@ cudaError_t launchBatchWave(const void *dtables, size_t segTableOffset, const Ba
     const uint32_t *qin = b == 0 ? nullptr : qs[cin];
     k_trace_queue<false, false, true><<<traceBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
         noScene, ws, qin, ws.counters + cin, ws.counters + 3, reqs);
-    k_pt_shade<true><<<shadeBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(noCtx, ws, qin, ws.counters + cin, qs[cout],
-                                                                         ws.counters + cout, ws.counters + 2, reqs);
+    k_pt_shade<true, false><<<shadeBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
+        noCtx, ws, qin, ws.counters + cin, qs[cout], ws.counters + cout, ws.counters + 2, reqs, NrcFrameD{});
     k_trace_queue<true, false, true><<<traceBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
         noScene, ws, nullptr, ws.counters + 2, ws.counters + 4, reqs);
   }
