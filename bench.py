@@ -653,18 +653,96 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
+def run_nrc(args):
+    """Learned-cache path tracer vs plain path tracer on the instanced-spheres
+    scene: 1920x1080, 1 spp per frame, maxPathLength 8, static camera, up to
+    `--nrc-frames` frames each; both judged by relMSE against a 4096-spp plain
+    render (256 frames x 16 spp).  Reports each arm's device time to reach
+    relMSE <= 0.01 and the relMSE after every frame count in a coarse curve."""
+    import torch  # noqa: F401  (device init order as the other arms)
+    import ospray_gb300 as og
+    from ospray_gb300 import scenes
+    w, h = (int(x) for x in args.size.split("x")) if args.size else (1920, 1080)
+    data = scenes.pt_instanced_scene(width=w, height=h)
+    dev = og.Device(0)
+    scene = og.Scene(dev)
+    scenes.build_pt_scene(scene, data)
+    scene.set_lights([og.quad_light(L["position"], L["edge1"], L["edge2"], L["intensity"]) if L["type"] == "quad"
+                      else og.ambient_light(L["intensity"]) for L in data["lights"]])
+    c = data["camera"]
+    cam = og.camera_desc(c["position"], c["direction"], c["up"], fovy=c["fovy"], aspect=c["aspect"])
+    mats = og.materials_array(data["materials"])
+    ref_frames = max(1, args.nrc_ref_spp // 16)
+    t0 = time.perf_counter()
+    ref = og.Frame(dev, w, h, og.FB_COLOR | og.FB_ACCUM)
+    p16 = og.pt_params(spp=16, max_path_length=8, roulette_path_length=3)
+    for _ in range(ref_frames):
+        og.render_pt(scene, cam, p16, mats, ref)
+    dev.sync()
+    ref_s = time.perf_counter() - t0
+    p1 = og.pt_params(spp=1, max_path_length=8, roulette_path_length=3)
+    b = scene.bounds()
+
+    def arm(render):
+        fb = og.Frame(dev, w, h, og.FB_COLOR | og.FB_ACCUM)
+        total = 0.0
+        curve = []
+        reached = None
+        with Clocks(0) as clk:
+            for i in range(args.nrc_frames):
+                e0 = dev.record_event()
+                render(fb)
+                e1 = dev.record_event()
+                dev.sync()
+                total += dev.event_ms(e0, e1) * 1e-3
+                dev.release_event(e0)
+                dev.release_event(e1)
+                err = og.relmse(fb, ref)
+                if reached is None and err <= 0.01:
+                    reached = (i + 1, total)
+                if (i + 1) in (1, 2, 4, 8, 16, 32, 64, 128, 256, 512) or i + 1 == args.nrc_frames:
+                    curve.append({"frames": i + 1, "seconds": round(total, 4), "relmse": round(err, 5)})
+        return {"seconds_to_relmse_0.01": round(reached[1], 4) if reached else None,
+                "frames_to_relmse_0.01": reached[0] if reached else None,
+                "relmse_final": curve[-1]["relmse"], "seconds_total": round(total, 4),
+                "ms_per_frame": round(total / args.nrc_frames * 1e3, 3), "curve": curve, "clocks": clk.summary()}
+
+    plain = arm(lambda fb: og.render_pt(scene, cam, p1, mats, fb))
+    cache = og.RadianceCache(dev, b[:3], b[3:], learning_rate=1e-2, seed=1)
+    learned = arm(lambda fb: og.render_pt_nrc(scene, cam, p1, mats, fb, cache))
+    value = learned["seconds_to_relmse_0.01"]
+    line = {"metric": "seconds to relMSE<=0.01 (learned cache)", "value": value, "unit": "s", "n_gpus": 1,
+            "steps": args.nrc_frames, "warmup": 0, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 render, bf16 MLP", "data": "synthetic (seeded generators)",
+            "config": {"workload": "nrc_instanced_spheres_1080p", "width": w, "height": h, "spp_per_frame": 1,
+                       "maxPathLength": 8, "roulettePathLength": 3, "frames": args.nrc_frames,
+                       "cache": "16-level hash grid (2^19 x 2 fp16 per level) + 64x4 ReLU MLP, bf16 mma, Adam 1e-2, "
+                                "16384 training paths, 4 x 16384 samples per frame",
+                       "reference": {"spp": ref_frames * 16, "renderer": "plain GPU path tracer",
+                                     "seconds": round(ref_s, 2)}},
+            "learned": learned, "plain": plain,
+            "speedup_time_to_relmse": (round(plain["seconds_to_relmse_0.01"] / value, 3)
+                                       if value and plain["seconds_to_relmse_0.01"] else None)}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
-    ap.add_argument("--workload", default="pt", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="pt", choices=sorted(WORKLOADS) + ["nrc"])
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU-baseline work")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--size", default=None, help="WxH override (profiling small cases; not the bench config)")
     ap.add_argument("--spp", type=int, default=None, help="spp override (path tracer; profiling only)")
+    ap.add_argument("--nrc-frames", type=int, default=256, help="frames per arm of the nrc workload")
+    ap.add_argument("--nrc-ref-spp", type=int, default=4096, help="spp of the nrc workload's reference image")
     args = ap.parse_args()
+    if args.workload == "nrc":
+        run_nrc(args)
+        return
     if args.size or args.spp:
         base = WORKLOADS[args.workload]
         w, h = (int(x) for x in args.size.split("x")) if args.size else (None, None)
