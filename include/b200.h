@@ -365,6 +365,8 @@ typedef struct {
   int trainSteps; /* default 4 */
   int trainBatch; /* default 16384 (4 x 16384 = 65,536 samples per frame) */
   int train;      /* default 1 */
+  int useCache;   /* default 1; 0: a warm-up frame (plain path tracing that only trains) */
+  int epochs;     /* default 1: passes of the trainSteps batches over the frame's samples */
 } b200_nrc_frame;
 void b200_nrc_frame_defaults(b200_nrc_frame *f);
 int b200_render_pt_nrc(b200_scene scene, const b200_camera_desc *camera, const b200_pt_params *params,

@@ -12,7 +12,7 @@ import os
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-BUILD = os.path.join(HERE, "_build")
+BUILD = os.environ.get("B200_BUILD_DIR") or os.path.join(HERE, "_build")
 
 _lib = None
 _scenes = None
@@ -591,13 +591,14 @@ class RadianceCache:
 
 class NrcFrame(ctypes.Structure):
     _fields_ = [("trainPaths", ctypes.c_int), ("trainSteps", ctypes.c_int), ("trainBatch", ctypes.c_int),
-                ("train", ctypes.c_int)]
+                ("train", ctypes.c_int), ("useCache", ctypes.c_int), ("epochs", ctypes.c_int)]
 
 
 def render_pt_nrc(scene, camera, params, materials, frame, cache, train=True, train_paths=16384, train_steps=4,
-                  train_batch=16384, stream=None):
+                  train_batch=16384, use_cache=True, epochs=1, stream=None):
     """One path-traced frame ending paths in the radiance cache (and training it)."""
-    f = NrcFrame(int(train_paths), int(train_steps), int(train_batch), int(bool(train)))
+    f = NrcFrame(int(train_paths), int(train_steps), int(train_batch), int(bool(train)), int(bool(use_cache)),
+                 int(epochs))
     arr, n = materials
     scene.device._check(lib().b200_render_pt_nrc(scene._h, ctypes.byref(camera), ctypes.byref(params),
                                                  ctypes.cast(arr, ctypes.c_void_p), n, frame._h, cache._h,

@@ -9,16 +9,32 @@ libb200_scenes.so (seeded synthetic scene generators).
 Translation units are compiled in parallel; a unit is rebuilt only when it or
 a header it may include is newer than its object file.
 """
+import json
 import os
 import shutil
 import subprocess
 import sys
+import time
 from concurrent.futures import ThreadPoolExecutor
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
-OUT = os.path.join(HERE, "_build")
+OUT = os.environ.get("B200_BUILD_DIR") or os.path.join(HERE, "_build")
 ROOT = os.path.dirname(HERE)
+TUNED = os.path.join(HERE, "tuned.json")
+
+
+def tuned_defines():
+    """-D flags of the build parameters chosen by tune_build.py (tuned.json),
+    overridden by B200_DEFINES (e.g. "B200_STACK_SMEM=32 B200_TRACE_MINBLOCKS=6")."""
+    vals = {}
+    if os.path.exists(TUNED):
+        with open(TUNED) as f:
+            vals.update(json.load(f).get("defines", {}))
+    for kv in os.environ.get("B200_DEFINES", "").split():
+        k, _, v = kv.partition("=")
+        vals[k] = v
+    return ["-D%s=%s" % (k, v) for k, v in sorted(vals.items())]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + [
@@ -59,6 +75,12 @@ def _run(cmd):
 def build(verbose=False):
     os.makedirs(OUT, exist_ok=True)
     hdr = _newest_header()
+    if os.path.exists(TUNED):
+        hdr = max(hdr, os.path.getmtime(TUNED))
+    defines = tuned_defines()
+    stamp = os.path.join(OUT, "defines.txt")
+    if not os.path.exists(stamp) or open(stamp).read() != " ".join(defines):
+        hdr = max(hdr, time.time())  # parameters changed: rebuild every unit
     nv = nvcc()
     jobs = []
     objs = []
@@ -67,7 +89,7 @@ def build(verbose=False):
         obj = os.path.join(OUT, u + ".o")
         objs.append(obj)
         if not os.path.exists(obj) or os.path.getmtime(obj) < max(os.path.getmtime(src), hdr):
-            jobs.append([nv] + NVCC_FLAGS + ["-c", src, "-o", obj])
+            jobs.append([nv] + NVCC_FLAGS + defines + ["-c", src, "-o", obj])
     with ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
         for r in ex.map(_run, jobs):
             if verbose and r.stderr:
@@ -75,6 +97,8 @@ def build(verbose=False):
     lib = os.path.join(OUT, "libb200.so")
     if jobs or not os.path.exists(lib):
         _run([nv] + ARCH + ["-shared", "-o", lib] + objs)
+    with open(stamp, "w") as f:
+        f.write(" ".join(defines))
     _build_ospray(hdr)
     scenes = os.path.join(OUT, "libb200_scenes.so")
     src = os.path.join(CSRC, "scenegen.cpp")

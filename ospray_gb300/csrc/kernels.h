@@ -66,6 +66,7 @@ struct NrcFrameD {
   float *trainVerts;   // trainSlots x maxLen1 x 20
   float *samples;      // sampleCap x 16
   uint32_t maxLen1, trainStride, trainOffset, trainSlots, sampleCap;
+  uint32_t useCache;  // 0: no path ends in the cache (training-data frames)
 };
 
 cudaError_t computeAlbedoTables(AlbedoTablesD *T, cudaStream_t st);

@@ -622,6 +622,8 @@ void b200_nrc_frame_defaults(b200_nrc_frame *f) {
   f->trainSteps = 4;
   f->trainBatch = 16384;
   f->train = 1;
+  f->useCache = 1;
+  f->epochs = 1;
 }
 
 int b200_render_pt_nrc(b200_scene s, const b200_camera_desc *camera, const b200_pt_params *p,
@@ -640,7 +642,7 @@ int b200_render_pt_nrc(b200_scene s, const b200_camera_desc *camera, const b200_
     if (!(p->pixelSamples >= 1 && p->maxPathLength >= 0 && p->pixelFilter >= B200_PF_POINT &&
           p->pixelFilter <= B200_PF_BLACKMAN_HARRIS && nmaterials >= 0 && (nmaterials == 0 || materials)))
       throw Error(B200_INVALID_ARGUMENT, "bad path tracer parameters");
-    if (np.trainPaths < 0 || np.trainSteps < 0 || np.trainBatch < 1)
+    if (np.trainPaths < 0 || np.trainSteps < 0 || np.trainBatch < 1 || np.epochs < 0)
       throw Error(B200_INVALID_ARGUMENT, "bad radiance cache frame parameters");
     cudaStream_t st = stream ? (cudaStream_t)stream : sc->dev->stream;
     uploadMaterials(sc, materials, nmaterials);
@@ -666,6 +668,7 @@ int b200_render_pt_nrc(b200_scene s, const b200_camera_desc *camera, const b200_
     hsh ^= hsh >> 15;
     nf.trainOffset = hsh % nf.trainStride;
     nf.sampleCap = uint32_t(o->vcap);
+    nf.useCache = np.useCache ? 1u : 0u;
     check(launchRenderPT(dev->tables, sc->view(), makeCamera(*camera), dev->filter(p->pixelFilter), d,
                          sc->dMaterials, sc->dLights, sc->dLightCdf, dev->albedoTables(), fb->view(), false, dev->ptWs,
                          dev->ptWsBytes, st, &nf, &NrcObj::inferHook, o),
@@ -673,8 +676,9 @@ int b200_render_pt_nrc(b200_scene s, const b200_camera_desc *camera, const b200_
     fb->frameID++;
     framePostProcess(fb, st);
     if (np.train)
-      for (int k = 0; k < np.trainSteps; k++)
-        o->train(o->samples, np.trainBatch, st, o->fcounters + 1, (long long)k * np.trainBatch);
+      for (int e = 0; e < np.epochs; e++)
+        for (int k = 0; k < np.trainSteps; k++)
+          o->train(o->samples, np.trainBatch, st, o->fcounters + 1, (long long)k * np.trainBatch);
   });
 }
 

@@ -324,7 +324,7 @@ __global__ void k_pt_generate(PtCtx c, CameraD cam, PixelFilterD pf, FrameInfo f
 // new ones with one atomic, so no lane idles while work remains.
 // In a batch (BATCH) every ray traverses its own request's scene.
 template <bool SHADOW, bool STATS, bool BATCH>
-__global__ void __launch_bounds__(TRACE_BLOCK) k_trace_queue(Scene sc, Workspace ws, const uint32_t *queue,
+__global__ void __launch_bounds__(TRACE_BLOCK, B200_TRACE_MINBLOCKS) k_trace_queue(Scene sc, Workspace ws, const uint32_t *queue,
                                                             const uint32_t *count, uint32_t *fetch,
                                                             const ReqD *reqs) {
   static_assert(!(BATCH && STATS), "batched traversal keeps no per-scene statistics");
@@ -579,7 +579,7 @@ __global__ void __launch_bounds__(128) k_pt_shade(PtCtx c, Workspace ws, const u
                                     mat.roughness, mat.r, mat.g, mat.b, throughput.x, throughput.y, throughput.z,
                                     contribution.x, contribution.y, contribution.z, __uint_as_float(p)};
               for (int k = 0; k < 20; k++) v[k] = rv[k];
-            } else if (depth >= 1 && diffuseSeen) {  // end in the cache
+            } else if (nf.useCache && depth >= 1 && diffuseSeen) {  // end in the cache
               const uint32_t qn = atomicAdd(nf.counters, 1u);
               float *q = nf.queries + size_t(qn) * 16;
               const float qv[16] = {dg.P.x, dg.P.y, dg.P.z, wo.x, wo.y, wo.z, dg.Ns.x, dg.Ns.y, dg.Ns.z,
@@ -1057,7 +1057,7 @@ cudaError_t launchRenderPT(const SamplerTables *T, const Scene &sc, const Camera
     else
       k_trace_queue<true, false, false><<<shadowBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
           sc, ws, nullptr, ws.counters + 2, ws.counters + 4, nullptr);
-    if (nrc) {  // answer this bounce's cache queries
+    if (nrc && nf.useCache) {  // answer this bounce's cache queries
       nrcInfer(nrcCtx, st);
       k_nrc_apply<<<unsigned((fi.npaths + 255) / 256), 256, 0, st>>>(nf, ws.paths, uint32_t(fi.npaths));
     }

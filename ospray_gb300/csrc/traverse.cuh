@@ -210,9 +210,18 @@ B200_D float pick8(const float (&a)[8], int i) {
 // warp's accesses are conflict-free); deeper items spill to a short local
 // array.  Kernels that trace declare TRACE_SMEM_BYTES of dynamic shared
 // memory and launch TRACE_BLOCK threads per block.
+// The shared-memory stack depth and the trace kernels' minimum resident
+// blocks per SM are build parameters (ospray_gb300/tuned.json, chosen by
+// ospray_gb300/tune_build.py on the GPU).
+#ifndef B200_STACK_SMEM
+#define B200_STACK_SMEM 24
+#endif
+#ifndef B200_TRACE_MINBLOCKS
+#define B200_TRACE_MINBLOCKS 1
+#endif
 constexpr int TRACE_BLOCK = 128;
-constexpr int STACK_SMEM = 24;
-constexpr int STACK_LOCAL = 40;
+constexpr int STACK_SMEM = B200_STACK_SMEM;
+constexpr int STACK_LOCAL = STACK_SMEM < 56 ? 64 - STACK_SMEM : 8;  // 64 entries in all
 constexpr size_t TRACE_SMEM_BYTES = size_t(STACK_SMEM) * TRACE_BLOCK * sizeof(uint2);
 
 constexpr uint32_t TAG_TLAS = 0u, TAG_BLAS = 1u << 30, TAG_INST = 2u << 30, TAG_MASK = 3u << 30;

@@ -1,0 +1,69 @@
+"""Build-time autotuner of the traversal kernels' compile-time shape.
+
+    python -m ospray_gb300.tune_build [--out tuned.json]
+
+The shared-memory traversal stack depth (B200_STACK_SMEM) and the trace
+kernels' minimum resident blocks per SM (B200_TRACE_MINBLOCKS, which bounds
+their registers) are compile-time constants, so each candidate is a separate
+build of libb200.so (into ospray_gb300/_variants/<tag>).  Each build renders
+the path-tracing workload at 960x540, 8 spp (bench.py, 3 warm-up frames and
+5 timed frames) on the GPU, and the fastest candidate's defines are written
+to tuned.json, which build.py then compiles with.  The run-time launch shape
+of batches is tuned separately (b200_batch_autotune).
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+
+CANDIDATES = [
+    {"B200_STACK_SMEM": 24, "B200_TRACE_MINBLOCKS": 1},
+    {"B200_STACK_SMEM": 32, "B200_TRACE_MINBLOCKS": 1},
+    {"B200_STACK_SMEM": 40, "B200_TRACE_MINBLOCKS": 1},
+    {"B200_STACK_SMEM": 32, "B200_TRACE_MINBLOCKS": 6},
+]
+
+
+def tag(c):
+    return "s%d_b%d" % (c["B200_STACK_SMEM"], c["B200_TRACE_MINBLOCKS"])
+
+
+def measure(c, size, spp):
+    env = dict(os.environ)
+    env["B200_BUILD_DIR"] = os.path.join(HERE, "_variants", tag(c))
+    env["B200_DEFINES"] = " ".join("%s=%s" % kv for kv in sorted(c.items()))
+    subprocess.run([sys.executable, "-m", "ospray_gb300.build"], cwd=ROOT, env=env, check=True,
+                   capture_output=True, text=True)
+    r = subprocess.run([sys.executable, "bench.py", "--workload", "pt", "--size", size, "--spp", str(spp),
+                        "--steps", "5", "--warmup", "3", "--no-cpu-baseline"], cwd=ROOT, env=env,
+                       capture_output=True, text=True, timeout=600)
+    if r.returncode != 0:
+        raise RuntimeError("candidate %s failed:\n%s" % (tag(c), r.stderr[-2000:]))
+    line = json.loads([ln for ln in r.stdout.splitlines() if ln.startswith("{")][-1])
+    return line["value"], line["ms_per_step"]
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--out", default=os.path.join(HERE, "tuned.json"))
+    ap.add_argument("--size", default="960x540")
+    ap.add_argument("--spp", type=int, default=8)
+    args = ap.parse_args()
+    results = []
+    for c in CANDIDATES:
+        mrays, ms = measure(c, args.size, args.spp)
+        results.append({"defines": c, "mrays_s": mrays, "ms_per_frame": ms})
+        print(json.dumps(results[-1]), flush=True)
+    best = max(results, key=lambda r: r["mrays_s"])
+    out = {"defines": best["defines"], "workload": "pt %s %d spp" % (args.size, args.spp), "candidates": results}
+    with open(args.out, "w") as f:
+        json.dump(out, f, indent=1)
+    print(json.dumps(out["defines"]))
+
+
+if __name__ == "__main__":
+    main()
