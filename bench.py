@@ -709,7 +709,11 @@ def run_nrc(args):
 
     plain = arm(lambda fb: og.render_pt(scene, cam, p1, mats, fb))
     cache = og.RadianceCache(dev, b[:3], b[3:], learning_rate=1e-2, seed=1)
-    learned = arm(lambda fb: og.render_pt_nrc(scene, cam, p1, mats, fb, cache))
+    # the cache's first frames train several epochs over their samples (it
+    # starts from random parameters); every frame after them trains one
+    learned = arm(lambda fb: og.render_pt_nrc(
+        scene, cam, p1, mats, fb, cache,
+        epochs=args.nrc_early_epochs if fb.frame_id < args.nrc_early_frames else 1))
     value = learned["seconds_to_relmse_0.01"]
     line = {"metric": "seconds to relMSE<=0.01 (learned cache)", "value": value, "unit": "s", "n_gpus": 1,
             "steps": args.nrc_frames, "warmup": 0, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
@@ -717,7 +721,8 @@ def run_nrc(args):
             "config": {"workload": "nrc_instanced_spheres_1080p", "width": w, "height": h, "spp_per_frame": 1,
                        "maxPathLength": 8, "roulettePathLength": 3, "frames": args.nrc_frames,
                        "cache": "16-level hash grid (2^19 x 2 fp16 per level) + 64x4 ReLU MLP, bf16 mma, Adam 1e-2, "
-                                "16384 training paths, 4 x 16384 samples per frame",
+                                "16384 training paths, 4 x 16384 samples per frame; the first %d frames train %d "
+                                "epochs" % (args.nrc_early_frames, args.nrc_early_epochs),
                        "reference": {"spp": ref_frames * 16, "renderer": "plain GPU path tracer",
                                      "seconds": round(ref_s, 2)}},
             "learned": learned, "plain": plain,
@@ -739,6 +744,8 @@ def main():
     ap.add_argument("--spp", type=int, default=None, help="spp override (path tracer; profiling only)")
     ap.add_argument("--nrc-frames", type=int, default=256, help="frames per arm of the nrc workload")
     ap.add_argument("--nrc-ref-spp", type=int, default=4096, help="spp of the nrc workload's reference image")
+    ap.add_argument("--nrc-early-frames", type=int, default=4, help="frames that train --nrc-early-epochs epochs")
+    ap.add_argument("--nrc-early-epochs", type=int, default=4)
     args = ap.parse_args()
     if args.workload == "nrc":
         run_nrc(args)

@@ -296,9 +296,13 @@ struct Traverser {
   template <bool STATS>
   B200_D bool step(const Scene &sc, TraceStats *ts) {
     if (!have) {
-      if (st.sp == 0) return true;
-      const uint2 s = st.pop();
-      if (__uint_as_float(s.y) > hit.t) return false;
+      // pop until an entry that can still hold a closer hit (culled entries
+      // cost no step of their own)
+      uint2 s;
+      do {
+        if (st.sp == 0) return true;
+        s = st.pop();
+      } while (__uint_as_float(s.y) > hit.t);
       const uint32_t tag = s.x & TAG_MASK;
       if (tag != TAG_BLAS && inBlas) {
         inBlas = false;
@@ -336,11 +340,21 @@ struct Traverser {
     const uint32_t mask = intersectChildren(n, org, rdir, ray.tnear, hit.t, dist);
     if (!mask) return false;
     if (!inBlas) {
-      // TLAS node: internal children and instances go on the stack
-      for (uint32_t m = mask; m; m &= m - 1) {
-        const int i = __ffs(m) - 1;
+      // TLAS node: internal children and instances go on the stack, farthest
+      // first, so the nearest is popped first and tightens hit.t early
+      for (uint32_t m = mask; m;) {
+        int i = __ffs(m) - 1;
+        float di = pick8(dist, i);
+        for (uint32_t r = m & (m - 1); r; r &= r - 1) {
+          const int j = __ffs(r) - 1;
+          const float dj = pick8(dist, j);
+          if (dj > di) {
+            i = j;
+            di = dj;
+          }
+        }
+        m &= ~(1u << i);
         const uint32_t meta = n.meta(i);
-        const float di = pick8(dist, i);
         if (meta & 0x80u) {
           st.push(TAG_TLAS | (n.childBase() + (meta & 7u)), di, sc.status);
         } else {
@@ -387,25 +401,32 @@ struct Traverser {
       }
     }
     if (anyHit && found) return true;
-    uint32_t nearest = 0xffffffffu;
-    float nearestD = INFINITY;
+    // internal children still in reach: the nearest is visited next, the
+    // others are pushed farthest first
+    uint32_t inner = 0;
     for (uint32_t m = mask; m; m &= m - 1) {
       const int i = __ffs(m) - 1;
-      const uint32_t meta = n.meta(i);
-      const float di = pick8(dist, i);
-      if (!(meta & 0x80u) || di > hit.t) continue;
-      const uint32_t child = n.childBase() + (meta & 7u);
-      if (di < nearestD) {
-        if (nearest != 0xffffffffu) st.push(TAG_BLAS | nearest, nearestD, sc.status);
-        nearest = child;
-        nearestD = di;
+      if ((n.meta(i) & 0x80u) && pick8(dist, i) <= hit.t) inner |= 1u << i;
+    }
+    while (inner) {
+      int i = __ffs(inner) - 1;
+      float di = pick8(dist, i);
+      for (uint32_t r = inner & (inner - 1); r; r &= r - 1) {
+        const int j = __ffs(r) - 1;
+        const float dj = pick8(dist, j);
+        if (dj > di) {
+          i = j;
+          di = dj;
+        }
+      }
+      inner &= ~(1u << i);
+      const uint32_t child = n.childBase() + (n.meta(i) & 7u);
+      if (!inner) {
+        node = child;
+        have = true;
       } else {
         st.push(TAG_BLAS | child, di, sc.status);
       }
-    }
-    if (nearest != 0xffffffffu) {
-      node = nearest;
-      have = true;
     }
     return false;
   }
