@@ -82,6 +82,11 @@ int b200_scene_add_spheres(b200_scene scene, const float *spheres, int64_t n, in
  * material_id indexes the renderer's material list (or -1 for none) */
 int b200_scene_add_instance(b200_scene scene, int geom, uint32_t inst_id, uint32_t geom_id, const float *xfm,
                             int material_id);
+/* build quality of the commits that follow (Group/World "dynamicScene",
+ * common/Group.cpp:17-31 selects Embree's low build quality): dynamic != 0
+ * builds the plain LBVH hierarchy (fastest build); the default splits the
+ * Morton-ordered primitive ranges by binned SAH */
+int b200_scene_set_dynamic(b200_scene scene, int dynamic);
 /* builds every BLAS not yet built and the TLAS */
 int b200_scene_commit(b200_scene scene);
 /* world bounds after commit: lo xyz, hi xyz */
@@ -155,6 +160,14 @@ typedef struct {
 } b200_tonemapper;
 /* fills `tm` with the defaults above */
 void b200_tonemapper_defaults(b200_tonemapper *tm);
+
+/* ospGetVariance: the framebuffer's error estimate (needs the VARIANCE
+ * channel; updated after every odd frame): per 8x8 task the mean over its
+ * pixels of |colour - odd-frame colour|_1 / sqrt(r + g + b + 1 - a) x 64;
+ * the mean of the tasks' errors at or above `threshold`, else the largest;
+ * inf before the first estimate (fb/frame_ops/Variance.ispc:11-49,
+ * Variance.cpp:32-46).  Synchronous.  Batched renders do not update it. */
+int b200_frame_variance(b200_frame fb, float threshold, float *out);
 
 /* image error of a framebuffer's accumulated colour against a reference
  * framebuffer of the same size: relMSE = mean over pixels and rgb of

@@ -160,6 +160,7 @@ def lib():
             "b200_scene_add_spheres": (I, [P, P, I64, ctypes.POINTER(I)]),
             "b200_scene_add_instance": (I, [P, I, U32, U32, P, I]),
             "b200_scene_commit": (I, [P]),
+            "b200_scene_set_dynamic": (I, [P, I]),
             "b200_scene_bounds": (I, [P, P]),
             "b200_scene_stats": (I, [P, P]),
             "b200_scene_counters": (I, [P, P, I]),
@@ -190,6 +191,7 @@ def lib():
             "b200_nrc_frame_defaults": (None, [P]),
             "b200_render_pt_nrc": (I, [P, ctypes.POINTER(CameraDesc), ctypes.POINTER(PTParams), P, I, P, P, P, P]),
             "b200_frame_relmse": (I, [P, P, ctypes.POINTER(ctypes.c_double)]),
+            "b200_frame_variance": (I, [P, F, ctypes.POINTER(F)]),
             "b200_event_record": (I, [P, ctypes.POINTER(P)]),
             "b200_event_query": (I, [P]),
             "b200_event_wait": (I, [P]),
@@ -297,6 +299,10 @@ class Scene:
         x = None if xfm is None else np.ascontiguousarray(xfm, dtype=np.float32).reshape(12)
         self.device._check(lib().b200_scene_add_instance(self._h, geom, inst_id, geom_id, _ptr(x), material))
 
+    def set_dynamic(self, dynamic=True):
+        """LBVH-only builds for the commits that follow (default: binned-SAH splits)."""
+        self.device._check(lib().b200_scene_set_dynamic(self._h, int(bool(dynamic))))
+
     def commit(self):
         self.device._check(lib().b200_scene_commit(self._h))
 
@@ -365,6 +371,12 @@ class Frame:
         self.width, self.height, self.channels, self.format = width, height, channels, format
         self._h = ctypes.c_void_p()
         device._check(lib().b200_frame_create(device._h, width, height, format, channels, ctypes.byref(self._h)))
+
+    def variance(self, threshold=0.0):
+        """ospGetVariance: the task error estimate (inf before the first odd frame)."""
+        v = ctypes.c_float()
+        self.device._check(lib().b200_frame_variance(self._h, float(threshold), ctypes.byref(v)))
+        return v.value
 
     def set_tonemapper(self, tm):
         """tm: ToneMapper (see tonemapper()) or None to remove it; applies from the next render."""

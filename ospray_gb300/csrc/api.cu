@@ -308,9 +308,9 @@ void SceneObj::commit() {
   for (auto &g : geoms) {
     if (g.built) continue;
     if (g.type == GEOM_TRIANGLES)
-      check(buildTriangleBLAS(g.dverts, g.dindex, int(g.nprims), st, g.blas), "BLAS build");
+      check(buildTriangleBLAS(g.dverts, g.dindex, int(g.nprims), st, g.blas, !dynamic), "BLAS build");
     else
-      check(buildSphereBLAS(g.dsph, int(g.nprims), st, g.blas), "BLAS build");
+      check(buildSphereBLAS(g.dsph, int(g.nprims), st, g.blas, !dynamic), "BLAS build");
     g.built = true;
   }
   // entries and their world boxes
@@ -385,7 +385,7 @@ void SceneObj::commit() {
     check(cudaMallocAsync(&dhi, sizeof(float4) * n, st), "alloc");
     check(cudaMemcpyAsync(dlo, lo.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, st), "upload");
     check(cudaMemcpyAsync(dhi, hi.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, st), "upload");
-    check(buildWide(dlo, dhi, int(n), st, tlas), "TLAS build");
+    check(buildWide(dlo, dhi, int(n), st, tlas, !dynamic), "TLAS build");
     cudaFreeAsync(dlo, st);
     cudaFreeAsync(dhi, st);
   }
@@ -414,7 +414,10 @@ FrameObj::FrameObj(DeviceObj *d, int w, int h, int fmt, uint32_t ch) : dev(d), W
   };
   alloc((void **)&color, n * sizeof(float4));
   if (ch & B200_FB_DEPTH) alloc((void **)&depth, n * 4);
-  if (ch & B200_FB_VARIANCE) alloc((void **)&variance, n * sizeof(float4));
+  if (ch & B200_FB_VARIANCE) {
+    alloc((void **)&variance, n * sizeof(float4));
+    alloc((void **)&taskErr, size_t(tasksX()) * tasksY() * 4);
+  }
   if (ch & B200_FB_NORMAL) alloc((void **)&normal, n * sizeof(float3));
   if (ch & B200_FB_ALBEDO) alloc((void **)&albedo, n * sizeof(float3));
   if (ch & B200_FB_ID_PRIMITIVE) alloc((void **)&primID, n * 4);
@@ -425,6 +428,7 @@ FrameObj::FrameObj(DeviceObj *d, int w, int h, int fmt, uint32_t ch) : dev(d), W
 
 FrameObj::~FrameObj() {
   cudaStreamSynchronize(dev->stream);
+  if (taskErr) cudaFree(taskErr);
   for (void *p : {(void *)color, (void *)depth, (void *)variance, (void *)normal, (void *)albedo, (void *)primID,
                   (void *)geomID, (void *)instID, mapped})
     if (p) cudaFree(p);
@@ -606,6 +610,12 @@ int b200_scene_add_instance(b200_scene s, int geom, uint32_t inst_id, uint32_t g
   });
 }
 
+int b200_scene_set_dynamic(b200_scene s, int dynamic) {
+  if (!s) return B200_INVALID_ARGUMENT;
+  reinterpret_cast<SceneObj *>(s)->dynamic = dynamic != 0;
+  return B200_NO_ERROR;
+}
+
 int b200_scene_commit(b200_scene s) {
   if (!s) return B200_INVALID_ARGUMENT;
   SceneObj *sc = reinterpret_cast<SceneObj *>(s);
@@ -693,6 +703,7 @@ int b200_frame_release(b200_frame f) {
 int b200_frame_reset(b200_frame f) {
   if (!f) return B200_INVALID_ARGUMENT;
   reinterpret_cast<FrameObj *>(f)->frameID = 0;
+  reinterpret_cast<FrameObj *>(f)->taskErrValid = false;
   return B200_NO_ERROR;
 }
 

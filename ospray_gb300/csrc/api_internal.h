@@ -75,6 +75,7 @@ struct SceneObj {
   uint32_t *status = nullptr;
   unsigned long long *counters = nullptr;  // traversal statistics (render stats mode)
   bool committed = false;
+  bool dynamic = false;  // LBVH-only builds (fast build, lower quality)
   float bounds[6] = {0, 0, 0, 0, 0, 0};
   // path-tracer state: world lights and the renderer's material list
   LightD *dLights = nullptr;
@@ -114,6 +115,13 @@ struct FrameObj {
   float *depth = nullptr;
   float3 *normal = nullptr, *albedo = nullptr;
   uint32_t *primID = nullptr, *geomID = nullptr, *instID = nullptr;
+  // per 8x8 render task: the variance estimate of the last odd frame
+  // (Variance_kernel, fb/frame_ops/Variance.ispc:11-49); valid once computed
+  static constexpr int TASK = 8;
+  float *taskErr = nullptr;
+  bool taskErrValid = false;
+  int tasksX() const { return (W + TASK - 1) / TASK; }
+  int tasksY() const { return (H + TASK - 1) / TASK; }
   FrameObj(DeviceObj *d, int w, int h, int format, uint32_t ch);
   ~FrameObj();
   FrameD view() const;
@@ -129,6 +137,6 @@ AOParamsD makeAOParams(const b200_ao_params &p);
 ToneMapD makeToneMap(const b200_tonemapper &u);
 // tonemap (if set) + conversion of the accumulated colour into fb->mapped,
 // enqueued after every render (LocalFrameBuffer::postProcess)
-void framePostProcess(FrameObj *fb, cudaStream_t st);
+void framePostProcess(FrameObj *fb, cudaStream_t st, bool variance = true);
 
 }  // namespace b200

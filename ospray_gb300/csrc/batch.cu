@@ -148,7 +148,7 @@ struct BatchObj {
     check(launchStamp(dStamps, n, n + 1, st), "stamp");
     for (const BatchWave &w : waves) {
       check(launchBatchWave(dtables, segOff, w, tune, ws, wsBytes, dRays, st), "batch wave");
-      for (int r = w.completeFirst; r >= 0 && r < w.completeEnd; r++) framePostProcess(reqs[r].fb, st);
+      for (int r = w.completeFirst; r >= 0 && r < w.completeEnd; r++) framePostProcess(reqs[r].fb, st, false);
       if (w.completeFirst >= 0) check(launchStamp(dStamps, w.completeFirst, w.completeEnd, st), "stamp");
     }
   }

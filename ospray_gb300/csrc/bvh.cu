@@ -1,6 +1,6 @@
 // GPU acceleration-structure build: linear BVH (Morton order, Karras 2012
-// hierarchy) collapsed into the 80-byte quantised 8-wide node format of
-// common.cuh.  Replaces the Embree BLAS/TLAS builds the reference issues from
+// hierarchy, or binned-SAH splits of the Morton-ordered ranges) collapsed
+// into the 80-byte quantised 8-wide node format of common.cuh.  Replaces the Embree BLAS/TLAS builds the reference issues from
 // Mesh::commit / Spheres::commit / Group::commit / World::commit
 // (modules/cpu/geometry/Mesh.cpp:140-167, geometry/Spheres.cpp:63-97,
 // common/Group.cpp:17-31,69-143, common/World.cpp:16-35,70-188).
@@ -189,6 +189,122 @@ __global__ void k_bottom_up(int n, const uint32_t *left, const uint32_t *right, 
   }
 }
 
+// ---------------------------------------------------------------- binned-SAH refinement
+// The binary hierarchy is rebuilt top-down over the same Morton order: a node
+// covering the sorted range [first, first + count) is cut where the surface
+// area heuristic over SAH_BINS equal-count bins of its range is lowest,
+// instead of at the highest differing Morton bit.  Ranges stay contiguous, so
+// the output has the Karras layout (left/right/first, boxes with the count in
+// lo.w) that the 8-wide collapse reads.
+constexpr int SAH_BINS = 32;
+
+struct RangeTask {
+  uint32_t first, count;  // sorted range
+  uint32_t node;          // internal node to fill
+  uint32_t binOff;        // this task's bins in the level's bin array
+};
+
+// one warp per bin: the box of the bin's primitives
+__global__ void k_sah_bins(const RangeTask *tasks, int ntasks, const uint32_t *sorted, const float4 *plo,
+                           const float4 *phi, float4 *binLo, float4 *binHi, int nbins) {
+  const long long gw = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (gw >= nbins) return;
+  // the task owning bin gw: binOff is increasing over the task list
+  int lo = 0, hi = ntasks - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (tasks[mid].binOff <= uint32_t(gw))
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  const RangeTask t = tasks[lo];
+  const uint32_t B = min(uint32_t(SAH_BINS), t.count);
+  const uint32_t b = uint32_t(gw) - t.binOff;
+  if (b >= B) return;
+  const uint32_t s0 = t.first + uint32_t((unsigned long long)t.count * b / B);
+  const uint32_t s1 = t.first + uint32_t((unsigned long long)t.count * (b + 1) / B);
+  float4 l = make_float4(INFINITY, INFINITY, INFINITY, 0.f), h = make_float4(-INFINITY, -INFINITY, -INFINITY, 0.f);
+  for (uint32_t s = s0 + lane; s < s1; s += 32) {
+    const uint32_t p = sorted[s];
+    const float4 a = plo[p], c = phi[p];
+    l = make_float4(fminf(l.x, a.x), fminf(l.y, a.y), fminf(l.z, a.z), 0.f);
+    h = make_float4(fmaxf(h.x, c.x), fmaxf(h.y, c.y), fmaxf(h.z, c.z), 0.f);
+  }
+  for (int o = 16; o; o >>= 1) {
+    l.x = fminf(l.x, __shfl_xor_sync(0xffffffffu, l.x, o));
+    l.y = fminf(l.y, __shfl_xor_sync(0xffffffffu, l.y, o));
+    l.z = fminf(l.z, __shfl_xor_sync(0xffffffffu, l.z, o));
+    h.x = fmaxf(h.x, __shfl_xor_sync(0xffffffffu, h.x, o));
+    h.y = fmaxf(h.y, __shfl_xor_sync(0xffffffffu, h.y, o));
+    h.z = fmaxf(h.z, __shfl_xor_sync(0xffffffffu, h.z, o));
+  }
+  if (lane == 0) {
+    binLo[gw] = l;
+    binHi[gw] = h;
+  }
+}
+
+__device__ __forceinline__ float halfArea(float4 l, float4 h) {
+  const float dx = h.x - l.x, dy = h.y - l.y, dz = h.z - l.z;
+  return dx * dy + dy * dz + dz * dx;
+}
+
+// one thread per task: the SAH-best bin boundary, the node's box, its
+// children (leaf references for single primitives, new tasks otherwise)
+__global__ void k_sah_split(const RangeTask *tasks, int ntasks, const float4 *binLo, const float4 *binHi,
+                            RangeTask *next, uint32_t *nodeCounter, unsigned long long *taskBins, uint32_t *left,
+                            uint32_t *right, uint32_t *first, float4 *blo, float4 *bhi) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ntasks) return;
+  const RangeTask t = tasks[i];
+  const uint32_t B = min(uint32_t(SAH_BINS), t.count);
+  float sufA[SAH_BINS];
+  float4 sl = make_float4(INFINITY, INFINITY, INFINITY, 0.f), sh = make_float4(-INFINITY, -INFINITY, -INFINITY, 0.f);
+  for (int b = int(B) - 1; b >= 0; b--) {
+    const float4 a = binLo[t.binOff + b], c = binHi[t.binOff + b];
+    sl = make_float4(fminf(sl.x, a.x), fminf(sl.y, a.y), fminf(sl.z, a.z), 0.f);
+    sh = make_float4(fmaxf(sh.x, c.x), fmaxf(sh.y, c.y), fmaxf(sh.z, c.z), 0.f);
+    sufA[b] = halfArea(sl, sh);
+  }
+  // sl/sh now hold the node's box
+  float4 pl = make_float4(INFINITY, INFINITY, INFINITY, 0.f), ph = make_float4(-INFINITY, -INFINITY, -INFINITY, 0.f);
+  uint32_t bestN = t.count / 2;
+  float bestC = INFINITY;
+  for (uint32_t b = 1; b < B; b++) {
+    const float4 a = binLo[t.binOff + b - 1], c = binHi[t.binOff + b - 1];
+    pl = make_float4(fminf(pl.x, a.x), fminf(pl.y, a.y), fminf(pl.z, a.z), 0.f);
+    ph = make_float4(fmaxf(ph.x, c.x), fmaxf(ph.y, c.y), fmaxf(ph.z, c.z), 0.f);
+    const uint32_t nl = uint32_t((unsigned long long)t.count * b / B);
+    const float cost = halfArea(pl, ph) * float(nl) + sufA[b] * float(t.count - nl);
+    if (cost < bestC) {
+      bestC = cost;
+      bestN = nl;
+    }
+  }
+  bestN = min(max(bestN, 1u), t.count - 1);
+  first[t.node] = t.first;
+  blo[t.node] = make_float4(sl.x, sl.y, sl.z, __uint_as_float(t.count));
+  bhi[t.node] = make_float4(sh.x, sh.y, sh.z, 0.f);
+  const uint32_t cf[2] = {t.first, t.first + bestN}, cc[2] = {bestN, t.count - bestN};
+  uint32_t ref[2];
+  for (int k = 0; k < 2; k++) {
+    if (cc[k] == 1) {
+      ref[k] = LEAF_BIT | cf[k];
+    } else {
+      ref[k] = atomicAdd(nodeCounter, 1u);
+      // task slot (low word) and bin offset (high word) from one atomic, so
+      // bin offsets increase with the slots
+      const unsigned long long old =
+          atomicAdd(taskBins, (unsigned long long)min(uint32_t(SAH_BINS), cc[k]) << 32 | 1ull);
+      next[uint32_t(old)] = {cf[k], cc[k], ref[k], uint32_t(old >> 32)};
+    }
+  }
+  left[t.node] = ref[0];
+  right[t.node] = ref[1];
+}
+
 struct Task {
   uint32_t ref;   // binary node reference (internal index or LEAF_BIT|sorted index)
   uint32_t wide;  // wide node index to write
@@ -361,15 +477,17 @@ inline int blocks(int n, int b) { return (n + b - 1) / b; }
 }  // namespace
 
 // Builds the wide BVH over n primitive boxes (device arrays lo/hi, float4).
-cudaError_t buildWide(const float4 *lo, const float4 *hi, int n, cudaStream_t st, WideBVH &out) {
+cudaError_t buildWide(const float4 *lo, const float4 *hi, int n, cudaStream_t st, WideBVH &out, bool sah) {
   out = WideBVH{};
   out.nprims = n;
   if (n <= 0) return cudaSuccess;
   cudaError_t err;
   const int ni = n > 1 ? n - 1 : 1;
   uint32_t *acc, *keys, *vals, *keys2, *vals2, *left, *right, *first, *parentInt, *parentLeaf, *flags, *counters;
-  float4 *blo, *bhi;
+  float4 *blo, *bhi, *binLo, *binHi;
   Task *qa, *qb;
+  RangeTask *ra, *rb;
+  unsigned long long *taskBins;
   // one scratch allocation, carved into 16-byte aligned pieces; the sizing
   // pass (base == null) and the carving pass use the same sequence
   char *base = nullptr;
@@ -397,6 +515,12 @@ cudaError_t buildWide(const float4 *lo, const float4 *hi, int n, cudaStream_t st
     bhi = (float4 *)carve(sizeof(float4) * size_t(ni));
     qa = (Task *)carve(sizeof(Task) * size_t(n + 1));
     qb = (Task *)carve(sizeof(Task) * size_t(n + 1));
+    const size_t ns = sah ? size_t(n) + SAH_BINS : 0;
+    ra = (RangeTask *)carve(sizeof(RangeTask) * ns);
+    rb = (RangeTask *)carve(sizeof(RangeTask) * ns);
+    binLo = (float4 *)carve(sizeof(float4) * ns);
+    binHi = (float4 *)carve(sizeof(float4) * ns);
+    taskBins = (unsigned long long *)carve(8);
   };
   layout();  // sizing pass with base == null
   if ((err = cudaMallocAsync(&base, off, st))) return err;
@@ -418,17 +542,46 @@ cudaError_t buildWide(const float4 *lo, const float4 *hi, int n, cudaStream_t st
   cudaFreeAsync(tmp, st);
   const uint32_t *sorted = vals2;
   Task root = {n > 1 ? 0u : LEAF_BIT, 0u};
-  if (n > 1) {
+  uint32_t *hcnt = nullptr;
+  cudaMallocHost(&hcnt, 16);
+  if (n > 1 && !sah) {
     cudaMemsetAsync(flags, 0, 4 * size_t(ni), st);
     k_karras<<<blocks(n - 1, 256), 256, 0, st>>>(keys2, n, left, right, first, parentInt, parentLeaf);
     k_bottom_up<<<blocks(n, 256), 256, 0, st>>>(n, left, right, parentInt, parentLeaf, sorted, lo, hi, blo, bhi,
                                                  flags);
+  } else if (n > 1) {
+    // top-down binned SAH over the Morton order, one level per pass
+    const RangeTask rootTask = {0u, uint32_t(n), 0u, 0u};
+    cudaMemcpyAsync(ra, &rootTask, sizeof(rootTask), cudaMemcpyHostToDevice, st);
+    const uint32_t one = 1;
+    cudaMemcpyAsync(counters, &one, 4, cudaMemcpyHostToDevice, st);
+    int nt = 1, nb = std::min(n, SAH_BINS);
+    for (int level = 0; nt > 0; level++) {
+      if (level > n + 64) {
+        err = cudaErrorUnknown;
+        break;
+      }
+      k_sah_bins<<<blocks(nb, 8), 256, 0, st>>>(ra, nt, sorted, lo, hi, binLo, binHi, nb);
+      cudaMemsetAsync(taskBins, 0, 8, st);
+      k_sah_split<<<blocks(nt, 128), 128, 0, st>>>(ra, nt, binLo, binHi, rb, counters, taskBins, left, right, first,
+                                                   blo, bhi);
+      unsigned long long tb = 0;
+      cudaMemcpyAsync(hcnt, taskBins, 8, cudaMemcpyDeviceToHost, st);
+      if ((err = cudaStreamSynchronize(st))) break;
+      memcpy(&tb, hcnt, 8);
+      nt = int(tb & 0xffffffffull);
+      nb = int(tb >> 32);
+      std::swap(ra, rb);
+    }
+  }
+  if (err != cudaSuccess) {
+    cudaFreeHost(hcnt);
+    cudaFreeAsync(base, st);
+    return err;
   }
   const uint32_t cinit[4] = {1, 0, 0, 0};
   cudaMemcpyAsync(qa, &root, sizeof(Task), cudaMemcpyHostToDevice, st);
   int ntasks = 1;
-  uint32_t *hcnt = nullptr;
-  cudaMallocHost(&hcnt, 16);
   cudaMemcpyAsync(counters, cinit, sizeof(cinit), cudaMemcpyHostToDevice, st);
   // every level consumes at least one binary level, so 2n+64 levels bound it
   for (int level = 0; ntasks > 0; level++) {
@@ -464,7 +617,8 @@ cudaError_t buildWide(const float4 *lo, const float4 *hi, int n, cudaStream_t st
   return cudaGetLastError();
 }
 
-cudaError_t buildTriangleBLAS(const float *d_verts, const uint32_t *d_index, int ntris, cudaStream_t st, BLAS &out) {
+cudaError_t buildTriangleBLAS(const float *d_verts, const uint32_t *d_index, int ntris, cudaStream_t st, BLAS &out,
+                              bool sah) {
   out = BLAS{};
   if (ntris <= 0) return cudaSuccess;
   float4 *lo, *hi;
@@ -472,7 +626,7 @@ cudaError_t buildTriangleBLAS(const float *d_verts, const uint32_t *d_index, int
   if ((err = cudaMallocAsync(&lo, sizeof(float4) * ntris, st))) return err;
   if ((err = cudaMallocAsync(&hi, sizeof(float4) * ntris, st))) return err;
   k_tri_bounds<<<blocks(ntris, 256), 256, 0, st>>>(d_verts, d_index, ntris, lo, hi);
-  if ((err = buildWide(lo, hi, ntris, st, out.bvh))) return err;
+  if ((err = buildWide(lo, hi, ntris, st, out.bvh, sah))) return err;
   if ((err = cudaMallocAsync(&out.prims, sizeof(float4) * 3 * size_t(ntris), st))) return err;
   k_gather_tris<<<blocks(ntris, 256), 256, 0, st>>>(out.bvh.leafPrim, ntris, d_verts, d_index, out.prims);
   cudaFreeAsync(lo, st);
@@ -480,7 +634,7 @@ cudaError_t buildTriangleBLAS(const float *d_verts, const uint32_t *d_index, int
   return cudaStreamSynchronize(st);
 }
 
-cudaError_t buildSphereBLAS(const float4 *d_sph, int n, cudaStream_t st, BLAS &out) {
+cudaError_t buildSphereBLAS(const float4 *d_sph, int n, cudaStream_t st, BLAS &out, bool sah) {
   out = BLAS{};
   if (n <= 0) return cudaSuccess;
   float4 *lo, *hi;
@@ -488,7 +642,7 @@ cudaError_t buildSphereBLAS(const float4 *d_sph, int n, cudaStream_t st, BLAS &o
   if ((err = cudaMallocAsync(&lo, sizeof(float4) * n, st))) return err;
   if ((err = cudaMallocAsync(&hi, sizeof(float4) * n, st))) return err;
   k_sph_bounds<<<blocks(n, 256), 256, 0, st>>>(d_sph, n, lo, hi);
-  if ((err = buildWide(lo, hi, n, st, out.bvh))) return err;
+  if ((err = buildWide(lo, hi, n, st, out.bvh, sah))) return err;
   if ((err = cudaMallocAsync(&out.prims, sizeof(float4) * size_t(n), st))) return err;
   if ((err = cudaMallocAsync(&out.primIDs, sizeof(uint32_t) * size_t(n), st))) return err;
   k_gather_sph<<<blocks(n, 256), 256, 0, st>>>(out.bvh.leafPrim, n, d_sph, out.prims, out.primIDs);

@@ -9,6 +9,7 @@
 // pixel once (16 B) and writes only the mapped result (4 B for RGBA8/SRGBA,
 // 16 B for RGBA32F); it is HBM-bound.
 #include <cmath>
+#include <vector>
 
 #include "api_internal.h"
 
@@ -104,7 +105,41 @@ ToneMapD makeToneMap(const b200_tonemapper &u) {
   return t;
 }
 
-void framePostProcess(FrameObj *fb, cudaStream_t st) {
+namespace {
+// Variance_kernel (fb/frame_ops/Variance.ispc:11-49): per 8x8 task, the mean
+// over its pixels (with den2 = r + g + b + 1 - a > 0) of the L1 difference
+// between the accumulated colour and the odd-frame accumulation, over
+// sqrt(den2), times 64
+__global__ void k_task_variance(const float4 *__restrict__ color, const float4 *__restrict__ var, int W, int H,
+                                int tx, int ty, float *__restrict__ err) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= tx * ty) return;
+  const int x0 = (t % tx) * FrameObj::TASK, y0 = (t / tx) * FrameObj::TASK;
+  float v = 0.f;
+  int cnt = 0;
+  for (int y = y0; y < min(y0 + FrameObj::TASK, H); y++)
+    for (int x = x0; x < min(x0 + FrameObj::TASK, W); x++) {
+      const float4 c = color[size_t(y) * W + x], s = var[size_t(y) * W + x];
+      const float den2 = c.x + c.y + c.z + (1.f - c.w);
+      if (den2 > 0.f) {
+        cnt++;
+        v += (fabsf(c.x - s.x) + fabsf(c.y - s.y) + fabsf(c.z - s.z) + fabsf(c.w - s.w)) / sqrtf(den2);
+      }
+    }
+  if (cnt) v /= float(cnt);
+  err[t] = v * 64.f;
+}
+}  // namespace
+
+void framePostProcess(FrameObj *fb, cudaStream_t st, bool variance) {
+  // the variance estimate follows every odd frame (LocalFrameBuffer::postProcess)
+  if (variance && fb->taskErr && fb->frameID >= 2 && ((fb->frameID - 1) & 1)) {
+    const int nt = fb->tasksX() * fb->tasksY();
+    k_task_variance<<<(nt + 127) / 128, 128, 0, st>>>(fb->color, fb->variance, fb->W, fb->H, fb->tasksX(),
+                                                       fb->tasksY(), fb->taskErr);
+    check(cudaGetLastError(), "variance estimate");
+    fb->taskErrValid = true;
+  }
   if (fb->format == B200_FB_NONE) return;
   const long long n = (long long)fb->W * fb->H;
   int sms = 152;
@@ -157,6 +192,39 @@ extern "C" int b200_frame_relmse(b200_frame f, b200_frame ref, double *out) {
     return B200_NO_ERROR;
   } catch (const Error &e) {
     a->dev->lastError = e.what();
+    return e.code;
+  }
+}
+
+// LiveVarianceFrameOp::getAvgError (fb/frame_ops/Variance.cpp:32-46): the mean
+// error of the tasks at or above the threshold, or the largest error when
+// none is; inf before any estimate (FrameBuffer::getVariance)
+extern "C" int b200_frame_variance(b200_frame f, float threshold, float *out) {
+  using namespace b200;
+  if (!f || !out) return B200_INVALID_ARGUMENT;
+  FrameObj *fb = reinterpret_cast<FrameObj *>(f);
+  if (!fb->taskErr || !fb->taskErrValid) {
+    *out = INFINITY;
+    return B200_NO_ERROR;
+  }
+  try {
+    check(cudaSetDevice(fb->dev->dev), "cudaSetDevice");
+    std::vector<float> e(size_t(fb->tasksX()) * fb->tasksY());
+    check(cudaMemcpyAsync(e.data(), fb->taskErr, e.size() * 4, cudaMemcpyDeviceToHost, fb->dev->stream), "read");
+    check(cudaStreamSynchronize(fb->dev->stream), "sync");
+    float mx = 0.f, sum = 0.f;
+    int active = 0;
+    for (float v : e) {
+      mx = std::fmax(mx, v);
+      if (v >= threshold) {
+        sum += v;
+        active++;
+      }
+    }
+    *out = active ? sum / float(active) : mx;
+    return B200_NO_ERROR;
+  } catch (const Error &e) {
+    fb->dev->lastError = e.what();
     return e.code;
   }
 }

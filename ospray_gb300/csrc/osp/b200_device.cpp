@@ -241,11 +241,14 @@ void B200Device::unmapFrameBuffer(const void *mapped, OSPFrameBuffer h) {
   f->release();
 }
 
-// no variance estimate is kept: the reference returns inf when no variance
-// buffer has been accumulated either (FrameBuffer::getVariance)
+// LocalFrameBuffer::getVariance (fb/LocalFB.cpp:263-272): the task error
+// estimate against the last renderer's varianceThreshold; inf without a
+// VARIANCE channel or before the first odd frame
 float B200Device::variance(OSPFrameBuffer h) {
-  asKind<FrameBufferObj>(h, OSP_FRAMEBUFFER, "ospGetVariance");
-  return INFINITY;
+  FrameBufferObj *f = asKind<FrameBufferObj>(h, OSP_FRAMEBUFFER, "ospGetVariance");
+  float v = INFINITY;
+  check(b200_frame_variance(f->fb, f->errorThreshold, &v));
+  return v;
 }
 
 void B200Device::resetAccumulation(OSPFrameBuffer h) {
@@ -287,6 +290,7 @@ OSPFuture B200Device::renderFrame(OSPFrameBuffer hf, OSPRenderer hr, OSPCamera h
     fut->release();
     throw;
   }
+  f->errorThreshold = r->varianceThreshold;
   for (Obj *o : {static_cast<Obj *>(f), static_cast<Obj *>(r), static_cast<Obj *>(c), static_cast<Obj *>(w)}) {
     o->retain();
     fut->held.push_back(o);

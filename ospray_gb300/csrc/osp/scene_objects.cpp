@@ -258,6 +258,7 @@ void WorldObj::commit(B200Device &dev) {
 
   b200_scene s = nullptr;
   dev.check(b200_scene_create(dev.handle(), &s));
+  dev.check(b200_scene_set_dynamic(s, getBool("dynamicScene", false) ? 1 : 0));
   try {
     std::map<GeometryObj *, int> geomIndex;
     std::map<MaterialObj *, int> matIndex;
@@ -340,6 +341,7 @@ void RendererObj::commit(B200Device &) {
   float bg[4];
   getColor4("backgroundColor", bg, bg0);
   const int pf = getInt("pixelFilter", OSP_PIXELFILTER_GAUSS);
+  varianceThreshold = getFloat("varianceThreshold", 0.f);
   const int maxDepth = std::max(0, getInt("maxPathLength", 20));
   const float minContribution = getFloat("minContribution", 0.001f);
   materials = objectList<MaterialObj>(getData("material"), OSP_MATERIAL, "renderer 'material'");

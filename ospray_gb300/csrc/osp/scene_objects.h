@@ -125,6 +125,7 @@ struct RendererObj : SceneObj {
   b200_pt_params pt = {};
   b200_scivis_params scivis = {};
   std::vector<Ref<MaterialObj>> materials;  // the "material" list
+  float varianceThreshold = 0.f;
   void commit(B200Device &) override;
 };
 
@@ -144,6 +145,7 @@ struct FrameBufferObj : SceneObj {
   OSPFrameBufferFormat format;
   uint32_t channels;
   std::map<const void *, std::vector<unsigned char>> mapped;
+  float errorThreshold = 0.f;  // varianceThreshold of the last renderer
   void commit(B200Device &) override;
 };
 

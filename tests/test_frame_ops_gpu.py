@@ -111,3 +111,31 @@ def test_pick_matches_oracle(b200_device):
                 misses += 1
                 assert (inst, geom, prim) == (0xffffffff,) * 3
     assert hits >= 10 and misses >= 10  # both surfaces and the sky were picked
+
+
+def test_variance_estimate_matches_oracle(b200_device, pt_world):
+    """ospGetVariance: inf until an odd frame has been accumulated, then the
+    task-error estimate of the oracle restatement of Variance_kernel."""
+    import os
+    import sys
+    import ospray_gb300 as og
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle"))
+    import variance as vref
+    d, g = pt_world
+    c = d["camera"]
+    cam = og.camera_desc(c["position"], c["direction"], c["up"], fovy=c["fovy"], aspect=c["aspect"])
+    fb = og.Frame(b200_device, W, H, og.FB_COLOR | og.FB_ACCUM | og.FB_VARIANCE)
+    p = og.pt_params(spp=1, max_path_length=4)
+    og.render_pt(g, cam, p, og.materials_array(d["materials"]), fb)
+    assert fb.variance() == float("inf")
+    values = []
+    for frame in range(2, 9):
+        og.render_pt(g, cam, p, og.materials_array(d["materials"]), fb)
+        if frame % 2 == 0:  # an odd frame (0-based) was just accumulated
+            err = vref.task_errors(fb.read(og.FB_ACCUM), fb.read(og.FB_VARIANCE))
+            for thr in (0.0, float(np.median(err))):
+                exp = vref.avg_error(err, thr)
+                got = fb.variance(thr)
+                assert abs(got - exp) <= 1e-4 * max(1.0, exp), (frame, thr, got, exp)
+            values.append(fb.variance(0.0))
+    assert values[-1] < values[0]  # the estimate falls as frames accumulate
