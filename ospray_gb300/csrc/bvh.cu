@@ -1,6 +1,7 @@
-// GPU acceleration-structure build: linear BVH (Morton order, Karras 2012
-// hierarchy, or binned-SAH splits of the Morton-ordered ranges) collapsed
-// into the 80-byte quantised 8-wide node format of common.cuh.  Replaces the Embree BLAS/TLAS builds the reference issues from
+// GPU acceleration-structure build: Morton-ordered primitives split either by
+// a top-down 3-axis binned SAH (default) or by the Karras 2012 LBVH hierarchy
+// (dynamic scenes), collapsed into the 80-byte quantised 8-wide node format
+// of common.cuh.  Replaces the Embree BLAS/TLAS builds the reference issues from
 // Mesh::commit / Spheres::commit / Group::commit / World::commit
 // (modules/cpu/geometry/Mesh.cpp:140-167, geometry/Spheres.cpp:63-97,
 // common/Group.cpp:17-31,69-143, common/World.cpp:16-35,70-188).
@@ -189,120 +190,237 @@ __global__ void k_bottom_up(int n, const uint32_t *left, const uint32_t *right, 
   }
 }
 
-// ---------------------------------------------------------------- binned-SAH refinement
-// The binary hierarchy is rebuilt top-down over the same Morton order: a node
-// covering the sorted range [first, first + count) is cut where the surface
-// area heuristic over SAH_BINS equal-count bins of its range is lowest,
-// instead of at the highest differing Morton bit.  Ranges stay contiguous, so
-// the output has the Karras layout (left/right/first, boxes with the count in
-// lo.w) that the 8-wide collapse reads.
-constexpr int SAH_BINS = 32;
+// ---------------------------------------------------------------- binned-SAH build
+// Top-down binned SAH (Wald 2007, "On fast construction of SAH-based bounding
+// volume hierarchies"): a node over the primitive range [first, first+count)
+// bins the primitives' centroids into SAH_BINS equal-width bins per axis of
+// the range's centroid bounds, takes the axis/boundary with the lowest
+// A_L*N_L + A_R*N_R, and partitions the range stably in place.  The Morton
+// order is the starting order, so sub-ranges keep spatial locality.  One block
+// per node and one launch per tree level; the output is the Karras layout
+// (left/right/first, boxes with the count in lo.w) that the 8-wide collapse
+// reads, down to single-primitive leaves.
+constexpr int SAH_BINS = 16;
+constexpr int SAH_MAX_THREADS = 256;
 
-struct RangeTask {
-  uint32_t first, count;  // sorted range
+struct SahTask {
+  uint32_t first, count;  // primitive range in the index array
   uint32_t node;          // internal node to fill
-  uint32_t binOff;        // this task's bins in the level's bin array
+  uint32_t pad;
+  float4 clo, chi;        // centroid bounds of the range
 };
 
-// one warp per bin: the box of the bin's primitives
-__global__ void k_sah_bins(const RangeTask *tasks, int ntasks, const uint32_t *sorted, const float4 *plo,
-                           const float4 *phi, float4 *binLo, float4 *binHi, int nbins) {
-  const long long gw = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (gw >= nbins) return;
-  // the task owning bin gw: binOff is increasing over the task list
-  int lo = 0, hi = ntasks - 1;
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (tasks[mid].binOff <= uint32_t(gw))
-      lo = mid;
-    else
-      hi = mid - 1;
-  }
-  const RangeTask t = tasks[lo];
-  const uint32_t B = min(uint32_t(SAH_BINS), t.count);
-  const uint32_t b = uint32_t(gw) - t.binOff;
-  if (b >= B) return;
-  const uint32_t s0 = t.first + uint32_t((unsigned long long)t.count * b / B);
-  const uint32_t s1 = t.first + uint32_t((unsigned long long)t.count * (b + 1) / B);
-  float4 l = make_float4(INFINITY, INFINITY, INFINITY, 0.f), h = make_float4(-INFINITY, -INFINITY, -INFINITY, 0.f);
-  for (uint32_t s = s0 + lane; s < s1; s += 32) {
-    const uint32_t p = sorted[s];
-    const float4 a = plo[p], c = phi[p];
-    l = make_float4(fminf(l.x, a.x), fminf(l.y, a.y), fminf(l.z, a.z), 0.f);
-    h = make_float4(fmaxf(h.x, c.x), fmaxf(h.y, c.y), fmaxf(h.z, c.z), 0.f);
-  }
-  for (int o = 16; o; o >>= 1) {
-    l.x = fminf(l.x, __shfl_xor_sync(0xffffffffu, l.x, o));
-    l.y = fminf(l.y, __shfl_xor_sync(0xffffffffu, l.y, o));
-    l.z = fminf(l.z, __shfl_xor_sync(0xffffffffu, l.z, o));
-    h.x = fmaxf(h.x, __shfl_xor_sync(0xffffffffu, h.x, o));
-    h.y = fmaxf(h.y, __shfl_xor_sync(0xffffffffu, h.y, o));
-    h.z = fmaxf(h.z, __shfl_xor_sync(0xffffffffu, h.z, o));
-  }
-  if (lane == 0) {
-    binLo[gw] = l;
-    binHi[gw] = h;
-  }
+// centroid and bin with explicit rounding, so the binning pass and the
+// partition pass compute identical bins
+__device__ __forceinline__ float3 centroidOf(const float4 *plo, const float4 *phi, uint32_t p) {
+  const float4 a = plo[p], b = phi[p];
+  return make_float3(__fmul_rn(0.5f, __fadd_rn(a.x, b.x)), __fmul_rn(0.5f, __fadd_rn(a.y, b.y)),
+                     __fmul_rn(0.5f, __fadd_rn(a.z, b.z)));
 }
+__device__ __forceinline__ int sahBin(float c, float lo, float scale) {
+  const float f = __fmul_rn(__fsub_rn(c, lo), scale);
+  return f >= float(SAH_BINS - 1) ? SAH_BINS - 1 : (f > 0.f ? int(f) : 0);
+}
+__device__ __forceinline__ float comp(float3 v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : v.z); }
+__device__ __forceinline__ float comp(float4 v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : v.z); }
 
-__device__ __forceinline__ float halfArea(float4 l, float4 h) {
-  const float dx = h.x - l.x, dy = h.y - l.y, dz = h.z - l.z;
+__device__ __forceinline__ float halfArea3(const float l[3], const float h[3]) {
+  const float dx = h[0] - l[0], dy = h[1] - l[1], dz = h[2] - l[2];
   return dx * dy + dy * dz + dz * dx;
 }
 
-// one thread per task: the SAH-best bin boundary, the node's box, its
-// children (leaf references for single primitives, new tasks otherwise)
-__global__ void k_sah_split(const RangeTask *tasks, int ntasks, const float4 *binLo, const float4 *binHi,
-                            RangeTask *next, uint32_t *nodeCounter, unsigned long long *taskBins, uint32_t *left,
-                            uint32_t *right, uint32_t *first, float4 *blo, float4 *bhi) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= ntasks) return;
-  const RangeTask t = tasks[i];
-  const uint32_t B = min(uint32_t(SAH_BINS), t.count);
-  float sufA[SAH_BINS];
-  float4 sl = make_float4(INFINITY, INFINITY, INFINITY, 0.f), sh = make_float4(-INFINITY, -INFINITY, -INFINITY, 0.f);
-  for (int b = int(B) - 1; b >= 0; b--) {
-    const float4 a = binLo[t.binOff + b], c = binHi[t.binOff + b];
-    sl = make_float4(fminf(sl.x, a.x), fminf(sl.y, a.y), fminf(sl.z, a.z), 0.f);
-    sh = make_float4(fmaxf(sh.x, c.x), fmaxf(sh.y, c.y), fmaxf(sh.z, c.z), 0.f);
-    sufA[b] = halfArea(sl, sh);
-  }
-  // sl/sh now hold the node's box
-  float4 pl = make_float4(INFINITY, INFINITY, INFINITY, 0.f), ph = make_float4(-INFINITY, -INFINITY, -INFINITY, 0.f);
-  uint32_t bestN = t.count / 2;
-  float bestC = INFINITY;
-  for (uint32_t b = 1; b < B; b++) {
-    const float4 a = binLo[t.binOff + b - 1], c = binHi[t.binOff + b - 1];
-    pl = make_float4(fminf(pl.x, a.x), fminf(pl.y, a.y), fminf(pl.z, a.z), 0.f);
-    ph = make_float4(fmaxf(ph.x, c.x), fmaxf(ph.y, c.y), fmaxf(ph.z, c.z), 0.f);
-    const uint32_t nl = uint32_t((unsigned long long)t.count * b / B);
-    const float cost = halfArea(pl, ph) * float(nl) + sufA[b] * float(t.count - nl);
-    if (cost < bestC) {
-      bestC = cost;
-      bestN = nl;
+__global__ void k_sah_root(const uint32_t *acc, int n, SahTask *tasks) {
+  SahTask t;
+  t.first = 0;
+  t.count = uint32_t(n);
+  t.node = 0;
+  t.pad = 0;
+  t.clo = make_float4(floatUnflip(acc[0]), floatUnflip(acc[1]), floatUnflip(acc[2]), 0.f);
+  t.chi = make_float4(floatUnflip(acc[3]), floatUnflip(acc[4]), floatUnflip(acc[5]), 0.f);
+  tasks[0] = t;
+}
+
+// counters[0]: next internal node, counters[1]: tasks of the next level
+__global__ void __launch_bounds__(SAH_MAX_THREADS) k_sah_level(const SahTask *tasks, SahTask *next, uint32_t *idx,
+                                                              uint32_t *tmp, const float4 *plo, const float4 *phi,
+                                                              uint32_t *counters, uint32_t *left, uint32_t *right,
+                                                              uint32_t *first, float4 *blo, float4 *bhi) {
+  __shared__ uint32_t sCnt[3][SAH_BINS];
+  __shared__ uint32_t sLo[3][SAH_BINS][3], sHi[3][SAH_BINS][3];  // flipped floats
+  __shared__ uint32_t sCb[2][6];                                  // children's centroid bounds, flipped
+  __shared__ float sCost[SAH_MAX_THREADS / 32];
+  __shared__ int sArg[SAH_MAX_THREADS / 32];
+  __shared__ uint32_t sWarp[SAH_MAX_THREADS / 32];
+  __shared__ int sBest;
+  __shared__ uint32_t sNL;
+  const SahTask t = tasks[blockIdx.x];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
+  const uint32_t end = t.first + t.count;
+  for (int i = tid; i < 3 * SAH_BINS; i += blockDim.x) {
+    (&sCnt[0][0])[i] = 0;
+    for (int k = 0; k < 3; k++) {
+      (&sLo[0][0][0])[3 * i + k] = 0xffffffffu;
+      (&sHi[0][0][0])[3 * i + k] = 0u;
     }
   }
-  bestN = min(max(bestN, 1u), t.count - 1);
-  first[t.node] = t.first;
-  blo[t.node] = make_float4(sl.x, sl.y, sl.z, __uint_as_float(t.count));
-  bhi[t.node] = make_float4(sh.x, sh.y, sh.z, 0.f);
-  const uint32_t cf[2] = {t.first, t.first + bestN}, cc[2] = {bestN, t.count - bestN};
-  uint32_t ref[2];
-  for (int k = 0; k < 2; k++) {
-    if (cc[k] == 1) {
-      ref[k] = LEAF_BIT | cf[k];
-    } else {
-      ref[k] = atomicAdd(nodeCounter, 1u);
-      // task slot (low word) and bin offset (high word) from one atomic, so
-      // bin offsets increase with the slots
-      const unsigned long long old =
-          atomicAdd(taskBins, (unsigned long long)min(uint32_t(SAH_BINS), cc[k]) << 32 | 1ull);
-      next[uint32_t(old)] = {cf[k], cc[k], ref[k], uint32_t(old >> 32)};
+  if (tid < 12) (&sCb[0][0])[tid] = (tid % 6) < 3 ? 0xffffffffu : 0u;
+  float clo[3], scale[3];
+  for (int k = 0; k < 3; k++) {
+    clo[k] = comp(t.clo, k);
+    const float ext = __fsub_rn(comp(t.chi, k), clo[k]);
+    scale[k] = ext > 0.f ? __fdiv_rn(float(SAH_BINS), ext) : 0.f;
+  }
+  __syncthreads();
+  // bin centroids; per bin the count and the box of its primitives
+  for (uint32_t s = t.first + tid; s < end; s += blockDim.x) {
+    const uint32_t p = idx[s];
+    const float4 a = plo[p], b = phi[p];
+    const float3 c = centroidOf(plo, phi, p);
+    for (int k = 0; k < 3; k++) {
+      const int bin = sahBin(comp(c, k), clo[k], scale[k]);
+      atomicAdd(&sCnt[k][bin], 1u);
+      atomicMin(&sLo[k][bin][0], floatFlip(a.x));
+      atomicMin(&sLo[k][bin][1], floatFlip(a.y));
+      atomicMin(&sLo[k][bin][2], floatFlip(a.z));
+      atomicMax(&sHi[k][bin][0], floatFlip(b.x));
+      atomicMax(&sHi[k][bin][1], floatFlip(b.y));
+      atomicMax(&sHi[k][bin][2], floatFlip(b.z));
     }
   }
-  left[t.node] = ref[0];
-  right[t.node] = ref[1];
+  __syncthreads();
+  // candidate splits: axis k after bin j, one thread each
+  constexpr int NCAND = 3 * (SAH_BINS - 1);
+  float cost = INFINITY;
+  if (tid < NCAND) {
+    const int k = tid / (SAH_BINS - 1), j = tid % (SAH_BINS - 1);
+    float ll[3] = {INFINITY, INFINITY, INFINITY}, lh[3] = {-INFINITY, -INFINITY, -INFINITY};
+    float rl[3] = {INFINITY, INFINITY, INFINITY}, rh[3] = {-INFINITY, -INFINITY, -INFINITY};
+    uint32_t nl = 0, nr = 0;
+    for (int b = 0; b < SAH_BINS; b++) {
+      const uint32_t cnt = sCnt[k][b];
+      if (!cnt) continue;
+      float *L = b <= j ? ll : rl, *H = b <= j ? lh : rh;
+      for (int q = 0; q < 3; q++) {
+        L[q] = fminf(L[q], floatUnflip(sLo[k][b][q]));
+        H[q] = fmaxf(H[q], floatUnflip(sHi[k][b][q]));
+      }
+      (b <= j ? nl : nr) += cnt;
+    }
+    if (nl && nr) cost = halfArea3(ll, lh) * float(nl) + halfArea3(rl, rh) * float(nr);
+  }
+  // block argmin, lowest candidate index on ties
+  int arg = tid;
+  for (int o = 16; o; o >>= 1) {
+    const float oc = __shfl_xor_sync(0xffffffffu, cost, o);
+    const int oa = __shfl_xor_sync(0xffffffffu, arg, o);
+    if (oc < cost || (oc == cost && oa < arg)) {
+      cost = oc;
+      arg = oa;
+    }
+  }
+  if (lane == 0) {
+    sCost[warp] = cost;
+    sArg[warp] = arg;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    float bc = sCost[0];
+    int ba = sArg[0];
+    for (int w = 1; w < nwarps; w++)
+      if (sCost[w] < bc) {
+        bc = sCost[w];
+        ba = sArg[w];
+      }
+    sBest = bc < INFINITY ? ba : -1;
+  }
+  __syncthreads();
+  const int best = sBest;
+  uint32_t nL = t.count / 2;  // identical centroids: split the range in the middle
+  if (best >= 0) {
+    const int bk = best / (SAH_BINS - 1), bj = best % (SAH_BINS - 1);
+    nL = 0;
+    for (int b = 0; b <= bj; b++) nL += sCnt[bk][b];
+    // stable partition into tmp: left part at [first, first+nL), right after
+    uint32_t doneL = 0, doneR = 0;
+    for (uint32_t c0 = t.first; c0 < end; c0 += blockDim.x) {
+      const uint32_t s = c0 + tid;
+      const bool valid = s < end;
+      const uint32_t p = valid ? idx[s] : 0u;
+      bool goL = false;
+      float3 c = make_float3(0.f, 0.f, 0.f);
+      if (valid) {
+        c = centroidOf(plo, phi, p);
+        goL = sahBin(comp(c, bk), clo[bk], scale[bk]) <= bj;
+      }
+      const uint32_t bal = __ballot_sync(0xffffffffu, goL);
+      if (lane == 0) sWarp[warp] = __popc(bal);
+      __syncthreads();
+      uint32_t offL = 0, totL = 0;
+      for (int w = 0; w < nwarps; w++) {
+        const uint32_t v = sWarp[w];
+        if (w < warp) offL += v;
+        totL += v;
+      }
+      const uint32_t inChunk = min(uint32_t(blockDim.x), end - c0);
+      if (valid) {
+        const uint32_t rankL = offL + __popc(bal & ((1u << lane) - 1u));
+        const uint32_t rankR = uint32_t(tid) - rankL;
+        const uint32_t dst = goL ? t.first + doneL + rankL : t.first + nL + doneR + rankR;
+        if (dst < end) tmp[dst] = p;
+        uint32_t *cb = sCb[goL ? 0 : 1];
+        atomicMin(&cb[0], floatFlip(c.x));
+        atomicMin(&cb[1], floatFlip(c.y));
+        atomicMin(&cb[2], floatFlip(c.z));
+        atomicMax(&cb[3], floatFlip(c.x));
+        atomicMax(&cb[4], floatFlip(c.y));
+        atomicMax(&cb[5], floatFlip(c.z));
+      }
+      doneL += totL;
+      doneR += inChunk - totL;
+      __syncthreads();
+    }
+    if (tid == 0) sNL = doneL;
+    __syncthreads();
+    for (uint32_t s = t.first + tid; s < end; s += blockDim.x) idx[s] = tmp[s];
+    nL = sNL;
+  }
+  if (tid == 0) {
+    // node box: the union of all bins of one axis
+    float l[3] = {INFINITY, INFINITY, INFINITY}, h[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int b = 0; b < SAH_BINS; b++)
+      for (int q = 0; q < 3; q++) {
+        l[q] = fminf(l[q], floatUnflip(sLo[0][b][q]));
+        h[q] = fmaxf(h[q], floatUnflip(sHi[0][b][q]));
+      }
+    first[t.node] = t.first;
+    blo[t.node] = make_float4(l[0], l[1], l[2], __uint_as_float(t.count));
+    bhi[t.node] = make_float4(h[0], h[1], h[2], 0.f);
+    if (nL == 0 || nL >= t.count) nL = t.count / 2;  // never taken: the partition matches the bins
+    const uint32_t cf[2] = {t.first, t.first + nL}, cc[2] = {nL, t.count - nL};
+    uint32_t ref[2];
+    for (int k = 0; k < 2; k++) {
+      if (cc[k] == 1) {
+        ref[k] = LEAF_BIT | cf[k];
+      } else {
+        ref[k] = atomicAdd(&counters[0], 1u);
+        SahTask ct;
+        ct.first = cf[k];
+        ct.count = cc[k];
+        ct.node = ref[k];
+        ct.pad = 0;
+        if (best >= 0) {
+          ct.clo = make_float4(floatUnflip(sCb[k][0]), floatUnflip(sCb[k][1]), floatUnflip(sCb[k][2]), 0.f);
+          ct.chi = make_float4(floatUnflip(sCb[k][3]), floatUnflip(sCb[k][4]), floatUnflip(sCb[k][5]), 0.f);
+        } else {
+          ct.clo = t.clo;
+          ct.chi = t.chi;
+        }
+        next[atomicAdd(&counters[1], 1u)] = ct;
+      }
+    }
+    left[t.node] = ref[0];
+    right[t.node] = ref[1];
+  }
 }
 
 struct Task {
@@ -484,10 +602,9 @@ cudaError_t buildWide(const float4 *lo, const float4 *hi, int n, cudaStream_t st
   cudaError_t err;
   const int ni = n > 1 ? n - 1 : 1;
   uint32_t *acc, *keys, *vals, *keys2, *vals2, *left, *right, *first, *parentInt, *parentLeaf, *flags, *counters;
-  float4 *blo, *bhi, *binLo, *binHi;
+  float4 *blo, *bhi;
   Task *qa, *qb;
-  RangeTask *ra, *rb;
-  unsigned long long *taskBins;
+  SahTask *ra, *rb;
   // one scratch allocation, carved into 16-byte aligned pieces; the sizing
   // pass (base == null) and the carving pass use the same sequence
   char *base = nullptr;
@@ -515,12 +632,10 @@ cudaError_t buildWide(const float4 *lo, const float4 *hi, int n, cudaStream_t st
     bhi = (float4 *)carve(sizeof(float4) * size_t(ni));
     qa = (Task *)carve(sizeof(Task) * size_t(n + 1));
     qb = (Task *)carve(sizeof(Task) * size_t(n + 1));
-    const size_t ns = sah ? size_t(n) + SAH_BINS : 0;
-    ra = (RangeTask *)carve(sizeof(RangeTask) * ns);
-    rb = (RangeTask *)carve(sizeof(RangeTask) * ns);
-    binLo = (float4 *)carve(sizeof(float4) * ns);
-    binHi = (float4 *)carve(sizeof(float4) * ns);
-    taskBins = (unsigned long long *)carve(8);
+    // a level holds at most n/2 tasks (each covers two or more primitives)
+    const size_t ns = sah ? size_t(n) / 2 + 1 : 0;
+    ra = (SahTask *)carve(sizeof(SahTask) * ns);
+    rb = (SahTask *)carve(sizeof(SahTask) * ns);
   };
   layout();  // sizing pass with base == null
   if ((err = cudaMallocAsync(&base, off, st))) return err;
@@ -550,27 +665,25 @@ cudaError_t buildWide(const float4 *lo, const float4 *hi, int n, cudaStream_t st
     k_bottom_up<<<blocks(n, 256), 256, 0, st>>>(n, left, right, parentInt, parentLeaf, sorted, lo, hi, blo, bhi,
                                                  flags);
   } else if (n > 1) {
-    // top-down binned SAH over the Morton order, one level per pass
-    const RangeTask rootTask = {0u, uint32_t(n), 0u, 0u};
-    cudaMemcpyAsync(ra, &rootTask, sizeof(rootTask), cudaMemcpyHostToDevice, st);
-    const uint32_t one = 1;
-    cudaMemcpyAsync(counters, &one, 4, cudaMemcpyHostToDevice, st);
-    int nt = 1, nb = std::min(n, SAH_BINS);
+    // top-down binned SAH from the Morton order, one level per launch; the
+    // index array (sorted) is partitioned in place, keys serve as scratch
+    k_sah_root<<<1, 1, 0, st>>>(acc, n, ra);
+    uint32_t *idx = vals2;
+    const uint32_t cinitSah[2] = {1, 0};
+    cudaMemcpyAsync(counters, cinitSah, sizeof(cinitSah), cudaMemcpyHostToDevice, st);
+    int nt = 1;
     for (int level = 0; nt > 0; level++) {
       if (level > n + 64) {
         err = cudaErrorUnknown;
         break;
       }
-      k_sah_bins<<<blocks(nb, 8), 256, 0, st>>>(ra, nt, sorted, lo, hi, binLo, binHi, nb);
-      cudaMemsetAsync(taskBins, 0, 8, st);
-      k_sah_split<<<blocks(nt, 128), 128, 0, st>>>(ra, nt, binLo, binHi, rb, counters, taskBins, left, right, first,
-                                                   blo, bhi);
-      unsigned long long tb = 0;
-      cudaMemcpyAsync(hcnt, taskBins, 8, cudaMemcpyDeviceToHost, st);
+      cudaMemsetAsync(counters + 1, 0, 4, st);
+      // few large ranges near the root: wide blocks; many small ones: narrow
+      const int threads = nt <= 4 * 152 ? SAH_MAX_THREADS : 64;
+      k_sah_level<<<nt, threads, 0, st>>>(ra, rb, idx, keys, lo, hi, counters, left, right, first, blo, bhi);
+      cudaMemcpyAsync(hcnt, counters, 8, cudaMemcpyDeviceToHost, st);
       if ((err = cudaStreamSynchronize(st))) break;
-      memcpy(&tb, hcnt, 8);
-      nt = int(tb & 0xffffffffull);
-      nb = int(tb >> 32);
+      nt = int(hcnt[1]);
       std::swap(ra, rb);
     }
   }

@@ -17,8 +17,9 @@ struct BLAS {
   uint32_t *primIDs = nullptr;  // spheres: primID per slot
 };
 
-// sah: split the Morton-ordered ranges by binned SAH (high quality); false:
-// the plain LBVH hierarchy (fastest build, the reference's dynamicScene)
+// sah: top-down 3-axis binned SAH (high quality, the reference's default
+// build quality); false: the plain LBVH hierarchy (fastest build, the
+// reference's dynamicScene)
 cudaError_t buildWide(const float4 *lo, const float4 *hi, int n, cudaStream_t st, WideBVH &out, bool sah = true);
 cudaError_t buildTriangleBLAS(const float *d_verts, const uint32_t *d_index, int ntris, cudaStream_t st, BLAS &out,
                               bool sah = true);
