@@ -476,42 +476,91 @@ __global__ void k_collapse(const Task *tasks, int ntasks, Task *next, uint32_t *
       ch[nc++] = right[r];
     }
   }
-  float4 lo[8], hi[8];
-  uint32_t cnt[8], fst[8];
-  int nInt = 0, nPrim = 0;
-  bool isInt[8];
+  float4 clo[8], chi[8];
+  uint32_t ccnt[8], cfst[8];
   for (int c = 0; c < nc; c++) {
     if (ch[c] & LEAF_BIT) {
       const uint32_t s = ch[c] & ~LEAF_BIT;
-      lo[c] = plo[sorted[s]];
-      hi[c] = phi[sorted[s]];
-      cnt[c] = 1;
-      fst[c] = s;
+      clo[c] = plo[sorted[s]];
+      chi[c] = phi[sorted[s]];
+      ccnt[c] = 1;
+      cfst[c] = s;
     } else {
-      lo[c] = blo[ch[c]];
-      hi[c] = bhi[ch[c]];
-      cnt[c] = __float_as_uint(lo[c].w);
-      fst[c] = first[ch[c]];
+      clo[c] = blo[ch[c]];
+      chi[c] = bhi[ch[c]];
+      ccnt[c] = __float_as_uint(clo[c].w);
+      cfst[c] = first[ch[c]];
     }
-    isInt[c] = cnt[c] > LEAF_MAX;
-    if (isInt[c])
+  }
+  // node box and quantisation grid
+  float nlo[3] = {INFINITY, INFINITY, INFINITY}, nhi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  for (int c = 0; c < nc; c++) {
+    nlo[0] = fminf(nlo[0], clo[c].x);
+    nlo[1] = fminf(nlo[1], clo[c].y);
+    nlo[2] = fminf(nlo[2], clo[c].z);
+    nhi[0] = fmaxf(nhi[0], chi[c].x);
+    nhi[1] = fmaxf(nhi[1], chi[c].y);
+    nhi[2] = fmaxf(nhi[2], chi[c].z);
+  }
+  // Octant slot order (Ylitie, Karras, Laine, HPG 2017, sec. 3.2): slot s
+  // takes the child lying farthest back along the direction of octant s
+  // (bit k set: negative along axis k), assigned greedily by lowest cost
+  // dot(child centre - node centre, d_s).  A ray of octant o then visits the
+  // slots in the order s ^ o = 0, 1, 2, ..., roughly near to far.
+  int bySlot[8];
+  {
+    float cost[8][8];
+    for (int c = 0; c < nc; c++) {
+      const float dx = 0.5f * (clo[c].x + chi[c].x) - 0.5f * (nlo[0] + nhi[0]);
+      const float dy = 0.5f * (clo[c].y + chi[c].y) - 0.5f * (nlo[1] + nhi[1]);
+      const float dz = 0.5f * (clo[c].z + chi[c].z) - 0.5f * (nlo[2] + nhi[2]);
+      for (int s = 0; s < 8; s++) cost[c][s] = ((s & 1) ? -dx : dx) + ((s & 2) ? -dy : dy) + ((s & 4) ? -dz : dz);
+    }
+    for (int s = 0; s < 8; s++) bySlot[s] = -1;
+    uint32_t freeC = (1u << nc) - 1u, freeS = 0xffu;
+    for (int it = 0; it < nc; it++) {
+      int bc = -1, bs = -1;
+      float bcost = INFINITY;
+      for (int c = 0; c < nc; c++) {
+        if (!(freeC >> c & 1u)) continue;
+        for (int s = 0; s < 8; s++) {
+          if (!(freeS >> s & 1u)) continue;
+          if (bc < 0 || cost[c][s] < bcost) {
+            bcost = cost[c][s];
+            bc = c;
+            bs = s;
+          }
+        }
+      }
+      bySlot[bs] = bc;
+      freeC &= ~(1u << bc);
+      freeS &= ~(1u << bs);
+    }
+  }
+  // children in slot order
+  float4 lo[8], hi[8];
+  uint32_t cnt[8], fst[8], ref[8];
+  bool used[8], isInt[8];
+  int nInt = 0, nPrim = 0;
+  for (int s = 0; s < 8; s++) {
+    const int c = bySlot[s];
+    used[s] = c >= 0;
+    isInt[s] = false;
+    if (!used[s]) continue;
+    lo[s] = clo[c];
+    hi[s] = chi[c];
+    cnt[s] = ccnt[c];
+    fst[s] = cfst[c];
+    ref[s] = ch[c];
+    isInt[s] = cnt[s] > LEAF_MAX;
+    if (isInt[s])
       nInt++;
     else
-      nPrim += int(cnt[c]);
+      nPrim += int(cnt[s]);
   }
   const uint32_t childBase = nInt ? atomicAdd(&counters[0], uint32_t(nInt)) : 0u;
   const uint32_t primBase = nPrim ? atomicAdd(&counters[1], uint32_t(nPrim)) : 0u;
   const uint32_t taskBase = nInt ? atomicAdd(&counters[2], uint32_t(nInt)) : 0u;
-  // node box and quantisation grid
-  float nlo[3] = {INFINITY, INFINITY, INFINITY}, nhi[3] = {-INFINITY, -INFINITY, -INFINITY};
-  for (int c = 0; c < nc; c++) {
-    nlo[0] = fminf(nlo[0], lo[c].x);
-    nlo[1] = fminf(nlo[1], lo[c].y);
-    nlo[2] = fminf(nlo[2], lo[c].z);
-    nhi[0] = fmaxf(nhi[0], hi[c].x);
-    nhi[1] = fmaxf(nhi[1], hi[c].y);
-    nhi[2] = fmaxf(nhi[2], hi[c].z);
-  }
   Node8 node;
   node.px = nlo[0];
   node.py = nlo[1];
@@ -535,37 +584,40 @@ __global__ void k_collapse(const Task *tasks, int ntasks, Task *next, uint32_t *
       }
       const float scale = __uint_as_float(uint32_t(e + 127) << 23);
       bool ok = true;
-      for (int c = 0; c < nc; c++) {
-        const float l = k == 0 ? lo[c].x : (k == 1 ? lo[c].y : lo[c].z);
-        const float h = k == 0 ? hi[c].x : (k == 1 ? hi[c].y : hi[c].z);
-        ok = ok && quantAxis(l, h, nlo[k], scale, ql[c], qh[c]);
+      for (int s = 0; s < 8; s++) {
+        if (!used[s]) continue;
+        const float l = k == 0 ? lo[s].x : (k == 1 ? lo[s].y : lo[s].z);
+        const float h = k == 0 ? hi[s].x : (k == 1 ? hi[s].y : hi[s].z);
+        ok = ok && quantAxis(l, h, nlo[k], scale, ql[s], qh[s]);
       }
       if (ok || e >= 127) break;
     }
     e8[k] = uint8_t(e + 127);
-    for (int c = 0; c < 8; c++) {
-      node.qlo[k][c] = c < nc ? ql[c] : uint8_t(255);
-      node.qhi[k][c] = c < nc ? qh[c] : uint8_t(0);
+    for (int s = 0; s < 8; s++) {
+      node.qlo[k][s] = used[s] ? ql[s] : uint8_t(255);
+      node.qhi[k][s] = used[s] ? qh[s] : uint8_t(0);
     }
   }
   node.ex = e8[0];
   node.ey = e8[1];
   node.ez = e8[2];
+  // internal children are stored in slot order, so child slot s is node
+  // childBase + popc(imask & ((1 << s) - 1)); leaf primitives likewise
   int ii = 0, po = 0;
-  for (int c = 0; c < 8; c++) {
-    if (c >= nc) {
-      node.meta[c] = 0;
+  for (int s = 0; s < 8; s++) {
+    if (!used[s]) {
+      node.meta[s] = 0;
       continue;
     }
-    if (isInt[c]) {
-      node.meta[c] = uint8_t(0x80 | ii);
-      node.imask |= uint8_t(1u << c);
-      next[taskBase + ii] = {ch[c], childBase + uint32_t(ii)};
+    if (isInt[s]) {
+      node.meta[s] = uint8_t(0x80 | ii);
+      node.imask |= uint8_t(1u << s);
+      next[taskBase + ii] = {ref[s], childBase + uint32_t(ii)};
       ii++;
     } else {
-      node.meta[c] = uint8_t((cnt[c] << 5) | uint32_t(po));
-      for (uint32_t j = 0; j < cnt[c]; j++) leafPrim[primBase + po + j] = sorted[fst[c] + j];
-      po += int(cnt[c]);
+      node.meta[s] = uint8_t((cnt[s] << 5) | uint32_t(po));
+      for (uint32_t j = 0; j < cnt[s]; j++) leafPrim[primBase + po + j] = sorted[fst[s] + j];
+      po += int(cnt[s]);
     }
   }
   nodes[task.wide] = node;

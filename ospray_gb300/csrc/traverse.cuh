@@ -132,8 +132,7 @@ B200_D bool better(float t, uint32_t inst, uint32_t geom, uint32_t prim, const H
   return prim < h.primID;
 }
 
-// Loads a node and intersects its 8 child boxes.  Returns a bit mask of hit
-// children; dist[i] holds the entry distance of hit child i.
+// The 80-byte node as five 16-byte words in registers.
 struct NodeView {
   uint4 q[5];
   B200_D float px() const { return __uint_as_float(q[0].x); }
@@ -160,7 +159,12 @@ B200_D NodeView loadNode(const Node8 *nodes, uint32_t i) {
   return n;
 }
 
-B200_D uint32_t intersectChildren(const NodeView &n, V3 org, V3 rdir, float tnear, float tfar, float dist[8]) {
+// Intersects the node's 8 child boxes with the ray (direction octant oct).
+// keys: the hit internal children, child slot i at bit i ^ oct, so the
+// lowest set bit is the next child in the octant's visiting order.  prims:
+// the leaf primitive slots (relative to primBase) of the hit leaf children.
+B200_D void intersectChildren(const NodeView &n, V3 org, V3 rdir, float tnear, float tfar, uint32_t oct,
+                              uint32_t &keys, uint32_t &prims) {
   const uint32_t e = n.exw();
   const float sx = __uint_as_float((e & 0xffu) << 23);
   const float sy = __uint_as_float(((e >> 8) & 0xffu) << 23);
@@ -169,11 +173,12 @@ B200_D uint32_t intersectChildren(const NodeView &n, V3 org, V3 rdir, float tnea
   // a compile-time constant so the node stays in registers
   const bool xn = rdir.x < 0.f, yn = rdir.y < 0.f, zn = rdir.z < 0.f;
   const float ox = n.px() - org.x, oy = n.py() - org.y, oz = n.pz() - org.z;
-  uint32_t mask = 0;
+  keys = 0;
+  prims = 0;
 #pragma unroll
   for (int i = 0; i < 8; i++) {
-    dist[i] = INFINITY;
-    if (n.meta(i) == 0) continue;
+    const uint32_t meta = n.meta(i);
+    if (meta == 0) continue;
     const float lx = fmaf(float(n.qbyte(0 + i)), sx, ox), hx = fmaf(float(n.qbyte(24 + i)), sx, ox);
     const float ly = fmaf(float(n.qbyte(8 + i)), sy, oy), hy = fmaf(float(n.qbyte(32 + i)), sy, oy);
     const float lz = fmaf(float(n.qbyte(16 + i)), sz, oz), hz = fmaf(float(n.qbyte(40 + i)), sz, oz);
@@ -183,64 +188,73 @@ B200_D uint32_t intersectChildren(const NodeView &n, V3 org, V3 rdir, float tnea
     const float t0 = fmaxf(fmaxf(t0x, t0y), fmaxf(t0z, tnear));
     const float t1 = fminf(fminf(t1x, t1y), t1z) * 1.0000004f;
     if (t0 <= fminf(t1, tfar)) {
-      mask |= 1u << i;
-      dist[i] = t0;
+      if (meta & 0x80u)
+        keys |= 1u << (uint32_t(i) ^ oct);
+      else
+        prims |= ((1u << (meta >> 5)) - 1u) << (meta & 31u);
     }
   }
-  return mask;
 }
 
-// a[i] for a runtime i without dynamic indexing (keeps `a` in registers)
-B200_D float pick8(const float (&a)[8], int i) {
-  float r = a[0];
-#pragma unroll
-  for (int k = 1; k < 8; k++) r = (i == k) ? a[k] : r;
-  return r;
+B200_D uint32_t octantOf(V3 d) {
+  return (d.x < 0.f ? 1u : 0u) | (d.y < 0.f ? 2u : 0u) | (d.z < 0.f ? 4u : 0u);
 }
 
 // ---------------------------------------------------------------- traversal
-// One stack serves both levels.  Items carry a 2-bit tag in the top bits of
-// the word: TLAS node, BLAS node of the instance being traversed, or an
-// instance (entry index) still to enter.  BLAS items always sit above the
-// TLAS/instance items pushed before their instance was entered, so popping a
-// non-BLAS item means the current instance is finished.
+// Compressed-wide-BVH traversal after Ylitie, Karras, Laine, "Efficient
+// Incoherent Ray Traversal on GPUs Through Compressed Wide BVHs" (HPG 2017).
+// Nothing is sorted at run time: a node's hit internal children form one
+// node group (child base, 8 hit bits in the octant's visiting order, the
+// node's internal-child mask) and its hit leaf primitives one primitive group
+// (primitive base, 24 hit bits).  Each node visit pushes at most the rest of
+// the current node group.  Primitive tests are postponed (the group pushed)
+// while only a few lanes of the warp would run them and node work is
+// pending, so lanes stay busy with node visits.
 //
-// The first STACK_SMEM items of each thread live in shared memory, one
-// column per thread (item k of thread t at word k * TRACE_BLOCK + t, so a
-// warp's accesses are conflict-free); deeper items spill to a short local
+// Both levels share one stack.  Entries carry their kind in the top two bits
+// of the second word: TLAS node group, BLAS node group, TLAS instance group
+// (TLAS leaf slots) or BLAS primitive group.  Popping a TLAS entry while in a
+// BLAS ends the current instance.
+//
+// The first STACK_SMEM entries of each thread live in shared memory, one
+// column per thread (entry k of thread t at word k * TRACE_BLOCK + t, so a
+// warp's accesses are conflict-free); deeper entries spill to a short local
 // array.  Kernels that trace declare TRACE_SMEM_BYTES of dynamic shared
 // memory and launch TRACE_BLOCK threads per block.
 // The shared-memory stack depth and the trace kernels' minimum resident
 // blocks per SM are build parameters (ospray_gb300/tuned.json, chosen by
 // ospray_gb300/tune_build.py on the GPU).
 #ifndef B200_STACK_SMEM
-#define B200_STACK_SMEM 24
+#define B200_STACK_SMEM 16
 #endif
 #ifndef B200_TRACE_MINBLOCKS
 #define B200_TRACE_MINBLOCKS 1
 #endif
+#ifndef B200_POSTPONE_LANES
+#define B200_POSTPONE_LANES 8
+#endif
 constexpr int TRACE_BLOCK = 128;
 constexpr int STACK_SMEM = B200_STACK_SMEM;
-constexpr int STACK_LOCAL = STACK_SMEM < 56 ? 64 - STACK_SMEM : 8;  // 64 entries in all
+constexpr int STACK_LOCAL = STACK_SMEM < 40 ? 48 - STACK_SMEM : 8;  // 48 entries in all
 constexpr size_t TRACE_SMEM_BYTES = size_t(STACK_SMEM) * TRACE_BLOCK * sizeof(uint2);
 
-constexpr uint32_t TAG_TLAS = 0u, TAG_BLAS = 1u << 30, TAG_INST = 2u << 30, TAG_MASK = 3u << 30;
+constexpr uint32_t G_TNODE = 0u << 30, G_BNODE = 1u << 30, G_TINST = 2u << 30, G_BPRIM = 3u << 30;
+constexpr uint32_t G_KIND = 3u << 30, G_BLAS = 1u << 30, G_PRIMS = 2u << 30;
 
 struct TraceStack {
   uint2 *smem;  // this thread's column
   uint2 local[STACK_LOCAL];
   int sp;
-  B200_D bool push(uint32_t item, float dist, uint32_t *status) {
+  B200_D void push(uint2 item, uint32_t *status) {
     if (sp < STACK_SMEM) {
-      smem[sp * TRACE_BLOCK] = make_uint2(item, __float_as_uint(dist));
+      smem[sp * TRACE_BLOCK] = item;
     } else if (sp < STACK_SMEM + STACK_LOCAL) {
-      local[sp - STACK_SMEM] = make_uint2(item, __float_as_uint(dist));
+      local[sp - STACK_SMEM] = item;
     } else {
-      atomicOr(status, 1u);  // overflow: the item is dropped and reported
-      return false;
+      atomicOr(status, 1u);  // overflow: the entry is dropped and reported
+      return;
     }
     sp++;
-    return true;
   }
   B200_D uint2 pop() {
     --sp;
@@ -254,9 +268,9 @@ B200_D uint2 *traceStackBase() {
   return s_traceStack + threadIdx.x;
 }
 
-// Resumable traversal of one ray: init() sets it up, each step() pops or
-// visits one node (testing the node's leaf primitives), until it reports the
-// ray finished.  Kernels drive the steps so that the lanes of a warp stay in
+// Resumable traversal of one ray: init() sets it up, each step() visits one
+// node and tests the primitives it exposes, until it reports the ray
+// finished.  Kernels drive the steps so that the lanes of a warp stay in
 // lockstep and can replace finished rays with new ones.
 struct Traverser {
   TraceStack st;
@@ -266,8 +280,11 @@ struct Traverser {
   const Node8 *nodes;
   const float4 *prims;
   const uint32_t *primIDs;
-  uint32_t etype, einst, egeom, eidx, node;
-  bool inBlas, have, anyHit, found;
+  uint32_t etype, einst, egeom, eidx;
+  uint32_t nbase, nbits;  // node group: child base; hit keys (bits 0-7) | imask << 8
+  uint32_t pbase, pbits;  // primitive group: slot base; hit slots (bits 0-23)
+  uint32_t oct;           // direction octant of the current frame
+  bool inBlas, anyHit, found;
   HitRec hit;
 
   B200_D void init(const Scene &sc, const Ray &r, bool any) {
@@ -282,150 +299,131 @@ struct Traverser {
     org = r.org;
     dir = r.dir;
     rdir = wrdir;
+    oct = octantOf(r.dir);
     nodes = sc.tlas;
     prims = nullptr;
     primIDs = nullptr;
     etype = einst = egeom = eidx = 0;
-    node = 0;
     inBlas = false;
     found = false;
-    have = sc.ntlas > 0;
+    // the TLAS root as a one-child group
+    nbase = 0;
+    nbits = sc.ntlas > 0 ? ((1u << oct) | (1u << 8)) : 0u;
+    pbase = pbits = 0;
+  }
+
+  B200_D bool idle() const { return !(nbits & 0xffu) && !pbits && st.sp == 0; }
+
+  B200_D void enterInstance(const Scene &sc, uint32_t entry) {
+    eidx = entry;
+    const Entry &e = sc.entries[eidx];
+    nodes = e.nodes;
+    prims = e.prims;
+    primIDs = e.primIDs;
+    etype = e.type;
+    einst = e.instID;
+    egeom = e.geomID;
+    if (!e.identity) {
+      const Xfm r = e.rcp;
+      org = xfmPoint(r, ray.org);
+      dir = xfmVector(r, ray.dir);
+      rdir = mk(1.f / dir.x, 1.f / dir.y, 1.f / dir.z);
+    }
+    pre = triPre(dir);
+    oct = octantOf(dir);
+    inBlas = true;
+    nbase = 0;
+    nbits = (1u << oct) | (1u << 8);
+  }
+
+  B200_D void leaveInstance(const Scene &sc) {
+    inBlas = false;
+    nodes = sc.tlas;
+    org = ray.org;
+    dir = ray.dir;
+    rdir = wrdir;
+    oct = octantOf(ray.dir);
   }
 
   // one traversal step; true when the ray is finished
   template <bool STATS>
   B200_D bool step(const Scene &sc, TraceStats *ts) {
-    if (!have) {
-      // pop until an entry that can still hold a closer hit (culled entries
-      // cost no step of their own)
-      uint2 s;
-      do {
-        if (st.sp == 0) return true;
-        s = st.pop();
-      } while (__uint_as_float(s.y) > hit.t);
-      const uint32_t tag = s.x & TAG_MASK;
-      if (tag != TAG_BLAS && inBlas) {
-        inBlas = false;
-        nodes = sc.tlas;
-        org = ray.org;
-        dir = ray.dir;
-        rdir = wrdir;
+    // 1) the next node of the current node group
+    if (nbits & 0xffu) {
+      const uint32_t key = uint32_t(__ffs(nbits & 0xffu) - 1);
+      nbits &= ~(1u << key);
+      const uint32_t slot = key ^ oct;
+      const uint32_t child = nbase + uint32_t(__popc((nbits >> 8) & ((1u << slot) - 1u)));
+      if (nbits & 0xffu) st.push(make_uint2(nbase, nbits | (inBlas ? G_BNODE : G_TNODE)), sc.status);
+      const NodeView n = loadNode(nodes, child);
+      if (STATS) ts->nodes++;
+      uint32_t keys, hitPrims;
+      intersectChildren(n, org, rdir, ray.tnear, hit.t, oct, keys, hitPrims);
+      nbase = n.childBase();
+      nbits = keys | (((n.exw() >> 24) & 0xffu) << 8);
+      pbase = n.primBase();
+      pbits = hitPrims;
+    }
+    // 2) the primitives of the current primitive group
+    while (pbits) {
+      if ((nbits & 0xffu) && __popc(__activemask()) < B200_POSTPONE_LANES) {
+        st.push(make_uint2(pbase, pbits | (inBlas ? G_BPRIM : G_TINST)), sc.status);
+        pbits = 0;
+        break;
       }
-      if (tag == TAG_INST) {
-        eidx = s.x & ~TAG_MASK;
-        const Entry &e = sc.entries[eidx];
-        nodes = e.nodes;
-        prims = e.prims;
-        primIDs = e.primIDs;
-        etype = e.type;
-        einst = e.instID;
-        egeom = e.geomID;
-        if (!e.identity) {
-          const Xfm r = e.rcp;
-          org = xfmPoint(r, ray.org);
-          dir = xfmVector(r, ray.dir);
-          rdir = mk(1.f / dir.x, 1.f / dir.y, 1.f / dir.z);
-        }
-        pre = triPre(dir);
-        inBlas = true;
-        node = 0;
+      const uint32_t k = uint32_t(__ffs(pbits) - 1);
+      pbits &= pbits - 1u;
+      const uint32_t slot = pbase + k;
+      if (!inBlas) {
+        // a TLAS leaf slot: enter its instance; the rest of this level waits
+        // on the stack (remaining instances above the node group)
+        if (nbits & 0xffu) st.push(make_uint2(nbase, nbits | G_TNODE), sc.status);
+        if (pbits) st.push(make_uint2(pbase, pbits | G_TINST), sc.status);
+        pbits = 0;
+        enterInstance(sc, __ldg(sc.tlasLeaf + slot));
+        break;
+      }
+      float t, u = 0.f, v = 0.f;
+      V3 Ng;
+      uint32_t prim;
+      bool h;
+      if (STATS) (etype == GEOM_TRIANGLES ? ts->tris : ts->spheres)++;
+      if (etype == GEOM_TRIANGLES) {
+        const float4 a = __ldg(prims + 3 * slot), b = __ldg(prims + 3 * slot + 1), c = __ldg(prims + 3 * slot + 2);
+        const V3 v0 = mk(a.x, a.y, a.z), v1 = mk(b.x, b.y, b.z), v2 = mk(c.x, c.y, c.z);
+        h = triTest(pre, org, ray.tnear, hit.t, v0, v1, v2, t, u, v);
+        if (h) Ng = cross(sub(v1, v0), sub(v2, v0));
+        prim = __float_as_uint(a.w);
       } else {
-        node = s.x & ~TAG_MASK;
+        h = sphTest(org, dir, ray.tnear, hit.t, __ldg(prims + slot), t, Ng);
+        prim = __ldg(primIDs + slot);
+      }
+      if (h && better(t, einst, egeom, prim, hit)) {
+        hit.t = t;
+        hit.u = u;
+        hit.v = v;
+        hit.Ng = Ng;
+        hit.primID = prim;
+        hit.geomID = egeom;
+        hit.instID = einst;
+        hit.entry = eidx;
+        found = true;
+        if (anyHit) return true;
       }
     }
-    have = false;
-    const NodeView n = loadNode(nodes, node);
-    if (STATS) ts->nodes++;
-    float dist[8];
-    const uint32_t mask = intersectChildren(n, org, rdir, ray.tnear, hit.t, dist);
-    if (!mask) return false;
-    if (!inBlas) {
-      // TLAS node: internal children and instances go on the stack, farthest
-      // first, so the nearest is popped first and tightens hit.t early
-      for (uint32_t m = mask; m;) {
-        int i = __ffs(m) - 1;
-        float di = pick8(dist, i);
-        for (uint32_t r = m & (m - 1); r; r &= r - 1) {
-          const int j = __ffs(r) - 1;
-          const float dj = pick8(dist, j);
-          if (dj > di) {
-            i = j;
-            di = dj;
-          }
-        }
-        m &= ~(1u << i);
-        const uint32_t meta = n.meta(i);
-        if (meta & 0x80u) {
-          st.push(TAG_TLAS | (n.childBase() + (meta & 7u)), di, sc.status);
-        } else {
-          const uint32_t cnt = meta >> 5, first = n.primBase() + (meta & 31u);
-          for (uint32_t k = 0; k < cnt; k++) st.push(TAG_INST | __ldg(sc.tlasLeaf + first + k), di, sc.status);
-        }
-      }
-      return false;
-    }
-    // BLAS node: leaves first (they tighten hit.t), then internal children
-    for (uint32_t m = mask; m; m &= m - 1) {
-      const int i = __ffs(m) - 1;
-      const uint32_t meta = n.meta(i);
-      if (meta & 0x80u) continue;
-      const uint32_t cnt = meta >> 5, first = n.primBase() + (meta & 31u);
-      for (uint32_t k = 0; k < cnt; k++) {
-        const uint32_t slot = first + k;
-        float t, u = 0.f, v = 0.f;
-        V3 Ng;
-        uint32_t prim;
-        bool h;
-        if (STATS) (etype == GEOM_TRIANGLES ? ts->tris : ts->spheres)++;
-        if (etype == GEOM_TRIANGLES) {
-          const float4 a = __ldg(prims + 3 * slot), b = __ldg(prims + 3 * slot + 1), c = __ldg(prims + 3 * slot + 2);
-          const V3 v0 = mk(a.x, a.y, a.z), v1 = mk(b.x, b.y, b.z), v2 = mk(c.x, c.y, c.z);
-          h = triTest(pre, org, ray.tnear, hit.t, v0, v1, v2, t, u, v);
-          if (h) Ng = cross(sub(v1, v0), sub(v2, v0));
-          prim = __float_as_uint(a.w);
-        } else {
-          h = sphTest(org, dir, ray.tnear, hit.t, __ldg(prims + slot), t, Ng);
-          prim = __ldg(primIDs + slot);
-        }
-        if (h && better(t, einst, egeom, prim, hit)) {
-          hit.t = t;
-          hit.u = u;
-          hit.v = v;
-          hit.Ng = Ng;
-          hit.primID = prim;
-          hit.geomID = egeom;
-          hit.instID = einst;
-          hit.entry = eidx;
-          found = true;
-        }
-      }
-    }
-    if (anyHit && found) return true;
-    // internal children still in reach: the nearest is visited next, the
-    // others are pushed farthest first
-    uint32_t inner = 0;
-    for (uint32_t m = mask; m; m &= m - 1) {
-      const int i = __ffs(m) - 1;
-      if ((n.meta(i) & 0x80u) && pick8(dist, i) <= hit.t) inner |= 1u << i;
-    }
-    while (inner) {
-      int i = __ffs(inner) - 1;
-      float di = pick8(dist, i);
-      for (uint32_t r = inner & (inner - 1); r; r &= r - 1) {
-        const int j = __ffs(r) - 1;
-        const float dj = pick8(dist, j);
-        if (dj > di) {
-          i = j;
-          di = dj;
-        }
-      }
-      inner &= ~(1u << i);
-      const uint32_t child = n.childBase() + (n.meta(i) & 7u);
-      if (!inner) {
-        node = child;
-        have = true;
+    // 3) both groups empty: the next group from the stack
+    if (!(nbits & 0xffu) && !pbits) {
+      if (st.sp == 0) return true;
+      const uint2 s = st.pop();
+      const uint32_t kind = s.y & G_KIND;
+      if (inBlas && !(kind & G_BLAS)) leaveInstance(sc);
+      if (kind & G_PRIMS) {
+        pbase = s.x;
+        pbits = s.y & 0xffffffu;
+        nbits = 0;
       } else {
-        st.push(TAG_BLAS | child, di, sc.status);
+        nbase = s.x;
+        nbits = s.y & 0xffffu;
       }
     }
     return false;
@@ -449,7 +447,7 @@ B200_D bool traceRay(const Scene &sc, const Ray &ray, HitRec &hit, bool anyHit, 
   const unsigned group = __activemask();
   Traverser tv;
   tv.init(sc, ray, anyHit);
-  bool done = !active || !tv.have;
+  bool done = !active || tv.idle();
   for (int guard = 0; guard < (1 << 18); guard++) {
     if (!__any_sync(group, !done)) break;
     if (!done) done = tv.step<STATS>(sc, ts);
