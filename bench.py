@@ -38,6 +38,12 @@ sys.path.insert(0, ROOT)
 
 L2_FLUSH_BYTES = 512 << 20
 
+# DRAM traffic of the dominant kernel per algorithmic byte, from one ncu
+# capture (dram__bytes_read.sum + dram__bytes_write.sum of the captured
+# launches / their algorithmic bytes); the summaries under profiles/ give the
+# commands.  Scaled to the bench's launches by their algorithmic bytes.
+TRAFFIC = {}
+
 
 def peaks():
     try:
@@ -501,6 +507,12 @@ class BatchWorkload:
 
 
 AOWorkload.launches_per_frame = 2  # render + post-process (colour conversion)
+AOWorkload.timed_kernels = ("ao",)
+AOWorkload.roofline_kernel = "k_render_ao (camera + AO rays, one launch per frame)"
+PTWorkload.timed_kernels = ("trace_closest", "trace_shadow")
+PTWorkload.roofline_kernel = "k_trace_queue (closest-hit and shadow instantiations)"
+ScivisWorkload.timed_kernels = ("scivis",)
+ScivisWorkload.roofline_kernel = "k_render_scivis_volume"
 PTWorkload.launches_per_frame = 3 + 6 * 4  # generate, finalize, post-process, 6 bounces x (reset, trace, shade, shadow)
 BatchWorkload.launches_per_frame = None  # taken from the batch plan (b200_batch_info)
 WORKLOADS = {"ao": AOWorkload, "pt": PTWorkload, "scivis": ScivisWorkload, "batch": BatchWorkload}
@@ -565,6 +577,10 @@ def run_ours(args):
         torch.distributed.barrier()
     torch.cuda.synchronize(local)
     dev.sync()
+    timed_kernels = getattr(wl, "timed_kernels", None)
+    if timed_kernels:
+        dev.kernel_timing(True)
+        dev.kernel_times(reset=True)
     with Clocks(local) as clk:
         for i in range(args.steps):
             with torch.cuda.stream(stream):
@@ -575,6 +591,10 @@ def run_ours(args):
                 evs[i][1].record(stream)
         dev.sync()
         torch.cuda.synchronize(local)
+    ktimes = None
+    if timed_kernels:
+        ktimes = dev.kernel_times(reset=True)
+        dev.kernel_timing(False)
     if ws > 1:
         torch.distributed.barrier()
     times = [a.elapsed_time(b) for a, b in evs]
@@ -618,14 +638,32 @@ def run_ours(args):
     value = rays_all / (dev_ms_max * 1e-3) / 1e6
     e2e_val = rays_all / e2e_max / 1e6
     if hasattr(wl, "bytes_per_unit"):
-        bytes_per_frame = wl.bytes_per_unit() * units / args.steps
-        note = "algorithmic volume bytes (32 B per trilinear sample) per frame / frame time"
+        alg_bytes = wl.bytes_per_unit() * units
+        note = "algorithmic volume bytes (32 B per trilinear sample)"
     else:
-        bytes_per_frame = (48.0 * rays + 80.0 * nodes + 48.0 * tris + 20.0 * sph) / args.steps
-        note = "algorithmic traversal bytes per frame / frame time"
-    frame_s = dev_ms / args.steps * 1e-3
+        alg_bytes = 48.0 * rays + 80.0 * nodes + 48.0 * tris + 20.0 * sph
+        note = "algorithmic traversal bytes (48 B ray record + 80 B per node visit + 48 B per triangle, 20 B per sphere)"
     peak, kind = peaks()
-    achieved = bytes_per_frame / frame_s / 1e9
+    if ktimes:
+        # the dominant kernel, timed live with CUDA events around its launches
+        kms = sum(ktimes[k][0] for k in timed_kernels)
+        klaunches = sum(ktimes[k][1] for k in timed_kernels)
+        achieved = alg_bytes / (kms * 1e-3) / 1e9
+        per_launch = alg_bytes / max(klaunches, 1)
+        roof_kernel = {"kernel": wl.roofline_kernel, "launches": klaunches, "ms": round(kms, 3),
+                       "share_of_step": round(kms / dev_ms, 4), "bytes_per_launch": round(per_launch)}
+        note += " of the timed launches / their summed CUDA-event time"
+    else:
+        achieved = alg_bytes / (dev_ms * 1e-3) / 1e9
+        per_launch = None
+        roof_kernel = {"kernel": "whole step (launches captured in a CUDA graph)"}
+        note += " per step / step time"
+    traffic = None
+    tp = TRAFFIC.get(wl.name)
+    if tp and per_launch is not None:
+        # ncu dram bytes per algorithmic byte of the same kernel, scaled to this launch size
+        traffic = round(tp["dram_per_alg_byte"] * per_launch)
+        note += "; traffic from %s" % tp["source"]
     line = {"metric": wl.metric, "value": round(value, 3), "unit": wl.metric, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(dev_ms_max / args.steps, 4), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generators)",
@@ -636,9 +674,10 @@ def run_ours(args):
             "e2e": {"value": round(e2e_val, 3), "unit": wl.metric, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": args.steps * (wl.launches_per_frame or wl.kernels_per_frame()),
-            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                         "frac": round(achieved / peak, 4), "traffic": None,
-                         "note": "%s; peak %s" % (note, kind)},
+            "roofline": dict({"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                              "frac": round(achieved / peak, 4), "traffic": traffic,
+                              "note": "%s; peak %s (%s)" % (note, kind, "of measured" if kind == "measured"
+                                                           else "of fallback")}, **roof_kernel),
             "clocks": clk.summary()}
     if hasattr(wl, "latency"):
         line["latency"] = wl.latency()

@@ -49,6 +49,16 @@ const char *b200_device_last_error(b200_device dev);
 void *b200_device_stream(b200_device dev);
 int b200_device_sync(b200_device dev);
 
+/* Live kernel timing (no reference counterpart; the reference reports frame
+ * times only, ospray/include/ospray/ospray.h:335 ospGetTaskDuration).  While enabled, the
+ * renderers record a pair of CUDA events on the launch stream around every
+ * launch of their hot kernels; b200_kernel_timing_read waits for them and
+ * returns per kind (0 closest-hit trace, 1 shadow trace, 2 path-tracer
+ * shade, 3 AO frame kernel, 4 SciVis volume kernel) the summed device
+ * milliseconds and launch counts, optionally resetting them. */
+int b200_kernel_timing(b200_device dev, int enable);
+int b200_kernel_timing_read(b200_device dev, double *ms, int64_t *launches, int n, int reset);
+
 /* ---- completion events on the device stream: what an OSPFuture waits on
  *      (ospRenderFrame / ospIsReady / ospWait / ospGetTaskDuration,
  *      ospray/include/ospray/ospray.h:315-336; the reference's future is a

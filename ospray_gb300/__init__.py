@@ -154,6 +154,8 @@ def lib():
             "b200_device_last_error": (ctypes.c_char_p, [P]),
             "b200_device_stream": (P, [P]),
             "b200_device_sync": (I, [P]),
+            "b200_kernel_timing": (I, [P, I]),
+            "b200_kernel_timing_read": (I, [P, P, P, I, I]),
             "b200_scene_create": (I, [P, ctypes.POINTER(P)]),
             "b200_scene_release": (I, [P]),
             "b200_scene_add_mesh": (I, [P, P, I64, P, I64, ctypes.POINTER(I)]),
@@ -260,6 +262,20 @@ class Device:
 
     def sync(self):
         self._check(lib().b200_device_sync(self._h))
+
+    KERNEL_KINDS = ("trace_closest", "trace_shadow", "pt_shade", "ao", "scivis")
+
+    def kernel_timing(self, enable):
+        """Starts (True) or stops live event timing of the hot kernels."""
+        self._check(lib().b200_kernel_timing(self._h, 1 if enable else 0))
+
+    def kernel_times(self, reset=False):
+        """{kind: (device ms, launches)} since timing started or the last reset."""
+        n = len(self.KERNEL_KINDS)
+        ms = np.zeros(n, np.float64)
+        cnt = np.zeros(n, np.int64)
+        self._check(lib().b200_kernel_timing_read(self._h, ms.ctypes.data, cnt.ctypes.data, n, 1 if reset else 0))
+        return {k: (float(ms[i]), int(cnt[i])) for i, k in enumerate(self.KERNEL_KINDS)}
 
     def release(self):
         if self._h:

@@ -149,6 +149,7 @@ DeviceObj::~DeviceObj() {
   cudaFree(pickBuf);
   if (albedo) cudaFree(albedo);
   if (ptWs) cudaFree(ptWs);
+  delete timer;
   for (auto &L : luts) {
     cudaFree(L.cdf_x);
     cudaFree(L.cdf_y);
@@ -538,6 +539,37 @@ int b200_device_sync(b200_device d) {
   return guarded(dev, [&]() { check(cudaStreamSynchronize(dev->stream), "sync"); });
 }
 
+int b200_kernel_timing(b200_device d, int enable) {
+  if (!d) return B200_INVALID_ARGUMENT;
+  DeviceObj *dev = reinterpret_cast<DeviceObj *>(d);
+  return guarded(dev, [&]() {
+    if (enable && !dev->timer) dev->timer = new KernelTimer();
+    if (!enable && dev->timer) {
+      check(cudaStreamSynchronize(dev->stream), "sync");
+      delete dev->timer;
+      dev->timer = nullptr;
+    }
+  });
+}
+
+int b200_kernel_timing_read(b200_device d, double *ms, int64_t *launches, int n, int reset) {
+  if (!d || n < 0 || (n > 0 && (!ms || !launches))) return B200_INVALID_ARGUMENT;
+  DeviceObj *dev = reinterpret_cast<DeviceObj *>(d);
+  return guarded(dev, [&]() {
+    if (!dev->timer) throw Error(B200_INVALID_OPERATION, "kernel timing is not enabled");
+    dev->timer->collect();
+    for (int k = 0; k < n; k++) {
+      ms[k] = k < KK_COUNT ? dev->timer->ms[k] : 0.0;
+      launches[k] = k < KK_COUNT ? dev->timer->launches[k] : 0;
+    }
+    if (reset)
+      for (int k = 0; k < KK_COUNT; k++) {
+        dev->timer->ms[k] = 0.0;
+        dev->timer->launches[k] = 0;
+      }
+  });
+}
+
 int b200_scene_create(b200_device d, b200_scene *out) {
   if (!d || !out) return B200_INVALID_ARGUMENT;
   DeviceObj *dev = reinterpret_cast<DeviceObj *>(d);
@@ -734,7 +766,7 @@ int b200_render_ao(b200_scene s, const b200_camera_desc *camera, const b200_ao_p
     const AOParamsD d = makeAOParams(*p);
     cudaStream_t st = stream ? (cudaStream_t)stream : sc->dev->stream;
     check(launchRenderAO(sc->dev->tables, sc->view(), makeCamera(*camera), sc->dev->filter(p->pixelFilter), d,
-                         fb->view(), p->collectStats != 0, st),
+                         fb->view(), p->collectStats != 0, st, sc->dev->timer),
           "AO launch");
     fb->frameID++;
     framePostProcess(fb, st);
@@ -804,7 +836,8 @@ int b200_render_pt(b200_scene s, const b200_camera_desc *camera, const b200_pt_p
     ensurePtWorkspace(dev, ptWorkspaceBytes((long long)fb->W * fb->H * p->pixelSamples));
     check(launchRenderPT(dev->tables, sc->view(), makeCamera(*camera), dev->filter(p->pixelFilter), d,
                          sc->dMaterials, sc->dLights, sc->dLightCdf, dev->albedoTables(), fb->view(),
-                         p->collectStats != 0, dev->ptWs, dev->ptWsBytes, st),
+                         p->collectStats != 0, dev->ptWs, dev->ptWsBytes, st, nullptr, nullptr, nullptr,
+                         dev->timer),
           "path tracer launch");
     fb->frameID++;
     framePostProcess(fb, st);
@@ -877,7 +910,8 @@ int b200_render_scivis(b200_scene s, const b200_camera_desc *camera, const b200_
     for (int k = 0; k < 4; k++) d.bg[k] = p->backgroundColor[k];
     cudaStream_t st = stream ? (cudaStream_t)stream : sc->dev->stream;
     check(launchRenderScivisVolume(sc->dev->tables, sc->view(), sc->vol, makeCamera(*camera),
-                                   sc->dev->filter(p->pixelFilter), d, fb->view(), p->collectStats != 0, st),
+                                   sc->dev->filter(p->pixelFilter), d, fb->view(), p->collectStats != 0, st,
+                                   sc->dev->timer),
           "scivis launch");
     fb->frameID++;
     framePostProcess(fb, st);

@@ -42,6 +42,7 @@ struct DeviceObj {
   uint32_t *pickBuf = nullptr;      // one pick result (8 words)
   void *ptWs = nullptr;             // path-tracer path/queue workspace
   size_t ptWsBytes = 0;
+  KernelTimer *timer = nullptr;     // live kernel timing (b200_kernel_timing)
   explicit DeviceObj(int cudaDev);
   const AlbedoTablesD *albedoTables();
   ~DeviceObj();

@@ -7,6 +7,77 @@
 
 namespace b200 {
 
+// Device time of the hot kernels, measured live: while a device's timer is
+// enabled, the renderers record a pair of CUDA events on the launch stream
+// around each launch of the kinds below; read() sums their elapsed times.
+enum KernelKind : int { KK_TRACE_CLOSEST = 0, KK_TRACE_SHADOW = 1, KK_SHADE = 2, KK_AO = 3, KK_SCIVIS = 4, KK_COUNT = 5 };
+
+struct KernelTimer {
+  struct Rec {
+    int kind;
+    cudaEvent_t a, b;
+  };
+  std::vector<cudaEvent_t> pool;
+  std::vector<Rec> recs;
+  cudaEvent_t open = nullptr;
+  double ms[KK_COUNT] = {};
+  long long launches[KK_COUNT] = {};
+  cudaEvent_t get() {
+    if (pool.empty()) {
+      cudaEvent_t e = nullptr;
+      cudaEventCreate(&e);
+      return e;
+    }
+    cudaEvent_t e = pool.back();
+    pool.pop_back();
+    return e;
+  }
+  void begin(cudaStream_t st) {
+    open = get();
+    cudaEventRecord(open, st);
+  }
+  void end(int kind, cudaStream_t st) {
+    cudaEvent_t b = get();
+    cudaEventRecord(b, st);
+    recs.push_back({kind, open, b});
+    open = nullptr;
+  }
+  // folds the recorded pairs into ms/launches (waits for the last one)
+  void collect() {
+    for (const Rec &r : recs) {
+      float t = 0.f;
+      cudaEventSynchronize(r.b);
+      if (cudaEventElapsedTime(&t, r.a, r.b) == cudaSuccess) {
+        ms[r.kind] += t;
+        launches[r.kind]++;
+      }
+      pool.push_back(r.a);
+      pool.push_back(r.b);
+    }
+    recs.clear();
+  }
+  ~KernelTimer() {
+    for (const Rec &r : recs) {
+      cudaEventDestroy(r.a);
+      cudaEventDestroy(r.b);
+    }
+    for (cudaEvent_t e : pool) cudaEventDestroy(e);
+  }
+};
+
+// scoped begin/end around one launch (no-op without a timer)
+struct KernelScope {
+  KernelTimer *t;
+  int kind;
+  cudaStream_t st;
+  KernelScope(KernelTimer *t_, int k, cudaStream_t s) : t(t_), kind(k), st(s) {
+    if (t) t->begin(st);
+  }
+  ~KernelScope() {
+    if (t) t->end(kind, st);
+  }
+};
+
 enum LightType : int { LIGHT_QUAD = 0, LIGHT_AMBIENT = 1 };
 
 // light in world space; quad: nnormal = normalize(edge2 x edge1), ppdf = 1/area
@@ -46,7 +117,7 @@ struct ScivisParamsD {
 cudaError_t buildMacrocells(VolumeD &v, uint8_t *empty, cudaStream_t st);
 cudaError_t launchRenderScivisVolume(const SamplerTables *T, const Scene &sc, const VolumeD &vol, const CameraD &cam,
                                      const PixelFilterD &pf, const ScivisParamsD &p, const FrameD &fb, bool stats,
-                                     cudaStream_t st);
+                                     cudaStream_t st, KernelTimer *kt = nullptr);
 
 // Path tracing with the neural radiance cache: per frame, paths whose index
 // p satisfies (p + trainOffset) % trainStride == 0 are training paths (slot
@@ -74,7 +145,8 @@ cudaError_t launchRenderPT(const SamplerTables *T, const Scene &sc, const Camera
                            const PtParamsD &p, const MaterialD *mats, const LightD *lights, const float *lightCdf,
                            const AlbedoTablesD *AT, const FrameD &fb, bool stats, void *workspace,
                            size_t wsBytes, cudaStream_t st, const NrcFrameD *nrc = nullptr,
-                           void (*nrcInfer)(void *ctx, cudaStream_t st) = nullptr, void *nrcCtx = nullptr);
+                           void (*nrcInfer)(void *ctx, cudaStream_t st) = nullptr, void *nrcCtx = nullptr,
+                           KernelTimer *kt = nullptr);
 // bytes of path-tracer workspace for a frame of npaths = W * H * spp paths
 size_t ptWorkspaceBytes(long long npaths);
 
@@ -134,6 +206,6 @@ cudaError_t launchPick(const Scene &sc, const CameraD &cam, float sx, float sy, 
 cudaError_t launchTrace(const Scene &sc, const float4 *rays, long long n, int occlusion, float *outF, uint32_t *outI,
                         cudaStream_t st);
 cudaError_t launchRenderAO(const SamplerTables *T, const Scene &sc, const CameraD &cam, const PixelFilterD &pf, const AOParamsD &p,
-                           const FrameD &fb, bool stats, cudaStream_t st);
+                           const FrameD &fb, bool stats, cudaStream_t st, KernelTimer *kt = nullptr);
 
 }  // namespace b200

@@ -184,8 +184,9 @@ cudaError_t launchPick(const Scene &sc, const CameraD &cam, float sx, float sy, 
 }
 
 cudaError_t launchRenderAO(const SamplerTables *T, const Scene &sc, const CameraD &cam, const PixelFilterD &pf, const AOParamsD &p,
-                           const FrameD &fb, bool stats, cudaStream_t st) {
+                           const FrameD &fb, bool stats, cudaStream_t st, KernelTimer *kt) {
   dim3 grid((fb.W + 15) / 16, (fb.H + 7) / 8);
+  KernelScope ks(kt, KK_AO, st);
   if (stats)
     k_render_ao<true><<<grid, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(T, sc, cam, pf, p, fb);
   else

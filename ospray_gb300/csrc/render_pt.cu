@@ -334,6 +334,7 @@ __global__ void __launch_bounds__(TRACE_BLOCK, B200_TRACE_MINBLOCKS) k_trace_que
   Scene bsc = sc;  // this lane's scene in a batch
   const Scene &S = BATCH ? bsc : sc;
   Traverser tv;
+  TraceSpill spill;
   bool has = false, exhausted = false;
   uint32_t item = 0;
   for (int guard = 0; guard < (1 << 30); guard++) {
@@ -364,7 +365,7 @@ __global__ void __launch_bounds__(TRACE_BLOCK, B200_TRACE_MINBLOCKS) k_trace_que
             r.tfar = INFINITY;
             if (BATCH) bsc = reqs[ws.paths[item].meta2.y].c.sc;
           }
-          tv.init(S, r, SHADOW);
+          tv.init(S, r, SHADOW, &spill);
           if (STATS) ts.rays++;
           has = true;
         } else {
@@ -383,6 +384,7 @@ __global__ void __launch_bounds__(TRACE_BLOCK, B200_TRACE_MINBLOCKS) k_trace_que
           atomicAdd(con + 2, s.c.z);
         }
       } else {
+        tv.finish(S);
         HitBuf hb;
         hb.a = make_float4(tv.hit.t, __uint_as_float(tv.hit.primID), __uint_as_float(tv.hit.entry),
                            tv.found ? 1.f : 0.f);
@@ -1007,7 +1009,7 @@ cudaError_t launchRenderPT(const SamplerTables *T, const Scene &sc, const Camera
                            const PtParamsD &p, const MaterialD *mats, const LightD *lights, const float *lightCdf,
                            const AlbedoTablesD *AT, const FrameD &fb, bool stats, void *workspace, size_t wsBytes,
                            cudaStream_t st, const NrcFrameD *nrc, void (*nrcInfer)(void *, cudaStream_t),
-                           void *nrcCtx) {
+                           void *nrcCtx, KernelTimer *kt) {
   FrameInfo fi;
   fi.W = fb.W;
   fi.H = fb.H;
@@ -1039,24 +1041,33 @@ cudaError_t launchRenderPT(const SamplerTables *T, const Scene &sc, const Camera
     const int cin = b & 1, cout = cin ^ 1;
     k_bounce_reset<<<1, 1, 0, st>>>(ws.counters, cin, cout, nullptr);
     const uint32_t *qin = b == 0 ? nullptr : qs[cin];
-    if (stats)
-      k_trace_queue<false, true, false><<<traceBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
-          sc, ws, qin, ws.counters + cin, ws.counters + 3, nullptr);
-    else
-      k_trace_queue<false, false, false><<<traceBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
-          sc, ws, qin, ws.counters + cin, ws.counters + 3, nullptr);
-    if (nrc)
-      k_pt_shade<false, true><<<shadeNrcBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
-          c, ws, qin, ws.counters + cin, qs[cout], ws.counters + cout, ws.counters + 2, nullptr, nf);
-    else
-      k_pt_shade<false, false><<<shadeBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
-          c, ws, qin, ws.counters + cin, qs[cout], ws.counters + cout, ws.counters + 2, nullptr, nf);
-    if (stats)
-      k_trace_queue<true, true, false><<<shadowBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
-          sc, ws, nullptr, ws.counters + 2, ws.counters + 4, nullptr);
-    else
-      k_trace_queue<true, false, false><<<shadowBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
-          sc, ws, nullptr, ws.counters + 2, ws.counters + 4, nullptr);
+    {
+      KernelScope ks(kt, KK_TRACE_CLOSEST, st);
+      if (stats)
+        k_trace_queue<false, true, false><<<traceBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
+            sc, ws, qin, ws.counters + cin, ws.counters + 3, nullptr);
+      else
+        k_trace_queue<false, false, false><<<traceBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
+            sc, ws, qin, ws.counters + cin, ws.counters + 3, nullptr);
+    }
+    {
+      KernelScope ks(kt, KK_SHADE, st);
+      if (nrc)
+        k_pt_shade<false, true><<<shadeNrcBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
+            c, ws, qin, ws.counters + cin, qs[cout], ws.counters + cout, ws.counters + 2, nullptr, nf);
+      else
+        k_pt_shade<false, false><<<shadeBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
+            c, ws, qin, ws.counters + cin, qs[cout], ws.counters + cout, ws.counters + 2, nullptr, nf);
+    }
+    {
+      KernelScope ks(kt, KK_TRACE_SHADOW, st);
+      if (stats)
+        k_trace_queue<true, true, false><<<shadowBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
+            sc, ws, nullptr, ws.counters + 2, ws.counters + 4, nullptr);
+      else
+        k_trace_queue<true, false, false><<<shadowBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
+            sc, ws, nullptr, ws.counters + 2, ws.counters + 4, nullptr);
+    }
     if (nrc && nf.useCache) {  // answer this bounce's cache queries
       nrcInfer(nrcCtx, st);
       k_nrc_apply<<<unsigned((fi.npaths + 255) / 256), 256, 0, st>>>(nf, ws.paths, uint32_t(fi.npaths));

@@ -263,8 +263,9 @@ cudaError_t buildMacrocells(VolumeD &v, uint8_t *empty, cudaStream_t st) {
 
 cudaError_t launchRenderScivisVolume(const SamplerTables *T, const Scene &sc, const VolumeD &vol, const CameraD &cam,
                                      const PixelFilterD &pf, const ScivisParamsD &p, const FrameD &fb, bool stats,
-                                     cudaStream_t st) {
+                                     cudaStream_t st, KernelTimer *kt) {
   dim3 grid((fb.W + 15) / 16, (fb.H + 7) / 8);
+  KernelScope ks(kt, KK_SCIVIS, st);
   if (stats)
     k_render_scivis_volume<true><<<grid, 128, 0, st>>>(T, sc, vol, cam, pf, p, fb);
   else

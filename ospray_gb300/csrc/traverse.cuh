@@ -51,40 +51,47 @@ B200_D void flushStats(const Scene &sc, const TraceStats &t) {
       if (v[k]) atomicAdd(sc.counters + k, (unsigned long long)v[k]);
 }
 
+// Per-ray constants of the watertight test: the axis permutation (kx, ky,
+// kz packed in two bits each) and the shear.
 struct TriPre {
-  int kx, ky, kz;
+  uint32_t k;
   float Sx, Sy, Sz;
+  B200_D int kx() const { return int(k & 3u); }
+  B200_D int ky() const { return int((k >> 2) & 3u); }
+  B200_D int kz() const { return int(k >> 4); }
 };
 
 B200_D TriPre triPre(V3 d) {
   TriPre p;
   const V3 a = vabs(d);
-  p.kz = 0;
-  if (a.y > comp(a, p.kz)) p.kz = 1;
-  if (a.z > comp(a, p.kz)) p.kz = 2;
-  p.kx = p.kz == 2 ? 0 : p.kz + 1;
-  p.ky = p.kx == 2 ? 0 : p.kx + 1;
-  if (comp(d, p.kz) < 0.f) {
-    const int t = p.kx;
-    p.kx = p.ky;
-    p.ky = t;
+  int kz = 0;
+  if (a.y > comp(a, kz)) kz = 1;
+  if (a.z > comp(a, kz)) kz = 2;
+  int kx = kz == 2 ? 0 : kz + 1;
+  int ky = kx == 2 ? 0 : kx + 1;
+  if (comp(d, kz) < 0.f) {
+    const int t = kx;
+    kx = ky;
+    ky = t;
   }
-  p.Sx = fdiv(comp(d, p.kx), comp(d, p.kz));
-  p.Sy = fdiv(comp(d, p.ky), comp(d, p.kz));
-  p.Sz = fdiv(1.f, comp(d, p.kz));
+  p.k = uint32_t(kx) | uint32_t(ky) << 2 | uint32_t(kz) << 4;
+  p.Sx = fdiv(comp(d, kx), comp(d, kz));
+  p.Sy = fdiv(comp(d, ky), comp(d, kz));
+  p.Sz = fdiv(1.f, comp(d, kz));
   return p;
 }
 
 B200_D bool triTest(const TriPre &p, V3 org, float tnear, float tfar, V3 v0, V3 v1, V3 v2, float &t, float &u,
                     float &v) {
   const V3 A = sub(v0, org), B = sub(v1, org), C = sub(v2, org);
-  const float Akz = comp(A, p.kz), Bkz = comp(B, p.kz), Ckz = comp(C, p.kz);
-  const float Ax = fsub(comp(A, p.kx), fmul(p.Sx, Akz));
-  const float Ay = fsub(comp(A, p.ky), fmul(p.Sy, Akz));
-  const float Bx = fsub(comp(B, p.kx), fmul(p.Sx, Bkz));
-  const float By = fsub(comp(B, p.ky), fmul(p.Sy, Bkz));
-  const float Cx = fsub(comp(C, p.kx), fmul(p.Sx, Ckz));
-  const float Cy = fsub(comp(C, p.ky), fmul(p.Sy, Ckz));
+  const int kx = p.kx(), ky = p.ky(), kz = p.kz();
+  const float Akz = comp(A, kz), Bkz = comp(B, kz), Ckz = comp(C, kz);
+  const float Ax = fsub(comp(A, kx), fmul(p.Sx, Akz));
+  const float Ay = fsub(comp(A, ky), fmul(p.Sy, Akz));
+  const float Bx = fsub(comp(B, kx), fmul(p.Sx, Bkz));
+  const float By = fsub(comp(B, ky), fmul(p.Sy, Bkz));
+  const float Cx = fsub(comp(C, kx), fmul(p.Sx, Ckz));
+  const float Cy = fsub(comp(C, ky), fmul(p.Sy, Ckz));
   float U = fsub(fmul(Cx, By), fmul(Cy, Bx));
   float V = fsub(fmul(Ax, Cy), fmul(Ay, Cx));
   float W = fsub(fmul(Bx, Ay), fmul(By, Ax));
@@ -125,11 +132,19 @@ B200_D bool sphTest(V3 org, V3 d, float tnear, float tfar, float4 s, float &t, V
   return true;
 }
 
-B200_D bool better(float t, uint32_t inst, uint32_t geom, uint32_t prim, const HitRec &h) {
-  if (t != h.t) return t < h.t;
-  if (inst != h.instID) return inst < h.instID;
-  if (geom != h.geomID) return geom < h.geomID;
-  return prim < h.primID;
+// Is a hit at t of (entry e, prim) better than the current closest
+// (ht, hentry, hprim)?  Equal t resolves to the smallest (instID, geomID,
+// primID); the IDs are read from the entries only for such ties.
+B200_D bool better(const Scene &sc, float t, uint32_t e, uint32_t prim, float ht, uint32_t hentry,
+                   uint32_t hprim) {
+  if (t != ht) return t < ht;
+  if (hentry == INVALID_ID) return true;
+  if (e != hentry) {
+    const uint32_t i0 = sc.entries[e].instID, i1 = sc.entries[hentry].instID;
+    if (i0 != i1) return i0 < i1;
+    return sc.entries[e].geomID < sc.entries[hentry].geomID;
+  }
+  return prim < hprim;
 }
 
 // The 80-byte node as five 16-byte words in registers.
@@ -241,9 +256,17 @@ constexpr size_t TRACE_SMEM_BYTES = size_t(STACK_SMEM) * TRACE_BLOCK * sizeof(ui
 constexpr uint32_t G_TNODE = 0u << 30, G_BNODE = 1u << 30, G_TINST = 2u << 30, G_BPRIM = 3u << 30;
 constexpr uint32_t G_KIND = 3u << 30, G_BLAS = 1u << 30, G_PRIMS = 2u << 30;
 
+// Entries beyond the shared-memory column go to a per-thread overflow array
+// that the caller declares (TraceSpill) and the stack points to; keeping that
+// dynamically indexed array outside the traverser lets the compiler hold the
+// traverser's own fields in registers.
+struct TraceSpill {
+  uint2 e[STACK_LOCAL];
+};
+
 struct TraceStack {
-  uint2 *smem;  // this thread's column
-  uint2 local[STACK_LOCAL];
+  uint2 *smem;   // this thread's column
+  uint2 *local;  // this thread's overflow array
   int sp;
   B200_D void push(uint2 item, uint32_t *status) {
     if (sp < STACK_SMEM) {
@@ -275,35 +298,38 @@ B200_D uint2 *traceStackBase() {
 struct Traverser {
   TraceStack st;
   Ray ray;
-  V3 wrdir, org, dir, rdir;  // world reciprocal direction; current frame
+  V3 org, dir, rdir;  // current frame
   TriPre pre;
   const Node8 *nodes;
   const float4 *prims;
   const uint32_t *primIDs;
-  uint32_t etype, einst, egeom, eidx;
+  uint32_t etype, eidx;
   uint32_t nbase, nbits;  // node group: child base; hit keys (bits 0-7) | imask << 8
   uint32_t pbase, pbits;  // primitive group: slot base; hit slots (bits 0-23)
   uint32_t oct;           // direction octant of the current frame
   bool inBlas, anyHit, found;
+  // the closest hit so far: distance, primitive ID, entry, leaf slot; the
+  // rest of the record is formed once by finish()
+  float ht;
+  uint32_t hprim, hentry, hslot;
   HitRec hit;
 
-  B200_D void init(const Scene &sc, const Ray &r, bool any) {
+  B200_D void init(const Scene &sc, const Ray &r, bool any, TraceSpill *spill) {
     ray = r;
     anyHit = any;
     st.smem = traceStackBase();
+    st.local = spill->e;
     st.sp = 0;
-    hit.t = r.tfar;
-    hit.u = hit.v = 0.f;
-    hit.primID = hit.geomID = hit.instID = hit.entry = INVALID_ID;
-    wrdir = mk(1.f / r.dir.x, 1.f / r.dir.y, 1.f / r.dir.z);
+    ht = r.tfar;
+    hprim = hentry = hslot = INVALID_ID;
     org = r.org;
     dir = r.dir;
-    rdir = wrdir;
+    rdir = mk(1.f / r.dir.x, 1.f / r.dir.y, 1.f / r.dir.z);
     oct = octantOf(r.dir);
     nodes = sc.tlas;
     prims = nullptr;
     primIDs = nullptr;
-    etype = einst = egeom = eidx = 0;
+    etype = eidx = 0;
     inBlas = false;
     found = false;
     // the TLAS root as a one-child group
@@ -321,8 +347,6 @@ struct Traverser {
     prims = e.prims;
     primIDs = e.primIDs;
     etype = e.type;
-    einst = e.instID;
-    egeom = e.geomID;
     if (!e.identity) {
       const Xfm r = e.rcp;
       org = xfmPoint(r, ray.org);
@@ -341,8 +365,40 @@ struct Traverser {
     nodes = sc.tlas;
     org = ray.org;
     dir = ray.dir;
-    rdir = wrdir;
+    rdir = mk(1.f / ray.dir.x, 1.f / ray.dir.y, 1.f / ray.dir.z);
     oct = octantOf(ray.dir);
+  }
+
+  // The full hit record of the closest hit: u, v and the geometric normal
+  // re-evaluated on the hit primitive in its entry's frame with the same
+  // operations as during traversal (so identical values), and the IDs.
+  B200_D void finish(const Scene &sc) {
+    hit.t = ht;
+    hit.primID = hprim;
+    hit.entry = hentry;
+    hit.u = hit.v = 0.f;
+    hit.Ng = mk(0.f, 0.f, 0.f);
+    hit.instID = hit.geomID = INVALID_ID;
+    if (!found) return;
+    const Entry &e = sc.entries[hentry];
+    hit.instID = e.instID;
+    hit.geomID = e.geomID;
+    V3 o = ray.org, d = ray.dir;
+    if (!e.identity) {
+      const Xfm r = e.rcp;
+      o = xfmPoint(r, ray.org);
+      d = xfmVector(r, ray.dir);
+    }
+    float t;
+    if (e.type == GEOM_TRIANGLES) {
+      const float4 a = __ldg(e.prims + 3 * hslot), b = __ldg(e.prims + 3 * hslot + 1),
+                   c = __ldg(e.prims + 3 * hslot + 2);
+      const V3 v0 = mk(a.x, a.y, a.z), v1 = mk(b.x, b.y, b.z), v2 = mk(c.x, c.y, c.z);
+      triTest(triPre(d), o, ray.tnear, ht, v0, v1, v2, t, hit.u, hit.v);
+      hit.Ng = cross(sub(v1, v0), sub(v2, v0));
+    } else {
+      sphTest(o, d, ray.tnear, ht, __ldg(e.prims + hslot), t, hit.Ng);
+    }
   }
 
   // one traversal step; true when the ray is finished
@@ -358,7 +414,7 @@ struct Traverser {
       const NodeView n = loadNode(nodes, child);
       if (STATS) ts->nodes++;
       uint32_t keys, hitPrims;
-      intersectChildren(n, org, rdir, ray.tnear, hit.t, oct, keys, hitPrims);
+      intersectChildren(n, org, rdir, ray.tnear, ht, oct, keys, hitPrims);
       nbase = n.childBase();
       nbits = keys | (((n.exw() >> 24) & 0xffu) << 8);
       pbase = n.primBase();
@@ -383,30 +439,25 @@ struct Traverser {
         enterInstance(sc, __ldg(sc.tlasLeaf + slot));
         break;
       }
-      float t, u = 0.f, v = 0.f;
-      V3 Ng;
+      float t;
       uint32_t prim;
       bool h;
       if (STATS) (etype == GEOM_TRIANGLES ? ts->tris : ts->spheres)++;
       if (etype == GEOM_TRIANGLES) {
         const float4 a = __ldg(prims + 3 * slot), b = __ldg(prims + 3 * slot + 1), c = __ldg(prims + 3 * slot + 2);
-        const V3 v0 = mk(a.x, a.y, a.z), v1 = mk(b.x, b.y, b.z), v2 = mk(c.x, c.y, c.z);
-        h = triTest(pre, org, ray.tnear, hit.t, v0, v1, v2, t, u, v);
-        if (h) Ng = cross(sub(v1, v0), sub(v2, v0));
+        float u, v;
+        h = triTest(pre, org, ray.tnear, ht, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), mk(c.x, c.y, c.z), t, u, v);
         prim = __float_as_uint(a.w);
       } else {
-        h = sphTest(org, dir, ray.tnear, hit.t, __ldg(prims + slot), t, Ng);
+        V3 Ng;
+        h = sphTest(org, dir, ray.tnear, ht, __ldg(prims + slot), t, Ng);
         prim = __ldg(primIDs + slot);
       }
-      if (h && better(t, einst, egeom, prim, hit)) {
-        hit.t = t;
-        hit.u = u;
-        hit.v = v;
-        hit.Ng = Ng;
-        hit.primID = prim;
-        hit.geomID = egeom;
-        hit.instID = einst;
-        hit.entry = eidx;
+      if (h && better(sc, t, eidx, prim, ht, hentry, hprim)) {
+        ht = t;
+        hprim = prim;
+        hentry = eidx;
+        hslot = slot;
         found = true;
         if (anyHit) return true;
       }
@@ -446,12 +497,14 @@ B200_D bool traceRay(const Scene &sc, const Ray &ray, HitRec &hit, bool anyHit, 
   if (STATS && active) ts->rays++;
   const unsigned group = __activemask();
   Traverser tv;
-  tv.init(sc, ray, anyHit);
+  TraceSpill spill;
+  tv.init(sc, ray, anyHit, &spill);
   bool done = !active || tv.idle();
   for (int guard = 0; guard < (1 << 18); guard++) {
     if (!__any_sync(group, !done)) break;
     if (!done) done = tv.step<STATS>(sc, ts);
   }
+  if (!anyHit) tv.finish(sc);
   hit = tv.hit;
   return tv.found;
 }
