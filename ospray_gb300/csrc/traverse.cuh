@@ -174,35 +174,59 @@ B200_D NodeView loadNode(const Node8 *nodes, uint32_t i) {
   return n;
 }
 
+B200_D float max3f(float a, float b, float c) {
+  float r;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+B200_D float min3f(float a, float b, float c) {
+  float r;
+  asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+
 // Intersects the node's 8 child boxes with the ray (direction octant oct).
 // keys: the hit internal children, child slot i at bit i ^ oct, so the
 // lowest set bit is the next child in the octant's visiting order.  prims:
 // the leaf primitive slots (relative to primBase) of the hit leaf children.
+//
+// Slab distances are formed on the quantisation grid directly in t units,
+// t = q * (2^e * rdir) + (p - org) * rdir, one FMA per plane; the near and
+// far planes of each axis are chosen per ray octant on whole 4-child words.
+// The comparison is widened by 8e-7 relative (about 7 ulp) on the exit and on
+// tfar, so rounding never culls a box the ray touches.
 B200_D void intersectChildren(const NodeView &n, V3 org, V3 rdir, float tnear, float tfar, uint32_t oct,
                               uint32_t &keys, uint32_t &prims) {
   const uint32_t e = n.exw();
-  const float sx = __uint_as_float((e & 0xffu) << 23);
-  const float sy = __uint_as_float(((e >> 8) & 0xffu) << 23);
-  const float sz = __uint_as_float(((e >> 16) & 0xffu) << 23);
-  // near/far planes chosen per axis from the ray octant; every byte index is
-  // a compile-time constant so the node stays in registers
+  const float ax = __uint_as_float((e & 0xffu) << 23) * rdir.x;
+  const float ay = __uint_as_float(((e >> 8) & 0xffu) << 23) * rdir.y;
+  const float az = __uint_as_float(((e >> 16) & 0xffu) << 23) * rdir.z;
+  const float bx = (n.px() - org.x) * rdir.x, by = (n.py() - org.y) * rdir.y, bz = (n.pz() - org.z) * rdir.z;
   const bool xn = rdir.x < 0.f, yn = rdir.y < 0.f, zn = rdir.z < 0.f;
-  const float ox = n.px() - org.x, oy = n.py() - org.y, oz = n.pz() - org.z;
+  // box block words: qlo x/y/z = q2.xy, q2.zw, q3.xy; qhi x/y/z = q3.zw, q4.xy, q4.zw
+  const uint32_t nx0 = xn ? n.q[3].z : n.q[2].x, nx1 = xn ? n.q[3].w : n.q[2].y;
+  const uint32_t fx0 = xn ? n.q[2].x : n.q[3].z, fx1 = xn ? n.q[2].y : n.q[3].w;
+  const uint32_t ny0 = yn ? n.q[4].x : n.q[2].z, ny1 = yn ? n.q[4].y : n.q[2].w;
+  const uint32_t fy0 = yn ? n.q[2].z : n.q[4].x, fy1 = yn ? n.q[2].w : n.q[4].y;
+  const uint32_t nz0 = zn ? n.q[4].z : n.q[3].x, nz1 = zn ? n.q[4].w : n.q[3].y;
+  const uint32_t fz0 = zn ? n.q[3].x : n.q[4].z, fz1 = zn ? n.q[3].y : n.q[4].w;
+  const float tmax = tfar * 1.0000008f;
   keys = 0;
   prims = 0;
 #pragma unroll
   for (int i = 0; i < 8; i++) {
     const uint32_t meta = n.meta(i);
     if (meta == 0) continue;
-    const float lx = fmaf(float(n.qbyte(0 + i)), sx, ox), hx = fmaf(float(n.qbyte(24 + i)), sx, ox);
-    const float ly = fmaf(float(n.qbyte(8 + i)), sy, oy), hy = fmaf(float(n.qbyte(32 + i)), sy, oy);
-    const float lz = fmaf(float(n.qbyte(16 + i)), sz, oz), hz = fmaf(float(n.qbyte(40 + i)), sz, oz);
-    const float t0x = (xn ? hx : lx) * rdir.x, t1x = (xn ? lx : hx) * rdir.x;
-    const float t0y = (yn ? hy : ly) * rdir.y, t1y = (yn ? ly : hy) * rdir.y;
-    const float t0z = (zn ? hz : lz) * rdir.z, t1z = (zn ? lz : hz) * rdir.z;
-    const float t0 = fmaxf(fmaxf(t0x, t0y), fmaxf(t0z, tnear));
-    const float t1 = fminf(fminf(t1x, t1y), t1z) * 1.0000004f;
-    if (t0 <= fminf(t1, tfar)) {
+    const int sh = 8 * (i & 3);
+    const float tnx = fmaf(float(((i < 4 ? nx0 : nx1) >> sh) & 0xffu), ax, bx);
+    const float tfx = fmaf(float(((i < 4 ? fx0 : fx1) >> sh) & 0xffu), ax, bx);
+    const float tny = fmaf(float(((i < 4 ? ny0 : ny1) >> sh) & 0xffu), ay, by);
+    const float tfy = fmaf(float(((i < 4 ? fy0 : fy1) >> sh) & 0xffu), ay, by);
+    const float tnz = fmaf(float(((i < 4 ? nz0 : nz1) >> sh) & 0xffu), az, bz);
+    const float tfz = fmaf(float(((i < 4 ? fz0 : fz1) >> sh) & 0xffu), az, bz);
+    const float t0 = max3f(tnx, tny, fmaxf(tnz, tnear));
+    const float t1 = min3f(tfx, tfy, tfz) * 1.0000008f;
+    if (t0 <= fminf(t1, tmax)) {
       if (meta & 0x80u)
         keys |= 1u << (uint32_t(i) ^ oct);
       else

@@ -21,10 +21,11 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 
 CANDIDATES = [
+    {"B200_STACK_SMEM": 16, "B200_TRACE_MINBLOCKS": 1},
+    {"B200_STACK_SMEM": 16, "B200_TRACE_MINBLOCKS": 6},
     {"B200_STACK_SMEM": 24, "B200_TRACE_MINBLOCKS": 1},
-    {"B200_STACK_SMEM": 32, "B200_TRACE_MINBLOCKS": 1},
-    {"B200_STACK_SMEM": 40, "B200_TRACE_MINBLOCKS": 1},
-    {"B200_STACK_SMEM": 32, "B200_TRACE_MINBLOCKS": 6},
+    {"B200_STACK_SMEM": 12, "B200_TRACE_MINBLOCKS": 6},
+    {"B200_STACK_SMEM": 12, "B200_TRACE_MINBLOCKS": 8},
 ]
 
 
