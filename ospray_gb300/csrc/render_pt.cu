@@ -476,7 +476,10 @@ B200_D void aoShade(const PtCtx &C, const AOParamsD &A, int W, PathRec &pr, cons
 // NRC: the radiance-cache mode (training paths record their vertices; the
 // others end in a cache query at their first vertex after a diffuse bounce).
 template <bool BATCH, bool NRC>
-__global__ void __launch_bounds__(128) k_pt_shade(PtCtx c, Workspace ws, const uint32_t *qin, const uint32_t *cin,
+#ifndef B200_SHADE_MINBLOCKS
+#define B200_SHADE_MINBLOCKS 2
+#endif
+__global__ void __launch_bounds__(128, B200_SHADE_MINBLOCKS) k_pt_shade(PtCtx c, Workspace ws, const uint32_t *qin, const uint32_t *cin,
                                                   uint32_t *qout, uint32_t *cout, uint32_t *cshadow,
                                                   const ReqD *reqs, NrcFrameD nf) {
   static_assert(!(BATCH && NRC), "the radiance cache runs on single-request frames");

@@ -2,9 +2,10 @@
 
     python -m ospray_gb300.tune_build [--out tuned.json]
 
-The shared-memory traversal stack depth (B200_STACK_SMEM) and the trace
-kernels' minimum resident blocks per SM (B200_TRACE_MINBLOCKS, which bounds
-their registers) are compile-time constants, so each candidate is a separate
+The shared-memory traversal stack depth (B200_STACK_SMEM) and the minimum
+resident blocks per SM of the trace kernels (B200_TRACE_MINBLOCKS) and of the
+path-tracer shade kernel (B200_SHADE_MINBLOCKS), which bound their registers,
+are compile-time constants, so each candidate is a separate
 build of libb200.so (into ospray_gb300/_variants/<tag>).  Each build renders
 the path-tracing workload at 960x540, 8 spp (bench.py, 3 warm-up frames and
 5 timed frames) on the GPU, and the fastest candidate's defines are written
@@ -21,16 +22,15 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 
 CANDIDATES = [
-    {"B200_STACK_SMEM": 16, "B200_TRACE_MINBLOCKS": 1},
-    {"B200_STACK_SMEM": 16, "B200_TRACE_MINBLOCKS": 6},
-    {"B200_STACK_SMEM": 24, "B200_TRACE_MINBLOCKS": 1},
-    {"B200_STACK_SMEM": 12, "B200_TRACE_MINBLOCKS": 6},
-    {"B200_STACK_SMEM": 12, "B200_TRACE_MINBLOCKS": 8},
+    {"B200_STACK_SMEM": 16, "B200_TRACE_MINBLOCKS": 6, "B200_SHADE_MINBLOCKS": 2},
+    {"B200_STACK_SMEM": 16, "B200_TRACE_MINBLOCKS": 6, "B200_SHADE_MINBLOCKS": 3},
+    {"B200_STACK_SMEM": 16, "B200_TRACE_MINBLOCKS": 6, "B200_SHADE_MINBLOCKS": 4},
+    {"B200_STACK_SMEM": 16, "B200_TRACE_MINBLOCKS": 5, "B200_SHADE_MINBLOCKS": 3},
 ]
 
 
 def tag(c):
-    return "s%d_b%d" % (c["B200_STACK_SMEM"], c["B200_TRACE_MINBLOCKS"])
+    return "s%d_b%d_h%d" % (c["B200_STACK_SMEM"], c["B200_TRACE_MINBLOCKS"], c.get("B200_SHADE_MINBLOCKS", 2))
 
 
 def measure(c, size, spp):
