@@ -863,10 +863,18 @@ int b200_scene_set_volume(b200_scene s, const float *data, int nx, int ny, int n
     sc->hasVolume = false;
     const size_t nvox = size_t(nx) * ny * nz;
     cudaStream_t st = sc->dev->stream;
-    check(cudaMalloc(&sc->dVolData, nvox * sizeof(float)), "alloc volume");
+    struct Staging {
+      float *p = nullptr;
+      ~Staging() {
+        if (p) cudaFree(p);
+      }
+    } staging;
+    check(cudaMalloc(&staging.p, nvox * sizeof(float)), "alloc volume staging");
+    float *linear = staging.p;
+    check(cudaMalloc(&sc->dVolData, brickedVolumeBytes(nx, ny, nz)), "alloc volume");
     check(cudaMalloc(&sc->dTfColor, ncolor * sizeof(float3)), "alloc transfer function");
     check(cudaMalloc(&sc->dTfOpacity, nopacity * sizeof(float)), "alloc transfer function");
-    check(cudaMemcpyAsync(sc->dVolData, data, nvox * sizeof(float), cudaMemcpyHostToDevice, st), "upload volume");
+    check(cudaMemcpyAsync(linear, data, nvox * sizeof(float), cudaMemcpyHostToDevice, st), "upload volume");
     check(cudaMemcpyAsync(sc->dTfColor, color, ncolor * sizeof(float3), cudaMemcpyHostToDevice, st), "upload tf");
     check(cudaMemcpyAsync(sc->dTfOpacity, opacity, nopacity * sizeof(float), cudaMemcpyHostToDevice, st),
           "upload tf");
@@ -875,6 +883,9 @@ int b200_scene_set_volume(b200_scene s, const float *data, int nx, int ny, int n
     v.nx = nx;
     v.ny = ny;
     v.nz = nz;
+    v.bx = (nx + VOL_BRICK - 1) / VOL_BRICK;
+    v.by = (ny + VOL_BRICK - 1) / VOL_BRICK;
+    v.bz = (nz + VOL_BRICK - 1) / VOL_BRICK;
     v.origin = mk(origin[0], origin[1], origin[2]);
     v.spacing = mk(spacing[0], spacing[1], spacing[2]);
     v.cx = std::max(1, (nx - 1 + 15) / 16);
@@ -887,6 +898,8 @@ int b200_scene_set_volume(b200_scene s, const float *data, int nx, int ny, int n
     v.vlo = valueRange[0];
     v.vhi = valueRange[1];
     v.densityScale = densityScale;
+    check(brickVolume(v, linear, sc->dVolData, st), "brick volume");
+    check(cudaStreamSynchronize(st), "brick volume");
     check(cudaMalloc(&sc->dCellEmpty, size_t(v.cx) * v.cy * v.cz), "alloc macrocells");
     check(buildMacrocells(v, sc->dCellEmpty, st), "macrocells");
     v.cellEmpty = sc->dCellEmpty;

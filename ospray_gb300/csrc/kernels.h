@@ -94,11 +94,15 @@ struct PtParamsD {
   float bg[4];
 };
 
-// structured-regular volume (x fastest) with its transfer function and
-// macrocell emptiness grid (16^3-voxel cells)
+// structured-regular volume with its transfer function and macrocell
+// emptiness grid (16^3-voxel cells).  The voxels are stored in 8^3-voxel
+// bricks (2 KB, x fastest inside a brick, bricks x fastest), so the 8 taps
+// of a trilinear sample and the next samples along a ray share cache lines
+// and DRAM pages; voxel (i, j, k) is at data[ax(i) + ay(j) + az(k)] (brickAddr).
 struct VolumeD {
   const float *data;
   int nx, ny, nz;
+  int bx, by, bz;  // bricks per axis
   V3 origin, spacing;
   int cx, cy, cz;
   const uint8_t *cellEmpty;
@@ -114,6 +118,11 @@ struct ScivisParamsD {
   float bg[4];
 };
 
+constexpr int VOL_BRICK = 8;
+// bytes of the bricked copy of an nx x ny x nz volume
+size_t brickedVolumeBytes(int nx, int ny, int nz);
+// linear (x fastest) -> bricked layout of v (v.data is the bricked output)
+cudaError_t brickVolume(const VolumeD &v, const float *linear, float *bricked, cudaStream_t st);
 cudaError_t buildMacrocells(VolumeD &v, uint8_t *empty, cudaStream_t st);
 cudaError_t launchRenderScivisVolume(const SamplerTables *T, const Scene &sc, const VolumeD &vol, const CameraD &cam,
                                      const PixelFilterD &pf, const ScivisParamsD &p, const FrameD &fb, bool stats,

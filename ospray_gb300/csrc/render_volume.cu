@@ -17,23 +17,58 @@ namespace {
 
 constexpr int CELL = 16;
 
-B200_D float vload(const VolumeD &v, int i, int j, int k) {
-  return __ldg(v.data + (size_t(k) * v.ny + j) * v.nx + i);
+// separable brick addressing: offset of coordinate i along x, j along y, k along z
+B200_D uint32_t brickX(int i) { return uint32_t(i >> 3) * 512u + uint32_t(i & 7); }
+B200_D size_t brickY(const VolumeD &v, int j) { return size_t(j >> 3) * size_t(v.bx) * 512u + size_t(j & 7) * 8u; }
+B200_D size_t brickZ(const VolumeD &v, int k) {
+  return size_t(k >> 3) * size_t(v.bx) * size_t(v.by) * 512u + size_t(k & 7) * 64u;
 }
 
-B200_D float sampleVolume(const VolumeD &v, V3 p) {
+B200_D float vload(const VolumeD &v, int i, int j, int k) {
+  return __ldg(v.data + brickX(i) + brickY(v, j) + brickZ(v, k));
+}
+
+// The 8 taps of a vertex-centred trilinear sample and its fractions, fetched
+// ahead of their use so a ray keeps the next sample's loads in flight while it
+// composites the current one.
+struct Taps {
+  float c[8];  // (x, y, z) = (0,0,0) (1,0,0) (0,1,0) (1,1,0) (0,0,1) (1,0,1) (0,1,1) (1,1,1)
+  float fx, fy, fz;
+  bool inside;
+};
+
+B200_D void fetchTaps(const VolumeD &v, V3 p, Taps &s) {
   const float u = (p.x - v.origin.x) / v.spacing.x, w1 = (p.y - v.origin.y) / v.spacing.y,
               w2 = (p.z - v.origin.z) / v.spacing.z;
-  if (!(u >= 0.f && w1 >= 0.f && w2 >= 0.f && u <= float(v.nx - 1) && w1 <= float(v.ny - 1) &&
-        w2 <= float(v.nz - 1)))
-    return NAN;
-  const int i = min(int(u), v.nx - 2), j = min(int(w1), v.ny - 2), k = min(int(w2), v.nz - 2);
-  const float fx = u - float(i), fy = w1 - float(j), fz = w2 - float(k);
-  const float c00 = lerpF(fx, vload(v, i, j, k), vload(v, i + 1, j, k));
-  const float c10 = lerpF(fx, vload(v, i, j + 1, k), vload(v, i + 1, j + 1, k));
-  const float c01 = lerpF(fx, vload(v, i, j, k + 1), vload(v, i + 1, j, k + 1));
-  const float c11 = lerpF(fx, vload(v, i, j + 1, k + 1), vload(v, i + 1, j + 1, k + 1));
-  return lerpF(fz, lerpF(fy, c00, c10), lerpF(fy, c01, c11));
+  s.inside = u >= 0.f && w1 >= 0.f && w2 >= 0.f && u <= float(v.nx - 1) && w1 <= float(v.ny - 1) &&
+             w2 <= float(v.nz - 1);
+  // outside the grid the (clamped) taps are fetched but not used
+  const int i = min(max(int(u), 0), v.nx - 2), j = min(max(int(w1), 0), v.ny - 2), k = min(max(int(w2), 0), v.nz - 2);
+  s.fx = u - float(i);
+  s.fy = w1 - float(j);
+  s.fz = w2 - float(k);
+  const uint32_t x0 = brickX(i), x1 = brickX(i + 1);
+  const size_t y0 = brickY(v, j), y1 = brickY(v, j + 1), z0 = brickZ(v, k), z1 = brickZ(v, k + 1);
+  const float *d = v.data;
+  const size_t r00 = y0 + z0, r10 = y1 + z0, r01 = y0 + z1, r11 = y1 + z1;
+  s.c[0] = __ldg(d + r00 + x0);
+  s.c[1] = __ldg(d + r00 + x1);
+  s.c[2] = __ldg(d + r10 + x0);
+  s.c[3] = __ldg(d + r10 + x1);
+  s.c[4] = __ldg(d + r01 + x0);
+  s.c[5] = __ldg(d + r01 + x1);
+  s.c[6] = __ldg(d + r11 + x0);
+  s.c[7] = __ldg(d + r11 + x1);
+}
+
+// the trilinear value (NaN outside the grid)
+B200_D float tapsValue(const Taps &s) {
+  if (!s.inside) return NAN;
+  const float c00 = lerpF(s.fx, s.c[0], s.c[1]);
+  const float c10 = lerpF(s.fx, s.c[2], s.c[3]);
+  const float c01 = lerpF(s.fx, s.c[4], s.c[5]);
+  const float c11 = lerpF(s.fx, s.c[6], s.c[7]);
+  return lerpF(s.fz, lerpF(s.fy, c00, c10), lerpF(s.fy, c01, c11));
 }
 
 B200_D float4 tfGet(const VolumeD &v, float value) {
@@ -148,52 +183,71 @@ struct IntervalIter {
   }
 };
 
-B200_D float4 integrate(const VolumeD &v, const Ray &ray, float jitter, float samplingRate, float minContribution,
-                        uint32_t &samples) {
+// Sample positions along the ray: the interval iteration and step rule of
+// integrateVolumeIntervalsGradient; next() yields each sample's distance and
+// its compositing step dt (distance since the previous sample minus the empty
+// space skipped in between).
+struct SampleWalk {
   IntervalIter it;
-  it.init(v, ray.org, ray.dir, ray.tnear, ray.tfar);
-  const float nominalDeltaT = fminf(v.spacing.x, fminf(v.spacing.y, v.spacing.z));
-  V3 color = splat(0.f);
-  float T = 1.f;
-  float distance = INFINITY, iuDistance = jitter, iuLength = 0.f, step = 0.f;
-  float ilo = 0.f, ihi = INFINITY;
-  for (int g = 0; g < (1 << 24) && T > minContribution; g++) {
+  float step, distance, iuDistance, iuLength, ilo, ihi;
+  B200_D void init(const VolumeD &v, const Ray &ray, float jitter, float samplingRate) {
+    it.init(v, ray.org, ray.dir, ray.tnear, ray.tfar);
+    step = fminf(v.spacing.x, fminf(v.spacing.y, v.spacing.z)) / samplingRate;
+    distance = INFINITY;
+    iuDistance = jitter;
+    iuLength = 0.f;
+    ilo = 0.f;
+    ihi = INFINITY;
+  }
+  B200_D bool next(const VolumeD &v, float &newDistance, float &dt) {
     float emptySpace = 0.f;
-    bool more = true;
     while (iuDistance > iuLength) {
       const float prevUpper = ihi;
-      if (it.next(v, ilo, ihi)) {
-        emptySpace += fmaxf(ilo - prevUpper, 0.f);
-        iuDistance -= iuLength;
-        step = nominalDeltaT / samplingRate;
-        iuLength = (ihi - ilo) / step;
-        distance = distance == INFINITY ? ilo : distance;
-      } else {
-        more = false;
-        break;
-      }
+      if (!it.next(v, ilo, ihi)) return false;
+      emptySpace += fmaxf(ilo - prevUpper, 0.f);
+      iuDistance -= iuLength;
+      iuLength = (ihi - ilo) / step;
+      distance = distance == INFINITY ? ilo : distance;
     }
-    if (!more) break;
-    const float newDistance = ilo + iuDistance * step;
-    const V3 p = ray.org + newDistance * ray.dir;
-    const float val = sampleVolume(v, p);
+    newDistance = ilo + iuDistance * step;
+    dt = newDistance - distance - emptySpace;
+    iuDistance += 1.f;
+    distance = newDistance;
+    return true;
+  }
+};
+
+// Front-to-back compositing (SciVis ray march with the transfer function,
+// alpha = exp(-a * dt * densityScale)) until the transmittance falls to
+// minContribution.
+B200_D float4 integrate(const VolumeD &v, const Ray &ray, float jitter, float samplingRate, float minContribution,
+                        uint32_t &samples) {
+  SampleWalk w;
+  w.init(v, ray, jitter, samplingRate);
+  V3 color = splat(0.f);
+  float T = 1.f;
+  float d, dt;
+  for (int g = 0; g < (1 << 24) && T > minContribution && w.next(v, d, dt); g++) {
+    Taps tp;
+    fetchTaps(v, ray.org + d * ray.dir, tp);
+    const float val = tapsValue(tp);
     samples++;
     if (!isnan(val)) {
       float4 c = tfGet(v, val);
-      const float dt = newDistance - distance - emptySpace;
       c.w = expf(-c.w * dt * v.densityScale);
       const float k = T * (1.f - c.w);
       color = color + k * mk(c.x, c.y, c.z);
       T *= c.w;
     }
-    iuDistance += 1.f;
-    distance = newDistance;
   }
   return make_float4(color.x, color.y, color.z, T);
 }
 
+#ifndef B200_VOL_MINBLOCKS
+#define B200_VOL_MINBLOCKS 8  // 64 registers: 67.6 vs 66.4 (6 blocks) G samples/s on 512^3, 1024^2 x 4 spp
+#endif
 template <bool STATS>
-__global__ void __launch_bounds__(128) k_render_scivis_volume(const SamplerTables *T, Scene sc, VolumeD vol,
+__global__ void __launch_bounds__(128, B200_VOL_MINBLOCKS) k_render_scivis_volume(const SamplerTables *T, Scene sc, VolumeD vol,
                                                               CameraD cam, PixelFilterD pf, ScivisParamsD p,
                                                               FrameD fb) {
   const int x = blockIdx.x * 16 + (threadIdx.x & 15);
@@ -253,7 +307,30 @@ __global__ void k_macrocells(VolumeD v, uint8_t *empty) {
   empty[ci] = m <= 0.f ? 1 : 0;
 }
 
+// one thread per voxel of the bricked layout (padding voxels get 0)
+__global__ void k_brick(VolumeD v, const float *linear, float *bricked, long long total) {
+  const long long o = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (o >= total) return;
+  const long long b = o >> 9;
+  const int w = int(o & 511);
+  const long long bxy = (long long)v.bx * v.by;
+  const int I = int(b % v.bx), J = int((b / v.bx) % v.by), K = int(b / bxy);
+  const int i = I * 8 + (w & 7), j = J * 8 + ((w >> 3) & 7), k = K * 8 + (w >> 6);
+  bricked[o] = (i < v.nx && j < v.ny && k < v.nz) ? linear[(size_t(k) * v.ny + j) * v.nx + i] : 0.f;
+}
+
 }  // namespace
+
+size_t brickedVolumeBytes(int nx, int ny, int nz) {
+  const size_t bx = (nx + 7) / 8, by = (ny + 7) / 8, bz = (nz + 7) / 8;
+  return bx * by * bz * 512 * sizeof(float);
+}
+
+cudaError_t brickVolume(const VolumeD &v, const float *linear, float *bricked, cudaStream_t st) {
+  const long long total = (long long)v.bx * v.by * v.bz * 512;
+  k_brick<<<unsigned((total + 255) / 256), 256, 0, st>>>(v, linear, bricked, total);
+  return cudaGetLastError();
+}
 
 cudaError_t buildMacrocells(VolumeD &v, uint8_t *empty, cudaStream_t st) {
   const int n = v.cx * v.cy * v.cz;
