@@ -46,6 +46,9 @@ TRAFFIC = {
     # 12 trace launches of one 1920x1080 16 spp frame: 12.6 GB DRAM vs 130.4 GB algorithmic
     "pt_instanced_spheres_1080p": {"dram_per_alg_byte": 0.0966,
                                    "source": "profiles/k_trace_queue_pt_instanced_1080p_traffic.md"},
+    # one 1024x1024 4 spp frame: 2.65 GB DRAM vs 12.6 GB algorithmic (32 B per sample)
+    "scivis_volume_512cube_1024": {"dram_per_alg_byte": 0.21,
+                                   "source": "profiles/k_render_scivis_volume_512cube.md"},
 }
 
 
