@@ -268,20 +268,43 @@ int b200_scene_set_volume(b200_scene scene, const float *data, int nx, int ny, i
                           const float *spacing, const float *color, int ncolor, const float *opacity, int nopacity,
                           const float *valueRange, float densityScale);
 
-/* ---- SciVis renderer over a volume-only world (SciVis::commit
- *      render/scivis/SciVis.cpp:27-84, SciVis_renderSample
- *      render/scivis/SciVis.ispc:24-222).  Gradient shading is off (the
- *      volumetric model's default gradientShadingScale 0); with no lights in
- *      the world, shadows and AO have nothing to act on. */
+/* ---- SciVis renderer (SciVis::commit render/scivis/SciVis.cpp:27-84,
+ *      SciVis_renderSample render/scivis/SciVis.ispc:24-222,
+ *      SciVis_computeShading render/scivis/surfaces.ispc:90-128,
+ *      lightAlpha render/scivis/lightAlpha.ispc:19-122).
+ * Worlds with surfaces: Blinn-Phong over the non-ambient lights of
+ * b200_scene_set_lights (area lights sampled at their centre), hard shadows
+ * through translucent surfaces and the volume when `shadows` is set, AO
+ * (`aoSamples` rays up to `aoDistance`) tinted by the summed ambient
+ * radiance x pi, lights seen directly when `visibleLights` is set, and the
+ * volume (if any) composited in front of each surface.  Volume-only worlds
+ * take a dedicated kernel.  Gradient shading of volumes is off (the
+ * volumetric model's default gradientShadingScale 0). */
 typedef struct {
   int pixelSamples;
   float volumeSamplingRate; /* default 1 */
   float backgroundColor[4];
   int pixelFilter;
-  int collectStats;         /* counters: [rays, volume samples, 0, 0] */
+  int collectStats;         /* volume-only worlds: [rays, volume samples, 0, 0]; else traversal counters */
+  int shadows;              /* default 0 */
+  int visibleLights;        /* default 0 */
+  int aoSamples;            /* default 0 */
+  float aoDistance;         /* default 1e20 */
+  float minContribution;    /* default 0.001 */
 } b200_scivis_params;
+/* The material parameters SciVis reads (evalMaterial,
+ * render/scivis/surfaces.ih:44-84): isObj != 0 for an "obj" material (kd,
+ * ks, ns, d, tf as in OBJMaterial::commit render/materials/OBJ.cpp); any
+ * other material shades white and opaque.  material_id of an instance
+ * indexes this array; ids outside it shade with the defaults. */
+typedef struct {
+  int isObj;
+  float kd[3], ks[3];
+  float ns, d;
+  float tf[3];
+} b200_scivis_material;
 int b200_render_scivis(b200_scene scene, const b200_camera_desc *camera, const b200_scivis_params *params,
-                       b200_frame fb, void *stream);
+                       const b200_scivis_material *materials, int nmaterials, b200_frame fb, void *stream);
 
 /* Traversal counters accumulated by renders with collectStats set:
  * [rays traced, BVH node visits, triangle tests, sphere tests]; reset != 0

@@ -15,6 +15,7 @@
 #include <cstring>
 #include <vector>
 
+#include "pt_bsdf.h"
 #include "render.h"
 
 namespace orc {
@@ -239,6 +240,299 @@ V4 integrateVolume(const VolumeModel &m, const Ray &ray, float jitter, float sam
   return {color.x, color.y, color.z, T};
 }
 
+// ---------------------------------------------------------------- SciVis with surfaces
+//   SciVis_renderSample        render/scivis/SciVis.ispc:24-222
+//   SciVis_computeAO           render/scivis/SciVis.ispc:224-281
+//   directIllumination, SciVis_computeShading, evaluateLights
+//                              render/scivis/surfaces.ispc:17-128
+//   evalMaterial               render/scivis/surfaces.ih:44-84
+//   lightAlpha                 render/scivis/lightAlpha.ispc:19-122
+//   integrateVolumeIntervals   render/ao/volumes.ispc:32-240 (shadow/AO rays)
+//   light list and aoColorPi   render/scivis/SciVisData.cpp:15-105
+// Surfaces carry no per-vertex colour here, so dg.color = (1, 1, 1, 1).
+
+struct SvMaterial {
+  int isObj;
+  V3 kd, ks;
+  float ns, d;
+  V3 tf;
+};
+
+struct SvBSDF {
+  V3 diffuse, specular;
+  float shininess;
+  V3 transmission, albedo;
+  float opacity;
+};
+
+SvBSDF svEvalMaterial(const SvMaterial *m) {
+  SvBSDF r;
+  r.diffuse = v3(1.f);
+  r.specular = v3(0.f);
+  r.shininess = 10.f;
+  r.transmission = v3(0.f);
+  r.opacity = 1.f;
+  if (m && m->isObj) {
+    const float d = m->d;
+    r.diffuse = r.diffuse * m->kd;
+    r.diffuse = r.diffuse * d;
+    r.specular = d * m->ks;
+    r.shininess = m->ns;
+    r.transmission = m->tf * d + v3(1.f - d);
+    r.opacity = d;
+  }
+  r.albedo = r.diffuse + r.specular;
+  r.shininess *= 4.f;
+  r.diffuse = r.diffuse * float(1.0 / M_PI);
+  r.specular = r.specular * ((r.shininess + 2.f) * float(0.25 / M_PI) *
+                             (1.f / (2.f - std::exp(r.shininess * -float(M_LN2 / 2.0)))));
+  return r;
+}
+
+struct SvLight {
+  int kind;  // 0 quad, 1 ambient
+  bool visible;
+  QuadLight quad;
+  AmbientLight amb;
+  LightSample sample(const DG &dg, V2 s) const { return kind == 0 ? quad.sample(dg, s) : amb.sample(dg, s); }
+  LightEval eval(const DG &dg, V3 dir, float lo, float hi) const {
+    return kind == 0 ? quad.eval(dg, dir, lo, hi) : amb.eval(dg, dir, lo, hi);
+  }
+};
+
+struct SvParams {
+  int spp;
+  float samplingRate;
+  V4 bg;
+  int shadows, visibleLights, aoSamples;
+  float aoRadius, minContribution;
+};
+
+struct SvWorld {
+  const Scene *scene;
+  const VolumeModel *vm;  // may be null
+  std::vector<SvLight> lights;  // SciVisData order: visible-only (ambient) lights first
+  uint32_t numVisibleOnly = 0;
+  V3 aoColor = v3(0.f);  // sum of the ambient radiances (aoColorPi = aoColor * pi)
+  std::vector<SvMaterial> mats;
+  // SciVisData::SciVisData / addVisibleOnlyToArray: an ambient light goes to
+  // slot numVisibleOnly (the light there moves to the end) and adds its
+  // radiance to the AO colour
+  void addLight(const SvLight &L) {
+    if (L.kind == 1) {
+      if (numVisibleOnly == lights.size()) {
+        lights.push_back(L);
+      } else {
+        lights.push_back(lights[numVisibleOnly]);
+        lights[numVisibleOnly] = L;
+      }
+      numVisibleOnly++;
+      aoColor = aoColor + L.amb.radiance;
+    } else {
+      lights.push_back(L);
+    }
+  }
+  const SvMaterial *material(const Hit &h) const {
+    const int m = scene->entries[h.entry].material;
+    return (m >= 0 && m < int(mats.size())) ? &mats[size_t(m)] : nullptr;
+  }
+};
+
+// does [ray.tnear, ray.tfar] overlap the volume's grid box (the test that
+// starts IntervalIter)
+bool svVolumeOverlaps(const Volume &vol, const Ray &ray) {
+  IntervalIter it;
+  it.init(vol, ray.org, ray.dir, ray.tnear, ray.tfar);
+  return !it.done;
+}
+
+// integrateVolumeIntervals (render/ao/volumes.ispc): opacity accumulated
+// front to back until 0.99; NaN samples are skipped inside sampleVolume
+float svVolumeAlpha(const VolumeModel &m, const Ray &ray, float jitter, float samplingRate) {
+  IntervalIter it;
+  it.init(m.vol, ray.org, ray.dir, ray.tnear, ray.tfar);
+  const float nominalDeltaT = std::fmin(m.vol.spacing.x, std::fmin(m.vol.spacing.y, m.vol.spacing.z));
+  float alpha = 0.f, distance = INFINITY, iuDistance = jitter, iuLength = 0.f, step = 0.f;
+  float ilo = 0.f, ihi = INFINITY;
+  for (int g = 0; g < (1 << 24) && alpha < 0.99f; g++) {
+    float dt = 0.f, val = NAN;
+    for (int h = 0; h < (1 << 24) && std::isnan(val); h++) {
+      float emptySpace = 0.f;
+      while (iuDistance > iuLength) {
+        const float prevUpper = ihi;
+        if (!it.next(ilo, ihi)) return alpha;
+        emptySpace += std::fmax(ilo - prevUpper, 0.f);
+        iuDistance -= iuLength;
+        step = nominalDeltaT / samplingRate;
+        iuLength = (ihi - ilo) / step;
+        distance = distance == INFINITY ? ilo : distance;
+      }
+      const float newDistance = ilo + iuDistance * step;
+      val = m.vol.sample(ray.org + newDistance * ray.dir);
+      iuDistance += 1.f;
+      dt = newDistance - distance - emptySpace;
+      distance = newDistance;
+    }
+    const V4 c = m.tf.get(val);
+    const float op = 1.f - std::exp(-c.w * dt * m.densityScale);
+    alpha = alpha + (1.f - alpha) * op;
+  }
+  return alpha;
+}
+
+inline float svLuminance(V3 c) { return 0.212671f * c.x + 0.715160f * c.y + 0.072169f * c.z; }
+
+V3 svLightAlpha(const SvWorld &w, const SvParams &p, Ray ray, RandomSampler &rs, V3 weight, float quality) {
+  V3 alpha = v3(1.f);
+  const float orgTMax = ray.tfar;
+  for (int g = 0; g < 1024; g++) {
+    Hit hit;
+    tl_rays++;
+    const bool h = w.scene->intersect(ray, hit);
+    if (w.vm) {
+      Ray vr = ray;
+      vr.tfar = h ? hit.t : ray.tfar;
+      if (svVolumeOverlaps(w.vm->vol, vr)) {
+        const float jitter = rs.getFloat();
+        alpha = alpha * (1.f - svVolumeAlpha(*w.vm, vr, jitter, p.samplingRate * quality));
+      }
+    }
+    if (!h) break;
+    const DG dg = postIntersect(*w.scene, ray, hit);
+    alpha = alpha * svEvalMaterial(w.material(hit)).transmission;
+    ray.tnear = hit.t + dg.epsilon;
+    ray.tfar = orgTMax;
+    if (svLuminance(alpha * weight) < p.minContribution) {
+      alpha = v3(0.f);
+      break;
+    }
+  }
+  return alpha;
+}
+
+V3 svComputeAO(const SvWorld &w, const SvParams &p, const DG &dg, int px, int py, uint32_t sampleZ,
+                RandomSampler &rs) {
+  const uint32_t accumID = sampleZ * uint32_t(p.aoSamples);
+  uint32_t t0 = uint32_t(px), t1 = uint32_t(py);
+  tea8(t0, t1);
+  const V2 rot = {to_float_unorm(t0), to_float_unorm(t1)};
+  V3 hits = v3(0.f);
+  const L3 l2w = frame(dg.Ns);
+  for (int i = 0; i < p.aoSamples; i++) {
+    const float hx = PermHalton_sample5(accumID + uint32_t(i)), hy = PermHalton_sample7(accumID + uint32_t(i));
+    const float rx = CranleyPattersonRotation(hx, rot.x), ry = CranleyPattersonRotation(hy, rot.y);
+    const float phi = float(2.0 * M_PI) * rx;
+    const float cosT = std::sqrt(ry), sinT = std::sqrt(1.f - ry);
+    const V3 dir = xfmVector(l2w, {std::cos(phi) * sinT, std::sin(phi) * sinT, cosT});
+    if (dot(dir, dg.Ns) < 0.01f) {
+      hits = hits + v3(1.f);
+      continue;
+    }
+    const Ray aoRay = {dg.P, dg.epsilon, dir, p.aoRadius};
+    hits = hits + (v3(1.f) - svLightAlpha(w, p, aoRay, rs, v3(1.f), 0.1f));
+  }
+  return v3(1.f) - hits * (1.f / float(p.aoSamples));
+}
+
+struct SvShading {
+  V3 shadedColor, transmission;
+  float opacity;
+};
+
+SvShading svComputeShading(const SvWorld &w, const SvParams &p, const DG &dg, const SvMaterial *mat, V3 inDir,
+                           int px, int py, uint32_t sampleZ, RandomSampler &rs) {
+  const SvBSDF bsdf = svEvalMaterial(mat);
+  V3 color = v3(0.f);
+  for (size_t i = w.numVisibleOnly; i < w.lights.size(); i++) {
+    const LightSample ls = w.lights[i].sample(dg, {0.f, 0.f});  // area lights at their centre
+    if (std::fmax(ls.weight.x, std::fmax(ls.weight.y, ls.weight.z)) > 0.f) {
+      const float cosNL = dot(ls.dir, dg.Ns);
+      if (cosNL < 0.f) continue;
+      const V3 H = normalize(ls.dir - inDir);
+      const float cosNH = dot(H, dg.Ns);
+      const V3 specular = bsdf.specular * std::pow(cosNH, bsdf.shininess);
+      const V3 diffuse = bsdf.diffuse * cosNL;
+      const V3 contrib = (diffuse + specular) * ls.weight;
+      if (p.shadows) {
+        if (svLuminance(contrib) > p.minContribution) {
+          V3 P = dg.P;
+          if (dot(dg.Ng, ls.dir) < 0.f) P = P - (2.f * dg.epsilon) * dg.Ng;
+          const V3 la = svLightAlpha(w, p, {P, 0.f, ls.dir, ls.dist}, rs, contrib, 0.25f);
+          color = color + la * contrib;
+        }
+      } else {
+        color = color + contrib;
+      }
+    }
+  }
+  V3 ao = v3(1.f);
+  if (p.aoSamples > 0 && svLuminance(w.aoColor * float(M_PI)) > p.minContribution)
+    ao = svComputeAO(w, p, dg, px, py, sampleZ, rs);
+  color = color + bsdf.diffuse * ao * (w.aoColor * float(M_PI));
+  return {color, bsdf.transmission, bsdf.opacity};
+}
+
+ScreenSample svRenderSample(const SvWorld &w, const SvParams &p, Ray ray, int x, int y, int W, uint32_t sid,
+                            uint64_t &samples) {
+  RandomSampler rs;
+  rs.init(uint32_t(x + W * y), sid);
+  ScreenSample smp;
+  bool firstHit = true, allTrans = true;
+  const float originalTFar = ray.tfar;
+  V3 outColor = v3(0.f), outT = v3(1.f);
+  for (int g = 0; g < 1024; g++) {
+    Hit hit;
+    tl_rays++;
+    const bool h = w.scene->intersect(ray, hit);
+    const float rayT = h ? hit.t : ray.tfar;
+    if (w.vm) {
+      Ray vr = ray;
+      vr.tfar = rayT;
+      if (svVolumeOverlaps(w.vm->vol, vr)) {
+        const float jitter = rs.getFloat();
+        const V4 vc = integrateVolume(*w.vm, vr, jitter, p.samplingRate, p.minContribution, samples);
+        outColor = outColor + outT * v3(vc.x, vc.y, vc.z);
+        outT = outT * vc.w;
+      }
+    }
+    if (p.visibleLights) {
+      DG ldg;
+      ldg.P = ray.org;
+      V3 lc = v3(0.f);
+      for (const SvLight &L : w.lights)
+        if (L.visible) lc = lc + L.eval(ldg, ray.dir, ray.tnear, rayT).radiance;
+      outColor = outColor + outT * lc;
+    }
+    if (firstHit || allTrans) smp.z = rayT;
+    if (h) {
+      const DG dg = postIntersect(*w.scene, ray, hit);
+      const SvShading sh = svComputeShading(w, p, dg, w.material(hit), ray.dir, x, y, sid, rs);
+      if (firstHit || allTrans) {
+        smp.primID = dg.primID;
+        smp.geomID = dg.geomID;
+        smp.instID = dg.instID;
+        firstHit = false;
+      }
+      allTrans = allTrans && sh.opacity < p.minContribution;
+      outColor = outColor + outT * sh.shadedColor;
+      outT = outT * sh.transmission;
+      if (svLuminance(outT) < p.minContribution) {
+        outT = v3(0.f);
+        break;
+      }
+      ray.tnear = hit.t + dg.epsilon;
+      ray.tfar = originalTFar;
+    } else {
+      outColor = outColor + outT * v3(p.bg.x, p.bg.y, p.bg.z);
+      outT = outT * (1.f - p.bg.w);
+      break;
+    }
+  }
+  smp.rgb = outColor;
+  smp.alpha = 1.f - svLuminance(outT);
+  return smp;
+}
+
 }  // namespace orc
 
 using namespace orc;
@@ -335,6 +629,99 @@ void or_render_scivis_volume(void *mp, const OrCameraV *c, int pixelFilter, int 
     fb.frameID++;
   }
   std::memcpy(color, fb.color.data(), size_t(W) * H * 16);
+}
+
+struct OrScivisLight {
+  int kind, visible;
+  float pos[3], e1[3], e2[3], radiance[3];
+};
+struct OrScivisMaterial {
+  int isObj;
+  float kd[3], ks[3], ns, d, tf[3];
+};
+struct OrScivisParams {
+  int spp;
+  float samplingRate;
+  float bg[4];
+  int shadows, visibleLights, aoSamples;
+  float aoRadius, minContribution;
+  int pixelFilter;
+};
+
+// SciVis frames of a world with surfaces (and optionally the volume mp);
+// rows [y0, y1) (y1 <= 0: all); color RGBA, depth, ids = primID|geomID|instID planes
+void or_render_scivis(void *scp, void *mp, const OrCameraV *c, const OrScivisParams *pp, const OrScivisLight *lights,
+                      int nlights, const OrScivisMaterial *mats, int nmats, int W, int H, int frames, int y0, int y1,
+                      float *color, float *depth, uint32_t *ids, int nthreads) {
+  SvWorld w;
+  w.scene = static_cast<Scene *>(scp);
+  w.vm = static_cast<VolumeModel *>(mp);
+  for (int i = 0; i < nlights; i++) {
+    const OrScivisLight &l = lights[i];
+    SvLight L;
+    L.kind = l.kind;
+    L.visible = l.visible != 0;
+    const V3 rad = {l.radiance[0], l.radiance[1], l.radiance[2]};
+    if (l.kind == 0) {
+      L.quad.init({l.pos[0], l.pos[1], l.pos[2]}, {l.e1[0], l.e1[1], l.e1[2]}, {l.e2[0], l.e2[1], l.e2[2]}, rad);
+      L.quad.visible = L.visible;
+    } else {
+      L.amb = {rad, L.visible};
+    }
+    w.addLight(L);
+  }
+  for (int i = 0; i < nmats; i++) {
+    const OrScivisMaterial &m = mats[i];
+    w.mats.push_back({m.isObj, {m.kd[0], m.kd[1], m.kd[2]}, {m.ks[0], m.ks[1], m.ks[2]}, m.ns, m.d,
+                      {m.tf[0], m.tf[1], m.tf[2]}});
+  }
+  SvParams p = {pp->spp, pp->samplingRate, {pp->bg[0], pp->bg[1], pp->bg[2], pp->bg[3]}, pp->shadows,
+                pp->visibleLights, pp->aoSamples, pp->aoRadius, pp->minContribution};
+  const Camera cam = makeCamera({c->pos[0], c->pos[1], c->pos[2]}, {c->dir[0], c->dir[1], c->dir[2]},
+                                {c->up[0], c->up[1], c->up[2]}, c->fovy, c->aspect, c->nearClip);
+  PixelFilter pf;
+  pf.init(pp->pixelFilter);
+  FrameBuffer fb;
+  fb.resize(W, H);
+  if (y1 <= 0) {
+    y0 = 0;
+    y1 = H;
+  }
+  const V2 rcpSize = {1.f / float(W), 1.f / float(H)};
+  for (int f = 0; f < frames; f++) {
+    const uint32_t start = uint32_t(fb.frameID * p.spp + 1);
+    parallelRows(y1 - y0, nthreads, [&](int yy) {
+      const int y = y0 + yy;
+      uint64_t samples = 0;
+      for (int x = 0; x < W; x++) {
+        ScreenSample acc;
+        for (int s = 0; s < p.spp; s++) {
+          const uint32_t sid = start + uint32_t(s);
+          const V2 ps = {Halton_sample2(sid), CranleyPattersonRotation(Halton_sample3(sid), 1.f / 6.f)};
+          const V2 pfs = pf.sample(ps);
+          const V2 center = {(float(x) + 0.5f) * rcpSize.x, (float(y) + 0.5f) * rcpSize.y};
+          const Ray ray = cameraRay(cam, {center.x + pfs.x * rcpSize.x, center.y + pfs.y * rcpSize.y});
+          accumulateScreen(acc, svRenderSample(w, p, ray, x, y, W, sid, samples));
+        }
+        const float rspp = 1.f / float(p.spp);
+        acc.rgb = acc.rgb * rspp;
+        acc.alpha *= rspp;
+        fbAccumulate(fb, x, y, acc);
+      }
+      g_volSamples.fetch_add(samples);
+      g_rayCount.fetch_add(tl_rays);
+      tl_rays = 0;
+    });
+    fb.frameID++;
+  }
+  const size_t N = size_t(W) * H;
+  if (color) std::memcpy(color, fb.color.data(), N * 16);
+  if (depth) std::memcpy(depth, fb.depth.data(), N * 4);
+  if (ids) {
+    std::memcpy(ids, fb.primID.data(), N * 4);
+    std::memcpy(ids + N, fb.geomID.data(), N * 4);
+    std::memcpy(ids + 2 * N, fb.instID.data(), N * 4);
+  }
 }
 
 }  // extern "C"

@@ -124,15 +124,39 @@ def pt_params(spp=1, max_path_length=20, roulette_path_length=5, max_scattering_
 class ScivisParams(ctypes.Structure):
     _fields_ = [("pixelSamples", ctypes.c_int), ("volumeSamplingRate", ctypes.c_float),
                 ("backgroundColor", ctypes.c_float * 4), ("pixelFilter", ctypes.c_int),
-                ("collectStats", ctypes.c_int)]
+                ("collectStats", ctypes.c_int), ("shadows", ctypes.c_int), ("visibleLights", ctypes.c_int),
+                ("aoSamples", ctypes.c_int), ("aoDistance", ctypes.c_float), ("minContribution", ctypes.c_float)]
 
 
-def scivis_params(spp=1, sampling_rate=1.0, bg=(0, 0, 0, 0), pixel_filter=PF_GAUSS, stats=False):
+def scivis_params(spp=1, sampling_rate=1.0, bg=(0, 0, 0, 0), pixel_filter=PF_GAUSS, stats=False, shadows=False,
+                  visible_lights=False, ao_samples=0, ao_distance=1e20, min_contribution=0.001):
     p = ScivisParams()
     p.pixelSamples, p.volumeSamplingRate = int(spp), float(sampling_rate)
     p.backgroundColor[:] = list(map(float, bg))
     p.pixelFilter, p.collectStats = int(pixel_filter), int(bool(stats))
+    p.shadows, p.visibleLights, p.aoSamples = int(bool(shadows)), int(bool(visible_lights)), int(ao_samples)
+    p.aoDistance, p.minContribution = float(ao_distance), float(min_contribution)
     return p
+
+
+class ScivisMaterial(ctypes.Structure):
+    _fields_ = [("isObj", ctypes.c_int), ("kd", ctypes.c_float * 3), ("ks", ctypes.c_float * 3),
+                ("ns", ctypes.c_float), ("d", ctypes.c_float), ("tf", ctypes.c_float * 3)]
+
+
+def scivis_materials_array(mats):
+    """mats: iterable of dicts {"kd", "ks", "ns", "d", "tf"} for "obj"
+    materials (values after OBJ commit), or None for any other material."""
+    arr = (ScivisMaterial * max(1, len(mats)))()
+    for i, m in enumerate(mats):
+        if m is None:
+            continue
+        arr[i].isObj = 1
+        arr[i].kd[:] = [float(x) for x in m.get("kd", (0.8, 0.8, 0.8))]
+        arr[i].ks[:] = [float(x) for x in m.get("ks", (0, 0, 0))]
+        arr[i].ns, arr[i].d = float(m.get("ns", 10.0)), float(m.get("d", 1.0))
+        arr[i].tf[:] = [float(x) for x in m.get("tf", (0, 0, 0))]
+    return arr, len(mats)
 
 
 def lib_path():
@@ -207,7 +231,7 @@ def lib():
             "b200_render_ao": (I, [P, ctypes.POINTER(CameraDesc), ctypes.POINTER(AOParams), P, P]),
             "b200_scene_set_lights": (I, [P, P, I]),
             "b200_scene_set_volume": (I, [P, P, I, I, I, P, P, P, I, P, I, P, F]),
-            "b200_render_scivis": (I, [P, ctypes.POINTER(CameraDesc), ctypes.POINTER(ScivisParams), P, P]),
+            "b200_render_scivis": (I, [P, ctypes.POINTER(CameraDesc), ctypes.POINTER(ScivisParams), P, I, P, P]),
             "b200_render_pt": (I, [P, ctypes.POINTER(CameraDesc), ctypes.POINTER(PTParams), P, I, P, P]),
         }
         for name, (res, args) in sig.items():
@@ -468,9 +492,12 @@ def render_ao(scene, camera, params, frame, stream=None):
                                              ctypes.c_void_p(stream) if stream else None))
 
 
-def render_scivis(scene, camera, params, frame, stream=None):
-    scene.device._check(lib().b200_render_scivis(scene._h, ctypes.byref(camera), ctypes.byref(params), frame._h,
-                                                 ctypes.c_void_p(stream) if stream else None))
+def render_scivis(scene, camera, params, frame, materials=None, stream=None):
+    """materials: (ctypes array, count) from scivis_materials_array(), or None."""
+    arr, n = materials if materials else (None, 0)
+    scene.device._check(lib().b200_render_scivis(scene._h, ctypes.byref(camera), ctypes.byref(params),
+                                                 ctypes.cast(arr, ctypes.c_void_p) if arr is not None else None, n,
+                                                 frame._h, ctypes.c_void_p(stream) if stream else None))
 
 
 def render_pt(scene, camera, params, materials, frame, stream=None):

@@ -295,6 +295,8 @@ SceneObj::~SceneObj() {
   if (dEntries) cudaFreeAsync(dEntries, st);
   cudaStreamSynchronize(st);
   if (dLights) cudaFree(dLights);
+  if (dScivisLights) cudaFree(dScivisLights);
+  if (dScivisMats) cudaFree(dScivisMats);
   if (dLightCdf) cudaFree(dLightCdf);
   if (dMaterials) cudaFree(dMaterials);
   for (void *p : {(void *)dVolData, (void *)dTfOpacity, (void *)dTfColor, (void *)dCellEmpty})
@@ -805,16 +807,41 @@ int b200_scene_set_lights(b200_scene s, const b200_light *lights, int n) {
       const float r = 1.f / sum;
       for (auto &c : cdf) c = c >= sum ? 0x1.000002p+0f : c * r;
     }
+    // SciVisData order (render/scivis/SciVisData.cpp:15-58): an ambient light
+    // takes slot numVisibleOnly, the light there moves to the end
+    std::vector<LightD> sv;
+    int visibleOnly = 0;
+    V3 aoColor = mk(0.f, 0.f, 0.f);
+    for (int i = 0; i < n; i++) {
+      if (h[i].type == LIGHT_AMBIENT) {
+        if (visibleOnly == int(sv.size())) {
+          sv.push_back(h[i]);
+        } else {
+          sv.push_back(sv[visibleOnly]);
+          sv[visibleOnly] = h[i];
+        }
+        visibleOnly++;
+        aoColor = aoColor + h[i].radiance;
+      } else {
+        sv.push_back(h[i]);
+      }
+    }
     if (sc->dLights) cudaFree(sc->dLights);
     if (sc->dLightCdf) cudaFree(sc->dLightCdf);
+    if (sc->dScivisLights) cudaFree(sc->dScivisLights);
     sc->dLights = nullptr;
     sc->dLightCdf = nullptr;
+    sc->dScivisLights = nullptr;
     sc->nLights = n;
+    sc->numVisibleOnly = visibleOnly;
+    sc->aoColor = aoColor;
     if (n) {
       check(cudaMalloc(&sc->dLights, sizeof(LightD) * n), "alloc lights");
       check(cudaMalloc(&sc->dLightCdf, sizeof(float) * n), "alloc lights");
+      check(cudaMalloc(&sc->dScivisLights, sizeof(LightD) * n), "alloc lights");
       check(cudaMemcpy(sc->dLights, h.data(), sizeof(LightD) * n, cudaMemcpyHostToDevice), "upload lights");
       check(cudaMemcpy(sc->dLightCdf, cdf.data(), sizeof(float) * n, cudaMemcpyHostToDevice), "upload lights");
+      check(cudaMemcpy(sc->dScivisLights, sv.data(), sizeof(LightD) * n, cudaMemcpyHostToDevice), "upload lights");
     }
   });
 }
@@ -908,24 +935,81 @@ int b200_scene_set_volume(b200_scene s, const float *data, int nx, int ny, int n
   });
 }
 
-int b200_render_scivis(b200_scene s, const b200_camera_desc *camera, const b200_scivis_params *p, b200_frame f,
-                       void *stream) {
+int b200_render_scivis(b200_scene s, const b200_camera_desc *camera, const b200_scivis_params *p,
+                       const b200_scivis_material *materials, int nmaterials, b200_frame f, void *stream) {
   if (!s || !camera || !p || !f) return B200_INVALID_ARGUMENT;
   SceneObj *sc = reinterpret_cast<SceneObj *>(s);
   FrameObj *fb = reinterpret_cast<FrameObj *>(f);
   return guarded(sc->dev, [&]() {
-    if (!sc->hasVolume) throw Error(B200_INVALID_OPERATION, "world has no volume");
+    const bool surfaces = sc->committed && sc->tlas.nnodes > 0;
+    if (!surfaces && !sc->hasVolume) throw Error(B200_INVALID_OPERATION, "world has no surfaces and no volume");
     require(p->pixelSamples >= 1 && p->volumeSamplingRate > 0.f, "bad scivis parameters");
     require(p->pixelFilter >= B200_PF_POINT && p->pixelFilter <= B200_PF_BLACKMAN_HARRIS, "bad pixel filter");
+    require(p->aoSamples >= 0, "bad scivis parameters");
+    require(nmaterials >= 0 && (nmaterials == 0 || materials), "bad material array");
     ScivisParamsD d;
     d.spp = p->pixelSamples;
     d.samplingRate = p->volumeSamplingRate;
     for (int k = 0; k < 4; k++) d.bg[k] = p->backgroundColor[k];
     cudaStream_t st = stream ? (cudaStream_t)stream : sc->dev->stream;
-    check(launchRenderScivisVolume(sc->dev->tables, sc->view(), sc->vol, makeCamera(*camera),
-                                   sc->dev->filter(p->pixelFilter), d, fb->view(), p->collectStats != 0, st,
-                                   sc->dev->timer),
-          "scivis launch");
+    if (!surfaces) {
+      check(launchRenderScivisVolume(sc->dev->tables, sc->view(), sc->vol, makeCamera(*camera),
+                                     sc->dev->filter(p->pixelFilter), d, fb->view(), p->collectStats != 0, st,
+                                     sc->dev->timer),
+            "scivis launch");
+    } else {
+      const bool same = int(sc->lastScivisMats.size()) == nmaterials &&
+                        (nmaterials == 0 || std::memcmp(sc->lastScivisMats.data(), materials,
+                                                        sizeof(b200_scivis_material) * nmaterials) == 0);
+      bool opaque = true;
+      for (int i = 0; i < nmaterials; i++) {
+        const b200_scivis_material &m = materials[i];
+        if (m.isObj && !(m.d == 1.f && m.tf[0] * m.d == 0.f && m.tf[1] * m.d == 0.f && m.tf[2] * m.d == 0.f))
+          opaque = false;
+      }
+      if (!same) {
+        std::vector<ScivisMatD> h(nmaterials);
+        for (int i = 0; i < nmaterials; i++) {
+          const b200_scivis_material &m = materials[i];
+          h[i].isObj = m.isObj != 0;
+          for (int k = 0; k < 3; k++) {
+            h[i].kd[k] = m.kd[k];
+            h[i].ks[k] = m.ks[k];
+            h[i].tf[k] = m.tf[k];
+          }
+          h[i].ns = m.ns;
+          h[i].d = m.d;
+        }
+        if (nmaterials > sc->capScivisMats) {
+          if (sc->dScivisMats) cudaFree(sc->dScivisMats);
+          sc->dScivisMats = nullptr;
+          check(cudaMalloc(&sc->dScivisMats, sizeof(ScivisMatD) * nmaterials), "alloc materials");
+          sc->capScivisMats = nmaterials;
+        }
+        if (nmaterials)
+          check(cudaMemcpy(sc->dScivisMats, h.data(), sizeof(ScivisMatD) * nmaterials, cudaMemcpyHostToDevice),
+                "upload materials");
+        sc->lastScivisMats.assign(materials, materials + nmaterials);
+      }
+      ScivisSurfD S;
+      S.mats = sc->dScivisMats;
+      S.nmats = nmaterials;
+      S.lights = sc->dScivisLights;
+      S.nlights = sc->nLights;
+      S.numVisibleOnly = sc->numVisibleOnly;
+      S.aoColor = sc->aoColor;
+      S.shadows = p->shadows != 0;
+      S.visibleLights = p->visibleLights != 0;
+      S.aoSamples = p->aoSamples;
+      S.aoRadius = p->aoDistance;
+      S.minContribution = p->minContribution;
+      S.hasVolume = sc->hasVolume;
+      S.opaqueShadows = opaque && !sc->hasVolume;
+      check(launchRenderScivisSurfaces(sc->dev->tables, sc->view(), sc->vol, makeCamera(*camera),
+                                       sc->dev->filter(p->pixelFilter), d, S, fb->view(), p->collectStats != 0, st,
+                                       sc->dev->timer),
+            "scivis launch");
+    }
     fb->frameID++;
     framePostProcess(fb, st);
   });

@@ -84,6 +84,14 @@ struct SceneObj {
   int nLights = 0;
   MaterialD *dMaterials = nullptr;
   int nMaterials = 0, capMaterials = 0;
+  // SciVis state: the lights in SciVisData order, the summed ambient radiance
+  // and the renderer's material list
+  LightD *dScivisLights = nullptr;
+  int numVisibleOnly = 0;
+  V3 aoColor = {0.f, 0.f, 0.f};
+  ScivisMatD *dScivisMats = nullptr;
+  int capScivisMats = 0;
+  std::vector<b200_scivis_material> lastScivisMats;
   // one structured-regular volumetric model (device copies)
   bool hasVolume = false;
   VolumeD vol = {};

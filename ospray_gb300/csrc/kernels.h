@@ -118,6 +118,30 @@ struct ScivisParamsD {
   float bg[4];
 };
 
+// SciVis surfaces: per renderer material slot the OBJ parameters that
+// evalMaterial reads (render/scivis/surfaces.ih:44-84); isObj 0 = any other
+// material type, shaded with the SciVis defaults (white, opaque).
+struct ScivisMatD {
+  int isObj;
+  float kd[3], ks[3], ns, d, tf[3];
+};
+
+// SciVis surface shading inputs: lights in SciVisData order (the ambient,
+// visible-only lights first, render/scivis/SciVisData.cpp:15-105), the summed
+// ambient radiance (aoColorPi = aoColor * pi) and the renderer parameters
+// (render/scivis/SciVis.cpp:29-36, render/Renderer.cpp:43).
+struct ScivisSurfD {
+  const ScivisMatD *mats;
+  int nmats;
+  const LightD *lights;
+  int nlights, numVisibleOnly;
+  V3 aoColor;
+  int shadows, visibleLights, aoSamples;
+  float aoRadius, minContribution;
+  int hasVolume;
+  int opaqueShadows;  // every material opaque and no volume: shadow and AO rays as any-hit queries
+};
+
 constexpr int VOL_BRICK = 8;
 // bytes of the bricked copy of an nx x ny x nz volume
 size_t brickedVolumeBytes(int nx, int ny, int nz);
@@ -127,6 +151,9 @@ cudaError_t buildMacrocells(VolumeD &v, uint8_t *empty, cudaStream_t st);
 cudaError_t launchRenderScivisVolume(const SamplerTables *T, const Scene &sc, const VolumeD &vol, const CameraD &cam,
                                      const PixelFilterD &pf, const ScivisParamsD &p, const FrameD &fb, bool stats,
                                      cudaStream_t st, KernelTimer *kt = nullptr);
+cudaError_t launchRenderScivisSurfaces(const SamplerTables *T, const Scene &sc, const VolumeD &vol, const CameraD &cam,
+                                       const PixelFilterD &pf, const ScivisParamsD &p, const ScivisSurfD &S,
+                                       const FrameD &fb, bool stats, cudaStream_t st, KernelTimer *kt = nullptr);
 
 // Path tracing with the neural radiance cache: per frame, paths whose index
 // p satisfies (p + trainOffset) % trainStride == 0 are training paths (slot

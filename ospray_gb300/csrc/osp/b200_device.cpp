@@ -280,10 +280,12 @@ OSPFuture B200Device::renderFrame(OSPFrameBuffer hf, OSPRenderer hr, OSPCamera h
       for (const auto &m : r->materials) mats.push_back(m->mat);
       check(b200_render_pt(w->scene, &c->desc, &r->pt, mats.data(), int(mats.size()), f->fb, nullptr));
     } else {
-      if (w->hasGeometry)
-        throw Error(OSP_INVALID_OPERATION, "scivis renderer: the b200 device renders volume-only worlds");
-      if (!w->hasVolume) throw Error(OSP_INVALID_OPERATION, "scivis renderer: the world has no volume");
-      check(b200_render_scivis(w->scene, &c->desc, &r->scivis, f->fb, nullptr));
+      if (!w->hasGeometry && !w->hasVolume)
+        throw Error(OSP_INVALID_OPERATION, "scivis renderer: the world has no geometry and no volume");
+      std::vector<b200_scivis_material> mats;
+      for (const auto &m : w->objectMaterials) mats.push_back(m->sv);
+      for (const auto &m : r->materials) mats.push_back(m->sv);
+      check(b200_render_scivis(w->scene, &c->desc, &r->scivis, mats.data(), int(mats.size()), f->fb, nullptr));
     }
     check(b200_event_record(dev_, &fut->end));
   } catch (...) {

@@ -93,6 +93,7 @@ void GeometryObj::bounds(float lo[3], float hi[3]) const {
 // ---------------------------------------------------------------- materials
 
 void MaterialObj::commit(B200Device &dev) {
+  sv = {};
   if (type == "principled") {
     const float def[3] = {0.8f, 0.8f, 0.8f};
     getVec3("baseColor", mat.baseColor, def);
@@ -111,16 +112,37 @@ void MaterialObj::commit(B200Device &dev) {
       if (has(d.name) && getFloat(d.name, d.value) != d.value)
         dev.warn(std::string("principled material: '") + d.name + "' other than " + std::to_string(d.value) +
                  " is not supported by the b200 device; using the default");
-  } else {  // obj: Lambertian kd (the OBJ model with its default ks = 0, d = 1)
+  } else {  // obj (OBJMaterial::commit, render/materials/OBJ.cpp:30-64)
     const float def[3] = {0.8f, 0.8f, 0.8f};
-    getVec3("kd", mat.baseColor, def);
+    float kd[3], ks[3], tf[3];
+    getVec3("kd", kd, def);
+    getVec3("ks", ks, kZero3);
+    getVec3("tf", tf, kZero3);
+    // energy conservation: kd + ks + tf scaled down to at most 1
+    float total = 0.f;
+    for (int k = 0; k < 3; k++) total = std::max(total, kd[k] + ks[k] + tf[k]);
+    if (total > 1.f)
+      for (int k = 0; k < 3; k++) {
+        kd[k] /= total;
+        ks[k] /= total;
+        tf[k] /= total;
+      }
+    sv.isObj = 1;
+    for (int k = 0; k < 3; k++) {
+      sv.kd[k] = kd[k];
+      sv.ks[k] = ks[k];
+      sv.tf[k] = tf[k];
+    }
+    sv.ns = getFloat("ns", 10.f);
+    sv.d = getFloat("d", 1.f);
+    // the path tracer renders it as Lambertian kd
+    for (int k = 0; k < 3; k++) mat.baseColor[k] = kd[k];
     mat.roughness = 0.f;
     mat.metallic = 0.f;
-    float ks[3];
-    getVec3("ks", ks, kZero3);
     if (ks[0] != 0.f || ks[1] != 0.f || ks[2] != 0.f)
-      dev.warn("obj material: specular 'ks' is not supported by the b200 device; rendered diffuse only");
-    if (getFloat("d", 1.f) != 1.f) dev.warn("obj material: 'd' < 1 (transparency) is not supported by the b200 device");
+      dev.warn("obj material: the b200 path tracer renders 'ks' as diffuse only (the scivis renderer uses it)");
+    if (sv.d != 1.f)
+      dev.warn("obj material: the b200 path tracer renders 'd' < 1 as opaque (the scivis renderer uses it)");
   }
 }
 
@@ -365,14 +387,17 @@ void RendererObj::commit(B200Device &) {
     std::memcpy(pt.backgroundColor, bg, 16);
     pt.pixelFilter = pf;
     pt.collectStats = 0;
-  } else {  // scivis
+  } else {  // scivis (SciVis::commit, render/scivis/SciVis.cpp:27-36)
     scivis.pixelSamples = spp;
     scivis.volumeSamplingRate = getFloat("volumeSamplingRate", 1.f);
     std::memcpy(scivis.backgroundColor, bg, 16);
     scivis.pixelFilter = pf;
     scivis.collectStats = 0;
-    getBool("shadows", false);  // inert on volume-only worlds without lights
-    getInt("aoSamples", 0);
+    scivis.shadows = getBool("shadows", false) ? 1 : 0;
+    scivis.visibleLights = getBool("visibleLights", false) ? 1 : 0;
+    scivis.aoSamples = std::max(0, getInt("aoSamples", 0));
+    scivis.aoDistance = getFloat("aoDistance", 1e20f);
+    scivis.minContribution = minContribution;
   }
 }
 

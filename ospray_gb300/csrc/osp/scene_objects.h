@@ -37,7 +37,8 @@ struct GeometryObj : SceneObj {
 // GB300 path tracer evaluates
 struct MaterialObj : SceneObj {
   using SceneObj::SceneObj;
-  b200_material mat = {};
+  b200_material mat = {};        // as the path tracer reads it
+  b200_scivis_material sv = {};  // as the SciVis renderer reads it
   void commit(B200Device &) override;
 };
 

@@ -1,0 +1,251 @@
+// SciVis renderer over worlds with surfaces (and optionally the volume in
+// front of them), following
+//   SciVis_renderSample        render/scivis/SciVis.ispc:24-222
+//   SciVis_computeAO           render/scivis/SciVis.ispc:224-281
+//   directIllumination, SciVis_computeShading, evaluateLights
+//                              render/scivis/surfaces.ispc:17-128
+//   evalMaterial               render/scivis/surfaces.ih:44-84
+//   lightAlpha                 render/scivis/lightAlpha.ispc:19-122
+//   integrateVolumeIntervals   render/ao/volumes.ispc:32-240 (shadow/AO rays)
+// One thread per pixel; surfaces carry no per-vertex colour, so dg.color is
+// (1, 1, 1, 1).  Volume-only worlds use k_render_scivis_volume.
+#include "kernels.h"
+#include "lights.cuh"
+#include "volume.cuh"
+
+namespace b200 {
+
+namespace {
+
+struct SvBSDF {
+  V3 diffuse, specular;
+  float shininess;
+  V3 transmission;
+  float opacity;
+};
+
+B200_D SvBSDF svEvalMaterial(const ScivisSurfD &S, uint32_t entry, const Scene &sc) {
+  SvBSDF r;
+  r.diffuse = splat(1.f);
+  r.specular = splat(0.f);
+  r.shininess = 10.f;
+  r.transmission = splat(0.f);
+  r.opacity = 1.f;
+  const uint32_t mi = sc.entries[entry].materialID;
+  if (mi < uint32_t(S.nmats)) {
+    const ScivisMatD m = S.mats[mi];
+    if (m.isObj) {
+      const float d = m.d;
+      r.diffuse = r.diffuse * mk(m.kd[0], m.kd[1], m.kd[2]);
+      r.diffuse = r.diffuse * d;
+      r.specular = d * mk(m.ks[0], m.ks[1], m.ks[2]);
+      r.shininess = m.ns;
+      r.transmission = mk(m.tf[0], m.tf[1], m.tf[2]) * d + splat(1.f - d);
+      r.opacity = d;
+    }
+  }
+  r.shininess *= 4.f;
+  r.diffuse = r.diffuse * 0.318309886f;  // 1/pi
+  r.specular = r.specular * ((r.shininess + 2.f) * 0.0795774715f *  // 1/(4 pi)
+                             (1.f / (2.f - expf(r.shininess * -0.346573590f))));  // ln(2)/2
+  return r;
+}
+
+// Transmission of a shadow or AO ray through translucent surfaces and the
+// volume; any-hit when every material is opaque and there is no volume.
+template <bool STATS>
+B200_D V3 svLightAlpha(const Scene &sc, const VolumeD &vol, const ScivisSurfD &S, float samplingRate, Ray ray,
+                       PCG &rs, V3 weight, float quality, TraceStats *ts) {
+  if (S.opaqueShadows) {
+    HitRec h;
+    return traceScene<true, STATS>(sc, ray, h, ts) ? splat(0.f) : splat(1.f);
+  }
+  V3 alpha = splat(1.f);
+  const float orgTMax = ray.tfar;
+  for (int g = 0; g < 1024; g++) {
+    HitRec h;
+    const bool hit = traceScene<false, STATS>(sc, ray, h, ts);
+    if (S.hasVolume) {
+      Ray vr = ray;
+      vr.tfar = hit ? h.t : ray.tfar;
+      if (volumeOverlaps(vol, vr)) {
+        const float jitter = rs.getFloat();
+        alpha = alpha * (1.f - volumeAlpha(vol, vr, jitter, samplingRate * quality));
+      }
+    }
+    if (!hit) break;
+    const DG dg = postIntersect(sc, ray, h);
+    alpha = alpha * svEvalMaterial(S, dg.entry, sc).transmission;
+    ray.tnear = h.t + dg.epsilon;
+    ray.tfar = orgTMax;
+    if (luminance(alpha * weight) < S.minContribution) {
+      alpha = splat(0.f);
+      break;
+    }
+  }
+  return alpha;
+}
+
+template <bool STATS>
+B200_D V3 svComputeAO(const SamplerTables *T, const Scene &sc, const VolumeD &vol, const ScivisSurfD &S,
+                      float samplingRate, const DG &dg, int px, int py, uint32_t sampleZ, PCG &rs, TraceStats *ts) {
+  const uint32_t accumID = sampleZ * uint32_t(S.aoSamples);
+  const AOBasis B = aoBasis(dg, px, py);
+  V3 hits = splat(0.f);
+  for (int i = 0; i < S.aoSamples; i++) {
+    const V3 dir = aoDirection(T, B, dg.Ns, accumID + uint32_t(i));
+    if (dot(dir, dg.Ns) < 0.01f) {
+      hits = hits + splat(1.f);
+      continue;
+    }
+    Ray r;
+    r.org = dg.P;
+    r.tnear = dg.epsilon;
+    r.dir = dir;
+    r.tfar = S.aoRadius;
+    hits = hits + (splat(1.f) - svLightAlpha<STATS>(sc, vol, S, samplingRate, r, rs, splat(1.f), 0.1f, ts));
+  }
+  return splat(1.f) - hits * (1.f / float(S.aoSamples));
+}
+
+template <bool STATS>
+__global__ void __launch_bounds__(128) k_render_scivis_surfaces(const SamplerTables *T, Scene sc, VolumeD vol,
+                                                                CameraD cam, PixelFilterD pf, ScivisParamsD p,
+                                                                ScivisSurfD S, FrameD fb) {
+  const int x = blockIdx.x * 16 + (threadIdx.x & 15);
+  const int y = blockIdx.y * 8 + (threadIdx.x >> 4);
+  TraceStats ts = {0, 0, 0, 0};
+  if (x < fb.W && y < fb.H) {
+    const float rcpW = fdiv(1.f, float(fb.W)), rcpH = fdiv(1.f, float(fb.H));
+    const uint32_t start = uint32_t(fb.frameID * p.spp + 1);
+    const V3 aoColorPi = S.aoColor * 3.14159265358979323846f;
+    PixelOut acc = {0.f, 0.f, 0.f, 0.f, INFINITY, INVALID_ID, INVALID_ID, INVALID_ID};
+    for (int s = 0; s < p.spp; s++) {
+      const uint32_t sid = start + uint32_t(s);
+      Ray ray = primaryRay(T, cam, pf, x, y, rcpW, rcpH, sid);
+      PCG rs;
+      rs.init(uint32_t(x + fb.W * y), sid);
+      bool firstHit = true, allTrans = true;
+      const float originalTFar = ray.tfar;
+      V3 outColor = splat(0.f), outT = splat(1.f);
+      float z = INFINITY;
+      uint32_t prim = INVALID_ID, geom = INVALID_ID, inst = INVALID_ID;
+      uint32_t vsamples = 0;
+      for (int g = 0; g < 1024; g++) {
+        HitRec h;
+        const bool hit = traceScene<false, STATS>(sc, ray, h, &ts);
+        const float rayT = hit ? h.t : ray.tfar;
+        if (S.hasVolume) {
+          Ray vr = ray;
+          vr.tfar = rayT;
+          if (volumeOverlaps(vol, vr)) {
+            const float jitter = rs.getFloat();
+            const float4 vc = integrate(vol, vr, jitter, p.samplingRate, S.minContribution, vsamples);
+            outColor = outColor + outT * mk(vc.x, vc.y, vc.z);
+            outT = outT * vc.w;
+          }
+        }
+        if (S.visibleLights) {
+          V3 lc = splat(0.f);
+          for (int i = 0; i < S.nlights; i++) {
+            const LightD &L = S.lights[i];
+            if (!L.visible) continue;
+            float lpdf;
+            lc = lc + evalLight(L, ray.org, splat(0.f), ray.dir, ray.tnear, rayT, lpdf);
+          }
+          outColor = outColor + outT * lc;
+        }
+        if (firstHit || allTrans) z = rayT;
+        if (!hit) {
+          outColor = outColor + outT * mk(p.bg[0], p.bg[1], p.bg[2]);
+          outT = outT * (1.f - p.bg[3]);
+          break;
+        }
+        const DG dg = postIntersect(sc, ray, h);
+        // SciVis_computeShading: Blinn-Phong over the non-ambient lights
+        // (area lights sampled at their centre), AO tinted by the ambient lights
+        const SvBSDF bsdf = svEvalMaterial(S, dg.entry, sc);
+        V3 color = splat(0.f);
+        for (int i = S.numVisibleOnly; i < S.nlights; i++) {
+          const LightSampleD ls = sampleLight(S.lights[i], dg.P, dg.Ng, dg.Ns, 0.f, 0.f);
+          if (maxc(ls.weight) > 0.f) {
+            const float cosNL = fdot(ls.dir, dg.Ns);
+            if (cosNL < 0.f) continue;
+            const V3 H = fnormalize(ls.dir - ray.dir);
+            const float cosNH = fdot(H, dg.Ns);
+            const V3 specular = bsdf.specular * powf(cosNH, bsdf.shininess);
+            const V3 diffuse = bsdf.diffuse * cosNL;
+            const V3 contrib = (diffuse + specular) * ls.weight;
+            if (S.shadows) {
+              if (luminance(contrib) > S.minContribution) {
+                V3 P = dg.P;
+                if (fdot(dg.Ng, ls.dir) < 0.f) P = P - (2.f * dg.epsilon) * dg.Ng;
+                Ray sr;
+                sr.org = P;
+                sr.tnear = 0.f;
+                sr.dir = ls.dir;
+                sr.tfar = ls.dist;
+                const V3 la = svLightAlpha<STATS>(sc, vol, S, p.samplingRate, sr, rs, contrib, 0.25f, &ts);
+                color = color + la * contrib;
+              }
+            } else {
+              color = color + contrib;
+            }
+          }
+        }
+        V3 ao = splat(1.f);
+        if (S.aoSamples > 0 && luminance(aoColorPi) > S.minContribution)
+          ao = svComputeAO<STATS>(T, sc, vol, S, p.samplingRate, dg, x, y, sid, rs, &ts);
+        color = color + bsdf.diffuse * ao * aoColorPi;
+        if (firstHit || allTrans) {
+          prim = h.primID;
+          geom = h.geomID;
+          inst = h.instID;
+          firstHit = false;
+        }
+        allTrans = allTrans && bsdf.opacity < S.minContribution;
+        outColor = outColor + outT * color;
+        outT = outT * bsdf.transmission;
+        if (luminance(outT) < S.minContribution) {
+          outT = splat(0.f);
+          break;
+        }
+        ray.tnear = h.t + dg.epsilon;
+        ray.tfar = originalTFar;
+      }
+      acc.r += outColor.x;
+      acc.g += outColor.y;
+      acc.b += outColor.z;
+      acc.a += 1.f - luminance(outT);
+      if (fabsf(z) < fabsf(acc.z)) {
+        acc.z = z;
+        acc.primID = prim;
+        acc.geomID = geom;
+        acc.instID = inst;
+      }
+    }
+    const float rspp = 1.f / float(p.spp);
+    acc.r *= rspp;
+    acc.g *= rspp;
+    acc.b *= rspp;
+    acc.a *= rspp;
+    fbAccumulate(fb, x, y, acc);
+  }
+  if (STATS) flushStats(sc, ts);
+}
+
+}  // namespace
+
+cudaError_t launchRenderScivisSurfaces(const SamplerTables *T, const Scene &sc, const VolumeD &vol, const CameraD &cam,
+                                       const PixelFilterD &pf, const ScivisParamsD &p, const ScivisSurfD &S,
+                                       const FrameD &fb, bool stats, cudaStream_t st, KernelTimer *kt) {
+  dim3 grid((fb.W + 15) / 16, (fb.H + 7) / 8);
+  KernelScope ks(kt, KK_SCIVIS, st);
+  if (stats)
+    k_render_scivis_surfaces<true><<<grid, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(T, sc, vol, cam, pf, p, S, fb);
+  else
+    k_render_scivis_surfaces<false><<<grid, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(T, sc, vol, cam, pf, p, S, fb);
+  return cudaGetLastError();
+}
+
+}  // namespace b200

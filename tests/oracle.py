@@ -143,6 +143,8 @@ def lib():
         L.or_volume_sample_count.restype = ctypes.c_uint64
         L.or_volume_sample_count.argtypes = [I]
         L.or_render_scivis_volume.argtypes = [P, ctypes.POINTER(OrCamera), I, I, I, I, F, P, I, I, I, P, I]
+        L.or_render_scivis.argtypes = [P, P, ctypes.POINTER(OrCamera), ctypes.POINTER(OrScivisParams), P, I, P, I,
+                                       I, I, I, I, I, P, P, P, I]
         L.or_scene_commit.argtypes = [P]
         L.or_trace.argtypes = [P, P, I, I, P, P, I]
         L.or_camera_rays.argtypes = [ctypes.POINTER(OrCamera), I, I, I, I, I, P]
@@ -255,3 +257,58 @@ def render_scivis_volume(model, cam, pixel_filter, w, h, spp=1, sampling_rate=1.
     lib().or_render_scivis_volume(model.h, ctypes.byref(cam), pixel_filter, w, h, spp, sampling_rate, _p(bgv),
                                   frames, y0, y1, _p(color), nthreads)
     return color
+
+
+class OrScivisLight(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int), ("visible", ctypes.c_int), ("pos", ctypes.c_float * 3),
+                ("e1", ctypes.c_float * 3), ("e2", ctypes.c_float * 3), ("radiance", ctypes.c_float * 3)]
+
+
+class OrScivisMaterial(ctypes.Structure):
+    _fields_ = [("isObj", ctypes.c_int), ("kd", ctypes.c_float * 3), ("ks", ctypes.c_float * 3),
+                ("ns", ctypes.c_float), ("d", ctypes.c_float), ("tf", ctypes.c_float * 3)]
+
+
+class OrScivisParams(ctypes.Structure):
+    _fields_ = [("spp", ctypes.c_int), ("samplingRate", ctypes.c_float), ("bg", ctypes.c_float * 4),
+                ("shadows", ctypes.c_int), ("visibleLights", ctypes.c_int), ("aoSamples", ctypes.c_int),
+                ("aoRadius", ctypes.c_float), ("minContribution", ctypes.c_float), ("pixelFilter", ctypes.c_int)]
+
+
+def render_scivis(scene, volume, cam, lights, materials, w, h, spp=1, pixel_filter=2, sampling_rate=1.0,
+                  bg=(0, 0, 0, 0), shadows=False, visible_lights=False, ao_samples=0, ao_radius=1e20,
+                  min_contribution=0.001, frames=1, rows=None, nthreads=0):
+    """SciVis over a world with surfaces (and optionally `volume`, a
+    VolumeModel).  lights: dicts as PtWorld takes them (+ "visible");
+    materials: dicts {"kd", "ks", "ns", "d", "tf"} for obj materials or None.
+    Returns color (h,w,4), depth (h,w), ids (3,h,w)."""
+    L = (OrScivisLight * max(1, len(lights)))()
+    for i, l in enumerate(lights):
+        rad = np.asarray(l.get("color", (1, 1, 1)), np.float32) * np.float32(l["intensity"])
+        L[i].kind = 0 if l["type"] == "quad" else 1
+        L[i].visible = int(l.get("visible", True))
+        L[i].radiance[:] = [float(x) for x in rad]
+        if l["type"] == "quad":
+            L[i].pos[:], L[i].e1[:], L[i].e2[:] = ([float(x) for x in l[k]] for k in ("position", "edge1", "edge2"))
+    M = (OrScivisMaterial * max(1, len(materials)))()
+    for i, m in enumerate(materials):
+        if m is None:
+            continue
+        M[i].isObj = 1
+        M[i].kd[:] = [float(x) for x in m.get("kd", (0.8, 0.8, 0.8))]
+        M[i].ks[:] = [float(x) for x in m.get("ks", (0, 0, 0))]
+        M[i].ns, M[i].d = float(m.get("ns", 10.0)), float(m.get("d", 1.0))
+        M[i].tf[:] = [float(x) for x in m.get("tf", (0, 0, 0))]
+    p = OrScivisParams()
+    p.spp, p.samplingRate = int(spp), float(sampling_rate)
+    p.bg[:] = [float(x) for x in bg]
+    p.shadows, p.visibleLights, p.aoSamples = int(bool(shadows)), int(bool(visible_lights)), int(ao_samples)
+    p.aoRadius, p.minContribution, p.pixelFilter = float(ao_radius), float(min_contribution), int(pixel_filter)
+    color = np.zeros((h, w, 4), np.float32)
+    depth = np.zeros((h, w), np.float32)
+    ids = np.zeros((3, h, w), np.uint32)
+    y0, y1 = rows if rows else (0, 0)
+    lib().or_render_scivis(scene.h, volume.h if volume is not None else None, ctypes.byref(cam), ctypes.byref(p), L,
+                           len(lights), M, len(materials), w, h, frames, y0, y1, _p(color), _p(depth), _p(ids),
+                           nthreads)
+    return dict(color=color, depth=depth, primID=ids[0], geomID=ids[1], instID=ids[2])

@@ -1,0 +1,111 @@
+"""SciVis over worlds with surfaces: b200_render_scivis against the oracle's
+restatement of SciVis_renderSample (render/scivis/SciVis.ispc:24-222) with
+SciVis_computeShading / directIllumination (render/scivis/surfaces.ispc),
+evalMaterial (render/scivis/surfaces.ih:44-84), lightAlpha
+(render/scivis/lightAlpha.ispc) and SciVis_computeAO, on a seeded height
+field with spheres, OBJ materials (one translucent), a quad and an ambient
+light, and optionally a volume over the surfaces.
+
+Both sides trace the same rays with the same watertight/sphere tests (IDs and
+depth bit-exact) and draw the same random numbers; they differ only in float
+contraction and transcendental rounding of the shading, so colours agree to
+1e-3 relative on nearly every pixel."""
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+W, H = 96, 80
+CAM = dict(position=(0.5, 0.9, -0.35), direction=(0.0, -0.6, 0.8), up=(0.0, 1.0, 0.0), fovy=60.0, aspect=W / H)
+LIGHTS = [dict(type="quad", position=(0.2, 0.9, 0.2), edge1=(0.4, 0.0, 0.0), edge2=(0.0, 0.0, 0.4), intensity=4.0,
+               visible=True),
+          dict(type="ambient", intensity=0.35, color=(0.9, 0.95, 1.0), visible=True)]
+MATS = [dict(kd=(0.7, 0.6, 0.5), ks=(0.25, 0.25, 0.25), ns=24.0),
+        dict(kd=(0.2, 0.4, 0.8), ks=(0.1, 0.1, 0.1), ns=8.0, d=0.55, tf=(0.3, 0.3, 0.1))]
+
+
+@pytest.fixture(scope="module")
+def world(b200_device):
+    import ospray_gb300 as og
+    from ospray_gb300 import scenes
+    d = scenes.ao_heightfield_scene(n=64, nspheres=150)
+    v = scenes.volume_scene(n=24)
+    out = {}
+    for with_volume in (False, True):
+        g = og.Scene(b200_device)
+        o = oracle.Scene()
+        for s in (g, o):
+            gm = s.add_mesh(d["vertex"], d["index"])
+            gs = s.add_spheres(d["spheres"])
+            s.add_instance(gm, 0, 0, material=0)
+            s.add_instance(gs, 0, 1, material=1)
+            s.commit()
+        g.set_lights([og.quad_light(L["position"], L["edge1"], L["edge2"], L["intensity"], visible=L["visible"])
+                      if L["type"] == "quad" else og.ambient_light(L["intensity"], L["color"], visible=L["visible"])
+                      for L in LIGHTS])
+        ov = None
+        if with_volume:
+            g.set_volume(v["volume"], v["origin"], v["spacing"], v["color"], v["opacity"], v["value_range"])
+            ov = oracle.VolumeModel(v["volume"], v["origin"], v["spacing"], v["color"], v["opacity"],
+                                    v["value_range"])
+        out[with_volume] = (g, o, ov)
+    return out
+
+
+def render_both(world, b200_device, with_volume=False, spp=2, frames=1, **kw):
+    import ospray_gb300 as og
+    g, o, ov = world[with_volume]
+    fb = og.Frame(b200_device, W, H, og.FB_COLOR | og.FB_DEPTH | og.FB_ID_PRIMITIVE | og.FB_ID_OBJECT | og.FB_ACCUM)
+    cam = og.camera_desc(CAM["position"], CAM["direction"], CAM["up"], fovy=CAM["fovy"], aspect=CAM["aspect"])
+    params = og.scivis_params(spp=spp, shadows=kw.get("shadows", False), visible_lights=kw.get("visible_lights", False),
+                              ao_samples=kw.get("ao_samples", 0), bg=kw.get("bg", (0, 0, 0, 0)))
+    for _ in range(frames):
+        og.render_scivis(g, cam, params, fb, og.scivis_materials_array(MATS))
+    gpu = dict(color=fb.read(og.FB_COLOR), depth=fb.read(og.FB_DEPTH), primID=fb.read(og.FB_ID_PRIMITIVE))
+    ocam = oracle.camera(CAM["position"], CAM["direction"], CAM["up"], fovy=CAM["fovy"], aspect=CAM["aspect"])
+    ref = oracle.render_scivis(o, ov, ocam, LIGHTS, MATS, W, H, spp=spp, frames=frames,
+                               shadows=kw.get("shadows", False), visible_lights=kw.get("visible_lights", False),
+                               ao_samples=kw.get("ao_samples", 0), bg=kw.get("bg", (0, 0, 0, 0)))
+    return gpu, ref
+
+
+def assert_close(gpu, ref, frac=0.995):
+    hit = ref["primID"] != 0xFFFFFFFF
+    assert hit.mean() > 0.3, hit.mean()  # the surfaces fill the view
+    assert (gpu["primID"] == ref["primID"]).mean() >= 0.999
+    same_depth = gpu["depth"].view(np.uint32) == ref["depth"].view(np.uint32)
+    assert same_depth.mean() >= 0.999
+    c, r = gpu["color"], ref["color"]
+    assert np.isfinite(c).all()
+    close = np.all(np.abs(c - r) <= 1e-3 * np.maximum(1.0, np.abs(r)) + 1e-5, axis=2)
+    assert close.mean() >= frac, close.mean()
+    assert np.abs(c.mean(axis=(0, 1)) - r.mean(axis=(0, 1))).max() < 1e-4
+
+
+@pytest.mark.parametrize("shadows,ao", [(False, 0), (True, 0), (True, 2)])
+def test_scivis_surfaces_match_oracle(world, b200_device, shadows, ao):
+    gpu, ref = render_both(world, b200_device, shadows=shadows, ao_samples=ao)
+    assert ref["color"][..., :3].max() > 0.05  # lit
+    assert_close(gpu, ref)
+
+
+def test_scivis_shadows_and_ao_darken(world, b200_device):
+    """Shadows and AO only remove light: the lit image without them is
+    brighter pixel by pixel (both renders on the GPU, same samples)."""
+    plain, _ = render_both(world, b200_device, shadows=False, ao_samples=0)
+    shaded, _ = render_both(world, b200_device, shadows=True, ao_samples=2)
+    p, s = plain["color"][..., :3], shaded["color"][..., :3]
+    assert (s <= p + 1e-5).mean() >= 0.999
+    assert s.mean() < p.mean()
+
+
+def test_scivis_surfaces_with_volume(world, b200_device):
+    gpu, ref = render_both(world, b200_device, with_volume=True, shadows=True, ao_samples=1, bg=(0.1, 0.1, 0.2, 1.0))
+    assert_close(gpu, ref, frac=0.99)
+
+
+def test_scivis_visible_lights_and_accumulation(world, b200_device):
+    gpu, ref = render_both(world, b200_device, spp=1, frames=3, visible_lights=True, shadows=True)
+    assert_close(gpu, ref)
