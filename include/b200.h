@@ -268,6 +268,17 @@ int b200_scene_set_volume(b200_scene scene, const float *data, int nx, int ny, i
                           const float *spacing, const float *color, int ncolor, const float *opacity, int nopacity,
                           const float *valueRange, float densityScale);
 
+/* Gradient shading of the volume (VolumetricModel::commit
+ * volume/VolumetricModel.cpp:76 "gradientShadingScale", used by
+ * integrateVolumeIntervalsGradient render/scivis/volumes.ispc:384-414):
+ * 0 (the default) renders the transfer function's colour; s > 0 shades each sample of non-zero opacity like a surface (Blinn-Phong over the
+ * lights, shadows and AO as the SciVis parameters ask) with normal
+ * -normalize(gradient) and blends the shaded RGBA into it by s.  The gradient
+ * is the finite difference of the trilinear sample at one grid spacing
+ * (forward; backward at the upper boundary).  Values <= 0 turn it off; a
+ * non-finite value is refused.  Kept across b200_scene_set_volume calls. */
+int b200_scene_set_volume_gradient_shading(b200_scene scene, float gradientShadingScale);
+
 /* ---- SciVis renderer (SciVis::commit render/scivis/SciVis.cpp:27-84,
  *      SciVis_renderSample render/scivis/SciVis.ispc:24-222,
  *      SciVis_computeShading render/scivis/surfaces.ispc:90-128,
@@ -278,8 +289,8 @@ int b200_scene_set_volume(b200_scene scene, const float *data, int nx, int ny, i
  * (`aoSamples` rays up to `aoDistance`) tinted by the summed ambient
  * radiance x pi, lights seen directly when `visibleLights` is set, and the
  * volume (if any) composited in front of each surface.  Volume-only worlds
- * take a dedicated kernel.  Gradient shading of volumes is off (the
- * volumetric model's default gradientShadingScale 0). */
+ * take a dedicated kernel unless the volume is gradient shaded
+ * (b200_scene_set_volume_gradient_shading). */
 typedef struct {
   int pixelSamples;
   float volumeSamplingRate; /* default 1 */

@@ -2,7 +2,9 @@
 // structured-regular volume through a piecewise-linear transfer function.
 //   SciVis_renderSample              render/scivis/SciVis.ispc:24-222
 //   integrateVolumeIntervalsGradient render/scivis/volumes.ispc:302-439
-//     (the single-volume variant; gradient shading off, its default)
+//     (the single-volume variant, with gradient shading: SciVis_computeShading
+//     of each sample with Ns = -normalize(gradient), blended by
+//     gradientShadingScale)
 //   LinearTransferFunction_get       volume/transferFunction/LinearTransferFunction.ispc:11-43
 //   value ranges / max opacity       volume/transferFunction/LinearTransferFunction.cpp:40-155
 // Volume sampling and interval iteration are Open VKL 2.0.1 (not vendored).
@@ -69,6 +71,28 @@ struct Volume {
     const float c11 = lerpf(fx, at(i, j + 1, k + 1), at(i + 1, j + 1, k + 1));
     return lerpf(fz, lerpf(fy, c00, c10), lerpf(fy, c01, c11));
   }
+  // Volume_getGradient (volume/Volume.ih:26-56) over Open VKL's gradient,
+  // restated as finite differences of the trilinear sample at one grid
+  // spacing: forward, or backward where the forward point leaves the grid;
+  // a NaN component becomes 1 (as Volume_getGradient does).
+  V3 gradient(V3 p, float s0) const {
+    const float h[3] = {spacing.x, spacing.y, spacing.z};
+    float g[3];
+    for (int a = 0; a < 3; a++) {
+      V3 q = p;
+      (a == 0 ? q.x : a == 1 ? q.y : q.z) += h[a];
+      const float f = sample(q);
+      if (!std::isnan(f)) {
+        g[a] = (f - s0) / h[a];
+      } else {
+        V3 r = p;
+        (a == 0 ? r.x : a == 1 ? r.y : r.z) -= h[a];
+        g[a] = (s0 - sample(r)) / h[a];
+      }
+      if (std::isnan(g[a])) g[a] = 1.f;
+    }
+    return {g[0], g[1], g[2]};
+  }
 };
 
 struct TransferFunction {
@@ -103,6 +127,7 @@ struct VolumeModel {
   Volume vol;
   TransferFunction tf;
   float densityScale = 1.f;
+  float gradientShadingScale = 0.f;  // VolumetricModel::commit volume/VolumetricModel.cpp:76
   void finalize() {
     vol.buildCells();
     vol.cellEmpty.resize(vol.cmin.size());
@@ -249,7 +274,8 @@ V4 integrateVolume(const VolumeModel &m, const Ray &ray, float jitter, float sam
 //   lightAlpha                 render/scivis/lightAlpha.ispc:19-122
 //   integrateVolumeIntervals   render/ao/volumes.ispc:32-240 (shadow/AO rays)
 //   light list and aoColorPi   render/scivis/SciVisData.cpp:15-105
-// Surfaces carry no per-vertex colour here, so dg.color = (1, 1, 1, 1).
+// Surfaces carry no per-vertex colour here, so dg.color = (1, 1, 1, 1);
+// gradient-shaded volume samples pass their transfer-function colour.
 
 struct SvMaterial {
   int isObj;
@@ -265,15 +291,15 @@ struct SvBSDF {
   float opacity;
 };
 
-SvBSDF svEvalMaterial(const SvMaterial *m) {
+SvBSDF svEvalMaterial(const SvMaterial *m, V4 color = {1.f, 1.f, 1.f, 1.f}) {
   SvBSDF r;
-  r.diffuse = v3(1.f);
+  r.diffuse = v3(color.x, color.y, color.z);
   r.specular = v3(0.f);
   r.shininess = 10.f;
-  r.transmission = v3(0.f);
-  r.opacity = 1.f;
+  r.transmission = v3(1.f - color.w);
+  r.opacity = color.w;
   if (m && m->isObj) {
-    const float d = m->d;
+    const float d = m->d * color.w;
     r.diffuse = r.diffuse * m->kd;
     r.diffuse = r.diffuse * d;
     r.specular = d * m->ks;
@@ -388,7 +414,7 @@ V3 svLightAlpha(const SvWorld &w, const SvParams &p, Ray ray, RandomSampler &rs,
   for (int g = 0; g < 1024; g++) {
     Hit hit;
     tl_rays++;
-    const bool h = w.scene->intersect(ray, hit);
+    const bool h = w.scene && w.scene->intersect(ray, hit);
     if (w.vm) {
       Ray vr = ray;
       vr.tfar = h ? hit.t : ray.tfar;
@@ -439,9 +465,9 @@ struct SvShading {
   float opacity;
 };
 
-SvShading svComputeShading(const SvWorld &w, const SvParams &p, const DG &dg, const SvMaterial *mat, V3 inDir,
-                           int px, int py, uint32_t sampleZ, RandomSampler &rs) {
-  const SvBSDF bsdf = svEvalMaterial(mat);
+SvShading svComputeShading(const SvWorld &w, const SvParams &p, const DG &dg, const SvMaterial *mat, V4 dgColor,
+                           V3 inDir, int px, int py, uint32_t sampleZ, RandomSampler &rs) {
+  const SvBSDF bsdf = svEvalMaterial(mat, dgColor);
   V3 color = v3(0.f);
   for (size_t i = w.numVisibleOnly; i < w.lights.size(); i++) {
     const LightSample ls = w.lights[i].sample(dg, {0.f, 0.f});  // area lights at their centre
@@ -472,6 +498,67 @@ SvShading svComputeShading(const SvWorld &w, const SvParams &p, const DG &dg, co
   return {color, bsdf.transmission, bsdf.opacity};
 }
 
+// integrateVolumeIntervalsGradient (render/scivis/volumes.ispc:302-439) with
+// gradient shading: a sample of non-zero opacity whose gradient is not
+// vanishing is shaded like a surface with no material, colour = its
+// transfer-function RGBA, Ns = Ng = -normalize(gradient), epsilon = dt / 2,
+// and blended into the sample by gradientShadingScale before the Beer-law
+// opacity.  Shadow and AO rays of the shading draw from the ray's sampler.
+V4 integrateVolumeShaded(const SvWorld &w, const SvParams &p, const Ray &ray, float jitter, int px, int py,
+                         uint32_t sid, RandomSampler &rs, uint64_t &samples) {
+  const VolumeModel &m = *w.vm;
+  IntervalIter it;
+  it.init(m.vol, ray.org, ray.dir, ray.tnear, ray.tfar);
+  const float nominalDeltaT = std::fmin(m.vol.spacing.x, std::fmin(m.vol.spacing.y, m.vol.spacing.z));
+  V3 color = v3(0.f);
+  float T = 1.f;
+  float distance = INFINITY, iuDistance = jitter, iuLength = 0.f, step = 0.f;
+  float ilo = 0.f, ihi = INFINITY;
+  for (int g = 0; g < (1 << 24) && T > p.minContribution; g++) {
+    float emptySpace = 0.f;
+    while (iuDistance > iuLength) {
+      const float prevUpper = ihi;
+      if (it.next(ilo, ihi)) {
+        emptySpace += std::fmax(ilo - prevUpper, 0.f);
+        iuDistance -= iuLength;
+        step = nominalDeltaT / p.samplingRate;
+        iuLength = (ihi - ilo) / step;
+        distance = distance == INFINITY ? ilo : distance;
+      } else {
+        return {color.x, color.y, color.z, T};
+      }
+    }
+    const float newDistance = ilo + iuDistance * step;
+    const V3 pos = ray.org + newDistance * ray.dir;
+    const float v = m.vol.sample(pos);
+    samples++;
+    if (!std::isnan(v)) {
+      V4 c = m.tf.get(v);
+      const float dt = newDistance - distance - emptySpace;
+      if (c.w > 0.f) {
+        const V3 grad = m.vol.gradient(pos, v);
+        if (dot(grad, grad) > 1e-6f) {
+          DG dg;
+          dg.epsilon = dt / 2.f;
+          dg.Ns = dg.Ng = normalize(-grad);
+          dg.P = pos;
+          dg.primID = dg.geomID = dg.instID = 0xFFFFFFFFu;
+          const SvShading sh = svComputeShading(w, p, dg, nullptr, c, ray.dir, px, py, sid, rs);
+          const float a = 1.f - svLuminance(sh.transmission), f = m.gradientShadingScale;
+          c = {lerpf(f, c.x, sh.shadedColor.x), lerpf(f, c.y, sh.shadedColor.y), lerpf(f, c.z, sh.shadedColor.z),
+               lerpf(f, c.w, a)};
+        }
+      }
+      c.w = std::exp(-c.w * dt * m.densityScale);
+      color = color + (T * (1.f - c.w)) * v3(c.x, c.y, c.z);
+      T *= c.w;
+    }
+    iuDistance += 1.f;
+    distance = newDistance;
+  }
+  return {color.x, color.y, color.z, T};
+}
+
 ScreenSample svRenderSample(const SvWorld &w, const SvParams &p, Ray ray, int x, int y, int W, uint32_t sid,
                             uint64_t &samples) {
   RandomSampler rs;
@@ -483,14 +570,16 @@ ScreenSample svRenderSample(const SvWorld &w, const SvParams &p, Ray ray, int x,
   for (int g = 0; g < 1024; g++) {
     Hit hit;
     tl_rays++;
-    const bool h = w.scene->intersect(ray, hit);
+    const bool h = w.scene && w.scene->intersect(ray, hit);
     const float rayT = h ? hit.t : ray.tfar;
     if (w.vm) {
       Ray vr = ray;
       vr.tfar = rayT;
       if (svVolumeOverlaps(w.vm->vol, vr)) {
         const float jitter = rs.getFloat();
-        const V4 vc = integrateVolume(*w.vm, vr, jitter, p.samplingRate, p.minContribution, samples);
+        const V4 vc = w.vm->gradientShadingScale > 0.f
+                          ? integrateVolumeShaded(w, p, vr, jitter, x, y, sid, rs, samples)
+                          : integrateVolume(*w.vm, vr, jitter, p.samplingRate, p.minContribution, samples);
         outColor = outColor + outT * v3(vc.x, vc.y, vc.z);
         outT = outT * vc.w;
       }
@@ -506,7 +595,7 @@ ScreenSample svRenderSample(const SvWorld &w, const SvParams &p, Ray ray, int x,
     if (firstHit || allTrans) smp.z = rayT;
     if (h) {
       const DG dg = postIntersect(*w.scene, ray, hit);
-      const SvShading sh = svComputeShading(w, p, dg, w.material(hit), ray.dir, x, y, sid, rs);
+      const SvShading sh = svComputeShading(w, p, dg, w.material(hit), {1.f, 1.f, 1.f, 1.f}, ray.dir, x, y, sid, rs);
       if (firstHit || allTrans) {
         smp.primID = dg.primID;
         smp.geomID = dg.geomID;
@@ -561,6 +650,8 @@ void *or_volume_new(const float *data, int nx, int ny, int nz, const float *orig
 }
 
 void or_volume_free(void *m) { delete static_cast<VolumeModel *>(m); }
+
+void or_volume_set_gradient_shading(void *m, float scale) { static_cast<VolumeModel *>(m)->gradientShadingScale = scale; }
 
 uint64_t or_volume_sample_count(int reset) {
   const uint64_t n = g_volSamples.load();

@@ -231,6 +231,7 @@ def lib():
             "b200_render_ao": (I, [P, ctypes.POINTER(CameraDesc), ctypes.POINTER(AOParams), P, P]),
             "b200_scene_set_lights": (I, [P, P, I]),
             "b200_scene_set_volume": (I, [P, P, I, I, I, P, P, P, I, P, I, P, F]),
+            "b200_scene_set_volume_gradient_shading": (I, [P, F]),
             "b200_render_scivis": (I, [P, ctypes.POINTER(CameraDesc), ctypes.POINTER(ScivisParams), P, I, P, P]),
             "b200_render_pt": (I, [P, ctypes.POINTER(CameraDesc), ctypes.POINTER(PTParams), P, I, P, P]),
         }
@@ -356,6 +357,10 @@ class Scene:
         vr = np.asarray(value_range, np.float32)
         self.device._check(lib().b200_scene_set_volume(self._h, _ptr(d), nx, ny, nz, _ptr(o), _ptr(sp), _ptr(c),
                                                        len(c), _ptr(op), len(op), _ptr(vr), float(density_scale)))
+
+    def set_volume_gradient_shading(self, scale):
+        """The volumetric model's gradientShadingScale (0: off)."""
+        self.device._check(lib().b200_scene_set_volume_gradient_shading(self._h, float(scale)))
 
     def set_lights(self, lights):
         arr = (Light * max(1, len(lights)))(*lights)

@@ -925,6 +925,7 @@ int b200_scene_set_volume(b200_scene s, const float *data, int nx, int ny, int n
     v.vlo = valueRange[0];
     v.vhi = valueRange[1];
     v.densityScale = densityScale;
+    v.gradientShadingScale = sc->gradientShadingScale;
     check(brickVolume(v, linear, sc->dVolData, st), "brick volume");
     check(cudaStreamSynchronize(st), "brick volume");
     check(cudaMalloc(&sc->dCellEmpty, size_t(v.cx) * v.cy * v.cz), "alloc macrocells");
@@ -932,6 +933,16 @@ int b200_scene_set_volume(b200_scene s, const float *data, int nx, int ny, int n
     v.cellEmpty = sc->dCellEmpty;
     check(cudaStreamSynchronize(st), "volume commit");
     sc->hasVolume = true;
+  });
+}
+
+int b200_scene_set_volume_gradient_shading(b200_scene s, float gradientShadingScale) {
+  if (!s) return B200_INVALID_ARGUMENT;
+  SceneObj *sc = reinterpret_cast<SceneObj *>(s);
+  return guarded(sc->dev, [&]() {
+    require(std::isfinite(gradientShadingScale), "gradientShadingScale is not finite");
+    sc->gradientShadingScale = gradientShadingScale;
+    sc->vol.gradientShadingScale = gradientShadingScale;
   });
 }
 
@@ -952,7 +963,7 @@ int b200_render_scivis(b200_scene s, const b200_camera_desc *camera, const b200_
     d.samplingRate = p->volumeSamplingRate;
     for (int k = 0; k < 4; k++) d.bg[k] = p->backgroundColor[k];
     cudaStream_t st = stream ? (cudaStream_t)stream : sc->dev->stream;
-    if (!surfaces) {
+    if (!surfaces && !(sc->vol.gradientShadingScale > 0.f)) {
       check(launchRenderScivisVolume(sc->dev->tables, sc->view(), sc->vol, makeCamera(*camera),
                                      sc->dev->filter(p->pixelFilter), d, fb->view(), p->collectStats != 0, st,
                                      sc->dev->timer),
@@ -1004,6 +1015,7 @@ int b200_render_scivis(b200_scene s, const b200_camera_desc *camera, const b200_
       S.aoRadius = p->aoDistance;
       S.minContribution = p->minContribution;
       S.hasVolume = sc->hasVolume;
+      S.hasSurfaces = surfaces;
       S.opaqueShadows = opaque && !sc->hasVolume;
       check(launchRenderScivisSurfaces(sc->dev->tables, sc->view(), sc->vol, makeCamera(*camera),
                                        sc->dev->filter(p->pixelFilter), d, S, fb->view(), p->collectStats != 0, st,

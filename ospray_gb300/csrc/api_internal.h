@@ -95,6 +95,7 @@ struct SceneObj {
   // one structured-regular volumetric model (device copies)
   bool hasVolume = false;
   VolumeD vol = {};
+  float gradientShadingScale = 0.f;  // kept across b200_scene_set_volume calls
   float *dVolData = nullptr, *dTfOpacity = nullptr;
   float3 *dTfColor = nullptr;
   uint8_t *dCellEmpty = nullptr;

@@ -110,6 +110,7 @@ struct VolumeD {
   const float *tfOpacity;
   int ncolor, nopacity;
   float vlo, vhi, densityScale;
+  float gradientShadingScale;  // VolumetricModel "gradientShadingScale" (0: off)
 };
 
 struct ScivisParamsD {
@@ -139,6 +140,7 @@ struct ScivisSurfD {
   int shadows, visibleLights, aoSamples;
   float aoRadius, minContribution;
   int hasVolume;
+  int hasSurfaces;    // 0: a volume-only world (no ray is traced against surfaces)
   int opaqueShadows;  // every material opaque and no volume: shadow and AO rays as any-hit queries
 };
 

@@ -204,8 +204,7 @@ void VolumetricModelObj::commit(B200Device &dev) {
   tf = Ref<TransferFunctionObj>(static_cast<TransferFunctionObj *>(getObject("transferFunction", OSP_TRANSFER_FUNCTION)));
   if (!volume || !tf) throw Error(OSP_INVALID_ARGUMENT, "volumetric model needs 'volume' and 'transferFunction'");
   densityScale = getFloat("densityScale", 1.f);
-  if (getFloat("gradientShadingScale", 0.f) != 0.f)
-    dev.warn("volumetric model: gradient shading is not supported by the b200 device");
+  gradientShadingScale = getFloat("gradientShadingScale", 0.f);
 }
 
 // ---------------------------------------------------------------- hierarchy
@@ -327,6 +326,7 @@ void WorldObj::commit(B200Device &dev) {
         dev.check(b200_scene_set_volume(s, v->voxels.data(), v->dims[0], v->dims[1], v->dims[2], v->origin,
                                         v->spacing, tf->color.data(), int(tf->color.size() / 3), tf->opacity.data(),
                                         int(tf->opacity.size()), tf->range, vm->densityScale));
+        dev.check(b200_scene_set_volume_gradient_shading(s, vm->gradientShadingScale));
         hasVolume = true;
       }
     }

@@ -74,6 +74,7 @@ struct VolumetricModelObj : SceneObj {
   Ref<VolumeObj> volume;
   Ref<TransferFunctionObj> tf;
   float densityScale = 1.f;
+  float gradientShadingScale = 0.f;
   void commit(B200Device &) override;
 };
 

@@ -7,8 +7,12 @@
 //   evalMaterial               render/scivis/surfaces.ih:44-84
 //   lightAlpha                 render/scivis/lightAlpha.ispc:19-122
 //   integrateVolumeIntervals   render/ao/volumes.ispc:32-240 (shadow/AO rays)
+//   integrateVolumeIntervalsGradient render/scivis/volumes.ispc:302-439
+//                              (gradient shading of volume samples)
 // One thread per pixel; surfaces carry no per-vertex colour, so dg.color is
-// (1, 1, 1, 1).  Volume-only worlds use k_render_scivis_volume.
+// (1, 1, 1, 1); a gradient-shaded volume sample passes its transfer-function
+// RGBA.  Volume-only worlds without gradient shading use
+// k_render_scivis_volume.
 #include "kernels.h"
 #include "lights.cuh"
 #include "volume.cuh"
@@ -24,18 +28,20 @@ struct SvBSDF {
   float opacity;
 };
 
-B200_D SvBSDF svEvalMaterial(const ScivisSurfD &S, uint32_t entry, const Scene &sc) {
+// material slot of a surface hit; ~0u (no material) for volume samples
+B200_D uint32_t svMaterialSlot(const Scene &sc, uint32_t entry) { return sc.entries[entry].materialID; }
+
+B200_D SvBSDF svEvalMaterial(const ScivisSurfD &S, uint32_t mi, float4 color) {
   SvBSDF r;
-  r.diffuse = splat(1.f);
+  r.diffuse = mk(color.x, color.y, color.z);
   r.specular = splat(0.f);
   r.shininess = 10.f;
-  r.transmission = splat(0.f);
-  r.opacity = 1.f;
-  const uint32_t mi = sc.entries[entry].materialID;
+  r.transmission = splat(1.f - color.w);
+  r.opacity = color.w;
   if (mi < uint32_t(S.nmats)) {
     const ScivisMatD m = S.mats[mi];
     if (m.isObj) {
-      const float d = m.d;
+      const float d = m.d * color.w;
       r.diffuse = r.diffuse * mk(m.kd[0], m.kd[1], m.kd[2]);
       r.diffuse = r.diffuse * d;
       r.specular = d * mk(m.ks[0], m.ks[1], m.ks[2]);
@@ -64,7 +70,7 @@ B200_D V3 svLightAlpha(const Scene &sc, const VolumeD &vol, const ScivisSurfD &S
   const float orgTMax = ray.tfar;
   for (int g = 0; g < 1024; g++) {
     HitRec h;
-    const bool hit = traceScene<false, STATS>(sc, ray, h, ts);
+    const bool hit = S.hasSurfaces && traceScene<false, STATS>(sc, ray, h, ts);
     if (S.hasVolume) {
       Ray vr = ray;
       vr.tfar = hit ? h.t : ray.tfar;
@@ -75,7 +81,7 @@ B200_D V3 svLightAlpha(const Scene &sc, const VolumeD &vol, const ScivisSurfD &S
     }
     if (!hit) break;
     const DG dg = postIntersect(sc, ray, h);
-    alpha = alpha * svEvalMaterial(S, dg.entry, sc).transmission;
+    alpha = alpha * svEvalMaterial(S, svMaterialSlot(sc, dg.entry), make_float4(1.f, 1.f, 1.f, 1.f)).transmission;
     ray.tnear = h.t + dg.epsilon;
     ray.tfar = orgTMax;
     if (luminance(alpha * weight) < S.minContribution) {
@@ -108,7 +114,108 @@ B200_D V3 svComputeAO(const SamplerTables *T, const Scene &sc, const VolumeD &vo
   return splat(1.f) - hits * (1.f / float(S.aoSamples));
 }
 
+struct SvShading {
+  V3 color, transmission;
+  float opacity;
+};
+
+// SciVis_computeShading (render/scivis/surfaces.ispc:90-128) with
+// directIllumination: Blinn-Phong over the non-ambient lights (area lights
+// sampled at their centre), hard shadows through lightAlpha, AO tinted by the
+// ambient lights x pi.
 template <bool STATS>
+B200_D SvShading svComputeShading(const SamplerTables *T, const Scene &sc, const VolumeD &vol, const ScivisSurfD &S,
+                                  float samplingRate, const DG &dg, uint32_t mi, float4 dgColor, V3 inDir, int x,
+                                  int y, uint32_t sid, PCG &rs, TraceStats *ts) {
+  const SvBSDF bsdf = svEvalMaterial(S, mi, dgColor);
+  V3 color = splat(0.f);
+  for (int i = S.numVisibleOnly; i < S.nlights; i++) {
+    const LightSampleD ls = sampleLight(S.lights[i], dg.P, dg.Ng, dg.Ns, 0.f, 0.f);
+    if (maxc(ls.weight) > 0.f) {
+      const float cosNL = fdot(ls.dir, dg.Ns);
+      if (cosNL < 0.f) continue;
+      const V3 H = fnormalize(ls.dir - inDir);
+      const float cosNH = fdot(H, dg.Ns);
+      const V3 specular = bsdf.specular * powf(cosNH, bsdf.shininess);
+      const V3 diffuse = bsdf.diffuse * cosNL;
+      const V3 contrib = (diffuse + specular) * ls.weight;
+      if (S.shadows) {
+        if (luminance(contrib) > S.minContribution) {
+          V3 P = dg.P;
+          if (fdot(dg.Ng, ls.dir) < 0.f) P = P - (2.f * dg.epsilon) * dg.Ng;
+          Ray sr;
+          sr.org = P;
+          sr.tnear = 0.f;
+          sr.dir = ls.dir;
+          sr.tfar = ls.dist;
+          const V3 la = svLightAlpha<STATS>(sc, vol, S, samplingRate, sr, rs, contrib, 0.25f, ts);
+          color = color + la * contrib;
+        }
+      } else {
+        color = color + contrib;
+      }
+    }
+  }
+  const V3 aoColorPi = S.aoColor * 3.14159265358979323846f;
+  V3 ao = splat(1.f);
+  if (S.aoSamples > 0 && luminance(aoColorPi) > S.minContribution)
+    ao = svComputeAO<STATS>(T, sc, vol, S, samplingRate, dg, x, y, sid, rs, ts);
+  color = color + bsdf.diffuse * ao * aoColorPi;
+  SvShading r;
+  r.color = color;
+  r.transmission = bsdf.transmission;
+  r.opacity = bsdf.opacity;
+  return r;
+}
+
+// integrateVolumeIntervalsGradient (render/scivis/volumes.ispc:302-439) with
+// gradient shading: a sample of non-zero opacity whose gradient does not
+// vanish is shaded like a surface without material (colour = its transfer
+// function RGBA, Ns = Ng = -normalize(gradient), epsilon = dt / 2) and
+// blended into the sample by gradientShadingScale before the Beer-law
+// opacity.  The shading's shadow and AO rays draw from the ray's sampler.
+template <bool STATS>
+B200_D float4 integrateShaded(const SamplerTables *T, const Scene &sc, const VolumeD &vol, const ScivisSurfD &S,
+                              float samplingRate, const Ray &ray, float jitter, int x, int y, uint32_t sid, PCG &rs,
+                              uint32_t &samples, TraceStats *ts) {
+  SampleWalk w;
+  w.init(vol, ray, jitter, samplingRate);
+  V3 color = splat(0.f);
+  float Tr = 1.f;
+  float d, dt;
+  for (int g = 0; g < (1 << 24) && Tr > S.minContribution && w.next(vol, d, dt); g++) {
+    const V3 pos = ray.org + d * ray.dir;
+    const float val = sampleAt(vol, pos);
+    samples++;
+    if (!isnan(val)) {
+      float4 c = tfGet(vol, val);
+      if (c.w > 0.f) {
+        const V3 grad = volumeGradient(vol, pos, val);
+        if (dot(grad, grad) > 1e-6f) {
+          DG dg;
+          dg.P = pos;
+          dg.Ns = dg.Ng = fnormalize(mk(-grad.x, -grad.y, -grad.z));
+          dg.epsilon = dt / 2.f;
+          dg.entry = ~0u;
+          const SvShading sh = svComputeShading<STATS>(T, sc, vol, S, samplingRate, dg, ~0u, c, ray.dir, x, y, sid,
+                                                       rs, ts);
+          const float a = 1.f - luminance(sh.transmission), f = vol.gradientShadingScale;
+          c = make_float4(lerpF(f, c.x, sh.color.x), lerpF(f, c.y, sh.color.y), lerpF(f, c.z, sh.color.z),
+                          lerpF(f, c.w, a));
+        }
+      }
+      c.w = expf(-c.w * dt * vol.densityScale);
+      const float k = Tr * (1.f - c.w);
+      color = color + k * mk(c.x, c.y, c.z);
+      Tr *= c.w;
+    }
+  }
+  return make_float4(color.x, color.y, color.z, Tr);
+}
+
+// SHADED: the volume is gradient shaded (an instantiation of its own, so the
+// common path keeps its registers)
+template <bool STATS, bool SHADED>
 __global__ void __launch_bounds__(128) k_render_scivis_surfaces(const SamplerTables *T, Scene sc, VolumeD vol,
                                                                 CameraD cam, PixelFilterD pf, ScivisParamsD p,
                                                                 ScivisSurfD S, FrameD fb) {
@@ -118,7 +225,6 @@ __global__ void __launch_bounds__(128) k_render_scivis_surfaces(const SamplerTab
   if (x < fb.W && y < fb.H) {
     const float rcpW = fdiv(1.f, float(fb.W)), rcpH = fdiv(1.f, float(fb.H));
     const uint32_t start = uint32_t(fb.frameID * p.spp + 1);
-    const V3 aoColorPi = S.aoColor * 3.14159265358979323846f;
     PixelOut acc = {0.f, 0.f, 0.f, 0.f, INFINITY, INVALID_ID, INVALID_ID, INVALID_ID};
     for (int s = 0; s < p.spp; s++) {
       const uint32_t sid = start + uint32_t(s);
@@ -133,14 +239,17 @@ __global__ void __launch_bounds__(128) k_render_scivis_surfaces(const SamplerTab
       uint32_t vsamples = 0;
       for (int g = 0; g < 1024; g++) {
         HitRec h;
-        const bool hit = traceScene<false, STATS>(sc, ray, h, &ts);
+        const bool hit = S.hasSurfaces && traceScene<false, STATS>(sc, ray, h, &ts);
         const float rayT = hit ? h.t : ray.tfar;
         if (S.hasVolume) {
           Ray vr = ray;
           vr.tfar = rayT;
           if (volumeOverlaps(vol, vr)) {
             const float jitter = rs.getFloat();
-            const float4 vc = integrate(vol, vr, jitter, p.samplingRate, S.minContribution, vsamples);
+            const float4 vc = SHADED
+                                  ? integrateShaded<STATS>(T, sc, vol, S, p.samplingRate, vr, jitter, x, y, sid, rs,
+                                                           vsamples, &ts)
+                                  : integrate(vol, vr, jitter, p.samplingRate, S.minContribution, vsamples);
             outColor = outColor + outT * mk(vc.x, vc.y, vc.z);
             outT = outT * vc.w;
           }
@@ -162,50 +271,17 @@ __global__ void __launch_bounds__(128) k_render_scivis_surfaces(const SamplerTab
           break;
         }
         const DG dg = postIntersect(sc, ray, h);
-        // SciVis_computeShading: Blinn-Phong over the non-ambient lights
-        // (area lights sampled at their centre), AO tinted by the ambient lights
-        const SvBSDF bsdf = svEvalMaterial(S, dg.entry, sc);
-        V3 color = splat(0.f);
-        for (int i = S.numVisibleOnly; i < S.nlights; i++) {
-          const LightSampleD ls = sampleLight(S.lights[i], dg.P, dg.Ng, dg.Ns, 0.f, 0.f);
-          if (maxc(ls.weight) > 0.f) {
-            const float cosNL = fdot(ls.dir, dg.Ns);
-            if (cosNL < 0.f) continue;
-            const V3 H = fnormalize(ls.dir - ray.dir);
-            const float cosNH = fdot(H, dg.Ns);
-            const V3 specular = bsdf.specular * powf(cosNH, bsdf.shininess);
-            const V3 diffuse = bsdf.diffuse * cosNL;
-            const V3 contrib = (diffuse + specular) * ls.weight;
-            if (S.shadows) {
-              if (luminance(contrib) > S.minContribution) {
-                V3 P = dg.P;
-                if (fdot(dg.Ng, ls.dir) < 0.f) P = P - (2.f * dg.epsilon) * dg.Ng;
-                Ray sr;
-                sr.org = P;
-                sr.tnear = 0.f;
-                sr.dir = ls.dir;
-                sr.tfar = ls.dist;
-                const V3 la = svLightAlpha<STATS>(sc, vol, S, p.samplingRate, sr, rs, contrib, 0.25f, &ts);
-                color = color + la * contrib;
-              }
-            } else {
-              color = color + contrib;
-            }
-          }
-        }
-        V3 ao = splat(1.f);
-        if (S.aoSamples > 0 && luminance(aoColorPi) > S.minContribution)
-          ao = svComputeAO<STATS>(T, sc, vol, S, p.samplingRate, dg, x, y, sid, rs, &ts);
-        color = color + bsdf.diffuse * ao * aoColorPi;
+        const SvShading sh = svComputeShading<STATS>(T, sc, vol, S, p.samplingRate, dg, svMaterialSlot(sc, dg.entry),
+                                                     make_float4(1.f, 1.f, 1.f, 1.f), ray.dir, x, y, sid, rs, &ts);
         if (firstHit || allTrans) {
           prim = h.primID;
           geom = h.geomID;
           inst = h.instID;
           firstHit = false;
         }
-        allTrans = allTrans && bsdf.opacity < S.minContribution;
-        outColor = outColor + outT * color;
-        outT = outT * bsdf.transmission;
+        allTrans = allTrans && sh.opacity < S.minContribution;
+        outColor = outColor + outT * sh.color;
+        outT = outT * sh.transmission;
         if (luminance(outT) < S.minContribution) {
           outT = splat(0.f);
           break;
@@ -241,10 +317,10 @@ cudaError_t launchRenderScivisSurfaces(const SamplerTables *T, const Scene &sc, 
                                        const FrameD &fb, bool stats, cudaStream_t st, KernelTimer *kt) {
   dim3 grid((fb.W + 15) / 16, (fb.H + 7) / 8);
   KernelScope ks(kt, KK_SCIVIS, st);
-  if (stats)
-    k_render_scivis_surfaces<true><<<grid, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(T, sc, vol, cam, pf, p, S, fb);
-  else
-    k_render_scivis_surfaces<false><<<grid, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(T, sc, vol, cam, pf, p, S, fb);
+  const bool shaded = S.hasVolume && vol.gradientShadingScale > 0.f;
+  auto k = stats ? (shaded ? k_render_scivis_surfaces<true, true> : k_render_scivis_surfaces<true, false>)
+                 : (shaded ? k_render_scivis_surfaces<false, true> : k_render_scivis_surfaces<false, false>);
+  k<<<grid, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(T, sc, vol, cam, pf, p, S, fb);
   return cudaGetLastError();
 }
 

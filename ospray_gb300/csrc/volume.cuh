@@ -71,6 +71,36 @@ B200_D float tapsValue(const Taps &s) {
   return lerpF(s.fz, lerpF(s.fy, c00, c10), lerpF(s.fy, c01, c11));
 }
 
+B200_D float sampleAt(const VolumeD &v, V3 p) {
+  Taps t;
+  fetchTaps(v, p, t);
+  return tapsValue(t);
+}
+
+// Volume_getGradient (volume/Volume.ih:26-56) over Open VKL's gradient,
+// restated as finite differences of the trilinear sample at one grid
+// spacing: forward, or backward where the forward point leaves the grid; a
+// NaN component becomes 1, as Volume_getGradient does.
+B200_D V3 volumeGradient(const VolumeD &v, V3 p, float s0) {
+  float g[3];
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    const float h = a == 0 ? v.spacing.x : (a == 1 ? v.spacing.y : v.spacing.z);
+    V3 q = p;
+    if (a == 0) q.x = __fadd_rn(q.x, h); else if (a == 1) q.y = __fadd_rn(q.y, h); else q.z = __fadd_rn(q.z, h);
+    const float f = sampleAt(v, q);
+    if (!isnan(f)) {
+      g[a] = __fdiv_rn(__fsub_rn(f, s0), h);
+    } else {
+      V3 r = p;
+      if (a == 0) r.x = __fsub_rn(r.x, h); else if (a == 1) r.y = __fsub_rn(r.y, h); else r.z = __fsub_rn(r.z, h);
+      g[a] = __fdiv_rn(__fsub_rn(s0, sampleAt(v, r)), h);
+    }
+    if (isnan(g[a])) g[a] = 1.f;
+  }
+  return mk(g[0], g[1], g[2]);
+}
+
 B200_D float4 tfGet(const VolumeD &v, float value) {
   value = (value - v.vlo) * (1.f / (v.vhi - v.vlo));
   value = fminf(fmaxf(value, 0.f), 0x1.fffffep-1f);

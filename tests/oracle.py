@@ -140,6 +140,7 @@ def lib():
         L.or_volume_new.restype = P
         L.or_volume_new.argtypes = [P, I, I, I, P, P, P, I, P, I, F, F, F]
         L.or_volume_free.argtypes = [P]
+        L.or_volume_set_gradient_shading.argtypes = [P, F]
         L.or_volume_sample_count.restype = ctypes.c_uint64
         L.or_volume_sample_count.argtypes = [I]
         L.or_render_scivis_volume.argtypes = [P, ctypes.POINTER(OrCamera), I, I, I, I, F, P, I, I, I, P, I]
@@ -242,6 +243,10 @@ class VolumeModel:
         self.h = lib().or_volume_new(_p(d), nx, ny, nz, _p(o), _p(sp), _p(c), len(c), _p(op), len(op),
                                      float(value_range[0]), float(value_range[1]), float(density_scale))
 
+    def set_gradient_shading(self, scale):
+        """The volumetric model's gradientShadingScale (default 0: off)."""
+        lib().or_volume_set_gradient_shading(self.h, float(scale))
+
     def __del__(self):
         try:
             lib().or_volume_free(self.h)
@@ -279,7 +284,8 @@ def render_scivis(scene, volume, cam, lights, materials, w, h, spp=1, pixel_filt
                   bg=(0, 0, 0, 0), shadows=False, visible_lights=False, ao_samples=0, ao_radius=1e20,
                   min_contribution=0.001, frames=1, rows=None, nthreads=0):
     """SciVis over a world with surfaces (and optionally `volume`, a
-    VolumeModel).  lights: dicts as PtWorld takes them (+ "visible");
+    VolumeModel); scene None renders the volume alone through the same
+    integrator (gradient shading included).  lights: dicts as PtWorld takes them (+ "visible");
     materials: dicts {"kd", "ks", "ns", "d", "tf"} for obj materials or None.
     Returns color (h,w,4), depth (h,w), ids (3,h,w)."""
     L = (OrScivisLight * max(1, len(lights)))()
@@ -308,7 +314,7 @@ def render_scivis(scene, volume, cam, lights, materials, w, h, spp=1, pixel_filt
     depth = np.zeros((h, w), np.float32)
     ids = np.zeros((3, h, w), np.uint32)
     y0, y1 = rows if rows else (0, 0)
-    lib().or_render_scivis(scene.h, volume.h if volume is not None else None, ctypes.byref(cam), ctypes.byref(p), L,
+    lib().or_render_scivis(scene.h if scene is not None else None, volume.h if volume is not None else None, ctypes.byref(cam), ctypes.byref(p), L,
                            len(lights), M, len(materials), w, h, frames, y0, y1, _p(color), _p(depth), _p(ids),
                            nthreads)
     return dict(color=color, depth=depth, primID=ids[0], geomID=ids[1], instID=ids[2])

@@ -150,3 +150,26 @@ def test_c_abi_library_exports_header_symbols():
     lib = ctypes.CDLL(og.lib_path())
     missing = [s for s in syms if not hasattr(lib, s)]
     assert not missing, missing
+
+
+def test_oracle_volume_gradient_shading_invariants():
+    """The SciVis integrator with gradient shading: scale 0 reproduces the
+    volume-only renderer exactly; scale 1 keeps every pixel's alpha (the
+    shaded opacity 1 - luminance(1 - a) equals a up to rounding) and only
+    recolours the volume (lit by a quad and a dim ambient light: darker)."""
+    from ospray_gb300 import scenes
+    W, H = 48, 40
+    v = scenes.volume_scene(n=20, width=W, height=H)
+    lights = [dict(type="quad", position=(-1.0, 2.5, -1.0), edge1=(0.5, 0.0, 0.0), edge2=(0.0, 0.0, 0.5),
+                   intensity=6.0, visible=False),
+              dict(type="ambient", intensity=0.25, color=(1.0, 1.0, 1.0), visible=False)]
+    ov = oracle.VolumeModel(v["volume"], v["origin"], v["spacing"], v["color"], v["opacity"], v["value_range"])
+    c = v["camera"]
+    cam = oracle.camera(c["position"], c["direction"], c["up"], fovy=c["fovy"], aspect=W / H)
+    plain = oracle.render_scivis(None, ov, cam, lights, [], W, H, spp=2, shadows=True)["color"]
+    assert np.array_equal(plain, oracle.render_scivis_volume(ov, cam, 2, W, H, spp=2))
+    ov.set_gradient_shading(1.0)
+    shaded = oracle.render_scivis(None, ov, cam, lights, [], W, H, spp=2, shadows=True)["color"]
+    assert plain[..., 3].max() > 0.3
+    assert np.abs(shaded[..., 3] - plain[..., 3]).max() < 1e-5
+    assert shaded[..., :3].mean() < plain[..., :3].mean()

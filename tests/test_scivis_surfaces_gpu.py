@@ -109,3 +109,57 @@ def test_scivis_surfaces_with_volume(world, b200_device):
 def test_scivis_visible_lights_and_accumulation(world, b200_device):
     gpu, ref = render_both(world, b200_device, spp=1, frames=3, visible_lights=True, shadows=True)
     assert_close(gpu, ref)
+
+
+@pytest.mark.parametrize("shadows,ao", [(False, 0), (True, 1)])
+def test_scivis_gradient_shading_with_surfaces(world, b200_device, shadows, ao):
+    """Gradient-shaded volume (integrateVolumeIntervalsGradient with
+    gradientShadingScale 0.75) in front of the surfaces: each opaque sample
+    is lit like a material-less surface with normal -grad, shadow and AO
+    rays through the surfaces and the volume."""
+    g, o, ov = world[True]
+    g.set_volume_gradient_shading(0.75)
+    ov.set_gradient_shading(0.75)
+    try:
+        gpu, ref = render_both(world, b200_device, with_volume=True, shadows=shadows, ao_samples=ao,
+                               bg=(0.1, 0.1, 0.2, 1.0))
+    finally:
+        g.set_volume_gradient_shading(0.0)
+        ov.set_gradient_shading(0.0)
+    assert_close(gpu, ref, frac=0.99)
+    unshaded, _ = render_both(world, b200_device, with_volume=True, shadows=shadows, ao_samples=ao,
+                              bg=(0.1, 0.1, 0.2, 1.0))
+    # the shading changes the volume's colour where it is seen
+    assert np.abs(unshaded["color"] - gpu["color"]).max() > 1e-2
+
+
+def test_scivis_gradient_shading_volume_only(b200_device):
+    """A volume-only world with gradient shading and lights renders through
+    the shaded integrator (no surfaces traced) and matches the oracle."""
+    import ospray_gb300 as og
+    from ospray_gb300 import scenes
+    v = scenes.volume_scene(n=24, width=W, height=H)
+    g = og.Scene(b200_device)
+    g.set_volume(v["volume"], v["origin"], v["spacing"], v["color"], v["opacity"], v["value_range"])
+    lights = [dict(type="quad", position=(-1.0, 2.5, -1.0), edge1=(0.5, 0.0, 0.0), edge2=(0.0, 0.0, 0.5),
+                   intensity=6.0, visible=False),
+              dict(type="ambient", intensity=0.25, color=(1.0, 1.0, 1.0), visible=False)]
+    g.set_lights([og.quad_light(L["position"], L["edge1"], L["edge2"], L["intensity"], visible=L["visible"])
+                  if L["type"] == "quad" else og.ambient_light(L["intensity"], L["color"], visible=L["visible"])
+                  for L in lights])
+    g.set_volume_gradient_shading(1.0)
+    ov = oracle.VolumeModel(v["volume"], v["origin"], v["spacing"], v["color"], v["opacity"], v["value_range"])
+    ov.set_gradient_shading(1.0)
+    c = v["camera"]
+    fb = og.Frame(b200_device, W, H, og.FB_COLOR | og.FB_ACCUM)
+    cam = og.camera_desc(c["position"], c["direction"], c["up"], fovy=c["fovy"], aspect=W / H)
+    params = og.scivis_params(spp=2, shadows=True, ao_samples=1, bg=(0, 0, 0, 0))
+    og.render_scivis(g, cam, params, fb)
+    col = fb.read(og.FB_COLOR)
+    ocam = oracle.camera(c["position"], c["direction"], c["up"], fovy=c["fovy"], aspect=W / H)
+    ref = oracle.render_scivis(None, ov, ocam, lights, [], W, H, spp=2, shadows=True, ao_samples=1)["color"]
+    assert np.isfinite(col).all()
+    assert ref[..., 3].max() > 0.3  # the volume is in view
+    close = np.all(np.abs(col - ref) <= 1e-3 * np.maximum(1.0, np.abs(ref)) + 1e-5, axis=2)
+    assert close.mean() >= 0.99, close.mean()
+    assert np.abs(col.mean(axis=(0, 1)) - ref.mean(axis=(0, 1))).max() < 1e-4
