@@ -179,6 +179,17 @@ void b200_tonemapper_defaults(b200_tonemapper *tm);
  * Variance.cpp:32-46).  Synchronous.  Batched renders do not update it. */
 int b200_frame_variance(b200_frame fb, float threshold, float *out);
 
+/* Adaptive accumulation: the renderer's "varianceThreshold"
+ * (Renderer::commit render/Renderer.cpp:44), applied by later render calls
+ * on this framebuffer (LocalTiledLoadBalancer::renderFrame
+ * render/LoadBalancer.cpp:15-30 with LocalFrameBuffer::getRenderTaskIDs
+ * fb/LocalFB.cpp:238-260).  With a threshold > 0, a VARIANCE channel and a
+ * frame ID >= max(2, 16 / pixelSamples), a render call renders only the
+ * 8x8 tasks whose last error estimate exceeds the threshold; the other
+ * pixels keep their accumulated values.  0 (the default) renders every task.
+ * A non-finite value is refused.  Batched renders ignore it. */
+int b200_frame_set_variance_threshold(b200_frame fb, float varianceThreshold);
+
 /* image error of a framebuffer's accumulated colour against a reference
  * framebuffer of the same size: relMSE = mean over pixels and rgb of
  * (x - r)^2 / (r^2 + 0.01).  Synchronous. */

@@ -33,3 +33,27 @@ def avg_error(err, threshold):
     e = np.asarray(err).ravel()
     act = e[e >= threshold]
     return float(act.mean()) if act.size else float(e.max())
+
+
+def variance_frame_picks(nframes, seed=43):
+    """FrameBuffer::beginFrame (modules/cpu/fb/FrameBuffer.cpp:121-136): of
+    every even/odd frame pair, one goes into the variance buffer; on each
+    even frame pickOdd = mt() & 1 with std::mt19937 seeded 43
+    (FrameBuffer.h:135-137), and frame f accumulates when
+    (f even) != pickOdd.  numpy's legacy RandomState is the same Mersenne
+    Twister with the same seeding (init_genrand), and its full-range uint32
+    draws are the raw outputs."""
+    rs = np.random.RandomState(seed)
+    picks, pick_odd = [], False
+    for f in range(nframes):
+        even = (f & 1) == 0
+        if even:
+            pick_odd = bool(rs.randint(0, 2 ** 32, dtype=np.uint32) & 1)
+        picks.append(even != pick_odd)
+    return picks
+
+
+def selected_tasks(err, threshold):
+    """LocalFrameBuffer::getRenderTaskIDs (fb/LocalFB.cpp:238-260): the
+    tasks whose error exceeds the threshold."""
+    return np.asarray(err) > threshold

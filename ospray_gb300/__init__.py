@@ -231,6 +231,7 @@ def lib():
             "b200_render_ao": (I, [P, ctypes.POINTER(CameraDesc), ctypes.POINTER(AOParams), P, P]),
             "b200_scene_set_lights": (I, [P, P, I]),
             "b200_scene_set_volume": (I, [P, P, I, I, I, P, P, P, I, P, I, P, F]),
+            "b200_frame_set_variance_threshold": (I, [P, F]),
             "b200_scene_set_volume_gradient_shading": (I, [P, F]),
             "b200_render_scivis": (I, [P, ctypes.POINTER(CameraDesc), ctypes.POINTER(ScivisParams), P, I, P, P]),
             "b200_render_pt": (I, [P, ctypes.POINTER(CameraDesc), ctypes.POINTER(PTParams), P, I, P, P]),
@@ -422,6 +423,11 @@ class Frame:
         v = ctypes.c_float()
         self.device._check(lib().b200_frame_variance(self._h, float(threshold), ctypes.byref(v)))
         return v.value
+
+    def set_variance_threshold(self, threshold):
+        """The renderer's varianceThreshold: later renders of this frame
+        render only the 8x8 tasks whose error estimate exceeds it (0: all)."""
+        self.device._check(lib().b200_frame_set_variance_threshold(self._h, float(threshold)))
 
     def set_tonemapper(self, tm):
         """tm: ToneMapper (see tonemapper()) or None to remove it; applies from the next render."""

@@ -420,6 +420,7 @@ FrameObj::FrameObj(DeviceObj *d, int w, int h, int fmt, uint32_t ch) : dev(d), W
   if (ch & B200_FB_VARIANCE) {
     alloc((void **)&variance, n * sizeof(float4));
     alloc((void **)&taskErr, size_t(tasksX()) * tasksY() * 4);
+    alloc((void **)&taskActive, size_t(tasksX()) * tasksY());
   }
   if (ch & B200_FB_NORMAL) alloc((void **)&normal, n * sizeof(float3));
   if (ch & B200_FB_ALBEDO) alloc((void **)&albedo, n * sizeof(float3));
@@ -432,6 +433,7 @@ FrameObj::FrameObj(DeviceObj *d, int w, int h, int fmt, uint32_t ch) : dev(d), W
 FrameObj::~FrameObj() {
   cudaStreamSynchronize(dev->stream);
   if (taskErr) cudaFree(taskErr);
+  if (taskActive) cudaFree(taskActive);
   for (void *p : {(void *)color, (void *)depth, (void *)variance, (void *)normal, (void *)albedo, (void *)primID,
                   (void *)geomID, (void *)instID, mapped})
     if (p) cudaFree(p);
@@ -451,6 +453,9 @@ FrameD FrameObj::view() const {
   f.W = W;
   f.H = H;
   f.frameID = frameID;
+  f.accumVariance = accumVariance ? 1 : 0;
+  f.taskActive = adaptive ? taskActive : nullptr;
+  f.tasksX = tasksX();
   return f;
 }
 
@@ -736,8 +741,22 @@ int b200_frame_release(b200_frame f) {
 
 int b200_frame_reset(b200_frame f) {
   if (!f) return B200_INVALID_ARGUMENT;
-  reinterpret_cast<FrameObj *>(f)->frameID = 0;
-  reinterpret_cast<FrameObj *>(f)->taskErrValid = false;
+  FrameObj *fb = reinterpret_cast<FrameObj *>(f);
+  fb->frameID = 0;
+  fb->taskErrValid = false;
+  fb->mtGen.seed(43u);  // FrameBuffer::clear: the coin flips start over
+  fb->pickOdd = false;
+  return B200_NO_ERROR;
+}
+
+int b200_frame_set_variance_threshold(b200_frame f, float threshold) {
+  if (!f) return B200_INVALID_ARGUMENT;
+  FrameObj *fb = reinterpret_cast<FrameObj *>(f);
+  if (!std::isfinite(threshold)) {
+    fb->dev->lastError = "varianceThreshold is not finite";
+    return B200_INVALID_ARGUMENT;
+  }
+  fb->errorThreshold = threshold;
   return B200_NO_ERROR;
 }
 
@@ -767,6 +786,7 @@ int b200_render_ao(b200_scene s, const b200_camera_desc *camera, const b200_ao_p
     require(p->pixelFilter >= B200_PF_POINT && p->pixelFilter <= B200_PF_BLACKMAN_HARRIS, "bad pixel filter");
     const AOParamsD d = makeAOParams(*p);
     cudaStream_t st = stream ? (cudaStream_t)stream : sc->dev->stream;
+    fb->beginFrame(p->pixelSamples, st);
     check(launchRenderAO(sc->dev->tables, sc->view(), makeCamera(*camera), sc->dev->filter(p->pixelFilter), d,
                          fb->view(), p->collectStats != 0, st, sc->dev->timer),
           "AO launch");
@@ -861,6 +881,7 @@ int b200_render_pt(b200_scene s, const b200_camera_desc *camera, const b200_pt_p
     const PtParamsD d = makePtParams(*p, sc->nLights, nmaterials);
     DeviceObj *dev = sc->dev;
     ensurePtWorkspace(dev, ptWorkspaceBytes((long long)fb->W * fb->H * p->pixelSamples));
+    fb->beginFrame(p->pixelSamples, st);
     check(launchRenderPT(dev->tables, sc->view(), makeCamera(*camera), dev->filter(p->pixelFilter), d,
                          sc->dMaterials, sc->dLights, sc->dLightCdf, dev->albedoTables(), fb->view(),
                          p->collectStats != 0, dev->ptWs, dev->ptWsBytes, st, nullptr, nullptr, nullptr,
@@ -963,6 +984,7 @@ int b200_render_scivis(b200_scene s, const b200_camera_desc *camera, const b200_
     d.samplingRate = p->volumeSamplingRate;
     for (int k = 0; k < 4; k++) d.bg[k] = p->backgroundColor[k];
     cudaStream_t st = stream ? (cudaStream_t)stream : sc->dev->stream;
+    fb->beginFrame(p->pixelSamples, st);
     if (!surfaces && !(sc->vol.gradientShadingScale > 0.f)) {
       check(launchRenderScivisVolume(sc->dev->tables, sc->view(), sc->vol, makeCamera(*camera),
                                      sc->dev->filter(p->pixelFilter), d, fb->view(), p->collectStats != 0, st,

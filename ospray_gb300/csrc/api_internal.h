@@ -2,6 +2,7 @@
 #pragma once
 #include <stdexcept>
 #include <string>
+#include <random>
 #include <vector>
 
 #include "../../include/b200.h"
@@ -130,6 +131,21 @@ struct FrameObj {
   static constexpr int TASK = 8;
   float *taskErr = nullptr;
   bool taskErrValid = false;
+  // Adaptive accumulation (the renderer's varianceThreshold,
+  // render/Renderer.cpp:44; LocalFrameBuffer::getRenderTaskIDs
+  // fb/LocalFB.cpp:238-260): once frameID >= max(2, 16 / spp), only the
+  // tasks whose error exceeds the threshold are rendered.
+  float errorThreshold = 0.f;
+  uint8_t *taskActive = nullptr;  // per task, written on the device each frame
+  bool adaptive = false;          // this frame renders the selected tasks only
+  // FrameBuffer::beginFrame (fb/FrameBuffer.cpp:121-136): of each even/odd
+  // frame pair one, picked by a coin flip of std::mt19937 seeded 43, goes into
+  // the variance buffer
+  std::mt19937 mtGen{43u};
+  bool pickOdd = false, accumVariance = false;
+  // called by every render entry point before its launch, for the frame
+  // frameID about to be rendered with spp samples per pixel
+  void beginFrame(int spp, cudaStream_t st);
   int tasksX() const { return (W + TASK - 1) / TASK; }
   int tasksY() const { return (H + TASK - 1) / TASK; }
   FrameObj(DeviceObj *d, int w, int h, int format, uint32_t ch);

@@ -81,6 +81,8 @@ struct BatchObj {
       d.lights = r.scene->dLights;
       d.lightCdf = r.scene->dLightCdf;
       d.fb = r.fb->view();
+      d.fb.accumVariance = 0;     // batched frames keep no variance estimate
+      d.fb.taskActive = nullptr;  // and render every task
     }
     return h;
   }

@@ -129,7 +129,28 @@ __global__ void k_task_variance(const float4 *__restrict__ color, const float4 *
   if (cnt) v /= float(cnt);
   err[t] = v * 64.f;
 }
+// LocalFrameBuffer::getRenderTaskIDs (fb/LocalFB.cpp:238-260): a task is
+// rendered when its error exceeds the threshold
+__global__ void k_task_select(const float *__restrict__ err, int n, float threshold, uint8_t *__restrict__ active) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) active[t] = err[t] > threshold ? 1 : 0;
+}
 }  // namespace
+
+void FrameObj::beginFrame(int spp, cudaStream_t st) {
+  // FrameBuffer::beginFrame: the coin flip on every even frame
+  const bool even = (frameID & 1) == 0;
+  if (even) pickOdd = (mtGen() & 1u) != 0;
+  accumVariance = variance != nullptr && even != pickOdd;
+  // FrameBuffer::minimumAdaptiveFrames: max(2, 16 / spp)
+  const int minFrames = std::max(2, 16 / std::max(1, spp));
+  adaptive = errorThreshold > 0.f && taskErr && taskErrValid && frameID >= minFrames;
+  if (adaptive) {
+    const int nt = tasksX() * tasksY();
+    k_task_select<<<(nt + 255) / 256, 256, 0, st>>>(taskErr, nt, errorThreshold, taskActive);
+    check(cudaGetLastError(), "task selection");
+  }
+}
 
 void framePostProcess(FrameObj *fb, cudaStream_t st, bool variance) {
   // the variance estimate follows every odd frame (LocalFrameBuffer::postProcess)

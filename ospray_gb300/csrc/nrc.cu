@@ -669,6 +669,7 @@ int b200_render_pt_nrc(b200_scene s, const b200_camera_desc *camera, const b200_
     nf.trainOffset = hsh % nf.trainStride;
     nf.sampleCap = uint32_t(o->vcap);
     nf.useCache = np.useCache ? 1u : 0u;
+    fb->beginFrame(p->pixelSamples, st);
     check(launchRenderPT(dev->tables, sc->view(), makeCamera(*camera), dev->filter(p->pixelFilter), d,
                          sc->dMaterials, sc->dLights, sc->dLightCdf, dev->albedoTables(), fb->view(), false, dev->ptWs,
                          dev->ptWsBytes, st, &nf, &NrcObj::inferHook, o),

@@ -269,6 +269,9 @@ OSPFuture B200Device::renderFrame(OSPFrameBuffer hf, OSPRenderer hr, OSPCamera h
     throw Error(OSP_INVALID_OPERATION, "ospRenderFrame: renderer, camera and world must be committed");
   auto *fut = new FutureObj();
   try {
+    // LocalTiledLoadBalancer::renderFrame (render/LoadBalancer.cpp:15-30):
+    // the renderer's varianceThreshold selects the tasks of this frame
+    check(b200_frame_set_variance_threshold(f->fb, r->varianceThreshold));
     check(b200_event_record(dev_, &fut->start));
     if (r->type == "ao") {
       if (w->hasVolume) warn("ao renderer: volumes are not rendered by the b200 device");

@@ -155,6 +155,11 @@ int b200_render_pt_noalloc(b200_scene s, const b200_camera_desc *camera, const b
   d.minContribution = p->minContribution;
   d.maxContribution = p->maxContribution;
   for (int k = 0; k < 4; k++) d.bg[k] = p->backgroundColor[k];
+  try {
+    fb->beginFrame(p->pixelSamples, st);
+  } catch (const Error &ex) {
+    return fail(ex.code, ex.what());
+  }
   e = launchRenderPT(dev->tables, sc->view(), makeCamera(*camera), dev->filter(p->pixelFilter), d,
                      reinterpret_cast<const MaterialD *>(base + OFF_MATERIALS), sc->dLights, sc->dLightCdf,
                      reinterpret_cast<const AlbedoTablesD *>(base + OFF_ALBEDO), fb->view(), p->collectStats != 0,

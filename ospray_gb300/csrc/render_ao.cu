@@ -73,7 +73,7 @@ __global__ void __launch_bounds__(128) k_render_ao(const SamplerTables *T, Scene
   const int x = blockIdx.x * 16 + (threadIdx.x & 15);
   const int y = blockIdx.y * 8 + (threadIdx.x >> 4);
   TraceStats ts = {0, 0, 0, 0};
-  if (x >= fb.W || y >= fb.H) {
+  if (x >= fb.W || y >= fb.H || !pixelActive(fb, x, y)) {
     if (STATS) flushStats(sc, ts);
     return;
   }

@@ -31,10 +31,18 @@ struct FrameD {
   float4 *color;
   float *depth;
   uint32_t *primID, *geomID, *instID;
-  float4 *variance;  // optional: accumulated on odd frames
+  float4 *variance;  // optional: accumulates the frames picked by accumVariance
   float3 *normal, *albedo;
   int W, H, frameID;
+  int accumVariance;          // this frame goes into the variance buffer (FrameBuffer::beginFrame)
+  const uint8_t *taskActive;  // adaptive accumulation: per 8x8 task, render it? (null: all)
+  int tasksX;
 };
+
+// Is pixel (x, y) in a render task of this frame (LocalFrameBuffer::getRenderTaskIDs)?
+B200_D bool pixelActive(const FrameD &fb, int x, int y) {
+  return !fb.taskActive || fb.taskActive[(y >> 3) * fb.tasksX + (x >> 3)] != 0;
+}
 
 B200_D Ray cameraRay(const CameraD &c, float sx, float sy) {
   const V3 d = add(add(c.dir_00, mul(sx, c.du_size)), mul(sy, c.dv_up));
@@ -189,7 +197,7 @@ B200_D void fbAccumulate(const FrameD &fb, int x, int y, const PixelOut &s) {
     }
     fb.color[i] = c;
   }
-  if (fb.variance && (fb.frameID & 1)) {
+  if (fb.variance && fb.accumVariance) {
     const float vs = fdiv(1.f, float(fb.frameID / 2 + 1));
     float4 v = make_float4(s.r, s.g, s.b, s.a);
     if (!(vs > 0.8f)) {

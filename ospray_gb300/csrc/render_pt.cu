@@ -137,17 +137,37 @@ B200_D PathRec genPT(const PtCtx &c, const CameraD &cam, const PixelFilterD &pf,
   return r;
 }
 
+// appends one entry per lane that wants to, with one atomic per warp
+B200_D uint32_t warpAppend(bool want, uint32_t *counter) {
+  const unsigned m = __ballot_sync(__activemask(), want);
+  if (!m) return 0;
+  const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+  uint32_t base = 0;
+  if (lane == leader) base = atomicAdd(counter, uint32_t(__popc(m)));
+  base = __shfl_sync(__activemask(), base, leader);
+  return base + uint32_t(__popc(m & ((1u << lane) - 1u)));
+}
+
 // nrcStride > 0: the radiance-cache training paths of this frame get their
 // slot in meta2.w (INVALID_ID for the others)
+//
+// Adaptive accumulation (fb.taskActive set): only the paths of pixels in
+// selected tasks are generated, appended to queue `active` (counted in
+// ws.counters[0], zeroed beforehand); the first bounce then reads that queue.
 __global__ void k_pt_generate(PtCtx c, CameraD cam, PixelFilterD pf, FrameInfo fi, Workspace ws, uint32_t nrcStride,
-                              uint32_t nrcOffset, uint32_t nrcSlots) {
+                              uint32_t nrcOffset, uint32_t nrcSlots, FrameD fb, uint32_t *active) {
   const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (p == 0) {
+  if (p == 0 && !active) {
     ws.counters[0] = uint32_t(fi.npaths);
     for (int k = 1; k < 16; k++) ws.counters[k] = 0;
   }
-  if (p >= fi.npaths) return;
   const int pix = int(p / fi.spp), s = int(p % fi.spp);
+  const bool live = p < fi.npaths && (!active || pixelActive(fb, pix % fi.W, pix / fi.W));
+  if (active) {
+    const uint32_t slot = warpAppend(live, ws.counters);
+    if (live) active[slot] = uint32_t(p);
+  }
+  if (!live) return;
   PathRec r = genPT(c, cam, pf, fi, pix % fi.W, pix / fi.W, s, 0u);
   if (nrcStride) {
     const uint32_t k = uint32_t(p) + nrcOffset;
@@ -234,16 +254,6 @@ __global__ void __launch_bounds__(TRACE_BLOCK, B200_TRACE_MINBLOCKS) k_trace_que
   if (STATS) flushStats(sc, ts);
 }
 
-// appends one entry per lane that wants to, with one atomic per warp
-B200_D uint32_t warpAppend(bool want, uint32_t *counter) {
-  const unsigned m = __ballot_sync(__activemask(), want);
-  if (!m) return 0;
-  const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
-  uint32_t base = 0;
-  if (lane == leader) base = atomicAdd(counter, uint32_t(__popc(m)));
-  base = __shfl_sync(__activemask(), base, leader);
-  return base + uint32_t(__popc(m & ((1u << lane) - 1u)));
-}
 
 // The shading step of an AO request's camera sample (AORenderer_renderSample,
 // render/ao/AORenderer.ispc:23-149, with computeAO render/util.ispc:12-54):
@@ -605,7 +615,7 @@ B200_D PixelOut finalizeAO(const PathRec *paths, int spp, const AOParamsD &A) {
 
 __global__ void k_pt_finalize(PtCtx c, Workspace ws, FrameInfo fi, FrameD fb) {
   const int pix = blockIdx.x * blockDim.x + threadIdx.x;
-  if (pix >= fi.W * fi.H) return;
+  if (pix >= fi.W * fi.H || !pixelActive(fb, pix % fi.W, pix / fi.W)) return;
   fbAccumulate(fb, pix % fi.W, pix / fi.W, finalizePT(ws.paths + size_t(pix) * fi.spp, fi.spp, c.p.maxContribution));
 }
 
@@ -875,12 +885,15 @@ cudaError_t launchRenderPT(const SamplerTables *T, const Scene &sc, const Camera
     cudaMemsetAsync(nf.trainVerts, 0xff, size_t(nf.trainSlots) * nf.maxLen1 * 20 * 4, st);
   }
   const int gen = int((fi.npaths + 255) / 256);
-  k_pt_generate<<<gen, 256, 0, st>>>(c, cam, pf, fi, ws, nf.trainStride, nf.trainOffset, nf.trainSlots);
+  const bool adaptive = fb.taskActive != nullptr;
+  if (adaptive) cudaMemsetAsync(ws.counters, 0, 16 * sizeof(uint32_t), st);
+  k_pt_generate<<<gen, 256, 0, st>>>(c, cam, pf, fi, ws, nf.trainStride, nf.trainOffset, nf.trainSlots, fb,
+                                     adaptive ? ws.qa : nullptr);
   uint32_t *qs[2] = {ws.qa, ws.qb};
   for (int b = 0; b <= p.maxPathLength; b++) {
     const int cin = b & 1, cout = cin ^ 1;
     k_bounce_reset<<<1, 1, 0, st>>>(ws.counters, cin, cout, nullptr);
-    const uint32_t *qin = b == 0 ? nullptr : qs[cin];
+    const uint32_t *qin = (b == 0 && !adaptive) ? nullptr : qs[cin];
     {
       KernelScope ks(kt, KK_TRACE_CLOSEST, st);
       if (stats)

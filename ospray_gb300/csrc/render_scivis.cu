@@ -222,7 +222,7 @@ __global__ void __launch_bounds__(128) k_render_scivis_surfaces(const SamplerTab
   const int x = blockIdx.x * 16 + (threadIdx.x & 15);
   const int y = blockIdx.y * 8 + (threadIdx.x >> 4);
   TraceStats ts = {0, 0, 0, 0};
-  if (x < fb.W && y < fb.H) {
+  if (x < fb.W && y < fb.H && pixelActive(fb, x, y)) {
     const float rcpW = fdiv(1.f, float(fb.W)), rcpH = fdiv(1.f, float(fb.H));
     const uint32_t start = uint32_t(fb.frameID * p.spp + 1);
     PixelOut acc = {0.f, 0.f, 0.f, 0.f, INFINITY, INVALID_ID, INVALID_ID, INVALID_ID};

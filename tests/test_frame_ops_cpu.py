@@ -58,3 +58,22 @@ def test_tonemapper_is_monotone_and_bounded():
         assert np.all(np.diff(g) >= -1e-6)
         assert g.min() >= 0.0 and g.max() <= 1.0
         assert np.all(out[0, :, 3] == 1.0)
+
+
+def test_variance_frame_picks_use_std_mt19937():
+    """The variance buffer's frame picks come from std::mt19937 (seed 43) in
+    the reference and in the b200 host code; the oracle draws them from
+    numpy's legacy RandomState.  Pinned by the C++ standard's known answer
+    for mt19937 ([rand.predef]: the 10000th output of a default-seeded
+    (5489) engine is 4123659995) and by the pair rule (exactly one frame of
+    every even/odd pair)."""
+    import os
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle"))
+    import variance as vref
+    rs = np.random.RandomState(5489)
+    assert int(rs.randint(0, 2 ** 32, size=10000, dtype=np.uint32)[-1]) == 4123659995
+    picks = vref.variance_frame_picks(64)
+    for k in range(0, 64, 2):
+        assert picks[k] != picks[k + 1]
+    assert 8 < sum(picks[0::2]) < 24  # a coin flip per pair, not a fixed parity

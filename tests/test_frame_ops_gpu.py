@@ -139,3 +139,95 @@ def test_variance_estimate_matches_oracle(b200_device, pt_world):
                 assert abs(got - exp) <= 1e-4 * max(1.0, exp), (frame, thr, got, exp)
             values.append(fb.variance(0.0))
     assert values[-1] < values[0]  # the estimate falls as frames accumulate
+
+
+def _vref():
+    import os
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle"))
+    import variance as vref
+    return vref
+
+
+def test_variance_buffer_accumulates_the_picked_frames(b200_device, pt_world):
+    """FrameBuffer::beginFrame: the variance buffer takes one frame of every
+    even/odd pair, picked by std::mt19937(43) coin flips (restated by the
+    oracle); a frame that is not picked leaves it bit for bit unchanged, and
+    the first pick stores that frame's samples exactly (scale 1)."""
+    import ospray_gb300 as og
+    vref = _vref()
+    d, g = pt_world
+    c = d["camera"]
+    cam = og.camera_desc(c["position"], c["direction"], c["up"], fovy=c["fovy"], aspect=c["aspect"])
+    fb = og.Frame(b200_device, W, H, og.FB_COLOR | og.FB_ACCUM | og.FB_VARIANCE)
+    p = og.pt_params(spp=1, max_path_length=3)
+    picks = vref.variance_frame_picks(8)
+    prev_v = np.zeros((H, W, 4), np.float32)
+    acc0 = None
+    for f in range(8):
+        og.render_pt(g, cam, p, og.materials_array(d["materials"]), fb)
+        acc, v = fb.read(og.FB_ACCUM), fb.read(og.FB_VARIANCE)
+        if f == 0:
+            acc0 = acc
+            if picks[0]:
+                np.testing.assert_array_equal(v, acc)
+        changed = not np.array_equal(v, prev_v)
+        assert changed == picks[f], (f, picks)
+        if f == 1 and picks[1]:  # the frame-1 samples: 2 * acc1 - acc0
+            np.testing.assert_allclose(v, 2.0 * acc - acc0, rtol=1e-4, atol=1e-5)
+        prev_v = v
+
+
+@pytest.mark.parametrize("renderer", ["pt", "ao"])
+def test_adaptive_accumulation_renders_selected_tasks(b200_device, pt_world, renderer):
+    """varianceThreshold (LocalFrameBuffer::getRenderTaskIDs): from frame
+    max(2, 16 / spp) on, a frame renders only the 8x8 tasks whose error
+    estimate exceeds the threshold.  Against a second framebuffer rendering
+    every task of the same frames: the selected tasks get the same new values
+    and every other pixel keeps its previous value bit for bit."""
+    import ospray_gb300 as og
+    vref = _vref()
+    d, g = pt_world
+    c = d["camera"]
+    cam = og.camera_desc(c["position"], c["direction"], c["up"], fovy=c["fovy"], aspect=c["aspect"])
+    mats = og.materials_array(d["materials"])
+    spp = 4 if renderer == "pt" else 1
+    start = max(2, 16 // spp)  # first adaptive frame
+    if renderer == "pt":
+        p = og.pt_params(spp=spp, max_path_length=3)
+
+        def render(fb):
+            og.render_pt(g, cam, p, mats, fb)
+    else:
+        p = og.ao_params(spp=spp, ao_samples=2)
+
+        def render(fb):
+            og.render_ao(g, cam, p, fb)
+    chans = og.FB_COLOR | og.FB_ACCUM | og.FB_VARIANCE | og.FB_DEPTH
+    fa, fr = og.Frame(b200_device, W, H, chans), og.Frame(b200_device, W, H, chans)
+    for _ in range(start):
+        render(fa)
+        render(fr)
+    acc_before = fa.read(og.FB_ACCUM)
+    err = vref.task_errors(acc_before, fa.read(og.FB_VARIANCE))
+    thr = float(np.median(err))
+    fa.set_variance_threshold(thr)
+    render(fa)
+    render(fr)
+    acc_a, acc_r = fa.read(og.FB_ACCUM), fr.read(og.FB_ACCUM)
+    ty, tx = err.shape
+    active = vref.selected_tasks(err, thr)
+    clear = np.abs(err - thr) > 1e-3 * max(thr, 1e-6)  # tasks not at the threshold's rounding edge
+    assert active[clear].sum() > 5 and (~active[clear]).sum() > 5
+    checked = 0
+    for y in range(ty):
+        for x in range(tx):
+            if not clear[y, x]:
+                continue
+            sl = (slice(8 * y, 8 * y + 8), slice(8 * x, 8 * x + 8))
+            if active[y, x]:
+                np.testing.assert_allclose(acc_a[sl], acc_r[sl], rtol=1e-5, atol=1e-6)
+            else:
+                np.testing.assert_array_equal(acc_a[sl], acc_before[sl])
+            checked += 1
+    assert checked > 0.8 * tx * ty
