@@ -85,6 +85,23 @@ int b200_scene_release(b200_scene scene);
 /* vertex: nverts x 3 float; index: ntris x 3 uint32 (vec3ui) */
 int b200_scene_add_mesh(b200_scene scene, const float *vertex, int64_t nverts, const uint32_t *index,
                         int64_t ntris, int *geom_out);
+/* Quad mesh (Mesh::commit with a vec4ui "index", Mesh.cpp:114-145;
+ * QuadMesh_postIntersect geometry/Mesh.ispc:67-176): index nquads x 4
+ * uint32.  A quad (v0, v1, v2, v3) is intersected as the triangles
+ * (v0, v1, v3) and (v2, v3, v1), Embree's quad decomposition; a hit reports
+ * the quad's index as primID, and the epsilon is taken over its 4 vertices.
+ * A triangle given as a quad with v2 == v3 adds a degenerate half that is
+ * never hit. */
+int b200_scene_add_quad_mesh(b200_scene scene, const float *vertex, int64_t nverts, const uint32_t *index,
+                             int64_t nquads, int *geom_out);
+/* Boxes (Boxes::commit geometry/Boxes.cpp:33-46, "box" data of box3f):
+ * boxes n x 6 float (lower xyz, upper xyz).  Each box is traced as its 12
+ * face triangles, which report the box's index as primID; a ray hits the
+ * first face in [tnear, tfar] (the exit face when it starts inside, as
+ * intersectBox with filterIntersectionBoth, common/Intersect.ih:195-223),
+ * the normal is the face's, and no geometry epsilon is added
+ * (Boxes_postIntersect). */
+int b200_scene_add_boxes(b200_scene scene, const float *boxes, int64_t n, int *geom_out);
 /* spheres: n x 4 float (center xyz, radius), OSP_SPHERE */
 int b200_scene_add_spheres(b200_scene scene, const float *spheres, int64_t n, int *geom_out);
 /* one (instance, geometric model) pair: geometry `geom` placed by the

@@ -51,6 +51,44 @@ int or_scene_add_mesh(void *sp, const float *verts, int nverts, const uint32_t *
   return int(s.geoms.size() - 1);
 }
 
+// quad (v0, v1, v2, v3) -> triangles (v0, v1, v3), (v2, v3, v1) (Embree's
+// quad decomposition), both reporting the quad's primID
+int or_scene_add_quad_mesh(void *sp, const float *verts, int nverts, const uint32_t *index, int nquads) {
+  Scene &s = *static_cast<Scene *>(sp);
+  Geometry g;
+  g.type = 0;
+  g.verts.resize(nverts);
+  std::memcpy(g.verts.data(), verts, sizeof(float) * 3 * nverts);
+  g.quadIndex.assign(index, index + 4 * size_t(nquads));
+  g.primDiv = 2;
+  for (int q = 0; q < nquads; q++) {
+    const uint32_t *v = index + 4 * size_t(q);
+    for (uint32_t k : {v[0], v[1], v[3], v[2], v[3], v[1]}) g.index.push_back(k);
+  }
+  s.geoms.push_back(std::move(g));
+  return int(s.geoms.size() - 1);
+}
+
+// box3f (lower, upper) -> 8 corners and 12 face triangles (corner c =
+// (x: c & 1, y: c >> 1 & 1, z: c >> 2)), all reporting the box's primID
+int or_scene_add_boxes(void *sp, const float *boxes, int n) {
+  Scene &s = *static_cast<Scene *>(sp);
+  Geometry g;
+  g.type = 0;
+  g.primDiv = 12;
+  g.boxFaces = true;
+  static const int F[6][4] = {{0, 4, 6, 2}, {1, 3, 7, 5}, {0, 1, 5, 4}, {2, 6, 7, 3}, {0, 2, 3, 1}, {4, 5, 7, 6}};
+  for (int b = 0; b < n; b++) {
+    const float *lo = boxes + 6 * size_t(b), *hi = lo + 3;
+    const uint32_t o = uint32_t(g.verts.size());
+    for (int c = 0; c < 8; c++) g.verts.push_back({(c & 1) ? hi[0] : lo[0], (c & 2) ? hi[1] : lo[1], (c & 4) ? hi[2] : lo[2]});
+    for (int f = 0; f < 6; f++)
+      for (int k : {0, 1, 2, 0, 2, 3}) g.index.push_back(o + uint32_t(F[f][k]));
+  }
+  s.geoms.push_back(std::move(g));
+  return int(s.geoms.size() - 1);
+}
+
 int or_scene_add_spheres(void *sp, const float *xyzr, int n) {
   Scene &s = *static_cast<Scene *>(sp);
   Geometry g;

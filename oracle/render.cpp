@@ -131,7 +131,14 @@ DG postIntersect(const Scene &s, const Ray &ray, const Hit &hit) {
   const Geometry &g = s.geoms[e->geom];
   V3 Ng = hit.Ng, Ns = hit.Ng;
   float eps;
-  if (g.type == 0) {
+  if (g.type == 0 && g.boxFaces) {
+    eps = 0.f;  // Boxes_postIntersect (geometry/Boxes.ispc) sets no geometry epsilon
+  } else if (g.type == 0 && !g.quadIndex.empty()) {
+    // QuadMesh_postIntersect (geometry/Mesh.ispc:67-176): calcEpsilon over the 4 vertices
+    const uint32_t *q = &g.quadIndex[4 * size_t(hit.primID)];
+    const V3 a = g.verts[q[0]], b = g.verts[q[1]], c = g.verts[q[2]], d = g.verts[q[3]];
+    eps = reduce_max(vmax(vmax(vabs(a), vabs(b)), vmax(vabs(c), vabs(d)))) * ulpEpsilon;
+  } else if (g.type == 0) {
     const V3 a = g.verts[g.index[3 * hit.primID]], b = g.verts[g.index[3 * hit.primID + 1]],
              c = g.verts[g.index[3 * hit.primID + 2]];
     eps = reduce_max(vmax(vmax(vabs(a), vabs(b)), vabs(c))) * ulpEpsilon;

@@ -285,12 +285,13 @@ bool traverseBLAS(const Geometry &g, V3 org, V3 dir, float tnear, Hit &hit, uint
       }
       if (!h) continue;
       if (ANY) return true;
-      if (better(t, instID, geomID, p, hit)) {
+      const uint32_t prim = g.type == 0 ? p / g.primDiv : p;  // quads, boxes: the application primitive
+      if (better(t, instID, geomID, prim, hit)) {
         hit.t = t;
         hit.u = u;
         hit.v = v;
         hit.Ng = Ng;
-        hit.primID = p;
+        hit.primID = prim;
         hit.geomID = geomID;
         hit.instID = instID;
         found = true;

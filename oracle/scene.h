@@ -42,6 +42,9 @@ struct Geometry {
   std::vector<Box> boxes;
   std::vector<V3> verts;
   std::vector<uint32_t> index;  // 3 per triangle
+  std::vector<uint32_t> quadIndex;  // quad meshes: 4 per quad; triangle p is half of quad p / 2
+  uint32_t primDiv = 1;  // triangles per application primitive (quads 2, boxes 12): primID = p / primDiv
+  bool boxFaces = false;  // box geometry as face triangles (no geometry epsilon)
   std::vector<V4> spheres;      // center, radius
   // BVH2 (binned SAH)
   struct Node {

@@ -183,6 +183,8 @@ def lib():
             "b200_scene_create": (I, [P, ctypes.POINTER(P)]),
             "b200_scene_release": (I, [P]),
             "b200_scene_add_mesh": (I, [P, P, I64, P, I64, ctypes.POINTER(I)]),
+            "b200_scene_add_quad_mesh": (I, [P, P, I64, P, I64, ctypes.POINTER(I)]),
+            "b200_scene_add_boxes": (I, [P, P, I64, ctypes.POINTER(I)]),
             "b200_scene_add_spheres": (I, [P, P, I64, ctypes.POINTER(I)]),
             "b200_scene_add_instance": (I, [P, I, U32, U32, P, I]),
             "b200_scene_commit": (I, [P]),
@@ -329,6 +331,21 @@ class Scene:
         i = np.ascontiguousarray(index, dtype=np.uint32).reshape(-1, 3)
         g = ctypes.c_int()
         self.device._check(lib().b200_scene_add_mesh(self._h, _ptr(v), len(v), _ptr(i), len(i), ctypes.byref(g)))
+        return g.value
+
+    def add_quad_mesh(self, vertex, index):
+        """index: (n, 4) uint32 quads (Embree's decomposition into two triangles)."""
+        v = np.ascontiguousarray(vertex, dtype=np.float32).reshape(-1, 3)
+        i = np.ascontiguousarray(index, dtype=np.uint32).reshape(-1, 4)
+        g = ctypes.c_int()
+        self.device._check(lib().b200_scene_add_quad_mesh(self._h, _ptr(v), len(v), _ptr(i), len(i), ctypes.byref(g)))
+        return g.value
+
+    def add_boxes(self, boxes):
+        """boxes: (n, 6) float32 (lower xyz, upper xyz)."""
+        b = np.ascontiguousarray(boxes, dtype=np.float32).reshape(-1, 6)
+        g = ctypes.c_int()
+        self.device._check(lib().b200_scene_add_boxes(self._h, _ptr(b), len(b), ctypes.byref(g)))
         return g.value
 
     def add_spheres(self, xyzr):

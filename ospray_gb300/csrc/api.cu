@@ -288,6 +288,7 @@ SceneObj::~SceneObj() {
     freeBLAS(g.blas, st);
     if (g.dverts) cudaFreeAsync(g.dverts, st);
     if (g.dindex) cudaFreeAsync(g.dindex, st);
+    if (g.dquad) cudaFreeAsync(g.dquad, st);
     if (g.dsph) cudaFreeAsync(g.dsph, st);
   }
   if (tlas.nodes) cudaFreeAsync(tlas.nodes, st);
@@ -311,7 +312,9 @@ void SceneObj::commit() {
   for (auto &g : geoms) {
     if (g.built) continue;
     if (g.type == GEOM_TRIANGLES)
-      check(buildTriangleBLAS(g.dverts, g.dindex, int(g.nprims), st, g.blas, !dynamic), "BLAS build");
+      check(buildTriangleBLAS(g.dverts, g.dindex, int(g.nprims), st, g.blas, !dynamic,
+                              g.meshKind == MESH_QUADS ? 2 : (g.meshKind == MESH_BOXES ? 12 : 1)),
+            "BLAS build");
     else
       check(buildSphereBLAS(g.dsph, int(g.nprims), st, g.blas, !dynamic), "BLAS build");
     g.built = true;
@@ -329,7 +332,8 @@ void SceneObj::commit() {
     d.prims = g.blas.prims;
     d.primIDs = g.blas.primIDs;
     d.verts = g.dverts;
-    d.index = g.dindex;
+    d.index = g.dquad ? g.dquad : g.dindex;
+    d.meshKind = g.meshKind;
     d.spheres = g.dsph;
     d.type = uint32_t(g.type);
     d.instID = e.instID;
@@ -608,6 +612,86 @@ int b200_scene_add_mesh(b200_scene s, const float *vertex, int64_t nverts, const
     if (nverts) check(cudaMemcpyAsync(g.dverts, vertex, 12 * size_t(nverts), cudaMemcpyHostToDevice, st), "upload");
     if (ntris) check(cudaMemcpyAsync(g.dindex, index, 12 * size_t(ntris), cudaMemcpyHostToDevice, st), "upload");
     check(cudaStreamSynchronize(st), "upload mesh");
+    sc->geoms.push_back(g);
+    if (geom_out) *geom_out = int(sc->geoms.size() - 1);
+  });
+}
+
+// A quad (v0, v1, v2, v3) is the triangle pair (v0, v1, v3), (v2, v3, v1),
+// Embree's quad decomposition; both carry the quad's primID.
+int b200_scene_add_quad_mesh(b200_scene s, const float *vertex, int64_t nverts, const uint32_t *index,
+                             int64_t nquads, int *geom_out) {
+  if (!s) return B200_INVALID_ARGUMENT;
+  SceneObj *sc = reinterpret_cast<SceneObj *>(s);
+  return guarded(sc->dev, [&]() {
+    require(nverts >= 0 && nquads >= 0 && (nverts == 0 || vertex) && (nquads == 0 || index), "bad mesh arrays");
+    require(nquads < (int64_t(1) << 30) && nverts < (int64_t(1) << 31), "mesh too large");
+    for (int64_t i = 0; i < 4 * nquads; i++) require(index[i] < uint64_t(nverts), "mesh index out of range");
+    std::vector<uint32_t> tri(size_t(6 * nquads));
+    for (int64_t q = 0; q < nquads; q++) {
+      const uint32_t *v = index + 4 * q;
+      uint32_t *t = tri.data() + 6 * q;
+      t[0] = v[0], t[1] = v[1], t[2] = v[3];
+      t[3] = v[2], t[4] = v[3], t[5] = v[1];
+    }
+    GeomObj g;
+    g.type = GEOM_TRIANGLES;
+    g.meshKind = MESH_QUADS;
+    g.nprims = 2 * nquads;
+    cudaStream_t st = sc->dev->stream;
+    check(cudaMallocAsync(&g.dverts, sizeof(float) * 3 * size_t(nverts > 0 ? nverts : 1), st), "alloc vertices");
+    check(cudaMallocAsync(&g.dindex, sizeof(uint32_t) * 6 * size_t(nquads > 0 ? nquads : 1), st), "alloc index");
+    check(cudaMallocAsync(&g.dquad, sizeof(uint32_t) * 4 * size_t(nquads > 0 ? nquads : 1), st), "alloc index");
+    if (nverts) check(cudaMemcpyAsync(g.dverts, vertex, 12 * size_t(nverts), cudaMemcpyHostToDevice, st), "upload");
+    if (nquads) {
+      check(cudaMemcpyAsync(g.dindex, tri.data(), 24 * size_t(nquads), cudaMemcpyHostToDevice, st), "upload");
+      check(cudaMemcpyAsync(g.dquad, index, 16 * size_t(nquads), cudaMemcpyHostToDevice, st), "upload");
+    }
+    check(cudaStreamSynchronize(st), "upload mesh");
+    sc->geoms.push_back(g);
+    if (geom_out) *geom_out = int(sc->geoms.size() - 1);
+  });
+}
+
+// Boxes::commit (geometry/Boxes.cpp:33-46): each box3f becomes its 8
+// corners and 12 triangles (two per face) carrying the box's primID; a ray
+// hits the first face in [tnear, tfar], the exit face when it starts inside,
+// as intersectBox + filterIntersectionBoth (common/Intersect.ih:195-223).
+int b200_scene_add_boxes(b200_scene s, const float *boxes, int64_t n, int *geom_out) {
+  if (!s) return B200_INVALID_ARGUMENT;
+  SceneObj *sc = reinterpret_cast<SceneObj *>(s);
+  return guarded(sc->dev, [&]() {
+    require(n >= 0 && (n == 0 || boxes) && n < (int64_t(1) << 26), "bad box array");
+    std::vector<float> v(size_t(24 * n));
+    std::vector<uint32_t> tri(size_t(36 * n));
+    // faces as corner quads; corner c = (x: c & 1, y: c >> 1 & 1, z: c >> 2)
+    static const int F[6][4] = {{0, 4, 6, 2}, {1, 3, 7, 5}, {0, 1, 5, 4}, {2, 6, 7, 3}, {0, 2, 3, 1}, {4, 5, 7, 6}};
+    for (int64_t b = 0; b < n; b++) {
+      const float *lo = boxes + 6 * b, *hi = lo + 3;
+      for (int c = 0; c < 8; c++) {
+        v[size_t(24 * b + 3 * c + 0)] = (c & 1) ? hi[0] : lo[0];
+        v[size_t(24 * b + 3 * c + 1)] = (c & 2) ? hi[1] : lo[1];
+        v[size_t(24 * b + 3 * c + 2)] = (c & 4) ? hi[2] : lo[2];
+      }
+      for (int f = 0; f < 6; f++) {
+        uint32_t *t = tri.data() + 36 * b + 6 * f;
+        const uint32_t o = uint32_t(8 * b);
+        t[0] = o + F[f][0], t[1] = o + F[f][1], t[2] = o + F[f][2];
+        t[3] = o + F[f][0], t[4] = o + F[f][2], t[5] = o + F[f][3];
+      }
+    }
+    GeomObj g;
+    g.type = GEOM_TRIANGLES;
+    g.meshKind = MESH_BOXES;
+    g.nprims = 12 * n;
+    cudaStream_t st = sc->dev->stream;
+    check(cudaMallocAsync(&g.dverts, sizeof(float) * 24 * size_t(n > 0 ? n : 1), st), "alloc vertices");
+    check(cudaMallocAsync(&g.dindex, sizeof(uint32_t) * 36 * size_t(n > 0 ? n : 1), st), "alloc index");
+    if (n) {
+      check(cudaMemcpyAsync(g.dverts, v.data(), 96 * size_t(n), cudaMemcpyHostToDevice, st), "upload");
+      check(cudaMemcpyAsync(g.dindex, tri.data(), 144 * size_t(n), cudaMemcpyHostToDevice, st), "upload");
+    }
+    check(cudaStreamSynchronize(st), "upload boxes");
     sc->geoms.push_back(g);
     if (geom_out) *geom_out = int(sc->geoms.size() - 1);
   });

@@ -52,9 +52,11 @@ struct DeviceObj {
 
 struct GeomObj {
   int type = GEOM_TRIANGLES;
-  int64_t nprims = 0;
+  int64_t nprims = 0;  // BLAS primitives (a quad mesh: two triangles per quad)
   float *dverts = nullptr;
-  uint32_t *dindex = nullptr;
+  uint32_t *dindex = nullptr;  // 3 per BLAS triangle
+  uint32_t *dquad = nullptr;   // quad meshes: the 4 indices per quad (postIntersect)
+  uint32_t meshKind = MESH_TRIANGLES;
   float4 *dsph = nullptr;
   BLAS blas;
   bool built = false;

@@ -623,13 +623,14 @@ __global__ void k_collapse(const Task *tasks, int ntasks, Task *next, uint32_t *
   nodes[task.wide] = node;
 }
 
+// triangle p belongs to primitive p / primDiv (quads 2, boxes 12), its primID
 __global__ void k_gather_tris(const uint32_t *leafPrim, int n, const float *verts, const uint32_t *index,
-                              float4 *prims) {
+                              float4 *prims, uint32_t primDiv) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n) return;
   const uint32_t p = leafPrim[s];
   const uint32_t a = index[3 * p], b = index[3 * p + 1], c = index[3 * p + 2];
-  prims[3 * s + 0] = make_float4(verts[3 * a], verts[3 * a + 1], verts[3 * a + 2], __uint_as_float(p));
+  prims[3 * s + 0] = make_float4(verts[3 * a], verts[3 * a + 1], verts[3 * a + 2], __uint_as_float(p / primDiv));
   prims[3 * s + 1] = make_float4(verts[3 * b], verts[3 * b + 1], verts[3 * b + 2], 0.f);
   prims[3 * s + 2] = make_float4(verts[3 * c], verts[3 * c + 1], verts[3 * c + 2], 0.f);
 }
@@ -783,7 +784,7 @@ cudaError_t buildWide(const float4 *lo, const float4 *hi, int n, cudaStream_t st
 }
 
 cudaError_t buildTriangleBLAS(const float *d_verts, const uint32_t *d_index, int ntris, cudaStream_t st, BLAS &out,
-                              bool sah) {
+                              bool sah, int primDiv) {
   out = BLAS{};
   if (ntris <= 0) return cudaSuccess;
   float4 *lo, *hi;
@@ -793,7 +794,8 @@ cudaError_t buildTriangleBLAS(const float *d_verts, const uint32_t *d_index, int
   k_tri_bounds<<<blocks(ntris, 256), 256, 0, st>>>(d_verts, d_index, ntris, lo, hi);
   if ((err = buildWide(lo, hi, ntris, st, out.bvh, sah))) return err;
   if ((err = cudaMallocAsync(&out.prims, sizeof(float4) * 3 * size_t(ntris), st))) return err;
-  k_gather_tris<<<blocks(ntris, 256), 256, 0, st>>>(out.bvh.leafPrim, ntris, d_verts, d_index, out.prims);
+  k_gather_tris<<<blocks(ntris, 256), 256, 0, st>>>(out.bvh.leafPrim, ntris, d_verts, d_index, out.prims,
+                                                    uint32_t(primDiv));
   cudaFreeAsync(lo, st);
   cudaFreeAsync(hi, st);
   return cudaStreamSynchronize(st);

@@ -21,8 +21,10 @@ struct BLAS {
 // build quality); false: the plain LBVH hierarchy (fastest build, the
 // reference's dynamicScene)
 cudaError_t buildWide(const float4 *lo, const float4 *hi, int n, cudaStream_t st, WideBVH &out, bool sah = true);
+// primDiv: BLAS triangles per application primitive (primID = triangle /
+// primDiv): 1 triangles, 2 quads, 12 boxes
 cudaError_t buildTriangleBLAS(const float *d_verts, const uint32_t *d_index, int ntris, cudaStream_t st, BLAS &out,
-                              bool sah = true);
+                              bool sah = true, int primDiv = 1);
 cudaError_t buildSphereBLAS(const float4 *d_sph, int n, cudaStream_t st, BLAS &out, bool sah = true);
 void freeBLAS(BLAS &b, cudaStream_t st);
 

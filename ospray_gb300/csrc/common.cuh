@@ -122,18 +122,24 @@ enum GeomType : uint32_t { GEOM_TRIANGLES = 0, GEOM_SPHERES = 1 };
 
 // One (instance, geometric model) pair of the world: the unit the TLAS is
 // built over.  BLAS arrays are shared between entries of the same geometry.
+// How a triangle BLAS maps to the application's primitives: plain triangles;
+// quads (each two BLAS triangles, primID = triangle / 2, index 4 per quad);
+// boxes (each twelve BLAS triangles, primID = triangle / 12, no index).
+constexpr uint32_t MESH_TRIANGLES = 0, MESH_QUADS = 1, MESH_BOXES = 2;
+
 struct Entry {
   const Node8 *nodes;        // BLAS nodes (root at 0)
   const float4 *prims;       // triangles: 3 float4 (v0+primID bits, v1, v2); spheres: 1 float4
   const uint32_t *primIDs;   // spheres only: primID per leaf slot
   const float *verts;        // original vertex array (xyz per vertex) for postIntersect
-  const uint32_t *index;     // original index array (3 per triangle)
+  const uint32_t *index;     // original index array (3 per triangle; 4 per quad for MESH_QUADS)
   const float4 *spheres;     // original sphere array
   uint32_t type, instID, geomID, identity;
   Xfm xfm, rcp;
   float epsScale;            // max |diag(xfm.l)|
   uint32_t materialID;       // per-entry material slot (renderers)
-  uint32_t pad[2];
+  uint32_t meshKind;         // triangles: MESH_TRIANGLES, MESH_QUADS or MESH_BOXES
+  uint32_t pad;
 };
 
 }  // namespace b200

@@ -20,18 +20,24 @@ struct Params {
 };
 
 constexpr int LAYER_OUT_OFF = HIDDEN * WIDTH * WIDTH;  // offset of the output layer (64 x 16)
+constexpr int W_ROWS = NUM_W / WIDTH;                 // rows of 64 in the [out][in] weights
 constexpr int WARPS = 4;                              // warps per block of the fused kernels
-constexpr int XS = WIDTH;                             // row stride of the activation tiles
+constexpr int XS = WIDTH;                             // row stride of the training kernel's activation tiles
+// The inference kernel pads its shared-memory rows (weights and the input
+// tile) to 72 BF16 (144 B): rows 64 wide (128 B) put the 8 rows an m16n8k16
+// fragment load reads into one bank (8-way conflicts); 144-byte rows shift
+// each row by 4 banks.
+constexpr int XI = WIDTH + 8;                         // inference: row stride of weights and input tile
 
 namespace {
 
 // ---------------------------------------------------------------- encoding
 // One warp encodes its 16 samples: lanes 0-15 the hash grid of sample `lane`,
 // lanes 16-31 the other inputs of sample `lane - 16`.
-B200_D void encodeTile(const Params &P, const float *rec, bool valid, __nv_bfloat16 *X, int lane) {
+B200_D void encodeTile(const Params &P, const float *rec, bool valid, __nv_bfloat16 *X, int ldx, int lane) {
   const int s = lane & 15;
   const float *r = rec + s * REC;
-  __nv_bfloat16 *row = X + s * XS;
+  __nv_bfloat16 *row = X + s * ldx;
   if (lane < 16) {
     for (int l = 0; l < LEVELS; l++) {
       float f0 = 0.f, f1 = 0.f;
@@ -69,7 +75,8 @@ B200_D void encodeTile(const Params &P, const float *rec, bool valid, __nv_bfloa
 // ---------------------------------------------------------------- forward
 // Runs the hidden layers on the A operand a[4][4] (replaced by the last
 // hidden activation); with `store`, writes every hidden activation H_1..H_4
-// (BF16, after ReLU) to H + (l * 16 * XS).
+// (BF16, after ReLU) to H + (l * 16 * XS).  LDW: the row stride of wt.
+template <int LDW>
 B200_D void hiddenLayers(const Params &P, const __nv_bfloat16 *wt, uint32_t a[4][4], __nv_bfloat16 *H, bool store,
                          int lane) {
   const int g = lane >> 2, t = lane & 3;
@@ -79,7 +86,7 @@ B200_D void hiddenLayers(const Params &P, const __nv_bfloat16 *wt, uint32_t a[4]
       c[j][0] = c[j][1] = c[j][2] = c[j][3] = 0.f;
       for (int kk = 0; kk < 4; kk++) {
         uint32_t b0, b1;
-        loadBT(wt + l * WIDTH * WIDTH, WIDTH, kk, j, lane, b0, b1);
+        loadBT(wt + l * WIDTH * LDW, LDW, kk, j, lane, b0, b1);
         mma16816(c[j], a[kk], b0, b1);
       }
     }
@@ -100,12 +107,13 @@ B200_D void hiddenLayers(const Params &P, const __nv_bfloat16 *wt, uint32_t a[4]
 }
 
 // output layer: o[j] accumulators of n-tile j (columns 8j..8j+7; 0..2 used)
+template <int LDW>
 B200_D void outputLayer(const __nv_bfloat16 *wt, const uint32_t a[4][4], float o[2][4], int lane) {
   for (int j = 0; j < 2; j++) {
     o[j][0] = o[j][1] = o[j][2] = o[j][3] = 0.f;
     for (int kk = 0; kk < 4; kk++) {
       uint32_t b0, b1;
-      loadBT(wt + LAYER_OUT_OFF, WIDTH, kk, j, lane, b0, b1);
+      loadBT(wt + HIDDEN * WIDTH * LDW, LDW, kk, j, lane, b0, b1);
       mma16816(o[j], a[kk], b0, b1);
     }
   }
@@ -124,10 +132,13 @@ __global__ void __launch_bounds__(WARPS * 32) k_nrc_infer(Params P, const float 
   extern __shared__ __align__(16) unsigned char smem[];
   __nv_bfloat16 *wt = reinterpret_cast<__nv_bfloat16 *>(smem);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  float *rec = reinterpret_cast<float *>(smem + NUM_W * 2) + warp * 16 * REC;
-  __nv_bfloat16 *X = reinterpret_cast<__nv_bfloat16 *>(smem + NUM_W * 2 + WARPS * 16 * REC * 4) + warp * 16 * XS;
-  for (int i = threadIdx.x; i < NUM_W / 2; i += blockDim.x)
-    reinterpret_cast<uint32_t *>(wt)[i] = reinterpret_cast<const uint32_t *>(P.wt)[i];
+  float *rec = reinterpret_cast<float *>(smem + W_ROWS * XI * 2) + warp * 16 * REC;
+  __nv_bfloat16 *X = reinterpret_cast<__nv_bfloat16 *>(smem + W_ROWS * XI * 2 + WARPS * 16 * REC * 4) + warp * 16 * XI;
+  // the [out][in] weights, rows of 64 padded to XI
+  for (int i = threadIdx.x; i < NUM_W / 2; i += blockDim.x) {
+    const int row = (2 * i) / WIDTH, col = (2 * i) % WIDTH;
+    reinterpret_cast<uint32_t *>(wt)[(row * XI + col) / 2] = reinterpret_cast<const uint32_t *>(P.wt)[i];
+  }
   __syncthreads();
   const long long tiles = (n + 15) / 16;
   for (long long tile = blockIdx.x * (long long)WARPS + warp; tile < tiles; tile += (long long)gridDim.x * WARPS) {
@@ -137,13 +148,13 @@ __global__ void __launch_bounds__(WARPS * 32) k_nrc_infer(Params P, const float 
       rec[k] = i < n ? q[i * REC + k % REC] : 0.f;
     }
     __syncwarp();
-    encodeTile(P, rec, base + (lane & 15) < n, X, lane);
+    encodeTile(P, rec, base + (lane & 15) < n, X, XI, lane);
     __syncwarp();
     uint32_t a[4][4];
-    for (int kk = 0; kk < 4; kk++) loadA(X, XS, kk, lane, a[kk]);
-    hiddenLayers(P, wt, a, nullptr, false, lane);
+    for (int kk = 0; kk < 4; kk++) loadA(X, XI, kk, lane, a[kk]);
+    hiddenLayers<XI>(P, wt, a, nullptr, false, lane);
     float o[2][4];
-    outputLayer(wt, a, o, lane);
+    outputLayer<XI>(wt, a, o, lane);
     const int g = lane >> 2, t = lane & 3;
     for (int h = 0; h < 2; h++) {
       const long long i = base + g + 8 * h;
@@ -239,13 +250,13 @@ __global__ void __launch_bounds__(WARPS * 32) k_nrc_train(Params P, const float 
       rec[k] = i < n ? samples[i * REC + k % REC] : 0.f;
     }
     __syncwarp();
-    encodeTile(P, rec, base + (lane & 15) < n, X, lane);
+    encodeTile(P, rec, base + (lane & 15) < n, X, XS, lane);
     __syncwarp();
     uint32_t a[4][4];
     for (int kk = 0; kk < 4; kk++) loadA(X, XS, kk, lane, a[kk]);
-    hiddenLayers(P, wt, a, H, true, lane);
+    hiddenLayers<WIDTH>(P, wt, a, H, true, lane);
     float o[2][4];
-    outputLayer(wt, a, o, lane);
+    outputLayer<WIDTH>(wt, a, o, lane);
     // loss gradient (columns 0..2 of n-tile 0), staged as dOut 16 x 16
     float d[4];
     for (int q = 0; q < 4; q++) {
@@ -325,7 +336,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_nrc_train(Params P, const float 
     if (dWs[i] != 0.f) atomicAdd(wgrad + i, dWs[i]);
 }
 
-constexpr size_t kInferSmem = size_t(NUM_W) * 2 + WARPS * 16 * REC * 4 + WARPS * 16 * XS * 2;
+constexpr size_t kInferSmem = size_t(W_ROWS) * XI * 2 + WARPS * 16 * REC * 4 + WARPS * 16 * XI * 2;
 constexpr size_t kTrainSmem = size_t(NUM_W) * 2 * 2 + size_t(NUM_W) * 4 +
                               WARPS * (16 * REC * 4 + 5 * 16 * XS * 2 + 16 * XS * 2 + 16 * 16 * 2);
 static_assert(kTrainSmem <= 227 * 1024, "training kernel shared memory");

@@ -34,6 +34,7 @@ void GeometryObj::commit(B200Device &) {
   verts.clear();
   index.clear();
   spheres.clear();
+  boxes.clear();
   if (type == "mesh") {
     DataObj *v = getData("vertex.position");
     DataObj *ix = getData("index");
@@ -42,15 +43,22 @@ void GeometryObj::commit(B200Device &) {
     verts.resize(v->count() * 3);
     std::memcpy(verts.data(), vb.data(), vb.size());
     if (!ix) throw Error(OSP_INVALID_ARGUMENT, "mesh: 'index' data is required");
-    if (ix->elem == OSP_VEC4UI || ix->elem == OSP_VEC4I)
-      throw Error(OSP_INVALID_ARGUMENT, "mesh: quad indices (vec4ui) are not supported by the b200 device");
-    if (ix->elem != OSP_VEC3UI && ix->elem != OSP_VEC3I)
-      throw Error(OSP_INVALID_ARGUMENT, "mesh: 'index' must be vec3ui data");
+    // Mesh::commit (geometry/Mesh.cpp:114-145): vec3ui triangles or vec4ui quads
+    quads = ix->elem == OSP_VEC4UI || ix->elem == OSP_VEC4I;
+    if (!quads && ix->elem != OSP_VEC3UI && ix->elem != OSP_VEC3I)
+      throw Error(OSP_INVALID_ARGUMENT, "mesh: 'index' must be vec3ui or vec4ui data");
     const auto ib = ix->compact();
-    index.resize(ix->count() * 3);
+    index.resize(ix->count() * (quads ? 4 : 3));
     std::memcpy(index.data(), ib.data(), ib.size());
     for (uint32_t i : index)
       if (i >= v->count()) throw Error(OSP_INVALID_ARGUMENT, "mesh: index out of range of 'vertex.position'");
+  } else if (type == "box") {
+    // Boxes::commit (geometry/Boxes.cpp:33-46): "box" data of box3f
+    DataObj *b = getData("box");
+    if (!b || b->elem != OSP_BOX3F) throw Error(OSP_INVALID_ARGUMENT, "box: 'box' must be box3f data");
+    const auto bb = b->compact();
+    boxes.resize(b->count() * 6);
+    std::memcpy(boxes.data(), bb.data(), bb.size());
   } else {  // sphere
     DataObj *p = getData("sphere.position");
     if (!p || p->elem != OSP_VEC3F) throw Error(OSP_INVALID_ARGUMENT, "sphere: 'sphere.position' must be vec3f data");
@@ -80,6 +88,12 @@ void GeometryObj::bounds(float lo[3], float hi[3]) const {
       for (int k = 0; k < 3; k++) {
         lo[k] = std::fmin(lo[k], verts[3 * i + k]);
         hi[k] = std::fmax(hi[k], verts[3 * i + k]);
+      }
+  } else if (type == "box") {
+    for (size_t i = 0; 6 * i < boxes.size(); i++)
+      for (int k = 0; k < 3; k++) {
+        lo[k] = std::fmin(lo[k], boxes[6 * i + k]);
+        hi[k] = std::fmax(hi[k], boxes[6 * i + 3 + k]);
       }
   } else {
     for (size_t i = 0; 4 * i < spheres.size(); i++)
@@ -300,9 +314,14 @@ void WorldObj::commit(B200Device &dev) {
         auto it = geomIndex.find(g);
         int gi;
         if (it == geomIndex.end()) {
-          if (g->type == "mesh")
+          if (g->type == "mesh" && g->quads)
+            dev.check(b200_scene_add_quad_mesh(s, g->verts.data(), int64_t(g->verts.size() / 3), g->index.data(),
+                                               int64_t(g->index.size() / 4), &gi));
+          else if (g->type == "mesh")
             dev.check(b200_scene_add_mesh(s, g->verts.data(), int64_t(g->verts.size() / 3), g->index.data(),
                                           int64_t(g->index.size() / 3), &gi));
+          else if (g->type == "box")
+            dev.check(b200_scene_add_boxes(s, g->boxes.data(), int64_t(g->boxes.size() / 6), &gi));
           else
             dev.check(b200_scene_add_spheres(s, g->spheres.data(), int64_t(g->spheres.size() / 4), &gi));
           geomIndex[g] = gi;

@@ -26,8 +26,10 @@ struct SceneObj : Obj {
 struct GeometryObj : SceneObj {
   using SceneObj::SceneObj;
   std::vector<float> verts;     // mesh: xyz per vertex
-  std::vector<uint32_t> index;  // mesh: 3 per triangle
+  std::vector<uint32_t> index;  // mesh: 3 per triangle, or 4 per quad when quads
+  bool quads = false;           // mesh with a vec4ui "index"
   std::vector<float> spheres;   // sphere: xyzr per sphere
+  std::vector<float> boxes;     // box: lower xyz, upper xyz per box
   void commit(B200Device &) override;
   void bounds(float lo[3], float hi[3]) const;
 };

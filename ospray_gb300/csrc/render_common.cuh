@@ -108,7 +108,18 @@ B200_D DG postIntersect(const Scene &sc, const Ray &ray, const HitRec &hit) {
   dg.P = add(ray.org, mul(hit.t, ray.dir));
   V3 Ng = hit.Ng, Ns = hit.Ng;
   float eps;
-  if (e.type == GEOM_TRIANGLES) {
+  if (e.type == GEOM_TRIANGLES && e.meshKind == MESH_BOXES) {
+    eps = 0.f;  // Boxes_postIntersect (geometry/Boxes.ispc) sets no geometry epsilon
+  } else if (e.type == GEOM_TRIANGLES && e.meshKind == MESH_QUADS) {
+    // QuadMesh_postIntersect (geometry/Mesh.ispc:67-176): epsilon over the 4 vertices
+    const uint4 q = __ldg(reinterpret_cast<const uint4 *>(e.index) + hit.primID);
+    const uint32_t ix[4] = {q.x, q.y, q.z, q.w};
+    V3 m = splat(0.f);
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+      m = vmax(m, vabs(mk(__ldg(e.verts + 3 * ix[k]), __ldg(e.verts + 3 * ix[k] + 1), __ldg(e.verts + 3 * ix[k] + 2))));
+    eps = fmul(reduce_max(m), ULP_EPSILON);
+  } else if (e.type == GEOM_TRIANGLES) {
     const uint32_t i0 = __ldg(e.index + 3 * hit.primID), i1 = __ldg(e.index + 3 * hit.primID + 1),
                    i2 = __ldg(e.index + 3 * hit.primID + 2);
     const V3 a = mk(__ldg(e.verts + 3 * i0), __ldg(e.verts + 3 * i0 + 1), __ldg(e.verts + 3 * i0 + 2));

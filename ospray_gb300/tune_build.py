@@ -7,8 +7,8 @@ resident blocks per SM of the trace kernels (B200_TRACE_MINBLOCKS) and of the
 path-tracer shade kernel (B200_SHADE_MINBLOCKS), which bound their registers,
 are compile-time constants, so each candidate is a separate
 build of libb200.so (into ospray_gb300/_variants/<tag>).  Each build renders
-the path-tracing workload at 960x540, 8 spp (bench.py, 3 warm-up frames and
-5 timed frames) on the GPU, and the fastest candidate's defines are written
+the path-tracing workload at 1920x1080, 16 spp (bench.py, 3 warm-up frames
+and 5 timed frames) on the GPU, and the fastest candidate's defines are written
 to tuned.json, which build.py then compiles with.  The run-time launch shape
 of batches is tuned separately (b200_batch_autotune).
 """
@@ -22,10 +22,13 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 
 CANDIDATES = [
-    {"B200_STACK_SMEM": 16, "B200_TRACE_MINBLOCKS": 6, "B200_SHADE_MINBLOCKS": 2},
-    {"B200_STACK_SMEM": 16, "B200_TRACE_MINBLOCKS": 6, "B200_SHADE_MINBLOCKS": 3},
     {"B200_STACK_SMEM": 16, "B200_TRACE_MINBLOCKS": 6, "B200_SHADE_MINBLOCKS": 4},
-    {"B200_STACK_SMEM": 16, "B200_TRACE_MINBLOCKS": 5, "B200_SHADE_MINBLOCKS": 3},
+    {"B200_STACK_SMEM": 16, "B200_TRACE_MINBLOCKS": 7, "B200_SHADE_MINBLOCKS": 4},
+    {"B200_STACK_SMEM": 16, "B200_TRACE_MINBLOCKS": 8, "B200_SHADE_MINBLOCKS": 4},
+    {"B200_STACK_SMEM": 12, "B200_TRACE_MINBLOCKS": 8, "B200_SHADE_MINBLOCKS": 4},
+    {"B200_STACK_SMEM": 16, "B200_TRACE_MINBLOCKS": 7, "B200_SHADE_MINBLOCKS": 5},
+    {"B200_STACK_SMEM": 16, "B200_TRACE_MINBLOCKS": 8, "B200_SHADE_MINBLOCKS": 5},
+    {"B200_STACK_SMEM": 12, "B200_TRACE_MINBLOCKS": 7, "B200_SHADE_MINBLOCKS": 4},
 ]
 
 
@@ -51,8 +54,8 @@ def measure(c, size, spp):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", default=os.path.join(HERE, "tuned.json"))
-    ap.add_argument("--size", default="960x540")
-    ap.add_argument("--spp", type=int, default=8)
+    ap.add_argument("--size", default="1920x1080")
+    ap.add_argument("--spp", type=int, default=16)
     args = ap.parse_args()
     results = []
     for c in CANDIDATES:

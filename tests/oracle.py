@@ -126,6 +126,8 @@ def lib():
         L.or_scene_new.restype = P
         L.or_scene_free.argtypes = [P]
         L.or_scene_add_mesh.argtypes = [P, P, I, P, I]
+        L.or_scene_add_quad_mesh.argtypes = [P, P, I, P, I]
+        L.or_scene_add_boxes.argtypes = [P, P, I]
         L.or_scene_add_spheres.argtypes = [P, P, I]
         L.or_scene_add_instance.argtypes = [P, I, U32, U32, P, I]
         L.or_pt_new.restype = P
@@ -180,6 +182,15 @@ class Scene:
         v = np.ascontiguousarray(vertex, np.float32)
         i = np.ascontiguousarray(index, np.uint32)
         return lib().or_scene_add_mesh(self.h, _p(v), len(v), _p(i), len(i))
+
+    def add_quad_mesh(self, vertex, index):
+        v = np.ascontiguousarray(vertex, np.float32)
+        i = np.ascontiguousarray(index, np.uint32).reshape(-1, 4)
+        return lib().or_scene_add_quad_mesh(self.h, _p(v), len(v), _p(i), len(i))
+
+    def add_boxes(self, boxes):
+        b = np.ascontiguousarray(boxes, np.float32).reshape(-1, 6)
+        return lib().or_scene_add_boxes(self.h, _p(b), len(b))
 
     def add_spheres(self, xyzr):
         s = np.ascontiguousarray(xyzr, np.float32)

@@ -173,3 +173,88 @@ def test_oracle_volume_gradient_shading_invariants():
     assert plain[..., 3].max() > 0.3
     assert np.abs(shaded[..., 3] - plain[..., 3]).max() < 1e-5
     assert shaded[..., :3].mean() < plain[..., :3].mean()
+
+
+def _heightfield_quads(n=24, seed=3):
+    rng = np.random.default_rng(seed)
+    xs = np.linspace(0.0, 1.0, n, dtype=np.float32)
+    X, Z = np.meshgrid(xs, xs)
+    Y = (0.08 * np.sin(7.0 * X + 1.3) * np.cos(5.0 * Z) + 0.01 * rng.standard_normal(X.shape)).astype(np.float32)
+    v = np.stack([X, Y, Z], -1).reshape(-1, 3)
+    i, j = np.meshgrid(np.arange(n - 1), np.arange(n - 1))
+    a = (j * n + i).ravel()
+    q = np.stack([a, a + 1, a + n + 1, a + n], 1).astype(np.uint32)
+    return v, q
+
+
+def test_oracle_quad_mesh_is_embree_triangle_pair():
+    """A quad (v0, v1, v2, v3) traces as the triangles (v0, v1, v3) and
+    (v2, v3, v1), Embree's quad decomposition, and reports the quad's index:
+    hit t bit for bit and primID = triangle // 2 against the same mesh given
+    as triangles."""
+    v, q = _heightfield_quads()
+    tri = np.stack([q[:, 0], q[:, 1], q[:, 3], q[:, 2], q[:, 3], q[:, 1]], 1).reshape(-1, 3)
+    sq, st = oracle.Scene(), oracle.Scene()
+    sq.add_instance(sq.add_quad_mesh(v, q), 0, 0)
+    st.add_instance(st.add_mesh(v, tri), 0, 0)
+    sq.commit()
+    st.commit()
+    rng = np.random.default_rng(1)
+    n = 20000
+    org = np.concatenate([rng.uniform(0, 1, (n, 1)), np.full((n, 1), 0.8), rng.uniform(0, 1, (n, 1))], 1)
+    d = np.concatenate([rng.normal(0, 0.3, (n, 1)), -np.ones((n, 1)), rng.normal(0, 0.3, (n, 1))], 1)
+    rays = np.concatenate([org, np.zeros((n, 1)), d, np.full((n, 1), np.inf)], 1).astype(np.float32)
+    fq, iq = sq.trace(rays)
+    ft, it = st.trace(rays)
+    hit = np.isfinite(ft[:, 0])
+    assert hit.mean() > 0.5
+    np.testing.assert_array_equal(fq[:, 0].view(np.uint32), ft[:, 0].view(np.uint32))
+    assert np.array_equal(iq[hit, 0], it[hit, 0] // 2)
+
+
+def _random_boxes(n=60, seed=4):
+    rng = np.random.default_rng(seed)
+    c = rng.uniform(0.0, 1.0, (n, 3))
+    h = rng.uniform(0.01, 0.08, (n, 3))
+    return np.concatenate([c - h, c + h], 1).astype(np.float32)
+
+
+def test_oracle_boxes_match_slab_test():
+    """Boxes traced as face triangles report the box hit of intersectBox +
+    filterIntersectionBoth (common/Intersect.ih:195-223, FilterIntersect.ih:
+    107-116): the entry face in range, else the exit face; checked against a
+    float64 slab test (t within 1e-5 relative, primID = box index, the
+    normal along the face's axis) away from edges."""
+    b = _random_boxes()
+    s = oracle.Scene()
+    s.add_instance(s.add_boxes(b), 0, 0)
+    s.commit()
+    rng = np.random.default_rng(7)
+    n = 20000
+    org = rng.uniform(-0.2, 1.2, (n, 3))
+    inside = rng.integers(0, len(b), 500)
+    org[:500] = (b[inside, :3] + b[inside, 3:]) / 2  # rays starting inside a box hit its exit face
+    d = rng.normal(size=(n, 3))
+    rays = np.concatenate([org, np.zeros((n, 1)), d, np.full((n, 1), np.inf)], 1).astype(np.float32)
+    f, ids = s.trace(rays)
+    o64, d64 = org.astype(np.float32).astype(np.float64), d.astype(np.float32).astype(np.float64)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        t0 = (b[None, :, :3] - o64[:, None]) / d64[:, None]
+        t1 = (b[None, :, 3:] - o64[:, None]) / d64[:, None]
+    tn, tf = np.minimum(t0, t1).max(2), np.maximum(t0, t1).min(2)
+    ok = tn < tf
+    t = np.where(ok & (tn >= 0), tn, np.where(ok & (tf >= 0), tf, np.inf))
+    best = t.min(1)
+    prim = t.argmin(1)
+    # skip near-ties between boxes and grazing rays
+    srt = np.sort(t, 1)
+    with np.errstate(invalid="ignore"):
+        clear = (srt[:, 1] - srt[:, 0] > 1e-4 * np.maximum(1.0, srt[:, 0])) | ~np.isfinite(srt[:, 1])
+    hit = np.isfinite(best)
+    assert hit[clear].sum() > 2000 and hit[:500].all()
+    m = clear & hit
+    np.testing.assert_allclose(f[m, 0], best[m], rtol=1e-5)
+    assert np.mean(ids[m, 0] == prim[m]) > 0.999
+    assert np.all(~np.isfinite(f[clear & ~hit, 0]))
+    ng = f[m, 3:6]
+    assert np.all(np.sum(np.abs(ng) > 0, 1) == 1)  # axis-aligned face normals
