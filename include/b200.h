@@ -232,13 +232,23 @@ typedef struct {
  *      lights/Light.cpp:22-35).  radiance = color * intensity (the default
  *      intensityQuantity of both).  The list order is the light index order of
  *      the path tracer's light CDF (render/pathtracer/PathTracerData.cpp:32-82). */
-enum { B200_LIGHT_QUAD = 0, B200_LIGHT_AMBIENT = 1 };
+enum { B200_LIGHT_QUAD = 0, B200_LIGHT_AMBIENT = 1, B200_LIGHT_DISTANT = 2, B200_LIGHT_SPHERE = 3 };
+/* distant (DirectionalLight::commit lights/DirectionalLight.cpp:77-105):
+ *   `direction` the light travels, `angularDiameter` in degrees (clamped to
+ *   [0, 180]); irradiance = color * intensity (intensityQuantity IRRADIANCE).
+ * sphere (PointLight::commit lights/PointLight.cpp:68-121): `position`,
+ *   `radius` (0: a point light); radiative intensity = color * intensity
+ *   (intensityQuantity INTENSITY), radiance = that / (pi radius^2).
+ * Unused fields are ignored; zero-initialise the struct. */
 typedef struct {
   int type;
   int visible;
   float position[3], edge1[3], edge2[3];
   float color[3];
   float intensity;
+  float direction[3];
+  float angularDiameter;
+  float radius;
 } b200_light;
 int b200_scene_set_lights(b200_scene scene, const b200_light *lights, int n);
 

@@ -23,9 +23,11 @@ struct PtParams {
 };
 
 struct PtLights {
-  std::vector<int> kind;  // 0 quad, 1 ambient
+  std::vector<int> kind;  // 0 quad, 1 ambient, 2 distant, 3 sphere
   std::vector<QuadLight> quads;
   std::vector<AmbientLight> ambients;
+  std::vector<DistantLight> distants;
+  std::vector<SphereLight> spheres;
   std::vector<int> index;
   std::vector<float> cdf;
   void finalize() {
@@ -37,12 +39,29 @@ struct PtLights {
     for (auto &c : cdf) c = c >= sum ? 0x1.000002p+0f : c * r;
   }
   LightSample sample(int i, const DG &dg, V2 s) const {
-    return kind[i] == 0 ? quads[index[i]].sample(dg, s) : ambients[index[i]].sample(dg, s);
+    switch (kind[i]) {
+      case 0: return quads[index[i]].sample(dg, s);
+      case 2: return distants[index[i]].sample(dg, s);
+      case 3: return spheres[index[i]].sample(dg, s);
+      default: return ambients[index[i]].sample(dg, s);
+    }
   }
   LightEval eval(int i, const DG &dg, V3 dir, float lo, float hi) const {
-    return kind[i] == 0 ? quads[index[i]].eval(dg, dir, lo, hi) : ambients[index[i]].eval(dg, dir, lo, hi);
+    switch (kind[i]) {
+      case 0: return quads[index[i]].eval(dg, dir, lo, hi);
+      case 2: return distants[index[i]].eval(dg, dir, lo, hi);
+      case 3: return spheres[index[i]].eval(dg, dir, lo, hi);
+      default: return ambients[index[i]].eval(dg, dir, lo, hi);
+    }
   }
-  bool visible(int i) const { return kind[i] == 0 ? quads[index[i]].visible : ambients[index[i]].visible; }
+  bool visible(int i) const {
+    switch (kind[i]) {
+      case 0: return quads[index[i]].visible;
+      case 2: return distants[index[i]].visible;
+      case 3: return spheres[index[i]].visible;
+      default: return ambients[index[i]].visible;
+    }
+  }
 };
 
 namespace {
@@ -299,6 +318,27 @@ void or_pt_add_ambient_light(void *p, const float *radiance) {
   s.lights.kind.push_back(1);
   s.lights.index.push_back(int(s.lights.ambients.size()));
   s.lights.ambients.push_back({{radiance[0], radiance[1], radiance[2]}, true});
+  s.lights.finalize();
+}
+
+// direction the light travels, angular diameter (degrees), irradiance rgb
+void or_pt_add_distant_light(void *p, const float *direction, float angularDiameter, const float *irradiance) {
+  OrPtScene &s = *static_cast<OrPtScene *>(p);
+  DistantLight d;
+  d.init({direction[0], direction[1], direction[2]}, angularDiameter, {irradiance[0], irradiance[1], irradiance[2]});
+  s.lights.kind.push_back(2);
+  s.lights.index.push_back(int(s.lights.distants.size()));
+  s.lights.distants.push_back(d);
+  s.lights.finalize();
+}
+// centre, radius, radiative intensity rgb (color * intensity)
+void or_pt_add_sphere_light(void *p, const float *pos, float radius, const float *intensity) {
+  OrPtScene &s = *static_cast<OrPtScene *>(p);
+  SphereLight l;
+  l.init({pos[0], pos[1], pos[2]}, radius, {intensity[0], intensity[1], intensity[2]});
+  s.lights.kind.push_back(3);
+  s.lights.index.push_back(int(s.lights.spheres.size()));
+  s.lights.spheres.push_back(l);
   s.lights.finalize();
 }
 

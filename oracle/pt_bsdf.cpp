@@ -504,4 +504,101 @@ LightEval AmbientLight::eval(const DG &dg, V3 dir, float, float maxDist) const {
   return res;
 }
 
+
+// uniformSampleCone (math/sampling.ih:92-97) about axis n
+static V3 sampleCone(V3 n, float cosAngle, V2 s) {
+  const float phi = 2.f * PI * s.x;
+  const float cosT = 1.f - s.y * (1.f - cosAngle);
+  const float sinT = std::sqrt(std::fmax(0.f, 1.f - cosT * cosT));
+  return xfmVector(frame(n), {std::cos(phi) * sinT, std::sin(phi) * sinT, cosT});
+}
+
+void DistantLight::init(V3 direction, float angularDiameterDeg, V3 irr) {
+  dir = -normalize(direction);
+  const float ad = std::fmin(std::fmax(angularDiameterDeg, 0.f), 180.f);
+  cosAngle = std::cos(ad * 0.5f * float(M_PI / 180.0));
+  pdf = cosAngle < 0.99999988f ? 1.f / (2.f * PI * (1.f - cosAngle)) : INFINITY;
+  irradiance = irr;
+  visible = true;
+}
+
+LightSample DistantLight::sample(const DG &, V2 s) const {
+  LightSample res;
+  res.dir = dir;
+  res.dist = INFINITY;
+  res.pdf = pdf;
+  if (cosAngle < 0.99999988f) res.dir = sampleCone(dir, cosAngle, s);
+  res.weight = irradiance;
+  return res;
+}
+
+LightEval DistantLight::eval(const DG &, V3 d, float, float maxDist) const {
+  LightEval res;
+  res.radiance = v3(0.f);
+  res.pdf = 0.f;
+  if (INFINITY <= maxDist && cosAngle < 0.99999988f && dot(dir, d) > cosAngle) {
+    res.radiance = irradiance * pdf;
+    res.pdf = pdf;
+  }
+  return res;
+}
+
+void SphereLight::init(V3 pos, float r, V3 coloredIntensity) {
+  position = pos;
+  radius = r;
+  intensity = coloredIntensity;
+  radiance = r > 0.f ? coloredIntensity * (1.f / (PI * r * r)) : v3(0.f);
+  visible = true;
+}
+
+LightSample SphereLight::sample(const DG &dg, V2 s) const {
+  LightSample res;
+  const V3 d = position - dg.P;
+  const float dist2 = dot(d, d);
+  const float invdist = 1.f / std::sqrt(dist2);
+  res.dir = d * invdist;
+  res.dist = dist2 * invdist;
+  res.pdf = INFINITY;
+  const float sinTheta = radius * invdist;
+  if (radius > 0.f && sinTheta > 0.005f) {
+    if (sinTheta < 1.f) {
+      const float cosTheta = std::sqrt(1.f - sinTheta * sinTheta);
+      const float phi = 2.f * PI * s.x;
+      const float c = 1.f - s.y * (1.f - cosTheta);
+      const float sn = std::sqrt(std::fmax(0.f, 1.f - c * c));
+      res.dir = xfmVector(frame(res.dir), {std::cos(phi) * sn, std::sin(phi) * sn, c});
+      res.pdf = 1.f / (2.f * PI * (1.f - cosTheta));
+      res.dist = c * res.dist - std::sqrt(std::fmax(0.f, radius * radius - (1.f - c * c) * dist2));
+      res.weight = radiance * (1.f / res.pdf);
+    } else {
+      res.weight = v3(0.f);
+    }
+  } else {
+    res.weight = intensity * (invdist * invdist);
+  }
+  return res;
+}
+
+LightEval SphereLight::eval(const DG &dg, V3 dir, float minDist, float maxDist) const {
+  LightEval res;
+  res.radiance = v3(0.f);
+  res.pdf = 0.f;
+  const V3 A = position - dg.P;
+  const float sinTheta2 = radius * radius / dot(A, A);
+  if (radius > 0.f && std::sqrt(sinTheta2) > 0.005f) {
+    const float rd2 = 1.f / dot(dir, dir);
+    const float projCO = dot(A, dir) * rd2;
+    const V3 perp = A - dir * projCO;
+    const float l2 = dot(perp, perp);
+    if (l2 <= radius * radius) {
+      const float t = projCO - std::sqrt((radius * radius - l2) * rd2);
+      if (t > minDist && t < maxDist) {
+        res.pdf = 1.f / (2.f * PI * (1.f - std::sqrt(1.f - sinTheta2)));
+        res.radiance = radiance;
+      }
+    }
+  }
+  return res;
+}
+
 }  // namespace orc

@@ -206,5 +206,25 @@ struct AmbientLight {
   LightSample sample(const DG &dg, V2 s) const;
   LightEval eval(const DG &dg, V3 dir, float minDist, float maxDist) const;
 };
+// DirectionalLight (lights/DirectionalLight.ispc:14-90, .cpp:77-105):
+// dir towards the light, cone of half the angular diameter, irradiance
+struct DistantLight {
+  V3 dir, irradiance;
+  float cosAngle, pdf;
+  bool visible;
+  void init(V3 direction, float angularDiameterDeg, V3 irr);
+  LightSample sample(const DG &dg, V2 s) const;
+  LightEval eval(const DG &dg, V3 dir, float minDist, float maxDist) const;
+};
+// PointLight (lights/PointLight.ispc:32-158, .cpp:68-121) with
+// intensityQuantity INTENSITY and no intensity distribution
+struct SphereLight {
+  V3 position, radiance, intensity;
+  float radius;
+  bool visible;
+  void init(V3 pos, float r, V3 coloredIntensity);
+  LightSample sample(const DG &dg, V2 s) const;
+  LightEval eval(const DG &dg, V3 dir, float minDist, float maxDist) const;
+};
 
 }  // namespace orc

@@ -316,13 +316,27 @@ SvBSDF svEvalMaterial(const SvMaterial *m, V4 color = {1.f, 1.f, 1.f, 1.f}) {
 }
 
 struct SvLight {
-  int kind;  // 0 quad, 1 ambient
+  int kind;  // 0 quad, 1 ambient, 2 distant, 3 sphere
   bool visible;
   QuadLight quad;
   AmbientLight amb;
-  LightSample sample(const DG &dg, V2 s) const { return kind == 0 ? quad.sample(dg, s) : amb.sample(dg, s); }
+  DistantLight dist;
+  SphereLight sph;
+  LightSample sample(const DG &dg, V2 s) const {
+    switch (kind) {
+      case 0: return quad.sample(dg, s);
+      case 2: return dist.sample(dg, s);
+      case 3: return sph.sample(dg, s);
+      default: return amb.sample(dg, s);
+    }
+  }
   LightEval eval(const DG &dg, V3 dir, float lo, float hi) const {
-    return kind == 0 ? quad.eval(dg, dir, lo, hi) : amb.eval(dg, dir, lo, hi);
+    switch (kind) {
+      case 0: return quad.eval(dg, dir, lo, hi);
+      case 2: return dist.eval(dg, dir, lo, hi);
+      case 3: return sph.eval(dg, dir, lo, hi);
+      default: return amb.eval(dg, dir, lo, hi);
+    }
   }
 };
 
@@ -725,6 +739,7 @@ void or_render_scivis_volume(void *mp, const OrCameraV *c, int pixelFilter, int 
 struct OrScivisLight {
   int kind, visible;
   float pos[3], e1[3], e2[3], radiance[3];
+  float dir[3], angularDiameter, radius;  // distant / sphere lights
 };
 struct OrScivisMaterial {
   int isObj;
@@ -756,6 +771,12 @@ void or_render_scivis(void *scp, void *mp, const OrCameraV *c, const OrScivisPar
     if (l.kind == 0) {
       L.quad.init({l.pos[0], l.pos[1], l.pos[2]}, {l.e1[0], l.e1[1], l.e1[2]}, {l.e2[0], l.e2[1], l.e2[2]}, rad);
       L.quad.visible = L.visible;
+    } else if (l.kind == 2) {
+      L.dist.init({l.dir[0], l.dir[1], l.dir[2]}, l.angularDiameter, rad);
+      L.dist.visible = L.visible;
+    } else if (l.kind == 3) {
+      L.sph.init({l.pos[0], l.pos[1], l.pos[2]}, l.radius, rad);
+      L.sph.visible = L.visible;
     } else {
       L.amb = {rad, L.visible};
     }

@@ -50,13 +50,14 @@ class AOParams(ctypes.Structure):
                 ("collectStats", ctypes.c_int)]
 
 
-LIGHT_QUAD, LIGHT_AMBIENT = 0, 1
+LIGHT_QUAD, LIGHT_AMBIENT, LIGHT_DISTANT, LIGHT_SPHERE = 0, 1, 2, 3
 
 
 class Light(ctypes.Structure):
     _fields_ = [("type", ctypes.c_int), ("visible", ctypes.c_int), ("position", ctypes.c_float * 3),
                 ("edge1", ctypes.c_float * 3), ("edge2", ctypes.c_float * 3), ("color", ctypes.c_float * 3),
-                ("intensity", ctypes.c_float)]
+                ("intensity", ctypes.c_float), ("direction", ctypes.c_float * 3), ("angularDiameter", ctypes.c_float),
+                ("radius", ctypes.c_float)]
 
 
 class ToneMapper(ctypes.Structure):
@@ -97,6 +98,39 @@ def ambient_light(intensity=1.0, color=(1, 1, 1), visible=True):
     L.type, L.visible = LIGHT_AMBIENT, int(visible)
     L.color[:], L.intensity = list(color), float(intensity)
     return L
+
+
+def distant_light(direction, intensity=1.0, color=(1, 1, 1), angular_diameter=0.0, visible=True):
+    """direction: the direction the light travels; irradiance = color * intensity."""
+    L = Light()
+    L.type, L.visible = LIGHT_DISTANT, int(visible)
+    L.direction[:] = list(direction)
+    L.angularDiameter = float(angular_diameter)
+    L.color[:], L.intensity = list(color), float(intensity)
+    return L
+
+
+def sphere_light(position, radius=0.0, intensity=1.0, color=(1, 1, 1), visible=True):
+    """Radiative intensity = color * intensity; radius 0 is a point light."""
+    L = Light()
+    L.type, L.visible = LIGHT_SPHERE, int(visible)
+    L.position[:] = list(position)
+    L.radius = float(radius)
+    L.color[:], L.intensity = list(color), float(intensity)
+    return L
+
+
+def light_from_dict(L):
+    """A b200 light from the dict form the tests and the oracle share."""
+    t = L["type"]
+    col, vis = L.get("color", (1, 1, 1)), L.get("visible", True)
+    if t == "quad":
+        return quad_light(L["position"], L["edge1"], L["edge2"], L["intensity"], color=col, visible=vis)
+    if t == "distant":
+        return distant_light(L["direction"], L["intensity"], col, L.get("angular_diameter", 0.0), vis)
+    if t == "sphere":
+        return sphere_light(L["position"], L.get("radius", 0.0), L["intensity"], col, vis)
+    return ambient_light(L["intensity"], col, visible=vis)
 
 
 def materials_array(mats):

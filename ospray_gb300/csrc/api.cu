@@ -887,7 +887,9 @@ int b200_scene_set_lights(b200_scene s, const b200_light *lights, int n) {
     std::vector<LightD> h(n);
     for (int i = 0; i < n; i++) {
       const b200_light &L = lights[i];
-      require(L.type == B200_LIGHT_QUAD || L.type == B200_LIGHT_AMBIENT, "unsupported light type");
+      require(L.type == B200_LIGHT_QUAD || L.type == B200_LIGHT_AMBIENT || L.type == B200_LIGHT_DISTANT ||
+                  L.type == B200_LIGHT_SPHERE,
+              "unsupported light type");
       LightD &d = h[i];
       std::memset(&d, 0, sizeof(d));
       d.type = L.type;
@@ -901,6 +903,23 @@ int b200_scene_set_lights(b200_scene s, const b200_light *lights, int n) {
         d.ppdf = 1.f / std::sqrt(dot(nd, nd));
         require(std::isfinite(d.ppdf), "degenerate quad light");
         d.nnormal = mul(nd, d.ppdf);
+      } else if (L.type == B200_LIGHT_DISTANT) {
+        // DirectionalLight::commit: towards the light, cone of half the angular diameter
+        const V3 dir = mk(L.direction[0], L.direction[1], L.direction[2]);
+        const float len = std::sqrt(dot(dir, dir));
+        require(len > 0.f && std::isfinite(len), "distant light: zero direction");
+        d.dir = mul(dir, -1.f / len);
+        const float ad = std::fmin(std::fmax(L.angularDiameter, 0.f), 180.f);
+        d.cosAngle = std::cos(ad * 0.5f * float(M_PI / 180.0));
+        d.conePdf = d.cosAngle < 0.99999988f ? 1.f / (2.f * float(M_PI) * (1.f - d.cosAngle)) : INFINITY;
+      } else if (L.type == B200_LIGHT_SPHERE) {
+        // PointLight::processIntensityQuantityType (INTENSITY): the radiance of the
+        // sphere's visible disk, and the intensity of a point light
+        require(L.radius >= 0.f, "sphere light: negative radius");
+        d.position = mk(L.position[0], L.position[1], L.position[2]);
+        d.radius = L.radius;
+        d.intensity = d.radiance;
+        d.radiance = L.radius > 0.f ? mul(d.radiance, 1.f / (float(M_PI) * L.radius * L.radius)) : mk(0.f, 0.f, 0.f);
       }
     }
     // uniform light-selection CDF (Distribution1D_create over all-ones)

@@ -3,6 +3,9 @@
 //   QuadLight_sample / QuadLight_eval   lights/QuadLight.ispc:43-215
 //     (spherical-quad solid-angle sampling, lights/SphericalQuadSampling.ih)
 //   AmbientLight_sample / _eval         lights/AmbientLight.ispc:17-57
+//   DirectionalLight_sample / _eval     lights/DirectionalLight.ispc:14-90
+//   PointLight_sample / _eval           lights/PointLight.ispc:32-158 (sphere
+//                                       lights; no intensity distribution)
 #pragma once
 #include "kernels.h"
 #include "pt_bsdf.cuh"
@@ -106,8 +109,56 @@ struct LightSampleD {
   float dist, pdf;
 };
 
+// uniformSampleCone (math/sampling.ih:92-97) about axis n
+B200_D V3 sampleCone(V3 n, float cosAngle, float sx, float sy) {
+  V3 dx, dy;
+  frame(n, dx, dy);
+  const float cosT = 1.f - sy * (1.f - cosAngle);
+  const float sinT = sqrtf(fmaxf(0.f, 1.f - cosT * cosT));
+  float sp, cp;
+  sincosf(2.f * PI_F * sx, &sp, &cp);
+  return dx * (cp * sinT) + dy * (sp * sinT) + n * cosT;
+}
+
 B200_D LightSampleD sampleLight(const LightD &L, V3 P, V3 Ng, V3 Ns, float sx, float sy) {
   LightSampleD r;
+  if (L.type == LIGHT_DISTANT) {
+    r.dir = L.dir;
+    r.dist = INFINITY;
+    r.pdf = L.conePdf;
+    if (L.cosAngle < 0.99999988f) r.dir = sampleCone(L.dir, L.cosAngle, sx, sy);
+    r.weight = L.radiance;  // irradiance: pdf / pdf cancel
+    return r;
+  }
+  if (L.type == LIGHT_SPHERE) {
+    const V3 d = L.position - P;
+    const float dist2 = fdot(d, d);
+    const float invdist = 1.f / sqrtf(dist2);
+    r.dir = d * invdist;
+    r.dist = dist2 * invdist;
+    r.pdf = INFINITY;
+    const float sinTheta = L.radius * invdist;
+    if (L.radius > 0.f && sinTheta > 0.005f) {
+      if (sinTheta < 1.f) {
+        const float cosTheta = sqrtf(1.f - sinTheta * sinTheta);
+        V3 dx, dy;
+        frame(r.dir, dx, dy);
+        const float c = 1.f - sy * (1.f - cosTheta);
+        const float sn = sqrtf(fmaxf(0.f, 1.f - c * c));
+        float sp, cp;
+        sincosf(2.f * PI_F * sx, &sp, &cp);
+        r.dir = dx * (cp * sn) + dy * (sp * sn) + r.dir * c;
+        r.pdf = 1.f / (2.f * PI_F * (1.f - cosTheta));
+        r.dist = c * r.dist - sqrtf(fmaxf(0.f, L.radius * L.radius - (1.f - c * c) * dist2));
+        r.weight = L.radiance * (1.f / r.pdf);
+      } else {
+        r.weight = splat(0.f);  // inside the sphere: it emits only outwards
+      }
+    } else {
+      r.weight = L.intensity * (invdist * invdist);
+    }
+    return r;
+  }
   if (L.type == LIGHT_QUAD) {
     if (sx == 0.f && sy == 0.f) {
       const V3 p = L.position + L.edge1 * 0.5f + L.edge2 * 0.5f;
@@ -160,6 +211,32 @@ B200_D V3 evalLight(const LightD &L, V3 P, V3 Ns, V3 dir, float minDist, float m
     if (q.S > 0.f) {
       pdf = 1.f / q.S;
       return L.radiance;
+    }
+    return splat(0.f);
+  }
+  if (L.type == LIGHT_DISTANT) {
+    if (INFINITY <= maxDist && L.cosAngle < 0.99999988f && fdot(L.dir, dir) > L.cosAngle) {
+      pdf = L.conePdf;
+      return L.radiance * L.conePdf;
+    }
+    return splat(0.f);
+  }
+  if (L.type == LIGHT_SPHERE) {
+    const V3 A = L.position - P;
+    const float sinTheta2 = L.radius * L.radius / fdot(A, A);
+    if (L.radius > 0.f && sqrtf(sinTheta2) > 0.005f) {
+      // intersectSphere (common/Intersect.ih:28-78): the entry distance
+      const float rd2 = 1.f / fdot(dir, dir);
+      const float projCO = fdot(A, dir) * rd2;
+      const V3 perp = A - dir * projCO;
+      const float l2 = fdot(perp, perp);
+      if (l2 <= L.radius * L.radius) {
+        const float t = projCO - sqrtf((L.radius * L.radius - l2) * rd2);
+        if (t > minDist && t < maxDist) {
+          pdf = 1.f / (2.f * PI_F * (1.f - sqrtf(1.f - sinTheta2)));
+          return L.radiance;
+        }
+      }
     }
     return splat(0.f);
   }

@@ -269,6 +269,35 @@ void LightObj::commit(B200Device &dev) {
       dev.warn("quad light: unsupported 'intensityQuantity' value");
       light.intensity = 0.f;
     }
+  } else if (type == "distant") {
+    // DirectionalLight::commit / processIntensityQuantityType (lights/DirectionalLight.cpp:77-105)
+    light.type = B200_LIGHT_DISTANT;
+    const float dz[3] = {0.f, 0.f, 1.f};
+    getVec3("direction", light.direction, dz);
+    light.angularDiameter = std::fmin(std::fmax(getFloat("angularDiameter", 0.f), 0.f), 180.f);
+    const int q = getInt("intensityQuantity", OSP_INTENSITY_QUANTITY_IRRADIANCE);
+    if (q == OSP_INTENSITY_QUANTITY_RADIANCE) {
+      const float cosAngle = std::cos(light.angularDiameter * 0.5f * float(M_PI / 180.0));
+      light.intensity *= 2.f * float(M_PI) * (1.f - cosAngle);
+    } else if (q != OSP_INTENSITY_QUANTITY_IRRADIANCE) {
+      dev.warn("distant light: unsupported 'intensityQuantity' value");
+      light.intensity = 0.f;
+    }
+  } else if (type == "sphere") {
+    // PointLight::commit / processIntensityQuantityType (lights/PointLight.cpp:68-121):
+    // the b200 light takes the radiative intensity
+    light.type = B200_LIGHT_SPHERE;
+    getVec3("position", light.position, kZero3);
+    light.radius = getFloat("radius", 0.f);
+    const int q = getInt("intensityQuantity", OSP_INTENSITY_QUANTITY_INTENSITY);
+    if (q == OSP_INTENSITY_QUANTITY_POWER) {
+      light.intensity /= 4.f * float(M_PI);
+    } else if (q == OSP_INTENSITY_QUANTITY_RADIANCE && light.radius > 0.f) {
+      light.intensity *= float(M_PI) * light.radius * light.radius;  // radiance x visible disk area
+    } else if (q != OSP_INTENSITY_QUANTITY_INTENSITY) {
+      dev.warn("sphere light: unsupported 'intensityQuantity' value");
+      light.intensity = 0.f;
+    }
   } else {  // ambient
     light.type = B200_LIGHT_AMBIENT;
     const int q = getInt("intensityQuantity", OSP_INTENSITY_QUANTITY_RADIANCE);

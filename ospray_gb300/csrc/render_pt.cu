@@ -181,7 +181,7 @@ __global__ void k_pt_generate(PtCtx c, CameraD cam, PixelFilterD pf, FrameInfo f
 // new ones with one atomic, so no lane idles while work remains.
 // In a batch (BATCH) every ray traverses its own request's scene.
 template <bool SHADOW, bool STATS, bool BATCH>
-__global__ void __launch_bounds__(TRACE_BLOCK, B200_TRACE_MINBLOCKS) k_trace_queue(Scene sc, Workspace ws, const uint32_t *queue,
+__global__ void __launch_bounds__(TRACE_BLOCK, BATCH ? B200_BATCH_TRACE_MINBLOCKS : B200_TRACE_MINBLOCKS) k_trace_queue(Scene sc, Workspace ws, const uint32_t *queue,
                                                             const uint32_t *count, uint32_t *fetch,
                                                             const ReqD *reqs) {
   static_assert(!(BATCH && STATS), "batched traversal keeps no per-scene statistics");

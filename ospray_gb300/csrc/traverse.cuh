@@ -266,6 +266,9 @@ B200_D uint32_t octantOf(V3 d) {
 #ifndef B200_STACK_SMEM
 #define B200_STACK_SMEM 16
 #endif
+#ifndef B200_BATCH_TRACE_MINBLOCKS
+#define B200_BATCH_TRACE_MINBLOCKS 6  // the batched wavefront's trace kernels (their own register budget)
+#endif
 #ifndef B200_TRACE_MINBLOCKS
 #define B200_TRACE_MINBLOCKS 1
 #endif

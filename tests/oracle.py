@@ -91,6 +91,12 @@ class PtWorld:
             if L["type"] == "quad":
                 a = [np.asarray(L[k], np.float32) for k in ("position", "edge1", "edge2")]
                 lib().or_pt_add_quad_light(self.h, _p(a[0]), _p(a[1]), _p(a[2]), _p(rad))
+            elif L["type"] == "distant":
+                d = np.asarray(L["direction"], np.float32)
+                lib().or_pt_add_distant_light(self.h, _p(d), float(L.get("angular_diameter", 0.0)), _p(rad))
+            elif L["type"] == "sphere":
+                pos = np.asarray(L["position"], np.float32)
+                lib().or_pt_add_sphere_light(self.h, _p(pos), float(L.get("radius", 0.0)), _p(rad))
             else:
                 lib().or_pt_add_ambient_light(self.h, _p(rad))
 
@@ -135,6 +141,8 @@ def lib():
         L.or_pt_add_material.argtypes = [P, P, F, F]
         L.or_pt_add_quad_light.argtypes = [P, P, P, P, P]
         L.or_pt_add_ambient_light.argtypes = [P, P]
+        L.or_pt_add_distant_light.argtypes = [P, P, F, P]
+        L.or_pt_add_sphere_light.argtypes = [P, P, F, P]
         L.or_render_pt.argtypes = [P, P, ctypes.POINTER(OrCamera), ctypes.POINTER(OrPtParams), I, I, I, I, I,
                                    P, P, P, I]
         L.or_ray_count.restype = ctypes.c_uint64
@@ -277,7 +285,8 @@ def render_scivis_volume(model, cam, pixel_filter, w, h, spp=1, sampling_rate=1.
 
 class OrScivisLight(ctypes.Structure):
     _fields_ = [("kind", ctypes.c_int), ("visible", ctypes.c_int), ("pos", ctypes.c_float * 3),
-                ("e1", ctypes.c_float * 3), ("e2", ctypes.c_float * 3), ("radiance", ctypes.c_float * 3)]
+                ("e1", ctypes.c_float * 3), ("e2", ctypes.c_float * 3), ("radiance", ctypes.c_float * 3),
+                ("dir", ctypes.c_float * 3), ("angularDiameter", ctypes.c_float), ("radius", ctypes.c_float)]
 
 
 class OrScivisMaterial(ctypes.Structure):
@@ -302,11 +311,17 @@ def render_scivis(scene, volume, cam, lights, materials, w, h, spp=1, pixel_filt
     L = (OrScivisLight * max(1, len(lights)))()
     for i, l in enumerate(lights):
         rad = np.asarray(l.get("color", (1, 1, 1)), np.float32) * np.float32(l["intensity"])
-        L[i].kind = 0 if l["type"] == "quad" else 1
+        L[i].kind = {"quad": 0, "ambient": 1, "distant": 2, "sphere": 3}[l["type"]]
         L[i].visible = int(l.get("visible", True))
         L[i].radiance[:] = [float(x) for x in rad]
         if l["type"] == "quad":
             L[i].pos[:], L[i].e1[:], L[i].e2[:] = ([float(x) for x in l[k]] for k in ("position", "edge1", "edge2"))
+        elif l["type"] == "distant":
+            L[i].dir[:] = [float(x) for x in l["direction"]]
+            L[i].angularDiameter = float(l.get("angular_diameter", 0.0))
+        elif l["type"] == "sphere":
+            L[i].pos[:] = [float(x) for x in l["position"]]
+            L[i].radius = float(l.get("radius", 0.0))
     M = (OrScivisMaterial * max(1, len(materials)))()
     for i, m in enumerate(materials):
         if m is None:
