@@ -165,7 +165,10 @@ int b200_frame_id(b200_frame fb);
 /* device pointer of one channel as ospMapFrameBuffer would return it:
  * COLOR = the converted colour (RGBA8/SRGBA: W*H uint32, RGBA32F: W*H*4
  * float; FB_NONE: the raw accumulation buffer), DEPTH float, NORMAL/ALBEDO
- * float3, IDs uint32, VARIANCE float4.  ACCUM gives the accumulated RGBA32F
+ * float3 (accumulated like the colour: AO and SciVis the first hit's shading
+ * normal and surface albedo, or on a miss the ray direction / background
+ * (AO); the path tracer the first vertex's normal and BSDF albedo; batched
+ * renders write 0), IDs uint32, VARIANCE float4.  ACCUM gives the accumulated RGBA32F
  * colour before post-processing (an addition: the reference cannot map it).
  * Rows bottom-up. */
 void *b200_frame_channel(b200_frame fb, uint32_t channel);

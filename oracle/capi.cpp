@@ -185,6 +185,13 @@ void or_camera_rays(const OrCamera *c, int pixelFilter, int W, int H, int spp, i
       }
 }
 
+// the renderers' next calls also copy the accumulated normal / albedo
+// channels (3 floats per pixel) to these (null: not wanted)
+void or_set_aux_output(float *normal, float *albedo) {
+  g_auxNormal = normal;
+  g_auxAlbedo = albedo;
+}
+
 struct OrFrame {
   float *color;      // W*H*4
   float *depth;      // W*H
@@ -212,6 +219,7 @@ void or_render_ao(void *sp, const OrCamera *c, int pixelFilter, int W, int H, in
   std::memcpy(out->primID, fb.primID.data(), N * 4);
   std::memcpy(out->geomID, fb.geomID.data(), N * 4);
   std::memcpy(out->instID, fb.instID.data(), N * 4);
+  copyAux(fb);
 }
 
 uint64_t or_ray_count(int reset) {

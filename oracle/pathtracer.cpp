@@ -156,10 +156,11 @@ struct PathOut {
   V3 rgb;
   float alpha, z;
   uint32_t primID, geomID, instID;
+  V3 normal, albedo;
 };
 
 PathOut samplePath(const Ctx &c, LDSampler &ld, Ray ray) {
-  PathOut out = {v3(0.f), 1.f, INFINITY, INVALID_ID, INVALID_ID, INVALID_ID};
+  PathOut out = {v3(0.f), 1.f, INFINITY, INVALID_ID, INVALID_ID, INVALID_ID, v3(0.f), v3(0.f)};
   V3 throughput = v3(1.f), contribution = v3(0.f);
   int depth = 0, scatteringEvents = 0;
   bool straightPath = true, firstBounceLight = true;
@@ -199,6 +200,10 @@ PathOut samplePath(const Ctx &c, LDSampler &ld, Ray ray) {
     ld.nextGroup();
     int numLS = 0;
     {  // isSmooth: diffuse or glossy lobes present
+      if (scatteringEvents == 0) {  // updateAuxilliaryData (PathTracerUtil.ih:48-60)
+        out.albedo = throughput * bsdf.albedo;
+        out.normal = throughput * bsdf.N;
+      }
       numLS = firstBounceLight ? c.nFirst : c.nIndirect;
       contribution = contribution + nee(c, ld, dg, bsdf, wo, throughput, numLS);
       firstBounceLight = false;
@@ -267,11 +272,15 @@ void renderPT(const Scene &sc, const PtLights &lights, const std::vector<Princip
         smp.primID = o.primID;
         smp.geomID = o.geomID;
         smp.instID = o.instID;
+        smp.normal = o.normal;
+        smp.albedo = o.albedo;
         accumulateScreen(acc, smp);
       }
       const float rspp = 1.f / float(p.spp);
       acc.rgb = acc.rgb * rspp;
       acc.alpha *= rspp;
+      acc.normal = acc.normal * rspp;
+      acc.albedo = acc.albedo * rspp;
       fbAccumulate(fb, x, y, acc);
     }
     g_rayCount.fetch_add(tl_rays);
@@ -373,6 +382,7 @@ void or_render_pt(void *scp, void *ptp, const OrCameraPT *cam, const OrPtParams 
   }
   const size_t N = size_t(W) * H;
   if (color) std::memcpy(color, fb.color.data(), N * 16);
+  copyAux(fb);
   if (depth) std::memcpy(depth, fb.depth.data(), N * 4);
   if (ids) {
     std::memcpy(ids, fb.primID.data(), N * 4);

@@ -1,3 +1,4 @@
+#include <cstring>
 // Oracle (test infrastructure only): camera, pixel filter, postIntersect,
 // framebuffer accumulation and the AO renderer; see render.h for citations.
 #include "render.h"
@@ -174,6 +175,11 @@ void fbAccumulate(FrameBuffer &fb, int x, int y, const ScreenSample &s) {
   const float c[4] = {s.rgb.x, s.rgb.y, s.rgb.z, s.alpha};
   for (int k = 0; k < 4; k++)
     fb.color[4 * i + k] = accScale > 0.8f ? c[k] : lerpf(accScale, fb.color[4 * i + k], c[k]);
+  const float a[6] = {s.normal.x, s.normal.y, s.normal.z, s.albedo.x, s.albedo.y, s.albedo.z};
+  for (int k = 0; k < 3; k++) {
+    fb.normal[3 * i + k] = accScale > 0.8f ? a[k] : lerpf(accScale, fb.normal[3 * i + k], a[k]);
+    fb.albedo[3 * i + k] = accScale > 0.8f ? a[3 + k] : lerpf(accScale, fb.albedo[3 * i + k], a[3 + k]);
+  }
   bool upd = fb.frameID == 0;
   if (fb.frameID > 0 && std::fabs(s.z) < std::fabs(fb.depth[i])) upd = true;
   if (upd) {
@@ -182,6 +188,12 @@ void fbAccumulate(FrameBuffer &fb, int x, int y, const ScreenSample &s) {
     fb.geomID[i] = s.geomID;
     fb.instID[i] = s.instID;
   }
+}
+
+float *g_auxNormal = nullptr, *g_auxAlbedo = nullptr;
+void copyAux(const FrameBuffer &fb) {
+  if (g_auxNormal) std::memcpy(g_auxNormal, fb.normal.data(), fb.normal.size() * 4);
+  if (g_auxAlbedo) std::memcpy(g_auxAlbedo, fb.albedo.data(), fb.albedo.size() * 4);
 }
 
 // ---------------------------------------------------------------- AO renderer
@@ -248,6 +260,8 @@ void renderAO(const Scene &s, const Camera &cam, const PixelFilter &pf, const AO
             }
             blended = {intensity, intensity, intensity, 1.f};
             if (first) {
+              smp.albedo = v3(1.f);  // surfaces without material: white
+              smp.normal = dg.Ns;
               smp.z = hit.t;
               smp.primID = dg.primID;
               smp.geomID = dg.geomID;
@@ -257,7 +271,11 @@ void renderAO(const Scene &s, const Camera &cam, const PixelFilter &pf, const AO
             ray.tfar = tfar0;
           } else {
             blended = p.bgColor;
-            if (first) smp.z = ray.tfar;
+            if (first) {
+              smp.z = ray.tfar;
+              smp.albedo = {p.bgColor.x, p.bgColor.y, p.bgColor.z};
+              smp.normal = ray.dir;
+            }
           }
           const float f = 1.f - out.w;
           out = {out.x + f * blended.x, out.y + f * blended.y, out.z + f * blended.z, out.w + f * blended.w};
@@ -271,6 +289,8 @@ void renderAO(const Scene &s, const Camera &cam, const PixelFilter &pf, const AO
       const float rspp = 1.f / float(p.spp);
       acc.rgb = acc.rgb * rspp;
       acc.alpha *= rspp;
+      acc.normal = acc.normal * rspp;
+      acc.albedo = acc.albedo * rspp;
       fbAccumulate(fb, x, y, acc);
     }
     g_rayCount.fetch_add(tl_rays);

@@ -62,10 +62,13 @@ struct FrameBuffer {
   std::vector<float> color;  // RGBA
   std::vector<float> depth;
   std::vector<uint32_t> primID, geomID, instID;
+  std::vector<float> normal, albedo;  // 3 per pixel
   void resize(int w, int h) {
     W = w;
     H = h;
     color.assign(size_t(W) * H * 4, 0.f);
+    normal.assign(size_t(W) * H * 3, 0.f);
+    albedo.assign(size_t(W) * H * 3, 0.f);
     depth.assign(size_t(W) * H, INFINITY);
     primID.assign(size_t(W) * H, INVALID_ID);
     geomID.assign(size_t(W) * H, INVALID_ID);
@@ -79,11 +82,14 @@ struct ScreenSample {
   float alpha = 0.f;
   float z = INFINITY;
   uint32_t primID = INVALID_ID, geomID = INVALID_ID, instID = INVALID_ID;
+  V3 normal = v3(0.f), albedo = v3(0.f);  // auxiliary channels (ScreenSample.ih)
 };
 
 inline void accumulateScreen(ScreenSample &acc, const ScreenSample &s) {
   acc.rgb = acc.rgb + s.rgb;
   acc.alpha += s.alpha;
+  acc.normal = acc.normal + s.normal;
+  acc.albedo = acc.albedo + s.albedo;
   if (std::fabs(s.z) < std::fabs(acc.z)) {
     acc.z = s.z;
     acc.primID = s.primID;
@@ -94,6 +100,11 @@ inline void accumulateScreen(ScreenSample &acc, const ScreenSample &s) {
 
 // LocalFB_accumulateSample: lerp accumulation, ID buffers from the closest |z|
 void fbAccumulate(FrameBuffer &fb, int x, int y, const ScreenSample &s);
+
+// where the renderers copy the accumulated normal / albedo channels after a
+// call (null: not wanted); set by or_set_aux_output
+extern float *g_auxNormal, *g_auxAlbedo;
+void copyAux(const FrameBuffer &fb);
 
 template <class F>
 void parallelRows(int H, int nthreads, F f) {

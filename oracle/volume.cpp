@@ -477,6 +477,7 @@ V3 svComputeAO(const SvWorld &w, const SvParams &p, const DG &dg, int px, int py
 struct SvShading {
   V3 shadedColor, transmission;
   float opacity;
+  V3 albedo;
 };
 
 SvShading svComputeShading(const SvWorld &w, const SvParams &p, const DG &dg, const SvMaterial *mat, V4 dgColor,
@@ -509,7 +510,7 @@ SvShading svComputeShading(const SvWorld &w, const SvParams &p, const DG &dg, co
   if (p.aoSamples > 0 && svLuminance(w.aoColor * float(M_PI)) > p.minContribution)
     ao = svComputeAO(w, p, dg, px, py, sampleZ, rs);
   color = color + bsdf.diffuse * ao * (w.aoColor * float(M_PI));
-  return {color, bsdf.transmission, bsdf.opacity};
+  return {color, bsdf.transmission, bsdf.opacity, bsdf.albedo};
 }
 
 // integrateVolumeIntervalsGradient (render/scivis/volumes.ispc:302-439) with
@@ -611,6 +612,8 @@ ScreenSample svRenderSample(const SvWorld &w, const SvParams &p, Ray ray, int x,
       const DG dg = postIntersect(*w.scene, ray, hit);
       const SvShading sh = svComputeShading(w, p, dg, w.material(hit), {1.f, 1.f, 1.f, 1.f}, ray.dir, x, y, sid, rs);
       if (firstHit || allTrans) {
+        smp.normal = dg.Ns;
+        smp.albedo = sh.albedo;
         smp.primID = dg.primID;
         smp.geomID = dg.geomID;
         smp.instID = dg.instID;
@@ -725,6 +728,8 @@ void or_render_scivis_volume(void *mp, const OrCameraV *c, int pixelFilter, int 
         const float rspp = 1.f / float(spp);
         acc.rgb = acc.rgb * rspp;
         acc.alpha *= rspp;
+        acc.normal = acc.normal * rspp;
+        acc.albedo = acc.albedo * rspp;
         fbAccumulate(fb, x, y, acc);
       }
       g_volSamples.fetch_add(samples);
@@ -818,6 +823,8 @@ void or_render_scivis(void *scp, void *mp, const OrCameraV *c, const OrScivisPar
         const float rspp = 1.f / float(p.spp);
         acc.rgb = acc.rgb * rspp;
         acc.alpha *= rspp;
+        acc.normal = acc.normal * rspp;
+        acc.albedo = acc.albedo * rspp;
         fbAccumulate(fb, x, y, acc);
       }
       g_volSamples.fetch_add(samples);
@@ -828,6 +835,7 @@ void or_render_scivis(void *scp, void *mp, const OrCameraV *c, const OrScivisPar
   }
   const size_t N = size_t(W) * H;
   if (color) std::memcpy(color, fb.color.data(), N * 16);
+  copyAux(fb);
   if (depth) std::memcpy(depth, fb.depth.data(), N * 4);
   if (ids) {
     std::memcpy(ids, fb.primID.data(), N * 4);

@@ -428,6 +428,7 @@ FrameObj::FrameObj(DeviceObj *d, int w, int h, int fmt, uint32_t ch) : dev(d), W
   }
   if (ch & B200_FB_NORMAL) alloc((void **)&normal, n * sizeof(float3));
   if (ch & B200_FB_ALBEDO) alloc((void **)&albedo, n * sizeof(float3));
+  if (ch & (B200_FB_NORMAL | B200_FB_ALBEDO)) alloc((void **)&aux, n * 6 * sizeof(float));
   if (ch & B200_FB_ID_PRIMITIVE) alloc((void **)&primID, n * 4);
   if (ch & B200_FB_ID_OBJECT) alloc((void **)&geomID, n * 4);
   if (ch & B200_FB_ID_INSTANCE) alloc((void **)&instID, n * 4);
@@ -438,6 +439,7 @@ FrameObj::~FrameObj() {
   cudaStreamSynchronize(dev->stream);
   if (taskErr) cudaFree(taskErr);
   if (taskActive) cudaFree(taskActive);
+  if (aux) cudaFree(aux);
   for (void *p : {(void *)color, (void *)depth, (void *)variance, (void *)normal, (void *)albedo, (void *)primID,
                   (void *)geomID, (void *)instID, mapped})
     if (p) cudaFree(p);
@@ -454,6 +456,7 @@ FrameD FrameObj::view() const {
   f.variance = variance;
   f.normal = normal;
   f.albedo = albedo;
+  f.aux = aux;
   f.W = W;
   f.H = H;
   f.frameID = frameID;

@@ -127,6 +127,7 @@ struct FrameObj {
   float4 *color = nullptr, *variance = nullptr;
   float *depth = nullptr;
   float3 *normal = nullptr, *albedo = nullptr;
+  float *aux = nullptr;  // NORMAL or ALBEDO: the path tracer's per-pixel sums of a frame (6 floats)
   uint32_t *primID = nullptr, *geomID = nullptr, *instID = nullptr;
   // per 8x8 render task: the variance estimate of the last odd frame
   // (Variance_kernel, fb/frame_ops/Variance.ispc:11-49); valid once computed

@@ -141,6 +141,7 @@ struct Principled {
   float cEavg;
   V3 diffuse;
   float eta, lEavg, lFms, lRavg, lAlbedoMax;
+  V3 albedo;  // MultiBSDF albedo: sum of the lobes' albedos x weights (the shading AOV)
 
   B200_D V3 toLocal(V3 v) const { return mk(fdot(v, fx), fdot(v, fy), fdot(v, N)); }
   B200_D V3 toGlobal(V3 v) const { return fx * v.x + fy * v.y + N * v.z; }
@@ -154,6 +155,7 @@ struct Principled {
     rough = clamp01f(m.roughness);
     alpha = fmaxf(sqrf(rough), 0.001f);
     wC = wP = impSum = 0.f;
+    albedo = splat(0.f);
     const float dielectric = 1.f - metallic;
     if (dielectric > MAT_EPS) {
       const float e = 1.f;  // outside ior 1 / ior 1, clamped to [1/3, 3]
@@ -167,6 +169,7 @@ struct Principled {
       lAlbedoMax = fmaxf(fmaxf(base.x * la, base.y * la), base.z * la);
       wP = dielectric;
       impSum += dielectric;
+      albedo = base * (la * wP);
     }
     const float conductor = metallic;
     if (conductor > MAT_EPS) {
@@ -192,6 +195,7 @@ struct Principled {
                 sqrf(fa[2]) * cEavg / (1.f - fa[2] * (1.f - cEavg)));
       wC = conductor;
       impSum += conductor;
+      albedo = albedo + mk(fa[0], fa[1], fa[2]) * (cEavg * conductor);
     }
   }
 

@@ -89,6 +89,7 @@ __global__ void __launch_bounds__(128) k_render_ao(const SamplerTables *T, Scene
     bool first = true;
     float z = INFINITY;
     uint32_t prim = INVALID_ID, geom = INVALID_ID, inst = INVALID_ID;
+    V3 sn = splat(0.f), sal = splat(0.f);
     for (int layer = 0; layer < 64 && o[3] < 0.99f; layer++) {
       HitRec h;
       const bool hit = traceScene<false, STATS>(sc, ray, h, &ts);
@@ -107,6 +108,8 @@ __global__ void __launch_bounds__(128) k_render_ao(const SamplerTables *T, Scene
           prim = h.primID;
           geom = h.geomID;
           inst = h.instID;
+          sn = dg.Ns;
+          sal = splat(1.f);  // AORenderer_computeShading: albedo = surface colour (white without material)
         }
         ray.tnear = fadd(h.t, dg.epsilon);
         ray.tfar = tfar0;
@@ -115,7 +118,11 @@ __global__ void __launch_bounds__(128) k_render_ao(const SamplerTables *T, Scene
         bl[1] = p.bg[1];
         bl[2] = p.bg[2];
         bl[3] = p.bg[3];
-        if (first) z = ray.tfar;
+        if (first) {
+          z = ray.tfar;
+          sn = ray.dir;
+          sal = mk(p.bg[0], p.bg[1], p.bg[2]);
+        }
       }
       const float f = fsub(1.f, o[3]);
       for (int k = 0; k < 4; k++) o[k] = fadd(o[k], fmul(f, bl[k]));
@@ -126,6 +133,8 @@ __global__ void __launch_bounds__(128) k_render_ao(const SamplerTables *T, Scene
     ag = fadd(ag, o[1]);
     ab = fadd(ab, o[2]);
     aa = fadd(aa, o[3]);
+    acc.n = add(acc.n, sn);
+    acc.al = add(acc.al, sal);
     if (fabsf(z) < fabsf(acc.z)) {
       acc.z = z;
       acc.primID = prim;
@@ -138,6 +147,8 @@ __global__ void __launch_bounds__(128) k_render_ao(const SamplerTables *T, Scene
   acc.g = fmul(ag, rspp);
   acc.b = fmul(ab, rspp);
   acc.a = fmul(aa, rspp);
+  acc.n = mul(acc.n, rspp);
+  acc.al = mul(acc.al, rspp);
   fbAccumulate(fb, x, y, acc);
   if (STATS) flushStats(sc, ts);
 }

@@ -34,6 +34,7 @@ struct FrameD {
   float4 *variance;  // optional: accumulates the frames picked by accumVariance
   float3 *normal, *albedo;
   int W, H, frameID;
+  float *aux;                 // NORMAL/ALBEDO requested: per pixel the path tracer's sums of this frame (6 floats)
   int accumVariance;          // this frame goes into the variance buffer (FrameBuffer::beginFrame)
   const uint8_t *taskActive;  // adaptive accumulation: per 8x8 task, render it? (null: all)
   int tasksX;
@@ -191,7 +192,11 @@ struct PixelOut {
   float r, g, b, a;
   float z;
   uint32_t primID, geomID, instID;
+  V3 n, al;  // normal and albedo channels (ScreenSample.normal / .albedo)
 };
+
+// FRAMEBUFFER_ACCUMULATE_VALUE's lerp, (1 - f) * old + f * new, rounded per operation
+B200_D float lerpAcc(float f, float o, float v) { return fadd(fmul(fsub(1.f, f), o), fmul(f, v)); }
 
 B200_D void fbAccumulate(const FrameD &fb, int x, int y, const PixelOut &s) {
   const size_t i = size_t(y) * fb.W + x;
@@ -220,6 +225,18 @@ B200_D void fbAccumulate(const FrameD &fb, int x, int y, const PixelOut &s) {
       v.w = fadd(fmul(k, o.w), fmul(vs, v.w));
     }
     fb.variance[i] = v;
+  }
+  if (fb.normal) {
+    const float3 o = fb.normal[i];
+    fb.normal[i] = accScale > 0.8f ? make_float3(s.n.x, s.n.y, s.n.z)
+                                   : make_float3(lerpAcc(accScale, o.x, s.n.x), lerpAcc(accScale, o.y, s.n.y),
+                                                 lerpAcc(accScale, o.z, s.n.z));
+  }
+  if (fb.albedo) {
+    const float3 o = fb.albedo[i];
+    fb.albedo[i] = accScale > 0.8f ? make_float3(s.al.x, s.al.y, s.al.z)
+                                   : make_float3(lerpAcc(accScale, o.x, s.al.x), lerpAcc(accScale, o.y, s.al.y),
+                                                 lerpAcc(accScale, o.z, s.al.z));
   }
   bool upd = fb.frameID == 0;
   if (fb.depth) {

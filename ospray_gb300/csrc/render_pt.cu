@@ -30,6 +30,7 @@ struct PtCtx {
   const float *lightCdf;
   const AlbedoTablesD *AT;
   int frameID;
+  float *aux;  // per pixel: sums of the first vertices' normal and albedo (null: not wanted)
 };
 
 struct PathResult {
@@ -423,6 +424,18 @@ __global__ void __launch_bounds__(128, B200_SHADE_MINBLOCKS) k_pt_shade(PtCtx c,
           Principled bsdf;
           const MaterialD &mat = C.mats[e.materialID];
           bsdf.init(mat, fxv, fyv, dg.Ns, C.AT);
+          if (depth == 0 && C.aux && bsdf.impSum > 0.f) {
+            // updateAuxilliaryData (render/pathtracer/PathTracerUtil.ih:48-60) at the
+            // first (smooth) vertex: throughput x BSDF albedo and x shading normal
+            float *a = C.aux + size_t(p / uint32_t(C.p.spp)) * 6;
+            const V3 an = throughput * bsdf.N, aa = throughput * bsdf.albedo;
+            atomicAdd(a + 0, an.x);
+            atomicAdd(a + 1, an.y);
+            atomicAdd(a + 2, an.z);
+            atomicAdd(a + 3, aa.x);
+            atomicAdd(a + 4, aa.y);
+            atomicAdd(a + 5, aa.z);
+          }
           bool cached = false;
           if (NRC) {
             if (pr.meta2.w != INVALID_ID) {  // training path: record the vertex
@@ -616,7 +629,15 @@ B200_D PixelOut finalizeAO(const PathRec *paths, int spp, const AOParamsD &A) {
 __global__ void k_pt_finalize(PtCtx c, Workspace ws, FrameInfo fi, FrameD fb) {
   const int pix = blockIdx.x * blockDim.x + threadIdx.x;
   if (pix >= fi.W * fi.H || !pixelActive(fb, pix % fi.W, pix / fi.W)) return;
-  fbAccumulate(fb, pix % fi.W, pix / fi.W, finalizePT(ws.paths + size_t(pix) * fi.spp, fi.spp, c.p.maxContribution));
+  PixelOut o = finalizePT(ws.paths + size_t(pix) * fi.spp, fi.spp, c.p.maxContribution);
+  if (c.aux) {  // the frame's normal / albedo sums; cleared for the next frame
+    float *a = c.aux + size_t(pix) * 6;
+    const float rspp = 1.f / float(fi.spp);
+    o.n = mk(a[0], a[1], a[2]) * rspp;
+    o.al = mk(a[3], a[4], a[5]) * rspp;
+    for (int k = 0; k < 6; k++) a[k] = 0.f;
+  }
+  fbAccumulate(fb, pix % fi.W, pix / fi.W, o);
 }
 
 // ---------------------------------------------------------------- batch kernels
@@ -871,7 +892,7 @@ cudaError_t launchRenderPT(const SamplerTables *T, const Scene &sc, const Camera
   if (ptWorkspaceBytes(fi.npaths) > wsBytes) return cudaErrorInvalidValue;
   if (nrc && (stats || !nrcInfer)) return cudaErrorInvalidValue;
   Workspace ws = carveWorkspace(workspace, fi.npaths);
-  PtCtx c = {T, sc, p, mats, lights, lightCdf, AT, fb.frameID};
+  PtCtx c = {T, sc, p, mats, lights, lightCdf, AT, fb.frameID, fb.aux};
   static int traceBlocks = 0, shadowBlocks = 0, shadeBlocks = 0, shadeNrcBlocks = 0;
   if (!traceBlocks) {
     traceBlocks = persistentBlocks((const void *)k_trace_queue<false, false, false>, TRACE_SMEM_BYTES);

@@ -26,6 +26,7 @@ struct SvBSDF {
   float shininess;
   V3 transmission;
   float opacity;
+  V3 albedo;  // diffuse + specular before the BRDF normalisation
 };
 
 // material slot of a surface hit; ~0u (no material) for volume samples
@@ -50,6 +51,7 @@ B200_D SvBSDF svEvalMaterial(const ScivisSurfD &S, uint32_t mi, float4 color) {
       r.opacity = d;
     }
   }
+  r.albedo = r.diffuse + r.specular;
   r.shininess *= 4.f;
   r.diffuse = r.diffuse * 0.318309886f;  // 1/pi
   r.specular = r.specular * ((r.shininess + 2.f) * 0.0795774715f *  // 1/(4 pi)
@@ -117,6 +119,7 @@ B200_D V3 svComputeAO(const SamplerTables *T, const Scene &sc, const VolumeD &vo
 struct SvShading {
   V3 color, transmission;
   float opacity;
+  V3 albedo;
 };
 
 // SciVis_computeShading (render/scivis/surfaces.ispc:90-128) with
@@ -165,6 +168,7 @@ B200_D SvShading svComputeShading(const SamplerTables *T, const Scene &sc, const
   r.color = color;
   r.transmission = bsdf.transmission;
   r.opacity = bsdf.opacity;
+  r.albedo = bsdf.albedo;
   return r;
 }
 
@@ -236,6 +240,7 @@ __global__ void __launch_bounds__(128) k_render_scivis_surfaces(const SamplerTab
       V3 outColor = splat(0.f), outT = splat(1.f);
       float z = INFINITY;
       uint32_t prim = INVALID_ID, geom = INVALID_ID, inst = INVALID_ID;
+      V3 sn = splat(0.f), sal = splat(0.f);
       uint32_t vsamples = 0;
       for (int g = 0; g < 1024; g++) {
         HitRec h;
@@ -274,6 +279,8 @@ __global__ void __launch_bounds__(128) k_render_scivis_surfaces(const SamplerTab
         const SvShading sh = svComputeShading<STATS>(T, sc, vol, S, p.samplingRate, dg, svMaterialSlot(sc, dg.entry),
                                                      make_float4(1.f, 1.f, 1.f, 1.f), ray.dir, x, y, sid, rs, &ts);
         if (firstHit || allTrans) {
+          sn = dg.Ns;
+          sal = sh.albedo;
           prim = h.primID;
           geom = h.geomID;
           inst = h.instID;
@@ -293,6 +300,8 @@ __global__ void __launch_bounds__(128) k_render_scivis_surfaces(const SamplerTab
       acc.g += outColor.y;
       acc.b += outColor.z;
       acc.a += 1.f - luminance(outT);
+      acc.n = acc.n + sn;
+      acc.al = acc.al + sal;
       if (fabsf(z) < fabsf(acc.z)) {
         acc.z = z;
         acc.primID = prim;
@@ -305,6 +314,8 @@ __global__ void __launch_bounds__(128) k_render_scivis_surfaces(const SamplerTab
     acc.g *= rspp;
     acc.b *= rspp;
     acc.a *= rspp;
+    acc.n = acc.n * rspp;
+    acc.al = acc.al * rspp;
     fbAccumulate(fb, x, y, acc);
   }
   if (STATS) flushStats(sc, ts);

@@ -134,6 +134,7 @@ def lib():
         L.or_scene_add_mesh.argtypes = [P, P, I, P, I]
         L.or_scene_add_quad_mesh.argtypes = [P, P, I, P, I]
         L.or_scene_add_boxes.argtypes = [P, P, I]
+        L.or_set_aux_output.argtypes = [P, P]
         L.or_scene_add_spheres.argtypes = [P, P, I]
         L.or_scene_add_instance.argtypes = [P, I, U32, U32, P, I]
         L.or_pt_new.restype = P
@@ -241,6 +242,22 @@ def render_ao(scene, cam, pixel_filter, w, h, spp=1, ao_samples=1, ao_radius=1e2
     lib().or_render_ao(scene.h, ctypes.byref(cam), pixel_filter, w, h, spp, ao_samples, ao_radius, ao_intensity,
                        _p(bgv), frames, ctypes.byref(fr), nthreads)
     return dict(color=color, depth=depth, primID=ids[0], geomID=ids[1], instID=ids[2])
+
+
+class AuxOutput:
+    """Within the block, oracle renders also return the accumulated normal
+    and albedo channels: `with AuxOutput(w, h) as aux: ...; aux.normal`."""
+
+    def __init__(self, w, h):
+        self.normal = np.zeros((h, w, 3), np.float32)
+        self.albedo = np.zeros((h, w, 3), np.float32)
+
+    def __enter__(self):
+        lib().or_set_aux_output(_p(self.normal), _p(self.albedo))
+        return self
+
+    def __exit__(self, *a):
+        lib().or_set_aux_output(None, None)
 
 
 def tables():

@@ -144,3 +144,103 @@ def test_unsupported_types_report_errors(osp_device):
     assert b"spot" in L.ospDeviceGetLastErrorMsg(dev)
     assert L.ospNewCamera(b"orthographic") is None
     L.ospDeviceRelease(dev)
+
+
+def test_quads_boxes_and_lights_through_ospray_api(osp_device):
+    """A mesh with vec4ui quads, a "box" geometry, and "distant" + "sphere"
+    lights through libospray.so (ospNewGeometry / ospNewLight), rendered by
+    the scivis renderer with shadows: IDs and depth bit-exact and colours
+    within 1e-3 of the oracle on the same world."""
+    from test_cpu_oracle import _heightfield_quads, _random_boxes
+    L = osp_device
+    keep = []
+    W = H = 128
+    v, q = _heightfield_quads(n=40)
+    boxes = _random_boxes(n=40, seed=11)
+    boxes[:, [1, 4]] = boxes[:, [1, 4]] * 0.3 + 0.05  # boxes standing on the height field
+    mesh = L.ospNewGeometry(b"mesh")
+    osp_api.set_data(mesh, "vertex.position", v.astype(np.float32), osp_api.OSP_VEC3F, len(v), keep)
+    osp_api.set_data(mesh, "index", q.astype(np.uint32), 4503, len(q), keep)  # OSP_VEC4UI
+    L.ospCommit(mesh)
+    box = L.ospNewGeometry(b"box")
+    osp_api.set_data(box, "box", boxes.astype(np.float32), 10002, len(boxes), keep)  # OSP_BOX3F
+    L.ospCommit(box)
+    models = []
+    for g in (mesh, box):
+        m = L.ospNewGeometricModel(g)
+        L.ospCommit(m)
+        models.append(m)
+        L.ospRelease(g)
+    arr = (ctypes.c_void_p * 2)(*models)
+    md = L.ospNewSharedData(ctypes.addressof(arr), osp_api.OSP_GEOMETRIC_MODEL, 2, 0, 1, 0, 1, 0, None, None)
+    group = L.ospNewGroup()
+    osp_api.set_param(group, "geometry", osp_api.OSP_DATA, md)
+    L.ospRelease(md)
+    for m in models:
+        L.ospRelease(m)
+    L.ospCommit(group)
+    inst = L.ospNewInstance(group)
+    L.ospCommit(inst)
+    L.ospRelease(group)
+    lights_d = [dict(type="distant", direction=(0.3, -1.0, 0.4), intensity=2.0, color=(1.0, 0.9, 0.8)),
+                dict(type="sphere", position=(0.2, 0.8, 0.3), radius=0.05, intensity=0.4)]
+    lights = []
+    for ld in lights_d:
+        lh = L.ospNewLight(ld["type"].encode())
+        assert lh, L.ospDeviceGetLastErrorMsg(L.ospGetCurrentDevice())
+        osp_api.set_param(lh, "intensity", osp_api.OSP_FLOAT, np.float32(ld["intensity"]))
+        if "color" in ld:
+            osp_api.set_param(lh, "color", osp_api.OSP_VEC3F, np.float32(ld["color"]))
+        if ld["type"] == "distant":
+            osp_api.set_param(lh, "direction", osp_api.OSP_VEC3F, np.float32(ld["direction"]))
+        else:
+            osp_api.set_param(lh, "position", osp_api.OSP_VEC3F, np.float32(ld["position"]))
+            osp_api.set_param(lh, "radius", osp_api.OSP_FLOAT, np.float32(ld["radius"]))
+        L.ospCommit(lh)
+        lights.append(lh)
+    la = (ctypes.c_void_p * 2)(*lights)
+    ld_data = L.ospNewSharedData(ctypes.addressof(la), osp_api.OSP_LIGHT, 2, 0, 1, 0, 1, 0, None, None)
+    world = L.ospNewWorld()
+    L.ospSetObjectAsData(world, b"instance", osp_api.OSP_INSTANCE, inst)
+    osp_api.set_param(world, "light", osp_api.OSP_DATA, ld_data)
+    L.ospRelease(ld_data)
+    for lh in lights:
+        L.ospRelease(lh)
+    L.ospRelease(inst)
+    L.ospCommit(world)
+    pos, dirn, up = (0.5, 1.1, -0.5), (0.0, -1.0, 1.1), (0.0, 1.0, 0.0)
+    cam = L.ospNewCamera(b"perspective")
+    osp_api.set_param(cam, "position", osp_api.OSP_VEC3F, np.float32(pos))
+    osp_api.set_param(cam, "direction", osp_api.OSP_VEC3F, np.float32(dirn))
+    osp_api.set_param(cam, "up", osp_api.OSP_VEC3F, np.float32(up))
+    osp_api.set_param(cam, "aspect", osp_api.OSP_FLOAT, np.float32(1.0))
+    L.ospCommit(cam)
+    ren = L.ospNewRenderer(b"scivis")
+    osp_api.set_param(ren, "pixelFilter", osp_api.OSP_UINT, np.uint32(0))
+    osp_api.set_param(ren, "shadows", osp_api.OSP_BOOL, np.uint8(1))
+    L.ospCommit(ren)
+    ch = osp_api.OSP_FB_COLOR | osp_api.OSP_FB_DEPTH | osp_api.OSP_FB_ACCUM | osp_api.OSP_FB_ID_PRIMITIVE | \
+        osp_api.OSP_FB_ID_OBJECT
+    fb = L.ospNewFrameBuffer(W, H, osp_api.OSP_FB_RGBA32F, ch)
+    fut = L.ospRenderFrame(fb, ren, cam, world)
+    assert fut, L.ospDeviceGetLastErrorMsg(L.ospGetCurrentDevice())
+    L.ospWait(fut, osp_api.OSP_TASK_FINISHED)
+    L.ospRelease(fut)
+    color = osp_api.map_channel(fb, osp_api.OSP_FB_COLOR, (H, W, 4), np.float32)
+    depth = osp_api.map_channel(fb, osp_api.OSP_FB_DEPTH, (H, W), np.float32)
+    prim = osp_api.map_channel(fb, osp_api.OSP_FB_ID_PRIMITIVE, (H, W), np.uint32)
+    geom = osp_api.map_channel(fb, osp_api.OSP_FB_ID_OBJECT, (H, W), np.uint32)
+    o = oracle.Scene()
+    o.add_instance(o.add_quad_mesh(v, q), 0, 0)
+    o.add_instance(o.add_boxes(boxes), 0, 1)
+    o.commit()
+    ref = oracle.render_scivis(o, None, oracle.camera(pos, dirn, up), lights_d, [], W, H, spp=1, pixel_filter=0,
+                               shadows=True)
+    assert {0, 1} <= set(np.unique(geom).tolist())  # quads and boxes both seen
+    assert np.mean(prim == ref["primID"]) >= 0.999
+    assert np.mean(depth.view(np.uint32) == ref["depth"].view(np.uint32)) >= 0.999
+    assert ref["color"][..., :3].mean() > 0.05
+    close = np.all(np.abs(color - ref["color"]) <= 1e-3 * np.maximum(1.0, np.abs(ref["color"])) + 1e-5, axis=2)
+    assert close.mean() >= 0.995, close.mean()
+    for h in (fb, ren, cam, world):
+        L.ospRelease(h)
