@@ -235,13 +235,18 @@ typedef struct {
  *      lights/Light.cpp:22-35).  radiance = color * intensity (the default
  *      intensityQuantity of both).  The list order is the light index order of
  *      the path tracer's light CDF (render/pathtracer/PathTracerData.cpp:32-82). */
-enum { B200_LIGHT_QUAD = 0, B200_LIGHT_AMBIENT = 1, B200_LIGHT_DISTANT = 2, B200_LIGHT_SPHERE = 3 };
+enum { B200_LIGHT_QUAD = 0, B200_LIGHT_AMBIENT = 1, B200_LIGHT_DISTANT = 2, B200_LIGHT_SPHERE = 3, B200_LIGHT_SPOT = 4 };
 /* distant (DirectionalLight::commit lights/DirectionalLight.cpp:77-105):
  *   `direction` the light travels, `angularDiameter` in degrees (clamped to
  *   [0, 180]); irradiance = color * intensity (intensityQuantity IRRADIANCE).
  * sphere (PointLight::commit lights/PointLight.cpp:68-121): `position`,
  *   `radius` (0: a point light); radiative intensity = color * intensity
  *   (intensityQuantity INTENSITY), radiance = that / (pi radius^2).
+ * spot (SpotLight::commit lights/SpotLight.cpp:76-140, no intensity
+ *   distribution): `position`, `direction` it points to, `openingAngle`
+ *   (degrees, clamped to [0, 360]), `penumbraAngle` (clamped to half the
+ *   opening), `radius` / `innerRadius` of its emitting ring (0: a point);
+ *   radiative intensity = color * intensity, radiance = that / ring area.
  * Unused fields are ignored; zero-initialise the struct. */
 typedef struct {
   int type;
@@ -252,6 +257,7 @@ typedef struct {
   float direction[3];
   float angularDiameter;
   float radius;
+  float openingAngle, penumbraAngle, innerRadius;
 } b200_light;
 int b200_scene_set_lights(b200_scene scene, const b200_light *lights, int n);
 

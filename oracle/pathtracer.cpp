@@ -23,11 +23,12 @@ struct PtParams {
 };
 
 struct PtLights {
-  std::vector<int> kind;  // 0 quad, 1 ambient, 2 distant, 3 sphere
+  std::vector<int> kind;  // 0 quad, 1 ambient, 2 distant, 3 sphere, 4 spot
   std::vector<QuadLight> quads;
   std::vector<AmbientLight> ambients;
   std::vector<DistantLight> distants;
   std::vector<SphereLight> spheres;
+  std::vector<SpotLight> spots;
   std::vector<int> index;
   std::vector<float> cdf;
   void finalize() {
@@ -43,6 +44,7 @@ struct PtLights {
       case 0: return quads[index[i]].sample(dg, s);
       case 2: return distants[index[i]].sample(dg, s);
       case 3: return spheres[index[i]].sample(dg, s);
+      case 4: return spots[index[i]].sample(dg, s);
       default: return ambients[index[i]].sample(dg, s);
     }
   }
@@ -51,6 +53,7 @@ struct PtLights {
       case 0: return quads[index[i]].eval(dg, dir, lo, hi);
       case 2: return distants[index[i]].eval(dg, dir, lo, hi);
       case 3: return spheres[index[i]].eval(dg, dir, lo, hi);
+      case 4: return spots[index[i]].eval(dg, dir, lo, hi);
       default: return ambients[index[i]].eval(dg, dir, lo, hi);
     }
   }
@@ -59,6 +62,7 @@ struct PtLights {
       case 0: return quads[index[i]].visible;
       case 2: return distants[index[i]].visible;
       case 3: return spheres[index[i]].visible;
+      case 4: return spots[index[i]].visible;
       default: return ambients[index[i]].visible;
     }
   }
@@ -348,6 +352,20 @@ void or_pt_add_sphere_light(void *p, const float *pos, float radius, const float
   s.lights.kind.push_back(3);
   s.lights.index.push_back(int(s.lights.spheres.size()));
   s.lights.spheres.push_back(l);
+  s.lights.finalize();
+}
+
+// position, direction, opening / penumbra angles (degrees), radius, inner
+// radius, radiative intensity rgb
+void or_pt_add_spot_light(void *p, const float *pos, const float *dir, float opening, float penumbra, float radius,
+                          float innerRadius, const float *intensity) {
+  OrPtScene &s = *static_cast<OrPtScene *>(p);
+  SpotLight l;
+  l.init({pos[0], pos[1], pos[2]}, {dir[0], dir[1], dir[2]}, opening, penumbra, radius, innerRadius,
+         {intensity[0], intensity[1], intensity[2]});
+  s.lights.kind.push_back(4);
+  s.lights.index.push_back(int(s.lights.spots.size()));
+  s.lights.spots.push_back(l);
   s.lights.finalize();
 }
 

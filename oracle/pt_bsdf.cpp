@@ -543,6 +543,75 @@ LightEval DistantLight::eval(const DG &, V3 d, float, float maxDist) const {
   return res;
 }
 
+void SpotLight::init(V3 pos, V3 direction, float openingDeg, float penumbraDeg, float r, float ri, V3 ci) {
+  position = pos;
+  dir = normalize(direction);
+  const V3 a = std::fabs(direction.x) < std::fabs(direction.y) ? V3{0.f, direction.z, direction.y}
+                                                                : V3{direction.z, 0.f, direction.x};
+  c90 = normalize(cross(a, dir));
+  c0 = cross(dir, c90);
+  const float opening = std::fmin(std::fmax(openingDeg, 0.f), 360.f);
+  const float penumbra = std::fmin(std::fmax(penumbraDeg, 0.f), 0.5f * opening);
+  const float deg = float(M_PI / 180.0);
+  cosAngleMax = std::cos(deg * 0.5f * opening);
+  cosAngleScale = 1.f / (std::cos(deg * (0.5f * opening - penumbra)) - cosAngleMax);
+  radius = std::fmax(0.f, r);
+  innerRadius = std::fmin(std::fmax(ri, 0.f), 0.999f * radius);
+  const float ring = PI * (radius * radius - innerRadius * innerRadius);
+  areaPdf = 1.f / ring;
+  intensity = ci;
+  radiance = radius > 0.f ? ci * (1.f / ring) : v3(0.f);
+  visible = true;
+}
+
+LightSample SpotLight::sample(const DG &dg, V2 s) const {
+  LightSample res;
+  res.dir = position - dg.P;
+  if (radius > 0.f) {
+    const float rr = std::sqrt((1.f - s.x) * (innerRadius * innerRadius) + s.x * (radius * radius));
+    const float phi = 2.f * PI * s.y;
+    res.dir = c0 * (rr * std::cos(phi)) + c90 * (rr * std::sin(phi)) + res.dir;
+  }
+  const float dist2 = dot(res.dir, res.dir);
+  const float invdist = 1.f / std::sqrt(dist2);
+  res.dir = res.dir * invdist;
+  res.dist = dist2 * invdist;
+  const float cosAngle = -dot(dir, res.dir);
+  float w = clampf((cosAngle - cosAngleMax) * cosAngleScale, 0.f, 1.f);
+  if (radius > 0.f) {
+    res.pdf = areaPdf * (dist2 / std::fabs(cosAngle));
+    w = w / res.pdf;
+    res.weight = radiance * w;
+  } else {
+    res.pdf = INFINITY;
+    w *= std::fabs(cosAngle);
+    res.weight = intensity * ((invdist * invdist) * w);
+  }
+  return res;
+}
+
+LightEval SpotLight::eval(const DG &dg, V3 d, float minDist, float maxDist) const {
+  LightEval res;
+  res.radiance = v3(0.f);
+  res.pdf = 0.f;
+  if (radius > 0.f) {
+    const float cosAngle = -dot(dir, d);
+    if (cosAngle > cosAngleMax) {
+      const V3 vp = dg.P - position;
+      const float t = dot(vp, dir) * (1.f / cosAngle);
+      if (t > minDist && t <= maxDist) {
+        const V3 vd = vp + d * t;
+        const float d2 = dot(vd, vd);
+        if (d2 < radius * radius && d2 > innerRadius * innerRadius) {
+          res.radiance = radiance * clampf((cosAngle - cosAngleMax) * cosAngleScale, 0.f, 1.f);
+          res.pdf = areaPdf * (t * t / std::fabs(cosAngle));
+        }
+      }
+    }
+  }
+  return res;
+}
+
 void SphereLight::init(V3 pos, float r, V3 coloredIntensity) {
   position = pos;
   radius = r;

@@ -218,6 +218,16 @@ struct DistantLight {
 };
 // PointLight (lights/PointLight.ispc:32-158, .cpp:68-121) with
 // intensityQuantity INTENSITY and no intensity distribution
+// SpotLight (lights/SpotLight.ispc:26-170, .cpp:76-140), intensityQuantity
+// INTENSITY, no intensity distribution
+struct SpotLight {
+  V3 position, dir, c0, c90, radiance, intensity;
+  float cosAngleMax, cosAngleScale, radius, innerRadius, areaPdf;
+  bool visible;
+  void init(V3 pos, V3 direction, float openingDeg, float penumbraDeg, float r, float ri, V3 coloredIntensity);
+  LightSample sample(const DG &dg, V2 s) const;
+  LightEval eval(const DG &dg, V3 dir, float minDist, float maxDist) const;
+};
 struct SphereLight {
   V3 position, radiance, intensity;
   float radius;

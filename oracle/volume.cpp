@@ -316,17 +316,19 @@ SvBSDF svEvalMaterial(const SvMaterial *m, V4 color = {1.f, 1.f, 1.f, 1.f}) {
 }
 
 struct SvLight {
-  int kind;  // 0 quad, 1 ambient, 2 distant, 3 sphere
+  int kind;  // 0 quad, 1 ambient, 2 distant, 3 sphere, 4 spot
   bool visible;
   QuadLight quad;
   AmbientLight amb;
   DistantLight dist;
   SphereLight sph;
+  SpotLight spot;
   LightSample sample(const DG &dg, V2 s) const {
     switch (kind) {
       case 0: return quad.sample(dg, s);
       case 2: return dist.sample(dg, s);
       case 3: return sph.sample(dg, s);
+      case 4: return spot.sample(dg, s);
       default: return amb.sample(dg, s);
     }
   }
@@ -335,6 +337,7 @@ struct SvLight {
       case 0: return quad.eval(dg, dir, lo, hi);
       case 2: return dist.eval(dg, dir, lo, hi);
       case 3: return sph.eval(dg, dir, lo, hi);
+      case 4: return spot.eval(dg, dir, lo, hi);
       default: return amb.eval(dg, dir, lo, hi);
     }
   }
@@ -744,7 +747,8 @@ void or_render_scivis_volume(void *mp, const OrCameraV *c, int pixelFilter, int 
 struct OrScivisLight {
   int kind, visible;
   float pos[3], e1[3], e2[3], radiance[3];
-  float dir[3], angularDiameter, radius;  // distant / sphere lights
+  float dir[3], angularDiameter, radius;  // distant / sphere / spot lights
+  float openingAngle, penumbraAngle, innerRadius;  // spot lights
 };
 struct OrScivisMaterial {
   int isObj;
@@ -782,6 +786,10 @@ void or_render_scivis(void *scp, void *mp, const OrCameraV *c, const OrScivisPar
     } else if (l.kind == 3) {
       L.sph.init({l.pos[0], l.pos[1], l.pos[2]}, l.radius, rad);
       L.sph.visible = L.visible;
+    } else if (l.kind == 4) {
+      L.spot.init({l.pos[0], l.pos[1], l.pos[2]}, {l.dir[0], l.dir[1], l.dir[2]}, l.openingAngle, l.penumbraAngle,
+                  l.radius, l.innerRadius, rad);
+      L.spot.visible = L.visible;
     } else {
       L.amb = {rad, L.visible};
     }

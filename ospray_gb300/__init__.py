@@ -50,14 +50,15 @@ class AOParams(ctypes.Structure):
                 ("collectStats", ctypes.c_int)]
 
 
-LIGHT_QUAD, LIGHT_AMBIENT, LIGHT_DISTANT, LIGHT_SPHERE = 0, 1, 2, 3
+LIGHT_QUAD, LIGHT_AMBIENT, LIGHT_DISTANT, LIGHT_SPHERE, LIGHT_SPOT = 0, 1, 2, 3, 4
 
 
 class Light(ctypes.Structure):
     _fields_ = [("type", ctypes.c_int), ("visible", ctypes.c_int), ("position", ctypes.c_float * 3),
                 ("edge1", ctypes.c_float * 3), ("edge2", ctypes.c_float * 3), ("color", ctypes.c_float * 3),
                 ("intensity", ctypes.c_float), ("direction", ctypes.c_float * 3), ("angularDiameter", ctypes.c_float),
-                ("radius", ctypes.c_float)]
+                ("radius", ctypes.c_float), ("openingAngle", ctypes.c_float), ("penumbraAngle", ctypes.c_float),
+                ("innerRadius", ctypes.c_float)]
 
 
 class ToneMapper(ctypes.Structure):
@@ -120,6 +121,18 @@ def sphere_light(position, radius=0.0, intensity=1.0, color=(1, 1, 1), visible=T
     return L
 
 
+def spot_light(position, direction, intensity=1.0, color=(1, 1, 1), opening_angle=180.0, penumbra_angle=5.0,
+               radius=0.0, inner_radius=0.0, visible=True):
+    """Radiative intensity = color * intensity; radius 0 is a point spot."""
+    L = Light()
+    L.type, L.visible = LIGHT_SPOT, int(visible)
+    L.position[:], L.direction[:] = list(position), list(direction)
+    L.openingAngle, L.penumbraAngle = float(opening_angle), float(penumbra_angle)
+    L.radius, L.innerRadius = float(radius), float(inner_radius)
+    L.color[:], L.intensity = list(color), float(intensity)
+    return L
+
+
 def light_from_dict(L):
     """A b200 light from the dict form the tests and the oracle share."""
     t = L["type"]
@@ -130,6 +143,9 @@ def light_from_dict(L):
         return distant_light(L["direction"], L["intensity"], col, L.get("angular_diameter", 0.0), vis)
     if t == "sphere":
         return sphere_light(L["position"], L.get("radius", 0.0), L["intensity"], col, vis)
+    if t == "spot":
+        return spot_light(L["position"], L["direction"], L["intensity"], col, L.get("opening_angle", 180.0),
+                          L.get("penumbra_angle", 5.0), L.get("radius", 0.0), L.get("inner_radius", 0.0), vis)
     return ambient_light(L["intensity"], col, visible=vis)
 
 

@@ -891,7 +891,7 @@ int b200_scene_set_lights(b200_scene s, const b200_light *lights, int n) {
     for (int i = 0; i < n; i++) {
       const b200_light &L = lights[i];
       require(L.type == B200_LIGHT_QUAD || L.type == B200_LIGHT_AMBIENT || L.type == B200_LIGHT_DISTANT ||
-                  L.type == B200_LIGHT_SPHERE,
+                  L.type == B200_LIGHT_SPHERE || L.type == B200_LIGHT_SPOT,
               "unsupported light type");
       LightD &d = h[i];
       std::memset(&d, 0, sizeof(d));
@@ -923,6 +923,29 @@ int b200_scene_set_lights(b200_scene s, const b200_light *lights, int n) {
         d.radius = L.radius;
         d.intensity = d.radiance;
         d.radiance = L.radius > 0.f ? mul(d.radiance, 1.f / (float(M_PI) * L.radius * L.radius)) : mk(0.f, 0.f, 0.f);
+      } else if (L.type == B200_LIGHT_SPOT) {
+        // SpotLight::commit / createSh / processIntensityQuantityType (INTENSITY)
+        const V3 dir = mk(L.direction[0], L.direction[1], L.direction[2]);
+        const float len = std::sqrt(dot(dir, dir));
+        require(len > 0.f && std::isfinite(len), "spot light: zero direction");
+        d.position = mk(L.position[0], L.position[1], L.position[2]);
+        d.dir = mul(dir, 1.f / len);
+        const V3 c0 = std::fabs(dir.x) < std::fabs(dir.y) ? mk(0.f, dir.z, dir.y) : mk(dir.z, 0.f, dir.x);
+        V3 c90 = cross(c0, d.dir);
+        c90 = mul(c90, 1.f / std::sqrt(dot(c90, c90)));
+        d.edge1 = cross(d.dir, c90);
+        d.edge2 = c90;
+        const float opening = std::fmin(std::fmax(L.openingAngle, 0.f), 360.f);
+        const float penumbra = std::fmin(std::fmax(L.penumbraAngle, 0.f), 0.5f * opening);
+        const float deg = float(M_PI / 180.0);
+        d.cosAngle = std::cos(deg * 0.5f * opening);
+        d.conePdf = 1.f / (std::cos(deg * (0.5f * opening - penumbra)) - d.cosAngle);
+        d.radius = std::fmax(0.f, L.radius);
+        d.innerRadius = std::fmin(std::fmax(L.innerRadius, 0.f), 0.999f * d.radius);
+        const float ring = float(M_PI) * (d.radius * d.radius - d.innerRadius * d.innerRadius);
+        d.ppdf = 1.f / ring;
+        d.intensity = d.radiance;
+        d.radiance = d.radius > 0.f ? mul(d.radiance, 1.f / ring) : mk(0.f, 0.f, 0.f);
       }
     }
     // uniform light-selection CDF (Distribution1D_create over all-ones)

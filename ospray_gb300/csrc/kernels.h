@@ -78,18 +78,21 @@ struct KernelScope {
   }
 };
 
-enum LightType : int { LIGHT_QUAD = 0, LIGHT_AMBIENT = 1, LIGHT_DISTANT = 2, LIGHT_SPHERE = 3 };
+enum LightType : int { LIGHT_QUAD = 0, LIGHT_AMBIENT = 1, LIGHT_DISTANT = 2, LIGHT_SPHERE = 3, LIGHT_SPOT = 4 };
 
 // light in world space; quad: nnormal = normalize(edge2 x edge1), ppdf = 1/area
 // quad: position, edge1/2, nnormal, ppdf; distant: dir (towards the light),
 // cosAngle, conePdf, radiance = irradiance; sphere: position, radius,
-// radiance (of the surface), intensity (radiative intensity of a point light)
+// radiance (of the surface), intensity (radiative intensity of a point light);
+// spot: position, dir (it points to), edge1/edge2 = c0/c90 (ring frame),
+// cosAngle = cosAngleMax, conePdf = cosAngleScale, ppdf = ring area pdf,
+// radius / innerRadius, radiance, intensity
 struct LightD {
   int type, visible;
   V3 position, edge1, edge2, nnormal, radiance;
   float ppdf;
   V3 dir, intensity;
-  float cosAngle, conePdf, radius;
+  float cosAngle, conePdf, radius, innerRadius;
 };
 
 struct PtParamsD {

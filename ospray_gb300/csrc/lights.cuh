@@ -6,6 +6,8 @@
 //   DirectionalLight_sample / _eval     lights/DirectionalLight.ispc:14-90
 //   PointLight_sample / _eval           lights/PointLight.ispc:32-158 (sphere
 //                                       lights; no intensity distribution)
+//   SpotLight_sample / _eval            lights/SpotLight.ispc:26-170 (no
+//                                       intensity distribution)
 #pragma once
 #include "kernels.h"
 #include "pt_bsdf.cuh"
@@ -130,6 +132,31 @@ B200_D LightSampleD sampleLight(const LightD &L, V3 P, V3 Ng, V3 Ns, float sx, f
     r.weight = L.radiance;  // irradiance: pdf / pdf cancel
     return r;
   }
+  if (L.type == LIGHT_SPOT) {
+    r.dir = L.position - P;
+    if (L.radius > 0.f) {  // uniformSampleRing (math/sampling.ih:114-122) in the (c0, c90) frame
+      const float rr = sqrtf((1.f - sx) * (L.innerRadius * L.innerRadius) + sx * (L.radius * L.radius));
+      float sp, cp;
+      sincosf(2.f * PI_F * sy, &sp, &cp);
+      r.dir = L.edge1 * (rr * cp) + L.edge2 * (rr * sp) + r.dir;
+    }
+    const float dist2 = fdot(r.dir, r.dir);
+    const float invdist = 1.f / sqrtf(dist2);
+    r.dir = r.dir * invdist;
+    r.dist = dist2 * invdist;
+    const float cosAngle = -fdot(L.dir, r.dir);
+    float w = fminf(fmaxf((cosAngle - L.cosAngle) * L.conePdf, 0.f), 1.f);
+    if (L.radius > 0.f) {
+      r.pdf = L.ppdf * (dist2 / fabsf(cosAngle));
+      w = w / r.pdf;
+      r.weight = L.radiance * w;
+    } else {
+      r.pdf = INFINITY;
+      w *= fabsf(cosAngle);
+      r.weight = L.intensity * ((invdist * invdist) * w);
+    }
+    return r;
+  }
   if (L.type == LIGHT_SPHERE) {
     const V3 d = L.position - P;
     const float dist2 = fdot(d, d);
@@ -218,6 +245,24 @@ B200_D V3 evalLight(const LightD &L, V3 P, V3 Ns, V3 dir, float minDist, float m
     if (INFINITY <= maxDist && L.cosAngle < 0.99999988f && fdot(L.dir, dir) > L.cosAngle) {
       pdf = L.conePdf;
       return L.radiance * L.conePdf;
+    }
+    return splat(0.f);
+  }
+  if (L.type == LIGHT_SPOT) {
+    if (L.radius > 0.f) {  // the emitting ring
+      const float cosAngle = -fdot(L.dir, dir);
+      if (cosAngle > L.cosAngle) {
+        const V3 vp = P - L.position;
+        const float t = fdot(vp, L.dir) * (1.f / cosAngle);
+        if (t > minDist && t <= maxDist) {
+          const V3 vd = vp + dir * t;
+          const float d2 = fdot(vd, vd);
+          if (d2 < L.radius * L.radius && d2 > L.innerRadius * L.innerRadius) {
+            pdf = L.ppdf * (t * t / fabsf(cosAngle));
+            return L.radiance * fminf(fmaxf((cosAngle - L.cosAngle) * L.conePdf, 0.f), 1.f);
+          }
+        }
+      }
     }
     return splat(0.f);
   }

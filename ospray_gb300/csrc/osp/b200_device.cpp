@@ -21,7 +21,7 @@ bool known(OSPDataType kind, const std::string &t) {
   switch (kind) {
     case OSP_GEOMETRY: return t == "mesh" || t == "sphere" || t == "box";
     case OSP_MATERIAL: return t == "principled" || t == "obj";
-    case OSP_LIGHT: return t == "quad" || t == "ambient" || t == "distant" || t == "sphere";
+    case OSP_LIGHT: return t == "quad" || t == "ambient" || t == "distant" || t == "sphere" || t == "spot";
     case OSP_CAMERA: return t == "perspective";
     case OSP_RENDERER: return t == "ao" || t == "pathtracer" || t == "scivis";
     case OSP_VOLUME: return t == "structuredRegular";

@@ -298,6 +298,29 @@ void LightObj::commit(B200Device &dev) {
       dev.warn("sphere light: unsupported 'intensityQuantity' value");
       light.intensity = 0.f;
     }
+  } else if (type == "spot") {
+    // SpotLight::commit / processIntensityQuantityType (lights/SpotLight.cpp:76-140)
+    light.type = B200_LIGHT_SPOT;
+    const float dz[3] = {0.f, 0.f, 1.f};
+    getVec3("position", light.position, kZero3);
+    getVec3("direction", light.direction, dz);
+    light.openingAngle = getFloat("openingAngle", 180.f);
+    light.penumbraAngle = getFloat("penumbraAngle", 5.f);
+    light.radius = std::fmax(0.f, getFloat("radius", 0.f));
+    light.innerRadius = std::fmin(std::fmax(getFloat("innerRadius", 0.f), 0.f), 0.999f * light.radius);
+    const int q = getInt("intensityQuantity", OSP_INTENSITY_QUANTITY_INTENSITY);
+    const float opening = std::fmin(std::fmax(light.openingAngle, 0.f), 360.f);
+    const float c = std::cos(float(M_PI) * opening * 0.5f / 180.f);
+    const float capCosInt = float(M_PI) * (1.f - c * c);
+    const float ring = float(M_PI) * (light.radius * light.radius - light.innerRadius * light.innerRadius);
+    if (q == OSP_INTENSITY_QUANTITY_POWER) {
+      light.intensity /= capCosInt;
+    } else if (q == OSP_INTENSITY_QUANTITY_RADIANCE && light.radius > 0.f) {
+      light.intensity *= ring;  // radiance x ring area
+    } else if (q != OSP_INTENSITY_QUANTITY_INTENSITY) {
+      dev.warn("spot light: unsupported 'intensityQuantity' value");
+      light.intensity = 0.f;
+    }
   } else {  // ambient
     light.type = B200_LIGHT_AMBIENT;
     const int q = getInt("intensityQuantity", OSP_INTENSITY_QUANTITY_RADIANCE);

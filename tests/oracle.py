@@ -97,6 +97,11 @@ class PtWorld:
             elif L["type"] == "sphere":
                 pos = np.asarray(L["position"], np.float32)
                 lib().or_pt_add_sphere_light(self.h, _p(pos), float(L.get("radius", 0.0)), _p(rad))
+            elif L["type"] == "spot":
+                pos, d = np.asarray(L["position"], np.float32), np.asarray(L["direction"], np.float32)
+                lib().or_pt_add_spot_light(self.h, _p(pos), _p(d), float(L.get("opening_angle", 180.0)),
+                                           float(L.get("penumbra_angle", 5.0)), float(L.get("radius", 0.0)),
+                                           float(L.get("inner_radius", 0.0)), _p(rad))
             else:
                 lib().or_pt_add_ambient_light(self.h, _p(rad))
 
@@ -144,6 +149,7 @@ def lib():
         L.or_pt_add_ambient_light.argtypes = [P, P]
         L.or_pt_add_distant_light.argtypes = [P, P, F, P]
         L.or_pt_add_sphere_light.argtypes = [P, P, F, P]
+        L.or_pt_add_spot_light.argtypes = [P, P, P, F, F, F, F, P]
         L.or_render_pt.argtypes = [P, P, ctypes.POINTER(OrCamera), ctypes.POINTER(OrPtParams), I, I, I, I, I,
                                    P, P, P, I]
         L.or_ray_count.restype = ctypes.c_uint64
@@ -303,7 +309,8 @@ def render_scivis_volume(model, cam, pixel_filter, w, h, spp=1, sampling_rate=1.
 class OrScivisLight(ctypes.Structure):
     _fields_ = [("kind", ctypes.c_int), ("visible", ctypes.c_int), ("pos", ctypes.c_float * 3),
                 ("e1", ctypes.c_float * 3), ("e2", ctypes.c_float * 3), ("radiance", ctypes.c_float * 3),
-                ("dir", ctypes.c_float * 3), ("angularDiameter", ctypes.c_float), ("radius", ctypes.c_float)]
+                ("dir", ctypes.c_float * 3), ("angularDiameter", ctypes.c_float), ("radius", ctypes.c_float),
+                ("openingAngle", ctypes.c_float), ("penumbraAngle", ctypes.c_float), ("innerRadius", ctypes.c_float)]
 
 
 class OrScivisMaterial(ctypes.Structure):
@@ -328,7 +335,7 @@ def render_scivis(scene, volume, cam, lights, materials, w, h, spp=1, pixel_filt
     L = (OrScivisLight * max(1, len(lights)))()
     for i, l in enumerate(lights):
         rad = np.asarray(l.get("color", (1, 1, 1)), np.float32) * np.float32(l["intensity"])
-        L[i].kind = {"quad": 0, "ambient": 1, "distant": 2, "sphere": 3}[l["type"]]
+        L[i].kind = {"quad": 0, "ambient": 1, "distant": 2, "sphere": 3, "spot": 4}[l["type"]]
         L[i].visible = int(l.get("visible", True))
         L[i].radiance[:] = [float(x) for x in rad]
         if l["type"] == "quad":
@@ -339,6 +346,13 @@ def render_scivis(scene, volume, cam, lights, materials, w, h, spp=1, pixel_filt
         elif l["type"] == "sphere":
             L[i].pos[:] = [float(x) for x in l["position"]]
             L[i].radius = float(l.get("radius", 0.0))
+        elif l["type"] == "spot":
+            L[i].pos[:] = [float(x) for x in l["position"]]
+            L[i].dir[:] = [float(x) for x in l["direction"]]
+            L[i].openingAngle = float(l.get("opening_angle", 180.0))
+            L[i].penumbraAngle = float(l.get("penumbra_angle", 5.0))
+            L[i].radius = float(l.get("radius", 0.0))
+            L[i].innerRadius = float(l.get("inner_radius", 0.0))
     M = (OrScivisMaterial * max(1, len(materials)))()
     for i, m in enumerate(materials):
         if m is None:

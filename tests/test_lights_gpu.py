@@ -2,7 +2,8 @@
 lights/DirectionalLight.ispc, lights/PointLight.ispc) in the path tracer and
 the SciVis renderer, against the oracle's restatement: a world lit by a
 distant light with a 5-degree cone, a sphere light of radius 1.5, a point
-light (radius 0) and an ambient light.  Same tolerances as the other path
+light (radius 0), a ring spot light, a point spot light and an ambient
+light (SpotLight, lights/SpotLight.ispc).  Same tolerances as the other path
 tracer parity tests: first hits exact, colours within 1e-3 on most pixels
 and image means within 3 standard errors."""
 import numpy as np
@@ -17,6 +18,10 @@ LIGHTS = [dict(type="distant", direction=(-0.3, -1.0, -0.2), angular_diameter=5.
                color=(1.0, 0.95, 0.85)),
           dict(type="sphere", position=(5.0, 14.0, 5.0), radius=1.5, intensity=400.0, color=(1.0, 0.9, 0.8)),
           dict(type="sphere", position=(2.0, 12.0, 8.0), radius=0.0, intensity=150.0),
+          dict(type="spot", position=(8.0, 13.0, 2.0), direction=(-0.3, -1.0, 0.3), opening_angle=60.0,
+               penumbra_angle=10.0, radius=0.8, inner_radius=0.2, intensity=300.0),
+          dict(type="spot", position=(1.0, 11.0, 1.0), direction=(0.4, -1.0, 0.4), opening_angle=40.0,
+               penumbra_angle=5.0, intensity=200.0),
           dict(type="ambient", intensity=0.1)]
 
 

@@ -139,9 +139,9 @@ def test_ao_through_ospray_api_matches_oracle(osp_device):
 def test_unsupported_types_report_errors(osp_device):
     L = osp_device
     dev = L.ospGetCurrentDevice()
-    assert L.ospNewLight(b"spot") is None
+    assert L.ospNewLight(b"hdri") is None
     assert L.ospDeviceGetLastErrorCode(dev) == 2
-    assert b"spot" in L.ospDeviceGetLastErrorMsg(dev)
+    assert b"hdri" in L.ospDeviceGetLastErrorMsg(dev)
     assert L.ospNewCamera(b"orthographic") is None
     L.ospDeviceRelease(dev)
 
