@@ -43,8 +43,8 @@ L2_FLUSH_BYTES = 512 << 20
 # launches / their algorithmic bytes); the summaries under profiles/ give the
 # commands.  Scaled to the bench's launches by their algorithmic bytes.
 TRAFFIC = {
-    # 12 trace launches of one 1920x1080 16 spp frame: 12.6 GB DRAM vs 130.4 GB algorithmic
-    "pt_instanced_spheres_1080p": {"dram_per_alg_byte": 0.0966,
+    # 12 trace launches of one 1920x1080 16 spp frame: 12.6 GB DRAM vs 130.3 GB algorithmic
+    "pt_instanced_spheres_1080p": {"dram_per_alg_byte": 0.0968,
                                    "source": "profiles/k_trace_queue_pt_instanced_1080p_traffic.md"},
     # one 1024x1024 4 spp frame: 2.65 GB DRAM vs 12.6 GB algorithmic (32 B per sample)
     "scivis_volume_512cube_1024": {"dram_per_alg_byte": 0.21,
