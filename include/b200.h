@@ -132,9 +132,17 @@ int b200_trace(b200_scene scene, const float *rays, int64_t n, int occlusion, fl
                void *stream);
 
 /* ---- camera (PerspectiveCamera::commit, modules/cpu/camera/PerspectiveCamera.cpp:30-117) */
+/* type: B200_CAMERA_PERSPECTIVE (PerspectiveCamera, fovy / aspect),
+ * B200_CAMERA_ORTHOGRAPHIC (OrthographicCamera::commit
+ * camera/OrthographicCamera.cpp:25-50: `height` of the image plane and
+ * aspect) or B200_CAMERA_PANORAMIC (PanoramicCamera, equirectangular; no
+ * stereo).  Stereo, depth of field and motion blur are not built. */
+enum { B200_CAMERA_PERSPECTIVE = 0, B200_CAMERA_ORTHOGRAPHIC = 1, B200_CAMERA_PANORAMIC = 2 };
 typedef struct {
   float position[3], direction[3], up[3];
   float fovy, aspect, nearClip;
+  int type;     /* default 0: perspective */
+  float height; /* orthographic: image-plane height (OSPRay default 1) */
 } b200_camera_desc;
 
 /* ---- framebuffer (LocalFrameBuffer, modules/cpu/fb/LocalFB.cpp:23-226;

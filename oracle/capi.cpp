@@ -33,6 +33,8 @@ A3 fromRowMajor(const float *X) {
 struct OrCamera {
   float pos[3], dir[3], up[3];
   float fovy, aspect, nearClip;
+  int type;  // 0 perspective, 1 orthographic, 2 panoramic
+  float height;  // orthographic image height
 };
 
 extern "C" {
@@ -159,7 +161,7 @@ void or_trace(void *sp, const float *rays, int n, int occlusion, float *out_f, u
 // exactly as the renderers generate them.  out: 8 floats per ray.
 void or_camera_rays(const OrCamera *c, int pixelFilter, int W, int H, int spp, int frameID, float *out) {
   const Camera cam = makeCamera({c->pos[0], c->pos[1], c->pos[2]}, {c->dir[0], c->dir[1], c->dir[2]},
-                                {c->up[0], c->up[1], c->up[2]}, c->fovy, c->aspect, c->nearClip);
+                                {c->up[0], c->up[1], c->up[2]}, c->fovy, c->aspect, c->nearClip, c->type, c->height);
   PixelFilter pf;
   pf.init(pixelFilter);
   const V2 rcpSize = {1.f / float(W), 1.f / float(H)};
@@ -206,7 +208,7 @@ void or_render_ao(void *sp, const OrCamera *c, int pixelFilter, int W, int H, in
                   float aoRadius, float aoIntensity, const float *bg, int frames, OrFrame *out, int nthreads) {
   const Scene &s = *static_cast<Scene *>(sp);
   const Camera cam = makeCamera({c->pos[0], c->pos[1], c->pos[2]}, {c->dir[0], c->dir[1], c->dir[2]},
-                                {c->up[0], c->up[1], c->up[2]}, c->fovy, c->aspect, c->nearClip);
+                                {c->up[0], c->up[1], c->up[2]}, c->fovy, c->aspect, c->nearClip, c->type, c->height);
   PixelFilter pf;
   pf.init(pixelFilter);
   FrameBuffer fb;

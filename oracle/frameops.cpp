@@ -128,12 +128,14 @@ void or_tonemap_coefficients(const OrToneMapper *tm, float *out5) {
 struct OrCameraP {
   float pos[3], dir[3], up[3];
   float fovy, aspect, nearClip;
+  int type;  // 0 perspective, 1 orthographic, 2 panoramic
+  float height;  // orthographic image height
 };
 
 int or_pick(void *sp, const OrCameraP *c, float sx, float sy, float *pos3, uint32_t *ids3) {
   const Scene &s = *static_cast<Scene *>(sp);
   const Camera cam = makeCamera({c->pos[0], c->pos[1], c->pos[2]}, {c->dir[0], c->dir[1], c->dir[2]},
-                                {c->up[0], c->up[1], c->up[2]}, c->fovy, c->aspect, c->nearClip);
+                                {c->up[0], c->up[1], c->up[2]}, c->fovy, c->aspect, c->nearClip, c->type, c->height);
   const Ray ray = cameraRay(cam, {sx, sy});
   Hit h;
   if (!s.intersect(ray, h)) {

@@ -299,6 +299,8 @@ using namespace orc;
 struct OrCameraPT {
   float pos[3], dir[3], up[3];
   float fovy, aspect, nearClip;
+  int type;  // 0 perspective, 1 orthographic, 2 panoramic
+  float height;  // orthographic image height
 };
 
 struct OrPtScene {
@@ -382,7 +384,7 @@ void or_render_pt(void *scp, void *ptp, const OrCameraPT *cam, const OrPtParams 
   const Scene &sc = *static_cast<Scene *>(scp);
   const OrPtScene &pt = *static_cast<OrPtScene *>(ptp);
   const Camera c = makeCamera({cam->pos[0], cam->pos[1], cam->pos[2]}, {cam->dir[0], cam->dir[1], cam->dir[2]},
-                              {cam->up[0], cam->up[1], cam->up[2]}, cam->fovy, cam->aspect, cam->nearClip);
+                              {cam->up[0], cam->up[1], cam->up[2]}, cam->fovy, cam->aspect, cam->nearClip, cam->type, cam->height);
   PixelFilter pf;
   pf.init(pp->pixelFilter);
   PtParams p = {pp->spp, pp->maxPathLength, pp->roulettePathLength, pp->maxScatteringEvents, pp->lightSamples,

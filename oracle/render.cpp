@@ -15,8 +15,30 @@ const Tables &tables() {
 std::atomic<uint64_t> g_rayCount{0};
 thread_local uint64_t tl_rays = 0;  // flushed into g_rayCount once per image row
 
-Camera makeCamera(V3 pos, V3 dir, V3 up, float fovy, float aspect, float nearClip) {
+Camera makeCamera(V3 pos, V3 dir, V3 up, float fovy, float aspect, float nearClip, int type, float height) {
   Camera c;
+  c.type = type;
+  c.nearClip = nearClip;
+  if (type == 1) {
+    const V3 d = normalize(dir);
+    V3 du = normalize(cross(d, up));
+    V3 dv = cross(du, d) * height;
+    du = du * (height * aspect);
+    c.dir_00 = d;
+    c.du_size = du;
+    c.dv_up = dv;
+    c.org = pos - 0.5f * du - 0.5f * dv;
+    return c;
+  }
+  if (type == 2) {
+    const V3 vz = -normalize(dir);
+    const V3 vx = normalize(cross(up, vz));
+    c.du_size = vx;
+    c.dv_up = cross(vz, vx);
+    c.dir_00 = vz;
+    c.org = pos;
+    return c;
+  }
   const float deg2rad = float(1.745329251994329576923690768489e-2);
   const float ipy = 2.f * std::tan(deg2rad * (0.5f * fovy));
   const float ipx = ipy * aspect;

@@ -22,15 +22,32 @@
 
 namespace orc {
 
+// type 0 perspective (dir_00, du_size, dv_up as PerspectiveCamera), 1
+// orthographic (org = lower-left corner, dir_00 = the view direction), 2
+// panoramic (org, frame vx, vy, vz in du_size, dv_up, dir_00)
 struct Camera {
   V3 org, dir_00, du_size, dv_up;
   float nearClip;
+  int type = 0;
 };
 
-// PerspectiveCamera::commit without stereo/aperture/motion blur
-Camera makeCamera(V3 pos, V3 dir, V3 up, float fovy, float aspect, float nearClip);
+// PerspectiveCamera::commit (camera/PerspectiveCamera.cpp:30-117),
+// OrthographicCamera::commit (camera/OrthographicCamera.cpp:25-50) and
+// PanoramicCamera::commit (camera/PanoramicCamera.cpp:30-47), without stereo,
+// aperture or motion blur
+Camera makeCamera(V3 pos, V3 dir, V3 up, float fovy, float aspect, float nearClip, int type = 0,
+                  float height = 1.f);
 
 inline Ray cameraRay(const Camera &c, V2 screen) {
+  if (c.type == 1)  // OrthographicCamera_initRay (camera/OrthographicCamera.ispc:11-49)
+    return {c.org + screen.x * c.du_size + screen.y * c.dv_up, c.nearClip, c.dir_00, INFINITY};
+  if (c.type == 2) {  // PanoramicCamera_initRay (camera/PanoramicCamera.ispc:12-90), mono
+    const float phi = 6.28318530717958647692f * screen.x, theta = 3.14159265358979323846f * screen.y;
+    const float st = std::sin(theta), ct = std::cos(theta);
+    const V3 l = {std::cos(phi) * st, std::sin(phi) * st, ct};
+    const V3 d = c.du_size * -l.y + c.dv_up * -l.z + c.dir_00 * l.x;
+    return {c.org, c.nearClip, d, INFINITY};
+  }
   const V3 d = c.dir_00 + screen.x * c.du_size + screen.y * c.dv_up;
   return {c.org, c.nearClip, normalize(d), INFINITY};
 }

@@ -682,6 +682,8 @@ uint64_t or_volume_sample_count(int reset) {
 struct OrCameraV {
   float pos[3], dir[3], up[3];
   float fovy, aspect, nearClip;
+  int type;  // 0 perspective, 1 orthographic, 2 panoramic
+  float height;  // orthographic image height
 };
 
 // SciVis frames of a volume-only world; rows [y0, y1) (y1 <= 0: all)
@@ -689,7 +691,7 @@ void or_render_scivis_volume(void *mp, const OrCameraV *c, int pixelFilter, int 
                              const float *bg, int frames, int y0, int y1, float *color, int nthreads) {
   const VolumeModel &m = *static_cast<VolumeModel *>(mp);
   const Camera cam = makeCamera({c->pos[0], c->pos[1], c->pos[2]}, {c->dir[0], c->dir[1], c->dir[2]},
-                                {c->up[0], c->up[1], c->up[2]}, c->fovy, c->aspect, c->nearClip);
+                                {c->up[0], c->up[1], c->up[2]}, c->fovy, c->aspect, c->nearClip, c->type, c->height);
   PixelFilter pf;
   pf.init(pixelFilter);
   FrameBuffer fb;
@@ -803,7 +805,7 @@ void or_render_scivis(void *scp, void *mp, const OrCameraV *c, const OrScivisPar
   SvParams p = {pp->spp, pp->samplingRate, {pp->bg[0], pp->bg[1], pp->bg[2], pp->bg[3]}, pp->shadows,
                 pp->visibleLights, pp->aoSamples, pp->aoRadius, pp->minContribution};
   const Camera cam = makeCamera({c->pos[0], c->pos[1], c->pos[2]}, {c->dir[0], c->dir[1], c->dir[2]},
-                                {c->up[0], c->up[1], c->up[2]}, c->fovy, c->aspect, c->nearClip);
+                                {c->up[0], c->up[1], c->up[2]}, c->fovy, c->aspect, c->nearClip, c->type, c->height);
   PixelFilter pf;
   pf.init(pp->pixelFilter);
   FrameBuffer fb;

@@ -40,7 +40,7 @@ class B200Error(RuntimeError):
 class CameraDesc(ctypes.Structure):
     _fields_ = [("position", ctypes.c_float * 3), ("direction", ctypes.c_float * 3),
                 ("up", ctypes.c_float * 3), ("fovy", ctypes.c_float), ("aspect", ctypes.c_float),
-                ("nearClip", ctypes.c_float)]
+                ("nearClip", ctypes.c_float), ("type", ctypes.c_int), ("height", ctypes.c_float)]
 
 
 class AOParams(ctypes.Structure):
@@ -538,8 +538,14 @@ class Frame:
             pass
 
 
-def camera_desc(position, direction, up=(0, 1, 0), fovy=60.0, aspect=1.0, near_clip=1e-6):
+CAMERA_PERSPECTIVE, CAMERA_ORTHOGRAPHIC, CAMERA_PANORAMIC = 0, 1, 2
+
+
+def camera_desc(position, direction, up=(0, 1, 0), fovy=60.0, aspect=1.0, near_clip=1e-6, kind=CAMERA_PERSPECTIVE,
+                height=1.0):
+    """kind: CAMERA_PERSPECTIVE (fovy), CAMERA_ORTHOGRAPHIC (image `height`) or CAMERA_PANORAMIC."""
     c = CameraDesc()
+    c.type, c.height = int(kind), float(height)
     c.position[:] = list(map(float, position))
     c.direction[:] = list(map(float, direction))
     c.up[:] = list(map(float, up))

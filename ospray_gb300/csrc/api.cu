@@ -242,6 +242,33 @@ CameraD makeCamera(const b200_camera_desc &c) {
   const V3 pos = mk(c.position[0], c.position[1], c.position[2]);
   const V3 dir = mk(c.direction[0], c.direction[1], c.direction[2]);
   const V3 up = mk(c.up[0], c.up[1], c.up[2]);
+  if (c.type == B200_CAMERA_ORTHOGRAPHIC) {  // OrthographicCamera::commit
+    const float h = c.height;
+    const V3 d = normalize(dir);
+    V3 du = normalize(cross(d, up));
+    const V3 dv = mul(cross(du, d), h);
+    du = mul(du, h * c.aspect);
+    CameraD cam;
+    cam.type = 1;
+    cam.dir_00 = d;
+    cam.du_size = du;
+    cam.dv_up = dv;
+    cam.org = sub(sub(pos, mul(0.5f, du)), mul(0.5f, dv));
+    cam.nearClip = c.nearClip > 0.f ? c.nearClip : 0.f;
+    return cam;
+  }
+  if (c.type == B200_CAMERA_PANORAMIC) {  // PanoramicCamera::commit
+    const V3 vz = mul(normalize(dir), -1.f);
+    const V3 vx = normalize(cross(up, vz));
+    CameraD cam;
+    cam.type = 2;
+    cam.du_size = vx;
+    cam.dv_up = cross(vz, vx);
+    cam.dir_00 = vz;
+    cam.org = pos;
+    cam.nearClip = c.nearClip > 0.f ? c.nearClip : 0.f;
+    return cam;
+  }
   const float deg2rad = float(1.745329251994329576923690768489e-2);
   const float ipy = 2.f * std::tan(deg2rad * (0.5f * c.fovy));
   const float ipx = ipy * c.aspect;
@@ -257,6 +284,7 @@ CameraD makeCamera(const b200_camera_desc &c) {
   cam.du_size = du;
   cam.dv_up = dv;
   cam.nearClip = c.nearClip > 0.f ? c.nearClip : 0.f;
+  cam.type = 0;
   return cam;
 }
 

@@ -22,7 +22,7 @@ bool known(OSPDataType kind, const std::string &t) {
     case OSP_GEOMETRY: return t == "mesh" || t == "sphere" || t == "box";
     case OSP_MATERIAL: return t == "principled" || t == "obj";
     case OSP_LIGHT: return t == "quad" || t == "ambient" || t == "distant" || t == "sphere" || t == "spot";
-    case OSP_CAMERA: return t == "perspective";
+    case OSP_CAMERA: return t == "perspective" || t == "orthographic" || t == "panoramic";
     case OSP_RENDERER: return t == "ao" || t == "pathtracer" || t == "scivis";
     case OSP_VOLUME: return t == "structuredRegular";
     case OSP_TRANSFER_FUNCTION: return t == "piecewiseLinear";

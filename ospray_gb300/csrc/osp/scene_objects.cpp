@@ -423,9 +423,13 @@ void CameraObj::commit(B200Device &dev) {
   desc.fovy = getFloat("fovy", 60.f);
   desc.aspect = getFloat("aspect", 1.f);
   desc.nearClip = getFloat("nearClip", 1e-6f);
-  if (getFloat("apertureRadius", 0.f) != 0.f) dev.warn("perspective camera: depth of field is not supported by the b200 device");
+  // OrthographicCamera::commit "height"; PanoramicCamera (equirectangular)
+  desc.type = type == "orthographic" ? B200_CAMERA_ORTHOGRAPHIC
+                                     : (type == "panoramic" ? B200_CAMERA_PANORAMIC : B200_CAMERA_PERSPECTIVE);
+  desc.height = getFloat("height", 1.f);
+  if (getFloat("apertureRadius", 0.f) != 0.f) dev.warn("camera: depth of field is not supported by the b200 device");
   if (getInt("stereoMode", OSP_STEREO_NONE) != OSP_STEREO_NONE)
-    dev.warn("perspective camera: stereo is not supported by the b200 device");
+    dev.warn("camera: stereo is not supported by the b200 device");
 }
 
 void RendererObj::commit(B200Device &) {

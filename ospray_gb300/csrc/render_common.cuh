@@ -14,9 +14,13 @@
 
 namespace b200 {
 
+// type 0 perspective; 1 orthographic (org = lower-left corner of the image
+// plane, dir_00 = view direction); 2 panoramic (frame vx, vy, vz in
+// du_size, dv_up, dir_00)
 struct CameraD {
   V3 org, dir_00, du_size, dv_up;
   float nearClip;
+  int type;
 };
 
 struct PixelFilterD {
@@ -46,12 +50,26 @@ B200_D bool pixelActive(const FrameD &fb, int x, int y) {
 }
 
 B200_D Ray cameraRay(const CameraD &c, float sx, float sy) {
-  const V3 d = add(add(c.dir_00, mul(sx, c.du_size)), mul(sy, c.dv_up));
   Ray r;
-  r.org = c.org;
   r.tnear = c.nearClip;
-  r.dir = normalize(d);
   r.tfar = INFINITY;
+  if (c.type == 1) {  // OrthographicCamera_initRay (camera/OrthographicCamera.ispc:11-49)
+    r.org = add(add(c.org, mul(sx, c.du_size)), mul(sy, c.dv_up));
+    r.dir = c.dir_00;
+    return r;
+  }
+  if (c.type == 2) {  // PanoramicCamera_initRay (camera/PanoramicCamera.ispc:12-90), mono
+    float sp, cp, st, ct;
+    sincosf(6.28318530717958647692f * sx, &sp, &cp);
+    sincosf(3.14159265358979323846f * sy, &st, &ct);
+    const V3 l = mk(cp * st, sp * st, ct);
+    r.org = c.org;
+    r.dir = add(add(mul(c.du_size, -l.y), mul(c.dv_up, -l.z)), mul(c.dir_00, l.x));
+    return r;
+  }
+  const V3 d = add(add(c.dir_00, mul(sx, c.du_size)), mul(sy, c.dv_up));
+  r.org = c.org;
+  r.dir = normalize(d);
   return r;
 }
 

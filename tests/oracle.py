@@ -18,7 +18,8 @@ P, I, U32, F = ctypes.c_void_p, ctypes.c_int, ctypes.c_uint32, ctypes.c_float
 
 
 class OrCamera(ctypes.Structure):
-    _fields_ = [("pos", F * 3), ("dir", F * 3), ("up", F * 3), ("fovy", F), ("aspect", F), ("nearClip", F)]
+    _fields_ = [("pos", F * 3), ("dir", F * 3), ("up", F * 3), ("fovy", F), ("aspect", F), ("nearClip", F),
+                ("type", I), ("height", F)]
 
 
 class OrFrame(ctypes.Structure):
@@ -181,10 +182,12 @@ def _p(a):
     return ctypes.c_void_p(a.ctypes.data) if a is not None else None
 
 
-def camera(position, direction, up=(0, 1, 0), fovy=60.0, aspect=1.0, near_clip=1e-6):
+def camera(position, direction, up=(0, 1, 0), fovy=60.0, aspect=1.0, near_clip=1e-6, kind=0, height=1.0):
+    """kind 0 perspective, 1 orthographic (image `height`), 2 panoramic."""
     c = OrCamera()
     c.pos[:], c.dir[:], c.up[:] = list(position), list(direction), list(up)
     c.fovy, c.aspect, c.nearClip = fovy, aspect, near_clip
+    c.type, c.height = int(kind), float(height)
     return c
 
 

@@ -142,7 +142,7 @@ def test_unsupported_types_report_errors(osp_device):
     assert L.ospNewLight(b"hdri") is None
     assert L.ospDeviceGetLastErrorCode(dev) == 2
     assert b"hdri" in L.ospDeviceGetLastErrorMsg(dev)
-    assert L.ospNewCamera(b"orthographic") is None
+    assert L.ospNewCamera(b"omnidirectional") is None
     L.ospDeviceRelease(dev)
 
 
