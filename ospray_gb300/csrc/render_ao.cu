@@ -68,8 +68,15 @@ B200_D float computeAO(const SamplerTables *T, const Scene &sc, const DG &dg, in
   return 1.f - float(hits) / float(sampleCnt);
 }
 
+// Resident blocks per SM the single-frame AO kernel is compiled for.  1 (no
+// register cap, 153 registers, 3 blocks per SM) measured best on the 512^2
+// AO workload: 1,417 Mrays/s against 1,313 / 1,268 / 1,240 when capped for
+// 4 / 5 / 6 blocks (the cap spills the traversal and shading state).
+#ifndef B200_AO_MINBLOCKS
+#define B200_AO_MINBLOCKS 1
+#endif
 template <bool STATS>
-__global__ void __launch_bounds__(128) k_render_ao(const SamplerTables *T, Scene sc, CameraD cam, PixelFilterD pf, AOParamsD p, FrameD fb) {
+__global__ void __launch_bounds__(128, B200_AO_MINBLOCKS) k_render_ao(const SamplerTables *T, Scene sc, CameraD cam, PixelFilterD pf, AOParamsD p, FrameD fb) {
   const int x = blockIdx.x * 16 + (threadIdx.x & 15);
   const int y = blockIdx.y * 8 + (threadIdx.x >> 4);
   TraceStats ts = {0, 0, 0, 0};
