@@ -236,6 +236,8 @@ typedef struct {
   float backgroundColor[4];
   int pixelFilter;   /* B200_PF_* */
   int collectStats;  /* nonzero: count rays / node visits / primitive tests */
+  float volumeSamplingRate; /* the scene's volume, composited in front of each layer (render/ao/volumes.ispc);
+                               <= 0: 1 */
 } b200_ao_params;
 
 /* ---- lights of the world (QuadLight::commit lights/QuadLight.cpp:68-108,

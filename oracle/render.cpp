@@ -213,6 +213,7 @@ void fbAccumulate(FrameBuffer &fb, int x, int y, const ScreenSample &s) {
 }
 
 float *g_auxNormal = nullptr, *g_auxAlbedo = nullptr;
+AOVolume g_aoVolume;
 void copyAux(const FrameBuffer &fb) {
   if (g_auxNormal) std::memcpy(g_auxNormal, fb.normal.data(), fb.normal.size() * 4);
   if (g_auxAlbedo) std::memcpy(g_auxAlbedo, fb.albedo.data(), fb.albedo.size() * 4);
@@ -267,10 +268,22 @@ void renderAO(const Scene &s, const Camera &cam, const PixelFilter &pf, const AO
         V4 out = {0, 0, 0, 0};
         bool first = true;
         const float tfar0 = ray.tfar;
+        RandomSampler rs;
+        rs.init(uint32_t(x + W * y), sid);
         while (out.w < 0.99f) {
           Hit hit;
           tl_rays++;
           const bool h = s.intersect(ray, hit);
+          if (g_aoVolume.vm) {
+            Ray vr = ray;
+            vr.tfar = h ? hit.t : ray.tfar;
+            if (g_aoVolume.overlaps(g_aoVolume.vm, vr)) {
+              const float jitter = rs.getFloat();
+              const V4 vc = g_aoVolume.integrate(g_aoVolume.vm, vr, jitter, g_aoVolume.samplingRate);
+              const float f = 1.f - out.w;
+              out = {out.x + f * vc.x, out.y + f * vc.y, out.z + f * vc.z, out.w + f * vc.w};
+            }
+          }
           V4 blended;
           if (h) {
             const DG dg = postIntersect(s, ray, hit);

@@ -121,6 +121,16 @@ void fbAccumulate(FrameBuffer &fb, int x, int y, const ScreenSample &s);
 // where the renderers copy the accumulated normal / albedo channels after a
 // call (null: not wanted); set by or_set_aux_output
 extern float *g_auxNormal, *g_auxAlbedo;
+
+// the AO renderer's volume (or_set_ao_volume): integrateVolumeIntervals of
+// render/ao/volumes.ispc composited in front of each layer (null: none)
+struct AOVolume {
+  const void *vm = nullptr;
+  float samplingRate = 1.f;
+  bool (*overlaps)(const void *vm, const Ray &r) = nullptr;
+  V4 (*integrate)(const void *vm, const Ray &r, float jitter, float samplingRate) = nullptr;
+};
+extern AOVolume g_aoVolume;
 void copyAux(const FrameBuffer &fb);
 
 template <class F>

@@ -389,21 +389,24 @@ bool svVolumeOverlaps(const Volume &vol, const Ray &ray) {
   return !it.done;
 }
 
-// integrateVolumeIntervals (render/ao/volumes.ispc): opacity accumulated
-// front to back until 0.99; NaN samples are skipped inside sampleVolume
-float svVolumeAlpha(const VolumeModel &m, const Ray &ray, float jitter, float samplingRate) {
+// integrateVolumeIntervals (render/ao/volumes.ispc:251-352): colour and
+// opacity accumulated front to back until 0.99; NaN samples are skipped
+// inside the sample search.  The SciVis shadow and AO rays use the opacity,
+// the AO renderer both.
+V4 aoVolumeIntegrate(const VolumeModel &m, const Ray &ray, float jitter, float samplingRate) {
   IntervalIter it;
   it.init(m.vol, ray.org, ray.dir, ray.tnear, ray.tfar);
   const float nominalDeltaT = std::fmin(m.vol.spacing.x, std::fmin(m.vol.spacing.y, m.vol.spacing.z));
   float alpha = 0.f, distance = INFINITY, iuDistance = jitter, iuLength = 0.f, step = 0.f;
   float ilo = 0.f, ihi = INFINITY;
+  V3 color = v3(0.f);
   for (int g = 0; g < (1 << 24) && alpha < 0.99f; g++) {
     float dt = 0.f, val = NAN;
     for (int h = 0; h < (1 << 24) && std::isnan(val); h++) {
       float emptySpace = 0.f;
       while (iuDistance > iuLength) {
         const float prevUpper = ihi;
-        if (!it.next(ilo, ihi)) return alpha;
+        if (!it.next(ilo, ihi)) return {color.x, color.y, color.z, alpha};
         emptySpace += std::fmax(ilo - prevUpper, 0.f);
         iuDistance -= iuLength;
         step = nominalDeltaT / samplingRate;
@@ -418,9 +421,14 @@ float svVolumeAlpha(const VolumeModel &m, const Ray &ray, float jitter, float sa
     }
     const V4 c = m.tf.get(val);
     const float op = 1.f - std::exp(-c.w * dt * m.densityScale);
+    color = color + ((1.f - alpha) * op) * v3(c.x, c.y, c.z);
     alpha = alpha + (1.f - alpha) * op;
   }
-  return alpha;
+  return {color.x, color.y, color.z, alpha};
+}
+
+float svVolumeAlpha(const VolumeModel &m, const Ray &ray, float jitter, float samplingRate) {
+  return aoVolumeIntegrate(m, ray, jitter, samplingRate).w;
 }
 
 inline float svLuminance(V3 c) { return 0.212671f * c.x + 0.715160f * c.y + 0.072169f * c.z; }
@@ -670,6 +678,18 @@ void *or_volume_new(const float *data, int nx, int ny, int nz, const float *orig
 }
 
 void or_volume_free(void *m) { delete static_cast<VolumeModel *>(m); }
+
+// the AO renderer's volume and volumeSamplingRate for later or_render_ao calls (null: none)
+void or_set_ao_volume(void *m, float samplingRate) {
+  g_aoVolume.vm = m;
+  g_aoVolume.samplingRate = samplingRate;
+  g_aoVolume.overlaps = [](const void *vm, const Ray &r) {
+    return svVolumeOverlaps(static_cast<const VolumeModel *>(vm)->vol, r);
+  };
+  g_aoVolume.integrate = [](const void *vm, const Ray &r, float jitter, float rate) {
+    return aoVolumeIntegrate(*static_cast<const VolumeModel *>(vm), r, jitter, rate);
+  };
+}
 
 void or_volume_set_gradient_shading(void *m, float scale) { static_cast<VolumeModel *>(m)->gradientShadingScale = scale; }
 

@@ -47,7 +47,7 @@ class AOParams(ctypes.Structure):
     _fields_ = [("pixelSamples", ctypes.c_int), ("aoSamples", ctypes.c_int),
                 ("aoDistance", ctypes.c_float), ("aoIntensity", ctypes.c_float),
                 ("backgroundColor", ctypes.c_float * 4), ("pixelFilter", ctypes.c_int),
-                ("collectStats", ctypes.c_int)]
+                ("collectStats", ctypes.c_int), ("volumeSamplingRate", ctypes.c_float)]
 
 
 LIGHT_QUAD, LIGHT_AMBIENT, LIGHT_DISTANT, LIGHT_SPHERE, LIGHT_SPOT = 0, 1, 2, 3, 4
@@ -554,8 +554,9 @@ def camera_desc(position, direction, up=(0, 1, 0), fovy=60.0, aspect=1.0, near_c
 
 
 def ao_params(spp=1, ao_samples=1, ao_distance=1e20, ao_intensity=1.0, bg=(0, 0, 0, 0), pixel_filter=PF_GAUSS,
-              stats=False):
+              stats=False, volume_sampling_rate=1.0):
     p = AOParams()
+    p.volumeSamplingRate = float(volume_sampling_rate)
     p.collectStats = int(bool(stats))
     p.pixelSamples, p.aoSamples = int(spp), int(ao_samples)
     p.aoDistance, p.aoIntensity = float(ao_distance), float(ao_intensity)

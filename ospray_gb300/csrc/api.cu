@@ -233,6 +233,7 @@ AOParamsD makeAOParams(const b200_ao_params &p) {
   d.aoSamples = p.aoSamples;
   d.aoRadius = p.aoDistance;
   d.aoIntensity = p.aoIntensity;
+  d.volumeSamplingRate = p.volumeSamplingRate > 0.f ? p.volumeSamplingRate : 1.f;
   for (int k = 0; k < 4; k++) d.bg[k] = p.backgroundColor[k];
   return d;
 }
@@ -903,7 +904,7 @@ int b200_render_ao(b200_scene s, const b200_camera_desc *camera, const b200_ao_p
     cudaStream_t st = stream ? (cudaStream_t)stream : sc->dev->stream;
     fb->beginFrame(p->pixelSamples, st);
     check(launchRenderAO(sc->dev->tables, sc->view(), makeCamera(*camera), sc->dev->filter(p->pixelFilter), d,
-                         fb->view(), p->collectStats != 0, st, sc->dev->timer),
+                         fb->view(), p->collectStats != 0, st, sc->dev->timer, sc->hasVolume ? &sc->vol : nullptr),
           "AO launch");
     fb->frameID++;
     framePostProcess(fb, st);

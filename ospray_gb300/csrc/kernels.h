@@ -200,6 +200,7 @@ struct AOParamsD {
   int spp, aoSamples;
   float aoRadius, aoIntensity;
   float bg[4];
+  float volumeSamplingRate;
 };
 
 // ---- batches: many render requests in one wavefront
@@ -252,6 +253,6 @@ cudaError_t launchPick(const Scene &sc, const CameraD &cam, float sx, float sy, 
 cudaError_t launchTrace(const Scene &sc, const float4 *rays, long long n, int occlusion, float *outF, uint32_t *outI,
                         cudaStream_t st);
 cudaError_t launchRenderAO(const SamplerTables *T, const Scene &sc, const CameraD &cam, const PixelFilterD &pf, const AOParamsD &p,
-                           const FrameD &fb, bool stats, cudaStream_t st, KernelTimer *kt = nullptr);
+                           const FrameD &fb, bool stats, cudaStream_t st, KernelTimer *kt = nullptr, const VolumeD *vol = nullptr);
 
 }  // namespace b200

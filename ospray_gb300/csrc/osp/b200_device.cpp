@@ -274,7 +274,6 @@ OSPFuture B200Device::renderFrame(OSPFrameBuffer hf, OSPRenderer hr, OSPCamera h
     check(b200_frame_set_variance_threshold(f->fb, r->varianceThreshold));
     check(b200_event_record(dev_, &fut->start));
     if (r->type == "ao") {
-      if (w->hasVolume) warn("ao renderer: volumes are not rendered by the b200 device");
       check(b200_render_ao(w->scene, &c->desc, &r->ao, f->fb, nullptr));
     } else if (r->type == "pathtracer") {
       if (w->hasVolume) warn("pathtracer: volumes are not rendered by the b200 device");

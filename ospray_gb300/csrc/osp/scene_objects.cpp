@@ -450,6 +450,7 @@ void RendererObj::commit(B200Device &) {
     std::memcpy(ao.backgroundColor, bg, 16);
     ao.pixelFilter = pf;
     ao.collectStats = 0;
+    ao.volumeSamplingRate = getFloat("volumeSamplingRate", 1.f);  // AORenderer::commit
   } else if (type == "pathtracer") {
     pt.pixelSamples = spp;
     pt.maxPathLength = maxDepth;

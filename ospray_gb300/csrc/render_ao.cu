@@ -5,6 +5,7 @@
 //   computeAO                  modules/cpu/render/util.ispc:12-54
 #include "kernels.h"
 #include "render_common.cuh"
+#include "volume.cuh"
 
 namespace b200 {
 
@@ -75,8 +76,10 @@ B200_D float computeAO(const SamplerTables *T, const Scene &sc, const DG &dg, in
 #ifndef B200_AO_MINBLOCKS
 #define B200_AO_MINBLOCKS 1
 #endif
-template <bool STATS>
-__global__ void __launch_bounds__(128, B200_AO_MINBLOCKS) k_render_ao(const SamplerTables *T, Scene sc, CameraD cam, PixelFilterD pf, AOParamsD p, FrameD fb) {
+// VOL: the scene's volume is composited in front of each layer
+// (integrateVolumeIntervals, render/ao/volumes.ispc:251-352)
+template <bool STATS, bool VOL>
+__global__ void __launch_bounds__(128, B200_AO_MINBLOCKS) k_render_ao(const SamplerTables *T, Scene sc, CameraD cam, PixelFilterD pf, AOParamsD p, FrameD fb, VolumeD vol) {
   const int x = blockIdx.x * 16 + (threadIdx.x & 15);
   const int y = blockIdx.y * 8 + (threadIdx.x >> 4);
   TraceStats ts = {0, 0, 0, 0};
@@ -97,9 +100,24 @@ __global__ void __launch_bounds__(128, B200_AO_MINBLOCKS) k_render_ao(const Samp
     float z = INFINITY;
     uint32_t prim = INVALID_ID, geom = INVALID_ID, inst = INVALID_ID;
     V3 sn = splat(0.f), sal = splat(0.f);
+    PCG rs;
+    if (VOL) rs.init(uint32_t(x + fb.W * y), sid);
     for (int layer = 0; layer < 64 && o[3] < 0.99f; layer++) {
       HitRec h;
       const bool hit = traceScene<false, STATS>(sc, ray, h, &ts);
+      if (VOL) {
+        Ray vr = ray;
+        vr.tfar = hit ? h.t : ray.tfar;
+        if (volumeOverlaps(vol, vr)) {
+          const float jitter = rs.getFloat();
+          const float4 vc = volumeIntegrateAO<true>(vol, vr, jitter, p.volumeSamplingRate);
+          const float f = fsub(1.f, o[3]);
+          o[0] = fadd(o[0], fmul(f, vc.x));
+          o[1] = fadd(o[1], fmul(f, vc.y));
+          o[2] = fadd(o[2], fmul(f, vc.z));
+          o[3] = fadd(o[3], fmul(f, vc.w));
+        }
+      }
       float bl[4];
       if (hit) {
         const DG dg = postIntersect(sc, ray, h);
@@ -202,13 +220,13 @@ cudaError_t launchPick(const Scene &sc, const CameraD &cam, float sx, float sy, 
 }
 
 cudaError_t launchRenderAO(const SamplerTables *T, const Scene &sc, const CameraD &cam, const PixelFilterD &pf, const AOParamsD &p,
-                           const FrameD &fb, bool stats, cudaStream_t st, KernelTimer *kt) {
+                           const FrameD &fb, bool stats, cudaStream_t st, KernelTimer *kt, const VolumeD *vol) {
   dim3 grid((fb.W + 15) / 16, (fb.H + 7) / 8);
   KernelScope ks(kt, KK_AO, st);
-  if (stats)
-    k_render_ao<true><<<grid, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(T, sc, cam, pf, p, fb);
-  else
-    k_render_ao<false><<<grid, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(T, sc, cam, pf, p, fb);
+  const VolumeD v = vol ? *vol : VolumeD{};
+  auto k = stats ? (vol ? k_render_ao<true, true> : k_render_ao<true, false>)
+                 : (vol ? k_render_ao<false, true> : k_render_ao<false, false>);
+  k<<<grid, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(T, sc, cam, pf, p, fb, v);
   return cudaGetLastError();
 }
 

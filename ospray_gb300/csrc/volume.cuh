@@ -281,22 +281,26 @@ B200_D bool volumeOverlaps(const VolumeD &v, const Ray &ray) {
   return !it.done;
 }
 
-// integrateVolumeIntervals (render/ao/volumes.ispc): opacity accumulated
-// front to back until 0.99, alpha += (1 - alpha) * (1 - exp(-a dt density));
-// NaN samples are skipped inside the sample search.
-B200_D float volumeAlpha(const VolumeD &v, const Ray &ray, float jitter, float samplingRate) {
+// integrateVolumeIntervals (render/ao/volumes.ispc:251-352): colour and
+// opacity accumulated front to back until 0.99, alpha += (1 - alpha) *
+// (1 - exp(-a dt density)), colour += (1 - alpha) * op * rgb (COLOR); NaN
+// samples are skipped inside the sample search.  Shadow and AO rays of the
+// SciVis renderer use the opacity; the AO renderer composites both.
+template <bool COLOR>
+B200_D float4 volumeIntegrateAO(const VolumeD &v, const Ray &ray, float jitter, float samplingRate) {
   IntervalIter it;
   it.init(v, ray.org, ray.dir, ray.tnear, ray.tfar);
   const float nominalDeltaT = fminf(v.spacing.x, fminf(v.spacing.y, v.spacing.z));
   float alpha = 0.f, distance = INFINITY, iuDistance = jitter, iuLength = 0.f, step = 0.f;
   float ilo = 0.f, ihi = INFINITY;
+  V3 color = splat(0.f);
   for (int g = 0; g < (1 << 24) && alpha < 0.99f; g++) {
     float dt = 0.f, val = NAN;
     for (int h = 0; h < (1 << 24) && isnan(val); h++) {
       float emptySpace = 0.f;
       while (iuDistance > iuLength) {
         const float prevUpper = ihi;
-        if (!it.next(v, ilo, ihi)) return alpha;
+        if (!it.next(v, ilo, ihi)) return make_float4(color.x, color.y, color.z, alpha);
         emptySpace += fmaxf(ilo - prevUpper, 0.f);
         iuDistance -= iuLength;
         step = nominalDeltaT / samplingRate;
@@ -313,9 +317,14 @@ B200_D float volumeAlpha(const VolumeD &v, const Ray &ray, float jitter, float s
     }
     const float4 c = tfGet(v, val);
     const float op = 1.f - expf(-c.w * dt * v.densityScale);
+    if (COLOR) color = color + ((1.f - alpha) * op) * mk(c.x, c.y, c.z);
     alpha = alpha + (1.f - alpha) * op;
   }
-  return alpha;
+  return make_float4(color.x, color.y, color.z, alpha);
+}
+
+B200_D float volumeAlpha(const VolumeD &v, const Ray &ray, float jitter, float samplingRate) {
+  return volumeIntegrateAO<false>(v, ray, jitter, samplingRate).w;
 }
 
 }  // namespace

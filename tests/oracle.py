@@ -141,6 +141,7 @@ def lib():
         L.or_scene_add_quad_mesh.argtypes = [P, P, I, P, I]
         L.or_scene_add_boxes.argtypes = [P, P, I]
         L.or_set_aux_output.argtypes = [P, P]
+        L.or_set_ao_volume.argtypes = [P, F]
         L.or_scene_add_spheres.argtypes = [P, P, I]
         L.or_scene_add_instance.argtypes = [P, I, U32, U32, P, I]
         L.or_pt_new.restype = P
@@ -251,6 +252,22 @@ def render_ao(scene, cam, pixel_filter, w, h, spp=1, ao_samples=1, ao_radius=1e2
     lib().or_render_ao(scene.h, ctypes.byref(cam), pixel_filter, w, h, spp, ao_samples, ao_radius, ao_intensity,
                        _p(bgv), frames, ctypes.byref(fr), nthreads)
     return dict(color=color, depth=depth, primID=ids[0], geomID=ids[1], instID=ids[2])
+
+
+class AOVolume:
+    """Within the block, oracle AO renders composite `model` (a
+    VolumeModel) in front of each layer at `rate` (the AO renderer's
+    volumeSamplingRate)."""
+
+    def __init__(self, model, rate=1.0):
+        self.model, self.rate = model, rate
+
+    def __enter__(self):
+        lib().or_set_ao_volume(self.model.h, float(self.rate))
+        return self
+
+    def __exit__(self, *a):
+        lib().or_set_ao_volume(None, 1.0)
 
 
 class AuxOutput:

@@ -163,3 +163,25 @@ def test_scivis_gradient_shading_volume_only(b200_device):
     close = np.all(np.abs(col - ref) <= 1e-3 * np.maximum(1.0, np.abs(ref)) + 1e-5, axis=2)
     assert close.mean() >= 0.99, close.mean()
     assert np.abs(col.mean(axis=(0, 1)) - ref.mean(axis=(0, 1))).max() < 1e-4
+
+
+def test_ao_renderer_composites_the_volume(world, b200_device):
+    """The AO renderer over a world with surfaces and a volume
+    (AORenderer_renderSample with integrateVolumeIntervals,
+    render/ao/AORenderer.ispc:59-80, render/ao/volumes.ispc:251-352): the
+    volume's colour and opacity in front of each layer, against the oracle."""
+    import ospray_gb300 as og
+    g, o, ov = world[True]
+    fb = og.Frame(b200_device, W, H, og.FB_COLOR | og.FB_DEPTH | og.FB_ID_PRIMITIVE)
+    cam = og.camera_desc(CAM["position"], CAM["direction"], CAM["up"], fovy=CAM["fovy"], aspect=CAM["aspect"])
+    og.render_ao(g, cam, og.ao_params(spp=2, ao_samples=1, volume_sampling_rate=0.5, bg=(0.1, 0.1, 0.2, 1.0)), fb)
+    ocam = oracle.camera(CAM["position"], CAM["direction"], CAM["up"], fovy=CAM["fovy"], aspect=CAM["aspect"])
+    with oracle.AOVolume(ov, 0.5):
+        ref = oracle.render_ao(o, ocam, 2, W, H, spp=2, ao_samples=1, bg=(0.1, 0.1, 0.2, 1.0))
+    plain = oracle.render_ao(o, ocam, 2, W, H, spp=2, ao_samples=1, bg=(0.1, 0.1, 0.2, 1.0))
+    assert np.abs(ref["color"] - plain["color"]).max() > 0.05  # the volume is seen
+    assert np.mean(fb.read(og.FB_ID_PRIMITIVE) == ref["primID"]) >= 0.999
+    c, r = fb.read(og.FB_COLOR), ref["color"]
+    close = np.all(np.abs(c - r) <= 1e-3 * np.maximum(1.0, np.abs(r)) + 1e-5, axis=2)
+    assert close.mean() >= 0.99, close.mean()
+    assert np.abs(c.mean(axis=(0, 1)) - r.mean(axis=(0, 1))).max() < 1e-4
