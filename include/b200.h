@@ -336,6 +336,14 @@ int b200_scene_set_volume(b200_scene scene, const float *data, int nx, int ny, i
  * non-finite value is refused.  Kept across b200_scene_set_volume calls. */
 int b200_scene_set_volume_gradient_shading(b200_scene scene, float gradientShadingScale);
 
+/* The volume's instance transform (Instance "transform" of the instance
+ * whose group holds the volumetric model; rays go to volume space by its
+ * inverse, transformRay render/scivis/volumes.ispc:311-313, and gradient
+ * normals back by the inverse transpose): xfm 3x4 row-major as
+ * b200_scene_add_instance takes it, null = identity.  Kept across
+ * b200_scene_set_volume calls; a singular transform is refused. */
+int b200_scene_set_volume_transform(b200_scene scene, const float *xfm);
+
 /* ---- SciVis renderer (SciVis::commit render/scivis/SciVis.cpp:27-84,
  *      SciVis_renderSample render/scivis/SciVis.ispc:24-222,
  *      SciVis_computeShading render/scivis/surfaces.ispc:90-128,

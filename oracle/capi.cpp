@@ -7,9 +7,8 @@
 
 using namespace orc;
 
-namespace {
 // rkcommon rcp(AffineSpace3f): adjoint / det in float, p' = -(l' p)
-A3 rcpAffine(const A3 &a) {
+A3 orc::rcpAffine(const A3 &a) {
   const L3 &l = a.l;
   const float det = dot(l.vx, cross(l.vy, l.vz));
   const L3 adjT = {cross(l.vy, l.vz), cross(l.vz, l.vx), cross(l.vx, l.vy)};
@@ -20,6 +19,7 @@ A3 rcpAffine(const A3 &a) {
   r.p = -xfmVector(il, a.p);
   return r;
 }
+namespace {
 A3 fromRowMajor(const float *X) {
   A3 a;
   a.l.vx = {X[0], X[4], X[8]};

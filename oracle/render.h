@@ -131,6 +131,9 @@ struct AOVolume {
   V4 (*integrate)(const void *vm, const Ray &r, float jitter, float samplingRate) = nullptr;
 };
 extern AOVolume g_aoVolume;
+
+// rkcommon rcp(AffineSpace3f) (capi.cpp)
+A3 rcpAffine(const A3 &a);
 void copyAux(const FrameBuffer &fb);
 
 template <class F>

@@ -128,6 +128,13 @@ struct VolumeModel {
   TransferFunction tf;
   float densityScale = 1.f;
   float gradientShadingScale = 0.f;  // VolumetricModel::commit volume/VolumetricModel.cpp:76
+  bool identity = true;  // the instance transform of the volume (rays go to volume space by rcp)
+  A3 rcp;
+  // transformRay(tRay, instance->rcp_xfm) (render/scivis/volumes.ispc:311-313)
+  Ray toVolume(const Ray &r) const {
+    if (identity) return r;
+    return {xfmPoint(rcp, r.org), r.tnear, xfmVector(rcp.l, r.dir), r.tfar};
+  }
   void finalize() {
     vol.buildCells();
     vol.cellEmpty.resize(vol.cmin.size());
@@ -225,8 +232,9 @@ struct IntervalIter {
   }
 };
 
-V4 integrateVolume(const VolumeModel &m, const Ray &ray, float jitter, float samplingRate, float minContribution,
+V4 integrateVolume(const VolumeModel &m, const Ray &wray, float jitter, float samplingRate, float minContribution,
                    uint64_t &samples) {
+  const Ray ray = m.toVolume(wray);
   IntervalIter it;
   it.init(m.vol, ray.org, ray.dir, ray.tnear, ray.tfar);
   const float nominalDeltaT = std::fmin(m.vol.spacing.x, std::fmin(m.vol.spacing.y, m.vol.spacing.z));
@@ -383,9 +391,10 @@ struct SvWorld {
 
 // does [ray.tnear, ray.tfar] overlap the volume's grid box (the test that
 // starts IntervalIter)
-bool svVolumeOverlaps(const Volume &vol, const Ray &ray) {
+bool svVolumeOverlaps(const VolumeModel &m, const Ray &wray) {
+  const Ray ray = m.toVolume(wray);
   IntervalIter it;
-  it.init(vol, ray.org, ray.dir, ray.tnear, ray.tfar);
+  it.init(m.vol, ray.org, ray.dir, ray.tnear, ray.tfar);
   return !it.done;
 }
 
@@ -393,7 +402,8 @@ bool svVolumeOverlaps(const Volume &vol, const Ray &ray) {
 // opacity accumulated front to back until 0.99; NaN samples are skipped
 // inside the sample search.  The SciVis shadow and AO rays use the opacity,
 // the AO renderer both.
-V4 aoVolumeIntegrate(const VolumeModel &m, const Ray &ray, float jitter, float samplingRate) {
+V4 aoVolumeIntegrate(const VolumeModel &m, const Ray &wray, float jitter, float samplingRate) {
+  const Ray ray = m.toVolume(wray);
   IntervalIter it;
   it.init(m.vol, ray.org, ray.dir, ray.tnear, ray.tfar);
   const float nominalDeltaT = std::fmin(m.vol.spacing.x, std::fmin(m.vol.spacing.y, m.vol.spacing.z));
@@ -443,7 +453,7 @@ V3 svLightAlpha(const SvWorld &w, const SvParams &p, Ray ray, RandomSampler &rs,
     if (w.vm) {
       Ray vr = ray;
       vr.tfar = h ? hit.t : ray.tfar;
-      if (svVolumeOverlaps(w.vm->vol, vr)) {
+      if (svVolumeOverlaps(*w.vm, vr)) {
         const float jitter = rs.getFloat();
         alpha = alpha * (1.f - svVolumeAlpha(*w.vm, vr, jitter, p.samplingRate * quality));
       }
@@ -530,9 +540,10 @@ SvShading svComputeShading(const SvWorld &w, const SvParams &p, const DG &dg, co
 // transfer-function RGBA, Ns = Ng = -normalize(gradient), epsilon = dt / 2,
 // and blended into the sample by gradientShadingScale before the Beer-law
 // opacity.  Shadow and AO rays of the shading draw from the ray's sampler.
-V4 integrateVolumeShaded(const SvWorld &w, const SvParams &p, const Ray &ray, float jitter, int px, int py,
+V4 integrateVolumeShaded(const SvWorld &w, const SvParams &p, const Ray &wray, float jitter, int px, int py,
                          uint32_t sid, RandomSampler &rs, uint64_t &samples) {
   const VolumeModel &m = *w.vm;
+  const Ray ray = m.toVolume(wray);
   IntervalIter it;
   it.init(m.vol, ray.org, ray.dir, ray.tnear, ray.tfar);
   const float nominalDeltaT = std::fmin(m.vol.spacing.x, std::fmin(m.vol.spacing.y, m.vol.spacing.z));
@@ -566,10 +577,10 @@ V4 integrateVolumeShaded(const SvWorld &w, const SvParams &p, const Ray &ray, fl
         if (dot(grad, grad) > 1e-6f) {
           DG dg;
           dg.epsilon = dt / 2.f;
-          dg.Ns = dg.Ng = normalize(-grad);
-          dg.P = pos;
+          dg.Ns = dg.Ng = normalize(m.identity ? -grad : xfmVector(transposed(m.rcp.l), -grad));
+          dg.P = wray.org + newDistance * wray.dir;  // world space
           dg.primID = dg.geomID = dg.instID = 0xFFFFFFFFu;
-          const SvShading sh = svComputeShading(w, p, dg, nullptr, c, ray.dir, px, py, sid, rs);
+          const SvShading sh = svComputeShading(w, p, dg, nullptr, c, wray.dir, px, py, sid, rs);
           const float a = 1.f - svLuminance(sh.transmission), f = m.gradientShadingScale;
           c = {lerpf(f, c.x, sh.shadedColor.x), lerpf(f, c.y, sh.shadedColor.y), lerpf(f, c.z, sh.shadedColor.z),
                lerpf(f, c.w, a)};
@@ -601,7 +612,7 @@ ScreenSample svRenderSample(const SvWorld &w, const SvParams &p, Ray ray, int x,
     if (w.vm) {
       Ray vr = ray;
       vr.tfar = rayT;
-      if (svVolumeOverlaps(w.vm->vol, vr)) {
+      if (svVolumeOverlaps(*w.vm, vr)) {
         const float jitter = rs.getFloat();
         const V4 vc = w.vm->gradientShadingScale > 0.f
                           ? integrateVolumeShaded(w, p, vr, jitter, x, y, sid, rs, samples)
@@ -684,11 +695,25 @@ void or_set_ao_volume(void *m, float samplingRate) {
   g_aoVolume.vm = m;
   g_aoVolume.samplingRate = samplingRate;
   g_aoVolume.overlaps = [](const void *vm, const Ray &r) {
-    return svVolumeOverlaps(static_cast<const VolumeModel *>(vm)->vol, r);
+    return svVolumeOverlaps(*static_cast<const VolumeModel *>(vm), r);
   };
   g_aoVolume.integrate = [](const void *vm, const Ray &r, float jitter, float rate) {
     return aoVolumeIntegrate(*static_cast<const VolumeModel *>(vm), r, jitter, rate);
   };
+}
+
+// the volume's instance transform, 3x4 row-major (null: identity)
+void or_volume_set_transform(void *mp, const float *X) {
+  VolumeModel &m = *static_cast<VolumeModel *>(mp);
+  m.identity = X == nullptr;
+  if (X) {
+    A3 a;
+    a.l.vx = {X[0], X[4], X[8]};
+    a.l.vy = {X[1], X[5], X[9]};
+    a.l.vz = {X[2], X[6], X[10]};
+    a.p = {X[3], X[7], X[11]};
+    m.rcp = rcpAffine(a);
+  }
 }
 
 void or_volume_set_gradient_shading(void *m, float scale) { static_cast<VolumeModel *>(m)->gradientShadingScale = scale; }

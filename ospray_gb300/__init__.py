@@ -285,6 +285,7 @@ def lib():
             "b200_scene_set_volume": (I, [P, P, I, I, I, P, P, P, I, P, I, P, F]),
             "b200_frame_set_variance_threshold": (I, [P, F]),
             "b200_scene_set_volume_gradient_shading": (I, [P, F]),
+            "b200_scene_set_volume_transform": (I, [P, P]),
             "b200_render_scivis": (I, [P, ctypes.POINTER(CameraDesc), ctypes.POINTER(ScivisParams), P, I, P, P]),
             "b200_render_pt": (I, [P, ctypes.POINTER(CameraDesc), ctypes.POINTER(PTParams), P, I, P, P]),
         }
@@ -425,6 +426,11 @@ class Scene:
         vr = np.asarray(value_range, np.float32)
         self.device._check(lib().b200_scene_set_volume(self._h, _ptr(d), nx, ny, nz, _ptr(o), _ptr(sp), _ptr(c),
                                                        len(c), _ptr(op), len(op), _ptr(vr), float(density_scale)))
+
+    def set_volume_transform(self, xfm):
+        """The volume's instance transform (3x4 row-major) or None."""
+        x = None if xfm is None else np.ascontiguousarray(xfm, np.float32).reshape(12)
+        self.device._check(lib().b200_scene_set_volume_transform(self._h, _ptr(x) if x is not None else None))
 
     def set_volume_gradient_shading(self, scale):
         """The volumetric model's gradientShadingScale (0: off)."""

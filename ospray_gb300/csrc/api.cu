@@ -1105,6 +1105,8 @@ int b200_scene_set_volume(b200_scene s, const float *data, int nx, int ny, int n
     v.vhi = valueRange[1];
     v.densityScale = densityScale;
     v.gradientShadingScale = sc->gradientShadingScale;
+    v.identity = sc->volIdentity ? 1 : 0;
+    v.rcp = sc->volRcp;
     check(brickVolume(v, linear, sc->dVolData, st), "brick volume");
     check(cudaStreamSynchronize(st), "brick volume");
     check(cudaMalloc(&sc->dCellEmpty, size_t(v.cx) * v.cy * v.cz), "alloc macrocells");
@@ -1112,6 +1114,21 @@ int b200_scene_set_volume(b200_scene s, const float *data, int nx, int ny, int n
     v.cellEmpty = sc->dCellEmpty;
     check(cudaStreamSynchronize(st), "volume commit");
     sc->hasVolume = true;
+  });
+}
+
+int b200_scene_set_volume_transform(b200_scene s, const float *xfm) {
+  if (!s) return B200_INVALID_ARGUMENT;
+  SceneObj *sc = reinterpret_cast<SceneObj *>(s);
+  return guarded(sc->dev, [&]() {
+    sc->volIdentity = xfm == nullptr;
+    if (xfm) {
+      for (int k = 0; k < 12; k++) require(std::isfinite(xfm[k]), "volume transform is not finite");
+      rcpAffine(xfm, sc->volRcp.m);
+      for (int k = 0; k < 12; k++) require(std::isfinite(sc->volRcp.m[k]), "volume transform is singular");
+    }
+    sc->vol.identity = sc->volIdentity ? 1 : 0;
+    sc->vol.rcp = sc->volRcp;
   });
 }
 

@@ -99,6 +99,8 @@ struct SceneObj {
   bool hasVolume = false;
   VolumeD vol = {};
   float gradientShadingScale = 0.f;  // kept across b200_scene_set_volume calls
+  bool volIdentity = true;           // the volume's instance transform (kept likewise)
+  Xfm volRcp = {};
   float *dVolData = nullptr, *dTfOpacity = nullptr;
   float3 *dTfColor = nullptr;
   uint8_t *dCellEmpty = nullptr;

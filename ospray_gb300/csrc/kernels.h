@@ -119,6 +119,8 @@ struct VolumeD {
   int ncolor, nopacity;
   float vlo, vhi, densityScale;
   float gradientShadingScale;  // VolumetricModel "gradientShadingScale" (0: off)
+  int identity;                // no instance transform; else rays go to volume space by rcp
+  Xfm rcp;
 };
 
 struct ScivisParamsD {

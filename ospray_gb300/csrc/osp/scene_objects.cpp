@@ -391,13 +391,13 @@ void WorldObj::commit(B200Device &dev) {
           dev.warn("world: the b200 device renders one volumetric model per world; further ones are ignored");
           continue;
         }
-        if (!inst->identity) dev.warn("world: instance transforms of volumes are not supported by the b200 device");
         VolumeObj *v = vm->volume.get();
         TransferFunctionObj *tf = vm->tf.get();
         dev.check(b200_scene_set_volume(s, v->voxels.data(), v->dims[0], v->dims[1], v->dims[2], v->origin,
                                         v->spacing, tf->color.data(), int(tf->color.size() / 3), tf->opacity.data(),
                                         int(tf->opacity.size()), tf->range, vm->densityScale));
         dev.check(b200_scene_set_volume_gradient_shading(s, vm->gradientShadingScale));
+        dev.check(b200_scene_set_volume_transform(s, inst->identity ? nullptr : inst->xfm));
         hasVolume = true;
       }
     }

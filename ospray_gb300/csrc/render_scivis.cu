@@ -180,8 +180,9 @@ B200_D SvShading svComputeShading(const SamplerTables *T, const Scene &sc, const
 // opacity.  The shading's shadow and AO rays draw from the ray's sampler.
 template <bool STATS>
 B200_D float4 integrateShaded(const SamplerTables *T, const Scene &sc, const VolumeD &vol, const ScivisSurfD &S,
-                              float samplingRate, const Ray &ray, float jitter, int x, int y, uint32_t sid, PCG &rs,
+                              float samplingRate, const Ray &wray, float jitter, int x, int y, uint32_t sid, PCG &rs,
                               uint32_t &samples, TraceStats *ts) {
+  const Ray ray = toVolume(vol, wray);  // sampling in volume space, shading in world space
   SampleWalk w;
   w.init(vol, ray, jitter, samplingRate);
   V3 color = splat(0.f);
@@ -197,11 +198,12 @@ B200_D float4 integrateShaded(const SamplerTables *T, const Scene &sc, const Vol
         const V3 grad = volumeGradient(vol, pos, val);
         if (dot(grad, grad) > 1e-6f) {
           DG dg;
-          dg.P = pos;
-          dg.Ns = dg.Ng = fnormalize(mk(-grad.x, -grad.y, -grad.z));
+          dg.P = wray.org + d * wray.dir;
+          const V3 ng = mk(-grad.x, -grad.y, -grad.z);
+          dg.Ns = dg.Ng = fnormalize(vol.identity ? ng : xfmVectorT(vol.rcp, ng));
           dg.epsilon = dt / 2.f;
           dg.entry = ~0u;
-          const SvShading sh = svComputeShading<STATS>(T, sc, vol, S, samplingRate, dg, ~0u, c, ray.dir, x, y, sid,
+          const SvShading sh = svComputeShading<STATS>(T, sc, vol, S, samplingRate, dg, ~0u, c, wray.dir, x, y, sid,
                                                        rs, ts);
           const float a = 1.f - luminance(sh.transmission), f = vol.gradientShadingScale;
           c = make_float4(lerpF(f, c.x, sh.color.x), lerpF(f, c.y, sh.color.y), lerpF(f, c.z, sh.color.z),

@@ -71,6 +71,16 @@ B200_D float tapsValue(const Taps &s) {
   return lerpF(s.fz, lerpF(s.fy, c00, c10), lerpF(s.fy, c01, c11));
 }
 
+// transformRay(tRay, instance->rcp_xfm) (render/scivis/volumes.ispc:311-313):
+// the ray in the volume's space, same t
+B200_D Ray toVolume(const VolumeD &v, const Ray &r) {
+  if (v.identity) return r;
+  Ray t = r;
+  t.org = xfmPoint(v.rcp, r.org);
+  t.dir = xfmVector(v.rcp, r.dir);
+  return t;
+}
+
 B200_D float sampleAt(const VolumeD &v, V3 p) {
   Taps t;
   fetchTaps(v, p, t);
@@ -250,8 +260,9 @@ struct SampleWalk {
 // Front-to-back compositing (SciVis ray march with the transfer function,
 // alpha = exp(-a * dt * densityScale)) until the transmittance falls to
 // minContribution.
-B200_D float4 integrate(const VolumeD &v, const Ray &ray, float jitter, float samplingRate, float minContribution,
+B200_D float4 integrate(const VolumeD &v, const Ray &wray, float jitter, float samplingRate, float minContribution,
                         uint32_t &samples) {
+  const Ray ray = toVolume(v, wray);
   SampleWalk w;
   w.init(v, ray, jitter, samplingRate);
   V3 color = splat(0.f);
@@ -275,7 +286,8 @@ B200_D float4 integrate(const VolumeD &v, const Ray &ray, float jitter, float sa
 
 // Does [ray.tnear, ray.tfar] overlap the volume's grid box (the test that
 // starts the interval iteration)?
-B200_D bool volumeOverlaps(const VolumeD &v, const Ray &ray) {
+B200_D bool volumeOverlaps(const VolumeD &v, const Ray &wray) {
+  const Ray ray = toVolume(v, wray);
   IntervalIter it;
   it.init(v, ray.org, ray.dir, ray.tnear, ray.tfar);
   return !it.done;
@@ -287,7 +299,8 @@ B200_D bool volumeOverlaps(const VolumeD &v, const Ray &ray) {
 // samples are skipped inside the sample search.  Shadow and AO rays of the
 // SciVis renderer use the opacity; the AO renderer composites both.
 template <bool COLOR>
-B200_D float4 volumeIntegrateAO(const VolumeD &v, const Ray &ray, float jitter, float samplingRate) {
+B200_D float4 volumeIntegrateAO(const VolumeD &v, const Ray &wray, float jitter, float samplingRate) {
+  const Ray ray = toVolume(v, wray);
   IntervalIter it;
   it.init(v, ray.org, ray.dir, ray.tnear, ray.tfar);
   const float nominalDeltaT = fminf(v.spacing.x, fminf(v.spacing.y, v.spacing.z));

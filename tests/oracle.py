@@ -160,6 +160,7 @@ def lib():
         L.or_volume_new.argtypes = [P, I, I, I, P, P, P, I, P, I, F, F, F]
         L.or_volume_free.argtypes = [P]
         L.or_volume_set_gradient_shading.argtypes = [P, F]
+        L.or_volume_set_transform.argtypes = [P, P]
         L.or_volume_sample_count.restype = ctypes.c_uint64
         L.or_volume_sample_count.argtypes = [I]
         L.or_render_scivis_volume.argtypes = [P, ctypes.POINTER(OrCamera), I, I, I, I, F, P, I, I, I, P, I]
@@ -304,6 +305,11 @@ class VolumeModel:
         op = np.ascontiguousarray(opacity, np.float32).reshape(-1)
         self.h = lib().or_volume_new(_p(d), nx, ny, nz, _p(o), _p(sp), _p(c), len(c), _p(op), len(op),
                                      float(value_range[0]), float(value_range[1]), float(density_scale))
+
+    def set_transform(self, xfm):
+        """The volume's instance transform (3x4 row-major) or None."""
+        self._xfm = None if xfm is None else np.ascontiguousarray(xfm, np.float32).reshape(12)
+        lib().or_volume_set_transform(self.h, _p(self._xfm) if self._xfm is not None else None)
 
     def set_gradient_shading(self, scale):
         """The volumetric model's gradientShadingScale (default 0: off)."""
