@@ -2,22 +2,35 @@
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME] [--impl ours|reference]
 
-A step is one rendered frame of the workload (one ospRenderFrame into an
-accumulating framebuffer).  Prints one JSON line (rank 0).
+A step is one rendered frame of the workload into an accumulating
+framebuffer.  Prints one JSON line (rank 0).  The headline workload is the
+path tracer on the instanced displaced spheres at 1920x1080, 16 spp; with
+N = 1 the same line also carries, under "configs", one object per other
+measured configuration: the AO renderer (C0), the SciVis volume (C2), the
+batched requests (C3) and the learned-cache study (C4: time to relMSE
+<= 0.01 of the learned-cache path tracer against the plain one).
 
 value      Mrays/s of all ranks: rays traced (counted by the kernels' stats
            pass over the same frames) / device time of the timed frames
            (CUDA events on the render stream; L2 flushed before every frame).
-e2e        the same metric through the C ABI with host buffers: per step the
-           camera/renderer parameters go host->device and the RGBA32F colour
-           buffer comes back device->host (ospRenderFrame + ospMapFrameBuffer).
-roofline   algorithmic bytes of the traversal (48 B ray record + 80 B per BVH
-           node visit + 48 B per triangle and 20 B per sphere fetched) per
-           frame / frame time, against the measured HBM copy bandwidth.
+e2e        the same metric end to end through the public API with host
+           buffers.  Path tracer: an OSPRay application's frame loop on
+           libospray.so (ospRenderFrame + ospWait + ospMapFrameBuffer with
+           the RGBA32F colour copied to host memory + ospUnmapFrameBuffer; the
+           world is committed once, as an application does); the other
+           workloads through the b200 C ABI (render call + b200_frame_read).
+roofline   algorithmic bytes of the dominant kernel (traversal: 48 B ray
+           record + 80 B per BVH node visit + 48 B per triangle and 20 B per
+           sphere fetched) per launch / its CUDA-event launch time, against
+           the measured HBM copy bandwidth; plus the issue activity, lanes
+           per instruction and L2 throughput of a small-case ncu capture of
+           the same kernel, which name the real limiter ("bound").
 cpu_baseline  the CPU oracle (a restatement of the reference's ISPC path) on
-           this machine's host cores, on a bounded sample of the same frames.
---impl reference  times that CPU implementation alone, as the reference arm
-           (the reference's ISPC+Embree device cannot be built here).
+           this machine's host cores, on a bounded, fixed sample of the same
+           frames (row bands spread over the whole frame).
+--impl reference  times that CPU implementation alone on the same sample,
+           as the reference arm (the reference's ISPC+Embree device cannot be
+           built here).
 
 Multi-GPU: the render path does not exchange data between GPUs; N ranks
 render N independent replicas ("replicas only"), scaling is weak.
@@ -39,16 +52,34 @@ sys.path.insert(0, ROOT)
 L2_FLUSH_BYTES = 512 << 20
 
 # DRAM traffic of the dominant kernel per algorithmic byte, from one ncu
-# capture (dram__bytes_read.sum + dram__bytes_write.sum of the captured
-# launches / their algorithmic bytes); the summaries under profiles/ give the
-# commands.  Scaled to the bench's launches by their algorithmic bytes.
+# capture of a small case of the same kernel (dram__bytes_read.sum +
+# dram__bytes_write.sum of the captured launches / their algorithmic bytes);
+# the summaries under profiles/ give the commands.  Scaled to the bench's
+# launches by their algorithmic bytes.
 TRAFFIC = {
-    # 12 trace launches of one 1920x1080 16 spp frame: 12.6 GB DRAM vs 130.3 GB algorithmic
-    "pt_instanced_spheres_1080p": {"dram_per_alg_byte": 0.0968,
-                                   "source": "profiles/k_trace_queue_pt_instanced_1080p_traffic.md"},
-    # one 1024x1024 4 spp frame: 2.65 GB DRAM vs 12.6 GB algorithmic (32 B per sample)
+    "pt_instanced_spheres_1080p": {"dram_per_alg_byte": 0.098,
+                                   "source": "profiles/k_trace_queue_pt_instanced_480x270_limiter.md"},
     "scivis_volume_512cube_1024": {"dram_per_alg_byte": 0.21,
                                    "source": "profiles/k_render_scivis_volume_512cube.md"},
+}
+
+# What limits the dominant kernel, from the same small-case ncu captures:
+# issue activity (smsp__issue_active), active lanes per warp instruction
+# (smsp__thread_inst_executed_per_inst_executed), L2 throughput
+# (lts__t_bytes per second) per instantiation.
+LIMITER = {
+    "pt_instanced_spheres_1080p": {
+        "bound": "issue",
+        "issue_active": {"closest": 0.669, "shadow": 0.732},
+        "lanes_per_instruction": {"closest": 13.79, "shadow": 9.47},
+        "l2_gbs": {"closest": 1238.0, "shadow": 1396.0},
+        "source": "profiles/k_trace_queue_pt_instanced_480x270_limiter.md"},
+    "scivis_volume_512cube_1024": {
+        "bound": "latency",
+        "source": "profiles/k_render_scivis_volume_512cube.md"},
+    "ao_heightfield_512": {
+        "bound": "latency",
+        "source": "profiles/k_render_ao_heightfield_512.md"},
 }
 
 
@@ -229,10 +260,20 @@ class PTWorkload:
     def step(self, stats=False):
         self.og.render_pt(self.scene, self.cam, self.sparams if stats else self.params, self.mats, self.fb)
 
+    def e2e_setup(self):
+        """The same workload built by an OSPRay application on libospray.so."""
+        from ospray_gb300 import osp
+        if getattr(self, "app", None) is None:
+            L = osp.lib()
+            if L.ospInit(None, None) != 0:
+                raise RuntimeError("ospInit: %s" % L.ospDeviceGetLastErrorMsg(None))
+            self.app = osp.PathTracerApp(self.data, self.spp, 5, 3, self.w, self.h)
+        self.app.reset()
+
     def e2e_step(self):
-        self.og.render_pt(self.scene, self.cam, self.params, self.mats, self.fb)
-        self.og.lib().b200_frame_read(self.fb._h, self.og.FB_COLOR, self.color.ctypes.data, self.color.nbytes)
-        return 40 + 76, self.color.nbytes
+        return self.app.frame()
+
+    e2e_api = "libospray.so: ospRenderFrame + ospWait + ospMapFrameBuffer (RGBA32F colour to host) + ospUnmapFrameBuffer"
 
     def reset(self):
         self.fb.reset()
@@ -240,8 +281,18 @@ class PTWorkload:
     def counters(self, reset=False):
         return self.scene.counters(reset)
 
-    def cpu_frames(self, budget_s, nthreads):
-        """Oracle on a band of whole rows of the frame, sized to budget_s."""
+    def cpu_bands(self, nbands=12, rows=8):
+        """A fixed sample of the frame: `nbands` bands of `rows` rows centred on
+        evenly spaced heights, so the sample sees the whole frame's content."""
+        out = []
+        for i in range(nbands):
+            c = int((i + 0.5) * self.h / nbands)
+            out.append((max(0, c - rows // 2), min(self.h, c + rows // 2)))
+        return out
+
+    def cpu_frames(self, budget_s, nthreads, passes=None):
+        """Oracle passes over the fixed band sample until budget_s (or
+        `passes` passes): (rays, seconds, passes)."""
         sys.path.insert(0, os.path.join(ROOT, "tests"))
         import oracle
         from ospray_gb300 import scenes
@@ -253,21 +304,23 @@ class PTWorkload:
             self._ocam = oracle.camera(c["position"], c["direction"], c["up"], fovy=c["fovy"], aspect=c["aspect"])
             self._op = oracle.pt_params(spp=self.spp, max_path_length=5, roulette_path_length=3)
             oracle.render_pt(o, self._orc[1], self._ocam, oracle.pt_params(spp=1), 4, 4)  # albedo tables
-            self._rows = 2
         o, ow = self._orc
-        y0 = self.h // 2 - self._rows // 2
+        bands = self.cpu_bands()
         oracle.lib().or_ray_count(1)
         t0 = time.perf_counter()
-        oracle.render_pt(o, ow, self._ocam, self._op, self.w, self.h, rows=(y0, y0 + self._rows), nthreads=nthreads)
-        dt = time.perf_counter() - t0
+        n = 0
+        while True:
+            for y0, y1 in bands:
+                oracle.render_pt(o, ow, self._ocam, self._op, self.w, self.h, rows=(y0, y1), nthreads=nthreads)
+            n += 1
+            dt = time.perf_counter() - t0
+            if (passes is not None and n >= passes) or (passes is None and dt >= budget_s):
+                break
         rays = int(oracle.lib().or_ray_count(1))
-        rows = self._rows
-        # grow the band toward the budget for the next call
-        self._rows = int(max(2, min(self.h, rows * min(8.0, budget_s / max(dt, 1e-3)))))
-        if dt < 0.25 * budget_s and self._rows > rows:
-            return self.cpu_frames(budget_s, nthreads)
-        self.cpu_sample = "%d centre rows x %d px x %d spp" % (rows, self.w, self.spp)
-        return rays, dt, rows / self.h
+        nrows = sum(b - a for a, b in bands)
+        self.cpu_sample = "%d bands of 8 rows spread over the frame (%d of %d rows) x %d px x %d spp, %d pass(es)" % (
+            len(bands), nrows, self.h, self.w, self.spp, n)
+        return rays, dt, n
 
 
 class ScivisWorkload:
@@ -284,7 +337,7 @@ class ScivisWorkload:
         self.data = scenes.volume_scene(n=n, width=w, height=h)
         self.config = {"workload": self.name, "renderer": "scivis", "width": w, "height": h, "spp": spp,
                        "volume": "%d^3 float32" % n, "volumeSamplingRate": 1.0, "transfer_function": 256,
-                       "pixelFilter": "gauss"}
+                       "shadows": True, "lights": "none (shadows inert)", "pixelFilter": "gauss"}
 
     def setup(self, og, dev):
         self.og = og
@@ -295,8 +348,9 @@ class ScivisWorkload:
         self.build_ms = (time.perf_counter() - t0) * 1e3
         c = d["camera"]
         self.cam = og.camera_desc(c["position"], c["direction"], c["up"], fovy=c["fovy"], aspect=c["aspect"])
-        self.params = og.scivis_params(spp=self.spp)
-        self.sparams = og.scivis_params(spp=self.spp, stats=True)
+        # shadows on as the configuration names them; the world has no lights, so they cast nothing
+        self.params = og.scivis_params(spp=self.spp, shadows=True)
+        self.sparams = og.scivis_params(spp=self.spp, shadows=True, stats=True)
         self.fb = og.Frame(dev, self.w, self.h, og.FB_COLOR | og.FB_ACCUM)
         self.color = np.empty((self.h, self.w, 4), np.float32)
 
@@ -321,7 +375,8 @@ class ScivisWorkload:
     def bytes_per_unit(self):
         return 32.0
 
-    def cpu_frames(self, budget_s, nthreads):
+    def cpu_frames(self, budget_s, nthreads, passes=None):
+        """Oracle passes over 8 bands of 4 rows spread over the frame."""
         sys.path.insert(0, os.path.join(ROOT, "tests"))
         import oracle
         d = self.data
@@ -330,20 +385,22 @@ class ScivisWorkload:
                                            d["value_range"])
             c = d["camera"]
             self._ocam = oracle.camera(c["position"], c["direction"], c["up"], fovy=c["fovy"], aspect=c["aspect"])
-            self._rows = 4
-        y0 = self.h // 2 - self._rows // 2
+        bands = [(int((i + 0.5) * self.h / 8) - 2, int((i + 0.5) * self.h / 8) + 2) for i in range(8)]
         oracle.lib().or_volume_sample_count(1)
         t0 = time.perf_counter()
-        oracle.render_scivis_volume(self._orc, self._ocam, 2, self.w, self.h, spp=self.spp,
-                                    rows=(y0, y0 + self._rows), nthreads=nthreads)
-        dt = time.perf_counter() - t0
+        n = 0
+        while True:
+            for y0, y1 in bands:
+                oracle.render_scivis_volume(self._orc, self._ocam, 2, self.w, self.h, spp=self.spp, rows=(y0, y1),
+                                            nthreads=nthreads)
+            n += 1
+            dt = time.perf_counter() - t0
+            if (passes is not None and n >= passes) or (passes is None and dt >= budget_s):
+                break
         samples = int(oracle.lib().or_volume_sample_count(1))
-        rows = self._rows
-        self._rows = int(max(2, min(self.h, rows * min(8.0, budget_s / max(dt, 1e-3)))))
-        if dt < 0.25 * budget_s and self._rows > rows:
-            return self.cpu_frames(budget_s, nthreads)
-        self.cpu_sample = "%d centre rows x %d px x %d spp" % (rows, self.w, self.spp)
-        return samples, dt, rows / self.h
+        self.cpu_sample = "8 bands of 4 rows spread over the frame x %d px x %d spp, %d pass(es)" % (
+            self.w, self.spp, n)
+        return samples, dt, n
 
 
 class BatchWorkload:
@@ -516,12 +573,15 @@ class BatchWorkload:
 AOWorkload.launches_per_frame = 2  # render + post-process (colour conversion)
 AOWorkload.timed_kernels = ("ao",)
 AOWorkload.roofline_kernel = "k_render_ao (camera + AO rays, one launch per frame)"
+AOWorkload.e2e_api = "b200 C ABI: b200_render_ao + b200_frame_read (RGBA32F colour to host)"
 PTWorkload.timed_kernels = ("trace_closest", "trace_shadow")
 PTWorkload.roofline_kernel = "k_trace_queue (closest-hit and shadow instantiations)"
 ScivisWorkload.timed_kernels = ("scivis",)
 ScivisWorkload.roofline_kernel = "k_render_scivis_volume"
+ScivisWorkload.e2e_api = "b200 C ABI: b200_render_scivis + b200_frame_read (RGBA32F colour to host)"
 PTWorkload.launches_per_frame = 3 + 6 * 4  # generate, finalize, post-process, 6 bounces x (reset, trace, shade, shadow)
 BatchWorkload.launches_per_frame = None  # taken from the batch plan (b200_batch_info)
+BatchWorkload.e2e_api = "b200 C ABI: b200_batch_render (graph replay) + b200_frame_read of every request"
 WORKLOADS = {"ao": AOWorkload, "pt": PTWorkload, "scivis": ScivisWorkload, "batch": BatchWorkload}
 
 
@@ -536,6 +596,8 @@ def dist_setup(args):
 
 
 def run_reference(args):
+    """The reference arm: the CPU implementation of the path on the host
+    cores, each step one pass over the workload's fixed CPU sample."""
     ws, rank, local = dist_setup(args)
     if rank != 0:
         return
@@ -544,7 +606,10 @@ def run_reference(args):
     per_step = []
     rays_total = 0
     for i in range(args.warmup + args.steps):
-        rays, dt, frames = wl.cpu_frames(args.cpu_budget / max(1, args.steps), nthreads)
+        if hasattr(wl, "cpu_bands") or isinstance(wl, ScivisWorkload):
+            rays, dt, _ = wl.cpu_frames(0.0, nthreads, passes=1)
+        else:
+            rays, dt, _ = wl.cpu_frames(args.cpu_budget / max(1, args.steps), nthreads)
         if i >= args.warmup:
             per_step.append((rays, dt))
             rays_total += rays
@@ -555,26 +620,20 @@ def run_reference(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded generators)", "config": wl.config, "impl": "reference",
             "cpu_baseline": {"value": round(value, 3), "unit": wl.metric, "cores": nthreads, "kind": "port",
-                             "sample": "%s, about %.1f s of CPU work per step"
-                                       % (getattr(wl, "cpu_sample", "whole frames"), args.cpu_budget / max(1, args.steps))},
+                             "sample": "%s per step" % getattr(wl, "cpu_sample", "whole frames")},
             "e2e": {"value": round(value, 3), "unit": wl.metric, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
-def run_ours(args):
+def measure(wl, args, og, dev, local, ws, cpu_budget):
+    """Times `args.steps` frames of a set-up workload: device value, e2e,
+    roofline of the dominant kernel, clocks, and (cpu_budget > 0) the CPU
+    baseline.  Returns the JSON line as a dict (rank 0) or None."""
     import torch
-    import ospray_gb300 as og
-    ws, rank, local = dist_setup(args)
-    if ws > 1:
-        import torch.distributed as tdist
-        torch.cuda.set_device(local)
-        tdist.init_process_group("nccl")
-    wl = WORKLOADS[args.workload]()
-    dev = og.Device(local)
-    wl.setup(og, dev)
+    rank = int(os.environ.get("RANK", "0"))
     stream = torch.cuda.ExternalStream(dev.stream, device=torch.device("cuda", local))
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=torch.device("cuda", local))
-
+    wl.reset()
     for _ in range(args.warmup):
         wl.step()
     dev.sync()
@@ -606,6 +665,7 @@ def run_ours(args):
         torch.distributed.barrier()
     times = [a.elapsed_time(b) for a, b in evs]
     dev_ms = float(sum(times))
+    del flush
     # rays of exactly the timed frames: replay the same frame sequence in stats mode
     wl.reset()
     for _ in range(first_timed):
@@ -616,16 +676,18 @@ def run_ours(args):
     c = wl.counters(reset=True)
     rays, nodes, tris, sph = (int(x) for x in c)
     units = wl.units(c) if hasattr(wl, "units") else rays
-    # end-to-end through the C ABI with host buffers
-    wl.reset()
+    # end to end through the public API with host buffers
+    if hasattr(wl, "e2e_setup"):
+        wl.e2e_setup()
+    else:
+        wl.reset()
     for _ in range(2):
         wl.e2e_step()
     dev.sync()
     t0 = time.perf_counter()
     h2d = d2h = 0
     for _ in range(args.steps):
-        hb, db = wl.e2e_step()
-        h2d, d2h = hb, db
+        h2d, d2h = wl.e2e_step()
     dev.sync()
     e2e_s = time.perf_counter() - t0
 
@@ -635,15 +697,13 @@ def run_ours(args):
         torch.distributed.all_reduce(mx, op=torch.distributed.ReduceOp.MAX)
         sm = local_vals.clone()
         torch.distributed.all_reduce(sm, op=torch.distributed.ReduceOp.SUM)
-        dev_ms_max, e2e_max, rays_all = float(mx[0]), float(mx[1]), float(sm[2])
+        dev_ms_max, e2e_max, units_all = float(mx[0]), float(mx[1]), float(sm[2])
     else:
-        dev_ms_max, e2e_max, rays_all = dev_ms, e2e_s, float(units)
+        dev_ms_max, e2e_max, units_all = dev_ms, e2e_s, float(units)
     if rank != 0:
-        if ws > 1:
-            torch.distributed.destroy_process_group()
-        return
-    value = rays_all / (dev_ms_max * 1e-3) / 1e6
-    e2e_val = rays_all / e2e_max / 1e6
+        return None
+    value = units_all / (dev_ms_max * 1e-3) / 1e6
+    e2e_val = units_all / e2e_max / 1e6
     if hasattr(wl, "bytes_per_unit"):
         alg_bytes = wl.bytes_per_unit() * units
         note = "algorithmic volume bytes (32 B per trilinear sample)"
@@ -671,6 +731,16 @@ def run_ours(args):
         # ncu dram bytes per algorithmic byte of the same kernel, scaled to this launch size
         traffic = round(tp["dram_per_alg_byte"] * per_launch)
         note += "; traffic from %s" % tp["source"]
+    lim = LIMITER.get(wl.name, {})
+    roof = {"bound": lim.get("bound", "hbm"), "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 4), "traffic": traffic,
+            "note": "%s; peak %s (%s)" % (note, kind, "of measured" if kind == "measured" else "of fallback")}
+    for k in ("issue_active", "lanes_per_instruction", "l2_gbs"):
+        if k in lim:
+            roof[k] = lim[k]
+    if "source" in lim:
+        roof["limiter_source"] = lim["source"]
+    roof.update(roof_kernel)
     line = {"metric": wl.metric, "value": round(value, 3), "unit": wl.metric, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(dev_ms_max / args.steps, 4), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generators)",
@@ -679,38 +749,78 @@ def run_ours(args):
                            rays_per_frame=rays / args.steps, node_visits_per_ray=round(nodes / max(rays, 1), 3),
                            tri_tests_per_ray=round(tris / max(rays, 1), 3)),
             "e2e": {"value": round(e2e_val, 3), "unit": wl.metric, "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h},
+                    "d2h_bytes_per_step": d2h, "api": getattr(wl, "e2e_api", "b200 C ABI")},
             "gpu_launches": args.steps * (wl.launches_per_frame or wl.kernels_per_frame()),
-            "roofline": dict({"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                              "frac": round(achieved / peak, 4), "traffic": traffic,
-                              "note": "%s; peak %s (%s)" % (note, kind, "of measured" if kind == "measured"
-                                                           else "of fallback")}, **roof_kernel),
+            "roofline": roof,
             "clocks": clk.summary()}
     if hasattr(wl, "latency"):
         line["latency"] = wl.latency()
-    if not args.no_cpu_baseline:
+    if cpu_budget > 0:
         nthreads = os.cpu_count() or 1
-        crays, cdt, cframes = wl.cpu_frames(args.cpu_budget, nthreads)
-        sample = getattr(wl, "cpu_sample", "%s frames of the same workload" % cframes)
+        crays, cdt, _ = wl.cpu_frames(cpu_budget, nthreads)
+        sample = getattr(wl, "cpu_sample", "frames of the same workload")
         line["cpu_baseline"] = {"value": round(crays / cdt / 1e6, 3), "unit": wl.metric, "cores": nthreads,
                                 "kind": "port", "sample": "%s (%.1f s)" % (sample, cdt)}
-    print(json.dumps(line), flush=True)
+    return line
+
+
+def run_ours(args):
+    import torch
+    import ospray_gb300 as og
+    ws, rank, local = dist_setup(args)
+    if ws > 1:
+        import torch.distributed as tdist
+        torch.cuda.set_device(local)
+        tdist.init_process_group("nccl")
+    dev = og.Device(local)
+    wl = WORKLOADS[args.workload]()
+    wl.setup(og, dev)
+    line = measure(wl, args, og, dev, local, ws, 0.0 if args.no_cpu_baseline else args.cpu_budget)
     if ws > 1:
         torch.distributed.destroy_process_group()
+    if line is None:
+        return
+    if ws == 1 and args.workload == "pt" and not args.headline_only:
+        # the other configurations, each in its own object of the same line
+        del wl
+        extras = {}
+        for key, name in (("C0_ao", "ao"), ("C2_scivis", "scivis"), ("C3_batch", "batch")):
+            t0 = time.perf_counter()
+            try:
+                w2 = WORKLOADS[name]()
+                w2.setup(og, dev)
+                sub = measure(w2, args, og, dev, local, 1, 0.0 if args.no_cpu_baseline else args.extra_cpu_budget)
+                sub.pop("n_gpus", None)
+                sub.pop("scaling", None)
+                sub.pop("vs_baseline", None)
+                sub.pop("data", None)
+                del w2
+            except Exception as e:  # a failed extra is reported, not fatal to the headline
+                sub = {"error": "%s: %s" % (type(e).__name__, e)}
+            sub["wall_s"] = round(time.perf_counter() - t0, 1)
+            extras[key] = sub
+        t0 = time.perf_counter()
+        try:
+            extras["C4_learned_cache"] = nrc_study(args, og, dev)
+        except Exception as e:
+            extras["C4_learned_cache"] = {"error": "%s: %s" % (type(e).__name__, e)}
+        extras["C4_learned_cache"]["wall_s"] = round(time.perf_counter() - t0, 1)
+        line["configs"] = extras
+    print(json.dumps(line), flush=True)
 
 
-def run_nrc(args):
+def nrc_study(args, og, dev):
     """Learned-cache path tracer vs plain path tracer on the instanced-spheres
     scene: 1920x1080, 1 spp per frame, maxPathLength 8, static camera, up to
     `--nrc-frames` frames each; both judged by relMSE against a 4096-spp plain
-    render (256 frames x 16 spp).  Reports each arm's device time to reach
-    relMSE <= 0.01 and the relMSE after every frame count in a coarse curve."""
-    import torch  # noqa: F401  (device init order as the other arms)
-    import ospray_gb300 as og
+    render (256 frames x 16 spp).  relMSE is taken over all pixels and over
+    the pixels whose first hit is geometry (background pixels of constant
+    radiance excluded).  Per arm: device seconds and frames to reach each
+    relMSE level, end-to-end seconds (host-timed, including the relMSE
+    reads), and a coarse curve."""
     from ospray_gb300 import scenes
     w, h = (int(x) for x in args.size.split("x")) if args.size else (1920, 1080)
     data = scenes.pt_instanced_scene(width=w, height=h)
-    dev = og.Device(0)
     scene = og.Scene(dev)
     scenes.build_pt_scene(scene, data)
     scene.set_lights([og.quad_light(L["position"], L["edge1"], L["edge2"], L["intensity"]) if L["type"] == "quad"
@@ -720,7 +830,7 @@ def run_nrc(args):
     mats = og.materials_array(data["materials"])
     ref_frames = max(1, args.nrc_ref_spp // 16)
     t0 = time.perf_counter()
-    ref = og.Frame(dev, w, h, og.FB_COLOR | og.FB_ACCUM)
+    ref = og.Frame(dev, w, h, og.FB_COLOR | og.FB_ACCUM | og.FB_DEPTH)
     p16 = og.pt_params(spp=16, max_path_length=8, roulette_path_length=3)
     for _ in range(ref_frames):
         og.render_pt(scene, cam, p16, mats, ref)
@@ -728,12 +838,14 @@ def run_nrc(args):
     ref_s = time.perf_counter() - t0
     p1 = og.pt_params(spp=1, max_path_length=8, roulette_path_length=3)
     b = scene.bounds()
+    levels = (0.01, 0.005, 0.002, 0.001)
 
     def arm(render):
         fb = og.Frame(dev, w, h, og.FB_COLOR | og.FB_ACCUM)
         total = 0.0
         curve = []
-        reached = None
+        reached = {"all": {}, "hits": {}}
+        e2e0 = time.perf_counter()
         with Clocks(0) as clk:
             for i in range(args.nrc_frames):
                 e0 = dev.record_event()
@@ -743,15 +855,25 @@ def run_nrc(args):
                 total += dev.event_ms(e0, e1) * 1e-3
                 dev.release_event(e0)
                 dev.release_event(e1)
-                err = og.relmse(fb, ref)
-                if reached is None and err <= 0.01:
-                    reached = (i + 1, total)
+                err = {"all": og.relmse(fb, ref), "hits": og.relmse_hits(fb, ref)[0]}
+                for k, e in err.items():
+                    for lv in levels:
+                        if lv not in reached[k] and e <= lv:
+                            reached[k][lv] = (i + 1, total, time.perf_counter() - e2e0)
                 if (i + 1) in (1, 2, 4, 8, 16, 32, 64, 128, 256, 512) or i + 1 == args.nrc_frames:
-                    curve.append({"frames": i + 1, "seconds": round(total, 4), "relmse": round(err, 5)})
-        return {"seconds_to_relmse_0.01": round(reached[1], 4) if reached else None,
-                "frames_to_relmse_0.01": reached[0] if reached else None,
-                "relmse_final": curve[-1]["relmse"], "seconds_total": round(total, 4),
-                "ms_per_frame": round(total / args.nrc_frames * 1e3, 3), "curve": curve, "clocks": clk.summary()}
+                    curve.append({"frames": i + 1, "seconds": round(total, 4), "relmse": round(err["all"], 5),
+                                  "relmse_hits": round(err["hits"], 5)})
+
+        def table(k):
+            return {str(lv): ({"frames": reached[k][lv][0], "device_s": round(reached[k][lv][1], 4),
+                               "e2e_s": round(reached[k][lv][2], 4)} if lv in reached[k] else None) for lv in levels}
+        return {"seconds_to_relmse_0.01": round(reached["all"][0.01][1], 4) if 0.01 in reached["all"] else None,
+                "e2e_seconds_to_relmse_0.01": round(reached["all"][0.01][2], 4) if 0.01 in reached["all"] else None,
+                "frames_to_relmse_0.01": reached["all"][0.01][0] if 0.01 in reached["all"] else None,
+                "to_level": table("all"), "to_level_hit_pixels": table("hits"),
+                "relmse_final": curve[-1]["relmse"], "relmse_hits_final": curve[-1]["relmse_hits"],
+                "seconds_total": round(total, 4), "ms_per_frame": round(total / args.nrc_frames * 1e3, 3),
+                "curve": curve, "clocks": clk.summary()}
 
     plain = arm(lambda fb: og.render_pt(scene, cam, p1, mats, fb))
     cache = og.RadianceCache(dev, b[:3], b[3:], learning_rate=1e-2, seed=1)
@@ -761,19 +883,33 @@ def run_nrc(args):
         scene, cam, p1, mats, fb, cache,
         epochs=args.nrc_early_epochs if fb.frame_id < args.nrc_early_frames else 1))
     value = learned["seconds_to_relmse_0.01"]
-    line = {"metric": "seconds to relMSE<=0.01 (learned cache)", "value": value, "unit": "s", "n_gpus": 1,
-            "steps": args.nrc_frames, "warmup": 0, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32 render, bf16 MLP", "data": "synthetic (seeded generators)",
+    _, nhit = og.relmse_hits(ref, ref)
+
+    def speedup(k, lv):
+        a, bb = learned[k][str(lv)], plain[k][str(lv)]
+        return round(bb["device_s"] / a["device_s"], 3) if a and bb else None
+    return {"metric": "seconds to relMSE<=0.01 (learned cache)", "value": value, "unit": "s",
+            "higher_is_better": False, "steps": args.nrc_frames, "dtype": "f32 render, bf16 MLP",
             "config": {"workload": "nrc_instanced_spheres_1080p", "width": w, "height": h, "spp_per_frame": 1,
                        "maxPathLength": 8, "roulettePathLength": 3, "frames": args.nrc_frames,
-                       "cache": "16-level hash grid (2^19 x 2 fp16 per level) + 64x4 ReLU MLP, bf16 mma, Adam 1e-2, "
-                                "16384 training paths, 4 x 16384 samples per frame; the first %d frames train %d "
-                                "epochs" % (args.nrc_early_frames, args.nrc_early_epochs),
+                       "hit_pixels": int(nhit),
+                       "cache": "16-level hash grid (2^19 x 2 fp16 per level) + 64x4 ReLU MLP, bf16 tensor cores, "
+                                "Adam 1e-2, 16384 training paths, 4 x 16384 samples per frame; the first %d frames "
+                                "train %d epochs" % (args.nrc_early_frames, args.nrc_early_epochs),
                        "reference": {"spp": ref_frames * 16, "renderer": "plain GPU path tracer",
                                      "seconds": round(ref_s, 2)}},
             "learned": learned, "plain": plain,
-            "speedup_time_to_relmse": (round(plain["seconds_to_relmse_0.01"] / value, 3)
-                                       if value and plain["seconds_to_relmse_0.01"] else None)}
+            "speedup_time_to_relmse": {"all_pixels": {str(lv): speedup("to_level", lv) for lv in levels},
+                                       "hit_pixels": {str(lv): speedup("to_level_hit_pixels", lv) for lv in levels}}}
+
+
+def run_nrc(args):
+    import torch  # noqa: F401  (device init order as the other arms)
+    import ospray_gb300 as og
+    dev = og.Device(0)
+    line = nrc_study(args, og, dev)
+    line.update({"n_gpus": 1, "warmup": 0, "scaling": "weak", "vs_baseline": None,
+                 "data": "synthetic (seeded generators)"})
     print(json.dumps(line), flush=True)
 
 
@@ -785,11 +921,14 @@ def main():
     ap.add_argument("--workload", default="pt", choices=sorted(WORKLOADS) + ["nrc"])
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU-baseline work")
+    ap.add_argument("--extra-cpu-budget", type=float, default=4.0,
+                    help="seconds of CPU-baseline work for each of the other configurations")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--headline-only", action="store_true", help="skip the other configurations' objects")
     ap.add_argument("--size", default=None, help="WxH override (profiling small cases; not the bench config)")
     ap.add_argument("--spp", type=int, default=None, help="spp override (path tracer; profiling only)")
-    ap.add_argument("--nrc-frames", type=int, default=256, help="frames per arm of the nrc workload")
-    ap.add_argument("--nrc-ref-spp", type=int, default=4096, help="spp of the nrc workload's reference image")
+    ap.add_argument("--nrc-frames", type=int, default=256, help="frames per arm of the learned-cache study")
+    ap.add_argument("--nrc-ref-spp", type=int, default=4096, help="spp of the learned-cache study's reference image")
     ap.add_argument("--nrc-early-frames", type=int, default=4, help="frames that train --nrc-early-epochs epochs")
     ap.add_argument("--nrc-early-epochs", type=int, default=4)
     args = ap.parse_args()
@@ -797,6 +936,7 @@ def main():
         run_nrc(args)
         return
     if args.size or args.spp:
+        args.headline_only = True
         base = WORKLOADS[args.workload]
         w, h = (int(x) for x in args.size.split("x")) if args.size else (None, None)
 

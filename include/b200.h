@@ -222,6 +222,11 @@ int b200_frame_set_variance_threshold(b200_frame fb, float varianceThreshold);
  * framebuffer of the same size: relMSE = mean over pixels and rgb of
  * (x - r)^2 / (r^2 + 0.01).  Synchronous. */
 int b200_frame_relmse(b200_frame fb, b200_frame reference, double *out);
+/* the same over the pixels whose first hit in the reference is geometry
+ * (finite reference DEPTH; the reference needs that channel), so pixels of
+ * constant background radiance do not dilute the mean; npix (may be null)
+ * receives their count.  Synchronous. */
+int b200_frame_relmse_hits(b200_frame fb, b200_frame reference, double *out, int64_t *npix);
 int b200_frame_set_tonemapper(b200_frame fb, const b200_tonemapper *tm);
 
 /* ---- AO renderer (AORenderer::commit modules/cpu/render/ao/AORenderer.cpp:26-35,
@@ -273,15 +278,58 @@ int b200_scene_set_lights(b200_scene scene, const b200_light *lights, int n);
 
 /* ---- path tracer (PathTracer::commit render/pathtracer/PathTracer.cpp:29-51,
  *      PathTracer_renderPixel render/pathtracer/PathTracer.ispc:75-216).
- * Materials are "principled" (render/materials/Principled.cpp:37-79) with the
- * parameters below; every other principled parameter has its default
- * (specular 1, ior 1, edgeColor 1, opacity 1, no coat/sheen/transmission).
- * material_id of an instance (b200_scene_add_instance) indexes `materials`. */
+ * material_id of an instance (b200_scene_add_instance) indexes `materials`.
+ * A material is one of the reference's material types with the parameters
+ * below; fill a struct with b200_material_defaults first (the reference's
+ * parameter defaults), then set what differs.
+ *   B200_MATERIAL_PRINCIPLED  (render/materials/Principled.ispc:81-455,
+ *     Principled.cpp:37-79): baseColor, roughness, metallic, opacity (the
+ *     cut-out: a specular transmission lobe of importance 1 - opacity, and
+ *     shadow rays pass with transparency 1 - opacity); the other principled
+ *     parameters keep their defaults (specular 1, ior 1, edgeColor 1, no
+ *     transmission, coat or sheen; roughness 0 is treated as the smallest
+ *     microfacet roughness).
+ *   B200_MATERIAL_OBJ  (render/materials/OBJ.ispc:29-126, OBJ.cpp:28-65):
+ *     kd = baseColor, ks, ns, d = opacity, tf: Lambert (kd d) + Blinn
+ *     specular (ks d, exponent ns) + specular transmission (tf d + 1 - d);
+ *     kd + ks + tf above 1 is scaled down to 1 as OBJ::commit does.
+ *   B200_MATERIAL_METAL  (render/materials/Metal.ispc:16-48, Metal.cpp:27-70):
+ *     complex index of refraction eta + i k per RGB channel (default
+ *     aluminium) and roughness: a specular conductor at roughness 0, else a
+ *     GGX microfacet conductor.
+ *   B200_MATERIAL_GLASS  (render/materials/Glass.ispc:16-60, Glass.cpp:27-50):
+ *     eta[0] = etaInside, eta[1] = etaOutside, attenuationColor and
+ *     attenuationDistance of the inside medium: a smooth dielectric; paths
+ *     track the medium they travel in and attenuate by Beer's law.
+ *   B200_MATERIAL_THINGLASS  (render/materials/ThinGlass.ispc:16-70,
+ *     ThinGlass.cpp:27-45): eta[0] = eta, attenuationColor,
+ *     attenuationDistance, thickness: a thin dielectric slab. */
+enum {
+  B200_MATERIAL_PRINCIPLED = 0,
+  B200_MATERIAL_OBJ = 1,
+  B200_MATERIAL_METAL = 2,
+  B200_MATERIAL_GLASS = 3,
+  B200_MATERIAL_THINGLASS = 4
+};
 typedef struct {
-  float baseColor[3];
-  float roughness;
-  float metallic;
+  float baseColor[3];  /* principled baseColor; obj kd */
+  float roughness;     /* principled, metal */
+  float metallic;      /* principled */
+  int type;            /* B200_MATERIAL_* */
+  float opacity;       /* principled opacity; obj d */
+  float ks[3], ns;     /* obj */
+  float tf[3];         /* obj transmission filter */
+  float eta[3], k[3];  /* metal: eta + i k per RGB; glass: etaInside, etaOutside; thinGlass: eta */
+  float attenuationColor[3];
+  float attenuationDistance;
+  float thickness;     /* thinGlass */
 } b200_material;
+/* the reference's defaults for a material of `type` (principled: baseColor
+ * 0.8, roughness 0, metallic 0, opacity 1; obj: kd 0.8, ks 0, ns 10, d 1,
+ * tf 0; metal: aluminium, roughness 0.1; glass: etaInside 1.5, etaOutside
+ * 1, attenuation colour 1 over distance 1; thinGlass: eta 1.5, attenuation
+ * colour 1, distance 1, thickness 1) */
+void b200_material_defaults(b200_material *m, int type);
 typedef struct {
   int pixelSamples;        /* spp */
   int maxPathLength;       /* default 20 */

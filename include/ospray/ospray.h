@@ -5,8 +5,8 @@
  * lists, the handle types and the enumeration values (OSPEnums.h) are the
  * API's.  The device behind it is "b200", the GB300 module
  * (libospray_module_b200.so, entry point ospray_module_init_b200), which
- * renders with CUDA.  What the b200 device supports of the object types is
- * listed in INTEGRATION.md of this project. */
+ * renders with CUDA.  Object types the b200 device does not implement are
+ * refused at creation with OSP_INVALID_ARGUMENT and a message naming them. */
 #pragma once
 
 #include <stdint.h>

@@ -45,7 +45,7 @@ OSPRAY_INTERFACE void ospSetVec4i(OSPObject, const char *n, int x, int y, int z,
 /* wraps obj in a one-element data array of `type` and sets it */
 OSPRAY_INTERFACE void ospSetObjectAsData(OSPObject target, const char *n, OSPDataType type, OSPObject obj);
 
-/* ospRenderFrame + ospWait; returns the frame's task duration (ospGetTaskDuration) */
+/* ospRenderFrame + ospWait; returns the framebuffer's variance estimate (ospGetVariance) */
 OSPRAY_INTERFACE float ospRenderFrameBlocking(OSPFrameBuffer, OSPRenderer, OSPCamera, OSPWorld);
 
 #ifdef __cplusplus

@@ -269,6 +269,7 @@ def lib():
             "b200_nrc_frame_defaults": (None, [P]),
             "b200_render_pt_nrc": (I, [P, ctypes.POINTER(CameraDesc), ctypes.POINTER(PTParams), P, I, P, P, P, P]),
             "b200_frame_relmse": (I, [P, P, ctypes.POINTER(ctypes.c_double)]),
+            "b200_frame_relmse_hits": (I, [P, P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int64)]),
             "b200_frame_variance": (I, [P, F, ctypes.POINTER(F)]),
             "b200_event_record": (I, [P, ctypes.POINTER(P)]),
             "b200_event_query": (I, [P]),
@@ -756,3 +757,11 @@ def relmse(frame, reference):
     v = ctypes.c_double()
     frame.device._check(lib().b200_frame_relmse(frame._h, reference._h, ctypes.byref(v)))
     return v.value
+
+
+def relmse_hits(frame, reference):
+    """relmse over the pixels whose reference depth is finite (first hit is
+    geometry); the reference needs FB_DEPTH.  Returns (relmse, pixels)."""
+    v, n = ctypes.c_double(), ctypes.c_int64()
+    frame.device._check(lib().b200_frame_relmse_hits(frame._h, reference._h, ctypes.byref(v), ctypes.byref(n)))
+    return v.value, n.value

@@ -176,45 +176,69 @@ void framePostProcess(FrameObj *fb, cudaStream_t st, bool variance) {
 // ---------------------------------------------------------------- relMSE
 namespace b200 {
 namespace {
-// sum over pixels of the mean over rgb of (x - r)^2 / (r^2 + 0.01)
-__global__ void k_relmse(const float4 *__restrict__ x, const float4 *__restrict__ r, long long n, double *sum) {
-  double acc = 0.0;
+// sum over pixels of the mean over rgb of (x - r)^2 / (r^2 + 0.01); with a
+// reference depth channel, only over the pixels whose reference depth is
+// finite (their first hit is geometry), counted in sum[1]
+__global__ void k_relmse(const float4 *__restrict__ x, const float4 *__restrict__ r, const float *__restrict__ rdepth,
+                         long long n, double *sum) {
+  double acc = 0.0, cnt = 0.0;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    if (rdepth && !isfinite(rdepth[i])) continue;
     const float4 a = x[i], b = r[i];
     const float e = ((a.x - b.x) * (a.x - b.x) / (b.x * b.x + 0.01f) + (a.y - b.y) * (a.y - b.y) / (b.y * b.y + 0.01f) +
                      (a.z - b.z) * (a.z - b.z) / (b.z * b.z + 0.01f)) *
                     (1.f / 3.f);
     acc += double(e);
+    cnt += 1.0;
   }
-  for (int off = 16; off; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
-  if ((threadIdx.x & 31) == 0) atomicAdd(sum, acc);
+  for (int off = 16; off; off >>= 1) {
+    acc += __shfl_xor_sync(0xffffffffu, acc, off);
+    cnt += __shfl_xor_sync(0xffffffffu, cnt, off);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(sum, acc);
+    atomicAdd(sum + 1, cnt);
+  }
 }
-}  // namespace
-}  // namespace b200
 
-extern "C" int b200_frame_relmse(b200_frame f, b200_frame ref, double *out) {
-  using namespace b200;
+int relmse(b200_frame f, b200_frame ref, bool hitsOnly, double *out, int64_t *npix) {
   if (!f || !ref || !out) return B200_INVALID_ARGUMENT;
   FrameObj *a = reinterpret_cast<FrameObj *>(f), *b = reinterpret_cast<FrameObj *>(ref);
   if (a->W != b->W || a->H != b->H || a->dev != b->dev) return B200_INVALID_ARGUMENT;
+  if (hitsOnly && !b->depth) {
+    a->dev->lastError = "relMSE over hit pixels: the reference framebuffer has no DEPTH channel";
+    return B200_INVALID_ARGUMENT;
+  }
   try {
     check(cudaSetDevice(a->dev->dev), "cudaSetDevice");
     cudaStream_t st = a->dev->stream;
     double *d = nullptr;
-    check(cudaMallocAsync(&d, sizeof(double), st), "alloc");
-    check(cudaMemsetAsync(d, 0, sizeof(double), st), "clear");
+    check(cudaMallocAsync(&d, 2 * sizeof(double), st), "alloc");
+    check(cudaMemsetAsync(d, 0, 2 * sizeof(double), st), "clear");
     const long long n = (long long)a->W * a->H;
-    k_relmse<<<unsigned(std::min<long long>((n + 255) / 256, 152 * 8)), 256, 0, st>>>(a->color, b->color, n, d);
-    double h = 0.0;
-    check(cudaMemcpyAsync(&h, d, sizeof(double), cudaMemcpyDeviceToHost, st), "read");
+    k_relmse<<<unsigned(std::min<long long>((n + 255) / 256, 152 * 8)), 256, 0, st>>>(
+        a->color, b->color, hitsOnly ? b->depth : nullptr, n, d);
+    double h[2] = {0.0, 0.0};
+    check(cudaMemcpyAsync(h, d, sizeof(h), cudaMemcpyDeviceToHost, st), "read");
     check(cudaFreeAsync(d, st), "free");
     check(cudaStreamSynchronize(st), "sync");
-    *out = h / double(n);
+    *out = h[1] > 0.0 ? h[0] / h[1] : 0.0;
+    if (npix) *npix = int64_t(h[1]);
     return B200_NO_ERROR;
   } catch (const Error &e) {
     a->dev->lastError = e.what();
     return e.code;
   }
+}
+}  // namespace
+}  // namespace b200
+
+extern "C" int b200_frame_relmse(b200_frame f, b200_frame ref, double *out) {
+  return b200::relmse(f, ref, false, out, nullptr);
+}
+
+extern "C" int b200_frame_relmse_hits(b200_frame f, b200_frame ref, double *out, int64_t *npix) {
+  return b200::relmse(f, ref, true, out, npix);
 }
 
 // LiveVarianceFrameOp::getAvgError (fb/frame_ops/Variance.cpp:32-46): the mean

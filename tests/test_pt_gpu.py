@@ -8,8 +8,9 @@ intersection) and evaluate the same BSDF and light formulas; transcendental
 functions differ in the last ulp between CUDA and the host libm, which can
 flip a Russian-roulette or occlusion decision in a small fraction of paths.
 So: first-hit IDs and depth agree exactly, per-pixel colours agree to 1e-3
-on the large majority of pixels, and the image means agree within 3
-standard errors of the per-pixel difference."""
+on >= 99.9 % of pixels (all of them in the runs so far; the margin is for a
+rare flipped decision), and the image means agree within 3 standard errors
+of the per-pixel difference."""
 import numpy as np
 import pytest
 
@@ -68,7 +69,7 @@ def test_pt_first_hit_and_image_match_oracle(pt_setup, b200_device):
     assert np.isfinite(g).all()
     close = np.all(np.abs(g - r) <= 1e-3 * np.maximum(1.0, np.abs(r)), axis=2)
     print("pixels within 1e-3: %.4f  mean gpu %.5f oracle %.5f" % (close.mean(), g.mean(), r.mean()))
-    assert close.mean() >= 0.90, close.mean()
+    assert close.mean() >= 0.999, close.mean()
     diff = (g - r).reshape(-1)
     se = diff.std() / np.sqrt(diff.size)
     assert abs(diff.mean()) <= 3 * se + 1e-6, (diff.mean(), se)
@@ -79,7 +80,8 @@ def test_pt_accumulation_matches_oracle(pt_setup, b200_device):
     gpu, ref = render_both(pt_setup, b200_device, spp=1, frames=3, pf=0, maxlen=3, rr=1)
     g, r = gpu["color"][..., :3], ref["color"][..., :3]
     close = np.all(np.abs(g - r) <= 1e-3 * np.maximum(1.0, np.abs(r)), axis=2)
-    assert close.mean() >= 0.90, close.mean()
+    print("accumulated: pixels within 1e-3: %.4f  mean gpu %.5f oracle %.5f" % (close.mean(), g.mean(), r.mean()))
+    assert close.mean() >= 0.999, close.mean()
     assert abs(g.mean() - r.mean()) <= 0.02 * r.mean() + 1e-4
 
 
