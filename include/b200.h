@@ -491,7 +491,9 @@ int b200_batch_info(b200_batch batch, int64_t *info4);
  * entries per level, resolutions 16..2048 over the cube around the bounds)
  * of the position, real spherical harmonics (degree 3, 16 terms) of the
  * direction, the normal, roughness and albedo, into a 64-wide MLP with 4
- * hidden ReLU layers and a 3-wide output, BF16 weights on the tensor cores
+ * hidden ReLU layers and a 3-wide output, BF16 weights on the 5th-generation
+ * tensor cores (tcgen05.mma, 128 samples per tile, FP32 accumulators in
+ * tensor memory)
  * with FP32 accumulation; trained with Adam on the relative L2 loss.
  * Records are 16 floats: position[3], direction[3] (unit, pointing away from
  * the surface), normal[3], roughness, albedo[3], target rgb[3] (training) or
@@ -520,6 +522,13 @@ int b200_nrc_set_params(b200_nrc nrc, const float *weights, const float *table);
 /* the grid: lo xyz and 1/extent; per level the scale (N_l - 1) and the dense
  * side length (0 = hashed) */
 int b200_nrc_grid(b200_nrc nrc, float *lo_invext4, float *scales16, uint32_t *dense16);
+
+/* Check of the radiance cache's tensor-core building block (no counterpart in
+ * the reference): one 128 x n x 64 BF16 product D = A B^T on the device's
+ * 5th-generation tensor cores (tcgen05.mma, FP32 accumulator in tensor
+ * memory).  Host arrays: a 128 x 64, b n x 64 (rounded to BF16), out 128 x n;
+ * n = 16, 32 or 64.  Synchronous. */
+int b200_tensor_core_check(b200_device dev, const float *a, const float *b, int n, float *out);
 
 /* ---- path tracing with the radiance cache.  Renders one frame like
  * b200_render_pt, except: every other path, at its first vertex after a

@@ -4,7 +4,6 @@
 //   nextEventEstimation     render/pathtracer/NextEventEstimation.ispc:25-160
 //   evaluateVirtualLights   render/pathtracer/VirtualLight.ispc:38-107
 //   transparentShadow       render/pathtracer/TransparentShadow.ispc:18-85
-//                           (opaque materials: the first hit blocks the light)
 //   misHeuristic            render/pathtracer/PathTracerUtil.ih:30-46
 //   light list + CDF        render/pathtracer/PathTracerData.cpp:32-82
 //   parameters              render/pathtracer/PathTracer.cpp:29-51
@@ -86,22 +85,47 @@ struct Vertex {
 struct Ctx {
   const Scene &sc;
   const PtLights &L;
-  const std::vector<PrincipledParams> &mats;
+  const std::vector<MaterialParams> &mats;
   const PtParams &p;
   int nFirst, nIndirect;
+  bool transparentShadows;  // some material lets shadow rays through
 };
 
-// shading frame: makeShadingFrame(dg) with dPds = instance xfm * (1,0,0)
-L3 shadingFrame(const DG &dg, V3 dPds) {
-  const V3 N = dg.Ns;
-  V3 U = normalize(dPds);
-  V3 V = cross(N, U);
-  if (dot(V, V) > 0.f) {
-    V = normalize(V);
-    U = cross(V, N);
-    return {U, V, N};
+const MaterialParams *materialOf(const Ctx &c, const Hit &hit) {
+  const InstanceEntry &e = c.sc.entries[hit.entry];
+  if (e.material < 0 || size_t(e.material) >= c.mats.size()) return nullptr;
+  return &c.mats[e.material];
+}
+
+// transparentShadow (render/pathtracer/TransparentShadow.ispc:18-85): the
+// shadow ray's closest hits in turn, each multiplying the contribution by
+// the material's transparency and the medium's Beer attenuation over the
+// segment, until the light is reached (the remaining contribution) or the
+// contribution drops to minContribution / maxPathLength surfaces were crossed
+// (0).  Without transparent materials the first hit blocks the light.
+V3 transparentShadow(const Ctx &c, V3 lightContrib, Ray shadowRay, Medium medium) {
+  if (!c.transparentShadows) {
+    tl_rays++;
+    return c.sc.occluded(shadowRay) ? v3(0.f) : lightContrib;
   }
-  return frame(N);
+  int maxDepth = c.p.maxPathLength;
+  const float tOriginal = shadowRay.tfar;
+  for (;;) {
+    Hit hit;
+    tl_rays++;
+    if (!c.sc.intersect(shadowRay, hit)) return lightContrib;
+    const DG dg = postIntersect(c.sc, shadowRay, hit);
+    const MaterialParams *m = materialOf(c, hit);
+    const V3 T = m ? materialTransparency(*m, dg, shadowRay.dir, medium) : v3(0.f);
+    lightContrib = lightContrib * T;
+    if (medium.att.x != 0.f || medium.att.y != 0.f || medium.att.z != 0.f) {
+      const V3 a = medium.att * (hit.t - shadowRay.tnear);
+      lightContrib = lightContrib * V3{std::exp(a.x), std::exp(a.y), std::exp(a.z)};
+    }
+    if (reduce_max(lightContrib) <= c.p.minContribution || --maxDepth <= 0) return v3(0.f);
+    if (m) medium = nextMedium(*m, medium);
+    shadowRay = {shadowRay.org, hit.t + dg.epsilon, shadowRay.dir, tOriginal};
+  }
 }
 
 V3 virtualLights(const Ctx &c, bool straightPath, const Vertex &last, bool env, const Ray &ray, float t,
@@ -121,7 +145,8 @@ V3 virtualLights(const Ctx &c, bool straightPath, const Vertex &last, bool env, 
   return L;
 }
 
-V3 nee(const Ctx &c, LDSampler &ld, const DG &dg, const Principled &bsdf, V3 wo, V3 throughput, int numLS) {
+V3 nee(const Ctx &c, LDSampler &ld, const DG &dg, const SurfaceBSDF &bsdf, V3 wo, V3 throughput, int numLS,
+       const Medium &medium) {
   V3 L = v3(0.f);
   const int nl = int(c.L.kind.size());
   for (int i = 0; i < numLS; i++) {
@@ -148,10 +173,8 @@ V3 nee(const Ctx &c, LDSampler &ld, const DG &dg, const Principled &bsdf, V3 wo,
     if (reduce_max(fe.value) <= 0.f) continue;
     V3 org = dg.P;
     if (dot(dg.Ng, ls.dir) < 0.f) org = org - (2.f * dg.epsilon) * dg.Ng;
-    tl_rays++;
-    if (c.sc.occluded({org, 0.f, ls.dir, ls.dist})) continue;
-    const V3 contrib = throughput * fe.value * ls.weight;
-    L = L + contrib * mis(ls.pdf, fe.pdf);
+    const V3 contrib = transparentShadow(c, throughput * fe.value * ls.weight, {org, 0.f, ls.dir, ls.dist}, medium);
+    if (reduce_max(contrib) > 0.f) L = L + contrib * mis(ls.pdf, fe.pdf);
   }
   return L;
 }
@@ -168,6 +191,7 @@ PathOut samplePath(const Ctx &c, LDSampler &ld, Ray ray) {
   V3 throughput = v3(1.f), contribution = v3(0.f);
   int depth = 0, scatteringEvents = 0;
   bool straightPath = true, firstBounceLight = true;
+  Medium medium = vacuum();
   Vertex last;
   last.env = false;
   last.pdf_w = INFINITY;
@@ -197,27 +221,28 @@ PathOut samplePath(const Ctx &c, LDSampler &ld, Ray ray) {
     }
     if (depth >= c.p.maxPathLength || scatteringEvents >= c.p.maxScatteringEvents) break;
     const InstanceEntry *e = &c.sc.entries[hit.entry];
-    if (e->material < 0 || size_t(e->material) >= c.mats.size()) break;  // no material: no BSDF
-    Principled bsdf;
-    bsdf.init(c.mats[e->material], shadingFrame(dg, e->identity ? v3(1, 0, 0) : e->xfm.l.vx));
-    if (bsdf.impSum == 0.f) break;
+    const MaterialParams *mat = materialOf(c, hit);
+    if (!mat) break;  // no material: no BSDF
+    const SurfaceBSDF bsdf = makeBSDF(*mat, dg, e->identity ? v3(1, 0, 0) : e->xfm.l.vx, medium);
     ld.nextGroup();
     int numLS = 0;
-    {  // isSmooth: diffuse or glossy lobes present
+    if (bsdf.smooth) {
       if (scatteringEvents == 0) {  // updateAuxilliaryData (PathTracerUtil.ih:48-60)
         out.albedo = throughput * bsdf.albedo;
         out.normal = throughput * bsdf.N;
       }
       numLS = firstBounceLight ? c.nFirst : c.nIndirect;
-      contribution = contribution + nee(c, ld, dg, bsdf, wo, throughput, numLS);
+      contribution = contribution + nee(c, ld, dg, bsdf, wo, throughput, numLS, medium);
       firstBounceLight = false;
     }
     float ss;
     uint32_t uu3;
     const V2 s = ld.getNext4Samples(ss, uu3);
     BSDFSample fs = bsdf.sample(wo, s, ss);
+    // consistent side of the surface (light leaks)
     const bool sameSide = dot(fs.wi, dg.Ng) >= 0.f;
-    if (!sameSide) fs.weight = v3(0.f);  // every lobe here is a reflection
+    const bool reflection = (fs.type & SCATTER_REFLECTION) != 0;
+    if (sameSide != reflection) fs.weight = v3(0.f);
     if (reduce_max(fs.weight) <= 0.f || fs.pdf <= 0.f) break;
     throughput = throughput * fs.weight;
     if (depth >= c.p.roulettePathLength) {
@@ -226,13 +251,26 @@ PathOut samplePath(const Ctx &c, LDSampler &ld, Ray ray) {
       if (rr > contProb) break;
       throughput = throughput * (1.f / contProb);
     }
-    last.dg = dg;
-    last.pdf_w = fs.pdf;
-    last.numLightSamples = numLS;
+    // Beer's law over the segment that reached this vertex
+    if (std::fmin(std::fmin(medium.att.x, medium.att.y), medium.att.z) < 0.f) {
+      const V3 a = medium.att * t;
+      throughput = throughput * V3{std::exp(a.x), std::exp(a.y), std::exp(a.z)};
+    }
+    V3 org = dg.P;
+    if (fs.type & SCATTER_TRANSMISSION) {
+      org = org - (2.f * dg.epsilon) * dg.Ng;
+      medium = nextMedium(*mat, medium);
+    }
+    // a specular transmission keeps the last vertex (MIS through transparencies)
+    if (fs.type & ~SCATTER_SPEC_T) {
+      last.dg = dg;
+      last.pdf_w = fs.pdf;
+      last.numLightSamples = numLS;
+    }
     if (!(ray.dir.x == fs.wi.x && ray.dir.y == fs.wi.y && ray.dir.z == fs.wi.z)) straightPath = false;
-    ray = {dg.P, 0.f, fs.wi, INFINITY};
+    ray = {org, 0.f, fs.wi, INFINITY};
     depth++;
-    scatteringEvents++;
+    if (fs.type & SCATTER_SMOOTH) scatteringEvents++;
   } while (reduce_max(throughput) > c.p.minContribution);
   out.rgb = contribution;
   if (std::isnan(contribution.x) || std::isnan(contribution.y) || std::isnan(contribution.z)) {
@@ -244,13 +282,15 @@ PathOut samplePath(const Ctx &c, LDSampler &ld, Ray ray) {
 
 }  // namespace
 
-void renderPT(const Scene &sc, const PtLights &lights, const std::vector<PrincipledParams> &mats, const Camera &cam,
+void renderPT(const Scene &sc, const PtLights &lights, const std::vector<MaterialParams> &mats, const Camera &cam,
               const PixelFilter &pf, const PtParams &p, FrameBuffer &fb, int nthreads, int y0, int y1) {
   const int W = fb.W;
   const int nl = int(lights.kind.size());
   const int nFirst = p.lightSamples >= 0 && nl > 0 ? p.lightSamples : std::min(1024, nl);
   const int nIndirect = p.limitIndirectLightSamples && nFirst >= 1 ? 1 : nFirst;
-  const Ctx c = {sc, lights, mats, p, nFirst, nIndirect};
+  bool transparent = false;
+  for (const MaterialParams &m : mats) transparent = transparent || transparentMaterial(m);
+  const Ctx c = {sc, lights, mats, p, nFirst, nIndirect, transparent};
   const V2 rcpSize = {1.f / float(fb.W), 1.f / float(fb.H)};
   const uint32_t accumID = uint32_t(fb.frameID);
   parallelRows(y1 - y0, nthreads, [&](int yy) {
@@ -305,7 +345,7 @@ struct OrCameraPT {
 
 struct OrPtScene {
   PtLights lights;
-  std::vector<PrincipledParams> mats;
+  std::vector<MaterialParams> mats;
 };
 
 extern "C" {
@@ -314,7 +354,14 @@ void *or_pt_new() { return new OrPtScene(); }
 void or_pt_free(void *p) { delete static_cast<OrPtScene *>(p); }
 int or_pt_add_material(void *p, const float *baseColor, float roughness, float metallic) {
   OrPtScene &s = *static_cast<OrPtScene *>(p);
-  s.mats.push_back({{baseColor[0], baseColor[1], baseColor[2]}, roughness, metallic});
+  const float f[24] = {baseColor[0], baseColor[1], baseColor[2], roughness, metallic, 1.f};
+  s.mats.push_back(commitMaterial(MAT_PRINCIPLED, f));
+  return int(s.mats.size() - 1);
+}
+// type MAT_*, params: 24 floats in b200_material order after its type field
+int or_pt_add_material2(void *p, int type, const float *params) {
+  OrPtScene &s = *static_cast<OrPtScene *>(p);
+  s.mats.push_back(commitMaterial(type, params));
   return int(s.mats.size() - 1);
 }
 // position, edge1, edge2 (3 floats each), radiance rgb

@@ -140,7 +140,8 @@ struct AlbedoTables {
 const AlbedoTables &albedoTables();
 
 // ---- principled BSDF restricted to the plastic + conductor lobes
-enum : int { SCATTER_DIFFUSE_R = 1, SCATTER_GLOSSY_R = 4 };
+// scattering types (render/pathtracer/Scattering.ih:8-47)
+enum : int { SCATTER_SPEC_R = 1, SCATTER_GLOSSY_R = 2, SCATTER_DIFFUSE_R = 4 };
 
 struct PrincipledParams {
   V3 baseColor;
@@ -236,5 +237,84 @@ struct SphereLight {
   LightSample sample(const DG &dg, V2 s) const;
   LightEval eval(const DG &dg, V3 dir, float minDist, float maxDist) const;
 };
+
+// ---- materials of the path tracer beyond the principled stack
+//   render/materials/Principled.ispc:81-455 (root MultiBSDF with the cut-out)
+//   render/materials/OBJ.ispc:29-126, OBJ.cpp:28-65; bsdfs/Lambert.ih,
+//     Specular.ih, Transmission.ih, math/sampling.ih
+//   render/materials/Metal.ispc:16-48, Metal.cpp:27-70; bsdfs/Conductor.ih,
+//     MicrofacetConductor.ih, Fresnel.ih (FresnelConductorRGBUniform)
+//   render/materials/Glass.ispc:16-60, Glass.cpp:27-50; bsdfs/RobustDielectric.ih
+//   render/materials/ThinGlass.ispc:16-70, ThinGlass.cpp:27-45;
+//     bsdfs/RobustThinDielectric.ih
+//   render/materials/Medium.ih
+enum : int { MAT_PRINCIPLED = 0, MAT_OBJ = 1, MAT_METAL = 2, MAT_GLASS = 3, MAT_THINGLASS = 4 };
+enum : int {
+  SCATTER_SPEC_T = 8,
+  SCATTER_GLOSSY_T = 16,
+  SCATTER_DIFFUSE_T = 32,
+  SCATTER_REFLECTION = SCATTER_SPEC_R | SCATTER_GLOSSY_R | SCATTER_DIFFUSE_R,
+  SCATTER_TRANSMISSION = SCATTER_SPEC_T | SCATTER_GLOSSY_T | SCATTER_DIFFUSE_T,
+  SCATTER_SPECULAR = SCATTER_SPEC_R | SCATTER_SPEC_T,
+  SCATTER_SMOOTH = SCATTER_GLOSSY_R | SCATTER_DIFFUSE_R | SCATTER_GLOSSY_T | SCATTER_DIFFUSE_T
+};
+
+struct Medium {
+  float ior;
+  V3 att;
+};
+inline bool sameMedium(const Medium &a, const Medium &b) {
+  return a.ior == b.ior && a.att.x == b.att.x && a.att.y == b.att.y && a.att.z == b.att.z;
+}
+inline Medium vacuum() { return {1.f, v3(0.f)}; }
+
+// a material after its type's commit
+struct MaterialParams {
+  int type = MAT_PRINCIPLED;
+  V3 baseColor = v3(0.8f);  // principled baseColor; obj kd (energy-scaled)
+  float roughness = 0.f, metallic = 0.f, opacity = 1.f;
+  V3 ks = v3(0.f), tf = v3(0.f);  // obj (energy-scaled)
+  float ns = 10.f;
+  V3 eta = v3(0.f), k = v3(0.f);  // metal
+  Medium inside = {1.f, v3(0.f)}, outside = {1.f, v3(0.f)};  // glass
+  float thinEta = 1.f;  // thin glass: 1 / eta
+  V3 thinAtt = v3(0.f);
+};
+// p: baseColor[3], roughness, metallic, opacity, ks[3], ns, tf[3], eta[3],
+// k[3], attenuationColor[3], attenuationDistance, thickness (24 floats, the
+// b200_material fields after its type)
+MaterialParams commitMaterial(int type, const float *p);
+bool transparentMaterial(const MaterialParams &m);
+
+struct SurfaceBSDF {
+  int type = MAT_PRINCIPLED;
+  bool smooth = false;
+  V3 albedo = v3(0.f), N = v3(0.f);
+  // principled: base stack + root (transmission importance tr, stack weight op)
+  Principled st;
+  float op = 0.f, tr = 0.f, impSum = 0.f;
+  bool hasStack = false, hasCut = false;
+  // obj
+  L3 fr;
+  V3 Kd = v3(0.f), T = v3(0.f), ksN = v3(0.f), specW = v3(0.f);
+  float nsB = 0.f, iL = 0.f, iT = 0.f, iS = 0.f;
+  // metal
+  V3 ceta = v3(0.f), ck = v3(0.f);
+  float rough = 0.f;
+  GGX ggx = {0.f, 0.f};
+  bool specular = false;
+  // glass (RobustDielectric) and thin glass
+  float geta = 1.f;
+  V3 Ns = v3(0.f), Ng = v3(0.f), tatt = v3(0.f);
+  BSDFEval eval(V3 wo, V3 wi) const;
+  BSDFSample sample(V3 wo, V2 s, float ss) const;
+};
+// Material_dispatch_getBSDF for a hit with differential geometry dg; dPds the
+// instance's x axis (makeShadingFrame), cur the path's current medium
+SurfaceBSDF makeBSDF(const MaterialParams &m, const DG &dg, V3 dPds, const Medium &cur);
+// Material_getTransparency for a shadow ray of direction rayDir
+V3 materialTransparency(const MaterialParams &m, const DG &dg, V3 rayDir, const Medium &cur);
+// Material_selectNextMedium (glass; the others keep the medium)
+Medium nextMedium(const MaterialParams &m, const Medium &cur);
 
 }  // namespace orc

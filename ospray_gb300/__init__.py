@@ -74,7 +74,59 @@ class PickResult(ctypes.Structure):
 
 
 class Material(ctypes.Structure):
-    _fields_ = [("baseColor", ctypes.c_float * 3), ("roughness", ctypes.c_float), ("metallic", ctypes.c_float)]
+    _fields_ = [("baseColor", ctypes.c_float * 3), ("roughness", ctypes.c_float), ("metallic", ctypes.c_float),
+                ("type", ctypes.c_int), ("opacity", ctypes.c_float), ("ks", ctypes.c_float * 3),
+                ("ns", ctypes.c_float), ("tf", ctypes.c_float * 3), ("eta", ctypes.c_float * 3),
+                ("k", ctypes.c_float * 3), ("attenuationColor", ctypes.c_float * 3),
+                ("attenuationDistance", ctypes.c_float), ("thickness", ctypes.c_float)]
+
+
+MATERIAL_PRINCIPLED, MATERIAL_OBJ, MATERIAL_METAL, MATERIAL_GLASS, MATERIAL_THINGLASS = 0, 1, 2, 3, 4
+_MATERIAL_TYPES = {"principled": MATERIAL_PRINCIPLED, "obj": MATERIAL_OBJ, "metal": MATERIAL_METAL,
+                   "glass": MATERIAL_GLASS, "thinGlass": MATERIAL_THINGLASS}
+
+
+def principled(base_color=(0.8, 0.8, 0.8), roughness=0.0, metallic=0.0, opacity=1.0):
+    return dict(type="principled", baseColor=base_color, roughness=roughness, metallic=metallic, opacity=opacity)
+
+
+def obj_material(kd=(0.8, 0.8, 0.8), ks=(0.0, 0.0, 0.0), ns=10.0, d=1.0, tf=(0.0, 0.0, 0.0)):
+    return dict(type="obj", baseColor=kd, ks=ks, ns=ns, opacity=d, tf=tf)
+
+
+def metal(eta=(1.47, 0.984, 0.602), k=(7.64, 6.55, 5.36), roughness=0.1):
+    return dict(type="metal", eta=eta, k=k, roughness=roughness)
+
+
+def glass(eta_inside=1.5, eta_outside=1.0, attenuation_color=(1.0, 1.0, 1.0), attenuation_distance=1.0):
+    return dict(type="glass", eta=(eta_inside, eta_outside, 0.0), attenuationColor=attenuation_color,
+                attenuationDistance=attenuation_distance)
+
+
+def thin_glass(eta=1.5, attenuation_color=(1.0, 1.0, 1.0), attenuation_distance=1.0, thickness=1.0):
+    return dict(type="thinGlass", eta=(eta, 0.0, 0.0), attenuationColor=attenuation_color,
+                attenuationDistance=attenuation_distance, thickness=thickness)
+
+
+def material_struct(m):
+    """A b200_material from a (r, g, b, roughness, metallic) principled tuple
+    or a dict made by principled / obj_material / metal / glass / thin_glass."""
+    out = Material()
+    if isinstance(m, dict):
+        t = _MATERIAL_TYPES[m.get("type", "principled")]
+        lib().b200_material_defaults(ctypes.byref(out), t)
+        for key, val in m.items():
+            if key == "type":
+                continue
+            if isinstance(val, (tuple, list, np.ndarray)):
+                getattr(out, key)[:] = [float(x) for x in val]
+            else:
+                setattr(out, key, float(val))
+        return out
+    lib().b200_material_defaults(ctypes.byref(out), MATERIAL_PRINCIPLED)
+    out.baseColor[:] = [float(m[0]), float(m[1]), float(m[2])]
+    out.roughness, out.metallic = float(m[3]), float(m[4])
+    return out
 
 
 class PTParams(ctypes.Structure):
@@ -150,11 +202,11 @@ def light_from_dict(L):
 
 
 def materials_array(mats):
-    """mats: iterable of (r, g, b, roughness, metallic)."""
+    """mats: iterable of principled (r, g, b, roughness, metallic) tuples or
+    material dicts (principled / obj_material / metal / glass / thin_glass)."""
     arr = (Material * max(1, len(mats)))()
     for i, m in enumerate(mats):
-        arr[i].baseColor[:] = [float(m[0]), float(m[1]), float(m[2])]
-        arr[i].roughness, arr[i].metallic = float(m[3]), float(m[4])
+        arr[i] = material_struct(m)
     return arr, len(mats)
 
 
@@ -246,6 +298,8 @@ def lib():
             "b200_frame_create": (I, [P, I, I, I, U32, ctypes.POINTER(P)]),
             "b200_frame_channel_bytes": (ctypes.c_size_t, [P, U32]),
             "b200_tonemapper_defaults": (None, [ctypes.POINTER(ToneMapper)]),
+            "b200_material_defaults": (None, [ctypes.POINTER(Material), I]),
+            "b200_tensor_core_check": (I, [P, P, P, I, P]),
             "b200_frame_set_tonemapper": (I, [P, ctypes.POINTER(ToneMapper)]),
             "b200_pick": (I, [P, ctypes.POINTER(CameraDesc), F, F, ctypes.POINTER(PickResult)]),
             "b200_batch_create": (I, [P, ctypes.POINTER(P)]),
@@ -757,6 +811,15 @@ def relmse(frame, reference):
     v = ctypes.c_double()
     frame.device._check(lib().b200_frame_relmse(frame._h, reference._h, ctypes.byref(v)))
     return v.value
+
+
+def tensor_core_check(device, a, b):
+    """D = A B^T (A 128 x 64, B n x 64, BF16 operands) on the tcgen05 tensor cores."""
+    a = np.ascontiguousarray(a, np.float32)
+    b = np.ascontiguousarray(b, np.float32)
+    out = np.zeros((128, b.shape[0]), np.float32)
+    device._check(lib().b200_tensor_core_check(device._h, _ptr(a), _ptr(b), int(b.shape[0]), _ptr(out)))
+    return out
 
 
 def relmse_hits(frame, reference):

@@ -171,6 +171,97 @@ PixelFilterD DeviceObj::filter(int type) const {
   return pf;
 }
 
+// A material as the shading kernels read it, with each type's commit-time
+// normalisation: OBJ scales kd + ks + tf down to 1 (OBJ::commit,
+// render/materials/OBJ.cpp:45-53); glass keeps the inside and outside media
+// as (ior, log(attenuation colour) / attenuation distance) (Glass::commit,
+// Glass.cpp:27-50); thin glass keeps 1 / eta and log(colour) x thickness /
+// distance (ThinGlass::commit, ThinGlass.cpp:27-45).
+MaterialD toMaterialD(const b200_material &m) {
+  MaterialD d;
+  std::memset(&d, 0, sizeof(d));
+  d.kind = uint32_t(m.type);
+  d.opacity = 1.f;
+  d.iorIn = d.iorOut = 1.f;
+  const float eps = 1e-6f;
+  switch (m.type) {
+    case B200_MATERIAL_PRINCIPLED:
+      d.r = m.baseColor[0];
+      d.g = m.baseColor[1];
+      d.b = m.baseColor[2];
+      d.roughness = m.roughness;
+      d.metallic = m.metallic;
+      d.opacity = m.opacity;
+      if (1.f - m.opacity > eps) d.flags |= MATF_TRANSPARENT;
+      break;
+    case B200_MATERIAL_OBJ: {
+      float kd[3], ks[3], tf[3], total = 0.f;
+      for (int c = 0; c < 3; c++) {
+        kd[c] = m.baseColor[c];
+        ks[c] = m.ks[c];
+        tf[c] = m.tf[c];
+        total = std::max(total, kd[c] + ks[c] + tf[c]);
+      }
+      if (total > 1.f)
+        for (int c = 0; c < 3; c++) {
+          kd[c] /= total;
+          ks[c] /= total;
+          tf[c] /= total;
+        }
+      d.r = kd[0];
+      d.g = kd[1];
+      d.b = kd[2];
+      for (int c = 0; c < 3; c++) {
+        d.ks[c] = ks[c];
+        d.tf[c] = tf[c];
+      }
+      d.ns = m.ns;
+      d.opacity = m.opacity;
+      for (int c = 0; c < 3; c++)
+        if (tf[c] * m.opacity + (1.f - m.opacity) > 0.f) d.flags |= MATF_TRANSPARENT;
+      break;
+    }
+    case B200_MATERIAL_METAL:
+      d.roughness = m.roughness;
+      for (int c = 0; c < 3; c++) {
+        d.ceta[c] = m.eta[c];
+        d.ck[c] = m.k[c];
+      }
+      break;
+    case B200_MATERIAL_GLASS:
+      d.iorIn = m.eta[0];
+      d.iorOut = m.eta[1];
+      for (int c = 0; c < 3; c++) d.att[c] = std::log(m.attenuationColor[c]) / std::max(m.attenuationDistance, eps);
+      d.flags |= MATF_TRANSPARENT;
+      break;
+    case B200_MATERIAL_THINGLASS: {
+      d.eta = 1.f / m.eta[0];
+      const float scale = m.thickness * (1.f / std::max(m.attenuationDistance, eps));
+      for (int c = 0; c < 3; c++) d.att[c] = std::log(m.attenuationColor[c]) * scale;
+      d.flags |= MATF_TRANSPARENT;
+      break;
+    }
+    default:
+      throw Error(B200_INVALID_ARGUMENT, "unknown material type " + std::to_string(m.type));
+  }
+  return d;
+}
+
+bool anyTransparent(const b200_material *materials, int n) {
+  for (int i = 0; i < n; i++)
+    if (toMaterialD(materials[i]).flags & MATF_TRANSPARENT) return true;
+  return false;
+}
+
+// a material list that needs the shading kernel with every material type:
+// a type other than principled, or a material shadow rays pass through
+bool anyNonPrincipled(const b200_material *materials, int n) {
+  for (int i = 0; i < n; i++)
+    if (materials[i].type != B200_MATERIAL_PRINCIPLED || (toMaterialD(materials[i]).flags & MATF_TRANSPARENT))
+      return true;
+  return false;
+}
+
 // the renderer's material list on the device, uploaded when it changed
 void uploadMaterials(SceneObj *sc, const b200_material *materials, int nmaterials) {
   const bool same = int(sc->lastMaterials.size()) == nmaterials &&
@@ -178,9 +269,11 @@ void uploadMaterials(SceneObj *sc, const b200_material *materials, int nmaterial
                      std::memcmp(sc->lastMaterials.data(), materials, sizeof(b200_material) * nmaterials) == 0);
   if (!same) {
     std::vector<MaterialD> h(nmaterials);
-    for (int i = 0; i < nmaterials; i++)
-      h[i] = {materials[i].baseColor[0], materials[i].baseColor[1], materials[i].baseColor[2], materials[i].roughness,
-              materials[i].metallic};
+    bool transparent = false;
+    for (int i = 0; i < nmaterials; i++) {
+      h[i] = toMaterialD(materials[i]);
+      transparent = transparent || (h[i].flags & MATF_TRANSPARENT);
+    }
     if (nmaterials > sc->capMaterials) {
       if (sc->dMaterials) cudaFree(sc->dMaterials);
       check(cudaMalloc(&sc->dMaterials, sizeof(MaterialD) * nmaterials), "alloc materials");
@@ -190,6 +283,7 @@ void uploadMaterials(SceneObj *sc, const b200_material *materials, int nmaterial
       check(cudaMemcpy(sc->dMaterials, h.data(), sizeof(MaterialD) * nmaterials, cudaMemcpyHostToDevice),
             "upload materials");
     sc->lastMaterials.assign(materials, materials + nmaterials);
+    sc->transparentMaterials = transparent;
   }
   sc->nMaterials = nmaterials;
 }
@@ -210,8 +304,11 @@ void ensurePtWorkspace(DeviceObj *dev, size_t need) {
 // PathTracer::commit (render/pathtracer/PathTracer.cpp:29-51): light sample
 // counts (lightSamples < 0: all lights at the first bounce; one after it
 // when limitIndirectLightSamples)
-PtParamsD makePtParams(const b200_pt_params &p, int nl, int nmaterials) {
+PtParamsD makePtParams(const b200_pt_params &p, int nl, int nmaterials, bool transparentShadows,
+                       bool allMaterials) {
   PtParamsD d;
+  d.transparentShadows = transparentShadows ? 1 : 0;
+  d.allMaterials = allMaterials ? 1 : 0;
   d.spp = p.pixelSamples;
   d.maxPathLength = p.maxPathLength;
   d.roulettePathLength = p.roulettePathLength;
@@ -838,6 +935,41 @@ void b200_tonemapper_defaults(b200_tonemapper *tm) {
   tm->acesColor = 1;
 }
 
+void b200_material_defaults(b200_material *m, int type) {
+  if (!m) return;
+  std::memset(m, 0, sizeof(*m));
+  m->type = type;
+  m->opacity = 1.f;
+  m->attenuationColor[0] = m->attenuationColor[1] = m->attenuationColor[2] = 1.f;
+  m->attenuationDistance = 1.f;
+  m->thickness = 1.f;
+  switch (type) {
+    case B200_MATERIAL_PRINCIPLED:  // Principled::commit, render/materials/Principled.cpp:37-79
+    case B200_MATERIAL_OBJ:         // OBJMaterial::commit, OBJ.cpp:28-38
+      m->baseColor[0] = m->baseColor[1] = m->baseColor[2] = 0.8f;
+      m->ns = 10.f;
+      break;
+    case B200_MATERIAL_METAL:  // Metal::commit, Metal.cpp:27-31: aluminium (math/spectrum.h RGB_AL_ETA / RGB_AL_K)
+      m->eta[0] = 1.47f;
+      m->eta[1] = 0.984f;
+      m->eta[2] = 0.602f;
+      m->k[0] = 7.64f;
+      m->k[1] = 6.55f;
+      m->k[2] = 5.36f;
+      m->roughness = 0.1f;
+      break;
+    case B200_MATERIAL_GLASS:  // Glass::commit, Glass.cpp:27-38
+      m->eta[0] = 1.5f;
+      m->eta[1] = 1.f;
+      break;
+    case B200_MATERIAL_THINGLASS:  // ThinGlass::commit, ThinGlass.cpp:27-33
+      m->eta[0] = 1.5f;
+      break;
+    default:
+      break;
+  }
+}
+
 int b200_frame_set_tonemapper(b200_frame f, const b200_tonemapper *tm) {
   if (!f) return B200_INVALID_ARGUMENT;
   FrameObj *fb = reinterpret_cast<FrameObj *>(f);
@@ -1036,7 +1168,8 @@ int b200_render_pt(b200_scene s, const b200_camera_desc *camera, const b200_pt_p
     require(nmaterials >= 0 && (nmaterials == 0 || materials), "bad material array");
     cudaStream_t st = stream ? (cudaStream_t)stream : sc->dev->stream;
     uploadMaterials(sc, materials, nmaterials);
-    const PtParamsD d = makePtParams(*p, sc->nLights, nmaterials);
+    const PtParamsD d =
+        makePtParams(*p, sc->nLights, nmaterials, sc->transparentMaterials, anyNonPrincipled(materials, nmaterials));
     DeviceObj *dev = sc->dev;
     ensurePtWorkspace(dev, ptWorkspaceBytes((long long)fb->W * fb->H * p->pixelSamples));
     fb->beginFrame(p->pixelSamples, st);

@@ -105,6 +105,7 @@ struct SceneObj {
   float3 *dTfColor = nullptr;
   uint8_t *dCellEmpty = nullptr;
   std::vector<b200_material> lastMaterials;
+  bool transparentMaterials = false;  // some material of lastMaterials lets shadow rays through
   explicit SceneObj(DeviceObj *d);
   ~SceneObj();
   void commit();
@@ -161,7 +162,12 @@ struct FrameObj {
 };
 
 CameraD makeCamera(const b200_camera_desc &c);
-PtParamsD makePtParams(const b200_pt_params &p, int numLights, int numMaterials);
+PtParamsD makePtParams(const b200_pt_params &p, int numLights, int numMaterials, bool transparentShadows,
+                       bool allMaterials);
+// b200_material -> device record (throws Error on an unknown type)
+MaterialD toMaterialD(const b200_material &m);
+bool anyTransparent(const b200_material *materials, int n);
+bool anyNonPrincipled(const b200_material *materials, int n);
 void uploadMaterials(SceneObj *sc, const b200_material *materials, int nmaterials);
 void ensurePtWorkspace(DeviceObj *dev, size_t need);
 AOParamsD makeAOParams(const b200_ao_params &p);

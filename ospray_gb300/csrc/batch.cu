@@ -264,13 +264,15 @@ int b200_batch_add_pt(b200_batch h, b200_scene s, const b200_camera_desc *camera
     r.fb = fb;
     r.cam = *camera;
     r.pixelFilter = p->pixelFilter;
-    r.pt = makePtParams(*p, sc->nLights, nmaterials);
+    // the batched wavefront traces shadow rays as any-hit queries only
+    requireArg(!anyTransparent(materials, nmaterials),
+               "batch: materials that let shadow rays through (opacity < 1, obj tf / d, glass) are rendered by "
+               "b200_render_pt only");
+    r.pt = makePtParams(*p, sc->nLights, nmaterials, false, true);
     r.ao = AOParamsD{};
     if (nmaterials) {
       std::vector<MaterialD> m(nmaterials);
-      for (int i = 0; i < nmaterials; i++)
-        m[i] = {materials[i].baseColor[0], materials[i].baseColor[1], materials[i].baseColor[2],
-                materials[i].roughness, materials[i].metallic};
+      for (int i = 0; i < nmaterials; i++) m[i] = toMaterialD(materials[i]);
       check(cudaMalloc(&r.dMats, sizeof(MaterialD) * nmaterials), "batch materials");
       check(cudaMemcpy(r.dMats, m.data(), sizeof(MaterialD) * nmaterials, cudaMemcpyHostToDevice),
             "upload batch materials");

@@ -100,6 +100,8 @@ struct PtParamsD {
   int nFirst, nIndirect, numLights, numMaterials;
   float minContribution, maxContribution;
   float bg[4];
+  int transparentShadows;  // some material lets shadow rays through: shadow rays loop over closest hits
+  int allMaterials;        // some material is not opaque principled: the shading kernel with every material type
 };
 
 // structured-regular volume with its transfer function and macrocell

@@ -313,8 +313,7 @@ B200_D float misH(float p1, float p2) {
   const float p = sqrf(p1) / (sqrf(p1) + sqrf(p2));
   return p1 > 1e17f ? 1.f : p;
 }
-B200_D float maxc(V3 v) { return fmaxf(fmaxf(v.x, v.y), v.z); }
-B200_D float luminance(V3 c) { return 0.212671f * c.x + 0.715160f * c.y + 0.072169f * c.z; }
+B200_D float luminance(V3 c) { return luminanceV(c); }
 
 }  // namespace
 }  // namespace b200

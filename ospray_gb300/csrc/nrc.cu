@@ -8,6 +8,7 @@
 
 #include "api_internal.h"
 #include "nrc.cuh"
+#include "tcgen05.cuh"
 
 namespace b200 {
 namespace nrc {
@@ -20,183 +21,14 @@ struct Params {
 };
 
 constexpr int LAYER_OUT_OFF = HIDDEN * WIDTH * WIDTH;  // offset of the output layer (64 x 16)
-constexpr int W_ROWS = NUM_W / WIDTH;                 // rows of 64 in the [out][in] weights
-constexpr int WARPS = 4;                              // warps per block of the fused kernels
-constexpr int XS = WIDTH;                             // row stride of the training kernel's activation tiles
-// The inference kernel pads its shared-memory rows (weights and the input
-// tile) to 72 BF16 (144 B): rows 64 wide (128 B) put the 8 rows an m16n8k16
-// fragment load reads into one bank (8-way conflicts); 144-byte rows shift
-// each row by 4 banks.
-constexpr int XI = WIDTH + 8;                         // inference: row stride of weights and input tile
 
 namespace {
-
-// ---------------------------------------------------------------- encoding
-// One warp encodes its 16 samples: lanes 0-15 the hash grid of sample `lane`,
-// lanes 16-31 the other inputs of sample `lane - 16`.
-B200_D void encodeTile(const Params &P, const float *rec, bool valid, __nv_bfloat16 *X, int ldx, int lane) {
-  const int s = lane & 15;
-  const float *r = rec + s * REC;
-  __nv_bfloat16 *row = X + s * ldx;
-  if (lane < 16) {
-    for (int l = 0; l < LEVELS; l++) {
-      float f0 = 0.f, f1 = 0.f;
-      if (valid) {
-        const Cell c = gridCell(P.grid, l, r);
-        const __half2 *T = P.table + size_t(l) * TSIZE;
-        for (int k = 0; k < 8; k++) {
-          const uint32_t dx = k & 1, dy = (k >> 1) & 1, dz = k >> 2;
-          const float w = (dx ? c.fx : 1.f - c.fx) * (dy ? c.fy : 1.f - c.fy) * (dz ? c.fz : 1.f - c.fz);
-          const float2 v = __half22float2(T[gridIndex(P.grid, l, c.x + dx, c.y + dy, c.z + dz)]);
-          f0 += w * v.x;
-          f1 += w * v.y;
-        }
-      }
-      *reinterpret_cast<uint32_t *>(row + 2 * l) = packBF16(f0, f1);
-    }
-  } else {
-    float o[32];
-    for (int k = 0; k < 32; k++) o[k] = 0.f;
-    if (valid) {
-      shEncode(r[3], r[4], r[5], o);
-      o[COL_N - COL_SH + 0] = r[6];
-      o[COL_N - COL_SH + 1] = r[7];
-      o[COL_N - COL_SH + 2] = r[8];
-      o[COL_R - COL_SH] = r[9];
-      o[COL_A - COL_SH + 0] = r[10];
-      o[COL_A - COL_SH + 1] = r[11];
-      o[COL_A - COL_SH + 2] = r[12];
-      o[COL_ONE - COL_SH] = 1.f;
-    }
-    for (int k = 0; k < 32; k += 2) *reinterpret_cast<uint32_t *>(row + COL_SH + k) = packBF16(o[k], o[k + 1]);
-  }
-}
-
-// ---------------------------------------------------------------- forward
-// Runs the hidden layers on the A operand a[4][4] (replaced by the last
-// hidden activation); with `store`, writes every hidden activation H_1..H_4
-// (BF16, after ReLU) to H + (l * 16 * XS).  LDW: the row stride of wt.
-template <int LDW>
-B200_D void hiddenLayers(const Params &P, const __nv_bfloat16 *wt, uint32_t a[4][4], __nv_bfloat16 *H, bool store,
-                         int lane) {
-  const int g = lane >> 2, t = lane & 3;
-  for (int l = 0; l < HIDDEN; l++) {
-    float c[8][4];
-    for (int j = 0; j < 8; j++) {
-      c[j][0] = c[j][1] = c[j][2] = c[j][3] = 0.f;
-      for (int kk = 0; kk < 4; kk++) {
-        uint32_t b0, b1;
-        loadBT(wt + l * WIDTH * LDW, LDW, kk, j, lane, b0, b1);
-        mma16816(c[j], a[kk], b0, b1);
-      }
-    }
-    for (int kk = 0; kk < 4; kk++) {
-      a[kk][0] = packBF16(fmaxf(c[2 * kk][0], 0.f), fmaxf(c[2 * kk][1], 0.f));
-      a[kk][1] = packBF16(fmaxf(c[2 * kk][2], 0.f), fmaxf(c[2 * kk][3], 0.f));
-      a[kk][2] = packBF16(fmaxf(c[2 * kk + 1][0], 0.f), fmaxf(c[2 * kk + 1][1], 0.f));
-      a[kk][3] = packBF16(fmaxf(c[2 * kk + 1][2], 0.f), fmaxf(c[2 * kk + 1][3], 0.f));
-      if (store) {
-        __nv_bfloat16 *Hl = H + l * 16 * XS;
-        *reinterpret_cast<uint32_t *>(Hl + g * XS + 16 * kk + 2 * t) = a[kk][0];
-        *reinterpret_cast<uint32_t *>(Hl + (g + 8) * XS + 16 * kk + 2 * t) = a[kk][1];
-        *reinterpret_cast<uint32_t *>(Hl + g * XS + 16 * kk + 8 + 2 * t) = a[kk][2];
-        *reinterpret_cast<uint32_t *>(Hl + (g + 8) * XS + 16 * kk + 8 + 2 * t) = a[kk][3];
-      }
-    }
-  }
-}
-
-// output layer: o[j] accumulators of n-tile j (columns 8j..8j+7; 0..2 used)
-template <int LDW>
-B200_D void outputLayer(const __nv_bfloat16 *wt, const uint32_t a[4][4], float o[2][4], int lane) {
-  for (int j = 0; j < 2; j++) {
-    o[j][0] = o[j][1] = o[j][2] = o[j][3] = 0.f;
-    for (int kk = 0; kk < 4; kk++) {
-      uint32_t b0, b1;
-      loadBT(wt + HIDDEN * WIDTH * LDW, LDW, kk, j, lane, b0, b1);
-      mma16816(o[j], a[kk], b0, b1);
-    }
-  }
-}
 
 // n = min(*dn, nmax) when dn is given (a count produced on the device)
 B200_D long long deviceCount(long long nmax, const uint32_t *dn, long long offset) {
   if (!dn) return nmax;
   const long long c = (long long)*(volatile const uint32_t *)dn - offset;
   return c < 0 ? 0 : (c < nmax ? c : nmax);
-}
-
-__global__ void __launch_bounds__(WARPS * 32) k_nrc_infer(Params P, const float *__restrict__ q, long long nmax,
-                                                          const uint32_t *dn, float *__restrict__ out) {
-  const long long n = deviceCount(nmax, dn, 0);
-  extern __shared__ __align__(16) unsigned char smem[];
-  __nv_bfloat16 *wt = reinterpret_cast<__nv_bfloat16 *>(smem);
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  float *rec = reinterpret_cast<float *>(smem + W_ROWS * XI * 2) + warp * 16 * REC;
-  __nv_bfloat16 *X = reinterpret_cast<__nv_bfloat16 *>(smem + W_ROWS * XI * 2 + WARPS * 16 * REC * 4) + warp * 16 * XI;
-  // the [out][in] weights, rows of 64 padded to XI
-  for (int i = threadIdx.x; i < NUM_W / 2; i += blockDim.x) {
-    const int row = (2 * i) / WIDTH, col = (2 * i) % WIDTH;
-    reinterpret_cast<uint32_t *>(wt)[(row * XI + col) / 2] = reinterpret_cast<const uint32_t *>(P.wt)[i];
-  }
-  __syncthreads();
-  const long long tiles = (n + 15) / 16;
-  for (long long tile = blockIdx.x * (long long)WARPS + warp; tile < tiles; tile += (long long)gridDim.x * WARPS) {
-    const long long base = tile * 16;
-    for (int k = lane; k < 16 * REC; k += 32) {
-      const long long i = base + k / REC;
-      rec[k] = i < n ? q[i * REC + k % REC] : 0.f;
-    }
-    __syncwarp();
-    encodeTile(P, rec, base + (lane & 15) < n, X, XI, lane);
-    __syncwarp();
-    uint32_t a[4][4];
-    for (int kk = 0; kk < 4; kk++) loadA(X, XI, kk, lane, a[kk]);
-    hiddenLayers<XI>(P, wt, a, nullptr, false, lane);
-    float o[2][4];
-    outputLayer<XI>(wt, a, o, lane);
-    const int g = lane >> 2, t = lane & 3;
-    for (int h = 0; h < 2; h++) {
-      const long long i = base + g + 8 * h;
-      if (i >= n) continue;
-      for (int e = 0; e < 2; e++) {
-        const int col = 2 * t + e;
-        if (col < 3) out[i * 3 + col] = o[0][2 * h + e];
-      }
-    }
-    __syncwarp();
-  }
-}
-
-// ---------------------------------------------------------------- backward
-B200_D uint32_t pack2(const __nv_bfloat16 *p0, const __nv_bfloat16 *p1) {
-  return uint32_t(*reinterpret_cast<const uint16_t *>(p0)) | (uint32_t(*reinterpret_cast<const uint16_t *>(p1)) << 16);
-}
-
-// dW[in][out] += Act^T x dZ over the tile's 16 samples (K = samples):
-// Act 16 x 64, dZ 16 x (8 * ntiles) with row stride ldz; dW row stride ldz
-B200_D void weightGrad(const __nv_bfloat16 *Act, const __nv_bfloat16 *dZ, int ntiles, int ldz, float *dW, int lane) {
-  const int g = lane >> 2, t = lane & 3;
-  for (int mi = 0; mi < 4; mi++) {
-    uint32_t a[4];
-    const int m0 = 16 * mi + g;
-    a[0] = pack2(Act + (2 * t) * XS + m0, Act + (2 * t + 1) * XS + m0);
-    a[1] = pack2(Act + (2 * t) * XS + m0 + 8, Act + (2 * t + 1) * XS + m0 + 8);
-    a[2] = pack2(Act + (2 * t + 8) * XS + m0, Act + (2 * t + 9) * XS + m0);
-    a[3] = pack2(Act + (2 * t + 8) * XS + m0 + 8, Act + (2 * t + 9) * XS + m0 + 8);
-    for (int j = 0; j < ntiles; j++) {
-      const int n0 = 8 * j + g;
-      const uint32_t b0 = pack2(dZ + (2 * t) * ldz + n0, dZ + (2 * t + 1) * ldz + n0);
-      const uint32_t b1 = pack2(dZ + (2 * t + 8) * ldz + n0, dZ + (2 * t + 9) * ldz + n0);
-      float c[4] = {0.f, 0.f, 0.f, 0.f};
-      mma16816(c, a, b0, b1);
-      const int col = 8 * j + 2 * t;
-      atomicAdd(dW + m0 * ldz + col, c[0]);
-      atomicAdd(dW + m0 * ldz + col + 1, c[1]);
-      atomicAdd(dW + (m0 + 8) * ldz + col, c[2]);
-      atomicAdd(dW + (m0 + 8) * ldz + col + 1, c[3]);
-    }
-  }
 }
 
 // the table gradient of one sample and level: d(features) spread over the cell
@@ -212,134 +44,362 @@ B200_D void scatterGrid(const Params &P, const float *r, int level, float d0, fl
   }
 }
 
-// Forward + backward of the relative L2 loss (Mueller et al. 2021):
-//   L = 1/(3N) sum_s sum_c (o - y)^2 / (sg(o)^2 + 0.01)
-// Gradients are summed into wgrad (17,408) and tgrad (table, FP32); the loss
-// sum into *loss.
-__global__ void __launch_bounds__(WARPS * 32) k_nrc_train(Params P, const float *__restrict__ samples, long long nmax,
-                                                          const uint32_t *dn, long long offset, float *wgrad,
-                                                          float *tgrad, float *loss) {
+// ---------------------------------------------------------------- tensor-core check
+// One 128 x N x 64 BF16 GEMM through the tcgen05 path (operands staged in the
+// K-major shared-memory layout, accumulator in TMEM, read back by the four
+// warps' lane quadrants): the building block of the MLP kernels, checkable
+// against a host matrix product.
+__global__ void __launch_bounds__(128) k_tc_check(const float *A, const float *B, int N, float *D, uint32_t *status) {
+  __shared__ __align__(128) unsigned char sA[128 * 64 * 2];
+  __shared__ __align__(128) unsigned char sB[64 * 64 * 2];
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ uint32_t tmemBase;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  for (int i = tid; i < 128 * 64; i += 128)
+    *reinterpret_cast<__nv_bfloat16 *>(sA + tc::kmajorOffset(i / 64, i % 64, 64)) = __float2bfloat16_rn(A[i]);
+  for (int i = tid; i < N * 64; i += 128)
+    *reinterpret_cast<__nv_bfloat16 *>(sB + tc::kmajorOffset(i / 64, i % 64, 64)) = __float2bfloat16_rn(B[i]);
+  if (warp == 0) tc::tmemAlloc(&tmemBase, 64);
+  if (tid == 0) tc::mbarInit(&bar, 1);
+  tc::fenceProxyAsync();
+  tc::fenceBeforeSync();
+  __syncthreads();
+  tc::fenceAfterSync();
+  const uint32_t tmem = tmemBase;
+  if (tid == 0) {
+    tc::gemmIssue(tmem, tc::smemAddr(sA), 64, tc::smemAddr(sB), 64, 64, tc::idescBF16(128, N));
+    tc::commit(&bar);
+  }
+  const bool ok = __syncthreads_and(tc::mbarWait(&bar, 0)) != 0;
+  tc::fenceAfterSync();
+  if (ok) {
+    for (int c0 = 0; c0 < N; c0 += 16) {
+      float v[16];
+      tc::tmemLoad16(tmem + (uint32_t(warp * 32) << 16) + uint32_t(c0), v);
+      for (int k = 0; k < 16; k++) D[size_t(tid) * N + c0 + k] = v[k];
+    }
+  } else if (tid == 0) {
+    atomicOr(status, 1u);
+  }
+  tc::fenceBeforeSync();
+  __syncthreads();
+  if (warp == 0) tc::tmemDealloc(tmem, 64);
+}
+
+// ---------------------------------------------------------------- tcgen05 kernels
+// The same model on the 5th-generation tensor cores.  A CTA of 128 threads
+// (4 warps) owns tiles of 128 samples: thread t encodes sample t into row t
+// of the BF16 input tile in shared memory (K-major no-swizzle layout, see
+// tcgen05.cuh); one thread issues each layer's GEMM (128 x N x 64 as four
+// K = 16 tcgen05.mma) with the FP32 accumulator in tensor memory; every
+// thread reads its row back with tcgen05.ld (warp w owns TMEM lanes
+// 32w..32w+31 = rows of its threads), applies the ReLU and writes the next
+// layer's BF16 input row.  Training also runs the backward data path
+// (dA_l = dZ_l W_l^T) on the tensor cores; the weight gradients
+// dW_l = A_l^T dZ_l (K = the 128 samples) are reduced per warp with
+// mma.sync and added to the global gradient once per tile.
+constexpr int TC_M = 128;                          // samples per tile
+constexpr uint32_t TC_LAYER_BYTES = 64 * 64 * 2;   // one 64 x 64 BF16 operand
+constexpr uint32_t TC_OUT_BYTES = OUT_PAD * 64 * 2;
+constexpr uint32_t TC_TILE_BYTES = TC_M * 64 * 2;  // 128 x 64 activation tile
+constexpr uint32_t TC_W_BYTES = HIDDEN * TC_LAYER_BYTES + TC_OUT_BYTES;
+constexpr uint32_t TC_TMEM_COLS = 64;
+
+// stages the weights as tcgen05 B operands (N x K K-major): `wt` [out][in] as
+// forward operands (N = out, K = in), `w` [in][out] as backward ones (N = in,
+// K = out; the output layer's K is 16)
+B200_D void stageWeights(const Params &P, unsigned char *sWt, unsigned char *sW) {
+  for (int i = threadIdx.x; i < NUM_W; i += blockDim.x) {
+    const int l = i / (WIDTH * WIDTH), r = i % (WIDTH * WIDTH);
+    if (l < HIDDEN) {
+      const int o = r / WIDTH, in = r % WIDTH;  // wt: [out][in]
+      *reinterpret_cast<__nv_bfloat16 *>(sWt + l * TC_LAYER_BYTES + tc::kmajorOffset(o, in, 64)) = P.wt[i];
+      if (sW) {  // w: [in][out] -> operand rows = in, K = out
+        const int in2 = r / WIDTH, o2 = r % WIDTH;
+        *reinterpret_cast<__nv_bfloat16 *>(sW + l * TC_LAYER_BYTES + tc::kmajorOffset(in2, o2, 64)) = P.w[i];
+      }
+    } else {
+      const int j = i - LAYER_OUT_OFF;
+      const int o = j / WIDTH, in = j % WIDTH;  // wt output layer: [16 out][64 in]
+      *reinterpret_cast<__nv_bfloat16 *>(sWt + HIDDEN * TC_LAYER_BYTES + tc::kmajorOffset(o, in, 64)) = P.wt[i];
+      if (sW) {  // w output layer: [64 in][16 out] -> rows = in, K = 16
+        const int in2 = j / OUT_PAD, o2 = j % OUT_PAD;
+        *reinterpret_cast<__nv_bfloat16 *>(sW + HIDDEN * TC_LAYER_BYTES + tc::kmajorOffset(in2, o2, OUT_PAD)) =
+            P.w[i];
+      }
+    }
+  }
+}
+
+// the 64 encoded inputs of one sample (record r), FP32
+B200_D void encodeRow(const Params &P, const float *r, float *x) {
+  for (int l = 0; l < LEVELS; l++) {
+    const Cell c = gridCell(P.grid, l, r);
+    const __half2 *T = P.table + size_t(l) * TSIZE;
+    float f0 = 0.f, f1 = 0.f;
+    for (int k = 0; k < 8; k++) {
+      const uint32_t dx = k & 1, dy = (k >> 1) & 1, dz = k >> 2;
+      const float w = (dx ? c.fx : 1.f - c.fx) * (dy ? c.fy : 1.f - c.fy) * (dz ? c.fz : 1.f - c.fz);
+      const float2 v = __half22float2(T[gridIndex(P.grid, l, c.x + dx, c.y + dy, c.z + dz)]);
+      f0 += w * v.x;
+      f1 += w * v.y;
+    }
+    x[2 * l] = f0;
+    x[2 * l + 1] = f1;
+  }
+  shEncode(r[3], r[4], r[5], x + COL_SH);
+  for (int k = COL_N; k < WIDTH; k++) x[k] = 0.f;
+  x[COL_N + 0] = r[6];
+  x[COL_N + 1] = r[7];
+  x[COL_N + 2] = r[8];
+  x[COL_R] = r[9];
+  x[COL_A + 0] = r[10];
+  x[COL_A + 1] = r[11];
+  x[COL_A + 2] = r[12];
+  x[COL_ONE] = 1.f;
+}
+
+// row `row` of a K-wide BF16 operand tile from FP32 values (optionally ReLU'd)
+template <int K>
+B200_D void storeRow(unsigned char *tile, int row, const float *v, bool relu) {
+#pragma unroll
+  for (int c = 0; c < K; c += 8) {
+    uint4 q;
+    uint32_t *w = reinterpret_cast<uint32_t *>(&q);
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+      float a = v[c + 2 * e], b = v[c + 2 * e + 1];
+      if (relu) {
+        a = fmaxf(a, 0.f);
+        b = fmaxf(b, 0.f);
+      }
+      w[e] = packBF16(a, b);
+    }
+    *reinterpret_cast<uint4 *>(tile + tc::kmajorOffset(row, c, K)) = q;
+  }
+}
+
+// this thread's accumulator row: `n` FP32 columns from column c0
+B200_D void loadRow(uint32_t tmem, int warp, int c0, int n, float *v) {
+  for (int c = 0; c < n; c += 16) tc::tmemLoad16(tmem + (uint32_t(warp * 32) << 16) + uint32_t(c0 + c), v + c);
+}
+
+// one GEMM on the tensor cores: thread 0 issues, everyone waits (the
+// operands written by the threads are made visible to the async proxy first).
+// false if the MMA did not complete in time (reported via *status).
+B200_D bool tcGemm(uint32_t tmem, const unsigned char *a, int aK, const unsigned char *b, int bK, int K, int N,
+                   uint64_t *bar, uint32_t &phase, uint32_t *status) {
+  tc::fenceProxyAsync();
+  tc::fenceBeforeSync();
+  __syncthreads();
+  tc::fenceAfterSync();
+  if (threadIdx.x == 0) {
+    tc::gemmIssue(tmem, tc::smemAddr(a), aK, tc::smemAddr(b), bK, K, tc::idescBF16(TC_M, N));
+    tc::commit(bar);
+  }
+  const bool ok = __syncthreads_and(tc::mbarWait(bar, phase)) != 0;
+  phase ^= 1u;
+  tc::fenceAfterSync();
+  if (!ok && threadIdx.x == 0) atomicOr(status, 1u);
+  return ok;
+}
+
+__global__ void __launch_bounds__(TC_M) k_nrc_infer_tc(Params P, const float *__restrict__ q, long long nmax,
+                                                       const uint32_t *dn, float *__restrict__ out, uint32_t *status) {
+  const long long n = deviceCount(nmax, dn, 0);
+  extern __shared__ __align__(128) unsigned char smem[];
+  unsigned char *sWt = smem;                 // forward B operands
+  unsigned char *sX = smem + TC_W_BYTES;     // the activation tile
+  uint64_t *bar = reinterpret_cast<uint64_t *>(sX + TC_TILE_BYTES);
+  uint32_t *tmemSlot = reinterpret_cast<uint32_t *>(bar + 1);
+  const int tid = threadIdx.x, warp = tid >> 5;
+  stageWeights(P, sWt, nullptr);
+  if (warp == 0) tc::tmemAlloc(tmemSlot, TC_TMEM_COLS);
+  if (tid == 0) tc::mbarInit(bar, 1);
+  tc::fenceBeforeSync();
+  __syncthreads();
+  tc::fenceAfterSync();
+  const uint32_t tmem = *tmemSlot;
+  uint32_t phase = 0;
+  const long long tiles = (n + TC_M - 1) / TC_M;
+  bool ok = true;
+  for (long long tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x) {
+    const long long i = tile * TC_M + tid;
+    float x[WIDTH];
+    if (i < n) {
+      float r[REC];
+      for (int k = 0; k < REC; k += 4) *reinterpret_cast<float4 *>(r + k) = *reinterpret_cast<const float4 *>(q + i * REC + k);
+      encodeRow(P, r, x);
+    } else {
+      for (int k = 0; k < WIDTH; k++) x[k] = 0.f;
+    }
+    storeRow<WIDTH>(sX, tid, x, false);
+    for (int l = 0; l < HIDDEN && ok; l++) {
+      ok = tcGemm(tmem, sX, WIDTH, sWt + l * TC_LAYER_BYTES, WIDTH, WIDTH, WIDTH, bar, phase, status);
+      if (!ok) break;
+      loadRow(tmem, warp, 0, WIDTH, x);
+      tc::fenceBeforeSync();
+      storeRow<WIDTH>(sX, tid, x, true);  // the MMA that read sX has completed
+    }
+    if (!ok) break;
+    ok = tcGemm(tmem, sX, WIDTH, sWt + HIDDEN * TC_LAYER_BYTES, WIDTH, WIDTH, OUT_PAD, bar, phase, status);
+    if (!ok) break;
+    float o[16];
+    loadRow(tmem, warp, 0, 16, o);
+    tc::fenceBeforeSync();
+    if (i < n)
+      for (int c = 0; c < 3; c++) out[i * 3 + c] = o[c];
+  }
+  tc::fenceBeforeSync();
+  __syncthreads();
+  if (warp == 0) tc::tmemDealloc(tmem, TC_TMEM_COLS);
+}
+
+// mma.sync fragment reads from K-major tiles: A[m][k] = Act[sample k][feature m]
+// (two samples per register), B[k][n] = G[sample k][column n]
+B200_D uint32_t tilePair(const unsigned char *tile, int K, int s0, int c) {
+  const uint16_t lo = *reinterpret_cast<const uint16_t *>(tile + tc::kmajorOffset(s0, c, K));
+  const uint16_t hi = *reinterpret_cast<const uint16_t *>(tile + tc::kmajorOffset(s0 + 1, c, K));
+  return uint32_t(lo) | (uint32_t(hi) << 16);
+}
+
+// dW[in][out] += Act^T G over the tile's 128 samples; warp w owns the input
+// rows 16w..16w+15 and all `nOut` output columns; one global add per weight
+template <int NOUT>
+B200_D void weightGradTile(const unsigned char *act, const unsigned char *G, float *dW, int warp, int lane) {
+  const int g = lane >> 2, t = lane & 3;
+  float c[NOUT / 8][4];
+#pragma unroll
+  for (int j = 0; j < NOUT / 8; j++) c[j][0] = c[j][1] = c[j][2] = c[j][3] = 0.f;
+  const int m0 = 16 * warp + g;
+  for (int kk = 0; kk < TC_M / 16; kk++) {
+    const int s = 16 * kk + 2 * t;
+    uint32_t a[4];
+    a[0] = tilePair(act, WIDTH, s, m0);
+    a[1] = tilePair(act, WIDTH, s, m0 + 8);
+    a[2] = tilePair(act, WIDTH, s + 8, m0);
+    a[3] = tilePair(act, WIDTH, s + 8, m0 + 8);
+#pragma unroll
+    for (int j = 0; j < NOUT / 8; j++) {
+      const uint32_t b0 = tilePair(G, NOUT, s, 8 * j + g), b1 = tilePair(G, NOUT, s + 8, 8 * j + g);
+      mma16816(c[j], a, b0, b1);
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < NOUT / 8; j++) {
+    const int col = 8 * j + 2 * t;
+    atomicAdd(dW + m0 * NOUT + col, c[j][0]);
+    atomicAdd(dW + m0 * NOUT + col + 1, c[j][1]);
+    atomicAdd(dW + (m0 + 8) * NOUT + col, c[j][2]);
+    atomicAdd(dW + (m0 + 8) * NOUT + col + 1, c[j][3]);
+  }
+}
+
+__global__ void __launch_bounds__(TC_M) k_nrc_train_tc(Params P, const float *__restrict__ samples, long long nmax,
+                                                       const uint32_t *dn, long long offset, float *wgrad,
+                                                       float *tgrad, float *loss, uint32_t *status) {
   const long long n = deviceCount(nmax, dn, offset);
   const float invN3 = n > 0 ? 1.f / (3.f * float(n)) : 0.f;
-  extern __shared__ __align__(16) unsigned char smem[];
-  __nv_bfloat16 *w = reinterpret_cast<__nv_bfloat16 *>(smem);
-  __nv_bfloat16 *wt = w + NUM_W;
-  float *dWs = reinterpret_cast<float *>(wt + NUM_W);
-  unsigned char *per = reinterpret_cast<unsigned char *>(dWs + NUM_W);
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  // per warp: records (16 x 16 floats), X + H1..H4 (5 x 16 x 64), dZ (16 x 64), dOut (16 x 16)
-  constexpr int PER_WARP = 16 * REC * 4 + 5 * 16 * XS * 2 + 16 * XS * 2 + 16 * 16 * 2;
-  float *rec = reinterpret_cast<float *>(per + warp * PER_WARP);
-  __nv_bfloat16 *X = reinterpret_cast<__nv_bfloat16 *>(rec + 16 * REC);
-  __nv_bfloat16 *H = X + 16 * XS;  // H1..H4
-  __nv_bfloat16 *dZ = H + 4 * 16 * XS;
-  __nv_bfloat16 *dO = dZ + 16 * XS;
-  for (int i = threadIdx.x; i < NUM_W / 2; i += blockDim.x) {
-    reinterpret_cast<uint32_t *>(w)[i] = reinterpret_cast<const uint32_t *>(P.w)[i];
-    reinterpret_cast<uint32_t *>(wt)[i] = reinterpret_cast<const uint32_t *>(P.wt)[i];
-  }
-  for (int i = threadIdx.x; i < NUM_W; i += blockDim.x) dWs[i] = 0.f;
+  extern __shared__ __align__(128) unsigned char smem[];
+  unsigned char *sWt = smem;                        // forward B operands
+  unsigned char *sW = sWt + TC_W_BYTES;             // backward B operands
+  unsigned char *sA = sW + TC_W_BYTES;              // X, H1..H4 (5 tiles)
+  unsigned char *sZ = sA + 5 * TC_TILE_BYTES;       // dZ tile
+  unsigned char *sO = sZ + TC_TILE_BYTES;           // dOut tile (128 x 16)
+  uint64_t *bar = reinterpret_cast<uint64_t *>(sO + TC_M * OUT_PAD * 2);
+  uint32_t *tmemSlot = reinterpret_cast<uint32_t *>(bar + 1);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  stageWeights(P, sWt, sW);
+  if (warp == 0) tc::tmemAlloc(tmemSlot, TC_TMEM_COLS);
+  if (tid == 0) tc::mbarInit(bar, 1);
+  tc::fenceBeforeSync();
   __syncthreads();
-  const int g = lane >> 2, t = lane & 3;
+  tc::fenceAfterSync();
+  const uint32_t tmem = *tmemSlot;
+  uint32_t phase = 0;
   float lossSum = 0.f;
-  const long long tiles = (n + 15) / 16;
-  for (long long tile = blockIdx.x * (long long)WARPS + warp; tile < tiles; tile += (long long)gridDim.x * WARPS) {
-    const long long base = tile * 16;
-    for (int k = lane; k < 16 * REC; k += 32) {
-      const long long i = base + k / REC;
-      rec[k] = i < n ? samples[i * REC + k % REC] : 0.f;
+  const long long tiles = (n + TC_M - 1) / TC_M;
+  bool ok = true;
+  for (long long tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x) {
+    const long long i = tile * TC_M + tid;
+    const bool valid = i < n;
+    float r[REC];
+    float v[WIDTH];
+    if (valid) {
+      for (int k = 0; k < REC; k += 4)
+        *reinterpret_cast<float4 *>(r + k) = *reinterpret_cast<const float4 *>(samples + (offset + i) * REC + k);
+      encodeRow(P, r, v);
+    } else {
+      for (int k = 0; k < REC; k++) r[k] = 0.f;
+      for (int k = 0; k < WIDTH; k++) v[k] = 0.f;
     }
-    __syncwarp();
-    encodeTile(P, rec, base + (lane & 15) < n, X, XS, lane);
-    __syncwarp();
-    uint32_t a[4][4];
-    for (int kk = 0; kk < 4; kk++) loadA(X, XS, kk, lane, a[kk]);
-    hiddenLayers<WIDTH>(P, wt, a, H, true, lane);
-    float o[2][4];
-    outputLayer<WIDTH>(wt, a, o, lane);
-    // loss gradient (columns 0..2 of n-tile 0), staged as dOut 16 x 16
-    float d[4];
-    for (int q = 0; q < 4; q++) {
-      const int row = g + 8 * (q >> 1), col = 2 * t + (q & 1);
-      d[q] = 0.f;
-      if (col < 3 && base + row < n) {
-        const float y = rec[row * REC + 13 + col], ov = o[0][q];
+    __syncthreads();  // the previous tile's readers of the tiles are done
+    storeRow<WIDTH>(sA, tid, v, false);
+    // forward: H_{l+1} = ReLU(A_l W_l)
+    for (int l = 0; l < HIDDEN && ok; l++) {
+      ok = tcGemm(tmem, sA + l * TC_TILE_BYTES, WIDTH, sWt + l * TC_LAYER_BYTES, WIDTH, WIDTH, WIDTH, bar, phase,
+                  status);
+      if (!ok) break;
+      loadRow(tmem, warp, 0, WIDTH, v);
+      tc::fenceBeforeSync();
+      storeRow<WIDTH>(sA + (l + 1) * TC_TILE_BYTES, tid, v, true);
+    }
+    if (!ok) break;
+    ok = tcGemm(tmem, sA + HIDDEN * TC_TILE_BYTES, WIDTH, sWt + HIDDEN * TC_LAYER_BYTES, WIDTH, WIDTH, OUT_PAD, bar,
+                phase, status);
+    if (!ok) break;
+    // relative L2 loss and its gradient (columns 0..2), staged as dOut
+    float o[16], d[16];
+    loadRow(tmem, warp, 0, 16, o);
+    tc::fenceBeforeSync();
+    for (int c = 0; c < 16; c++) d[c] = 0.f;
+    if (valid)
+      for (int c = 0; c < 3; c++) {
+        const float y = r[13 + c], ov = o[c];
         const float den = ov * ov + 0.01f;
         const float diff = ov - y;
         lossSum += diff * diff / den;
-        d[q] = 2.f * diff / den * invN3;
+        d[c] = 2.f * diff / den * invN3;
       }
+    storeRow<OUT_PAD>(sO, tid, d, false);
+    // dH4 = dOut W_out^T (K = 16) on the tensor cores; dW_out by the warps
+    ok = tcGemm(tmem, sO, OUT_PAD, sW + HIDDEN * TC_LAYER_BYTES, OUT_PAD, OUT_PAD, WIDTH, bar, phase, status);
+    if (!ok) break;
+    weightGradTile<OUT_PAD>(sA + HIDDEN * TC_TILE_BYTES, sO, wgrad + LAYER_OUT_OFF, warp, lane);
+    for (int l = HIDDEN - 1; l >= 0 && ok; l--) {
+      // dZ_l = dH_{l+1} through the ReLU of H_{l+1}
+      loadRow(tmem, warp, 0, WIDTH, v);
+      tc::fenceBeforeSync();
+      const unsigned char *H = sA + (l + 1) * TC_TILE_BYTES;
+      for (int c = 0; c < WIDTH; c++)
+        if (!(__bfloat162float(*reinterpret_cast<const __nv_bfloat16 *>(H + tc::kmajorOffset(tid, c, WIDTH))) > 0.f))
+          v[c] = 0.f;
+      __syncthreads();  // every warp's reads of the previous dZ are done
+      storeRow<WIDTH>(sZ, tid, v, false);
+      // dA_l = dZ_l W_l^T on the tensor cores; dW_l = A_l^T dZ_l by the warps
+      ok = tcGemm(tmem, sZ, WIDTH, sW + l * TC_LAYER_BYTES, WIDTH, WIDTH, WIDTH, bar, phase, status);
+      if (!ok) break;
+      weightGradTile<WIDTH>(sA + l * TC_TILE_BYTES, sZ, wgrad + l * WIDTH * WIDTH, warp, lane);
     }
-    *reinterpret_cast<uint32_t *>(dO + g * 16 + 2 * t) = packBF16(d[0], d[1]);
-    *reinterpret_cast<uint32_t *>(dO + (g + 8) * 16 + 2 * t) = packBF16(d[2], d[3]);
-    *reinterpret_cast<uint32_t *>(dO + g * 16 + 8 + 2 * t) = 0u;
-    *reinterpret_cast<uint32_t *>(dO + (g + 8) * 16 + 8 + 2 * t) = 0u;
-    __syncwarp();
-    // output layer: dW4 += H4^T dOut, dH4 = dOut W4^T
-    weightGrad(H + 3 * 16 * XS, dO, 2, OUT_PAD, dWs + LAYER_OUT_OFF, lane);
-    uint32_t ad[4];
-    ad[0] = packBF16(d[0], d[1]);
-    ad[1] = packBF16(d[2], d[3]);
-    ad[2] = 0u;
-    ad[3] = 0u;
-    float c[8][4];
-    for (int j = 0; j < 8; j++) {
-      c[j][0] = c[j][1] = c[j][2] = c[j][3] = 0.f;
-      uint32_t b0, b1;
-      loadBT(w + LAYER_OUT_OFF, OUT_PAD, 0, j, lane, b0, b1);
-      mma16816(c[j], ad, b0, b1);
-    }
-    for (int l = HIDDEN - 1; l >= 0; l--) {
-      // c = dH_{l+1}; through the ReLU into dZ_l (stored and as the A operand)
-      const __nv_bfloat16 *Hl = H + l * 16 * XS;  // H_{l+1}
-      uint32_t az[4][4];
-      for (int j = 0; j < 8; j++) {
-        const int col = 8 * j + 2 * t;
-        const __nv_bfloat16 *h0 = Hl + g * XS + col, *h1 = Hl + (g + 8) * XS + col;
-        const float v0 = __bfloat162float(h0[0]) > 0.f ? c[j][0] : 0.f;
-        const float v1 = __bfloat162float(h0[1]) > 0.f ? c[j][1] : 0.f;
-        const float v2 = __bfloat162float(h1[0]) > 0.f ? c[j][2] : 0.f;
-        const float v3 = __bfloat162float(h1[1]) > 0.f ? c[j][3] : 0.f;
-        const uint32_t p01 = packBF16(v0, v1), p23 = packBF16(v2, v3);
-        *reinterpret_cast<uint32_t *>(dZ + g * XS + col) = p01;
-        *reinterpret_cast<uint32_t *>(dZ + (g + 8) * XS + col) = p23;
-        az[j >> 1][(j & 1) * 2 + 0] = p01;
-        az[j >> 1][(j & 1) * 2 + 1] = p23;
-      }
-      __syncwarp();
-      const __nv_bfloat16 *Al = l == 0 ? X : H + (l - 1) * 16 * XS;
-      weightGrad(Al, dZ, 8, WIDTH, dWs + l * WIDTH * WIDTH, lane);
-      // dA_l = dZ_l W_l^T
-      for (int j = 0; j < 8; j++) {
-        c[j][0] = c[j][1] = c[j][2] = c[j][3] = 0.f;
-        for (int kk = 0; kk < 4; kk++) {
-          uint32_t b0, b1;
-          loadBT(w + l * WIDTH * WIDTH, WIDTH, kk, j, lane, b0, b1);
-          mma16816(c[j], az[kk], b0, b1);
-        }
-      }
-      __syncwarp();
-    }
-    // c = dX: the hash-grid columns 0..31 (n-tiles 0..3): level 4j + t
-    for (int j = 0; j < 4; j++)
-      for (int h = 0; h < 2; h++) {
-        const int row = g + 8 * h;
-        if (base + row < n) scatterGrid(P, rec + row * REC, 4 * j + t, c[j][2 * h], c[j][2 * h + 1], tgrad);
-      }
-    __syncwarp();
+    if (!ok) break;
+    // dX: the hash-grid columns 0..31 -> the table gradient
+    loadRow(tmem, warp, 0, 32, v);
+    tc::fenceBeforeSync();
+    if (valid)
+      for (int lv = 0; lv < LEVELS; lv++) scatterGrid(P, r, lv, v[2 * lv], v[2 * lv + 1], tgrad);
   }
-  // warp loss sums, then the block's weight gradients into the global sum
   for (int off = 16; off; off >>= 1) lossSum += __shfl_xor_sync(0xffffffffu, lossSum, off);
   if (lane == 0) atomicAdd(loss, lossSum * invN3);
+  tc::fenceBeforeSync();
   __syncthreads();
-  for (int i = threadIdx.x; i < NUM_W; i += blockDim.x)
-    if (dWs[i] != 0.f) atomicAdd(wgrad + i, dWs[i]);
+  if (warp == 0) tc::tmemDealloc(tmem, TC_TMEM_COLS);
 }
 
-constexpr size_t kInferSmem = size_t(W_ROWS) * XI * 2 + WARPS * 16 * REC * 4 + WARPS * 16 * XI * 2;
-constexpr size_t kTrainSmem = size_t(NUM_W) * 2 * 2 + size_t(NUM_W) * 4 +
-                              WARPS * (16 * REC * 4 + 5 * 16 * XS * 2 + 16 * XS * 2 + 16 * 16 * 2);
-static_assert(kTrainSmem <= 227 * 1024, "training kernel shared memory");
+constexpr size_t kInferTcSmem = TC_W_BYTES + TC_TILE_BYTES + 16;
+constexpr size_t kTrainTcSmem = 2 * TC_W_BYTES + 6 * TC_TILE_BYTES + TC_M * OUT_PAD * 2 + 16;
+static_assert(kTrainTcSmem <= 227 * 1024, "tcgen05 training kernel shared memory");
+
+
 
 // ---------------------------------------------------------------- Adam and parameter copies
 // skipped when the step's device-side sample count (dn - offset) is zero
@@ -412,6 +472,7 @@ struct NrcObj {
   __nv_bfloat16 *w = nullptr, *wt = nullptr;
   float *wMaster = nullptr, *wGrad = nullptr, *wM = nullptr, *wV = nullptr;
   float *dLoss = nullptr;
+  uint32_t *dStatus = nullptr;  // bit 0: a tensor-core MMA did not complete in time
   bool attrsSet = false;
 
   NrcObj(DeviceObj *d, const float lo[3], const float hi[3], float learningRate, uint32_t seed) : dev(d) {
@@ -438,7 +499,9 @@ struct NrcObj {
     alloc((void **)&wt, NUM_W * 2);
     for (float **p : {&wMaster, &wGrad, &wM, &wV}) alloc((void **)p, NUM_W * 4);
     alloc((void **)&dLoss, 4);
+    alloc((void **)&dStatus, 4);
     cudaStream_t st = dev->stream;
+    check(cudaMemsetAsync(dStatus, 0, 4, st), "clear");
     check(cudaMemsetAsync(tM, 0, NUM_T * 4, st), "clear");
     check(cudaMemsetAsync(tV, 0, NUM_T * 4, st), "clear");
     check(cudaMemsetAsync(wM, 0, NUM_W * 4, st), "clear");
@@ -451,7 +514,8 @@ struct NrcObj {
     cudaSetDevice(dev->dev);
     cudaStreamSynchronize(dev->stream);
     for (void *p : {(void *)table, (void *)tMaster, (void *)tGrad, (void *)tM, (void *)tV, (void *)w, (void *)wt,
-                    (void *)wMaster, (void *)wGrad, (void *)wM, (void *)wV, (void *)dLoss, (void *)queries,
+                    (void *)wMaster, (void *)wGrad, (void *)wM, (void *)wV, (void *)dLoss, (void *)dStatus,
+                    (void *)queries,
                     (void *)qout, (void *)trainVerts, (void *)samples, (void *)qpath, (void *)fcounters})
       if (p) cudaFree(p);
     dev->release();
@@ -492,9 +556,18 @@ struct NrcObj {
   }
   void setAttrs() {
     if (attrsSet) return;
-    check(cudaFuncSetAttribute(k_nrc_train, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kTrainSmem)), "smem");
-    check(cudaFuncSetAttribute(k_nrc_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kInferSmem)), "smem");
+    check(cudaFuncSetAttribute(k_nrc_train_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kTrainTcSmem)),
+          "smem");
+    check(cudaFuncSetAttribute(k_nrc_infer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kInferTcSmem)),
+          "smem");
     attrsSet = true;
+  }
+  // raises if a kernel of this cache reported an MMA that did not complete
+  // (synchronous; called where the API waits anyway)
+  void checkStatus() {
+    uint32_t h = 0;
+    check(cudaMemcpy(&h, dStatus, 4, cudaMemcpyDeviceToHost), "radiance cache status");
+    if (h) throw Error(B200_UNKNOWN_ERROR, "radiance cache: a tensor-core MMA did not complete");
   }
   // n queries, or min(*dn, n) when dn (a device count) is given
   void infer(const float *q, long long n, float *out, cudaStream_t st, const uint32_t *dn = nullptr) {
@@ -502,9 +575,9 @@ struct NrcObj {
     setAttrs();
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev->dev);
-    const long long tiles = (n + 15) / 16;
-    const long long blocks = std::min<long long>((tiles + WARPS - 1) / WARPS, (long long)sms * 4);
-    k_nrc_infer<<<unsigned(blocks), WARPS * 32, kInferSmem, st>>>(params(), q, n, dn, out);
+    const long long tiles = (n + TC_M - 1) / TC_M;
+    const long long blocks = std::min<long long>(tiles, (long long)sms * 4);
+    k_nrc_infer_tc<<<unsigned(blocks), TC_M, kInferTcSmem, st>>>(params(), q, n, dn, out, dStatus);
     check(cudaGetLastError(), "radiance cache inference");
   }
   // gradients of the loss over n samples into wGrad / tGrad (cleared first)
@@ -516,10 +589,10 @@ struct NrcObj {
     if (n <= 0) return;
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev->dev);
-    const long long tiles = (n + 15) / 16;
-    const long long blocks = std::min<long long>((tiles + WARPS - 1) / WARPS, (long long)sms);
-    k_nrc_train<<<unsigned(blocks), WARPS * 32, kTrainSmem, st>>>(params(), s + offset * REC, n, dn, offset, wGrad,
-                                                                   tGrad, dLoss);
+    const long long tiles = (n + TC_M - 1) / TC_M;
+    const long long blocks = std::min<long long>(tiles, (long long)sms);
+    k_nrc_train_tc<<<unsigned(blocks), TC_M, kTrainTcSmem, st>>>(params(), s, n, dn, offset, wGrad, tGrad, dLoss,
+                                                                   dStatus);
     check(cudaGetLastError(), "radiance cache training");
   }
   // one Adam step on n samples (with dn: on min(*dn - offset, n) samples
@@ -606,10 +679,12 @@ int b200_nrc_gradients(b200_nrc h, const float *samples, int64_t n, float *wgrad
 }
 
 int b200_nrc_get_params(b200_nrc h, float *weights, float *table) {
+  // (also reports a tensor-core MMA that did not complete in an earlier call)
   if (!h) return B200_INVALID_ARGUMENT;
   NrcObj *o = reinterpret_cast<NrcObj *>(h);
   return nrcGuard(o->dev, [&]() {
     check(cudaStreamSynchronize(o->dev->stream), "sync");
+    o->checkStatus();
     if (weights) check(cudaMemcpy(weights, o->wMaster, nrc::NUM_W * 4, cudaMemcpyDeviceToHost), "read weights");
     if (table) check(cudaMemcpy(table, o->tMaster, nrc::NUM_T * 4, cudaMemcpyDeviceToHost), "read table");
   });
@@ -657,7 +732,8 @@ int b200_render_pt_nrc(b200_scene s, const b200_camera_desc *camera, const b200_
       throw Error(B200_INVALID_ARGUMENT, "bad radiance cache frame parameters");
     cudaStream_t st = stream ? (cudaStream_t)stream : sc->dev->stream;
     uploadMaterials(sc, materials, nmaterials);
-    const PtParamsD d = makePtParams(*p, sc->nLights, nmaterials);
+    const PtParamsD d = makePtParams(*p, sc->nLights, nmaterials, sc->transparentMaterials,
+                                     anyNonPrincipled(materials, nmaterials));
     DeviceObj *dev = sc->dev;
     const long long npaths = (long long)fb->W * fb->H * p->pixelSamples;
     ensurePtWorkspace(dev, ptWorkspaceBytes(npaths));
@@ -707,3 +783,45 @@ int b200_nrc_grid(b200_nrc h, float *lo_invext4, float *scales16, uint32_t *dens
 }
 
 }  // extern "C"
+
+extern "C" int b200_tensor_core_check(b200_device d, const float *a, const float *b, int n, float *out) {
+  using namespace b200;
+  if (!d || !a || !b || !out) return B200_INVALID_ARGUMENT;
+  DeviceObj *dev = reinterpret_cast<DeviceObj *>(d);
+  if (n != 16 && n != 32 && n != 64) {
+    dev->lastError = "b200_tensor_core_check: n must be 16, 32 or 64";
+    return B200_INVALID_ARGUMENT;
+  }
+  float *dA = nullptr, *dB = nullptr, *dD = nullptr;
+  uint32_t *dS = nullptr;
+  auto cleanup = [&]() {
+    for (void *p : {(void *)dA, (void *)dB, (void *)dD, (void *)dS})
+      if (p) cudaFree(p);
+  };
+  try {
+    check(cudaSetDevice(dev->dev), "cudaSetDevice");
+    check(cudaMalloc(&dA, 128 * 64 * 4), "alloc");
+    check(cudaMalloc(&dB, size_t(n) * 64 * 4), "alloc");
+    check(cudaMalloc(&dD, size_t(128) * n * 4), "alloc");
+    check(cudaMalloc(&dS, 4), "alloc");
+    check(cudaMemset(dS, 0, 4), "clear");
+    check(cudaMemcpy(dA, a, 128 * 64 * 4, cudaMemcpyHostToDevice), "upload");
+    check(cudaMemcpy(dB, b, size_t(n) * 64 * 4, cudaMemcpyHostToDevice), "upload");
+    nrc::k_tc_check<<<1, 128, 0, dev->stream>>>(dA, dB, n, dD, dS);
+    check(cudaGetLastError(), "tensor-core check launch");
+    check(cudaStreamSynchronize(dev->stream), "tensor-core check");
+    uint32_t st = 0;
+    check(cudaMemcpy(&st, dS, 4, cudaMemcpyDeviceToHost), "status");
+    check(cudaMemcpy(out, dD, size_t(128) * n * 4, cudaMemcpyDeviceToHost), "download");
+    cleanup();
+    if (st) {
+      dev->lastError = "b200_tensor_core_check: the MMA did not complete";
+      return B200_UNKNOWN_ERROR;
+    }
+    return B200_NO_ERROR;
+  } catch (const Error &e) {
+    cleanup();
+    dev->lastError = e.what();
+    return e.code;
+  }
+}

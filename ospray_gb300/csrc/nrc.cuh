@@ -12,12 +12,10 @@
 //     resolution, spatial hash with primes 1, 2654435761, 805459861 where the
 //     dense grid would not fit, trilinear interpolation of F features).
 //
-// Layout of one warp's work: 16 samples (an m16 tile).  The encoding of the
-// 16 samples is staged in shared memory as a 16 x 64 BF16 matrix; each
-// layer is 4 (k16) x 8 (n8) mma.m16n8k16 with the weights read from shared
-// memory, and the FP32 accumulators of layer l are re-packed in registers as
-// the BF16 A operand of layer l+1 (the m16n8 accumulator layout of two
-// adjacent n8 tiles is the m16k16 operand layout).
+// The MLP runs on the 5th-generation tensor cores (tcgen05.mma, BF16 operands
+// in shared memory, FP32 accumulators in tensor memory; nrc.cu), 128 samples
+// per CTA tile; the weight gradients, reductions over the tile's samples,
+// use the warp-level mma.sync below.
 #pragma once
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
@@ -122,26 +120,6 @@ B200_D void mma16816(float c[4], const uint32_t a[4], uint32_t b0, uint32_t b1) 
       "{%0,%1,%2,%3};\n"
       : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
       : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
-}
-
-// A operand (16 x 64 BF16 row-major in shared memory, row stride `ld`
-// elements) for k-slice kk: the registers of lane (g, t)
-B200_D void loadA(const __nv_bfloat16 *X, int ld, int kk, int lane, uint32_t a[4]) {
-  const int g = lane >> 2, t = lane & 3;
-  const __nv_bfloat16 *r0 = X + g * ld + 16 * kk + 2 * t, *r1 = r0 + 8 * ld;
-  a[0] = *reinterpret_cast<const uint32_t *>(r0);
-  a[1] = *reinterpret_cast<const uint32_t *>(r1);
-  a[2] = *reinterpret_cast<const uint32_t *>(r0 + 8);
-  a[3] = *reinterpret_cast<const uint32_t *>(r1 + 8);
-}
-
-// B operand for C = A x B where B[k][n] = M[n][k] with M row-major (row
-// stride `ld` elements): k-slice kk, n-tile j
-B200_D void loadBT(const __nv_bfloat16 *M, int ld, int kk, int j, int lane, uint32_t &b0, uint32_t &b1) {
-  const int g = lane >> 2, t = lane & 3;
-  const __nv_bfloat16 *r = M + (8 * j + g) * ld + 16 * kk + 2 * t;
-  b0 = *reinterpret_cast<const uint32_t *>(r);
-  b1 = *reinterpret_cast<const uint32_t *>(r + 8);
 }
 
 }  // namespace nrc

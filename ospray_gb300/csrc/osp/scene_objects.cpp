@@ -108,31 +108,43 @@ void GeometryObj::bounds(float lo[3], float hi[3]) const {
 
 void MaterialObj::commit(B200Device &dev) {
   sv = {};
-  if (type == "principled") {
+  static const float kOne3[3] = {1.f, 1.f, 1.f};
+  if (type == "principled") {  // Principled::commit, render/materials/Principled.cpp:37-79
+    b200_material_defaults(&mat, B200_MATERIAL_PRINCIPLED);
     const float def[3] = {0.8f, 0.8f, 0.8f};
     getVec3("baseColor", mat.baseColor, def);
     mat.roughness = getFloat("roughness", 0.f);
     mat.metallic = getFloat("metallic", 0.f);
+    mat.opacity = getFloat("opacity", 1.f);
     // parameters of the principled model the GB300 path tracer does not
     // evaluate: accepted at their defaults, reported otherwise
     struct Def {
       const char *name;
       float value;
     };
-    static const Def fixed[] = {{"specular", 1.f}, {"ior", 1.f},      {"transmission", 0.f}, {"diffuse", 1.f},
-                                {"anisotropy", 0.f}, {"coat", 0.f},   {"sheen", 0.f},        {"backlight", 0.f},
-                                {"opacity", 1.f},    {"thin", 0.f}};
+    static const Def fixed[] = {{"specular", 1.f}, {"ior", 1.f},    {"transmission", 0.f}, {"diffuse", 1.f},
+                                {"anisotropy", 0.f}, {"coat", 0.f}, {"sheen", 0.f},        {"backlight", 0.f},
+                                {"thin", 0.f}};
     for (const Def &d : fixed)
       if (has(d.name) && getFloat(d.name, d.value) != d.value)
         dev.warn(std::string("principled material: '") + d.name + "' other than " + std::to_string(d.value) +
                  " is not supported by the b200 device; using the default");
-  } else {  // obj (OBJMaterial::commit, render/materials/OBJ.cpp:30-64)
+  } else if (type == "obj") {  // OBJMaterial::commit, render/materials/OBJ.cpp:28-65
+    b200_material_defaults(&mat, B200_MATERIAL_OBJ);
     const float def[3] = {0.8f, 0.8f, 0.8f};
     float kd[3], ks[3], tf[3];
     getVec3("kd", kd, def);
     getVec3("ks", ks, kZero3);
     getVec3("tf", tf, kZero3);
-    // energy conservation: kd + ks + tf scaled down to at most 1
+    // the path tracer gets the raw parameters (the device scales kd + ks + tf
+    // down to 1 itself); SciVis reads the scaled ones
+    for (int k = 0; k < 3; k++) {
+      mat.baseColor[k] = kd[k];
+      mat.ks[k] = ks[k];
+      mat.tf[k] = tf[k];
+    }
+    mat.ns = getFloat("ns", 10.f);
+    mat.opacity = getFloat("d", 1.f);
     float total = 0.f;
     for (int k = 0; k < 3; k++) total = std::max(total, kd[k] + ks[k] + tf[k]);
     if (total > 1.f)
@@ -147,16 +159,32 @@ void MaterialObj::commit(B200Device &dev) {
       sv.ks[k] = ks[k];
       sv.tf[k] = tf[k];
     }
-    sv.ns = getFloat("ns", 10.f);
-    sv.d = getFloat("d", 1.f);
-    // the path tracer renders it as Lambertian kd
-    for (int k = 0; k < 3; k++) mat.baseColor[k] = kd[k];
-    mat.roughness = 0.f;
-    mat.metallic = 0.f;
-    if (ks[0] != 0.f || ks[1] != 0.f || ks[2] != 0.f)
-      dev.warn("obj material: the b200 path tracer renders 'ks' as diffuse only (the scivis renderer uses it)");
-    if (sv.d != 1.f)
-      dev.warn("obj material: the b200 path tracer renders 'd' < 1 as opaque (the scivis renderer uses it)");
+    sv.ns = mat.ns;
+    sv.d = mat.opacity;
+  } else if (type == "metal") {  // Metal::commit, render/materials/Metal.cpp:27-70 (RGB eta / k)
+    b200_material_defaults(&mat, B200_MATERIAL_METAL);
+    const float e0[3] = {mat.eta[0], mat.eta[1], mat.eta[2]}, k0[3] = {mat.k[0], mat.k[1], mat.k[2]};
+    getVec3("eta", mat.eta, e0);
+    getVec3("k", mat.k, k0);
+    mat.roughness = getFloat("roughness", 0.1f);
+    if (has("ior")) dev.warn("metal material: spectral 'ior' data is not supported by the b200 device; using eta / k");
+  } else if (type == "glass") {  // Glass::commit, render/materials/Glass.cpp:27-50
+    b200_material_defaults(&mat, B200_MATERIAL_GLASS);
+    mat.eta[0] = getFloat("etaInside", getFloat("eta", 1.5f));
+    mat.eta[1] = getFloat("etaOutside", 1.f);
+    float c[3];
+    getVec3("attenuationColorInside", c, kOne3);
+    if (!has("attenuationColorInside")) getVec3("attenuationColor", c, kOne3);
+    for (int k = 0; k < 3; k++) mat.attenuationColor[k] = c[k];
+    mat.attenuationDistance = getFloat("attenuationDistance", 1.f);
+    if (has("attenuationColorOutside"))
+      dev.warn("glass material: 'attenuationColorOutside' is not supported by the b200 device; using 1");
+  } else {  // thinGlass: ThinGlass::commit, render/materials/ThinGlass.cpp:27-45
+    b200_material_defaults(&mat, B200_MATERIAL_THINGLASS);
+    mat.eta[0] = getFloat("eta", 1.5f);
+    getVec3("attenuationColor", mat.attenuationColor, kOne3);
+    mat.attenuationDistance = getFloat("attenuationDistance", 1.f);
+    mat.thickness = getFloat("thickness", 1.f);
   }
 }
 

@@ -15,9 +15,32 @@ namespace b200 {
 constexpr float PI_F = 3.14159265358979323846f;
 constexpr float MAT_EPS = 1e-6f;
 
-struct MaterialD {
-  float r, g, b, roughness, metallic;
+// Material types of the path tracer (render/materials/*.ispc) and the
+// device record the shading kernels read, prepared on the host from
+// b200_material (parameters normalised as each type's commit does).
+enum : uint32_t { MAT_PRINCIPLED = 0, MAT_OBJ = 1, MAT_METAL = 2, MAT_GLASS = 3, MAT_THINGLASS = 4 };
+constexpr uint32_t MATF_TRANSPARENT = 1u;  // getTransparency can be non-zero (shadow rays continue through it)
+
+struct __align__(16) MaterialD {
+  float r, g, b, roughness;  // principled baseColor, roughness; obj kd (scaled); metal roughness
+  float metallic, opacity;   // principled metallic, opacity; obj d
+  uint32_t kind, flags;      // MAT_*, MATF_*
+  float ks[3], ns;           // obj ks (scaled), ns
+  float tf[3], eta;          // obj tf (scaled); thin glass: 1 / eta
+  float ceta[3], pad0;       // metal: eta per channel
+  float ck[3], pad1;         // metal: k per channel
+  float att[3], iorIn;       // glass: inside medium attenuation (log(colour) / distance) and ior; thin glass: attenuation
+  float attOut[3], iorOut;   // glass: outside medium
 };
+static_assert(sizeof(MaterialD) == 128, "MaterialD layout");
+
+// scattering types (render/pathtracer/Scattering.ih:8-47)
+constexpr uint32_t ST_SPEC_R = 1u, ST_GLOSSY_R = 2u, ST_DIFFUSE_R = 4u, ST_SPEC_T = 8u, ST_GLOSSY_T = 16u,
+                   ST_DIFFUSE_T = 32u;
+constexpr uint32_t ST_REFLECTION = ST_SPEC_R | ST_GLOSSY_R | ST_DIFFUSE_R;
+constexpr uint32_t ST_TRANSMISSION = ST_SPEC_T | ST_GLOSSY_T | ST_DIFFUSE_T;
+constexpr uint32_t ST_SPECULAR = ST_SPEC_R | ST_SPEC_T;
+constexpr uint32_t ST_SMOOTH = ST_GLOSSY_R | ST_DIFFUSE_R | ST_GLOSSY_T | ST_DIFFUSE_T;
 
 // GGX albedo tables: dir 32x32 (cosThetaO fastest, roughness), avg 32;
 // dielectric reflection: dir 16^3 (cos, eta in [1/3,1], roughness), avg 16^2
@@ -29,6 +52,8 @@ struct AlbedoTablesD {
 };
 
 B200_D float sqrf(float x) { return x * x; }
+B200_D float maxc(V3 v) { return fmaxf(fmaxf(v.x, v.y), v.z); }
+B200_D float luminanceV(V3 c) { return 0.212671f * c.x + 0.715160f * c.y + 0.072169f * c.z; }
 B200_D float clamp01f(float x) { return fminf(fmaxf(x, 0.f), 1.f); }
 B200_D float rcpSafe(float x) { return 1.f / (fabsf(x) < 1e-8f ? copysignf(1e-8f, x) : x); }
 B200_D float lerpF(float f, float a, float b) { return (1.f - f) * a + f * b; }
@@ -128,6 +153,7 @@ struct BsdfEval {
 struct BsdfSample {
   V3 wi, weight;
   float pdf;
+  uint32_t type;  // ST_* of the sampled lobe
 };
 
 // Principled with its opacity-1, coat/sheen-free structure: a MultiBSDF of
@@ -215,7 +241,7 @@ struct Principled {
   }
 
   B200_D BsdfSample sampleConductor(V3 wo, float sx, float sy, const AlbedoTablesD *T) const {
-    BsdfSample r = {splat(0.f), splat(0.f), 0.f};
+    BsdfSample r = {splat(0.f), splat(0.f), 0.f, 0u};
     const float cosO = fdot(wo, N);
     if (cosO <= 0.f) return r;
     const V3 wo0 = toLocal(wo);
@@ -233,6 +259,7 @@ struct Principled {
     r.wi = wi;
     r.pdf = whPdf / (4.f * fabsf(cosOH));
     r.weight = F * (G * rcpSafe(ggxG1(alpha, wo0, cosOH))) + fms * (1.f / r.pdf);
+    r.type = ST_GLOSSY_R;
     return r;
   }
 
@@ -271,7 +298,7 @@ struct Principled {
   }
 
   B200_D BsdfSample samplePlastic(V3 wo, float sx, float sy, float ss, const AlbedoTablesD *T) const {
-    BsdfSample r = {splat(0.f), splat(0.f), 0.f};
+    BsdfSample r = {splat(0.f), splat(0.f), 0.f, 0u};
     const float cosO = fdot(wo, N);
     if (cosO <= 0.f) return r;
     const V3 wo0 = toLocal(wo);
@@ -285,12 +312,14 @@ struct Principled {
       float whPdf;
       wh = toGlobal(ggxSampleVisible(alpha, wo0, whPdf, sx, sy));
       r.wi = reflectV(wo, wh, fdot(wo, wh));
+      r.type = ST_GLOSSY_R;
       sub = evalOrenNayar(wo, r.wi);
     } else {
       float sp, cp;
       sincosf(2.f * PI_F * sx, &sp, &cp);
       const float cosT = sqrtf(sy), sinT = sqrtf(1.f - sy);
       r.wi = toGlobal(mk(cp * sinT, sp * sinT, cosT));
+      r.type = ST_DIFFUSE_R;
       const BsdfEval e = evalOrenNayar(wo, r.wi);
       r.pdf = e.pdf;
       r.weight = e.value * (1.f / e.pdf);
@@ -335,7 +364,7 @@ struct Principled {
   }
 
   B200_D BsdfSample sample(V3 wo, float sx, float sy, float ss, const AlbedoTablesD *T) const {
-    BsdfSample r = {splat(0.f), splat(0.f), 0.f};
+    BsdfSample r = {splat(0.f), splat(0.f), 0.f, 0u};
     if (impSum == 0.f) return r;
     const float x = ss * impSum;
     int choice;
@@ -351,7 +380,7 @@ struct Principled {
       return r;
     }
     if ((r.weight.x == 0.f && r.weight.y == 0.f && r.weight.z == 0.f) || r.pdf == 0.f)
-      return {splat(0.f), splat(0.f), 0.f};
+      return {splat(0.f), splat(0.f), 0.f, 0u};
     V3 value = r.weight * r.pdf;
     float pdf = r.pdf * (choice == 0 ? wC : wP);
     if (choice != 0 && wC > 0.f) {
@@ -369,5 +398,497 @@ struct Principled {
     return r;
   }
 };
+
+// ---------------------------------------------------------------- surface BSDFs by material type
+// Each type has init / eval / sample with MultiBSDF semantics
+// (render/bsdfs/MultiBSDF.ih): eval sums the evaluable children's values
+// (x weight) and their pdfs x importance / importance sum; sample picks a
+// child by importance, and unless it is specular adds the other children's
+// eval.  `smooth` = the BSDF has a diffuse or glossy lobe (isSmooth,
+// render/pathtracer/PathTracerUtil.ih:13-28): such vertices do next-event
+// estimation.
+
+B200_D V3 expV(V3 a) { return mk(expf(a.x), expf(a.y), expf(a.z)); }
+
+// Principled_BSDF root (render/materials/Principled.ispc:81-429): child 0 the
+// cut-out Transmission (weight 1, importance 1 - opacity), child 1 the base
+// stack (weight = importance = opacity), built only when opacity > EPS.
+// CUT = false: every material of the frame is opaque (1 - opacity <= EPS), so
+// the root has the stack child only and the cut-out state drops out.
+template <bool CUT>
+struct PrincipledBsdfT {
+  Principled st;
+  float op, tr, impSum;
+  bool hasStack, hasCut, smooth;
+  B200_D V3 N() const { return st.N; }
+  B200_D V3 albedoV() const {
+    V3 a = hasStack ? st.albedo * op : splat(0.f);
+    if (CUT && hasCut) a = a + splat(tr);
+    return a;
+  }
+  B200_D void init(const MaterialD &m, V3 U, V3 V, V3 Nn, const AlbedoTablesD *T) {
+    op = clamp01f(m.opacity);
+    tr = CUT ? 1.f - op : 0.f;
+    hasStack = !CUT || m.opacity > MAT_EPS;
+    hasCut = CUT && 1.f - m.opacity > MAT_EPS;
+    if (hasStack) {
+      st.init(m, U, V, Nn, T);
+    } else {
+      st.fx = U;
+      st.fy = V;
+      st.N = Nn;
+      st.impSum = 0.f;
+      st.albedo = splat(0.f);
+    }
+    smooth = hasStack && st.impSum > 0.f;
+    impSum = (hasCut ? tr : 0.f) + (hasStack ? op : 0.f);
+  }
+  B200_D BsdfEval eval(V3 wo, V3 wi, const AlbedoTablesD *T) const {
+    BsdfEval r = {splat(0.f), 0.f};
+    if (hasStack && op > 0.f) {
+      const BsdfEval e = st.eval(wo, wi, T);
+      r.value = e.value * op;
+      r.pdf = e.pdf * op;
+    }
+    r.pdf *= 1.f / impSum;
+    return r;
+  }
+  B200_D BsdfSample sample(V3 wo, float sx, float sy, float ss, const AlbedoTablesD *T) const {
+    BsdfSample r = {splat(0.f), splat(0.f), 0.f, 0u};
+    if (impSum == 0.f) return r;
+    const float x = ss * impSum;
+    float prefix = 0.f;
+    if (CUT && hasCut && x < (prefix += tr)) {
+      // Transmission_sample: straight through, a Dirac lobe
+      r.wi = -wo;
+      r.pdf = INFINITY;
+      r.type = ST_SPEC_T;
+      r.weight = splat(tr) * (impSum * (1.f / tr));
+      return r;
+    }
+    if (!hasStack) return r;
+    prefix += op;
+    r = st.sample(wo, sx, sy, (x + op - prefix) * (1.f / op), T);
+    r.weight = r.weight * op;
+    if ((r.weight.x == 0.f && r.weight.y == 0.f && r.weight.z == 0.f) || r.pdf == 0.f)
+      return {splat(0.f), splat(0.f), 0.f, 0u};
+    if (r.type & ST_SPECULAR) {
+      r.weight = r.weight * (impSum * (1.f / op));
+      return r;
+    }
+    const V3 value = r.weight * r.pdf;
+    r.pdf = r.pdf * op * (1.f / impSum);
+    r.weight = value * (1.f / r.pdf);
+    return r;
+  }
+};
+using PrincipledBsdf = PrincipledBsdfT<true>;
+
+// OBJ_BSDF (render/materials/OBJ.ispc:29-126): Lambert (child 0), specular
+// Transmission (child 1), Blinn "Specular" (child 2, bsdfs/Specular.ih),
+// each with weight 1 and importance = luminance of its albedo.
+struct ObjBsdf {
+  V3 fx, fy, Nn;
+  V3 Kd, Tt, ksN, specW;
+  float ns, iL, iT, iS, impSum;
+  bool smooth;
+  V3 albedo;
+  B200_D V3 albedoV() const { return albedo; }
+  B200_D V3 N() const { return Nn; }
+  B200_D V3 toGlobal(V3 v) const { return fx * v.x + fy * v.y + Nn * v.z; }
+  B200_D void init(const MaterialD &m, V3 U, V3 V, V3 N) {
+    fx = U;
+    fy = V;
+    Nn = N;
+    const float d = m.opacity;
+    Kd = mk(m.r, m.g, m.b) * d;
+    Tt = mk(m.tf[0], m.tf[1], m.tf[2]) * d + splat(1.f - d);
+    const V3 Ks = mk(m.ks[0], m.ks[1], m.ks[2]) * d;
+    iL = iT = iS = impSum = 0.f;
+    albedo = splat(0.f);
+    if (maxc(Kd) > 0.f) {
+      iL = luminanceV(Kd);
+      impSum += iL;
+      albedo = albedo + Kd;
+    }
+    if (maxc(Tt) > 0.f) {
+      iT = luminanceV(Tt);
+      impSum += iT;
+      albedo = albedo + Tt;
+    }
+    // Specular_Constructor: Phong exponent to Blinn, energy normalisation
+    ns = m.ns * 4.f;
+    const float tmp = (ns + 2.f) * (1.f / (2.f - expf(ns * -0.34657359027997264f)));
+    ksN = Ks * ((1.f / (4.f * PI_F)) * tmp);
+    specW = Ks * (2.f * tmp * (1.f / (ns + 1.f)));
+    if (maxc(Ks) > 0.f) {
+      iS = luminanceV(Ks);
+      impSum += iS;
+      albedo = albedo + Ks;
+    }
+    smooth = iL > 0.f || iS > 0.f;
+  }
+  B200_D BsdfEval evalLambert(V3 wi) const {
+    const float c = fmaxf(fdot(wi, Nn), 0.f);
+    return {Kd * ((1.f / PI_F) * c), c * (1.f / PI_F)};
+  }
+  B200_D BsdfEval evalSpecular(V3 wo, V3 wi) const {
+    const float cosO = fdot(wo, Nn), cosI = fdot(wi, Nn);
+    if (cosO <= 0.f || cosI <= 0.f) return {splat(0.f), 0.f};
+    const V3 wh = fnormalize(wo + wi);
+    const float cosH = fdot(wh, Nn);
+    const float pdf = (ns + 1.f) * (1.f / (2.f * PI_F)) * powf(cosH, ns) * (1.f / (4.f * fdot(wo, wh)));
+    return {ksN * powf(cosH, ns), pdf};
+  }
+  B200_D BsdfEval eval(V3 wo, V3 wi, const AlbedoTablesD *) const { return evalSkip(wo, wi, -1); }
+  // the children's eval except child `skip` (-1: all, pdf normalised)
+  B200_D BsdfEval evalSkip(V3 wo, V3 wi, int skip) const {
+    BsdfEval r = {splat(0.f), 0.f};
+    if (iL > 0.f && skip != 0) {
+      const BsdfEval c = evalLambert(wi);
+      r.value = r.value + c.value;
+      r.pdf += c.pdf * iL;
+    }
+    if (iS > 0.f && skip != 2) {
+      const BsdfEval c = evalSpecular(wo, wi);
+      r.value = r.value + c.value;
+      r.pdf += c.pdf * iS;
+    }
+    if (skip < 0) r.pdf *= 1.f / impSum;
+    return r;
+  }
+  B200_D BsdfSample sample(V3 wo, float sx, float sy, float ss, const AlbedoTablesD *) const {
+    BsdfSample r = {splat(0.f), splat(0.f), 0.f, 0u};
+    if (impSum == 0.f) return r;
+    const float x = ss * impSum;
+    float prefix = 0.f, imp = 0.f;
+    int choice;
+    if (x < (prefix += iL)) {
+      choice = 0;
+      imp = iL;
+      float sp, cp;
+      sincosf(2.f * PI_F * sx, &sp, &cp);
+      const float cosT = sqrtf(sy), sinT = sqrtf(1.f - sy);
+      const V3 l = mk(cp * sinT, sp * sinT, cosT);
+      r.wi = toGlobal(l);
+      r.pdf = l.z * (1.f / PI_F);
+      r.type = ST_DIFFUSE_R;
+      r.weight = Kd;
+    } else if (x < (prefix += iT)) {
+      choice = 1;
+      imp = iT;
+      r.wi = -wo;
+      r.pdf = INFINITY;
+      r.type = ST_SPEC_T;
+      r.weight = Tt;
+    } else if (x < (prefix += iS)) {
+      choice = 2;
+      imp = iS;
+      // powerCosineSampleHemisphere(ns, s) about N, reflected about the half vector
+      const float phi = 2.f * PI_F * sx;
+      const float cosT = powf(sy, 1.f / (ns + 1.f));
+      float sp, cp;
+      sincosf(phi, &sp, &cp);
+      const float sinT = sqrtf(fmaxf(0.f, 1.f - cosT * cosT));
+      const V3 whl = mk(cp * sinT, sp * sinT, cosT);
+      const V3 wh = toGlobal(whl);
+      const float cosOH = fdot(wo, wh);
+      r.wi = reflectV(wo, wh, cosOH);
+      if (fdot(r.wi, Nn) <= 0.f) return {splat(0.f), splat(0.f), 0.f, 0u};
+      r.pdf = (ns + 1.f) * (1.f / (2.f * PI_F)) * powf(whl.z, ns) * (1.f / (4.f * cosOH));
+      r.type = ST_GLOSSY_R;
+      r.weight = specW * cosOH;
+    } else {
+      return r;
+    }
+    if ((r.weight.x == 0.f && r.weight.y == 0.f && r.weight.z == 0.f) || r.pdf == 0.f)
+      return {splat(0.f), splat(0.f), 0.f, 0u};
+    if (r.type & ST_SPECULAR) {
+      r.weight = r.weight * (impSum * (1.f / imp));
+      return r;
+    }
+    V3 value = r.weight * r.pdf;
+    float pdf = r.pdf * imp;
+    const BsdfEval o = evalSkip(wo, r.wi, choice);
+    value = value + o.value;
+    pdf += o.pdf;
+    r.pdf = pdf * (1.f / impSum);
+    r.weight = value * (1.f / r.pdf);
+    return r;
+  }
+};
+
+// Metal (render/materials/Metal.ispc:16-48): RGB conductor Fresnel (eta, k)
+// in the frame about Ns; roughness 0 the specular Conductor
+// (bsdfs/Conductor.ih), else MicrofacetConductor with no energy
+// compensation (the RGB Fresnel's average is 0, so fmsScale and the albedo
+// are 0).
+struct MetalBsdf {
+  V3 fx, fy, Nn, ceta, ck;
+  float rough, alpha;
+  bool specular, smooth;
+  V3 albedo;
+  B200_D V3 albedoV() const { return albedo; }
+  B200_D V3 N() const { return Nn; }
+  B200_D V3 toLocal(V3 v) const { return mk(fdot(v, fx), fdot(v, fy), fdot(v, Nn)); }
+  B200_D V3 toGlobal(V3 v) const { return fx * v.x + fy * v.y + Nn * v.z; }
+  B200_D V3 fresnel(float c) const {
+    return mk(fresnelCond(c, ceta.x, ck.x), fresnelCond(c, ceta.y, ck.y), fresnelCond(c, ceta.z, ck.z));
+  }
+  B200_D void init(const MaterialD &m, V3 Ns) {
+    Nn = Ns;
+    frame(Ns, fx, fy);
+    ceta = mk(m.ceta[0], m.ceta[1], m.ceta[2]);
+    ck = mk(m.ck[0], m.ck[1], m.ck[2]);
+    rough = m.roughness;
+    alpha = fmaxf(sqrf(rough), 0.001f);
+    specular = rough == 0.f;
+    smooth = !specular;
+    albedo = splat(0.f);
+  }
+  B200_D BsdfEval eval(V3 wo, V3 wi, const AlbedoTablesD *) const {
+    if (specular) return {splat(0.f), 0.f};
+    const float cosO = fdot(wo, Nn), cosI = fdot(wi, Nn);
+    if (cosO <= 0.f || cosI <= 0.f) return {splat(0.f), 0.f};
+    const V3 wh = fnormalize(wi + wo);
+    const float cosOH = fdot(wo, wh), cosIH = fdot(wi, wh);
+    const V3 wo0 = toLocal(wo), wi0 = toLocal(wi), wh0 = toLocal(wh);
+    float whPdf;
+    const float D = ggxEvalVisible(alpha, wh0, wo0, cosOH, whPdf);
+    const float G = ggxG2(alpha, wo0, wi0, cosOH, cosIH);
+    return {fresnel(cosOH) * (D * G * (1.f / (4.f * cosO))), whPdf * (1.f / (4.f * fabsf(cosOH)))};
+  }
+  B200_D BsdfSample sample(V3 wo, float sx, float sy, float, const AlbedoTablesD *) const {
+    BsdfSample r = {splat(0.f), splat(0.f), 0.f, 0u};
+    if (specular) {
+      const float c = fdot(wo, Nn);
+      r.wi = reflectV(wo, Nn, c);
+      r.pdf = INFINITY;
+      r.type = ST_SPEC_R;
+      r.weight = fresnel(c);
+      return r;
+    }
+    const float cosO = fdot(wo, Nn);
+    if (cosO <= 0.f) return r;
+    const V3 wo0 = toLocal(wo);
+    float whPdf;
+    const V3 wh = toGlobal(ggxSampleVisible(alpha, wo0, whPdf, sx, sy));
+    const V3 wi = reflectV(wo, wh, fdot(wo, wh));
+    const float cosI = fdot(wi, Nn);
+    if (cosI <= 0.f) return r;
+    const float cosOH = fdot(wo, wh), cosIH = fdot(wi, wh);
+    const float G = ggxG2(alpha, wo0, toLocal(wi), cosOH, cosIH);
+    r.wi = wi;
+    r.type = ST_GLOSSY_R;
+    r.pdf = whPdf * (1.f / (4.f * fabsf(cosOH)));
+    r.weight = fresnel(cosOH) * (G * rcpSafe(ggxG1(alpha, wo0, cosOH)));
+    return r;
+  }
+};
+
+// Glass (render/materials/Glass.ispc:16-60) as RobustDielectric
+// (bsdfs/RobustDielectric.ih): eta = ior outside / ior inside when the path
+// comes from the outside medium, else the inverse; Dirac reflection or
+// refraction picked by the Fresnel reflectance, with the robust normal flips
+// and grazing nudges.
+struct GlassBsdf {
+  V3 Ns, Ng;
+  float eta;  // as RobustDielectric stores it: the inverse of the refraction ratio it applies
+  bool smooth;
+  V3 albedo;
+  B200_D V3 albedoV() const { return albedo; }
+  B200_D V3 N() const { return Ns; }
+  B200_D void init(float eta_, V3 ns, V3 ng) {
+    eta = eta_;
+    Ns = ns;
+    Ng = ng;
+    smooth = false;
+    albedo = splat(1.f);
+  }
+  B200_D BsdfEval eval(V3, V3, const AlbedoTablesD *) const { return {splat(0.f), 0.f}; }
+  B200_D BsdfSample sample(V3 wo, float, float, float ss, const AlbedoTablesD *) const {
+    BsdfSample r;
+    r.pdf = INFINITY;
+    r.weight = splat(1.f);
+    const V3 inc = -wo;
+    V3 sn = Ns, gn = Ng;
+    const float e = 1.f / eta;
+    const float geps = 1e-6f;
+    const bool canReflect = e < 1.f - geps || e > 1.f + geps;
+    if (fdot(inc, sn) > 0.f) sn = -sn;
+    if (fdot(inc, gn) > 0.f) gn = -gn;
+    // ReflectionDirection
+    const V3 par = sn * fdot(inc, sn);
+    const V3 dirR = (inc - par) - par;
+    // RefractionDirection
+    V3 dirT;
+    float FR;
+    bool mustReflect = false;
+    {
+      const float cos1 = fdot(inc, sn);
+      const float c1 = fabsf(cos1);
+      const bool headOn = 1.f - 1e-6f < c1 && c1 < 1.f - 1e-6f;  // never true, as in the reference
+      if (headOn) {
+        FR = sqrf((e - 1.f) / (e + 1.f));
+        dirT = inc;
+      } else {
+        const V3 dpar = sn * cos1;
+        const V3 dperp = inc - dpar;
+        const V3 b = fnormalize(dperp);
+        const float sin1 = fdot(dperp, b);
+        const float sin2 = sin1 / e;
+        if (sin2 > 1.f) {
+          dirT = splat(0.f);
+          FR = 1.f;
+          mustReflect = true;
+        } else {
+          const float cos2 = sqrtf(clamp01f(1.f - sin2 * sin2));
+          const V3 N2 = fnormalize(dpar);
+          dirT = N2 * cos2 + b * sin2;
+          const float q1 = (e * c1 - cos2) / (e * c1 + cos2);
+          const float q2 = (c1 - e * cos2) / (c1 + e * cos2);
+          FR = 0.5f * (q1 * q1 + q2 * q2);
+        }
+      }
+      FR = clamp01f(FR);
+    }
+    if ((ss < FR && canReflect) || mustReflect) {
+      r.wi = dirR;
+      r.type = ST_SPEC_R;
+      const float gc = fdot(r.wi, gn);
+      if (gc >= 0.f) {
+        if (gc < geps) r.wi = fnormalize(r.wi + gn * geps);
+      } else {
+        r.wi = r.wi - gn * (2.f * gc);
+      }
+    } else {
+      r.wi = dirT;
+      r.type = ST_SPEC_T;
+      const float gc = fdot(r.wi, gn);
+      if (gc <= 0.f) {
+        if (gc > -geps) r.wi = fnormalize(r.wi - gn * geps);
+      } else {
+        r.type = ST_SPEC_R;
+      }
+    }
+    return r;
+  }
+};
+
+// ThinGlass (render/materials/ThinGlass.ispc:16-70) as RobustThinDielectric
+// (bsdfs/RobustThinDielectric.ih): a slab whose inner reflections are summed
+// in closed form; reflection or straight transmission picked by luminance.
+B200_D float fresnelDielEx(float cosI, float &cosT, float eta) {
+  const float c2 = 1.f - sqrf(eta) * (1.f - sqrf(cosI));
+  if (c2 < 0.f) {
+    cosT = 0.f;
+    return 1.f;
+  }
+  cosT = sqrtf(c2);
+  const float Rper = (eta * cosI - cosT) / (eta * cosI + cosT);
+  const float Rpar = (cosI - eta * cosT) / (cosI + eta * cosT);
+  return 0.5f * (sqrf(Rpar) + sqrf(Rper));
+}
+B200_D void thinSlab(float cosO, float eta, V3 att, V3 &R, V3 &T) {
+  float cosT;
+  const float Fo = fresnelDielEx(cosO, cosT, eta);
+  const float Ft = fresnelDiel(cosT, 1.f / eta);
+  const V3 A = expV(att * (1.f / cosT));
+  const V3 FA = A * Ft;
+  const V3 FA2 = FA * FA;
+  const V3 inv = mk(1.f / (1.f - FA2.x), 1.f / (1.f - FA2.y), 1.f / (1.f - FA2.z));
+  R = splat(Fo) + (A * A) * ((1.f - Fo) * (1.f - Ft) * Ft) * inv;
+  T = A * ((1.f - Fo) * (1.f - Ft)) * (splat(1.f) + FA2 * inv);
+}
+struct ThinGlassBsdf {
+  V3 Nn, att;
+  float eta;
+  bool smooth;
+  V3 albedo;
+  B200_D V3 albedoV() const { return albedo; }
+  B200_D V3 N() const { return Nn; }
+  B200_D void init(const MaterialD &m, V3 Ns) {
+    Nn = Ns;
+    eta = m.eta;
+    att = mk(m.att[0], m.att[1], m.att[2]);
+    smooth = false;
+    albedo = expV(att);
+  }
+  B200_D BsdfEval eval(V3, V3, const AlbedoTablesD *) const { return {splat(0.f), 0.f}; }
+  B200_D BsdfSample sample(V3 wo, float, float, float ss, const AlbedoTablesD *) const {
+    BsdfSample r;
+    const float cosO = fmaxf(fdot(wo, Nn), 0.f);
+    V3 R, T;
+    thinSlab(cosO, eta, att, R, T);
+    const float pR = luminanceV(R), pT = luminanceV(T);
+    const float p = fminf(fmaxf(pR * (1.f / (pR + pT)), 0.25f), 0.75f);
+    if (ss <= p) {
+      r.wi = reflectV(wo, Nn, cosO);
+      r.type = ST_SPEC_R;
+      r.weight = R * (1.f / p);
+    } else {
+      r.wi = -wo;
+      r.type = ST_SPEC_T;
+      r.weight = T * (1.f / (1.f - p));
+    }
+    r.pdf = INFINITY;
+    return r;
+  }
+};
+
+// A medium: ior and attenuation (render/materials/Medium.ih).  Paths carry
+// the id of the medium they travel in: MEDIUM_VACUUM, or material m's inside
+// (2m) or outside (2m + 1) medium (glass); media compare by value.
+constexpr uint32_t MEDIUM_VACUUM = 0xffffffffu;
+struct MediumD {
+  float ior;
+  V3 att;
+};
+B200_D MediumD mediumOf(const MaterialD *mats, uint32_t id) {
+  if (id == MEDIUM_VACUUM) return {1.f, splat(0.f)};
+  const MaterialD &m = mats[id >> 1];
+  if (id & 1u) return {m.iorOut, mk(m.attOut[0], m.attOut[1], m.attOut[2])};
+  return {m.iorIn, mk(m.att[0], m.att[1], m.att[2])};
+}
+B200_D bool sameMedium(const MediumD &a, const MediumD &b) {
+  return a.ior == b.ior && a.att.x == b.att.x && a.att.y == b.att.y && a.att.z == b.att.z;
+}
+// Glass_selectNextMedium / the eta of Glass_getBSDF: from the outside medium
+// into the inside one, otherwise back out
+B200_D bool glassFromOutside(const MaterialD *mats, uint32_t mat, uint32_t cur) {
+  return sameMedium(mediumOf(mats, cur), mediumOf(mats, 2u * mat + 1u));
+}
+
+// Material_getTransparency of the hit material for a shadow ray
+// (TransparentShadow.ispc:18-85): principled 1 - opacity, obj tf d + 1 - d,
+// glass 1 - Fresnel, thin glass the slab's transmission, metal 0.
+B200_D V3 materialTransparency(const MaterialD *mats, uint32_t mi, V3 rayDir, V3 Ns, uint32_t medium) {
+  const MaterialD &m = mats[mi];
+  switch (m.kind) {
+    case MAT_PRINCIPLED: {
+      const float op = clamp01f(m.opacity);
+      const float tr = 1.f - op;
+      if (tr <= MAT_EPS) return splat(0.f);
+      return splat(tr);
+    }
+    case MAT_OBJ: {
+      const float d = m.opacity;
+      return mk(m.tf[0], m.tf[1], m.tf[2]) * d + splat(1.f - d);
+    }
+    case MAT_GLASS: {
+      const bool out = glassFromOutside(mats, mi, medium);
+      const float eta = out ? m.iorOut * (1.f / m.iorIn) : m.iorIn * (1.f / m.iorOut);
+      const float cosO = fmaxf(-fdot(rayDir, Ns), 0.f);
+      return splat(1.f - fresnelDiel(cosO, eta));
+    }
+    case MAT_THINGLASS: {
+      V3 R, T;
+      thinSlab(fmaxf(-fdot(rayDir, Ns), 0.f), m.eta, mk(m.att[0], m.att[1], m.att[2]), R, T);
+      return T;
+    }
+    default:
+      return splat(0.f);
+  }
+}
 
 }  // namespace b200

@@ -36,6 +36,10 @@ constexpr size_t OFF_MATERIALS = alignUp(sizeof(AlbedoTablesD));
 constexpr size_t OFF_WORKSPACE = OFF_MATERIALS + alignUp(sizeof(MaterialD) * NOALLOC_MAX_MATERIALS);
 constexpr size_t WORKSPACE_BYTES = NOALLOC_SCRATCH_BYTES - OFF_WORKSPACE;
 
+// host staging for the material list (pageable, so an async copy from it has
+// left it when the call returns)
+MaterialD g_hostMaterials[NOALLOC_MAX_MATERIALS];
+
 struct DeviceScratch {
   unsigned char *base = nullptr;  // device address of g_ptScratch
   bool tablesReady = false;
@@ -102,76 +106,69 @@ extern "C" {
 // it before capturing any stream.  All calls share one scratch array and
 // keep its last contents: calls that overlap on the GPU (different streams,
 // or different host threads, without ordering) race and must not be issued.
+// The caller's material array may be reused as soon as the call returns: the
+// materials are converted into a static host staging array and copied from
+// there (pageable memory, so the copy has left it when the call returns).
 int b200_render_pt_noalloc(b200_scene s, const b200_camera_desc *camera, const b200_pt_params *p,
                            const b200_material *materials, int nmaterials, b200_frame f, void *stream) {
   if (!s || !camera || !p || !f) return B200_INVALID_ARGUMENT;
   SceneObj *sc = reinterpret_cast<SceneObj *>(s);
   FrameObj *fb = reinterpret_cast<FrameObj *>(f);
   DeviceObj *dev = sc->dev;
-  cudaError_t e = cudaSetDevice(dev->dev);
-  if (e != cudaSuccess) {
-    dev->lastError = std::string("cudaSetDevice: ") + cudaGetErrorString(e);
-    return B200_UNKNOWN_ERROR;
-  }
   auto fail = [&](int code, const std::string &msg) {
     dev->lastError = msg;
     return code;
   };
-  if (!sc->committed) return fail(B200_INVALID_OPERATION, "scene not committed");
-  if (p->pixelSamples < 1 || p->maxPathLength < 0) return fail(B200_INVALID_ARGUMENT, "bad path tracer parameters");
-  if (p->pixelFilter < B200_PF_POINT || p->pixelFilter > B200_PF_BLACKMAN_HARRIS)
-    return fail(B200_INVALID_ARGUMENT, "bad pixel filter");
-  if (nmaterials < 0 || (nmaterials > 0 && !materials)) return fail(B200_INVALID_ARGUMENT, "bad material array");
-  if (nmaterials > NOALLOC_MAX_MATERIALS)
-    return fail(B200_INVALID_ARGUMENT, "b200_render_pt_noalloc: more than 4096 materials");
-  const long long npaths = (long long)fb->W * fb->H * p->pixelSamples;
-  const long long maxPaths = ptNoallocMaxPaths();
-  if (npaths > maxPaths)
-    return fail(B200_INVALID_ARGUMENT, "b200_render_pt_noalloc: width*height*pixelSamples = " +
-                                           std::to_string(npaths) + " exceeds the static scratch limit of " +
-                                           std::to_string(maxPaths) + " paths");
-  std::string err;
-  const int rc = setupDevice(dev, err);
-  if (rc != B200_NO_ERROR) return fail(rc, err);
-  unsigned char *base = g_scratch[dev->dev].base;
-  cudaStream_t st = stream ? (cudaStream_t)stream : dev->stream;
-  // the caller's material list straight into the scratch (same layout)
-  static_assert(sizeof(b200_material) == sizeof(MaterialD), "material layouts differ");
-  if (nmaterials > 0) {
-    e = cudaMemcpyAsync(base + OFF_MATERIALS, materials, sizeof(MaterialD) * nmaterials, cudaMemcpyHostToDevice, st);
-    if (e != cudaSuccess) return fail(B200_UNKNOWN_ERROR, std::string("upload materials: ") + cudaGetErrorString(e));
-  }
-  PtParamsD d;
-  d.spp = p->pixelSamples;
-  d.maxPathLength = p->maxPathLength;
-  d.roulettePathLength = p->roulettePathLength;
-  d.maxScatteringEvents = p->maxScatteringEvents;
-  const int nl = sc->nLights;
-  d.nFirst = p->lightSamples >= 0 && nl > 0 ? p->lightSamples : std::min(1024, nl);
-  d.nIndirect = p->limitIndirectLightSamples && d.nFirst >= 1 ? 1 : d.nFirst;
-  if (nl == 0) d.nFirst = d.nIndirect = 0;
-  d.numLights = nl;
-  d.numMaterials = nmaterials;
-  d.minContribution = p->minContribution;
-  d.maxContribution = p->maxContribution;
-  for (int k = 0; k < 4; k++) d.bg[k] = p->backgroundColor[k];
   try {
+    cudaError_t e = cudaSetDevice(dev->dev);
+    if (e != cudaSuccess) return fail(B200_UNKNOWN_ERROR, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
+    if (!sc->committed) return fail(B200_INVALID_OPERATION, "scene not committed");
+    if (p->pixelSamples < 1 || p->maxPathLength < 0) return fail(B200_INVALID_ARGUMENT, "bad path tracer parameters");
+    if (p->pixelFilter < B200_PF_POINT || p->pixelFilter > B200_PF_BLACKMAN_HARRIS)
+      return fail(B200_INVALID_ARGUMENT, "bad pixel filter");
+    if (nmaterials < 0 || (nmaterials > 0 && !materials)) return fail(B200_INVALID_ARGUMENT, "bad material array");
+    if (nmaterials > NOALLOC_MAX_MATERIALS)
+      return fail(B200_INVALID_ARGUMENT, "b200_render_pt_noalloc: more than 4096 materials");
+    const long long npaths = (long long)fb->W * fb->H * p->pixelSamples;
+    const long long maxPaths = ptNoallocMaxPaths();
+    if (npaths > maxPaths)
+      return fail(B200_INVALID_ARGUMENT, "b200_render_pt_noalloc: width*height*pixelSamples = " +
+                                             std::to_string(npaths) + " exceeds the static scratch limit of " +
+                                             std::to_string(maxPaths) + " paths");
+    std::string err;
+    const int rc = setupDevice(dev, err);
+    if (rc != B200_NO_ERROR) return fail(rc, err);
+    unsigned char *base = g_scratch[dev->dev].base;
+    cudaStream_t st = stream ? (cudaStream_t)stream : dev->stream;
+    bool transparent = false;
+    if (nmaterials > 0) {
+      std::lock_guard<std::mutex> lock(g_setupMutex);
+      for (int i = 0; i < nmaterials; i++) {
+        g_hostMaterials[i] = toMaterialD(materials[i]);
+        transparent = transparent || (g_hostMaterials[i].flags & MATF_TRANSPARENT);
+      }
+      e = cudaMemcpyAsync(base + OFF_MATERIALS, g_hostMaterials, sizeof(MaterialD) * nmaterials,
+                          cudaMemcpyHostToDevice, st);
+      if (e != cudaSuccess) return fail(B200_UNKNOWN_ERROR, std::string("upload materials: ") + cudaGetErrorString(e));
+    }
+    const PtParamsD d =
+        makePtParams(*p, sc->nLights, nmaterials, transparent, anyNonPrincipled(materials, nmaterials));
     fb->beginFrame(p->pixelSamples, st);
+    e = launchRenderPT(dev->tables, sc->view(), makeCamera(*camera), dev->filter(p->pixelFilter), d,
+                       reinterpret_cast<const MaterialD *>(base + OFF_MATERIALS), sc->dLights, sc->dLightCdf,
+                       reinterpret_cast<const AlbedoTablesD *>(base + OFF_ALBEDO), fb->view(), p->collectStats != 0,
+                       base + OFF_WORKSPACE, WORKSPACE_BYTES, st);
+    if (e != cudaSuccess) return fail(B200_UNKNOWN_ERROR, std::string("path tracer launch: ") + cudaGetErrorString(e));
+    fb->frameID++;
+    framePostProcess(fb, st);
+    return B200_NO_ERROR;
   } catch (const Error &ex) {
     return fail(ex.code, ex.what());
+  } catch (const std::bad_alloc &) {
+    return fail(B200_OUT_OF_MEMORY, "host out of memory");
+  } catch (const std::exception &ex) {
+    return fail(B200_UNKNOWN_ERROR, ex.what());
   }
-  e = launchRenderPT(dev->tables, sc->view(), makeCamera(*camera), dev->filter(p->pixelFilter), d,
-                     reinterpret_cast<const MaterialD *>(base + OFF_MATERIALS), sc->dLights, sc->dLightCdf,
-                     reinterpret_cast<const AlbedoTablesD *>(base + OFF_ALBEDO), fb->view(), p->collectStats != 0,
-                     base + OFF_WORKSPACE, WORKSPACE_BYTES, st);
-  if (e != cudaSuccess) return fail(B200_UNKNOWN_ERROR, std::string("path tracer launch: ") + cudaGetErrorString(e));
-  fb->frameID++;
-  try {
-    framePostProcess(fb, st);
-  } catch (const Error &er) {
-    return fail(er.code, er.what());
-  }
-  return B200_NO_ERROR;
 }
 
 }  // extern "C"

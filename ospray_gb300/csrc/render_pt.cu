@@ -53,7 +53,7 @@ struct __align__(16) PathRec {
   float4 org;   // ray origin, first-hit depth z
   float4 dir;   // ray direction, last vertex BSDF pdf
   float4 thr;   // throughput, alpha
-  float4 con;   // contribution, (unused)
+  float4 con;   // contribution, medium id (bits)
   float4 lastP; // previous vertex position, (unused)
   float4 lastN; // previous vertex shading normal, (unused)
   uint4 meta;   // LDSampler scramble, flags, first-hit primID, geomID
@@ -73,8 +73,11 @@ struct __align__(16) ShadowRec {
 };
 
 // flags: depth 0..7, straightPath bit 8, firstBounceLight bit 9, ended bit 10,
-// lastNLS 16..31
-constexpr uint32_t F_STRAIGHT = 1u << 8, F_FIRST = 1u << 9, F_ENDED = 1u << 10;
+// (11, 12 below), auxiliary data recorded bit 13, scattering events 14..20,
+// lastNLS 21..31
+constexpr uint32_t F_STRAIGHT = 1u << 8, F_FIRST = 1u << 9, F_ENDED = 1u << 10, F_AUXDONE = 1u << 13;
+constexpr int F_SCATTER_SHIFT = 14, F_NLS_SHIFT = 21;
+constexpr uint32_t F_SCATTER_MAX = 127u, F_NLS_MAX = 2047u;
 
 struct Workspace {
   PathRec *paths;
@@ -130,7 +133,7 @@ B200_D PathRec genPT(const PtCtx &c, const CameraD &cam, const PixelFilterD &pf,
   r.org = make_float4(ray.org.x, ray.org.y, ray.org.z, INFINITY);
   r.dir = make_float4(ray.dir.x, ray.dir.y, ray.dir.z, INFINITY);
   r.thr = make_float4(1.f, 1.f, 1.f, 1.f);
-  r.con = make_float4(0.f, 0.f, 0.f, 0.f);
+  r.con = make_float4(0.f, 0.f, 0.f, __uint_as_float(MEDIUM_VACUUM));  // w: the medium the path travels in
   r.lastP = make_float4(ray.org.x, ray.org.y, ray.org.z, ray.tnear);
   r.lastN = make_float4(ray.dir.x, ray.dir.y, ray.dir.z, 0.f);
   r.meta = make_uint4(ld.scramble, F_STRAIGHT | F_FIRST, INVALID_ID, INVALID_ID);
@@ -177,15 +180,31 @@ __global__ void k_pt_generate(PtCtx c, CameraD cam, PixelFilterD pf, FrameInfo f
   ws.paths[p] = r;
 }
 
+// What the transparent-shadow trace needs of the materials
+// (TransparentShadow.ispc:18-85): the material list, the renderer's
+// minContribution and its maxPathLength as the limit of surfaces crossed.
+struct ShadowMatD {
+  const MaterialD *mats;
+  int nmats, maxDepth;
+  float minContribution;
+};
+
 // Persistent any/closest-hit tracing over a queue with per-lane dynamic
 // fetch: whenever lanes of a warp finish their rays, the warp takes that many
 // new ones with one atomic, so no lane idles while work remains.
 // In a batch (BATCH) every ray traverses its own request's scene.
-template <bool SHADOW, bool STATS, bool BATCH>
+// TRANSP (shadow rays of scenes with transparent materials): each shadow ray
+// is a loop of closest-hit queries; at every hit its contribution is
+// multiplied by the material's transparency (and the medium's attenuation
+// over the segment), and the lane restarts the same ray just past the hit,
+// until it reaches the light or is blocked.  The shadow record's fourth
+// contribution word then carries the path's medium (tnear is 0).
+template <bool SHADOW, bool STATS, bool BATCH, bool TRANSP = false>
 __global__ void __launch_bounds__(TRACE_BLOCK, BATCH ? B200_BATCH_TRACE_MINBLOCKS : B200_TRACE_MINBLOCKS) k_trace_queue(Scene sc, Workspace ws, const uint32_t *queue,
                                                             const uint32_t *count, uint32_t *fetch,
-                                                            const ReqD *reqs) {
+                                                            const ReqD *reqs, ShadowMatD sm) {
   static_assert(!(BATCH && STATS), "batched traversal keeps no per-scene statistics");
+  static_assert(!TRANSP || (SHADOW && !BATCH), "transparent shadows: single-request shadow rays only");
   const int lane = threadIdx.x & 31;
   const uint32_t n = *(volatile const uint32_t *)count;
   TraceStats ts = {0, 0, 0, 0};
@@ -195,6 +214,11 @@ __global__ void __launch_bounds__(TRACE_BLOCK, BATCH ? B200_BATCH_TRACE_MINBLOCK
   TraceSpill spill;
   bool has = false, exhausted = false;
   uint32_t item = 0;
+  // transparent shadows: the ray, its remaining contribution, medium and crossing budget
+  Ray tray;
+  V3 tcon = splat(0.f);
+  uint32_t tmed = MEDIUM_VACUUM;
+  int tdepth = 0;
   for (int guard = 0; guard < (1 << 30); guard++) {
     const unsigned need = __ballot_sync(0xffffffffu, !has && !exhausted);
     if (need) {
@@ -207,12 +231,18 @@ __global__ void __launch_bounds__(TRACE_BLOCK, BATCH ? B200_BATCH_TRACE_MINBLOCK
         if (idx < n) {
           Ray r;
           if (SHADOW) {
-            const ShadowRec s = ws.shadows[idx];
+            item = queue ? __ldg(queue + idx) : idx;  // a shadow queue, when given, holds record indices
+            const ShadowRec s = ws.shadows[item];
             r.org = mk(s.a.x, s.a.y, s.a.z);
-            r.tnear = s.c.w;
+            r.tnear = TRANSP ? 0.f : s.c.w;
             r.dir = mk(s.b.x, s.b.y, s.b.z);
             r.tfar = s.a.w;
-            item = idx;
+            if (TRANSP) {
+              tray = r;
+              tcon = mk(s.c.x, s.c.y, s.c.z);
+              tmed = __float_as_uint(s.c.w);
+              tdepth = sm.maxDepth;
+            }
             if (BATCH) bsc = reqs[ws.paths[__float_as_uint(s.b.w)].meta2.y].c.sc;
           } else {
             item = queue ? __ldg(queue + idx) : idx;
@@ -223,7 +253,7 @@ __global__ void __launch_bounds__(TRACE_BLOCK, BATCH ? B200_BATCH_TRACE_MINBLOCK
             r.tfar = INFINITY;
             if (BATCH) bsc = reqs[ws.paths[item].meta2.y].c.sc;
           }
-          tv.init(S, r, SHADOW, &spill);
+          tv.init(S, r, SHADOW && !TRANSP, &spill);
           if (STATS) ts.rays++;
           has = true;
         } else {
@@ -233,23 +263,51 @@ __global__ void __launch_bounds__(TRACE_BLOCK, BATCH ? B200_BATCH_TRACE_MINBLOCK
     }
     if (!__any_sync(0xffffffffu, has)) break;
     if (has && tv.step<STATS>(S, &ts)) {
-      if (SHADOW) {
+      if (TRANSP) {
+        bool done = true;
         if (!tv.found) {
-          const ShadowRec s = ws.shadows[item];
-          float *con = &ws.paths[__float_as_uint(s.b.w)].con.x;
-          atomicAdd(con + 0, s.c.x);
-          atomicAdd(con + 1, s.c.y);
-          atomicAdd(con + 2, s.c.z);
+          float *con = &ws.paths[__float_as_uint(ws.shadows[item].b.w)].con.x;
+          atomicAdd(con + 0, tcon.x);
+          atomicAdd(con + 1, tcon.y);
+          atomicAdd(con + 2, tcon.z);
+        } else {
+          tv.finish(S);
+          const DG dg = postIntersect(S, tray, tv.hit);
+          const uint32_t mi = S.entries[tv.hit.entry].materialID;
+          const bool hasMat = mi < uint32_t(sm.nmats);
+          tcon = tcon * (hasMat ? materialTransparency(sm.mats, mi, tray.dir, dg.Ns, tmed) : splat(0.f));
+          const MediumD md = mediumOf(sm.mats, tmed);
+          if (md.att.x != 0.f || md.att.y != 0.f || md.att.z != 0.f)
+            tcon = tcon * expV(md.att * (tv.hit.t - tray.tnear));
+          if (!(maxc(tcon) <= sm.minContribution || --tdepth <= 0)) {
+            if (hasMat && sm.mats[mi].kind == MAT_GLASS)
+              tmed = glassFromOutside(sm.mats, mi, tmed) ? 2u * mi : 2u * mi + 1u;
+            tray.tnear = tv.hit.t + dg.epsilon;
+            tv.init(S, tray, false, &spill);  // the same ray again, past this surface
+            if (STATS) ts.rays++;
+            done = false;
+          }
         }
+        has = !done;
       } else {
-        tv.finish(S);
-        HitBuf hb;
-        hb.a = make_float4(tv.hit.t, __uint_as_float(tv.hit.primID), __uint_as_float(tv.hit.entry),
-                           tv.found ? 1.f : 0.f);
-        hb.b = make_float4(tv.hit.Ng.x, tv.hit.Ng.y, tv.hit.Ng.z, 0.f);
-        ws.hits[item] = hb;
+        if (SHADOW) {
+          if (!tv.found) {
+            const ShadowRec s = ws.shadows[item];
+            float *con = &ws.paths[__float_as_uint(s.b.w)].con.x;
+            atomicAdd(con + 0, s.c.x);
+            atomicAdd(con + 1, s.c.y);
+            atomicAdd(con + 2, s.c.z);
+          }
+        } else {
+          tv.finish(S);
+          HitBuf hb;
+          hb.a = make_float4(tv.hit.t, __uint_as_float(tv.hit.primID), __uint_as_float(tv.hit.entry),
+                             tv.found ? 1.f : 0.f);
+          hb.b = make_float4(tv.hit.Ng.x, tv.hit.Ng.y, tv.hit.Ng.z, 0.f);
+          ws.hits[item] = hb;
+        }
+        has = false;
       }
-      has = false;
     }
   }
   if (STATS) flushStats(sc, ts);
@@ -317,13 +375,204 @@ B200_D void aoShade(const PtCtx &C, const AOParamsD &A, int W, PathRec &pr, cons
   pr.meta.y = flags;
 }
 
+// The mutable state of a path between bounces (PathState,
+// render/pathtracer/PathStructs.ih), unpacked from its record.
+struct PathVars {
+  V3 throughput, contribution;
+  int depth, scatter, lastNLS;
+  bool straightPath, firstBounceLight, diffuseSeen, auxDone, cont;
+  uint32_t medium;
+};
+
+// transparentShadow (render/pathtracer/TransparentShadow.ispc:18-85) for one
+// shadow ray traced in place: closest hits in turn, each multiplying the
+// contribution by its material's transparency (and the medium's Beer
+// attenuation over the segment), until the ray reaches tfar (unblocked) or
+// the contribution drops to minContribution or maxPathLength surfaces were
+// crossed.  Opaque scenes use one any-hit query.
+template <bool TRANSP>
+B200_D V3 shadowInPlace(const PtCtx &C, Ray sr, V3 contrib, uint32_t medium) {
+  HitRec h;
+  if (!TRANSP) return traceRay<false>(C.sc, sr, h, true, true, nullptr) ? splat(0.f) : contrib;
+  const float tfar = sr.tfar;
+  int maxDepth = C.p.maxPathLength;
+  for (int guard = 0; guard < 4096; guard++) {
+    if (!traceRay<false>(C.sc, sr, h, false, true, nullptr)) return contrib;
+    const Entry &e = C.sc.entries[h.entry];
+    h.geomID = e.geomID;
+    h.instID = e.instID;
+    const DG dg = postIntersect(C.sc, sr, h);
+    const uint32_t mi = e.materialID;
+    const bool hasMat = mi < uint32_t(C.p.numMaterials);
+    contrib = contrib * (hasMat ? materialTransparency(C.mats, mi, sr.dir, dg.Ns, medium) : splat(0.f));
+    const MediumD md = mediumOf(C.mats, medium);
+    if (md.att.x != 0.f || md.att.y != 0.f || md.att.z != 0.f) contrib = contrib * expV(md.att * (h.t - sr.tnear));
+    if (maxc(contrib) <= C.p.minContribution || --maxDepth <= 0) return splat(0.f);
+    if (hasMat && C.mats[mi].kind == MAT_GLASS)
+      medium = glassFromOutside(C.mats, mi, medium) ? 2u * mi : 2u * mi + 1u;
+    sr.tnear = h.t + dg.epsilon;
+    sr.tfar = tfar;
+  }
+  return splat(0.f);
+}
+
+// The shading part of one samplePath iteration at a surface with BSDF `bsdf`
+// (render/pathtracer/PathSampler.ispc:290-411): auxiliary data, next-event
+// estimation at smooth vertices (shadow rays to the shadow queue), BSDF
+// sampling with the same-side check, Russian roulette, Beer attenuation in
+// the current medium, medium change on transmission, and the continuation
+// ray.  A specular transmission keeps the previous vertex for MIS.
+template <class B, bool NRC, bool ALLMAT>
+B200_D void scatterSurface(const PtCtx &C, const B &bsdf, const MaterialD &mat, uint32_t mi, const DG &dg,
+                           const Ray &ray, float t, V3 wo, PathRec &pr, PathVars &v, uint32_t p, ShadowRec *sh,
+                           int &nsh, const NrcFrameD &nf) {
+  const int nl = C.p.numLights;
+  const bool transparentShadows = ALLMAT && C.p.transparentShadows != 0;
+  if (bsdf.smooth && v.scatter == 0 && !v.auxDone && C.aux) {
+    // updateAuxilliaryData (render/pathtracer/PathTracerUtil.ih:48-60) at the
+    // first smooth vertex: throughput x BSDF albedo and x shading normal
+    float *a = C.aux + size_t(p / uint32_t(C.p.spp)) * 6;
+    const V3 an = v.throughput * bsdf.N(), aa = v.throughput * bsdf.albedoV();
+    atomicAdd(a + 0, an.x);
+    atomicAdd(a + 1, an.y);
+    atomicAdd(a + 2, an.z);
+    atomicAdd(a + 3, aa.x);
+    atomicAdd(a + 4, aa.y);
+    atomicAdd(a + 5, aa.z);
+    v.auxDone = true;
+  }
+  bool cached = false;
+  if (NRC) {
+    if (pr.meta2.w != INVALID_ID) {  // training path: record the vertex
+      float *q = nf.trainVerts + (size_t(pr.meta2.w) * nf.maxLen1 + v.depth) * 20;
+      const float rv[20] = {dg.P.x, dg.P.y, dg.P.z, wo.x, wo.y, wo.z, dg.Ns.x, dg.Ns.y, dg.Ns.z,
+                            mat.roughness, mat.r, mat.g, mat.b, v.throughput.x, v.throughput.y, v.throughput.z,
+                            v.contribution.x, v.contribution.y, v.contribution.z, __uint_as_float(p)};
+      for (int k = 0; k < 20; k++) q[k] = rv[k];
+    } else if (nf.useCache && v.depth >= 1 && v.diffuseSeen && bsdf.smooth) {  // end in the cache
+      const uint32_t qn = atomicAdd(nf.counters, 1u);
+      float *q = nf.queries + size_t(qn) * 16;
+      const float qv[16] = {dg.P.x, dg.P.y, dg.P.z, wo.x, wo.y, wo.z, dg.Ns.x, dg.Ns.y, dg.Ns.z,
+                            mat.roughness, mat.r, mat.g, mat.b, v.throughput.x, v.throughput.y, v.throughput.z};
+      for (int k = 0; k < 16; k++) q[k] = qv[k];
+      nf.qpath[qn] = p;
+      cached = true;
+    }
+  }
+  if (cached) return;
+  // LDSampler of this path at its current group; advanced unconditionally
+  const uint32_t sampleID = pr.meta2.z;
+  LDSampler ld;
+  ld.init(C.T, pr.meta.x, sampleID, sampleID * uint32_t(C.p.nFirst), 16, 16);
+  ld.nextGroup();
+  int numLS = 0;
+  if (bsdf.smooth) {
+    numLS = v.firstBounceLight ? C.p.nFirst : C.p.nIndirect;
+    for (int i = 0; i < numLS; i++) {
+      float ss;
+      const float2 sl = ld.get3LightSamples(uint32_t(i), numLS > 1, ss);
+      int first = 0, len = nl;
+      while (len > 0) {
+        const int half = len >> 1, mid = first + half;
+        if (ss < __ldg(C.lightCdf + mid)) {
+          len = half;
+        } else {
+          first = mid + 1;
+          len -= half + 1;
+        }
+      }
+      first = min(first, nl - 1);
+      const float prob = __ldg(C.lightCdf + first) - (first == 0 ? 0.f : __ldg(C.lightCdf + first - 1));
+      const float selProb = prob * float(numLS);
+      LightSampleD ls = sampleLight(C.lights[first], dg.P, dg.Ng, dg.Ns, sl.x, sl.y);
+      ls.weight = ls.weight * (1.f / selProb);
+      ls.pdf *= selProb;
+      if (maxc(ls.weight) <= 0.f || ls.pdf <= 0.f) continue;
+      const BsdfEval fe = bsdf.eval(wo, ls.dir, C.AT);
+      if (maxc(fe.value) <= 0.f) continue;
+      V3 org = dg.P;
+      if (fdot(dg.Ng, ls.dir) < 0.f) org = org - (2.f * dg.epsilon) * dg.Ng;
+      const V3 cval = v.throughput * fe.value * ls.weight * misH(ls.pdf, fe.pdf);
+      if (nsh < 2) {
+        sh[nsh].a = make_float4(org.x, org.y, org.z, ls.dist);
+        sh[nsh].b = make_float4(ls.dir.x, ls.dir.y, ls.dir.z, __uint_as_float(p));
+        // transparent shadows carry the path's medium in place of tnear (0)
+        sh[nsh].c = make_float4(cval.x, cval.y, cval.z, transparentShadows ? __uint_as_float(v.medium) : 0.f);
+        nsh++;
+      } else {
+        // beyond two light samples per vertex: trace in place
+        Ray sr;
+        sr.org = org;
+        sr.tnear = 0.f;
+        sr.dir = ls.dir;
+        sr.tfar = ls.dist;
+        v.contribution = v.contribution + (transparentShadows ? shadowInPlace<ALLMAT>(C, sr, cval, v.medium)
+                                                              : shadowInPlace<false>(C, sr, cval, v.medium));
+      }
+    }
+    v.firstBounceLight = false;
+  }
+  float ss;
+  uint32_t uu3;
+  const float2 sb = ld.getNext4Samples(ss, uu3);
+  BsdfSample fs = bsdf.sample(wo, sb.x, sb.y, ss, C.AT);
+  // consistent side of the surface (light leaks)
+  const bool sameSide = fdot(fs.wi, dg.Ng) >= 0.f;
+  if (sameSide != ((fs.type & ST_REFLECTION) != 0)) fs.weight = splat(0.f);
+  bool cont = !(maxc(fs.weight) <= 0.f || fs.pdf <= 0.f);
+  if (cont) {
+    v.throughput = v.throughput * fs.weight;
+    if (v.depth >= C.p.roulettePathLength) {
+      const float rr = ld.finalizeDim3(uu3);
+      const float contProb = fminf(maxc(v.throughput), 0.95f);
+      if (rr > contProb)
+        cont = false;
+      else
+        v.throughput = v.throughput * (1.f / contProb);
+    }
+  }
+  if (cont) {
+    V3 org = dg.P;
+    if (ALLMAT) {  // (opaque principled materials neither change nor attenuate the medium)
+      // Beer's law over the segment that reached this vertex
+      const MediumD md = mediumOf(C.mats, v.medium);
+      if (fminf(fminf(md.att.x, md.att.y), md.att.z) < 0.f) v.throughput = v.throughput * expV(md.att * t);
+    }
+    if (ALLMAT && (fs.type & ST_TRANSMISSION)) {
+      org = org - (2.f * dg.epsilon) * dg.Ng;
+      if (mat.kind == MAT_GLASS) v.medium = glassFromOutside(C.mats, mi, v.medium) ? 2u * mi : 2u * mi + 1u;
+    }
+    // a rough or non-metallic vertex counts as the path's diffuse bounce
+    if (mat.kind == MAT_PRINCIPLED ? (mat.metallic < 0.5f || mat.roughness > 0.3f) : (fs.type & ST_DIFFUSE_R) != 0)
+      v.diffuseSeen = true;
+    if (!(ray.dir.x == fs.wi.x && ray.dir.y == fs.wi.y && ray.dir.z == fs.wi.z)) v.straightPath = false;
+    if (fs.type & ~ST_SPEC_T) {  // the new last vertex for MIS
+      pr.lastP = make_float4(dg.P.x, dg.P.y, dg.P.z, 0.f);
+      pr.lastN = make_float4(dg.Ns.x, dg.Ns.y, dg.Ns.z, 0.f);
+      pr.dir.w = fs.pdf;
+      v.lastNLS = numLS;
+    }
+    pr.org = make_float4(org.x, org.y, org.z, pr.org.w);
+    pr.dir = make_float4(fs.wi.x, fs.wi.y, fs.wi.z, pr.dir.w);
+    v.depth++;
+    if (fs.type & ST_SMOOTH) v.scatter++;
+    if (!(maxc(v.throughput) > C.p.minContribution)) cont = false;
+  }
+  pr.meta.x = ld.scramble;
+  v.cont = cont;
+}
+
 // One bounce of samplePath for every queued path (render/pathtracer/
 // PathSampler.ispc:109-415): environment and virtual lights, postIntersect,
-// principled BSDF, NEE light samples (to the shadow queue), BSDF sample and
-// Russian roulette (to the next queue).
+// the material's BSDF, NEE light samples (to the shadow queue), BSDF sample
+// and Russian roulette (to the next queue).
 // NRC: the radiance-cache mode (training paths record their vertices; the
 // others end in a cache query at their first vertex after a diffuse bounce).
-template <bool BATCH, bool NRC>
+// ALLMAT: the material list has types other than principled (obj, metal,
+// glass, thin glass) or lets shadow rays through; without it the kernel
+// carries the opaque principled BSDF only (a smaller kernel for the common
+// case).
+template <bool BATCH, bool NRC, bool ALLMAT = true>
 #ifndef B200_SHADE_MINBLOCKS
 #define B200_SHADE_MINBLOCKS 2
 #endif
@@ -353,12 +602,19 @@ __global__ void __launch_bounds__(128, B200_SHADE_MINBLOCKS) k_pt_shade(PtCtx c,
         ws.paths[p] = pr;
       } else {
       const int nl = C.p.numLights;
-      uint32_t flags = pr.meta.y;
-      bool diffuseSeen = (flags & F_DIFFUSE) != 0;
-      int depth = int(flags & 0xffu);
-      bool straightPath = (flags & F_STRAIGHT) != 0, firstBounceLight = (flags & F_FIRST) != 0;
-      int lastNLS = int(flags >> 16);
-      V3 throughput = mk(pr.thr.x, pr.thr.y, pr.thr.z), contribution = mk(pr.con.x, pr.con.y, pr.con.z);
+      const uint32_t flags = pr.meta.y;
+      PathVars v;
+      v.diffuseSeen = (flags & F_DIFFUSE) != 0;
+      v.auxDone = (flags & F_AUXDONE) != 0;
+      v.depth = int(flags & 0xffu);
+      v.scatter = int((flags >> F_SCATTER_SHIFT) & F_SCATTER_MAX);
+      v.straightPath = (flags & F_STRAIGHT) != 0;
+      v.firstBounceLight = (flags & F_FIRST) != 0;
+      v.lastNLS = int(flags >> F_NLS_SHIFT);
+      v.throughput = mk(pr.thr.x, pr.thr.y, pr.thr.z);
+      v.contribution = mk(pr.con.x, pr.con.y, pr.con.z);
+      v.medium = __float_as_uint(pr.con.w);
+      v.cont = false;
       float alpha = pr.thr.w;
       Ray ray;
       ray.org = mk(pr.org.x, pr.org.y, pr.org.z);
@@ -370,10 +626,10 @@ __global__ void __launch_bounds__(128, B200_SHADE_MINBLOCKS) k_pt_shade(PtCtx c,
       const bool hit = hb.a.w != 0.f;
       const float t = hit ? hb.a.x : INFINITY;
       const V3 wo = -ray.dir;
-      if (depth == 0) pr.org.w = t;
-      if (!hit && straightPath) {
-        alpha -= luminance(throughput) * (1.f - C.p.bg[3]);
-        contribution = contribution + throughput * mk(C.p.bg[0], C.p.bg[1], C.p.bg[2]);
+      if (v.depth == 0) pr.org.w = t;
+      if (!hit && v.straightPath) {
+        alpha -= luminance(v.throughput) * (1.f - C.p.bg[3]);
+        v.contribution = v.contribution + v.throughput * mk(C.p.bg[0], C.p.bg[1], C.p.bg[2]);
       }
       if (nl > 0) {  // evaluateVirtualLights
         const V3 d0 = lastP - ray.org;
@@ -383,19 +639,19 @@ __global__ void __launch_bounds__(128, B200_SHADE_MINBLOCKS) k_pt_shade(PtCtx c,
           const V3 d1 = lastP - (ray.org + t * ray.dir);
           hiD = sqrtf(fdot(d1, d1));
         }
-        const float selPdf = float(lastNLS) / float(nl);
+        const float selPdf = float(v.lastNLS) / float(nl);
         for (int i = 0; i < nl; i++) {
           const LightD &L = C.lights[i];
-          if (straightPath && !L.visible) continue;
+          if (v.straightPath && !L.visible) continue;
           float lpdf;
           const V3 rad = evalLight(L, lastP, lastNs, ray.dir, lo, hiD, lpdf);
           if (maxc(rad) > 0.f) {
             const float w = selPdf != 0.f ? misH(lastPdf, selPdf * lpdf) : 1.f;
-            contribution = contribution + throughput * rad * w;
+            v.contribution = v.contribution + v.throughput * rad * w;
           }
         }
       }
-      if (hit && depth < C.p.maxPathLength) {
+      if (hit && v.depth < C.p.maxPathLength) {
         HitRec h;
         h.t = t;
         h.primID = __float_as_uint(hb.a.y);
@@ -405,141 +661,77 @@ __global__ void __launch_bounds__(128, B200_SHADE_MINBLOCKS) k_pt_shade(PtCtx c,
         h.geomID = e.geomID;
         h.instID = e.instID;
         const DG dg = postIntersect(C.sc, ray, h);
-        if (depth == 0) {
+        if (v.depth == 0) {
           pr.meta.z = h.primID;
           pr.meta.w = h.geomID;
           pr.meta2.x = h.instID;
         }
-        if (depth < C.p.maxScatteringEvents && e.materialID < uint32_t(C.p.numMaterials)) {
-          V3 U = e.identity ? mk(1.f, 0.f, 0.f) : mk(e.xfm.m[0], e.xfm.m[4], e.xfm.m[8]);
-          U = fnormalize(U);
-          const V3 Vv = fcross(dg.Ns, U);
-          V3 fxv, fyv;
-          if (fdot(Vv, Vv) > 0.f) {
-            fyv = fnormalize(Vv);
-            fxv = fcross(fyv, dg.Ns);
-          } else {
-            frame(dg.Ns, fxv, fyv);
-          }
-          Principled bsdf;
-          const MaterialD &mat = C.mats[e.materialID];
-          bsdf.init(mat, fxv, fyv, dg.Ns, C.AT);
-          if (depth == 0 && C.aux && bsdf.impSum > 0.f) {
-            // updateAuxilliaryData (render/pathtracer/PathTracerUtil.ih:48-60) at the
-            // first (smooth) vertex: throughput x BSDF albedo and x shading normal
-            float *a = C.aux + size_t(p / uint32_t(C.p.spp)) * 6;
-            const V3 an = throughput * bsdf.N, aa = throughput * bsdf.albedo;
-            atomicAdd(a + 0, an.x);
-            atomicAdd(a + 1, an.y);
-            atomicAdd(a + 2, an.z);
-            atomicAdd(a + 3, aa.x);
-            atomicAdd(a + 4, aa.y);
-            atomicAdd(a + 5, aa.z);
-          }
-          bool cached = false;
-          if (NRC) {
-            if (pr.meta2.w != INVALID_ID) {  // training path: record the vertex
-              float *v = nf.trainVerts + (size_t(pr.meta2.w) * nf.maxLen1 + depth) * 20;
-              const float rv[20] = {dg.P.x, dg.P.y, dg.P.z, wo.x, wo.y, wo.z, dg.Ns.x, dg.Ns.y, dg.Ns.z,
-                                    mat.roughness, mat.r, mat.g, mat.b, throughput.x, throughput.y, throughput.z,
-                                    contribution.x, contribution.y, contribution.z, __uint_as_float(p)};
-              for (int k = 0; k < 20; k++) v[k] = rv[k];
-            } else if (nf.useCache && depth >= 1 && diffuseSeen) {  // end in the cache
-              const uint32_t qn = atomicAdd(nf.counters, 1u);
-              float *q = nf.queries + size_t(qn) * 16;
-              const float qv[16] = {dg.P.x, dg.P.y, dg.P.z, wo.x, wo.y, wo.z, dg.Ns.x, dg.Ns.y, dg.Ns.z,
-                                    mat.roughness, mat.r, mat.g, mat.b, throughput.x, throughput.y, throughput.z};
-              for (int k = 0; k < 16; k++) q[k] = qv[k];
-              nf.qpath[qn] = p;
-              cached = true;
-            }
-          }
-          if (!cached && bsdf.impSum != 0.f) {
-            // LDSampler of this path at its current group
-            const uint32_t sampleID = pr.meta2.z;
-            LDSampler ld;
-            ld.init(C.T, pr.meta.x, sampleID, sampleID * uint32_t(C.p.nFirst), 16, 16);
-            ld.nextGroup();
-            const int numLS = firstBounceLight ? C.p.nFirst : C.p.nIndirect;
-            for (int i = 0; i < numLS; i++) {
-              float ss;
-              const float2 sl = ld.get3LightSamples(uint32_t(i), numLS > 1, ss);
-              int first = 0, len = nl;
-              while (len > 0) {
-                const int half = len >> 1, mid = first + half;
-                if (ss < __ldg(C.lightCdf + mid)) {
-                  len = half;
-                } else {
-                  first = mid + 1;
-                  len -= half + 1;
-                }
-              }
-              first = min(first, nl - 1);
-              const float prob = __ldg(C.lightCdf + first) - (first == 0 ? 0.f : __ldg(C.lightCdf + first - 1));
-              const float selProb = prob * float(numLS);
-              LightSampleD ls = sampleLight(C.lights[first], dg.P, dg.Ng, dg.Ns, sl.x, sl.y);
-              ls.weight = ls.weight * (1.f / selProb);
-              ls.pdf *= selProb;
-              if (maxc(ls.weight) <= 0.f || ls.pdf <= 0.f) continue;
-              const BsdfEval fe = bsdf.eval(wo, ls.dir, C.AT);
-              if (maxc(fe.value) <= 0.f) continue;
-              V3 org = dg.P;
-              if (fdot(dg.Ng, ls.dir) < 0.f) org = org - (2.f * dg.epsilon) * dg.Ng;
-              const V3 cval = throughput * fe.value * ls.weight * misH(ls.pdf, fe.pdf);
-              if (nsh < 2) {
-                sh[nsh].a = make_float4(org.x, org.y, org.z, ls.dist);
-                sh[nsh].b = make_float4(ls.dir.x, ls.dir.y, ls.dir.z, __uint_as_float(p));
-                sh[nsh].c = make_float4(cval.x, cval.y, cval.z, 0.f);
-                nsh++;
+        const uint32_t mi = e.materialID;
+        if (v.scatter < C.p.maxScatteringEvents && mi < uint32_t(C.p.numMaterials)) {
+          const MaterialD &mat = C.mats[mi];
+          switch (ALLMAT ? mat.kind : MAT_PRINCIPLED) {
+            case MAT_OBJ:
+            case MAT_PRINCIPLED: {
+              // makeShadingFrame with dPds = the instance's x axis
+              V3 U = e.identity ? mk(1.f, 0.f, 0.f) : mk(e.xfm.m[0], e.xfm.m[4], e.xfm.m[8]);
+              U = fnormalize(U);
+              const V3 Vv = fcross(dg.Ns, U);
+              V3 fxv, fyv;
+              if (fdot(Vv, Vv) > 0.f) {
+                fyv = fnormalize(Vv);
+                fxv = fcross(fyv, dg.Ns);
               } else {
-                // beyond two light samples per vertex: trace in place
-                Ray sr;
-                sr.org = org;
-                sr.tnear = 0.f;
-                sr.dir = ls.dir;
-                sr.tfar = ls.dist;
-                HitRec shh;
-                if (!traceRay<false>(C.sc, sr, shh, true, true, nullptr)) contribution = contribution + cval;
+                frame(dg.Ns, fxv, fyv);
               }
-            }
-            lastNLS = numLS;
-            firstBounceLight = false;
-            float ss;
-            uint32_t uu3;
-            const float2 sb = ld.getNext4Samples(ss, uu3);
-            BsdfSample fs = bsdf.sample(wo, sb.x, sb.y, ss, C.AT);
-            if (fdot(fs.wi, dg.Ng) < 0.f) fs.weight = splat(0.f);  // reflection lobes only
-            cont = !(maxc(fs.weight) <= 0.f || fs.pdf <= 0.f);
-            if (cont) {
-              throughput = throughput * fs.weight;
-              if (depth >= C.p.roulettePathLength) {
-                const float rr = ld.finalizeDim3(uu3);
-                const float contProb = fminf(maxc(throughput), 0.95f);
-                if (rr > contProb)
-                  cont = false;
-                else
-                  throughput = throughput * (1.f / contProb);
+              if (ALLMAT && mat.kind == MAT_OBJ) {
+                ObjBsdf b;
+                b.init(mat, fxv, fyv, dg.Ns);
+                scatterSurface<ObjBsdf, NRC, ALLMAT>(C, b, mat, mi, dg, ray, t, wo, pr, v, p, sh, nsh, nf);
+              } else {
+                PrincipledBsdfT<ALLMAT> b;
+                b.init(mat, fxv, fyv, dg.Ns, C.AT);
+                scatterSurface<PrincipledBsdfT<ALLMAT>, NRC, ALLMAT>(C, b, mat, mi, dg, ray, t, wo, pr, v, p, sh, nsh,
+                                                                    nf);
               }
+              break;
             }
-            if (cont) {
-              // a rough or non-metallic vertex counts as the path's diffuse bounce
-              if (mat.metallic < 0.5f || mat.roughness > 0.3f) diffuseSeen = true;
-              if (!(ray.dir.x == fs.wi.x && ray.dir.y == fs.wi.y && ray.dir.z == fs.wi.z)) straightPath = false;
-              pr.lastP = make_float4(dg.P.x, dg.P.y, dg.P.z, 0.f);
-              pr.lastN = make_float4(dg.Ns.x, dg.Ns.y, dg.Ns.z, 0.f);
-              pr.org = make_float4(dg.P.x, dg.P.y, dg.P.z, pr.org.w);
-              pr.dir = make_float4(fs.wi.x, fs.wi.y, fs.wi.z, fs.pdf);
-              depth++;
-              if (!(maxc(throughput) > C.p.minContribution)) cont = false;
+            case MAT_METAL: {
+              if (ALLMAT) {
+                MetalBsdf b;
+                b.init(mat, dg.Ns);
+                scatterSurface<MetalBsdf, NRC, ALLMAT>(C, b, mat, mi, dg, ray, t, wo, pr, v, p, sh, nsh, nf);
+              }
+              break;
             }
-            pr.meta.x = ld.scramble;
+            case MAT_GLASS: {
+              if (ALLMAT) {
+                GlassBsdf b;
+                const bool out = glassFromOutside(C.mats, mi, v.medium);
+                b.init(out ? mat.iorOut * (1.f / mat.iorIn) : mat.iorIn * (1.f / mat.iorOut), dg.Ns, dg.Ng);
+                scatterSurface<GlassBsdf, NRC, ALLMAT>(C, b, mat, mi, dg, ray, t, wo, pr, v, p, sh, nsh, nf);
+              }
+              break;
+            }
+            case MAT_THINGLASS: {
+              if (ALLMAT) {
+                ThinGlassBsdf b;
+                b.init(mat, dg.Ns);
+                scatterSurface<ThinGlassBsdf, NRC, ALLMAT>(C, b, mat, mi, dg, ray, t, wo, pr, v, p, sh, nsh, nf);
+              }
+              break;
+            }
+            default:
+              break;
           }
+          cont = v.cont;
         }
       }
-      pr.thr = make_float4(throughput.x, throughput.y, throughput.z, alpha);
-      pr.con = make_float4(contribution.x, contribution.y, contribution.z, 0.f);
-      pr.meta.y = uint32_t(depth) | (straightPath ? F_STRAIGHT : 0u) | (firstBounceLight ? F_FIRST : 0u) |
-                  (cont ? 0u : F_ENDED) | (diffuseSeen ? F_DIFFUSE : 0u) | (uint32_t(lastNLS) << 16);
+      pr.thr = make_float4(v.throughput.x, v.throughput.y, v.throughput.z, alpha);
+      pr.con = make_float4(v.contribution.x, v.contribution.y, v.contribution.z, __uint_as_float(v.medium));
+      pr.meta.y = uint32_t(v.depth) | (v.straightPath ? F_STRAIGHT : 0u) | (v.firstBounceLight ? F_FIRST : 0u) |
+                  (cont ? 0u : F_ENDED) | (v.diffuseSeen ? F_DIFFUSE : 0u) | (v.auxDone ? F_AUXDONE : 0u) |
+                  (uint32_t(min(v.scatter, int(F_SCATTER_MAX))) << F_SCATTER_SHIFT) |
+                  (uint32_t(min(v.lastNLS, int(F_NLS_MAX))) << F_NLS_SHIFT);
       ws.paths[p] = pr;
       }
     }
@@ -893,14 +1085,19 @@ cudaError_t launchRenderPT(const SamplerTables *T, const Scene &sc, const Camera
   if (nrc && (stats || !nrcInfer)) return cudaErrorInvalidValue;
   Workspace ws = carveWorkspace(workspace, fi.npaths);
   PtCtx c = {T, sc, p, mats, lights, lightCdf, AT, fb.frameID, fb.aux};
-  static int traceBlocks = 0, shadowBlocks = 0, shadeBlocks = 0, shadeNrcBlocks = 0;
+  static int traceBlocks = 0, shadowBlocks = 0, transpBlocks = 0, shadeBlocks = 0, shadeAllBlocks = 0,
+             shadeNrcBlocks = 0;
   if (!traceBlocks) {
     traceBlocks = persistentBlocks((const void *)k_trace_queue<false, false, false>, TRACE_SMEM_BYTES);
     shadowBlocks = persistentBlocks((const void *)k_trace_queue<true, false, false>, TRACE_SMEM_BYTES);
-    shadeBlocks = persistentBlocks((const void *)k_pt_shade<false, false>, TRACE_SMEM_BYTES);
-    shadeNrcBlocks = persistentBlocks((const void *)k_pt_shade<false, true>, TRACE_SMEM_BYTES);
+    transpBlocks = persistentBlocks((const void *)k_trace_queue<true, false, false, true>, TRACE_SMEM_BYTES);
+    shadeBlocks = persistentBlocks((const void *)k_pt_shade<false, false, false>, TRACE_SMEM_BYTES);
+    shadeAllBlocks = persistentBlocks((const void *)k_pt_shade<false, false, true>, TRACE_SMEM_BYTES);
+    shadeNrcBlocks = persistentBlocks((const void *)k_pt_shade<false, true, false>, TRACE_SMEM_BYTES);
   }
   const NrcFrameD nf = nrc ? *nrc : NrcFrameD{};
+  const ShadowMatD sm = {mats, p.numMaterials, p.maxPathLength, p.minContribution};
+  const bool transp = p.transparentShadows != 0;
   if (nrc) {
     cudaMemsetAsync(nf.counters, 0, 16, st);
     cudaMemsetAsync(nf.trainVerts, 0xff, size_t(nf.trainSlots) * nf.maxLen1 * 20 * 4, st);
@@ -919,28 +1116,41 @@ cudaError_t launchRenderPT(const SamplerTables *T, const Scene &sc, const Camera
       KernelScope ks(kt, KK_TRACE_CLOSEST, st);
       if (stats)
         k_trace_queue<false, true, false><<<traceBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
-            sc, ws, qin, ws.counters + cin, ws.counters + 3, nullptr);
+            sc, ws, qin, ws.counters + cin, ws.counters + 3, nullptr, sm);
       else
         k_trace_queue<false, false, false><<<traceBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
-            sc, ws, qin, ws.counters + cin, ws.counters + 3, nullptr);
+            sc, ws, qin, ws.counters + cin, ws.counters + 3, nullptr, sm);
     }
     {
       KernelScope ks(kt, KK_SHADE, st);
-      if (nrc)
-        k_pt_shade<false, true><<<shadeNrcBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
+      if (nrc && p.allMaterials)
+        k_pt_shade<false, true, true><<<shadeNrcBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
+            c, ws, qin, ws.counters + cin, qs[cout], ws.counters + cout, ws.counters + 2, nullptr, nf);
+      else if (nrc)
+        k_pt_shade<false, true, false><<<shadeNrcBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
+            c, ws, qin, ws.counters + cin, qs[cout], ws.counters + cout, ws.counters + 2, nullptr, nf);
+      else if (p.allMaterials)
+        k_pt_shade<false, false, true><<<shadeAllBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
             c, ws, qin, ws.counters + cin, qs[cout], ws.counters + cout, ws.counters + 2, nullptr, nf);
       else
-        k_pt_shade<false, false><<<shadeBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
+        k_pt_shade<false, false, false><<<shadeBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
             c, ws, qin, ws.counters + cin, qs[cout], ws.counters + cout, ws.counters + 2, nullptr, nf);
     }
+    const uint32_t *sq = nullptr;  // shadow records in queue order
     {
       KernelScope ks(kt, KK_TRACE_SHADOW, st);
-      if (stats)
+      if (transp && stats)
+        k_trace_queue<true, true, false, true><<<transpBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
+            sc, ws, sq, ws.counters + 2, ws.counters + 4, nullptr, sm);
+      else if (transp)
+        k_trace_queue<true, false, false, true><<<transpBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
+            sc, ws, sq, ws.counters + 2, ws.counters + 4, nullptr, sm);
+      else if (stats)
         k_trace_queue<true, true, false><<<shadowBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
-            sc, ws, nullptr, ws.counters + 2, ws.counters + 4, nullptr);
+            sc, ws, sq, ws.counters + 2, ws.counters + 4, nullptr, sm);
       else
         k_trace_queue<true, false, false><<<shadowBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
-            sc, ws, nullptr, ws.counters + 2, ws.counters + 4, nullptr);
+            sc, ws, sq, ws.counters + 2, ws.counters + 4, nullptr, sm);
     }
     if (nrc && nf.useCache) {  // answer this bounce's cache queries
       nrcInfer(nrcCtx, st);
@@ -1042,11 +1252,11 @@ cudaError_t launchBatchWave(const void *dtables, size_t segTableOffset, const Ba
     k_bounce_reset<<<1, 1, 0, st>>>(ws.counters, cin, cout, rayCount);
     const uint32_t *qin = b == 0 ? nullptr : qs[cin];
     k_trace_queue<false, false, true><<<traceBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
-        noScene, ws, qin, ws.counters + cin, ws.counters + 3, reqs);
-    k_pt_shade<true, false><<<shadeBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
+        noScene, ws, qin, ws.counters + cin, ws.counters + 3, reqs, ShadowMatD{});
+    k_pt_shade<true, false, true><<<shadeBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
         noCtx, ws, qin, ws.counters + cin, qs[cout], ws.counters + cout, ws.counters + 2, reqs, NrcFrameD{});
     k_trace_queue<true, false, true><<<traceBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
-        noScene, ws, nullptr, ws.counters + 2, ws.counters + 4, reqs);
+        noScene, ws, nullptr, ws.counters + 2, ws.counters + 4, reqs, ShadowMatD{});
   }
   if (rayCount) k_count_tail<<<1, 1, 0, st>>>(ws.counters, rayCount);
   k_batch_finalize<<<unsigned((w.npix + 127) / 128), 128, 0, st>>>(reqs, segs, w.nseg, w.npix, ws);

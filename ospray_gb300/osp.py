@@ -144,7 +144,10 @@ class PathTracerApp:
     accumulation.  frame() is one ospRenderFrame + ospWait +
     ospMapFrameBuffer (colour copied to host memory) + ospUnmapFrameBuffer."""
 
-    def __init__(self, data, spp, max_path_length=5, roulette_path_length=3, width=None, height=None):
+    def __init__(self, data, spp, max_path_length=5, roulette_path_length=3, width=None, height=None,
+                 materials=None):
+        """materials: optional (OSPRay material type, {parameter: value}) per
+        sphere instance in place of the workload's principled ones."""
         L = lib()
         self.keep = []
         self.W = width or data["width"]
@@ -163,11 +166,22 @@ class PathTracerApp:
         insts = []
         n = len(data["xfm"])
         for k in range(n + 1):
-            mt = data["materials"][k]
-            mat = L.ospNewMaterial(b"principled")
-            set_param(mat, "baseColor", OSP_VEC3F, np.float32(mt[:3]))
-            set_param(mat, "roughness", OSP_FLOAT, np.float32(mt[3]))
-            set_param(mat, "metallic", OSP_FLOAT, np.float32(mt[4]))
+            if materials is not None and k < n:
+                typ, params = materials[k]
+                mat = L.ospNewMaterial(typ.encode())
+                if not mat:
+                    raise RuntimeError(L.ospDeviceGetLastErrorMsg(L.ospGetCurrentDevice()))
+                for key, val in params.items():
+                    if isinstance(val, (tuple, list)):
+                        set_param(mat, key, OSP_VEC3F, np.float32(val))
+                    else:
+                        set_param(mat, key, OSP_FLOAT, np.float32(val))
+            else:
+                mt = data["materials"][k]
+                mat = L.ospNewMaterial(b"principled")
+                set_param(mat, "baseColor", OSP_VEC3F, np.float32(mt[:3]))
+                set_param(mat, "roughness", OSP_FLOAT, np.float32(mt[3]))
+                set_param(mat, "metallic", OSP_FLOAT, np.float32(mt[4]))
             L.ospCommit(mat)
             model = _new_model(mesh if k < n else ground, mat)
             L.ospRelease(mat)

@@ -79,12 +79,45 @@ def pt_params(spp=1, max_path_length=20, roulette_path_length=5, max_scattering_
     return p
 
 
+# the reference's material parameter defaults per type (Principled.cpp:37-79,
+# OBJ.cpp:28-38, Metal.cpp:27-31 with math/spectrum.h's aluminium, Glass.cpp:27-38,
+# ThinGlass.cpp:27-33), in the 24-float order of or_pt_add_material2
+MATERIAL_TYPES = {"principled": 0, "obj": 1, "metal": 2, "glass": 3, "thinGlass": 4}
+_MAT_FIELDS = [("baseColor", 3), ("roughness", 1), ("metallic", 1), ("opacity", 1), ("ks", 3), ("ns", 1),
+               ("tf", 3), ("eta", 3), ("k", 3), ("attenuationColor", 3), ("attenuationDistance", 1),
+               ("thickness", 1)]
+_MAT_DEFAULTS = {
+    0: dict(baseColor=(0.8, 0.8, 0.8)),
+    1: dict(baseColor=(0.8, 0.8, 0.8), ns=10.0),
+    2: dict(eta=(1.47, 0.984, 0.602), k=(7.64, 6.55, 5.36), roughness=0.1),
+    3: dict(eta=(1.5, 1.0, 0.0)),
+    4: dict(eta=(1.5, 0.0, 0.0)),
+}
+
+
+def material_floats(m):
+    """(type, 24 floats) of a material dict, the reference's defaults filled in."""
+    t = MATERIAL_TYPES[m.get("type", "principled")]
+    vals = dict(opacity=1.0, attenuationColor=(1.0, 1.0, 1.0), attenuationDistance=1.0, thickness=1.0, ns=10.0)
+    vals.update(_MAT_DEFAULTS[t])
+    vals.update({k: v for k, v in m.items() if k != "type"})
+    out = []
+    for name, n in _MAT_FIELDS:
+        v = vals.get(name, (0.0,) * n if n > 1 else 0.0)
+        out.extend([float(x) for x in v] if n > 1 else [float(v)])
+    return t, np.asarray(out, np.float32)
+
+
 class PtWorld:
     """Materials and lights of the oracle path tracer."""
 
     def __init__(self, materials, lights):
         self.h = lib().or_pt_new()
         for m in materials:
+            if isinstance(m, dict):
+                t, f = material_floats(m)
+                lib().or_pt_add_material2(self.h, t, _p(f))
+                continue
             bc = np.asarray(m[:3], np.float32)
             lib().or_pt_add_material(self.h, _p(bc), float(m[3]), float(m[4]))
         for L in lights:
@@ -147,6 +180,7 @@ def lib():
         L.or_pt_new.restype = P
         L.or_pt_free.argtypes = [P]
         L.or_pt_add_material.argtypes = [P, P, F, F]
+        L.or_pt_add_material2.argtypes = [P, I, P]
         L.or_pt_add_quad_light.argtypes = [P, P, P, P, P]
         L.or_pt_add_ambient_light.argtypes = [P, P]
         L.or_pt_add_distant_light.argtypes = [P, P, F, P]
