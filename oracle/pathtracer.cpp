@@ -220,10 +220,9 @@ PathOut samplePath(const Ctx &c, LDSampler &ld, Ray ray) {
       out.instID = dg.instID;
     }
     if (depth >= c.p.maxPathLength || scatteringEvents >= c.p.maxScatteringEvents) break;
-    const InstanceEntry *e = &c.sc.entries[hit.entry];
     const MaterialParams *mat = materialOf(c, hit);
     if (!mat) break;  // no material: no BSDF
-    const SurfaceBSDF bsdf = makeBSDF(*mat, dg, e->identity ? v3(1, 0, 0) : e->xfm.l.vx, medium);
+    const SurfaceBSDF bsdf = makeBSDF(*mat, dg, dg.dPds, medium);
     ld.nextGroup();
     int numLS = 0;
     if (bsdf.smooth) {

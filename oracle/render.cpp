@@ -153,21 +153,26 @@ DG postIntersect(const Scene &s, const Ray &ray, const Hit &hit) {
   const InstanceEntry *e = &s.entries[hit.entry];
   const Geometry &g = s.geoms[e->geom];
   V3 Ng = hit.Ng, Ns = hit.Ng;
+  V3 dPds = v3(1.f, 0.f, 0.f);  // World.ih postIntersect default tangent
   float eps;
   if (g.type == 0 && g.boxFaces) {
     eps = 0.f;  // Boxes_postIntersect (geometry/Boxes.ispc) sets no geometry epsilon
   } else if (g.type == 0 && !g.quadIndex.empty()) {
-    // QuadMesh_postIntersect (geometry/Mesh.ispc:67-176): calcEpsilon over the 4 vertices
+    // QuadMesh_postIntersect (geometry/Mesh.ispc:67-176): calcEpsilon over the 4 vertices, dPds = vb - va
     const uint32_t *q = &g.quadIndex[4 * size_t(hit.primID)];
     const V3 a = g.verts[q[0]], b = g.verts[q[1]], c = g.verts[q[2]], d = g.verts[q[3]];
     eps = reduce_max(vmax(vmax(vabs(a), vabs(b)), vmax(vabs(c), vabs(d)))) * ulpEpsilon;
+    dPds = b - a;
   } else if (g.type == 0) {
+    // TriangleMesh_postIntersect (geometry/Mesh.ispc:178-276): dPds = vb - va without texcoords
     const V3 a = g.verts[g.index[3 * hit.primID]], b = g.verts[g.index[3 * hit.primID + 1]],
              c = g.verts[g.index[3 * hit.primID + 2]];
     eps = reduce_max(vmax(vmax(vabs(a), vabs(b)), vabs(c))) * ulpEpsilon;
+    dPds = b - a;
   } else {
     eps = g.spheres[hit.primID].w * ulpEpsilon;
   }
+  dg.dPds = xfmVector(e->xfm.l, dPds);  // Instance_postIntersect (common/Instance.ih:95-98)
   // Instance_postIntersect: normals by the inverse transpose, epsilon by the
   // largest diagonal scale
   const L3 it = transposed(e->rcp.l);

@@ -65,6 +65,7 @@ struct PixelFilter {
 
 struct DG {
   V3 P, Ng, Ns;
+  V3 dPds;  // DG_TANGENTS: a mesh's first edge (Mesh.ispc:172-175), else (1, 0, 0); world space
   float epsilon;
   uint32_t primID, geomID, instID;
 };

@@ -115,6 +115,7 @@ B200_D Ray primaryRay(const SamplerTables *T, const CameraD &cam, const PixelFil
 
 struct DG {
   V3 P, Ng, Ns;
+  V3 dPds;  // surface tangent (DG_TANGENTS): the triangle's first edge, else (1, 0, 0), in world space
   float epsilon;
   uint32_t entry;
 };
@@ -126,6 +127,10 @@ B200_D DG postIntersect(const Scene &sc, const Ray &ray, const HitRec &hit) {
   const Entry &e = sc.entries[hit.entry];
   dg.P = add(ray.org, mul(hit.t, ray.dir));
   V3 Ng = hit.Ng, Ns = hit.Ng;
+  // DG_TANGENTS: meshes take their first edge (TriangleMesh_postIntersect
+  // geometry/Mesh.ispc:172-175, QuadMesh_postIntersect :171-174), other
+  // geometry keeps the default (1, 0, 0) (World.ih postIntersect)
+  V3 dPds = mk(1.f, 0.f, 0.f);
   float eps;
   if (e.type == GEOM_TRIANGLES && e.meshKind == MESH_BOXES) {
     eps = 0.f;  // Boxes_postIntersect (geometry/Boxes.ispc) sets no geometry epsilon
@@ -133,11 +138,15 @@ B200_D DG postIntersect(const Scene &sc, const Ray &ray, const HitRec &hit) {
     // QuadMesh_postIntersect (geometry/Mesh.ispc:67-176): epsilon over the 4 vertices
     const uint4 q = __ldg(reinterpret_cast<const uint4 *>(e.index) + hit.primID);
     const uint32_t ix[4] = {q.x, q.y, q.z, q.w};
-    V3 m = splat(0.f);
+    V3 m = splat(0.f), v[2];
 #pragma unroll
-    for (int k = 0; k < 4; k++)
-      m = vmax(m, vabs(mk(__ldg(e.verts + 3 * ix[k]), __ldg(e.verts + 3 * ix[k] + 1), __ldg(e.verts + 3 * ix[k] + 2))));
+    for (int k = 0; k < 4; k++) {
+      const V3 p = mk(__ldg(e.verts + 3 * ix[k]), __ldg(e.verts + 3 * ix[k] + 1), __ldg(e.verts + 3 * ix[k] + 2));
+      if (k < 2) v[k] = p;
+      m = vmax(m, vabs(p));
+    }
     eps = fmul(reduce_max(m), ULP_EPSILON);
+    dPds = sub(v[1], v[0]);
   } else if (e.type == GEOM_TRIANGLES) {
     const uint32_t i0 = __ldg(e.index + 3 * hit.primID), i1 = __ldg(e.index + 3 * hit.primID + 1),
                    i2 = __ldg(e.index + 3 * hit.primID + 2);
@@ -145,6 +154,7 @@ B200_D DG postIntersect(const Scene &sc, const Ray &ray, const HitRec &hit) {
     const V3 b = mk(__ldg(e.verts + 3 * i1), __ldg(e.verts + 3 * i1 + 1), __ldg(e.verts + 3 * i1 + 2));
     const V3 c = mk(__ldg(e.verts + 3 * i2), __ldg(e.verts + 3 * i2 + 1), __ldg(e.verts + 3 * i2 + 2));
     eps = fmul(reduce_max(vmax(vmax(vabs(a), vabs(b)), vabs(c))), ULP_EPSILON);
+    dPds = sub(b, a);
   } else {
     eps = fmul(__ldg(&e.spheres[hit.primID].w), ULP_EPSILON);
   }
@@ -152,7 +162,9 @@ B200_D DG postIntersect(const Scene &sc, const Ray &ray, const HitRec &hit) {
     Ns = xfmVectorT(e.rcp, Ns);
     Ng = xfmVectorT(e.rcp, Ng);
     eps = fmul(eps, e.epsScale);
+    dPds = xfmVector(e.xfm, dPds);  // Instance_postIntersect (common/Instance.ih:95-98)
   }
+  dg.dPds = dPds;
   const float e2 = fmul(fmaxf(reduce_max(vabs(dg.P)), fmul(reduce_max(vabs(ray.dir)), hit.t)), ULP_EPSILON);
   dg.epsilon = fmaxf(eps, e2);
   V3 ffnng = normalize(Ng);

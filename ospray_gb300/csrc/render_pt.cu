@@ -422,10 +422,13 @@ B200_D V3 shadowInPlace(const PtCtx &C, Ray sr, V3 contrib, uint32_t medium) {
 // sampling with the same-side check, Russian roulette, Beer attenuation in
 // the current medium, medium change on transmission, and the continuation
 // ray.  A specular transmission keeps the previous vertex for MIS.
+// The path record is read and written field by field (gp: the record in
+// memory; org4 / dir4 / meta: the fields the kernel keeps in registers), so
+// the whole 128-byte record is never live at once.
 template <class B, bool NRC, bool ALLMAT>
 B200_D void scatterSurface(const PtCtx &C, const B &bsdf, const MaterialD &mat, uint32_t mi, const DG &dg,
-                           const Ray &ray, float t, V3 wo, PathRec &pr, PathVars &v, uint32_t p, ShadowRec *sh,
-                           int &nsh, const NrcFrameD &nf) {
+                           const Ray &ray, float t, V3 wo, PathRec *gp, float4 &org4, float4 &dir4, uint4 &meta,
+                           PathVars &v, uint32_t p, ShadowRec *sh, int &nsh, const NrcFrameD &nf) {
   const int nl = C.p.numLights;
   const bool transparentShadows = ALLMAT && C.p.transparentShadows != 0;
   if (bsdf.smooth && v.scatter == 0 && !v.auxDone && C.aux) {
@@ -443,8 +446,9 @@ B200_D void scatterSurface(const PtCtx &C, const B &bsdf, const MaterialD &mat, 
   }
   bool cached = false;
   if (NRC) {
-    if (pr.meta2.w != INVALID_ID) {  // training path: record the vertex
-      float *q = nf.trainVerts + (size_t(pr.meta2.w) * nf.maxLen1 + v.depth) * 20;
+    const uint32_t slot = gp->meta2.w;
+    if (slot != INVALID_ID) {  // training path: record the vertex
+      float *q = nf.trainVerts + (size_t(slot) * nf.maxLen1 + v.depth) * 20;
       const float rv[20] = {dg.P.x, dg.P.y, dg.P.z, wo.x, wo.y, wo.z, dg.Ns.x, dg.Ns.y, dg.Ns.z,
                             mat.roughness, mat.r, mat.g, mat.b, v.throughput.x, v.throughput.y, v.throughput.z,
                             v.contribution.x, v.contribution.y, v.contribution.z, __uint_as_float(p)};
@@ -461,9 +465,9 @@ B200_D void scatterSurface(const PtCtx &C, const B &bsdf, const MaterialD &mat, 
   }
   if (cached) return;
   // LDSampler of this path at its current group; advanced unconditionally
-  const uint32_t sampleID = pr.meta2.z;
+  const uint32_t sampleID = gp->meta2.z;
   LDSampler ld;
-  ld.init(C.T, pr.meta.x, sampleID, sampleID * uint32_t(C.p.nFirst), 16, 16);
+  ld.init(C.T, meta.x, sampleID, sampleID * uint32_t(C.p.nFirst), 16, 16);
   ld.nextGroup();
   int numLS = 0;
   if (bsdf.smooth) {
@@ -547,18 +551,18 @@ B200_D void scatterSurface(const PtCtx &C, const B &bsdf, const MaterialD &mat, 
       v.diffuseSeen = true;
     if (!(ray.dir.x == fs.wi.x && ray.dir.y == fs.wi.y && ray.dir.z == fs.wi.z)) v.straightPath = false;
     if (fs.type & ~ST_SPEC_T) {  // the new last vertex for MIS
-      pr.lastP = make_float4(dg.P.x, dg.P.y, dg.P.z, 0.f);
-      pr.lastN = make_float4(dg.Ns.x, dg.Ns.y, dg.Ns.z, 0.f);
-      pr.dir.w = fs.pdf;
+      gp->lastP = make_float4(dg.P.x, dg.P.y, dg.P.z, 0.f);
+      gp->lastN = make_float4(dg.Ns.x, dg.Ns.y, dg.Ns.z, 0.f);
+      dir4.w = fs.pdf;
       v.lastNLS = numLS;
     }
-    pr.org = make_float4(org.x, org.y, org.z, pr.org.w);
-    pr.dir = make_float4(fs.wi.x, fs.wi.y, fs.wi.z, pr.dir.w);
+    org4 = make_float4(org.x, org.y, org.z, org4.w);
+    dir4 = make_float4(fs.wi.x, fs.wi.y, fs.wi.z, dir4.w);
     v.depth++;
     if (fs.type & ST_SMOOTH) v.scatter++;
     if (!(maxc(v.throughput) > C.p.minContribution)) cont = false;
   }
-  pr.meta.x = ld.scramble;
+  meta.x = ld.scramble;
   v.cont = cont;
 }
 
@@ -593,16 +597,20 @@ __global__ void __launch_bounds__(128, B200_SHADE_MINBLOCKS) k_pt_shade(PtCtx c,
     int nsh = 0;
     ShadowRec sh[2];
     if (valid) {
-      PathRec pr = ws.paths[p];
+      PathRec *gp = ws.paths + p;
       const HitBuf hb = ws.hits[p];
-      const ReqD *R = BATCH ? reqs + pr.meta2.y : nullptr;
+      const ReqD *R = BATCH ? reqs + gp->meta2.y : nullptr;
       const PtCtx &C = BATCH ? R->c : c;
       if (BATCH && R->kind == BATCH_AO) {
+        PathRec pr = *gp;
         aoShade(C, R->ao, R->fi.W, pr, hb, p, sh, nsh);
-        ws.paths[p] = pr;
+        *gp = pr;
       } else {
       const int nl = C.p.numLights;
-      const uint32_t flags = pr.meta.y;
+      float4 org4 = gp->org, dir4 = gp->dir;
+      const float4 thr4 = gp->thr, con4 = gp->con;
+      uint4 meta = gp->meta;
+      const uint32_t flags = meta.y;
       PathVars v;
       v.diffuseSeen = (flags & F_DIFFUSE) != 0;
       v.auxDone = (flags & F_AUXDONE) != 0;
@@ -611,27 +619,28 @@ __global__ void __launch_bounds__(128, B200_SHADE_MINBLOCKS) k_pt_shade(PtCtx c,
       v.straightPath = (flags & F_STRAIGHT) != 0;
       v.firstBounceLight = (flags & F_FIRST) != 0;
       v.lastNLS = int(flags >> F_NLS_SHIFT);
-      v.throughput = mk(pr.thr.x, pr.thr.y, pr.thr.z);
-      v.contribution = mk(pr.con.x, pr.con.y, pr.con.z);
-      v.medium = __float_as_uint(pr.con.w);
+      v.throughput = mk(thr4.x, thr4.y, thr4.z);
+      v.contribution = mk(con4.x, con4.y, con4.z);
+      v.medium = __float_as_uint(con4.w);
       v.cont = false;
-      float alpha = pr.thr.w;
+      float alpha = thr4.w;
       Ray ray;
-      ray.org = mk(pr.org.x, pr.org.y, pr.org.z);
+      ray.org = mk(org4.x, org4.y, org4.z);
       ray.tnear = 0.f;
-      ray.dir = mk(pr.dir.x, pr.dir.y, pr.dir.z);
+      ray.dir = mk(dir4.x, dir4.y, dir4.z);
       ray.tfar = INFINITY;
-      const V3 lastP = mk(pr.lastP.x, pr.lastP.y, pr.lastP.z), lastNs = mk(pr.lastN.x, pr.lastN.y, pr.lastN.z);
-      const float lastPdf = pr.dir.w;
       const bool hit = hb.a.w != 0.f;
       const float t = hit ? hb.a.x : INFINITY;
       const V3 wo = -ray.dir;
-      if (v.depth == 0) pr.org.w = t;
+      if (v.depth == 0) org4.w = t;
       if (!hit && v.straightPath) {
         alpha -= luminance(v.throughput) * (1.f - C.p.bg[3]);
         v.contribution = v.contribution + v.throughput * mk(C.p.bg[0], C.p.bg[1], C.p.bg[2]);
       }
       if (nl > 0) {  // evaluateVirtualLights
+        const float4 lp = gp->lastP, ln = gp->lastN;
+        const V3 lastP = mk(lp.x, lp.y, lp.z), lastNs = mk(ln.x, ln.y, ln.z);
+        const float lastPdf = dir4.w;
         const V3 d0 = lastP - ray.org;
         const float lo = sqrtf(fdot(d0, d0));
         float hiD = INFINITY;
@@ -662,9 +671,9 @@ __global__ void __launch_bounds__(128, B200_SHADE_MINBLOCKS) k_pt_shade(PtCtx c,
         h.instID = e.instID;
         const DG dg = postIntersect(C.sc, ray, h);
         if (v.depth == 0) {
-          pr.meta.z = h.primID;
-          pr.meta.w = h.geomID;
-          pr.meta2.x = h.instID;
+          meta.z = h.primID;
+          meta.w = h.geomID;
+          gp->meta2.x = h.instID;
         }
         const uint32_t mi = e.materialID;
         if (v.scatter < C.p.maxScatteringEvents && mi < uint32_t(C.p.numMaterials)) {
@@ -672,9 +681,8 @@ __global__ void __launch_bounds__(128, B200_SHADE_MINBLOCKS) k_pt_shade(PtCtx c,
           switch (ALLMAT ? mat.kind : MAT_PRINCIPLED) {
             case MAT_OBJ:
             case MAT_PRINCIPLED: {
-              // makeShadingFrame with dPds = the instance's x axis
-              V3 U = e.identity ? mk(1.f, 0.f, 0.f) : mk(e.xfm.m[0], e.xfm.m[4], e.xfm.m[8]);
-              U = fnormalize(U);
+              // makeShadingFrame (common/DifferentialGeometry.ih) with the surface tangent dPds
+              const V3 U = fnormalize(dg.dPds);
               const V3 Vv = fcross(dg.Ns, U);
               V3 fxv, fyv;
               if (fdot(Vv, Vv) > 0.f) {
@@ -686,12 +694,13 @@ __global__ void __launch_bounds__(128, B200_SHADE_MINBLOCKS) k_pt_shade(PtCtx c,
               if (ALLMAT && mat.kind == MAT_OBJ) {
                 ObjBsdf b;
                 b.init(mat, fxv, fyv, dg.Ns);
-                scatterSurface<ObjBsdf, NRC, ALLMAT>(C, b, mat, mi, dg, ray, t, wo, pr, v, p, sh, nsh, nf);
+                scatterSurface<ObjBsdf, NRC, ALLMAT>(C, b, mat, mi, dg, ray, t, wo, gp, org4, dir4, meta, v, p, sh,
+                                                     nsh, nf);
               } else {
                 PrincipledBsdfT<ALLMAT> b;
                 b.init(mat, fxv, fyv, dg.Ns, C.AT);
-                scatterSurface<PrincipledBsdfT<ALLMAT>, NRC, ALLMAT>(C, b, mat, mi, dg, ray, t, wo, pr, v, p, sh, nsh,
-                                                                    nf);
+                scatterSurface<PrincipledBsdfT<ALLMAT>, NRC, ALLMAT>(C, b, mat, mi, dg, ray, t, wo, gp, org4, dir4,
+                                                                    meta, v, p, sh, nsh, nf);
               }
               break;
             }
@@ -699,7 +708,8 @@ __global__ void __launch_bounds__(128, B200_SHADE_MINBLOCKS) k_pt_shade(PtCtx c,
               if (ALLMAT) {
                 MetalBsdf b;
                 b.init(mat, dg.Ns);
-                scatterSurface<MetalBsdf, NRC, ALLMAT>(C, b, mat, mi, dg, ray, t, wo, pr, v, p, sh, nsh, nf);
+                scatterSurface<MetalBsdf, NRC, ALLMAT>(C, b, mat, mi, dg, ray, t, wo, gp, org4, dir4, meta, v, p, sh,
+                                                       nsh, nf);
               }
               break;
             }
@@ -708,7 +718,8 @@ __global__ void __launch_bounds__(128, B200_SHADE_MINBLOCKS) k_pt_shade(PtCtx c,
                 GlassBsdf b;
                 const bool out = glassFromOutside(C.mats, mi, v.medium);
                 b.init(out ? mat.iorOut * (1.f / mat.iorIn) : mat.iorIn * (1.f / mat.iorOut), dg.Ns, dg.Ng);
-                scatterSurface<GlassBsdf, NRC, ALLMAT>(C, b, mat, mi, dg, ray, t, wo, pr, v, p, sh, nsh, nf);
+                scatterSurface<GlassBsdf, NRC, ALLMAT>(C, b, mat, mi, dg, ray, t, wo, gp, org4, dir4, meta, v, p, sh,
+                                                       nsh, nf);
               }
               break;
             }
@@ -716,7 +727,8 @@ __global__ void __launch_bounds__(128, B200_SHADE_MINBLOCKS) k_pt_shade(PtCtx c,
               if (ALLMAT) {
                 ThinGlassBsdf b;
                 b.init(mat, dg.Ns);
-                scatterSurface<ThinGlassBsdf, NRC, ALLMAT>(C, b, mat, mi, dg, ray, t, wo, pr, v, p, sh, nsh, nf);
+                scatterSurface<ThinGlassBsdf, NRC, ALLMAT>(C, b, mat, mi, dg, ray, t, wo, gp, org4, dir4, meta, v, p,
+                                                           sh, nsh, nf);
               }
               break;
             }
@@ -726,13 +738,15 @@ __global__ void __launch_bounds__(128, B200_SHADE_MINBLOCKS) k_pt_shade(PtCtx c,
           cont = v.cont;
         }
       }
-      pr.thr = make_float4(v.throughput.x, v.throughput.y, v.throughput.z, alpha);
-      pr.con = make_float4(v.contribution.x, v.contribution.y, v.contribution.z, __uint_as_float(v.medium));
-      pr.meta.y = uint32_t(v.depth) | (v.straightPath ? F_STRAIGHT : 0u) | (v.firstBounceLight ? F_FIRST : 0u) |
-                  (cont ? 0u : F_ENDED) | (v.diffuseSeen ? F_DIFFUSE : 0u) | (v.auxDone ? F_AUXDONE : 0u) |
-                  (uint32_t(min(v.scatter, int(F_SCATTER_MAX))) << F_SCATTER_SHIFT) |
-                  (uint32_t(min(v.lastNLS, int(F_NLS_MAX))) << F_NLS_SHIFT);
-      ws.paths[p] = pr;
+      meta.y = uint32_t(v.depth) | (v.straightPath ? F_STRAIGHT : 0u) | (v.firstBounceLight ? F_FIRST : 0u) |
+               (cont ? 0u : F_ENDED) | (v.diffuseSeen ? F_DIFFUSE : 0u) | (v.auxDone ? F_AUXDONE : 0u) |
+               (uint32_t(min(v.scatter, int(F_SCATTER_MAX))) << F_SCATTER_SHIFT) |
+               (uint32_t(min(v.lastNLS, int(F_NLS_MAX))) << F_NLS_SHIFT);
+      gp->org = org4;
+      gp->dir = dir4;
+      gp->thr = make_float4(v.throughput.x, v.throughput.y, v.throughput.z, alpha);
+      gp->con = make_float4(v.contribution.x, v.contribution.y, v.contribution.z, __uint_as_float(v.medium));
+      gp->meta = meta;
       }
     }
     // queue appends (warp-uniform region)
