@@ -104,6 +104,16 @@ int b200_scene_add_quad_mesh(b200_scene scene, const float *vertex, int64_t nver
 int b200_scene_add_boxes(b200_scene scene, const float *boxes, int64_t n, int *geom_out);
 /* spheres: n x 4 float (center xyz, radius), OSP_SPHERE */
 int b200_scene_add_spheres(b200_scene scene, const float *spheres, int64_t n, int *geom_out);
+/* Per-vertex attributes of a triangle mesh (Mesh::commit "vertex.normal",
+ * "vertex.color", "vertex.texcoord", geometry/Mesh.cpp:37-204;
+ * TriangleMesh_postIntersect geometry/Mesh.ispc:178-276), each nverts x
+ * (3, 4, 2) floats or null; call before the scene's commit.  Normals give the
+ * interpolated shading normal, colours multiply the path tracer's material
+ * colours (alpha the OBJ d), texture coordinates address material textures
+ * and define the shading tangents (without them textures see the hit's
+ * barycentric u, v).  Used by the path tracer. */
+int b200_scene_set_mesh_attributes(b200_scene scene, int geom, const float *normal, const float *color,
+                                   const float *texcoord);
 /* one (instance, geometric model) pair: geometry `geom` placed by the
  * row-major 3x4 affine `xfm` (null = identity), reported as instID/geomID;
  * material_id indexes the renderer's material list (or -1 for none) */
@@ -276,6 +286,30 @@ typedef struct {
 } b200_light;
 int b200_scene_set_lights(b200_scene scene, const b200_light *lights, int n);
 
+/* ---- 2D textures (Texture2D::commit texture/Texture2D.cpp:42-146,
+ *      Texture2D_get texture/Texture2D.ispc:130-164).
+ * data: width x height texels of `format` (OSPTextureFormat values: RGBA8,
+ * SRGBA, RGBA32F, RGB8, SRGB, RGB32F, R8, R32F, L8, RA8, LA8, RGBA16, RGB16,
+ * RA16, R16, RA32F; the half-float formats are refused), rows from the
+ * bottom, copied at the call; filter OSPTextureFilter (0 linear, 1 nearest);
+ * wrap modes OSPTextureWrapMode per axis (0 repeat, 1 mirrored repeat,
+ * 2 clamp to edge).  mipmaps != 0 generates the MIP chain on the device
+ * (MipMap_generate, texture/MipMapGeneration.ispc) and lookups then pick the
+ * level from the ray cone's footprint.  A texture must outlive the materials
+ * and renders that use it. */
+typedef struct b200_texture_t *b200_texture;
+int b200_texture_create(b200_device dev, int width, int height, int format, int filter, int wrapS, int wrapT,
+                        int mipmaps, const void *data, b200_texture *out);
+int b200_texture_release(b200_texture tex);
+/* number of levels (1 + MIP levels) */
+int b200_texture_levels(b200_texture tex);
+/* copies level `level` (max(w >> level, 1) x max(h >> level, 1) texels of the
+ * texture's format) into host memory `dst` of `bytes` bytes */
+int b200_texture_read_level(b200_texture tex, int level, void *dst, size_t bytes);
+/* Texture2D_get at n texture coordinates (st: 2 floats each, host memory)
+ * with per-lookup pixel footprints (0: level 0); out: n x RGBA floats */
+int b200_texture_sample(b200_texture tex, int64_t n, const float *st, const float *footprint, float *out);
+
 /* ---- path tracer (PathTracer::commit render/pathtracer/PathTracer.cpp:29-51,
  *      PathTracer_renderPixel render/pathtracer/PathTracer.ispc:75-216).
  * material_id of an instance (b200_scene_add_instance) indexes `materials`.
@@ -323,6 +357,8 @@ typedef struct {
   float attenuationColor[3];
   float attenuationDistance;
   float thickness;     /* thinGlass */
+  b200_texture baseColorMap; /* principled map_baseColor (rgb x baseColor, alpha x opacity); obj map_kd (rgb x
+                                kd, alpha x d); looked up at the hit's texture coordinates; null: none */
 } b200_material;
 /* the reference's defaults for a material of `type` (principled: baseColor
  * 0.8, roughness 0, metallic 0, opacity 1; obj: kd 0.8, ks 0, ns 10, d 1,
@@ -342,6 +378,10 @@ typedef struct {
   float backgroundColor[4];
   int pixelFilter;
   int collectStats;
+  b200_texture backplate; /* "map_backplate" (Renderer_getBackground render/Renderer.ispc:19-29): looked up at
+                             the camera sample's screen position for paths that see the background; null: the
+                             background colour */
+  float mipMapBias;       /* "mipMapBias" (Renderer.cpp:41): footprint x 2^bias for MIP level selection */
 } b200_pt_params;
 int b200_render_pt(b200_scene scene, const b200_camera_desc *camera, const b200_pt_params *params,
                    const b200_material *materials, int nmaterials, b200_frame fb, void *stream);

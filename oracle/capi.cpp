@@ -4,6 +4,7 @@
 #include <cstring>
 
 #include "render.h"
+#include "texture.h"
 
 using namespace orc;
 
@@ -89,6 +90,47 @@ int or_scene_add_boxes(void *sp, const float *boxes, int n) {
   }
   s.geoms.push_back(std::move(g));
   return int(s.geoms.size() - 1);
+}
+
+// per-vertex normals (3), colours (4) and texture coordinates (2) of
+// triangle mesh `geom`, each null or one per vertex
+void or_scene_set_mesh_attributes(void *sp, int geom, const float *normals, const float *colors,
+                                  const float *texcoords) {
+  Geometry &g = static_cast<Scene *>(sp)->geoms[size_t(geom)];
+  const size_t n = g.verts.size();
+  g.normals.clear();
+  g.colors.clear();
+  g.texcoords.clear();
+  for (size_t i = 0; normals && i < n; i++) g.normals.push_back({normals[3 * i], normals[3 * i + 1], normals[3 * i + 2]});
+  for (size_t i = 0; colors && i < n; i++)
+    g.colors.push_back({colors[4 * i], colors[4 * i + 1], colors[4 * i + 2], colors[4 * i + 3]});
+  for (size_t i = 0; texcoords && i < n; i++) g.texcoords.push_back({texcoords[2 * i], texcoords[2 * i + 1]});
+}
+
+// 2D textures: w x h texels of an OSPTextureFormat, rows from the bottom
+void *or_texture_new(int w, int h, int format, int filter, int wrapS, int wrapT, int mipmaps, const void *data) {
+  return makeTexture(w, h, format, filter, wrapS, wrapT, mipmaps != 0, data);
+}
+void or_texture_free(void *t) { delete static_cast<Texture *>(t); }
+int or_texture_levels(const void *t) { return int(static_cast<const Texture *>(t)->levels.size()); }
+// copies level `level`'s texels into dst (bytes must cover them); returns the bytes copied
+size_t or_texture_read_level(const void *tp, int level, void *dst, size_t bytes) {
+  const Texture &t = *static_cast<const Texture *>(tp);
+  const std::vector<uint8_t> &l = t.levels[size_t(level)];
+  if (bytes < l.size()) return 0;
+  std::memcpy(dst, l.data(), l.size());
+  return l.size();
+}
+// Texture2D_get at n texture coordinates st (2 floats each) with footprints fp
+void or_texture_sample(const void *tp, int n, const float *st, const float *fp, float *out) {
+  const Texture &t = *static_cast<const Texture *>(tp);
+  for (int i = 0; i < n; i++) {
+    const V4 v = t.get({st[2 * i], st[2 * i + 1]}, fp[i]);
+    out[4 * i] = v.x;
+    out[4 * i + 1] = v.y;
+    out[4 * i + 2] = v.z;
+    out[4 * i + 3] = v.w;
+  }
 }
 
 int or_scene_add_spheres(void *sp, const float *xyzr, int n) {

@@ -112,6 +112,7 @@ MaterialParams commitMaterial(int type, const float *p) {
 }
 
 bool transparentMaterial(const MaterialParams &m) {
+  if (m.mapAlpha && (m.type == MAT_PRINCIPLED || m.type == MAT_OBJ)) return true;
   switch (m.type) {
     case MAT_PRINCIPLED: return 1.f - m.opacity > EPS;
     case MAT_OBJ: {
@@ -139,7 +140,34 @@ static L3 shadingFrameOf(const DG &dg, V3 dPds) {
 
 static bool glassFromOutside(const MaterialParams &m, const Medium &cur) { return sameMedium(cur, m.outside); }
 
-SurfaceBSDF makeBSDF(const MaterialParams &m, const DG &dg, V3 dPds, const Medium &cur) {
+// The colour map's texel at the hit (1 without a map)
+static V4 mapTexel(const MaterialParams &m, const DG &dg, float footprint) {
+  return m.map ? m.map->get(dg.st, footprint) : V4{1.f, 1.f, 1.f, 1.f};
+}
+
+// Principled.ispc:110-135 (baseColor x map.rgb x colour.rgb, clamped; opacity
+// x map alpha) and OBJ.ispc:52-66 (d x colour alpha x map alpha, kd x map.rgb
+// x colour.rgb): the material at this hit; `opacity` principled's effective one
+static MaterialParams atHit(const MaterialParams &m0, const DG &dg, float footprint, float &opacity) {
+  MaterialParams m = m0;
+  opacity = clamp01(m0.opacity);
+  if (m0.type == MAT_PRINCIPLED) {
+    const V4 t = mapTexel(m0, dg, footprint);
+    m.baseColor = {clamp01(m0.baseColor.x * t.x * dg.color.x), clamp01(m0.baseColor.y * t.y * dg.color.y),
+                   clamp01(m0.baseColor.z * t.z * dg.color.z)};
+    if (m0.mapAlpha) opacity *= t.w;
+  } else if (m0.type == MAT_OBJ) {
+    const V4 t = mapTexel(m0, dg, footprint);
+    m.opacity = m0.opacity * dg.color.w * t.w;
+    m.baseColor = {m0.baseColor.x * t.x * dg.color.x, m0.baseColor.y * t.y * dg.color.y,
+                   m0.baseColor.z * t.z * dg.color.z};
+  }
+  return m;
+}
+
+SurfaceBSDF makeBSDF(const MaterialParams &m0, const DG &dg, V3 dPds, const Medium &cur, float footprint) {
+  float opacity;
+  const MaterialParams m = atHit(m0, dg, footprint, opacity);
   SurfaceBSDF b;
   b.type = m.type;
   switch (m.type) {
@@ -206,10 +234,10 @@ SurfaceBSDF makeBSDF(const MaterialParams &m, const DG &dg, V3 dPds, const Mediu
     }
     default: {
       const L3 f = shadingFrameOf(dg, dPds);
-      b.op = clamp01(m.opacity);
+      b.op = opacity;
       b.tr = 1.f - b.op;
       b.hasStack = m.opacity > EPS;
-      b.hasCut = 1.f - m.opacity > EPS;
+      b.hasCut = 1.f - m.opacity > EPS || m.mapAlpha;
       b.N = f.vz;
       b.st.frame = f;
       b.st.N = f.vz;
@@ -483,14 +511,20 @@ BSDFSample SurfaceBSDF::sample(V3 wo, V2 s, float ss) const {
   }
 }
 
-V3 materialTransparency(const MaterialParams &m, const DG &dg, V3 rayDir, const Medium &cur) {
+V3 materialTransparency(const MaterialParams &m, const DG &dg, V3 rayDir, const Medium &cur, float footprint) {
   switch (m.type) {
-    case MAT_PRINCIPLED: {  // Principled_getTransparency, no glass lobe
-      const float tr = 1.f - clamp01(m.opacity);
+    case MAT_PRINCIPLED: {  // Principled_getTransparency (Principled.ispc:432-580), no glass lobe
+      float op = clamp01(m.opacity);
+      if (m.mapAlpha) op *= mapTexel(m, dg, footprint).w;
+      const float tr = 1.f - op;
       if (tr <= EPS) return v3(0.f);
       return v3(tr);
     }
-    case MAT_OBJ: return m.tf * m.opacity + v3(1.f - m.opacity);
+    case MAT_OBJ: {  // OBJ_getTransparency (OBJ.ispc:93-110)
+      float d = m.opacity * dg.color.w;
+      if (m.mapAlpha) d *= mapTexel(m, dg, footprint).w;
+      return m.tf * d + v3(1.f - d);
+    }
     case MAT_GLASS: {
       const float eta = glassFromOutside(m, cur) ? m.outside.ior * (1.f / m.inside.ior)
                                                  : m.inside.ior * (1.f / m.outside.ior);

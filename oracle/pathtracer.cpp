@@ -7,6 +7,10 @@
 //   misHeuristic            render/pathtracer/PathTracerUtil.ih:30-46
 //   light list + CDF        render/pathtracer/PathTracerData.cpp:32-82
 //   parameters              render/pathtracer/PathTracer.cpp:29-51
+//   ray cones               common/World.ih:458-464, camera/*Camera.ispc
+//                           initRay, PathTracer.ispc:183-187,
+//                           NextEventEstimation.ispc:103-106
+//   backplate               render/Renderer.ispc:19-29, PathSampler.ispc:200-215
 #include <cstring>
 
 #include "pt_bsdf.h"
@@ -19,6 +23,8 @@ struct PtParams {
   int spp, maxPathLength, roulettePathLength, maxScatteringEvents, lightSamples, limitIndirectLightSamples;
   float minContribution, maxContribution;
   V4 bg;
+  const Texture *backplate = nullptr;  // map_backplate
+  float mipBiasFactor = 1.f;           // 2^mipMapBias
 };
 
 struct PtLights {
@@ -103,20 +109,25 @@ const MaterialParams *materialOf(const Ctx &c, const Hit &hit) {
 // segment, until the light is reached (the remaining contribution) or the
 // contribution drops to minContribution / maxPathLength surfaces were crossed
 // (0).  Without transparent materials the first hit blocks the light.
-V3 transparentShadow(const Ctx &c, V3 lightContrib, Ray shadowRay, Medium medium) {
+// coneWidth: the path's ray cone width at the shadow ray's origin; the
+// shadow cone narrows to 0 at the light and restarts from that width after
+// every surface crossed.
+V3 transparentShadow(const Ctx &c, V3 lightContrib, Ray shadowRay, Medium medium, float coneWidth) {
   if (!c.transparentShadows) {
     tl_rays++;
     return c.sc.occluded(shadowRay) ? v3(0.f) : lightContrib;
   }
   int maxDepth = c.p.maxPathLength;
   const float tOriginal = shadowRay.tfar;
+  const float dwdt = -coneWidth * (1.f / tOriginal);
   for (;;) {
     Hit hit;
     tl_rays++;
     if (!c.sc.intersect(shadowRay, hit)) return lightContrib;
-    const DG dg = postIntersect(c.sc, shadowRay, hit);
+    const DG dg = postIntersect(c.sc, shadowRay, hit, true);
     const MaterialParams *m = materialOf(c, hit);
-    const V3 T = m ? materialTransparency(*m, dg, shadowRay.dir, medium) : v3(0.f);
+    const float fp = m && m->map ? pixelFootprint(coneWidth + dwdt * hit.t, shadowRay.dir, dg, c.p.mipBiasFactor) : 0.f;
+    const V3 T = m ? materialTransparency(*m, dg, shadowRay.dir, medium, fp) : v3(0.f);
     lightContrib = lightContrib * T;
     if (medium.att.x != 0.f || medium.att.y != 0.f || medium.att.z != 0.f) {
       const V3 a = medium.att * (hit.t - shadowRay.tnear);
@@ -146,7 +157,7 @@ V3 virtualLights(const Ctx &c, bool straightPath, const Vertex &last, bool env, 
 }
 
 V3 nee(const Ctx &c, LDSampler &ld, const DG &dg, const SurfaceBSDF &bsdf, V3 wo, V3 throughput, int numLS,
-       const Medium &medium) {
+       const Medium &medium, float coneWidth) {
   V3 L = v3(0.f);
   const int nl = int(c.L.kind.size());
   for (int i = 0; i < numLS; i++) {
@@ -173,7 +184,8 @@ V3 nee(const Ctx &c, LDSampler &ld, const DG &dg, const SurfaceBSDF &bsdf, V3 wo
     if (reduce_max(fe.value) <= 0.f) continue;
     V3 org = dg.P;
     if (dot(dg.Ng, ls.dir) < 0.f) org = org - (2.f * dg.epsilon) * dg.Ng;
-    const V3 contrib = transparentShadow(c, throughput * fe.value * ls.weight, {org, 0.f, ls.dir, ls.dist}, medium);
+    const V3 contrib =
+        transparentShadow(c, throughput * fe.value * ls.weight, {org, 0.f, ls.dir, ls.dist}, medium, coneWidth);
     if (reduce_max(contrib) > 0.f) L = L + contrib * mis(ls.pdf, fe.pdf);
   }
   return L;
@@ -186,7 +198,10 @@ struct PathOut {
   V3 normal, albedo;
 };
 
-PathOut samplePath(const Ctx &c, LDSampler &ld, Ray ray) {
+// cone: the camera ray's cone (width, dwdt) in units of the frame height;
+// screen: the pixel centre (the backplate's lookup position)
+PathOut samplePath(const Ctx &c, LDSampler &ld, Ray ray, V2 cone, V2 screen) {
+  float coneWidth = cone.x;
   PathOut out = {v3(0.f), 1.f, INFINITY, INVALID_ID, INVALID_ID, INVALID_ID, v3(0.f), v3(0.f)};
   V3 throughput = v3(1.f), contribution = v3(0.f);
   int depth = 0, scatteringEvents = 0;
@@ -207,13 +222,15 @@ PathOut samplePath(const Ctx &c, LDSampler &ld, Ray ray) {
     const V3 wo = -ray.dir;
     if (depth == 0) out.z = t;
     if (!h && straightPath) {
-      out.alpha -= luminance(throughput) * (1.f - c.p.bg.w);
-      contribution = contribution + throughput * v3(c.p.bg.x, c.p.bg.y, c.p.bg.z);
+      const V4 bg = c.p.backplate ? c.p.backplate->getScreen(screen) : c.p.bg;
+      out.alpha -= luminance(throughput) * (1.f - bg.w);
+      contribution = contribution + throughput * v3(bg.x, bg.y, bg.z);
     }
     contribution = contribution + virtualLights(c, straightPath, last, !h, ray, t, throughput);
     if (!h) break;
     if (depth >= c.p.maxPathLength) break;  // no geometry lights
-    const DG dg = postIntersect(c.sc, ray, hit);
+    const DG dg = postIntersect(c.sc, ray, hit, true);
+    coneWidth += cone.y * hit.t;  // propagated to the hit
     if (depth == 0) {
       out.primID = dg.primID;
       out.geomID = dg.geomID;
@@ -222,7 +239,8 @@ PathOut samplePath(const Ctx &c, LDSampler &ld, Ray ray) {
     if (depth >= c.p.maxPathLength || scatteringEvents >= c.p.maxScatteringEvents) break;
     const MaterialParams *mat = materialOf(c, hit);
     if (!mat) break;  // no material: no BSDF
-    const SurfaceBSDF bsdf = makeBSDF(*mat, dg, dg.dPds, medium);
+    const float fp = mat->map ? pixelFootprint(coneWidth, ray.dir, dg, c.p.mipBiasFactor) : 0.f;
+    const SurfaceBSDF bsdf = makeBSDF(*mat, dg, dg.dPds, medium, fp);
     ld.nextGroup();
     int numLS = 0;
     if (bsdf.smooth) {
@@ -231,7 +249,7 @@ PathOut samplePath(const Ctx &c, LDSampler &ld, Ray ray) {
         out.normal = throughput * bsdf.N;
       }
       numLS = firstBounceLight ? c.nFirst : c.nIndirect;
-      contribution = contribution + nee(c, ld, dg, bsdf, wo, throughput, numLS, medium);
+      contribution = contribution + nee(c, ld, dg, bsdf, wo, throughput, numLS, medium, coneWidth);
       firstBounceLight = false;
     }
     float ss;
@@ -287,8 +305,16 @@ void renderPT(const Scene &sc, const PtLights &lights, const std::vector<Materia
   const int nl = int(lights.kind.size());
   const int nFirst = p.lightSamples >= 0 && nl > 0 ? p.lightSamples : std::min(1024, nl);
   const int nIndirect = p.limitIndirectLightSamples && nFirst >= 1 ? 1 : nFirst;
-  bool transparent = false;
-  for (const MaterialParams &m : mats) transparent = transparent || transparentMaterial(m);
+  // shadow rays loop over closest hits when a material lets them through or
+  // vertex colours with alpha < 1 meet an obj material (d x alpha)
+  bool transparent = false, anyObj = false, colorAlpha = false;
+  for (const MaterialParams &m : mats) {
+    transparent = transparent || transparentMaterial(m);
+    anyObj = anyObj || m.type == MAT_OBJ;
+  }
+  for (const Geometry &g : sc.geoms)
+    for (const V4 &col : g.colors) colorAlpha = colorAlpha || col.w != 1.f;
+  transparent = transparent || (colorAlpha && anyObj);
   const Ctx c = {sc, lights, mats, p, nFirst, nIndirect, transparent};
   const V2 rcpSize = {1.f / float(fb.W), 1.f / float(fb.H)};
   const uint32_t accumID = uint32_t(fb.frameID);
@@ -307,7 +333,7 @@ void renderPT(const Scene &sc, const PtLights &lights, const std::vector<Materia
         const V2 center = {(float(x) + 0.5f) * rcpSize.x, (float(y) + 0.5f) * rcpSize.y};
         const V2 screen = {center.x + pfs.x * rcpSize.x, center.y + pfs.y * rcpSize.y};
         const Ray ray = cameraRay(cam, screen);
-        const PathOut o = samplePath(c, ld, ray);
+        const PathOut o = samplePath(c, ld, ray, cameraCone(cam, screen, rcpSize.y), center);
         ScreenSample smp;
         smp.rgb = vmin(o.rgb, v3(p.maxContribution));
         smp.alpha = o.alpha;
@@ -362,6 +388,15 @@ int or_pt_add_material2(void *p, int type, const float *params) {
   OrPtScene &s = *static_cast<OrPtScene *>(p);
   s.mats.push_back(commitMaterial(type, params));
   return int(s.mats.size() - 1);
+}
+// material `mat`'s colour map (principled map_baseColor / obj map_kd): a
+// Texture from or_texture_new
+void or_pt_set_material_map(void *p, int mat, const void *tex) {
+  OrPtScene &s = *static_cast<OrPtScene *>(p);
+  MaterialParams &m = s.mats[size_t(mat)];
+  if (m.type != MAT_PRINCIPLED && m.type != MAT_OBJ) return;
+  m.map = static_cast<const Texture *>(tex);
+  m.mapAlpha = m.map && m.map->hasAlpha;
 }
 // position, edge1, edge2 (3 floats each), radiance rgb
 void or_pt_add_quad_light(void *p, const float *pos, const float *e1, const float *e2, const float *radiance) {
@@ -422,6 +457,8 @@ struct OrPtParams {
   float minContribution, maxContribution;
   float bg[4];
   int pixelFilter;
+  const void *backplate;  // a Texture from or_texture_new, or null
+  float mipMapBias;
 };
 
 // Renders `frames` accumulated frames of rows [y0, y1) (y1 <= 0: all rows).
@@ -435,7 +472,8 @@ void or_render_pt(void *scp, void *ptp, const OrCameraPT *cam, const OrPtParams 
   pf.init(pp->pixelFilter);
   PtParams p = {pp->spp, pp->maxPathLength, pp->roulettePathLength, pp->maxScatteringEvents, pp->lightSamples,
                 pp->limitIndirectLightSamples, pp->minContribution, pp->maxContribution,
-                {pp->bg[0], pp->bg[1], pp->bg[2], pp->bg[3]}};
+                {pp->bg[0], pp->bg[1], pp->bg[2], pp->bg[3]}, static_cast<const Texture *>(pp->backplate),
+                std::pow(2.f, pp->mipMapBias)};
   if (y1 <= 0) {
     y0 = 0;
     y1 = H;

@@ -14,6 +14,7 @@
 #include <vector>
 
 #include "render.h"
+#include "texture.h"
 
 namespace orc {
 
@@ -279,6 +280,9 @@ struct MaterialParams {
   Medium inside = {1.f, v3(0.f)}, outside = {1.f, v3(0.f)};  // glass
   float thinEta = 1.f;  // thin glass: 1 / eta
   V3 thinAtt = v3(0.f);
+  // principled map_baseColor / obj map_kd (null: none); mapAlpha: it has alpha
+  const Texture *map = nullptr;
+  bool mapAlpha = false;
 };
 // p: baseColor[3], roughness, metallic, opacity, ks[3], ns, tf[3], eta[3],
 // k[3], attenuationColor[3], attenuationDistance, thickness (24 floats, the
@@ -310,10 +314,11 @@ struct SurfaceBSDF {
   BSDFSample sample(V3 wo, V2 s, float ss) const;
 };
 // Material_dispatch_getBSDF for a hit with differential geometry dg; dPds the
-// instance's x axis (makeShadingFrame), cur the path's current medium
-SurfaceBSDF makeBSDF(const MaterialParams &m, const DG &dg, V3 dPds, const Medium &cur);
+// instance's x axis (makeShadingFrame), cur the path's current medium,
+// footprint the hit's pixel footprint for the colour map's level selection
+SurfaceBSDF makeBSDF(const MaterialParams &m, const DG &dg, V3 dPds, const Medium &cur, float footprint = 0.f);
 // Material_getTransparency for a shadow ray of direction rayDir
-V3 materialTransparency(const MaterialParams &m, const DG &dg, V3 rayDir, const Medium &cur);
+V3 materialTransparency(const MaterialParams &m, const DG &dg, V3 rayDir, const Medium &cur, float footprint = 0.f);
 // Material_selectNextMedium (glass; the others keep the medium)
 Medium nextMedium(const MaterialParams &m, const Medium &cur);
 

@@ -143,8 +143,9 @@ V2 PixelFilter::sample(V2 s) const {
   return {(uv.x - 0.5f) * width, (uv.y - 0.5f) * width};
 }
 
-DG postIntersect(const Scene &s, const Ray &ray, const Hit &hit) {
+DG postIntersect(const Scene &s, const Ray &ray, const Hit &hit, bool attrs) {
   DG dg;
+  dg.st = {hit.u, hit.v};
   dg.primID = hit.primID;
   dg.geomID = hit.geomID;
   dg.instID = hit.instID;
@@ -163,16 +164,41 @@ DG postIntersect(const Scene &s, const Ray &ray, const Hit &hit) {
     const V3 a = g.verts[q[0]], b = g.verts[q[1]], c = g.verts[q[2]], d = g.verts[q[3]];
     eps = reduce_max(vmax(vmax(vabs(a), vabs(b)), vmax(vabs(c), vabs(d)))) * ulpEpsilon;
     dPds = b - a;
+    dg.dPdt = d - a;
   } else if (g.type == 0) {
     // TriangleMesh_postIntersect (geometry/Mesh.ispc:178-276): dPds = vb - va without texcoords
-    const V3 a = g.verts[g.index[3 * hit.primID]], b = g.verts[g.index[3 * hit.primID + 1]],
-             c = g.verts[g.index[3 * hit.primID + 2]];
+    const uint32_t i0 = g.index[3 * hit.primID], i1 = g.index[3 * hit.primID + 1], i2 = g.index[3 * hit.primID + 2];
+    const V3 a = g.verts[i0], b = g.verts[i1], c = g.verts[i2];
     eps = reduce_max(vmax(vmax(vabs(a), vabs(b)), vabs(c))) * ulpEpsilon;
     dPds = b - a;
+    dg.dPdt = c - a;
+    if (attrs && !g.boxFaces) {
+      const float w0 = 1.f - hit.u - hit.v, w1 = hit.u, w2 = hit.v;
+      if (!g.normals.empty()) Ns = w0 * g.normals[i0] + w1 * g.normals[i1] + w2 * g.normals[i2];
+      if (!g.colors.empty()) {
+        const V4 c0 = g.colors[i0], c1 = g.colors[i1], c2 = g.colors[i2];
+        dg.color = {w0 * c0.x + w1 * c1.x + w2 * c2.x, w0 * c0.y + w1 * c1.y + w2 * c2.y,
+                    w0 * c0.z + w1 * c1.z + w2 * c2.z, w0 * c0.w + w1 * c1.w + w2 * c2.w};
+      }
+      if (!g.texcoords.empty()) {
+        const V2 t0 = g.texcoords[i0], t1 = g.texcoords[i1], t2 = g.texcoords[i2];
+        dg.st = {w0 * t0.x + w1 * t1.x + w2 * t2.x, w0 * t0.y + w1 * t1.y + w2 * t2.y};
+        const V2 d02 = {t0.x - t2.x, t0.y - t2.y}, d12 = {t1.x - t2.x, t1.y - t2.y};
+        const float det = d02.x * d12.y - d02.y * d12.x;
+        if (det != 0.f) {
+          const float inv = 1.f / det;
+          const V3 p02 = a - c, p12 = b - c;
+          dPds = (d12.y * p02 - d02.y * p12) * inv;
+          dg.dPdt = (d02.x * p12 - d12.x * p02) * inv;
+        }
+      }
+    }
   } else {
     eps = g.spheres[hit.primID].w * ulpEpsilon;
   }
   dg.dPds = xfmVector(e->xfm.l, dPds);  // Instance_postIntersect (common/Instance.ih:95-98)
+  dg.dPdt = xfmVector(e->xfm.l, dg.dPdt);
+  if (g.type != 0 || g.boxFaces) dg.st = {0.f, 0.f};  // spheres, boxes: no texture coordinates in these scenes
   // Instance_postIntersect: normals by the inverse transpose, epsilon by the
   // largest diagonal scale
   const L3 it = transposed(e->rcp.l);

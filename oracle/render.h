@@ -52,6 +52,19 @@ inline Ray cameraRay(const Camera &c, V2 screen) {
   return {c.org, c.nearClip, normalize(d), INFINITY};
 }
 
+// The camera ray's cone at `screen`, in units of the frame height (x: width,
+// y: dwdt): perspective 0 wide, widening by the image plane height x
+// rsqrt(|unnormalised direction|^2) (PerspectiveCamera.ispc:58-63);
+// orthographic as wide as the image height, parallel
+// (OrthographicCamera.ispc:52-53); panoramic pi sin(theta)
+// (PanoramicCamera.ispc:86-90); all times 1 / height (PathTracer.ispc:186-187)
+inline V2 cameraCone(const Camera &c, V2 screen, float rcpH) {
+  if (c.type == 1) return {length(c.dv_up) * rcpH, 0.f};
+  if (c.type == 2) return {0.f, 3.14159265358979323846f * std::sin(3.14159265358979323846f * screen.y) * rcpH};
+  const V3 d = c.dir_00 + screen.x * c.du_size + screen.y * c.dv_up;
+  return {0.f, length(c.dv_up) * (1.f / std::sqrt(dot(d, d))) * rcpH};
+}
+
 enum PixelFilterType { PF_POINT = 0, PF_BOX = 1, PF_GAUSS = 2, PF_MITCHELL = 3, PF_BLACKMAN_HARRIS = 4 };
 
 struct PixelFilter {
@@ -68,11 +81,25 @@ struct DG {
   V3 dPds;  // DG_TANGENTS: a mesh's first edge (Mesh.ispc:172-175), else (1, 0, 0); world space
   float epsilon;
   uint32_t primID, geomID, instID;
+  // with attrs: DG_COLOR (1 without vertex colours), DG_TEXCOORD (the hit's
+  // u, v without texture coordinates) and the second tangent dPdt
+  V4 color = {1.f, 1.f, 1.f, 1.f};
+  V2 st = {0.f, 0.f};
+  V3 dPdt = {0.f, 1.f, 0.f};
 };
 
-// postIntersect with DG_NG | DG_NS | DG_NORMALIZE | DG_FACEFORWARD (meshes
-// carry no per-vertex normals or colours in these scenes)
-DG postIntersect(const Scene &s, const Ray &ray, const Hit &hit);
+// postIntersect with DG_NG | DG_NS | DG_NORMALIZE | DG_FACEFORWARD; attrs
+// adds the triangle mesh's vertex normals, colours and texture coordinates
+// (TriangleMesh_postIntersect geometry/Mesh.ispc:178-276, QuadMesh's default
+// tangents :171-174, World.ih:397-407 defaults)
+DG postIntersect(const Scene &s, const Ray &ray, const Hit &hit, bool attrs = false);
+
+// World.ih:458-464: the ray cone's width projected onto the surface, in
+// texture space, times the renderer's mipBiasFactor
+inline float pixelFootprint(float coneWidth, V3 rayDir, const DG &dg, float mipBiasFactor) {
+  const float texArea = length(cross(dg.dPds, dg.dPdt));
+  return coneWidth / -dot(rayDir, dg.Ng) * (1.f / std::sqrt(texArea)) * mipBiasFactor;
+}
 
 struct FrameBuffer {
   int W = 0, H = 0;

@@ -286,6 +286,11 @@ bool traverseBLAS(const Geometry &g, V3 org, V3 dir, float tnear, Hit &hit, uint
       if (!h) continue;
       if (ANY) return true;
       const uint32_t prim = g.type == 0 ? p / g.primDiv : p;  // quads, boxes: the application primitive
+      // a quad's second triangle (v2, v3, v1) reports the quad's (u, v) = 1 - its own (Embree's quad hits)
+      if (g.type == 0 && g.primDiv == 2 && !g.boxFaces && (p & 1u)) {
+        u = 1.f - u;
+        v = 1.f - v;
+      }
       if (better(t, instID, geomID, prim, hit)) {
         hit.t = t;
         hit.u = u;

@@ -46,6 +46,10 @@ struct Geometry {
   uint32_t primDiv = 1;  // triangles per application primitive (quads 2, boxes 12): primID = p / primDiv
   bool boxFaces = false;  // box geometry as face triangles (no geometry epsilon)
   std::vector<V4> spheres;      // center, radius
+  // per-vertex attributes of a triangle mesh (empty: absent)
+  std::vector<V3> normals;
+  std::vector<V4> colors;
+  std::vector<V2> texcoords;
   // BVH2 (binned SAH)
   struct Node {
     Box box;

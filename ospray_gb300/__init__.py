@@ -78,7 +78,8 @@ class Material(ctypes.Structure):
                 ("type", ctypes.c_int), ("opacity", ctypes.c_float), ("ks", ctypes.c_float * 3),
                 ("ns", ctypes.c_float), ("tf", ctypes.c_float * 3), ("eta", ctypes.c_float * 3),
                 ("k", ctypes.c_float * 3), ("attenuationColor", ctypes.c_float * 3),
-                ("attenuationDistance", ctypes.c_float), ("thickness", ctypes.c_float)]
+                ("attenuationDistance", ctypes.c_float), ("thickness", ctypes.c_float),
+                ("baseColorMap", ctypes.c_void_p)]
 
 
 MATERIAL_PRINCIPLED, MATERIAL_OBJ, MATERIAL_METAL, MATERIAL_GLASS, MATERIAL_THINGLASS = 0, 1, 2, 3, 4
@@ -86,12 +87,15 @@ _MATERIAL_TYPES = {"principled": MATERIAL_PRINCIPLED, "obj": MATERIAL_OBJ, "meta
                    "glass": MATERIAL_GLASS, "thinGlass": MATERIAL_THINGLASS}
 
 
-def principled(base_color=(0.8, 0.8, 0.8), roughness=0.0, metallic=0.0, opacity=1.0):
-    return dict(type="principled", baseColor=base_color, roughness=roughness, metallic=metallic, opacity=opacity)
+def principled(base_color=(0.8, 0.8, 0.8), roughness=0.0, metallic=0.0, opacity=1.0, base_color_map=None):
+    """base_color_map: a Texture (map_baseColor)."""
+    return dict(type="principled", baseColor=base_color, roughness=roughness, metallic=metallic, opacity=opacity,
+                baseColorMap=base_color_map)
 
 
-def obj_material(kd=(0.8, 0.8, 0.8), ks=(0.0, 0.0, 0.0), ns=10.0, d=1.0, tf=(0.0, 0.0, 0.0)):
-    return dict(type="obj", baseColor=kd, ks=ks, ns=ns, opacity=d, tf=tf)
+def obj_material(kd=(0.8, 0.8, 0.8), ks=(0.0, 0.0, 0.0), ns=10.0, d=1.0, tf=(0.0, 0.0, 0.0), map_kd=None):
+    """map_kd: a Texture."""
+    return dict(type="obj", baseColor=kd, ks=ks, ns=ns, opacity=d, tf=tf, baseColorMap=map_kd)
 
 
 def metal(eta=(1.47, 0.984, 0.602), k=(7.64, 6.55, 5.36), roughness=0.1):
@@ -118,6 +122,9 @@ def material_struct(m):
         for key, val in m.items():
             if key == "type":
                 continue
+            if key == "baseColorMap":
+                out.baseColorMap = None if val is None else val._h.value
+                continue
             if isinstance(val, (tuple, list, np.ndarray)):
                 getattr(out, key)[:] = [float(x) for x in val]
             else:
@@ -135,7 +142,7 @@ class PTParams(ctypes.Structure):
                 ("lightSamples", ctypes.c_int), ("limitIndirectLightSamples", ctypes.c_int),
                 ("minContribution", ctypes.c_float), ("maxContribution", ctypes.c_float),
                 ("backgroundColor", ctypes.c_float * 4), ("pixelFilter", ctypes.c_int),
-                ("collectStats", ctypes.c_int)]
+                ("collectStats", ctypes.c_int), ("backplate", ctypes.c_void_p), ("mipMapBias", ctypes.c_float)]
 
 
 def quad_light(position, edge1, edge2, intensity=1.0, color=(1, 1, 1), visible=True):
@@ -212,7 +219,8 @@ def materials_array(mats):
 
 def pt_params(spp=1, max_path_length=20, roulette_path_length=5, max_scattering_events=20, light_samples=-1,
               limit_indirect_light_samples=True, min_contribution=0.001, max_contribution=float("inf"),
-              bg=(0, 0, 0, 0), pixel_filter=PF_GAUSS, stats=False):
+              bg=(0, 0, 0, 0), pixel_filter=PF_GAUSS, stats=False, backplate=None, mip_map_bias=0.0):
+    """backplate: a Texture (map_backplate) or None."""
     p = PTParams()
     p.pixelSamples, p.maxPathLength, p.roulettePathLength = int(spp), int(max_path_length), int(roulette_path_length)
     p.maxScatteringEvents, p.lightSamples = int(max_scattering_events), int(light_samples)
@@ -220,6 +228,8 @@ def pt_params(spp=1, max_path_length=20, roulette_path_length=5, max_scattering_
     p.minContribution, p.maxContribution = float(min_contribution), float(max_contribution)
     p.backgroundColor[:] = list(map(float, bg))
     p.pixelFilter, p.collectStats = int(pixel_filter), int(bool(stats))
+    p.backplate = None if backplate is None else backplate._h.value
+    p.mipMapBias = float(mip_map_bias)
     return p
 
 
@@ -343,6 +353,12 @@ def lib():
             "b200_scene_set_volume_transform": (I, [P, P]),
             "b200_render_scivis": (I, [P, ctypes.POINTER(CameraDesc), ctypes.POINTER(ScivisParams), P, I, P, P]),
             "b200_render_pt": (I, [P, ctypes.POINTER(CameraDesc), ctypes.POINTER(PTParams), P, I, P, P]),
+            "b200_scene_set_mesh_attributes": (I, [P, I, P, P, P]),
+            "b200_texture_create": (I, [P, I, I, I, I, I, I, I, P, ctypes.POINTER(P)]),
+            "b200_texture_release": (I, [P]),
+            "b200_texture_levels": (I, [P]),
+            "b200_texture_read_level": (I, [P, I, P, ctypes.c_size_t]),
+            "b200_texture_sample": (I, [P, I64, P, P, P]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -423,6 +439,60 @@ class Device:
             pass
 
 
+# OSPTextureFormat / OSPTextureFilter / OSPTextureWrapMode values
+(TEX_RGBA8, TEX_SRGBA, TEX_RGBA32F, TEX_RGB8, TEX_SRGB, TEX_RGB32F, TEX_R8, TEX_R32F, TEX_L8, TEX_RA8, TEX_LA8,
+ TEX_RGBA16, TEX_RGB16, TEX_RA16, TEX_R16, TEX_RA32F) = range(16)
+TEX_FILTER_LINEAR, TEX_FILTER_NEAREST = 0, 1
+TEX_WRAP_REPEAT, TEX_WRAP_MIRRORED_REPEAT, TEX_WRAP_CLAMP_TO_EDGE = 0, 1, 2
+_TEX_CHANNELS = {TEX_RGBA8: 4, TEX_SRGBA: 4, TEX_RGBA32F: 4, TEX_RGB8: 3, TEX_SRGB: 3, TEX_RGB32F: 3, TEX_R8: 1,
+                 TEX_R32F: 1, TEX_L8: 1, TEX_RA8: 2, TEX_LA8: 2, TEX_RGBA16: 4, TEX_RGB16: 3, TEX_RA16: 2,
+                 TEX_R16: 1, TEX_RA32F: 2}
+_TEX_DTYPE = {TEX_RGBA32F: np.float32, TEX_RGB32F: np.float32, TEX_R32F: np.float32, TEX_RA32F: np.float32,
+              TEX_RGBA16: np.uint16, TEX_RGB16: np.uint16, TEX_RA16: np.uint16, TEX_R16: np.uint16}
+
+
+class Texture:
+    """A 2D texture (texture2d): data (height, width[, channels]) with rows
+    from the bottom, of the dtype its format names (uint8, uint16, float32)."""
+
+    def __init__(self, device, data, format, filter=TEX_FILTER_LINEAR, wrap=(TEX_WRAP_REPEAT, TEX_WRAP_REPEAT),
+                 mipmaps=True):
+        a = np.ascontiguousarray(data, dtype=_TEX_DTYPE.get(format, np.uint8))
+        h, w = a.shape[0], a.shape[1]
+        if a.size != h * w * _TEX_CHANNELS[format]:
+            raise ValueError("texture data does not match its format")
+        if isinstance(wrap, int):
+            wrap = (wrap, wrap)
+        self.device, self.data, self.format = device, a, format
+        self._h = ctypes.c_void_p()
+        device._check(lib().b200_texture_create(device._h, w, h, format, filter, wrap[0], wrap[1], int(bool(mipmaps)),
+                                                _ptr(a), ctypes.byref(self._h)))
+
+    @property
+    def levels(self):
+        return lib().b200_texture_levels(self._h)
+
+    def read_level(self, level):
+        """The texels of one level (the MIP chain as generated on the device)."""
+        h, w = max(self.data.shape[0] >> level, 1), max(self.data.shape[1] >> level, 1)
+        out = np.empty((h, w) + self.data.shape[2:], dtype=self.data.dtype)
+        self.device._check(lib().b200_texture_read_level(self._h, level, _ptr(out), out.nbytes))
+        return out
+
+    def sample(self, st, footprint):
+        """Texture2D_get at texture coordinates st (n, 2) with pixel footprints (n,) or a scalar: (n, 4)."""
+        st = np.ascontiguousarray(st, dtype=np.float32).reshape(-1, 2)
+        fp = np.ascontiguousarray(np.broadcast_to(np.asarray(footprint, np.float32), (len(st),)))
+        out = np.zeros((len(st), 4), np.float32)
+        self.device._check(lib().b200_texture_sample(self._h, len(st), _ptr(st), _ptr(fp), _ptr(out)))
+        return out
+
+    def release(self):
+        if self._h:
+            lib().b200_texture_release(self._h)
+            self._h = ctypes.c_void_p()
+
+
 class Scene:
     """A committed world: geometries (BLAS each) and instance entries (TLAS)."""
 
@@ -438,6 +508,19 @@ class Scene:
         g = ctypes.c_int()
         self.device._check(lib().b200_scene_add_mesh(self._h, _ptr(v), len(v), _ptr(i), len(i), ctypes.byref(g)))
         return g.value
+
+    def set_mesh_attributes(self, geom, normal=None, color=None, texcoord=None):
+        """Per-vertex normals (n, 3), colours (n, 4 or 3: alpha 1) and texture
+        coordinates (n, 2) of triangle mesh `geom`, before the commit."""
+        n = None if normal is None else np.ascontiguousarray(normal, dtype=np.float32).reshape(-1, 3)
+        c = None
+        if color is not None:
+            c = np.asarray(color, dtype=np.float32)
+            if c.shape[-1] == 3:
+                c = np.concatenate([c.reshape(-1, 3), np.ones((c.size // 3, 1), np.float32)], axis=1)
+            c = np.ascontiguousarray(c, dtype=np.float32).reshape(-1, 4)
+        t = None if texcoord is None else np.ascontiguousarray(texcoord, dtype=np.float32).reshape(-1, 2)
+        self.device._check(lib().b200_scene_set_mesh_attributes(self._h, geom, _ptr(n), _ptr(c), _ptr(t)))
 
     def add_quad_mesh(self, vertex, index):
         """index: (n, 4) uint32 quads (Embree's decomposition into two triangles)."""

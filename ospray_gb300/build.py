@@ -41,7 +41,7 @@ NVCC_FLAGS = ARCH + [
     "-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr",
     "-Xcompiler", "-fPIC,-ffp-contract=off", "-I" + os.path.join(ROOT, "include"),
 ]
-CUDA_UNITS = ["bvh.cu", "render_ao.cu", "render_pt.cu", "render_volume.cu", "render_scivis.cu", "api.cu", "pt_noalloc.cu", "frame_ops.cu", "batch.cu", "nrc.cu"]
+CUDA_UNITS = ["bvh.cu", "render_ao.cu", "render_pt.cu", "render_volume.cu", "render_scivis.cu", "api.cu", "pt_noalloc.cu", "frame_ops.cu", "batch.cu", "nrc.cu", "texture.cu"]
 
 
 def nvcc():

@@ -244,6 +244,10 @@ MaterialD toMaterialD(const b200_material &m) {
     default:
       throw Error(B200_INVALID_ARGUMENT, "unknown material type " + std::to_string(m.type));
   }
+  if (m.baseColorMap && (m.type == B200_MATERIAL_PRINCIPLED || m.type == B200_MATERIAL_OBJ)) {
+    d.map = textureDevice(m.baseColorMap);
+    if (textureHasAlpha(m.baseColorMap)) d.flags |= MATF_MAP_ALPHA | MATF_TRANSPARENT;
+  }
   return d;
 }
 
@@ -257,23 +261,26 @@ bool anyTransparent(const b200_material *materials, int n) {
 // a type other than principled, or a material shadow rays pass through
 bool anyNonPrincipled(const b200_material *materials, int n) {
   for (int i = 0; i < n; i++)
-    if (materials[i].type != B200_MATERIAL_PRINCIPLED || (toMaterialD(materials[i]).flags & MATF_TRANSPARENT))
+    if (materials[i].type != B200_MATERIAL_PRINCIPLED || materials[i].baseColorMap ||
+        (toMaterialD(materials[i]).flags & MATF_TRANSPARENT))
       return true;
   return false;
 }
 
 // the renderer's material list on the device, uploaded when it changed
+// (compared as device records: a texture made again at a reused host address
+// still has a new device descriptor)
 void uploadMaterials(SceneObj *sc, const b200_material *materials, int nmaterials) {
+  std::vector<MaterialD> h(nmaterials);
+  bool transparent = false;
+  for (int i = 0; i < nmaterials; i++) {
+    h[i] = toMaterialD(materials[i]);
+    transparent = transparent || (h[i].flags & MATF_TRANSPARENT);
+  }
   const bool same = int(sc->lastMaterials.size()) == nmaterials &&
                     (nmaterials == 0 ||
-                     std::memcmp(sc->lastMaterials.data(), materials, sizeof(b200_material) * nmaterials) == 0);
+                     std::memcmp(sc->lastMaterials.data(), h.data(), sizeof(MaterialD) * nmaterials) == 0);
   if (!same) {
-    std::vector<MaterialD> h(nmaterials);
-    bool transparent = false;
-    for (int i = 0; i < nmaterials; i++) {
-      h[i] = toMaterialD(materials[i]);
-      transparent = transparent || (h[i].flags & MATF_TRANSPARENT);
-    }
     if (nmaterials > sc->capMaterials) {
       if (sc->dMaterials) cudaFree(sc->dMaterials);
       check(cudaMalloc(&sc->dMaterials, sizeof(MaterialD) * nmaterials), "alloc materials");
@@ -282,7 +289,7 @@ void uploadMaterials(SceneObj *sc, const b200_material *materials, int nmaterial
     if (nmaterials)
       check(cudaMemcpy(sc->dMaterials, h.data(), sizeof(MaterialD) * nmaterials, cudaMemcpyHostToDevice),
             "upload materials");
-    sc->lastMaterials.assign(materials, materials + nmaterials);
+    sc->lastMaterials = h;
     sc->transparentMaterials = transparent;
   }
   sc->nMaterials = nmaterials;
@@ -303,12 +310,20 @@ void ensurePtWorkspace(DeviceObj *dev, size_t need) {
 
 // PathTracer::commit (render/pathtracer/PathTracer.cpp:29-51): light sample
 // counts (lightSamples < 0: all lights at the first bounce; one after it
-// when limitIndirectLightSamples)
-PtParamsD makePtParams(const b200_pt_params &p, int nl, int nmaterials, bool transparentShadows,
-                       bool allMaterials) {
+// when limitIndirectLightSamples), the backplate and mipMapBias
+// (Renderer::commit render/Renderer.cpp:41-91).  Shadow rays loop over
+// closest hits when a material lets them through (`transparentMaterials`) or
+// vertex colours with alpha < 1 meet an obj material (its d scales by the
+// colour's alpha); the shading kernel with every material type runs for
+// other types than opaque principled, colour maps or vertex attributes.
+PtParamsD makePtParams(const b200_pt_params &p, const SceneObj *sc, const b200_material *materials, int nmaterials,
+                       bool transparentMaterials) {
+  const int nl = sc->nLights;
+  bool anyObj = false;
+  for (int i = 0; i < nmaterials; i++) anyObj = anyObj || materials[i].type == B200_MATERIAL_OBJ;
   PtParamsD d;
-  d.transparentShadows = transparentShadows ? 1 : 0;
-  d.allMaterials = allMaterials ? 1 : 0;
+  d.transparentShadows = transparentMaterials || (sc->colorAlpha && anyObj) ? 1 : 0;
+  d.allMaterials = anyNonPrincipled(materials, nmaterials) || sc->hasAttributes ? 1 : 0;
   d.spp = p.pixelSamples;
   d.maxPathLength = p.maxPathLength;
   d.roulettePathLength = p.roulettePathLength;
@@ -321,6 +336,8 @@ PtParamsD makePtParams(const b200_pt_params &p, int nl, int nmaterials, bool tra
   d.minContribution = p.minContribution;
   d.maxContribution = p.maxContribution;
   for (int k = 0; k < 4; k++) d.bg[k] = p.backgroundColor[k];
+  d.backplate = textureDevice(p.backplate);
+  d.mipBiasFactor = std::pow(2.f, p.mipMapBias);
   return d;
 }
 
@@ -416,6 +433,8 @@ SceneObj::~SceneObj() {
     if (g.dindex) cudaFreeAsync(g.dindex, st);
     if (g.dquad) cudaFreeAsync(g.dquad, st);
     if (g.dsph) cudaFreeAsync(g.dsph, st);
+    for (float *p : {g.dnormals, g.dcolors, g.dtexcoords})
+      if (p) cudaFreeAsync(p, st);
   }
   if (tlas.nodes) cudaFreeAsync(tlas.nodes, st);
   if (tlas.leafPrim) cudaFreeAsync(tlas.leafPrim, st);
@@ -446,6 +465,7 @@ void SceneObj::commit() {
     g.built = true;
   }
   // entries and their world boxes
+  hasAttributes = colorAlpha = false;
   std::vector<Entry> he(entries.size());
   std::vector<float4> lo(entries.size()), hi(entries.size());
   float wlo[3] = {INFINITY, INFINITY, INFINITY}, whi[3] = {-INFINITY, -INFINITY, -INFINITY};
@@ -461,6 +481,11 @@ void SceneObj::commit() {
     d.index = g.dquad ? g.dquad : g.dindex;
     d.meshKind = g.meshKind;
     d.spheres = g.dsph;
+    d.normals = g.dnormals;
+    d.colors = g.dcolors;
+    d.texcoords = g.dtexcoords;
+    hasAttributes = hasAttributes || g.dnormals || g.dcolors || g.dtexcoords;
+    colorAlpha = colorAlpha || g.colorAlpha;
     d.type = uint32_t(g.type);
     d.instID = e.instID;
     d.geomID = e.geomID;
@@ -735,6 +760,7 @@ int b200_scene_add_mesh(b200_scene s, const float *vertex, int64_t nverts, const
     GeomObj g;
     g.type = GEOM_TRIANGLES;
     g.nprims = ntris;
+    g.nverts = nverts;
     cudaStream_t st = sc->dev->stream;
     check(cudaMallocAsync(&g.dverts, sizeof(float) * 3 * size_t(nverts > 0 ? nverts : 1), st), "alloc vertices");
     check(cudaMallocAsync(&g.dindex, sizeof(uint32_t) * 3 * size_t(ntris > 0 ? ntris : 1), st), "alloc index");
@@ -743,6 +769,35 @@ int b200_scene_add_mesh(b200_scene s, const float *vertex, int64_t nverts, const
     check(cudaStreamSynchronize(st), "upload mesh");
     sc->geoms.push_back(g);
     if (geom_out) *geom_out = int(sc->geoms.size() - 1);
+  });
+}
+
+int b200_scene_set_mesh_attributes(b200_scene s, int geom, const float *normal, const float *color,
+                                   const float *texcoord) {
+  if (!s) return B200_INVALID_ARGUMENT;
+  SceneObj *sc = reinterpret_cast<SceneObj *>(s);
+  return guarded(sc->dev, [&]() {
+    require(geom >= 0 && geom < int(sc->geoms.size()), "bad geometry index");
+    GeomObj &g = sc->geoms[geom];
+    require(g.type == GEOM_TRIANGLES && g.meshKind == MESH_TRIANGLES,
+            "vertex attributes: triangle meshes only (quad meshes, boxes and spheres take none)");
+    require(!g.built, "vertex attributes: set them before the scene's commit");
+    cudaStream_t st = sc->dev->stream;
+    auto upload = [&](float *&dst, const float *src, int comps) {
+      if (dst) cudaFreeAsync(dst, st);
+      dst = nullptr;
+      if (!src || g.nverts == 0) return;
+      check(cudaMallocAsync(&dst, sizeof(float) * comps * size_t(g.nverts), st), "alloc vertex attributes");
+      check(cudaMemcpyAsync(dst, src, sizeof(float) * comps * size_t(g.nverts), cudaMemcpyHostToDevice, st),
+            "upload vertex attributes");
+    };
+    upload(g.dnormals, normal, 3);
+    upload(g.dcolors, color, 4);
+    g.colorAlpha = false;
+    for (int64_t i = 0; color && i < g.nverts; i++) g.colorAlpha = g.colorAlpha || color[4 * i + 3] != 1.f;
+    upload(g.dtexcoords, texcoord, 2);
+    check(cudaStreamSynchronize(st), "upload vertex attributes");
+    sc->committed = false;
   });
 }
 
@@ -1169,7 +1224,7 @@ int b200_render_pt(b200_scene s, const b200_camera_desc *camera, const b200_pt_p
     cudaStream_t st = stream ? (cudaStream_t)stream : sc->dev->stream;
     uploadMaterials(sc, materials, nmaterials);
     const PtParamsD d =
-        makePtParams(*p, sc->nLights, nmaterials, sc->transparentMaterials, anyNonPrincipled(materials, nmaterials));
+        makePtParams(*p, sc, materials, nmaterials, sc->transparentMaterials);
     DeviceObj *dev = sc->dev;
     ensurePtWorkspace(dev, ptWorkspaceBytes((long long)fb->W * fb->H * p->pixelSamples));
     fb->beginFrame(p->pixelSamples, st);

@@ -57,6 +57,9 @@ struct GeomObj {
   uint32_t *dindex = nullptr;  // 3 per BLAS triangle
   uint32_t *dquad = nullptr;   // quad meshes: the 4 indices per quad (postIntersect)
   uint32_t meshKind = MESH_TRIANGLES;
+  int64_t nverts = 0;
+  float *dnormals = nullptr, *dcolors = nullptr, *dtexcoords = nullptr;  // per-vertex attributes
+  bool colorAlpha = false;  // some vertex colour has alpha != 1
   float4 *dsph = nullptr;
   BLAS blas;
   bool built = false;
@@ -104,8 +107,10 @@ struct SceneObj {
   float *dVolData = nullptr, *dTfOpacity = nullptr;
   float3 *dTfColor = nullptr;
   uint8_t *dCellEmpty = nullptr;
-  std::vector<b200_material> lastMaterials;
+  std::vector<MaterialD> lastMaterials;  // the device records last uploaded
   bool transparentMaterials = false;  // some material of lastMaterials lets shadow rays through
+  // set at commit: some mesh has vertex attributes; some vertex colour has alpha < 1
+  bool hasAttributes = false, colorAlpha = false;
   explicit SceneObj(DeviceObj *d);
   ~SceneObj();
   void commit();
@@ -162,11 +167,14 @@ struct FrameObj {
 };
 
 CameraD makeCamera(const b200_camera_desc &c);
-PtParamsD makePtParams(const b200_pt_params &p, int numLights, int numMaterials, bool transparentShadows,
-                       bool allMaterials);
+PtParamsD makePtParams(const b200_pt_params &p, const SceneObj *sc, const b200_material *materials, int nmaterials,
+                       bool transparentMaterials);
 // b200_material -> device record (throws Error on an unknown type)
 MaterialD toMaterialD(const b200_material &m);
 bool anyTransparent(const b200_material *materials, int n);
+// the device descriptor of a texture (null for null)
+const TextureD *textureDevice(b200_texture t);
+bool textureHasAlpha(b200_texture t);
 bool anyNonPrincipled(const b200_material *materials, int n);
 void uploadMaterials(SceneObj *sc, const b200_material *materials, int nmaterials);
 void ensurePtWorkspace(DeviceObj *dev, size_t need);

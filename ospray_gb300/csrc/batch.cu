@@ -264,11 +264,18 @@ int b200_batch_add_pt(b200_batch h, b200_scene s, const b200_camera_desc *camera
     r.fb = fb;
     r.cam = *camera;
     r.pixelFilter = p->pixelFilter;
-    // the batched wavefront traces shadow rays as any-hit queries only
+    // the batched wavefront traces shadow rays as any-hit queries only and
+    // keeps no ray cones (texture level selection) in its path records
     requireArg(!anyTransparent(materials, nmaterials),
                "batch: materials that let shadow rays through (opacity < 1, obj tf / d, glass) are rendered by "
                "b200_render_pt only");
-    r.pt = makePtParams(*p, sc->nLights, nmaterials, false, true);
+    for (int i = 0; i < nmaterials; i++)
+      requireArg(!materials[i].baseColorMap, "batch: textured materials are rendered by b200_render_pt only");
+    requireArg(!p->backplate, "batch: a backplate is rendered by b200_render_pt only");
+    r.pt = makePtParams(*p, sc, materials, nmaterials, false);
+    requireArg(!r.pt.transparentShadows,
+               "batch: vertex colours with alpha < 1 under obj materials are rendered by b200_render_pt only");
+    r.pt.allMaterials = 1;
     r.ao = AOParamsD{};
     if (nmaterials) {
       std::vector<MaterialD> m(nmaterials);

@@ -140,6 +140,10 @@ struct Entry {
   uint32_t materialID;       // per-entry material slot (renderers)
   uint32_t meshKind;         // triangles: MESH_TRIANGLES, MESH_QUADS or MESH_BOXES
   uint32_t pad;
+  // per-vertex attributes of a triangle mesh (null: absent)
+  const float *normals;      // 3 per vertex
+  const float *colors;       // 4 per vertex
+  const float *texcoords;    // 2 per vertex
 };
 
 }  // namespace b200

@@ -102,6 +102,8 @@ struct PtParamsD {
   float bg[4];
   int transparentShadows;  // some material lets shadow rays through: shadow rays loop over closest hits
   int allMaterials;        // some material is not opaque principled: the shading kernel with every material type
+  const TextureD *backplate;  // the renderer's backplate (null: bg)
+  float mipBiasFactor;        // 2^mipMapBias
 };
 
 // structured-regular volume with its transfer function and macrocell

@@ -732,8 +732,7 @@ int b200_render_pt_nrc(b200_scene s, const b200_camera_desc *camera, const b200_
       throw Error(B200_INVALID_ARGUMENT, "bad radiance cache frame parameters");
     cudaStream_t st = stream ? (cudaStream_t)stream : sc->dev->stream;
     uploadMaterials(sc, materials, nmaterials);
-    const PtParamsD d = makePtParams(*p, sc->nLights, nmaterials, sc->transparentMaterials,
-                                     anyNonPrincipled(materials, nmaterials));
+    const PtParamsD d = makePtParams(*p, sc, materials, nmaterials, sc->transparentMaterials);
     DeviceObj *dev = sc->dev;
     const long long npaths = (long long)fb->W * fb->H * p->pixelSamples;
     ensurePtWorkspace(dev, ptWorkspaceBytes(npaths));

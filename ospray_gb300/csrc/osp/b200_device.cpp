@@ -27,6 +27,7 @@ bool known(OSPDataType kind, const std::string &t) {
     case OSP_VOLUME: return t == "structuredRegular";
     case OSP_TRANSFER_FUNCTION: return t == "piecewiseLinear";
     case OSP_IMAGE_OPERATION: return t == "tonemapper";
+    case OSP_TEXTURE: return t == "texture2d";
     default: return false;
   }
 }
@@ -130,6 +131,7 @@ OSPObject B200Device::newObject(OSPDataType kind, const char *type) {
     case OSP_VOLUME: o = new VolumeObj(kind, t); break;
     case OSP_TRANSFER_FUNCTION: o = new TransferFunctionObj(kind, t); break;
     case OSP_IMAGE_OPERATION: o = new ImageOpObj(kind, t); break;
+    case OSP_TEXTURE: o = new TextureObj(kind, t); break;
     default: break;
   }
   return reinterpret_cast<OSPObject>(static_cast<Obj *>(o));
@@ -278,9 +280,15 @@ OSPFuture B200Device::renderFrame(OSPFrameBuffer hf, OSPRenderer hr, OSPCamera h
     } else if (r->type == "pathtracer") {
       if (w->hasVolume) warn("pathtracer: volumes are not rendered by the b200 device");
       std::vector<b200_material> mats;
-      for (const auto &m : w->objectMaterials) mats.push_back(m->mat);
-      for (const auto &m : r->materials) mats.push_back(m->mat);
-      check(b200_render_pt(w->scene, &c->desc, &r->pt, mats.data(), int(mats.size()), f->fb, nullptr));
+      // texture handles as of now (a texture committed again since has a new one)
+      for (const auto *list : {&w->objectMaterials, &r->materials})
+        for (const auto &m : *list) {
+          mats.push_back(m->mat);
+          mats.back().baseColorMap = m->colorMapHandle();
+        }
+      b200_pt_params pt = r->pt;
+      pt.backplate = r->backplate ? r->backplate->tex : nullptr;
+      check(b200_render_pt(w->scene, &c->desc, &pt, mats.data(), int(mats.size()), f->fb, nullptr));
     } else {
       if (!w->hasGeometry && !w->hasVolume)
         throw Error(OSP_INVALID_OPERATION, "scivis renderer: the world has no geometry and no volume");

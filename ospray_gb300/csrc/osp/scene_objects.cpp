@@ -28,10 +28,53 @@ std::vector<Ref<T>> objectList(DataObj *d, OSPDataType kind, const char *what) {
 float length3(const float v[3]) { return std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]); }
 }  // namespace
 
+// ---------------------------------------------------------------- textures
+
+TextureObj::~TextureObj() {
+  if (tex) b200_texture_release(tex);
+}
+
+void TextureObj::commit(B200Device &dev) {
+  DataObj *d = getData("data");
+  if (!d || d->n[2] > 1)
+    throw Error(OSP_INVALID_ARGUMENT, "texture2d must have 2D 'data' array using the first two dimensions");
+  const int format = getInt("format", OSP_TEXTURE_FORMAT_INVALID);
+  if (format == OSP_TEXTURE_FORMAT_INVALID) throw Error(OSP_INVALID_ARGUMENT, "texture2d: invalid 'format'");
+  const int filter = getInt("filter", OSP_TEXTURE_FILTER_LINEAR);
+  int wrap[2] = {OSP_TEXTURE_WRAP_REPEAT, OSP_TEXTURE_WRAP_REPEAT};
+  const Param *wp = find("wrapMode");
+  if (wp && (wp->type == OSP_VEC2UI || wp->type == OSP_VEC2I)) {
+    std::memcpy(wrap, wp->bytes.data(), 8);
+  } else if (wp) {
+    wrap[0] = wrap[1] = getInt("wrapMode", OSP_TEXTURE_WRAP_REPEAT);
+  }
+  static const int texel[16] = {4, 4, 16, 3, 3, 12, 1, 4, 1, 2, 2, 8, 6, 4, 2, 8};
+  if (format < 0 || format > 15)
+    throw Error(OSP_INVALID_ARGUMENT, "texture2d: 'format' not supported by the b200 device (half-float formats)");
+  if (size_t(texel[format]) != sizeOfType(d->elem))
+    throw Error(OSP_INVALID_ARGUMENT, "texture2d: 'format' does not match the type of 'data'");
+  const auto bytes = d->compact();
+  b200_texture t = nullptr;
+  dev.check(b200_texture_create(dev.handle(), int(d->n[0]), int(d->n[1]), format, filter, wrap[0], wrap[1], 1,
+                                bytes.data(), &t));
+  if (tex) b200_texture_release(tex);
+  tex = t;
+}
+
+namespace {
+// a texture parameter (the object itself, as OSPRay's getParamObject<Texture>)
+Ref<TextureObj> textureParam(Obj &o, const char *name) {
+  return Ref<TextureObj>(static_cast<TextureObj *>(o.getObject(name, OSP_TEXTURE)));
+}
+}  // namespace
+
 // ---------------------------------------------------------------- geometry
 
-void GeometryObj::commit(B200Device &) {
+void GeometryObj::commit(B200Device &dev) {
   verts.clear();
+  normals.clear();
+  colors.clear();
+  texcoords.clear();
   index.clear();
   spheres.clear();
   boxes.clear();
@@ -52,6 +95,35 @@ void GeometryObj::commit(B200Device &) {
     std::memcpy(index.data(), ib.data(), ib.size());
     for (uint32_t i : index)
       if (i >= v->count()) throw Error(OSP_INVALID_ARGUMENT, "mesh: index out of range of 'vertex.position'");
+    // per-vertex attributes (Mesh::commit geometry/Mesh.cpp:37-113)
+    auto attr = [&](const char *name, OSPDataType want, std::vector<float> &dst, int comps) {
+      DataObj *a = getData(name);
+      if (!a) return;
+      const bool rgb = comps == 4 && a->elem == OSP_VEC3F;
+      if (a->elem != want && !rgb)
+        throw Error(OSP_INVALID_ARGUMENT, std::string("mesh: '") + name + "' has an unsupported element type");
+      if (a->count() != v->count())
+        throw Error(OSP_INVALID_ARGUMENT, std::string("mesh: '") + name + "' must have one element per vertex");
+      const auto b = a->compact();
+      dst.resize(a->count() * comps);
+      if (rgb) {
+        for (uint64_t i = 0; i < a->count(); i++) {
+          std::memcpy(&dst[4 * i], b.data() + 12 * i, 12);
+          dst[4 * i + 3] = 1.f;
+        }
+      } else {
+        std::memcpy(dst.data(), b.data(), b.size());
+      }
+    };
+    attr("vertex.normal", OSP_VEC3F, normals, 3);
+    attr("vertex.color", OSP_VEC4F, colors, 4);
+    attr("vertex.texcoord", OSP_VEC2F, texcoords, 2);
+    if (quads && (!normals.empty() || !colors.empty() || !texcoords.empty())) {
+      dev.warn("mesh: per-vertex attributes of quad meshes are not supported by the b200 device; ignored");
+      normals.clear();
+      colors.clear();
+      texcoords.clear();
+    }
   } else if (type == "box") {
     // Boxes::commit (geometry/Boxes.cpp:33-46): "box" data of box3f
     DataObj *b = getData("box");
@@ -113,6 +185,7 @@ void MaterialObj::commit(B200Device &dev) {
     b200_material_defaults(&mat, B200_MATERIAL_PRINCIPLED);
     const float def[3] = {0.8f, 0.8f, 0.8f};
     getVec3("baseColor", mat.baseColor, def);
+    colorMap = textureParam(*this, "map_baseColor");
     mat.roughness = getFloat("roughness", 0.f);
     mat.metallic = getFloat("metallic", 0.f);
     mat.opacity = getFloat("opacity", 1.f);
@@ -136,6 +209,8 @@ void MaterialObj::commit(B200Device &dev) {
     getVec3("kd", kd, def);
     getVec3("ks", ks, kZero3);
     getVec3("tf", tf, kZero3);
+    colorMap = textureParam(*this, "map_kd");
+    if (!colorMap) colorMap = textureParam(*this, "map_Kd");
     // the path tracer gets the raw parameters (the device scales kd + ks + tf
     // down to 1 itself); SciVis reads the scaled ones
     for (int k = 0; k < 3; k++) {
@@ -186,6 +261,8 @@ void MaterialObj::commit(B200Device &dev) {
     mat.attenuationDistance = getFloat("attenuationDistance", 1.f);
     mat.thickness = getFloat("thickness", 1.f);
   }
+  if (type != "principled" && type != "obj") colorMap = Ref<TextureObj>();
+  mat.baseColorMap = nullptr;  // set from colorMap at each render
 }
 
 void GeometricModelObj::commit(B200Device &) {
@@ -397,9 +474,14 @@ void WorldObj::commit(B200Device &dev) {
           if (g->type == "mesh" && g->quads)
             dev.check(b200_scene_add_quad_mesh(s, g->verts.data(), int64_t(g->verts.size() / 3), g->index.data(),
                                                int64_t(g->index.size() / 4), &gi));
-          else if (g->type == "mesh")
+          else if (g->type == "mesh") {
             dev.check(b200_scene_add_mesh(s, g->verts.data(), int64_t(g->verts.size() / 3), g->index.data(),
                                           int64_t(g->index.size() / 3), &gi));
+            if (!g->normals.empty() || !g->colors.empty() || !g->texcoords.empty())
+              dev.check(b200_scene_set_mesh_attributes(s, gi, g->normals.empty() ? nullptr : g->normals.data(),
+                                                       g->colors.empty() ? nullptr : g->colors.data(),
+                                                       g->texcoords.empty() ? nullptr : g->texcoords.data()));
+          }
           else if (g->type == "box")
             dev.check(b200_scene_add_boxes(s, g->boxes.data(), int64_t(g->boxes.size() / 6), &gi));
           else
@@ -470,6 +552,7 @@ void RendererObj::commit(B200Device &) {
   const int maxDepth = std::max(0, getInt("maxPathLength", 20));
   const float minContribution = getFloat("minContribution", 0.001f);
   materials = objectList<MaterialObj>(getData("material"), OSP_MATERIAL, "renderer 'material'");
+  backplate = textureParam(*this, "map_backplate");
   if (type == "ao") {
     ao.pixelSamples = spp;
     ao.aoSamples = getInt("aoSamples", 1);
@@ -491,6 +574,8 @@ void RendererObj::commit(B200Device &) {
     std::memcpy(pt.backgroundColor, bg, 16);
     pt.pixelFilter = pf;
     pt.collectStats = 0;
+    pt.backplate = backplate ? backplate->tex : nullptr;
+    pt.mipMapBias = getFloat("mipMapBias", 0.f);
   } else {  // scivis (SciVis::commit, render/scivis/SciVis.cpp:27-36)
     scivis.pixelSamples = spp;
     scivis.volumeSamplingRate = getFloat("volumeSamplingRate", 1.f);

@@ -2,7 +2,8 @@
 // reference's module_cpu that the GB300 path implements:
 // geometry/registration.cpp "mesh", "sphere"; camera "perspective";
 // render/registration.cpp "ao", "scivis", "pathtracer", "principled",
-// "obj"; lights/registration.cpp "quad", "ambient"; volume
+// "obj"; lights/registration.cpp "quad", "ambient"; texture/registration
+// "texture2d"; volume
 // "structuredRegular"; transferFunction "piecewiseLinear";
 // fb/registration.cpp "tonemapper").  commit() reads the parameters each
 // type understands (names and defaults of the reference's ::commit methods,
@@ -22,10 +23,22 @@ struct SceneObj : Obj {
   virtual void commit(B200Device &) {}
 };
 
+// Texture2D::commit (texture/Texture2D.cpp:55-135): "data" (2D), "format",
+// "filter", "wrapMode"; the MIP chain is generated on the device
+struct TextureObj : SceneObj {
+  using SceneObj::SceneObj;
+  ~TextureObj() override;
+  b200_texture tex = nullptr;
+  void commit(B200Device &) override;
+};
+
 // Mesh::commit (geometry/Mesh.cpp:37-204), Spheres::commit (geometry/Spheres.cpp:46-106)
 struct GeometryObj : SceneObj {
   using SceneObj::SceneObj;
   std::vector<float> verts;     // mesh: xyz per vertex
+  // mesh: "vertex.normal" (3), "vertex.color" (4; vec3f gets alpha 1) and
+  // "vertex.texcoord" (2) per vertex, empty when absent
+  std::vector<float> normals, colors, texcoords;
   std::vector<uint32_t> index;  // mesh: 3 per triangle, or 4 per quad when quads
   bool quads = false;           // mesh with a vec4ui "index"
   std::vector<float> spheres;   // sphere: xyzr per sphere
@@ -39,7 +52,9 @@ struct GeometryObj : SceneObj {
 // GB300 path tracer evaluates
 struct MaterialObj : SceneObj {
   using SceneObj::SceneObj;
-  b200_material mat = {};        // as the path tracer reads it
+  Ref<TextureObj> colorMap;      // principled "map_baseColor" / obj "map_kd"
+  b200_material mat = {};        // as the path tracer reads it (baseColorMap: see colorMapHandle)
+  b200_texture colorMapHandle() const { return colorMap ? colorMap->tex : nullptr; }
   b200_scivis_material sv = {};  // as the SciVis renderer reads it
   void commit(B200Device &) override;
 };
@@ -129,6 +144,7 @@ struct RendererObj : SceneObj {
   b200_pt_params pt = {};
   b200_scivis_params scivis = {};
   std::vector<Ref<MaterialObj>> materials;  // the "material" list
+  Ref<TextureObj> backplate;                // "map_backplate"
   float varianceThreshold = 0.f;
   void commit(B200Device &) override;
 };

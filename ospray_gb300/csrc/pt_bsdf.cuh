@@ -9,6 +9,7 @@
 //   lights/AmbientLight.ispc:17-57
 #pragma once
 #include "render_common.cuh"
+#include "texture.cuh"
 
 namespace b200 {
 
@@ -20,6 +21,7 @@ constexpr float MAT_EPS = 1e-6f;
 // b200_material (parameters normalised as each type's commit does).
 enum : uint32_t { MAT_PRINCIPLED = 0, MAT_OBJ = 1, MAT_METAL = 2, MAT_GLASS = 3, MAT_THINGLASS = 4 };
 constexpr uint32_t MATF_TRANSPARENT = 1u;  // getTransparency can be non-zero (shadow rays continue through it)
+constexpr uint32_t MATF_MAP_ALPHA = 2u;    // the colour map has alpha (it scales opacity / d)
 
 struct __align__(16) MaterialD {
   float r, g, b, roughness;  // principled baseColor, roughness; obj kd (scaled); metal roughness
@@ -31,8 +33,10 @@ struct __align__(16) MaterialD {
   float ck[3], pad1;         // metal: k per channel
   float att[3], iorIn;       // glass: inside medium attenuation (log(colour) / distance) and ior; thin glass: attenuation
   float attOut[3], iorOut;   // glass: outside medium
+  const TextureD *map;       // principled map_baseColor / obj map_kd (null: none)
+  uint32_t pad2, pad3;
 };
-static_assert(sizeof(MaterialD) == 128, "MaterialD layout");
+static_assert(sizeof(MaterialD) == 144, "MaterialD layout");
 
 // scattering types (render/pathtracer/Scattering.ih:8-47)
 constexpr uint32_t ST_SPEC_R = 1u, ST_GLOSSY_R = 2u, ST_DIFFUSE_R = 4u, ST_SPEC_T = 8u, ST_GLOSSY_T = 16u,
@@ -427,10 +431,16 @@ struct PrincipledBsdfT {
     return a;
   }
   B200_D void init(const MaterialD &m, V3 U, V3 V, V3 Nn, const AlbedoTablesD *T) {
-    op = clamp01f(m.opacity);
+    init(m, U, V, Nn, T, clamp01f(m.opacity));
+  }
+  // opacity: the material's opacity times its colour map's alpha (clamped);
+  // the stack exists for the material's own opacity > EPS, the cut-out child
+  // for its own opacity < 1 - EPS or a colour map with alpha
+  B200_D void init(const MaterialD &m, V3 U, V3 V, V3 Nn, const AlbedoTablesD *T, float opacity) {
+    op = opacity;
     tr = CUT ? 1.f - op : 0.f;
     hasStack = !CUT || m.opacity > MAT_EPS;
-    hasCut = CUT && 1.f - m.opacity > MAT_EPS;
+    hasCut = CUT && (1.f - m.opacity > MAT_EPS || (m.flags & MATF_MAP_ALPHA) != 0);
     if (hasStack) {
       st.init(m, U, V, Nn, T);
     } else {
@@ -859,20 +869,55 @@ B200_D bool glassFromOutside(const MaterialD *mats, uint32_t mat, uint32_t cur) 
   return sameMedium(mediumOf(mats, cur), mediumOf(mats, 2u * mat + 1u));
 }
 
+// The colour map's texel at a hit (Texture2D_get with the hit's texture
+// coordinates and pixel footprint), 1 without a map.
+B200_D float4 colorMapTexel(const MaterialD &m, const DGAttr &at, float footprint) {
+  return m.map ? texGet(*m.map, at.s, at.t, footprint) : make_float4(1.f, 1.f, 1.f, 1.f);
+}
+
+// A material's parameters at a hit with its colour map and the vertex colour
+// applied (Principled.ispc:110-135: baseColor x map.rgb x colour.rgb,
+// clamped, opacity x map alpha; OBJ.ispc:52-66: d x colour alpha x map alpha,
+// kd x map.rgb x colour.rgb).  `opacity` gets principled's effective opacity
+// (the material's own stays in the record); obj's d goes into the record.
+B200_D MaterialD shadedMaterial(const MaterialD &m, const DGAttr &at, float footprint, float &opacity) {
+  MaterialD r = m;
+  opacity = clamp01f(m.opacity);
+  if (m.kind == MAT_PRINCIPLED) {
+    const float4 tx = colorMapTexel(m, at, footprint);
+    r.r = clamp01f(m.r * tx.x * at.color.x);
+    r.g = clamp01f(m.g * tx.y * at.color.y);
+    r.b = clamp01f(m.b * tx.z * at.color.z);
+    if (m.flags & MATF_MAP_ALPHA) opacity *= tx.w;
+  } else if (m.kind == MAT_OBJ) {
+    const float4 tx = colorMapTexel(m, at, footprint);
+    r.opacity = m.opacity * at.color.w * tx.w;
+    r.r = m.r * tx.x * at.color.x;
+    r.g = m.g * tx.y * at.color.y;
+    r.b = m.b * tx.z * at.color.z;
+  }
+  return r;
+}
+
 // Material_getTransparency of the hit material for a shadow ray
-// (TransparentShadow.ispc:18-85): principled 1 - opacity, obj tf d + 1 - d,
-// glass 1 - Fresnel, thin glass the slab's transmission, metal 0.
-B200_D V3 materialTransparency(const MaterialD *mats, uint32_t mi, V3 rayDir, V3 Ns, uint32_t medium) {
+// (TransparentShadow.ispc:18-85): principled 1 - opacity (Principled.ispc:
+// 432-580, the opaque base passes nothing), obj tf d + 1 - d (OBJ.ispc:
+// 93-110), glass 1 - Fresnel, thin glass the slab's transmission, metal 0;
+// opacity and d with the colour map's alpha and the vertex colour's alpha.
+B200_D V3 materialTransparency(const MaterialD *mats, uint32_t mi, V3 rayDir, V3 Ns, uint32_t medium,
+                               const DGAttr &at, float footprint) {
   const MaterialD &m = mats[mi];
   switch (m.kind) {
     case MAT_PRINCIPLED: {
-      const float op = clamp01f(m.opacity);
+      float op = clamp01f(m.opacity);
+      if (m.flags & MATF_MAP_ALPHA) op *= colorMapTexel(m, at, footprint).w;
       const float tr = 1.f - op;
       if (tr <= MAT_EPS) return splat(0.f);
       return splat(tr);
     }
     case MAT_OBJ: {
-      const float d = m.opacity;
+      float d = m.opacity * at.color.w;
+      if (m.flags & MATF_MAP_ALPHA) d *= colorMapTexel(m, at, footprint).w;
       return mk(m.tf[0], m.tf[1], m.tf[2]) * d + splat(1.f - d);
     }
     case MAT_GLASS: {

@@ -151,8 +151,7 @@ int b200_render_pt_noalloc(b200_scene s, const b200_camera_desc *camera, const b
                           cudaMemcpyHostToDevice, st);
       if (e != cudaSuccess) return fail(B200_UNKNOWN_ERROR, std::string("upload materials: ") + cudaGetErrorString(e));
     }
-    const PtParamsD d =
-        makePtParams(*p, sc->nLights, nmaterials, transparent, anyNonPrincipled(materials, nmaterials));
+    const PtParamsD d = makePtParams(*p, sc, materials, nmaterials, transparent);
     fb->beginFrame(p->pixelSamples, st);
     e = launchRenderPT(dev->tables, sc->view(), makeCamera(*camera), dev->filter(p->pixelFilter), d,
                        reinterpret_cast<const MaterialD *>(base + OFF_MATERIALS), sc->dLights, sc->dLightCdf,

@@ -120,8 +120,40 @@ struct DG {
   uint32_t entry;
 };
 
-// postIntersect with DG_NG | DG_NS | DG_NORMALIZE | DG_FACEFORWARD
-B200_D DG postIntersect(const Scene &sc, const Ray &ray, const HitRec &hit) {
+// What the path tracer's materials read beyond DG (DG_COLOR, DG_TEXCOORD and
+// the second tangent of DG_TANGENTS): the interpolated vertex colour (1 when
+// the mesh has none), the texture coordinates (the hit's u, v when the mesh
+// has none, World.ih postIntersect) and dPdt, in world space.
+// The hit's barycentric u, v are recomputed here from the hit point rather
+// than carried from traversal (the closest-hit kernel stays as small as it
+// is): triangles (a, b, c) give P = a + u (b - a) + v (c - a); quads
+// (v0, v1, v2, v3) the same over (v0, v1, v3), which is the quad's bilinear
+// (u, v) for a parallelogram; spheres and boxes 0.
+struct DGAttr {
+  float4 color;
+  float s, t;
+  V3 dPdt;
+};
+
+// (u, v) with P = a + u (b - a) + v (c - a) for the hit at distance t, in the
+// entry's object space: least squares over the plane of (a, b, c)
+B200_D float2 hitBarycentrics(const Entry &e, const Ray &ray, float t, V3 a, V3 b, V3 c) {
+  V3 P = add(ray.org, mul(t, ray.dir));
+  if (!e.identity) P = xfmPoint(e.rcp, P);
+  const V3 e1 = sub(b, a), e2 = sub(c, a), d = sub(P, a);
+  const float d11 = dot(e1, e1), d12 = dot(e1, e2), d22 = dot(e2, e2);
+  const float r1 = dot(d, e1), r2 = dot(d, e2);
+  const float det = d11 * d22 - d12 * d12;
+  if (!(det > 0.f)) return make_float2(0.f, 0.f);
+  const float inv = 1.f / det;
+  return make_float2((d22 * r1 - d12 * r2) * inv, (d11 * r2 - d12 * r1) * inv);
+}
+
+// postIntersect with DG_NG | DG_NS | DG_NORMALIZE | DG_FACEFORWARD (and with
+// ATTR also DG_COLOR | DG_TEXCOORD and the mesh's vertex normals:
+// TriangleMesh_postIntersect geometry/Mesh.ispc:178-276)
+template <bool ATTR = false>
+B200_D DG postIntersect(const Scene &sc, const Ray &ray, const HitRec &hit, DGAttr *at = nullptr) {
   DG dg;
   dg.entry = hit.entry;
   const Entry &e = sc.entries[hit.entry];
@@ -130,7 +162,11 @@ B200_D DG postIntersect(const Scene &sc, const Ray &ray, const HitRec &hit) {
   // DG_TANGENTS: meshes take their first edge (TriangleMesh_postIntersect
   // geometry/Mesh.ispc:172-175, QuadMesh_postIntersect :171-174), other
   // geometry keeps the default (1, 0, 0) (World.ih postIntersect)
-  V3 dPds = mk(1.f, 0.f, 0.f);
+  V3 dPds = mk(1.f, 0.f, 0.f), dPdt = mk(0.f, 1.f, 0.f);
+  if (ATTR) {
+    at->color = make_float4(1.f, 1.f, 1.f, 1.f);
+    at->s = at->t = 0.f;
+  }
   float eps;
   if (e.type == GEOM_TRIANGLES && e.meshKind == MESH_BOXES) {
     eps = 0.f;  // Boxes_postIntersect (geometry/Boxes.ispc) sets no geometry epsilon
@@ -138,15 +174,21 @@ B200_D DG postIntersect(const Scene &sc, const Ray &ray, const HitRec &hit) {
     // QuadMesh_postIntersect (geometry/Mesh.ispc:67-176): epsilon over the 4 vertices
     const uint4 q = __ldg(reinterpret_cast<const uint4 *>(e.index) + hit.primID);
     const uint32_t ix[4] = {q.x, q.y, q.z, q.w};
-    V3 m = splat(0.f), v[2];
+    V3 m = splat(0.f), v[4];
 #pragma unroll
     for (int k = 0; k < 4; k++) {
       const V3 p = mk(__ldg(e.verts + 3 * ix[k]), __ldg(e.verts + 3 * ix[k] + 1), __ldg(e.verts + 3 * ix[k] + 2));
-      if (k < 2) v[k] = p;
+      v[k] = p;
       m = vmax(m, vabs(p));
     }
     eps = fmul(reduce_max(m), ULP_EPSILON);
     dPds = sub(v[1], v[0]);
+    if (ATTR) {
+      dPdt = sub(v[3], v[0]);
+      const float2 uv = hitBarycentrics(e, ray, hit.t, v[0], v[1], v[3]);
+      at->s = uv.x;
+      at->t = uv.y;
+    }
   } else if (e.type == GEOM_TRIANGLES) {
     const uint32_t i0 = __ldg(e.index + 3 * hit.primID), i1 = __ldg(e.index + 3 * hit.primID + 1),
                    i2 = __ldg(e.index + 3 * hit.primID + 2);
@@ -155,6 +197,41 @@ B200_D DG postIntersect(const Scene &sc, const Ray &ray, const HitRec &hit) {
     const V3 c = mk(__ldg(e.verts + 3 * i2), __ldg(e.verts + 3 * i2 + 1), __ldg(e.verts + 3 * i2 + 2));
     eps = fmul(reduce_max(vmax(vmax(vabs(a), vabs(b)), vabs(c))), ULP_EPSILON);
     dPds = sub(b, a);
+    if (ATTR) {
+      dPdt = sub(c, a);
+      // barycentric weights (1 - u - v, u, v) of vertices (i0, i1, i2)
+      const float2 uv = hitBarycentrics(e, ray, hit.t, a, b, c);
+      at->s = uv.x;
+      at->t = uv.y;
+      const float w0 = 1.f - uv.x - uv.y, w1 = uv.x, w2 = uv.y;
+      if (e.normals) {
+        const float *n = e.normals;
+        Ns = mk(w0 * __ldg(n + 3 * i0) + w1 * __ldg(n + 3 * i1) + w2 * __ldg(n + 3 * i2),
+                w0 * __ldg(n + 3 * i0 + 1) + w1 * __ldg(n + 3 * i1 + 1) + w2 * __ldg(n + 3 * i2 + 1),
+                w0 * __ldg(n + 3 * i0 + 2) + w1 * __ldg(n + 3 * i1 + 2) + w2 * __ldg(n + 3 * i2 + 2));
+      }
+      if (e.colors) {
+        const float4 *cl = reinterpret_cast<const float4 *>(e.colors);
+        const float4 c0 = __ldg(cl + i0), c1 = __ldg(cl + i1), c2 = __ldg(cl + i2);
+        at->color = make_float4(w0 * c0.x + w1 * c1.x + w2 * c2.x, w0 * c0.y + w1 * c1.y + w2 * c2.y,
+                                w0 * c0.z + w1 * c1.z + w2 * c2.z, w0 * c0.w + w1 * c1.w + w2 * c2.w);
+      }
+      if (e.texcoords) {
+        const float2 *tc = reinterpret_cast<const float2 *>(e.texcoords);
+        const float2 t0 = __ldg(tc + i0), t1 = __ldg(tc + i1), t2 = __ldg(tc + i2);
+        at->s = w0 * t0.x + w1 * t1.x + w2 * t2.x;
+        at->t = w0 * t0.y + w1 * t1.y + w2 * t2.y;
+        // tangents along the texture axes where the texture map is not degenerate
+        const float ds02 = t0.x - t2.x, dt02 = t0.y - t2.y, ds12 = t1.x - t2.x, dt12 = t1.y - t2.y;
+        const float det = ds02 * dt12 - dt02 * ds12;
+        if (det != 0.f) {
+          const float inv = 1.f / det;
+          const V3 dp02 = sub(a, c), dp12 = sub(b, c);
+          dPds = mul(sub(mul(dt12, dp02), mul(dt02, dp12)), inv);
+          dPdt = mul(sub(mul(ds02, dp12), mul(ds12, dp02)), inv);
+        }
+      }
+    }
   } else {
     eps = fmul(__ldg(&e.spheres[hit.primID].w), ULP_EPSILON);
   }
@@ -163,8 +240,10 @@ B200_D DG postIntersect(const Scene &sc, const Ray &ray, const HitRec &hit) {
     Ng = xfmVectorT(e.rcp, Ng);
     eps = fmul(eps, e.epsScale);
     dPds = xfmVector(e.xfm, dPds);  // Instance_postIntersect (common/Instance.ih:95-98)
+    if (ATTR) dPdt = xfmVector(e.xfm, dPdt);
   }
   dg.dPds = dPds;
+  if (ATTR) at->dPdt = dPdt;
   const float e2 = fmul(fmaxf(reduce_max(vabs(dg.P)), fmul(reduce_max(vabs(ray.dir)), hit.t)), ULP_EPSILON);
   dg.epsilon = fmaxf(eps, e2);
   V3 ffnng = normalize(Ng);
@@ -179,6 +258,15 @@ B200_D DG postIntersect(const Scene &sc, const Ray &ray, const HitRec &hit) {
   dg.Ns = Ns;
   dg.P = add(dg.P, mul(dg.epsilon, ffnng));
   return dg;
+}
+
+// the pixel footprint of a hit for texture level selection (World.ih
+// postIntersect: the ray cone's width projected onto the surface, in texture
+// space, times 2^mipMapBias); coneWidth: the cone's width at the hit
+B200_D float pixelFootprint(float coneWidth, V3 rayDir, const DG &dg, const DGAttr &at, float mipBias) {
+  const V3 x = cross(dg.dPds, at.dPdt);
+  const float texArea = sqrtf(dot(x, x));
+  return coneWidth / -dot(rayDir, dg.Ng) * (1.f / sqrtf(texArea)) * mipBias;
 }
 
 // Shading frame around N (rkcommon frame(N))

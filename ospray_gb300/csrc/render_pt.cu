@@ -5,7 +5,9 @@
 //   nextEventEstimation     render/pathtracer/NextEventEstimation.ispc:25-160
 //   evaluateVirtualLights   render/pathtracer/VirtualLight.ispc:38-107
 //   transparentShadow       render/pathtracer/TransparentShadow.ispc:18-85
-//     (all materials here are opaque, so a shadow ray is an any-hit query)
+//     (scenes whose materials are all opaque trace shadow rays as any-hit queries)
+//   ray cones               common/World.ih:458-464 (postIntersect), camera
+//                           initRay (camera/*Camera.ispc), PathTracer.ispc:186-187
 //   misHeuristic            render/pathtracer/PathTracerUtil.ih:30-46
 // and, for AO requests of a batch, AORenderer_renderSample
 // (render/ao/AORenderer.ispc:23-149) with its AO rays in the shadow queue.
@@ -31,6 +33,8 @@ struct PtCtx {
   const AlbedoTablesD *AT;
   int frameID;
   float *aux;  // per pixel: sums of the first vertices' normal and albedo (null: not wanted)
+  int W;       // single frames: framebuffer width and reciprocal size (backplate lookups)
+  float rcpW, rcpH;
 };
 
 struct PathResult {
@@ -54,10 +58,11 @@ struct __align__(16) PathRec {
   float4 dir;   // ray direction, last vertex BSDF pdf
   float4 thr;   // throughput, alpha
   float4 con;   // contribution, medium id (bits)
-  float4 lastP; // previous vertex position, (unused)
-  float4 lastN; // previous vertex shading normal, (unused)
+  float4 lastP; // previous vertex position, tnear of the next ray
+  float4 lastN; // previous vertex shading normal, ray cone width at the last hit (at the camera before)
   uint4 meta;   // LDSampler scramble, flags, first-hit primID, geomID
-  uint4 meta2;  // first-hit instID, (unused)
+  uint4 meta2;  // first-hit instID, request (batch) / ray cone dwdt bits (single frame), sampleID,
+                // pixel / radiance-cache training slot
 };
 static_assert(sizeof(PathRec) == 128, "PathRec must be 128 bytes");
 
@@ -119,7 +124,7 @@ constexpr uint32_t F_AOHIT = 1u << 11, F_DIFFUSE = 1u << 12;
 // the camera ray of sample s of pixel (x, y) of a path-traced frame, as a
 // fresh path record (meta2: first-hit instID, request, sampleID, pixel)
 B200_D PathRec genPT(const PtCtx &c, const CameraD &cam, const PixelFilterD &pf, const FrameInfo &fi, int x, int y,
-                     int s, uint32_t rid) {
+                     int s, uint32_t rid, float2 *screen = nullptr) {
   const uint32_t seed = 0x49c5f37eu ^ uint32_t(fi.W * y + x);
   const uint32_t sampleID = uint32_t(fi.frameID) * uint32_t(fi.spp) + uint32_t(s);
   LDSampler ld;
@@ -128,7 +133,9 @@ B200_D PathRec genPT(const PtCtx &c, const CameraD &cam, const PixelFilterD &pf,
   const float2 ps = ld.getNext5Samples(ss234);
   const float2 pfs = filterSample(pf, ps.x, ps.y);
   const float cx = fmul(fadd(float(x), 0.5f), fi.rcpW), cy = fmul(fadd(float(y), 0.5f), fi.rcpH);
-  const Ray ray = cameraRay(cam, fadd(cx, fmul(pfs.x, fi.rcpW)), fadd(cy, fmul(pfs.y, fi.rcpH)));
+  const float sx = fadd(cx, fmul(pfs.x, fi.rcpW)), sy = fadd(cy, fmul(pfs.y, fi.rcpH));
+  const Ray ray = cameraRay(cam, sx, sy);
+  if (screen) *screen = make_float2(sx, sy);
   PathRec r;
   r.org = make_float4(ray.org.x, ray.org.y, ray.org.z, INFINITY);
   r.dir = make_float4(ray.dir.x, ray.dir.y, ray.dir.z, INFINITY);
@@ -139,6 +146,19 @@ B200_D PathRec genPT(const PtCtx &c, const CameraD &cam, const PixelFilterD &pf,
   r.meta = make_uint4(ld.scramble, F_STRAIGHT | F_FIRST, INVALID_ID, INVALID_ID);
   r.meta2 = make_uint4(INVALID_ID, rid, sampleID, uint32_t(fi.W * y + x));
   return r;
+}
+
+// The camera ray's cone at screen position (sx, sy), in units of the frame
+// height (PathTracer.ispc:186-187): perspective 0 wide, widening by the
+// image plane height x rsqrt(|unnormalised direction|^2)
+// (PerspectiveCamera.ispc:58-63); orthographic as wide as the image height,
+// parallel (OrthographicCamera.ispc:52-53); panoramic pi sin(theta)
+// (PanoramicCamera.ispc:86-90).
+B200_D float2 cameraCone(const CameraD &c, float sx, float sy, float rcpH) {
+  if (c.type == 1) return make_float2(sqrtf(dot(c.dv_up, c.dv_up)) * rcpH, 0.f);
+  if (c.type == 2) return make_float2(0.f, PI_F * sinf(PI_F * sy) * rcpH);
+  const V3 d = add(add(c.dir_00, mul(sx, c.du_size)), mul(sy, c.dv_up));
+  return make_float2(0.f, sqrtf(dot(c.dv_up, c.dv_up)) * rsqrtf(dot(d, d)) * rcpH);
 }
 
 // appends one entry per lane that wants to, with one atomic per warp
@@ -172,7 +192,11 @@ __global__ void k_pt_generate(PtCtx c, CameraD cam, PixelFilterD pf, FrameInfo f
     if (live) active[slot] = uint32_t(p);
   }
   if (!live) return;
-  PathRec r = genPT(c, cam, pf, fi, pix % fi.W, pix / fi.W, s, 0u);
+  float2 scr;
+  PathRec r = genPT(c, cam, pf, fi, pix % fi.W, pix / fi.W, s, 0u, &scr);
+  const float2 cone = cameraCone(cam, scr.x, scr.y, fi.rcpH);
+  r.lastN.w = cone.x;
+  r.meta2.y = __float_as_uint(cone.y);
   if (nrcStride) {
     const uint32_t k = uint32_t(p) + nrcOffset;
     r.meta2.w = (k % nrcStride == 0 && k / nrcStride < nrcSlots) ? k / nrcStride : INVALID_ID;
@@ -187,6 +211,7 @@ struct ShadowMatD {
   const MaterialD *mats;
   int nmats, maxDepth;
   float minContribution;
+  float mipBiasFactor;
 };
 
 // Persistent any/closest-hit tracing over a queue with per-lane dynamic
@@ -219,6 +244,7 @@ __global__ void __launch_bounds__(TRACE_BLOCK, BATCH ? B200_BATCH_TRACE_MINBLOCK
   V3 tcon = splat(0.f);
   uint32_t tmed = MEDIUM_VACUUM;
   int tdepth = 0;
+  float tcone = 0.f;  // the path's ray cone width at the shadow ray's origin
   for (int guard = 0; guard < (1 << 30); guard++) {
     const unsigned need = __ballot_sync(0xffffffffu, !has && !exhausted);
     if (need) {
@@ -242,6 +268,7 @@ __global__ void __launch_bounds__(TRACE_BLOCK, BATCH ? B200_BATCH_TRACE_MINBLOCK
               tcon = mk(s.c.x, s.c.y, s.c.z);
               tmed = __float_as_uint(s.c.w);
               tdepth = sm.maxDepth;
+              tcone = ws.paths[__float_as_uint(s.b.w)].lastN.w;
             }
             if (BATCH) bsc = reqs[ws.paths[__float_as_uint(s.b.w)].meta2.y].c.sc;
           } else {
@@ -272,10 +299,15 @@ __global__ void __launch_bounds__(TRACE_BLOCK, BATCH ? B200_BATCH_TRACE_MINBLOCK
           atomicAdd(con + 2, tcon.z);
         } else {
           tv.finish(S);
-          const DG dg = postIntersect(S, tray, tv.hit);
+          DGAttr at;
+          const DG dg = postIntersect<true>(S, tray, tv.hit, &at);
           const uint32_t mi = S.entries[tv.hit.entry].materialID;
           const bool hasMat = mi < uint32_t(sm.nmats);
-          tcon = tcon * (hasMat ? materialTransparency(sm.mats, mi, tray.dir, dg.Ns, tmed) : splat(0.f));
+          // the shadow cone narrows from the path's width to 0 at the light
+          // (NextEventEstimation.ispc:103-106), re-widened at every surface
+          const float w = tcone + (-tcone * (1.f / tray.tfar)) * tv.hit.t;
+          const float fp = hasMat && sm.mats[mi].map ? pixelFootprint(w, tray.dir, dg, at, sm.mipBiasFactor) : 0.f;
+          tcon = tcon * (hasMat ? materialTransparency(sm.mats, mi, tray.dir, dg.Ns, tmed, at, fp) : splat(0.f));
           const MediumD md = mediumOf(sm.mats, tmed);
           if (md.att.x != 0.f || md.att.y != 0.f || md.att.z != 0.f)
             tcon = tcon * expV(md.att * (tv.hit.t - tray.tnear));
@@ -382,6 +414,7 @@ struct PathVars {
   int depth, scatter, lastNLS;
   bool straightPath, firstBounceLight, diffuseSeen, auxDone, cont;
   uint32_t medium;
+  float cone;  // ray cone width at this vertex
 };
 
 // transparentShadow (render/pathtracer/TransparentShadow.ispc:18-85) for one
@@ -391,7 +424,7 @@ struct PathVars {
 // the contribution drops to minContribution or maxPathLength surfaces were
 // crossed.  Opaque scenes use one any-hit query.
 template <bool TRANSP>
-B200_D V3 shadowInPlace(const PtCtx &C, Ray sr, V3 contrib, uint32_t medium) {
+B200_D V3 shadowInPlace(const PtCtx &C, Ray sr, V3 contrib, uint32_t medium, float cone) {
   HitRec h;
   if (!TRANSP) return traceRay<false>(C.sc, sr, h, true, true, nullptr) ? splat(0.f) : contrib;
   const float tfar = sr.tfar;
@@ -401,10 +434,13 @@ B200_D V3 shadowInPlace(const PtCtx &C, Ray sr, V3 contrib, uint32_t medium) {
     const Entry &e = C.sc.entries[h.entry];
     h.geomID = e.geomID;
     h.instID = e.instID;
-    const DG dg = postIntersect(C.sc, sr, h);
+    DGAttr at;
+    const DG dg = postIntersect<true>(C.sc, sr, h, &at);
     const uint32_t mi = e.materialID;
     const bool hasMat = mi < uint32_t(C.p.numMaterials);
-    contrib = contrib * (hasMat ? materialTransparency(C.mats, mi, sr.dir, dg.Ns, medium) : splat(0.f));
+    const float w = cone + (-cone * (1.f / tfar)) * h.t;
+    const float fp = hasMat && C.mats[mi].map ? pixelFootprint(w, sr.dir, dg, at, C.p.mipBiasFactor) : 0.f;
+    contrib = contrib * (hasMat ? materialTransparency(C.mats, mi, sr.dir, dg.Ns, medium, at, fp) : splat(0.f));
     const MediumD md = mediumOf(C.mats, medium);
     if (md.att.x != 0.f || md.att.y != 0.f || md.att.z != 0.f) contrib = contrib * expV(md.att * (h.t - sr.tnear));
     if (maxc(contrib) <= C.p.minContribution || --maxDepth <= 0) return splat(0.f);
@@ -431,6 +467,7 @@ B200_D void scatterSurface(const PtCtx &C, const B &bsdf, const MaterialD &mat, 
                            PathVars &v, uint32_t p, ShadowRec *sh, int &nsh, const NrcFrameD &nf) {
   const int nl = C.p.numLights;
   const bool transparentShadows = ALLMAT && C.p.transparentShadows != 0;
+  if (ALLMAT) gp->lastN.w = v.cone;  // this vertex's cone width (shadow rays, the next bounce)
   if (bsdf.smooth && v.scatter == 0 && !v.auxDone && C.aux) {
     // updateAuxilliaryData (render/pathtracer/PathTracerUtil.ih:48-60) at the
     // first smooth vertex: throughput x BSDF albedo and x shading normal
@@ -510,8 +547,8 @@ B200_D void scatterSurface(const PtCtx &C, const B &bsdf, const MaterialD &mat, 
         sr.tnear = 0.f;
         sr.dir = ls.dir;
         sr.tfar = ls.dist;
-        v.contribution = v.contribution + (transparentShadows ? shadowInPlace<ALLMAT>(C, sr, cval, v.medium)
-                                                              : shadowInPlace<false>(C, sr, cval, v.medium));
+        v.contribution = v.contribution + (transparentShadows ? shadowInPlace<ALLMAT>(C, sr, cval, v.medium, v.cone)
+                                                              : shadowInPlace<false>(C, sr, cval, v.medium, 0.f));
       }
     }
     v.firstBounceLight = false;
@@ -552,9 +589,11 @@ B200_D void scatterSurface(const PtCtx &C, const B &bsdf, const MaterialD &mat, 
     if (!(ray.dir.x == fs.wi.x && ray.dir.y == fs.wi.y && ray.dir.z == fs.wi.z)) v.straightPath = false;
     if (fs.type & ~ST_SPEC_T) {  // the new last vertex for MIS
       gp->lastP = make_float4(dg.P.x, dg.P.y, dg.P.z, 0.f);
-      gp->lastN = make_float4(dg.Ns.x, dg.Ns.y, dg.Ns.z, 0.f);
+      gp->lastN = make_float4(dg.Ns.x, dg.Ns.y, dg.Ns.z, ALLMAT ? v.cone : 0.f);
       dir4.w = fs.pdf;
       v.lastNLS = numLS;
+    } else if (ALLMAT && v.depth == 0) {
+      gp->lastP.w = 0.f;  // the continuation ray starts at this surface, not at the camera's near clip
     }
     org4 = make_float4(org.x, org.y, org.z, org4.w);
     dir4 = make_float4(fs.wi.x, fs.wi.y, fs.wi.z, dir4.w);
@@ -623,6 +662,7 @@ __global__ void __launch_bounds__(128, B200_SHADE_MINBLOCKS) k_pt_shade(PtCtx c,
       v.contribution = mk(con4.x, con4.y, con4.z);
       v.medium = __float_as_uint(con4.w);
       v.cont = false;
+      v.cone = 0.f;
       float alpha = thr4.w;
       Ray ray;
       ray.org = mk(org4.x, org4.y, org4.z);
@@ -634,8 +674,15 @@ __global__ void __launch_bounds__(128, B200_SHADE_MINBLOCKS) k_pt_shade(PtCtx c,
       const V3 wo = -ray.dir;
       if (v.depth == 0) org4.w = t;
       if (!hit && v.straightPath) {
-        alpha -= luminance(v.throughput) * (1.f - C.p.bg[3]);
-        v.contribution = v.contribution + v.throughput * mk(C.p.bg[0], C.p.bg[1], C.p.bg[2]);
+        // Renderer_getBackground (render/Renderer.ispc:19-29) at the pixel centre
+        float4 bg = make_float4(C.p.bg[0], C.p.bg[1], C.p.bg[2], C.p.bg[3]);
+        if (ALLMAT && !BATCH && C.p.backplate) {
+          const uint32_t pix = p / uint32_t(C.p.spp);
+          bg = texGetScreen(*C.p.backplate, (float(pix % uint32_t(C.W)) + 0.5f) * C.rcpW,
+                            (float(pix / uint32_t(C.W)) + 0.5f) * C.rcpH);
+        }
+        alpha -= luminance(v.throughput) * (1.f - bg.w);
+        v.contribution = v.contribution + v.throughput * mk(bg.x, bg.y, bg.z);
       }
       if (nl > 0) {  // evaluateVirtualLights
         const float4 lp = gp->lastP, ln = gp->lastN;
@@ -669,7 +716,9 @@ __global__ void __launch_bounds__(128, B200_SHADE_MINBLOCKS) k_pt_shade(PtCtx c,
         const Entry &e = C.sc.entries[h.entry];
         h.geomID = e.geomID;
         h.instID = e.instID;
-        const DG dg = postIntersect(C.sc, ray, h);
+        DGAttr at;
+        const DG dg = ALLMAT ? postIntersect<true>(C.sc, ray, h, &at) : postIntersect(C.sc, ray, h);
+        if (ALLMAT && !BATCH) v.cone = gp->lastN.w + __uint_as_float(gp->meta2.y) * t;
         if (v.depth == 0) {
           meta.z = h.primID;
           meta.w = h.geomID;
@@ -677,7 +726,15 @@ __global__ void __launch_bounds__(128, B200_SHADE_MINBLOCKS) k_pt_shade(PtCtx c,
         }
         const uint32_t mi = e.materialID;
         if (v.scatter < C.p.maxScatteringEvents && mi < uint32_t(C.p.numMaterials)) {
-          const MaterialD &mat = C.mats[mi];
+          // the colour map and vertex colour applied (principled, obj)
+          float opacity = 0.f;
+          MaterialD mloc;
+          if (ALLMAT) {
+            const MaterialD &mrec = C.mats[mi];
+            mloc = shadedMaterial(
+                mrec, at, mrec.map ? pixelFootprint(v.cone, ray.dir, dg, at, C.p.mipBiasFactor) : 0.f, opacity);
+          }
+          const MaterialD &mat = ALLMAT ? mloc : C.mats[mi];
           switch (ALLMAT ? mat.kind : MAT_PRINCIPLED) {
             case MAT_OBJ:
             case MAT_PRINCIPLED: {
@@ -698,7 +755,10 @@ __global__ void __launch_bounds__(128, B200_SHADE_MINBLOCKS) k_pt_shade(PtCtx c,
                                                      nsh, nf);
               } else {
                 PrincipledBsdfT<ALLMAT> b;
-                b.init(mat, fxv, fyv, dg.Ns, C.AT);
+                if (ALLMAT)
+                  b.init(mat, fxv, fyv, dg.Ns, C.AT, opacity);
+                else
+                  b.init(mat, fxv, fyv, dg.Ns, C.AT);
                 scatterSurface<PrincipledBsdfT<ALLMAT>, NRC, ALLMAT>(C, b, mat, mi, dg, ray, t, wo, gp, org4, dir4,
                                                                     meta, v, p, sh, nsh, nf);
               }
@@ -1098,7 +1158,7 @@ cudaError_t launchRenderPT(const SamplerTables *T, const Scene &sc, const Camera
   if (ptWorkspaceBytes(fi.npaths) > wsBytes) return cudaErrorInvalidValue;
   if (nrc && (stats || !nrcInfer)) return cudaErrorInvalidValue;
   Workspace ws = carveWorkspace(workspace, fi.npaths);
-  PtCtx c = {T, sc, p, mats, lights, lightCdf, AT, fb.frameID, fb.aux};
+  PtCtx c = {T, sc, p, mats, lights, lightCdf, AT, fb.frameID, fb.aux, fb.W, fi.rcpW, fi.rcpH};
   static int traceBlocks = 0, shadowBlocks = 0, transpBlocks = 0, shadeBlocks = 0, shadeAllBlocks = 0,
              shadeNrcBlocks = 0;
   if (!traceBlocks) {
@@ -1110,7 +1170,7 @@ cudaError_t launchRenderPT(const SamplerTables *T, const Scene &sc, const Camera
     shadeNrcBlocks = persistentBlocks((const void *)k_pt_shade<false, true, false>, TRACE_SMEM_BYTES);
   }
   const NrcFrameD nf = nrc ? *nrc : NrcFrameD{};
-  const ShadowMatD sm = {mats, p.numMaterials, p.maxPathLength, p.minContribution};
+  const ShadowMatD sm = {mats, p.numMaterials, p.maxPathLength, p.minContribution, p.mipBiasFactor};
   const bool transp = p.transparentShadows != 0;
   if (nrc) {
     cudaMemsetAsync(nf.counters, 0, 16, st);

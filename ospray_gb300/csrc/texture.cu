@@ -1,6 +1,7 @@
 // 2D texture objects: upload, the MIP chain generated on the device, and the
 // b200_texture_* C ABI (Texture2D::commit, texture/Texture2D.cpp:42-146;
 // MipMap_generate, texture/MipMapGeneration.ispc).
+#include <algorithm>
 #include <cstring>
 #include <string>
 
@@ -74,16 +75,21 @@ __device__ void setTexel(int fmt, unsigned char *d, uint32_t i, float4 v) {
   }
 }
 
-__device__ float4 add4(float4 a, float4 b) { return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
-__device__ float4 scale4(float s, float4 a) { return make_float4(s * a.x, s * a.y, s * a.z, s * a.w); }
+// (every product and sum rounded on its own: no fused multiply-adds)
+__device__ float4 add4(float4 a, float4 b) {
+  return make_float4(__fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y), __fadd_rn(a.z, b.z), __fadd_rn(a.w, b.w));
+}
+__device__ float4 scale4(float s, float4 a) {
+  return make_float4(__fmul_rn(s, a.x), __fmul_rn(s, a.y), __fmul_rn(s, a.z), __fmul_rn(s, a.w));
+}
 
 // MipMap_generateRows: a dst texel averages a 2x2 (3-tap along an odd axis)
 // source block with the weights of a box filter of the source's footprint
 __global__ void k_mip_rows(const unsigned char *src, int sw, int sh, unsigned char *dst, int dw, int dh, int fmt) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
   if (x >= dw || y >= dh) return;
-  float rx = 1.f / float(sw), ry = 1.f / float(sh);
-  float hx = float(dw) * rx, hy = float(dh) * ry;
+  float rx = __fdiv_rn(1.f, float(sw)), ry = __fdiv_rn(1.f, float(sh));
+  float hx = __fmul_rn(float(dw), rx), hy = __fmul_rn(float(dh), ry);
   const int srcy = 2 * y * sw;
   int ofsx = 2, ofsy = srcy + 2 * sw;
   if ((sw & 1) == 0) {
@@ -96,13 +102,13 @@ __global__ void k_mip_rows(const unsigned char *src, int sw, int sh, unsigned ch
     ry = 0.f;
     ofsy = srcy;
   }
-  const float wy0 = hy - float(y) * ry, wy2 = ry + float(y) * ry;
-  const float tx = float(x) * rx;
+  const float wy0 = __fsub_rn(hy, __fmul_rn(float(y), ry)), wy2 = __fadd_rn(ry, __fmul_rn(float(y), ry));
+  const float tx = __fmul_rn(float(x), rx);
   const int sx = 2 * x;
   auto row = [&](int base) {
-    return add4(add4(scale4(hx - tx, getTexel(fmt, src, uint32_t(base + sx))),
+    return add4(add4(scale4(__fsub_rn(hx, tx), getTexel(fmt, src, uint32_t(base + sx))),
                      scale4(hx, getTexel(fmt, src, uint32_t(base + sx + 1)))),
-                scale4(rx + tx, getTexel(fmt, src, uint32_t(base + sx + ofsx))));
+                scale4(__fadd_rn(rx, tx), getTexel(fmt, src, uint32_t(base + sx + ofsx))));
   };
   const float4 v0 = row(srcy), v1 = row(srcy + sw), v2 = row(ofsy);
   setTexel(fmt, dst, uint32_t(y * dw + x), add4(add4(scale4(wy0, v0), scale4(hy, v1)), scale4(wy2, v2)));
@@ -112,21 +118,30 @@ __global__ void k_mip_rows(const unsigned char *src, int sw, int sh, unsigned ch
 __global__ void k_mip_row(const unsigned char *src, int ssize, unsigned char *dst, int dsize, int fmt) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   if (x >= dsize) return;
-  float r = 1.f / float(ssize), h = float(dsize) * r;
+  float r = __fdiv_rn(1.f, float(ssize)), h = __fmul_rn(float(dsize), r);
   int ofs2 = 2;
   if ((ssize & 1) == 0) {
     h = 0.5f;
     r = 0.f;
     ofs2 = 0;
   }
-  const float tx = float(x) * r;
+  const float tx = __fmul_rn(float(x), r);
   const int sx = 2 * x;
-  const float4 v = add4(add4(scale4(h - tx, getTexel(fmt, src, uint32_t(sx))), scale4(h, getTexel(fmt, src, uint32_t(sx + 1)))),
-                        scale4(r + tx, getTexel(fmt, src, uint32_t(sx + ofs2))));
+  const float4 v = add4(add4(scale4(__fsub_rn(h, tx), getTexel(fmt, src, uint32_t(sx))),
+                             scale4(h, getTexel(fmt, src, uint32_t(sx + 1)))),
+                        scale4(__fadd_rn(r, tx), getTexel(fmt, src, uint32_t(sx + ofs2))));
   setTexel(fmt, dst, uint32_t(x), v);
 }
 
 bool formatSupported(int f) { return f >= TEX_RGBA8 && f <= TEX_RA32F; }
+
+// Texture2D_get at n texture coordinates with per-lookup footprints
+__global__ void k_tex_sample(const TextureD *t, int n, const float2 *st, const float *fp, float4 *out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float2 c = st[i];
+  out[i] = texGet(*t, c.x, c.y, fp[i]);
+}
 
 }  // namespace
 
@@ -236,5 +251,45 @@ int b200_texture_release(b200_texture t) {
 }
 
 int b200_texture_levels(b200_texture t) { return t ? reinterpret_cast<TextureObj *>(t)->desc.maxLevel + 1 : 0; }
+
+int b200_texture_sample(b200_texture t, int64_t n, const float *st, const float *footprint, float *out) {
+  if (!t || n < 0 || (n > 0 && (!st || !footprint || !out))) return B200_INVALID_ARGUMENT;
+  if (n == 0) return B200_NO_ERROR;
+  if (n > (int64_t(1) << 31) - 1) return B200_INVALID_ARGUMENT;
+  TextureObj *o = reinterpret_cast<TextureObj *>(t);
+  cudaStream_t s = o->dev->stream;
+  void *buf = nullptr;
+  const size_t outOff = (size_t(n) * 12 + 15) & ~size_t(15);  // st (8 B each), footprints (4 B), then 16-aligned results
+  const size_t bytes = outOff + size_t(n) * 16;
+  if (cudaSetDevice(o->dev->dev) != cudaSuccess || cudaMallocAsync(&buf, bytes, s) != cudaSuccess)
+    return B200_OUT_OF_MEMORY;
+  float2 *dst = static_cast<float2 *>(buf);
+  float *dfp = reinterpret_cast<float *>(dst + n);
+  float4 *dout = reinterpret_cast<float4 *>(static_cast<char *>(buf) + outOff);
+  bool ok = cudaMemcpyAsync(dst, st, size_t(n) * 8, cudaMemcpyHostToDevice, s) == cudaSuccess &&
+            cudaMemcpyAsync(dfp, footprint, size_t(n) * 4, cudaMemcpyHostToDevice, s) == cudaSuccess;
+  if (ok) {
+    k_tex_sample<<<unsigned((n + 255) / 256), 256, 0, s>>>(o->dDesc, int(n), dst, dfp, dout);
+    ok = cudaGetLastError() == cudaSuccess &&
+         cudaMemcpyAsync(out, dout, size_t(n) * 16, cudaMemcpyDeviceToHost, s) == cudaSuccess;
+  }
+  cudaFreeAsync(buf, s);
+  ok = cudaStreamSynchronize(s) == cudaSuccess && ok;
+  return ok ? B200_NO_ERROR : B200_UNKNOWN_ERROR;
+}
+
+int b200_texture_read_level(b200_texture t, int level, void *dst, size_t bytes) {
+  if (!t || !dst) return B200_INVALID_ARGUMENT;
+  TextureObj *o = reinterpret_cast<TextureObj *>(t);
+  if (level < 0 || level > o->desc.maxLevel) return B200_INVALID_ARGUMENT;
+  const size_t need = size_t(std::max(o->desc.w >> level, 1)) * size_t(std::max(o->desc.h >> level, 1)) *
+                      size_t(texelBytes(o->desc.format));
+  if (bytes < need) return B200_INVALID_ARGUMENT;
+  if (cudaSetDevice(o->dev->dev) != cudaSuccess ||
+      cudaMemcpyAsync(dst, o->desc.level[level], need, cudaMemcpyDeviceToHost, o->dev->stream) != cudaSuccess ||
+      cudaStreamSynchronize(o->dev->stream) != cudaSuccess)
+    return B200_UNKNOWN_ERROR;
+  return B200_NO_ERROR;
+}
 
 }  // extern "C"

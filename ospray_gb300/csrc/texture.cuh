@@ -42,7 +42,7 @@ struct TextureD {
   int w, h, maxLevel, format, filter, wrapS, wrapT, hasAlpha;
 };
 
-B200_HD inline int texelBytes(int fmt) {
+B200_HD int texelBytes(int fmt) {
   switch (fmt) {
     case TEX_RGBA8:
     case TEX_SRGBA: return 4;

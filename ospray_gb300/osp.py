@@ -17,6 +17,8 @@ OSP_GEOMETRIC_MODEL, OSP_INSTANCE, OSP_LIGHT, OSP_MATERIAL = (0x8000000 + 104, 0
                                                              0x8000000 + 109, 0x8000000 + 110)
 OSP_INT, OSP_UINT, OSP_FLOAT, OSP_VEC3F, OSP_VEC4F, OSP_VEC3UI = 4000, 4500, 6000, 6002, 6003, 4502
 OSP_AFFINE3F, OSP_BOOL = 12003, 250
+OSP_TEXTURE = 0x8000000 + 112
+OSP_UCHAR, OSP_VEC3UC, OSP_VEC4UC, OSP_VEC2F, OSP_VEC2UI = 2500, 2502, 2503, 6001, 4501
 OSP_FB_NONE, OSP_FB_RGBA8, OSP_FB_SRGBA, OSP_FB_RGBA32F = 0, 1, 2, 3
 OSP_FB_COLOR, OSP_FB_DEPTH, OSP_FB_ACCUM = 1, 2, 4
 OSP_FB_ID_PRIMITIVE, OSP_FB_ID_OBJECT, OSP_FB_ID_INSTANCE = 64, 128, 256
@@ -58,6 +60,7 @@ def lib():
             "ospNewCamera": (P, [ctypes.c_char_p]),
             "ospNewRenderer": (P, [ctypes.c_char_p]),
             "ospNewImageOperation": (P, [ctypes.c_char_p]),
+            "ospNewTexture": (P, [ctypes.c_char_p]),
             "ospNewGeometricModel": (P, [P]),
             "ospNewGroup": (P, []),
             "ospNewInstance": (P, [P]),
@@ -108,6 +111,28 @@ def set_data(obj, name, arr, typ, count, keep):
     lib().ospCommit(d)
     set_param(obj, name, OSP_DATA, d)
     lib().ospRelease(d)
+
+
+def new_texture(img, fmt, data_type, filter=0, wrap=0, keep=None):
+    """A committed "texture2d" over an (h, w[, c]) array with OSPTextureFormat
+    `fmt` and OSPDataType `data_type` (its texel type); wrap: one mode or two."""
+    L = lib()
+    keep = [] if keep is None else keep
+    a = np.ascontiguousarray(img)
+    keep.append(a)
+    d = L.ospNewSharedData(a.ctypes.data, data_type, a.shape[1], 0, a.shape[0], 0, 1, 0, None, None)
+    L.ospCommit(d)
+    t = L.ospNewTexture(b"texture2d")
+    set_param(t, "data", OSP_DATA, d)
+    L.ospRelease(d)
+    set_param(t, "format", OSP_UINT, np.uint32(fmt))
+    set_param(t, "filter", OSP_UINT, np.uint32(filter))
+    if isinstance(wrap, (tuple, list)):
+        set_param(t, "wrapMode", OSP_VEC2UI, np.asarray(wrap, np.uint32))
+    else:
+        set_param(t, "wrapMode", OSP_UINT, np.uint32(wrap))
+    L.ospCommit(t)
+    return t
 
 
 def map_channel(fb, ch, shape, dtype):

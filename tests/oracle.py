@@ -63,13 +63,16 @@ def pick(scene, cam, x, y):
 class OrPtParams(ctypes.Structure):
     _fields_ = [("spp", I), ("maxPathLength", I), ("roulettePathLength", I), ("maxScatteringEvents", I),
                 ("lightSamples", I), ("limitIndirectLightSamples", I), ("minContribution", F),
-                ("maxContribution", F), ("bg", F * 4), ("pixelFilter", I)]
+                ("maxContribution", F), ("bg", F * 4), ("pixelFilter", I), ("backplate", P), ("mipMapBias", F)]
 
 
 def pt_params(spp=1, max_path_length=20, roulette_path_length=5, max_scattering_events=20, light_samples=-1,
               limit_indirect=True, min_contribution=0.001, max_contribution=float("inf"), bg=(0, 0, 0, 0),
-              pixel_filter=2):
+              pixel_filter=2, backplate=None, mip_map_bias=0.0):
+    """backplate: an OrTexture or None."""
     p = OrPtParams()
+    p.backplate = None if backplate is None else backplate.h
+    p.mipMapBias = float(mip_map_bias)
     p.spp, p.maxPathLength, p.roulettePathLength = spp, max_path_length, roulette_path_length
     p.maxScatteringEvents, p.lightSamples, p.limitIndirectLightSamples = max_scattering_events, light_samples, \
         int(limit_indirect)
@@ -108,15 +111,71 @@ def material_floats(m):
     return t, np.asarray(out, np.float32)
 
 
+class OrTexture:
+    """A CPU texture: data (height, width[, channels]) of an OSPTextureFormat,
+    rows from the bottom (the layout b200_texture_create takes)."""
+
+    def __init__(self, data, format, filter=0, wrap=(0, 0), mipmaps=True):
+        a = np.ascontiguousarray(data)
+        if isinstance(wrap, int):
+            wrap = (wrap, wrap)
+        self.data = a
+        self.h = lib().or_texture_new(a.shape[1], a.shape[0], format, filter, wrap[0], wrap[1], int(bool(mipmaps)),
+                                      _p(a))
+
+    @property
+    def levels(self):
+        return lib().or_texture_levels(self.h)
+
+    def read_level(self, level):
+        h, w = max(self.data.shape[0] >> level, 1), max(self.data.shape[1] >> level, 1)
+        out = np.empty((h, w) + self.data.shape[2:], dtype=self.data.dtype)
+        lib().or_texture_read_level(self.h, level, _p(out), out.nbytes)
+        return out
+
+    def sample(self, st, footprint):
+        st = np.ascontiguousarray(st, np.float32).reshape(-1, 2)
+        fp = np.ascontiguousarray(np.broadcast_to(np.asarray(footprint, np.float32), (len(st),)))
+        out = np.zeros((len(st), 4), np.float32)
+        lib().or_texture_sample(self.h, len(st), _p(st), _p(fp), _p(out))
+        return out
+
+    def __del__(self):
+        try:
+            lib().or_texture_free(self.h)
+        except Exception:
+            pass
+
+
+def set_mesh_attributes(scene, geom, normal=None, color=None, texcoord=None):
+    """The oracle scene's per-vertex attributes of triangle mesh `geom`
+    (colours (n, 4) or (n, 3): alpha 1)."""
+    n = None if normal is None else np.ascontiguousarray(normal, np.float32).reshape(-1, 3)
+    c = None
+    if color is not None:
+        c = np.asarray(color, np.float32)
+        if c.shape[-1] == 3:
+            c = np.concatenate([c.reshape(-1, 3), np.ones((c.size // 3, 1), np.float32)], axis=1)
+        c = np.ascontiguousarray(c, np.float32).reshape(-1, 4)
+    t = None if texcoord is None else np.ascontiguousarray(texcoord, np.float32).reshape(-1, 2)
+    lib().or_scene_set_mesh_attributes(scene.h, geom, _p(n), _p(c), _p(t))
+
+
 class PtWorld:
-    """Materials and lights of the oracle path tracer."""
+    """Materials and lights of the oracle path tracer.  A material dict's
+    "baseColorMap" is an OrTexture (principled map_baseColor / obj map_kd)."""
 
     def __init__(self, materials, lights):
         self.h = lib().or_pt_new()
+        self._keep = []
         for m in materials:
             if isinstance(m, dict):
-                t, f = material_floats(m)
-                lib().or_pt_add_material2(self.h, t, _p(f))
+                tex = m.get("baseColorMap")
+                t, f = material_floats({k: v for k, v in m.items() if k != "baseColorMap"})
+                idx = lib().or_pt_add_material2(self.h, t, _p(f))
+                if tex is not None:
+                    lib().or_pt_set_material_map(self.h, idx, tex.h)
+                    self._keep.append(tex)
                 continue
             bc = np.asarray(m[:3], np.float32)
             lib().or_pt_add_material(self.h, _p(bc), float(m[3]), float(m[4]))
@@ -181,6 +240,15 @@ def lib():
         L.or_pt_free.argtypes = [P]
         L.or_pt_add_material.argtypes = [P, P, F, F]
         L.or_pt_add_material2.argtypes = [P, I, P]
+        L.or_pt_set_material_map.argtypes = [P, I, P]
+        L.or_scene_set_mesh_attributes.argtypes = [P, I, P, P, P]
+        L.or_texture_new.restype = P
+        L.or_texture_new.argtypes = [I, I, I, I, I, I, I, P]
+        L.or_texture_free.argtypes = [P]
+        L.or_texture_levels.argtypes = [P]
+        L.or_texture_read_level.restype = ctypes.c_size_t
+        L.or_texture_read_level.argtypes = [P, I, P, ctypes.c_size_t]
+        L.or_texture_sample.argtypes = [P, I, P, P, P]
         L.or_pt_add_quad_light.argtypes = [P, P, P, P, P]
         L.or_pt_add_ambient_light.argtypes = [P, P]
         L.or_pt_add_distant_light.argtypes = [P, P, F, P]
