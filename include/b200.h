@@ -104,6 +104,15 @@ int b200_scene_add_quad_mesh(b200_scene scene, const float *vertex, int64_t nver
 int b200_scene_add_boxes(b200_scene scene, const float *boxes, int64_t n, int *geom_out);
 /* spheres: n x 4 float (center xyz, radius), OSP_SPHERE */
 int b200_scene_add_spheres(b200_scene scene, const float *spheres, int64_t n, int *geom_out);
+/* discs (Spheres::commit "type", geometry/Spheres.cpp:21-22,43-54): n x 4
+ * float (center xyz, radius); normals null: OSP_DISC, discs facing the ray;
+ * normals n x 3 float: OSP_ORIENTED_DISC ("sphere.normal") */
+int b200_scene_add_discs(b200_scene scene, const float *discs, int64_t n, const float *normals, int *geom_out);
+/* planes (Planes::commit geometry/Planes.cpp, Planes.ispc): n x 4 float
+ * "plane.coefficients" (a, b, c, d: the plane a x + b y + c z = d, as the
+ * reference's intersectPlane), bounds null (unbounded, +-1e18) or n x 6 float
+ * "plane.bounds" (lower xyz, upper xyz) */
+int b200_scene_add_planes(b200_scene scene, const float *coeffs, int64_t n, const float *bounds, int *geom_out);
 /* Per-vertex attributes of a triangle mesh (Mesh::commit "vertex.normal",
  * "vertex.color", "vertex.texcoord", geometry/Mesh.cpp:37-204;
  * TriangleMesh_postIntersect geometry/Mesh.ispc:178-276), each nverts x

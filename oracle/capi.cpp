@@ -143,6 +143,36 @@ int or_scene_add_spheres(void *sp, const float *xyzr, int n) {
   return int(s.geoms.size() - 1);
 }
 
+// discs: xyzr per disc; normals null (ray-facing discs) or 3 per disc (oriented discs)
+int or_scene_add_discs(void *sp, const float *xyzr, int n, const float *normals) {
+  Scene &s = *static_cast<Scene *>(sp);
+  Geometry g;
+  g.type = 1;
+  g.sphereKind = normals ? 2 : 1;
+  g.spheres.resize(n);
+  std::memcpy(g.spheres.data(), xyzr, sizeof(float) * 4 * n);
+  for (int i = 0; normals && i < n; i++) g.discNormals.push_back({normals[3 * i], normals[3 * i + 1], normals[3 * i + 2]});
+  s.geoms.push_back(std::move(g));
+  return int(s.geoms.size() - 1);
+}
+
+// planes: (a, b, c, d) per plane (a x + b y + c z = d); bounds null or 6 per plane (lower, upper)
+int or_scene_add_planes(void *sp, const float *coeffs, int n, const float *bounds) {
+  Scene &s = *static_cast<Scene *>(sp);
+  Geometry g;
+  g.type = 3;
+  g.planeBounded = bounds != nullptr;
+  for (int i = 0; i < n; i++) {
+    g.planes.push_back({coeffs[4 * i], coeffs[4 * i + 1], coeffs[4 * i + 2], coeffs[4 * i + 3]});
+    if (bounds) {
+      const float *b = bounds + 6 * i;
+      g.planeBounds.push_back({{b[0], b[1], b[2]}, {b[3], b[4], b[5]}});
+    }
+  }
+  s.geoms.push_back(std::move(g));
+  return int(s.geoms.size() - 1);
+}
+
 // xfm: row-major 3x4 affine or null for identity
 void or_scene_add_instance(void *sp, int geom, uint32_t instID, uint32_t geomID, const float *xfm, int material) {
   Scene &s = *static_cast<Scene *>(sp);

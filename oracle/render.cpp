@@ -193,8 +193,10 @@ DG postIntersect(const Scene &s, const Ray &ray, const Hit &hit, bool attrs) {
         }
       }
     }
+  } else if (g.type == 3) {
+    eps = 0.f;  // Planes_postIntersect (geometry/Planes.ispc:115-121) sets no geometry epsilon
   } else {
-    eps = g.spheres[hit.primID].w * ulpEpsilon;
+    eps = g.spheres[hit.primID].w * ulpEpsilon;  // Spheres_postIntersect, also for discs
   }
   dg.dPds = xfmVector(e->xfm.l, dPds);  // Instance_postIntersect (common/Instance.ih:95-98)
   dg.dPdt = xfmVector(e->xfm.l, dg.dPdt);

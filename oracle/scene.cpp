@@ -110,6 +110,55 @@ inline bool sphTest(V3 org, V3 d, float tnear, float tfar, V4 s, float &t, V3 &N
   return true;
 }
 
+// Embree 4.3.3's point primitives (the reference's OSP_DISC and
+// OSP_ORIENTED_DISC, geometry/Spheres.cpp:21-22): a ray-facing disc is hit at
+// the centre's projection onto the ray when the ray passes within the radius
+// (Ng = -d); an oriented disc where the ray meets its plane inside the radius
+// (Ng = its normal).
+inline bool discTest(V3 org, V3 d, float tnear, float tfar, V4 s, float &t, V3 &Ng) {
+  const float rd2 = 1.f / dot(d, d);
+  const V3 c0 = v3(s.x, s.y, s.z) - org;
+  const float projC0 = dot(c0, d) * rd2;
+  if (!(projC0 >= tnear && projC0 <= tfar)) return false;
+  const V3 perp = c0 - projC0 * d;
+  if (!(dot(perp, perp) <= s.w * s.w)) return false;
+  t = projC0;
+  Ng = -d;
+  return true;
+}
+inline bool orientedDiscTest(V3 org, V3 d, float tnear, float tfar, V4 s, V3 n, float &t, V3 &Ng) {
+  const float div = dot(d, n);
+  if (div == 0.f) return false;
+  const V3 c = v3(s.x, s.y, s.z);
+  const float tt = dot(c - org, n) / div;
+  if (!(tt >= tnear && tt <= tfar)) return false;
+  const V3 q = (org + d * tt) - c;
+  if (!(dot(q, q) < s.w * s.w)) return false;
+  t = tt;
+  Ng = n;
+  return true;
+}
+// Planes_intersect_kernel (geometry/Planes.ispc:40-78) with intersectPlane /
+// intersectBox (common/Intersect.ih:195-237) and filterIntersectionSingle's
+// tnear < t <= tfar (common/FilterIntersect.ih)
+inline bool planeTest(V3 org, V3 d, float tnear, float tfar, V4 c, const Box *bounds, float &t, V3 &Ng) {
+  const V3 n = v3(c.x, c.y, c.z);
+  const float DdN = dot(d, n);
+  if (DdN == 0.f) return false;
+  const float tt = (c.w - dot(org, n)) / DdN;
+  if (!(tt > tnear && tt <= tfar)) return false;
+  if (bounds) {
+    auto rs = [](float x) { return 1.f / (std::fabs(x) < 1e-18f ? std::copysign(1e-18f, x) : x); };
+    const V3 r = v3(rs(d.x), rs(d.y), rs(d.z));
+    const V3 m0 = (bounds->lo - org) * r, m1 = (bounds->hi - org) * r;
+    const float en = reduce_max(vmin(m0, m1)), ex = reduce_min(vmax(m0, m1));
+    if (!(en < ex) || tt < en || tt > ex) return false;
+  }
+  t = tt;
+  Ng = n;
+  return true;
+}
+
 inline bool better(float t, uint32_t inst, uint32_t geom, uint32_t prim, const Hit &h) {
   if (t != h.t) return t < h.t;
   if (inst != h.instID) return inst < h.instID;
@@ -124,6 +173,11 @@ Box Geometry::primBox(uint32_t p) const {
   if (type == 0) {
     const V3 a = verts[index[3 * p]], b = verts[index[3 * p + 1]], c = verts[index[3 * p + 2]];
     return {vmin(a, vmin(b, c)), vmax(a, vmax(b, c))};
+  }
+  if (type == 3) {  // Planes_bounds (geometry/Planes.ispc:17-33)
+    const float M = 1e18f;
+    if (!planeBounded) return {v3(-M), v3(M)};
+    return {vmax(planeBounds[p].lo, v3(-M)), vmin(planeBounds[p].hi, v3(M))};
   }
   const V4 s = spheres[p];
   return {v3(s.x - s.w, s.y - s.w, s.z - s.w), v3(s.x + s.w, s.y + s.w, s.z + s.w)};
@@ -280,6 +334,12 @@ bool traverseBLAS(const Geometry &g, V3 org, V3 dir, float tnear, Hit &hit, uint
                  v2 = g.verts[g.index[3 * p + 2]];
         h = triTest(pre, org, tnear, hit.t, v0, v1, v2, t, u, v);
         if (h) Ng = cross(v1 - v0, v2 - v0);
+      } else if (g.type == 3) {
+        h = planeTest(org, dir, tnear, hit.t, g.planes[p], g.planeBounded ? &g.planeBounds[p] : nullptr, t, Ng);
+      } else if (g.sphereKind == 1) {
+        h = discTest(org, dir, tnear, hit.t, g.spheres[p], t, Ng);
+      } else if (g.sphereKind == 2) {
+        h = orientedDiscTest(org, dir, tnear, hit.t, g.spheres[p], g.discNormals[p], t, Ng);
       } else {
         h = sphTest(org, dir, tnear, hit.t, g.spheres[p], t, Ng);
       }

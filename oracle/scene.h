@@ -38,7 +38,7 @@ struct Box {
 };
 
 struct Geometry {
-  int type;  // 0 triangles, 1 spheres, 2 boxes (instance level)
+  int type;  // 0 triangles, 1 spheres / discs, 2 boxes (instance level), 3 planes
   std::vector<Box> boxes;
   std::vector<V3> verts;
   std::vector<uint32_t> index;  // 3 per triangle
@@ -46,6 +46,11 @@ struct Geometry {
   uint32_t primDiv = 1;  // triangles per application primitive (quads 2, boxes 12): primID = p / primDiv
   bool boxFaces = false;  // box geometry as face triangles (no geometry epsilon)
   std::vector<V4> spheres;      // center, radius
+  int sphereKind = 0;           // OSP_SPHERE 0, OSP_DISC 1, OSP_ORIENTED_DISC 2
+  std::vector<V3> discNormals;  // oriented discs
+  std::vector<V4> planes;       // a, b, c, d: the plane a x + b y + c z = d
+  std::vector<Box> planeBounds; // per plane, when planeBounded
+  bool planeBounded = false;
   // per-vertex attributes of a triangle mesh (empty: absent)
   std::vector<V3> normals;
   std::vector<V4> colors;
@@ -59,7 +64,8 @@ struct Geometry {
   std::vector<Node> nodes;
   std::vector<uint32_t> prims;
   uint32_t nprims() const {
-    return type == 0 ? uint32_t(index.size() / 3) : (type == 1 ? uint32_t(spheres.size()) : uint32_t(boxes.size()));
+    return type == 0 ? uint32_t(index.size() / 3)
+                     : (type == 1 ? uint32_t(spheres.size()) : (type == 3 ? uint32_t(planes.size()) : uint32_t(boxes.size())));
   }
   Box primBox(uint32_t p) const;
   void build();

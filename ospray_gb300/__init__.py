@@ -298,6 +298,8 @@ def lib():
             "b200_scene_add_quad_mesh": (I, [P, P, I64, P, I64, ctypes.POINTER(I)]),
             "b200_scene_add_boxes": (I, [P, P, I64, ctypes.POINTER(I)]),
             "b200_scene_add_spheres": (I, [P, P, I64, ctypes.POINTER(I)]),
+            "b200_scene_add_discs": (I, [P, P, I64, P, ctypes.POINTER(I)]),
+            "b200_scene_add_planes": (I, [P, P, I64, P, ctypes.POINTER(I)]),
             "b200_scene_add_instance": (I, [P, I, U32, U32, P, I]),
             "b200_scene_commit": (I, [P]),
             "b200_scene_set_dynamic": (I, [P, I]),
@@ -541,6 +543,22 @@ class Scene:
         s = np.ascontiguousarray(xyzr, dtype=np.float32).reshape(-1, 4)
         g = ctypes.c_int()
         self.device._check(lib().b200_scene_add_spheres(self._h, _ptr(s), len(s), ctypes.byref(g)))
+        return g.value
+
+    def add_discs(self, xyzr, normals=None):
+        """Discs (n, 4): facing the ray (OSP_DISC), or oriented by normals (n, 3) (OSP_ORIENTED_DISC)."""
+        s = np.ascontiguousarray(xyzr, dtype=np.float32).reshape(-1, 4)
+        n = None if normals is None else np.ascontiguousarray(normals, dtype=np.float32).reshape(-1, 3)
+        g = ctypes.c_int()
+        self.device._check(lib().b200_scene_add_discs(self._h, _ptr(s), len(s), _ptr(n), ctypes.byref(g)))
+        return g.value
+
+    def add_planes(self, coeffs, bounds=None):
+        """Planes (n, 4) a x + b y + c z = d, optionally bounded by boxes (n, 6) lower, upper."""
+        c = np.ascontiguousarray(coeffs, dtype=np.float32).reshape(-1, 4)
+        b = None if bounds is None else np.ascontiguousarray(bounds, dtype=np.float32).reshape(-1, 6)
+        g = ctypes.c_int()
+        self.device._check(lib().b200_scene_add_planes(self._h, _ptr(c), len(c), _ptr(b), ctypes.byref(g)))
         return g.value
 
     def add_instance(self, geom, inst_id, geom_id, xfm=None, material=-1):

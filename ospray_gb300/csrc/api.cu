@@ -433,6 +433,7 @@ SceneObj::~SceneObj() {
     if (g.dindex) cudaFreeAsync(g.dindex, st);
     if (g.dquad) cudaFreeAsync(g.dquad, st);
     if (g.dsph) cudaFreeAsync(g.dsph, st);
+    if (g.duser) cudaFreeAsync(g.duser, st);
     for (float *p : {g.dnormals, g.dcolors, g.dtexcoords})
       if (p) cudaFreeAsync(p, st);
   }
@@ -460,8 +461,11 @@ void SceneObj::commit() {
       check(buildTriangleBLAS(g.dverts, g.dindex, int(g.nprims), st, g.blas, !dynamic,
                               g.meshKind == MESH_QUADS ? 2 : (g.meshKind == MESH_BOXES ? 12 : 1)),
             "BLAS build");
-    else
+    else if (g.type == GEOM_SPHERES)
       check(buildSphereBLAS(g.dsph, int(g.nprims), st, g.blas, !dynamic), "BLAS build");
+    else
+      check(buildUserBLAS(uint32_t(g.type), g.duser ? g.duser : g.dsph, int(g.nprims), st, g.blas, !dynamic),
+            "BLAS build");
     g.built = true;
   }
   // entries and their world boxes
@@ -893,6 +897,62 @@ int b200_scene_add_spheres(b200_scene s, const float *spheres, int64_t n, int *g
     check(cudaMallocAsync(&g.dsph, sizeof(float4) * size_t(n > 0 ? n : 1), st), "alloc spheres");
     if (n) check(cudaMemcpyAsync(g.dsph, spheres, 16 * size_t(n), cudaMemcpyHostToDevice, st), "upload");
     check(cudaStreamSynchronize(st), "upload spheres");
+    sc->geoms.push_back(g);
+    if (geom_out) *geom_out = int(sc->geoms.size() - 1);
+  });
+}
+
+int b200_scene_add_discs(b200_scene s, const float *discs, int64_t n, const float *normals, int *geom_out) {
+  if (!s) return B200_INVALID_ARGUMENT;
+  SceneObj *sc = reinterpret_cast<SceneObj *>(s);
+  return guarded(sc->dev, [&]() {
+    require(n >= 0 && (n == 0 || discs) && n < (int64_t(1) << 31), "bad disc array");
+    GeomObj g;
+    g.type = normals ? GEOM_ORIENTED_DISCS : GEOM_DISCS;
+    g.nprims = n;
+    cudaStream_t st = sc->dev->stream;
+    const size_t m = size_t(n > 0 ? n : 1);
+    check(cudaMallocAsync(&g.dsph, sizeof(float4) * m, st), "alloc discs");
+    if (n) check(cudaMemcpyAsync(g.dsph, discs, 16 * size_t(n), cudaMemcpyHostToDevice, st), "upload");
+    if (normals) {  // interleaved (centre, radius), (normal, 0)
+      std::vector<float4> h(2 * size_t(n));
+      for (int64_t i = 0; i < n; i++) {
+        h[2 * i] = make_float4(discs[4 * i], discs[4 * i + 1], discs[4 * i + 2], discs[4 * i + 3]);
+        h[2 * i + 1] = make_float4(normals[3 * i], normals[3 * i + 1], normals[3 * i + 2], 0.f);
+      }
+      check(cudaMallocAsync(&g.duser, sizeof(float4) * 2 * m, st), "alloc discs");
+      if (n) check(cudaMemcpyAsync(g.duser, h.data(), 32 * size_t(n), cudaMemcpyHostToDevice, st), "upload");
+    }
+    check(cudaStreamSynchronize(st), "upload discs");
+    sc->geoms.push_back(g);
+    if (geom_out) *geom_out = int(sc->geoms.size() - 1);
+  });
+}
+
+int b200_scene_add_planes(b200_scene s, const float *coeffs, int64_t n, const float *bounds, int *geom_out) {
+  if (!s) return B200_INVALID_ARGUMENT;
+  SceneObj *sc = reinterpret_cast<SceneObj *>(s);
+  return guarded(sc->dev, [&]() {
+    require(n >= 0 && (n == 0 || coeffs) && n < (int64_t(1) << 31), "bad plane array");
+    GeomObj g;
+    g.type = GEOM_PLANES;
+    g.nprims = n;
+    std::vector<float4> h(3 * size_t(n));
+    for (int64_t i = 0; i < n; i++) {
+      const float *c = coeffs + 4 * i;
+      h[3 * i] = make_float4(c[0], c[1], c[2], c[3]);
+      if (bounds) {
+        const float *b = bounds + 6 * i;
+        h[3 * i + 1] = make_float4(b[0], b[1], b[2], 1.f);
+        h[3 * i + 2] = make_float4(b[3], b[4], b[5], 0.f);
+      } else {
+        h[3 * i + 1] = h[3 * i + 2] = make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+    }
+    cudaStream_t st = sc->dev->stream;
+    check(cudaMallocAsync(&g.duser, sizeof(float4) * 3 * size_t(n > 0 ? n : 1), st), "alloc planes");
+    if (n) check(cudaMemcpyAsync(g.duser, h.data(), 48 * size_t(n), cudaMemcpyHostToDevice, st), "upload");
+    check(cudaStreamSynchronize(st), "upload planes");
     sc->geoms.push_back(g);
     if (geom_out) *geom_out = int(sc->geoms.size() - 1);
   });

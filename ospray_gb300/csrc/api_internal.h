@@ -60,7 +60,8 @@ struct GeomObj {
   int64_t nverts = 0;
   float *dnormals = nullptr, *dcolors = nullptr, *dtexcoords = nullptr;  // per-vertex attributes
   bool colorAlpha = false;  // some vertex colour has alpha != 1
-  float4 *dsph = nullptr;
+  float4 *dsph = nullptr;   // spheres, discs: (centre, radius) per primitive
+  float4 *duser = nullptr;  // oriented discs, planes: primStride(type) float4 per primitive
   BLAS blas;
   bool built = false;
 };

@@ -43,6 +43,26 @@ __global__ void k_sph_bounds(const float4 *s, int n, float4 *lo, float4 *hi) {
   hi[i] = make_float4(v.x + v.w, v.y + v.w, v.z + v.w, 0.f);
 }
 
+// user primitives (discs, oriented discs: the sphere's box; planes: their
+// box clipped to +-1e18, or +-1e18 without one, Planes_bounds
+// geometry/Planes.ispc:17-33); data: `stride` float4 per primitive
+__global__ void k_user_bounds(const float4 *data, int stride, int n, uint32_t type, float4 *lo, float4 *hi) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4 *p = data + size_t(i) * stride;
+  if (type == GEOM_PLANES) {
+    constexpr float M = 1e18f;
+    const float4 a = p[1], b = p[2];
+    const bool bounded = a.w != 0.f;
+    lo[i] = bounded ? make_float4(fmaxf(a.x, -M), fmaxf(a.y, -M), fmaxf(a.z, -M), 0.f) : make_float4(-M, -M, -M, 0.f);
+    hi[i] = bounded ? make_float4(fminf(b.x, M), fminf(b.y, M), fminf(b.z, M), 0.f) : make_float4(M, M, M, 0.f);
+    return;
+  }
+  const float4 v = p[0];
+  lo[i] = make_float4(v.x - v.w, v.y - v.w, v.z - v.w, 0.f);
+  hi[i] = make_float4(v.x + v.w, v.y + v.w, v.z + v.w, 0.f);
+}
+
 // centroid bounds (and overall bounds) via flipped-float atomics; acc[0..5]
 // centroid min/max, acc[6..11] box min/max
 __global__ void k_bounds(const float4 *lo, const float4 *hi, int n, uint32_t *acc) {
@@ -643,6 +663,15 @@ __global__ void k_gather_sph(const uint32_t *leafPrim, int n, const float4 *sph,
   ids[s] = p;
 }
 
+__global__ void k_gather_user(const uint32_t *leafPrim, int n, const float4 *data, int stride, float4 *prims,
+                              uint32_t *ids) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const uint32_t p = leafPrim[s];
+  for (int k = 0; k < stride; k++) prims[size_t(s) * stride + k] = data[size_t(p) * stride + k];
+  ids[s] = p;
+}
+
 inline int blocks(int n, int b) { return (n + b - 1) / b; }
 
 }  // namespace
@@ -813,6 +842,24 @@ cudaError_t buildSphereBLAS(const float4 *d_sph, int n, cudaStream_t st, BLAS &o
   if ((err = cudaMallocAsync(&out.prims, sizeof(float4) * size_t(n), st))) return err;
   if ((err = cudaMallocAsync(&out.primIDs, sizeof(uint32_t) * size_t(n), st))) return err;
   k_gather_sph<<<blocks(n, 256), 256, 0, st>>>(out.bvh.leafPrim, n, d_sph, out.prims, out.primIDs);
+  cudaFreeAsync(lo, st);
+  cudaFreeAsync(hi, st);
+  return cudaStreamSynchronize(st);
+}
+
+cudaError_t buildUserBLAS(uint32_t type, const float4 *d_data, int n, cudaStream_t st, BLAS &out, bool sah) {
+  out = BLAS{};
+  if (n <= 0) return cudaSuccess;
+  const int stride = primStride(type);
+  float4 *lo, *hi;
+  cudaError_t err;
+  if ((err = cudaMallocAsync(&lo, sizeof(float4) * n, st))) return err;
+  if ((err = cudaMallocAsync(&hi, sizeof(float4) * n, st))) return err;
+  k_user_bounds<<<blocks(n, 256), 256, 0, st>>>(d_data, stride, n, type, lo, hi);
+  if ((err = buildWide(lo, hi, n, st, out.bvh, sah))) return err;
+  if ((err = cudaMallocAsync(&out.prims, sizeof(float4) * size_t(n) * stride, st))) return err;
+  if ((err = cudaMallocAsync(&out.primIDs, sizeof(uint32_t) * size_t(n), st))) return err;
+  k_gather_user<<<blocks(n, 256), 256, 0, st>>>(out.bvh.leafPrim, n, d_data, stride, out.prims, out.primIDs);
   cudaFreeAsync(lo, st);
   cudaFreeAsync(hi, st);
   return cudaStreamSynchronize(st);

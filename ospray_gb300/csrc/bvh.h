@@ -26,6 +26,8 @@ cudaError_t buildWide(const float4 *lo, const float4 *hi, int n, cudaStream_t st
 cudaError_t buildTriangleBLAS(const float *d_verts, const uint32_t *d_index, int ntris, cudaStream_t st, BLAS &out,
                               bool sah = true, int primDiv = 1);
 cudaError_t buildSphereBLAS(const float4 *d_sph, int n, cudaStream_t st, BLAS &out, bool sah = true);
+// discs, oriented discs and planes: primStride(type) float4 per primitive
+cudaError_t buildUserBLAS(uint32_t type, const float4 *d_data, int n, cudaStream_t st, BLAS &out, bool sah = true);
 void freeBLAS(BLAS &b, cudaStream_t st);
 
 }  // namespace b200

@@ -118,7 +118,21 @@ struct __align__(16) Node8 {
 };
 static_assert(sizeof(Node8) == 80, "Node8 must be 80 bytes");
 
-enum GeomType : uint32_t { GEOM_TRIANGLES = 0, GEOM_SPHERES = 1 };
+// Spheres::commit "type" (geometry/Spheres.cpp:21-22,54: OSP_SPHERE, OSP_DISC,
+// OSP_ORIENTED_DISC) and Planes (geometry/Planes.ispc) are the user-primitive types
+enum GeomType : uint32_t {
+  GEOM_TRIANGLES = 0,
+  GEOM_SPHERES = 1,
+  GEOM_DISCS = 2,
+  GEOM_ORIENTED_DISCS = 3,
+  GEOM_PLANES = 4
+};
+// float4s per BLAS slot of each user-primitive type: spheres and discs
+// (centre, radius); oriented discs + (normal, 0); planes (a, b, c, d),
+// (lower, bounded flag), (upper, 0)
+B200_HD int primStride(uint32_t type) {
+  return type == GEOM_ORIENTED_DISCS ? 2 : (type == GEOM_PLANES ? 3 : 1);
+}
 
 // One (instance, geometric model) pair of the world: the unit the TLAS is
 // built over.  BLAS arrays are shared between entries of the same geometry.

@@ -19,7 +19,7 @@ T *asKind(const void *h, OSPDataType kind, const char *what) {
 
 bool known(OSPDataType kind, const std::string &t) {
   switch (kind) {
-    case OSP_GEOMETRY: return t == "mesh" || t == "sphere" || t == "box";
+    case OSP_GEOMETRY: return t == "mesh" || t == "sphere" || t == "box" || t == "plane";
     case OSP_MATERIAL: return t == "principled" || t == "obj" || t == "metal" || t == "glass" || t == "thinGlass";
     case OSP_LIGHT: return t == "quad" || t == "ambient" || t == "distant" || t == "sphere" || t == "spot";
     case OSP_CAMERA: return t == "perspective" || t == "orthographic" || t == "panoramic";

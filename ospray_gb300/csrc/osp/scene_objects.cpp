@@ -124,6 +124,21 @@ void GeometryObj::commit(B200Device &dev) {
       colors.clear();
       texcoords.clear();
     }
+  } else if (type == "plane") {
+    // Planes::commit (geometry/Planes.cpp): "plane.coefficients" vec4f, optional "plane.bounds" box3f
+    DataObj *c = getData("plane.coefficients");
+    if (!c || c->elem != OSP_VEC4F) throw Error(OSP_INVALID_ARGUMENT, "plane: 'plane.coefficients' must be vec4f data");
+    const auto cb = c->compact();
+    planes.resize(c->count() * 4);
+    std::memcpy(planes.data(), cb.data(), cb.size());
+    planeBounds.clear();
+    if (DataObj *b = getData("plane.bounds")) {
+      if (b->elem != OSP_BOX3F || b->count() != c->count())
+        throw Error(OSP_INVALID_ARGUMENT, "plane: 'plane.bounds' must be box3f data, one per plane");
+      const auto bb = b->compact();
+      planeBounds.resize(b->count() * 6);
+      std::memcpy(planeBounds.data(), bb.data(), bb.size());
+    }
   } else if (type == "box") {
     // Boxes::commit (geometry/Boxes.cpp:33-46): "box" data of box3f
     DataObj *b = getData("box");
@@ -147,6 +162,20 @@ void GeometryObj::commit(B200Device &dev) {
       std::memcpy(&spheres[4 * i], pb.data() + 12 * i, 12);
       spheres[4 * i + 3] = r ? radii[i] : radius;
     }
+    // Spheres::commit "type" (geometry/Spheres.cpp:43-54): spheres, ray-facing
+    // discs, or discs oriented by "sphere.normal"
+    sphereType = getInt("type", OSP_SPHERE);
+    if (sphereType != OSP_SPHERE && sphereType != OSP_DISC && sphereType != OSP_ORIENTED_DISC)
+      throw Error(OSP_INVALID_ARGUMENT, "sphere: unknown 'type'");
+    discNormals.clear();
+    if (sphereType == OSP_ORIENTED_DISC) {
+      DataObj *nd = getData("sphere.normal");
+      if (!nd || nd->elem != OSP_VEC3F || nd->count() != p->count())
+        throw Error(OSP_INVALID_ARGUMENT, "sphere: oriented discs need 'sphere.normal' vec3f data, one per disc");
+      const auto nb = nd->compact();
+      discNormals.resize(nd->count() * 3);
+      std::memcpy(discNormals.data(), nb.data(), nb.size());
+    }
   }
 }
 
@@ -160,6 +189,12 @@ void GeometryObj::bounds(float lo[3], float hi[3]) const {
       for (int k = 0; k < 3; k++) {
         lo[k] = std::fmin(lo[k], verts[3 * i + k]);
         hi[k] = std::fmax(hi[k], verts[3 * i + k]);
+      }
+  } else if (type == "plane") {  // Planes_bounds: the boxes clipped to +-1e18, or +-1e18
+    for (size_t i = 0; 4 * i < planes.size(); i++)
+      for (int k = 0; k < 3; k++) {
+        lo[k] = std::fmin(lo[k], planeBounds.empty() ? -1e18f : std::fmax(planeBounds[6 * i + k], -1e18f));
+        hi[k] = std::fmax(hi[k], planeBounds.empty() ? 1e18f : std::fmin(planeBounds[6 * i + 3 + k], 1e18f));
       }
   } else if (type == "box") {
     for (size_t i = 0; 6 * i < boxes.size(); i++)
@@ -484,6 +519,12 @@ void WorldObj::commit(B200Device &dev) {
           }
           else if (g->type == "box")
             dev.check(b200_scene_add_boxes(s, g->boxes.data(), int64_t(g->boxes.size() / 6), &gi));
+          else if (g->type == "plane")
+            dev.check(b200_scene_add_planes(s, g->planes.data(), int64_t(g->planes.size() / 4),
+                                            g->planeBounds.empty() ? nullptr : g->planeBounds.data(), &gi));
+          else if (g->sphereType != OSP_SPHERE)
+            dev.check(b200_scene_add_discs(s, g->spheres.data(), int64_t(g->spheres.size() / 4),
+                                           g->sphereType == OSP_ORIENTED_DISC ? g->discNormals.data() : nullptr, &gi));
           else
             dev.check(b200_scene_add_spheres(s, g->spheres.data(), int64_t(g->spheres.size() / 4), &gi));
           geomIndex[g] = gi;

@@ -43,6 +43,9 @@ struct GeometryObj : SceneObj {
   bool quads = false;           // mesh with a vec4ui "index"
   std::vector<float> spheres;   // sphere: xyzr per sphere
   std::vector<float> boxes;     // box: lower xyz, upper xyz per box
+  int sphereType = OSP_SPHERE;  // sphere: "type" (OSP_SPHERE, OSP_DISC, OSP_ORIENTED_DISC)
+  std::vector<float> discNormals;  // sphere of OSP_ORIENTED_DISC: "sphere.normal", xyz per disc
+  std::vector<float> planes, planeBounds;  // plane: "plane.coefficients" (4), "plane.bounds" (6) or empty
   void commit(B200Device &) override;
   void bounds(float lo[3], float hi[3]) const;
 };

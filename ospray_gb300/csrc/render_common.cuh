@@ -232,7 +232,10 @@ B200_D DG postIntersect(const Scene &sc, const Ray &ray, const HitRec &hit, DGAt
         }
       }
     }
+  } else if (e.type == GEOM_PLANES) {
+    eps = 0.f;  // Planes_postIntersect (geometry/Planes.ispc:115-121) sets no geometry epsilon
   } else {
+    // Spheres_postIntersect (geometry/Spheres.ispc:24-42): radius x ulpEpsilon, also for discs
     eps = fmul(__ldg(&e.spheres[hit.primID].w), ULP_EPSILON);
   }
   if (!e.identity) {

@@ -132,6 +132,77 @@ B200_D bool sphTest(V3 org, V3 d, float tnear, float tfar, float4 s, float &t, V
   return true;
 }
 
+// Ray-facing disc (Embree 4.3.3's DISC_POINT, the reference's OSP_DISC): the
+// disc through the centre perpendicular to the ray, hit at the centre's
+// projection onto the ray when the ray passes within the radius; Ng = -d.
+B200_D bool discTest(V3 org, V3 d, float tnear, float tfar, float4 s, float &t) {
+  const float rd2 = fdiv(1.f, dot(d, d));
+  const V3 c0 = sub(mk(s.x, s.y, s.z), org);
+  const float projC0 = fmul(dot(c0, d), rd2);
+  if (!(projC0 >= tnear && projC0 <= tfar)) return false;
+  const V3 perp = sub(c0, mul(projC0, d));
+  if (!(dot(perp, perp) <= fmul(s.w, s.w))) return false;
+  t = projC0;
+  return true;
+}
+
+// Oriented disc (Embree's ORIENTED_DISC_POINT, OSP_ORIENTED_DISC): the plane
+// through the centre with normal n, hit inside the radius; Ng = n.
+B200_D bool orientedDiscTest(V3 org, V3 d, float tnear, float tfar, float4 s, float4 n4, float &t) {
+  const V3 n = mk(n4.x, n4.y, n4.z);
+  const float div = dot(d, n);
+  if (div == 0.f) return false;
+  const V3 c = mk(s.x, s.y, s.z);
+  const float tt = fdiv(dot(sub(c, org), n), div);
+  if (!(tt >= tnear && tt <= tfar)) return false;
+  const V3 q = sub(add(org, mul(d, tt)), c);
+  if (!(dot(q, q) < fmul(s.w, s.w))) return false;
+  t = tt;
+  return true;
+}
+
+// Planes_intersect_kernel (geometry/Planes.ispc:40-78, intersectPlane and
+// intersectBox common/Intersect.ih:195-237, filterIntersectionSingle
+// common/FilterIntersect.ih): the plane n . P = d, hit for tnear < t <= tfar,
+// inside the plane's box when it has one; Ng = n.
+B200_D bool planeTest(V3 org, V3 d, float tnear, float tfar, const float4 *p, float &t) {
+  const float4 c = __ldg(p);
+  const V3 n = mk(c.x, c.y, c.z);
+  const float DdN = dot(d, n);
+  if (DdN == 0.f) return false;
+  const float tt = fdiv(fsub(c.w, dot(org, n)), DdN);
+  if (!(tt > tnear && tt <= tfar)) return false;
+  const float4 lo = __ldg(p + 1);
+  if (lo.w != 0.f) {
+    const float4 hi = __ldg(p + 2);
+    // rcp_safe: reciprocals of near-zero components clamped to 1e-18
+    auto rs = [](float x) { return fdiv(1.f, fabsf(x) < 1e-18f ? copysignf(1e-18f, x) : x); };
+    const V3 r = mk(rs(d.x), rs(d.y), rs(d.z));
+    const V3 m0 = mk(fmul(fsub(lo.x, org.x), r.x), fmul(fsub(lo.y, org.y), r.y), fmul(fsub(lo.z, org.z), r.z));
+    const V3 m1 = mk(fmul(fsub(hi.x, org.x), r.x), fmul(fsub(hi.y, org.y), r.y), fmul(fsub(hi.z, org.z), r.z));
+    const float en = fmaxf(fmaxf(fminf(m0.x, m1.x), fminf(m0.y, m1.y)), fminf(m0.z, m1.z));
+    const float ex = fminf(fminf(fmaxf(m0.x, m1.x), fmaxf(m0.y, m1.y)), fmaxf(m0.z, m1.z));
+    if (!(en < ex) || tt < en || tt > ex) return false;
+  }
+  t = tt;
+  return true;
+}
+
+// the disc and plane tests by type (out of line: the triangle and sphere
+// tests of the traversal loop keep their registers); Ng from userNormal
+static __device__ __noinline__ bool userTest(uint32_t type, V3 org, V3 d, float tnear, float tfar, const float4 *prims,
+                                      uint32_t slot, float &t) {
+  if (type == GEOM_DISCS) return discTest(org, d, tnear, tfar, __ldg(prims + slot), t);
+  if (type == GEOM_ORIENTED_DISCS)
+    return orientedDiscTest(org, d, tnear, tfar, __ldg(prims + 2 * slot), __ldg(prims + 2 * slot + 1), t);
+  return planeTest(org, d, tnear, tfar, prims + 3 * slot, t);
+}
+static __device__ __noinline__ V3 userNormal(uint32_t type, V3 d, const float4 *prims, uint32_t slot) {
+  if (type == GEOM_DISCS) return neg(d);
+  const float4 n = __ldg(prims + (type == GEOM_ORIENTED_DISCS ? 2 * slot + 1 : 3 * slot));
+  return mk(n.x, n.y, n.z);
+}
+
 // Is a hit at t of (entry e, prim) better than the current closest
 // (ht, hentry, hprim)?  Equal t resolves to the smallest (instID, geomID,
 // primID); the IDs are read from the entries only for such ties.
@@ -423,8 +494,10 @@ struct Traverser {
       const V3 v0 = mk(a.x, a.y, a.z), v1 = mk(b.x, b.y, b.z), v2 = mk(c.x, c.y, c.z);
       triTest(triPre(d), o, ray.tnear, ht, v0, v1, v2, t, hit.u, hit.v);
       hit.Ng = cross(sub(v1, v0), sub(v2, v0));
-    } else {
+    } else if (e.type == GEOM_SPHERES) {
       sphTest(o, d, ray.tnear, ht, __ldg(e.prims + hslot), t, hit.Ng);
+    } else {
+      hit.Ng = userNormal(e.type, d, e.prims, hslot);
     }
   }
 
@@ -476,8 +549,12 @@ struct Traverser {
         h = triTest(pre, org, ray.tnear, ht, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), mk(c.x, c.y, c.z), t, u, v);
         prim = __float_as_uint(a.w);
       } else {
-        V3 Ng;
-        h = sphTest(org, dir, ray.tnear, ht, __ldg(prims + slot), t, Ng);
+        if (etype == GEOM_SPHERES) {
+          V3 Ng;
+          h = sphTest(org, dir, ray.tnear, ht, __ldg(prims + slot), t, Ng);
+        } else {
+          h = userTest(etype, org, dir, ray.tnear, ht, prims, slot, t);
+        }
         prim = __ldg(primIDs + slot);
       }
       if (h && better(sc, t, eidx, prim, ht, hentry, hprim)) {

@@ -235,6 +235,8 @@ def lib():
         L.or_set_aux_output.argtypes = [P, P]
         L.or_set_ao_volume.argtypes = [P, F]
         L.or_scene_add_spheres.argtypes = [P, P, I]
+        L.or_scene_add_discs.argtypes = [P, P, I, P]
+        L.or_scene_add_planes.argtypes = [P, P, I, P]
         L.or_scene_add_instance.argtypes = [P, I, U32, U32, P, I]
         L.or_pt_new.restype = P
         L.or_pt_free.argtypes = [P]
@@ -317,6 +319,16 @@ class Scene:
     def add_spheres(self, xyzr):
         s = np.ascontiguousarray(xyzr, np.float32)
         return lib().or_scene_add_spheres(self.h, _p(s), len(s))
+
+    def add_discs(self, xyzr, normals=None):
+        s = np.ascontiguousarray(xyzr, np.float32).reshape(-1, 4)
+        n = None if normals is None else np.ascontiguousarray(normals, np.float32).reshape(-1, 3)
+        return lib().or_scene_add_discs(self.h, _p(s), len(s), _p(n))
+
+    def add_planes(self, coeffs, bounds=None):
+        c = np.ascontiguousarray(coeffs, np.float32).reshape(-1, 4)
+        b = None if bounds is None else np.ascontiguousarray(bounds, np.float32).reshape(-1, 6)
+        return lib().or_scene_add_planes(self.h, _p(c), len(c), _p(b))
 
     def add_instance(self, geom, inst_id, geom_id, xfm=None, material=-1):
         x = None if xfm is None else np.ascontiguousarray(xfm, np.float32).reshape(12)

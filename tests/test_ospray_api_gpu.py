@@ -136,6 +136,86 @@ def test_ao_through_ospray_api_matches_oracle(osp_device):
         L.ospRelease(h)
 
 
+def test_discs_and_planes_through_ospray_api_match_oracle(osp_device):
+    """"sphere" geometry of "type" OSP_DISC / OSP_ORIENTED_DISC (with
+    "sphere.normal") and "plane" geometry ("plane.coefficients", "plane.bounds")
+    made through libospray.so render the oracle's AO frame."""
+    L = osp_device
+    keep = []
+    W = H = 128
+    rng = np.random.default_rng(12)
+    c = np.concatenate([rng.uniform(-2, 2, (60, 1)), rng.uniform(0.3, 2, (60, 1)), rng.uniform(-2, 2, (60, 1))], 1)
+    r = rng.uniform(0.1, 0.4, 60).astype(np.float32)
+    nrm = rng.normal(size=(60, 3)).astype(np.float32)
+    geoms = []
+    for kind in (51, 52):  # OSP_DISC, OSP_ORIENTED_DISC
+        g = L.ospNewGeometry(b"sphere")
+        osp_api.set_data(g, "sphere.position", (c + (kind - 51) * 0.3).astype(np.float32), osp_api.OSP_VEC3F, 60, keep)
+        osp_api.set_data(g, "sphere.radius", r, osp_api.OSP_FLOAT, 60, keep)
+        osp_api.set_param(g, "type", osp_api.OSP_UINT, np.uint32(kind))
+        if kind == 52:
+            osp_api.set_data(g, "sphere.normal", nrm, osp_api.OSP_VEC3F, 60, keep)
+        L.ospCommit(g)
+        geoms.append(g)
+    pl = L.ospNewGeometry(b"plane")
+    coeffs = np.array([[0, 1, 0, 0], [0.3, 0.2, 1.0, 1.5]], np.float32)
+    bounds = np.array([[-1e30, -1e30, -1e30, 1e30, 1e30, 1e30], [-2, -1, -3, 2, 3, 3]], np.float32)
+    osp_api.set_data(pl, "plane.coefficients", coeffs, 6003, 2, keep)      # OSP_VEC4F
+    osp_api.set_data(pl, "plane.bounds", bounds, 10002, 2, keep)           # OSP_BOX3F
+    L.ospCommit(pl)
+    geoms.append(pl)
+    models = []
+    for g in geoms:
+        m = L.ospNewGeometricModel(g)
+        L.ospCommit(m)
+        models.append(m)
+        L.ospRelease(g)
+    arr = (ctypes.c_void_p * 3)(*models)
+    md = L.ospNewSharedData(ctypes.addressof(arr), osp_api.OSP_GEOMETRIC_MODEL, 3, 0, 1, 0, 1, 0, None, None)
+    group = L.ospNewGroup()
+    osp_api.set_param(group, "geometry", osp_api.OSP_DATA, md)
+    L.ospRelease(md)
+    for m in models:
+        L.ospRelease(m)
+    L.ospCommit(group)
+    inst = L.ospNewInstance(group)
+    L.ospCommit(inst)
+    L.ospRelease(group)
+    world = L.ospNewWorld()
+    L.ospSetObjectAsData(world, b"instance", osp_api.OSP_INSTANCE, inst)
+    L.ospRelease(inst)
+    L.ospCommit(world)
+    pos, dirc, up = (0.0, 3.0, -6.5), (0.0, -2.0, 6.0), (0.0, 1.0, 0.0)
+    cam = L.ospNewCamera(b"perspective")
+    for key, val in (("position", pos), ("direction", dirc), ("up", up)):
+        osp_api.set_param(cam, key, osp_api.OSP_VEC3F, np.float32(val))
+    osp_api.set_param(cam, "aspect", osp_api.OSP_FLOAT, np.float32(1.0))
+    L.ospCommit(cam)
+    ren = L.ospNewRenderer(b"ao")
+    osp_api.set_param(ren, "pixelFilter", osp_api.OSP_UINT, np.uint32(0))
+    osp_api.set_param(ren, "aoSamples", osp_api.OSP_INT, np.int32(1))
+    L.ospCommit(ren)
+    fb = L.ospNewFrameBuffer(W, H, osp_api.OSP_FB_RGBA32F,
+                             osp_api.OSP_FB_COLOR | osp_api.OSP_FB_ID_PRIMITIVE | osp_api.OSP_FB_ID_OBJECT)
+    fut = L.ospRenderFrame(fb, ren, cam, world)
+    assert fut, L.ospDeviceGetLastErrorMsg(L.ospGetCurrentDevice())
+    L.ospWait(fut, osp_api.OSP_TASK_FINISHED)
+    L.ospRelease(fut)
+    color = osp_api.map_channel(fb, osp_api.OSP_FB_COLOR, (H, W, 4), np.float32)
+    geom = osp_api.map_channel(fb, osp_api.OSP_FB_ID_OBJECT, (H, W), np.uint32)
+    for h in (fb, ren, cam, world):
+        L.ospRelease(h)
+    o = oracle.Scene()
+    o.add_instance(o.add_discs(np.concatenate([c, r[:, None]], 1)), 0, 0)
+    o.add_instance(o.add_discs(np.concatenate([c + 0.3, r[:, None]], 1), normals=nrm), 0, 1)
+    o.add_instance(o.add_planes(coeffs, bounds), 0, 2)
+    o.commit()
+    ref = oracle.render_ao(o, oracle.camera(pos, dirc, up), 0, W, H)
+    assert set(np.unique(geom).tolist()) >= {0, 1, 2}
+    assert np.mean(geom == ref["geomID"]) >= 0.999
+    assert np.mean(np.all(np.abs(color - ref["color"]) <= 1e-4, axis=2)) >= 0.999
+
+
 def test_unsupported_types_report_errors(osp_device):
     L = osp_device
     dev = L.ospGetCurrentDevice()

@@ -246,3 +246,77 @@ def test_boxes_match_oracle(b200_device):
     assert np.mean(fb.read(og.FB_ID_PRIMITIVE) == ref["primID"]) >= 0.999
     c, r = fb.read(og.FB_COLOR), ref["color"]
     assert np.mean(np.all(np.abs(c - r) <= 1e-4, axis=2)) >= 0.999
+
+
+def _discs_planes(s, rng_seed=4):
+    """Ray-facing discs, oriented discs (one instance moved and scaled), an
+    unbounded ground plane y = 0 and a tilted plane bounded by a box."""
+    rng = np.random.default_rng(rng_seed)
+    d = np.concatenate([rng.uniform(-3, 3, (300, 1)), rng.uniform(0.2, 2.5, (300, 1)), rng.uniform(-3, 3, (300, 1)),
+                        rng.uniform(0.05, 0.3, (300, 1))], 1).astype(np.float32)
+    od = d.copy()
+    od[:, 1] += 0.4
+    nrm = rng.normal(size=(300, 3)).astype(np.float32)
+    k0 = s.add_discs(d)
+    k1 = s.add_discs(od, normals=nrm)
+    k2 = s.add_planes(np.array([[0, 1, 0, 0]], np.float32))
+    k3 = s.add_planes(np.array([[0.3, 0.2, 1.0, 1.5]], np.float32), bounds=np.array([[-2, -1, -3, 2, 3, 3]], np.float32))
+    s.add_instance(k0, 0, 0, None, 0)
+    s.add_instance(k1, 1, 0, np.array([[1.1, 0, 0, 0.2], [0, 0.9, 0, 0.1], [0, 0, 1.0, -0.3]], np.float32), 1)
+    s.add_instance(k2, 2, 0, None, 2)
+    s.add_instance(k3, 3, 0, None, 1)
+    s.commit()
+
+
+def test_discs_and_planes_match_oracle(b200_device):
+    """Discs facing the ray, oriented discs and planes (unbounded and boxed):
+    closest hits (IDs, t bit for bit, Ng), any-hit, and AO frames with the
+    discs' radius epsilon and the planes' zero geometry epsilon."""
+    import ospray_gb300 as og
+    g, o = both(b200_device, _discs_planes)
+    rng = np.random.default_rng(5)
+    n = 100000
+    org = np.concatenate([rng.uniform(-4, 4, (n, 1)), rng.uniform(0.5, 4, (n, 1)), rng.uniform(-4, 4, (n, 1))], 1)
+    dirn = rng.normal(size=(n, 3))
+    rays = np.concatenate([org, np.zeros((n, 1)), dirn, np.full((n, 1), np.inf)], 1).astype(np.float32)
+    gf, gi = gpu_trace(g, rays)
+    of, oi = o.trace(rays)
+    hit = np.isfinite(of[:, 0])
+    for inst in range(4):
+        assert np.sum(oi[hit, 2] == inst) > 100, inst
+    assert_closest_parity(gf, gi, of, oi, min_agree=0.9999)
+    same = np.all(gi == oi, axis=1) & hit
+    np.testing.assert_allclose(gf[same, 3:6], of[same, 3:6], rtol=1e-5, atol=1e-6)
+    go, _ = gpu_trace(g, rays, occlusion=True)
+    oo, _ = o.trace(rays, occlusion=True)
+    assert np.mean(go[:, 0] == oo[:, 0]) >= 0.9999
+    W = H = 96
+    pos, dirc, up = (0.0, 3.0, -6.5), (0.0, -2.0, 6.0), (0.0, 1.0, 0.0)
+    fb = og.Frame(b200_device, W, H, og.FB_COLOR | og.FB_DEPTH | og.FB_ID_PRIMITIVE | og.FB_ID_INSTANCE)
+    og.render_ao(g, og.camera_desc(pos, dirc, up), og.ao_params(pixel_filter=og.PF_POINT, ao_samples=2), fb)
+    ref = oracle.render_ao(o, oracle.camera(pos, dirc, up), og.PF_POINT, W, H, ao_samples=2)
+    assert np.mean(fb.read(og.FB_ID_INSTANCE) == ref["instID"]) >= 0.999
+    assert np.mean(fb.read(og.FB_ID_PRIMITIVE) == ref["primID"]) >= 0.999
+    c, r = fb.read(og.FB_COLOR), ref["color"]
+    assert np.mean(np.all(np.abs(c - r) <= 1e-4, axis=2)) >= 0.999
+
+
+def test_discs_and_planes_path_traced_match_oracle(b200_device):
+    import ospray_gb300 as og
+    g, o = both(b200_device, _discs_planes)
+    lights = [dict(type="quad", position=(-1.0, 6.0, -1.0), edge1=(2.0, 0.0, 0.0), edge2=(0.0, 0.0, 2.0),
+                   intensity=10.0), dict(type="ambient", intensity=0.1)]
+    g.set_lights([og.quad_light(L["position"], L["edge1"], L["edge2"], L["intensity"]) if L["type"] == "quad"
+                  else og.ambient_light(L["intensity"]) for L in lights])
+    mats = [(0.8, 0.3, 0.2, 0.4, 0.0), (0.2, 0.7, 0.3, 0.2, 1.0), (0.7, 0.7, 0.7, 0.9, 0.0)]
+    W, H = 128, 96
+    pos, dirc, up = (0.0, 3.0, -6.5), (0.0, -2.0, 6.0), (0.0, 1.0, 0.0)
+    fb = og.Frame(b200_device, W, H, og.FB_COLOR | og.FB_ACCUM | og.FB_ID_PRIMITIVE)
+    og.render_pt(g, og.camera_desc(pos, dirc, up, aspect=W / H), og.pt_params(spp=4, max_path_length=4),
+                 og.materials_array(mats), fb)
+    ref = oracle.render_pt(o, oracle.PtWorld(mats, lights), oracle.camera(pos, dirc, up, aspect=W / H),
+                           oracle.pt_params(spp=4, max_path_length=4), W, H)
+    assert np.mean(fb.read(og.FB_ID_PRIMITIVE) == ref["primID"]) >= 0.999
+    gc, rc = fb.read(og.FB_ACCUM)[..., :3], ref["color"][..., :3]
+    close = np.all(np.abs(gc - rc) <= 1e-3 * np.maximum(1.0, np.abs(rc)), axis=2)
+    assert close.mean() >= 0.995, close.mean()

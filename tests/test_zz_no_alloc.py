@@ -80,3 +80,43 @@ def test_noalloc_refuses_requests_over_its_limit(b200_device):
     msg = og.lib().b200_device_last_error(b200_device._h).decode()
     assert "exceeds the static scratch limit" in msg
     assert big.frame_id == 0
+
+
+def test_noalloc_allocates_nothing_on_a_callers_stream(b200_device):
+    """Frames rendered on a stream the test created allocate no device
+    memory (cudaMemGetInfo's free bytes equal before and after, past the
+    first call) and match the allocating path tracer."""
+    torch = pytest.importorskip("torch")
+    import ospray_gb300 as og
+    d, g = _scene(b200_device)
+    c = d["camera"]
+    cam = og.camera_desc(c["position"], c["direction"], c["up"], fovy=c["fovy"], aspect=c["aspect"])
+    p = og.pt_params(spp=SPP, max_path_length=5, roulette_path_length=3)
+    mats = og.materials_array(d["materials"])
+    fa = og.Frame(b200_device, W, H, og.FB_COLOR)
+    fn = og.Frame(b200_device, W, H, og.FB_COLOR)
+    stream = torch.cuda.Stream()
+    fn_c = og.lib().b200_render_pt_noalloc
+    fn_c.restype = ctypes.c_int
+    fn_c.argtypes = [ctypes.c_void_p, ctypes.POINTER(og.CameraDesc), ctypes.POINTER(og.PTParams), ctypes.c_void_p,
+                     ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+    arr, n = mats
+
+    def call():
+        rc = fn_c(g._h, ctypes.byref(cam), ctypes.byref(p), ctypes.cast(arr, ctypes.c_void_p), n, fn._h,
+                  ctypes.c_void_p(stream.cuda_stream))
+        assert rc == 0, og.lib().b200_device_last_error(b200_device._h)
+
+    call()  # first call: module data and the scratch array's address are set up here
+    stream.synchronize()
+    fn.reset()
+    b200_device.sync()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(3):
+        call()
+    stream.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0, (free0, free1)
+    for _ in range(3):
+        og.render_pt(g, cam, p, mats, fa)
+    np.testing.assert_allclose(fn.read(og.FB_COLOR), fa.read(og.FB_COLOR), rtol=1e-4, atol=1e-5)
