@@ -262,6 +262,18 @@ typedef struct {
   int collectStats;  /* nonzero: count rays / node visits / primitive tests */
   float volumeSamplingRate; /* the scene's volume, composited in front of each layer (render/ao/volumes.ispc);
                                <= 0: 1 */
+  /* the renderer's "map_backplate" and "map_maxDepth" (Renderer_getBackground /
+   * Renderer_getMaxDepth render/Renderer.ispc:19-40), both looked up at the
+   * pixel centre; null: backgroundColor / no depth limit */
+  struct b200_texture_t *backplate;
+  struct b200_texture_t *maxDepth;
+  float mipMapBias;
+  /* surface colour and opacity (getSurfaceColor render/ao/surfaces.ispc:
+   * 17-42): obj materials' kd, d and map_kd times the vertex colour; a ray
+   * continues through surfaces that are not opaque.  Indexed by the
+   * instances' material_id; null / 0: white, opaque surfaces */
+  const struct b200_scivis_material_t *materials;
+  int nmaterials;
 } b200_ao_params;
 
 /* ---- lights of the world (QuadLight::commit lights/QuadLight.cpp:68-108,
@@ -328,10 +340,12 @@ int b200_texture_sample(b200_texture tex, int64_t n, const float *st, const floa
  *   B200_MATERIAL_PRINCIPLED  (render/materials/Principled.ispc:81-455,
  *     Principled.cpp:37-79): baseColor, roughness, metallic, opacity (the
  *     cut-out: a specular transmission lobe of importance 1 - opacity, and
- *     shadow rays pass with transparency 1 - opacity); the other principled
- *     parameters keep their defaults (specular 1, ior 1, edgeColor 1, no
- *     transmission, coat or sheen; roughness 0 is treated as the smallest
- *     microfacet roughness).
+ *     shadow rays pass with transparency 1 - opacity), specular (the
+ *     dielectric coating's weight), ior (the coating's index), diffuse (the
+ *     substrate's weight), edgeColor (the conductor's edge tint) and
+ *     specularMetallic; roughness 0 gives smooth (Dirac) coating and
+ *     conductor lobes over a Lambert substrate.  Transmission, thin, coat,
+ *     sheen, backlight and emission keep their defaults (off).
  *   B200_MATERIAL_OBJ  (render/materials/OBJ.ispc:29-126, OBJ.cpp:28-65):
  *     kd = baseColor, ks, ns, d = opacity, tf: Lambert (kd d) + Blinn
  *     specular (ks d, exponent ns) + specular transmission (tf d + 1 - d);
@@ -368,6 +382,11 @@ typedef struct {
   float thickness;     /* thinGlass */
   b200_texture baseColorMap; /* principled map_baseColor (rgb x baseColor, alpha x opacity); obj map_kd (rgb x
                                 kd, alpha x d); looked up at the hit's texture coordinates; null: none */
+  float specular;        /* principled, default 1 */
+  float ior;             /* principled, default 1 */
+  float diffuse;         /* principled, default 1 */
+  float edgeColor[3];    /* principled, default 1 */
+  int specularMetallic;  /* principled, default 1: the conductor's weight x specular */
 } b200_material;
 /* the reference's defaults for a material of `type` (principled: baseColor
  * 0.8, roughness 0, metallic 0, opacity 1; obj: kd 0.8, ks 0, ns 10, d 1,
@@ -388,9 +407,11 @@ typedef struct {
   int pixelFilter;
   int collectStats;
   b200_texture backplate; /* "map_backplate" (Renderer_getBackground render/Renderer.ispc:19-29): looked up at
-                             the camera sample's screen position for paths that see the background; null: the
+                             the pixel centre for paths that see the background straight; null: the
                              background colour */
   float mipMapBias;       /* "mipMapBias" (Renderer.cpp:41): footprint x 2^bias for MIP level selection */
+  b200_texture maxDepth;  /* "map_maxDepth" (Renderer_getMaxDepth render/Renderer.ispc:30-40, PathTracer.ispc:
+                             189-192): the camera ray's tfar = max(0, texel.r) at the sample's screen position */
 } b200_pt_params;
 int b200_render_pt(b200_scene scene, const b200_camera_desc *camera, const b200_pt_params *params,
                    const b200_material *materials, int nmaterials, b200_frame fb, void *stream);
@@ -464,17 +485,21 @@ typedef struct {
   int aoSamples;            /* default 0 */
   float aoDistance;         /* default 1e20 */
   float minContribution;    /* default 0.001 */
+  b200_texture backplate;   /* "map_backplate" at the pixel centre (null: backgroundColor) */
+  b200_texture maxDepth;    /* "map_maxDepth" at the pixel centre (null: no depth limit) */
+  float mipMapBias;         /* footprint x 2^bias for map_kd level selection */
 } b200_scivis_params;
 /* The material parameters SciVis reads (evalMaterial,
  * render/scivis/surfaces.ih:44-84): isObj != 0 for an "obj" material (kd,
  * ks, ns, d, tf as in OBJMaterial::commit render/materials/OBJ.cpp); any
  * other material shades white and opaque.  material_id of an instance
  * indexes this array; ids outside it shade with the defaults. */
-typedef struct {
+typedef struct b200_scivis_material_t {
   int isObj;
   float kd[3], ks[3];
   float ns, d;
   float tf[3];
+  b200_texture kdMap; /* obj "map_kd": kd x texel rgb, d x texel alpha (surfaces.ih:66-72); null: none */
 } b200_scivis_material;
 int b200_render_scivis(b200_scene scene, const b200_camera_desc *camera, const b200_scivis_params *params,
                        const b200_scivis_material *materials, int nmaterials, b200_frame fb, void *stream);

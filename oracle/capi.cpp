@@ -274,10 +274,26 @@ struct OrFrame {
   uint32_t *instID;
 };
 
+// the AO renderer's optional inputs: map_backplate, map_maxDepth (Textures
+// or null), mipMapBias, and obj materials (isObj, kd[3], ks[3], ns, d,
+// tf[3], map_kd as in b200_scivis_material; null / 0: white surfaces)
+struct OrAoExtra {
+  const void *backplate, *maxDepth;
+  float mipMapBias;
+  const void *materials;
+  int nmaterials;
+};
+struct OrAoMaterial {
+  int isObj;
+  float kd[3], ks[3], ns, d, tf[3];
+  const void *kdMap;
+};
+
 // Renders `frames` accumulated frames of the AO renderer; outputs the final
 // accumulation buffers.
 void or_render_ao(void *sp, const OrCamera *c, int pixelFilter, int W, int H, int spp, int aoSamples,
-                  float aoRadius, float aoIntensity, const float *bg, int frames, OrFrame *out, int nthreads) {
+                  float aoRadius, float aoIntensity, const float *bg, int frames, OrFrame *out, int nthreads,
+                  const OrAoExtra *extra) {
   const Scene &s = *static_cast<Scene *>(sp);
   const Camera cam = makeCamera({c->pos[0], c->pos[1], c->pos[2]}, {c->dir[0], c->dir[1], c->dir[2]},
                                 {c->up[0], c->up[1], c->up[2]}, c->fovy, c->aspect, c->nearClip, c->type, c->height);
@@ -285,7 +301,21 @@ void or_render_ao(void *sp, const OrCamera *c, int pixelFilter, int W, int H, in
   pf.init(pixelFilter);
   FrameBuffer fb;
   fb.resize(W, H);
-  AOParams p = {spp, aoSamples, aoRadius, aoIntensity, {bg[0], bg[1], bg[2], bg[3]}};
+  AOParams p;
+  p.spp = spp;
+  p.aoSamples = aoSamples;
+  p.aoRadius = aoRadius;
+  p.aoIntensity = aoIntensity;
+  p.bgColor = {bg[0], bg[1], bg[2], bg[3]};
+  if (extra) {
+    p.backplate = static_cast<const Texture *>(extra->backplate);
+    p.maxDepth = static_cast<const Texture *>(extra->maxDepth);
+    p.mipBiasFactor = std::pow(2.f, extra->mipMapBias);
+    const OrAoMaterial *m = static_cast<const OrAoMaterial *>(extra->materials);
+    for (int i = 0; i < extra->nmaterials; i++)
+      p.mats.push_back({m[i].isObj, {m[i].kd[0], m[i].kd[1], m[i].kd[2]}, m[i].d,
+                        static_cast<const Texture *>(m[i].kdMap)});
+  }
   for (int f = 0; f < frames; f++) renderAO(s, cam, pf, p, fb, nthreads);
   const size_t N = size_t(W) * H;
   std::memcpy(out->color, fb.color.data(), N * 4 * sizeof(float));

@@ -35,16 +35,7 @@ V3 fresnelConductorRGB(float c, V3 eta, V3 k) {
   return {fresnelConductor1(c, eta.x, k.x), fresnelConductor1(c, eta.y, k.y), fresnelConductor1(c, eta.z, k.z)};
 }
 
-// fresnelDielectricEx (bsdfs/Fresnel.ih:38-47)
-float fresnelDielectricEx(float cosI, float &cosT, float eta) {
-  const float c = sqrCosT(cosI, eta);
-  if (c < 0.f) {
-    cosT = 0.f;
-    return 1.f;
-  }
-  cosT = std::sqrt(c);
-  return fresnelDielectric(cosI, cosT, eta);
-}
+
 
 // RobustThinDielectric reflection R and transmission T of the slab
 void thinSlab(float cosO, float eta, V3 att, V3 &R, V3 &T) {
@@ -70,6 +61,11 @@ MaterialParams commitMaterial(int type, const float *p) {
   const V3 tf = {p[10], p[11], p[12]}, eta = {p[13], p[14], p[15]}, k = {p[16], p[17], p[18]};
   const V3 attColor = {p[19], p[20], p[21]};
   const float attDist = p[22], thickness = p[23];
+  m.specular = p[24];
+  m.ior = p[25];
+  m.diffuse = p[26];
+  m.edgeColor = {p[27], p[28], p[29]};
+  m.specularMetallic = p[30] != 0.f;
   constexpr float eps = 1e-6f;
   switch (type) {
     case MAT_OBJ: {
@@ -247,9 +243,15 @@ SurfaceBSDF makeBSDF(const MaterialParams &m0, const DG &dg, V3 dPds, const Medi
         pp.baseColor = m.baseColor;
         pp.roughness = m.roughness;
         pp.metallic = m.metallic;
+        pp.specular = m.specular;
+        pp.ior = m.ior;
+        pp.diffuse = m.diffuse;
+        pp.edgeColor = m.edgeColor;
+        pp.specularMetallic = m.specularMetallic;
+        pp.fromOutside = sameMedium(cur, vacuum());  // Principled's outside medium: vacuum
         b.st.init(pp, f);
         b.albedo = b.st.albedo * b.op;
-        b.smooth = b.st.impSum > 0.f;
+        b.smooth = b.st.smooth;
       }
       b.impSum = 0.f;
       if (b.hasCut) {

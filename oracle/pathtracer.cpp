@@ -25,6 +25,7 @@ struct PtParams {
   V4 bg;
   const Texture *backplate = nullptr;  // map_backplate
   float mipBiasFactor = 1.f;           // 2^mipMapBias
+  const Texture *maxDepth = nullptr;   // map_maxDepth
 };
 
 struct PtLights {
@@ -332,7 +333,9 @@ void renderPT(const Scene &sc, const PtLights &lights, const std::vector<Materia
         const V2 pfs = pf.sample(ps);
         const V2 center = {(float(x) + 0.5f) * rcpSize.x, (float(y) + 0.5f) * rcpSize.y};
         const V2 screen = {center.x + pfs.x * rcpSize.x, center.y + pfs.y * rcpSize.y};
-        const Ray ray = cameraRay(cam, screen);
+        Ray ray = cameraRay(cam, screen);
+        // Renderer_getMaxDepth at the sample's screen position (PathTracer.ispc:189-192)
+        if (p.maxDepth) ray.tfar = std::fmin(ray.tfar, std::fmax(0.f, p.maxDepth->get(screen, 0.f).x));
         const PathOut o = samplePath(c, ld, ray, cameraCone(cam, screen, rcpSize.y), center);
         ScreenSample smp;
         smp.rgb = vmin(o.rgb, v3(p.maxContribution));
@@ -379,11 +382,12 @@ void *or_pt_new() { return new OrPtScene(); }
 void or_pt_free(void *p) { delete static_cast<OrPtScene *>(p); }
 int or_pt_add_material(void *p, const float *baseColor, float roughness, float metallic) {
   OrPtScene &s = *static_cast<OrPtScene *>(p);
-  const float f[24] = {baseColor[0], baseColor[1], baseColor[2], roughness, metallic, 1.f};
+  float f[31] = {baseColor[0], baseColor[1], baseColor[2], roughness, metallic, 1.f};
+  for (int k = 24; k < 31; k++) f[k] = 1.f;  // specular, ior, diffuse, edgeColor, specularMetallic
   s.mats.push_back(commitMaterial(MAT_PRINCIPLED, f));
   return int(s.mats.size() - 1);
 }
-// type MAT_*, params: 24 floats in b200_material order after its type field
+// type MAT_*, params: 31 floats in b200_material order after its type field (no colour map)
 int or_pt_add_material2(void *p, int type, const float *params) {
   OrPtScene &s = *static_cast<OrPtScene *>(p);
   s.mats.push_back(commitMaterial(type, params));
@@ -459,6 +463,7 @@ struct OrPtParams {
   int pixelFilter;
   const void *backplate;  // a Texture from or_texture_new, or null
   float mipMapBias;
+  const void *maxDepth;   // a Texture or null
 };
 
 // Renders `frames` accumulated frames of rows [y0, y1) (y1 <= 0: all rows).
@@ -473,7 +478,7 @@ void or_render_pt(void *scp, void *ptp, const OrCameraPT *cam, const OrPtParams 
   PtParams p = {pp->spp, pp->maxPathLength, pp->roulettePathLength, pp->maxScatteringEvents, pp->lightSamples,
                 pp->limitIndirectLightSamples, pp->minContribution, pp->maxContribution,
                 {pp->bg[0], pp->bg[1], pp->bg[2], pp->bg[3]}, static_cast<const Texture *>(pp->backplate),
-                std::pow(2.f, pp->mipMapBias)};
+                std::pow(2.f, pp->mipMapBias), static_cast<const Texture *>(pp->maxDepth)};
   if (y1 <= 0) {
     y0 = 0;
     y1 = H;

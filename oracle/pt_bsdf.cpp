@@ -71,45 +71,64 @@ const AlbedoTables &albedoTables() {
   return t;
 }
 
+// The principled base stack (Principled.ispc:110-331) without
+// transmission, coat or sheen: a MultiBSDF of the conductor (child 0) and
+// the plastic layer (child 2).  roughness 0 (the parameter, < EPS): a smooth
+// DielectricLayer over Lambert (bsdfs/DielectricLayer.ih) and a smooth
+// Conductor (bsdfs/Conductor.ih); else MicrofacetDielectricLayer over
+// Oren-Nayar and MicrofacetConductor.  specular 0: a PassthroughLayer.
 void Principled::init(const PrincipledParams &p, const L3 &f) {
   frame = f;
   N = f.vz;
   const AlbedoTables &T = albedoTables();
   const V3 baseColor = {clamp01(p.baseColor.x), clamp01(p.baseColor.y), clamp01(p.baseColor.z)};
-  const float metallic = clamp01(p.metallic), specular = 1.f, diffuseW = 1.f;
+  const float metallic = clamp01(p.metallic), specular = clamp01(p.specular), diffuseW = clamp01(p.diffuse);
   roughness = clamp01(p.roughness);
   ggx = makeGGX(roughness);
+  smoothBase = p.roughness < EPS;
   albedo = v3(0.f);
   wC = iC = wP = iP = impSum = 0.f;
-  // dielectric part: ior 1 inside a vacuum -> eta = 1 (PrincipledShared.h:137)
+  smooth = hasLayer = false;
   const float dielectric = 1.f - metallic;
   if (dielectric > EPS) {
-    float ior = 1.f;
-    float e = 1.f / ior;  // fromOutside: outside ior (1) / ior
+    float ior = p.ior;
+    if (ior < 1.f) ior = 1.f / ior;
+    // eta = outside ior (vacuum, 1) / ior from outside, ior / outside ior inside
+    float e = p.fromOutside ? 1.f * (1.f / ior) : ior * (1.f / 1.f);
     e = clampf(e, 1.f / 3.f, 3.f);
     const float plastic = dielectric;  // transmission 0
     if (plastic > EPS) {
       diffuse = baseColor * diffuseW;
-      // MicrofacetDielectricLayer_Constructor.  The reference reads self->eta
-      // before assigning it when computing Ravg (MicrofacetDielectricLayer.ih
-      // constructor); the assigned value (eta folded to <= 1) is used here.
+      hasLayer = specular > EPS;
+      // the layer keeps eta folded to <= 1.  (MicrofacetDielectricLayer_Constructor
+      // reads self->eta before assigning it when computing Ravg; the assigned value
+      // is used here.)
       eta = e <= 1.f ? e : 1.f / e;
       lWeight = specular;
-      lEavg = T.evalAvg(roughness);
-      const float Favg = fresnelDielectricAvg(e);
-      lFmsScale = Favg * (1.f - lEavg) / (1.f - Favg * lEavg);
-      lRavg = (T.reflEvalAvg(eta, roughness) + lFmsScale * (1.f - lEavg)) * lWeight;
-      lAlbedo = diffuse * ((1.f - lWeight) + 1.f * (1.f - Favg));
+      lAlbedo = diffuse;  // PassthroughLayer: the substrate's albedo
+      if (hasLayer && smoothBase) {
+        lFavg = fresnelDielectricAvg(e) * lWeight;
+        lAlbedo = diffuse * ((1.f - lWeight) + 1.f * (1.f - lFavg));
+      } else if (hasLayer) {
+        lEavg = T.evalAvg(roughness);
+        const float Favg = fresnelDielectricAvg(e);
+        lFmsScale = Favg * (1.f - lEavg) / (1.f - Favg * lEavg);
+        lRavg = (T.reflEvalAvg(eta, roughness) + lFmsScale * (1.f - lEavg)) * lWeight;
+        lAlbedo = diffuse * ((1.f - lWeight) + 1.f * (1.f - Favg));
+      }
       wP = plastic;
       iP = plastic * std::fmax(diffuseW, specular);
       impSum += iP;
       albedo = albedo + lAlbedo * wP;
+      smooth = true;
     }
   }
-  const float conductor = metallic * specular;
+  const float conductor = metallic * (p.specularMetallic ? specular : 1.f);
   if (conductor > EPS) {
-    // FresnelConductorArtistic_create (edgeColor 1)
-    const V3 r = vmin(baseColor, v3(0.99f)), g = v3(1.f);
+    // FresnelConductorArtistic_create (bsdfs/Fresnel.ih): n between n_min and
+    // n_max by the edge colour, k from the reflectivity
+    const V3 r = vmin(baseColor, v3(0.99f));
+    const V3 g = {clamp01(p.edgeColor.x), clamp01(p.edgeColor.y), clamp01(p.edgeColor.z)};
     const float rr[3] = {r.x, r.y, r.z}, gg[3] = {g.x, g.y, g.z};
     float ne[3], nk[3], favg[3];
     for (int c = 0; c < 3; c++) {
@@ -125,22 +144,28 @@ void Principled::init(const PrincipledParams &p, const L3 &f) {
     }
     ceta = {ne[0], ne[1], ne[2]};
     ck = {nk[0], nk[1], nk[2]};
-    cEavg = T.evalAvg(roughness);
     const V3 Favg = {favg[0], favg[1], favg[2]};
-    // Stephen Hill's multiple-scattering tweak (MicrofacetConductor_Constructor)
-    cFmsScale = {sqr(Favg.x) * cEavg / (1.f - Favg.x * (1.f - cEavg)),
-                 sqr(Favg.y) * cEavg / (1.f - Favg.y * (1.f - cEavg)),
-                 sqr(Favg.z) * cEavg / (1.f - Favg.z * (1.f - cEavg))};
     wC = conductor;
     iC = conductor;
     impSum += iC;
-    albedo = albedo + (Favg * cEavg) * wC;
+    if (smoothBase) {
+      albedo = albedo + Favg * wC;  // Conductor: albedo = the Fresnel average
+    } else {
+      cEavg = T.evalAvg(roughness);
+      // Stephen Hill's multiple-scattering tweak (MicrofacetConductor_Constructor)
+      cFmsScale = {sqr(Favg.x) * cEavg / (1.f - Favg.x * (1.f - cEavg)),
+                   sqr(Favg.y) * cEavg / (1.f - Favg.y * (1.f - cEavg)),
+                   sqr(Favg.z) * cEavg / (1.f - Favg.z * (1.f - cEavg))};
+      albedo = albedo + (Favg * cEavg) * wC;
+      smooth = true;
+    }
   }
 }
 
 static V3 toLocal(const L3 &f, V3 v) { return {dot(v, f.vx), dot(v, f.vy), dot(v, f.vz)}; }
 
 BSDFEval Principled::evalConductor(V3 wo, V3 wi) const {
+  if (smoothBase) return {v3(0.f), 0.f};  // Dirac
   const float cosO = dot(wo, N), cosI = dot(wi, N);
   if (cosO <= 0.f || cosI <= 0.f) return {v3(0.f), 0.f};
   const V3 wh = normalize(wi + wo);
@@ -159,6 +184,15 @@ BSDFEval Principled::evalConductor(V3 wo, V3 wi) const {
 
 BSDFSample Principled::sampleConductor(V3 wo, V2 s) const {
   BSDFSample res = {v3(0.f), v3(0.f), 0.f, 0};
+  if (smoothBase) {  // Conductor_sample: mirror direction, weight = Fresnel
+    const float c = dot(wo, N);
+    res.wi = reflectV(wo, N, c);
+    res.pdf = INFINITY;
+    res.type = SCATTER_SPEC_R;
+    res.weight = {fresnelConductor1(c, ceta.x, ck.x), fresnelConductor1(c, ceta.y, ck.y),
+                  fresnelConductor1(c, ceta.z, ck.z)};
+    return res;
+  }
   const float cosO = dot(wo, N);
   if (cosO <= 0.f) return res;
   const V3 wo0 = toLocal(frame, wo);
@@ -181,6 +215,7 @@ BSDFSample Principled::sampleConductor(V3 wo, V2 s) const {
   return res;
 }
 
+// Oren-Nayar (bsdfs/OrenNayar.ih:13-63); Lambert at roughness 0
 BSDFEval Principled::evalOrenNayar(V3 wo, V3 wi) const {
   const float cosO = std::fmax(dot(wo, N), 0.f), cosI = std::fmax(dot(wi, N), 0.f);
   const float s = dot(wo, wi) - cosO * cosI;
@@ -189,12 +224,36 @@ BSDFEval Principled::evalOrenNayar(V3 wo, V3 wi) const {
   return {v, cosI / PI};
 }
 
-// MICROFACETDIELECTRICLAYER_EVAL with a diffuse substrate
+BSDFSample Principled::sampleDiffuse(V3 wo, V2 s) const {
+  BSDFSample res;
+  // cosine hemisphere in the shading frame
+  const float phi = 2.f * PI * s.x;
+  const float cosT = std::sqrt(s.y), sinT = std::sqrt(1.f - s.y);
+  const V3 local = {std::cos(phi) * sinT, std::sin(phi) * sinT, cosT};
+  res.wi = xfmVector(frame, local);
+  const BSDFEval e = evalOrenNayar(wo, res.wi);
+  res.pdf = e.pdf;
+  res.type = SCATTER_DIFFUSE_R;
+  res.weight = e.value * (1.f / e.pdf);
+  return res;
+}
+
+// MICROFACETDIELECTRICLAYER_EVAL / DIELECTRICLAYER_EVAL with a diffuse substrate
 BSDFEval Principled::evalPlastic(V3 wo, V3 wi) const {
+  if (!hasLayer) return evalOrenNayar(wo, wi);  // PassthroughLayer
   const float cosO = dot(wo, N);
   if (cosO <= 0.f) return {v3(0.f), 0.f};
   const float cosI = dot(wi, N);
   BSDFEval sub = evalOrenNayar(wo, wi);
+  if (smoothBase) {
+    float cosO1, cosI1;
+    const float F = fresnelDielectricEx(cosO, cosO1, eta);
+    const float Fo = F * lWeight, Fi = fresnelDielectricEx(std::fabs(cosI), cosI1, eta) * lWeight;
+    sub.value = sub.value * ((1.f - Fo) * (1.f - Fi) * (1.f / (1.f - lFavg)));
+    const float coatPick = Fo / ((1.f - F) * reduce_max(lAlbedo) + Fo);
+    sub.pdf *= 1.f - coatPick;
+    return sub;
+  }
   // substrate MultiBSDF (one child, weight 1, importance 1)
   // coating absorption: transmittance 1 -> factor 1 (lerp of equal values)
   const AlbedoTables &T = albedoTables();
@@ -225,14 +284,37 @@ BSDFEval Principled::evalPlastic(V3 wo, V3 wi) const {
   return sub;
 }
 
-// MICROFACETDIELECTRICLAYER_SAMPLE with a diffuse substrate
+// MICROFACETDIELECTRICLAYER_SAMPLE / DIELECTRICLAYER_SAMPLE with a diffuse substrate
 BSDFSample Principled::samplePlastic(V3 wo, V2 s, float ss) const {
   BSDFSample res = {v3(0.f), v3(0.f), 0.f, 0};
+  if (!hasLayer) return sampleDiffuse(wo, s);  // PassthroughLayer
   const float cosO = dot(wo, N);
   if (cosO <= 0.f) return res;
+  if (smoothBase) {
+    float cosO1;
+    const float F = fresnelDielectricEx(cosO, cosO1, eta);
+    const float Fo = F * lWeight;
+    const float coatPick = Fo / ((1.f - F) * reduce_max(lAlbedo) + Fo);
+    if (ss < coatPick) {
+      res.type = SCATTER_SPEC_R;
+      res.wi = reflectV(wo, N, cosO);
+      res.pdf = INFINITY;
+      res.weight = v3(Fo / coatPick);
+      return res;
+    }
+    res = sampleDiffuse(wo, s);
+    if (reduce_max(res.weight) <= 0.f) return res;
+    float cosI1;
+    const float Fi = fresnelDielectricEx(std::fabs(dot(res.wi, N)), cosI1, eta) * lWeight;
+    const float Tr = (1.f - Fo) * (1.f - Fi) * (1.f / (1.f - lFavg));
+    res.weight = res.weight * (Tr * (1.f / (1.f - coatPick)));
+    res.pdf *= 1.f - coatPick;
+    return res;
+  }
   const V3 wo0 = toLocal(frame, wo);
   const AlbedoTables &T = albedoTables();
   const float Eo = T.eval(cosO, roughness);
+  // (the reference's sample weighs only the multiple-scattering term here)
   const float Ro = T.reflEval(cosO, eta, roughness) + lFmsScale * (1.f - Eo) * lWeight;
   const float coatPick = lWeight * Ro / ((1.f - Ro) * reduce_max(lAlbedo) + lWeight * Ro);
   const float subPick = 1.f - coatPick;
@@ -245,15 +327,7 @@ BSDFSample Principled::samplePlastic(V3 wo, V2 s, float ss) const {
     res.wi = reflectV(wo, wh, dot(wo, wh));
     sub = evalOrenNayar(wo, res.wi);
   } else {
-    // Oren-Nayar sample: cosine hemisphere in the shading frame
-    const float phi = 2.f * PI * s.x;
-    const float cosT = std::sqrt(s.y), sinT = std::sqrt(1.f - s.y);
-    const V3 local = {std::cos(phi) * sinT, std::sin(phi) * sinT, cosT};
-    res.wi = xfmVector(frame, local);
-    const BSDFEval e = evalOrenNayar(wo, res.wi);
-    res.pdf = e.pdf;
-    res.type = SCATTER_DIFFUSE_R;
-    res.weight = e.value * (1.f / e.pdf);
+    res = sampleDiffuse(wo, s);
     if (reduce_max(res.weight) <= 0.f) return res;
     sub.pdf = res.pdf;
     sub.value = res.weight * res.pdf;
@@ -301,7 +375,8 @@ BSDFEval Principled::eval(V3 wo, V3 wi) const {
   return r;
 }
 
-// MultiBSDF sample over {conductor (0), plastic (2)}
+// MultiBSDF sample over {conductor (0), plastic (2)} (MultiBSDF.ih:81-127):
+// a Dirac lobe returns alone, scaled by 1 / its selection probability
 BSDFSample Principled::sample(V3 wo, V2 s, float ss) const {
   BSDFSample res = {v3(0.f), v3(0.f), 0.f, 0};
   if (impSum == 0.f) return res;
@@ -320,6 +395,10 @@ BSDFSample Principled::sample(V3 wo, V2 s, float ss) const {
   }
   if (choice < 0 || (res.weight.x == 0.f && res.weight.y == 0.f && res.weight.z == 0.f) || res.pdf == 0.f)
     return {v3(0.f), v3(0.f), 0.f, 0};
+  if (res.type & (SCATTER_SPEC_R | SCATTER_SPEC_T)) {
+    res.weight = res.weight * (impSum * (1.f / (choice == 0 ? iC : iP)));
+    return res;
+  }
   V3 value = res.weight * res.pdf;
   float pdf = res.pdf * (choice == 0 ? iC : iP);
   if (choice != 0 && iC > 0.f) {

@@ -111,6 +111,16 @@ inline float fresnelDielectric(float cosI, float eta) {
   if (c < 0.f) return 1.f;
   return fresnelDielectric(cosI, std::sqrt(c), eta);
 }
+// fresnelDielectricEx (bsdfs/Fresnel.ih:38-47)
+inline float fresnelDielectricEx(float cosI, float &cosT, float eta) {
+  const float k = sqrCosT(cosI, eta);
+  if (k < 0.f) {
+    cosT = 0.f;
+    return 1.f;
+  }
+  cosT = std::sqrt(k);
+  return fresnelDielectric(cosI, cosT, eta);
+}
 inline float fresnelDielectricAvg(float eta) {
   if (eta < 1.f) eta = 1.f / eta;
   return (eta - 1.f) / (4.08567f + 1.00071f * eta);
@@ -144,9 +154,15 @@ const AlbedoTables &albedoTables();
 // scattering types (render/pathtracer/Scattering.ih:8-47)
 enum : int { SCATTER_SPEC_R = 1, SCATTER_GLOSSY_R = 2, SCATTER_DIFFUSE_R = 4 };
 
+// Principled.cpp:37-79 parameters of the base stack (transmission, thin,
+// coat and sheen at their defaults)
 struct PrincipledParams {
   V3 baseColor;
   float roughness, metallic;
+  float specular = 1.f, ior = 1.f, diffuse = 1.f;
+  V3 edgeColor = {1.f, 1.f, 1.f};
+  bool specularMetallic = true;
+  bool fromOutside = true;  // the path travels in the outside medium (vacuum)
 };
 
 struct BSDFEval {
@@ -169,9 +185,11 @@ struct Principled {
   // conductor
   V3 ceta, ck, cFmsScale;
   float cEavg;
-  // plastic = dielectric layer (eta, weight = specular) over Oren-Nayar
+  // plastic = dielectric layer (eta, weight = specular) over Oren-Nayar;
+  // roughness 0: smooth DielectricLayer over Lambert and a smooth Conductor
   V3 diffuse;  // baseColor * diffuse
-  float eta, lEavg, lFmsScale, lRavg, lWeight;
+  float eta, lEavg, lFmsScale, lRavg, lWeight, lFavg;
+  bool smoothBase = false, hasLayer = false, smooth = false;
   V3 lAlbedo;  // layer albedo (substrate albedo scaled)
   V3 albedo;   // BSDF albedo (for the shading AOV / coat pick)
   void init(const PrincipledParams &p, const L3 &shadingFrame);
@@ -181,6 +199,7 @@ struct Principled {
   BSDFEval evalConductor(V3 wo, V3 wi) const;
   BSDFSample sampleConductor(V3 wo, V2 s) const;
   BSDFEval evalOrenNayar(V3 wo, V3 wi) const;
+  BSDFSample sampleDiffuse(V3 wo, V2 s) const;
   BSDFEval evalPlastic(V3 wo, V3 wi) const;
   BSDFSample samplePlastic(V3 wo, V2 s, float ss) const;
 };
@@ -280,13 +299,18 @@ struct MaterialParams {
   Medium inside = {1.f, v3(0.f)}, outside = {1.f, v3(0.f)};  // glass
   float thinEta = 1.f;  // thin glass: 1 / eta
   V3 thinAtt = v3(0.f);
+  // principled base-stack parameters
+  float specular = 1.f, ior = 1.f, diffuse = 1.f;
+  V3 edgeColor = v3(1.f);
+  bool specularMetallic = true;
   // principled map_baseColor / obj map_kd (null: none); mapAlpha: it has alpha
   const Texture *map = nullptr;
   bool mapAlpha = false;
 };
 // p: baseColor[3], roughness, metallic, opacity, ks[3], ns, tf[3], eta[3],
-// k[3], attenuationColor[3], attenuationDistance, thickness (24 floats, the
-// b200_material fields after its type)
+// k[3], attenuationColor[3], attenuationDistance, thickness, specular, ior,
+// diffuse, edgeColor[3], specularMetallic (31 floats, the b200_material
+// fields after its type without the colour map)
 MaterialParams commitMaterial(int type, const float *p);
 bool transparentMaterial(const MaterialParams &m);
 

@@ -297,6 +297,10 @@ void renderAO(const Scene &s, const Camera &cam, const PixelFilter &pf, const AO
         const V2 center = {(float(x) + 0.5f) * rcpSize.x, (float(y) + 0.5f) * rcpSize.y};
         const V2 screen = {center.x + pfs.x * rcpSize.x, center.y + pfs.y * rcpSize.y};
         Ray ray = cameraRay(cam, screen);
+        // Renderer_getMaxDepth at the pixel centre (RendererRenderTaskFn.inl:41-42)
+        if (p.maxDepth) ray.tfar = std::fmin(ray.tfar, std::fmax(0.f, p.maxDepth->get(center, 0.f).x));
+        const V2 cone = cameraCone(cam, screen, rcpSize.y);
+        float coneWidth = cone.x;
         ScreenSample smp;
         V4 out = {0, 0, 0, 0};
         bool first = true;
@@ -319,16 +323,33 @@ void renderAO(const Scene &s, const Camera &cam, const PixelFilter &pf, const AO
           }
           V4 blended;
           if (h) {
-            const DG dg = postIntersect(s, ray, hit);
-            const float eye = std::fabs(dot(dg.Ns, ray.dir));
+            const DG dg = postIntersect(s, ray, hit, true);
+            coneWidth += cone.y * hit.t;
+            // getSurfaceColor (render/ao/surfaces.ispc:17-42)
+            V3 color = v3(1.f);
+            float opacity = 1.f;
+            const int mi = s.entries[hit.entry].material;
+            if (mi >= 0 && size_t(mi) < p.mats.size() && p.mats[size_t(mi)].isObj) {
+              const AOMaterial &m = p.mats[size_t(mi)];
+              color = m.kd;
+              if (m.kdMap) {
+                const V4 t = m.kdMap->get(dg.st, pixelFootprint(coneWidth, ray.dir, dg, p.mipBiasFactor));
+                color = color * v3(t.x, t.y, t.z);
+                opacity *= t.w;
+              }
+              opacity *= m.d;
+            }
+            color = color * v3(dg.color.x, dg.color.y, dg.color.z);
+            opacity *= dg.color.w;
+            const float eye = std::fabs(dot(dg.Ns, ray.dir)) * opacity;
             float intensity = eye;
             if (p.aoSamples > 0 && p.aoIntensity > 0.01f) {
               const float ao = computeAO(s, dg, p.aoSamples, p.aoRadius, x, y, sid);
               intensity *= (1.f - p.aoIntensity) + ao * p.aoIntensity;
             }
-            blended = {intensity, intensity, intensity, 1.f};
+            blended = {color.x * intensity, color.y * intensity, color.z * intensity, opacity};
             if (first) {
-              smp.albedo = v3(1.f);  // surfaces without material: white
+              smp.albedo = color;  // AORenderer_computeShading: the surface colour
               smp.normal = dg.Ns;
               smp.z = hit.t;
               smp.primID = dg.primID;
@@ -338,10 +359,10 @@ void renderAO(const Scene &s, const Camera &cam, const PixelFilter &pf, const AO
             ray.tnear = hit.t + dg.epsilon;
             ray.tfar = tfar0;
           } else {
-            blended = p.bgColor;
+            blended = p.backplate ? p.backplate->getScreen(center) : p.bgColor;
             if (first) {
               smp.z = ray.tfar;
-              smp.albedo = {p.bgColor.x, p.bgColor.y, p.bgColor.z};
+              smp.albedo = {blended.x, blended.y, blended.z};
               smp.normal = ray.dir;
             }
           }

@@ -19,6 +19,7 @@
 
 #include "samplers.h"
 #include "scene.h"
+#include "texture.h"
 
 namespace orc {
 
@@ -181,11 +182,23 @@ constexpr float ulpEpsilon = 0x1.0fp-21f;
 // rays traced by the renderers since the last reset (CPU-baseline Mrays/s)
 extern std::atomic<uint64_t> g_rayCount;
 
+// an obj material as getSurfaceColor reads it (render/ao/surfaces.ispc:17-42)
+struct AOMaterial {
+  int isObj;
+  V3 kd;
+  float d;
+  const Texture *kdMap;
+};
 struct AOParams {
   int spp, aoSamples;
   float aoRadius, aoIntensity;
   V4 bgColor;
+  const Texture *backplate = nullptr, *maxDepth = nullptr;  // map_backplate, map_maxDepth
+  float mipBiasFactor = 1.f;
+  std::vector<AOMaterial> mats;  // by the instances' material slot; empty: white, opaque
 };
+// (with materials, attributes, maps, backplate and maxDepth as the AO renderer
+// reads them: AORenderer_renderSample, getSurfaceColor, RendererRenderTaskFn.inl)
 void renderAO(const Scene &s, const Camera &cam, const PixelFilter &pf, const AOParams &p, FrameBuffer &fb,
               int nthreads);
 

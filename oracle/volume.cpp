@@ -282,7 +282,9 @@ V4 integrateVolume(const VolumeModel &m, const Ray &wray, float jitter, float sa
 //   lightAlpha                 render/scivis/lightAlpha.ispc:19-122
 //   integrateVolumeIntervals   render/ao/volumes.ispc:32-240 (shadow/AO rays)
 //   light list and aoColorPi   render/scivis/SciVisData.cpp:15-105
-// Surfaces carry no per-vertex colour here, so dg.color = (1, 1, 1, 1);
+//   ray cones / map_maxDepth    render/RendererRenderTaskFn.inl:40-72
+//   background / backplate      render/Renderer.ispc:19-40
+// dg.color is the mesh's interpolated vertex colour (1 without one);
 // gradient-shaded volume samples pass their transfer-function colour.
 
 struct SvMaterial {
@@ -290,6 +292,7 @@ struct SvMaterial {
   V3 kd, ks;
   float ns, d;
   V3 tf;
+  const Texture *kdMap = nullptr;  // obj map_kd
 };
 
 struct SvBSDF {
@@ -299,7 +302,8 @@ struct SvBSDF {
   float opacity;
 };
 
-SvBSDF svEvalMaterial(const SvMaterial *m, V4 color = {1.f, 1.f, 1.f, 1.f}) {
+// dg (with footprint fp) addresses the obj map_kd; null: no lookup
+SvBSDF svEvalMaterial(const SvMaterial *m, V4 color = {1.f, 1.f, 1.f, 1.f}, const DG *dg = nullptr, float fp = 0.f) {
   SvBSDF r;
   r.diffuse = v3(color.x, color.y, color.z);
   r.specular = v3(0.f);
@@ -307,8 +311,13 @@ SvBSDF svEvalMaterial(const SvMaterial *m, V4 color = {1.f, 1.f, 1.f, 1.f}) {
   r.transmission = v3(1.f - color.w);
   r.opacity = color.w;
   if (m && m->isObj) {
-    const float d = m->d * color.w;
+    float d = m->d * color.w;
     r.diffuse = r.diffuse * m->kd;
+    if (m->kdMap && dg) {
+      const V4 t = m->kdMap->get(dg->st, fp);
+      r.diffuse = r.diffuse * v3(t.x, t.y, t.z);
+      d *= t.w;
+    }
     r.diffuse = r.diffuse * d;
     r.specular = d * m->ks;
     r.shininess = m->ns;
@@ -357,6 +366,8 @@ struct SvParams {
   V4 bg;
   int shadows, visibleLights, aoSamples;
   float aoRadius, minContribution;
+  const Texture *backplate = nullptr, *maxDepth = nullptr;
+  float mipBiasFactor = 1.f;
 };
 
 struct SvWorld {
@@ -443,7 +454,10 @@ float svVolumeAlpha(const VolumeModel &m, const Ray &ray, float jitter, float sa
 
 inline float svLuminance(V3 c) { return 0.212671f * c.x + 0.715160f * c.y + 0.072169f * c.z; }
 
-V3 svLightAlpha(const SvWorld &w, const SvParams &p, Ray ray, RandomSampler &rs, V3 weight, float quality) {
+// cone: the shadow cone (width at the origin, dwdt); its width restarts
+// from the origin's after every surface (lightAlpha.ispc:30,105)
+V3 svLightAlpha(const SvWorld &w, const SvParams &p, Ray ray, RandomSampler &rs, V3 weight, float quality,
+                V2 cone = {0.f, 0.f}) {
   V3 alpha = v3(1.f);
   const float orgTMax = ray.tfar;
   for (int g = 0; g < 1024; g++) {
@@ -459,8 +473,10 @@ V3 svLightAlpha(const SvWorld &w, const SvParams &p, Ray ray, RandomSampler &rs,
       }
     }
     if (!h) break;
-    const DG dg = postIntersect(*w.scene, ray, hit);
-    alpha = alpha * svEvalMaterial(w.material(hit)).transmission;
+    const DG dg = postIntersect(*w.scene, ray, hit, true);
+    const SvMaterial *m = w.material(hit);
+    const float fp = m && m->kdMap ? pixelFootprint(cone.x + cone.y * hit.t, ray.dir, dg, p.mipBiasFactor) : 0.f;
+    alpha = alpha * svEvalMaterial(m, dg.color, &dg, fp).transmission;
     ray.tnear = hit.t + dg.epsilon;
     ray.tfar = orgTMax;
     if (svLuminance(alpha * weight) < p.minContribution) {
@@ -472,7 +488,7 @@ V3 svLightAlpha(const SvWorld &w, const SvParams &p, Ray ray, RandomSampler &rs,
 }
 
 V3 svComputeAO(const SvWorld &w, const SvParams &p, const DG &dg, int px, int py, uint32_t sampleZ,
-                RandomSampler &rs) {
+                RandomSampler &rs, float coneWidth) {
   const uint32_t accumID = sampleZ * uint32_t(p.aoSamples);
   uint32_t t0 = uint32_t(px), t1 = uint32_t(py);
   tea8(t0, t1);
@@ -490,7 +506,7 @@ V3 svComputeAO(const SvWorld &w, const SvParams &p, const DG &dg, int px, int py
       continue;
     }
     const Ray aoRay = {dg.P, dg.epsilon, dir, p.aoRadius};
-    hits = hits + (v3(1.f) - svLightAlpha(w, p, aoRay, rs, v3(1.f), 0.1f));
+    hits = hits + (v3(1.f) - svLightAlpha(w, p, aoRay, rs, v3(1.f), 0.1f, {coneWidth, 0.f}));
   }
   return v3(1.f) - hits * (1.f / float(p.aoSamples));
 }
@@ -501,9 +517,11 @@ struct SvShading {
   V3 albedo;
 };
 
+// coneWidth: the ray cone's width at this hit; fp: the hit's footprint
 SvShading svComputeShading(const SvWorld &w, const SvParams &p, const DG &dg, const SvMaterial *mat, V4 dgColor,
-                           V3 inDir, int px, int py, uint32_t sampleZ, RandomSampler &rs) {
-  const SvBSDF bsdf = svEvalMaterial(mat, dgColor);
+                           V3 inDir, int px, int py, uint32_t sampleZ, RandomSampler &rs, float coneWidth = 0.f,
+                           float fp = 0.f) {
+  const SvBSDF bsdf = svEvalMaterial(mat, dgColor, &dg, fp);
   V3 color = v3(0.f);
   for (size_t i = w.numVisibleOnly; i < w.lights.size(); i++) {
     const LightSample ls = w.lights[i].sample(dg, {0.f, 0.f});  // area lights at their centre
@@ -519,7 +537,8 @@ SvShading svComputeShading(const SvWorld &w, const SvParams &p, const DG &dg, co
         if (svLuminance(contrib) > p.minContribution) {
           V3 P = dg.P;
           if (dot(dg.Ng, ls.dir) < 0.f) P = P - (2.f * dg.epsilon) * dg.Ng;
-          const V3 la = svLightAlpha(w, p, {P, 0.f, ls.dir, ls.dist}, rs, contrib, 0.25f);
+          const V3 la = svLightAlpha(w, p, {P, 0.f, ls.dir, ls.dist}, rs, contrib, 0.25f,
+                                     {coneWidth, -coneWidth * (1.f / ls.dist)});
           color = color + la * contrib;
         }
       } else {
@@ -529,7 +548,7 @@ SvShading svComputeShading(const SvWorld &w, const SvParams &p, const DG &dg, co
   }
   V3 ao = v3(1.f);
   if (p.aoSamples > 0 && svLuminance(w.aoColor * float(M_PI)) > p.minContribution)
-    ao = svComputeAO(w, p, dg, px, py, sampleZ, rs);
+    ao = svComputeAO(w, p, dg, px, py, sampleZ, rs, coneWidth);
   color = color + bsdf.diffuse * ao * (w.aoColor * float(M_PI));
   return {color, bsdf.transmission, bsdf.opacity, bsdf.albedo};
 }
@@ -596,11 +615,15 @@ V4 integrateVolumeShaded(const SvWorld &w, const SvParams &p, const Ray &wray, f
   return {color.x, color.y, color.z, T};
 }
 
+// cone: the camera ray's (width, dwdt); center: the pixel centre (backplate
+// and maxDepth lookups)
 ScreenSample svRenderSample(const SvWorld &w, const SvParams &p, Ray ray, int x, int y, int W, uint32_t sid,
-                            uint64_t &samples) {
+                            uint64_t &samples, V2 cone = {0.f, 0.f}, V2 center = {0.f, 0.f}) {
   RandomSampler rs;
   rs.init(uint32_t(x + W * y), sid);
   ScreenSample smp;
+  if (p.maxDepth) ray.tfar = std::fmin(ray.tfar, std::fmax(0.f, p.maxDepth->get(center, 0.f).x));
+  float coneWidth = cone.x;
   bool firstHit = true, allTrans = true;
   const float originalTFar = ray.tfar;
   V3 outColor = v3(0.f), outT = v3(1.f);
@@ -631,8 +654,11 @@ ScreenSample svRenderSample(const SvWorld &w, const SvParams &p, Ray ray, int x,
     }
     if (firstHit || allTrans) smp.z = rayT;
     if (h) {
-      const DG dg = postIntersect(*w.scene, ray, hit);
-      const SvShading sh = svComputeShading(w, p, dg, w.material(hit), {1.f, 1.f, 1.f, 1.f}, ray.dir, x, y, sid, rs);
+      const DG dg = postIntersect(*w.scene, ray, hit, true);
+      coneWidth += cone.y * hit.t;  // World.ih postIntersect, t from the ray's origin
+      const SvMaterial *m = w.material(hit);
+      const float fp = m && m->kdMap ? pixelFootprint(coneWidth, ray.dir, dg, p.mipBiasFactor) : 0.f;
+      const SvShading sh = svComputeShading(w, p, dg, m, dg.color, ray.dir, x, y, sid, rs, coneWidth, fp);
       if (firstHit || allTrans) {
         smp.normal = dg.Ns;
         smp.albedo = sh.albedo;
@@ -651,8 +677,9 @@ ScreenSample svRenderSample(const SvWorld &w, const SvParams &p, Ray ray, int x,
       ray.tnear = hit.t + dg.epsilon;
       ray.tfar = originalTFar;
     } else {
-      outColor = outColor + outT * v3(p.bg.x, p.bg.y, p.bg.z);
-      outT = outT * (1.f - p.bg.w);
+      const V4 bg = p.backplate ? p.backplate->getScreen(center) : p.bg;
+      outColor = outColor + outT * v3(bg.x, bg.y, bg.z);
+      outT = outT * (1.f - bg.w);
       break;
     }
   }
@@ -800,6 +827,7 @@ struct OrScivisLight {
 struct OrScivisMaterial {
   int isObj;
   float kd[3], ks[3], ns, d, tf[3];
+  const void *kdMap;  // a Texture or null
 };
 struct OrScivisParams {
   int spp;
@@ -808,6 +836,8 @@ struct OrScivisParams {
   int shadows, visibleLights, aoSamples;
   float aoRadius, minContribution;
   int pixelFilter;
+  const void *backplate, *maxDepth;  // Textures or null
+  float mipMapBias;
 };
 
 // SciVis frames of a world with surfaces (and optionally the volume mp);
@@ -845,10 +875,12 @@ void or_render_scivis(void *scp, void *mp, const OrCameraV *c, const OrScivisPar
   for (int i = 0; i < nmats; i++) {
     const OrScivisMaterial &m = mats[i];
     w.mats.push_back({m.isObj, {m.kd[0], m.kd[1], m.kd[2]}, {m.ks[0], m.ks[1], m.ks[2]}, m.ns, m.d,
-                      {m.tf[0], m.tf[1], m.tf[2]}});
+                      {m.tf[0], m.tf[1], m.tf[2]}, static_cast<const Texture *>(m.kdMap)});
   }
   SvParams p = {pp->spp, pp->samplingRate, {pp->bg[0], pp->bg[1], pp->bg[2], pp->bg[3]}, pp->shadows,
-                pp->visibleLights, pp->aoSamples, pp->aoRadius, pp->minContribution};
+                pp->visibleLights, pp->aoSamples, pp->aoRadius, pp->minContribution,
+                static_cast<const Texture *>(pp->backplate), static_cast<const Texture *>(pp->maxDepth),
+                std::pow(2.f, pp->mipMapBias)};
   const Camera cam = makeCamera({c->pos[0], c->pos[1], c->pos[2]}, {c->dir[0], c->dir[1], c->dir[2]},
                                 {c->up[0], c->up[1], c->up[2]}, c->fovy, c->aspect, c->nearClip, c->type, c->height);
   PixelFilter pf;
@@ -872,8 +904,10 @@ void or_render_scivis(void *scp, void *mp, const OrCameraV *c, const OrScivisPar
           const V2 ps = {Halton_sample2(sid), CranleyPattersonRotation(Halton_sample3(sid), 1.f / 6.f)};
           const V2 pfs = pf.sample(ps);
           const V2 center = {(float(x) + 0.5f) * rcpSize.x, (float(y) + 0.5f) * rcpSize.y};
-          const Ray ray = cameraRay(cam, {center.x + pfs.x * rcpSize.x, center.y + pfs.y * rcpSize.y});
-          accumulateScreen(acc, svRenderSample(w, p, ray, x, y, W, sid, samples));
+          const V2 screen = {center.x + pfs.x * rcpSize.x, center.y + pfs.y * rcpSize.y};
+          const Ray ray = cameraRay(cam, screen);
+          accumulateScreen(acc, svRenderSample(w, p, ray, x, y, W, sid, samples, cameraCone(cam, screen, rcpSize.y),
+                                               center));
         }
         const float rspp = 1.f / float(p.spp);
         acc.rgb = acc.rgb * rspp;

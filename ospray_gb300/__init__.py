@@ -47,7 +47,9 @@ class AOParams(ctypes.Structure):
     _fields_ = [("pixelSamples", ctypes.c_int), ("aoSamples", ctypes.c_int),
                 ("aoDistance", ctypes.c_float), ("aoIntensity", ctypes.c_float),
                 ("backgroundColor", ctypes.c_float * 4), ("pixelFilter", ctypes.c_int),
-                ("collectStats", ctypes.c_int), ("volumeSamplingRate", ctypes.c_float)]
+                ("collectStats", ctypes.c_int), ("volumeSamplingRate", ctypes.c_float),
+                ("backplate", ctypes.c_void_p), ("maxDepth", ctypes.c_void_p), ("mipMapBias", ctypes.c_float),
+                ("materials", ctypes.c_void_p), ("nmaterials", ctypes.c_int)]
 
 
 LIGHT_QUAD, LIGHT_AMBIENT, LIGHT_DISTANT, LIGHT_SPHERE, LIGHT_SPOT = 0, 1, 2, 3, 4
@@ -79,7 +81,8 @@ class Material(ctypes.Structure):
                 ("ns", ctypes.c_float), ("tf", ctypes.c_float * 3), ("eta", ctypes.c_float * 3),
                 ("k", ctypes.c_float * 3), ("attenuationColor", ctypes.c_float * 3),
                 ("attenuationDistance", ctypes.c_float), ("thickness", ctypes.c_float),
-                ("baseColorMap", ctypes.c_void_p)]
+                ("baseColorMap", ctypes.c_void_p), ("specular", ctypes.c_float), ("ior", ctypes.c_float),
+                ("diffuse", ctypes.c_float), ("edgeColor", ctypes.c_float * 3), ("specularMetallic", ctypes.c_int)]
 
 
 MATERIAL_PRINCIPLED, MATERIAL_OBJ, MATERIAL_METAL, MATERIAL_GLASS, MATERIAL_THINGLASS = 0, 1, 2, 3, 4
@@ -87,10 +90,12 @@ _MATERIAL_TYPES = {"principled": MATERIAL_PRINCIPLED, "obj": MATERIAL_OBJ, "meta
                    "glass": MATERIAL_GLASS, "thinGlass": MATERIAL_THINGLASS}
 
 
-def principled(base_color=(0.8, 0.8, 0.8), roughness=0.0, metallic=0.0, opacity=1.0, base_color_map=None):
+def principled(base_color=(0.8, 0.8, 0.8), roughness=0.0, metallic=0.0, opacity=1.0, base_color_map=None,
+               specular=1.0, ior=1.0, diffuse=1.0, edge_color=(1.0, 1.0, 1.0), specular_metallic=True):
     """base_color_map: a Texture (map_baseColor)."""
     return dict(type="principled", baseColor=base_color, roughness=roughness, metallic=metallic, opacity=opacity,
-                baseColorMap=base_color_map)
+                baseColorMap=base_color_map, specular=specular, ior=ior, diffuse=diffuse, edgeColor=edge_color,
+                specularMetallic=int(bool(specular_metallic)))
 
 
 def obj_material(kd=(0.8, 0.8, 0.8), ks=(0.0, 0.0, 0.0), ns=10.0, d=1.0, tf=(0.0, 0.0, 0.0), map_kd=None):
@@ -127,6 +132,8 @@ def material_struct(m):
                 continue
             if isinstance(val, (tuple, list, np.ndarray)):
                 getattr(out, key)[:] = [float(x) for x in val]
+            elif key == "specularMetallic":
+                out.specularMetallic = int(val)
             else:
                 setattr(out, key, float(val))
         return out
@@ -142,7 +149,8 @@ class PTParams(ctypes.Structure):
                 ("lightSamples", ctypes.c_int), ("limitIndirectLightSamples", ctypes.c_int),
                 ("minContribution", ctypes.c_float), ("maxContribution", ctypes.c_float),
                 ("backgroundColor", ctypes.c_float * 4), ("pixelFilter", ctypes.c_int),
-                ("collectStats", ctypes.c_int), ("backplate", ctypes.c_void_p), ("mipMapBias", ctypes.c_float)]
+                ("collectStats", ctypes.c_int), ("backplate", ctypes.c_void_p), ("mipMapBias", ctypes.c_float),
+                ("maxDepth", ctypes.c_void_p)]
 
 
 def quad_light(position, edge1, edge2, intensity=1.0, color=(1, 1, 1), visible=True):
@@ -219,9 +227,11 @@ def materials_array(mats):
 
 def pt_params(spp=1, max_path_length=20, roulette_path_length=5, max_scattering_events=20, light_samples=-1,
               limit_indirect_light_samples=True, min_contribution=0.001, max_contribution=float("inf"),
-              bg=(0, 0, 0, 0), pixel_filter=PF_GAUSS, stats=False, backplate=None, mip_map_bias=0.0):
-    """backplate: a Texture (map_backplate) or None."""
+              bg=(0, 0, 0, 0), pixel_filter=PF_GAUSS, stats=False, backplate=None, mip_map_bias=0.0,
+              max_depth=None):
+    """backplate / max_depth: Textures (map_backplate, map_maxDepth) or None."""
     p = PTParams()
+    p.maxDepth = _tex(max_depth)
     p.pixelSamples, p.maxPathLength, p.roulettePathLength = int(spp), int(max_path_length), int(roulette_path_length)
     p.maxScatteringEvents, p.lightSamples = int(max_scattering_events), int(light_samples)
     p.limitIndirectLightSamples = int(bool(limit_indirect_light_samples))
@@ -237,12 +247,20 @@ class ScivisParams(ctypes.Structure):
     _fields_ = [("pixelSamples", ctypes.c_int), ("volumeSamplingRate", ctypes.c_float),
                 ("backgroundColor", ctypes.c_float * 4), ("pixelFilter", ctypes.c_int),
                 ("collectStats", ctypes.c_int), ("shadows", ctypes.c_int), ("visibleLights", ctypes.c_int),
-                ("aoSamples", ctypes.c_int), ("aoDistance", ctypes.c_float), ("minContribution", ctypes.c_float)]
+                ("aoSamples", ctypes.c_int), ("aoDistance", ctypes.c_float), ("minContribution", ctypes.c_float),
+                ("backplate", ctypes.c_void_p), ("maxDepth", ctypes.c_void_p), ("mipMapBias", ctypes.c_float)]
+
+
+def _tex(t):
+    return None if t is None else t._h.value
 
 
 def scivis_params(spp=1, sampling_rate=1.0, bg=(0, 0, 0, 0), pixel_filter=PF_GAUSS, stats=False, shadows=False,
-                  visible_lights=False, ao_samples=0, ao_distance=1e20, min_contribution=0.001):
+                  visible_lights=False, ao_samples=0, ao_distance=1e20, min_contribution=0.001, backplate=None,
+                  max_depth=None, mip_map_bias=0.0):
+    """backplate / max_depth: Textures (map_backplate, map_maxDepth) or None."""
     p = ScivisParams()
+    p.backplate, p.maxDepth, p.mipMapBias = _tex(backplate), _tex(max_depth), float(mip_map_bias)
     p.pixelSamples, p.volumeSamplingRate = int(spp), float(sampling_rate)
     p.backgroundColor[:] = list(map(float, bg))
     p.pixelFilter, p.collectStats = int(pixel_filter), int(bool(stats))
@@ -253,12 +271,14 @@ def scivis_params(spp=1, sampling_rate=1.0, bg=(0, 0, 0, 0), pixel_filter=PF_GAU
 
 class ScivisMaterial(ctypes.Structure):
     _fields_ = [("isObj", ctypes.c_int), ("kd", ctypes.c_float * 3), ("ks", ctypes.c_float * 3),
-                ("ns", ctypes.c_float), ("d", ctypes.c_float), ("tf", ctypes.c_float * 3)]
+                ("ns", ctypes.c_float), ("d", ctypes.c_float), ("tf", ctypes.c_float * 3),
+                ("kdMap", ctypes.c_void_p)]
 
 
 def scivis_materials_array(mats):
-    """mats: iterable of dicts {"kd", "ks", "ns", "d", "tf"} for "obj"
-    materials (values after OBJ commit), or None for any other material."""
+    """mats: iterable of dicts {"kd", "ks", "ns", "d", "tf", "map_kd"} for
+    "obj" materials (values after OBJ commit; map_kd a Texture), or None for
+    any other material.  The AO renderer reads kd, d and map_kd of them."""
     arr = (ScivisMaterial * max(1, len(mats)))()
     for i, m in enumerate(mats):
         if m is None:
@@ -268,6 +288,7 @@ def scivis_materials_array(mats):
         arr[i].ks[:] = [float(x) for x in m.get("ks", (0, 0, 0))]
         arr[i].ns, arr[i].d = float(m.get("ns", 10.0)), float(m.get("d", 1.0))
         arr[i].tf[:] = [float(x) for x in m.get("tf", (0, 0, 0))]
+        arr[i].kdMap = _tex(m.get("map_kd"))
     return arr, len(mats)
 
 
@@ -716,8 +737,14 @@ def camera_desc(position, direction, up=(0, 1, 0), fovy=60.0, aspect=1.0, near_c
 
 
 def ao_params(spp=1, ao_samples=1, ao_distance=1e20, ao_intensity=1.0, bg=(0, 0, 0, 0), pixel_filter=PF_GAUSS,
-              stats=False, volume_sampling_rate=1.0):
+              stats=False, volume_sampling_rate=1.0, backplate=None, max_depth=None, mip_map_bias=0.0,
+              materials=None):
+    """materials: (ctypes array, count) from scivis_materials_array() (surface colours), or None."""
     p = AOParams()
+    p.backplate, p.maxDepth, p.mipMapBias = _tex(backplate), _tex(max_depth), float(mip_map_bias)
+    if materials:
+        p._materials = materials  # keeps the array alive with the parameters
+        p.materials, p.nmaterials = ctypes.cast(materials[0], ctypes.c_void_p), int(materials[1])
     p.volumeSamplingRate = float(volume_sampling_rate)
     p.collectStats = int(bool(stats))
     p.pixelSamples, p.aoSamples = int(spp), int(ao_samples)

@@ -192,6 +192,11 @@ MaterialD toMaterialD(const b200_material &m) {
       d.roughness = m.roughness;
       d.metallic = m.metallic;
       d.opacity = m.opacity;
+      d.ns = m.specular;
+      d.eta = m.ior;
+      d.tf[0] = m.diffuse;
+      for (int c = 0; c < 3; c++) d.ks[c] = m.edgeColor[c];
+      d.pad0 = m.specularMetallic ? 1.f : 0.f;
       if (1.f - m.opacity > eps) d.flags |= MATF_TRANSPARENT;
       break;
     case B200_MATERIAL_OBJ: {
@@ -257,14 +262,43 @@ bool anyTransparent(const b200_material *materials, int n) {
   return false;
 }
 
+// a principled material the principled-only shading kernel does not carry:
+// specular, ior, diffuse or edgeColor other than 1, or a smooth conductor
+// (roughness 0 with metallic > 0; a smooth dielectric coating at ior 1 and
+// Lambert equal that kernel's microfacet forms)
+static bool principledNeedsFull(const b200_material &m) {
+  return m.specular != 1.f || m.ior != 1.f || m.diffuse != 1.f || m.edgeColor[0] != 1.f || m.edgeColor[1] != 1.f ||
+         m.edgeColor[2] != 1.f || (m.roughness < 1e-6f && m.metallic > 1e-6f);
+}
+
 // a material list that needs the shading kernel with every material type:
-// a type other than principled, or a material shadow rays pass through
+// a type other than principled, a principled material beyond the defaults
+// above, a colour map, or a material shadow rays pass through
 bool anyNonPrincipled(const b200_material *materials, int n) {
   for (int i = 0; i < n; i++)
     if (materials[i].type != B200_MATERIAL_PRINCIPLED || materials[i].baseColorMap ||
-        (toMaterialD(materials[i]).flags & MATF_TRANSPARENT))
+        principledNeedsFull(materials[i]) || (toMaterialD(materials[i]).flags & MATF_TRANSPARENT))
       return true;
   return false;
+}
+
+std::vector<ScivisMatD> toScivisMats(const b200_scivis_material *materials, int n) {
+  std::vector<ScivisMatD> h(n);
+  for (int i = 0; i < n; i++) {
+    const b200_scivis_material &m = materials[i];
+    ScivisMatD &d = h[i];
+    std::memset(&d, 0, sizeof(d));
+    d.isObj = m.isObj != 0;
+    for (int k = 0; k < 3; k++) {
+      d.kd[k] = m.kd[k];
+      d.ks[k] = m.ks[k];
+      d.tf[k] = m.tf[k];
+    }
+    d.ns = m.ns;
+    d.d = m.d;
+    d.kdMap = m.isObj ? textureDevice(m.kdMap) : nullptr;
+  }
+  return h;
 }
 
 // the renderer's material list on the device, uploaded when it changed
@@ -338,6 +372,7 @@ PtParamsD makePtParams(const b200_pt_params &p, const SceneObj *sc, const b200_m
   for (int k = 0; k < 4; k++) d.bg[k] = p.backgroundColor[k];
   d.backplate = textureDevice(p.backplate);
   d.mipBiasFactor = std::pow(2.f, p.mipMapBias);
+  d.maxDepth = textureDevice(p.maxDepth);
   return d;
 }
 
@@ -349,6 +384,11 @@ AOParamsD makeAOParams(const b200_ao_params &p) {
   d.aoIntensity = p.aoIntensity;
   d.volumeSamplingRate = p.volumeSamplingRate > 0.f ? p.volumeSamplingRate : 1.f;
   for (int k = 0; k < 4; k++) d.bg[k] = p.backgroundColor[k];
+  d.backplate = textureDevice(p.backplate);
+  d.maxDepth = textureDevice(p.maxDepth);
+  d.mipBiasFactor = std::pow(2.f, p.mipMapBias);
+  d.mats = nullptr;  // set by the caller once the materials are on the device
+  d.nmats = 0;
   return d;
 }
 
@@ -444,6 +484,7 @@ SceneObj::~SceneObj() {
   if (dLights) cudaFree(dLights);
   if (dScivisLights) cudaFree(dScivisLights);
   if (dScivisMats) cudaFree(dScivisMats);
+  if (dAoMats) cudaFree(dAoMats);
   if (dLightCdf) cudaFree(dLightCdf);
   if (dMaterials) cudaFree(dMaterials);
   for (void *p : {(void *)dVolData, (void *)dTfOpacity, (void *)dTfColor, (void *)dCellEmpty})
@@ -1058,6 +1099,9 @@ void b200_material_defaults(b200_material *m, int type) {
   m->attenuationColor[0] = m->attenuationColor[1] = m->attenuationColor[2] = 1.f;
   m->attenuationDistance = 1.f;
   m->thickness = 1.f;
+  m->specular = m->ior = m->diffuse = 1.f;
+  m->edgeColor[0] = m->edgeColor[1] = m->edgeColor[2] = 1.f;
+  m->specularMetallic = 1;
   switch (type) {
     case B200_MATERIAL_PRINCIPLED:  // Principled::commit, render/materials/Principled.cpp:37-79
     case B200_MATERIAL_OBJ:         // OBJMaterial::commit, OBJ.cpp:28-38
@@ -1147,11 +1191,32 @@ int b200_render_ao(b200_scene s, const b200_camera_desc *camera, const b200_ao_p
     if (!sc->committed) throw Error(B200_INVALID_OPERATION, "scene not committed");
     require(p->pixelSamples >= 1 && p->aoSamples >= 0, "bad AO parameters");
     require(p->pixelFilter >= B200_PF_POINT && p->pixelFilter <= B200_PF_BLACKMAN_HARRIS, "bad pixel filter");
-    const AOParamsD d = makeAOParams(*p);
+    require(p->nmaterials >= 0 && (p->nmaterials == 0 || p->materials), "bad material array");
+    AOParamsD d = makeAOParams(*p);
     cudaStream_t st = stream ? (cudaStream_t)stream : sc->dev->stream;
+    if (p->nmaterials > 0) {  // the surface-colour materials, uploaded when they changed
+      const std::vector<ScivisMatD> h = toScivisMats(p->materials, p->nmaterials);
+      const bool same = sc->lastAoMats.size() == h.size() &&
+                        std::memcmp(sc->lastAoMats.data(), h.data(), sizeof(ScivisMatD) * h.size()) == 0;
+      if (!same) {
+        if (p->nmaterials > sc->capAoMats) {
+          check(cudaStreamSynchronize(st), "sync");
+          if (sc->dAoMats) cudaFree(sc->dAoMats);
+          sc->dAoMats = nullptr;
+          check(cudaMalloc(&sc->dAoMats, sizeof(ScivisMatD) * h.size()), "alloc materials");
+          sc->capAoMats = p->nmaterials;
+        }
+        check(cudaMemcpy(sc->dAoMats, h.data(), sizeof(ScivisMatD) * h.size(), cudaMemcpyHostToDevice),
+              "upload materials");
+        sc->lastAoMats = h;
+      }
+      d.mats = sc->dAoMats;
+      d.nmats = p->nmaterials;
+    }
     fb->beginFrame(p->pixelSamples, st);
     check(launchRenderAO(sc->dev->tables, sc->view(), makeCamera(*camera), sc->dev->filter(p->pixelFilter), d,
-                         fb->view(), p->collectStats != 0, st, sc->dev->timer, sc->hasVolume ? &sc->vol : nullptr),
+                         fb->view(), p->collectStats != 0, st, sc->dev->timer, sc->hasVolume ? &sc->vol : nullptr,
+                         d.nmats > 0 || sc->hasAttributes),
           "AO launch");
     fb->frameID++;
     framePostProcess(fb, st);
@@ -1406,36 +1471,36 @@ int b200_render_scivis(b200_scene s, const b200_camera_desc *camera, const b200_
     d.spp = p->pixelSamples;
     d.samplingRate = p->volumeSamplingRate;
     for (int k = 0; k < 4; k++) d.bg[k] = p->backgroundColor[k];
+    d.backplate = textureDevice(p->backplate);
+    d.maxDepth = textureDevice(p->maxDepth);
+    d.mipBiasFactor = std::pow(2.f, p->mipMapBias);
     cudaStream_t st = stream ? (cudaStream_t)stream : sc->dev->stream;
     fb->beginFrame(p->pixelSamples, st);
-    if (!surfaces && !(sc->vol.gradientShadingScale > 0.f)) {
+    if (!surfaces && !(sc->vol.gradientShadingScale > 0.f) && !p->backplate && !p->maxDepth) {
       check(launchRenderScivisVolume(sc->dev->tables, sc->view(), sc->vol, makeCamera(*camera),
                                      sc->dev->filter(p->pixelFilter), d, fb->view(), p->collectStats != 0, st,
                                      sc->dev->timer),
             "scivis launch");
     } else {
+      // (compared as device records: a texture made again at a reused host
+      // address still has a new device descriptor)
+      std::vector<ScivisMatD> h = toScivisMats(materials, nmaterials);
       const bool same = int(sc->lastScivisMats.size()) == nmaterials &&
-                        (nmaterials == 0 || std::memcmp(sc->lastScivisMats.data(), materials,
-                                                        sizeof(b200_scivis_material) * nmaterials) == 0);
-      bool opaque = true;
+                        (nmaterials == 0 ||
+                         std::memcmp(sc->lastScivisMats.data(), h.data(), sizeof(ScivisMatD) * nmaterials) == 0);
+      // opaque: no obj material lets light through (d < 1, tf, a map with
+      // alpha) and no vertex colour has alpha < 1
+      bool opaque = !sc->colorAlpha, mapped = false;
       for (int i = 0; i < nmaterials; i++) {
         const b200_scivis_material &m = materials[i];
         if (m.isObj && !(m.d == 1.f && m.tf[0] * m.d == 0.f && m.tf[1] * m.d == 0.f && m.tf[2] * m.d == 0.f))
           opaque = false;
+        if (m.isObj && m.kdMap) {
+          mapped = true;
+          if (textureHasAlpha(m.kdMap)) opaque = false;
+        }
       }
       if (!same) {
-        std::vector<ScivisMatD> h(nmaterials);
-        for (int i = 0; i < nmaterials; i++) {
-          const b200_scivis_material &m = materials[i];
-          h[i].isObj = m.isObj != 0;
-          for (int k = 0; k < 3; k++) {
-            h[i].kd[k] = m.kd[k];
-            h[i].ks[k] = m.ks[k];
-            h[i].tf[k] = m.tf[k];
-          }
-          h[i].ns = m.ns;
-          h[i].d = m.d;
-        }
         if (nmaterials > sc->capScivisMats) {
           if (sc->dScivisMats) cudaFree(sc->dScivisMats);
           sc->dScivisMats = nullptr;
@@ -1445,7 +1510,7 @@ int b200_render_scivis(b200_scene s, const b200_camera_desc *camera, const b200_
         if (nmaterials)
           check(cudaMemcpy(sc->dScivisMats, h.data(), sizeof(ScivisMatD) * nmaterials, cudaMemcpyHostToDevice),
                 "upload materials");
-        sc->lastScivisMats.assign(materials, materials + nmaterials);
+        sc->lastScivisMats = h;
       }
       ScivisSurfD S;
       S.mats = sc->dScivisMats;
@@ -1462,6 +1527,7 @@ int b200_render_scivis(b200_scene s, const b200_camera_desc *camera, const b200_
       S.hasVolume = sc->hasVolume;
       S.hasSurfaces = surfaces;
       S.opaqueShadows = opaque && !sc->hasVolume;
+      S.attrs = sc->hasAttributes || mapped;
       check(launchRenderScivisSurfaces(sc->dev->tables, sc->view(), sc->vol, makeCamera(*camera),
                                        sc->dev->filter(p->pixelFilter), d, S, fb->view(), p->collectStats != 0, st,
                                        sc->dev->timer),

@@ -98,7 +98,11 @@ struct SceneObj {
   V3 aoColor = {0.f, 0.f, 0.f};
   ScivisMatD *dScivisMats = nullptr;
   int capScivisMats = 0;
-  std::vector<b200_scivis_material> lastScivisMats;
+  std::vector<ScivisMatD> lastScivisMats;  // the device records last uploaded
+  // the AO renderer's surface-colour materials (b200_ao_params.materials)
+  ScivisMatD *dAoMats = nullptr;
+  int capAoMats = 0;
+  std::vector<ScivisMatD> lastAoMats;
   // one structured-regular volumetric model (device copies)
   bool hasVolume = false;
   VolumeD vol = {};
@@ -178,6 +182,8 @@ const TextureD *textureDevice(b200_texture t);
 bool textureHasAlpha(b200_texture t);
 bool anyNonPrincipled(const b200_material *materials, int n);
 void uploadMaterials(SceneObj *sc, const b200_material *materials, int nmaterials);
+// b200_scivis_material -> device records (SciVis surfaces, AO surface colours)
+std::vector<ScivisMatD> toScivisMats(const b200_scivis_material *materials, int n);
 void ensurePtWorkspace(DeviceObj *dev, size_t need);
 AOParamsD makeAOParams(const b200_ao_params &p);
 ToneMapD makeToneMap(const b200_tonemapper &u);

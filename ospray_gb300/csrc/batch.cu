@@ -234,6 +234,9 @@ int b200_batch_add_ao(b200_batch h, b200_scene s, const b200_camera_desc *camera
     requireArg(sc->committed, "scene not committed");
     requireArg(p->pixelSamples >= 1 && p->aoSamples >= 0, "bad AO parameters");
     requireArg(p->pixelFilter >= B200_PF_POINT && p->pixelFilter <= B200_PF_BLACKMAN_HARRIS, "bad pixel filter");
+    // the batched AO shading is the white, opaque surface case
+    requireArg(p->nmaterials == 0 && !p->backplate && !p->maxDepth && !sc->hasAttributes,
+               "batch: AO with materials, vertex attributes, backplate or maxDepth is rendered by b200_render_ao only");
     BatchObj::Req r;
     r.kind = BATCH_AO;
     r.scene = sc;
@@ -271,7 +274,7 @@ int b200_batch_add_pt(b200_batch h, b200_scene s, const b200_camera_desc *camera
                "b200_render_pt only");
     for (int i = 0; i < nmaterials; i++)
       requireArg(!materials[i].baseColorMap, "batch: textured materials are rendered by b200_render_pt only");
-    requireArg(!p->backplate, "batch: a backplate is rendered by b200_render_pt only");
+    requireArg(!p->backplate && !p->maxDepth, "batch: backplate and maxDepth textures are rendered by b200_render_pt only");
     r.pt = makePtParams(*p, sc, materials, nmaterials, false);
     requireArg(!r.pt.transparentShadows,
                "batch: vertex colours with alpha < 1 under obj materials are rendered by b200_render_pt only");

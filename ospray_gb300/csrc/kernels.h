@@ -104,6 +104,7 @@ struct PtParamsD {
   int allMaterials;        // some material is not opaque principled: the shading kernel with every material type
   const TextureD *backplate;  // the renderer's backplate (null: bg)
   float mipBiasFactor;        // 2^mipMapBias
+  const TextureD *maxDepth;   // the renderer's maxDepth texture (null: no limit)
 };
 
 // structured-regular volume with its transfer function and macrocell
@@ -131,6 +132,8 @@ struct ScivisParamsD {
   int spp;
   float samplingRate;
   float bg[4];
+  const TextureD *backplate, *maxDepth;  // renderer maps (null: bg / no limit)
+  float mipBiasFactor;
 };
 
 // SciVis surfaces: per renderer material slot the OBJ parameters that
@@ -139,6 +142,7 @@ struct ScivisParamsD {
 struct ScivisMatD {
   int isObj;
   float kd[3], ks[3], ns, d, tf[3];
+  const TextureD *kdMap;  // obj map_kd (null: none)
 };
 
 // SciVis surface shading inputs: lights in SciVisData order (the ambient,
@@ -156,6 +160,7 @@ struct ScivisSurfD {
   int hasVolume;
   int hasSurfaces;    // 0: a volume-only world (no ray is traced against surfaces)
   int opaqueShadows;  // every material opaque and no volume: shadow and AO rays as any-hit queries
+  int attrs;          // vertex attributes or an obj map_kd: the kernel with DG_COLOR / DG_TEXCOORD and ray cones
 };
 
 constexpr int VOL_BRICK = 8;
@@ -207,6 +212,10 @@ struct AOParamsD {
   float aoRadius, aoIntensity;
   float bg[4];
   float volumeSamplingRate;
+  const TextureD *backplate, *maxDepth;  // renderer maps (null: bg / no limit)
+  float mipBiasFactor;
+  const ScivisMatD *mats;  // surface colour / opacity materials (getSurfaceColor); null: white, opaque
+  int nmats;
 };
 
 // ---- batches: many render requests in one wavefront
@@ -259,6 +268,7 @@ cudaError_t launchPick(const Scene &sc, const CameraD &cam, float sx, float sy, 
 cudaError_t launchTrace(const Scene &sc, const float4 *rays, long long n, int occlusion, float *outF, uint32_t *outI,
                         cudaStream_t st);
 cudaError_t launchRenderAO(const SamplerTables *T, const Scene &sc, const CameraD &cam, const PixelFilterD &pf, const AOParamsD &p,
-                           const FrameD &fb, bool stats, cudaStream_t st, KernelTimer *kt = nullptr, const VolumeD *vol = nullptr);
+                           const FrameD &fb, bool stats, cudaStream_t st, KernelTimer *kt = nullptr, const VolumeD *vol = nullptr,
+                           bool surf = false);
 
 }  // namespace b200

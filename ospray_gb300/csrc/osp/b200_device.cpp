@@ -275,8 +275,19 @@ OSPFuture B200Device::renderFrame(OSPFrameBuffer hf, OSPRenderer hr, OSPCamera h
     // the renderer's varianceThreshold selects the tasks of this frame
     check(b200_frame_set_variance_threshold(f->fb, r->varianceThreshold));
     check(b200_event_record(dev_, &fut->start));
+    // texture handles as of now (a texture committed again since has a new one)
+    b200_texture bp = r->backplate ? r->backplate->tex : nullptr, md = r->maxDepth ? r->maxDepth->tex : nullptr;
     if (r->type == "ao") {
-      check(b200_render_ao(w->scene, &c->desc, &r->ao, f->fb, nullptr));
+      std::vector<b200_scivis_material> mats;
+      for (const auto *list : {&w->objectMaterials, &r->materials})
+        for (const auto &m : *list) mats.push_back(m->scivis());
+      b200_ao_params ao = r->ao;
+      ao.backplate = bp;
+      ao.maxDepth = md;
+      ao.mipMapBias = r->mipMapBias;
+      ao.materials = mats.data();
+      ao.nmaterials = int(mats.size());
+      check(b200_render_ao(w->scene, &c->desc, &ao, f->fb, nullptr));
     } else if (r->type == "pathtracer") {
       if (w->hasVolume) warn("pathtracer: volumes are not rendered by the b200 device");
       std::vector<b200_material> mats;
@@ -287,15 +298,20 @@ OSPFuture B200Device::renderFrame(OSPFrameBuffer hf, OSPRenderer hr, OSPCamera h
           mats.back().baseColorMap = m->colorMapHandle();
         }
       b200_pt_params pt = r->pt;
-      pt.backplate = r->backplate ? r->backplate->tex : nullptr;
+      pt.backplate = bp;
+      pt.maxDepth = md;
       check(b200_render_pt(w->scene, &c->desc, &pt, mats.data(), int(mats.size()), f->fb, nullptr));
     } else {
       if (!w->hasGeometry && !w->hasVolume)
         throw Error(OSP_INVALID_OPERATION, "scivis renderer: the world has no geometry and no volume");
       std::vector<b200_scivis_material> mats;
-      for (const auto &m : w->objectMaterials) mats.push_back(m->sv);
-      for (const auto &m : r->materials) mats.push_back(m->sv);
-      check(b200_render_scivis(w->scene, &c->desc, &r->scivis, mats.data(), int(mats.size()), f->fb, nullptr));
+      for (const auto *list : {&w->objectMaterials, &r->materials})
+        for (const auto &m : *list) mats.push_back(m->scivis());
+      b200_scivis_params sv = r->scivis;
+      sv.backplate = bp;
+      sv.maxDepth = md;
+      sv.mipMapBias = r->mipMapBias;
+      check(b200_render_scivis(w->scene, &c->desc, &sv, mats.data(), int(mats.size()), f->fb, nullptr));
     }
     check(b200_event_record(dev_, &fut->end));
   } catch (...) {

@@ -224,15 +224,19 @@ void MaterialObj::commit(B200Device &dev) {
     mat.roughness = getFloat("roughness", 0.f);
     mat.metallic = getFloat("metallic", 0.f);
     mat.opacity = getFloat("opacity", 1.f);
+    mat.specular = getFloat("specular", 1.f);
+    mat.ior = getFloat("ior", 1.f);
+    mat.diffuse = getFloat("diffuse", 1.f);
+    getVec3("edgeColor", mat.edgeColor, kOne3);
+    mat.specularMetallic = getBool("specularMetallic", true) ? 1 : 0;
     // parameters of the principled model the GB300 path tracer does not
     // evaluate: accepted at their defaults, reported otherwise
     struct Def {
       const char *name;
       float value;
     };
-    static const Def fixed[] = {{"specular", 1.f}, {"ior", 1.f},    {"transmission", 0.f}, {"diffuse", 1.f},
-                                {"anisotropy", 0.f}, {"coat", 0.f}, {"sheen", 0.f},        {"backlight", 0.f},
-                                {"thin", 0.f}};
+    static const Def fixed[] = {{"transmission", 0.f}, {"anisotropy", 0.f}, {"coat", 0.f},
+                                {"sheen", 0.f},        {"backlight", 0.f},  {"thin", 0.f}};
     for (const Def &d : fixed)
       if (has(d.name) && getFloat(d.name, d.value) != d.value)
         dev.warn(std::string("principled material: '") + d.name + "' other than " + std::to_string(d.value) +
@@ -594,6 +598,8 @@ void RendererObj::commit(B200Device &) {
   const float minContribution = getFloat("minContribution", 0.001f);
   materials = objectList<MaterialObj>(getData("material"), OSP_MATERIAL, "renderer 'material'");
   backplate = textureParam(*this, "map_backplate");
+  this->maxDepth = textureParam(*this, "map_maxDepth");
+  mipMapBias = getFloat("mipMapBias", 0.f);
   if (type == "ao") {
     ao.pixelSamples = spp;
     ao.aoSamples = getInt("aoSamples", 1);
@@ -615,8 +621,7 @@ void RendererObj::commit(B200Device &) {
     std::memcpy(pt.backgroundColor, bg, 16);
     pt.pixelFilter = pf;
     pt.collectStats = 0;
-    pt.backplate = backplate ? backplate->tex : nullptr;
-    pt.mipMapBias = getFloat("mipMapBias", 0.f);
+    pt.mipMapBias = mipMapBias;
   } else {  // scivis (SciVis::commit, render/scivis/SciVis.cpp:27-36)
     scivis.pixelSamples = spp;
     scivis.volumeSamplingRate = getFloat("volumeSamplingRate", 1.f);

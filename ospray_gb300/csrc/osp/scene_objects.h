@@ -58,6 +58,12 @@ struct MaterialObj : SceneObj {
   Ref<TextureObj> colorMap;      // principled "map_baseColor" / obj "map_kd"
   b200_material mat = {};        // as the path tracer reads it (baseColorMap: see colorMapHandle)
   b200_texture colorMapHandle() const { return colorMap ? colorMap->tex : nullptr; }
+  // the SciVis / AO record with the obj map_kd as of now
+  b200_scivis_material scivis() const {
+    b200_scivis_material m = sv;
+    m.kdMap = sv.isObj ? colorMapHandle() : nullptr;
+    return m;
+  }
   b200_scivis_material sv = {};  // as the SciVis renderer reads it
   void commit(B200Device &) override;
 };
@@ -148,6 +154,8 @@ struct RendererObj : SceneObj {
   b200_scivis_params scivis = {};
   std::vector<Ref<MaterialObj>> materials;  // the "material" list
   Ref<TextureObj> backplate;                // "map_backplate"
+  Ref<TextureObj> maxDepth;                 // "map_maxDepth"
+  float mipMapBias = 0.f;                   // "mipMapBias"
   float varianceThreshold = 0.f;
   void commit(B200Device &) override;
 };

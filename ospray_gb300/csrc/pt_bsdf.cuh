@@ -29,7 +29,7 @@ struct __align__(16) MaterialD {
   uint32_t kind, flags;      // MAT_*, MATF_*
   float ks[3], ns;           // obj ks (scaled), ns
   float tf[3], eta;          // obj tf (scaled); thin glass: 1 / eta
-  float ceta[3], pad0;       // metal: eta per channel
+  float ceta[3], pad0;       // metal: eta per channel; principled: pad0 = specularMetallic
   float ck[3], pad1;         // metal: k per channel
   float att[3], iorIn;       // glass: inside medium attenuation (log(colour) / distance) and ior; thin glass: attenuation
   float attOut[3], iorOut;   // glass: outside medium
@@ -160,76 +160,136 @@ struct BsdfSample {
   uint32_t type;  // ST_* of the sampled lobe
 };
 
-// Principled with its opacity-1, coat/sheen-free structure: a MultiBSDF of
-// a microfacet conductor (child 0) and a dielectric layer over Oren-Nayar
-// (child 2, "plastic").  ior = 1 (the default) gives eta = 1.
-struct Principled {
+// fresnelDielectricEx (bsdfs/Fresnel.ih:38-47): the Fresnel reflectance and
+// the cosine of the refracted direction (0 under total internal reflection)
+B200_D float fresnelDielEx(float cosI, float &cosT, float eta) {
+  const float c2 = 1.f - sqrf(eta) * (1.f - sqrf(cosI));
+  if (c2 < 0.f) {
+    cosT = 0.f;
+    return 1.f;
+  }
+  cosT = sqrtf(c2);
+  const float Rper = (eta * cosI - cosT) / (eta * cosI + cosT);
+  const float Rpar = (cosI - eta * cosT) / (cosI + eta * cosT);
+  return 0.5f * (sqrf(Rpar) + sqrf(Rper));
+}
+
+// The principled base stack without transmission, coat or sheen
+// (Principled.ispc:110-331): a MultiBSDF of a conductor (child 0) and a
+// "plastic" dielectric layer over a diffuse substrate (child 2).
+//   plastic: weight dielectric, importance dielectric x max(diffuse,
+//     specular); the layer has weight `specular` (a pass-through layer for
+//     specular 0) and eta = outside ior / ior (inverted inside), clamped to
+//     [1/3, 3]; roughness 0: Lambert under a smooth DielectricLayer
+//     (bsdfs/DielectricLayer.ih), else Oren-Nayar under a
+//     MicrofacetDielectricLayer (bsdfs/MicrofacetDielectricLayer.ih);
+//   conductor: weight = importance = metallic (x specular when
+//     specularMetallic), FresnelConductorArtistic from baseColor and
+//     edgeColor; roughness 0: the smooth Conductor (bsdfs/Conductor.ih), else
+//     MicrofacetConductor.
+// Material record fields: ns = specular, eta = ior, tf[0] = diffuse,
+// ks = edgeColor, pad0 = specularMetallic (0 / 1).
+// FULL = false: the parameters at their defaults (specular, ior, diffuse,
+// edgeColor 1, specularMetallic) and no smooth conductor (the frame's
+// materials are checked on the host, principledNeedsFull); the principled-only
+// shading kernel takes this smaller form.
+template <bool FULL>
+struct PrincipledT {
   V3 fx, fy, N;  // shading frame
   float rough, alpha;
-  float wC, wP, impSum;
+  float wC, wP, iP, impSum;
   V3 ceta, ck, cFms;
   float cEavg;
   V3 diffuse;
-  float eta, lEavg, lFms, lRavg, lAlbedoMax;
+  float eta, lEavg, lFms, lRavg, lAlbedoMax, lWeight, lFavg;
+  bool smoothBase, hasLayer, smooth;  // roughness 0; a coating layer (specular > 0); diffuse / glossy lobes
   V3 albedo;  // MultiBSDF albedo: sum of the lobes' albedos x weights (the shading AOV)
 
   B200_D V3 toLocal(V3 v) const { return mk(fdot(v, fx), fdot(v, fy), fdot(v, N)); }
   B200_D V3 toGlobal(V3 v) const { return fx * v.x + fy * v.y + N * v.z; }
 
-  B200_D void init(const MaterialD &m, V3 U, V3 V, V3 Nn, const AlbedoTablesD *T) {
+  // fromOutside: the path travels in the material's outside medium (vacuum)
+  B200_D void init(const MaterialD &m, V3 U, V3 V, V3 Nn, const AlbedoTablesD *T, bool fromOutside = true) {
     fx = U;
     fy = V;
     N = Nn;
     const V3 base = mk(clamp01f(m.r), clamp01f(m.g), clamp01f(m.b));
     const float metallic = clamp01f(m.metallic);
+    const float specular = FULL ? clamp01f(m.ns) : 1.f, diffuseW = FULL ? clamp01f(m.tf[0]) : 1.f;
     rough = clamp01f(m.roughness);
     alpha = fmaxf(sqrf(rough), 0.001f);
-    wC = wP = impSum = 0.f;
+    smoothBase = FULL && m.roughness < MAT_EPS;
+    wC = wP = iP = impSum = 0.f;
     albedo = splat(0.f);
+    smooth = false;
+    hasLayer = false;
     const float dielectric = 1.f - metallic;
     if (dielectric > MAT_EPS) {
-      const float e = 1.f;  // outside ior 1 / ior 1, clamped to [1/3, 3]
-      diffuse = base;
-      eta = e;
-      lEavg = tabAvg(T, rough);
-      const float Favg = fresnelDielAvg(e);
-      lFms = Favg * (1.f - lEavg) / (1.f - Favg * lEavg);
-      lRavg = tabReflAvg(T, eta, rough) + lFms * (1.f - lEavg);
-      const float la = 1.f - Favg;  // (1 - weight) + transmittance^thickness (1 - Favg), weight 1
-      lAlbedoMax = fmaxf(fmaxf(base.x * la, base.y * la), base.z * la);
+      float ior = FULL ? m.eta : 1.f;
+      if (ior < 1.f) ior = 1.f / ior;
+      float e = fromOutside ? 1.f * (1.f / ior) : ior * (1.f / 1.f);
+      e = fminf(fmaxf(e, 1.f / 3.f), 3.f);
+      diffuse = base * diffuseW;
+      hasLayer = !FULL || specular > MAT_EPS;
+      lWeight = specular;
+      eta = e <= 1.f ? e : 1.f / e;
+      V3 la = diffuse;  // pass-through: the substrate's albedo
+      if (FULL && hasLayer && smoothBase) {
+        lFavg = fresnelDielAvg(e) * specular;
+        la = diffuse * ((1.f - specular) + 1.f * (1.f - lFavg));
+      } else if (hasLayer) {
+        lEavg = tabAvg(T, rough);
+        const float Favg = fresnelDielAvg(e);
+        lFms = Favg * (1.f - lEavg) / (1.f - Favg * lEavg);
+        lRavg = (tabReflAvg(T, eta, rough) + lFms * (1.f - lEavg)) * specular;
+        la = diffuse * ((1.f - specular) + 1.f * (1.f - Favg));
+      }
+      lAlbedoMax = fmaxf(fmaxf(la.x, la.y), la.z);
       wP = dielectric;
-      impSum += dielectric;
-      albedo = base * (la * wP);
+      iP = dielectric * fmaxf(diffuseW, specular);
+      impSum += iP;
+      albedo = la * wP;
+      smooth = true;  // the diffuse substrate
     }
-    const float conductor = metallic;
+    const float conductor = metallic * (!FULL || m.pad0 != 0.f ? specular : 1.f);
     if (conductor > MAT_EPS) {
       const float rr[3] = {fminf(base.x, 0.99f), fminf(base.y, 0.99f), fminf(base.z, 0.99f)};
+      const float gg[3] = {FULL ? clamp01f(m.ks[0]) : 1.f, FULL ? clamp01f(m.ks[1]) : 1.f,
+                           FULL ? clamp01f(m.ks[2]) : 1.f};
       float ne[3], nk[3], fa[3];
 #pragma unroll
       for (int c = 0; c < 3; c++) {
-        const float R = rr[c];
+        // FresnelConductorArtistic (Fresnel.ih): n between n_min and n_max by the edge colour
+        const float R = rr[c], G = gg[c];
         const float nmin = (1.f - R) / (1.f + R);
-        // edge tint 1: n = n_min
-        const float n = nmin;
+        const float nmax = (1.f + sqrtf(R)) / (1.f - sqrtf(R));
+        const float n = G * nmin + (1.f - G) * nmax;
         const float k2 = (sqrf(n + 1.f) * R - sqrf(n - 1.f)) / (1.f - R);
         ne[c] = n;
         nk[c] = sqrtf(fmaxf(k2, 0.f));
-        const float R2 = R * R, R3 = R2 * R;
-        fa[c] = 0.087237f + 0.0230685f - 0.0864902f + 0.0774594f + 0.782654f * R - 0.136432f * R2 +
-                0.278708f * R3 + 0.19744f * R + 0.0360605f * R - 0.2586f * R2;
+        const float R2 = R * R, R3 = R2 * R, G2 = G * G, G3 = G2 * G;
+        fa[c] = 0.087237f + 0.0230685f * G - 0.0864902f * G2 + 0.0774594f * G3 + 0.782654f * R - 0.136432f * R2 +
+                0.278708f * R3 + 0.19744f * G * R + 0.0360605f * G2 * R - 0.2586f * G * R2;
       }
       ceta = mk(ne[0], ne[1], ne[2]);
       ck = mk(nk[0], nk[1], nk[2]);
-      cEavg = tabAvg(T, rough);
-      cFms = mk(sqrf(fa[0]) * cEavg / (1.f - fa[0] * (1.f - cEavg)), sqrf(fa[1]) * cEavg / (1.f - fa[1] * (1.f - cEavg)),
-                sqrf(fa[2]) * cEavg / (1.f - fa[2] * (1.f - cEavg)));
       wC = conductor;
       impSum += conductor;
-      albedo = albedo + mk(fa[0], fa[1], fa[2]) * (cEavg * conductor);
+      if (FULL && smoothBase) {
+        albedo = albedo + mk(fa[0], fa[1], fa[2]) * conductor;
+      } else {
+        cEavg = tabAvg(T, rough);
+        cFms = mk(sqrf(fa[0]) * cEavg / (1.f - fa[0] * (1.f - cEavg)),
+                  sqrf(fa[1]) * cEavg / (1.f - fa[1] * (1.f - cEavg)),
+                  sqrf(fa[2]) * cEavg / (1.f - fa[2] * (1.f - cEavg)));
+        albedo = albedo + mk(fa[0], fa[1], fa[2]) * (cEavg * conductor);
+        smooth = true;
+      }
     }
   }
 
   B200_D BsdfEval evalConductor(V3 wo, V3 wi, const AlbedoTablesD *T) const {
+    if (FULL && smoothBase) return {splat(0.f), 0.f};  // Dirac
     const float cosO = fdot(wo, N), cosI = fdot(wi, N);
     if (cosO <= 0.f || cosI <= 0.f) return {splat(0.f), 0.f};
     const V3 wh = fnormalize(wi + wo);
@@ -246,6 +306,14 @@ struct Principled {
 
   B200_D BsdfSample sampleConductor(V3 wo, float sx, float sy, const AlbedoTablesD *T) const {
     BsdfSample r = {splat(0.f), splat(0.f), 0.f, 0u};
+    if (FULL && smoothBase) {  // Conductor_sample: the mirror direction, weight = Fresnel
+      const float c = fdot(wo, N);
+      r.wi = reflectV(wo, N, c);
+      r.pdf = INFINITY;
+      r.type = ST_SPEC_R;
+      r.weight = mk(fresnelCond(c, ceta.x, ck.x), fresnelCond(c, ceta.y, ck.y), fresnelCond(c, ceta.z, ck.z));
+      return r;
+    }
     const float cosO = fdot(wo, N);
     if (cosO <= 0.f) return r;
     const V3 wo0 = toLocal(wo);
@@ -267,28 +335,51 @@ struct Principled {
     return r;
   }
 
+  // the substrate: Oren-Nayar (Lambert at roughness 0)
   B200_D BsdfEval evalOrenNayar(V3 wo, V3 wi) const {
     const float cosO = fmaxf(fdot(wo, N), 0.f), cosI = fmaxf(fdot(wi, N), 0.f);
     const float s = fdot(wo, wi) - cosO * cosI;
     const float sInvt = s > 0.f ? s * rcpSafe(fmaxf(cosO, cosI)) : s;
     return {diffuse * (cosI * (1.f + rough * sInvt) / (PI_F + (PI_F / 2.f - 2.f / 3.f) * rough)), cosI / PI_F};
   }
+  B200_D BsdfSample sampleDiffuse(V3 wo, float sx, float sy) const {
+    BsdfSample r;
+    float sp, cp;
+    sincosf(2.f * PI_F * sx, &sp, &cp);
+    const float cosT = sqrtf(sy), sinT = sqrtf(1.f - sy);
+    r.wi = toGlobal(mk(cp * sinT, sp * sinT, cosT));
+    r.type = ST_DIFFUSE_R;
+    const BsdfEval e = evalOrenNayar(wo, r.wi);
+    r.pdf = e.pdf;
+    r.weight = e.value * (1.f / e.pdf);
+    return r;
+  }
 
   B200_D BsdfEval evalPlastic(V3 wo, V3 wi, const AlbedoTablesD *T) const {
+    if (FULL && !hasLayer) return evalOrenNayar(wo, wi);  // PassthroughLayer
     const float cosO = fdot(wo, N);
     if (cosO <= 0.f) return {splat(0.f), 0.f};
     const float cosI = fdot(wi, N);
     BsdfEval sub = evalOrenNayar(wo, wi);
+    if (FULL && smoothBase) {  // DIELECTRICLAYER_EVAL over a diffuse substrate
+      float cosO1, cosI1;
+      const float F = fresnelDielEx(cosO, cosO1, eta);
+      const float Fo = F * lWeight, Fi = fresnelDielEx(fabsf(cosI), cosI1, eta) * lWeight;
+      sub.value = sub.value * ((1.f - Fo) * (1.f - Fi) * (1.f / (1.f - lFavg)));
+      const float coatPick = Fo / ((1.f - F) * lAlbedoMax + Fo);
+      sub.pdf *= 1.f - coatPick;
+      return sub;
+    }
     const float Eo = tabEval(T, cosO, rough), Ei = tabEval(T, fabsf(cosI), rough);
-    const float Ro = tabRefl(T, cosO, eta, rough) + lFms * (1.f - Eo);
-    const float Ri = tabRefl(T, fabsf(cosI), eta, rough) + lFms * (1.f - Ei);
+    const float Ro = (tabRefl(T, cosO, eta, rough) + lFms * (1.f - Eo)) * lWeight;
+    const float Ri = (tabRefl(T, fabsf(cosI), eta, rough) + lFms * (1.f - Ei)) * lWeight;
     sub.value = sub.value * ((1.f - Ro) * (1.f - Ri) / (1.f - lRavg));
-    const float coatPick = Ro / ((1.f - Ro) * lAlbedoMax + Ro);
+    const float coatPick = lWeight * Ro / ((1.f - Ro) * lAlbedoMax + lWeight * Ro);
     const float subPick = 1.f - coatPick;
     if (cosI > 0.f) {
       const V3 wh = fnormalize(wo + wi);
       const float cosOH = fdot(wo, wh), cosIH = fdot(wi, wh);
-      const float F = fresnelDiel(cosOH, eta);
+      const float F = fresnelDiel(cosOH, eta) * lWeight;
       float whPdf;
       const float D = ggxEvalVisible(alpha, toLocal(wh), toLocal(wo), cosOH, whPdf);
       const float G = ggxG2(alpha, toLocal(wo), toLocal(wi), cosOH, cosIH);
@@ -303,12 +394,35 @@ struct Principled {
 
   B200_D BsdfSample samplePlastic(V3 wo, float sx, float sy, float ss, const AlbedoTablesD *T) const {
     BsdfSample r = {splat(0.f), splat(0.f), 0.f, 0u};
+    if (FULL && !hasLayer) return sampleDiffuse(wo, sx, sy);  // PassthroughLayer
     const float cosO = fdot(wo, N);
     if (cosO <= 0.f) return r;
+    if (FULL && smoothBase) {  // DIELECTRICLAYER_SAMPLE over a diffuse substrate
+      float cosO1;
+      const float F = fresnelDielEx(cosO, cosO1, eta);
+      const float Fo = F * lWeight;
+      const float coatPick = Fo / ((1.f - F) * lAlbedoMax + Fo);
+      if (ss < coatPick) {
+        r.type = ST_SPEC_R;
+        r.wi = reflectV(wo, N, cosO);
+        r.pdf = INFINITY;
+        r.weight = splat(Fo / coatPick);
+        return r;
+      }
+      r = sampleDiffuse(wo, sx, sy);
+      if (maxc(r.weight) <= 0.f) return r;
+      float cosI1;
+      const float Fi = fresnelDielEx(fabsf(fdot(r.wi, N)), cosI1, eta) * lWeight;
+      const float Tr = (1.f - Fo) * (1.f - Fi) * (1.f / (1.f - lFavg));
+      r.weight = r.weight * (Tr * (1.f / (1.f - coatPick)));
+      r.pdf *= 1.f - coatPick;
+      return r;
+    }
     const V3 wo0 = toLocal(wo);
     const float Eo = tabEval(T, cosO, rough);
-    const float Ro = tabRefl(T, cosO, eta, rough) + lFms * (1.f - Eo);
-    const float coatPick = Ro / ((1.f - Ro) * lAlbedoMax + Ro);
+    // (the reference's sample weighs only the multiple-scattering term here)
+    const float Ro = tabRefl(T, cosO, eta, rough) + lFms * (1.f - Eo) * lWeight;
+    const float coatPick = lWeight * Ro / ((1.f - Ro) * lAlbedoMax + lWeight * Ro);
     const float subPick = 1.f - coatPick;
     V3 wh;
     BsdfEval sub;
@@ -319,28 +433,21 @@ struct Principled {
       r.type = ST_GLOSSY_R;
       sub = evalOrenNayar(wo, r.wi);
     } else {
-      float sp, cp;
-      sincosf(2.f * PI_F * sx, &sp, &cp);
-      const float cosT = sqrtf(sy), sinT = sqrtf(1.f - sy);
-      r.wi = toGlobal(mk(cp * sinT, sp * sinT, cosT));
-      r.type = ST_DIFFUSE_R;
-      const BsdfEval e = evalOrenNayar(wo, r.wi);
-      r.pdf = e.pdf;
-      r.weight = e.value * (1.f / e.pdf);
-      if (fmaxf(fmaxf(r.weight.x, r.weight.y), r.weight.z) <= 0.f) return r;
+      r = sampleDiffuse(wo, sx, sy);
+      if (maxc(r.weight) <= 0.f) return r;
       sub.pdf = r.pdf;
       sub.value = r.weight * r.pdf;
       wh = fnormalize(wo + r.wi);
     }
     const float cosI = fdot(r.wi, N), cosOH = fdot(wo, wh);
     const float Ei = tabEval(T, fabsf(cosI), rough);
-    const float Ri = tabRefl(T, fabsf(cosI), eta, rough) + lFms * (1.f - Ei);
+    const float Ri = (tabRefl(T, fabsf(cosI), eta, rough) + lFms * (1.f - Ei)) * lWeight;
     sub.value = sub.value * ((1.f - Ro) * (1.f - Ri) / (1.f - lRavg));
     if (cosI <= 0.f) {
       r.pdf = subPick * sub.pdf;
       r.weight = sub.value * (1.f / r.pdf);
     } else {
-      const float F = fresnelDiel(cosOH, eta);
+      const float F = fresnelDiel(cosOH, eta) * lWeight;
       float whPdf;
       const float D = ggxEvalVisible(alpha, toLocal(wh), wo0, cosOH, whPdf);
       const float G = ggxG2(alpha, wo0, toLocal(r.wi), cosOH, fdot(r.wi, wh));
@@ -358,10 +465,10 @@ struct Principled {
       r.value = r.value + c.value * wC;
       r.pdf += c.pdf * wC;
     }
-    if (wP > 0.f) {
+    if (iP > 0.f) {
       const BsdfEval c = evalPlastic(wo, wi, T);
       r.value = r.value + c.value * wP;
-      r.pdf += c.pdf * wP;
+      r.pdf += c.pdf * iP;
     }
     r.pdf *= 1.f / impSum;
     return r;
@@ -376,26 +483,30 @@ struct Principled {
       choice = 0;
       r = sampleConductor(wo, sx, sy, T);
       r.weight = r.weight * wC;
-    } else if (x < wC + wP) {
+    } else if (x < wC + iP) {
       choice = 2;
-      r = samplePlastic(wo, sx, sy, (x + wP - (wC + wP)) / wP, T);
+      r = samplePlastic(wo, sx, sy, (x + iP - (wC + iP)) / iP, T);
       r.weight = r.weight * wP;
     } else {
       return r;
     }
     if ((r.weight.x == 0.f && r.weight.y == 0.f && r.weight.z == 0.f) || r.pdf == 0.f)
       return {splat(0.f), splat(0.f), 0.f, 0u};
+    if (FULL && (r.type & ST_SPECULAR)) {  // a Dirac lobe: no other child adds (MultiBSDF_sample)
+      r.weight = r.weight * (impSum * (1.f / (choice == 0 ? wC : iP)));
+      return r;
+    }
     V3 value = r.weight * r.pdf;
-    float pdf = r.pdf * (choice == 0 ? wC : wP);
+    float pdf = r.pdf * (choice == 0 ? wC : iP);
     if (choice != 0 && wC > 0.f) {
       const BsdfEval c = evalConductor(wo, r.wi, T);
       value = value + c.value * wC;
       pdf += c.pdf * wC;
     }
-    if (choice != 2 && wP > 0.f) {
+    if (choice != 2 && iP > 0.f) {
       const BsdfEval c = evalPlastic(wo, r.wi, T);
       value = value + c.value * wP;
-      pdf += c.pdf * wP;
+      pdf += c.pdf * iP;
     }
     r.pdf = pdf * (1.f / impSum);
     r.weight = value * (1.f / r.pdf);
@@ -421,7 +532,7 @@ B200_D V3 expV(V3 a) { return mk(expf(a.x), expf(a.y), expf(a.z)); }
 // the root has the stack child only and the cut-out state drops out.
 template <bool CUT>
 struct PrincipledBsdfT {
-  Principled st;
+  PrincipledT<CUT> st;
   float op, tr, impSum;
   bool hasStack, hasCut, smooth;
   B200_D V3 N() const { return st.N; }
@@ -436,13 +547,15 @@ struct PrincipledBsdfT {
   // opacity: the material's opacity times its colour map's alpha (clamped);
   // the stack exists for the material's own opacity > EPS, the cut-out child
   // for its own opacity < 1 - EPS or a colour map with alpha
-  B200_D void init(const MaterialD &m, V3 U, V3 V, V3 Nn, const AlbedoTablesD *T, float opacity) {
+  // fromOutside: the path travels in vacuum, the principled material's outside medium
+  B200_D void init(const MaterialD &m, V3 U, V3 V, V3 Nn, const AlbedoTablesD *T, float opacity,
+                   bool fromOutside = true) {
     op = opacity;
     tr = CUT ? 1.f - op : 0.f;
     hasStack = !CUT || m.opacity > MAT_EPS;
     hasCut = CUT && (1.f - m.opacity > MAT_EPS || (m.flags & MATF_MAP_ALPHA) != 0);
     if (hasStack) {
-      st.init(m, U, V, Nn, T);
+      st.init(m, U, V, Nn, T, fromOutside);
     } else {
       st.fx = U;
       st.fy = V;
@@ -450,7 +563,7 @@ struct PrincipledBsdfT {
       st.impSum = 0.f;
       st.albedo = splat(0.f);
     }
-    smooth = hasStack && st.impSum > 0.f;
+    smooth = hasStack && st.smooth;
     impSum = (hasCut ? tr : 0.f) + (hasStack ? op : 0.f);
   }
   B200_D BsdfEval eval(V3 wo, V3 wi, const AlbedoTablesD *T) const {
@@ -788,17 +901,7 @@ struct GlassBsdf {
 // ThinGlass (render/materials/ThinGlass.ispc:16-70) as RobustThinDielectric
 // (bsdfs/RobustThinDielectric.ih): a slab whose inner reflections are summed
 // in closed form; reflection or straight transmission picked by luminance.
-B200_D float fresnelDielEx(float cosI, float &cosT, float eta) {
-  const float c2 = 1.f - sqrf(eta) * (1.f - sqrf(cosI));
-  if (c2 < 0.f) {
-    cosT = 0.f;
-    return 1.f;
-  }
-  cosT = sqrtf(c2);
-  const float Rper = (eta * cosI - cosT) / (eta * cosI + cosT);
-  const float Rpar = (cosI - eta * cosT) / (cosI + eta * cosT);
-  return 0.5f * (sqrf(Rpar) + sqrf(Rper));
-}
+
 B200_D void thinSlab(float cosO, float eta, V3 att, V3 &R, V3 &T) {
   float cosT;
   const float Fo = fresnelDielEx(cosO, cosT, eta);

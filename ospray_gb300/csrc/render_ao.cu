@@ -69,16 +69,41 @@ B200_D float computeAO(const SamplerTables *T, const Scene &sc, const DG &dg, in
   return 1.f - float(hits) / float(sampleCnt);
 }
 
-// Resident blocks per SM the single-frame AO kernel is compiled for.  1 (no
-// register cap, 153 registers, 3 blocks per SM) measured best on the 512^2
-// AO workload: 1,417 Mrays/s against 1,313 / 1,268 / 1,240 when capped for
-// 4 / 5 / 6 blocks (the cap spills the traversal and shading state).
+// Resident blocks per SM the single-frame AO kernel is compiled for.  3 (a
+// bound of 170 registers; uncapped the kernel takes 171, one too many for a
+// third block) measured best on the 512^2 AO workload: 1,417 Mrays/s at 3
+// blocks against 1,290 at 2 and 1,313 / 1,268 / 1,240 when capped for
+// 4 / 5 / 6 blocks (those caps spill the traversal and shading state).
 #ifndef B200_AO_MINBLOCKS
-#define B200_AO_MINBLOCKS 1
+#define B200_AO_MINBLOCKS 3
 #endif
+// getSurfaceColor (render/ao/surfaces.ispc:17-42): an obj material's kd x
+// map_kd rgb (d x map alpha) times the vertex colour; white and opaque
+// without an obj material
+B200_D float4 aoSurfaceColor(const AOParamsD &p, uint32_t mi, const DGAttr &at, float fp) {
+  V3 c = splat(1.f);
+  float op = 1.f;
+  if (mi < uint32_t(p.nmats) && p.mats[mi].isObj) {
+    const ScivisMatD &m = p.mats[mi];
+    c = mk(m.kd[0], m.kd[1], m.kd[2]);
+    if (m.kdMap) {
+      const float4 t = texGet(*m.kdMap, at.s, at.t, fp);
+      c = c * mk(t.x, t.y, t.z);
+      op *= t.w;
+    }
+    op *= m.d;
+  }
+  return make_float4(c.x * at.color.x, c.y * at.color.y, c.z * at.color.z, op * at.color.w);
+}
+
 // VOL: the scene's volume is composited in front of each layer
-// (integrateVolumeIntervals, render/ao/volumes.ispc:251-352)
-template <bool STATS, bool VOL>
+// (integrateVolumeIntervals, render/ao/volumes.ispc:251-352).
+// SURF: surface colours and opacities (materials, vertex attributes, maps
+// with ray-cone footprints; AORenderer_computeShading surfaces.ispc:44-77);
+// without it every surface is white and opaque.
+// The renderer's map_maxDepth limits the camera ray and map_backplate
+// replaces the background colour, both at the pixel centre.
+template <bool STATS, bool VOL, bool SURF>
 __global__ void __launch_bounds__(128, B200_AO_MINBLOCKS) k_render_ao(const SamplerTables *T, Scene sc, CameraD cam, PixelFilterD pf, AOParamsD p, FrameD fb, VolumeD vol) {
   const int x = blockIdx.x * 16 + (threadIdx.x & 15);
   const int y = blockIdx.y * 8 + (threadIdx.x >> 4);
@@ -93,7 +118,13 @@ __global__ void __launch_bounds__(128, B200_AO_MINBLOCKS) k_render_ao(const Samp
   PixelOut acc = {0, 0, 0, 0, INFINITY, INVALID_ID, INVALID_ID, INVALID_ID};
   for (int s = 0; s < p.spp; s++) {
     const uint32_t sid = start + s;
-    Ray ray = primaryRay(T, cam, pf, x, y, rcpW, rcpH, sid);
+    float2 scr;
+    Ray ray = primaryRay(T, cam, pf, x, y, rcpW, rcpH, sid, &scr);
+    if (p.maxDepth)
+      ray.tfar = fminf(ray.tfar, texMaxDepth(p.maxDepth, fmul(fadd(float(x), 0.5f), rcpW),
+                                             fmul(fadd(float(y), 0.5f), rcpH)));
+    const float2 cone = SURF ? cameraCone(cam, scr.x, scr.y, rcpH) : make_float2(0.f, 0.f);
+    float coneW = cone.x;
     const float tfar0 = ray.tfar;
     float o[4] = {0.f, 0.f, 0.f, 0.f};
     bool first = true;
@@ -120,33 +151,54 @@ __global__ void __launch_bounds__(128, B200_AO_MINBLOCKS) k_render_ao(const Samp
       }
       float bl[4];
       if (hit) {
-        const DG dg = postIntersect(sc, ray, h);
+        DGAttr at;
+        const DG dg = SURF ? postIntersect<true>(sc, ray, h, &at) : postIntersect(sc, ray, h);
+        float4 sc4 = make_float4(1.f, 1.f, 1.f, 1.f);
+        if (SURF) {
+          coneW += cone.y * h.t;  // World.ih postIntersect: t from the ray's origin
+          const uint32_t mi = sc.entries[h.entry].materialID;
+          const float fp = mi < uint32_t(p.nmats) && p.mats[mi].isObj && p.mats[mi].kdMap
+                               ? pixelFootprint(coneW, ray.dir, dg, at, p.mipBiasFactor)
+                               : 0.f;
+          sc4 = aoSurfaceColor(p, mi, at, fp);
+        }
         float intensity = fabsf(dot(dg.Ns, ray.dir));
+        if (SURF) intensity = fmul(intensity, sc4.w);
         if (p.aoSamples > 0 && p.aoIntensity > 0.01f) {
           const float ao = computeAO<STATS>(T, sc, dg, p.aoSamples, p.aoRadius, x, y, sid, &ts);
           intensity = fmul(intensity, fadd(fsub(1.f, p.aoIntensity), fmul(ao, p.aoIntensity)));
         }
-        bl[0] = bl[1] = bl[2] = intensity;
-        bl[3] = 1.f;
+        if (SURF) {
+          bl[0] = fmul(sc4.x, intensity);
+          bl[1] = fmul(sc4.y, intensity);
+          bl[2] = fmul(sc4.z, intensity);
+          bl[3] = sc4.w;
+        } else {
+          bl[0] = bl[1] = bl[2] = intensity;
+          bl[3] = 1.f;
+        }
         if (first) {
           z = h.t;
           prim = h.primID;
           geom = h.geomID;
           inst = h.instID;
           sn = dg.Ns;
-          sal = splat(1.f);  // AORenderer_computeShading: albedo = surface colour (white without material)
+          sal = mk(sc4.x, sc4.y, sc4.z);  // AORenderer_computeShading: albedo = surface colour
         }
         ray.tnear = fadd(h.t, dg.epsilon);
         ray.tfar = tfar0;
       } else {
-        bl[0] = p.bg[0];
-        bl[1] = p.bg[1];
-        bl[2] = p.bg[2];
-        bl[3] = p.bg[3];
+        const float4 bg = p.backplate ? texGetScreen(*p.backplate, fmul(fadd(float(x), 0.5f), rcpW),
+                                                     fmul(fadd(float(y), 0.5f), rcpH))
+                                      : make_float4(p.bg[0], p.bg[1], p.bg[2], p.bg[3]);
+        bl[0] = bg.x;
+        bl[1] = bg.y;
+        bl[2] = bg.z;
+        bl[3] = bg.w;
         if (first) {
           z = ray.tfar;
           sn = ray.dir;
-          sal = mk(p.bg[0], p.bg[1], p.bg[2]);
+          sal = mk(bg.x, bg.y, bg.z);
         }
       }
       const float f = fsub(1.f, o[3]);
@@ -220,12 +272,18 @@ cudaError_t launchPick(const Scene &sc, const CameraD &cam, float sx, float sy, 
 }
 
 cudaError_t launchRenderAO(const SamplerTables *T, const Scene &sc, const CameraD &cam, const PixelFilterD &pf, const AOParamsD &p,
-                           const FrameD &fb, bool stats, cudaStream_t st, KernelTimer *kt, const VolumeD *vol) {
+                           const FrameD &fb, bool stats, cudaStream_t st, KernelTimer *kt, const VolumeD *vol,
+                           bool surf) {
   dim3 grid((fb.W + 15) / 16, (fb.H + 7) / 8);
   KernelScope ks(kt, KK_AO, st);
   const VolumeD v = vol ? *vol : VolumeD{};
-  auto k = stats ? (vol ? k_render_ao<true, true> : k_render_ao<true, false>)
-                 : (vol ? k_render_ao<false, true> : k_render_ao<false, false>);
+  decltype(&k_render_ao<false, false, false>) k;
+  if (surf)
+    k = stats ? (vol ? k_render_ao<true, true, true> : k_render_ao<true, false, true>)
+              : (vol ? k_render_ao<false, true, true> : k_render_ao<false, false, true>);
+  else
+    k = stats ? (vol ? k_render_ao<true, true, false> : k_render_ao<true, false, false>)
+              : (vol ? k_render_ao<false, true, false> : k_render_ao<false, false, false>);
   k<<<grid, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(T, sc, cam, pf, p, fb, v);
   return cudaGetLastError();
 }

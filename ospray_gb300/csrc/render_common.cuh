@@ -105,13 +105,29 @@ B200_D float2 filterSample(const PixelFilterD &pf, float sx, float sy) {
 // screen position of sample `sid` of pixel (x, y): Halton(2), rotated
 // Halton(3), through the pixel filter
 B200_D Ray primaryRay(const SamplerTables *T, const CameraD &cam, const PixelFilterD &pf, int x, int y, float rcpW, float rcpH,
-                      uint32_t sid) {
+                      uint32_t sid, float2 *screen = nullptr) {
   const float ps_x = Halton_sample2(sid);
   const float ps_y = cpRotate(Halton_sample3(T, sid), 1.f / 6.f);
   const float2 pfs = filterSample(pf, ps_x, ps_y);
   const float cx = fmul(fadd(float(x), 0.5f), rcpW), cy = fmul(fadd(float(y), 0.5f), rcpH);
-  return cameraRay(cam, fadd(cx, fmul(pfs.x, rcpW)), fadd(cy, fmul(pfs.y, rcpH)));
+  const float sx = fadd(cx, fmul(pfs.x, rcpW)), sy = fadd(cy, fmul(pfs.y, rcpH));
+  if (screen) *screen = make_float2(sx, sy);
+  return cameraRay(cam, sx, sy);
 }
+
+// The camera ray's cone at screen position (sx, sy), in units of the frame
+// height (PathTracer.ispc:186-187): perspective 0 wide, widening by the
+// image plane height x rsqrt(|unnormalised direction|^2)
+// (PerspectiveCamera.ispc:58-63); orthographic as wide as the image height,
+// parallel (OrthographicCamera.ispc:52-53); panoramic pi sin(theta)
+// (PanoramicCamera.ispc:86-90).
+B200_D float2 cameraCone(const CameraD &c, float sx, float sy, float rcpH) {
+  if (c.type == 1) return make_float2(sqrtf(dot(c.dv_up, c.dv_up)) * rcpH, 0.f);
+  if (c.type == 2) return make_float2(0.f, 3.14159265358979323846f * sinf(3.14159265358979323846f * sy) * rcpH);
+  const V3 d = add(add(c.dir_00, mul(sx, c.du_size)), mul(sy, c.dv_up));
+  return make_float2(0.f, sqrtf(dot(c.dv_up, c.dv_up)) * rsqrtf(dot(d, d)) * rcpH);
+}
+
 
 struct DG {
   V3 P, Ng, Ns;

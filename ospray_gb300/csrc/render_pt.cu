@@ -148,19 +148,6 @@ B200_D PathRec genPT(const PtCtx &c, const CameraD &cam, const PixelFilterD &pf,
   return r;
 }
 
-// The camera ray's cone at screen position (sx, sy), in units of the frame
-// height (PathTracer.ispc:186-187): perspective 0 wide, widening by the
-// image plane height x rsqrt(|unnormalised direction|^2)
-// (PerspectiveCamera.ispc:58-63); orthographic as wide as the image height,
-// parallel (OrthographicCamera.ispc:52-53); panoramic pi sin(theta)
-// (PanoramicCamera.ispc:86-90).
-B200_D float2 cameraCone(const CameraD &c, float sx, float sy, float rcpH) {
-  if (c.type == 1) return make_float2(sqrtf(dot(c.dv_up, c.dv_up)) * rcpH, 0.f);
-  if (c.type == 2) return make_float2(0.f, PI_F * sinf(PI_F * sy) * rcpH);
-  const V3 d = add(add(c.dir_00, mul(sx, c.du_size)), mul(sy, c.dv_up));
-  return make_float2(0.f, sqrtf(dot(c.dv_up, c.dv_up)) * rsqrtf(dot(d, d)) * rcpH);
-}
-
 // appends one entry per lane that wants to, with one atomic per warp
 B200_D uint32_t warpAppend(bool want, uint32_t *counter) {
   const unsigned m = __ballot_sync(__activemask(), want);
@@ -194,6 +181,9 @@ __global__ void k_pt_generate(PtCtx c, CameraD cam, PixelFilterD pf, FrameInfo f
   if (!live) return;
   float2 scr;
   PathRec r = genPT(c, cam, pf, fi, pix % fi.W, pix / fi.W, s, 0u, &scr);
+  // Renderer_getMaxDepth at the sample's screen position (PathTracer.ispc:189-192):
+  // the camera ray's tfar, carried in org.w until the first hit sets the depth there
+  if (c.p.maxDepth) r.org.w = texMaxDepth(c.p.maxDepth, scr.x, scr.y);
   const float2 cone = cameraCone(cam, scr.x, scr.y, fi.rcpH);
   r.lastN.w = cone.x;
   r.meta2.y = __float_as_uint(cone.y);
@@ -224,6 +214,9 @@ struct ShadowMatD {
 // over the segment), and the lane restarts the same ray just past the hit,
 // until it reaches the light or is blocked.  The shadow record's fourth
 // contribution word then carries the path's medium (tnear is 0).
+#ifndef B200_REFILL_LANES
+#define B200_REFILL_LANES 8
+#endif
 template <bool SHADOW, bool STATS, bool BATCH, bool TRANSP = false>
 __global__ void __launch_bounds__(TRACE_BLOCK, BATCH ? B200_BATCH_TRACE_MINBLOCKS : B200_TRACE_MINBLOCKS) k_trace_queue(Scene sc, Workspace ws, const uint32_t *queue,
                                                             const uint32_t *count, uint32_t *fetch,
@@ -246,8 +239,10 @@ __global__ void __launch_bounds__(TRACE_BLOCK, BATCH ? B200_BATCH_TRACE_MINBLOCK
   int tdepth = 0;
   float tcone = 0.f;  // the path's ray cone width at the shadow ray's origin
   for (int guard = 0; guard < (1 << 30); guard++) {
+    // refill once at least B200_REFILL_LANES lanes wait (or no lane has a
+    // ray left), so the warp does not stop for every lane that finishes
     const unsigned need = __ballot_sync(0xffffffffu, !has && !exhausted);
-    if (need) {
+    if (need && (__popc(need) >= B200_REFILL_LANES || !__any_sync(0xffffffffu, has))) {
       const int leader = __ffs(need) - 1;
       uint32_t base = 0;
       if (lane == leader) base = atomicAdd(fetch, uint32_t(__popc(need)));
@@ -277,7 +272,8 @@ __global__ void __launch_bounds__(TRACE_BLOCK, BATCH ? B200_BATCH_TRACE_MINBLOCK
             r.org = mk(o.x, o.y, o.z);
             r.tnear = ws.paths[item].lastP.w;  // camera rays: nearClip; bounces: 0
             r.dir = mk(d.x, d.y, d.z);
-            r.tfar = INFINITY;
+            // camera rays: the maxDepth limit in org.w (infinite without one)
+            r.tfar = (ws.paths[item].meta.y & 0xffu) == 0u ? o.w : INFINITY;
             if (BATCH) bsc = reqs[ws.paths[item].meta2.y].c.sc;
           }
           tv.init(S, r, SHADOW && !TRANSP, &spill);
@@ -670,7 +666,7 @@ __global__ void __launch_bounds__(128, B200_SHADE_MINBLOCKS) k_pt_shade(PtCtx c,
       ray.dir = mk(dir4.x, dir4.y, dir4.z);
       ray.tfar = INFINITY;
       const bool hit = hb.a.w != 0.f;
-      const float t = hit ? hb.a.x : INFINITY;
+      const float t = hit ? hb.a.x : (v.depth == 0 ? org4.w : INFINITY);  // a miss of the camera ray: its tfar
       const V3 wo = -ray.dir;
       if (v.depth == 0) org4.w = t;
       if (!hit && v.straightPath) {
@@ -756,7 +752,8 @@ __global__ void __launch_bounds__(128, B200_SHADE_MINBLOCKS) k_pt_shade(PtCtx c,
               } else {
                 PrincipledBsdfT<ALLMAT> b;
                 if (ALLMAT)
-                  b.init(mat, fxv, fyv, dg.Ns, C.AT, opacity);
+                  b.init(mat, fxv, fyv, dg.Ns, C.AT, opacity,
+                         sameMedium(mediumOf(C.mats, v.medium), MediumD{1.f, splat(0.f)}));
                 else
                   b.init(mat, fxv, fyv, dg.Ns, C.AT);
                 scatterSurface<PrincipledBsdfT<ALLMAT>, NRC, ALLMAT>(C, b, mat, mi, dg, ray, t, wo, gp, org4, dir4,

@@ -9,8 +9,12 @@
 //   integrateVolumeIntervals   render/ao/volumes.ispc:32-240 (shadow/AO rays)
 //   integrateVolumeIntervalsGradient render/scivis/volumes.ispc:302-439
 //                              (gradient shading of volume samples)
-// One thread per pixel; surfaces carry no per-vertex colour, so dg.color is
-// (1, 1, 1, 1); a gradient-shaded volume sample passes its transfer-function
+//   ray cones, map_maxDepth    render/RendererRenderTaskFn.inl:40-72
+//   background, backplate      render/Renderer.ispc:19-40
+// One thread per pixel.  ATTR (a mesh has vertex attributes or a material a
+// map_kd): dg.color is the interpolated vertex colour and obj map_kd is
+// looked up with the ray cone's footprint; otherwise dg.color is
+// (1, 1, 1, 1).  A gradient-shaded volume sample passes its transfer-function
 // RGBA.  Volume-only worlds without gradient shading use
 // k_render_scivis_volume.
 #include "kernels.h"
@@ -32,7 +36,9 @@ struct SvBSDF {
 // material slot of a surface hit; ~0u (no material) for volume samples
 B200_D uint32_t svMaterialSlot(const Scene &sc, uint32_t entry) { return sc.entries[entry].materialID; }
 
-B200_D SvBSDF svEvalMaterial(const ScivisSurfD &S, uint32_t mi, float4 color) {
+// at (with footprint fp) addresses the obj map_kd; null: no lookup
+B200_D SvBSDF svEvalMaterial(const ScivisSurfD &S, uint32_t mi, float4 color, const DGAttr *at = nullptr,
+                             float fp = 0.f) {
   SvBSDF r;
   r.diffuse = mk(color.x, color.y, color.z);
   r.specular = splat(0.f);
@@ -42,8 +48,13 @@ B200_D SvBSDF svEvalMaterial(const ScivisSurfD &S, uint32_t mi, float4 color) {
   if (mi < uint32_t(S.nmats)) {
     const ScivisMatD m = S.mats[mi];
     if (m.isObj) {
-      const float d = m.d * color.w;
+      float d = m.d * color.w;
       r.diffuse = r.diffuse * mk(m.kd[0], m.kd[1], m.kd[2]);
+      if (at && m.kdMap) {
+        const float4 t = texGet(*m.kdMap, at->s, at->t, fp);
+        r.diffuse = r.diffuse * mk(t.x, t.y, t.z);
+        d *= t.w;
+      }
       r.diffuse = r.diffuse * d;
       r.specular = d * mk(m.ks[0], m.ks[1], m.ks[2]);
       r.shininess = m.ns;
@@ -61,9 +72,11 @@ B200_D SvBSDF svEvalMaterial(const ScivisSurfD &S, uint32_t mi, float4 color) {
 
 // Transmission of a shadow or AO ray through translucent surfaces and the
 // volume; any-hit when every material is opaque and there is no volume.
-template <bool STATS>
+// cone: the shadow cone (width at the origin, dwdt), restarted from the
+// origin's width after every surface (lightAlpha.ispc:30,105).
+template <bool STATS, bool ATTR>
 B200_D V3 svLightAlpha(const Scene &sc, const VolumeD &vol, const ScivisSurfD &S, float samplingRate, Ray ray,
-                       PCG &rs, V3 weight, float quality, TraceStats *ts) {
+                       PCG &rs, V3 weight, float quality, TraceStats *ts, float2 cone, float mipBias) {
   if (S.opaqueShadows) {
     HitRec h;
     return traceScene<true, STATS>(sc, ray, h, ts) ? splat(0.f) : splat(1.f);
@@ -82,8 +95,17 @@ B200_D V3 svLightAlpha(const Scene &sc, const VolumeD &vol, const ScivisSurfD &S
       }
     }
     if (!hit) break;
-    const DG dg = postIntersect(sc, ray, h);
-    alpha = alpha * svEvalMaterial(S, svMaterialSlot(sc, dg.entry), make_float4(1.f, 1.f, 1.f, 1.f)).transmission;
+    DGAttr at;
+    const DG dg = ATTR ? postIntersect<true>(sc, ray, h, &at) : postIntersect(sc, ray, h);
+    const uint32_t mi = svMaterialSlot(sc, dg.entry);
+    if (ATTR) {
+      const float fp = mi < uint32_t(S.nmats) && S.mats[mi].kdMap
+                           ? pixelFootprint(cone.x + cone.y * h.t, ray.dir, dg, at, mipBias)
+                           : 0.f;
+      alpha = alpha * svEvalMaterial(S, mi, at.color, &at, fp).transmission;
+    } else {
+      alpha = alpha * svEvalMaterial(S, mi, make_float4(1.f, 1.f, 1.f, 1.f)).transmission;
+    }
     ray.tnear = h.t + dg.epsilon;
     ray.tfar = orgTMax;
     if (luminance(alpha * weight) < S.minContribution) {
@@ -94,9 +116,10 @@ B200_D V3 svLightAlpha(const Scene &sc, const VolumeD &vol, const ScivisSurfD &S
   return alpha;
 }
 
-template <bool STATS>
+template <bool STATS, bool ATTR>
 B200_D V3 svComputeAO(const SamplerTables *T, const Scene &sc, const VolumeD &vol, const ScivisSurfD &S,
-                      float samplingRate, const DG &dg, int px, int py, uint32_t sampleZ, PCG &rs, TraceStats *ts) {
+                      float samplingRate, const DG &dg, int px, int py, uint32_t sampleZ, PCG &rs, TraceStats *ts,
+                      float coneWidth, float mipBias) {
   const uint32_t accumID = sampleZ * uint32_t(S.aoSamples);
   const AOBasis B = aoBasis(dg, px, py);
   V3 hits = splat(0.f);
@@ -111,7 +134,8 @@ B200_D V3 svComputeAO(const SamplerTables *T, const Scene &sc, const VolumeD &vo
     r.tnear = dg.epsilon;
     r.dir = dir;
     r.tfar = S.aoRadius;
-    hits = hits + (splat(1.f) - svLightAlpha<STATS>(sc, vol, S, samplingRate, r, rs, splat(1.f), 0.1f, ts));
+    hits = hits + (splat(1.f) - svLightAlpha<STATS, ATTR>(sc, vol, S, samplingRate, r, rs, splat(1.f), 0.1f, ts,
+                                                          make_float2(coneWidth, 0.f), mipBias));
   }
   return splat(1.f) - hits * (1.f / float(S.aoSamples));
 }
@@ -126,11 +150,14 @@ struct SvShading {
 // directIllumination: Blinn-Phong over the non-ambient lights (area lights
 // sampled at their centre), hard shadows through lightAlpha, AO tinted by the
 // ambient lights x pi.
-template <bool STATS>
+// at / fp: the hit's attributes and footprint (map_kd); coneWidth: the ray
+// cone's width at the hit (the shadow and AO cones start with it)
+template <bool STATS, bool ATTR>
 B200_D SvShading svComputeShading(const SamplerTables *T, const Scene &sc, const VolumeD &vol, const ScivisSurfD &S,
                                   float samplingRate, const DG &dg, uint32_t mi, float4 dgColor, V3 inDir, int x,
-                                  int y, uint32_t sid, PCG &rs, TraceStats *ts) {
-  const SvBSDF bsdf = svEvalMaterial(S, mi, dgColor);
+                                  int y, uint32_t sid, PCG &rs, TraceStats *ts, const DGAttr *at, float fp,
+                                  float coneWidth, float mipBias) {
+  const SvBSDF bsdf = svEvalMaterial(S, mi, dgColor, at, fp);
   V3 color = splat(0.f);
   for (int i = S.numVisibleOnly; i < S.nlights; i++) {
     const LightSampleD ls = sampleLight(S.lights[i], dg.P, dg.Ng, dg.Ns, 0.f, 0.f);
@@ -151,7 +178,8 @@ B200_D SvShading svComputeShading(const SamplerTables *T, const Scene &sc, const
           sr.tnear = 0.f;
           sr.dir = ls.dir;
           sr.tfar = ls.dist;
-          const V3 la = svLightAlpha<STATS>(sc, vol, S, samplingRate, sr, rs, contrib, 0.25f, ts);
+          const V3 la = svLightAlpha<STATS, ATTR>(sc, vol, S, samplingRate, sr, rs, contrib, 0.25f, ts,
+                                                  make_float2(coneWidth, -coneWidth * (1.f / ls.dist)), mipBias);
           color = color + la * contrib;
         }
       } else {
@@ -162,7 +190,7 @@ B200_D SvShading svComputeShading(const SamplerTables *T, const Scene &sc, const
   const V3 aoColorPi = S.aoColor * 3.14159265358979323846f;
   V3 ao = splat(1.f);
   if (S.aoSamples > 0 && luminance(aoColorPi) > S.minContribution)
-    ao = svComputeAO<STATS>(T, sc, vol, S, samplingRate, dg, x, y, sid, rs, ts);
+    ao = svComputeAO<STATS, ATTR>(T, sc, vol, S, samplingRate, dg, x, y, sid, rs, ts, coneWidth, mipBias);
   color = color + bsdf.diffuse * ao * aoColorPi;
   SvShading r;
   r.color = color;
@@ -178,10 +206,10 @@ B200_D SvShading svComputeShading(const SamplerTables *T, const Scene &sc, const
 // function RGBA, Ns = Ng = -normalize(gradient), epsilon = dt / 2) and
 // blended into the sample by gradientShadingScale before the Beer-law
 // opacity.  The shading's shadow and AO rays draw from the ray's sampler.
-template <bool STATS>
+template <bool STATS, bool ATTR>
 B200_D float4 integrateShaded(const SamplerTables *T, const Scene &sc, const VolumeD &vol, const ScivisSurfD &S,
                               float samplingRate, const Ray &wray, float jitter, int x, int y, uint32_t sid, PCG &rs,
-                              uint32_t &samples, TraceStats *ts) {
+                              uint32_t &samples, TraceStats *ts, float mipBias) {
   const Ray ray = toVolume(vol, wray);  // sampling in volume space, shading in world space
   SampleWalk w;
   w.init(vol, ray, jitter, samplingRate);
@@ -203,8 +231,9 @@ B200_D float4 integrateShaded(const SamplerTables *T, const Scene &sc, const Vol
           dg.Ns = dg.Ng = fnormalize(vol.identity ? ng : xfmVectorT(vol.rcp, ng));
           dg.epsilon = dt / 2.f;
           dg.entry = ~0u;
-          const SvShading sh = svComputeShading<STATS>(T, sc, vol, S, samplingRate, dg, ~0u, c, wray.dir, x, y, sid,
-                                                       rs, ts);
+          // (no cone width for volume samples, volumes.ispc:408-416)
+          const SvShading sh = svComputeShading<STATS, ATTR>(T, sc, vol, S, samplingRate, dg, ~0u, c, wray.dir, x, y,
+                                                             sid, rs, ts, nullptr, 0.f, 0.f, mipBias);
           const float a = 1.f - luminance(sh.transmission), f = vol.gradientShadingScale;
           c = make_float4(lerpF(f, c.x, sh.color.x), lerpF(f, c.y, sh.color.y), lerpF(f, c.z, sh.color.z),
                           lerpF(f, c.w, a));
@@ -221,7 +250,7 @@ B200_D float4 integrateShaded(const SamplerTables *T, const Scene &sc, const Vol
 
 // SHADED: the volume is gradient shaded (an instantiation of its own, so the
 // common path keeps its registers)
-template <bool STATS, bool SHADED>
+template <bool STATS, bool SHADED, bool ATTR>
 __global__ void __launch_bounds__(128) k_render_scivis_surfaces(const SamplerTables *T, Scene sc, VolumeD vol,
                                                                 CameraD cam, PixelFilterD pf, ScivisParamsD p,
                                                                 ScivisSurfD S, FrameD fb) {
@@ -234,7 +263,12 @@ __global__ void __launch_bounds__(128) k_render_scivis_surfaces(const SamplerTab
     PixelOut acc = {0.f, 0.f, 0.f, 0.f, INFINITY, INVALID_ID, INVALID_ID, INVALID_ID};
     for (int s = 0; s < p.spp; s++) {
       const uint32_t sid = start + uint32_t(s);
-      Ray ray = primaryRay(T, cam, pf, x, y, rcpW, rcpH, sid);
+      float2 scr;
+      Ray ray = primaryRay(T, cam, pf, x, y, rcpW, rcpH, sid, &scr);
+      const float cx = fmul(fadd(float(x), 0.5f), rcpW), cy = fmul(fadd(float(y), 0.5f), rcpH);
+      if (p.maxDepth) ray.tfar = fminf(ray.tfar, texMaxDepth(p.maxDepth, cx, cy));
+      const float2 cone = ATTR ? cameraCone(cam, scr.x, scr.y, rcpH) : make_float2(0.f, 0.f);
+      float coneW = cone.x;
       PCG rs;
       rs.init(uint32_t(x + fb.W * y), sid);
       bool firstHit = true, allTrans = true;
@@ -254,8 +288,8 @@ __global__ void __launch_bounds__(128) k_render_scivis_surfaces(const SamplerTab
           if (volumeOverlaps(vol, vr)) {
             const float jitter = rs.getFloat();
             const float4 vc = SHADED
-                                  ? integrateShaded<STATS>(T, sc, vol, S, p.samplingRate, vr, jitter, x, y, sid, rs,
-                                                           vsamples, &ts)
+                                  ? integrateShaded<STATS, ATTR>(T, sc, vol, S, p.samplingRate, vr, jitter, x, y, sid,
+                                                                 rs, vsamples, &ts, p.mipBiasFactor)
                                   : integrate(vol, vr, jitter, p.samplingRate, S.minContribution, vsamples);
             outColor = outColor + outT * mk(vc.x, vc.y, vc.z);
             outT = outT * vc.w;
@@ -273,13 +307,23 @@ __global__ void __launch_bounds__(128) k_render_scivis_surfaces(const SamplerTab
         }
         if (firstHit || allTrans) z = rayT;
         if (!hit) {
-          outColor = outColor + outT * mk(p.bg[0], p.bg[1], p.bg[2]);
-          outT = outT * (1.f - p.bg[3]);
+          const float4 bg = p.backplate ? texGetScreen(*p.backplate, cx, cy)
+                                        : make_float4(p.bg[0], p.bg[1], p.bg[2], p.bg[3]);
+          outColor = outColor + outT * mk(bg.x, bg.y, bg.z);
+          outT = outT * (1.f - bg.w);
           break;
         }
-        const DG dg = postIntersect(sc, ray, h);
-        const SvShading sh = svComputeShading<STATS>(T, sc, vol, S, p.samplingRate, dg, svMaterialSlot(sc, dg.entry),
-                                                     make_float4(1.f, 1.f, 1.f, 1.f), ray.dir, x, y, sid, rs, &ts);
+        DGAttr at;
+        const DG dg = ATTR ? postIntersect<true>(sc, ray, h, &at) : postIntersect(sc, ray, h);
+        const uint32_t mi = svMaterialSlot(sc, dg.entry);
+        float fp = 0.f;
+        if (ATTR) {
+          coneW += cone.y * h.t;  // World.ih postIntersect: t from the ray's origin
+          if (mi < uint32_t(S.nmats) && S.mats[mi].kdMap) fp = pixelFootprint(coneW, ray.dir, dg, at, p.mipBiasFactor);
+        }
+        const SvShading sh = svComputeShading<STATS, ATTR>(
+            T, sc, vol, S, p.samplingRate, dg, mi, ATTR ? at.color : make_float4(1.f, 1.f, 1.f, 1.f), ray.dir, x, y,
+            sid, rs, &ts, ATTR ? &at : nullptr, fp, coneW, p.mipBiasFactor);
         if (firstHit || allTrans) {
           sn = dg.Ns;
           sal = sh.albedo;
@@ -331,8 +375,13 @@ cudaError_t launchRenderScivisSurfaces(const SamplerTables *T, const Scene &sc, 
   dim3 grid((fb.W + 15) / 16, (fb.H + 7) / 8);
   KernelScope ks(kt, KK_SCIVIS, st);
   const bool shaded = S.hasVolume && vol.gradientShadingScale > 0.f;
-  auto k = stats ? (shaded ? k_render_scivis_surfaces<true, true> : k_render_scivis_surfaces<true, false>)
-                 : (shaded ? k_render_scivis_surfaces<false, true> : k_render_scivis_surfaces<false, false>);
+  decltype(&k_render_scivis_surfaces<false, false, false>) k;
+  if (S.attrs)
+    k = stats ? (shaded ? k_render_scivis_surfaces<true, true, true> : k_render_scivis_surfaces<true, false, true>)
+              : (shaded ? k_render_scivis_surfaces<false, true, true> : k_render_scivis_surfaces<false, false, true>);
+  else
+    k = stats ? (shaded ? k_render_scivis_surfaces<true, true, false> : k_render_scivis_surfaces<true, false, false>)
+              : (shaded ? k_render_scivis_surfaces<false, true, false> : k_render_scivis_surfaces<false, false, false>);
   k<<<grid, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(T, sc, vol, cam, pf, p, S, fb);
   return cudaGetLastError();
 }

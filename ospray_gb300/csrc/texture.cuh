@@ -194,8 +194,16 @@ B200_D float4 texGet(const TextureD &t, float s, float u, float footprint) {
   return lerp4(frac, a, b);
 }
 
+// Renderer_getMaxDepth (render/Renderer.ispc:30-40): max(0, red) of the
+// renderer's maxDepth texture at a screen position; no texture: no limit.
+// (The renderer-level lookups are out of line so the texel decoding does not
+// count against the register budget of the kernels that call them.)
+static __device__ __noinline__ float texMaxDepth(const TextureD *t, float sx, float sy) {
+  return t ? fmaxf(0.f, texGet(*t, sx, sy, 0.f).x) : INFINITY;
+}
+
 // clamp2edge + a level-0 lookup (the renderer's backplate at a screen position)
-B200_D float4 texGetScreen(const TextureD &t, float sx, float sy) {
+static __device__ __noinline__ float4 texGetScreen(const TextureD &t, float sx, float sy) {
   const float hx = (1.f / float(t.w)) * 0.5f, hy = (1.f / float(t.h)) * 0.5f;
   return texGet(t, fminf(fmaxf(sx, hx), 1.f - hx), fminf(fmaxf(sy, hy), 1.f - hy), 0.f);
 }

@@ -63,14 +63,16 @@ def pick(scene, cam, x, y):
 class OrPtParams(ctypes.Structure):
     _fields_ = [("spp", I), ("maxPathLength", I), ("roulettePathLength", I), ("maxScatteringEvents", I),
                 ("lightSamples", I), ("limitIndirectLightSamples", I), ("minContribution", F),
-                ("maxContribution", F), ("bg", F * 4), ("pixelFilter", I), ("backplate", P), ("mipMapBias", F)]
+                ("maxContribution", F), ("bg", F * 4), ("pixelFilter", I), ("backplate", P), ("mipMapBias", F),
+                ("maxDepth", P)]
 
 
 def pt_params(spp=1, max_path_length=20, roulette_path_length=5, max_scattering_events=20, light_samples=-1,
               limit_indirect=True, min_contribution=0.001, max_contribution=float("inf"), bg=(0, 0, 0, 0),
-              pixel_filter=2, backplate=None, mip_map_bias=0.0):
-    """backplate: an OrTexture or None."""
+              pixel_filter=2, backplate=None, mip_map_bias=0.0, max_depth=None):
+    """backplate / max_depth: OrTextures or None."""
     p = OrPtParams()
+    p.maxDepth = None if max_depth is None else max_depth.h
     p.backplate = None if backplate is None else backplate.h
     p.mipMapBias = float(mip_map_bias)
     p.spp, p.maxPathLength, p.roulettePathLength = spp, max_path_length, roulette_path_length
@@ -84,11 +86,12 @@ def pt_params(spp=1, max_path_length=20, roulette_path_length=5, max_scattering_
 
 # the reference's material parameter defaults per type (Principled.cpp:37-79,
 # OBJ.cpp:28-38, Metal.cpp:27-31 with math/spectrum.h's aluminium, Glass.cpp:27-38,
-# ThinGlass.cpp:27-33), in the 24-float order of or_pt_add_material2
+# ThinGlass.cpp:27-33), in the 31-float order of or_pt_add_material2
 MATERIAL_TYPES = {"principled": 0, "obj": 1, "metal": 2, "glass": 3, "thinGlass": 4}
 _MAT_FIELDS = [("baseColor", 3), ("roughness", 1), ("metallic", 1), ("opacity", 1), ("ks", 3), ("ns", 1),
                ("tf", 3), ("eta", 3), ("k", 3), ("attenuationColor", 3), ("attenuationDistance", 1),
-               ("thickness", 1)]
+               ("thickness", 1), ("specular", 1), ("ior", 1), ("diffuse", 1), ("edgeColor", 3),
+               ("specularMetallic", 1)]
 _MAT_DEFAULTS = {
     0: dict(baseColor=(0.8, 0.8, 0.8)),
     1: dict(baseColor=(0.8, 0.8, 0.8), ns=10.0),
@@ -99,9 +102,10 @@ _MAT_DEFAULTS = {
 
 
 def material_floats(m):
-    """(type, 24 floats) of a material dict, the reference's defaults filled in."""
+    """(type, 31 floats) of a material dict, the reference's defaults filled in."""
     t = MATERIAL_TYPES[m.get("type", "principled")]
-    vals = dict(opacity=1.0, attenuationColor=(1.0, 1.0, 1.0), attenuationDistance=1.0, thickness=1.0, ns=10.0)
+    vals = dict(opacity=1.0, attenuationColor=(1.0, 1.0, 1.0), attenuationDistance=1.0, thickness=1.0, ns=10.0,
+                specular=1.0, ior=1.0, diffuse=1.0, edgeColor=(1.0, 1.0, 1.0), specularMetallic=1.0)
     vals.update(_MAT_DEFAULTS[t])
     vals.update({k: v for k, v in m.items() if k != "type"})
     out = []
@@ -274,7 +278,7 @@ def lib():
         L.or_trace.argtypes = [P, P, I, I, P, P, I]
         L.or_camera_rays.argtypes = [ctypes.POINTER(OrCamera), I, I, I, I, I, P]
         L.or_render_ao.argtypes = [P, ctypes.POINTER(OrCamera), I, I, I, I, I, F, F, P, I,
-                                   ctypes.POINTER(OrFrame), I]
+                                   ctypes.POINTER(OrFrame), I, ctypes.POINTER(OrAoExtra)]
         L.or_tables.argtypes = [P, P, P, P]
         L.or_frame_post.argtypes = [P, ctypes.c_longlong, I, ctypes.POINTER(OrToneMapper), P]
         L.or_tonemap_coefficients.argtypes = [ctypes.POINTER(OrToneMapper), P]
@@ -357,15 +361,43 @@ def camera_rays(cam, pixel_filter, w, h, spp=1, frame_id=0):
     return out
 
 
+class OrAoExtra(ctypes.Structure):
+    _fields_ = [("backplate", P), ("maxDepth", P), ("mipMapBias", F), ("materials", P), ("nmaterials", I)]
+
+
+def _scivis_material_array(materials):
+    M = (OrScivisMaterial * max(1, len(materials)))()
+    for i, m in enumerate(materials):
+        if m is None:
+            continue
+        M[i].isObj = 1
+        M[i].kd[:] = [float(x) for x in m.get("kd", (0.8, 0.8, 0.8))]
+        M[i].ks[:] = [float(x) for x in m.get("ks", (0, 0, 0))]
+        M[i].ns, M[i].d = float(m.get("ns", 10.0)), float(m.get("d", 1.0))
+        M[i].tf[:] = [float(x) for x in m.get("tf", (0, 0, 0))]
+        M[i].kdMap = None if m.get("map_kd") is None else m["map_kd"].h
+    return M
+
+
 def render_ao(scene, cam, pixel_filter, w, h, spp=1, ao_samples=1, ao_radius=1e20, ao_intensity=1.0,
-              bg=(0, 0, 0, 0), frames=1, nthreads=0):
+              bg=(0, 0, 0, 0), frames=1, nthreads=0, backplate=None, max_depth=None, mip_map_bias=0.0,
+              materials=None):
+    """materials: obj material dicts (kd, d, map_kd an OrTexture) or None per slot;
+    backplate / max_depth: OrTextures."""
+    x = OrAoExtra()
+    x.backplate = None if backplate is None else backplate.h
+    x.maxDepth = None if max_depth is None else max_depth.h
+    x.mipMapBias = float(mip_map_bias)
+    M = _scivis_material_array(materials or [])
+    x.materials = ctypes.cast(M, P) if materials else None
+    x.nmaterials = len(materials) if materials else 0
     color = np.zeros((h, w, 4), np.float32)
     depth = np.zeros((h, w), np.float32)
     ids = [np.zeros((h, w), np.uint32) for _ in range(3)]
     fr = OrFrame(color.ctypes.data, depth.ctypes.data, ids[0].ctypes.data, ids[1].ctypes.data, ids[2].ctypes.data)
     bgv = np.asarray(bg, np.float32)
     lib().or_render_ao(scene.h, ctypes.byref(cam), pixel_filter, w, h, spp, ao_samples, ao_radius, ao_intensity,
-                       _p(bgv), frames, ctypes.byref(fr), nthreads)
+                       _p(bgv), frames, ctypes.byref(fr), nthreads, ctypes.byref(x))
     return dict(color=color, depth=depth, primID=ids[0], geomID=ids[1], instID=ids[2])
 
 
@@ -455,18 +487,20 @@ class OrScivisLight(ctypes.Structure):
 
 class OrScivisMaterial(ctypes.Structure):
     _fields_ = [("isObj", ctypes.c_int), ("kd", ctypes.c_float * 3), ("ks", ctypes.c_float * 3),
-                ("ns", ctypes.c_float), ("d", ctypes.c_float), ("tf", ctypes.c_float * 3)]
+                ("ns", ctypes.c_float), ("d", ctypes.c_float), ("tf", ctypes.c_float * 3), ("kdMap", P)]
 
 
 class OrScivisParams(ctypes.Structure):
     _fields_ = [("spp", ctypes.c_int), ("samplingRate", ctypes.c_float), ("bg", ctypes.c_float * 4),
                 ("shadows", ctypes.c_int), ("visibleLights", ctypes.c_int), ("aoSamples", ctypes.c_int),
-                ("aoRadius", ctypes.c_float), ("minContribution", ctypes.c_float), ("pixelFilter", ctypes.c_int)]
+                ("aoRadius", ctypes.c_float), ("minContribution", ctypes.c_float), ("pixelFilter", ctypes.c_int),
+                ("backplate", P), ("maxDepth", P), ("mipMapBias", F)]
 
 
 def render_scivis(scene, volume, cam, lights, materials, w, h, spp=1, pixel_filter=2, sampling_rate=1.0,
                   bg=(0, 0, 0, 0), shadows=False, visible_lights=False, ao_samples=0, ao_radius=1e20,
-                  min_contribution=0.001, frames=1, rows=None, nthreads=0):
+                  min_contribution=0.001, frames=1, rows=None, nthreads=0, backplate=None, max_depth=None,
+                  mip_map_bias=0.0):
     """SciVis over a world with surfaces (and optionally `volume`, a
     VolumeModel); scene None renders the volume alone through the same
     integrator (gradient shading included).  lights: dicts as PtWorld takes them (+ "visible");
@@ -493,16 +527,11 @@ def render_scivis(scene, volume, cam, lights, materials, w, h, spp=1, pixel_filt
             L[i].penumbraAngle = float(l.get("penumbra_angle", 5.0))
             L[i].radius = float(l.get("radius", 0.0))
             L[i].innerRadius = float(l.get("inner_radius", 0.0))
-    M = (OrScivisMaterial * max(1, len(materials)))()
-    for i, m in enumerate(materials):
-        if m is None:
-            continue
-        M[i].isObj = 1
-        M[i].kd[:] = [float(x) for x in m.get("kd", (0.8, 0.8, 0.8))]
-        M[i].ks[:] = [float(x) for x in m.get("ks", (0, 0, 0))]
-        M[i].ns, M[i].d = float(m.get("ns", 10.0)), float(m.get("d", 1.0))
-        M[i].tf[:] = [float(x) for x in m.get("tf", (0, 0, 0))]
+    M = _scivis_material_array(materials)
     p = OrScivisParams()
+    p.backplate = None if backplate is None else backplate.h
+    p.maxDepth = None if max_depth is None else max_depth.h
+    p.mipMapBias = float(mip_map_bias)
     p.spp, p.samplingRate = int(spp), float(sampling_rate)
     p.bg[:] = [float(x) for x in bg]
     p.shadows, p.visibleLights, p.aoSamples = int(bool(shadows)), int(bool(visible_lights)), int(ao_samples)

@@ -184,3 +184,23 @@ def _api_vs_abi(og, osp, scenes, b200_device):
     abi_img = fb.read(og.FB_COLOR)
     assert abi_img[..., :3].mean() > 0.0
     np.testing.assert_allclose(api_img, abi_img, rtol=1e-5, atol=1e-6)
+
+
+def test_principled_parameters_match_oracle(mat_scene, b200_device):
+    """Principled's ior and specular (the dielectric coating), diffuse,
+    edgeColor and specularMetallic, and roughness 0 (a smooth coating over
+    Lambert and a smooth conductor: Dirac lobes, Principled.ispc:146-331,
+    DielectricLayer.ih, Conductor.ih) against the oracle."""
+    import ospray_gb300 as og
+    d, g, o, _ = mat_scene
+    kinds = [og.principled((0.7, 0.3, 0.2), 0.3, 0.0, ior=1.5, specular=0.7),
+             og.principled((0.2, 0.5, 0.8), 0.0, 0.0, ior=1.45),
+             og.principled((0.9, 0.6, 0.3), 0.0, 1.0, edge_color=(0.9, 0.5, 0.3)),
+             og.principled((0.6, 0.6, 0.6), 0.25, 1.0, edge_color=(0.4, 0.8, 0.9), specular=0.4,
+                           specular_metallic=False),
+             og.principled((0.5, 0.8, 0.3), 0.5, 0.4, ior=2.0, diffuse=0.5),
+             og.principled((0.8, 0.8, 0.2), 0.0, 0.0, ior=1.6, specular=0.0),
+             og.principled((0.3, 0.7, 0.7), 0.15, 0.0, ior=1.3, opacity=0.6)]
+    mats = [kinds[i % len(kinds)] for i in range(len(d["xfm"]))] + [(0.8, 0.8, 0.8, 1.0, 0.0)]
+    gpu, ref = _render(og, b200_device, g, o, d, mats, spp=4)
+    _compare(gpu, ref, 0.995)
