@@ -189,13 +189,20 @@ B200_D bool planeTest(V3 org, V3 d, float tnear, float tfar, const float4 *p, fl
 }
 
 // the disc and plane tests by type (out of line: the triangle and sphere
-// tests of the traversal loop keep their registers); Ng from userNormal
-static __device__ __noinline__ bool userTest(uint32_t type, V3 org, V3 d, float tnear, float tfar, const float4 *prims,
-                                      uint32_t slot, float &t) {
-  if (type == GEOM_DISCS) return discTest(org, d, tnear, tfar, __ldg(prims + slot), t);
-  if (type == GEOM_ORIENTED_DISCS)
-    return orientedDiscTest(org, d, tnear, tfar, __ldg(prims + 2 * slot), __ldg(prims + 2 * slot + 1), t);
-  return planeTest(org, d, tnear, tfar, prims + 3 * slot, t);
+// tests of the traversal loop keep their registers); the hit distance, NaN
+// for no hit (a value, not a reference, so no local of the loop lives in
+// memory); Ng from userNormal
+static __device__ __noinline__ float userTest(uint32_t type, V3 org, V3 d, float tnear, float tfar,
+                                              const float4 *prims, uint32_t slot) {
+  float t = 0.f;
+  bool h;
+  if (type == GEOM_DISCS)
+    h = discTest(org, d, tnear, tfar, __ldg(prims + slot), t);
+  else if (type == GEOM_ORIENTED_DISCS)
+    h = orientedDiscTest(org, d, tnear, tfar, __ldg(prims + 2 * slot), __ldg(prims + 2 * slot + 1), t);
+  else
+    h = planeTest(org, d, tnear, tfar, prims + 3 * slot, t);
+  return h ? t : __int_as_float(0x7fffffff);
 }
 static __device__ __noinline__ V3 userNormal(uint32_t type, V3 d, const float4 *prims, uint32_t slot) {
   if (type == GEOM_DISCS) return neg(d);
@@ -553,7 +560,8 @@ struct Traverser {
           V3 Ng;
           h = sphTest(org, dir, ray.tnear, ht, __ldg(prims + slot), t, Ng);
         } else {
-          h = userTest(etype, org, dir, ray.tnear, ht, prims, slot, t);
+          t = userTest(etype, org, dir, ray.tnear, ht, prims, slot);
+          h = !isnan(t);
         }
         prim = __ldg(primIDs + slot);
       }
