@@ -407,13 +407,16 @@ class BatchWorkload:
     """Batched serving: 64 requests (resolution uniform over 256^2, 512^2,
     768^2, 1024^2, 1280x720; spp uniform in 1..8; AO or path tracer with
     probability 1/2; each on its own seeded height field of 65k-1M triangles
-    plus 1,000 spheres) rendered as one batched wavefront per step, replayed
-    as a CUDA graph, launch shape chosen by the autotuner at setup.  Reports
-    aggregate Mrays/s, and per-request latency (p50/p99 of completion times
-    after the render starts) of the batch and of the same requests rendered
-    one after another with single-request calls."""
+    plus 1,000 spheres) rendered as one batched wavefront per step: the
+    wavefront kernels replayed as a CUDA graph (mode "graph") or one
+    cooperative persistent launch (mode "persistent"), launch shape chosen by
+    the autotuner at setup.  Reports aggregate Mrays/s, and per-request
+    latency (p50/p99 of completion times after the render starts) of the
+    batch and of the same requests rendered one after another with
+    single-request calls."""
     name = "batch_64_requests"
     metric = "Mrays/s"
+    mode = "graph"
 
     def __init__(self, count=64, seed=0):
         from ospray_gb300 import scenes
@@ -463,16 +466,29 @@ class BatchWorkload:
             c = it["scene"].counters(reset=True)
             rays, nodes, tri, sph = rays + c[0], nodes + c[1], tri + c[2], sph + c[3]
         self.per_ray = (nodes / max(rays, 1), tri / max(rays, 1), sph / max(rays, 1))
+        self.set_mode(self.mode)
+        self.fb = self.items[0]["fb"]
+        self.colors = [np.empty((it["req"]["height"], it["req"]["width"], 4), np.float32) for it in self.items]
+        self._rays = 0
+
+    def _mode(self):
+        return self.og.BATCH_PERSISTENT if self.mode == "persistent" else self.og.BATCH_GRAPH
+
+    def set_mode(self, mode):
+        """Switches the batch's launch mode and autotunes for it (the
+        persistent launch tunes the wave size only)."""
+        self.mode = mode
+        self.batch.render(mode=self._mode())  # the mode the autotuner tunes for
         t1 = time.perf_counter()
         best = self.batch.autotune(candidates=int(os.environ.get("B200_BATCH_TUNE_CANDIDATES", "6")))
-        self.batch.render()
+        self.batch.render(mode=self._mode())
+        self.config["mode"] = mode
         self.config["plan"] = self.batch.info()
         self.config["autotune"] = {"wavePaths": int(best.wavePaths), "traceBlocksPerSM": best.traceBlocksPerSM,
                                    "shadeBlocksPerSM": best.shadeBlocksPerSM,
                                    "seconds": round(time.perf_counter() - t1, 2)}
-        self.fb = self.items[0]["fb"]
-        self.colors = [np.empty((it["req"]["height"], it["req"]["width"], 4), np.float32) for it in self.items]
-        self._rays = 0
+        if mode == "persistent":  # one grid of every co-resident block
+            del self.config["autotune"]["traceBlocksPerSM"], self.config["autotune"]["shadeBlocksPerSM"]
 
     def kernels_per_frame(self):
         return self.batch.info()["kernels"]
@@ -486,12 +502,12 @@ class BatchWorkload:
             self.og.render_pt(it["scene"], it["cam"], p, it["mats"], fb)
 
     def step(self, stats=False):
-        self.batch.render(use_graph=True)
+        self.batch.render(mode=self._mode())
         if stats:
             self._rays += self.batch.timings()[1]
 
     def e2e_step(self):
-        self.batch.render(use_graph=True)
+        self.batch.render(mode=self._mode())
         d2h = 0
         for it, col in zip(self.items, self.colors):
             self.og.lib().b200_frame_read(it["fb"]._h, self.og.FB_COLOR, col.ctypes.data, col.nbytes)
@@ -512,7 +528,7 @@ class BatchWorkload:
     def latency(self):
         """p50/p99 request completion (ms after the render starts): batch vs sequential."""
         og, dev = self.og, self.dev
-        self.batch.render(use_graph=True)
+        self.batch.render(mode=self._mode())
         bms, brays = self.batch.timings()
         for it in self.items:  # warm
             it["seq"].reset()
@@ -581,7 +597,8 @@ ScivisWorkload.roofline_kernel = "k_render_scivis_volume"
 ScivisWorkload.e2e_api = "b200 C ABI: b200_render_scivis + b200_frame_read (RGBA32F colour to host)"
 PTWorkload.launches_per_frame = 3 + 6 * 4  # generate, finalize, post-process, 6 bounces x (reset, trace, shade, shadow)
 BatchWorkload.launches_per_frame = None  # taken from the batch plan (b200_batch_info)
-BatchWorkload.e2e_api = "b200 C ABI: b200_batch_render (graph replay) + b200_frame_read of every request"
+BatchWorkload.e2e_api = ("b200 C ABI: b200_batch_render (graph replay of the wavefront kernels, or the one "
+                         "persistent launch) + b200_frame_read of every request")
 WORKLOADS = {"ao": AOWorkload, "pt": PTWorkload, "scivis": ScivisWorkload, "batch": BatchWorkload}
 
 
@@ -774,6 +791,8 @@ def run_ours(args):
         tdist.init_process_group("nccl")
     dev = og.Device(local)
     wl = WORKLOADS[args.workload]()
+    if args.workload == "batch":
+        wl.mode = args.batch_mode
     wl.setup(og, dev)
     line = measure(wl, args, og, dev, local, ws, 0.0 if args.no_cpu_baseline else args.cpu_budget)
     if ws > 1:
@@ -794,6 +813,17 @@ def run_ours(args):
                 sub.pop("scaling", None)
                 sub.pop("vs_baseline", None)
                 sub.pop("data", None)
+                if name == "batch":
+                    # the same requests as one persistent launch per frame
+                    try:
+                        w2.set_mode("persistent")
+                        p = measure(w2, args, og, dev, local, 1, 0.0)
+                        sub["persistent"] = {k: p[k] for k in ("value", "ms_per_step", "e2e", "gpu_launches",
+                                                               "latency", "clocks") if k in p}
+                        sub["persistent"].update(mode="persistent", plan=p["config"]["plan"],
+                                                 autotune=p["config"]["autotune"])
+                    except Exception as e:
+                        sub["persistent"] = {"error": "%s: %s" % (type(e).__name__, e)}
                 del w2
             except Exception as e:  # a failed extra is reported, not fatal to the headline
                 sub = {"error": "%s: %s" % (type(e).__name__, e)}
@@ -925,6 +955,8 @@ def main():
                     help="seconds of CPU-baseline work for each of the other configurations")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--headline-only", action="store_true", help="skip the other configurations' objects")
+    ap.add_argument("--batch-mode", default="graph", choices=["graph", "persistent"],
+                    help="batch workload: wavefront kernels as a graph, or one persistent launch")
     ap.add_argument("--size", default=None, help="WxH override (profiling small cases; not the bench config)")
     ap.add_argument("--spp", type=int, default=None, help="spp override (path tracer; profiling only)")
     ap.add_argument("--nrc-frames", type=int, default=256, help="frames per arm of the learned-cache study")

@@ -521,8 +521,9 @@ int b200_render_ao(b200_scene scene, const b200_camera_desc *camera, const b200_
  * requests share one set of wavefront queues (each ray traverses its own
  * request's scene), in waves of whole pixels, and each framebuffer
  * accumulates exactly as the single-request call would (AO: bit-identical;
- * path tracer: up to the order of the shadow-ray additions).  The launch
- * sequence is captured once as a CUDA graph and replayed.  Scenes and
+ * path tracer: up to the order of the shadow-ray additions).  The frame runs
+ * as wavefront kernels (directly or as a replayed CUDA graph) or as one
+ * persistent launch (b200_batch_render's mode).  Scenes and
  * framebuffers must outlive the batch; parameters and materials are copied
  * at the add call.  AO requests trace up to two AO rays per sample through
  * the shadow queue and further ones in place. */
@@ -534,7 +535,8 @@ int b200_batch_add_ao(b200_batch batch, b200_scene scene, const b200_camera_desc
 int b200_batch_add_pt(b200_batch batch, b200_scene scene, const b200_camera_desc *camera,
                       const b200_pt_params *params, const b200_material *materials, int nmaterials, b200_frame fb);
 /* launch shape: path slots per wave (the workspace, 264 bytes per slot) and
- * resident blocks per SM of the persistent trace and shade kernels */
+ * resident blocks per SM of the persistent trace and shade kernels (the
+ * persistent mode runs every co-resident block and uses wavePaths only) */
 typedef struct {
   int64_t wavePaths;
   int traceBlocksPerSM;
@@ -543,15 +545,35 @@ typedef struct {
 int b200_batch_get_tuning(b200_batch batch, b200_batch_tuning *out);
 int b200_batch_set_tuning(b200_batch batch, const b200_batch_tuning *tuning);
 /* The autotuner: renders the batch once per candidate launch shape (wave
- * sizes x trace / shade residency), timed with CUDA events after one warm-up
+ * sizes x trace / shade residency; wave sizes only when the last render
+ * used B200_BATCH_PERSISTENT), timed with CUDA events after one warm-up
  * render, and keeps the fastest; `candidates` <= 0 tries the full set.  The
  * framebuffers are reset afterwards (their accumulation restarts).  The
  * chosen shape is returned in `best` (may be null). */
 int b200_batch_autotune(b200_batch batch, int candidates, b200_batch_tuning *best);
-/* renders one frame of every request on the device stream; use_graph != 0
- * launches the captured CUDA graph (captured on first use and after any
- * change to the requests, the tuning or a framebuffer's post-processing) */
-int b200_batch_render(b200_batch batch, int use_graph);
+/* How b200_batch_render runs the frame:
+ * B200_BATCH_KERNELS     the wavefront kernels of every wave (generate, per
+ *                        bounce closest trace / shade / shadow trace,
+ *                        finalize) and the post-processing, launched directly;
+ * B200_BATCH_GRAPH       the same launches captured once as a CUDA graph and
+ *                        replayed;
+ * B200_BATCH_PERSISTENT  ONE cooperative persistent launch (captured as a
+ *                        one-kernel graph): all co-resident blocks run every
+ *                        wave's stages in order, separated by grid-wide
+ *                        barriers, pulling queue work dynamically, and
+ *                        post-process and stamp the requests each wave
+ *                        completes.  A barrier wait is bounded (4 s); one that
+ *                        runs out makes every block leave the kernel, and the
+ *                        next b200_batch_render or b200_batch_timings call
+ *                        returns B200_UNKNOWN_ERROR.
+ * The results are the same in all three modes (AO bit-identical, path
+ * tracing to the order of the shadow-ray additions). */
+enum { B200_BATCH_KERNELS = 0, B200_BATCH_GRAPH = 1, B200_BATCH_PERSISTENT = 2 };
+/* renders one frame of every request on the device stream in `mode` (a
+ * graph is captured on first use and after any change to the requests, the
+ * tuning, the mode or a framebuffer's post-processing); other values are
+ * refused (B200_INVALID_ARGUMENT) */
+int b200_batch_render(b200_batch batch, int mode);
 /* after a render has finished (b200_device_sync): each request's completion
  * time in ms after the render began (out n doubles, request order), and the
  * rays the render traced */

@@ -786,8 +786,12 @@ class BatchTuning(ctypes.Structure):
     _fields_ = [("wavePaths", ctypes.c_int64), ("traceBlocksPerSM", ctypes.c_int), ("shadeBlocksPerSM", ctypes.c_int)]
 
 
+BATCH_KERNELS, BATCH_GRAPH, BATCH_PERSISTENT = 0, 1, 2
+
+
 class Batch:
-    """b200_batch: many render requests served by one wavefront (CUDA graph)."""
+    """b200_batch: many render requests served by one wavefront (wavefront
+    kernels replayed as a CUDA graph, or one persistent launch)."""
 
     def __init__(self, device):
         self.device = device
@@ -824,8 +828,12 @@ class Batch:
         self.device._check(lib().b200_batch_autotune(self._h, candidates, ctypes.byref(t)))
         return t
 
-    def render(self, use_graph=True):
-        self.device._check(lib().b200_batch_render(self._h, int(bool(use_graph))))
+    def render(self, use_graph=True, mode=None):
+        """mode: BATCH_KERNELS, BATCH_GRAPH or BATCH_PERSISTENT (default: graph
+        if use_graph else kernels)."""
+        if mode is None:
+            mode = BATCH_GRAPH if use_graph else BATCH_KERNELS
+        self.device._check(lib().b200_batch_render(self._h, int(mode)))
 
     def timings(self):
         """(per-request completion ms since the render began, rays traced); waits for the device."""

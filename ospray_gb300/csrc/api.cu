@@ -603,6 +603,9 @@ Scene SceneObj::view() const {
   s.entries = dEntries;
   s.nentries = int(entries.size());
   s.ntlas = entries.empty() ? 0 : tlas.nnodes;
+  s.hasUser = 0;
+  for (const EntryH &e : entries)
+    if (geoms[e.geom].type != GEOM_TRIANGLES && geoms[e.geom].type != GEOM_SPHERES) s.hasUser = 1;
   s.status = status;
   s.counters = counters;
   return s;

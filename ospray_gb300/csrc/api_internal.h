@@ -122,12 +122,6 @@ struct SceneObj {
   Scene view() const;
 };
 
-// Tonemapper coefficients after ToneMapper::commit's clamping and solve.
-struct ToneMapD {
-  float exposure, a, b, c, d;
-  int aces;
-};
-
 struct FrameObj {
   DeviceObj *dev;
   int W, H;

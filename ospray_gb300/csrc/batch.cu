@@ -1,11 +1,15 @@
-// Batched rendering (b200_batch_*): many requests in one wavefront, captured
-// as a CUDA graph, with an autotuner over the wavefront's launch shape.
+// Batched rendering (b200_batch_*): many requests in one wavefront, run
+// either as a sequence of wavefront kernels per wave (launched directly or
+// captured as a CUDA graph) or as one cooperative persistent launch that
+// runs every wave's stages itself (captured as a one-kernel graph), with an
+// autotuner over the wavefront's launch shape.
 //
 // The host keeps the requests as (scene, frame, camera, parameters); each
-// render rebuilds the small device table of requests (frame IDs advance) and
-// uploads it before launching.  The kernel sequence itself depends only on
-// the wave plan, the tuning and the frames' post-processing, so it is
-// captured once and replayed until one of those changes.
+// render rebuilds the small device tables (requests, segments, waves,
+// post-processing; frame IDs advance) and uploads them before launching.
+// The launch sequence itself depends only on the wave plan, the tuning, the
+// mode and the frames' post-processing, so it is captured once and replayed
+// until one of those changes.
 #include <algorithm>
 #include <cstring>
 #include <string>
@@ -36,9 +40,11 @@ struct BatchObj {
   void *htables = nullptr;  // pinned staging copy of the table
   size_t htablesCap = 0;
   unsigned long long *dStamps = nullptr, *dRays = nullptr;
+  uint32_t *dBarrier = nullptr;  // the persistent kernel's grid barrier (4 words)
   int stampsCap = 0;
   std::vector<BatchWave> waves;
-  size_t segOff = 0;
+  BatchLayout layout = {};
+  int mode = B200_BATCH_GRAPH;  // of the last render (the autotuner tunes for it)
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   std::vector<float> graphKey;  // what the captured graph depends on
@@ -55,6 +61,7 @@ struct BatchObj {
     if (htables) cudaFreeHost(htables);
     if (dStamps) cudaFree(dStamps);
     if (dRays) cudaFree(dRays);
+    if (dBarrier) cudaFree(dBarrier);
     dev->release();
   }
   void dropGraph() {
@@ -83,14 +90,18 @@ struct BatchObj {
       d.fb = r.fb->view();
       d.fb.accumVariance = 0;     // batched frames keep no variance estimate
       d.fb.taskActive = nullptr;  // and render every task
+      d.postFormat = r.fb->format;
+      d.postTonemap = r.fb->toneMapOn ? 1 : 0;
+      d.postTm = r.fb->toneMap;
+      d.postOut = r.fb->mapped;
     }
     return h;
   }
 
   // everything the captured kernel sequence depends on, besides the table
   std::vector<float> key() const {
-    std::vector<float> k = {float(tune.wavePaths), float(tune.traceBlocksPerSM), float(tune.shadeBlocksPerSM),
-                            float(reqs.size())};
+    std::vector<float> k = {float(mode), float(tune.wavePaths), float(tune.traceBlocksPerSM),
+                            float(tune.shadeBlocksPerSM), float(reqs.size())};
     for (const Req &r : reqs) {
       const FrameObj *f = r.fb;
       k.insert(k.end(), {float(r.kind), float(f->W), float(f->H), float(f->format), f->toneMapOn ? 1.f : 0.f,
@@ -105,7 +116,7 @@ struct BatchObj {
   void prepare(cudaStream_t st) {
     std::vector<unsigned char> tables;
     const std::vector<BatchReqH> h = describe();
-    planBatch(dev->tables, dev->albedoTables(), h.data(), int(h.size()), tune.wavePaths, tables, waves, segOff);
+    planBatch(dev->tables, dev->albedoTables(), h.data(), int(h.size()), tune.wavePaths, tables, waves, layout);
     const size_t need = ptWorkspaceBytes(tune.wavePaths);
     if (need > wsBytes || tables.size() > tablesCap || int(reqs.size()) + 1 > stampsCap) {
       check(cudaStreamSynchronize(st), "sync");
@@ -137,29 +148,53 @@ struct BatchObj {
       check(cudaMalloc(&dStamps, sizeof(unsigned long long) * (reqs.size() + 1)), "batch stamps");
       stampsCap = int(reqs.size()) + 1;
     }
+    if (!dBarrier) {
+      check(cudaMalloc(&dBarrier, 4 * sizeof(uint32_t)), "batch barrier");
+      check(cudaMemset(dBarrier, 0, 4 * sizeof(uint32_t)), "clear batch barrier");
+    }
     // the staging buffer may still feed the previous render's copy
     check(cudaStreamSynchronize(st), "sync");
+    checkBarrier();
     std::memcpy(htables, tables.data(), tables.size());
     check(cudaMemcpyAsync(dtables, htables, tables.size(), cudaMemcpyHostToDevice, st), "upload batch table");
   }
 
-  // the whole frame of every request: the capturable kernel sequence
+  // after the stream has drained: did a barrier wait of the persistent
+  // kernel time out?  (It then left the frame incomplete.)
+  void checkBarrier() {
+    if (!dBarrier) return;
+    uint32_t w[4] = {0, 0, 0, 0};
+    check(cudaMemcpy(w, dBarrier, sizeof(w), cudaMemcpyDeviceToHost), "read batch barrier");
+    if (w[2]) {
+      check(cudaMemset(dBarrier, 0, sizeof(w)), "clear batch barrier");
+      throw Error(B200_UNKNOWN_ERROR, "batch: a grid barrier of the persistent kernel timed out; the frame is incomplete");
+    }
+  }
+
+  // the whole frame of every request: the capturable launch sequence
   void enqueue(cudaStream_t st) {
     const int n = int(reqs.size());
     check(cudaMemsetAsync(dRays, 0, sizeof(unsigned long long), st), "clear ray counter");
+    if (mode == B200_BATCH_PERSISTENT) {
+      check(launchBatchPersistent(dtables, layout, n, tune, ws, wsBytes, dRays, dStamps, dBarrier, st),
+            "persistent batch kernel");
+      return;
+    }
     check(launchStamp(dStamps, n, n + 1, st), "stamp");
     for (const BatchWave &w : waves) {
-      check(launchBatchWave(dtables, segOff, w, tune, ws, wsBytes, dRays, st), "batch wave");
+      check(launchBatchWave(dtables, layout.segs, w, tune, ws, wsBytes, dRays, st), "batch wave");
       for (int r = w.completeFirst; r >= 0 && r < w.completeEnd; r++) framePostProcess(reqs[r].fb, st, false);
       if (w.completeFirst >= 0) check(launchStamp(dStamps, w.completeFirst, w.completeEnd, st), "stamp");
     }
   }
 
-  void render(bool useGraph) {
+  void render(int m) {
     if (reqs.empty()) throw Error(B200_INVALID_OPERATION, "empty batch");
+    if (m < B200_BATCH_KERNELS || m > B200_BATCH_PERSISTENT) throw Error(B200_INVALID_ARGUMENT, "bad batch mode");
     cudaStream_t st = dev->stream;
+    mode = m;
     prepare(st);
-    if (useGraph) {
+    if (m != B200_BATCH_KERNELS) {
       const std::vector<float> k = key();
       if (!exec || k != graphKey) {
         dropGraph();
@@ -327,10 +362,16 @@ int b200_batch_autotune(b200_batch h, int candidates, b200_batch_tuning *best) {
     std::vector<long long> sizes;
     for (long long w = 1 << 21; w < (1 << 24) && w < total; w *= 2) sizes.push_back(w);
     sizes.push_back(std::max<long long>(std::min<long long>(total, 1 << 24), maxSpp));
+    // the persistent kernel's residency is fixed (all co-resident blocks):
+    // only the wave size varies for it
+    const int tuneMode = b->mode == B200_BATCH_PERSISTENT ? B200_BATCH_PERSISTENT : B200_BATCH_KERNELS;
     std::vector<BatchTuning> cands;
     for (long long w : sizes)
-      for (int tb : {2, 3, 4, 5})
-        for (int sb : {1, 2}) cands.push_back({w, tb, sb});
+      if (tuneMode == B200_BATCH_PERSISTENT)
+        cands.push_back({w, b->tune.traceBlocksPerSM, b->tune.shadeBlocksPerSM});
+      else
+        for (int tb : {2, 3, 4, 5})
+          for (int sb : {1, 2}) cands.push_back({w, tb, sb});
     if (candidates > 0 && size_t(candidates) < cands.size()) {
       // an even spread over the set
       std::vector<BatchTuning> pick;
@@ -348,9 +389,9 @@ int b200_batch_autotune(b200_batch h, int candidates, b200_batch_tuning *best) {
     try {
       for (const BatchTuning &t : cands) {
         b->tune = t;
-        b->render(false);  // warm-up (workspace, caches)
+        b->render(tuneMode);  // warm-up (workspace, caches)
         check(cudaEventRecord(e0, st), "event");
-        b->render(false);
+        b->render(tuneMode);
         check(cudaEventRecord(e1, st), "event");
         check(cudaEventSynchronize(e1), "event");
         float ms = 0.f;
@@ -378,23 +419,24 @@ int b200_batch_autotune(b200_batch h, int candidates, b200_batch_tuning *best) {
   });
 }
 
-int b200_batch_render(b200_batch h, int use_graph) {
+int b200_batch_render(b200_batch h, int mode) {
   if (!h) return B200_INVALID_ARGUMENT;
   BatchObj *b = reinterpret_cast<BatchObj *>(h);
-  return batchGuard(b, [&]() { b->render(use_graph != 0); });
+  return batchGuard(b, [&]() { b->render(mode); });
 }
 
 int b200_batch_info(b200_batch h, int64_t *info) {
   if (!h || !info) return B200_INVALID_ARGUMENT;
   const BatchObj *b = reinterpret_cast<BatchObj *>(h);
   int64_t kernels = 1, paths = 0;  // the start stamp
-  for (const BatchWave &w : b->waves) {
+  for (const BatchWave &w : b->waves) paths += w.npaths;
+  if (b->mode == B200_BATCH_PERSISTENT) kernels = 1;  // everything in one launch
+  else for (const BatchWave &w : b->waves) {
     kernels += 1 + 4 * int64_t(w.maxBounces + 1) + 1 + 1;  // generate, bounces, ray tail, finalize
     if (w.completeFirst >= 0) {
       kernels += 1;  // stamp
       for (int r = w.completeFirst; r < w.completeEnd; r++) kernels += b->reqs[r].fb->format != B200_FB_NONE;
     }
-    paths += w.npaths;
   }
   info[0] = int64_t(b->waves.size());
   info[1] = kernels;
@@ -408,6 +450,8 @@ int b200_batch_timings(b200_batch h, double *ms, int n, uint64_t *rays) {
   BatchObj *b = reinterpret_cast<BatchObj *>(h);
   return batchGuard(b, [&]() {
     requireArg(b->dStamps != nullptr, "batch not rendered");
+    check(cudaStreamSynchronize(b->dev->stream), "sync");
+    b->checkBarrier();
     const int nr = int(b->reqs.size());
     std::vector<unsigned long long> t(nr + 1);
     check(cudaMemcpy(t.data(), b->dStamps, sizeof(unsigned long long) * (nr + 1), cudaMemcpyDeviceToHost),

@@ -2,6 +2,7 @@
 #pragma once
 #include <vector>
 
+#include "frame_post.cuh"
 #include "pt_bsdf.cuh"
 #include "render_common.cuh"
 
@@ -233,6 +234,10 @@ struct BatchReqH {
   const LightD *lights;
   const float *lightCdf;
   FrameD fb;
+  // the frame's post-processing (framePostProcess): mapped format, tonemapper, mapped buffer
+  int postFormat, postTonemap;
+  ToneMapD postTm;
+  void *postOut;
 };
 
 // launch shape of the batched wavefront (what the autotuner picks)
@@ -253,12 +258,28 @@ struct BatchWave {
 // Splits the requests' paths (pixel-major, spp per pixel) into waves of at
 // most wavePaths paths and builds the device tables (requests + segments) in
 // `tables` (host bytes, uploaded by the caller before the waves run).
+// byte offsets of the tables after the request table, and the wave count
+struct BatchLayout {
+  size_t segs, waves, post;
+  int nwaves;
+};
 void planBatch(const SamplerTables *T, const AlbedoTablesD *AT, const BatchReqH *reqs, int n, long long wavePaths,
-               std::vector<unsigned char> &tables, std::vector<BatchWave> &waves, size_t &segTableOffset);
+               std::vector<unsigned char> &tables, std::vector<BatchWave> &waves, BatchLayout &layout);
 // Enqueues one wave: generate, bounces (closest trace, shade, shadow trace),
 // finalize into each request's framebuffer.  dtables = device copy of tables.
 cudaError_t launchBatchWave(const void *dtables, size_t segTableOffset, const BatchWave &w, const BatchTuning &tune,
                             void *workspace, size_t wsBytes, unsigned long long *rayCount, cudaStream_t st);
+// Enqueues the whole batch frame as ONE cooperative persistent launch: the
+// waves' stages (generate, per bounce closest trace / shade / shadow trace,
+// finalize) run in order inside the kernel, separated by grid-wide barriers;
+// completed requests are post-processed and stamped inside it (stamps[n] =
+// start).  `barrier` is 4 words the call clears; barrier[2] != 0 after the
+// launch means a barrier wait timed out (the frame is incomplete).
+cudaError_t launchBatchPersistent(const void *dtables, const BatchLayout &layout, int nreqs, const BatchTuning &tune,
+                                  void *workspace, size_t wsBytes, unsigned long long *rayCount,
+                                  unsigned long long *stamps, uint32_t *barrier, cudaStream_t st);
+// resident blocks per SM of the persistent batch kernel (its grid = SMs x this)
+int batchPersistentBlocksPerSM();
 // writes the global timer into stamps[first..end) (request completion times)
 cudaError_t launchStamp(unsigned long long *stamps, int first, int end, cudaStream_t st);
 

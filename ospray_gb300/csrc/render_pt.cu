@@ -217,10 +217,12 @@ struct ShadowMatD {
 #ifndef B200_REFILL_LANES
 #define B200_REFILL_LANES 8
 #endif
+// The body is a device function so that the persistent batch kernel runs it
+// as one of its stages; a batch reads its queue with coherent loads (in the
+// persistent kernel the queue was written earlier in the same launch).
 template <bool SHADOW, bool STATS, bool BATCH, bool TRANSP = false>
-__global__ void __launch_bounds__(TRACE_BLOCK, BATCH ? B200_BATCH_TRACE_MINBLOCKS : B200_TRACE_MINBLOCKS) k_trace_queue(Scene sc, Workspace ws, const uint32_t *queue,
-                                                            const uint32_t *count, uint32_t *fetch,
-                                                            const ReqD *reqs, ShadowMatD sm) {
+__device__ __forceinline__ void traceQueue(Scene sc, Workspace ws, const uint32_t *queue, const uint32_t *count,
+                                           uint32_t *fetch, const ReqD *reqs, ShadowMatD sm) {
   static_assert(!(BATCH && STATS), "batched traversal keeps no per-scene statistics");
   static_assert(!TRANSP || (SHADOW && !BATCH), "transparent shadows: single-request shadow rays only");
   const int lane = threadIdx.x & 31;
@@ -252,7 +254,8 @@ __global__ void __launch_bounds__(TRACE_BLOCK, BATCH ? B200_BATCH_TRACE_MINBLOCK
         if (idx < n) {
           Ray r;
           if (SHADOW) {
-            item = queue ? __ldg(queue + idx) : idx;  // a shadow queue, when given, holds record indices
+            // a shadow queue, when given, holds record indices
+            item = queue ? (BATCH ? queue[idx] : __ldg(queue + idx)) : idx;
             const ShadowRec s = ws.shadows[item];
             r.org = mk(s.a.x, s.a.y, s.a.z);
             r.tnear = TRANSP ? 0.f : s.c.w;
@@ -267,7 +270,7 @@ __global__ void __launch_bounds__(TRACE_BLOCK, BATCH ? B200_BATCH_TRACE_MINBLOCK
             }
             if (BATCH) bsc = reqs[ws.paths[__float_as_uint(s.b.w)].meta2.y].c.sc;
           } else {
-            item = queue ? __ldg(queue + idx) : idx;
+            item = queue ? (BATCH ? queue[idx] : __ldg(queue + idx)) : idx;
             const float4 o = ws.paths[item].org, d = ws.paths[item].dir;
             r.org = mk(o.x, o.y, o.z);
             r.tnear = ws.paths[item].lastP.w;  // camera rays: nearClip; bounces: 0
@@ -341,6 +344,13 @@ __global__ void __launch_bounds__(TRACE_BLOCK, BATCH ? B200_BATCH_TRACE_MINBLOCK
   if (STATS) flushStats(sc, ts);
 }
 
+template <bool SHADOW, bool STATS, bool BATCH, bool TRANSP = false>
+__global__ void __launch_bounds__(TRACE_BLOCK, BATCH ? B200_BATCH_TRACE_MINBLOCKS : B200_TRACE_MINBLOCKS)
+    k_trace_queue(Scene sc, Workspace ws, const uint32_t *queue, const uint32_t *count, uint32_t *fetch,
+                  const ReqD *reqs, ShadowMatD sm) {
+  traceQueue<SHADOW, STATS, BATCH, TRANSP>(sc, ws, queue, count, fetch, reqs, sm);
+}
+
 
 // The shading step of an AO request's camera sample (AORenderer_renderSample,
 // render/ao/AORenderer.ispc:23-149, with computeAO render/util.ispc:12-54):
@@ -394,7 +404,7 @@ B200_D void aoShade(const PtCtx &C, const AOParamsD &A, int W, PathRec &pr, cons
           r.dir = dir;
           r.tfar = A.aoRadius;
           HitRec hh;
-          if (!traceRay<false>(C.sc, r, hh, true, true, nullptr)) unblocked += 1.f;
+          if (!traceRay<false, false>(C.sc, r, hh, true, true, nullptr)) unblocked += 1.f;
         }
       }
     }
@@ -422,11 +432,11 @@ struct PathVars {
 template <bool TRANSP>
 B200_D V3 shadowInPlace(const PtCtx &C, Ray sr, V3 contrib, uint32_t medium, float cone) {
   HitRec h;
-  if (!TRANSP) return traceRay<false>(C.sc, sr, h, true, true, nullptr) ? splat(0.f) : contrib;
+  if (!TRANSP) return traceRay<false, false>(C.sc, sr, h, true, true, nullptr) ? splat(0.f) : contrib;
   const float tfar = sr.tfar;
   int maxDepth = C.p.maxPathLength;
   for (int guard = 0; guard < 4096; guard++) {
-    if (!traceRay<false>(C.sc, sr, h, false, true, nullptr)) return contrib;
+    if (!traceRay<false, false>(C.sc, sr, h, false, true, nullptr)) return contrib;
     const Entry &e = C.sc.entries[h.entry];
     h.geomID = e.geomID;
     h.instID = e.instID;
@@ -611,13 +621,10 @@ B200_D void scatterSurface(const PtCtx &C, const B &bsdf, const MaterialD &mat, 
 // glass, thin glass) or lets shadow rays through; without it the kernel
 // carries the opaque principled BSDF only (a smaller kernel for the common
 // case).
+// (A device function, a stage of the persistent batch kernel too.)
 template <bool BATCH, bool NRC, bool ALLMAT = true>
-#ifndef B200_SHADE_MINBLOCKS
-#define B200_SHADE_MINBLOCKS 2
-#endif
-__global__ void __launch_bounds__(128, B200_SHADE_MINBLOCKS) k_pt_shade(PtCtx c, Workspace ws, const uint32_t *qin, const uint32_t *cin,
-                                                  uint32_t *qout, uint32_t *cout, uint32_t *cshadow,
-                                                  const ReqD *reqs, NrcFrameD nf) {
+__device__ __forceinline__ void ptShade(PtCtx c, Workspace ws, const uint32_t *qin, const uint32_t *cin, uint32_t *qout,
+                                        uint32_t *cout, uint32_t *cshadow, const ReqD *reqs, NrcFrameD nf) {
   static_assert(!(BATCH && NRC), "the radiance cache runs on single-request frames");
   const uint32_t n = *(volatile const uint32_t *)cin;
   const uint32_t stride = gridDim.x * blockDim.x;
@@ -626,7 +633,7 @@ __global__ void __launch_bounds__(128, B200_SHADE_MINBLOCKS) k_pt_shade(PtCtx c,
   for (uint32_t r = 0; r < nround; r++) {
     const uint32_t qi = r * stride + blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = qi < n;
-    const uint32_t p = valid ? (qin ? __ldg(qin + qi) : qi) : 0u;
+    const uint32_t p = valid ? (qin ? (BATCH ? qin[qi] : __ldg(qin + qi)) : qi) : 0u;
     bool cont = false;
     // shadow requests of this lane (numLS <= MAX_NEE per bounce in the queue)
     int nsh = 0;
@@ -817,6 +824,16 @@ __global__ void __launch_bounds__(128, B200_SHADE_MINBLOCKS) k_pt_shade(PtCtx c,
   }
 }
 
+#ifndef B200_SHADE_MINBLOCKS
+#define B200_SHADE_MINBLOCKS 2
+#endif
+template <bool BATCH, bool NRC, bool ALLMAT = true>
+__global__ void __launch_bounds__(128, B200_SHADE_MINBLOCKS)
+    k_pt_shade(PtCtx c, Workspace ws, const uint32_t *qin, const uint32_t *cin, uint32_t *qout, uint32_t *cout,
+               uint32_t *cshadow, const ReqD *reqs, NrcFrameD nf) {
+  ptShade<BATCH, NRC, ALLMAT>(c, ws, qin, cin, qout, cout, cshadow, reqs, nf);
+}
+
 // averages each pixel's samples into the framebuffer (ScreenSample_accumulate
 // / normalize, maxContribution clamp, NaN -> 0 with alpha 1)
 B200_D PixelOut finalizePT(const PathRec *paths, int spp, float maxContribution) {
@@ -918,13 +935,8 @@ B200_D int findSeg(const SegD *segs, int nseg, long long slot, KeyFn key) {
   return lo;
 }
 
-__global__ void k_batch_generate(const ReqD *reqs, const SegD *segs, int nseg, long long npaths, Workspace ws) {
-  const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (p == 0) {
-    ws.counters[0] = uint32_t(npaths);
-    for (int k = 1; k < 8; k++) ws.counters[k] = 0;
-  }
-  if (p >= npaths) return;
+// path slot p of a wave: its request's camera ray (PT) or AO camera sample
+B200_D void batchGenerate(const ReqD *reqs, const SegD *segs, int nseg, long long p, const Workspace &ws) {
   const SegD &sg = segs[findSeg(segs, nseg, p, [](const SegD &q) { return q.start; })];
   const ReqD &R = reqs[sg.rid];
   const long long lp = sg.first + (p - sg.start);
@@ -949,9 +961,8 @@ __global__ void k_batch_generate(const ReqD *reqs, const SegD *segs, int nseg, l
   ws.paths[p] = r;
 }
 
-__global__ void k_batch_finalize(const ReqD *reqs, const SegD *segs, int nseg, long long npix, Workspace ws) {
-  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (q >= npix) return;
+// pixel slot q of a wave: its samples averaged into its request's framebuffer
+B200_D void batchFinalize(const ReqD *reqs, const SegD *segs, int nseg, long long q, const Workspace &ws) {
   const SegD &sg = segs[findSeg(segs, nseg, q, [](const SegD &g) { return g.pixStart; })];
   const ReqD &R = reqs[sg.rid];
   const int spp = R.fi.spp;
@@ -961,10 +972,207 @@ __global__ void k_batch_finalize(const ReqD *reqs, const SegD *segs, int nseg, l
   fbAccumulate(R.fb, int(pix % R.fi.W), int(pix / R.fi.W), o);
 }
 
-__global__ void k_stamp(unsigned long long *stamps, int first, int end) {
+__global__ void k_batch_generate(const ReqD *reqs, const SegD *segs, int nseg, long long npaths, Workspace ws) {
+  const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (p == 0) {
+    ws.counters[0] = uint32_t(npaths);
+    for (int k = 1; k < 8; k++) ws.counters[k] = 0;
+  }
+  if (p < npaths) batchGenerate(reqs, segs, nseg, p, ws);
+}
+
+__global__ void k_batch_finalize(const ReqD *reqs, const SegD *segs, int nseg, long long npix, Workspace ws) {
+  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (q < npix) batchFinalize(reqs, segs, nseg, q, ws);
+}
+
+B200_D unsigned long long globalTimer() {
   unsigned long long t;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__global__ void k_stamp(unsigned long long *stamps, int first, int end) {
+  const unsigned long long t = globalTimer();
   for (int i = first + int(threadIdx.x); i < end; i += blockDim.x) stamps[i] = t;
+}
+
+// ---------------------------------------------------------------- persistent batch kernel
+// A whole batch frame in one cooperative launch.  The reference hands render
+// tasks to threads through its tile scheduler (render/LoadBalancer.cpp:13-32);
+// here the work items are the waves' (request, pixel range) segments and
+// their queues: per wave, generate -> per bounce (closest trace -> shade ->
+// shadow trace) -> finalize, each stage a grid-stride loop or a dynamically
+// fetched queue over the whole resident grid, the stages separated by
+// grid-wide barriers.  The requests a wave completes are post-processed in
+// the next stage (beside the next wave's generation) and stamped after it.
+
+// a wave as the persistent kernel reads it (device table)
+struct WaveD {
+  long long npaths, npix;
+  int segOffset, nseg, maxBounces, completeFirst, completeEnd, pad;
+};
+
+// a request's post-processing (device table)
+struct PostD {
+  const float4 *color;
+  void *out;
+  long long n;
+  ToneMapD tm;
+  int format, tonemap;
+};
+
+struct BatchRunD {
+  const ReqD *reqs;
+  const SegD *segs;
+  const WaveD *waves;
+  const PostD *post;
+  int nwaves, nreqs;
+  Workspace ws;
+  uint32_t *bar;  // [0] arrivals, [1] generation, [2] error (a wait timed out)
+  unsigned long long *rays, *stamps;
+};
+
+#ifndef B200_BARRIER_TIMEOUT_NS
+#define B200_BARRIER_TIMEOUT_NS 4000000000ull
+#endif
+
+B200_D uint32_t loadAcquire(const uint32_t *p) {
+  uint32_t v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Grid-wide barrier of the cooperative launch.  A wait longer than
+// B200_BARRIER_TIMEOUT_NS sets the error word, and a block that finds the
+// error word set does not wait: every block then leaves the kernel (false)
+// instead of spinning on.
+B200_D bool gridBarrier(uint32_t *bar, uint32_t &gen) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = *(volatile uint32_t *)(bar + 2) == 0u;
+    if (ok) {
+      const uint32_t next = gen + 1u;
+      __threadfence();
+      if (atomicAdd(bar, 1u) == gridDim.x - 1u) {
+        atomicExch(bar, 0u);
+        __threadfence();
+        atomicExch(bar + 1, next);
+      } else {
+        const unsigned long long t0 = globalTimer();
+        while (loadAcquire(bar + 1) != next) {
+          if (*(volatile uint32_t *)(bar + 2) != 0u || globalTimer() - t0 > B200_BARRIER_TIMEOUT_NS) {
+            atomicExch(bar + 2, 1u);
+            ok = 0;
+            break;
+          }
+          __nanosleep(64);
+        }
+      }
+      __threadfence();
+    }
+    s_ok = ok;
+  }
+  __syncthreads();
+  gen++;
+  return s_ok != 0;
+}
+
+// the colour conversion of requests [first, end) (framePostProcess; batched
+// frames keep no variance estimate)
+B200_D void batchPost(const BatchRunD &R, int first, int end, long long tid, long long nthreads) {
+  for (int r = first; r >= 0 && r < end; r++) {
+    const PostD &P = R.post[r];
+    if (P.format == B200_FB_NONE) continue;
+    for (long long i = tid; i < P.n; i += nthreads) postPixel(P.color, i, P.format, P.tonemap, P.tm, P.out);
+  }
+}
+
+#ifndef B200_PERSIST_MINBLOCKS
+#define B200_PERSIST_MINBLOCKS 3
+#endif
+// B200_PERSIST_CALLS: the trace and shade stages as out-of-line functions,
+// each register-allocated on its own (within the kernel's budget) rather
+// than inlined into one body whose live ranges all compete (1,302 vs 1,263
+// Mrays/s on the 64-request batch; 4 blocks per SM: 1,278 / 1,270)
+#ifndef B200_PERSIST_CALLS
+#define B200_PERSIST_CALLS 1
+#endif
+#if B200_PERSIST_CALLS
+#define B200_STAGE static __device__ __noinline__
+#else
+#define B200_STAGE static __device__ __forceinline__
+#endif
+template <bool SHADOW>
+B200_STAGE void persistTrace(Workspace ws, const uint32_t *queue, const uint32_t *count, uint32_t *fetch,
+                             const ReqD *reqs) {
+  traceQueue<SHADOW, false, true>(Scene{}, ws, queue, count, fetch, reqs, ShadowMatD{});
+}
+B200_STAGE void persistShade(Workspace ws, const uint32_t *qin, const uint32_t *cin, uint32_t *qout, uint32_t *cout,
+                             uint32_t *cshadow, const ReqD *reqs) {
+  ptShade<true, false, true>(PtCtx{}, ws, qin, cin, qout, cout, cshadow, reqs, NrcFrameD{});
+}
+__global__ void __launch_bounds__(TRACE_BLOCK, B200_PERSIST_MINBLOCKS) k_batch_persistent(BatchRunD R) {
+  // little state lives across the stages (the wave's fields are re-read
+  // from its table entry where a stage needs them), so the shading stage
+  // keeps its registers
+  const bool lead = blockIdx.x == 0 && threadIdx.x == 0;
+  uint32_t *ctr = R.ws.counters;
+  volatile uint32_t *vctr = ctr;
+  uint32_t gen = 0;
+  if (lead) R.stamps[R.nreqs] = globalTimer();
+  for (int wi = 0; wi <= R.nwaves; wi++) {
+    // post-processing of the requests the previous wave completed, beside
+    // this wave's generation
+    {
+      const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+      const long long nthreads = (long long)gridDim.x * blockDim.x;
+      if (wi > 0) batchPost(R, R.waves[wi - 1].completeFirst, R.waves[wi - 1].completeEnd, tid, nthreads);
+      if (wi < R.nwaves) {
+        const WaveD &w = R.waves[wi];
+        if (lead) {
+          vctr[0] = uint32_t(w.npaths);
+          for (int k = 1; k < 8; k++) vctr[k] = 0u;
+        }
+        for (long long p = tid; p < w.npaths; p += nthreads) batchGenerate(R.reqs, R.segs + w.segOffset, w.nseg, p, R.ws);
+      }
+    }
+    if (!gridBarrier(R.bar, gen)) return;
+    if (lead && wi > 0)
+      for (int r = R.waves[wi - 1].completeFirst; r >= 0 && r < R.waves[wi - 1].completeEnd; r++)
+        R.stamps[r] = globalTimer();
+    if (wi == R.nwaves) break;
+    const int nb = R.waves[wi].maxBounces;
+    for (int b = 0; b <= nb; b++) {
+      const int cin = b & 1, cout = cin ^ 1;
+      const uint32_t *qin = b == 0 ? nullptr : (cin ? R.ws.qb : R.ws.qa);
+      // counter upkeep, each beside a stage that does not use that counter:
+      // the rays of the last bounce are counted, the shadow queue and its
+      // fetch counter cleared
+      if (lead) {
+        *R.rays += (unsigned long long)vctr[cin] + vctr[2];
+        vctr[2] = 0u;
+        vctr[4] = 0u;
+      }
+      persistTrace<false>(R.ws, qin, ctr + cin, ctr + 3, R.reqs);
+      if (!gridBarrier(R.bar, gen)) return;
+      if (lead) vctr[3] = 0u;  // closest-hit fetch counter of the next bounce
+      persistShade(R.ws, qin, ctr + cin, cout ? R.ws.qb : R.ws.qa, ctr + cout, ctr + 2, R.reqs);
+      if (!gridBarrier(R.bar, gen)) return;
+      if (lead) vctr[cin] = 0u;  // the next bounce's output queue
+      persistTrace<true>(R.ws, nullptr, ctr + 2, ctr + 4, R.reqs);
+      if (!gridBarrier(R.bar, gen)) return;
+    }
+    if (lead) *R.rays += vctr[2];
+    {
+      const WaveD &w = R.waves[wi];
+      const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+      for (long long q = tid; q < w.npix; q += (long long)gridDim.x * blockDim.x)
+        batchFinalize(R.reqs, R.segs + w.segOffset, w.nseg, q, R.ws);
+    }
+    if (!gridBarrier(R.bar, gen)) return;
+  }
 }
 
 // ---------------------------------------------------------------- radiance cache hooks
@@ -1237,7 +1445,7 @@ cudaError_t launchRenderPT(const SamplerTables *T, const Scene &sc, const Camera
 }
 
 void planBatch(const SamplerTables *T, const AlbedoTablesD *AT, const BatchReqH *reqs, int n, long long wavePaths,
-               std::vector<unsigned char> &tables, std::vector<BatchWave> &waves, size_t &segTableOffset) {
+               std::vector<unsigned char> &tables, std::vector<BatchWave> &waves, BatchLayout &layout) {
   std::vector<ReqD> rd(n);
   for (int i = 0; i < n; i++) {
     const BatchReqH &h = reqs[i];
@@ -1299,10 +1507,26 @@ void planBatch(const SamplerTables *T, const AlbedoTablesD *AT, const BatchReqH 
     }
   }
   close();
-  segTableOffset = (sizeof(ReqD) * n + 255) & ~size_t(255);
-  tables.assign(segTableOffset + sizeof(SegD) * segs.size(), 0);
+  std::vector<WaveD> wd(waves.size());
+  for (size_t i = 0; i < waves.size(); i++) {
+    const BatchWave &b = waves[i];
+    wd[i] = WaveD{b.npaths, b.npix, b.segOffset, b.nseg, b.maxBounces, b.completeFirst, b.completeEnd, 0};
+  }
+  std::vector<PostD> pd(n);
+  for (int i = 0; i < n; i++) {
+    const BatchReqH &h = reqs[i];
+    pd[i] = PostD{h.fb.color, h.postOut, (long long)h.fb.W * h.fb.H, h.postTm, h.postFormat, h.postTonemap};
+  }
+  auto up = [](size_t b) { return (b + 255) & ~size_t(255); };
+  layout.segs = up(sizeof(ReqD) * n);
+  layout.waves = up(layout.segs + sizeof(SegD) * segs.size());
+  layout.post = up(layout.waves + sizeof(WaveD) * wd.size());
+  layout.nwaves = int(wd.size());
+  tables.assign(layout.post + sizeof(PostD) * n, 0);
   std::memcpy(tables.data(), rd.data(), sizeof(ReqD) * n);
-  std::memcpy(tables.data() + segTableOffset, segs.data(), sizeof(SegD) * segs.size());
+  std::memcpy(tables.data() + layout.segs, segs.data(), sizeof(SegD) * segs.size());
+  if (!wd.empty()) std::memcpy(tables.data() + layout.waves, wd.data(), sizeof(WaveD) * wd.size());
+  std::memcpy(tables.data() + layout.post, pd.data(), sizeof(PostD) * n);
 }
 
 cudaError_t launchBatchWave(const void *dtables, size_t segTableOffset, const BatchWave &w, const BatchTuning &tune,
@@ -1332,6 +1556,49 @@ cudaError_t launchBatchWave(const void *dtables, size_t segTableOffset, const Ba
   if (rayCount) k_count_tail<<<1, 1, 0, st>>>(ws.counters, rayCount);
   k_batch_finalize<<<unsigned((w.npix + 127) / 128), 128, 0, st>>>(reqs, segs, w.nseg, w.npix, ws);
   return cudaGetLastError();
+}
+
+int batchPersistentBlocksPerSM() {
+  int per = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_batch_persistent, TRACE_BLOCK, TRACE_SMEM_BYTES) !=
+      cudaSuccess)
+    return 0;
+  return per;
+}
+
+cudaError_t launchBatchPersistent(const void *dtables, const BatchLayout &layout, int nreqs, const BatchTuning &tune,
+                                  void *workspace, size_t wsBytes, unsigned long long *rayCount,
+                                  unsigned long long *stamps, uint32_t *barrier, cudaStream_t st) {
+  if (ptWorkspaceBytes(tune.wavePaths) > wsBytes || !rayCount || !stamps || !barrier) return cudaErrorInvalidValue;
+  const int per = batchPersistentBlocksPerSM();
+  if (per < 1) return cudaErrorInvalidConfiguration;
+  const char *t = static_cast<const char *>(dtables);
+  BatchRunD R;
+  R.reqs = reinterpret_cast<const ReqD *>(t);
+  R.segs = reinterpret_cast<const SegD *>(t + layout.segs);
+  R.waves = reinterpret_cast<const WaveD *>(t + layout.waves);
+  R.post = reinterpret_cast<const PostD *>(t + layout.post);
+  R.nwaves = layout.nwaves;
+  R.nreqs = nreqs;
+  R.ws = carveWorkspace(workspace, tune.wavePaths);
+  R.bar = barrier;
+  R.rays = rayCount;
+  R.stamps = stamps;
+  cudaError_t e = cudaMemsetAsync(barrier, 0, 4 * sizeof(uint32_t), st);
+  if (e != cudaSuccess) return e;
+  // all blocks resident at once (the cooperative attribute makes the launch
+  // fail rather than run a grid that does not fit)
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(unsigned(smCount() * per));
+  cfg.blockDim = dim3(TRACE_BLOCK);
+  cfg.dynamicSmemBytes = TRACE_SMEM_BYTES;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k_batch_persistent, R);
 }
 
 cudaError_t launchStamp(unsigned long long *stamps, int first, int end, cudaStream_t st) {

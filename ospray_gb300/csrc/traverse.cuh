@@ -32,6 +32,7 @@ struct Scene {
   const Entry *entries;
   int nentries;
   int ntlas;
+  int hasUser;                // an entry holds discs or planes (the traversal's out-of-line tests)
   uint32_t *status;           // bit 0: traversal stack overflow seen
   unsigned long long *counters;  // [rays, node visits, triangle tests, sphere tests]
 };
@@ -477,6 +478,9 @@ struct Traverser {
   // The full hit record of the closest hit: u, v and the geometric normal
   // re-evaluated on the hit primitive in its entry's frame with the same
   // operations as during traversal (so identical values), and the IDs.
+  // USER = false: the scene has no discs or planes (Scene::hasUser), so no
+  // out-of-line call is compiled into the caller.
+  template <bool USER = true>
   B200_D void finish(const Scene &sc) {
     hit.t = ht;
     hit.primID = hprim;
@@ -501,15 +505,15 @@ struct Traverser {
       const V3 v0 = mk(a.x, a.y, a.z), v1 = mk(b.x, b.y, b.z), v2 = mk(c.x, c.y, c.z);
       triTest(triPre(d), o, ray.tnear, ht, v0, v1, v2, t, hit.u, hit.v);
       hit.Ng = cross(sub(v1, v0), sub(v2, v0));
-    } else if (e.type == GEOM_SPHERES) {
+    } else if (!USER || e.type == GEOM_SPHERES) {
       sphTest(o, d, ray.tnear, ht, __ldg(e.prims + hslot), t, hit.Ng);
     } else {
       hit.Ng = userNormal(e.type, d, e.prims, hslot);
     }
   }
 
-  // one traversal step; true when the ray is finished
-  template <bool STATS>
+  // one traversal step; true when the ray is finished (USER as for finish)
+  template <bool STATS, bool USER = true>
   B200_D bool step(const Scene &sc, TraceStats *ts) {
     // 1) the next node of the current node group
     if (nbits & 0xffu) {
@@ -556,7 +560,7 @@ struct Traverser {
         h = triTest(pre, org, ray.tnear, ht, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), mk(c.x, c.y, c.z), t, u, v);
         prim = __float_as_uint(a.w);
       } else {
-        if (etype == GEOM_SPHERES) {
+        if (!USER || etype == GEOM_SPHERES) {
           V3 Ng;
           h = sphTest(org, dir, ray.tnear, ht, __ldg(prims + slot), t, Ng);
         } else {
@@ -603,7 +607,11 @@ struct Traverser {
 // this the lanes of a warp drift to different points of the data-dependent
 // loop and execute one at a time.  `active == false` makes a lane take part
 // without tracing anything.
-template <bool STATS = false>
+//
+// SPLIT: two copies of the loop, one without the out-of-line disc and plane
+// tests for scenes that have none (Scene::hasUser); without SPLIT one loop
+// with them (smaller code, for callers inside large kernels).
+template <bool STATS = false, bool SPLIT = true>
 B200_D bool traceRay(const Scene &sc, const Ray &ray, HitRec &hit, bool anyHit, bool active = true,
                      TraceStats *ts = nullptr) {
   if (STATS && active) ts->rays++;
@@ -612,11 +620,20 @@ B200_D bool traceRay(const Scene &sc, const Ray &ray, HitRec &hit, bool anyHit, 
   TraceSpill spill;
   tv.init(sc, ray, anyHit, &spill);
   bool done = !active || tv.idle();
-  for (int guard = 0; guard < (1 << 18); guard++) {
-    if (!__any_sync(group, !done)) break;
-    if (!done) done = tv.step<STATS>(sc, ts);
+  // the lanes' scenes may differ in a batch: the choice is made for the group
+  if (!SPLIT || __any_sync(group, sc.hasUser != 0)) {
+    for (int guard = 0; guard < (1 << 18); guard++) {
+      if (!__any_sync(group, !done)) break;
+      if (!done) done = tv.step<STATS, true>(sc, ts);
+    }
+    if (!anyHit) tv.finish<true>(sc);
+  } else {
+    for (int guard = 0; guard < (1 << 18); guard++) {
+      if (!__any_sync(group, !done)) break;
+      if (!done) done = tv.step<STATS, false>(sc, ts);
+    }
+    if (!anyHit) tv.finish<false>(sc);
   }
-  if (!anyHit) tv.finish(sc);
   hit = tv.hit;
   return tv.found;
 }

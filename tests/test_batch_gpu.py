@@ -7,8 +7,10 @@ must equal what the single-request call renders on the same inputs: AO
 bit-identical (the batch forms each pixel from the same samples with the
 same operation order), path tracing within the tolerance of the shadow-ray
 addition order, depth and IDs exact.  Two frames check accumulation; the
-CUDA-graph replay and the plain launch agree; the autotuner returns one of
-its candidates and restarts accumulation."""
+CUDA-graph replay, the plain launches and the one persistent launch agree
+(including the mapped, tonemapped colour the persistent kernel converts
+itself); the autotuner returns one of its candidates and restarts
+accumulation."""
 import numpy as np
 import pytest
 
@@ -60,7 +62,8 @@ def _single(og, dev, ch, r):
     return fb
 
 
-def test_batch_matches_single_requests(b200_device):
+@pytest.mark.parametrize("mode", ["graph", "persistent"])
+def test_batch_matches_single_requests(b200_device, mode):
     import ospray_gb300 as og
     dev = b200_device
     ch, reqs = _requests(og, dev)
@@ -78,7 +81,7 @@ def test_batch_matches_single_requests(b200_device):
     t = og.BatchTuning(4096, 3, 1)  # small waves: requests split across waves
     batch.tuning = t
     for frame in range(2):
-        batch.render(use_graph=True)
+        batch.render(mode=og.BATCH_GRAPH if mode == "graph" else og.BATCH_PERSISTENT)
         for r, sf in zip(reqs, sfbs):
             if r[0] == "ao":
                 og.render_ao(r[1], r[2], r[3], sf)
@@ -97,6 +100,53 @@ def test_batch_matches_single_requests(b200_device):
     ms, rays = batch.timings()
     assert rays > sum(r[-2] * r[-1] for r in reqs)
     assert np.all(ms > 0) and np.all(np.diff(ms) >= 0)  # requests complete in order
+    info = batch.info()
+    assert info["waves"] > 1
+    if mode == "persistent":
+        assert info["kernels"] == 1
+
+
+def test_persistent_launch_equals_graph_with_post_processing(b200_device):
+    """AO requests with mapped RGBA8 (tonemapped) and sRGBA colour: the one
+    persistent launch post-processes each request after the wave that
+    completes it; bytes equal to the wavefront-kernel graph's, accumulation
+    over three frames, the same ray count."""
+    import ospray_gb300 as og
+    dev = b200_device
+    _, reqs = _requests(og, dev)
+    ao = [reqs[0], reqs[2]]
+    out, counts = {}, {}
+    for mode in (og.BATCH_GRAPH, og.BATCH_PERSISTENT):
+        batch = og.Batch(dev)
+        fbs = []
+        for r, fmt in zip(ao, (og.FB_RGBA8, og.FB_SRGBA)):
+            fb = og.Frame(dev, r[-2], r[-1], og.FB_COLOR | og.FB_DEPTH | og.FB_ACCUM, format=fmt)
+            if fmt == og.FB_RGBA8:
+                fb.set_tonemapper(og.tonemapper(exposure=1.5))
+            batch.add_ao(r[1], r[2], r[3], fb)
+            fbs.append(fb)
+        batch.tuning = og.BatchTuning(2048, 3, 1)
+        for _ in range(3):
+            batch.render(mode=mode)
+        out[mode] = [(fb.read(og.FB_COLOR), fb.read(og.FB_ACCUM), fb.read(og.FB_DEPTH)) for fb in fbs]
+        counts[mode] = batch.timings()[1]
+        assert all(fb.frame_id == 3 for fb in fbs)
+    for a, b in zip(out[og.BATCH_GRAPH], out[og.BATCH_PERSISTENT]):
+        for x, y in zip(a, b):
+            np.testing.assert_array_equal(x, y)
+    assert counts[og.BATCH_GRAPH] == counts[og.BATCH_PERSISTENT]
+    assert out[og.BATCH_GRAPH][0][0].dtype == np.uint8 and out[og.BATCH_GRAPH][0][0].max() > 0
+
+
+def test_bad_batch_mode_is_refused(b200_device):
+    import ospray_gb300 as og
+    dev = b200_device
+    _, reqs = _requests(og, dev)
+    batch = og.Batch(dev)
+    fb = og.Frame(dev, reqs[0][-2], reqs[0][-1])
+    batch.add_ao(reqs[0][1], reqs[0][2], reqs[0][3], fb)
+    with pytest.raises(og.B200Error):
+        batch.render(mode=7)
 
 
 def test_graph_replay_equals_plain_launch_and_autotune(b200_device):
