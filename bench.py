@@ -595,7 +595,8 @@ PTWorkload.roofline_kernel = "k_trace_queue (closest-hit and shadow instantiatio
 ScivisWorkload.timed_kernels = ("scivis",)
 ScivisWorkload.roofline_kernel = "k_render_scivis_volume"
 ScivisWorkload.e2e_api = "b200 C ABI: b200_render_scivis + b200_frame_read (RGBA32F colour to host)"
-PTWorkload.launches_per_frame = 3 + 6 * 4  # generate, finalize, post-process, 6 bounces x (reset, trace, shade, shadow)
+# generate, finalize, post-process, 6 bounces x (reset, trace, shade, shadow), queue partitions of bounces 1-5
+PTWorkload.launches_per_frame = 3 + 6 * 4 + 5
 BatchWorkload.launches_per_frame = None  # taken from the batch plan (b200_batch_info)
 BatchWorkload.e2e_api = ("b200 C ABI: b200_batch_render (graph replay of the wavefront kernels, or the one "
                          "persistent launch) + b200_frame_read of every request")

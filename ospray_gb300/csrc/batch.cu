@@ -433,6 +433,7 @@ int b200_batch_info(b200_batch h, int64_t *info) {
   if (b->mode == B200_BATCH_PERSISTENT) kernels = 1;  // everything in one launch
   else for (const BatchWave &w : b->waves) {
     kernels += 1 + 4 * int64_t(w.maxBounces + 1) + 1 + 1;  // generate, bounces, ray tail, finalize
+    if (B200_SHADE_PARTITION) kernels += w.maxBounces;     // the queue partitions
     if (w.completeFirst >= 0) {
       kernels += 1;  // stamp
       for (int r = w.completeFirst; r < w.completeEnd; r++) kernels += b->reqs[r].fb->format != B200_FB_NONE;

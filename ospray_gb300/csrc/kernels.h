@@ -240,6 +240,14 @@ struct BatchReqH {
   void *postOut;
 };
 
+// B200_SHADE_PARTITION: the path tracers split the queues of bounces >= 1
+// by material branch before shading (k_partition; 996 vs 910 Mrays/s on the
+// 1080p bench).  The camera rays' queue is left in pixel order, which is
+// already coherent (partitioning it too gave 977).
+#ifndef B200_SHADE_PARTITION
+#define B200_SHADE_PARTITION 1
+#endif
+
 // launch shape of the batched wavefront (what the autotuner picks)
 struct BatchTuning {
   long long wavePaths;  // path slots per wave (workspace size)

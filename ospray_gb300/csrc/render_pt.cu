@@ -217,6 +217,7 @@ struct ShadowMatD {
 #ifndef B200_REFILL_LANES
 #define B200_REFILL_LANES 8
 #endif
+
 // The body is a device function so that the persistent batch kernel runs it
 // as one of its stages; a batch reads its queue with coherent loads (in the
 // persistent kernel the queue was written earlier in the same launch).
@@ -1295,6 +1296,54 @@ __global__ void k_bounce_reset(uint32_t *counters, int cin, int cout, unsigned l
   counters[2] = 0;
   counters[3] = 0;
   counters[4] = 0;
+  counters[5] = 0;
+  counters[6] = 0;
+}
+
+// Splits a bounce's queue of traced paths by what their shading runs: the
+// front of `out` gets the hits on diffuse-based materials (principled with
+// metallic < 0.5, obj), the back everything else (conductors, metal, glass,
+// misses), so that most warps of the shading kernel take one branch of the
+// BSDF code.  front / back count the two ends (cleared per bounce).
+// In a batch (BATCH) each path's request gives the scene and materials.
+template <bool BATCH>
+__global__ void k_partition(Scene sc, const MaterialD *mats, int nmats, Workspace ws, const uint32_t *qin,
+                            const uint32_t *count, uint32_t *out, uint32_t *front, uint32_t *back,
+                            const ReqD *reqs) {
+  const uint32_t n = *(volatile const uint32_t *)count;
+  const uint32_t stride = gridDim.x * blockDim.x;
+  const uint32_t nround = (n + stride - 1) / stride;  // warp-uniform loop (warp appends)
+  for (uint32_t r = 0; r < nround; r++) {
+    const uint32_t i = r * stride + blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = i < n;
+    uint32_t p = 0;
+    bool diffuse = false;
+    if (valid) {
+      p = qin ? qin[i] : i;
+      const float4 a = ws.hits[p].a;
+      if (a.w != 0.f) {
+        const Entry *entries = sc.entries;
+        const MaterialD *M = mats;
+        int nm = nmats;
+        if (BATCH) {
+          const ReqD &R = reqs[ws.paths[p].meta2.y];
+          entries = R.c.sc.entries;
+          M = R.c.mats;
+          nm = R.kind == BATCH_PT ? R.c.p.numMaterials : 0;
+        }
+        const uint32_t mi = __ldg(&entries[__float_as_uint(a.z)].materialID);
+        if (mi >= uint32_t(nm)) {
+          diffuse = true;
+        } else {
+          const uint32_t kind = __ldg(&M[mi].kind);
+          diffuse = kind == MAT_OBJ || (kind == MAT_PRINCIPLED && __ldg(&M[mi].metallic) < 0.5f);
+        }
+      }
+    }
+    const uint32_t f = warpAppend(valid && diffuse, front);
+    const uint32_t k = warpAppend(valid && !diffuse, back);
+    if (valid) out[diffuse ? f : n - 1u - k] = p;
+  }
 }
 
 __global__ void k_count_tail(const uint32_t *counters, unsigned long long *rays) { *rays += counters[2]; }
@@ -1386,11 +1435,21 @@ cudaError_t launchRenderPT(const SamplerTables *T, const Scene &sc, const Camera
   if (adaptive) cudaMemsetAsync(ws.counters, 0, 16 * sizeof(uint32_t), st);
   k_pt_generate<<<gen, 256, 0, st>>>(c, cam, pf, fi, ws, nf.trainStride, nf.trainOffset, nf.trainSlots, fb,
                                      adaptive ? ws.qa : nullptr);
-  uint32_t *qs[2] = {ws.qa, ws.qb};
+  // the queue a bounce traces (camera rays of a whole frame: none, the
+  // identity); shading appends the continuing paths to another buffer, and
+  // with the partition the partitioned copy takes the third role
+  uint32_t *inBuf = adaptive ? ws.qa : nullptr;
+  const bool partition = B200_SHADE_PARTITION != 0;
+  static int partBlocks = 0;
+  if (!partBlocks) partBlocks = smCount() * 8;
   for (int b = 0; b <= p.maxPathLength; b++) {
     const int cin = b & 1, cout = cin ^ 1;
     k_bounce_reset<<<1, 1, 0, st>>>(ws.counters, cin, cout, nullptr);
-    const uint32_t *qin = (b == 0 && !adaptive) ? nullptr : qs[cin];
+    const uint32_t *qin = inBuf;
+    uint32_t *other = inBuf == ws.qb ? ws.qa : ws.qb;  // not the traced queue
+    uint32_t *third = other == ws.qa ? ws.qb : ws.qa;  // the traced queue, or at bounce 0 the free buffer
+    const uint32_t *qshade = qin;
+    uint32_t *qnext = other;
     {
       KernelScope ks(kt, KK_TRACE_CLOSEST, st);
       if (stats)
@@ -1400,21 +1459,28 @@ cudaError_t launchRenderPT(const SamplerTables *T, const Scene &sc, const Camera
         k_trace_queue<false, false, false><<<traceBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
             sc, ws, qin, ws.counters + cin, ws.counters + 3, nullptr, sm);
     }
+    if (partition && b > 0) {
+      k_partition<false><<<partBlocks, 256, 0, st>>>(sc, mats, p.numMaterials, ws, qin, ws.counters + cin, other,
+                                                     ws.counters + 5, ws.counters + 6, nullptr);
+      qshade = other;
+      qnext = third;
+    }
     {
       KernelScope ks(kt, KK_SHADE, st);
       if (nrc && p.allMaterials)
         k_pt_shade<false, true, true><<<shadeNrcBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
-            c, ws, qin, ws.counters + cin, qs[cout], ws.counters + cout, ws.counters + 2, nullptr, nf);
+            c, ws, qshade, ws.counters + cin, qnext, ws.counters + cout, ws.counters + 2, nullptr, nf);
       else if (nrc)
         k_pt_shade<false, true, false><<<shadeNrcBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
-            c, ws, qin, ws.counters + cin, qs[cout], ws.counters + cout, ws.counters + 2, nullptr, nf);
+            c, ws, qshade, ws.counters + cin, qnext, ws.counters + cout, ws.counters + 2, nullptr, nf);
       else if (p.allMaterials)
         k_pt_shade<false, false, true><<<shadeAllBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
-            c, ws, qin, ws.counters + cin, qs[cout], ws.counters + cout, ws.counters + 2, nullptr, nf);
+            c, ws, qshade, ws.counters + cin, qnext, ws.counters + cout, ws.counters + 2, nullptr, nf);
       else
         k_pt_shade<false, false, false><<<shadeBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
-            c, ws, qin, ws.counters + cin, qs[cout], ws.counters + cout, ws.counters + 2, nullptr, nf);
+            c, ws, qshade, ws.counters + cin, qnext, ws.counters + cout, ws.counters + 2, nullptr, nf);
     }
+    inBuf = qnext;
     const uint32_t *sq = nullptr;  // shadow records in queue order
     {
       KernelScope ks(kt, KK_TRACE_SHADOW, st);
@@ -1541,15 +1607,27 @@ cudaError_t launchBatchWave(const void *dtables, size_t segTableOffset, const Ba
   const Scene noScene = {};
   const PtCtx noCtx = {};
   k_batch_generate<<<unsigned((w.npaths + 255) / 256), 256, 0, st>>>(reqs, segs, w.nseg, w.npaths, ws);
-  uint32_t *qs[2] = {ws.qa, ws.qb};
+  // queue buffers as in launchRenderPT (the partition from the second bounce on)
+  uint32_t *inBuf = nullptr;
   for (int b = 0; b <= w.maxBounces; b++) {
     const int cin = b & 1, cout = cin ^ 1;
     k_bounce_reset<<<1, 1, 0, st>>>(ws.counters, cin, cout, rayCount);
-    const uint32_t *qin = b == 0 ? nullptr : qs[cin];
+    const uint32_t *qin = inBuf;
+    uint32_t *other = inBuf == ws.qb ? ws.qa : ws.qb;
+    uint32_t *third = other == ws.qa ? ws.qb : ws.qa;
+    const uint32_t *qshade = qin;
+    uint32_t *qnext = other;
     k_trace_queue<false, false, true><<<traceBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
         noScene, ws, qin, ws.counters + cin, ws.counters + 3, reqs, ShadowMatD{});
+    if (B200_SHADE_PARTITION && b > 0) {
+      k_partition<true><<<unsigned(sms * 8), 256, 0, st>>>(noScene, nullptr, 0, ws, qin, ws.counters + cin, other,
+                                                           ws.counters + 5, ws.counters + 6, reqs);
+      qshade = other;
+      qnext = third;
+    }
     k_pt_shade<true, false, true><<<shadeBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
-        noCtx, ws, qin, ws.counters + cin, qs[cout], ws.counters + cout, ws.counters + 2, reqs, NrcFrameD{});
+        noCtx, ws, qshade, ws.counters + cin, qnext, ws.counters + cout, ws.counters + 2, reqs, NrcFrameD{});
+    inBuf = qnext;
     k_trace_queue<true, false, true><<<traceBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
         noScene, ws, nullptr, ws.counters + 2, ws.counters + 4, reqs, ShadowMatD{});
   }
