@@ -225,10 +225,10 @@ class PTWorkload:
     name = "pt_instanced_spheres_1080p"
     metric = "Mrays/s"
 
-    def __init__(self, w=1920, h=1080, spp=16):
+    def __init__(self, w=1920, h=1080, spp=16, seed=1, count=64, levels=6):
         from ospray_gb300 import scenes
         self.w, self.h, self.spp = w, h, spp
-        self.data = scenes.pt_instanced_scene(width=w, height=h)
+        self.data = scenes.pt_instanced_scene(seed=seed, count=count, levels=levels, width=w, height=h)
         self.config = {"workload": self.name, "renderer": "pathtracer", "width": w, "height": h, "spp": spp,
                        "maxPathLength": 5, "roulettePathLength": 3, "instances": len(self.data["xfm"]),
                        "triangles_per_instance": int(len(self.data["index"])),
@@ -960,6 +960,9 @@ def main():
                     help="batch workload: wavefront kernels as a graph, or one persistent launch")
     ap.add_argument("--size", default=None, help="WxH override (profiling small cases; not the bench config)")
     ap.add_argument("--spp", type=int, default=None, help="spp override (path tracer; profiling only)")
+    ap.add_argument("--scene", default=None,
+                    help="path tracer scene override SEED,INSTANCES,LEVELS (the build tuner's held-out scene; "
+                         "not the bench config)")
     ap.add_argument("--nrc-frames", type=int, default=256, help="frames per arm of the learned-cache study")
     ap.add_argument("--nrc-ref-spp", type=int, default=4096, help="spp of the learned-cache study's reference image")
     ap.add_argument("--nrc-early-frames", type=int, default=4, help="frames that train --nrc-early-epochs epochs")
@@ -968,18 +971,24 @@ def main():
     if args.workload == "nrc":
         run_nrc(args)
         return
-    if args.size or args.spp:
+    if args.size or args.spp or args.scene:
         args.headline_only = True
         base = WORKLOADS[args.workload]
         w, h = (int(x) for x in args.size.split("x")) if args.size else (None, None)
+        scene = [int(x) for x in args.scene.split(",")] if args.scene else None
 
-        def make(base=base, w=w, h=h, spp=args.spp):
+        def make(base=base, w=w, h=h, spp=args.spp, scene=scene):
             kw = {}
             if w:
                 kw.update(w=w, h=h)
             if spp and base is PTWorkload:
                 kw.update(spp=spp)
-            return base(**kw)
+            if scene and base is PTWorkload:
+                kw.update(seed=scene[0], count=scene[1], levels=scene[2])
+            wl = base(**kw)
+            if scene:
+                wl.config.update(scene_seed=scene[0])
+            return wl
         WORKLOADS[args.workload] = make
     if args.warmup < 3:
         args.warmup = 3

@@ -241,9 +241,11 @@ struct BatchReqH {
 };
 
 // B200_SHADE_PARTITION: the path tracers split the queues of bounces >= 1
-// by material branch before shading (k_partition; 996 vs 910 Mrays/s on the
-// 1080p bench).  The camera rays' queue is left in pixel order, which is
-// already coherent (partitioning it too gave 977).
+// into diffuse-based hits, other hits and misses before shading
+// (k_partition; 1,051 vs 910 Mrays/s on the 1080p bench, 996 with misses
+// and other hits in one part).  The camera rays' queue is left in pixel
+// order, which is already coherent (partitioning it too gave 977 with two
+// parts).
 #ifndef B200_SHADE_PARTITION
 #define B200_SHADE_PARTITION 1
 #endif

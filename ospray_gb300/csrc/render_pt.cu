@@ -89,7 +89,14 @@ struct Workspace {
   HitBuf *hits;
   uint32_t *qa, *qb;  // path queues
   ShadowRec *shadows;
-  uint32_t *counters;  // [0] qa count, [1] qb count, [2] shadow count, [3..5] fetch counters
+  // a bounce's misses (k_partition), in the last 4 bytes per path of the
+  // shadow records' space: a bounce's shading writes at most 2 records per
+  // hit, so with n paths of which m miss, the records end at 96 (n - m)
+  // bytes and the misses start at 92 npaths + 4 (n - m) bytes, never below
+  uint32_t *misses;
+  // [0] qa count, [1] qb count, [2] shadow count, [3] closest fetch, [4]
+  // shadow fetch, [5..7] partition part sizes
+  uint32_t *counters;
 };
 
 struct FrameInfo {
@@ -217,6 +224,11 @@ struct ShadowMatD {
 #ifndef B200_REFILL_LANES
 #define B200_REFILL_LANES 8
 #endif
+// the same threshold for the shadow (any-hit) instantiations (4: 1,050, 8:
+// 1,051, 16: 1,035 Mrays/s with the closest-hit threshold at 8)
+#ifndef B200_REFILL_LANES_SHADOW
+#define B200_REFILL_LANES_SHADOW B200_REFILL_LANES
+#endif
 
 // The body is a device function so that the persistent batch kernel runs it
 // as one of its stages; a batch reads its queue with coherent loads (in the
@@ -245,7 +257,8 @@ __device__ __forceinline__ void traceQueue(Scene sc, Workspace ws, const uint32_
     // refill once at least B200_REFILL_LANES lanes wait (or no lane has a
     // ray left), so the warp does not stop for every lane that finishes
     const unsigned need = __ballot_sync(0xffffffffu, !has && !exhausted);
-    if (need && (__popc(need) >= B200_REFILL_LANES || !__any_sync(0xffffffffu, has))) {
+    if (need && (__popc(need) >= (SHADOW ? B200_REFILL_LANES_SHADOW : B200_REFILL_LANES) ||
+                 !__any_sync(0xffffffffu, has))) {
       const int leader = __ffs(need) - 1;
       uint32_t base = 0;
       if (lane == leader) base = atomicAdd(fetch, uint32_t(__popc(need)));
@@ -624,17 +637,29 @@ B200_D void scatterSurface(const PtCtx &C, const B &bsdf, const MaterialD &mat, 
 // case).
 // (A device function, a stage of the persistent batch kernel too.)
 template <bool BATCH, bool NRC, bool ALLMAT = true>
+// qmiss (a partitioned queue, k_partition): the queue is [diffuse hits |
+// other hits | misses] with the first two parts in qin (other hits at its
+// end) and the misses at the end of qmiss (Workspace::misses); cpart holds
+// the part sizes.
 __device__ __forceinline__ void ptShade(PtCtx c, Workspace ws, const uint32_t *qin, const uint32_t *cin, uint32_t *qout,
-                                        uint32_t *cout, uint32_t *cshadow, const ReqD *reqs, NrcFrameD nf) {
+                                        uint32_t *cout, uint32_t *cshadow, const ReqD *reqs, NrcFrameD nf,
+                                        const uint32_t *qmiss, const uint32_t *cpart) {
   static_assert(!(BATCH && NRC), "the radiance cache runs on single-request frames");
   const uint32_t n = *(volatile const uint32_t *)cin;
+  const uint32_t nd = qmiss ? cpart[0] : 0u, nm = qmiss ? cpart[2] : 0u;
   const uint32_t stride = gridDim.x * blockDim.x;
   // warp-uniform loop so the appends can use warp votes
   const uint32_t nround = (n + stride - 1) / stride;
   for (uint32_t r = 0; r < nround; r++) {
     const uint32_t qi = r * stride + blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = qi < n;
-    const uint32_t p = valid ? (qin ? (BATCH ? qin[qi] : __ldg(qin + qi)) : qi) : 0u;
+    uint32_t p = 0u;
+    if (valid) {
+      if (qmiss)
+        p = qi < nd ? qin[qi] : (qi < n - nm ? qin[qi + nm] : qmiss[qi]);
+      else
+        p = qin ? (BATCH ? qin[qi] : __ldg(qin + qi)) : qi;
+    }
     bool cont = false;
     // shadow requests of this lane (numLS <= MAX_NEE per bounce in the queue)
     int nsh = 0;
@@ -831,8 +856,8 @@ __device__ __forceinline__ void ptShade(PtCtx c, Workspace ws, const uint32_t *q
 template <bool BATCH, bool NRC, bool ALLMAT = true>
 __global__ void __launch_bounds__(128, B200_SHADE_MINBLOCKS)
     k_pt_shade(PtCtx c, Workspace ws, const uint32_t *qin, const uint32_t *cin, uint32_t *qout, uint32_t *cout,
-               uint32_t *cshadow, const ReqD *reqs, NrcFrameD nf) {
-  ptShade<BATCH, NRC, ALLMAT>(c, ws, qin, cin, qout, cout, cshadow, reqs, nf);
+               uint32_t *cshadow, const ReqD *reqs, NrcFrameD nf, const uint32_t *qmiss, const uint32_t *cpart) {
+  ptShade<BATCH, NRC, ALLMAT>(c, ws, qin, cin, qout, cout, cshadow, reqs, nf, qmiss, cpart);
 }
 
 // averages each pixel's samples into the framebuffer (ScreenSample_accumulate
@@ -1112,7 +1137,7 @@ B200_STAGE void persistTrace(Workspace ws, const uint32_t *queue, const uint32_t
 }
 B200_STAGE void persistShade(Workspace ws, const uint32_t *qin, const uint32_t *cin, uint32_t *qout, uint32_t *cout,
                              uint32_t *cshadow, const ReqD *reqs) {
-  ptShade<true, false, true>(PtCtx{}, ws, qin, cin, qout, cout, cshadow, reqs, NrcFrameD{});
+  ptShade<true, false, true>(PtCtx{}, ws, qin, cin, qout, cout, cshadow, reqs, NrcFrameD{}, nullptr, nullptr);
 }
 __global__ void __launch_bounds__(TRACE_BLOCK, B200_PERSIST_MINBLOCKS) k_batch_persistent(BatchRunD R) {
   // little state lives across the stages (the wave's fields are re-read
@@ -1298,18 +1323,21 @@ __global__ void k_bounce_reset(uint32_t *counters, int cin, int cout, unsigned l
   counters[4] = 0;
   counters[5] = 0;
   counters[6] = 0;
+  counters[7] = 0;
 }
 
 // Splits a bounce's queue of traced paths by what their shading runs: the
 // front of `out` gets the hits on diffuse-based materials (principled with
-// metallic < 0.5, obj), the back everything else (conductors, metal, glass,
-// misses), so that most warps of the shading kernel take one branch of the
-// BSDF code.  front / back count the two ends (cleared per bounce).
+// metallic < 0.5, obj), its back the other hits (conductors, metal, glass),
+// and the misses go to the end of ws.misses, so that most warps of the
+// shading kernel take one branch of the BSDF code.  cpart[0..2] count the
+// three parts (cleared per bounce).  The shading kernel reads them in the
+// order diffuse, other, misses.  (`out` is not the traced queue: this
+// kernel reads that one throughout.)
 // In a batch (BATCH) each path's request gives the scene and materials.
 template <bool BATCH>
 __global__ void k_partition(Scene sc, const MaterialD *mats, int nmats, Workspace ws, const uint32_t *qin,
-                            const uint32_t *count, uint32_t *out, uint32_t *front, uint32_t *back,
-                            const ReqD *reqs) {
+                            const uint32_t *count, uint32_t *out, uint32_t *cpart, const ReqD *reqs) {
   const uint32_t n = *(volatile const uint32_t *)count;
   const uint32_t stride = gridDim.x * blockDim.x;
   const uint32_t nround = (n + stride - 1) / stride;  // warp-uniform loop (warp appends)
@@ -1317,11 +1345,12 @@ __global__ void k_partition(Scene sc, const MaterialD *mats, int nmats, Workspac
     const uint32_t i = r * stride + blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = i < n;
     uint32_t p = 0;
-    bool diffuse = false;
+    bool diffuse = false, hit = false;
     if (valid) {
       p = qin ? qin[i] : i;
       const float4 a = ws.hits[p].a;
-      if (a.w != 0.f) {
+      hit = a.w != 0.f;
+      if (hit) {
         const Entry *entries = sc.entries;
         const MaterialD *M = mats;
         int nm = nmats;
@@ -1340,9 +1369,17 @@ __global__ void k_partition(Scene sc, const MaterialD *mats, int nmats, Workspac
         }
       }
     }
-    const uint32_t f = warpAppend(valid && diffuse, front);
-    const uint32_t k = warpAppend(valid && !diffuse, back);
-    if (valid) out[diffuse ? f : n - 1u - k] = p;
+    const uint32_t f = warpAppend(valid && diffuse, cpart);
+    const uint32_t k = warpAppend(valid && hit && !diffuse, cpart + 1);
+    const uint32_t m = warpAppend(valid && !hit, cpart + 2);
+    if (valid) {
+      if (diffuse)
+        out[f] = p;
+      else if (hit)
+        out[n - 1u - k] = p;
+      else
+        ws.misses[n - 1u - m] = p;
+    }
   }
 }
 
@@ -1372,6 +1409,7 @@ Workspace carveWorkspace(void *workspace, long long npaths) {
   ws.qa = (uint32_t *)carve(4 * npaths);
   ws.qb = (uint32_t *)carve(4 * npaths);
   ws.shadows = (ShadowRec *)carve(sizeof(ShadowRec) * 2 * npaths);
+  ws.misses = reinterpret_cast<uint32_t *>(ws.shadows + 2 * npaths) - npaths;
   ws.counters = (uint32_t *)carve(64);
   return ws;
 }
@@ -1459,26 +1497,29 @@ cudaError_t launchRenderPT(const SamplerTables *T, const Scene &sc, const Camera
         k_trace_queue<false, false, false><<<traceBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
             sc, ws, qin, ws.counters + cin, ws.counters + 3, nullptr, sm);
     }
+    const uint32_t *qmiss = nullptr, *cpart = nullptr;
     if (partition && b > 0) {
       k_partition<false><<<partBlocks, 256, 0, st>>>(sc, mats, p.numMaterials, ws, qin, ws.counters + cin, other,
-                                                     ws.counters + 5, ws.counters + 6, nullptr);
+                                                     ws.counters + 5, nullptr);
       qshade = other;
       qnext = third;
+      qmiss = ws.misses;
+      cpart = ws.counters + 5;
     }
     {
       KernelScope ks(kt, KK_SHADE, st);
       if (nrc && p.allMaterials)
         k_pt_shade<false, true, true><<<shadeNrcBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
-            c, ws, qshade, ws.counters + cin, qnext, ws.counters + cout, ws.counters + 2, nullptr, nf);
+            c, ws, qshade, ws.counters + cin, qnext, ws.counters + cout, ws.counters + 2, nullptr, nf, qmiss, cpart);
       else if (nrc)
         k_pt_shade<false, true, false><<<shadeNrcBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
-            c, ws, qshade, ws.counters + cin, qnext, ws.counters + cout, ws.counters + 2, nullptr, nf);
+            c, ws, qshade, ws.counters + cin, qnext, ws.counters + cout, ws.counters + 2, nullptr, nf, qmiss, cpart);
       else if (p.allMaterials)
         k_pt_shade<false, false, true><<<shadeAllBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
-            c, ws, qshade, ws.counters + cin, qnext, ws.counters + cout, ws.counters + 2, nullptr, nf);
+            c, ws, qshade, ws.counters + cin, qnext, ws.counters + cout, ws.counters + 2, nullptr, nf, qmiss, cpart);
       else
         k_pt_shade<false, false, false><<<shadeBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
-            c, ws, qshade, ws.counters + cin, qnext, ws.counters + cout, ws.counters + 2, nullptr, nf);
+            c, ws, qshade, ws.counters + cin, qnext, ws.counters + cout, ws.counters + 2, nullptr, nf, qmiss, cpart);
     }
     inBuf = qnext;
     const uint32_t *sq = nullptr;  // shadow records in queue order
@@ -1619,14 +1660,18 @@ cudaError_t launchBatchWave(const void *dtables, size_t segTableOffset, const Ba
     uint32_t *qnext = other;
     k_trace_queue<false, false, true><<<traceBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
         noScene, ws, qin, ws.counters + cin, ws.counters + 3, reqs, ShadowMatD{});
+    const uint32_t *qmiss = nullptr, *cpart = nullptr;
     if (B200_SHADE_PARTITION && b > 0) {
       k_partition<true><<<unsigned(sms * 8), 256, 0, st>>>(noScene, nullptr, 0, ws, qin, ws.counters + cin, other,
-                                                           ws.counters + 5, ws.counters + 6, reqs);
+                                                           ws.counters + 5, reqs);
       qshade = other;
       qnext = third;
+      qmiss = ws.misses;
+      cpart = ws.counters + 5;
     }
     k_pt_shade<true, false, true><<<shadeBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
-        noCtx, ws, qshade, ws.counters + cin, qnext, ws.counters + cout, ws.counters + 2, reqs, NrcFrameD{});
+        noCtx, ws, qshade, ws.counters + cin, qnext, ws.counters + cout, ws.counters + 2, reqs, NrcFrameD{}, qmiss,
+        cpart);
     inBuf = qnext;
     k_trace_queue<true, false, true><<<traceBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
         noScene, ws, nullptr, ws.counters + 2, ws.counters + 4, reqs, ShadowMatD{});
