@@ -264,6 +264,11 @@ B200_D float min3f(float a, float b, float c) {
   return r;
 }
 
+// byte b of w as a float (an integer-to-float conversion: forming it as a
+// byte permute into the mantissa of 2^23 minus 2^23 instead cost the
+// issue-bound path-tracer trace kernels 3 %)
+B200_D float u8f(uint32_t w, int b) { return float((w >> (8 * b)) & 0xffu); }
+
 // Intersects the node's 8 child boxes with the ray (direction octant oct).
 // keys: the hit internal children, child slot i at bit i ^ oct, so the
 // lowest set bit is the next child in the octant's visiting order.  prims:
@@ -296,13 +301,13 @@ B200_D void intersectChildren(const NodeView &n, V3 org, V3 rdir, float tnear, f
   for (int i = 0; i < 8; i++) {
     const uint32_t meta = n.meta(i);
     if (meta == 0) continue;
-    const int sh = 8 * (i & 3);
-    const float tnx = fmaf(float(((i < 4 ? nx0 : nx1) >> sh) & 0xffu), ax, bx);
-    const float tfx = fmaf(float(((i < 4 ? fx0 : fx1) >> sh) & 0xffu), ax, bx);
-    const float tny = fmaf(float(((i < 4 ? ny0 : ny1) >> sh) & 0xffu), ay, by);
-    const float tfy = fmaf(float(((i < 4 ? fy0 : fy1) >> sh) & 0xffu), ay, by);
-    const float tnz = fmaf(float(((i < 4 ? nz0 : nz1) >> sh) & 0xffu), az, bz);
-    const float tfz = fmaf(float(((i < 4 ? fz0 : fz1) >> sh) & 0xffu), az, bz);
+    const int by8 = i & 3;
+    const float tnx = fmaf(u8f(i < 4 ? nx0 : nx1, by8), ax, bx);
+    const float tfx = fmaf(u8f(i < 4 ? fx0 : fx1, by8), ax, bx);
+    const float tny = fmaf(u8f(i < 4 ? ny0 : ny1, by8), ay, by);
+    const float tfy = fmaf(u8f(i < 4 ? fy0 : fy1, by8), ay, by);
+    const float tnz = fmaf(u8f(i < 4 ? nz0 : nz1, by8), az, bz);
+    const float tfz = fmaf(u8f(i < 4 ? fz0 : fz1, by8), az, bz);
     const float t0 = max3f(tnx, tny, fmaxf(tnz, tnear));
     const float t1 = min3f(tfx, tfy, tfz) * 1.0000008f;
     if (t0 <= fminf(t1, tmax)) {
