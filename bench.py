@@ -70,9 +70,9 @@ TRAFFIC = {
 LIMITER = {
     "pt_instanced_spheres_1080p": {
         "bound": "issue",
-        "issue_active": {"closest": 0.661, "shadow": 0.746},
-        "lanes_per_instruction": {"closest": 14.31, "shadow": 9.81},
-        "l2_gbs": {"closest": 1045.0, "shadow": 1246.0},
+        "issue_active": {"closest": 0.667, "shadow": 0.745},
+        "lanes_per_instruction": {"closest": 14.59, "shadow": 10.39},
+        "l2_gbs": {"closest": 1052.0, "shadow": 1576.0},
         "source": "profiles/k_trace_queue_pt_instanced_480x270_limiter.md"},
     "scivis_volume_512cube_1024": {
         "bound": "latency",

@@ -302,7 +302,7 @@ __device__ __forceinline__ void traceQueue(Scene sc, Workspace ws, const uint32_
       }
     }
     if (!__any_sync(0xffffffffu, has)) break;
-    if (has && tv.step<STATS>(S, &ts)) {
+    if (has && tv.step<STATS, true, B200_QUEUE_PRIMS_PER_STEP, B200_QUEUE_POSTPONE_LANES>(S, &ts)) {
       if (TRANSP) {
         bool done = true;
         if (!tv.found) {

@@ -356,8 +356,26 @@ B200_D uint32_t octantOf(V3 d) {
 #ifndef B200_TRACE_MINBLOCKS
 #define B200_TRACE_MINBLOCKS 1
 #endif
+// Primitive tests per traversal step, and the lane count below which a
+// lane postpones its primitive group while a node group is pending: the
+// persistent queue kernels (B200_QUEUE_*, whose warps refill finished lanes)
+// run one test per step and never postpone the first (1,102 Mrays/s on the
+// 1080p path tracer; postponing below 8 lanes: 1,077, below 16: 1,073; 2
+// tests per step: 1,060, 4: 1,042, a whole group: 1,039); traceRay (whole
+// warps that trace together, the AO and SciVis kernels) keeps a whole group
+// per step, postponing below 8 lanes (AO within its run-to-run spread
+// either way: 1,343-1,390 Mrays/s).
+#ifndef B200_PRIMS_PER_STEP
+#define B200_PRIMS_PER_STEP 64
+#endif
 #ifndef B200_POSTPONE_LANES
 #define B200_POSTPONE_LANES 8
+#endif
+#ifndef B200_QUEUE_PRIMS_PER_STEP
+#define B200_QUEUE_PRIMS_PER_STEP 1
+#endif
+#ifndef B200_QUEUE_POSTPONE_LANES
+#define B200_QUEUE_POSTPONE_LANES 0
 #endif
 constexpr int TRACE_BLOCK = 128;
 constexpr int STACK_SMEM = B200_STACK_SMEM;
@@ -517,8 +535,9 @@ struct Traverser {
     }
   }
 
-  // one traversal step; true when the ray is finished (USER as for finish)
-  template <bool STATS, bool USER = true>
+  // one traversal step; true when the ray is finished (USER as for finish;
+  // PPS and POSTPONE as B200_PRIMS_PER_STEP and B200_POSTPONE_LANES)
+  template <bool STATS, bool USER = true, int PPS = B200_PRIMS_PER_STEP, int POSTPONE = B200_POSTPONE_LANES>
   B200_D bool step(const Scene &sc, TraceStats *ts) {
     // 1) the next node of the current node group
     if (nbits & 0xffu) {
@@ -536,13 +555,16 @@ struct Traverser {
       pbase = n.primBase();
       pbits = hitPrims;
     }
-    // 2) the primitives of the current primitive group
-    while (pbits) {
-      if ((nbits & 0xffu) && __popc(__activemask()) < B200_POSTPONE_LANES) {
+    // 2) the primitives of the current primitive group (at most PPS per
+    // step: the rest wait for the next step, on the stack when a node group
+    // is pending)
+    for (int np = 0; pbits; np++) {
+      if ((nbits & 0xffu) && (np >= PPS || __popc(__activemask()) < POSTPONE)) {
         st.push(make_uint2(pbase, pbits | (inBlas ? G_BPRIM : G_TINST)), sc.status);
         pbits = 0;
         break;
       }
+      if (np >= PPS) break;
       const uint32_t k = uint32_t(__ffs(pbits) - 1);
       pbits &= pbits - 1u;
       const uint32_t slot = pbase + k;
