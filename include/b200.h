@@ -128,6 +128,16 @@ int b200_scene_set_mesh_attributes(b200_scene scene, int geom, const float *norm
  * material_id indexes the renderer's material list (or -1 for none) */
 int b200_scene_add_instance(b200_scene scene, int geom, uint32_t inst_id, uint32_t geom_id, const float *xfm,
                             int material_id);
+/* A motion-blurred (instance, geometric model) pair (Instance "motion.transform"
+ * and "time", MotionTransform::readParams common/MotionTransform.cpp:10-66):
+ * nkeys >= 2 row-major 3x4 transforms `xfms` at times evenly spaced over
+ * [t0, t1] (t1 < t0 is raised to t0).  A ray at time t sees the geometry
+ * under the two keys around t blended component-wise, (1 - f) A + f B, the
+ * interpolation Embree applies to key-framed instance matrices; times
+ * outside [t0, t1] take the end keys.  The TLAS bounds the instance by the
+ * union of its keys' boxes, which contains every blend. */
+int b200_scene_add_instance_motion(b200_scene scene, int geom, uint32_t inst_id, uint32_t geom_id,
+                                   const float *xfms, int nkeys, float t0, float t1, int material_id);
 /* build quality of the commits that follow (Group/World "dynamicScene",
  * common/Group.cpp:17-31 selects Embree's low build quality): dynamic != 0
  * builds the plain LBVH hierarchy (fastest build); the default splits the
@@ -155,13 +165,27 @@ int b200_trace(b200_scene scene, const float *rays, int64_t n, int occlusion, fl
  * B200_CAMERA_ORTHOGRAPHIC (OrthographicCamera::commit
  * camera/OrthographicCamera.cpp:25-50: `height` of the image plane and
  * aspect) or B200_CAMERA_PANORAMIC (PanoramicCamera, equirectangular; no
- * stereo).  Stereo, depth of field and motion blur are not built. */
+ * stereo).
+ * Shutter (Camera::commit camera/Camera.cpp:44-52,100-119 and
+ * Camera_shutterTime camera/Camera.ih:33-42): "shutter" [lower, upper]
+ * clamped to [0, 1], "shutterType" (OSPShutterType: 0 global, 1 rolling
+ * right, 2 rolling left, 3 rolling down, 4 rolling up) and
+ * "rollingShutterDuration".  The path tracer draws each camera sample's
+ * time from its own sample stream when the shutter is open (global: upper >
+ * lower; rolling: duration > 0), else takes the shutter time of 0.5; the AO
+ * and SciVis renderers always take 0.5.  The ray's time places
+ * motion-blurred instances (b200_scene_add_instance_motion).  A
+ * zero-initialised shutter traces every ray at time 0; OSPRay's default is
+ * [0.5, 0.5].  Stereo, depth of field and camera motion are not built. */
 enum { B200_CAMERA_PERSPECTIVE = 0, B200_CAMERA_ORTHOGRAPHIC = 1, B200_CAMERA_PANORAMIC = 2 };
 typedef struct {
   float position[3], direction[3], up[3];
   float fovy, aspect, nearClip;
   int type;     /* default 0: perspective */
   float height; /* orthographic: image-plane height (OSPRay default 1) */
+  float shutter[2];
+  int shutterType;
+  float rollingShutterDuration;
 } b200_camera_desc;
 
 /* ---- framebuffer (LocalFrameBuffer, modules/cpu/fb/LocalFB.cpp:23-226;

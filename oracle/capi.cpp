@@ -36,6 +36,9 @@ struct OrCamera {
   float fovy, aspect, nearClip;
   int type;  // 0 perspective, 1 orthographic, 2 panoramic
   float height;  // orthographic image height
+  float shutter[2];
+  int shutterType;
+  float rollingDuration;
 };
 
 extern "C" {
@@ -188,6 +191,24 @@ void or_scene_add_instance(void *sp, int geom, uint32_t instID, uint32_t geomID,
   s.entries.push_back(e);
 }
 
+// xfms: nkeys >= 2 row-major 3x4 keys over [t0, t1]
+void or_scene_add_instance_motion(void *sp, int geom, uint32_t instID, uint32_t geomID, const float *xfms, int nkeys,
+                                  float t0, float t1, int material) {
+  Scene &s = *static_cast<Scene *>(sp);
+  InstanceEntry e;
+  e.material = material;
+  e.geom = geom;
+  e.instID = instID;
+  e.geomID = geomID;
+  e.identity = false;
+  e.xfm = fromRowMajor(xfms);
+  e.rcp = rcpAffine(e.xfm);
+  e.motion.assign(xfms, xfms + 12 * size_t(nkeys));
+  e.t0 = t0;
+  e.t1 = t1 < t0 ? t0 : t1;
+  s.entries.push_back(e);
+}
+
 void or_scene_commit(void *sp) { static_cast<Scene *>(sp)->commit(); }
 
 // rays: n x 8 floats (org xyz, tnear, dir xyz, tfar).
@@ -295,8 +316,9 @@ void or_render_ao(void *sp, const OrCamera *c, int pixelFilter, int W, int H, in
                   float aoRadius, float aoIntensity, const float *bg, int frames, OrFrame *out, int nthreads,
                   const OrAoExtra *extra) {
   const Scene &s = *static_cast<Scene *>(sp);
-  const Camera cam = makeCamera({c->pos[0], c->pos[1], c->pos[2]}, {c->dir[0], c->dir[1], c->dir[2]},
-                                {c->up[0], c->up[1], c->up[2]}, c->fovy, c->aspect, c->nearClip, c->type, c->height);
+  Camera cam = makeCamera({c->pos[0], c->pos[1], c->pos[2]}, {c->dir[0], c->dir[1], c->dir[2]},
+                          {c->up[0], c->up[1], c->up[2]}, c->fovy, c->aspect, c->nearClip, c->type, c->height);
+  setShutter(cam, c->shutter[0], c->shutter[1], c->shutterType, c->rollingDuration);
   PixelFilter pf;
   pf.init(pixelFilter);
   FrameBuffer fb;

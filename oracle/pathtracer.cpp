@@ -334,6 +334,8 @@ void renderPT(const Scene &sc, const PtLights &lights, const std::vector<Materia
         const V2 center = {(float(x) + 0.5f) * rcpSize.x, (float(y) + 0.5f) * rcpSize.y};
         const V2 screen = {center.x + pfs.x * rcpSize.x, center.y + pfs.y * rcpSize.y};
         Ray ray = cameraRay(cam, screen);
+        // the camera sample's time (PathTracer.ispc:177-180, Camera_shutterTime)
+        rayTime = shutterTime(cam, screen, cam.needTime ? ld.finalizeDim4(ss234) : 0.5f);
         // Renderer_getMaxDepth at the sample's screen position (PathTracer.ispc:189-192)
         if (p.maxDepth) ray.tfar = std::fmin(ray.tfar, std::fmax(0.f, p.maxDepth->get(screen, 0.f).x));
         const PathOut o = samplePath(c, ld, ray, cameraCone(cam, screen, rcpSize.y), center);
@@ -369,6 +371,9 @@ struct OrCameraPT {
   float fovy, aspect, nearClip;
   int type;  // 0 perspective, 1 orthographic, 2 panoramic
   float height;  // orthographic image height
+  float shutter[2];
+  int shutterType;
+  float rollingDuration;
 };
 
 struct OrPtScene {
@@ -471,8 +476,9 @@ void or_render_pt(void *scp, void *ptp, const OrCameraPT *cam, const OrPtParams 
                   int y0, int y1, float *color, float *depth, uint32_t *ids, int nthreads) {
   const Scene &sc = *static_cast<Scene *>(scp);
   const OrPtScene &pt = *static_cast<OrPtScene *>(ptp);
-  const Camera c = makeCamera({cam->pos[0], cam->pos[1], cam->pos[2]}, {cam->dir[0], cam->dir[1], cam->dir[2]},
-                              {cam->up[0], cam->up[1], cam->up[2]}, cam->fovy, cam->aspect, cam->nearClip, cam->type, cam->height);
+  Camera c = makeCamera({cam->pos[0], cam->pos[1], cam->pos[2]}, {cam->dir[0], cam->dir[1], cam->dir[2]},
+                        {cam->up[0], cam->up[1], cam->up[2]}, cam->fovy, cam->aspect, cam->nearClip, cam->type, cam->height);
+  setShutter(c, cam->shutter[0], cam->shutter[1], cam->shutterType, cam->rollingDuration);
   PixelFilter pf;
   pf.init(pp->pixelFilter);
   PtParams p = {pp->spp, pp->maxPathLength, pp->roulettePathLength, pp->maxScatteringEvents, pp->lightSamples,

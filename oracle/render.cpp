@@ -15,6 +15,22 @@ const Tables &tables() {
 std::atomic<uint64_t> g_rayCount{0};
 thread_local uint64_t tl_rays = 0;  // flushed into g_rayCount once per image row
 
+void setShutter(Camera &c, float lower, float upper, int type, float duration) {
+  auto cl = [](float v) { return std::fmin(std::fmax(v, 0.f), 1.f); };
+  float lo = cl(lower), hi = cl(upper);
+  if (lo > hi) lo = hi;
+  const float dur = std::fmin(std::fmax(duration, 0.f), hi - lo);
+  c.needTime = type == 0 ? hi - lo != 0.f : dur != 0.f;
+  if (type != 0) {
+    hi -= dur;
+    if (type == 2 || type == 3) std::swap(lo, hi);
+  }
+  c.shutterLo = lo;
+  c.shutterHi = hi;
+  c.rollingDuration = dur;
+  c.shutterMode = type == 0 ? 0 : (type == 1 || type == 2 ? 1 : 2);
+}
+
 Camera makeCamera(V3 pos, V3 dir, V3 up, float fovy, float aspect, float nearClip, int type, float height) {
   Camera c;
   c.type = type;
@@ -198,15 +214,19 @@ DG postIntersect(const Scene &s, const Ray &ray, const Hit &hit, bool attrs) {
   } else {
     eps = g.spheres[hit.primID].w * ulpEpsilon;  // Spheres_postIntersect, also for discs
   }
-  dg.dPds = xfmVector(e->xfm.l, dPds);  // Instance_postIntersect (common/Instance.ih:95-98)
-  dg.dPdt = xfmVector(e->xfm.l, dg.dPdt);
+  // the instance transform (motion blur: at the ray time, Instance.ih:57-91)
+  const bool moving = e->motion.size() >= 24;
+  const A3 X = moving ? e->xfmAt(rayTime) : e->xfm;
+  const A3 R = moving ? rcpAffine(X) : e->rcp;
+  dg.dPds = xfmVector(X.l, dPds);  // Instance_postIntersect (common/Instance.ih:95-98)
+  dg.dPdt = xfmVector(X.l, dg.dPdt);
   if (g.type != 0 || g.boxFaces) dg.st = {0.f, 0.f};  // spheres, boxes: no texture coordinates in these scenes
   // Instance_postIntersect: normals by the inverse transpose, epsilon by the
   // largest diagonal scale
-  const L3 it = transposed(e->rcp.l);
+  const L3 it = transposed(R.l);
   Ns = xfmVector(it, Ns);
   Ng = xfmVector(it, Ng);
-  eps *= std::fmax(std::fabs(e->xfm.l.vx.x), std::fmax(std::fabs(e->xfm.l.vy.y), std::fabs(e->xfm.l.vz.z)));
+  eps *= std::fmax(std::fabs(X.l.vx.x), std::fmax(std::fabs(X.l.vy.y), std::fabs(X.l.vz.z)));
   // calcEpsilon(P, dir, t)
   const float e2 = std::fmax(reduce_max(vabs(dg.P)), reduce_max(vabs(ray.dir)) * hit.t) * ulpEpsilon;
   dg.epsilon = std::fmax(eps, e2);
@@ -297,6 +317,7 @@ void renderAO(const Scene &s, const Camera &cam, const PixelFilter &pf, const AO
         const V2 center = {(float(x) + 0.5f) * rcpSize.x, (float(y) + 0.5f) * rcpSize.y};
         const V2 screen = {center.x + pfs.x * rcpSize.x, center.y + pfs.y * rcpSize.y};
         Ray ray = cameraRay(cam, screen);
+        rayTime = shutterTime(cam, screen, 0.5f);  // RendererRenderTaskFn.inl:64: time sample 0.5
         // Renderer_getMaxDepth at the pixel centre (RendererRenderTaskFn.inl:41-42)
         if (p.maxDepth) ray.tfar = std::fmin(ray.tfar, std::fmax(0.f, p.maxDepth->get(center, 0.f).x));
         const V2 cone = cameraCone(cam, screen, rcpSize.y);

@@ -30,7 +30,25 @@ struct Camera {
   V3 org, dir_00, du_size, dv_up;
   float nearClip;
   int type = 0;
+  // the shutter after Camera::commit (camera/Camera.cpp:44-52,100-119):
+  // mode 0 global, 1 rolling along screen x, 2 along screen y
+  float shutterLo = 0.5f, shutterHi = 0.5f, rollingDuration = 0.f;
+  int shutterMode = 0;
+  bool needTime = false;
 };
+
+// Camera::commit's shutter from the "shutter", "shutterType" and
+// "rollingShutterDuration" parameters
+void setShutter(Camera &c, float lower, float upper, int type, float duration);
+
+// Camera_shutterTime (camera/Camera.ih:33-42); rkcommon lerp(f, a, b) = (1 - f) a + f b
+inline float shutterTime(const Camera &c, V2 screen, float time) {
+  if (c.shutterMode == 0) return (1.f - time) * c.shutterLo + time * c.shutterHi;
+  const float t = time * c.rollingDuration;
+  const float pos = c.shutterMode == 1 ? screen.x : screen.y;
+  const float v = t + ((1.f - pos) * c.shutterLo + pos * c.shutterHi);
+  return std::fmin(std::fmax(v, 0.f), 1.f);
+}
 
 // PerspectiveCamera::commit (camera/PerspectiveCamera.cpp:30-117),
 // OrthographicCamera::commit (camera/OrthographicCamera.cpp:25-50) and

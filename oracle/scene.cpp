@@ -278,19 +278,47 @@ void Geometry::build() {
   }
 }
 
+thread_local float rayTime = 0.f;
+
+namespace {
+A3 fromRowMajor12(const float *X) {
+  A3 a;
+  a.l.vx = {X[0], X[4], X[8]};
+  a.l.vy = {X[1], X[5], X[9]};
+  a.l.vz = {X[2], X[6], X[10]};
+  a.p = {X[3], X[7], X[11]};
+  return a;
+}
+}  // namespace
+
+A3 InstanceEntry::xfmAt(float time) const {
+  const int n = int(motion.size() / 12);
+  float f = t1 > t0 ? (time - t0) / (t1 - t0) * float(n - 1) : 0.f;
+  f = std::fmin(std::fmax(f, 0.f), float(n - 1));
+  const int fi = int(std::floor(f)), i = fi < n - 2 ? fi : n - 2;
+  const float u = f - float(i), w = 1.f - u;
+  float X[12];
+  for (int k = 0; k < 12; k++) X[k] = w * motion[12 * i + k] + u * motion[12 * (i + 1) + k];
+  return fromRowMajor12(X);
+}
+
 void Scene::commit() {
   for (auto &g : geoms) g.build();
   for (auto &e : entries) {
     const Box b = geoms[e.geom].nodes.empty() ? Box{v3(0), v3(0)} : geoms[e.geom].nodes[0].box;
-    if (e.identity) {
+    const int nkeys = int(e.motion.size() / 12);
+    if (e.identity && nkeys < 2) {
       e.worldBox = b;
       continue;
     }
     Box wb = emptyBox();
-    for (int c = 0; c < 8; c++) {
-      const V3 p = {c & 1 ? b.hi.x : b.lo.x, c & 2 ? b.hi.y : b.lo.y, c & 4 ? b.hi.z : b.lo.z};
-      const V3 q = xfmPoint(e.xfm, p);
-      grow(wb, {q, q});
+    for (int k = 0; k < (nkeys >= 2 ? nkeys : 1); k++) {  // the union over the keys
+      const A3 X = nkeys >= 2 ? fromRowMajor12(&e.motion[12 * k]) : e.xfm;
+      for (int c = 0; c < 8; c++) {
+        const V3 p = {c & 1 ? b.hi.x : b.lo.x, c & 2 ? b.hi.y : b.lo.y, c & 4 ? b.hi.z : b.lo.z};
+        const V3 q = xfmPoint(X, p);
+        grow(wb, {q, q});
+      }
     }
     // pad by a relative ulp margin for the transform's rounding
     const V3 pad = 1e-6f * (vabs(wb.lo) + vabs(wb.hi)) + v3(1e-30f);
@@ -390,7 +418,11 @@ bool traverse(const Scene &s, const Ray &ray, Hit &hit) {
       const InstanceEntry &e = s.entries[ei];
       if (!hitBox(e.worldBox, ray.org, rdir, ray.tnear, hit.t)) continue;
       V3 o = ray.org, d = ray.dir;
-      if (!e.identity) {
+      if (e.motion.size() >= 24) {
+        const A3 r = rcpAffine(e.xfmAt(rayTime));
+        o = xfmPoint(r, ray.org);
+        d = xfmVector(r.l, ray.dir);
+      } else if (!e.identity) {
         o = xfmPoint(e.rcp, ray.org);
         d = xfmVector(e.rcp.l, ray.dir);
       }

@@ -79,7 +79,22 @@ struct InstanceEntry {
   int material = -1;  // renderer material slot of the geometric model
   A3 xfm, rcp;
   Box worldBox;
+  // motion blur: >= 2 row-major 3x4 keys evenly spaced over [t0, t1]
+  std::vector<float> motion;
+  float t0 = 0.f, t1 = 1.f;
+  // the transform at `time`: the two keys around it blended component-wise,
+  // (1 - f) A + f B, times outside [t0, t1] taking the end keys (Embree's
+  // key-framed instance, restated)
+  A3 xfmAt(float time) const;
 };
+
+// rkcommon rcp(AffineSpace3f)
+A3 rcpAffine(const A3 &a);
+
+// The ray time of the calling thread's current camera sample (motion blur):
+// every query and postIntersect of that sample (camera, extension, shadow
+// and AO rays) is taken at it.  Set by the renderers per sample; 0 otherwise.
+extern thread_local float rayTime;
 
 struct Scene {
   std::vector<Geometry> geoms;

@@ -40,7 +40,9 @@ class B200Error(RuntimeError):
 class CameraDesc(ctypes.Structure):
     _fields_ = [("position", ctypes.c_float * 3), ("direction", ctypes.c_float * 3),
                 ("up", ctypes.c_float * 3), ("fovy", ctypes.c_float), ("aspect", ctypes.c_float),
-                ("nearClip", ctypes.c_float), ("type", ctypes.c_int), ("height", ctypes.c_float)]
+                ("nearClip", ctypes.c_float), ("type", ctypes.c_int), ("height", ctypes.c_float),
+                ("shutter", ctypes.c_float * 2), ("shutterType", ctypes.c_int),
+                ("rollingShutterDuration", ctypes.c_float)]
 
 
 class AOParams(ctypes.Structure):
@@ -322,6 +324,7 @@ def lib():
             "b200_scene_add_discs": (I, [P, P, I64, P, ctypes.POINTER(I)]),
             "b200_scene_add_planes": (I, [P, P, I64, P, ctypes.POINTER(I)]),
             "b200_scene_add_instance": (I, [P, I, U32, U32, P, I]),
+            "b200_scene_add_instance_motion": (I, [P, I, U32, U32, P, I, ctypes.c_float, ctypes.c_float, I]),
             "b200_scene_commit": (I, [P]),
             "b200_scene_set_dynamic": (I, [P, I]),
             "b200_scene_bounds": (I, [P, P]),
@@ -586,6 +589,12 @@ class Scene:
         x = None if xfm is None else np.ascontiguousarray(xfm, dtype=np.float32).reshape(12)
         self.device._check(lib().b200_scene_add_instance(self._h, geom, inst_id, geom_id, _ptr(x), material))
 
+    def add_instance_motion(self, geom, inst_id, geom_id, xfms, time=(0.0, 1.0), material=-1):
+        """xfms: (n >= 2, 3, 4) key transforms evenly spaced over `time`."""
+        x = np.ascontiguousarray(xfms, dtype=np.float32).reshape(-1, 12)
+        self.device._check(lib().b200_scene_add_instance_motion(self._h, geom, inst_id, geom_id, _ptr(x), len(x),
+                                                                float(time[0]), float(time[1]), material))
+
     def set_dynamic(self, dynamic=True):
         """LBVH-only builds for the commits that follow (default: binned-SAH splits)."""
         self.device._check(lib().b200_scene_set_dynamic(self._h, int(bool(dynamic))))
@@ -725,10 +734,13 @@ CAMERA_PERSPECTIVE, CAMERA_ORTHOGRAPHIC, CAMERA_PANORAMIC = 0, 1, 2
 
 
 def camera_desc(position, direction, up=(0, 1, 0), fovy=60.0, aspect=1.0, near_clip=1e-6, kind=CAMERA_PERSPECTIVE,
-                height=1.0):
-    """kind: CAMERA_PERSPECTIVE (fovy), CAMERA_ORTHOGRAPHIC (image `height`) or CAMERA_PANORAMIC."""
+                height=1.0, shutter=(0.5, 0.5), shutter_type=0, rolling_shutter_duration=0.0):
+    """kind: CAMERA_PERSPECTIVE (fovy), CAMERA_ORTHOGRAPHIC (image `height`) or CAMERA_PANORAMIC.
+    shutter / shutter_type (OSPShutterType) / rolling_shutter_duration: the ray times (motion blur)."""
     c = CameraDesc()
     c.type, c.height = int(kind), float(height)
+    c.shutter[:] = [float(shutter[0]), float(shutter[1])]
+    c.shutterType, c.rollingShutterDuration = int(shutter_type), float(rolling_shutter_duration)
     c.position[:] = list(map(float, position))
     c.direction[:] = list(map(float, direction))
     c.up[:] = list(map(float, up))

@@ -149,6 +149,7 @@ DeviceObj::~DeviceObj() {
   cudaFree(pickBuf);
   if (albedo) cudaFree(albedo);
   if (ptWs) cudaFree(ptWs);
+  if (ptTimes) cudaFree(ptTimes);
   delete timer;
   for (auto &L : luts) {
     cudaFree(L.cdf_x);
@@ -342,6 +343,19 @@ void ensurePtWorkspace(DeviceObj *dev, size_t need) {
   dev->ptWsBytes = need;
 }
 
+// the per-path ray times of a frame of n paths (motion blur)
+float *ensurePtTimes(DeviceObj *dev, long long n) {
+  if (size_t(n) > dev->ptTimesCap) {
+    check(cudaStreamSynchronize(dev->stream), "sync");
+    if (dev->ptTimes) cudaFree(dev->ptTimes);
+    dev->ptTimes = nullptr;
+    dev->ptTimesCap = 0;
+    check(cudaMalloc(&dev->ptTimes, sizeof(float) * size_t(n)), "path times");
+    dev->ptTimesCap = size_t(n);
+  }
+  return dev->ptTimes;
+}
+
 // PathTracer::commit (render/pathtracer/PathTracer.cpp:29-51): light sample
 // counts (lightSamples < 0: all lights at the first bounce; one after it
 // when limitIndirectLightSamples), the backplate and mipMapBias
@@ -393,7 +407,33 @@ AOParamsD makeAOParams(const b200_ao_params &p) {
 }
 
 // PerspectiveCamera::commit without stereo, aperture or motion blur
+// Camera::commit's shutter (camera/Camera.cpp:44-52,100-119)
+static void setShutter(const b200_camera_desc &c, CameraD &cam) {
+  auto cl = [](float v) { return std::fmin(std::fmax(v, 0.f), 1.f); };
+  float lo = cl(c.shutter[0]), hi = cl(c.shutter[1]);
+  if (lo > hi) lo = hi;
+  const int type = c.shutterType;
+  const float dur = std::fmin(std::fmax(c.rollingShutterDuration, 0.f), hi - lo);
+  cam.needTime = type == 0 ? hi - lo != 0.f : dur != 0.f;
+  if (type != 0) {  // rolling: upper reduced by the duration; left / down run backwards
+    hi -= dur;
+    if (type == 2 || type == 3) std::swap(lo, hi);
+  }
+  cam.shutterLo = lo;
+  cam.shutterHi = hi;
+  cam.rollingDuration = dur;
+  cam.shutterMode = type == 0 ? 0 : (type == 1 || type == 2 ? 1 : 2);
+}
+
+static CameraD makeCameraFrame(const b200_camera_desc &c);
+
 CameraD makeCamera(const b200_camera_desc &c) {
+  CameraD cam = makeCameraFrame(c);
+  setShutter(c, cam);
+  return cam;
+}
+
+static CameraD makeCameraFrame(const b200_camera_desc &c) {
   const V3 pos = mk(c.position[0], c.position[1], c.position[2]);
   const V3 dir = mk(c.direction[0], c.direction[1], c.direction[2]);
   const V3 up = mk(c.up[0], c.up[1], c.up[2]);
@@ -443,18 +483,12 @@ CameraD makeCamera(const b200_camera_desc &c) {
   return cam;
 }
 
-// rkcommon rcp(AffineSpace3f): adjoint / det in float, p' = -(l' p)
+// rkcommon rcp(AffineSpace3f) (rcpXfm) on a row-major 3x4 array
 static void rcpAffine(const float *X, float *R) {
-  const V3 vx = mk(X[0], X[4], X[8]), vy = mk(X[1], X[5], X[9]), vz = mk(X[2], X[6], X[10]);
-  const float det = dot(vx, cross(vy, vz));
-  const V3 a = cross(vy, vz), b = cross(vz, vx), c = cross(vx, vy);
-  // adjoint = transpose of (a, b, c) as columns -> rows a, b, c; inverse
-  // columns are the rows of (a b c) divided by det
-  const V3 ix = vdiv(mk(a.x, b.x, c.x), det), iy = vdiv(mk(a.y, b.y, c.y), det), iz = vdiv(mk(a.z, b.z, c.z), det);
-  const V3 p = mk(X[3], X[7], X[11]);
-  const V3 ip = add(add(mul(ix, p.x), mul(iy, p.y)), mul(iz, p.z));
-  const float r[12] = {ix.x, iy.x, iz.x, -ip.x, ix.y, iy.y, iz.y, -ip.y, ix.z, iy.z, iz.z, -ip.z};
-  std::memcpy(R, r, sizeof(r));
+  Xfm x;
+  std::memcpy(x.m, X, sizeof(x.m));
+  const Xfm r = rcpXfm(x);
+  std::memcpy(R, r.m, sizeof(r.m));
 }
 
 SceneObj::SceneObj(DeviceObj *d) : dev(d) {
@@ -480,6 +514,7 @@ SceneObj::~SceneObj() {
   if (tlas.nodes) cudaFreeAsync(tlas.nodes, st);
   if (tlas.leafPrim) cudaFreeAsync(tlas.leafPrim, st);
   if (dEntries) cudaFreeAsync(dEntries, st);
+  if (dMotion) cudaFreeAsync(dMotion, st);
   cudaStreamSynchronize(st);
   if (dLights) cudaFree(dLights);
   if (dScivisLights) cudaFree(dScivisLights);
@@ -512,6 +547,8 @@ void SceneObj::commit() {
   // entries and their world boxes
   hasAttributes = colorAlpha = false;
   std::vector<Entry> he(entries.size());
+  std::vector<float> keys;             // the motion-blurred entries' keys, one array
+  std::vector<size_t> keyOff(entries.size(), 0);
   std::vector<float4> lo(entries.size()), hi(entries.size());
   float wlo[3] = {INFINITY, INFINITY, INFINITY}, whi[3] = {-INFINITY, -INFINITY, -INFINITY};
   for (size_t i = 0; i < entries.size(); i++) {
@@ -539,22 +576,36 @@ void SceneObj::commit() {
     rcpAffine(e.xfm, d.rcp.m);
     d.epsScale = std::fmax(std::fabs(e.xfm[0]), std::fmax(std::fabs(e.xfm[5]), std::fabs(e.xfm[10])));
     d.materialID = uint32_t(e.material);
+    const int nkeys = int(e.motion.size() / 12);
+    if (nkeys >= 2) {
+      keyOff[i] = keys.size();
+      keys.insert(keys.end(), e.motion.begin(), e.motion.end());
+      d.identity = 0u;
+      d.motionCount = nkeys;
+      d.motionT0 = e.t0;
+      d.motionT1 = e.t1;
+    }
     const float *blo = g.blas.bvh.lo, *bhi = g.blas.bvh.hi;
     float l[3] = {INFINITY, INFINITY, INFINITY}, h[3] = {-INFINITY, -INFINITY, -INFINITY};
     if (g.nprims == 0) {
       l[0] = l[1] = l[2] = h[0] = h[1] = h[2] = 0.f;
-    } else if (e.identity) {
+    } else if (e.identity && nkeys < 2) {
       for (int k = 0; k < 3; k++) {
         l[k] = blo[k];
         h[k] = bhi[k];
       }
     } else {
-      for (int c = 0; c < 8; c++) {
-        const float p[3] = {c & 1 ? bhi[0] : blo[0], c & 2 ? bhi[1] : blo[1], c & 4 ? bhi[2] : blo[2]};
-        for (int r = 0; r < 3; r++) {
-          const float v = ((e.xfm[4 * r] * p[0] + e.xfm[4 * r + 1] * p[1]) + e.xfm[4 * r + 2] * p[2]) + e.xfm[4 * r + 3];
-          l[r] = std::fmin(l[r], v);
-          h[r] = std::fmax(h[r], v);
+      // the box under each key (a blend of two keys maps every point to a
+      // blend of its images, inside the union)
+      for (int kk = 0; kk < std::max(nkeys, 1); kk++) {
+        const float *X = nkeys >= 2 ? e.motion.data() + 12 * kk : e.xfm;
+        for (int c = 0; c < 8; c++) {
+          const float p[3] = {c & 1 ? bhi[0] : blo[0], c & 2 ? bhi[1] : blo[1], c & 4 ? bhi[2] : blo[2]};
+          for (int r = 0; r < 3; r++) {
+            const float v = ((X[4 * r] * p[0] + X[4 * r + 1] * p[1]) + X[4 * r + 2] * p[2]) + X[4 * r + 3];
+            l[r] = std::fmin(l[r], v);
+            h[r] = std::fmax(h[r], v);
+          }
         }
       }
       for (int k = 0; k < 3; k++) {
@@ -577,8 +628,18 @@ void SceneObj::commit() {
   if (tlas.nodes) cudaFreeAsync(tlas.nodes, st);
   if (tlas.leafPrim) cudaFreeAsync(tlas.leafPrim, st);
   if (dEntries) cudaFreeAsync(dEntries, st);
+  if (dMotion) cudaFreeAsync(dMotion, st);
   tlas = WideBVH{};
   dEntries = nullptr;
+  dMotion = nullptr;
+  if (!keys.empty()) {
+    check(cudaMallocAsync(&dMotion, sizeof(float) * keys.size(), st), "alloc motion keys");
+    check(cudaMemcpyAsync(dMotion, keys.data(), sizeof(float) * keys.size(), cudaMemcpyHostToDevice, st),
+          "upload motion keys");
+    check(cudaStreamSynchronize(st), "sync");  // the host key array goes out of scope
+    for (size_t i = 0; i < entries.size(); i++)
+      if (he[i].motionCount >= 2) he[i].motionKeys = dMotion + keyOff[i];
+  }
   if (!entries.empty()) {
     float4 *dlo, *dhi;
     const size_t n = entries.size();
@@ -605,7 +666,9 @@ Scene SceneObj::view() const {
   s.ntlas = entries.empty() ? 0 : tlas.nnodes;
   s.hasUser = 0;
   for (const EntryH &e : entries)
-    if (geoms[e.geom].type != GEOM_TRIANGLES && geoms[e.geom].type != GEOM_SPHERES) s.hasUser = 1;
+    if ((geoms[e.geom].type != GEOM_TRIANGLES && geoms[e.geom].type != GEOM_SPHERES) || e.motion.size() > 12)
+      s.hasUser = 1;
+  s.time = 0.f;
   s.status = status;
   s.counters = counters;
   return s;
@@ -1021,6 +1084,30 @@ int b200_scene_add_instance(b200_scene s, int geom, uint32_t inst_id, uint32_t g
   });
 }
 
+int b200_scene_add_instance_motion(b200_scene s, int geom, uint32_t inst_id, uint32_t geom_id, const float *xfms,
+                                   int nkeys, float t0, float t1, int material_id) {
+  if (!s) return B200_INVALID_ARGUMENT;
+  SceneObj *sc = reinterpret_cast<SceneObj *>(s);
+  return guarded(sc->dev, [&]() {
+    require(geom >= 0 && size_t(geom) < sc->geoms.size(), "no such geometry");
+    require(xfms && nkeys >= 2, "motion blur needs at least two transforms");
+    require(std::isfinite(t0) && std::isfinite(t1), "time range is not finite");
+    for (int k = 0; k < 12 * nkeys; k++) require(std::isfinite(xfms[k]), "motion transform is not finite");
+    EntryH e;
+    e.geom = geom;
+    e.instID = inst_id;
+    e.geomID = geom_id;
+    e.identity = false;
+    std::memcpy(e.xfm, xfms, sizeof(e.xfm));
+    e.material = material_id;
+    e.motion.assign(xfms, xfms + 12 * size_t(nkeys));
+    e.t0 = t0;
+    e.t1 = t1 < t0 ? t0 : t1;  // MotionTransform::readParams: upper raised to lower
+    sc->entries.push_back(e);
+    sc->committed = false;
+  });
+}
+
 int b200_scene_set_dynamic(b200_scene s, int dynamic) {
   if (!s) return B200_INVALID_ARGUMENT;
   reinterpret_cast<SceneObj *>(s)->dynamic = dynamic != 0;
@@ -1354,12 +1441,14 @@ int b200_render_pt(b200_scene s, const b200_camera_desc *camera, const b200_pt_p
     const PtParamsD d =
         makePtParams(*p, sc, materials, nmaterials, sc->transparentMaterials);
     DeviceObj *dev = sc->dev;
-    ensurePtWorkspace(dev, ptWorkspaceBytes((long long)fb->W * fb->H * p->pixelSamples));
+    const long long npaths = (long long)fb->W * fb->H * p->pixelSamples;
+    ensurePtWorkspace(dev, ptWorkspaceBytes(npaths));
+    float *times = sc->hasMotion() ? ensurePtTimes(dev, npaths) : nullptr;
     fb->beginFrame(p->pixelSamples, st);
     check(launchRenderPT(dev->tables, sc->view(), makeCamera(*camera), dev->filter(p->pixelFilter), d,
                          sc->dMaterials, sc->dLights, sc->dLightCdf, dev->albedoTables(), fb->view(),
                          p->collectStats != 0, dev->ptWs, dev->ptWsBytes, st, nullptr, nullptr, nullptr,
-                         dev->timer),
+                         dev->timer, times),
           "path tracer launch");
     fb->frameID++;
     framePostProcess(fb, st);

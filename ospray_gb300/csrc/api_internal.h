@@ -43,6 +43,8 @@ struct DeviceObj {
   uint32_t *pickBuf = nullptr;      // one pick result (8 words)
   void *ptWs = nullptr;             // path-tracer path/queue workspace
   size_t ptWsBytes = 0;
+  float *ptTimes = nullptr;         // per-path ray times (frames with motion-blurred instances)
+  size_t ptTimesCap = 0;
   KernelTimer *timer = nullptr;     // live kernel timing (b200_kernel_timing)
   explicit DeviceObj(int cudaDev);
   const AlbedoTablesD *albedoTables();
@@ -72,6 +74,8 @@ struct EntryH {
   bool identity;
   float xfm[12];
   int material;
+  std::vector<float> motion;  // motion blur: >= 2 row-major 3x4 keys (else empty)
+  float t0 = 0.f, t1 = 1.f;   // the keys' time range
 };
 
 struct SceneObj {
@@ -116,6 +120,12 @@ struct SceneObj {
   bool transparentMaterials = false;  // some material of lastMaterials lets shadow rays through
   // set at commit: some mesh has vertex attributes; some vertex colour has alpha < 1
   bool hasAttributes = false, colorAlpha = false;
+  float *dMotion = nullptr;  // every motion-blurred entry's keys
+  bool hasMotion() const {
+    for (const EntryH &e : entries)
+      if (!e.motion.empty()) return true;
+    return false;
+  }
   explicit SceneObj(DeviceObj *d);
   ~SceneObj();
   void commit();

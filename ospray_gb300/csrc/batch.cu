@@ -267,6 +267,7 @@ int b200_batch_add_ao(b200_batch h, b200_scene s, const b200_camera_desc *camera
     FrameObj *fb = reinterpret_cast<FrameObj *>(f);
     requireArg(sc->dev == b->dev && fb->dev == b->dev, "scene and framebuffer must belong to the batch's device");
     requireArg(sc->committed, "scene not committed");
+    requireArg(!sc->hasMotion(), "batch: scenes with motion-blurred instances are rendered by the single-request calls");
     requireArg(p->pixelSamples >= 1 && p->aoSamples >= 0, "bad AO parameters");
     requireArg(p->pixelFilter >= B200_PF_POINT && p->pixelFilter <= B200_PF_BLACKMAN_HARRIS, "bad pixel filter");
     // the batched AO shading is the white, opaque surface case
@@ -293,6 +294,7 @@ int b200_batch_add_pt(b200_batch h, b200_scene s, const b200_camera_desc *camera
     FrameObj *fb = reinterpret_cast<FrameObj *>(f);
     requireArg(sc->dev == b->dev && fb->dev == b->dev, "scene and framebuffer must belong to the batch's device");
     requireArg(sc->committed, "scene not committed");
+    requireArg(!sc->hasMotion(), "batch: scenes with motion-blurred instances are rendered by the single-request calls");
     requireArg(p->pixelSamples >= 1 && p->maxPathLength >= 0, "bad path tracer parameters");
     requireArg(p->pixelFilter >= B200_PF_POINT && p->pixelFilter <= B200_PF_BLACKMAN_HARRIS, "bad pixel filter");
     requireArg(nmaterials >= 0 && (nmaterials == 0 || materials), "bad material array");

@@ -90,6 +90,34 @@ B200_HD V3 xfmVectorT(const Xfm &a, V3 v) {
           fadd(fadd(fmul(a.m[2], v.x), fmul(a.m[6], v.y)), fmul(a.m[10], v.z))};
 }
 
+// rkcommon rcp(AffineSpace3f): the adjoint over the determinant in float,
+// p' = -(L' p)
+B200_HD Xfm rcpXfm(const Xfm &X) {
+  const V3 vx = mk(X.m[0], X.m[4], X.m[8]), vy = mk(X.m[1], X.m[5], X.m[9]), vz = mk(X.m[2], X.m[6], X.m[10]);
+  const V3 a = cross(vy, vz), b = cross(vz, vx), c = cross(vx, vy);
+  const float det = dot(vx, a);
+  const V3 ix = vdiv(mk(a.x, b.x, c.x), det), iy = vdiv(mk(a.y, b.y, c.y), det), iz = vdiv(mk(a.z, b.z, c.z), det);
+  const V3 p = mk(X.m[3], X.m[7], X.m[11]);
+  const V3 ip = add(add(mul(ix, p.x), mul(iy, p.y)), mul(iz, p.z));
+  return Xfm{{ix.x, iy.x, iz.x, -ip.x, ix.y, iy.y, iz.y, -ip.y, ix.z, iy.z, iz.z, -ip.z}};
+}
+
+// A key-framed instance transform at `time` (Embree's motion-blurred
+// instance behind MotionTransform, common/MotionTransform.cpp:10-66: n keys
+// evenly spaced over [t0, t1], the two keys around the time blended
+// component-wise as (1 - f) a + f b; times outside [t0, t1] take the end
+// keys).  keys: n row-major 3x4 matrices.
+B200_HD Xfm motionXfm(const float *keys, int n, float t0, float t1, float time) {
+  float f = t1 > t0 ? fmul(fdiv(fsub(time, t0), fsub(t1, t0)), float(n - 1)) : 0.f;
+  f = fminf(fmaxf(f, 0.f), float(n - 1));
+  const int fi = int(floorf(f)), i = fi < n - 2 ? fi : n - 2;
+  const float u = fsub(f, float(i));
+  const float w = fsub(1.f, u);
+  Xfm X;
+  for (int k = 0; k < 12; k++) X.m[k] = fadd(fmul(w, keys[12 * i + k]), fmul(u, keys[12 * (i + 1) + k]));
+  return X;
+}
+
 struct Ray {
   V3 org;
   float tnear;
@@ -158,6 +186,12 @@ struct Entry {
   const float *normals;      // 3 per vertex
   const float *colors;       // 4 per vertex
   const float *texcoords;    // 2 per vertex
+  // motion blur: motionCount >= 2 row-major 3x4 keys over [motionT0,
+  // motionT1] (motionXfm); xfm / rcp then unused
+  const float *motionKeys;
+  int motionCount;
+  float motionT0, motionT1;
+  int motionPad;
 };
 
 }  // namespace b200

@@ -204,7 +204,7 @@ cudaError_t launchRenderPT(const SamplerTables *T, const Scene &sc, const Camera
                            const AlbedoTablesD *AT, const FrameD &fb, bool stats, void *workspace,
                            size_t wsBytes, cudaStream_t st, const NrcFrameD *nrc = nullptr,
                            void (*nrcInfer)(void *ctx, cudaStream_t st) = nullptr, void *nrcCtx = nullptr,
-                           KernelTimer *kt = nullptr);
+                           KernelTimer *kt = nullptr, float *rayTimes = nullptr);
 // bytes of path-tracer workspace for a frame of npaths = W * H * spp paths
 size_t ptWorkspaceBytes(long long npaths);
 

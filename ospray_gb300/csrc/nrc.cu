@@ -724,6 +724,8 @@ int b200_render_pt_nrc(b200_scene s, const b200_camera_desc *camera, const b200_
   if (nfp) np = *nfp;
   return nrcGuard(sc->dev, [&]() {
     if (!sc->committed) throw Error(B200_INVALID_OPERATION, "scene not committed");
+    if (sc->hasMotion())
+      throw Error(B200_INVALID_ARGUMENT, "radiance cache: scenes with motion-blurred instances are rendered by b200_render_pt");
     if (o->dev != sc->dev) throw Error(B200_INVALID_ARGUMENT, "the cache belongs to another device");
     if (!(p->pixelSamples >= 1 && p->maxPathLength >= 0 && p->pixelFilter >= B200_PF_POINT &&
           p->pixelFilter <= B200_PF_BLACKMAN_HARRIS && nmaterials >= 0 && (nmaterials == 0 || materials)))

@@ -388,6 +388,40 @@ void InstanceObj::commit(B200Device &) {
     static const float id[12] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0};
     identity = std::memcmp(xfm, id, sizeof(id)) == 0;
   }
+  // MotionTransform::readParams (common/MotionTransform.cpp:10-66): key
+  // transforms "motion.transform" over "time" (default [0, 1]); one key is
+  // the plain transform.  The quaternion form (motion.scale / rotation /
+  // translation) is not supported.
+  motion.clear();
+  if (DataObj *m = getData("motion.transform")) {
+    if (m->elem != OSP_AFFINE3F) throw Error(OSP_INVALID_ARGUMENT, "instance: 'motion.transform' must be affine3f data");
+    const auto mb = m->compact();
+    const uint64_t nk = m->count();
+    std::vector<float> keys(12 * nk);
+    for (uint64_t k = 0; k < nk; k++) {
+      float a2[12];
+      std::memcpy(a2, mb.data() + 48 * k, 48);
+      for (int r = 0; r < 3; r++) {
+        keys[12 * k + 4 * r + 0] = a2[0 + r];
+        keys[12 * k + 4 * r + 1] = a2[3 + r];
+        keys[12 * k + 4 * r + 2] = a2[6 + r];
+        keys[12 * k + 4 * r + 3] = a2[9 + r];
+      }
+    }
+    if (nk == 1) {
+      std::memcpy(xfm, keys.data(), sizeof(xfm));
+      static const float id[12] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0};
+      identity = std::memcmp(xfm, id, sizeof(id)) == 0;
+    } else if (nk > 1) {
+      motion = keys;
+      identity = false;
+      time[0] = 0.f;
+      time[1] = 1.f;
+      getBox1("time", time);
+    }
+  }
+  if (has("motion.scale") || has("motion.rotation") || has("motion.translation") || has("motion.pivot"))
+    throw Error(OSP_INVALID_ARGUMENT, "instance: quaternion motion blur is not supported by the b200 device");
 }
 
 void LightObj::commit(B200Device &dev) {
@@ -537,7 +571,12 @@ void WorldObj::commit(B200Device &dev) {
         }
         const int mat =
             m->material ? matIndex[m->material.get()] : (m->materialIndex >= 0 ? K + m->materialIndex : -1);
-        dev.check(b200_scene_add_instance(s, gi, uint32_t(i), uint32_t(j), inst->identity ? nullptr : inst->xfm, mat));
+        if (inst->motion.size() >= 24)
+          dev.check(b200_scene_add_instance_motion(s, gi, uint32_t(i), uint32_t(j), inst->motion.data(),
+                                                   int(inst->motion.size() / 12), inst->time[0], inst->time[1], mat));
+        else
+          dev.check(
+              b200_scene_add_instance(s, gi, uint32_t(i), uint32_t(j), inst->identity ? nullptr : inst->xfm, mat));
         hasGeometry = true;
       }
       for (const auto &vmr : inst->group->volumes) {
@@ -582,6 +621,15 @@ void CameraObj::commit(B200Device &dev) {
   desc.type = type == "orthographic" ? B200_CAMERA_ORTHOGRAPHIC
                                      : (type == "panoramic" ? B200_CAMERA_PANORAMIC : B200_CAMERA_PERSPECTIVE);
   desc.height = getFloat("height", 1.f);
+  // Camera::commit (camera/Camera.cpp:44-52): shutter, shutter type, rolling duration
+  desc.shutter[0] = desc.shutter[1] = 0.5f;
+  getBox1("shutter", desc.shutter);
+  desc.shutterType = getInt("shutterType", OSP_SHUTTER_GLOBAL);
+  if (desc.shutterType < OSP_SHUTTER_GLOBAL || desc.shutterType > OSP_SHUTTER_ROLLING_UP)
+    throw Error(OSP_INVALID_ARGUMENT, "camera: unknown 'shutterType'");
+  desc.rollingShutterDuration = getFloat("rollingShutterDuration", 0.f);
+  if (getData("motion.transform") || has("motion.scale") || has("motion.rotation") || has("motion.translation"))
+    dev.warn("camera: camera motion blur is not supported by the b200 device");
   if (getFloat("apertureRadius", 0.f) != 0.f) dev.warn("camera: depth of field is not supported by the b200 device");
   if (getInt("stereoMode", OSP_STEREO_NONE) != OSP_STEREO_NONE)
     dev.warn("camera: stereo is not supported by the b200 device");

@@ -118,6 +118,8 @@ struct InstanceObj : SceneObj {
   Ref<GroupObj> group;
   float xfm[12] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0};  // row-major 3x4
   bool identity = true;
+  std::vector<float> motion;  // "motion.transform" keys, row-major 3x4 each (>= 2: motion blur)
+  float time[2] = {0.f, 1.f};  // "time" of the keys
   void commit(B200Device &) override;
 };
 

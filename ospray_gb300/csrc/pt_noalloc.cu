@@ -123,6 +123,8 @@ int b200_render_pt_noalloc(b200_scene s, const b200_camera_desc *camera, const b
     cudaError_t e = cudaSetDevice(dev->dev);
     if (e != cudaSuccess) return fail(B200_UNKNOWN_ERROR, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
     if (!sc->committed) return fail(B200_INVALID_OPERATION, "scene not committed");
+    if (sc->hasMotion())  // the per-path ray times would need memory of their own
+      return fail(B200_INVALID_ARGUMENT, "scenes with motion-blurred instances are rendered by b200_render_pt");
     if (p->pixelSamples < 1 || p->maxPathLength < 0) return fail(B200_INVALID_ARGUMENT, "bad path tracer parameters");
     if (p->pixelFilter < B200_PF_POINT || p->pixelFilter > B200_PF_BLACKMAN_HARRIS)
       return fail(B200_INVALID_ARGUMENT, "bad pixel filter");

@@ -120,6 +120,7 @@ __global__ void __launch_bounds__(128, B200_AO_MINBLOCKS) k_render_ao(const Samp
     const uint32_t sid = start + s;
     float2 scr;
     Ray ray = primaryRay(T, cam, pf, x, y, rcpW, rcpH, sid, &scr);
+    sc.time = shutterTime(cam, scr.x, scr.y, 0.5f);  // RendererRenderTaskFn.inl:64: time sample 0.5
     if (p.maxDepth)
       ray.tfar = fminf(ray.tfar, texMaxDepth(p.maxDepth, fmul(fadd(float(x), 0.5f), rcpW),
                                              fmul(fadd(float(y), 0.5f), rcpH)));

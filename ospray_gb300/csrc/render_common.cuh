@@ -21,7 +21,24 @@ struct CameraD {
   V3 org, dir_00, du_size, dv_up;
   float nearClip;
   int type;
+  // shutter after Camera::commit (rolling: upper reduced by the duration,
+  // swapped for the left / down types); mode 0 global, 1 rolling along
+  // screen x, 2 rolling along screen y; needTime: the path tracer draws a
+  // time sample
+  float shutterLo, shutterHi, rollingDuration;
+  int shutterMode, needTime;
 };
+
+// Camera_shutterTime (camera/Camera.ih:33-42): the ray time of a camera
+// sample with time sample `time` at screen position (sx, sy); rkcommon's
+// lerp(f, a, b) = (1 - f) a + f b
+B200_D float shutterTime(const CameraD &c, float sx, float sy, float time) {
+  if (c.shutterMode == 0) return fadd(fmul(fsub(1.f, time), c.shutterLo), fmul(time, c.shutterHi));
+  const float t = fmul(time, c.rollingDuration);
+  const float pos = c.shutterMode == 1 ? sx : sy;
+  const float v = fadd(t, fadd(fmul(fsub(1.f, pos), c.shutterLo), fmul(pos, c.shutterHi)));
+  return fminf(fmaxf(v, 0.f), 1.f);
+}
 
 struct PixelFilterD {
   int type;  // 0 point, 1 box, 2.. LUT
@@ -153,9 +170,9 @@ struct DGAttr {
 
 // (u, v) with P = a + u (b - a) + v (c - a) for the hit at distance t, in the
 // entry's object space: least squares over the plane of (a, b, c)
-B200_D float2 hitBarycentrics(const Entry &e, const Ray &ray, float t, V3 a, V3 b, V3 c) {
+B200_D float2 hitBarycentrics(bool identity, const Xfm &R, const Ray &ray, float t, V3 a, V3 b, V3 c) {
   V3 P = add(ray.org, mul(t, ray.dir));
-  if (!e.identity) P = xfmPoint(e.rcp, P);
+  if (!identity) P = xfmPoint(R, P);
   const V3 e1 = sub(b, a), e2 = sub(c, a), d = sub(P, a);
   const float d11 = dot(e1, e1), d12 = dot(e1, e2), d22 = dot(e2, e2);
   const float r1 = dot(d, e1), r2 = dot(d, e2);
@@ -168,11 +185,24 @@ B200_D float2 hitBarycentrics(const Entry &e, const Ray &ray, float t, V3 a, V3 
 // postIntersect with DG_NG | DG_NS | DG_NORMALIZE | DG_FACEFORWARD (and with
 // ATTR also DG_COLOR | DG_TEXCOORD and the mesh's vertex normals:
 // TriangleMesh_postIntersect geometry/Mesh.ispc:178-276)
-template <bool ATTR = false>
-B200_D DG postIntersect(const Scene &sc, const Ray &ray, const HitRec &hit, DGAttr *at = nullptr) {
+//
+// MOTION: the entry is motion-blurred, its transform taken at the ray's time
+// (Instance_postIntersect, common/Instance.ih:57-91, with Embree's
+// interpolated transform).
+template <bool ATTR, bool MOTION>
+B200_D DG postIntersectT(const Entry &e, const Ray &ray, const HitRec &hit, DGAttr *at, float time) {
   DG dg;
   dg.entry = hit.entry;
-  const Entry &e = sc.entries[hit.entry];
+  Xfm mx, mr;
+  float mEps = 0.f;
+  if (MOTION) {
+    mx = motionXfm(e.motionKeys, e.motionCount, e.motionT0, e.motionT1, time);
+    mr = rcpXfm(mx);
+    mEps = fmaxf(fabsf(mx.m[0]), fmaxf(fabsf(mx.m[5]), fabsf(mx.m[10])));
+  }
+  const Xfm &X = MOTION ? mx : e.xfm;
+  const Xfm &R = MOTION ? mr : e.rcp;
+  const bool identity = !MOTION && e.identity;
   dg.P = add(ray.org, mul(hit.t, ray.dir));
   V3 Ng = hit.Ng, Ns = hit.Ng;
   // DG_TANGENTS: meshes take their first edge (TriangleMesh_postIntersect
@@ -201,7 +231,7 @@ B200_D DG postIntersect(const Scene &sc, const Ray &ray, const HitRec &hit, DGAt
     dPds = sub(v[1], v[0]);
     if (ATTR) {
       dPdt = sub(v[3], v[0]);
-      const float2 uv = hitBarycentrics(e, ray, hit.t, v[0], v[1], v[3]);
+      const float2 uv = hitBarycentrics(identity, R, ray, hit.t, v[0], v[1], v[3]);
       at->s = uv.x;
       at->t = uv.y;
     }
@@ -216,7 +246,7 @@ B200_D DG postIntersect(const Scene &sc, const Ray &ray, const HitRec &hit, DGAt
     if (ATTR) {
       dPdt = sub(c, a);
       // barycentric weights (1 - u - v, u, v) of vertices (i0, i1, i2)
-      const float2 uv = hitBarycentrics(e, ray, hit.t, a, b, c);
+      const float2 uv = hitBarycentrics(identity, R, ray, hit.t, a, b, c);
       at->s = uv.x;
       at->t = uv.y;
       const float w0 = 1.f - uv.x - uv.y, w1 = uv.x, w2 = uv.y;
@@ -254,12 +284,12 @@ B200_D DG postIntersect(const Scene &sc, const Ray &ray, const HitRec &hit, DGAt
     // Spheres_postIntersect (geometry/Spheres.ispc:24-42): radius x ulpEpsilon, also for discs
     eps = fmul(__ldg(&e.spheres[hit.primID].w), ULP_EPSILON);
   }
-  if (!e.identity) {
-    Ns = xfmVectorT(e.rcp, Ns);
-    Ng = xfmVectorT(e.rcp, Ng);
-    eps = fmul(eps, e.epsScale);
-    dPds = xfmVector(e.xfm, dPds);  // Instance_postIntersect (common/Instance.ih:95-98)
-    if (ATTR) dPdt = xfmVector(e.xfm, dPdt);
+  if (!identity) {
+    Ns = xfmVectorT(R, Ns);
+    Ng = xfmVectorT(R, Ng);
+    eps = fmul(eps, MOTION ? mEps : e.epsScale);
+    dPds = xfmVector(X, dPds);  // Instance_postIntersect (common/Instance.ih:95-98)
+    if (ATTR) dPdt = xfmVector(X, dPdt);
   }
   dg.dPds = dPds;
   if (ATTR) at->dPdt = dPdt;
@@ -277,6 +307,34 @@ B200_D DG postIntersect(const Scene &sc, const Ray &ray, const HitRec &hit, DGAt
   dg.Ns = Ns;
   dg.P = add(dg.P, mul(dg.epsilon, ffnng));
   return dg;
+}
+
+// the motion-blurred case out of line (the shading kernels keep their
+// registers); a hit the wavefront trace kernels left unevaluated
+// (Traverser::finish with DEFER; `slot` its leaf slot) is re-evaluated here
+// first
+template <bool ATTR>
+static __device__ __noinline__ DG postIntersectMotion(const Entry &e, Ray ray, HitRec hit, DGAttr *at, float time,
+                                                      uint32_t slot) {
+  if (slot != INVALID_ID) {
+    const HitSurface f = finishMotion(e, time, ray, hit.t, slot);
+    hit.u = f.u;
+    hit.v = f.v;
+    hit.Ng = f.Ng;
+  }
+  return postIntersectT<ATTR, true>(e, ray, hit, at, time);
+}
+
+// postIntersect at the ray's `time` (motion-blurred instances only; a
+// negative time: the scene's); deferredSlot: the leaf slot of a hit whose
+// motion-blurred evaluation the trace kernel deferred
+template <bool ATTR = false, bool MOTION = true>
+B200_D DG postIntersect(const Scene &sc, const Ray &ray, const HitRec &hit, DGAttr *at = nullptr, float time = -1.f,
+                        uint32_t deferredSlot = INVALID_ID) {
+  const Entry &e = sc.entries[hit.entry];
+  if (MOTION && sc.hasUser && e.motionCount > 1)
+    return postIntersectMotion<ATTR>(e, ray, hit, at, time >= 0.f ? time : sc.time, deferredSlot);
+  return postIntersectT<ATTR, false>(e, ray, hit, at, time);
 }
 
 // the pixel footprint of a hit for texture level selection (World.ih

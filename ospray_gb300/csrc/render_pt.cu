@@ -94,6 +94,8 @@ struct Workspace {
   // hit, so with n paths of which m miss, the records end at 96 (n - m)
   // bytes and the misses start at 92 npaths + 4 (n - m) bytes, never below
   uint32_t *misses;
+  // each path's ray time (scenes with motion-blurred instances; else null)
+  float *times;
   // [0] qa count, [1] qb count, [2] shadow count, [3] closest fetch, [4]
   // shadow fetch, [5..7] partition part sizes
   uint32_t *counters;
@@ -131,7 +133,7 @@ constexpr uint32_t F_AOHIT = 1u << 11, F_DIFFUSE = 1u << 12;
 // the camera ray of sample s of pixel (x, y) of a path-traced frame, as a
 // fresh path record (meta2: first-hit instID, request, sampleID, pixel)
 B200_D PathRec genPT(const PtCtx &c, const CameraD &cam, const PixelFilterD &pf, const FrameInfo &fi, int x, int y,
-                     int s, uint32_t rid, float2 *screen = nullptr) {
+                     int s, uint32_t rid, float2 *screen = nullptr, float *time = nullptr) {
   const uint32_t seed = 0x49c5f37eu ^ uint32_t(fi.W * y + x);
   const uint32_t sampleID = uint32_t(fi.frameID) * uint32_t(fi.spp) + uint32_t(s);
   LDSampler ld;
@@ -143,6 +145,8 @@ B200_D PathRec genPT(const PtCtx &c, const CameraD &cam, const PixelFilterD &pf,
   const float sx = fadd(cx, fmul(pfs.x, fi.rcpW)), sy = fadd(cy, fmul(pfs.y, fi.rcpH));
   const Ray ray = cameraRay(cam, sx, sy);
   if (screen) *screen = make_float2(sx, sy);
+  // the camera sample's time (PathTracer.ispc:177-180, Camera_shutterTime)
+  if (time) *time = shutterTime(cam, sx, sy, cam.needTime ? ld.finalizeDim4(ss234) : 0.5f);
   PathRec r;
   r.org = make_float4(ray.org.x, ray.org.y, ray.org.z, INFINITY);
   r.dir = make_float4(ray.dir.x, ray.dir.y, ray.dir.z, INFINITY);
@@ -187,7 +191,9 @@ __global__ void k_pt_generate(PtCtx c, CameraD cam, PixelFilterD pf, FrameInfo f
   }
   if (!live) return;
   float2 scr;
-  PathRec r = genPT(c, cam, pf, fi, pix % fi.W, pix / fi.W, s, 0u, &scr);
+  float time;
+  PathRec r = genPT(c, cam, pf, fi, pix % fi.W, pix / fi.W, s, 0u, &scr, ws.times ? &time : nullptr);
+  if (ws.times) ws.times[p] = time;
   // Renderer_getMaxDepth at the sample's screen position (PathTracer.ispc:189-192):
   // the camera ray's tfar, carried in org.w until the first hit sets the depth there
   if (c.p.maxDepth) r.org.w = texMaxDepth(c.p.maxDepth, scr.x, scr.y);
@@ -233,7 +239,7 @@ struct ShadowMatD {
 // The body is a device function so that the persistent batch kernel runs it
 // as one of its stages; a batch reads its queue with coherent loads (in the
 // persistent kernel the queue was written earlier in the same launch).
-template <bool SHADOW, bool STATS, bool BATCH, bool TRANSP = false>
+template <bool SHADOW, bool STATS, bool BATCH, bool TRANSP = false, bool USER = true>
 __device__ __forceinline__ void traceQueue(Scene sc, Workspace ws, const uint32_t *queue, const uint32_t *count,
                                            uint32_t *fetch, const ReqD *reqs, ShadowMatD sm) {
   static_assert(!(BATCH && STATS), "batched traversal keeps no per-scene statistics");
@@ -245,6 +251,7 @@ __device__ __forceinline__ void traceQueue(Scene sc, Workspace ws, const uint32_
   const Scene &S = BATCH ? bsc : sc;
   Traverser tv;
   TraceSpill spill;
+  if (USER) spill.time = 0.f;
   bool has = false, exhausted = false;
   uint32_t item = 0;
   // transparent shadows: the ray, its remaining contribution, medium and crossing budget
@@ -283,6 +290,7 @@ __device__ __forceinline__ void traceQueue(Scene sc, Workspace ws, const uint32_
               tcone = ws.paths[__float_as_uint(s.b.w)].lastN.w;
             }
             if (BATCH) bsc = reqs[ws.paths[__float_as_uint(s.b.w)].meta2.y].c.sc;
+            if (USER && !BATCH && ws.times) spill.time = ws.times[__float_as_uint(s.b.w)];
           } else {
             item = queue ? (BATCH ? queue[idx] : __ldg(queue + idx)) : idx;
             const float4 o = ws.paths[item].org, d = ws.paths[item].dir;
@@ -292,6 +300,7 @@ __device__ __forceinline__ void traceQueue(Scene sc, Workspace ws, const uint32_
             // camera rays: the maxDepth limit in org.w (infinite without one)
             r.tfar = (ws.paths[item].meta.y & 0xffu) == 0u ? o.w : INFINITY;
             if (BATCH) bsc = reqs[ws.paths[item].meta2.y].c.sc;
+            if (USER && !BATCH && ws.times) spill.time = ws.times[item];
           }
           tv.init(S, r, SHADOW && !TRANSP, &spill);
           if (STATS) ts.rays++;
@@ -302,7 +311,7 @@ __device__ __forceinline__ void traceQueue(Scene sc, Workspace ws, const uint32_
       }
     }
     if (!__any_sync(0xffffffffu, has)) break;
-    if (has && tv.step<STATS, true, B200_QUEUE_PRIMS_PER_STEP, B200_QUEUE_POSTPONE_LANES>(S, &ts)) {
+    if (has && tv.step<STATS, USER, B200_QUEUE_PRIMS_PER_STEP, B200_QUEUE_POSTPONE_LANES>(S, &ts)) {
       if (TRANSP) {
         bool done = true;
         if (!tv.found) {
@@ -311,9 +320,9 @@ __device__ __forceinline__ void traceQueue(Scene sc, Workspace ws, const uint32_
           atomicAdd(con + 1, tcon.y);
           atomicAdd(con + 2, tcon.z);
         } else {
-          tv.finish(S);
+          tv.finish<true, true>(S);
           DGAttr at;
-          const DG dg = postIntersect<true>(S, tray, tv.hit, &at);
+          const DG dg = postIntersect<true>(S, tray, tv.hit, &at, spill.time, tv.hslot);
           const uint32_t mi = S.entries[tv.hit.entry].materialID;
           const bool hasMat = mi < uint32_t(sm.nmats);
           // the shadow cone narrows from the path's width to 0 at the light
@@ -344,11 +353,12 @@ __device__ __forceinline__ void traceQueue(Scene sc, Workspace ws, const uint32_
             atomicAdd(con + 2, s.c.z);
           }
         } else {
-          tv.finish(S);
+          tv.finish<true, true>(S);
           HitBuf hb;
           hb.a = make_float4(tv.hit.t, __uint_as_float(tv.hit.primID), __uint_as_float(tv.hit.entry),
                              tv.found ? 1.f : 0.f);
-          hb.b = make_float4(tv.hit.Ng.x, tv.hit.Ng.y, tv.hit.Ng.z, 0.f);
+          // w: the leaf slot (a deferred motion-blurred hit is re-evaluated from it)
+          hb.b = make_float4(tv.hit.Ng.x, tv.hit.Ng.y, tv.hit.Ng.z, USER ? __uint_as_float(tv.hslot) : 0.f);
           ws.hits[item] = hb;
         }
         has = false;
@@ -358,11 +368,13 @@ __device__ __forceinline__ void traceQueue(Scene sc, Workspace ws, const uint32_
   if (STATS) flushStats(sc, ts);
 }
 
-template <bool SHADOW, bool STATS, bool BATCH, bool TRANSP = false>
+// USER = false: an instantiation for scenes without discs, planes or
+// motion-blurred instances (Scene::hasUser), without their code
+template <bool SHADOW, bool STATS, bool BATCH, bool TRANSP = false, bool USER = true>
 __global__ void __launch_bounds__(TRACE_BLOCK, BATCH ? B200_BATCH_TRACE_MINBLOCKS : B200_TRACE_MINBLOCKS)
     k_trace_queue(Scene sc, Workspace ws, const uint32_t *queue, const uint32_t *count, uint32_t *fetch,
                   const ReqD *reqs, ShadowMatD sm) {
-  traceQueue<SHADOW, STATS, BATCH, TRANSP>(sc, ws, queue, count, fetch, reqs, sm);
+  traceQueue<SHADOW, STATS, BATCH, TRANSP, USER>(sc, ws, queue, count, fetch, reqs, sm);
 }
 
 
@@ -392,7 +404,7 @@ B200_D void aoShade(const PtCtx &C, const AOParamsD &A, int W, PathRec &pr, cons
     const Entry &e = C.sc.entries[h.entry];
     h.geomID = e.geomID;
     h.instID = e.instID;
-    const DG dg = postIntersect(C.sc, ray, h);
+    const DG dg = postIntersect<false, false>(C.sc, ray, h);  // batches hold no motion-blurred instances
     pr.org.w = h.t;
     pr.meta.z = h.primID;
     pr.meta.w = h.geomID;
@@ -418,7 +430,7 @@ B200_D void aoShade(const PtCtx &C, const AOParamsD &A, int W, PathRec &pr, cons
           r.dir = dir;
           r.tfar = A.aoRadius;
           HitRec hh;
-          if (!traceRay<false, false>(C.sc, r, hh, true, true, nullptr)) unblocked += 1.f;
+          if (!traceRay<false, false, false>(C.sc, r, hh, true, true, nullptr)) unblocked += 1.f;
         }
       }
     }
@@ -435,6 +447,7 @@ struct PathVars {
   bool straightPath, firstBounceLight, diffuseSeen, auxDone, cont;
   uint32_t medium;
   float cone;  // ray cone width at this vertex
+  float time;  // the path's ray time (motion blur; negative: none)
 };
 
 // transparentShadow (render/pathtracer/TransparentShadow.ispc:18-85) for one
@@ -443,19 +456,19 @@ struct PathVars {
 // attenuation over the segment), until the ray reaches tfar (unblocked) or
 // the contribution drops to minContribution or maxPathLength surfaces were
 // crossed.  Opaque scenes use one any-hit query.
-template <bool TRANSP>
-B200_D V3 shadowInPlace(const PtCtx &C, Ray sr, V3 contrib, uint32_t medium, float cone) {
+template <bool TRANSP, bool MOTION>
+B200_D V3 shadowInPlace(const PtCtx &C, Ray sr, V3 contrib, uint32_t medium, float cone, float time) {
   HitRec h;
-  if (!TRANSP) return traceRay<false, false>(C.sc, sr, h, true, true, nullptr) ? splat(0.f) : contrib;
+  if (!TRANSP) return traceRay<false, false, MOTION>(C.sc, sr, h, true, true, nullptr, time) ? splat(0.f) : contrib;
   const float tfar = sr.tfar;
   int maxDepth = C.p.maxPathLength;
   for (int guard = 0; guard < 4096; guard++) {
-    if (!traceRay<false, false>(C.sc, sr, h, false, true, nullptr)) return contrib;
+    if (!traceRay<false, false, MOTION>(C.sc, sr, h, false, true, nullptr, time)) return contrib;
     const Entry &e = C.sc.entries[h.entry];
     h.geomID = e.geomID;
     h.instID = e.instID;
     DGAttr at;
-    const DG dg = postIntersect<true>(C.sc, sr, h, &at);
+    const DG dg = postIntersect<true, MOTION>(C.sc, sr, h, &at, time);
     const uint32_t mi = e.materialID;
     const bool hasMat = mi < uint32_t(C.p.numMaterials);
     const float w = cone + (-cone * (1.f / tfar)) * h.t;
@@ -481,7 +494,7 @@ B200_D V3 shadowInPlace(const PtCtx &C, Ray sr, V3 contrib, uint32_t medium, flo
 // The path record is read and written field by field (gp: the record in
 // memory; org4 / dir4 / meta: the fields the kernel keeps in registers), so
 // the whole 128-byte record is never live at once.
-template <class B, bool NRC, bool ALLMAT>
+template <class B, bool NRC, bool ALLMAT, bool MOTION = false>
 B200_D void scatterSurface(const PtCtx &C, const B &bsdf, const MaterialD &mat, uint32_t mi, const DG &dg,
                            const Ray &ray, float t, V3 wo, PathRec *gp, float4 &org4, float4 &dir4, uint4 &meta,
                            PathVars &v, uint32_t p, ShadowRec *sh, int &nsh, const NrcFrameD &nf) {
@@ -567,8 +580,9 @@ B200_D void scatterSurface(const PtCtx &C, const B &bsdf, const MaterialD &mat, 
         sr.tnear = 0.f;
         sr.dir = ls.dir;
         sr.tfar = ls.dist;
-        v.contribution = v.contribution + (transparentShadows ? shadowInPlace<ALLMAT>(C, sr, cval, v.medium, v.cone)
-                                                              : shadowInPlace<false>(C, sr, cval, v.medium, 0.f));
+        v.contribution = v.contribution + (transparentShadows
+                                               ? shadowInPlace<ALLMAT, MOTION>(C, sr, cval, v.medium, v.cone, v.time)
+                                               : shadowInPlace<false, MOTION>(C, sr, cval, v.medium, 0.f, v.time));
       }
     }
     v.firstBounceLight = false;
@@ -636,7 +650,8 @@ B200_D void scatterSurface(const PtCtx &C, const B &bsdf, const MaterialD &mat, 
 // carries the opaque principled BSDF only (a smaller kernel for the common
 // case).
 // (A device function, a stage of the persistent batch kernel too.)
-template <bool BATCH, bool NRC, bool ALLMAT = true>
+// MOTION: the scene has motion-blurred instances.
+template <bool BATCH, bool NRC, bool ALLMAT = true, bool MOTION = false>
 // qmiss (a partitioned queue, k_partition): the queue is [diffuse hits |
 // other hits | misses] with the first two parts in qin (other hits at its
 // end) and the misses at the end of qmiss (Workspace::misses); cpart holds
@@ -692,6 +707,7 @@ __device__ __forceinline__ void ptShade(PtCtx c, Workspace ws, const uint32_t *q
       v.medium = __float_as_uint(con4.w);
       v.cont = false;
       v.cone = 0.f;
+      v.time = ws.times ? ws.times[p] : -1.f;
       float alpha = thr4.w;
       Ray ray;
       ray.org = mk(org4.x, org4.y, org4.z);
@@ -746,7 +762,9 @@ __device__ __forceinline__ void ptShade(PtCtx c, Workspace ws, const uint32_t *q
         h.geomID = e.geomID;
         h.instID = e.instID;
         DGAttr at;
-        const DG dg = ALLMAT ? postIntersect<true>(C.sc, ray, h, &at) : postIntersect(C.sc, ray, h);
+        // hb.b.w: the leaf slot (a motion-blurred hit is re-evaluated from it)
+        const DG dg = ALLMAT ? postIntersect<true, MOTION>(C.sc, ray, h, &at, v.time, __float_as_uint(hb.b.w))
+                             : postIntersect<false, MOTION>(C.sc, ray, h, nullptr, v.time, __float_as_uint(hb.b.w));
         if (ALLMAT && !BATCH) v.cone = gp->lastN.w + __uint_as_float(gp->meta2.y) * t;
         if (v.depth == 0) {
           meta.z = h.primID;
@@ -780,7 +798,7 @@ __device__ __forceinline__ void ptShade(PtCtx c, Workspace ws, const uint32_t *q
               if (ALLMAT && mat.kind == MAT_OBJ) {
                 ObjBsdf b;
                 b.init(mat, fxv, fyv, dg.Ns);
-                scatterSurface<ObjBsdf, NRC, ALLMAT>(C, b, mat, mi, dg, ray, t, wo, gp, org4, dir4, meta, v, p, sh,
+                scatterSurface<ObjBsdf, NRC, ALLMAT, MOTION>(C, b, mat, mi, dg, ray, t, wo, gp, org4, dir4, meta, v, p, sh,
                                                      nsh, nf);
               } else {
                 PrincipledBsdfT<ALLMAT> b;
@@ -789,7 +807,7 @@ __device__ __forceinline__ void ptShade(PtCtx c, Workspace ws, const uint32_t *q
                          sameMedium(mediumOf(C.mats, v.medium), MediumD{1.f, splat(0.f)}));
                 else
                   b.init(mat, fxv, fyv, dg.Ns, C.AT);
-                scatterSurface<PrincipledBsdfT<ALLMAT>, NRC, ALLMAT>(C, b, mat, mi, dg, ray, t, wo, gp, org4, dir4,
+                scatterSurface<PrincipledBsdfT<ALLMAT>, NRC, ALLMAT, MOTION>(C, b, mat, mi, dg, ray, t, wo, gp, org4, dir4,
                                                                     meta, v, p, sh, nsh, nf);
               }
               break;
@@ -798,7 +816,7 @@ __device__ __forceinline__ void ptShade(PtCtx c, Workspace ws, const uint32_t *q
               if (ALLMAT) {
                 MetalBsdf b;
                 b.init(mat, dg.Ns);
-                scatterSurface<MetalBsdf, NRC, ALLMAT>(C, b, mat, mi, dg, ray, t, wo, gp, org4, dir4, meta, v, p, sh,
+                scatterSurface<MetalBsdf, NRC, ALLMAT, MOTION>(C, b, mat, mi, dg, ray, t, wo, gp, org4, dir4, meta, v, p, sh,
                                                        nsh, nf);
               }
               break;
@@ -808,7 +826,7 @@ __device__ __forceinline__ void ptShade(PtCtx c, Workspace ws, const uint32_t *q
                 GlassBsdf b;
                 const bool out = glassFromOutside(C.mats, mi, v.medium);
                 b.init(out ? mat.iorOut * (1.f / mat.iorIn) : mat.iorIn * (1.f / mat.iorOut), dg.Ns, dg.Ng);
-                scatterSurface<GlassBsdf, NRC, ALLMAT>(C, b, mat, mi, dg, ray, t, wo, gp, org4, dir4, meta, v, p, sh,
+                scatterSurface<GlassBsdf, NRC, ALLMAT, MOTION>(C, b, mat, mi, dg, ray, t, wo, gp, org4, dir4, meta, v, p, sh,
                                                        nsh, nf);
               }
               break;
@@ -817,7 +835,7 @@ __device__ __forceinline__ void ptShade(PtCtx c, Workspace ws, const uint32_t *q
               if (ALLMAT) {
                 ThinGlassBsdf b;
                 b.init(mat, dg.Ns);
-                scatterSurface<ThinGlassBsdf, NRC, ALLMAT>(C, b, mat, mi, dg, ray, t, wo, gp, org4, dir4, meta, v, p,
+                scatterSurface<ThinGlassBsdf, NRC, ALLMAT, MOTION>(C, b, mat, mi, dg, ray, t, wo, gp, org4, dir4, meta, v, p,
                                                            sh, nsh, nf);
               }
               break;
@@ -853,11 +871,11 @@ __device__ __forceinline__ void ptShade(PtCtx c, Workspace ws, const uint32_t *q
 #ifndef B200_SHADE_MINBLOCKS
 #define B200_SHADE_MINBLOCKS 2
 #endif
-template <bool BATCH, bool NRC, bool ALLMAT = true>
+template <bool BATCH, bool NRC, bool ALLMAT = true, bool MOTION = false>
 __global__ void __launch_bounds__(128, B200_SHADE_MINBLOCKS)
     k_pt_shade(PtCtx c, Workspace ws, const uint32_t *qin, const uint32_t *cin, uint32_t *qout, uint32_t *cout,
                uint32_t *cshadow, const ReqD *reqs, NrcFrameD nf, const uint32_t *qmiss, const uint32_t *cpart) {
-  ptShade<BATCH, NRC, ALLMAT>(c, ws, qin, cin, qout, cout, cshadow, reqs, nf, qmiss, cpart);
+  ptShade<BATCH, NRC, ALLMAT, MOTION>(c, ws, qin, cin, qout, cout, cshadow, reqs, nf, qmiss, cpart);
 }
 
 // averages each pixel's samples into the framebuffer (ScreenSample_accumulate
@@ -1410,6 +1428,7 @@ Workspace carveWorkspace(void *workspace, long long npaths) {
   ws.qb = (uint32_t *)carve(4 * npaths);
   ws.shadows = (ShadowRec *)carve(sizeof(ShadowRec) * 2 * npaths);
   ws.misses = reinterpret_cast<uint32_t *>(ws.shadows + 2 * npaths) - npaths;
+  ws.times = nullptr;
   ws.counters = (uint32_t *)carve(64);
   return ws;
 }
@@ -1438,7 +1457,7 @@ cudaError_t launchRenderPT(const SamplerTables *T, const Scene &sc, const Camera
                            const PtParamsD &p, const MaterialD *mats, const LightD *lights, const float *lightCdf,
                            const AlbedoTablesD *AT, const FrameD &fb, bool stats, void *workspace, size_t wsBytes,
                            cudaStream_t st, const NrcFrameD *nrc, void (*nrcInfer)(void *, cudaStream_t),
-                           void *nrcCtx, KernelTimer *kt) {
+                           void *nrcCtx, KernelTimer *kt, float *rayTimes) {
   FrameInfo fi;
   fi.W = fb.W;
   fi.H = fb.H;
@@ -1450,6 +1469,7 @@ cudaError_t launchRenderPT(const SamplerTables *T, const Scene &sc, const Camera
   if (ptWorkspaceBytes(fi.npaths) > wsBytes) return cudaErrorInvalidValue;
   if (nrc && (stats || !nrcInfer)) return cudaErrorInvalidValue;
   Workspace ws = carveWorkspace(workspace, fi.npaths);
+  ws.times = rayTimes;
   PtCtx c = {T, sc, p, mats, lights, lightCdf, AT, fb.frameID, fb.aux, fb.W, fi.rcpW, fi.rcpH};
   static int traceBlocks = 0, shadowBlocks = 0, transpBlocks = 0, shadeBlocks = 0, shadeAllBlocks = 0,
              shadeNrcBlocks = 0;
@@ -1493,8 +1513,11 @@ cudaError_t launchRenderPT(const SamplerTables *T, const Scene &sc, const Camera
       if (stats)
         k_trace_queue<false, true, false><<<traceBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
             sc, ws, qin, ws.counters + cin, ws.counters + 3, nullptr, sm);
-      else
+      else if (sc.hasUser)
         k_trace_queue<false, false, false><<<traceBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
+            sc, ws, qin, ws.counters + cin, ws.counters + 3, nullptr, sm);
+      else
+        k_trace_queue<false, false, false, false, false><<<traceBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
             sc, ws, qin, ws.counters + cin, ws.counters + 3, nullptr, sm);
     }
     const uint32_t *qmiss = nullptr, *cpart = nullptr;
@@ -1513,6 +1536,9 @@ cudaError_t launchRenderPT(const SamplerTables *T, const Scene &sc, const Camera
             c, ws, qshade, ws.counters + cin, qnext, ws.counters + cout, ws.counters + 2, nullptr, nf, qmiss, cpart);
       else if (nrc)
         k_pt_shade<false, true, false><<<shadeNrcBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
+            c, ws, qshade, ws.counters + cin, qnext, ws.counters + cout, ws.counters + 2, nullptr, nf, qmiss, cpart);
+      else if (ws.times)  // motion-blurred instances: the general kernel with their code
+        k_pt_shade<false, false, true, true><<<shadeAllBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
             c, ws, qshade, ws.counters + cin, qnext, ws.counters + cout, ws.counters + 2, nullptr, nf, qmiss, cpart);
       else if (p.allMaterials)
         k_pt_shade<false, false, true><<<shadeAllBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
@@ -1534,8 +1560,11 @@ cudaError_t launchRenderPT(const SamplerTables *T, const Scene &sc, const Camera
       else if (stats)
         k_trace_queue<true, true, false><<<shadowBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
             sc, ws, sq, ws.counters + 2, ws.counters + 4, nullptr, sm);
-      else
+      else if (sc.hasUser)
         k_trace_queue<true, false, false><<<shadowBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
+            sc, ws, sq, ws.counters + 2, ws.counters + 4, nullptr, sm);
+      else
+        k_trace_queue<true, false, false, false, false><<<shadowBlocks, TRACE_BLOCK, TRACE_SMEM_BYTES, st>>>(
             sc, ws, sq, ws.counters + 2, ws.counters + 4, nullptr, sm);
     }
     if (nrc && nf.useCache) {  // answer this bounce's cache queries

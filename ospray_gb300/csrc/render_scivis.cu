@@ -265,6 +265,7 @@ __global__ void __launch_bounds__(128) k_render_scivis_surfaces(const SamplerTab
       const uint32_t sid = start + uint32_t(s);
       float2 scr;
       Ray ray = primaryRay(T, cam, pf, x, y, rcpW, rcpH, sid, &scr);
+      sc.time = shutterTime(cam, scr.x, scr.y, 0.5f);  // RendererRenderTaskFn.inl:64: time sample 0.5
       const float cx = fmul(fadd(float(x), 0.5f), rcpW), cy = fmul(fadd(float(y), 0.5f), rcpH);
       if (p.maxDepth) ray.tfar = fminf(ray.tfar, texMaxDepth(p.maxDepth, cx, cy));
       const float2 cone = ATTR ? cameraCone(cam, scr.x, scr.y, rcpH) : make_float2(0.f, 0.f);

@@ -32,7 +32,8 @@ struct Scene {
   const Entry *entries;
   int nentries;
   int ntlas;
-  int hasUser;                // an entry holds discs or planes (the traversal's out-of-line tests)
+  int hasUser;                // an entry holds discs or planes or is motion-blurred (the traversal's out-of-line calls)
+  float time;                 // ray time of the lane's queries (renderers set it per sample; 0 by default)
   uint32_t *status;           // bit 0: traversal stack overflow seen
   unsigned long long *counters;  // [rays, node visits, triangle tests, sphere tests]
 };
@@ -205,6 +206,45 @@ static __device__ __noinline__ float userTest(uint32_t type, V3 org, V3 d, float
     h = planeTest(org, d, tnear, tfar, prims + 3 * slot, t);
   return h ? t : __int_as_float(0x7fffffff);
 }
+// the ray (origin, direction) in a motion-blurred entry's frame at `time`
+// (out of line, as the disc and plane tests; returned by value, so no
+// traversal state has its address taken)
+struct RayFrame {
+  V3 o, d;
+};
+static __device__ __noinline__ RayFrame motionFrame(const Entry &e, float time, V3 org, V3 dir) {
+  const Xfm r = rcpXfm(motionXfm(e.motionKeys, e.motionCount, e.motionT0, e.motionT1, time));
+  return RayFrame{xfmPoint(r, org), xfmVector(r, dir)};
+}
+static __device__ __noinline__ V3 userNormal(uint32_t type, V3 d, const float4 *prims, uint32_t slot);
+
+// The closest hit's u, v and geometric normal on a motion-blurred entry,
+// re-evaluated in the entry's frame at the ray's time (Traverser::finish
+// for such entries, out of line so that the traversal kernels keep their
+// registers)
+struct HitSurface {
+  float u, v;
+  V3 Ng;
+};
+static __device__ __noinline__ HitSurface finishMotion(const Entry &e, float time, Ray ray, float ht,
+                                                        uint32_t hslot) {
+  const RayFrame f = motionFrame(e, time, ray.org, ray.dir);
+  HitSurface r = {0.f, 0.f, mk(0.f, 0.f, 0.f)};
+  float t;
+  if (e.type == GEOM_TRIANGLES) {
+    const float4 a = __ldg(e.prims + 3 * hslot), b = __ldg(e.prims + 3 * hslot + 1),
+                 c = __ldg(e.prims + 3 * hslot + 2);
+    const V3 v0 = mk(a.x, a.y, a.z), v1 = mk(b.x, b.y, b.z), v2 = mk(c.x, c.y, c.z);
+    triTest(triPre(f.d), f.o, ray.tnear, ht, v0, v1, v2, t, r.u, r.v);
+    r.Ng = cross(sub(v1, v0), sub(v2, v0));
+  } else if (e.type == GEOM_SPHERES) {
+    sphTest(f.o, f.d, ray.tnear, ht, __ldg(e.prims + hslot), t, r.Ng);
+  } else {
+    r.Ng = userNormal(e.type, f.d, e.prims, hslot);
+  }
+  return r;
+}
+
 static __device__ __noinline__ V3 userNormal(uint32_t type, V3 d, const float4 *prims, uint32_t slot) {
   if (type == GEOM_DISCS) return neg(d);
   const float4 n = __ldg(prims + (type == GEOM_ORIENTED_DISCS ? 2 * slot + 1 : 3 * slot));
@@ -391,6 +431,7 @@ constexpr uint32_t G_KIND = 3u << 30, G_BLAS = 1u << 30, G_PRIMS = 2u << 30;
 // traverser's own fields in registers.
 struct TraceSpill {
   uint2 e[STACK_LOCAL];
+  float time;  // the ray's time (motion-blurred instances), read by the traverser from here
 };
 
 struct TraceStack {
@@ -469,6 +510,10 @@ struct Traverser {
 
   B200_D bool idle() const { return !(nbits & 0xffu) && !pbits && st.sp == 0; }
 
+  // the ray's time, kept beside the local stack entries (TraceSpill)
+  B200_D float rayTime() const { return reinterpret_cast<const TraceSpill *>(st.local)->time; }
+
+  template <bool MOTION = true>
   B200_D void enterInstance(const Scene &sc, uint32_t entry) {
     eidx = entry;
     const Entry &e = sc.entries[eidx];
@@ -476,7 +521,12 @@ struct Traverser {
     prims = e.prims;
     primIDs = e.primIDs;
     etype = e.type;
-    if (!e.identity) {
+    if (MOTION && e.motionCount > 1) {
+      const RayFrame f = motionFrame(e, rayTime(), ray.org, ray.dir);
+      org = f.o;
+      dir = f.d;
+      rdir = mk(1.f / dir.x, 1.f / dir.y, 1.f / dir.z);
+    } else if (!e.identity) {
       const Xfm r = e.rcp;
       org = xfmPoint(r, ray.org);
       dir = xfmVector(r, ray.dir);
@@ -502,8 +552,13 @@ struct Traverser {
   // re-evaluated on the hit primitive in its entry's frame with the same
   // operations as during traversal (so identical values), and the IDs.
   // USER = false: the scene has no discs or planes (Scene::hasUser), so no
-  // out-of-line call is compiled into the caller.
-  template <bool USER = true>
+  // out-of-line call is compiled into the caller.  DEFER: u, v and Ng of a
+  // hit on a motion-blurred entry are not valid (taken in the entry's static
+  // frame); the caller hands the leaf slot hslot to postIntersect, which
+  // re-evaluates them at the ray's time, so the wavefront trace kernels
+  // carry no call here.
+  // MOTION = false: no entry is motion-blurred (no motion code compiled in).
+  template <bool USER = true, bool DEFER = false, bool MOTION = USER>
   B200_D void finish(const Scene &sc) {
     hit.t = ht;
     hit.primID = hprim;
@@ -515,6 +570,13 @@ struct Traverser {
     const Entry &e = sc.entries[hentry];
     hit.instID = e.instID;
     hit.geomID = e.geomID;
+    if (MOTION && !DEFER && e.motionCount > 1) {  // the whole re-evaluation out of line
+      const HitSurface f = finishMotion(e, rayTime(), ray, ht, hslot);
+      hit.u = f.u;
+      hit.v = f.v;
+      hit.Ng = f.Ng;
+      return;
+    }
     V3 o = ray.org, d = ray.dir;
     if (!e.identity) {
       const Xfm r = e.rcp;
@@ -537,7 +599,8 @@ struct Traverser {
 
   // one traversal step; true when the ray is finished (USER as for finish;
   // PPS and POSTPONE as B200_PRIMS_PER_STEP and B200_POSTPONE_LANES)
-  template <bool STATS, bool USER = true, int PPS = B200_PRIMS_PER_STEP, int POSTPONE = B200_POSTPONE_LANES>
+  template <bool STATS, bool USER = true, int PPS = B200_PRIMS_PER_STEP, int POSTPONE = B200_POSTPONE_LANES,
+            bool MOTION = USER>
   B200_D bool step(const Scene &sc, TraceStats *ts) {
     // 1) the next node of the current node group
     if (nbits & 0xffu) {
@@ -574,7 +637,7 @@ struct Traverser {
         if (nbits & 0xffu) st.push(make_uint2(nbase, nbits | G_TNODE), sc.status);
         if (pbits) st.push(make_uint2(pbase, pbits | G_TINST), sc.status);
         pbits = 0;
-        enterInstance(sc, __ldg(sc.tlasLeaf + slot));
+        enterInstance<MOTION>(sc, __ldg(sc.tlasLeaf + slot));
         break;
       }
       float t;
@@ -638,22 +701,24 @@ struct Traverser {
 // SPLIT: two copies of the loop, one without the out-of-line disc and plane
 // tests for scenes that have none (Scene::hasUser); without SPLIT one loop
 // with them (smaller code, for callers inside large kernels).
-template <bool STATS = false, bool SPLIT = true>
+// MOTION = false: the caller never sees motion-blurred instances.
+template <bool STATS = false, bool SPLIT = true, bool MOTION = true>
 B200_D bool traceRay(const Scene &sc, const Ray &ray, HitRec &hit, bool anyHit, bool active = true,
-                     TraceStats *ts = nullptr) {
+                     TraceStats *ts = nullptr, float time = -1.f) {
   if (STATS && active) ts->rays++;
   const unsigned group = __activemask();
   Traverser tv;
   TraceSpill spill;
+  spill.time = time >= 0.f ? time : sc.time;  // (a negative time: the scene's)
   tv.init(sc, ray, anyHit, &spill);
   bool done = !active || tv.idle();
   // the lanes' scenes may differ in a batch: the choice is made for the group
   if (!SPLIT || __any_sync(group, sc.hasUser != 0)) {
     for (int guard = 0; guard < (1 << 18); guard++) {
       if (!__any_sync(group, !done)) break;
-      if (!done) done = tv.step<STATS, true>(sc, ts);
+      if (!done) done = tv.step<STATS, true, B200_PRIMS_PER_STEP, B200_POSTPONE_LANES, MOTION>(sc, ts);
     }
-    if (!anyHit) tv.finish<true>(sc);
+    if (!anyHit) tv.finish<true, false, MOTION>(sc);
   } else {
     for (int guard = 0; guard < (1 << 18); guard++) {
       if (!__any_sync(group, !done)) break;
@@ -665,7 +730,7 @@ B200_D bool traceRay(const Scene &sc, const Ray &ray, HitRec &hit, bool anyHit, 
   return tv.found;
 }
 
-// Closest hit (ANY = false) or any hit (ANY = true).
+// Closest hit (ANY = false) or any hit (ANY = true), at the scene's ray time.
 template <bool ANY, bool STATS = false>
 B200_D bool traceScene(const Scene &sc, const Ray &ray, HitRec &hit, TraceStats *ts = nullptr) {
   return traceRay<STATS>(sc, ray, hit, ANY, true, ts);

@@ -19,7 +19,7 @@ P, I, U32, F = ctypes.c_void_p, ctypes.c_int, ctypes.c_uint32, ctypes.c_float
 
 class OrCamera(ctypes.Structure):
     _fields_ = [("pos", F * 3), ("dir", F * 3), ("up", F * 3), ("fovy", F), ("aspect", F), ("nearClip", F),
-                ("type", I), ("height", F)]
+                ("type", I), ("height", F), ("shutter", F * 2), ("shutterType", I), ("rollingDuration", F)]
 
 
 class OrFrame(ctypes.Structure):
@@ -242,6 +242,7 @@ def lib():
         L.or_scene_add_discs.argtypes = [P, P, I, P]
         L.or_scene_add_planes.argtypes = [P, P, I, P]
         L.or_scene_add_instance.argtypes = [P, I, U32, U32, P, I]
+        L.or_scene_add_instance_motion.argtypes = [P, I, U32, U32, P, I, F, F, I]
         L.or_pt_new.restype = P
         L.or_pt_free.argtypes = [P]
         L.or_pt_add_material.argtypes = [P, P, F, F]
@@ -292,12 +293,15 @@ def _p(a):
     return ctypes.c_void_p(a.ctypes.data) if a is not None else None
 
 
-def camera(position, direction, up=(0, 1, 0), fovy=60.0, aspect=1.0, near_clip=1e-6, kind=0, height=1.0):
-    """kind 0 perspective, 1 orthographic (image `height`), 2 panoramic."""
+def camera(position, direction, up=(0, 1, 0), fovy=60.0, aspect=1.0, near_clip=1e-6, kind=0, height=1.0,
+           shutter=(0.5, 0.5), shutter_type=0, rolling_shutter_duration=0.0):
+    """kind 0 perspective, 1 orthographic (image `height`), 2 panoramic; shutter as the b200 camera."""
     c = OrCamera()
     c.pos[:], c.dir[:], c.up[:] = list(position), list(direction), list(up)
     c.fovy, c.aspect, c.nearClip = fovy, aspect, near_clip
     c.type, c.height = int(kind), float(height)
+    c.shutter[:] = [float(shutter[0]), float(shutter[1])]
+    c.shutterType, c.rollingDuration = int(shutter_type), float(rolling_shutter_duration)
     return c
 
 
@@ -333,6 +337,11 @@ class Scene:
         c = np.ascontiguousarray(coeffs, np.float32).reshape(-1, 4)
         b = None if bounds is None else np.ascontiguousarray(bounds, np.float32).reshape(-1, 6)
         return lib().or_scene_add_planes(self.h, _p(c), len(c), _p(b))
+
+    def add_instance_motion(self, geom, inst_id, geom_id, xfms, time=(0.0, 1.0), material=-1):
+        x = np.ascontiguousarray(xfms, dtype=np.float32).reshape(-1, 12)
+        lib().or_scene_add_instance_motion(self.h, geom, inst_id, geom_id, _p(x), len(x), float(time[0]),
+                                           float(time[1]), material)
 
     def add_instance(self, geom, inst_id, geom_id, xfm=None, material=-1):
         x = None if xfm is None else np.ascontiguousarray(xfm, np.float32).reshape(12)
