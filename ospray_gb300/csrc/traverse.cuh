@@ -398,13 +398,15 @@ B200_D uint32_t octantOf(V3 d) {
 #endif
 // Primitive tests per traversal step, and the lane count below which a
 // lane postpones its primitive group while a node group is pending: the
-// persistent queue kernels (B200_QUEUE_*, whose warps refill finished lanes)
-// run one test per step and never postpone the first (1,102 Mrays/s on the
-// 1080p path tracer; postponing below 8 lanes: 1,077, below 16: 1,073; 2
-// tests per step: 1,060, 4: 1,042, a whole group: 1,039); traceRay (whole
-// warps that trace together, the AO and SciVis kernels) keeps a whole group
-// per step, postponing below 8 lanes (AO within its run-to-run spread
-// either way: 1,343-1,390 Mrays/s).
+// single-frame path tracer's persistent queue kernels (B200_QUEUE_*, whose
+// warps refill finished lanes) run one test per step and never postpone the
+// first (1,102 Mrays/s on the 1080p instanced-spheres frame; postponing
+// below 8 lanes: 1,077, below 16: 1,073; 2 tests per step: 1,060, 4: 1,042,
+// a whole group: 1,039).  The choice depends on the scene: on the batch's
+// height fields whole groups are faster (1,505 vs 1,469 Mrays/s batched,
+// 1,121 vs 1,103 for the same requests one at a time), so the batch keeps
+// them, as does traceRay (whole warps that trace together, the AO and
+// SciVis kernels: AO within its run-to-run spread either way).
 #ifndef B200_PRIMS_PER_STEP
 #define B200_PRIMS_PER_STEP 64
 #endif

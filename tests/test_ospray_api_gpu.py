@@ -324,3 +324,67 @@ def test_quads_boxes_and_lights_through_ospray_api(osp_device):
     assert close.mean() >= 0.995, close.mean()
     for h in (fb, ren, cam, world):
         L.ospRelease(h)
+
+
+def test_motion_blurred_instance_through_ospray_api_matches_oracle(osp_device):
+    """An instance with "motion.transform" keys and "time", rendered by the
+    AO renderer under a camera with a rolling "shutter" through libospray.so,
+    equals the oracle's frame."""
+    from test_motion_gpu import _keys, _sphere
+    L = osp_device
+    keep = []
+    W, H = 96, 72
+    sv, si = _sphere()
+    g = L.ospNewGeometry(b"mesh")
+    osp_api.set_data(g, "vertex.position", sv, osp_api.OSP_VEC3F, len(sv), keep)
+    osp_api.set_data(g, "index", si, osp_api.OSP_VEC3UI, len(si), keep)
+    L.ospCommit(g)
+    m = L.ospNewGeometricModel(g)
+    L.ospCommit(m)
+    L.ospRelease(g)
+    group = L.ospNewGroup()
+    L.ospSetObjectAsData(group, b"geometry", osp_api.OSP_GEOMETRIC_MODEL, m)
+    L.ospRelease(m)
+    L.ospCommit(group)
+    inst = L.ospNewInstance(group)
+    keys = _keys()  # row-major 3x4 -> affine3f (l.vx, l.vy, l.vz, p)
+    aff = np.ascontiguousarray(np.concatenate([keys[:, :, 0], keys[:, :, 1], keys[:, :, 2], keys[:, :, 3]], 1),
+                               np.float32)
+    osp_api.set_data(inst, "motion.transform", aff, osp_api.OSP_AFFINE3F, len(keys), keep)
+    osp_api.set_param(inst, "time", 10000, np.float32([0.1, 0.9]))  # OSP_BOX1F
+    L.ospCommit(inst)
+    L.ospRelease(group)
+    world = L.ospNewWorld()
+    L.ospSetObjectAsData(world, b"instance", osp_api.OSP_INSTANCE, inst)
+    L.ospRelease(inst)
+    L.ospCommit(world)
+    pos, dirc, up = (0.0, 2.5, -8.0), (0.0, -1.0, 7.0), (0.0, 1.0, 0.0)
+    cam = L.ospNewCamera(b"perspective")
+    for key, val in (("position", pos), ("direction", dirc), ("up", up)):
+        osp_api.set_param(cam, key, osp_api.OSP_VEC3F, np.float32(val))
+    osp_api.set_param(cam, "aspect", osp_api.OSP_FLOAT, np.float32(W / H))
+    osp_api.set_param(cam, "shutter", 10000, np.float32([0.0, 1.0]))  # OSP_BOX1F
+    osp_api.set_param(cam, "shutterType", osp_api.OSP_UINT, np.uint32(3))  # OSP_SHUTTER_ROLLING_DOWN
+    osp_api.set_param(cam, "rollingShutterDuration", osp_api.OSP_FLOAT, np.float32(0.25))
+    L.ospCommit(cam)
+    ren = L.ospNewRenderer(b"ao")
+    osp_api.set_param(ren, "pixelFilter", osp_api.OSP_UINT, np.uint32(0))
+    osp_api.set_param(ren, "aoSamples", osp_api.OSP_INT, np.int32(1))
+    L.ospCommit(ren)
+    fb = L.ospNewFrameBuffer(W, H, osp_api.OSP_FB_RGBA32F, osp_api.OSP_FB_COLOR | osp_api.OSP_FB_ID_PRIMITIVE)
+    fut = L.ospRenderFrame(fb, ren, cam, world)
+    assert fut, L.ospDeviceGetLastErrorMsg(L.ospGetCurrentDevice())
+    L.ospWait(fut, osp_api.OSP_TASK_FINISHED)
+    L.ospRelease(fut)
+    color = osp_api.map_channel(fb, osp_api.OSP_FB_COLOR, (H, W, 4), np.float32)
+    prim = osp_api.map_channel(fb, osp_api.OSP_FB_ID_PRIMITIVE, (H, W), np.uint32)
+    for h in (fb, ren, cam, world):
+        L.ospRelease(h)
+    o = oracle.Scene()
+    o.add_instance_motion(o.add_mesh(sv, si), 0, 0, keys, (0.1, 0.9))
+    o.commit()
+    ref = oracle.render_ao(o, oracle.camera(pos, dirc, up, aspect=W / H, shutter=(0.0, 1.0), shutter_type=3,
+                                            rolling_shutter_duration=0.25), 0, W, H)
+    assert np.mean(prim != 0xFFFFFFFF) > 0.01  # the moving sphere is in view
+    np.testing.assert_array_equal(prim, ref["primID"])
+    assert np.mean(np.all(np.abs(color - ref["color"]) <= 1e-4, axis=2)) >= 0.999
