@@ -230,6 +230,12 @@ struct ShadowMatD {
 #ifndef B200_REFILL_LANES
 #define B200_REFILL_LANES 8
 #endif
+#ifndef B200_TRACE_CARVEOUT
+#define B200_TRACE_CARVEOUT -1
+#endif
+#ifndef B200_SHADE_CARVEOUT
+#define B200_SHADE_CARVEOUT -1
+#endif
 // the same threshold for the shadow (any-hit) instantiations (4: 1,050, 8:
 // 1,051, 16: 1,035 Mrays/s with the closest-hit threshold at 8)
 #ifndef B200_REFILL_LANES_SHADOW
@@ -1477,6 +1483,24 @@ cudaError_t launchRenderPT(const SamplerTables *T, const Scene &sc, const Camera
   static int traceBlocks = 0, shadowBlocks = 0, transpBlocks = 0, shadeBlocks = 0, shadeAllBlocks = 0,
              shadeNrcBlocks = 0;
   if (!traceBlocks) {
+    // shared-memory carveout preferences (percent of the SM's shared memory;
+    // the rest is L1, which caches the BVH nodes and the shading kernel's
+    // spills); negative: the driver's choice, which measured as good as the
+    // best setting (1,097 vs 1,098 Mrays/s at 50 % trace / 25 % shade; 100 %
+    // for the trace kernels: 1,001; 0 % for the shading kernels: 948)
+    if (B200_TRACE_CARVEOUT >= 0) {
+      const void *tk[] = {(const void *)k_trace_queue<false, false, false>,
+                          (const void *)k_trace_queue<true, false, false>,
+                          (const void *)k_trace_queue<false, false, false, false, false>,
+                          (const void *)k_trace_queue<true, false, false, false, false>};
+      for (const void *k : tk)
+        cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, B200_TRACE_CARVEOUT);
+    }
+    if (B200_SHADE_CARVEOUT >= 0) {
+      const void *sk[] = {(const void *)k_pt_shade<false, false, false>, (const void *)k_pt_shade<false, false, true>};
+      for (const void *k : sk)
+        cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, B200_SHADE_CARVEOUT);
+    }
     traceBlocks = persistentBlocks((const void *)k_trace_queue<false, false, false>, TRACE_SMEM_BYTES);
     shadowBlocks = persistentBlocks((const void *)k_trace_queue<true, false, false>, TRACE_SMEM_BYTES);
     transpBlocks = persistentBlocks((const void *)k_trace_queue<true, false, false, true>, TRACE_SMEM_BYTES);
