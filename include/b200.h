@@ -227,6 +227,12 @@ void *b200_frame_channel(b200_frame fb, uint32_t channel);
 size_t b200_frame_channel_bytes(b200_frame fb, uint32_t channel);
 /* ospMapFrameBuffer: copies a channel to host memory (waits for the device) */
 int b200_frame_read(b200_frame fb, uint32_t channel, void *host_dst, size_t bytes);
+/* ospMapFrameBuffer into page-locked host memory owned by the frame (one
+ * buffer per channel, allocated at its first map, freed with the frame):
+ * copies the channel there, waits, and returns the pointer in *out.  The
+ * contents stay valid until the next b200_frame_map of the same channel or
+ * the frame's release. */
+int b200_frame_map(b200_frame fb, uint32_t channel, const void **out);
 
 /* ---- tonemapper frame operation (ToneMapper::commit
  *      fb/frame_ops/ToneMapper.cpp:16-51, ToneMapper_kernel

@@ -371,6 +371,7 @@ def lib():
             "b200_frame_id": (I, [P]),
             "b200_frame_channel": (P, [P, U32]),
             "b200_frame_read": (I, [P, U32, P, ctypes.c_size_t]),
+            "b200_frame_map": (I, [P, U32, ctypes.POINTER(P)]),
             "b200_render_ao": (I, [P, ctypes.POINTER(CameraDesc), ctypes.POINTER(AOParams), P, P]),
             "b200_scene_set_lights": (I, [P, P, I]),
             "b200_scene_set_volume": (I, [P, P, I, I, I, P, P, P, I, P, I, P, F]),

@@ -699,6 +699,7 @@ FrameObj::FrameObj(DeviceObj *d, int w, int h, int fmt, uint32_t ch) : dev(d), W
 
 FrameObj::~FrameObj() {
   cudaStreamSynchronize(dev->stream);
+  for (auto &m : hostMaps) cudaFreeHost(m.second.first);
   if (taskErr) cudaFree(taskErr);
   if (taskActive) cudaFree(taskActive);
   if (aux) cudaFree(aux);
@@ -1270,6 +1271,33 @@ int b200_frame_read(b200_frame f, uint32_t c, void *dst, size_t bytes) {
     require(bytes >= fb->channelBytes(c), "destination too small");
     check(cudaMemcpyAsync(dst, src, fb->channelBytes(c), cudaMemcpyDeviceToHost, fb->dev->stream), "read");
     check(cudaStreamSynchronize(fb->dev->stream), "read");
+  });
+}
+
+int b200_frame_map(b200_frame f, uint32_t c, const void **out) {
+  if (!f || !out) return B200_INVALID_ARGUMENT;
+  FrameObj *fb = reinterpret_cast<FrameObj *>(f);
+  return guarded(fb->dev, [&]() {
+    void *src = fb->channel(c);
+    require(src != nullptr, "channel not present");
+    const size_t bytes = fb->channelBytes(c);
+    std::pair<void *, size_t> *buf = nullptr;
+    for (auto &m : fb->hostMaps)
+      if (m.first == c) buf = &m.second;
+    if (!buf) {
+      fb->hostMaps.push_back({c, {nullptr, 0}});
+      buf = &fb->hostMaps.back().second;
+    }
+    if (buf->second < bytes) {
+      if (buf->first) cudaFreeHost(buf->first);
+      buf->first = nullptr;
+      buf->second = 0;
+      check(cudaMallocHost(&buf->first, bytes), "pinned map buffer");
+      buf->second = bytes;
+    }
+    check(cudaMemcpyAsync(buf->first, src, bytes, cudaMemcpyDeviceToHost, fb->dev->stream), "map");
+    check(cudaStreamSynchronize(fb->dev->stream), "map");
+    *out = buf->first;
   });
 }
 

@@ -139,6 +139,7 @@ struct FrameObj {
   uint32_t channels;
   int frameID = 0;
   void *mapped = nullptr;  // converted colour (what ospMapFrameBuffer returns)
+  std::vector<std::pair<uint32_t, std::pair<void *, size_t>>> hostMaps;  // b200_frame_map: channel -> pinned buffer
   bool toneMapOn = false;
   ToneMapD toneMap = {};
   float4 *color = nullptr, *variance = nullptr;

@@ -227,6 +227,16 @@ const void *B200Device::mapFrameBuffer(OSPFrameBuffer h, OSPFrameBufferChannel c
   if (!(f->channels & ch) && ch != OSP_FB_COLOR) return nullptr;
   const size_t bytes = b200_frame_channel_bytes(f->fb, uint32_t(ch));
   if (!bytes) return nullptr;
+  // the frame's page-locked buffer for the channel, unless it is mapped already
+  bool inUse = false;
+  for (const auto &m : f->pinnedMapped) inUse = inUse || m.second == uint32_t(ch);
+  if (!inUse) {
+    const void *p = nullptr;
+    check(b200_frame_map(f->fb, uint32_t(ch), &p));
+    f->pinnedMapped[p] = uint32_t(ch);
+    f->retain();
+    return p;
+  }
   std::vector<unsigned char> buf(bytes);
   check(b200_frame_read(f->fb, uint32_t(ch), buf.data(), bytes));
   const void *p = buf.data();
@@ -237,6 +247,12 @@ const void *B200Device::mapFrameBuffer(OSPFrameBuffer h, OSPFrameBufferChannel c
 
 void B200Device::unmapFrameBuffer(const void *mapped, OSPFrameBuffer h) {
   FrameBufferObj *f = asKind<FrameBufferObj>(h, OSP_FRAMEBUFFER, "ospUnmapFrameBuffer");
+  auto pt = f->pinnedMapped.find(mapped);
+  if (pt != f->pinnedMapped.end()) {
+    f->pinnedMapped.erase(pt);
+    f->release();
+    return;
+  }
   auto it = f->mapped.find(mapped);
   if (it == f->mapped.end()) throw Error(OSP_INVALID_ARGUMENT, "ospUnmapFrameBuffer: pointer was not mapped");
   f->mapped.erase(it);

@@ -177,7 +177,8 @@ struct FrameBufferObj : SceneObj {
   int width, height;
   OSPFrameBufferFormat format;
   uint32_t channels;
-  std::map<const void *, std::vector<unsigned char>> mapped;
+  std::map<const void *, std::vector<unsigned char>> mapped;  // heap copies (a channel mapped twice)
+  std::map<const void *, uint32_t> pinnedMapped;  // b200_frame_map buffers in use: pointer -> channel
   float errorThreshold = 0.f;  // varianceThreshold of the last renderer
   void commit(B200Device &) override;
 };

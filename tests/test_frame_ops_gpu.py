@@ -231,3 +231,30 @@ def test_adaptive_accumulation_renders_selected_tasks(b200_device, pt_world, ren
                 np.testing.assert_array_equal(acc_a[sl], acc_before[sl])
             checked += 1
     assert checked > 0.8 * tx * ty
+
+
+def test_frame_map_returns_the_channel_in_page_locked_memory(b200_device):
+    """b200_frame_map copies a channel into the frame's page-locked buffer for
+    it (reused by later maps of the channel) with the bytes b200_frame_read
+    returns."""
+    import ctypes
+    import ospray_gb300 as og
+    from ospray_gb300 import scenes
+    dev = b200_device
+    d = scenes.ao_heightfield_scene()
+    g = og.Scene(dev)
+    scenes.build_ao_scene(g, d)
+    c = d["camera"]
+    fb = og.Frame(dev, 64, 48, og.FB_COLOR | og.FB_DEPTH, format=og.FB_RGBA8)
+    og.render_ao(g, og.camera_desc(c["position"], c["direction"], c["up"], aspect=64 / 48), og.ao_params(), fb)
+    ptrs = []
+    for ch, shape, dt in ((og.FB_COLOR, (48, 64, 4), np.uint8), (og.FB_DEPTH, (48, 64), np.float32)):
+        p = ctypes.c_void_p()
+        dev._check(og.lib().b200_frame_map(fb._h, ch, ctypes.byref(p)))
+        n = int(np.prod(shape)) * np.dtype(dt).itemsize
+        got = np.frombuffer(ctypes.string_at(p.value, n), dt).reshape(shape)
+        np.testing.assert_array_equal(got, fb.read(ch))
+        ptrs.append(p.value)
+    p2 = ctypes.c_void_p()
+    dev._check(og.lib().b200_frame_map(fb._h, og.FB_COLOR, ctypes.byref(p2)))
+    assert p2.value == ptrs[0] and ptrs[0] != ptrs[1]
