@@ -592,7 +592,8 @@ int b200_batch_autotune(b200_batch batch, int candidates, b200_batch_tuning *bes
  *                        wave's stages in order, separated by grid-wide
  *                        barriers, pulling queue work dynamically, and
  *                        post-process and stamp the requests each wave
- *                        completes.  A barrier wait is bounded (4 s); one that
+ *                        completes.  A barrier wait is bounded (4 s by default,
+ *                        b200_batch_set_barrier_timeout); one that
  *                        runs out makes every block leave the kernel, and the
  *                        next b200_batch_render or b200_batch_timings call
  *                        returns B200_UNKNOWN_ERROR.
@@ -604,6 +605,10 @@ enum { B200_BATCH_KERNELS = 0, B200_BATCH_GRAPH = 1, B200_BATCH_PERSISTENT = 2 }
  * tuning, the mode or a framebuffer's post-processing); other values are
  * refused (B200_INVALID_ARGUMENT) */
 int b200_batch_render(b200_batch batch, int mode);
+/* the bound of the persistent launch's barrier waits in ns (0: the default
+ * of 4 s); a bound shorter than a stage makes the frame fail as a timed-out
+ * wait does, which is how the failure path is tested */
+int b200_batch_set_barrier_timeout(b200_batch batch, uint64_t ns);
 /* after a render has finished (b200_device_sync): each request's completion
  * time in ms after the render began (out n doubles, request order), and the
  * rays the render traced */

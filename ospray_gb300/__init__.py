@@ -346,6 +346,7 @@ def lib():
             "b200_batch_set_tuning": (I, [P, ctypes.POINTER(BatchTuning)]),
             "b200_batch_autotune": (I, [P, I, ctypes.POINTER(BatchTuning)]),
             "b200_batch_render": (I, [P, I]),
+            "b200_batch_set_barrier_timeout": (I, [P, ctypes.c_uint64]),
             "b200_batch_timings": (I, [P, P, I, ctypes.POINTER(ctypes.c_uint64)]),
             "b200_batch_info": (I, [P, P]),
             "b200_nrc_create": (I, [P, ctypes.POINTER(NrcDesc), ctypes.POINTER(P)]),
@@ -847,6 +848,10 @@ class Batch:
         if mode is None:
             mode = BATCH_GRAPH if use_graph else BATCH_KERNELS
         self.device._check(lib().b200_batch_render(self._h, int(mode)))
+
+    def set_barrier_timeout(self, ns):
+        """Bound of the persistent launch's barrier waits in ns (0: default 4 s)."""
+        self.device._check(lib().b200_batch_set_barrier_timeout(self._h, int(ns)))
 
     def timings(self):
         """(per-request completion ms since the render began, rays traced); waits for the device."""

@@ -45,6 +45,7 @@ struct BatchObj {
   std::vector<BatchWave> waves;
   BatchLayout layout = {};
   int mode = B200_BATCH_GRAPH;  // of the last render (the autotuner tunes for it)
+  unsigned long long barrierTimeoutNs = 4000000000ull;  // the persistent kernel's bounded barrier wait
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   std::vector<float> graphKey;  // what the captured graph depends on
@@ -101,7 +102,7 @@ struct BatchObj {
   // everything the captured kernel sequence depends on, besides the table
   std::vector<float> key() const {
     std::vector<float> k = {float(mode), float(tune.wavePaths), float(tune.traceBlocksPerSM),
-                            float(tune.shadeBlocksPerSM), float(reqs.size())};
+                            float(tune.shadeBlocksPerSM), float(reqs.size()), float(barrierTimeoutNs)};
     for (const Req &r : reqs) {
       const FrameObj *f = r.fb;
       k.insert(k.end(), {float(r.kind), float(f->W), float(f->H), float(f->format), f->toneMapOn ? 1.f : 0.f,
@@ -176,7 +177,8 @@ struct BatchObj {
     const int n = int(reqs.size());
     check(cudaMemsetAsync(dRays, 0, sizeof(unsigned long long), st), "clear ray counter");
     if (mode == B200_BATCH_PERSISTENT) {
-      check(launchBatchPersistent(dtables, layout, n, tune, ws, wsBytes, dRays, dStamps, dBarrier, st),
+      check(launchBatchPersistent(dtables, layout, n, tune, ws, wsBytes, dRays, dStamps, dBarrier, barrierTimeoutNs,
+                                  st),
             "persistent batch kernel");
       return;
     }
@@ -419,6 +421,12 @@ int b200_batch_autotune(b200_batch h, int candidates, b200_batch_tuning *best) {
       best->shadeBlocksPerSM = bestT.shadeBlocksPerSM;
     }
   });
+}
+
+int b200_batch_set_barrier_timeout(b200_batch h, uint64_t ns) {
+  if (!h) return B200_INVALID_ARGUMENT;
+  reinterpret_cast<BatchObj *>(h)->barrierTimeoutNs = ns ? ns : 4000000000ull;
+  return B200_NO_ERROR;
 }
 
 int b200_batch_render(b200_batch h, int mode) {

@@ -284,10 +284,12 @@ cudaError_t launchBatchWave(const void *dtables, size_t segTableOffset, const Ba
 // finalize) run in order inside the kernel, separated by grid-wide barriers;
 // completed requests are post-processed and stamped inside it (stamps[n] =
 // start).  `barrier` is 4 words the call clears; barrier[2] != 0 after the
-// launch means a barrier wait timed out (the frame is incomplete).
+// launch means a barrier wait ran longer than timeoutNs (every block then
+// left the kernel; the frame is incomplete).
 cudaError_t launchBatchPersistent(const void *dtables, const BatchLayout &layout, int nreqs, const BatchTuning &tune,
                                   void *workspace, size_t wsBytes, unsigned long long *rayCount,
-                                  unsigned long long *stamps, uint32_t *barrier, cudaStream_t st);
+                                  unsigned long long *stamps, uint32_t *barrier, unsigned long long timeoutNs,
+                                  cudaStream_t st);
 // resident blocks per SM of the persistent batch kernel (its grid = SMs x this)
 int batchPersistentBlocksPerSM();
 // writes the global timer into stamps[first..end) (request completion times)

@@ -1084,11 +1084,9 @@ struct BatchRunD {
   Workspace ws;
   uint32_t *bar;  // [0] arrivals, [1] generation, [2] error (a wait timed out)
   unsigned long long *rays, *stamps;
+  unsigned long long timeoutNs;  // the bound of a barrier wait
 };
 
-#ifndef B200_BARRIER_TIMEOUT_NS
-#define B200_BARRIER_TIMEOUT_NS 4000000000ull
-#endif
 
 B200_D uint32_t loadAcquire(const uint32_t *p) {
   uint32_t v;
@@ -1097,10 +1095,10 @@ B200_D uint32_t loadAcquire(const uint32_t *p) {
 }
 
 // Grid-wide barrier of the cooperative launch.  A wait longer than
-// B200_BARRIER_TIMEOUT_NS sets the error word, and a block that finds the
-// error word set does not wait: every block then leaves the kernel (false)
-// instead of spinning on.
-B200_D bool gridBarrier(uint32_t *bar, uint32_t &gen) {
+// timeoutNs sets the error word, and a block that finds the error word set
+// does not wait: every block then leaves the kernel (false) instead of
+// spinning on.
+B200_D bool gridBarrier(uint32_t *bar, uint32_t &gen, unsigned long long timeoutNs) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -1115,7 +1113,7 @@ B200_D bool gridBarrier(uint32_t *bar, uint32_t &gen) {
       } else {
         const unsigned long long t0 = globalTimer();
         while (loadAcquire(bar + 1) != next) {
-          if (*(volatile uint32_t *)(bar + 2) != 0u || globalTimer() - t0 > B200_BARRIER_TIMEOUT_NS) {
+          if (*(volatile uint32_t *)(bar + 2) != 0u || globalTimer() - t0 > timeoutNs) {
             atomicExch(bar + 2, 1u);
             ok = 0;
             break;
@@ -1191,7 +1189,7 @@ __global__ void __launch_bounds__(TRACE_BLOCK, B200_PERSIST_MINBLOCKS) k_batch_p
         for (long long p = tid; p < w.npaths; p += nthreads) batchGenerate(R.reqs, R.segs + w.segOffset, w.nseg, p, R.ws);
       }
     }
-    if (!gridBarrier(R.bar, gen)) return;
+    if (!gridBarrier(R.bar, gen, R.timeoutNs)) return;
     if (lead && wi > 0)
       for (int r = R.waves[wi - 1].completeFirst; r >= 0 && r < R.waves[wi - 1].completeEnd; r++)
         R.stamps[r] = globalTimer();
@@ -1209,13 +1207,13 @@ __global__ void __launch_bounds__(TRACE_BLOCK, B200_PERSIST_MINBLOCKS) k_batch_p
         vctr[4] = 0u;
       }
       persistTrace<false>(R.ws, qin, ctr + cin, ctr + 3, R.reqs);
-      if (!gridBarrier(R.bar, gen)) return;
+      if (!gridBarrier(R.bar, gen, R.timeoutNs)) return;
       if (lead) vctr[3] = 0u;  // closest-hit fetch counter of the next bounce
       persistShade(R.ws, qin, ctr + cin, cout ? R.ws.qb : R.ws.qa, ctr + cout, ctr + 2, R.reqs);
-      if (!gridBarrier(R.bar, gen)) return;
+      if (!gridBarrier(R.bar, gen, R.timeoutNs)) return;
       if (lead) vctr[cin] = 0u;  // the next bounce's output queue
       persistTrace<true>(R.ws, nullptr, ctr + 2, ctr + 4, R.reqs);
-      if (!gridBarrier(R.bar, gen)) return;
+      if (!gridBarrier(R.bar, gen, R.timeoutNs)) return;
     }
     if (lead) *R.rays += vctr[2];
     {
@@ -1224,7 +1222,7 @@ __global__ void __launch_bounds__(TRACE_BLOCK, B200_PERSIST_MINBLOCKS) k_batch_p
       for (long long q = tid; q < w.npix; q += (long long)gridDim.x * blockDim.x)
         batchFinalize(R.reqs, R.segs + w.segOffset, w.nseg, q, R.ws);
     }
-    if (!gridBarrier(R.bar, gen)) return;
+    if (!gridBarrier(R.bar, gen, R.timeoutNs)) return;
   }
 }
 
@@ -1747,7 +1745,8 @@ int batchPersistentBlocksPerSM() {
 
 cudaError_t launchBatchPersistent(const void *dtables, const BatchLayout &layout, int nreqs, const BatchTuning &tune,
                                   void *workspace, size_t wsBytes, unsigned long long *rayCount,
-                                  unsigned long long *stamps, uint32_t *barrier, cudaStream_t st) {
+                                  unsigned long long *stamps, uint32_t *barrier, unsigned long long timeoutNs,
+                                  cudaStream_t st) {
   if (ptWorkspaceBytes(tune.wavePaths) > wsBytes || !rayCount || !stamps || !barrier) return cudaErrorInvalidValue;
   const int per = batchPersistentBlocksPerSM();
   if (per < 1) return cudaErrorInvalidConfiguration;
@@ -1763,6 +1762,7 @@ cudaError_t launchBatchPersistent(const void *dtables, const BatchLayout &layout
   R.bar = barrier;
   R.rays = rayCount;
   R.stamps = stamps;
+  R.timeoutNs = timeoutNs;
   cudaError_t e = cudaMemsetAsync(barrier, 0, 4 * sizeof(uint32_t), st);
   if (e != cudaSuccess) return e;
   // all blocks resident at once (the cooperative attribute makes the launch

@@ -172,3 +172,37 @@ def test_graph_replay_equals_plain_launch_and_autotune(b200_device):
             np.testing.assert_array_equal(fbs[0].read(og.FB_DEPTH), fbs[0].read(og.FB_DEPTH))
     for a, b in zip(out[0], out[1]):
         np.testing.assert_array_equal(a, b)
+
+
+def test_persistent_barrier_timeout_is_reported_and_recovers(b200_device):
+    """Failure detection of the persistent launch without a GPU fault: with a
+    barrier bound far shorter than a stage, a wait runs out, every block
+    leaves the kernel and the host reports the frame as failed; with the
+    default bound the next frames render as the graph does."""
+    import ospray_gb300 as og
+    dev = b200_device
+    _, reqs = _requests(og, dev)
+    ao = [reqs[0], reqs[2]]
+    out = {}
+    for mode in (og.BATCH_GRAPH, og.BATCH_PERSISTENT):
+        batch = og.Batch(dev)
+        fbs = []
+        for r in ao:
+            fb = og.Frame(dev, r[-2], r[-1], og.FB_COLOR | og.FB_DEPTH | og.FB_ACCUM)
+            batch.add_ao(r[1], r[2], r[3], fb)
+            fbs.append(fb)
+        batch.tuning = og.BatchTuning(2048, 3, 1)
+        if mode == og.BATCH_PERSISTENT:
+            batch.set_barrier_timeout(1000)  # 1 us: shorter than any stage
+            batch.render(mode=mode)
+            with pytest.raises(og.B200Error, match="timed out"):
+                batch.timings()
+            batch.set_barrier_timeout(0)
+            for fb in fbs:
+                fb.reset()
+        for _ in range(2):
+            batch.render(mode=mode)
+        batch.timings()
+        out[mode] = [fb.read(og.FB_ACCUM) for fb in fbs]
+    for a, b in zip(out[og.BATCH_GRAPH], out[og.BATCH_PERSISTENT]):
+        np.testing.assert_array_equal(a, b)
