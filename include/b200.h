@@ -176,7 +176,10 @@ int b200_trace(b200_scene scene, const float *rays, int64_t n, int occlusion, fl
  * and SciVis renderers always take 0.5.  The ray's time places
  * motion-blurred instances (b200_scene_add_instance_motion).  A
  * zero-initialised shutter traces every ray at time 0; OSPRay's default is
- * [0.5, 0.5].  Stereo, depth of field and camera motion are not built. */
+ * [0.5, 0.5].  The path tracer draws the lens sample of a perspective
+ * camera with an aperture from its sample stream; AO and SciVis use a
+ * pinhole (RendererRenderTaskFn.inl:61-63).  Stereo and camera motion are
+ * not built. */
 enum { B200_CAMERA_PERSPECTIVE = 0, B200_CAMERA_ORTHOGRAPHIC = 1, B200_CAMERA_PANORAMIC = 2 };
 typedef struct {
   float position[3], direction[3], up[3];
@@ -186,6 +189,11 @@ typedef struct {
   float shutter[2];
   int shutterType;
   float rollingShutterDuration;
+  /* perspective: depth of field ("apertureRadius", "focusDistance"; a zero
+   * radius is a pinhole) and "architectural" (the image plane parallel to
+   * up) as PerspectiveCamera::commit camera/PerspectiveCamera.cpp:30-117 */
+  float apertureRadius, focusDistance;
+  int architectural;
 } b200_camera_desc;
 
 /* ---- framebuffer (LocalFrameBuffer, modules/cpu/fb/LocalFB.cpp:23-226;

@@ -39,6 +39,8 @@ struct OrCamera {
   float shutter[2];
   int shutterType;
   float rollingDuration;
+  float apertureRadius, focusDistance;
+  int architectural;
 };
 
 extern "C" {
@@ -317,7 +319,8 @@ void or_render_ao(void *sp, const OrCamera *c, int pixelFilter, int W, int H, in
                   const OrAoExtra *extra) {
   const Scene &s = *static_cast<Scene *>(sp);
   Camera cam = makeCamera({c->pos[0], c->pos[1], c->pos[2]}, {c->dir[0], c->dir[1], c->dir[2]},
-                          {c->up[0], c->up[1], c->up[2]}, c->fovy, c->aspect, c->nearClip, c->type, c->height);
+                          {c->up[0], c->up[1], c->up[2]}, c->fovy, c->aspect, c->nearClip, c->type, c->height,
+                          c->apertureRadius, c->focusDistance, c->architectural != 0);
   setShutter(cam, c->shutter[0], c->shutter[1], c->shutterType, c->rollingDuration);
   PixelFilter pf;
   pf.init(pixelFilter);

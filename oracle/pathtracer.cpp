@@ -333,7 +333,8 @@ void renderPT(const Scene &sc, const PtLights &lights, const std::vector<Materia
         const V2 pfs = pf.sample(ps);
         const V2 center = {(float(x) + 0.5f) * rcpSize.x, (float(y) + 0.5f) * rcpSize.y};
         const V2 screen = {center.x + pfs.x * rcpSize.x, center.y + pfs.y * rcpSize.y};
-        Ray ray = cameraRay(cam, screen);
+        // the lens sample from the sample stream when the camera has an aperture (PathTracer.ispc:172-175)
+        Ray ray = cameraRay(cam, screen, cam.scaledAperture > 0.f ? ld.finalizeDim23(ss234) : V2{0.5f, 0.5f});
         // the camera sample's time (PathTracer.ispc:177-180, Camera_shutterTime)
         rayTime = shutterTime(cam, screen, cam.needTime ? ld.finalizeDim4(ss234) : 0.5f);
         // Renderer_getMaxDepth at the sample's screen position (PathTracer.ispc:189-192)
@@ -374,6 +375,8 @@ struct OrCameraPT {
   float shutter[2];
   int shutterType;
   float rollingDuration;
+  float apertureRadius, focusDistance;
+  int architectural;
 };
 
 struct OrPtScene {
@@ -477,7 +480,8 @@ void or_render_pt(void *scp, void *ptp, const OrCameraPT *cam, const OrPtParams 
   const Scene &sc = *static_cast<Scene *>(scp);
   const OrPtScene &pt = *static_cast<OrPtScene *>(ptp);
   Camera c = makeCamera({cam->pos[0], cam->pos[1], cam->pos[2]}, {cam->dir[0], cam->dir[1], cam->dir[2]},
-                        {cam->up[0], cam->up[1], cam->up[2]}, cam->fovy, cam->aspect, cam->nearClip, cam->type, cam->height);
+                        {cam->up[0], cam->up[1], cam->up[2]}, cam->fovy, cam->aspect, cam->nearClip, cam->type, cam->height,
+                        cam->apertureRadius, cam->focusDistance, cam->architectural != 0);
   setShutter(c, cam->shutter[0], cam->shutter[1], cam->shutterType, cam->rollingDuration);
   PixelFilter pf;
   pf.init(pp->pixelFilter);

@@ -31,7 +31,8 @@ void setShutter(Camera &c, float lower, float upper, int type, float duration) {
   c.shutterMode = type == 0 ? 0 : (type == 1 || type == 2 ? 1 : 2);
 }
 
-Camera makeCamera(V3 pos, V3 dir, V3 up, float fovy, float aspect, float nearClip, int type, float height) {
+Camera makeCamera(V3 pos, V3 dir, V3 up, float fovy, float aspect, float nearClip, int type, float height,
+                  float apertureRadius, float focusDistance, bool architectural) {
   Camera c;
   c.type = type;
   c.nearClip = nearClip;
@@ -60,10 +61,18 @@ Camera makeCamera(V3 pos, V3 dir, V3 up, float fovy, float aspect, float nearCli
   const float ipx = ipy * aspect;
   V3 d00 = normalize(dir);
   V3 du = normalize(cross(d00, up));
-  V3 dv = cross(du, d00);
+  V3 dv = architectural ? normalize(up) : cross(du, d00);
   du = du * ipx;
   dv = dv * ipy;
   d00 = d00 - 0.5f * du - 0.5f * dv;
+  c.scaledAperture = apertureRadius != 0.f ? apertureRadius / (ipx * focusDistance) : 0.f;
+  if (c.scaledAperture > 0.f) {  // prescaled to the focal plane
+    du = du * focusDistance;
+    dv = dv * focusDistance;
+    d00 = d00 * focusDistance;
+  }
+  c.aspect = aspect;
+  c.imgPlaneY = ipy;
   c.org = pos;
   c.dir_00 = d00;
   c.du_size = du;

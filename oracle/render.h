@@ -35,6 +35,9 @@ struct Camera {
   float shutterLo = 0.5f, shutterHi = 0.5f, rollingDuration = 0.f;
   int shutterMode = 0;
   bool needTime = false;
+  // perspective depth of field (PerspectiveCamera::commit): lens radius over
+  // the image plane (0: pinhole), aspect, image-plane height
+  float scaledAperture = 0.f, aspect = 1.f, imgPlaneY = 1.f;
 };
 
 // Camera::commit's shutter from the "shutter", "shutterType" and
@@ -55,9 +58,11 @@ inline float shutterTime(const Camera &c, V2 screen, float time) {
 // PanoramicCamera::commit (camera/PanoramicCamera.cpp:30-47), without stereo,
 // aperture or motion blur
 Camera makeCamera(V3 pos, V3 dir, V3 up, float fovy, float aspect, float nearClip, int type = 0,
-                  float height = 1.f);
+                  float height = 1.f, float apertureRadius = 0.f, float focusDistance = 1.f,
+                  bool architectural = false);
 
-inline Ray cameraRay(const Camera &c, V2 screen) {
+// lens: the lens sample (PerspectiveCamera.ispc:44-52: uniformSampleDisk)
+inline Ray cameraRay(const Camera &c, V2 screen, V2 lens = {0.f, 0.f}) {
   if (c.type == 1)  // OrthographicCamera_initRay (camera/OrthographicCamera.ispc:11-49)
     return {c.org + screen.x * c.du_size + screen.y * c.dv_up, c.nearClip, c.dir_00, INFINITY};
   if (c.type == 2) {  // PanoramicCamera_initRay (camera/PanoramicCamera.ispc:12-90), mono
@@ -67,8 +72,15 @@ inline Ray cameraRay(const Camera &c, V2 screen) {
     const V3 d = c.du_size * -l.y + c.dv_up * -l.z + c.dir_00 * l.x;
     return {c.org, c.nearClip, d, INFINITY};
   }
-  const V3 d = c.dir_00 + screen.x * c.du_size + screen.y * c.dv_up;
-  return {c.org, c.nearClip, normalize(d), INFINITY};
+  V3 d = c.dir_00 + screen.x * c.du_size + screen.y * c.dv_up;
+  V3 org = c.org;
+  if (c.scaledAperture > 0.f) {
+    const float r = std::sqrt(lens.x) * c.scaledAperture, phi = 6.28318530717958647692f * lens.y;
+    const V3 lp = (r * std::cos(phi)) * c.du_size + ((r * std::sin(phi)) * c.aspect) * c.dv_up;
+    org = org + lp;
+    d = d - lp;
+  }
+  return {org, c.nearClip, normalize(d), INFINITY};
 }
 
 // The camera ray's cone at `screen`, in units of the frame height (x: width,
@@ -81,7 +93,7 @@ inline V2 cameraCone(const Camera &c, V2 screen, float rcpH) {
   if (c.type == 1) return {length(c.dv_up) * rcpH, 0.f};
   if (c.type == 2) return {0.f, 3.14159265358979323846f * std::sin(3.14159265358979323846f * screen.y) * rcpH};
   const V3 d = c.dir_00 + screen.x * c.du_size + screen.y * c.dv_up;
-  return {0.f, length(c.dv_up) * (1.f / std::sqrt(dot(d, d))) * rcpH};
+  return {0.f, c.imgPlaneY * (1.f / std::sqrt(dot(d, d))) * rcpH};
 }
 
 enum PixelFilterType { PF_POINT = 0, PF_BOX = 1, PF_GAUSS = 2, PF_MITCHELL = 3, PF_BLACKMAN_HARRIS = 4 };

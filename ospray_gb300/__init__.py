@@ -42,7 +42,8 @@ class CameraDesc(ctypes.Structure):
                 ("up", ctypes.c_float * 3), ("fovy", ctypes.c_float), ("aspect", ctypes.c_float),
                 ("nearClip", ctypes.c_float), ("type", ctypes.c_int), ("height", ctypes.c_float),
                 ("shutter", ctypes.c_float * 2), ("shutterType", ctypes.c_int),
-                ("rollingShutterDuration", ctypes.c_float)]
+                ("rollingShutterDuration", ctypes.c_float), ("apertureRadius", ctypes.c_float),
+                ("focusDistance", ctypes.c_float), ("architectural", ctypes.c_int)]
 
 
 class AOParams(ctypes.Structure):
@@ -736,13 +737,16 @@ CAMERA_PERSPECTIVE, CAMERA_ORTHOGRAPHIC, CAMERA_PANORAMIC = 0, 1, 2
 
 
 def camera_desc(position, direction, up=(0, 1, 0), fovy=60.0, aspect=1.0, near_clip=1e-6, kind=CAMERA_PERSPECTIVE,
-                height=1.0, shutter=(0.5, 0.5), shutter_type=0, rolling_shutter_duration=0.0):
+                height=1.0, shutter=(0.5, 0.5), shutter_type=0, rolling_shutter_duration=0.0, aperture_radius=0.0,
+                focus_distance=1.0, architectural=False):
     """kind: CAMERA_PERSPECTIVE (fovy), CAMERA_ORTHOGRAPHIC (image `height`) or CAMERA_PANORAMIC.
     shutter / shutter_type (OSPShutterType) / rolling_shutter_duration: the ray times (motion blur)."""
     c = CameraDesc()
     c.type, c.height = int(kind), float(height)
     c.shutter[:] = [float(shutter[0]), float(shutter[1])]
     c.shutterType, c.rollingShutterDuration = int(shutter_type), float(rolling_shutter_duration)
+    c.apertureRadius, c.focusDistance = float(aperture_radius), float(focus_distance)
+    c.architectural = int(bool(architectural))
     c.position[:] = list(map(float, position))
     c.direction[:] = list(map(float, direction))
     c.up[:] = list(map(float, up))

@@ -443,7 +443,7 @@ static CameraD makeCameraFrame(const b200_camera_desc &c) {
     V3 du = normalize(cross(d, up));
     const V3 dv = mul(cross(du, d), h);
     du = mul(du, h * c.aspect);
-    CameraD cam;
+    CameraD cam = {};
     cam.type = 1;
     cam.dir_00 = d;
     cam.du_size = du;
@@ -455,7 +455,7 @@ static CameraD makeCameraFrame(const b200_camera_desc &c) {
   if (c.type == B200_CAMERA_PANORAMIC) {  // PanoramicCamera::commit
     const V3 vz = mul(normalize(dir), -1.f);
     const V3 vx = normalize(cross(up, vz));
-    CameraD cam;
+    CameraD cam = {};
     cam.type = 2;
     cam.du_size = vx;
     cam.dv_up = cross(vz, vx);
@@ -469,11 +469,21 @@ static CameraD makeCameraFrame(const b200_camera_desc &c) {
   const float ipx = ipy * c.aspect;
   V3 d00 = normalize(dir);
   V3 du = normalize(cross(d00, up));
-  V3 dv = cross(du, d00);
+  V3 dv = c.architectural ? normalize(up) : cross(du, d00);  // architectural: the film parallel to up
   du = mul(du, ipx);
   dv = mul(dv, ipy);
   d00 = sub(sub(d00, mul(0.5f, du)), mul(0.5f, dv));
-  CameraD cam;
+  CameraD cam = {};
+  // depth of field: the lens radius over the image plane, the frame
+  // prescaled to the focal plane
+  cam.scaledAperture = c.apertureRadius != 0.f ? c.apertureRadius / (ipx * c.focusDistance) : 0.f;
+  if (cam.scaledAperture > 0.f) {
+    du = mul(du, c.focusDistance);
+    dv = mul(dv, c.focusDistance);
+    d00 = mul(d00, c.focusDistance);
+  }
+  cam.aspect = c.aspect;
+  cam.imgPlaneY = ipy;
   cam.org = pos;
   cam.dir_00 = d00;
   cam.du_size = du;

@@ -630,7 +630,12 @@ void CameraObj::commit(B200Device &dev) {
   desc.rollingShutterDuration = getFloat("rollingShutterDuration", 0.f);
   if (getData("motion.transform") || has("motion.scale") || has("motion.rotation") || has("motion.translation"))
     dev.warn("camera: camera motion blur is not supported by the b200 device");
-  if (getFloat("apertureRadius", 0.f) != 0.f) dev.warn("camera: depth of field is not supported by the b200 device");
+  // PerspectiveCamera::commit (camera/PerspectiveCamera.cpp:30-36): depth of field, architectural
+  desc.apertureRadius = getFloat("apertureRadius", 0.f);
+  desc.focusDistance = getFloat("focusDistance", 1.f);
+  desc.architectural = getBool("architectural", false) ? 1 : 0;
+  if (desc.apertureRadius != 0.f && desc.type != B200_CAMERA_PERSPECTIVE)
+    dev.warn("camera: depth of field is supported by the perspective camera only");
   if (getInt("stereoMode", OSP_STEREO_NONE) != OSP_STEREO_NONE)
     dev.warn("camera: stereo is not supported by the b200 device");
 }

@@ -27,6 +27,9 @@ struct CameraD {
   // time sample
   float shutterLo, shutterHi, rollingDuration;
   int shutterMode, needTime;
+  // perspective: lens radius over the image plane (0: pinhole; the frame is
+  // then prescaled to the focal plane), aspect, image-plane height
+  float scaledAperture, aspect, imgPlaneY;
 };
 
 // Camera_shutterTime (camera/Camera.ih:33-42): the ray time of a camera
@@ -66,7 +69,9 @@ B200_D bool pixelActive(const FrameD &fb, int x, int y) {
   return !fb.taskActive || fb.taskActive[(y >> 3) * fb.tasksX + (x >> 3)] != 0;
 }
 
-B200_D Ray cameraRay(const CameraD &c, float sx, float sy) {
+// lens: the lens sample (PerspectiveCamera_initRay, camera/PerspectiveCamera.ispc:44-52:
+// uniformSampleDisk over scaledAperture, the offset along du and aspect x dv)
+B200_D Ray cameraRay(const CameraD &c, float sx, float sy, float2 lens = make_float2(0.f, 0.f)) {
   Ray r;
   r.tnear = c.nearClip;
   r.tfar = INFINITY;
@@ -84,8 +89,16 @@ B200_D Ray cameraRay(const CameraD &c, float sx, float sy) {
     r.dir = add(add(mul(c.du_size, -l.y), mul(c.dv_up, -l.z)), mul(c.dir_00, l.x));
     return r;
   }
-  const V3 d = add(add(c.dir_00, mul(sx, c.du_size)), mul(sy, c.dv_up));
+  V3 d = add(add(c.dir_00, mul(sx, c.du_size)), mul(sy, c.dv_up));
   r.org = c.org;
+  if (c.scaledAperture > 0.f) {
+    const float rr = fmul(sqrtf(lens.x), c.scaledAperture);
+    float sp, cp;
+    sincosf(fmul(6.28318530717958647692f, lens.y), &sp, &cp);
+    const V3 lp = add(mul(fmul(rr, cp), c.du_size), mul(fmul(fmul(rr, sp), c.aspect), c.dv_up));
+    r.org = add(r.org, lp);
+    d = sub(d, lp);
+  }
   r.dir = normalize(d);
   return r;
 }
@@ -142,7 +155,7 @@ B200_D float2 cameraCone(const CameraD &c, float sx, float sy, float rcpH) {
   if (c.type == 1) return make_float2(sqrtf(dot(c.dv_up, c.dv_up)) * rcpH, 0.f);
   if (c.type == 2) return make_float2(0.f, 3.14159265358979323846f * sinf(3.14159265358979323846f * sy) * rcpH);
   const V3 d = add(add(c.dir_00, mul(sx, c.du_size)), mul(sy, c.dv_up));
-  return make_float2(0.f, sqrtf(dot(c.dv_up, c.dv_up)) * rsqrtf(dot(d, d)) * rcpH);
+  return make_float2(0.f, c.imgPlaneY * rsqrtf(dot(d, d)) * rcpH);
 }
 
 

@@ -143,7 +143,9 @@ B200_D PathRec genPT(const PtCtx &c, const CameraD &cam, const PixelFilterD &pf,
   const float2 pfs = filterSample(pf, ps.x, ps.y);
   const float cx = fmul(fadd(float(x), 0.5f), fi.rcpW), cy = fmul(fadd(float(y), 0.5f), fi.rcpH);
   const float sx = fadd(cx, fmul(pfs.x, fi.rcpW)), sy = fadd(cy, fmul(pfs.y, fi.rcpH));
-  const Ray ray = cameraRay(cam, sx, sy);
+  // the lens sample (PathTracer.ispc:172-175): from the sample stream when
+  // the camera has an aperture
+  const Ray ray = cameraRay(cam, sx, sy, cam.scaledAperture > 0.f ? ld.finalizeDim23(ss234) : make_float2(0.5f, 0.5f));
   if (screen) *screen = make_float2(sx, sy);
   // the camera sample's time (PathTracer.ispc:177-180, Camera_shutterTime)
   if (time) *time = shutterTime(cam, sx, sy, cam.needTime ? ld.finalizeDim4(ss234) : 0.5f);

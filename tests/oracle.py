@@ -19,7 +19,8 @@ P, I, U32, F = ctypes.c_void_p, ctypes.c_int, ctypes.c_uint32, ctypes.c_float
 
 class OrCamera(ctypes.Structure):
     _fields_ = [("pos", F * 3), ("dir", F * 3), ("up", F * 3), ("fovy", F), ("aspect", F), ("nearClip", F),
-                ("type", I), ("height", F), ("shutter", F * 2), ("shutterType", I), ("rollingDuration", F)]
+                ("type", I), ("height", F), ("shutter", F * 2), ("shutterType", I), ("rollingDuration", F),
+                ("apertureRadius", F), ("focusDistance", F), ("architectural", I)]
 
 
 class OrFrame(ctypes.Structure):
@@ -294,7 +295,8 @@ def _p(a):
 
 
 def camera(position, direction, up=(0, 1, 0), fovy=60.0, aspect=1.0, near_clip=1e-6, kind=0, height=1.0,
-           shutter=(0.5, 0.5), shutter_type=0, rolling_shutter_duration=0.0):
+           shutter=(0.5, 0.5), shutter_type=0, rolling_shutter_duration=0.0, aperture_radius=0.0,
+           focus_distance=1.0, architectural=False):
     """kind 0 perspective, 1 orthographic (image `height`), 2 panoramic; shutter as the b200 camera."""
     c = OrCamera()
     c.pos[:], c.dir[:], c.up[:] = list(position), list(direction), list(up)
@@ -302,6 +304,8 @@ def camera(position, direction, up=(0, 1, 0), fovy=60.0, aspect=1.0, near_clip=1
     c.type, c.height = int(kind), float(height)
     c.shutter[:] = [float(shutter[0]), float(shutter[1])]
     c.shutterType, c.rollingDuration = int(shutter_type), float(rolling_shutter_duration)
+    c.apertureRadius, c.focusDistance = float(aperture_radius), float(focus_distance)
+    c.architectural = int(bool(architectural))
     return c
 
 
