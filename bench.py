@@ -256,9 +256,41 @@ class PTWorkload:
         self.mats = og.materials_array(self.data["materials"])
         self.fb = og.Frame(dev, self.w, self.h, og.FB_COLOR | og.FB_DEPTH | og.FB_ACCUM)
         self.color = np.empty((self.h, self.w, 4), np.float32)
+        self.dev = dev
 
     def step(self, stats=False):
         self.og.render_pt(self.scene, self.cam, self.sparams if stats else self.params, self.mats, self.fb)
+
+    def image_stats(self, ref_spp):
+        """Image statistics of one benchmark frame (frame 0, spp samples per
+        pixel) against a ref_spp-sample render of the same scene on the GPU:
+        relMSE over the frame; over the CPU baseline's bands the GPU's and the
+        CPU oracle's relMSE and mean, with the mean's standard error (the
+        CPU bands render the same frame 0 samples)."""
+        og = self.og
+        self.fb.reset()
+        self.step()
+        ref = og.Frame(self.dev, self.w, self.h, og.FB_COLOR | og.FB_ACCUM)
+        for _ in range(max(1, ref_spp // self.spp)):
+            og.render_pt(self.scene, self.cam, self.params, self.mats, ref)
+        out = {"reference_spp": int(max(1, ref_spp // self.spp) * self.spp), "frame_spp": self.spp,
+               "relmse_gpu": round(og.relmse(self.fb, ref), 6)}
+        cpu = getattr(self, "cpu_color", None)
+        if cpu is not None:
+            r = ref.read(og.FB_ACCUM)[..., :3]
+            g = self.fb.read(og.FB_ACCUM)[..., :3]
+            rows = np.concatenate([np.arange(a, b) for a, b in self.cpu_bands()])
+
+            def rel(x):
+                return float(np.mean((x[rows] - r[rows]) ** 2 / (r[rows] ** 2 + 0.01)))
+            c = cpu[..., :3]
+            d = (g[rows] - c[rows]).reshape(-1)
+            out.update({"bands_relmse_gpu": round(rel(g), 6), "bands_relmse_cpu": round(rel(c), 6),
+                        "bands_mean_gpu": round(float(g[rows].mean()), 6),
+                        "bands_mean_cpu": round(float(c[rows].mean()), 6),
+                        "bands_mean_diff_se": round(float(d.std() / np.sqrt(d.size)), 8)})
+        self.fb.reset()
+        return out
 
     def e2e_setup(self):
         """The same workload built by an OSPRay application on libospray.so."""
@@ -309,10 +341,13 @@ class PTWorkload:
         oracle.lib().or_ray_count(1)
         t0 = time.perf_counter()
         n = 0
+        color = np.zeros((self.h, self.w, 4), np.float32)
         while True:
             for y0, y1 in bands:
-                oracle.render_pt(o, ow, self._ocam, self._op, self.w, self.h, rows=(y0, y1), nthreads=nthreads)
+                img = oracle.render_pt(o, ow, self._ocam, self._op, self.w, self.h, rows=(y0, y1), nthreads=nthreads)
+                color[y0:y1] = img["color"][y0:y1]
             n += 1
+            self.cpu_color = color
             dt = time.perf_counter() - t0
             if (passes is not None and n >= passes) or (passes is None and dt >= budget_s):
                 break
@@ -800,6 +835,11 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
     if line is None:
         return
+    if args.workload == "pt" and not args.headline_only and args.ref_spp > 0:
+        try:  # untimed: the frame's error against a long render, GPU and CPU
+            line["image_stats"] = wl.image_stats(args.ref_spp)
+        except Exception as e:
+            line["image_stats"] = {"error": "%s: %s" % (type(e).__name__, e)}
     if ws == 1 and args.workload == "pt" and not args.headline_only:
         # the other configurations, each in its own object of the same line
         del wl
@@ -964,6 +1004,8 @@ def main():
                     help="path tracer scene override SEED,INSTANCES,LEVELS (the build tuner's held-out scene; "
                          "not the bench config)")
     ap.add_argument("--nrc-frames", type=int, default=256, help="frames per arm of the learned-cache study")
+    ap.add_argument("--ref-spp", type=int, default=4096,
+                    help="samples per pixel of the reference render for the headline frame's relMSE (0: skip)")
     ap.add_argument("--nrc-ref-spp", type=int, default=4096, help="spp of the learned-cache study's reference image")
     ap.add_argument("--nrc-early-frames", type=int, default=4, help="frames that train --nrc-early-epochs epochs")
     ap.add_argument("--nrc-early-epochs", type=int, default=4)
