@@ -850,6 +850,8 @@ def run_ours(args):
                 w2 = WORKLOADS[name]()
                 w2.setup(og, dev)
                 sub = measure(w2, args, og, dev, local, 1, 0.0 if args.no_cpu_baseline else args.extra_cpu_budget)
+                if name in ("ao", "scivis") and args.ref_spp > 0:
+                    sub["image_stats"] = frame_relmse(w2, args.ref_spp)
                 sub.pop("n_gpus", None)
                 sub.pop("scaling", None)
                 sub.pop("vs_baseline", None)
@@ -878,6 +880,27 @@ def run_ours(args):
         extras["C4_learned_cache"]["wall_s"] = round(time.perf_counter() - t0, 1)
         line["configs"] = extras
     print(json.dumps(line), flush=True)
+
+
+def frame_relmse(wl, ref_spp):
+    """relMSE of one frame of the workload (frame 0, its own spp) against a
+    ref_spp-sample render of it on the GPU (untimed)."""
+    og = wl.og
+    spp = getattr(wl, "spp", 1)
+    wl.reset()
+    wl.step()
+    ref = og.Frame(wl.fb.device, wl.w, wl.h, og.FB_COLOR | og.FB_ACCUM)
+    frame = wl.fb
+    wl.fb = ref
+    try:
+        for _ in range(max(1, ref_spp // spp)):
+            wl.step()
+    finally:
+        wl.fb = frame
+    out = {"reference_spp": int(max(1, ref_spp // spp) * spp), "frame_spp": spp,
+           "relmse_gpu": round(og.relmse(frame, ref), 6)}
+    wl.reset()
+    return out
 
 
 def nrc_study(args, og, dev):
