@@ -149,6 +149,11 @@ class Clocks:
                 "samples": len(sm)}
 
 
+def _sig(x, digits=4):
+    """x to `digits` significant figures (relMSE values span many decades)."""
+    return float("%.*g" % (digits, x))
+
+
 # --------------------------------------------------------------------------- workloads
 
 
@@ -274,7 +279,7 @@ class PTWorkload:
         for _ in range(max(1, ref_spp // self.spp)):
             og.render_pt(self.scene, self.cam, self.params, self.mats, ref)
         out = {"reference_spp": int(max(1, ref_spp // self.spp) * self.spp), "frame_spp": self.spp,
-               "relmse_gpu": round(og.relmse(self.fb, ref), 6)}
+               "relmse_gpu": _sig(og.relmse(self.fb, ref))}
         cpu = getattr(self, "cpu_color", None)
         if cpu is not None:
             r = ref.read(og.FB_ACCUM)[..., :3]
@@ -285,7 +290,7 @@ class PTWorkload:
                 return float(np.mean((x[rows] - r[rows]) ** 2 / (r[rows] ** 2 + 0.01)))
             c = cpu[..., :3]
             d = (g[rows] - c[rows]).reshape(-1)
-            out.update({"bands_relmse_gpu": round(rel(g), 6), "bands_relmse_cpu": round(rel(c), 6),
+            out.update({"bands_relmse_gpu": _sig(rel(g)), "bands_relmse_cpu": _sig(rel(c)),
                         "bands_mean_gpu": round(float(g[rows].mean()), 6),
                         "bands_mean_cpu": round(float(c[rows].mean()), 6),
                         "bands_mean_diff_se": round(float(d.std() / np.sqrt(d.size)), 8)})
@@ -898,7 +903,7 @@ def frame_relmse(wl, ref_spp):
     finally:
         wl.fb = frame
     out = {"reference_spp": int(max(1, ref_spp // spp) * spp), "frame_spp": spp,
-           "relmse_gpu": round(og.relmse(frame, ref), 6)}
+           "relmse_gpu": _sig(og.relmse(frame, ref))}
     wl.reset()
     return out
 
@@ -906,7 +911,7 @@ def frame_relmse(wl, ref_spp):
 def nrc_study(args, og, dev):
     """Learned-cache path tracer vs plain path tracer on the instanced-spheres
     scene: 1920x1080, 1 spp per frame, maxPathLength 8, static camera, up to
-    `--nrc-frames` frames each; both judged by relMSE against a 4096-spp plain
+    `--nrc-frames` frames each; both compared by relMSE with a 4096-spp plain
     render (256 frames x 16 spp).  relMSE is taken over all pixels and over
     the pixels whose first hit is geometry (background pixels of constant
     radiance excluded).  Per arm: device seconds and frames to reach each

@@ -2,7 +2,7 @@
 trained cache against the plain path tracer (the same method without it), on
 the instanced-spheres scene at reduced size with maxPathLength 8.
 
-Both are judged against a 1024-spp plain reference.  After the cache has
+Both are compared with a 1024-spp plain reference.  After the cache has
 trained on 48 frames, 16 frames of 1 spp with the cache have a lower relMSE
 than 16 frames of the plain path tracer (lower variance for a small bias),
 and the cached image's mean stays within 10 % of the reference's.  Also:
