@@ -178,8 +178,13 @@ int b200_trace(b200_scene scene, const float *rays, int64_t n, int occlusion, fl
  * zero-initialised shutter traces every ray at time 0; OSPRay's default is
  * [0.5, 0.5].  The path tracer draws the lens sample of a perspective
  * camera with an aperture from its sample stream; AO and SciVis use a
- * pinhole (RendererRenderTaskFn.inl:61-63).  Stereo and camera motion are
- * not built. */
+ * pinhole (RendererRenderTaskFn.inl:61-63).  "imageStart" / "imageEnd"
+ * select the sub-image the frame covers (Camera_subRegion,
+ * camera/Camera.ih:28-31); an all-zero pair is the whole image [0, 1]^2.
+ * "stereoMode" (OSPStereoMode: 0 none, 1 left, 2 right, 3 side by side, 4
+ * top / bottom, left eye at the top) with "interpupillaryDistance" applies
+ * to perspective and panoramic cameras (PerspectiveCamera.cpp:37-91,
+ * PanoramicCamera.cpp:45-52).  Camera motion is not built. */
 enum { B200_CAMERA_PERSPECTIVE = 0, B200_CAMERA_ORTHOGRAPHIC = 1, B200_CAMERA_PANORAMIC = 2 };
 typedef struct {
   float position[3], direction[3], up[3];
@@ -194,6 +199,9 @@ typedef struct {
    * up) as PerspectiveCamera::commit camera/PerspectiveCamera.cpp:30-117 */
   float apertureRadius, focusDistance;
   int architectural;
+  float imageStart[2], imageEnd[2];
+  int stereoMode;
+  float interpupillaryDistance;
 } b200_camera_desc;
 
 /* ---- framebuffer (LocalFrameBuffer, modules/cpu/fb/LocalFB.cpp:23-226;

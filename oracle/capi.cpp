@@ -41,6 +41,9 @@ struct OrCamera {
   float rollingDuration;
   float apertureRadius, focusDistance;
   int architectural;
+  float imageStart[2], imageEnd[2];  // the sub-image (all zero: whole)
+  int stereoMode;
+  float interpupillaryDistance;
 };
 
 extern "C" {
@@ -255,8 +258,10 @@ void or_trace(void *sp, const float *rays, int n, int occlusion, float *out_f, u
 // samples per pixel (sample s of pixel (x,y) at index ((y*W)+x)*spp+s),
 // exactly as the renderers generate them.  out: 8 floats per ray.
 void or_camera_rays(const OrCamera *c, int pixelFilter, int W, int H, int spp, int frameID, float *out) {
-  const Camera cam = makeCamera({c->pos[0], c->pos[1], c->pos[2]}, {c->dir[0], c->dir[1], c->dir[2]},
-                                {c->up[0], c->up[1], c->up[2]}, c->fovy, c->aspect, c->nearClip, c->type, c->height);
+  Camera cam = makeCamera({c->pos[0], c->pos[1], c->pos[2]}, {c->dir[0], c->dir[1], c->dir[2]},
+                          {c->up[0], c->up[1], c->up[2]}, c->fovy, c->aspect, c->nearClip, c->type, c->height,
+                          0.f, 1.f, false, c->stereoMode, c->interpupillaryDistance);
+  setSubImage(cam, c->imageStart, c->imageEnd, c->stereoMode);
   PixelFilter pf;
   pf.init(pixelFilter);
   const V2 rcpSize = {1.f / float(W), 1.f / float(H)};
@@ -268,8 +273,9 @@ void or_camera_rays(const OrCamera *c, int pixelFilter, int W, int H, int spp, i
         const V2 ps = {Halton_sample2(sid), CranleyPattersonRotation(Halton_sample3(sid), 1.f / 6.f)};
         const V2 pfs = pf.sample(ps);
         const V2 center = {(float(x) + 0.5f) * rcpSize.x, (float(y) + 0.5f) * rcpSize.y};
-        const V2 screen = {center.x + pfs.x * rcpSize.x, center.y + pfs.y * rcpSize.y};
-        const Ray r = cameraRay(cam, screen);
+        V2 screen = {center.x + pfs.x * rcpSize.x, center.y + pfs.y * rcpSize.y};
+        const float eye = cameraScreen(cam, screen, center);
+        const Ray r = cameraRay(cam, screen, {0.f, 0.f}, eye);
         float *o = out + 8 * ((size_t(y) * W + x) * spp + sp);
         o[0] = r.org.x;
         o[1] = r.org.y;
@@ -320,8 +326,10 @@ void or_render_ao(void *sp, const OrCamera *c, int pixelFilter, int W, int H, in
   const Scene &s = *static_cast<Scene *>(sp);
   Camera cam = makeCamera({c->pos[0], c->pos[1], c->pos[2]}, {c->dir[0], c->dir[1], c->dir[2]},
                           {c->up[0], c->up[1], c->up[2]}, c->fovy, c->aspect, c->nearClip, c->type, c->height,
-                          c->apertureRadius, c->focusDistance, c->architectural != 0);
+                          c->apertureRadius, c->focusDistance, c->architectural != 0, c->stereoMode,
+                          c->interpupillaryDistance);
   setShutter(cam, c->shutter[0], c->shutter[1], c->shutterType, c->rollingDuration);
+  setSubImage(cam, c->imageStart, c->imageEnd, c->stereoMode);
   PixelFilter pf;
   pf.init(pixelFilter);
   FrameBuffer fb;

@@ -333,13 +333,15 @@ void renderPT(const Scene &sc, const PtLights &lights, const std::vector<Materia
         const V2 pfs = pf.sample(ps);
         const V2 center = {(float(x) + 0.5f) * rcpSize.x, (float(y) + 0.5f) * rcpSize.y};
         const V2 screen = {center.x + pfs.x * rcpSize.x, center.y + pfs.y * rcpSize.y};
+        V2 mapped = screen;
+        const float eye = cameraScreen(cam, mapped, center);
         // the lens sample from the sample stream when the camera has an aperture (PathTracer.ispc:172-175)
-        Ray ray = cameraRay(cam, screen, cam.scaledAperture > 0.f ? ld.finalizeDim23(ss234) : V2{0.5f, 0.5f});
+        Ray ray = cameraRay(cam, mapped, cam.scaledAperture > 0.f ? ld.finalizeDim23(ss234) : V2{0.5f, 0.5f}, eye);
         // the camera sample's time (PathTracer.ispc:177-180, Camera_shutterTime)
-        rayTime = shutterTime(cam, screen, cam.needTime ? ld.finalizeDim4(ss234) : 0.5f);
-        // Renderer_getMaxDepth at the sample's screen position (PathTracer.ispc:189-192)
+        rayTime = shutterTime(cam, mapped, cam.needTime ? ld.finalizeDim4(ss234) : 0.5f);
+        // Renderer_getMaxDepth at the sample's (unmapped) screen position (PathTracer.ispc:189-192)
         if (p.maxDepth) ray.tfar = std::fmin(ray.tfar, std::fmax(0.f, p.maxDepth->get(screen, 0.f).x));
-        const PathOut o = samplePath(c, ld, ray, cameraCone(cam, screen, rcpSize.y), center);
+        const PathOut o = samplePath(c, ld, ray, cameraCone(cam, mapped, rcpSize.y), center);
         ScreenSample smp;
         smp.rgb = vmin(o.rgb, v3(p.maxContribution));
         smp.alpha = o.alpha;
@@ -377,6 +379,9 @@ struct OrCameraPT {
   float rollingDuration;
   float apertureRadius, focusDistance;
   int architectural;
+  float imageStart[2], imageEnd[2];  // the sub-image (all zero: whole)
+  int stereoMode;
+  float interpupillaryDistance;
 };
 
 struct OrPtScene {
@@ -481,8 +486,10 @@ void or_render_pt(void *scp, void *ptp, const OrCameraPT *cam, const OrPtParams 
   const OrPtScene &pt = *static_cast<OrPtScene *>(ptp);
   Camera c = makeCamera({cam->pos[0], cam->pos[1], cam->pos[2]}, {cam->dir[0], cam->dir[1], cam->dir[2]},
                         {cam->up[0], cam->up[1], cam->up[2]}, cam->fovy, cam->aspect, cam->nearClip, cam->type, cam->height,
-                        cam->apertureRadius, cam->focusDistance, cam->architectural != 0);
+                        cam->apertureRadius, cam->focusDistance, cam->architectural != 0, cam->stereoMode,
+                        cam->interpupillaryDistance);
   setShutter(c, cam->shutter[0], cam->shutter[1], cam->shutterType, cam->rollingDuration);
+  setSubImage(c, cam->imageStart, cam->imageEnd, cam->stereoMode);
   PixelFilter pf;
   pf.init(pp->pixelFilter);
   PtParams p = {pp->spp, pp->maxPathLength, pp->roulettePathLength, pp->maxScatteringEvents, pp->lightSamples,

@@ -32,7 +32,8 @@ void setShutter(Camera &c, float lower, float upper, int type, float duration) {
 }
 
 Camera makeCamera(V3 pos, V3 dir, V3 up, float fovy, float aspect, float nearClip, int type, float height,
-                  float apertureRadius, float focusDistance, bool architectural) {
+                  float apertureRadius, float focusDistance, bool architectural, int stereoMode,
+                  float interpupillaryDistance) {
   Camera c;
   c.type = type;
   c.nearClip = nearClip;
@@ -54,14 +55,31 @@ Camera makeCamera(V3 pos, V3 dir, V3 up, float fovy, float aspect, float nearCli
     c.dv_up = cross(vz, vx);
     c.dir_00 = vz;
     c.org = pos;
+    // PanoramicCamera::commit (camera/PanoramicCamera.cpp:45-52): the offset
+    // negated for top / bottom; left / right keep a fixed eye
+    const float h = 0.5f * interpupillaryDistance;
+    c.ipdOffset = {stereoMode == 4 ? -h : h, 0.f, 0.f};
+    c.monoEye = stereoMode == 1 ? -1.f : stereoMode == 2 ? 1.f : 0.f;
+    c.split = stereoMode == 3 ? 1 : stereoMode == 4 ? 2 : 0;
     return c;
   }
+  // PerspectiveCamera::commit (camera/PerspectiveCamera.cpp:37-91): side by
+  // side halves the aspect, top / bottom doubles it; left / right move the
+  // origin by half the interpupillary distance along the film's x axis
+  if (stereoMode == 3) aspect = aspect * 0.5f;
+  if (stereoMode == 4) aspect = aspect * 2.f;
   const float deg2rad = float(1.745329251994329576923690768489e-2);
   const float ipy = 2.f * std::tan(deg2rad * (0.5f * fovy));
   const float ipx = ipy * aspect;
   V3 d00 = normalize(dir);
   V3 du = normalize(cross(d00, up));
   V3 dv = architectural ? normalize(up) : cross(du, d00);
+  V3 ipd = (0.5f * interpupillaryDistance) * du;
+  if (stereoMode == 1) pos = pos - ipd;
+  if (stereoMode == 2) pos = pos + ipd;
+  if (stereoMode == 4) ipd = -1.f * ipd;
+  c.ipdOffset = ipd;
+  c.split = stereoMode == 3 ? 1 : stereoMode == 4 ? 2 : 0;
   du = du * ipx;
   dv = dv * ipy;
   d00 = d00 - 0.5f * du - 0.5f * dv;
@@ -79,6 +97,13 @@ Camera makeCamera(V3 pos, V3 dir, V3 up, float fovy, float aspect, float nearCli
   c.dv_up = dv;
   c.nearClip = nearClip;
   return c;
+}
+
+void setSubImage(Camera &c, const float lo[2], const float hi[2], int stereoMode) {
+  const bool whole = lo[0] == 0.f && lo[1] == 0.f && hi[0] == 0.f && hi[1] == 0.f;
+  c.subLo = whole ? V2{0.f, 0.f} : V2{lo[0], lo[1]};
+  c.subHi = whole ? V2{1.f, 1.f} : V2{hi[0], hi[1]};
+  c.coneScale = std::fabs(c.subHi.y - c.subLo.y) * (c.type != 1 && stereoMode == 4 ? 2.f : 1.f);
 }
 
 namespace {
@@ -324,8 +349,9 @@ void renderAO(const Scene &s, const Camera &cam, const PixelFilter &pf, const AO
         const V2 ps = {Halton_sample2(sid), CranleyPattersonRotation(Halton_sample3(sid), 1.f / 6.f)};
         const V2 pfs = pf.sample(ps);
         const V2 center = {(float(x) + 0.5f) * rcpSize.x, (float(y) + 0.5f) * rcpSize.y};
-        const V2 screen = {center.x + pfs.x * rcpSize.x, center.y + pfs.y * rcpSize.y};
-        Ray ray = cameraRay(cam, screen);
+        V2 screen = {center.x + pfs.x * rcpSize.x, center.y + pfs.y * rcpSize.y};
+        const float eye = cameraScreen(cam, screen, center);
+        Ray ray = cameraRay(cam, screen, {0.f, 0.f}, eye);
         rayTime = shutterTime(cam, screen, 0.5f);  // RendererRenderTaskFn.inl:64: time sample 0.5
         // Renderer_getMaxDepth at the pixel centre (RendererRenderTaskFn.inl:41-42)
         if (p.maxDepth) ray.tfar = std::fmin(ray.tfar, std::fmax(0.f, p.maxDepth->get(center, 0.f).x));

@@ -38,7 +38,42 @@ struct Camera {
   // perspective depth of field (PerspectiveCamera::commit): lens radius over
   // the image plane (0: pinhole), aspect, image-plane height
   float scaledAperture = 0.f, aspect = 1.f, imgPlaneY = 1.f;
+  // the sub-image (Camera::commit camera/Camera.cpp:42-43,108-109) and
+  // stereo: split 0 none, 1 side by side, 2 top / bottom; monoEye the fixed
+  // eye of a panoramic left / right camera; ipdOffset half the
+  // interpupillary distance (perspective: along the film's x axis;
+  // panoramic: x); coneScale |imageEnd.y - imageStart.y|, x2 top / bottom
+  V2 subLo = {0.f, 0.f}, subHi = {1.f, 1.f};
+  int split = 0;
+  float monoEye = 0.f;
+  V3 ipdOffset = {0.f, 0.f, 0.f};
+  float coneScale = 1.f;
 };
+
+// imageStart / imageEnd (all zero: the whole image) with the cone scale of
+// the stereo mode
+void setSubImage(Camera &c, const float lo[2], const float hi[2], int stereoMode);
+
+// The stereo split and Camera_subRegion (PerspectiveCamera.ispc:28-41,
+// PanoramicCamera.ispc:24-45, Camera.ih:28-31): maps `screen` of a sample of
+// the pixel centred at `center` in place and returns its eye (-1 left, +1
+// right, 0 mono)
+inline float cameraScreen(const Camera &c, V2 &screen, V2 center) {
+  float eye = c.monoEye;
+  if (c.split) {
+    float &s = c.split == 1 ? screen.x : screen.y;
+    s = s * 2.f;
+    if ((c.split == 1 ? center.x : center.y) < 0.5f) {
+      eye = -1.f;
+    } else {
+      eye = 1.f;
+      s = s - 1.f;
+    }
+  }
+  screen.x = (1.f - screen.x) * c.subLo.x + screen.x * c.subHi.x;
+  screen.y = (1.f - screen.y) * c.subLo.y + screen.y * c.subHi.y;
+  return eye;
+}
 
 // Camera::commit's shutter from the "shutter", "shutterType" and
 // "rollingShutterDuration" parameters
@@ -59,10 +94,11 @@ inline float shutterTime(const Camera &c, V2 screen, float time) {
 // aperture or motion blur
 Camera makeCamera(V3 pos, V3 dir, V3 up, float fovy, float aspect, float nearClip, int type = 0,
                   float height = 1.f, float apertureRadius = 0.f, float focusDistance = 1.f,
-                  bool architectural = false);
+                  bool architectural = false, int stereoMode = 0, float interpupillaryDistance = 0.0635f);
 
-// lens: the lens sample (PerspectiveCamera.ispc:44-52: uniformSampleDisk)
-inline Ray cameraRay(const Camera &c, V2 screen, V2 lens = {0.f, 0.f}) {
+// lens: the lens sample (PerspectiveCamera.ispc:44-52: uniformSampleDisk);
+// screen: the mapped position (cameraScreen), eye its eye
+inline Ray cameraRay(const Camera &c, V2 screen, V2 lens = {0.f, 0.f}, float eye = 0.f) {
   if (c.type == 1)  // OrthographicCamera_initRay (camera/OrthographicCamera.ispc:11-49)
     return {c.org + screen.x * c.du_size + screen.y * c.dv_up, c.nearClip, c.dir_00, INFINITY};
   if (c.type == 2) {  // PanoramicCamera_initRay (camera/PanoramicCamera.ispc:12-90), mono
@@ -70,10 +106,11 @@ inline Ray cameraRay(const Camera &c, V2 screen, V2 lens = {0.f, 0.f}) {
     const float st = std::sin(theta), ct = std::cos(theta);
     const V3 l = {std::cos(phi) * st, std::sin(phi) * st, ct};
     const V3 d = c.du_size * -l.y + c.dv_up * -l.z + c.dir_00 * l.x;
-    return {c.org, c.nearClip, d, INFINITY};
+    const V3 org = eye != 0.f ? c.org + (eye * c.ipdOffset.x) * cross(d, c.dv_up) : c.org;
+    return {org, c.nearClip, d, INFINITY};
   }
   V3 d = c.dir_00 + screen.x * c.du_size + screen.y * c.dv_up;
-  V3 org = c.org;
+  V3 org = eye < 0.f ? c.org - c.ipdOffset : eye > 0.f ? c.org + c.ipdOffset : c.org;
   if (c.scaledAperture > 0.f) {
     const float r = std::sqrt(lens.x) * c.scaledAperture, phi = 6.28318530717958647692f * lens.y;
     const V3 lp = (r * std::cos(phi)) * c.du_size + ((r * std::sin(phi)) * c.aspect) * c.dv_up;
@@ -89,11 +126,13 @@ inline Ray cameraRay(const Camera &c, V2 screen, V2 lens = {0.f, 0.f}) {
 // orthographic as wide as the image height, parallel
 // (OrthographicCamera.ispc:52-53); panoramic pi sin(theta)
 // (PanoramicCamera.ispc:86-90); all times 1 / height (PathTracer.ispc:186-187)
+// (scaled by coneScale; screen: the mapped position)
 inline V2 cameraCone(const Camera &c, V2 screen, float rcpH) {
-  if (c.type == 1) return {length(c.dv_up) * rcpH, 0.f};
-  if (c.type == 2) return {0.f, 3.14159265358979323846f * std::sin(3.14159265358979323846f * screen.y) * rcpH};
+  if (c.type == 1) return {length(c.dv_up) * c.coneScale * rcpH, 0.f};
+  if (c.type == 2)
+    return {0.f, 3.14159265358979323846f * std::sin(3.14159265358979323846f * screen.y) * c.coneScale * rcpH};
   const V3 d = c.dir_00 + screen.x * c.du_size + screen.y * c.dv_up;
-  return {0.f, c.imgPlaneY * (1.f / std::sqrt(dot(d, d))) * rcpH};
+  return {0.f, c.imgPlaneY * c.coneScale * (1.f / std::sqrt(dot(d, d))) * rcpH};
 }
 
 enum PixelFilterType { PF_POINT = 0, PF_BOX = 1, PF_GAUSS = 2, PF_MITCHELL = 3, PF_BLACKMAN_HARRIS = 4 };

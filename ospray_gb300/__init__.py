@@ -43,7 +43,9 @@ class CameraDesc(ctypes.Structure):
                 ("nearClip", ctypes.c_float), ("type", ctypes.c_int), ("height", ctypes.c_float),
                 ("shutter", ctypes.c_float * 2), ("shutterType", ctypes.c_int),
                 ("rollingShutterDuration", ctypes.c_float), ("apertureRadius", ctypes.c_float),
-                ("focusDistance", ctypes.c_float), ("architectural", ctypes.c_int)]
+                ("focusDistance", ctypes.c_float), ("architectural", ctypes.c_int),
+                ("imageStart", ctypes.c_float * 2), ("imageEnd", ctypes.c_float * 2), ("stereoMode", ctypes.c_int),
+                ("interpupillaryDistance", ctypes.c_float)]
 
 
 class AOParams(ctypes.Structure):
@@ -738,10 +740,16 @@ CAMERA_PERSPECTIVE, CAMERA_ORTHOGRAPHIC, CAMERA_PANORAMIC = 0, 1, 2
 
 def camera_desc(position, direction, up=(0, 1, 0), fovy=60.0, aspect=1.0, near_clip=1e-6, kind=CAMERA_PERSPECTIVE,
                 height=1.0, shutter=(0.5, 0.5), shutter_type=0, rolling_shutter_duration=0.0, aperture_radius=0.0,
-                focus_distance=1.0, architectural=False):
+                focus_distance=1.0, architectural=False, image_start=(0.0, 0.0), image_end=(1.0, 1.0),
+                stereo_mode=0, interpupillary_distance=0.0635):
     """kind: CAMERA_PERSPECTIVE (fovy), CAMERA_ORTHOGRAPHIC (image `height`) or CAMERA_PANORAMIC.
-    shutter / shutter_type (OSPShutterType) / rolling_shutter_duration: the ray times (motion blur)."""
+    shutter / shutter_type (OSPShutterType) / rolling_shutter_duration: the ray times (motion blur).
+    image_start / image_end: the sub-image the frame covers; stereo_mode (OSPStereoMode: 0 none, 1 left,
+    2 right, 3 side by side, 4 top / bottom) with interpupillary_distance."""
     c = CameraDesc()
+    c.imageStart[:] = [float(image_start[0]), float(image_start[1])]
+    c.imageEnd[:] = [float(image_end[0]), float(image_end[1])]
+    c.stereoMode, c.interpupillaryDistance = int(stereo_mode), float(interpupillary_distance)
     c.type, c.height = int(kind), float(height)
     c.shutter[:] = [float(shutter[0]), float(shutter[1])]
     c.shutterType, c.rollingShutterDuration = int(shutter_type), float(rolling_shutter_duration)

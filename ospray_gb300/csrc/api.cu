@@ -430,6 +430,21 @@ static CameraD makeCameraFrame(const b200_camera_desc &c);
 CameraD makeCamera(const b200_camera_desc &c) {
   CameraD cam = makeCameraFrame(c);
   setShutter(c, cam);
+  // the sub-image (Camera::commit camera/Camera.cpp:42-43,108-109); all
+  // zero: the whole image
+  const bool whole = c.imageStart[0] == 0.f && c.imageStart[1] == 0.f && c.imageEnd[0] == 0.f && c.imageEnd[1] == 0.f;
+  cam.subLoX = whole ? 0.f : c.imageStart[0];
+  cam.subLoY = whole ? 0.f : c.imageStart[1];
+  cam.subHiX = whole ? 1.f : c.imageEnd[0];
+  cam.subHiY = whole ? 1.f : c.imageEnd[1];
+  const int sm = cam.type == 1 ? 0 : c.stereoMode;  // the orthographic camera has no stereo
+  cam.split = sm == 3 ? 1 : sm == 4 ? 2 : 0;
+  cam.coneScale = std::fabs(cam.subHiY - cam.subLoY) * (sm == 4 ? 2.f : 1.f);
+  if (cam.type == 2) {  // PanoramicCamera::commit (camera/PanoramicCamera.cpp:45-52)
+    const float h = 0.5f * c.interpupillaryDistance;
+    cam.ipdOffset = mk(sm == 4 ? -h : h, 0.f, 0.f);
+    cam.monoEye = sm == 1 ? -1.f : sm == 2 ? 1.f : 0.f;
+  }
   return cam;
 }
 
@@ -465,11 +480,21 @@ static CameraD makeCameraFrame(const b200_camera_desc &c) {
     return cam;
   }
   const float deg2rad = float(1.745329251994329576923690768489e-2);
+  // stereo (PerspectiveCamera.cpp:37-91): side by side halves the aspect,
+  // top / bottom doubles it; left / right move the origin by half the
+  // interpupillary distance along the film's x axis, the split modes keep
+  // the offset (negated for top / bottom: the left eye at the top)
+  const float aspect = c.stereoMode == 3 ? c.aspect * 0.5f : c.stereoMode == 4 ? c.aspect * 2.f : c.aspect;
   const float ipy = 2.f * std::tan(deg2rad * (0.5f * c.fovy));
-  const float ipx = ipy * c.aspect;
+  const float ipx = ipy * aspect;
   V3 d00 = normalize(dir);
   V3 du = normalize(cross(d00, up));
   V3 dv = c.architectural ? normalize(up) : cross(du, d00);  // architectural: the film parallel to up
+  V3 ipd = mul(0.5f * c.interpupillaryDistance, du);
+  V3 org = pos;
+  if (c.stereoMode == 1) org = sub(org, ipd);
+  if (c.stereoMode == 2) org = add(org, ipd);
+  if (c.stereoMode == 4) ipd = mul(-1.f, ipd);
   du = mul(du, ipx);
   dv = mul(dv, ipy);
   d00 = sub(sub(d00, mul(0.5f, du)), mul(0.5f, dv));
@@ -482,9 +507,10 @@ static CameraD makeCameraFrame(const b200_camera_desc &c) {
     dv = mul(dv, c.focusDistance);
     d00 = mul(d00, c.focusDistance);
   }
-  cam.aspect = c.aspect;
+  cam.aspect = aspect;
   cam.imgPlaneY = ipy;
-  cam.org = pos;
+  cam.org = org;
+  cam.ipdOffset = ipd;
   cam.dir_00 = d00;
   cam.du_size = du;
   cam.dv_up = dv;

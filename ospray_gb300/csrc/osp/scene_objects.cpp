@@ -636,8 +636,18 @@ void CameraObj::commit(B200Device &dev) {
   desc.architectural = getBool("architectural", false) ? 1 : 0;
   if (desc.apertureRadius != 0.f && desc.type != B200_CAMERA_PERSPECTIVE)
     dev.warn("camera: depth of field is supported by the perspective camera only");
-  if (getInt("stereoMode", OSP_STEREO_NONE) != OSP_STEREO_NONE)
-    dev.warn("camera: stereo is not supported by the b200 device");
+  // Camera::commit (camera/Camera.cpp:42-43): the sub-image, a vec2f pair
+  desc.imageStart[0] = desc.imageStart[1] = 0.f;
+  desc.imageEnd[0] = desc.imageEnd[1] = 1.f;
+  getBox1("imageStart", desc.imageStart);
+  getBox1("imageEnd", desc.imageEnd);
+  // PerspectiveCamera::commit / PanoramicCamera::commit: stereo
+  desc.stereoMode = getInt("stereoMode", OSP_STEREO_NONE);
+  if (desc.stereoMode < OSP_STEREO_NONE || desc.stereoMode > OSP_STEREO_TOP_BOTTOM)
+    throw Error(OSP_INVALID_ARGUMENT, "camera: unknown 'stereoMode'");
+  desc.interpupillaryDistance = getFloat("interpupillaryDistance", 0.0635f);
+  if (desc.stereoMode != OSP_STEREO_NONE && desc.type == B200_CAMERA_ORTHOGRAPHIC)
+    dev.warn("camera: the orthographic camera has no stereo mode");
 }
 
 void RendererObj::commit(B200Device &) {

@@ -247,7 +247,9 @@ cudaError_t launchTrace(const Scene &sc, const float4 *rays, long long n, int oc
 // its usual shape; lane 0 carries the ray.
 __global__ void k_pick(Scene sc, CameraD cam, float sx, float sy, uint32_t *out) {
   const bool active = threadIdx.x == 0;
-  Ray r = cameraRay(cam, sx, sy);
+  float mx = sx, my = sy;  // the pick position stands for the pixel centre of a stereo split
+  const float eye = cameraScreen(cam, mx, my, sx, sy);
+  Ray r = cameraRay(cam, mx, my, make_float2(0.f, 0.f), eye);
   HitRec h;
   bool hit = false;
   if (active) hit = traceScene<false>(sc, r, h);

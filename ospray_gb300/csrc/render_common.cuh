@@ -30,7 +30,42 @@ struct CameraD {
   // perspective: lens radius over the image plane (0: pinhole; the frame is
   // then prescaled to the focal plane), aspect, image-plane height
   float scaledAperture, aspect, imgPlaneY;
+  // the sub-image ("imageStart" / "imageEnd", Camera::commit
+  // camera/Camera.cpp:42-43,108-109): screen positions map to
+  // (1 - s) lo + s hi
+  float subLoX, subLoY, subHiX, subHiY;
+  // stereo: split 0 none, 1 side by side (screen x), 2 top / bottom (screen
+  // y); monoEye the fixed eye of a panoramic left (-1) / right (+1) camera
+  // (a perspective one has it folded into org); ipdOffset half the
+  // interpupillary distance, perspective along the film's x axis, panoramic
+  // in x, negated for top / bottom; coneScale |imageEnd.y - imageStart.y|,
+  // doubled for top / bottom
+  int split;
+  float monoEye;
+  V3 ipdOffset;
+  float coneScale;
 };
+
+// The stereo split and Camera_subRegion (PerspectiveCamera.ispc:28-41,
+// PanoramicCamera.ispc:24-45, Camera.ih:28-31): maps the screen position
+// (sx, sy) of a sample of the pixel with centre (cx, cy) in place and
+// returns its eye (-1 left, +1 right, 0 mono)
+B200_D float cameraScreen(const CameraD &c, float &sx, float &sy, float cx, float cy) {
+  float eye = c.monoEye;
+  if (c.split) {
+    float &s = c.split == 1 ? sx : sy;
+    s = fmul(s, 2.f);
+    if ((c.split == 1 ? cx : cy) < 0.5f) {
+      eye = -1.f;
+    } else {
+      eye = 1.f;
+      s = fsub(s, 1.f);
+    }
+  }
+  sx = fadd(fmul(fsub(1.f, sx), c.subLoX), fmul(sx, c.subHiX));
+  sy = fadd(fmul(fsub(1.f, sy), c.subLoY), fmul(sy, c.subHiY));
+  return eye;
+}
 
 // Camera_shutterTime (camera/Camera.ih:33-42): the ray time of a camera
 // sample with time sample `time` at screen position (sx, sy); rkcommon's
@@ -71,7 +106,8 @@ B200_D bool pixelActive(const FrameD &fb, int x, int y) {
 
 // lens: the lens sample (PerspectiveCamera_initRay, camera/PerspectiveCamera.ispc:44-52:
 // uniformSampleDisk over scaledAperture, the offset along du and aspect x dv)
-B200_D Ray cameraRay(const CameraD &c, float sx, float sy, float2 lens = make_float2(0.f, 0.f)) {
+// (sx, sy): the mapped screen position (cameraScreen); eye: its eye
+B200_D Ray cameraRay(const CameraD &c, float sx, float sy, float2 lens = make_float2(0.f, 0.f), float eye = 0.f) {
   Ray r;
   r.tnear = c.nearClip;
   r.tfar = INFINITY;
@@ -85,12 +121,13 @@ B200_D Ray cameraRay(const CameraD &c, float sx, float sy, float2 lens = make_fl
     sincosf(6.28318530717958647692f * sx, &sp, &cp);
     sincosf(3.14159265358979323846f * sy, &st, &ct);
     const V3 l = mk(cp * st, sp * st, ct);
-    r.org = c.org;
     r.dir = add(add(mul(c.du_size, -l.y), mul(c.dv_up, -l.z)), mul(c.dir_00, l.x));
+    // stereo: the eye's offset across the view direction (frame.vy = dv_up)
+    r.org = eye != 0.f ? add(c.org, mul(fmul(eye, c.ipdOffset.x), cross(r.dir, c.dv_up))) : c.org;
     return r;
   }
   V3 d = add(add(c.dir_00, mul(sx, c.du_size)), mul(sy, c.dv_up));
-  r.org = c.org;
+  r.org = eye < 0.f ? sub(c.org, c.ipdOffset) : eye > 0.f ? add(c.org, c.ipdOffset) : c.org;
   if (c.scaledAperture > 0.f) {
     const float rr = fmul(sqrtf(lens.x), c.scaledAperture);
     float sp, cp;
@@ -140,9 +177,10 @@ B200_D Ray primaryRay(const SamplerTables *T, const CameraD &cam, const PixelFil
   const float ps_y = cpRotate(Halton_sample3(T, sid), 1.f / 6.f);
   const float2 pfs = filterSample(pf, ps_x, ps_y);
   const float cx = fmul(fadd(float(x), 0.5f), rcpW), cy = fmul(fadd(float(y), 0.5f), rcpH);
-  const float sx = fadd(cx, fmul(pfs.x, rcpW)), sy = fadd(cy, fmul(pfs.y, rcpH));
-  if (screen) *screen = make_float2(sx, sy);
-  return cameraRay(cam, sx, sy);
+  float sx = fadd(cx, fmul(pfs.x, rcpW)), sy = fadd(cy, fmul(pfs.y, rcpH));
+  const float eye = cameraScreen(cam, sx, sy, cx, cy);
+  if (screen) *screen = make_float2(sx, sy);  // mapped: shutter time and ray cone
+  return cameraRay(cam, sx, sy, make_float2(0.f, 0.f), eye);
 }
 
 // The camera ray's cone at screen position (sx, sy), in units of the frame
@@ -150,12 +188,14 @@ B200_D Ray primaryRay(const SamplerTables *T, const CameraD &cam, const PixelFil
 // image plane height x rsqrt(|unnormalised direction|^2)
 // (PerspectiveCamera.ispc:58-63); orthographic as wide as the image height,
 // parallel (OrthographicCamera.ispc:52-53); panoramic pi sin(theta)
-// (PanoramicCamera.ispc:86-90).
+// (PanoramicCamera.ispc:86-90); all scaled by the sub-image height, twice
+// that for top / bottom stereo.  (sx, sy): the mapped screen position.
 B200_D float2 cameraCone(const CameraD &c, float sx, float sy, float rcpH) {
-  if (c.type == 1) return make_float2(sqrtf(dot(c.dv_up, c.dv_up)) * rcpH, 0.f);
-  if (c.type == 2) return make_float2(0.f, 3.14159265358979323846f * sinf(3.14159265358979323846f * sy) * rcpH);
+  if (c.type == 1) return make_float2(sqrtf(dot(c.dv_up, c.dv_up)) * c.coneScale * rcpH, 0.f);
+  if (c.type == 2)
+    return make_float2(0.f, 3.14159265358979323846f * sinf(3.14159265358979323846f * sy) * c.coneScale * rcpH);
   const V3 d = add(add(c.dir_00, mul(sx, c.du_size)), mul(sy, c.dv_up));
-  return make_float2(0.f, c.imgPlaneY * rsqrtf(dot(d, d)) * rcpH);
+  return make_float2(0.f, c.imgPlaneY * c.coneScale * rsqrtf(dot(d, d)) * rcpH);
 }
 
 

@@ -143,12 +143,16 @@ B200_D PathRec genPT(const PtCtx &c, const CameraD &cam, const PixelFilterD &pf,
   const float2 pfs = filterSample(pf, ps.x, ps.y);
   const float cx = fmul(fadd(float(x), 0.5f), fi.rcpW), cy = fmul(fadd(float(y), 0.5f), fi.rcpH);
   const float sx = fadd(cx, fmul(pfs.x, fi.rcpW)), sy = fadd(cy, fmul(pfs.y, fi.rcpH));
+  if (screen) *screen = make_float2(sx, sy);  // unmapped: Renderer_getMaxDepth (PathTracer.ispc:189-190)
+  float mx = sx, my = sy;
+  const float eye = cameraScreen(cam, mx, my, cx, cy);
   // the lens sample (PathTracer.ispc:172-175): from the sample stream when
   // the camera has an aperture
-  const Ray ray = cameraRay(cam, sx, sy, cam.scaledAperture > 0.f ? ld.finalizeDim23(ss234) : make_float2(0.5f, 0.5f));
-  if (screen) *screen = make_float2(sx, sy);
+  const Ray ray = cameraRay(cam, mx, my, cam.scaledAperture > 0.f ? ld.finalizeDim23(ss234) : make_float2(0.5f, 0.5f),
+                            eye);
+  if (screen) screen[1] = make_float2(mx, my);
   // the camera sample's time (PathTracer.ispc:177-180, Camera_shutterTime)
-  if (time) *time = shutterTime(cam, sx, sy, cam.needTime ? ld.finalizeDim4(ss234) : 0.5f);
+  if (time) *time = shutterTime(cam, mx, my, cam.needTime ? ld.finalizeDim4(ss234) : 0.5f);
   PathRec r;
   r.org = make_float4(ray.org.x, ray.org.y, ray.org.z, INFINITY);
   r.dir = make_float4(ray.dir.x, ray.dir.y, ray.dir.z, INFINITY);
@@ -192,14 +196,14 @@ __global__ void k_pt_generate(PtCtx c, CameraD cam, PixelFilterD pf, FrameInfo f
     if (live) active[slot] = uint32_t(p);
   }
   if (!live) return;
-  float2 scr;
+  float2 scr[2];  // the sample's screen position, unmapped and mapped
   float time;
-  PathRec r = genPT(c, cam, pf, fi, pix % fi.W, pix / fi.W, s, 0u, &scr, ws.times ? &time : nullptr);
+  PathRec r = genPT(c, cam, pf, fi, pix % fi.W, pix / fi.W, s, 0u, scr, ws.times ? &time : nullptr);
   if (ws.times) ws.times[p] = time;
   // Renderer_getMaxDepth at the sample's screen position (PathTracer.ispc:189-192):
   // the camera ray's tfar, carried in org.w until the first hit sets the depth there
-  if (c.p.maxDepth) r.org.w = texMaxDepth(c.p.maxDepth, scr.x, scr.y);
-  const float2 cone = cameraCone(cam, scr.x, scr.y, fi.rcpH);
+  if (c.p.maxDepth) r.org.w = texMaxDepth(c.p.maxDepth, scr[0].x, scr[0].y);
+  const float2 cone = cameraCone(cam, scr[1].x, scr[1].y, fi.rcpH);
   r.lastN.w = cone.x;
   r.meta2.y = __float_as_uint(cone.y);
   if (nrcStride) {

@@ -20,7 +20,8 @@ P, I, U32, F = ctypes.c_void_p, ctypes.c_int, ctypes.c_uint32, ctypes.c_float
 class OrCamera(ctypes.Structure):
     _fields_ = [("pos", F * 3), ("dir", F * 3), ("up", F * 3), ("fovy", F), ("aspect", F), ("nearClip", F),
                 ("type", I), ("height", F), ("shutter", F * 2), ("shutterType", I), ("rollingDuration", F),
-                ("apertureRadius", F), ("focusDistance", F), ("architectural", I)]
+                ("apertureRadius", F), ("focusDistance", F), ("architectural", I),
+                ("imageStart", F * 2), ("imageEnd", F * 2), ("stereoMode", I), ("interpupillaryDistance", F)]
 
 
 class OrFrame(ctypes.Structure):
@@ -296,9 +297,13 @@ def _p(a):
 
 def camera(position, direction, up=(0, 1, 0), fovy=60.0, aspect=1.0, near_clip=1e-6, kind=0, height=1.0,
            shutter=(0.5, 0.5), shutter_type=0, rolling_shutter_duration=0.0, aperture_radius=0.0,
-           focus_distance=1.0, architectural=False):
-    """kind 0 perspective, 1 orthographic (image `height`), 2 panoramic; shutter as the b200 camera."""
+           focus_distance=1.0, architectural=False, image_start=(0.0, 0.0), image_end=(1.0, 1.0), stereo_mode=0,
+           interpupillary_distance=0.0635):
+    """kind 0 perspective, 1 orthographic (image `height`), 2 panoramic; shutter, sub-image and stereo as the
+    b200 camera."""
     c = OrCamera()
+    c.imageStart[:], c.imageEnd[:] = list(map(float, image_start)), list(map(float, image_end))
+    c.stereoMode, c.interpupillaryDistance = int(stereo_mode), float(interpupillary_distance)
     c.pos[:], c.dir[:], c.up[:] = list(position), list(direction), list(up)
     c.fovy, c.aspect, c.nearClip = fovy, aspect, near_clip
     c.type, c.height = int(kind), float(height)

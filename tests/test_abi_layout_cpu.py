@@ -15,7 +15,8 @@ STRUCTS = {
     "b200_ao_params": ("AOParams", ["backplate", "maxDepth", "materials", "nmaterials"]),
     "b200_scivis_params": ("ScivisParams", ["backplate", "maxDepth", "mipMapBias"]),
     "b200_scivis_material": ("ScivisMaterial", ["kdMap"]),
-    "b200_camera_desc": ("CameraDesc", ["shutter", "shutterType", "rollingShutterDuration", "apertureRadius",
+    "b200_camera_desc": ("CameraDesc", ["shutter", "shutterType", "rollingShutterDuration", "apertureRadius", "imageStart",
+                                        "imageEnd", "stereoMode", "interpupillaryDistance",
                                         "architectural"]),
     "b200_light": ("Light", []),
 }
