@@ -50,7 +50,13 @@ def test_c_application_renders(tmp_path):
     assert os.path.getsize(tmp_path / "accumulatedFrame.ppm") > 320 * 240 * 3
 
 
-def test_ao_through_ospray_api_matches_oracle(osp_device):
+# a side-by-side stereo camera over a sub-image (Camera "imageStart" /
+# "imageEnd", PerspectiveCamera "stereoMode" / "interpupillaryDistance")
+STEREO = dict(stereo_mode=3, interpupillary_distance=0.05, image_start=(0.1, 0.2), image_end=(0.9, 0.95))
+
+
+@pytest.mark.parametrize("stereo", [False, True])
+def test_ao_through_ospray_api_matches_oracle(osp_device, stereo):
     from ospray_gb300 import scenes
     L = osp_device
     d = scenes.ao_heightfield_scene()
@@ -97,6 +103,12 @@ def test_ao_through_ospray_api_matches_oracle(osp_device):
     osp_api.set_param(cam, "up", osp_api.OSP_VEC3F, np.float32(c["up"]))
     osp_api.set_param(cam, "fovy", osp_api.OSP_FLOAT, np.float32(c["fovy"]))
     osp_api.set_param(cam, "aspect", osp_api.OSP_FLOAT, np.float32(1.0))
+    if stereo:
+        osp_api.set_param(cam, "stereoMode", osp_api.OSP_UINT, np.uint32(STEREO["stereo_mode"]))
+        osp_api.set_param(cam, "interpupillaryDistance", osp_api.OSP_FLOAT,
+                          np.float32(STEREO["interpupillary_distance"]))
+        osp_api.set_param(cam, "imageStart", osp_api.OSP_VEC2F, np.float32(STEREO["image_start"]))
+        osp_api.set_param(cam, "imageEnd", osp_api.OSP_VEC2F, np.float32(STEREO["image_end"]))
     L.ospCommit(cam)
     ren = L.ospNewRenderer(b"ao")
     osp_api.set_param(ren, "pixelFilter", osp_api.OSP_UINT, np.uint32(0))
@@ -116,12 +128,17 @@ def test_ao_through_ospray_api_matches_oracle(osp_device):
 
     o = oracle.Scene()
     scenes.build_ao_scene(o, d)
-    ref = oracle.render_ao(o, oracle.camera(c["position"], c["direction"], c["up"]), 0, W, H)
+    ref = oracle.render_ao(o, oracle.camera(c["position"], c["direction"], c["up"], **(STEREO if stereo else {})),
+                           0, W, H)
     assert np.mean(depth.view(np.uint32) == ref["depth"].view(np.uint32)) >= 0.9999
     for got, key in zip(ids, ("primID", "geomID", "instID")):
         assert np.mean(got == ref[key]) >= 0.9999, key
     assert np.mean(np.all(color == ref["color"], axis=2)) >= 0.999
     assert {0, 1} <= set(np.unique(ids[1]).tolist())  # both geometric models seen
+    if stereo:
+        for h in (fb, ren, cam, world):
+            L.ospRelease(h)
+        return
 
     res = osp_api.OSPPickResult()
     L.ospPick(ctypes.byref(res), fb, ren, cam, world, 0.5, 0.5)
