@@ -756,14 +756,30 @@ struct OrCameraV {
   float fovy, aspect, nearClip;
   int type;  // 0 perspective, 1 orthographic, 2 panoramic
   float height;  // orthographic image height
+  float shutter[2];  // (unused: a volume-only world does not move)
+  int shutterType;
+  float rollingDuration;
+  float apertureRadius, focusDistance;  // (unused: SciVis uses a pinhole)
+  int architectural;
+  float imageStart[2], imageEnd[2];  // the sub-image (all zero: whole)
+  int stereoMode;
+  float interpupillaryDistance;
 };
+
+// the camera of an OrCameraV with its stereo mode and sub-image
+static Camera volumeCamera(const OrCameraV *c) {
+  Camera cam = makeCamera({c->pos[0], c->pos[1], c->pos[2]}, {c->dir[0], c->dir[1], c->dir[2]},
+                          {c->up[0], c->up[1], c->up[2]}, c->fovy, c->aspect, c->nearClip, c->type, c->height, 0.f,
+                          1.f, c->architectural != 0, c->stereoMode, c->interpupillaryDistance);
+  setSubImage(cam, c->imageStart, c->imageEnd, c->stereoMode);
+  return cam;
+}
 
 // SciVis frames of a volume-only world; rows [y0, y1) (y1 <= 0: all)
 void or_render_scivis_volume(void *mp, const OrCameraV *c, int pixelFilter, int W, int H, int spp, float samplingRate,
                              const float *bg, int frames, int y0, int y1, float *color, int nthreads) {
   const VolumeModel &m = *static_cast<VolumeModel *>(mp);
-  const Camera cam = makeCamera({c->pos[0], c->pos[1], c->pos[2]}, {c->dir[0], c->dir[1], c->dir[2]},
-                                {c->up[0], c->up[1], c->up[2]}, c->fovy, c->aspect, c->nearClip, c->type, c->height);
+  const Camera cam = volumeCamera(c);
   PixelFilter pf;
   pf.init(pixelFilter);
   FrameBuffer fb;
@@ -786,7 +802,9 @@ void or_render_scivis_volume(void *mp, const OrCameraV *c, int pixelFilter, int 
           const V2 ps = {Halton_sample2(sid), CranleyPattersonRotation(Halton_sample3(sid), 1.f / 6.f)};
           const V2 pfs = pf.sample(ps);
           const V2 center = {(float(x) + 0.5f) * rcpSize.x, (float(y) + 0.5f) * rcpSize.y};
-          const Ray ray = cameraRay(cam, {center.x + pfs.x * rcpSize.x, center.y + pfs.y * rcpSize.y});
+          V2 screen = {center.x + pfs.x * rcpSize.x, center.y + pfs.y * rcpSize.y};
+          const float eye = cameraScreen(cam, screen, center);
+          const Ray ray = cameraRay(cam, screen, {0.f, 0.f}, eye);
           RandomSampler rs;
           rs.init(uint32_t(x + W * y), sid);
           const float jitter = rs.getFloat();
@@ -881,8 +899,7 @@ void or_render_scivis(void *scp, void *mp, const OrCameraV *c, const OrScivisPar
                 pp->visibleLights, pp->aoSamples, pp->aoRadius, pp->minContribution,
                 static_cast<const Texture *>(pp->backplate), static_cast<const Texture *>(pp->maxDepth),
                 std::pow(2.f, pp->mipMapBias)};
-  const Camera cam = makeCamera({c->pos[0], c->pos[1], c->pos[2]}, {c->dir[0], c->dir[1], c->dir[2]},
-                                {c->up[0], c->up[1], c->up[2]}, c->fovy, c->aspect, c->nearClip, c->type, c->height);
+  const Camera cam = volumeCamera(c);
   PixelFilter pf;
   pf.init(pp->pixelFilter);
   FrameBuffer fb;
@@ -904,8 +921,9 @@ void or_render_scivis(void *scp, void *mp, const OrCameraV *c, const OrScivisPar
           const V2 ps = {Halton_sample2(sid), CranleyPattersonRotation(Halton_sample3(sid), 1.f / 6.f)};
           const V2 pfs = pf.sample(ps);
           const V2 center = {(float(x) + 0.5f) * rcpSize.x, (float(y) + 0.5f) * rcpSize.y};
-          const V2 screen = {center.x + pfs.x * rcpSize.x, center.y + pfs.y * rcpSize.y};
-          const Ray ray = cameraRay(cam, screen);
+          V2 screen = {center.x + pfs.x * rcpSize.x, center.y + pfs.y * rcpSize.y};
+          const float eye = cameraScreen(cam, screen, center);
+          const Ray ray = cameraRay(cam, screen, {0.f, 0.f}, eye);
           accumulateScreen(acc, svRenderSample(w, p, ray, x, y, W, sid, samples, cameraCone(cam, screen, rcpSize.y),
                                                center));
         }

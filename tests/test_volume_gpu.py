@@ -23,17 +23,17 @@ def vol_setup(b200_device):
     return d, g, o
 
 
-def render_both(vol_setup, b200_device, spp=2, frames=1, pf=2, rate=1.0, bg=(0, 0, 0, 0)):
+def render_both(vol_setup, b200_device, spp=2, frames=1, pf=2, rate=1.0, bg=(0, 0, 0, 0), **cam_kw):
     import ospray_gb300 as og
     d, g, o = vol_setup
     W, H = d["width"], d["height"]
     c = d["camera"]
     fb = og.Frame(b200_device, W, H, og.FB_COLOR | og.FB_ACCUM)
-    cam = og.camera_desc(c["position"], c["direction"], c["up"], fovy=c["fovy"], aspect=c["aspect"])
+    cam = og.camera_desc(c["position"], c["direction"], c["up"], fovy=c["fovy"], aspect=c["aspect"], **cam_kw)
     for _ in range(frames):
         og.render_scivis(g, cam, og.scivis_params(spp=spp, sampling_rate=rate, bg=bg, pixel_filter=pf), fb)
     gpu = fb.read(og.FB_COLOR)
-    ocam = oracle.camera(c["position"], c["direction"], c["up"], fovy=c["fovy"], aspect=c["aspect"])
+    ocam = oracle.camera(c["position"], c["direction"], c["up"], fovy=c["fovy"], aspect=c["aspect"], **cam_kw)
     ref = oracle.render_scivis_volume(o, ocam, pf, W, H, spp=spp, sampling_rate=rate, bg=bg, frames=frames)
     return gpu, ref
 
@@ -45,6 +45,17 @@ def test_volume_matches_oracle(vol_setup, b200_device, pf, rate):
     close = np.all(np.abs(gpu - ref) <= 1e-4 * np.maximum(1.0, np.abs(ref)) + 1e-6, axis=2)
     assert close.mean() >= 0.999, close.mean()
     assert abs(gpu.mean() - ref.mean()) < 1e-5
+
+
+@pytest.mark.parametrize("mode", [3, 4])
+def test_stereo_volume_matches_oracle(vol_setup, b200_device, mode):
+    """Side-by-side and top / bottom stereo over a sub-image (the stereo
+    split and Camera_subRegion ahead of the march)."""
+    gpu, ref = render_both(vol_setup, b200_device, stereo_mode=mode, interpupillary_distance=0.2,
+                           image_start=(0.1, 0.05), image_end=(0.95, 0.9))
+    assert ref[..., 3].max() > 0.05
+    close = np.all(np.abs(gpu - ref) <= 1e-4 * np.maximum(1.0, np.abs(ref)) + 1e-6, axis=2)
+    assert close.mean() >= 0.999, close.mean()
 
 
 def test_volume_accumulation_and_background(vol_setup, b200_device):
